@@ -1,0 +1,443 @@
+/*
+ * scenes.c -- seeded synthetic workloads, built only through the public
+ * Chipmunk2D C API (cpSpaceNew, cpBodyNew, cpSpaceAddShape, ...).
+ *
+ * The same source is compiled into every library that implements the API
+ * (the GPU drop-in, the CPU restatement used as the test oracle, and the
+ * unmodified reference when it is available), so all of them receive
+ * identical scenes.  Random numbers come from xoshiro256** seeded through
+ * splitmix64; every derived quantity uses only +, -, *, / and sqrt, which
+ * are correctly rounded under IEEE 754, so a scene is bit-identical on x86
+ * and Arm hosts.  Normal variates use the Irwin-Hall sum of 12 uniforms
+ * (mean 0, variance 1).
+ *
+ * Workloads (sizes scale with the `size` argument; defaults in brackets):
+ *   1  pyramid: static ground segment (-600,-240)-(600,-240), r 0, u 1;
+ *      `size` rows [14] of 30x30 boxes, row i has size-i boxes spaced 32
+ *      apart centred on x=0 at y=-225+32i; mass 1, moment cpMomentForBox,
+ *      u 0.6, e 0.
+ *   2  circles: `size` [20000] circles r~U[0.5,2], mass pi r^2, u 0.7,
+ *      e 0.1, uniform in a W x H box (1000x2000 at 20000, area scaled with
+ *      the count) bounded by 4 static segments of radius 1; v~N(0,5)/axis.
+ *   3  mixed: `size` [30000] dynamic bodies split evenly among circles
+ *      r~U[0.5,3], convex polys (hull of 3..8 uniform points in a disk of
+ *      radius U[1,4]) and segments (length U[2,8], radius 0.5); size/60
+ *      chains [500] of 20 boxes 0.5x2 linked by pivot joints at shared
+ *      endpoints, hung from static anchors along the top; square container
+ *      (2000 at 30000) of 4 static segments r 1; u~U[0.3,1], e~U[0,0.3];
+ *      v~N(0,5)/axis; density 1.
+ *   4  tumble world: `size` bodies, 200x200 static box of 4 segments r 1,
+ *      50/50 circles r~U[1,4] and 3-6-vertex hull polys of radius U[1,4],
+ *      uniform positions, v~N(0,20)/axis, density 1, u 0.7, e 0.1.
+ *   5  adjoint world: `size`/2 circles r~U[1,3] and `size`/2 boxes with
+ *      sides U[2,6], dropped onto a static ground segment, density 1,
+ *      u 0.7, e 0.1.
+ * Gravity, time step and iterations are set by the caller.
+ */
+#include <stdlib.h>
+#include <string.h>
+#include <math.h>
+#include "../../include/chipmunk_gb300.h"
+
+typedef struct {
+	uint64_t s[4];
+} Rng;
+
+static uint64_t splitmix64(uint64_t *x)
+{
+	uint64_t z = (*x += 0x9e3779b97f4a7c15ULL);
+	z = (z ^ (z >> 30)) * 0xbf58476d1ce4e5b9ULL;
+	z = (z ^ (z >> 27)) * 0x94d049bb133111ebULL;
+	return z ^ (z >> 31);
+}
+
+static void rng_seed(Rng *r, uint64_t seed)
+{
+	uint64_t x = seed;
+	for(int i = 0; i < 4; i++) r->s[i] = splitmix64(&x);
+}
+
+static inline uint64_t rotl(const uint64_t x, int k) { return (x << k) | (x >> (64 - k)); }
+
+static uint64_t rng_next(Rng *r)
+{
+	uint64_t *s = r->s;
+	const uint64_t result = rotl(s[1] * 5, 7) * 9;
+	const uint64_t t = s[1] << 17;
+	s[2] ^= s[0];
+	s[3] ^= s[1];
+	s[1] ^= s[2];
+	s[0] ^= s[3];
+	s[2] ^= t;
+	s[3] = rotl(s[3], 45);
+	return result;
+}
+
+/* uniform in [0, 1) with 53 random bits */
+static double rng_u01(Rng *r) { return (double)(rng_next(r) >> 11) * 0x1.0p-53; }
+static double rng_uniform(Rng *r, double lo, double hi) { return lo + (hi - lo)*rng_u01(r); }
+static int rng_int(Rng *r, int lo, int hi) { return lo + (int)(rng_next(r) % (uint64_t)(hi - lo + 1)); }
+
+/* Irwin-Hall: sum of 12 U[0,1) minus 6 has mean 0 and variance 1. */
+static double rng_normal(Rng *r)
+{
+	double s = 0.0;
+	for(int i = 0; i < 12; i++) s += rng_u01(r);
+	return s - 6.0;
+}
+
+/* Point uniform in the disk of radius R by rejection from the square. */
+static cpVect rng_in_disk(Rng *r, double R)
+{
+	for(;;){
+		double x = rng_uniform(r, -1.0, 1.0), y = rng_uniform(r, -1.0, 1.0);
+		if(x*x + y*y <= 1.0) return cpv(x*R, y*R);
+	}
+}
+
+/* Random unit vector by rejection + normalisation (sqrt only). */
+static cpVect rng_direction(Rng *r)
+{
+	for(;;){
+		double x = rng_uniform(r, -1.0, 1.0), y = rng_uniform(r, -1.0, 1.0);
+		double l2 = x*x + y*y;
+		if(l2 > 1e-4 && l2 <= 1.0){ double l = sqrt(l2); return cpv(x/l, y/l); }
+	}
+}
+
+/* 2^(6u) for u in [0,1) from repeated square roots of 2 (portable: only
+ * sqrt and multiply), used for the log-uniform world sizes. */
+static double pow64_frac(double u)
+{
+	double x = 6.0*u;
+	double result = 1.0;
+	int whole = (int)x;
+	for(int i = 0; i < whole; i++) result *= 2.0;
+	double frac = x - (double)whole;
+	double root = 2.0;
+	for(int k = 0; k < 40; k++){
+		root = sqrt(root);
+		frac *= 2.0;
+		if(frac >= 1.0){ result *= root; frac -= 1.0; }
+	}
+	return result;
+}
+
+typedef struct cpxScene {
+	cpSpace *space;
+	int nbodies, cap_bodies;
+	cpBody **bodies;          /* dynamic bodies in the order they were added */
+	int nshapes, cap_shapes;
+	cpShape **shapes;         /* every shape (static ones included), add order */
+	int nconstraints, cap_constraints;
+	cpConstraint **constraints;
+} cpxScene;
+
+static void push_ptr(void ***arr, int *n, int *cap, void *p)
+{
+	if(*n == *cap){
+		*cap = (*cap ? 2*(*cap) : 64);
+		*arr = (void **)realloc(*arr, sizeof(void *)*(size_t)(*cap));
+	}
+	(*arr)[(*n)++] = p;
+}
+
+static cpBody *add_body(cpxScene *sc, cpBody *body)
+{
+	cpSpaceAddBody(sc->space, body);
+	push_ptr((void ***)&sc->bodies, &sc->nbodies, &sc->cap_bodies, body);
+	return body;
+}
+
+static cpShape *add_shape(cpxScene *sc, cpShape *shape)
+{
+	cpSpaceAddShape(sc->space, shape);
+	push_ptr((void ***)&sc->shapes, &sc->nshapes, &sc->cap_shapes, shape);
+	return shape;
+}
+
+static cpConstraint *add_constraint(cpxScene *sc, cpConstraint *c)
+{
+	cpSpaceAddConstraint(sc->space, c);
+	push_ptr((void ***)&sc->constraints, &sc->nconstraints, &sc->cap_constraints, c);
+	return c;
+}
+
+static void add_wall(cpxScene *sc, cpVect a, cpVect b, double r, double u, double e)
+{
+	cpShape *s = cpSegmentShapeNew(cpSpaceGetStaticBody(sc->space), a, b, r);
+	cpShapeSetFriction(s, u);
+	cpShapeSetElasticity(s, e);
+	add_shape(sc, s);
+}
+
+static void add_box_walls(cpxScene *sc, double hw, double hh, double r, double u, double e)
+{
+	add_wall(sc, cpv(-hw, -hh), cpv( hw, -hh), r, u, e);
+	add_wall(sc, cpv( hw, -hh), cpv( hw,  hh), r, u, e);
+	add_wall(sc, cpv( hw,  hh), cpv(-hw,  hh), r, u, e);
+	add_wall(sc, cpv(-hw,  hh), cpv(-hw, -hh), r, u, e);
+}
+
+static void add_circle(cpxScene *sc, cpVect p, cpVect v, double r, double u, double e)
+{
+	double m = 3.14159265358979323846*r*r;
+	cpBody *body = cpBodyNew(m, cpMomentForCircle(m, 0.0, r, cpvzero));
+	cpBodySetPosition(body, p);
+	cpBodySetVelocity(body, v);
+	add_body(sc, body);
+	cpShape *s = cpCircleShapeNew(body, r, cpvzero);
+	cpShapeSetFriction(s, u);
+	cpShapeSetElasticity(s, e);
+	add_shape(sc, s);
+}
+
+/* Convex hull of k random points in a disk, recentred on its centroid. */
+static void add_random_poly(cpxScene *sc, Rng *rng, cpVect p, cpVect v, int k, double R, double u, double e)
+{
+	cpVect pts[16], hull[16];
+	for(int i = 0; i < k; i++) pts[i] = rng_in_disk(rng, R);
+	int n = cpConvexHull(k, pts, hull, NULL, 0.0);
+	if(n < 3){
+		/* degenerate draw: fall back to a triangle of the disk radius */
+		hull[0] = cpv(R, 0.0); hull[1] = cpv(-0.5*R, 0.8660254037844386*R); hull[2] = cpv(-0.5*R, -0.8660254037844386*R);
+		n = 3;
+	}
+	cpVect c = cpCentroidForPoly(n, hull);
+	for(int i = 0; i < n; i++) hull[i] = cpvsub(hull[i], c);
+	double area = cpAreaForPoly(n, hull, 0.0);
+	double m = area;
+	cpBody *body = cpBodyNew(m, cpMomentForPoly(m, n, hull, cpvzero, 0.0));
+	cpBodySetPosition(body, p);
+	cpBodySetVelocity(body, v);
+	add_body(sc, body);
+	cpShape *s = cpPolyShapeNew(body, n, hull, cpTransformIdentity, 0.0);
+	cpShapeSetFriction(s, u);
+	cpShapeSetElasticity(s, e);
+	add_shape(sc, s);
+}
+
+static void add_box(cpxScene *sc, cpVect p, cpVect v, double w, double h, double m, double u, double e)
+{
+	cpBody *body = cpBodyNew(m, cpMomentForBox(m, w, h));
+	cpBodySetPosition(body, p);
+	cpBodySetVelocity(body, v);
+	add_body(sc, body);
+	cpShape *s = cpBoxShapeNew(body, w, h, 0.0);
+	cpShapeSetFriction(s, u);
+	cpShapeSetElasticity(s, e);
+	add_shape(sc, s);
+}
+
+static void build_pyramid(cpxScene *sc, int rows)
+{
+	add_wall(sc, cpv(-600.0, -240.0), cpv(600.0, -240.0), 0.0, 1.0, 0.0);
+	for(int i = 0; i < rows; i++){
+		for(int j = 0; j < rows - i; j++){
+			double x = ((double)j - (double)(rows - 1 - i)*0.5)*32.0;
+			double y = -225.0 + 32.0*(double)i;
+			add_box(sc, cpv(x, y), cpvzero, 30.0, 30.0, 1.0, 0.6, 0.0);
+		}
+	}
+}
+
+static void build_circles(cpxScene *sc, int n, uint64_t seed)
+{
+	Rng rng; rng_seed(&rng, seed);
+	double scale = sqrt((double)n/20000.0);
+	double hw = 500.0*scale, hh = 1000.0*scale;
+	add_box_walls(sc, hw, hh, 1.0, 0.7, 0.1);
+	for(int i = 0; i < n; i++){
+		double r = rng_uniform(&rng, 0.5, 2.0);
+		cpVect p = cpv(rng_uniform(&rng, -hw + 3.0, hw - 3.0), rng_uniform(&rng, -hh + 3.0, hh - 3.0));
+		cpVect v = cpv(5.0*rng_normal(&rng), 5.0*rng_normal(&rng));
+		add_circle(sc, p, v, r, 0.7, 0.1);
+	}
+}
+
+static void build_mixed(cpxScene *sc, int n, uint64_t seed)
+{
+	Rng rng; rng_seed(&rng, seed);
+	double half = 1000.0*sqrt((double)n/30000.0);
+	add_box_walls(sc, half, half, 1.0, 0.7, 0.1);
+
+	/* chains: size/60 chains of 20 links 0.5 x 2, hung from the top */
+	int chains = n/60;
+	if(chains < 1) chains = 1;
+	double top = half - 5.0;
+	for(int c = 0; c < chains; c++){
+		double x = -half + ((double)c + 0.5)*(2.0*half/(double)chains);
+		cpBody *prev = cpSpaceGetStaticBody(sc->space);
+		for(int l = 0; l < 20; l++){
+			double m = 1.0;
+			cpBody *link = cpBodyNew(m, cpMomentForBox(m, 0.5, 2.0));
+			cpBodySetPosition(link, cpv(x, top - 2.0*(double)l - 1.0));
+			add_body(sc, link);
+			cpShape *s = cpBoxShapeNew(link, 0.5, 2.0, 0.0);
+			cpShapeSetFriction(s, rng_uniform(&rng, 0.3, 1.0));
+			cpShapeSetElasticity(s, rng_uniform(&rng, 0.0, 0.3));
+			add_shape(sc, s);
+			cpConstraint *j = cpPivotJointNew(prev, link, cpv(x, top - 2.0*(double)l));
+			cpConstraintSetCollideBodies(j, cpFalse);
+			add_constraint(sc, j);
+			prev = link;
+		}
+	}
+
+	double ylo = -half + 5.0, yhi = top - 45.0;
+	for(int i = 0; i < n; i++){
+		cpVect p = cpv(rng_uniform(&rng, -half + 5.0, half - 5.0), rng_uniform(&rng, ylo, yhi));
+		cpVect v = cpv(5.0*rng_normal(&rng), 5.0*rng_normal(&rng));
+		double u = rng_uniform(&rng, 0.3, 1.0);
+		double e = rng_uniform(&rng, 0.0, 0.3);
+		int kind = i % 3;
+		if(kind == 0){
+			add_circle(sc, p, v, rng_uniform(&rng, 0.5, 3.0), u, e);
+		} else if(kind == 1){
+			int k = rng_int(&rng, 3, 8);
+			add_random_poly(sc, &rng, p, v, k, rng_uniform(&rng, 1.0, 4.0), u, e);
+		} else {
+			double len = rng_uniform(&rng, 2.0, 8.0);
+			cpVect d = rng_direction(&rng);
+			cpVect a = cpvmult(d, -0.5*len), b = cpvmult(d, 0.5*len);
+			double m = cpAreaForSegment(a, b, 0.5);
+			cpBody *body = cpBodyNew(m, cpMomentForSegment(m, a, b, 0.5));
+			cpBodySetPosition(body, p);
+			cpBodySetVelocity(body, v);
+			add_body(sc, body);
+			cpShape *s = cpSegmentShapeNew(body, a, b, 0.5);
+			cpShapeSetFriction(s, u);
+			cpShapeSetElasticity(s, e);
+			add_shape(sc, s);
+		}
+	}
+}
+
+static void build_tumble(cpxScene *sc, int n, uint64_t seed)
+{
+	Rng rng; rng_seed(&rng, seed);
+	add_box_walls(sc, 100.0, 100.0, 1.0, 0.7, 0.1);
+	for(int i = 0; i < n; i++){
+		cpVect p = cpv(rng_uniform(&rng, -94.0, 94.0), rng_uniform(&rng, -94.0, 94.0));
+		cpVect v = cpv(20.0*rng_normal(&rng), 20.0*rng_normal(&rng));
+		if(rng_u01(&rng) < 0.5){
+			add_circle(sc, p, v, rng_uniform(&rng, 1.0, 4.0), 0.7, 0.1);
+		} else {
+			int k = rng_int(&rng, 3, 6);
+			add_random_poly(sc, &rng, p, v, k, rng_uniform(&rng, 1.0, 4.0), 0.7, 0.1);
+		}
+	}
+}
+
+static void build_adjoint(cpxScene *sc, int n, uint64_t seed)
+{
+	Rng rng; rng_seed(&rng, seed);
+	add_wall(sc, cpv(-120.0, 0.0), cpv(120.0, 0.0), 0.0, 0.7, 0.1);
+	int half = n/2;
+	for(int i = 0; i < n; i++){
+		cpVect p = cpv(rng_uniform(&rng, -60.0, 60.0), rng_uniform(&rng, 8.0, 120.0));
+		cpVect v = cpv(rng_normal(&rng), rng_normal(&rng));
+		if(i < half){
+			add_circle(sc, p, v, rng_uniform(&rng, 1.0, 3.0), 0.7, 0.1);
+		} else {
+			double w = rng_uniform(&rng, 2.0, 6.0), h = rng_uniform(&rng, 2.0, 6.0);
+			add_box(sc, p, v, w, h, w*h, 0.7, 0.1);
+		}
+	}
+}
+
+/* ---- exported harness entry points (cpx_ prefix: workload plumbing, not
+ * part of the Chipmunk2D API) ---- */
+
+void *cpx_scene_build(int config, int size, unsigned long long seed)
+{
+	cpxScene *sc = (cpxScene *)calloc(1, sizeof(cpxScene));
+	sc->space = cpSpaceNew();
+	cpSpaceSetGravity(sc->space, cpv(0.0, -100.0));
+	switch(config){
+		case 1: build_pyramid(sc, size > 0 ? size : 14); cpSpaceSetIterations(sc->space, 10); break;
+		case 2: build_circles(sc, size > 0 ? size : 20000, seed); cpSpaceSetIterations(sc->space, 10); break;
+		case 3: build_mixed(sc, size > 0 ? size : 30000, seed); cpSpaceSetIterations(sc->space, 15); break;
+		case 4: build_tumble(sc, size > 0 ? size : 121, seed); cpSpaceSetIterations(sc->space, 10); break;
+		case 5: build_adjoint(sc, size > 0 ? size : 64, seed); cpSpaceSetIterations(sc->space, 10); break;
+		default: cpSpaceFree(sc->space); free(sc); return NULL;
+	}
+	return sc;
+}
+
+cpSpace *cpx_scene_space(void *h) { return ((cpxScene *)h)->space; }
+int cpx_scene_body_count(void *h) { return ((cpxScene *)h)->nbodies; }
+int cpx_scene_shape_count(void *h) { return ((cpxScene *)h)->nshapes; }
+int cpx_scene_constraint_count(void *h) { return ((cpxScene *)h)->nconstraints; }
+cpBody *cpx_scene_body(void *h, int i) { return ((cpxScene *)h)->bodies[i]; }
+cpShape *cpx_scene_shape(void *h, int i) { return ((cpxScene *)h)->shapes[i]; }
+cpConstraint *cpx_scene_constraint(void *h, int i) { return ((cpxScene *)h)->constraints[i]; }
+
+/* Public-getter view of every dynamic body: position (transform origin),
+ * velocity, angle, angular velocity, rotation -- 8 doubles per body. */
+int cpx_scene_dump_public(void *h, double *out)
+{
+	cpxScene *sc = (cpxScene *)h;
+	for(int i = 0; i < sc->nbodies; i++){
+		cpBody *b = sc->bodies[i];
+		cpVect p = cpBodyGetPosition(b), v = cpBodyGetVelocity(b), rot = cpBodyGetRotation(b);
+		double *o = out + 8*i;
+		o[0] = p.x; o[1] = p.y; o[2] = v.x; o[3] = v.y;
+		o[4] = cpBodyGetAngle(b); o[5] = cpBodyGetAngularVelocity(b); o[6] = rot.x; o[7] = rot.y;
+	}
+	return sc->nbodies;
+}
+
+/* Sum over every body's arbiters of cpArbiterTotalImpulse, through the
+ * public cpBodyEachArbiter iterator: 2 doubles per body. */
+static void sum_impulse(cpBody *body, cpArbiter *arb, void *data)
+{
+	(void)body;
+	cpVect j = cpArbiterTotalImpulse(arb);
+	double *acc = (double *)data;
+	acc[0] += j.x; acc[1] += j.y;
+}
+
+int cpx_scene_dump_impulses(void *h, double *out)
+{
+	cpxScene *sc = (cpxScene *)h;
+	for(int i = 0; i < sc->nbodies; i++){
+		out[2*i] = 0.0; out[2*i + 1] = 0.0;
+		cpBodyEachArbiter(sc->bodies[i], sum_impulse, out + 2*i);
+	}
+	return sc->nbodies;
+}
+
+void cpx_scene_step(void *h, double dt, int steps)
+{
+	cpxScene *sc = (cpxScene *)h;
+	for(int i = 0; i < steps; i++) cpSpaceStep(sc->space, dt);
+}
+
+void cpx_scene_free(void *h)
+{
+	cpxScene *sc = (cpxScene *)h;
+	if(!sc) return;
+	/* The space goes first: a space does not own its children, but freeing
+	 * it may still read the bodies it holds. */
+	cpSpaceFree(sc->space);
+	for(int i = 0; i < sc->nconstraints; i++) cpConstraintFree(sc->constraints[i]);
+	for(int i = 0; i < sc->nshapes; i++) cpShapeFree(sc->shapes[i]);
+	for(int i = 0; i < sc->nbodies; i++) cpBodyFree(sc->bodies[i]);
+	free(sc->bodies); free(sc->shapes); free(sc->constraints);
+	free(sc);
+}
+
+/* Body counts of a batch of tumble worlds: round(8 * 64^u), u ~ U[0,1),
+ * i.e. log-uniform in [8, 512]. */
+void cpx_batch_sizes(int count, unsigned long long seed, int *out)
+{
+	Rng rng; rng_seed(&rng, seed);
+	for(int i = 0; i < count; i++){
+		double n = 8.0*pow64_frac(rng_u01(&rng));
+		int k = (int)(n + 0.5);
+		if(k < 8) k = 8;
+		if(k > 512) k = 512;
+		out[i] = k;
+	}
+}

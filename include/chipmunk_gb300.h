@@ -1,0 +1,471 @@
+/*
+ * chipmunk_gb300.h -- C ABI of the GB300 drop-in for Chipmunk2D's cpSpaceStep path.
+ *
+ * Every function below keeps the name, argument meaning and error behaviour of
+ * the Chipmunk2D 7.0.3 public function it replaces; the comment beside each
+ * group cites the reference declaration (file:line, relative to the
+ * Chipmunk2D source tree).  The value types (cpVect, cpBB, cpTransform,
+ * cpShapeFilter, cpContactPointSet, ...) have the reference's exact memory
+ * layout, so an object file compiled against the reference headers links
+ * against libchipmunk_gb300.so unchanged: every object is handled through an
+ * opaque pointer and every by-value struct has the same layout.
+ *
+ * Functions prefixed cpGpu* have no counterpart in the reference; they are the
+ * GPU-only additions (solver mode, batching, error side channel, stream and
+ * debug state export).
+ *
+ * Threading and errors follow the reference: not thread-safe; API misuse
+ * aborts through cpMessage (include/chipmunk/chipmunk.h:48-58).  Device-side
+ * failures (bounded waits that timed out, table overflow) never abort; they
+ * are latched and reported by cpGpuGetLastError().
+ */
+#ifndef CHIPMUNK_GB300_H
+#define CHIPMUNK_GB300_H
+
+#include <stdint.h>
+#include <stddef.h>
+#include <math.h>
+#include <float.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- scalar types: include/chipmunk/chipmunk_types.h:55-67, 162-231 ---- */
+typedef double cpFloat;
+typedef uintptr_t cpHashValue;
+typedef uint32_t cpCollisionID;
+typedef unsigned char cpBool;
+typedef void *cpDataPointer;
+typedef uintptr_t cpCollisionType;
+typedef uintptr_t cpGroup;
+typedef unsigned int cpBitmask;
+typedef unsigned int cpTimestamp;
+
+#define cpTrue 1
+#define cpFalse 0
+#define CP_NO_GROUP ((cpGroup)0)
+#define CP_ALL_CATEGORIES (~(cpBitmask)0)
+#define CP_WILDCARD_COLLISION_TYPE (~(cpCollisionType)0)
+#define CP_MAX_CONTACTS_PER_ARBITER 2
+
+/* ---- value structs: chipmunk_types.h:236-266, cpBB.h:31-33 ---- */
+typedef struct cpVect { cpFloat x, y; } cpVect;
+typedef struct cpTransform { cpFloat a, b, c, d, tx, ty; } cpTransform;
+typedef struct cpMat2x2 { cpFloat a, b, c, d; } cpMat2x2;
+typedef struct cpBB { cpFloat l, b, r, t; } cpBB;
+
+/* ---- opaque handles: chipmunk.h:85-111 ---- */
+typedef struct cpBody cpBody;
+typedef struct cpShape cpShape;
+typedef struct cpCircleShape cpCircleShape;
+typedef struct cpSegmentShape cpSegmentShape;
+typedef struct cpPolyShape cpPolyShape;
+typedef struct cpConstraint cpConstraint;
+typedef struct cpPinJoint cpPinJoint;
+typedef struct cpSlideJoint cpSlideJoint;
+typedef struct cpPivotJoint cpPivotJoint;
+typedef struct cpArbiter cpArbiter;
+typedef struct cpSpace cpSpace;
+typedef struct cpCollisionHandler cpCollisionHandler;
+typedef struct cpContactPointSet cpContactPointSet;
+
+/* cpShape.h:27-58 */
+typedef struct cpPointQueryInfo {
+	const cpShape *shape;
+	cpVect point;
+	cpFloat distance;
+	cpVect gradient;
+} cpPointQueryInfo;
+
+typedef struct cpSegmentQueryInfo {
+	const cpShape *shape;
+	cpVect point;
+	cpVect normal;
+	cpFloat alpha;
+} cpSegmentQueryInfo;
+
+typedef struct cpShapeFilter {
+	cpGroup group;
+	cpBitmask categories;
+	cpBitmask mask;
+} cpShapeFilter;
+
+/* cpArbiter.h:81-96 */
+struct cpContactPointSet {
+	int count;
+	cpVect normal;
+	struct {
+		cpVect pointA, pointB;
+		cpFloat distance;
+	} points[CP_MAX_CONTACTS_PER_ARBITER];
+};
+
+/* cpBody.h:28-46, 175-185 */
+typedef enum cpBodyType {
+	CP_BODY_TYPE_DYNAMIC,
+	CP_BODY_TYPE_KINEMATIC,
+	CP_BODY_TYPE_STATIC,
+} cpBodyType;
+
+typedef void (*cpBodyVelocityFunc)(cpBody *body, cpVect gravity, cpFloat damping, cpFloat dt);
+typedef void (*cpBodyPositionFunc)(cpBody *body, cpFloat dt);
+typedef void (*cpBodyShapeIteratorFunc)(cpBody *body, cpShape *shape, void *data);
+typedef void (*cpBodyConstraintIteratorFunc)(cpBody *body, cpConstraint *constraint, void *data);
+typedef void (*cpBodyArbiterIteratorFunc)(cpBody *body, cpArbiter *arbiter, void *data);
+
+/* cpSpace.h:28-55, 220-236 */
+typedef cpBool (*cpCollisionBeginFunc)(cpArbiter *arb, cpSpace *space, cpDataPointer userData);
+typedef cpBool (*cpCollisionPreSolveFunc)(cpArbiter *arb, cpSpace *space, cpDataPointer userData);
+typedef void (*cpCollisionPostSolveFunc)(cpArbiter *arb, cpSpace *space, cpDataPointer userData);
+typedef void (*cpCollisionSeparateFunc)(cpArbiter *arb, cpSpace *space, cpDataPointer userData);
+
+struct cpCollisionHandler {
+	const cpCollisionType typeA;
+	const cpCollisionType typeB;
+	cpCollisionBeginFunc beginFunc;
+	cpCollisionPreSolveFunc preSolveFunc;
+	cpCollisionPostSolveFunc postSolveFunc;
+	cpCollisionSeparateFunc separateFunc;
+	cpDataPointer userData;
+};
+
+typedef void (*cpSpaceBodyIteratorFunc)(cpBody *body, void *data);
+typedef void (*cpSpaceShapeIteratorFunc)(cpShape *shape, void *data);
+typedef void (*cpSpaceConstraintIteratorFunc)(cpConstraint *constraint, void *data);
+
+/* cpConstraint.h:25-29 */
+typedef void (*cpConstraintPreSolveFunc)(cpConstraint *constraint, cpSpace *space);
+typedef void (*cpConstraintPostSolveFunc)(cpConstraint *constraint, cpSpace *space);
+
+/* ------------------------------------------------------------------------
+ * Inline value helpers.  The reference ships these as static inline
+ * functions (cpVect.h:35-225, cpBB.h:35-190, cpTransform.h:30-140); they
+ * compile into the caller, so they are restated here for programs that use
+ * this header instead of the reference's.
+ * ---------------------------------------------------------------------- */
+static const cpVect cpvzero = {0.0, 0.0};
+static inline cpVect cpv(const cpFloat x, const cpFloat y) { cpVect v = {x, y}; return v; }
+static inline cpBool cpveql(const cpVect a, const cpVect b) { return (a.x == b.x && a.y == b.y); }
+static inline cpVect cpvadd(const cpVect a, const cpVect b) { return cpv(a.x + b.x, a.y + b.y); }
+static inline cpVect cpvsub(const cpVect a, const cpVect b) { return cpv(a.x - b.x, a.y - b.y); }
+static inline cpVect cpvneg(const cpVect a) { return cpv(-a.x, -a.y); }
+static inline cpVect cpvmult(const cpVect a, const cpFloat s) { return cpv(a.x*s, a.y*s); }
+static inline cpFloat cpvdot(const cpVect a, const cpVect b) { return a.x*b.x + a.y*b.y; }
+static inline cpFloat cpvcross(const cpVect a, const cpVect b) { return a.x*b.y - a.y*b.x; }
+static inline cpVect cpvperp(const cpVect a) { return cpv(-a.y, a.x); }
+static inline cpVect cpvrperp(const cpVect a) { return cpv(a.y, -a.x); }
+static inline cpVect cpvrotate(const cpVect a, const cpVect b) { return cpv(a.x*b.x - a.y*b.y, a.x*b.y + a.y*b.x); }
+static inline cpVect cpvunrotate(const cpVect a, const cpVect b) { return cpv(a.x*b.x + a.y*b.y, a.y*b.x - a.x*b.y); }
+static inline cpFloat cpvlengthsq(const cpVect a) { return cpvdot(a, a); }
+static inline cpFloat cpvlength(const cpVect a) { return sqrt(cpvdot(a, a)); }
+static inline cpVect cpvlerp(const cpVect a, const cpVect b, const cpFloat t) { return cpvadd(cpvmult(a, 1.0 - t), cpvmult(b, t)); }
+static inline cpVect cpvnormalize(const cpVect a) { return cpvmult(a, 1.0/(cpvlength(a) + DBL_MIN)); }
+static inline cpFloat cpvdist(const cpVect a, const cpVect b) { return cpvlength(cpvsub(a, b)); }
+static inline cpFloat cpvdistsq(const cpVect a, const cpVect b) { return cpvlengthsq(cpvsub(a, b)); }
+static inline cpVect cpvforangle(const cpFloat a) { return cpv(cos(a), sin(a)); }
+static inline cpFloat cpvtoangle(const cpVect v) { return atan2(v.y, v.x); }
+
+static inline cpBB cpBBNew(const cpFloat l, const cpFloat b, const cpFloat r, const cpFloat t) { cpBB bb = {l, b, r, t}; return bb; }
+static inline cpBB cpBBNewForExtents(const cpVect c, const cpFloat hw, const cpFloat hh) { return cpBBNew(c.x - hw, c.y - hh, c.x + hw, c.y + hh); }
+static inline cpBB cpBBNewForCircle(const cpVect p, const cpFloat r) { return cpBBNewForExtents(p, r, r); }
+static inline cpBool cpBBIntersects(const cpBB a, const cpBB b) { return (a.l <= b.r && b.l <= a.r && a.b <= b.t && b.b <= a.t); }
+static inline cpBool cpBBContainsBB(const cpBB bb, const cpBB o) { return (bb.l <= o.l && bb.r >= o.r && bb.b <= o.b && bb.t >= o.t); }
+static inline cpVect cpBBCenter(cpBB bb) { return cpvlerp(cpv(bb.l, bb.b), cpv(bb.r, bb.t), 0.5); }
+static inline cpFloat cpBBArea(cpBB bb) { return (bb.r - bb.l)*(bb.t - bb.b); }
+
+static const cpTransform cpTransformIdentity = {1.0, 0.0, 0.0, 1.0, 0.0, 0.0};
+static inline cpTransform cpTransformNew(cpFloat a, cpFloat b, cpFloat c, cpFloat d, cpFloat tx, cpFloat ty) { cpTransform t = {a, b, c, d, tx, ty}; return t; }
+static inline cpTransform cpTransformNewTranspose(cpFloat a, cpFloat c, cpFloat tx, cpFloat b, cpFloat d, cpFloat ty) { cpTransform t = {a, b, c, d, tx, ty}; return t; }
+static inline cpVect cpTransformPoint(cpTransform t, cpVect p) { return cpv(t.a*p.x + t.c*p.y + t.tx, t.b*p.x + t.d*p.y + t.ty); }
+static inline cpVect cpTransformVect(cpTransform t, cpVect v) { return cpv(t.a*v.x + t.c*v.y, t.b*v.x + t.d*v.y); }
+
+static inline cpShapeFilter cpShapeFilterNew(cpGroup group, cpBitmask categories, cpBitmask mask) { cpShapeFilter f = {group, categories, mask}; return f; }
+static const cpShapeFilter CP_SHAPE_FILTER_ALL = {CP_NO_GROUP, CP_ALL_CATEGORIES, CP_ALL_CATEGORIES};
+static const cpShapeFilter CP_SHAPE_FILTER_NONE = {CP_NO_GROUP, ~CP_ALL_CATEGORIES, ~CP_ALL_CATEGORIES};
+
+/* ------------------------------------------------------------------------
+ * Misc: chipmunk.h:48, 134-171
+ * ---------------------------------------------------------------------- */
+void cpMessage(const char *condition, const char *file, int line, int isError, int isHardError, const char *message, ...);
+extern const char *cpVersionString;
+cpFloat cpMomentForCircle(cpFloat m, cpFloat r1, cpFloat r2, cpVect offset);
+cpFloat cpAreaForCircle(cpFloat r1, cpFloat r2);
+cpFloat cpMomentForSegment(cpFloat m, cpVect a, cpVect b, cpFloat radius);
+cpFloat cpAreaForSegment(cpVect a, cpVect b, cpFloat radius);
+cpFloat cpMomentForPoly(cpFloat m, int count, const cpVect *verts, cpVect offset, cpFloat radius);
+cpFloat cpAreaForPoly(const int count, const cpVect *verts, cpFloat radius);
+cpVect cpCentroidForPoly(const int count, const cpVect *verts);
+cpFloat cpMomentForBox(cpFloat m, cpFloat width, cpFloat height);
+cpFloat cpMomentForBox2(cpFloat m, cpBB box);
+int cpConvexHull(int count, const cpVect *verts, cpVect *result, int *first, cpFloat tol);
+
+/* ------------------------------------------------------------------------
+ * Space: cpSpace.h:68-255
+ * ---------------------------------------------------------------------- */
+cpSpace *cpSpaceNew(void);                                           /* cpSpace.h:72  */
+void cpSpaceFree(cpSpace *space);                                    /* cpSpace.h:77  */
+int cpSpaceGetIterations(const cpSpace *space);                      /* cpSpace.h:83  */
+void cpSpaceSetIterations(cpSpace *space, int iterations);           /* cpSpace.h:84  */
+cpVect cpSpaceGetGravity(const cpSpace *space);                      /* cpSpace.h:87  */
+void cpSpaceSetGravity(cpSpace *space, cpVect gravity);              /* cpSpace.h:88  */
+cpFloat cpSpaceGetDamping(const cpSpace *space);                     /* cpSpace.h:94  */
+void cpSpaceSetDamping(cpSpace *space, cpFloat damping);             /* cpSpace.h:95  */
+cpFloat cpSpaceGetIdleSpeedThreshold(const cpSpace *space);          /* cpSpace.h:99  */
+void cpSpaceSetIdleSpeedThreshold(cpSpace *space, cpFloat v);        /* cpSpace.h:100 */
+cpFloat cpSpaceGetSleepTimeThreshold(const cpSpace *space);          /* cpSpace.h:105 */
+void cpSpaceSetSleepTimeThreshold(cpSpace *space, cpFloat t);        /* cpSpace.h:106 */
+cpFloat cpSpaceGetCollisionSlop(const cpSpace *space);               /* cpSpace.h:112 */
+void cpSpaceSetCollisionSlop(cpSpace *space, cpFloat slop);          /* cpSpace.h:113 */
+cpFloat cpSpaceGetCollisionBias(const cpSpace *space);               /* cpSpace.h:118 */
+void cpSpaceSetCollisionBias(cpSpace *space, cpFloat bias);          /* cpSpace.h:119 */
+cpTimestamp cpSpaceGetCollisionPersistence(const cpSpace *space);    /* cpSpace.h:123 */
+void cpSpaceSetCollisionPersistence(cpSpace *space, cpTimestamp n);  /* cpSpace.h:124 */
+cpDataPointer cpSpaceGetUserData(const cpSpace *space);              /* cpSpace.h:129 */
+void cpSpaceSetUserData(cpSpace *space, cpDataPointer userData);     /* cpSpace.h:130 */
+cpBody *cpSpaceGetStaticBody(const cpSpace *space);                  /* cpSpace.h:134 */
+cpFloat cpSpaceGetCurrentTimeStep(const cpSpace *space);             /* cpSpace.h:138 */
+cpBool cpSpaceIsLocked(cpSpace *space);                              /* cpSpace.h:141 */
+cpShape *cpSpaceAddShape(cpSpace *space, cpShape *shape);            /* cpSpace.h:159 */
+cpBody *cpSpaceAddBody(cpSpace *space, cpBody *body);                /* cpSpace.h:161 */
+cpConstraint *cpSpaceAddConstraint(cpSpace *space, cpConstraint *c); /* cpSpace.h:163 */
+cpBool cpSpaceContainsShape(cpSpace *space, cpShape *shape);         /* cpSpace.h:173 */
+cpBool cpSpaceContainsBody(cpSpace *space, cpBody *body);            /* cpSpace.h:175 */
+cpBool cpSpaceContainsConstraint(cpSpace *space, cpConstraint *c);   /* cpSpace.h:177 */
+void cpSpaceEachBody(cpSpace *space, cpSpaceBodyIteratorFunc func, void *data);             /* cpSpace.h:226 */
+void cpSpaceEachShape(cpSpace *space, cpSpaceShapeIteratorFunc func, void *data);           /* cpSpace.h:231 */
+void cpSpaceEachConstraint(cpSpace *space, cpSpaceConstraintIteratorFunc func, void *data); /* cpSpace.h:236 */
+void cpSpaceStep(cpSpace *space, cpFloat dt);                        /* cpSpace.h:255 */
+
+/* ------------------------------------------------------------------------
+ * Body: cpBody.h:49-187
+ * ---------------------------------------------------------------------- */
+cpBody *cpBodyNew(cpFloat mass, cpFloat moment);                     /* cpBody.h:53  */
+cpBody *cpBodyNewKinematic(void);                                    /* cpBody.h:56  */
+cpBody *cpBodyNewStatic(void);                                       /* cpBody.h:58  */
+void cpBodyFree(cpBody *body);                                       /* cpBody.h:63  */
+void cpBodyActivate(cpBody *body);                                   /* cpBody.h:67  */
+cpBool cpBodyIsSleeping(const cpBody *body);                         /* cpBody.h:77  */
+cpBodyType cpBodyGetType(cpBody *body);                              /* cpBody.h:80  */
+cpSpace *cpBodyGetSpace(const cpBody *body);                         /* cpBody.h:85  */
+cpFloat cpBodyGetMass(const cpBody *body);                           /* cpBody.h:88  */
+void cpBodySetMass(cpBody *body, cpFloat m);                         /* cpBody.h:90  */
+cpFloat cpBodyGetMoment(const cpBody *body);                         /* cpBody.h:93  */
+void cpBodySetMoment(cpBody *body, cpFloat i);                       /* cpBody.h:95  */
+cpVect cpBodyGetPosition(const cpBody *body);                        /* cpBody.h:98  */
+void cpBodySetPosition(cpBody *body, cpVect pos);                    /* cpBody.h:100 */
+cpVect cpBodyGetCenterOfGravity(const cpBody *body);                 /* cpBody.h:103 */
+void cpBodySetCenterOfGravity(cpBody *body, cpVect cog);             /* cpBody.h:105 */
+cpVect cpBodyGetVelocity(const cpBody *body);                        /* cpBody.h:108 */
+void cpBodySetVelocity(cpBody *body, cpVect velocity);               /* cpBody.h:110 */
+cpVect cpBodyGetForce(const cpBody *body);                           /* cpBody.h:113 */
+void cpBodySetForce(cpBody *body, cpVect force);                     /* cpBody.h:115 */
+cpFloat cpBodyGetAngle(const cpBody *body);                          /* cpBody.h:118 */
+void cpBodySetAngle(cpBody *body, cpFloat a);                        /* cpBody.h:120 */
+cpFloat cpBodyGetAngularVelocity(const cpBody *body);                /* cpBody.h:123 */
+void cpBodySetAngularVelocity(cpBody *body, cpFloat w);              /* cpBody.h:125 */
+cpFloat cpBodyGetTorque(const cpBody *body);                         /* cpBody.h:128 */
+void cpBodySetTorque(cpBody *body, cpFloat torque);                  /* cpBody.h:130 */
+cpVect cpBodyGetRotation(const cpBody *body);                        /* cpBody.h:133 */
+cpDataPointer cpBodyGetUserData(const cpBody *body);                 /* cpBody.h:136 */
+void cpBodySetUserData(cpBody *body, cpDataPointer userData);        /* cpBody.h:138 */
+void cpBodySetVelocityUpdateFunc(cpBody *body, cpBodyVelocityFunc f);/* cpBody.h:141 */
+void cpBodySetPositionUpdateFunc(cpBody *body, cpBodyPositionFunc f);/* cpBody.h:144 */
+cpVect cpBodyLocalToWorld(const cpBody *body, const cpVect point);   /* cpBody.h:152 */
+cpVect cpBodyWorldToLocal(const cpBody *body, const cpVect point);   /* cpBody.h:154 */
+void cpBodyApplyForceAtWorldPoint(cpBody *body, cpVect force, cpVect point);     /* cpBody.h:157 */
+void cpBodyApplyForceAtLocalPoint(cpBody *body, cpVect force, cpVect point);     /* cpBody.h:159 */
+void cpBodyApplyImpulseAtWorldPoint(cpBody *body, cpVect impulse, cpVect point); /* cpBody.h:162 */
+void cpBodyApplyImpulseAtLocalPoint(cpBody *body, cpVect impulse, cpVect point); /* cpBody.h:164 */
+cpVect cpBodyGetVelocityAtWorldPoint(const cpBody *body, cpVect point);          /* cpBody.h:167 */
+cpVect cpBodyGetVelocityAtLocalPoint(const cpBody *body, cpVect point);          /* cpBody.h:169 */
+cpFloat cpBodyKineticEnergy(const cpBody *body);                                 /* cpBody.h:172 */
+void cpBodyEachShape(cpBody *body, cpBodyShapeIteratorFunc func, void *data);    /* cpBody.h:177 */
+void cpBodyEachConstraint(cpBody *body, cpBodyConstraintIteratorFunc func, void *data); /* cpBody.h:182 */
+void cpBodyEachArbiter(cpBody *body, cpBodyArbiterIteratorFunc func, void *data);       /* cpBody.h:187 */
+
+/* ------------------------------------------------------------------------
+ * Shapes: cpShape.h:78-197, cpPolyShape.h:26-54
+ * ---------------------------------------------------------------------- */
+void cpShapeFree(cpShape *shape);                                    /* cpShape.h:80  */
+cpBB cpShapeCacheBB(cpShape *shape);                                 /* cpShape.h:83  */
+cpSpace *cpShapeGetSpace(const cpShape *shape);                      /* cpShape.h:98  */
+cpBody *cpShapeGetBody(const cpShape *shape);                        /* cpShape.h:101 */
+cpFloat cpShapeGetMass(cpShape *shape);                              /* cpShape.h:107 */
+void cpShapeSetMass(cpShape *shape, cpFloat mass);                   /* cpShape.h:109 */
+cpFloat cpShapeGetDensity(cpShape *shape);                           /* cpShape.h:112 */
+void cpShapeSetDensity(cpShape *shape, cpFloat density);             /* cpShape.h:114 */
+cpFloat cpShapeGetMoment(cpShape *shape);                            /* cpShape.h:117 */
+cpFloat cpShapeGetArea(cpShape *shape);                              /* cpShape.h:119 */
+cpVect cpShapeGetCenterOfGravity(cpShape *shape);                    /* cpShape.h:121 */
+cpBB cpShapeGetBB(const cpShape *shape);                             /* cpShape.h:124 */
+cpBool cpShapeGetSensor(const cpShape *shape);                       /* cpShape.h:127 */
+void cpShapeSetSensor(cpShape *shape, cpBool sensor);                /* cpShape.h:129 */
+cpFloat cpShapeGetElasticity(const cpShape *shape);                  /* cpShape.h:132 */
+void cpShapeSetElasticity(cpShape *shape, cpFloat elasticity);       /* cpShape.h:134 */
+cpFloat cpShapeGetFriction(const cpShape *shape);                    /* cpShape.h:137 */
+void cpShapeSetFriction(cpShape *shape, cpFloat friction);           /* cpShape.h:139 */
+cpVect cpShapeGetSurfaceVelocity(const cpShape *shape);              /* cpShape.h:142 */
+void cpShapeSetSurfaceVelocity(cpShape *shape, cpVect v);            /* cpShape.h:144 */
+cpDataPointer cpShapeGetUserData(const cpShape *shape);              /* cpShape.h:147 */
+void cpShapeSetUserData(cpShape *shape, cpDataPointer userData);     /* cpShape.h:149 */
+cpCollisionType cpShapeGetCollisionType(const cpShape *shape);       /* cpShape.h:152 */
+void cpShapeSetCollisionType(cpShape *shape, cpCollisionType t);     /* cpShape.h:154 */
+cpShapeFilter cpShapeGetFilter(const cpShape *shape);                /* cpShape.h:157 */
+void cpShapeSetFilter(cpShape *shape, cpShapeFilter filter);         /* cpShape.h:159 */
+cpShape *cpCircleShapeNew(cpBody *body, cpFloat radius, cpVect offset);      /* cpShape.h:170 */
+cpVect cpCircleShapeGetOffset(const cpShape *shape);                         /* cpShape.h:173 */
+cpFloat cpCircleShapeGetRadius(const cpShape *shape);                        /* cpShape.h:175 */
+cpShape *cpSegmentShapeNew(cpBody *body, cpVect a, cpVect b, cpFloat radius);/* cpShape.h:185 */
+void cpSegmentShapeSetNeighbors(cpShape *shape, cpVect prev, cpVect next);   /* cpShape.h:188 */
+cpVect cpSegmentShapeGetA(const cpShape *shape);                             /* cpShape.h:191 */
+cpVect cpSegmentShapeGetB(const cpShape *shape);                             /* cpShape.h:193 */
+cpVect cpSegmentShapeGetNormal(const cpShape *shape);                        /* cpShape.h:195 */
+cpFloat cpSegmentShapeGetRadius(const cpShape *shape);                       /* cpShape.h:197 */
+cpShape *cpPolyShapeNew(cpBody *body, int count, const cpVect *verts, cpTransform transform, cpFloat radius); /* cpPolyShape.h:35 */
+cpShape *cpPolyShapeNewRaw(cpBody *body, int count, const cpVect *verts, cpFloat radius);                    /* cpPolyShape.h:38 */
+cpShape *cpBoxShapeNew(cpBody *body, cpFloat width, cpFloat height, cpFloat radius);                         /* cpPolyShape.h:45 */
+cpShape *cpBoxShapeNew2(cpBody *body, cpBB box, cpFloat radius);                                             /* cpPolyShape.h:47 */
+int cpPolyShapeGetCount(const cpShape *shape);                               /* cpPolyShape.h:50 */
+cpVect cpPolyShapeGetVert(const cpShape *shape, int index);                  /* cpPolyShape.h:52 */
+cpFloat cpPolyShapeGetRadius(const cpShape *shape);                          /* cpPolyShape.h:54 */
+
+/* ------------------------------------------------------------------------
+ * Constraints: cpConstraint.h:31-82, cpPivotJoint.h:26-45,
+ * cpPinJoint.h:26-48, cpSlideJoint.h:26-53
+ * ---------------------------------------------------------------------- */
+void cpConstraintFree(cpConstraint *constraint);                             /* cpConstraint.h:33 */
+cpSpace *cpConstraintGetSpace(const cpConstraint *constraint);               /* cpConstraint.h:36 */
+cpBody *cpConstraintGetBodyA(const cpConstraint *constraint);                /* cpConstraint.h:39 */
+cpBody *cpConstraintGetBodyB(const cpConstraint *constraint);                /* cpConstraint.h:42 */
+cpFloat cpConstraintGetMaxForce(const cpConstraint *constraint);             /* cpConstraint.h:45 */
+void cpConstraintSetMaxForce(cpConstraint *constraint, cpFloat maxForce);    /* cpConstraint.h:47 */
+cpFloat cpConstraintGetErrorBias(const cpConstraint *constraint);            /* cpConstraint.h:50 */
+void cpConstraintSetErrorBias(cpConstraint *constraint, cpFloat errorBias);  /* cpConstraint.h:54 */
+cpFloat cpConstraintGetMaxBias(const cpConstraint *constraint);              /* cpConstraint.h:57 */
+void cpConstraintSetMaxBias(cpConstraint *constraint, cpFloat maxBias);      /* cpConstraint.h:59 */
+cpBool cpConstraintGetCollideBodies(const cpConstraint *constraint);         /* cpConstraint.h:62 */
+void cpConstraintSetCollideBodies(cpConstraint *constraint, cpBool collideBodies); /* cpConstraint.h:64 */
+void cpConstraintSetPreSolveFunc(cpConstraint *constraint, cpConstraintPreSolveFunc f);   /* cpConstraint.h:69 */
+void cpConstraintSetPostSolveFunc(cpConstraint *constraint, cpConstraintPostSolveFunc f); /* cpConstraint.h:74 */
+cpDataPointer cpConstraintGetUserData(const cpConstraint *constraint);       /* cpConstraint.h:77 */
+void cpConstraintSetUserData(cpConstraint *constraint, cpDataPointer data);  /* cpConstraint.h:79 */
+cpFloat cpConstraintGetImpulse(cpConstraint *constraint);                    /* cpConstraint.h:82 */
+
+cpBool cpConstraintIsPivotJoint(const cpConstraint *constraint);             /* cpPivotJoint.h:26 */
+cpConstraint *cpPivotJointNew(cpBody *a, cpBody *b, cpVect pivot);           /* cpPivotJoint.h:33 */
+cpConstraint *cpPivotJointNew2(cpBody *a, cpBody *b, cpVect anchorA, cpVect anchorB); /* cpPivotJoint.h:35 */
+cpVect cpPivotJointGetAnchorA(const cpConstraint *constraint);               /* cpPivotJoint.h:38 */
+cpVect cpPivotJointGetAnchorB(const cpConstraint *constraint);               /* cpPivotJoint.h:43 */
+
+cpBool cpConstraintIsPinJoint(const cpConstraint *constraint);               /* cpPinJoint.h:26 */
+cpConstraint *cpPinJointNew(cpBody *a, cpBody *b, cpVect anchorA, cpVect anchorB);    /* cpPinJoint.h:33 */
+cpVect cpPinJointGetAnchorA(const cpConstraint *constraint);                 /* cpPinJoint.h:36 */
+cpVect cpPinJointGetAnchorB(const cpConstraint *constraint);                 /* cpPinJoint.h:41 */
+cpFloat cpPinJointGetDist(const cpConstraint *constraint);                   /* cpPinJoint.h:46 */
+
+cpBool cpConstraintIsSlideJoint(const cpConstraint *constraint);             /* cpSlideJoint.h:26 */
+cpConstraint *cpSlideJointNew(cpBody *a, cpBody *b, cpVect anchorA, cpVect anchorB, cpFloat min, cpFloat max); /* cpSlideJoint.h:33 */
+cpVect cpSlideJointGetAnchorA(const cpConstraint *constraint);               /* cpSlideJoint.h:36 */
+cpVect cpSlideJointGetAnchorB(const cpConstraint *constraint);               /* cpSlideJoint.h:41 */
+cpFloat cpSlideJointGetMin(const cpConstraint *constraint);                  /* cpSlideJoint.h:46 */
+cpFloat cpSlideJointGetMax(const cpConstraint *constraint);                  /* cpSlideJoint.h:51 */
+
+/* ------------------------------------------------------------------------
+ * Arbiters: cpArbiter.h:32-119.  Arbiter handles are valid from the
+ * cpBodyEachArbiter callback until the next cpSpaceStep, as in the reference.
+ * ---------------------------------------------------------------------- */
+cpFloat cpArbiterGetRestitution(const cpArbiter *arb);               /* cpArbiter.h:32  */
+cpFloat cpArbiterGetFriction(const cpArbiter *arb);                  /* cpArbiter.h:36  */
+cpVect cpArbiterGetSurfaceVelocity(cpArbiter *arb);                  /* cpArbiter.h:41  */
+cpVect cpArbiterTotalImpulse(const cpArbiter *arb);                  /* cpArbiter.h:55  */
+cpFloat cpArbiterTotalKE(const cpArbiter *arb);                      /* cpArbiter.h:58  */
+void cpArbiterGetShapes(const cpArbiter *arb, cpShape **a, cpShape **b); /* cpArbiter.h:67 */
+void cpArbiterGetBodies(const cpArbiter *arb, cpBody **a, cpBody **b);   /* cpArbiter.h:75 */
+cpContactPointSet cpArbiterGetContactPointSet(const cpArbiter *arb); /* cpArbiter.h:99  */
+cpBool cpArbiterIsFirstContact(const cpArbiter *arb);                /* cpArbiter.h:106 */
+int cpArbiterGetCount(const cpArbiter *arb);                         /* cpArbiter.h:111 */
+cpVect cpArbiterGetNormal(const cpArbiter *arb);                     /* cpArbiter.h:113 */
+cpVect cpArbiterGetPointA(const cpArbiter *arb, int i);              /* cpArbiter.h:115 */
+cpVect cpArbiterGetPointB(const cpArbiter *arb, int i);              /* cpArbiter.h:117 */
+cpFloat cpArbiterGetDepth(const cpArbiter *arb, int i);              /* cpArbiter.h:119 */
+
+/* ------------------------------------------------------------------------
+ * GPU-only additions (no counterpart in the reference).
+ * ---------------------------------------------------------------------- */
+
+/* Solver mode for a space.  ORDERED sweeps arbiters and constraints in the
+ * exact sequence cpSpaceStep uses (bit-compatible results); COLORED runs
+ * graph-coloured Gauss-Seidel over a device sweep-and-prune pair set, which
+ * is faster for large spaces but changes the sweep order. */
+typedef enum cpGpuSolverMode {
+	CP_GPU_SOLVER_ORDERED = 0,
+	CP_GPU_SOLVER_COLORED = 1,
+} cpGpuSolverMode;
+
+/* Error codes returned by cpGpuGetLastError(). */
+enum {
+	CP_GPU_OK = 0,
+	CP_GPU_ERR_CUDA = 1,          /* a CUDA runtime call failed */
+	CP_GPU_ERR_OVERFLOW = 2,      /* a device table or list ran out of room */
+	CP_GPU_ERR_UNSUPPORTED = 3,   /* the space uses a feature the GPU step does not run */
+	CP_GPU_ERR_TIMEOUT = 4,       /* a bounded device wait gave up */
+	CP_GPU_ERR_NO_DEVICE = 5,     /* no CUDA device is visible */
+	CP_GPU_ERR_ARGUMENT = 6,      /* invalid argument to a cpGpu* entry point */
+};
+
+void cpGpuSetSolverMode(cpSpace *space, int mode);
+int cpGpuGetSolverMode(const cpSpace *space);
+/* Returns and clears the last device-side error (CP_GPU_* code). */
+int cpGpuGetLastError(void);
+/* Human-readable description of the last error. */
+const char *cpGpuGetLastErrorString(void);
+/* Launch all of this library's work on the given cudaStream_t (NULL = the
+ * library's own stream).  Call before the first cpSpaceStep. */
+void cpGpuSetStream(void *cudaStream);
+/* Wait for all queued device work of the space; then host getters are free. */
+void cpGpuSpaceSync(cpSpace *space);
+
+/* Batched stepping: spaces added to a batch are stepped together, one
+ * persistent launch per phase for all of them.  Every space keeps its own
+ * parameters and its exact reference sweep order. */
+typedef struct cpGpuBatch cpGpuBatch;
+cpGpuBatch *cpGpuBatchNew(void);
+void cpGpuBatchFree(cpGpuBatch *batch);
+int cpGpuBatchAddSpace(cpGpuBatch *batch, cpSpace *space);
+/* Step every space of the batch `steps` times with time step dt.  With
+ * use_graph != 0 the per-step launches are captured once in a CUDA graph
+ * and replayed. */
+int cpGpuBatchStep(cpGpuBatch *batch, cpFloat dt, int steps, int use_graph);
+
+/* Debug/state export used by the parity tests.  Layouts are fixed:
+ *   bodies:      18 doubles per dynamic body, in space order:
+ *                p.x p.y v.x v.y a w f.x f.y t vb.x vb.y wb tf.a tf.b tf.c tf.d tf.tx tf.ty
+ *   arbiters:    34 doubles per arbiter, in solve order:
+ *                hashidA hashidB count state n.x n.y e u svr.x svr.y, then per
+ *                contact slot (2): r1.x r1.y r2.x r2.y nMass tMass bounce jnAcc jtAcc jBias bias hash
+ *   constraints: 8 doubles per constraint, in space order:
+ *                kind j0 j1 r1.x r1.y r2.x r2.y bias0
+ * Each returns the number of records available (writes at most max). */
+int cpGpuDebugBodies(cpSpace *space, double *out, int max);
+int cpGpuDebugArbiters(cpSpace *space, double *out, int max);
+int cpGpuDebugConstraints(cpSpace *space, double *out, int max);
+/* Overwrite the dynamic bodies' state (same 18-double layout) and the
+ * constraints' accumulated impulses; used to run one step from a state
+ * taken from another implementation. */
+int cpGpuDebugSetBodies(cpSpace *space, const double *in, int count);
+
+/* Per-phase device time of the last step of the space, in milliseconds,
+ * measured with CUDA events on the launching stream (0 when timing is off).
+ * Phases: 0 integrate+cache, 1 broadphase, 2 narrowphase, 3 arbiters,
+ * 4 schedule, 5 prestep+warmstart, 6 solve. */
+void cpGpuSetTiming(int enabled);
+int cpGpuGetPhaseTimes(cpSpace *space, double *ms, int max);
+/* Number of kernel launches issued by this library since the last reset. */
+long long cpGpuGetLaunchCount(int reset);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* CHIPMUNK_GB300_H */

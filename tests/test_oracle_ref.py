@@ -1,0 +1,68 @@
+"""Pins the CPU restatement (oracle/cp_oracle.c) to the unmodified reference.
+
+Both libraries are driven through the same C API on the same seeded scenes;
+after every step the full simulation state -- every dynamic body, every
+arbiter in solve order with all contact fields, every joint -- must be
+bit-identical.  Runs where the reference was built (oracle/build_ref.sh);
+skipped elsewhere.  The known-answer cases of the reference's own tests run
+on both libraries.
+"""
+import numpy as np
+import pytest
+
+from chipmunk2d_gb300 import Scene
+import known_answers as ka
+
+# (workload, size, steps, dt): small sizes keep the CPU suite to seconds.
+CASES = [
+    (1, 14, 400, 1 / 60),
+    (2, 800, 200, 1 / 60),
+    (3, 900, 120, 1 / 60),
+    (4, 300, 200, 1 / 60),
+    (5, 64, 240, 1 / 120),
+]
+
+
+@pytest.mark.parametrize("cfg,size,steps,dt", CASES)
+def test_oracle_bit_exact_per_step(ref_lib, oracle_lib, cfg, size, steps, dt):
+    r = Scene(ref_lib, cfg, size)
+    o = Scene(oracle_lib, cfg, size)
+    try:
+        assert r.nbodies == o.nbodies
+        for s in range(steps):
+            r.step(dt)
+            o.step(dt)
+            np.testing.assert_array_equal(o.bodies(), r.bodies(), err_msg="bodies, step %d" % s)
+            np.testing.assert_array_equal(o.arbiters(), r.arbiters(), err_msg="arbiters, step %d" % s)
+            np.testing.assert_array_equal(o.constraints(), r.constraints(), err_msg="joints, step %d" % s)
+        np.testing.assert_array_equal(o.public(), r.public())
+        np.testing.assert_array_equal(o.impulses(), r.impulses())
+    finally:
+        r.free()
+        o.free()
+
+
+@pytest.mark.parametrize("which", ["ref", "oracle"])
+def test_time_stepping_known_answer(request, which):
+    lib = request.getfixturevalue(which + "_lib")
+    assert ka.time_stepping(lib) == ka.TIME_STEPPING_EXPECTED
+
+
+@pytest.mark.parametrize("which", ["ref", "oracle"])
+def test_resting_ball_known_answer(request, which):
+    lib = request.getfixturevalue(which + "_lib")
+    y, slop = ka.resting_ball(lib)
+    assert abs(y - 2.0) <= 1.1 * slop
+
+
+@pytest.mark.parametrize("which", ["ref", "oracle"])
+@pytest.mark.parametrize("case", range(len(ka.HULL_CASES)))
+def test_convex_hull_known_answer(request, which, case):
+    lib = request.getfixturevalue(which + "_lib")
+    pts, count, expected = ka.HULL_CASES[case]
+    ka.check_hull_case(lib, pts, count, expected)
+
+
+def test_random_hulls_match_reference(ref_lib, oracle_lib):
+    for n, seed in ((100, 1), (1000, 2), (10000, 3)):
+        assert ka.random_hull_fixed_point(oracle_lib, n, seed) == ka.random_hull_fixed_point(ref_lib, n, seed)
