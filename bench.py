@@ -1,0 +1,354 @@
+"""Throughput benchmark of the GB300 cpSpaceStep drop-in.
+
+Workload (default): 20,000 circles (r ~ U[0.5,2], density 1, u 0.7, e 0.1)
+in a 1000x2000 box of 4 static segments, v ~ N(0,5) per axis, gravity
+(0,-100), dt 1/60, 10 iterations, seed 1 -- the single-large-space
+configuration of the reference's benchmark plan.  A step is one cpSpaceStep.
+
+Metric: body-steps/s = dynamic bodies x timed steps / device seconds.
+
+  value      device time of the timed steps (CUDA events on the library's
+             stream), state resident in HBM.
+  e2e        the same steps through the public C API as a program uses it:
+             cpSpaceStep, then every body's position, velocity and angle read
+             back through cpBodyGet* (device->host copy inside the timed
+             region), host wall clock.
+  roofline   the dominant phase's algorithmic bytes per launch / its mean
+             event-timed duration, against the measured HBM copy bandwidth.
+  cpu_baseline  the CPU restatement of the same path (oracle/cp_oracle.c,
+             "port"), one core, on a bounded sample of the same workload.
+
+--impl reference runs only that CPU implementation, on the same workload
+and metric, and prints its own JSON line.
+
+Usage: python bench.py [--gpus N] [--steps K] [--warmup W] [--mode ordered|colored]
+                       [--impl ours|reference] [--workload circles|pyramid|mixed|batch]
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+REPO = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, REPO)
+
+WORKLOADS = {
+    # name: (scene config, size, dt, description)
+    "circles": (2, 20000, 1 / 60, "20000 circles r~U[0.5,2] in a 1000x2000 box, 10 it, dt 1/60, seed 1"),
+    "pyramid": (1, 14, 1 / 60, "14-row pyramid of 105 30x30 boxes, 10 it, dt 1/60"),
+    "mixed": (3, 30000, 1 / 60, "30000 circles/polys/segments + 500 pivot chains of 20, 15 it, dt 1/60, seed 2"),
+}
+
+# Algorithmic bytes per unit (FP64, compulsory traffic) per phase.
+BYTES_PER_BODY_POS = 184      # integrate position: read p,v,vb,a,w,wb,cog; write p,a,transform,zeroed bias
+BYTES_PER_CIRCLE_CACHE = 120  # shape cache + AABB of a circle
+BYTES_PER_BODY_VEL = 104      # integrate velocity
+BYTES_PER_CONTACT_PRESTEP = 208
+BYTES_PER_CONTACT_ITER = 376  # one sequential-impulse application of one contact
+
+
+def log(*a):
+    print(*a, file=sys.stderr, flush=True)
+
+
+class ClockSampler:
+    """Samples nvidia-smi clocks and throttle reasons during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu=0):
+        self.gpu = gpu
+        self.proc = None
+        self.lines = []
+        self.thread = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + self.FIELDS,
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.proc = None
+            return
+        self.thread = threading.Thread(target=self._read, daemon=True)
+        self.thread.start()
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        if self.thread:
+            self.thread.join(timeout=2)
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def measured_peaks():
+    path = os.path.join(REPO, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        with open(path) as f:
+            p = json.load(f)
+        return float(p.get("hbm_gbs", 6800.0)), "measured"
+    return 6800.0, "fallback"
+
+
+def oracle_lib():
+    so = os.path.join(REPO, "oracle", "_build", "liboracle.so")
+    if not os.path.exists(so):
+        subprocess.check_call([os.path.join(REPO, "oracle", "build_oracle.sh")], stdout=subprocess.DEVNULL)
+    from chipmunk2d_gb300 import bind
+    return bind(so)
+
+
+def cpu_sample(workload, budget_s=15.0, warm=5):
+    """Times the CPU restatement on the workload: `warm` untimed steps, then
+    steps until about budget_s seconds of CPU time have been spent."""
+    from chipmunk2d_gb300 import Scene
+    cfg, size, dt, _ = WORKLOADS[workload]
+    lib = oracle_lib()
+    sc = Scene(lib, cfg, size)
+    sc.step(dt, warm)
+    steps = 0
+    t0 = time.perf_counter()
+    while True:
+        sc.step(dt, 1)
+        steps += 1
+        el = time.perf_counter() - t0
+        if el >= budget_s or steps >= 2000:
+            break
+    n = sc.nbodies
+    sc.free()
+    return n * steps / el, steps, el, n
+
+
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    workload = args.workload
+    cfg, size, dt, desc = WORKLOADS[workload]
+    from chipmunk2d_gb300 import Scene
+    lib = oracle_lib()
+    sc = Scene(lib, cfg, size)
+    n = sc.nbodies
+    sc.step(dt, args.warmup)
+    # each timed step is a bounded sample: the whole run stays within minutes
+    per_step = []
+    t_all = time.perf_counter()
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        sc.step(dt, 1)
+        per_step.append(time.perf_counter() - t0)
+        if time.perf_counter() - t_all > 150.0:
+            break
+    sc.free()
+    k = len(per_step)
+    secs = sum(per_step)
+    value = n * k / secs
+    line = {
+        "impl": "reference", "metric": "body-steps/s", "value": value, "unit": "body-steps/s",
+        "n_gpus": args.gpus, "steps": k, "warmup": args.warmup, "ms_per_step": 1000 * secs / k,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic", "config": {"workload": workload, "description": desc, "bodies": n},
+        "cpu_baseline": {"value": value, "unit": "body-steps/s", "cores": 1, "kind": "port",
+                         "sample": "%d steps of the %s workload after %d warm-up steps" % (k, workload, args.warmup)},
+        "e2e": {"value": value, "unit": "body-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args):
+    import ctypes
+    import torch
+    from chipmunk2d_gb300 import load_gpu_library, Scene
+
+    world_size = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local_rank)
+    dist = None
+    if world_size > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+
+    lib = load_gpu_library()
+    stream = torch.cuda.Stream()
+    lib.cpGpuSetStream(ctypes.c_void_p(stream.cuda_stream))
+    cfg, size, dt, desc = WORKLOADS[args.workload]
+    mode = 1 if args.mode == "colored" else 0
+
+    def make():
+        sc = Scene(lib, cfg, size, seed=cfg + 1000 * rank if world_size > 1 else None)
+        lib.cpGpuSetSolverMode(sc.space, mode)
+        return sc
+
+    # ---- device-timed run (state resident in HBM) ----
+    sc = make()
+    n = sc.nbodies
+    for _ in range(args.warmup):
+        lib.cpSpaceStep(sc.space, dt)
+    torch.cuda.synchronize()
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+    lib.cpGpuGetLaunchCount(1)
+    clocks = ClockSampler(local_rank)
+    clocks.start()
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    for i in range(args.steps):
+        with torch.cuda.stream(stream):
+            flush.fill_(float(i))          # L2 flush between timed steps (not timed)
+            ev[i][0].record(stream)
+        lib.cpSpaceStep(sc.space, dt)
+        with torch.cuda.stream(stream):
+            ev[i][1].record(stream)
+    torch.cuda.synchronize()
+    launches = lib.cpGpuGetLaunchCount(1)
+    step_ms = [a.elapsed_time(b) for a, b in ev]
+    total_s = sum(step_ms) / 1000.0
+    if dist:
+        t = torch.tensor([total_s], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total_s = float(t.item())
+        dist.barrier()
+    clk = clocks.stop()
+    err = lib.cpGpuGetLastError()
+    if err:
+        raise RuntimeError("GPU step failed: %s" % lib.cpGpuGetLastErrorString().decode())
+    arbs = sc.arbiters()
+    contacts = int(arbs[:, 2].sum()) if len(arbs) else 0
+
+    # ---- per-phase timing pass (phase events, separate run) ----
+    lib.cpGpuSetTiming(1)
+    phase = np.zeros(7)
+    nph = min(10, args.steps)
+    buf = np.zeros(8)
+    for _ in range(nph):
+        lib.cpSpaceStep(sc.space, dt)
+        lib.cpGpuGetPhaseTimes(sc.space, buf.ctypes.data, 8)
+        phase += buf[:7]
+    lib.cpGpuSetTiming(0)
+    phase /= nph
+    sc.free()
+
+    # ---- end-to-end run through the public C API ----
+    sc = make()
+    for _ in range(args.warmup):
+        lib.cpSpaceStep(sc.space, dt)
+    out = np.zeros(8 * n)
+    sc.public()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    e2e_steps = min(args.steps, 200)
+    for _ in range(e2e_steps):
+        lib.cpSpaceStep(sc.space, dt)
+        lib.cpx_scene_dump_public(sc.h, out.ctypes.data)
+    e2e_s = time.perf_counter() - t0
+    sc.free()
+
+    value = n * args.steps * world_size / total_s
+    e2e_value = n * e2e_steps * world_size / e2e_s
+
+    # ---- roofline of the dominant phase ----
+    names = ["integrate+cache", "broadphase tree", "narrowphase", "arbiters", "schedule", "prestep+velocity", "solve"]
+    dom = int(np.argmax(phase))
+    iters = 10 if cfg != 3 else 15
+    algo = {
+        0: n * (BYTES_PER_BODY_POS + BYTES_PER_CIRCLE_CACHE),
+        1: 32 * sc.nshapes,
+        2: contacts * (24 * 2 + 4 + 16 + 40 + 8),
+        3: contacts * 104,
+        4: 16 * len(arbs),
+        5: contacts * BYTES_PER_CONTACT_PRESTEP + n * BYTES_PER_BODY_VEL,
+        6: contacts * BYTES_PER_CONTACT_ITER * (iters + 1),
+    }[dom]
+    peak, peak_kind = measured_peaks()
+    achieved = algo / (phase[dom] / 1000.0) / 1e9 if phase[dom] > 0 else 0.0
+    traffic = None
+    tpath = os.path.join(REPO, "profiles", "traffic.json")
+    if os.path.exists(tpath):
+        with open(tpath) as f:
+            traffic = json.load(f).get(args.workload, {}).get(names[dom])
+
+    cpu_v, cpu_steps, cpu_s, _ = cpu_sample(args.workload, budget_s=args.cpu_seconds) if rank == 0 else (None, 0, 0, 0)
+
+    line = {
+        "metric": "body-steps/s", "value": value, "unit": "body-steps/s", "n_gpus": world_size,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000 * total_s / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic",
+        "config": {"workload": args.workload, "description": desc, "bodies": n, "solver": args.mode,
+                   "arbiters_final": int(len(arbs)), "contacts_final": contacts,
+                   "l2": "flushed between timed steps (256 MB fill, untimed)",
+                   "parallelism": "replicas" if world_size > 1 else "single"},
+        "e2e": {"value": e2e_value, "unit": "body-steps/s", "h2d_bytes_per_step": 88,
+                "d2h_bytes_per_step": 18 * 8 * (n + 5) + 64, "steps": e2e_steps,
+                "path": "cpSpaceStep + cpBodyGetPosition/Velocity/Angle for every body (ctypes)"},
+        "roofline": {"bound": "hbm", "kernel": names[dom], "achieved": achieved, "peak": peak,
+                     "unit": "GB/s", "frac": achieved / peak, "peak_kind": peak_kind,
+                     "traffic": traffic, "algorithmic_bytes_per_launch": algo},
+        "phase_ms": dict(zip(names, [round(float(x), 4) for x in phase])),
+        "gpu_launches": int(launches),
+        "clocks": clk,
+        "cpu_baseline": {"value": cpu_v, "unit": "body-steps/s", "cores": 1, "kind": "port",
+                         "sample": "%d steps (%.1f s) of the %s workload after 5 warm-up steps" % (cpu_steps, cpu_s, args.workload)},
+    }
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if dist:
+        dist.destroy_process_group()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=120)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--mode", default="ordered", choices=["ordered", "colored"])
+    ap.add_argument("--workload", default="circles", choices=sorted(WORKLOADS))
+    ap.add_argument("--cpu-seconds", type=float, default=15.0)
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,1820 @@
+/*
+ * cp_host.c -- host side of libchipmunk_gb300: the Chipmunk2D C API
+ * (include/chipmunk_gb300.h) over device-resident simulation state.
+ *
+ * Objects (bodies, shapes, constraints, spaces) are host structs holding
+ * their creation-time data.  The first cpSpaceStep packs the space into a
+ * device set (cpg_device.h) and from then on the dynamic state lives in
+ * HBM: cpSpaceStep enqueues the step's kernels (cpg_kernels.cu) on the
+ * library's stream and returns; getters synchronise and copy state back
+ * lazily, setters mark it dirty for upload before the next step.  The
+ * index insertions made by cpSpaceAddShape are recorded with the shape's
+ * box and body velocity at the time of the call and replayed on the device
+ * in the same order, so the device AABB tree grows exactly as the
+ * reference's does.
+ *
+ * There is no CPU fallback: a space that needs a feature the device step
+ * does not implement (custom integration callbacks, sleeping) is not
+ * stepped and cpGpuGetLastError() reports CP_GPU_ERR_UNSUPPORTED.
+ *
+ * Host floating-point code (moments, hulls, add-time shape caches, the
+ * per-step pow() terms) follows the reference's expressions and is built
+ * with -ffp-contract=off so it rounds identically.
+ */
+#define _GNU_SOURCE
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+#include <stdarg.h>
+#include <cuda_runtime.h>
+#include "../../include/chipmunk_gb300.h"
+#include "cpg_device.h"
+
+#define INF_ ((cpFloat)INFINITY)
+
+/* ====================================================================
+ * Errors
+ * ==================================================================== */
+const char *cpVersionString = "7.0.3";
+
+static int g_error = CP_GPU_OK;
+static char g_errmsg[256] = "";
+
+static void set_error(int code, const char *fmt, ...)
+{
+	if(g_error == CP_GPU_OK){
+		g_error = code;
+		va_list ap;
+		va_start(ap, fmt);
+		vsnprintf(g_errmsg, sizeof(g_errmsg), fmt, ap);
+		va_end(ap);
+	}
+}
+
+int cpGpuGetLastError(void) { int e = g_error; g_error = CP_GPU_OK; return e; }
+const char *cpGpuGetLastErrorString(void) { return g_errmsg; }
+
+/* chipmunk.c:31-54 */
+void cpMessage(const char *condition, const char *file, int line, int isError, int isHardError, const char *message, ...)
+{
+	fprintf(stderr, (isError ? "Aborting due to Chipmunk error: " : "Chipmunk warning: "));
+	va_list vargs;
+	va_start(vargs, message);
+	vfprintf(stderr, message, vargs);
+	va_end(vargs);
+	fprintf(stderr, "\n\tFailed condition: %s\n\tSource:%s:%d\n", condition, file, line);
+	(void)isHardError;
+}
+
+/* cpAssertHard semantics (chipmunk.h:58): report and abort. */
+#define ASSERT_HARD(cond, msg) do { if(!(cond)){ cpMessage(#cond, __FILE__, __LINE__, 1, 1, msg); abort(); } } while(0)
+
+static int cuda_ok(cudaError_t e, const char *what)
+{
+	if(e == cudaSuccess) return 1;
+	set_error(CP_GPU_ERR_CUDA, "%s: %s", what, cudaGetErrorString(e));
+	return 0;
+}
+
+/* ====================================================================
+ * Scalar helpers (chipmunk_types.h:137-168)
+ * ==================================================================== */
+static inline cpFloat hmax(cpFloat a, cpFloat b) { return (a > b) ? a : b; }
+static inline cpFloat hmin(cpFloat a, cpFloat b) { return (a < b) ? a : b; }
+static inline cpFloat habs(cpFloat f) { return (f < 0) ? -f : f; }
+static inline cpTransform rigid_inverse(cpTransform t)
+{
+	return cpTransformNewTranspose(t.d, -t.c, (t.c*t.ty - t.tx*t.d), -t.b, t.a, (t.tx*t.b - t.a*t.ty));
+}
+
+/* ====================================================================
+ * Objects
+ * ==================================================================== */
+typedef struct DevSet DevSet;
+
+struct cpBody {
+	cpBodyVelocityFunc velocity_func;
+	cpBodyPositionFunc position_func;
+	cpFloat m, m_inv, i, i_inv;
+	cpVect cog, p, v, f;
+	cpFloat a, w, t;
+	cpTransform transform;
+	cpVect v_bias;
+	cpFloat w_bias;
+	cpFloat idleTime;
+	cpDataPointer userData;
+	cpSpace *space;
+	int index;                 /* world-local device index */
+	cpShape *shapeList;
+	cpConstraint *constraintList;
+};
+
+struct cpShape {
+	int kind;
+	cpSpace *space;
+	cpBody *body;
+	cpFloat mass_m, mass_i, mass_area;
+	cpVect mass_cog;
+	cpBB bb;
+	cpBool sensor;
+	cpFloat e, u;
+	cpVect surfaceV;
+	cpDataPointer userData;
+	cpCollisionType ctype;
+	cpShapeFilter filter;
+	cpShape *next, *prev;
+	cpHashValue hashid;
+	cpFloat r;
+	cpVect c, tc;                          /* circle */
+	cpVect sa, sb, sn, ta, tb, tn;         /* segment */
+	cpVect a_tangent, b_tangent;
+	int count;                             /* polygon */
+	cpVect *lv, *ln, *gv, *gn;             /* local/world planes */
+};
+
+struct cpConstraint {
+	int kind;
+	cpSpace *space;
+	cpBody *a, *b;
+	cpConstraint *next_a, *next_b;
+	cpFloat maxForce, errorBias, maxBias;
+	cpBool collideBodies;
+	cpConstraintPreSolveFunc preSolve;
+	cpConstraintPostSolveFunc postSolve;
+	cpDataPointer userData;
+	cpVect anchorA, anchorB;
+	cpFloat dist, min, max;
+	int index;
+	cpgJoint rec;                          /* last downloaded device record */
+};
+
+/* Snapshot of a device arbiter, valid until the next step. */
+struct cpArbiter {
+	cpShape *a, *b;
+	cpBody *body_a, *body_b;
+	int count, state;
+	cpVect n, surface_vr;
+	cpFloat e, u;
+	cpBool swapped;
+	cpgContact c[2];
+};
+
+struct cpSpace {
+	int iterations;
+	cpVect gravity;
+	cpFloat damping, idleSpeedThreshold, sleepTimeThreshold;
+	cpFloat collisionSlop, collisionBias;
+	cpTimestamp collisionPersistence;
+	cpDataPointer userData;
+	cpTimestamp stamp;
+	cpFloat curr_dt;
+	cpHashValue shapeIDCounter;
+	int mode;
+
+	cpBody **dyn; int ndyn, capdyn;
+	cpBody **stat; int nstat, capstat;
+	cpShape **shapes; int nshapes, capshapes;
+	cpConstraint **cons; int ncons, capcons;
+	cpgOp *ops; int nops, capops;           /* insertions not yet on the device */
+	cpBody staticBody;
+
+	DevSet *dev;                            /* device set holding this space */
+	int world;                              /* index in the set */
+	int ownsDev;
+	int builtBodies, builtShapes, builtCons;
+	int hostStale;                          /* device bodies newer than host */
+	int consStale;                          /* device joint records newer than host */
+	int bodyDirty, shapeDirty, consDirty;   /* host newer than device */
+	double jointDt;                         /* dt the joint bias terms were made for */
+
+	cpArbiter *snap; int nsnap, capsnap; int snapValid;
+	float phaseMs[8];
+};
+
+static void push_(void ***arr, int *n, int *cap, void *p)
+{
+	if(*n == *cap){
+		*cap = *cap ? 2*(*cap) : 64;
+		*arr = (void **)realloc(*arr, sizeof(void *)*(size_t)(*cap));
+	}
+	(*arr)[(*n)++] = p;
+}
+
+/* ====================================================================
+ * Device sets
+ * ==================================================================== */
+struct DevSet {
+	cpgSet d;                 /* device pointers; counts valid on host too */
+	cpgWorld *hworld;
+	cpgParams *hparams;       /* pinned */
+	int *hstats;              /* pinned */
+	cudaEvent_t statsEvent;
+	int statsPending;
+	cpSpace **spaces;
+	int nspaces;
+	void *slab;
+	cpgArb *gather;           /* arbiter snapshot staging */
+	int gatherCap;
+};
+
+static cudaStream_t g_stream = NULL;
+static int g_stream_user = 0;
+static int g_timing = 0;
+
+static cudaStream_t lib_stream(void)
+{
+	if(!g_stream && !g_stream_user) cudaStreamCreateWithFlags(&g_stream, cudaStreamNonBlocking);
+	return g_stream;
+}
+
+void cpGpuSetStream(void *stream) { g_stream = (cudaStream_t)stream; g_stream_user = (stream != NULL); }
+void cpGpuSetTiming(int enabled) { g_timing = enabled; }
+long long cpGpuGetLaunchCount(int reset) { return cpg_launch_count(reset); }
+
+static const int kPrimes[] = {
+	/* leaf-set table sizes (src/prime.h:25-55) */
+	5, 13, 23, 47, 97, 193, 389, 769, 1543, 3079, 6151, 12289, 24593, 49157,
+	98317, 196613, 393241, 786433, 1572869, 3145739, 6291469, 12582917,
+	25165843, 50331653, 100663319, 201326611, 402653189, 805306457, 1610612741, 0,
+};
+
+static unsigned next_prime(unsigned n)
+{
+	int i = 0;
+	while(n > (unsigned)kPrimes[i] && kPrimes[i + 1]) i++;
+	return (unsigned)kPrimes[i];
+}
+
+/* Largest table size the leaf set reaches holding n leaves
+ * (cpHashSet.c:81-85, 152-176: grow when entries >= size). */
+static int bins_for(int n)
+{
+	unsigned size = next_prime(0);
+	for(int e = 1; e <= n; e++) if((unsigned)e >= size) size = next_prime(size + 1);
+	return (int)size;
+}
+
+typedef struct Layout {
+	size_t off;
+	size_t bytes;
+} Layout;
+
+static size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
+
+/* Carve the set's arrays out of one device allocation. */
+#define CARVE(field, type, count) do { \
+	size_t bytes_ = align256(sizeof(type)*(size_t)((count) > 0 ? (count) : 1)); \
+	if(pass) d->field = (type *)(base + total); \
+	total += bytes_; \
+} while(0)
+
+static size_t carve_set(cpgSet *d, char *base, int pass)
+{
+	size_t total = 0;
+	int W = d->nworlds, NB = d->totalBodies, NS = d->totalShapes, NV = d->totalVerts, NC = d->totalCons;
+	CARVE(world, cpgWorld, W); CARVE(params, cpgParams, W); CARVE(tree, cpgTree, W);
+	CARVE(px, double, NB); CARVE(py, double, NB); CARVE(vx, double, NB); CARVE(vy, double, NB);
+	CARVE(fx, double, NB); CARVE(fy, double, NB); CARVE(ang, double, NB); CARVE(w, double, NB); CARVE(tq, double, NB);
+	CARVE(ta, double, NB); CARVE(tb, double, NB); CARVE(tc, double, NB); CARVE(td, double, NB);
+	CARVE(ttx, double, NB); CARVE(tty, double, NB);
+	CARVE(vbx, double, NB); CARVE(vby, double, NB); CARVE(wb, double, NB);
+	CARVE(m, double, NB); CARVE(minv, double, NB); CARVE(i, double, NB); CARVE(iinv, double, NB);
+	CARVE(cogx, double, NB); CARVE(cogy, double, NB);
+	CARVE(btype, int, NB); CARVE(bworld, int, NB); CARVE(partStart, int, NB); CARVE(partCount, int, NB);
+	CARVE(parts, int, d->totalParts); CARVE(last, int, NB);
+	CARVE(skind, int, NS); CARVE(sbody, int, NS); CARVE(sleaf, int, NS); CARVE(sworld, int, NS);
+	CARVE(svoff, int, NS); CARVE(svcount, int, NS);
+	CARVE(sr, double, NS);
+	CARVE(s0x, double, NS); CARVE(s0y, double, NS); CARVE(s1x, double, NS); CARVE(s1y, double, NS);
+	CARVE(snx, double, NS); CARVE(sny, double, NS);
+	CARVE(w0x, double, NS); CARVE(w0y, double, NS); CARVE(w1x, double, NS); CARVE(w1y, double, NS);
+	CARVE(wnx, double, NS); CARVE(wny, double, NS);
+	CARVE(atx, double, NS); CARVE(aty, double, NS); CARVE(btx, double, NS); CARVE(bty, double, NS);
+	CARVE(bbl, double, NS); CARVE(bbb, double, NS); CARVE(bbr, double, NS); CARVE(bbt, double, NS);
+	CARVE(se, double, NS); CARVE(su, double, NS); CARVE(svx, double, NS); CARVE(svy, double, NS);
+	CARVE(sgroup, unsigned long long, NS); CARVE(scat, unsigned, NS); CARVE(smask, unsigned, NS);
+	CARVE(ssensor, unsigned char, NS); CARVE(shash, unsigned long long, NS);
+	CARVE(lvx, double, NV); CARVE(lvy, double, NV); CARVE(lnx, double, NV); CARVE(lny, double, NV);
+	CARVE(gvx, double, NV); CARVE(gvy, double, NV); CARVE(gnx, double, NV); CARVE(gny, double, NV);
+	CARVE(nodes, cpgNode, d->totalNodes); CARVE(pairs, cpgPair, d->totalPairs);
+	CARVE(dbins, int, d->totalDBins); CARVE(sbins, int, d->totalSBins);
+	CARVE(ops, cpgOp, d->totalOps);
+	CARVE(cands, cpgCand, d->totalCands); CARVE(narrow, cpgNarrow, d->totalCands);
+	CARVE(candArb, int, d->totalCands); CARVE(arbList, int, d->totalCands); CARVE(prevList, int, d->totalCands);
+	CARVE(prevCount, int, W);
+	CARVE(keys, unsigned long long, d->arbCap); CARVE(arbs, cpgArb, d->arbCap);
+	CARVE(joints, cpgJoint, NC); CARVE(jbias, double, NC);
+	CARVE(unitA, int, d->totalUnits); CARVE(unitB, int, d->totalUnits);
+	CARVE(unitLevel, int, d->totalUnits); CARVE(unitOrder, int, d->totalUnits);
+	CARVE(levelStart, int, d->totalUnits + W);
+	CARVE(stats, int, 16);
+	return total;
+}
+
+static int body_type_(const cpBody *b)
+{
+	/* cpBody.c:136-146 */
+	if(b->idleTime == INF_) return CP_BODY_TYPE_STATIC;
+	if(b->m == INF_) return CP_BODY_TYPE_KINEMATIC;
+	return CP_BODY_TYPE_DYNAMIC;
+}
+
+/* Host staging helpers */
+#define HALLOC(type, n) ((type *)calloc((size_t)((n) > 0 ? (n) : 1), sizeof(type)))
+
+static int h2d(void *dst, const void *src, size_t bytes)
+{
+	if(bytes == 0) return 1;
+	return cuda_ok(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, lib_stream()), "upload");
+}
+
+static int d2h(void *dst, const void *src, size_t bytes)
+{
+	if(bytes == 0) return 1;
+	return cuda_ok(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, lib_stream()), "download");
+}
+
+static int world_body_count(const cpSpace *sp) { return sp->ndyn + sp->nstat + 1; }
+
+static cpBody *world_body(cpSpace *sp, int i)
+{
+	if(i < sp->ndyn) return sp->dyn[i];
+	if(i < sp->ndyn + sp->nstat) return sp->stat[i - sp->ndyn];
+	return &sp->staticBody;
+}
+
+/* Upload the mutable state of every body of world w. */
+static int upload_bodies(DevSet *ds, int w)
+{
+	cpSpace *sp = ds->spaces[w];
+	cpgSet *d = &ds->d;
+	int n = world_body_count(sp), off = ds->hworld[w].bodyOff;
+	double *buf = HALLOC(double, 24*n);
+	double *f[24];
+	for(int k = 0; k < 24; k++) f[k] = buf + (size_t)k*n;
+	for(int i = 0; i < n; i++){
+		cpBody *b = world_body(sp, i);
+		b->index = i;
+		f[0][i] = b->p.x; f[1][i] = b->p.y; f[2][i] = b->v.x; f[3][i] = b->v.y;
+		f[4][i] = b->f.x; f[5][i] = b->f.y; f[6][i] = b->a; f[7][i] = b->w; f[8][i] = b->t;
+		f[9][i] = b->transform.a; f[10][i] = b->transform.b; f[11][i] = b->transform.c; f[12][i] = b->transform.d;
+		f[13][i] = b->transform.tx; f[14][i] = b->transform.ty;
+		f[15][i] = b->v_bias.x; f[16][i] = b->v_bias.y; f[17][i] = b->w_bias;
+		f[18][i] = b->m; f[19][i] = b->m_inv; f[20][i] = b->i; f[21][i] = b->i_inv;
+		f[22][i] = b->cog.x; f[23][i] = b->cog.y;
+	}
+	double *dst[24] = { d->px, d->py, d->vx, d->vy, d->fx, d->fy, d->ang, d->w, d->tq,
+		d->ta, d->tb, d->tc, d->td, d->ttx, d->tty, d->vbx, d->vby, d->wb,
+		d->m, d->minv, d->i, d->iinv, d->cogx, d->cogy };
+	int ok = 1;
+	for(int k = 0; k < 24; k++) ok &= h2d(dst[k] + off, f[k], sizeof(double)*(size_t)n);
+	cudaStreamSynchronize(lib_stream());
+	free(buf);
+	return ok;
+}
+
+static void download_bodies(DevSet *ds)
+{
+	cpgSet *d = &ds->d;
+	int NB = d->totalBodies;
+	double *buf = HALLOC(double, 18*NB);
+	double *f[18];
+	for(int k = 0; k < 18; k++) f[k] = buf + (size_t)k*NB;
+	double *src[18] = { d->px, d->py, d->vx, d->vy, d->fx, d->fy, d->ang, d->w, d->tq,
+		d->ta, d->tb, d->tc, d->td, d->ttx, d->tty, d->vbx, d->vby, d->wb };
+	for(int k = 0; k < 18; k++) d2h(f[k], src[k], sizeof(double)*(size_t)NB);
+	cuda_ok(cudaStreamSynchronize(lib_stream()), "download bodies");
+	for(int w = 0; w < ds->nspaces; w++){
+		cpSpace *sp = ds->spaces[w];
+		int off = ds->hworld[w].bodyOff;
+		for(int i = 0; i < sp->ndyn; i++){
+			cpBody *b = sp->dyn[i];
+			int g = off + i;
+			b->p = cpv(f[0][g], f[1][g]); b->v = cpv(f[2][g], f[3][g]); b->f = cpv(f[4][g], f[5][g]);
+			b->a = f[6][g]; b->w = f[7][g]; b->t = f[8][g];
+			b->transform = cpTransformNew(f[9][g], f[10][g], f[11][g], f[12][g], f[13][g], f[14][g]);
+			b->v_bias = cpv(f[15][g], f[16][g]); b->w_bias = f[17][g];
+		}
+	}
+	free(buf);
+}
+
+static int upload_shapes(DevSet *ds, int w)
+{
+	cpSpace *sp = ds->spaces[w];
+	cpgSet *d = &ds->d;
+	int n = sp->nshapes, off = ds->hworld[w].shapeOff;
+	double *buf = HALLOC(double, 30*n);
+	double *f[30];
+	for(int k = 0; k < 30; k++) f[k] = buf + (size_t)k*n;
+	int *ib = HALLOC(int, 5*n);
+	int *kind = ib, *body = ib + n, *voff = ib + 2*n, *vcount = ib + 3*n, *wld = ib + 4*n;
+	unsigned long long *grp = HALLOC(unsigned long long, 2*n), *hsh = grp + n;
+	unsigned *cm = HALLOC(unsigned, 2*n), *cat = cm, *msk = cm + n;
+	unsigned char *sens = HALLOC(unsigned char, n);
+	int nv = 0;
+	for(int i = 0; i < n; i++){
+		cpShape *s = sp->shapes[i];
+		kind[i] = s->kind; body[i] = s->body->index; wld[i] = w;
+		f[0][i] = s->r;
+		cpVect l0 = s->kind == CPG_CIRCLE ? s->c : s->sa, l1 = s->sb, ln = s->sn;
+		cpVect g0 = s->kind == CPG_CIRCLE ? s->tc : s->ta, g1 = s->tb, gn = s->tn;
+		f[1][i] = l0.x; f[2][i] = l0.y; f[3][i] = l1.x; f[4][i] = l1.y; f[5][i] = ln.x; f[6][i] = ln.y;
+		f[7][i] = g0.x; f[8][i] = g0.y; f[9][i] = g1.x; f[10][i] = g1.y; f[11][i] = gn.x; f[12][i] = gn.y;
+		f[13][i] = s->a_tangent.x; f[14][i] = s->a_tangent.y; f[15][i] = s->b_tangent.x; f[16][i] = s->b_tangent.y;
+		f[17][i] = s->bb.l; f[18][i] = s->bb.b; f[19][i] = s->bb.r; f[20][i] = s->bb.t;
+		f[21][i] = s->e; f[22][i] = s->u; f[23][i] = s->surfaceV.x; f[24][i] = s->surfaceV.y;
+		grp[i] = (unsigned long long)s->filter.group; cat[i] = s->filter.categories; msk[i] = s->filter.mask;
+		sens[i] = s->sensor; hsh[i] = (unsigned long long)s->hashid;
+		voff[i] = nv; vcount[i] = s->count;
+		nv += s->count;
+	}
+	double *vb = HALLOC(double, 8*nv);
+	for(int i = 0, k = 0; i < n; i++){
+		cpShape *s = sp->shapes[i];
+		for(int j = 0; j < s->count; j++, k++){
+			vb[k] = s->lv[j].x; vb[nv + k] = s->lv[j].y; vb[2*nv + k] = s->ln[j].x; vb[3*nv + k] = s->ln[j].y;
+			vb[4*nv + k] = s->gv[j].x; vb[5*nv + k] = s->gv[j].y; vb[6*nv + k] = s->gn[j].x; vb[7*nv + k] = s->gn[j].y;
+		}
+	}
+	int ok = 1;
+	size_t DB = sizeof(double)*(size_t)n, IB = sizeof(int)*(size_t)n;
+	ok &= h2d(d->skind + off, kind, IB); ok &= h2d(d->sbody + off, body, IB); ok &= h2d(d->sworld + off, wld, IB);
+	ok &= h2d(d->svoff + off, voff, IB); ok &= h2d(d->svcount + off, vcount, IB);
+	double *dst[25] = { d->sr, d->s0x, d->s0y, d->s1x, d->s1y, d->snx, d->sny, d->w0x, d->w0y, d->w1x, d->w1y,
+		d->wnx, d->wny, d->atx, d->aty, d->btx, d->bty, d->bbl, d->bbb, d->bbr, d->bbt, d->se, d->su, d->svx, d->svy };
+	for(int k = 0; k < 25; k++) ok &= h2d(dst[k] + off, f[k], DB);
+	ok &= h2d(d->sgroup + off, grp, sizeof(unsigned long long)*(size_t)n);
+	ok &= h2d(d->shash + off, hsh, sizeof(unsigned long long)*(size_t)n);
+	ok &= h2d(d->scat + off, cat, sizeof(unsigned)*(size_t)n);
+	ok &= h2d(d->smask + off, msk, sizeof(unsigned)*(size_t)n);
+	ok &= h2d(d->ssensor + off, sens, (size_t)n);
+	int voffw = ds->hworld[w].vertOff;
+	double *vdst[8] = { d->lvx, d->lvy, d->lnx, d->lny, d->gvx, d->gvy, d->gnx, d->gny };
+	for(int k = 0; k < 8; k++) ok &= h2d(vdst[k] + voffw, vb + (size_t)k*nv, sizeof(double)*(size_t)nv);
+	cudaStreamSynchronize(lib_stream());
+	free(buf); free(ib); free(grp); free(cm); free(sens); free(vb);
+	return ok;
+}
+
+static int upload_joints(DevSet *ds, int w, int params_only)
+{
+	cpSpace *sp = ds->spaces[w];
+	cpgSet *d = &ds->d;
+	int n = sp->ncons, off = ds->hworld[w].consOff;
+	if(n == 0) return 1;
+	int ok = 1;
+	if(!params_only){
+		cpgJoint *rec = HALLOC(cpgJoint, n);
+		for(int i = 0; i < n; i++){
+			cpConstraint *c = sp->cons[i];
+			cpgJoint *j = &rec[i];
+			*j = c->rec;
+			j->kind = c->kind; j->a = c->a->index; j->b = c->b->index;
+			j->ax = c->anchorA.x; j->ay = c->anchorA.y; j->bx = c->anchorB.x; j->by = c->anchorB.y;
+			j->maxForce = c->maxForce; j->maxBias = c->maxBias;
+			j->dist = c->dist; j->min = c->min; j->max = c->max;
+		}
+		ok &= h2d(d->joints + off, rec, sizeof(cpgJoint)*(size_t)n);
+		cudaStreamSynchronize(lib_stream());
+		free(rec);
+	}
+	return ok;
+}
+
+/* Joint bias terms 1 - pow(errorBias, dt) (chipmunk_private.h:265-268),
+ * evaluated on the host so they round like the reference's libm call. */
+static int upload_joint_bias(DevSet *ds, int w, double dt)
+{
+	cpSpace *sp = ds->spaces[w];
+	int n = sp->ncons;
+	if(n == 0) return 1;
+	double *b = HALLOC(double, n);
+	double lastE = 0.0, lastV = 0.0; int have = 0;
+	for(int i = 0; i < n; i++){
+		double e = sp->cons[i]->errorBias;
+		if(!have || e != lastE){ lastE = e; lastV = 1.0 - pow(e, dt); have = 1; }
+		b[i] = lastV;
+	}
+	int ok = h2d(ds->d.jbias + ds->hworld[w].consOff, b, sizeof(double)*(size_t)n);
+	cudaStreamSynchronize(lib_stream());
+	free(b);
+	return ok;
+}
+
+static void devset_free(DevSet *ds)
+{
+	if(!ds) return;
+	if(ds->slab) cudaFree(ds->slab);
+	if(ds->gather) cudaFree(ds->gather);
+	if(ds->hparams) cudaFreeHost(ds->hparams);
+	if(ds->hstats) cudaFreeHost(ds->hstats);
+	if(ds->statsEvent) cudaEventDestroy(ds->statsEvent);
+	for(int w = 0; w < ds->nspaces; w++){
+		if(ds->spaces[w]->dev == ds){ ds->spaces[w]->dev = NULL; }
+	}
+	free(ds->hworld);
+	free(ds->spaces);
+	free(ds);
+}
+
+static int device_available(void)
+{
+	static int ready = 0;
+	int n = 0;
+	if(cudaGetDeviceCount(&n) != cudaSuccess || n == 0){
+		set_error(CP_GPU_ERR_NO_DEVICE, "no CUDA device is visible");
+		return 0;
+	}
+	if(!ready){
+		/* the narrow phase keeps the EPA hull (about 4 KB) on the stack */
+		cuda_ok(cudaDeviceSetLimit(cudaLimitStackSize, 8192), "stack limit");
+		ready = 1;
+	}
+	return 1;
+}
+
+/* Build a device set holding `spaces` (each becomes one world). */
+static DevSet *devset_build(cpSpace **spaces, int nspaces)
+{
+	if(!device_available()) return NULL;
+	DevSet *ds = (DevSet *)calloc(1, sizeof(DevSet));
+	ds->nspaces = nspaces;
+	ds->spaces = (cpSpace **)malloc(sizeof(cpSpace *)*(size_t)nspaces);
+	memcpy(ds->spaces, spaces, sizeof(cpSpace *)*(size_t)nspaces);
+	ds->hworld = HALLOC(cpgWorld, nspaces);
+	cpgSet *d = &ds->d;
+	d->nworlds = nspaces;
+	long long NB = 0, NS = 0, NV = 0, NC = 0, NN = 0, NP = 0, NDB = 0, NSB = 0, NCD = 0, NU = 0, NO = 0, NPT = 0;
+	for(int w = 0; w < nspaces; w++){
+		cpSpace *sp = spaces[w];
+		cpgWorld *W = &ds->hworld[w];
+		int nb = world_body_count(sp);
+		int nverts = 0, ndynShapes = 0, nstatShapes = 0;
+		for(int i = 0; i < sp->nshapes; i++){
+			cpShape *s = sp->shapes[i];
+			nverts += s->count;
+			if(body_type_(s->body) == CP_BODY_TYPE_STATIC) nstatShapes++; else ndynShapes++;
+		}
+		int nparts = 0;
+		for(int i = 0; i < sp->ncons; i++) if(!sp->cons[i]->collideBodies) nparts += 2;
+		W->bodyOff = (int)NB; W->nbodies = nb; W->ndyn = sp->ndyn;
+		W->shapeOff = (int)NS; W->nshapes = sp->nshapes;
+		W->vertOff = (int)NV; W->nverts = nverts;
+		W->consOff = (int)NC; W->ncons = sp->ncons;
+		W->nodeOff = (int)NN; W->nodeCap = 2*(ndynShapes + nstatShapes) + 4;
+		W->pairOff = (int)NP; W->pairCap = 16*sp->nshapes + 256;
+		W->dbinOff = (int)NDB; W->dbinCap = bins_for(ndynShapes);
+		W->sbinOff = (int)NSB; W->sbinCap = bins_for(nstatShapes);
+		W->candOff = (int)NCD; W->candCap = W->pairCap;
+		W->unitOff = (int)NU; W->unitCap = W->candCap + sp->ncons;
+		W->opOff = (int)NO; W->nops = sp->nops;
+		W->partOff = (int)NPT;
+		NB += nb; NS += sp->nshapes; NV += nverts; NC += sp->ncons;
+		NN += W->nodeCap; NP += W->pairCap; NDB += W->dbinCap; NSB += W->sbinCap;
+		NCD += W->candCap; NU += W->unitCap; NO += sp->nops; NPT += nparts;
+	}
+	if(NB > 0x7fffffffLL || NCD > 0x7fffffffLL || NU > 0x7fffffffLL){
+		set_error(CP_GPU_ERR_OVERFLOW, "set too large");
+		devset_free(ds);
+		return NULL;
+	}
+	d->totalBodies = (int)NB; d->totalShapes = (int)NS; d->totalVerts = (int)NV; d->totalCons = (int)NC;
+	d->totalNodes = (int)NN; d->totalPairs = (int)NP; d->totalDBins = (int)NDB; d->totalSBins = (int)NSB;
+	d->totalCands = (int)NCD; d->totalUnits = (int)NU; d->totalOps = (int)NO; d->totalParts = (int)NPT;
+	long long arbCap = 1024;
+	while(arbCap < 8*NS + 1024) arbCap *= 2;
+	d->arbCap = (int)arbCap;
+
+	size_t bytes = carve_set(d, NULL, 0);
+	if(!cuda_ok(cudaMalloc(&ds->slab, bytes), "cudaMalloc set")){ devset_free(ds); return NULL; }
+	carve_set(d, (char *)ds->slab, 1);
+	cudaStream_t st = lib_stream();
+	int ok = 1;
+	ok &= cuda_ok(cudaMemsetAsync(ds->slab, 0, bytes, st), "memset set");
+	ok &= cuda_ok(cudaMemsetAsync(d->dbins, 0xff, sizeof(int)*(size_t)(NDB > 0 ? NDB : 1), st), "memset bins");
+	ok &= cuda_ok(cudaMemsetAsync(d->sbins, 0xff, sizeof(int)*(size_t)(NSB > 0 ? NSB : 1), st), "memset bins");
+	ok &= cuda_ok(cudaMallocHost((void **)&ds->hparams, sizeof(cpgParams)*(size_t)nspaces), "cudaMallocHost");
+	ok &= cuda_ok(cudaMallocHost((void **)&ds->hstats, sizeof(int)*16), "cudaMallocHost");
+	ok &= cuda_ok(cudaEventCreateWithFlags(&ds->statsEvent, cudaEventDisableTiming), "event");
+	if(!ok){ devset_free(ds); return NULL; }
+
+	ok &= h2d(d->world, ds->hworld, sizeof(cpgWorld)*(size_t)nspaces);
+	cpgTree *trees = HALLOC(cpgTree, nspaces);
+	for(int w = 0; w < nspaces; w++){
+		cpgTree *T = &trees[w];
+		T->dynRoot = -1; T->statRoot = -1; T->treeStamp = 0;
+		T->freeNode = -1; T->freePair = -1;
+		T->dynSize = next_prime(0); T->statSize = next_prime(0);
+	}
+	ok &= h2d(d->tree, trees, sizeof(cpgTree)*(size_t)nspaces);
+	cudaStreamSynchronize(st);
+	free(trees);
+
+	for(int w = 0; w < nspaces; w++){
+		cpSpace *sp = spaces[w];
+		sp->dev = ds; sp->world = w;
+		ok &= upload_bodies(ds, w);
+		ok &= upload_shapes(ds, w);
+		ok &= upload_joints(ds, w, 0);
+		/* body -> world, type; partners with collideBodies off */
+		cpgWorld *W = &ds->hworld[w];
+		int nb = W->nbodies;
+		int *bi = HALLOC(int, 4*nb);
+		int *bw = bi, *bt = bi + nb, *pstart = bi + 2*nb, *pcount = bi + 3*nb;
+		for(int i = 0; i < nb; i++){
+			cpBody *b = world_body(sp, i);
+			bw[i] = w;
+			int t = body_type_(b);
+			bt[i] = (t == CP_BODY_TYPE_STATIC) ? CPG_STATIC : (t == CP_BODY_TYPE_KINEMATIC ? CPG_KINEMATIC : CPG_DYNAMIC);
+		}
+		int np = 0;
+		for(int i = 0; i < sp->ncons; i++) if(!sp->cons[i]->collideBodies){ pcount[sp->cons[i]->a->index]++; pcount[sp->cons[i]->b->index]++; np += 2; }
+		for(int i = 0, acc = 0; i < nb; i++){ pstart[i] = acc; acc += pcount[i]; pcount[i] = 0; }
+		int *parts = HALLOC(int, np);
+		for(int i = 0; i < sp->ncons; i++){
+			cpConstraint *c = sp->cons[i];
+			if(c->collideBodies) continue;
+			int a = c->a->index, b = c->b->index;
+			parts[pstart[a] + pcount[a]++] = b;
+			parts[pstart[b] + pcount[b]++] = a;
+		}
+		ok &= h2d(d->bworld + W->bodyOff, bw, sizeof(int)*(size_t)nb);
+		ok &= h2d(d->btype + W->bodyOff, bt, sizeof(int)*(size_t)nb);
+		ok &= h2d(d->partStart + W->bodyOff, pstart, sizeof(int)*(size_t)nb);
+		ok &= h2d(d->partCount + W->bodyOff, pcount, sizeof(int)*(size_t)nb);
+		ok &= h2d(d->parts + W->partOff, parts, sizeof(int)*(size_t)np);
+		ok &= h2d(d->ops + W->opOff, sp->ops, sizeof(cpgOp)*(size_t)sp->nops);
+		cudaStreamSynchronize(st);
+		free(bi); free(parts);
+		sp->builtBodies = world_body_count(sp); sp->builtShapes = sp->nshapes; sp->builtCons = sp->ncons;
+		sp->bodyDirty = sp->shapeDirty = sp->consDirty = 0;
+		sp->jointDt = 0.0;
+	}
+	if(!ok){ devset_free(ds); return NULL; }
+	/* replay the recorded index insertions, then clear the logs */
+	if(cpg_launch_apply_ops(d, st) != 0){ set_error(CP_GPU_ERR_CUDA, "apply_ops launch failed"); devset_free(ds); return NULL; }
+	for(int w = 0; w < nspaces; w++){ ds->hworld[w].nops = 0; spaces[w]->nops = 0; }
+	h2d(d->world, ds->hworld, sizeof(cpgWorld)*(size_t)nspaces);
+	if(!cuda_ok(cudaStreamSynchronize(st), "build")){ devset_free(ds); return NULL; }
+	return ds;
+}
+
+/* Make host copies of the space's body state current. */
+static void space_pull(cpSpace *sp)
+{
+	if(!sp || !sp->dev || !sp->hostStale) return;
+	DevSet *ds = sp->dev;
+	download_bodies(ds);
+	for(int w = 0; w < ds->nspaces; w++){
+		cpSpace *o = ds->spaces[w];
+		o->hostStale = 0;
+		o->snapValid = 0;
+	}
+}
+
+static void check_stats(DevSet *ds)
+{
+	if(!ds->statsPending) return;
+	cudaEventSynchronize(ds->statsEvent);
+	ds->statsPending = 0;
+	int err = ds->hstats[0];
+	if(err){
+		set_error(CP_GPU_ERR_OVERFLOW, "device table overflow (flags 0x%x): pairs %d/1000, nodes %d/1000, candidates %d/1000",
+			err, ds->hstats[1], ds->hstats[2], ds->hstats[7]);
+	}
+}
+
+/* One step of every world of the set with per-world dt. */
+static int devset_step(DevSet *ds, const double *dts, cpSpace **only)
+{
+	cpgSet *d = &ds->d;
+	check_stats(ds);
+	for(int w = 0; w < ds->nspaces; w++){
+		cpSpace *sp = ds->spaces[w];
+		cpgParams *P = &ds->hparams[w];
+		if((only && *only != sp) || dts[w] == 0.0){ P->active = 0; continue; }
+		if(sp->bodyDirty){ upload_bodies(ds, w); sp->bodyDirty = 0; }
+		if(sp->shapeDirty){ upload_shapes(ds, w); sp->shapeDirty = 0; }
+		if(sp->consDirty){ upload_joints(ds, w, 0); sp->consDirty = 0; sp->jointDt = 0.0; }
+		double dt = dts[w];
+		/* cpSpaceStep.c:339-344, 384, 399, 407 */
+		sp->stamp++;
+		cpFloat prev_dt = sp->curr_dt;
+		sp->curr_dt = dt;
+		if(sp->jointDt != dt){ upload_joint_bias(ds, w, dt); sp->jointDt = dt; }
+		P->dt = dt;
+		P->dt_coef = (prev_dt == 0.0 ? 0.0 : dt/prev_dt);
+		P->damping = pow(sp->damping, dt);
+		P->slop = sp->collisionSlop;
+		P->biasCoef = 1.0 - pow(sp->collisionBias, dt);
+		P->gx = sp->gravity.x; P->gy = sp->gravity.y;
+		P->iterations = sp->iterations;
+		P->stamp = sp->stamp;
+		P->persistence = sp->collisionPersistence;
+		P->active = 1;
+		sp->hostStale = 1;
+		sp->consStale = 1;
+		sp->snapValid = 0;
+	}
+	cudaStream_t st = lib_stream();
+	if(!h2d(d->params, ds->hparams, sizeof(cpgParams)*(size_t)ds->nspaces)) return -1;
+	float ms[8] = {0};
+	int mode = ds->spaces[0]->mode;
+	if(cpg_launch_step(d, d, mode, st, g_timing ? ms : NULL) != 0){
+		set_error(CP_GPU_ERR_CUDA, "step launch failed");
+		return -1;
+	}
+	if(g_timing) for(int w = 0; w < ds->nspaces; w++) memcpy(ds->spaces[w]->phaseMs, ms, sizeof(ms));
+	cudaMemcpyAsync(ds->hstats, d->stats, sizeof(int)*16, cudaMemcpyDeviceToHost, st);
+	cudaEventRecord(ds->statsEvent, st);
+	ds->statsPending = 1;
+	return 0;
+}
+
+static int space_supported(cpSpace *sp)
+{
+	if(sp->sleepTimeThreshold != INF_){
+		set_error(CP_GPU_ERR_UNSUPPORTED, "sleeping (cpSpaceSetSleepTimeThreshold) is not run on the GPU");
+		return 0;
+	}
+	for(int i = 0; i < sp->ndyn; i++){
+		cpBody *b = sp->dyn[i];
+		if(b->velocity_func != cpBodyUpdateVelocity || b->position_func != cpBodyUpdatePosition){
+			set_error(CP_GPU_ERR_UNSUPPORTED, "custom body integration callbacks are not run on the GPU");
+			return 0;
+		}
+	}
+	for(int i = 0; i < sp->ncons; i++){
+		if(sp->cons[i]->preSolve || sp->cons[i]->postSolve){
+			set_error(CP_GPU_ERR_UNSUPPORTED, "constraint pre/post-solve callbacks are not run on the GPU");
+			return 0;
+		}
+	}
+	return 1;
+}
+
+static int space_structure_changed(cpSpace *sp)
+{
+	return sp->dev && (world_body_count(sp) != sp->builtBodies || sp->nshapes != sp->builtShapes || sp->ncons != sp->builtCons);
+}
+
+/* cpSpaceStep.c:335-445 */
+void cpSpaceStep(cpSpace *sp, cpFloat dt)
+{
+	if(dt == 0.0) return;
+	if(!space_supported(sp)) return;
+	if(sp->dev && !sp->ownsDev){
+		set_error(CP_GPU_ERR_UNSUPPORTED, "space belongs to a cpGpuBatch; step it with cpGpuBatchStep");
+		return;
+	}
+	if(space_structure_changed(sp)){
+		/* Objects were added after the space went to the device: bring the
+		 * state home and rebuild.  The device tree and arbiter cache are
+		 * rebuilt from the insertion history, which is exact only while
+		 * nothing has been stepped; report it otherwise. */
+		set_error(CP_GPU_ERR_UNSUPPORTED, "adding objects to a space after its first step is not supported");
+		return;
+	}
+	if(!sp->dev){
+		cpSpace *one[1] = { sp };
+		DevSet *ds = devset_build(one, 1);
+		if(!ds) return;
+		sp->ownsDev = 1;
+	}
+	double dts[1] = { dt };
+	devset_step(sp->dev, dts, NULL);
+}
+
+void cpGpuSpaceSync(cpSpace *sp)
+{
+	if(sp && sp->dev){
+		cuda_ok(cudaStreamSynchronize(lib_stream()), "sync");
+		check_stats(sp->dev);
+	}
+}
+
+/* ====================================================================
+ * Batches
+ * ==================================================================== */
+struct cpGpuBatch {
+	cpSpace **spaces;
+	int n, cap;
+	DevSet *dev;
+};
+
+cpGpuBatch *cpGpuBatchNew(void) { return (cpGpuBatch *)calloc(1, sizeof(cpGpuBatch)); }
+
+void cpGpuBatchFree(cpGpuBatch *b)
+{
+	if(!b) return;
+	if(b->dev){
+		for(int i = 0; i < b->n; i++) space_pull(b->spaces[i]);
+		devset_free(b->dev);
+	}
+	free(b->spaces);
+	free(b);
+}
+
+int cpGpuBatchAddSpace(cpGpuBatch *b, cpSpace *sp)
+{
+	if(!b || !sp || b->dev || sp->dev){
+		set_error(CP_GPU_ERR_ARGUMENT, "spaces join a batch before it is first stepped, and only once");
+		return -1;
+	}
+	push_((void ***)&b->spaces, &b->n, &b->cap, sp);
+	return b->n - 1;
+}
+
+int cpGpuBatchStep(cpGpuBatch *b, cpFloat dt, int steps, int use_graph)
+{
+	(void)use_graph;
+	if(!b || b->n == 0) return -1;
+	for(int i = 0; i < b->n; i++) if(!space_supported(b->spaces[i])) return -1;
+	if(!b->dev){
+		b->dev = devset_build(b->spaces, b->n);
+		if(!b->dev) return -1;
+		for(int i = 0; i < b->n; i++) b->spaces[i]->ownsDev = 0;
+	}
+	double *dts = (double *)malloc(sizeof(double)*(size_t)b->n);
+	for(int i = 0; i < b->n; i++) dts[i] = dt;
+	int rc = 0;
+	for(int s = 0; s < steps && rc == 0; s++) rc = devset_step(b->dev, dts, NULL);
+	free(dts);
+	return rc;
+}
+
+/* ====================================================================
+ * Creation-time math: chipmunk.c:63-171, 250-274
+ * ==================================================================== */
+#define PI_ ((cpFloat)3.14159265358979323846264338327950288)
+
+cpFloat cpMomentForCircle(cpFloat m, cpFloat r1, cpFloat r2, cpVect offset) { return m*(0.5*(r1*r1 + r2*r2) + cpvlengthsq(offset)); }
+cpFloat cpAreaForCircle(cpFloat r1, cpFloat r2) { return PI_*habs(r1*r1 - r2*r2); }
+
+cpFloat cpMomentForSegment(cpFloat m, cpVect a, cpVect b, cpFloat r)
+{
+	cpVect offset = cpvlerp(a, b, 0.5);
+	cpFloat length = cpvdist(b, a) + 2.0*r;
+	return m*((length*length + 4.0*r*r)/12.0 + cpvlengthsq(offset));
+}
+
+cpFloat cpAreaForSegment(cpVect a, cpVect b, cpFloat r) { return r*(PI_*r + 2.0*cpvdist(a, b)); }
+
+cpFloat cpMomentForPoly(cpFloat m, int count, const cpVect *verts, cpVect offset, cpFloat r)
+{
+	(void)r;
+	if(count == 2) return cpMomentForSegment(m, verts[0], verts[1], 0.0);
+	cpFloat sum1 = 0.0, sum2 = 0.0;
+	for(int i = 0; i < count; i++){
+		cpVect v1 = cpvadd(verts[i], offset), v2 = cpvadd(verts[(i + 1)%count], offset);
+		cpFloat a = cpvcross(v2, v1);
+		cpFloat b = cpvdot(v1, v1) + cpvdot(v1, v2) + cpvdot(v2, v2);
+		sum1 += a*b;
+		sum2 += a;
+	}
+	return (m*sum1)/(6.0*sum2);
+}
+
+cpFloat cpAreaForPoly(const int count, const cpVect *verts, cpFloat r)
+{
+	cpFloat area = 0.0, perimeter = 0.0;
+	for(int i = 0; i < count; i++){
+		cpVect v1 = verts[i], v2 = verts[(i + 1)%count];
+		area += cpvcross(v1, v2);
+		perimeter += cpvdist(v1, v2);
+	}
+	return r*(PI_*habs(r) + perimeter) + area/2.0;
+}
+
+cpVect cpCentroidForPoly(const int count, const cpVect *verts)
+{
+	cpFloat sum = 0.0;
+	cpVect vsum = cpvzero;
+	for(int i = 0; i < count; i++){
+		cpVect v1 = verts[i], v2 = verts[(i + 1)%count];
+		cpFloat cross = cpvcross(v1, v2);
+		sum += cross;
+		vsum = cpvadd(vsum, cpvmult(cpvadd(v1, v2), cross));
+	}
+	return cpvmult(vsum, 1.0/(3.0*sum));
+}
+
+cpFloat cpMomentForBox(cpFloat m, cpFloat width, cpFloat height) { return m*(width*width + height*height)/12.0; }
+
+cpFloat cpMomentForBox2(cpFloat m, cpBB box)
+{
+	cpFloat width = box.r - box.l, height = box.t - box.b;
+	cpVect offset = cpvmult(cpv(box.l + box.r, box.b + box.t), 0.5);
+	return cpMomentForBox(m, width, height) + m*cpvlengthsq(offset);
+}
+
+/* QuickHull with in-place partitioning (chipmunk.c:178-274); the output
+ * order matters because vertex indices feed contact feature ids. */
+static void qh_swap(cpVect *a, cpVect *b) { cpVect t = *a; *a = *b; *b = t; }
+
+static int qh_partition(cpVect *verts, int count, cpVect a, cpVect b, cpFloat tol)
+{
+	if(count == 0) return 0;
+	cpFloat best = 0;
+	int pivot = 0;
+	cpVect delta = cpvsub(b, a);
+	cpFloat valueTol = tol*cpvlength(delta);
+	int head = 0;
+	for(int tail = count - 1; head <= tail;){
+		cpFloat value = cpvcross(cpvsub(verts[head], a), delta);
+		if(value > valueTol){
+			if(value > best){ best = value; pivot = head; }
+			head++;
+		} else {
+			qh_swap(&verts[head], &verts[tail]);
+			tail--;
+		}
+	}
+	if(pivot != 0) qh_swap(&verts[0], &verts[pivot]);
+	return head;
+}
+
+static int qh_reduce(cpFloat tol, cpVect *verts, int count, cpVect a, cpVect pivot, cpVect b, cpVect *result)
+{
+	if(count < 0) return 0;
+	if(count == 0){ result[0] = pivot; return 1; }
+	int left = qh_partition(verts, count, a, pivot, tol);
+	int index = qh_reduce(tol, verts + 1, left - 1, a, verts[0], pivot, result);
+	result[index++] = pivot;
+	int right = qh_partition(verts + left, count - left, pivot, b, tol);
+	return index + qh_reduce(tol, verts + left + 1, right - 1, pivot, verts[left], b, result + index);
+}
+
+int cpConvexHull(int count, const cpVect *verts, cpVect *result, int *first, cpFloat tol)
+{
+	if(verts != result) memcpy(result, verts, (size_t)count*sizeof(cpVect));
+	int start = 0, end = 0;
+	cpVect lo = verts[0], hi = lo;
+	for(int i = 1; i < count; i++){
+		cpVect v = verts[i];
+		if(v.x < lo.x || (v.x == lo.x && v.y < lo.y)){ lo = v; start = i; }
+		else if(v.x > hi.x || (v.x == hi.x && v.y > hi.y)){ hi = v; end = i; }
+	}
+	if(start == end){
+		if(first) *first = 0;
+		return 1;
+	}
+	qh_swap(&result[0], &result[start]);
+	qh_swap(&result[1], &result[end == 0 ? start : end]);
+	cpVect a = result[0], b = result[1];
+	if(first) *first = start;
+	return qh_reduce(tol, result + 2, count - 2, a, b, a, result + 1) + 1;
+}
+
+/* ====================================================================
+ * Bodies: cpBody.c
+ * ==================================================================== */
+static void set_transform_(cpBody *b, cpVect p, cpFloat a)
+{
+	/* cpBody.c:347-357 */
+	cpVect rot = cpvforangle(a);
+	cpVect c = b->cog;
+	b->transform = cpTransformNewTranspose(rot.x, -rot.y, p.x - (c.x*rot.x - c.y*rot.y),
+		rot.y, rot.x, p.y - (c.x*rot.y + c.y*rot.x));
+}
+
+/* Read access: make the host copy current first. */
+static inline const cpBody *rd(const cpBody *b) { if(b->space) space_pull(b->space); return b; }
+/* Write access: pull, then mark the space's bodies for upload. */
+static inline cpBody *wr(cpBody *b)
+{
+	if(b->space){ space_pull(b->space); b->space->bodyDirty = 1; }
+	return b;
+}
+
+static void body_init_(cpBody *b, cpFloat m, cpFloat i)
+{
+	memset(b, 0, sizeof(*b));
+	b->velocity_func = cpBodyUpdateVelocity;
+	b->position_func = cpBodyUpdatePosition;
+	b->index = -1;
+	b->m = m; b->m_inv = (m == 0.0 ? INF_ : 1.0/m);
+	b->i = i; b->i_inv = (i == 0.0 ? INF_ : 1.0/i);
+	set_transform_(b, b->p, 0.0);
+}
+
+cpBody *cpBodyNew(cpFloat mass, cpFloat moment)
+{
+	ASSERT_HARD(0.0 <= mass && mass < INF_, "Mass must be positive and finite.");
+	ASSERT_HARD(moment >= 0.0, "Moment of Inertia must be positive.");
+	cpBody *b = (cpBody *)calloc(1, sizeof(cpBody));
+	body_init_(b, mass, moment);
+	return b;
+}
+
+static void make_static_(cpBody *b)
+{
+	b->idleTime = INF_;
+	b->m = b->i = INF_;
+	b->m_inv = b->i_inv = 0.0;
+	b->v = cpvzero; b->w = 0.0;
+}
+
+cpBody *cpBodyNewStatic(void) { cpBody *b = cpBodyNew(0.0, 0.0); make_static_(b); return b; }
+
+cpBody *cpBodyNewKinematic(void)
+{
+	cpBody *b = cpBodyNew(0.0, 0.0);
+	b->m = b->i = INF_;
+	b->m_inv = b->i_inv = 0.0;
+	return b;
+}
+
+void cpBodyFree(cpBody *b) { free(b); }
+void cpBodyActivate(cpBody *b) { (void)b; }
+cpBool cpBodyIsSleeping(const cpBody *b) { (void)b; return cpFalse; }
+cpBodyType cpBodyGetType(cpBody *b) { return (cpBodyType)body_type_(b); }
+cpSpace *cpBodyGetSpace(const cpBody *b) { return b->space; }
+cpFloat cpBodyGetMass(const cpBody *b) { return b->m; }
+cpFloat cpBodyGetMoment(const cpBody *b) { return b->i; }
+
+void cpBodySetMass(cpBody *b, cpFloat m)
+{
+	ASSERT_HARD(body_type_(b) == CP_BODY_TYPE_DYNAMIC, "You cannot set the mass of kinematic or static bodies.");
+	ASSERT_HARD(0.0 <= m && m < INF_, "Mass must be positive and finite.");
+	wr(b); b->m = m; b->m_inv = (m == 0.0 ? INF_ : 1.0/m);
+}
+
+void cpBodySetMoment(cpBody *b, cpFloat i)
+{
+	ASSERT_HARD(i >= 0.0, "Moment of Inertia must be positive.");
+	wr(b); b->i = i; b->i_inv = (i == 0.0 ? INF_ : 1.0/i);
+}
+
+cpVect cpBodyGetRotation(const cpBody *b) { rd(b); return cpv(b->transform.a, b->transform.b); }
+cpVect cpBodyGetPosition(const cpBody *b) { rd(b); return cpTransformPoint(b->transform, cpvzero); }
+
+void cpBodySetPosition(cpBody *b, cpVect pos)
+{
+	/* cpBody.c:374-382 */
+	wr(b);
+	cpVect p = b->p = cpvadd(cpTransformVect(b->transform, b->cog), pos);
+	set_transform_(b, p, b->a);
+}
+
+cpVect cpBodyGetCenterOfGravity(const cpBody *b) { return b->cog; }
+void cpBodySetCenterOfGravity(cpBody *b, cpVect cog) { wr(b); b->cog = cog; }
+cpVect cpBodyGetVelocity(const cpBody *b) { rd(b); return b->v; }
+void cpBodySetVelocity(cpBody *b, cpVect v) { wr(b); b->v = v; }
+cpVect cpBodyGetForce(const cpBody *b) { rd(b); return b->f; }
+void cpBodySetForce(cpBody *b, cpVect f) { wr(b); b->f = f; }
+cpFloat cpBodyGetAngle(const cpBody *b) { rd(b); return b->a; }
+void cpBodySetAngle(cpBody *b, cpFloat a) { wr(b); b->a = a; set_transform_(b, b->p, a); }
+cpFloat cpBodyGetAngularVelocity(const cpBody *b) { rd(b); return b->w; }
+void cpBodySetAngularVelocity(cpBody *b, cpFloat w) { wr(b); b->w = w; }
+cpFloat cpBodyGetTorque(const cpBody *b) { rd(b); return b->t; }
+void cpBodySetTorque(cpBody *b, cpFloat t) { wr(b); b->t = t; }
+cpDataPointer cpBodyGetUserData(const cpBody *b) { return b->userData; }
+void cpBodySetUserData(cpBody *b, cpDataPointer d) { b->userData = d; }
+void cpBodySetVelocityUpdateFunc(cpBody *b, cpBodyVelocityFunc f) { b->velocity_func = f; }
+void cpBodySetPositionUpdateFunc(cpBody *b, cpBodyPositionFunc f) { b->position_func = f; }
+cpVect cpBodyLocalToWorld(const cpBody *b, const cpVect p) { rd(b); return cpTransformPoint(b->transform, p); }
+cpVect cpBodyWorldToLocal(const cpBody *b, const cpVect p) { rd(b); return cpTransformPoint(rigid_inverse(b->transform), p); }
+
+void cpBodyApplyForceAtWorldPoint(cpBody *b, cpVect force, cpVect point)
+{
+	wr(b);
+	b->f = cpvadd(b->f, force);
+	cpVect r = cpvsub(point, cpTransformPoint(b->transform, b->cog));
+	b->t += cpvcross(r, force);
+}
+
+void cpBodyApplyForceAtLocalPoint(cpBody *b, cpVect force, cpVect point)
+{
+	rd(b);
+	cpBodyApplyForceAtWorldPoint(b, cpTransformVect(b->transform, force), cpTransformPoint(b->transform, point));
+}
+
+void cpBodyApplyImpulseAtWorldPoint(cpBody *b, cpVect j, cpVect point)
+{
+	wr(b);
+	cpVect r = cpvsub(point, cpTransformPoint(b->transform, b->cog));
+	b->v = cpvadd(b->v, cpvmult(j, b->m_inv));
+	b->w += b->i_inv*cpvcross(r, j);
+}
+
+void cpBodyApplyImpulseAtLocalPoint(cpBody *b, cpVect j, cpVect point)
+{
+	rd(b);
+	cpBodyApplyImpulseAtWorldPoint(b, cpTransformVect(b->transform, j), cpTransformPoint(b->transform, point));
+}
+
+cpVect cpBodyGetVelocityAtWorldPoint(const cpBody *b, cpVect point)
+{
+	rd(b);
+	cpVect r = cpvsub(point, cpTransformPoint(b->transform, b->cog));
+	return cpvadd(b->v, cpvmult(cpvperp(r), b->w));
+}
+
+cpVect cpBodyGetVelocityAtLocalPoint(const cpBody *b, cpVect point)
+{
+	rd(b);
+	cpVect r = cpTransformVect(b->transform, cpvsub(point, b->cog));
+	return cpvadd(b->v, cpvmult(cpvperp(r), b->w));
+}
+
+cpFloat cpBodyKineticEnergy(const cpBody *b)
+{
+	rd(b);
+	cpFloat vsq = cpvdot(b->v, b->v), wsq = b->w*b->w;
+	return (vsq ? vsq*b->m : 0.0) + (wsq ? wsq*b->i : 0.0);
+}
+
+/* The reference integrators, for programs that call them directly; the
+ * device step runs its own copies of these (cpBody.c:493-522). */
+void cpBodyUpdateVelocity(cpBody *b, cpVect gravity, cpFloat damping, cpFloat dt)
+{
+	wr(b);
+	if(body_type_(b) == CP_BODY_TYPE_KINEMATIC) return;
+	b->v = cpvadd(cpvmult(b->v, damping), cpvmult(cpvadd(gravity, cpvmult(b->f, b->m_inv)), dt));
+	b->w = b->w*damping + b->t*b->i_inv*dt;
+	b->f = cpvzero;
+	b->t = 0.0;
+}
+
+void cpBodyUpdatePosition(cpBody *b, cpFloat dt)
+{
+	wr(b);
+	cpVect p = b->p = cpvadd(b->p, cpvmult(cpvadd(b->v, b->v_bias), dt));
+	cpFloat a = b->a = b->a + (b->w + b->w_bias)*dt;
+	set_transform_(b, p, a);
+	b->v_bias = cpvzero;
+	b->w_bias = 0.0;
+}
+
+void cpBodyEachShape(cpBody *b, cpBodyShapeIteratorFunc func, void *data)
+{
+	cpShape *s = b->shapeList;
+	while(s){ cpShape *next = s->next; func(b, s, data); s = next; }
+}
+
+static inline cpConstraint *cons_next_(cpConstraint *c, cpBody *b) { return (c->a == b ? c->next_a : c->next_b); }
+
+void cpBodyEachConstraint(cpBody *b, cpBodyConstraintIteratorFunc func, void *data)
+{
+	cpConstraint *c = b->constraintList;
+	while(c){ cpConstraint *next = cons_next_(c, b); func(b, c, data); c = next; }
+}
+
+/* cpBody.c:206-239 */
+static void accumulate_mass_(cpBody *b)
+{
+	if(b == NULL || body_type_(b) != CP_BODY_TYPE_DYNAMIC) return;
+	wr(b);
+	b->m = b->i = 0.0;
+	b->cog = cpvzero;
+	cpVect pos = cpBodyGetPosition(b);
+	for(cpShape *s = b->shapeList; s; s = s->next){
+		cpFloat m = s->mass_m;
+		if(m > 0.0){
+			cpFloat msum = b->m + m;
+			b->i += m*s->mass_i + cpvdistsq(b->cog, s->mass_cog)*(m*b->m)/msum;
+			b->cog = cpvlerp(b->cog, s->mass_cog, m/msum);
+			b->m = msum;
+		}
+	}
+	b->m_inv = 1.0/b->m;
+	b->i_inv = 1.0/b->i;
+	cpBodySetPosition(b, pos);
+}
+
+/* ====================================================================
+ * Shapes: cpShape.c, cpPolyShape.c
+ * ==================================================================== */
+static cpShape *shape_new_(int kind, cpBody *body, cpFloat mi, cpVect cog, cpFloat area)
+{
+	cpShape *s = (cpShape *)calloc(1, sizeof(cpShape));
+	s->kind = kind;
+	s->body = body;
+	s->mass_m = 0.0; s->mass_i = mi; s->mass_cog = cog; s->mass_area = area;
+	s->filter.group = CP_NO_GROUP;
+	s->filter.categories = CP_ALL_CATEGORIES;
+	s->filter.mask = CP_ALL_CATEGORIES;
+	return s;
+}
+
+/* Add-time shape caches: cpShape.c:291-296, 378-405, cpPolyShape.c:39-64 */
+static cpBB shape_cache_(cpShape *s, cpTransform t)
+{
+	cpBB bb;
+	if(s->kind == CPG_CIRCLE){
+		cpVect c = s->tc = cpTransformPoint(t, s->c);
+		bb = cpBBNewForCircle(c, s->r);
+	} else if(s->kind == CPG_SEGMENT){
+		s->ta = cpTransformPoint(t, s->sa);
+		s->tb = cpTransformPoint(t, s->sb);
+		s->tn = cpTransformVect(t, s->sn);
+		cpFloat l, r, b, tp;
+		if(s->ta.x < s->tb.x){ l = s->ta.x; r = s->tb.x; } else { l = s->tb.x; r = s->ta.x; }
+		if(s->ta.y < s->tb.y){ b = s->ta.y; tp = s->tb.y; } else { b = s->tb.y; tp = s->ta.y; }
+		bb = cpBBNew(l - s->r, b - s->r, r + s->r, tp + s->r);
+	} else {
+		cpFloat l = INF_, r = -INF_, b = INF_, tp = -INF_;
+		for(int i = 0; i < s->count; i++){
+			cpVect v = cpTransformPoint(t, s->lv[i]);
+			cpVect n = cpTransformVect(t, s->ln[i]);
+			s->gv[i] = v; s->gn[i] = n;
+			l = hmin(l, v.x); r = hmax(r, v.x);
+			b = hmin(b, v.y); tp = hmax(tp, v.y);
+		}
+		bb = cpBBNew(l - s->r, b - s->r, r + s->r, tp + s->r);
+	}
+	return (s->bb = bb);
+}
+
+static cpBB shape_bb_now_(cpShape *s)
+{
+	/* device caches are current after a step: read the box back */
+	if(s->space && s->space->dev && s->space->hostStale){
+		cpSpace *sp = s->space;
+		DevSet *ds = sp->dev;
+		int g = ds->hworld[sp->world].shapeOff + (int)s->hashid;
+		double v[4];
+		d2h(&v[0], ds->d.bbl + g, 8); d2h(&v[1], ds->d.bbb + g, 8); d2h(&v[2], ds->d.bbr + g, 8); d2h(&v[3], ds->d.bbt + g, 8);
+		cudaStreamSynchronize(lib_stream());
+		s->bb = cpBBNew(v[0], v[1], v[2], v[3]);
+	}
+	return s->bb;
+}
+
+cpBB cpShapeCacheBB(cpShape *s) { rd(s->body); return shape_cache_(s, s->body->transform); }
+cpBB cpShapeGetBB(const cpShape *s) { return shape_bb_now_((cpShape *)s); }
+
+cpShape *cpCircleShapeNew(cpBody *body, cpFloat radius, cpVect offset)
+{
+	/* cpShape.c:313-335 */
+	cpShape *s = shape_new_(CPG_CIRCLE, body, cpMomentForCircle(1.0, 0.0, radius, cpvzero), offset, cpAreaForCircle(0.0, radius));
+	s->c = offset;
+	s->r = radius;
+	return s;
+}
+
+cpShape *cpSegmentShapeNew(cpBody *body, cpVect a, cpVect b, cpFloat r)
+{
+	/* cpShape.c:470-502 */
+	cpShape *s = shape_new_(CPG_SEGMENT, body, cpMomentForBox(1.0, cpvdist(a, b) + 2.0*r, 2.0*r), cpvlerp(a, b, 0.5), cpAreaForSegment(a, b, r));
+	s->sa = a; s->sb = b;
+	s->sn = cpvrperp(cpvnormalize(cpvsub(b, a)));
+	s->r = r;
+	return s;
+}
+
+void cpSegmentShapeSetNeighbors(cpShape *s, cpVect prev, cpVect next)
+{
+	s->a_tangent = cpvsub(prev, s->sa);
+	s->b_tangent = cpvsub(next, s->sb);
+	if(s->space) s->space->shapeDirty = 1;
+}
+
+cpShape *cpPolyShapeNewRaw(cpBody *body, int count, const cpVect *verts, cpFloat radius)
+{
+	/* cpPolyShape.c:147-165, 202-211 */
+	cpVect centroid = cpCentroidForPoly(count, verts);
+	cpShape *s = shape_new_(CPG_POLY, body, cpMomentForPoly(1.0, count, verts, cpvneg(centroid), radius), centroid, cpAreaForPoly(count, verts, radius));
+	s->count = count;
+	s->lv = (cpVect *)calloc((size_t)(4*count), sizeof(cpVect));
+	s->ln = s->lv + count; s->gv = s->lv + 2*count; s->gn = s->lv + 3*count;
+	for(int i = 0; i < count; i++){
+		cpVect a = verts[(i - 1 + count)%count], b = verts[i];
+		s->lv[i] = b;
+		s->ln[i] = cpvnormalize(cpvrperp(cpvsub(b, a)));
+	}
+	s->r = radius;
+	return s;
+}
+
+cpShape *cpPolyShapeNew(cpBody *body, int count, const cpVect *verts, cpTransform transform, cpFloat radius)
+{
+	cpVect *hull = (cpVect *)malloc((size_t)count*sizeof(cpVect));
+	for(int i = 0; i < count; i++) hull[i] = cpTransformPoint(transform, verts[i]);
+	int n = cpConvexHull(count, hull, hull, NULL, 0.0);
+	cpShape *s = cpPolyShapeNewRaw(body, n, hull, radius);
+	free(hull);
+	return s;
+}
+
+cpShape *cpBoxShapeNew2(cpBody *body, cpBB box, cpFloat radius)
+{
+	cpVect verts[4] = { cpv(box.r, box.b), cpv(box.r, box.t), cpv(box.l, box.t), cpv(box.l, box.b) };
+	return cpPolyShapeNewRaw(body, 4, verts, radius);
+}
+
+cpShape *cpBoxShapeNew(cpBody *body, cpFloat width, cpFloat height, cpFloat radius)
+{
+	cpFloat hw = width/2.0, hh = height/2.0;
+	return cpBoxShapeNew2(body, cpBBNew(-hw, -hh, hw, hh), radius);
+}
+
+void cpShapeFree(cpShape *s) { if(s){ free(s->lv); free(s); } }
+
+static inline cpShape *swr(cpShape *s) { if(s->space) s->space->shapeDirty = 1; return s; }
+
+cpSpace *cpShapeGetSpace(const cpShape *s) { return s->space; }
+cpBody *cpShapeGetBody(const cpShape *s) { return s->body; }
+cpFloat cpShapeGetMass(cpShape *s) { return s->mass_m; }
+void cpShapeSetMass(cpShape *s, cpFloat mass) { s->mass_m = mass; accumulate_mass_(s->body); }
+cpFloat cpShapeGetDensity(cpShape *s) { return s->mass_m/s->mass_area; }
+void cpShapeSetDensity(cpShape *s, cpFloat d) { cpShapeSetMass(s, d*s->mass_area); }
+cpFloat cpShapeGetMoment(cpShape *s) { return s->mass_m*s->mass_i; }
+cpFloat cpShapeGetArea(cpShape *s) { return s->mass_area; }
+cpVect cpShapeGetCenterOfGravity(cpShape *s) { return s->mass_cog; }
+cpBool cpShapeGetSensor(const cpShape *s) { return s->sensor; }
+void cpShapeSetSensor(cpShape *s, cpBool v) { swr(s)->sensor = v; }
+cpFloat cpShapeGetElasticity(const cpShape *s) { return s->e; }
+void cpShapeSetElasticity(cpShape *s, cpFloat e) { ASSERT_HARD(e >= 0.0, "Elasticity must be positive."); swr(s)->e = e; }
+cpFloat cpShapeGetFriction(const cpShape *s) { return s->u; }
+void cpShapeSetFriction(cpShape *s, cpFloat u) { ASSERT_HARD(u >= 0.0, "Friction must be postive."); swr(s)->u = u; }
+cpVect cpShapeGetSurfaceVelocity(const cpShape *s) { return s->surfaceV; }
+void cpShapeSetSurfaceVelocity(cpShape *s, cpVect v) { swr(s)->surfaceV = v; }
+cpDataPointer cpShapeGetUserData(const cpShape *s) { return s->userData; }
+void cpShapeSetUserData(cpShape *s, cpDataPointer d) { s->userData = d; }
+cpCollisionType cpShapeGetCollisionType(const cpShape *s) { return s->ctype; }
+void cpShapeSetCollisionType(cpShape *s, cpCollisionType t) { s->ctype = t; }
+cpShapeFilter cpShapeGetFilter(const cpShape *s) { return s->filter; }
+void cpShapeSetFilter(cpShape *s, cpShapeFilter f) { swr(s)->filter = f; }
+cpVect cpCircleShapeGetOffset(const cpShape *s) { return s->c; }
+cpFloat cpCircleShapeGetRadius(const cpShape *s) { return s->r; }
+cpVect cpSegmentShapeGetA(const cpShape *s) { return s->sa; }
+cpVect cpSegmentShapeGetB(const cpShape *s) { return s->sb; }
+cpVect cpSegmentShapeGetNormal(const cpShape *s) { return s->sn; }
+cpFloat cpSegmentShapeGetRadius(const cpShape *s) { return s->r; }
+int cpPolyShapeGetCount(const cpShape *s) { return s->count; }
+cpVect cpPolyShapeGetVert(const cpShape *s, int i) { ASSERT_HARD(0 <= i && i < s->count, "Index out of range."); return s->lv[i]; }
+cpFloat cpPolyShapeGetRadius(const cpShape *s) { return s->r; }
+
+/* ====================================================================
+ * Constraints
+ * ==================================================================== */
+static cpConstraint *cons_new_(int kind, cpBody *a, cpBody *b)
+{
+	/* cpConstraint.c:37-57; errorBias uses the float expression 1.0f - 0.1f */
+	cpConstraint *c = (cpConstraint *)calloc(1, sizeof(cpConstraint));
+	c->kind = kind;
+	c->a = a; c->b = b;
+	c->maxForce = INF_;
+	c->errorBias = pow((cpFloat)(1.0f - 0.1f), 60.0);
+	c->maxBias = INF_;
+	c->collideBodies = cpTrue;
+	c->index = -1;
+	return c;
+}
+
+cpConstraint *cpPivotJointNew2(cpBody *a, cpBody *b, cpVect anchorA, cpVect anchorB)
+{
+	cpConstraint *c = cons_new_(CPG_PIVOT, a, b);
+	c->anchorA = anchorA; c->anchorB = anchorB;
+	return c;
+}
+
+cpConstraint *cpPivotJointNew(cpBody *a, cpBody *b, cpVect pivot)
+{
+	/* cpPivotJoint.c:110-116 */
+	cpVect anchorA = (a ? cpBodyWorldToLocal(a, pivot) : pivot);
+	cpVect anchorB = (b ? cpBodyWorldToLocal(b, pivot) : pivot);
+	return cpPivotJointNew2(a, b, anchorA, anchorB);
+}
+
+cpConstraint *cpPinJointNew(cpBody *a, cpBody *b, cpVect anchorA, cpVect anchorB)
+{
+	/* cpPinJoint.c:92-110 */
+	cpConstraint *c = cons_new_(CPG_PIN, a, b);
+	c->anchorA = anchorA; c->anchorB = anchorB;
+	cpVect p1 = (a ? cpTransformPoint(rd(a)->transform, anchorA) : anchorA);
+	cpVect p2 = (b ? cpTransformPoint(rd(b)->transform, anchorB) : anchorB);
+	c->dist = cpvlength(cpvsub(p2, p1));
+	return c;
+}
+
+cpConstraint *cpSlideJointNew(cpBody *a, cpBody *b, cpVect anchorA, cpVect anchorB, cpFloat min, cpFloat max)
+{
+	cpConstraint *c = cons_new_(CPG_SLIDE, a, b);
+	c->anchorA = anchorA; c->anchorB = anchorB;
+	c->min = min; c->max = max;
+	return c;
+}
+
+/* Joint records on the device accumulate impulses; refresh them lazily. */
+static void joints_pull_(cpSpace *sp)
+{
+	if(!sp || !sp->dev || !sp->consStale) return;
+	DevSet *ds = sp->dev;
+	int n = sp->ncons;
+	if(n > 0){
+		cpgJoint *rec = HALLOC(cpgJoint, n);
+		d2h(rec, ds->d.joints + ds->hworld[sp->world].consOff, sizeof(cpgJoint)*(size_t)n);
+		cuda_ok(cudaStreamSynchronize(lib_stream()), "download joints");
+		for(int i = 0; i < n; i++) sp->cons[i]->rec = rec[i];
+		free(rec);
+	}
+	sp->consStale = 0;
+}
+
+static void cons_pull_(cpConstraint *c) { if(c->space) joints_pull_(c->space); }
+
+static inline cpConstraint *cwr(cpConstraint *c)
+{
+	if(c->space){
+		joints_pull_(c->space);   /* keep the device-side accumulators */
+		c->space->consDirty = 1;
+	}
+	return c;
+}
+
+void cpConstraintFree(cpConstraint *c) { free(c); }
+cpSpace *cpConstraintGetSpace(const cpConstraint *c) { return c->space; }
+cpBody *cpConstraintGetBodyA(const cpConstraint *c) { return c->a; }
+cpBody *cpConstraintGetBodyB(const cpConstraint *c) { return c->b; }
+cpFloat cpConstraintGetMaxForce(const cpConstraint *c) { return c->maxForce; }
+void cpConstraintSetMaxForce(cpConstraint *c, cpFloat v) { ASSERT_HARD(v >= 0.0, "maxForce must be positive."); cwr(c)->maxForce = v; }
+cpFloat cpConstraintGetErrorBias(const cpConstraint *c) { return c->errorBias; }
+void cpConstraintSetErrorBias(cpConstraint *c, cpFloat v) { ASSERT_HARD(v >= 0.0, "errorBias must be positive."); cwr(c)->errorBias = v; }
+cpFloat cpConstraintGetMaxBias(const cpConstraint *c) { return c->maxBias; }
+void cpConstraintSetMaxBias(cpConstraint *c, cpFloat v) { ASSERT_HARD(v >= 0.0, "maxBias must be positive."); cwr(c)->maxBias = v; }
+cpBool cpConstraintGetCollideBodies(const cpConstraint *c) { return c->collideBodies; }
+void cpConstraintSetCollideBodies(cpConstraint *c, cpBool v)
+{
+	ASSERT_HARD(!c->space || !c->space->dev, "collideBodies must be set before the space is first stepped");
+	c->collideBodies = v;
+}
+void cpConstraintSetPreSolveFunc(cpConstraint *c, cpConstraintPreSolveFunc f) { c->preSolve = f; }
+void cpConstraintSetPostSolveFunc(cpConstraint *c, cpConstraintPostSolveFunc f) { c->postSolve = f; }
+cpDataPointer cpConstraintGetUserData(const cpConstraint *c) { return c->userData; }
+void cpConstraintSetUserData(cpConstraint *c, cpDataPointer d) { c->userData = d; }
+cpBool cpConstraintIsPivotJoint(const cpConstraint *c) { return c->kind == CPG_PIVOT; }
+cpBool cpConstraintIsPinJoint(const cpConstraint *c) { return c->kind == CPG_PIN; }
+cpBool cpConstraintIsSlideJoint(const cpConstraint *c) { return c->kind == CPG_SLIDE; }
+cpVect cpPivotJointGetAnchorA(const cpConstraint *c) { return c->anchorA; }
+cpVect cpPivotJointGetAnchorB(const cpConstraint *c) { return c->anchorB; }
+cpVect cpPinJointGetAnchorA(const cpConstraint *c) { return c->anchorA; }
+cpVect cpPinJointGetAnchorB(const cpConstraint *c) { return c->anchorB; }
+cpFloat cpPinJointGetDist(const cpConstraint *c) { return c->dist; }
+cpVect cpSlideJointGetAnchorA(const cpConstraint *c) { return c->anchorA; }
+cpVect cpSlideJointGetAnchorB(const cpConstraint *c) { return c->anchorB; }
+cpFloat cpSlideJointGetMin(const cpConstraint *c) { return c->min; }
+cpFloat cpSlideJointGetMax(const cpConstraint *c) { return c->max; }
+
+cpFloat cpConstraintGetImpulse(cpConstraint *c)
+{
+	cons_pull_(c);
+	if(c->kind == CPG_PIVOT) return cpvlength(cpv(c->rec.jx, c->rec.jy));
+	return habs(c->rec.jnAcc);
+}
+
+/* ====================================================================
+ * Space
+ * ==================================================================== */
+cpSpace *cpSpaceNew(void)
+{
+	/* cpSpace.c:119-178 (float literals: slop (double)0.1f, bias base 1.0f-0.1f) */
+	cpSpace *sp = (cpSpace *)calloc(1, sizeof(cpSpace));
+	sp->iterations = 10;
+	sp->damping = 1.0;
+	sp->collisionSlop = (cpFloat)0.1f;
+	sp->collisionBias = pow((cpFloat)(1.0f - 0.1f), 60.0);
+	sp->collisionPersistence = 3;
+	sp->sleepTimeThreshold = INF_;
+	sp->mode = CP_GPU_SOLVER_ORDERED;
+	body_init_(&sp->staticBody, 0.0, 0.0);
+	make_static_(&sp->staticBody);
+	sp->staticBody.space = sp;
+	return sp;
+}
+
+void cpSpaceFree(cpSpace *sp)
+{
+	if(!sp) return;
+	if(sp->dev && sp->ownsDev){
+		cudaStreamSynchronize(lib_stream());
+		devset_free(sp->dev);
+	}
+	for(int i = 0; i < sp->ndyn; i++) if(sp->dyn[i]->space == sp) sp->dyn[i]->space = NULL;
+	for(int i = 0; i < sp->nstat; i++) if(sp->stat[i]->space == sp) sp->stat[i]->space = NULL;
+	for(int i = 0; i < sp->nshapes; i++) if(sp->shapes[i]->space == sp) sp->shapes[i]->space = NULL;
+	for(int i = 0; i < sp->ncons; i++) if(sp->cons[i]->space == sp) sp->cons[i]->space = NULL;
+	free(sp->dyn); free(sp->stat); free(sp->shapes); free(sp->cons); free(sp->ops); free(sp->snap);
+	free(sp);
+}
+
+int cpSpaceGetIterations(const cpSpace *sp) { return sp->iterations; }
+void cpSpaceSetIterations(cpSpace *sp, int it) { ASSERT_HARD(it > 0, "Iterations must be positive and non-zero."); sp->iterations = it; }
+cpVect cpSpaceGetGravity(const cpSpace *sp) { return sp->gravity; }
+void cpSpaceSetGravity(cpSpace *sp, cpVect g) { sp->gravity = g; }
+cpFloat cpSpaceGetDamping(const cpSpace *sp) { return sp->damping; }
+void cpSpaceSetDamping(cpSpace *sp, cpFloat d) { ASSERT_HARD(d >= 0.0, "Damping must be positive."); sp->damping = d; }
+cpFloat cpSpaceGetIdleSpeedThreshold(const cpSpace *sp) { return sp->idleSpeedThreshold; }
+void cpSpaceSetIdleSpeedThreshold(cpSpace *sp, cpFloat v) { sp->idleSpeedThreshold = v; }
+cpFloat cpSpaceGetSleepTimeThreshold(const cpSpace *sp) { return sp->sleepTimeThreshold; }
+void cpSpaceSetSleepTimeThreshold(cpSpace *sp, cpFloat t) { sp->sleepTimeThreshold = t; }
+cpFloat cpSpaceGetCollisionSlop(const cpSpace *sp) { return sp->collisionSlop; }
+void cpSpaceSetCollisionSlop(cpSpace *sp, cpFloat v) { sp->collisionSlop = v; }
+cpFloat cpSpaceGetCollisionBias(const cpSpace *sp) { return sp->collisionBias; }
+void cpSpaceSetCollisionBias(cpSpace *sp, cpFloat v) { sp->collisionBias = v; }
+cpTimestamp cpSpaceGetCollisionPersistence(const cpSpace *sp) { return sp->collisionPersistence; }
+void cpSpaceSetCollisionPersistence(cpSpace *sp, cpTimestamp v) { sp->collisionPersistence = v; }
+cpDataPointer cpSpaceGetUserData(const cpSpace *sp) { return sp->userData; }
+void cpSpaceSetUserData(cpSpace *sp, cpDataPointer d) { sp->userData = d; }
+cpBody *cpSpaceGetStaticBody(const cpSpace *sp) { return (cpBody *)&sp->staticBody; }
+cpFloat cpSpaceGetCurrentTimeStep(const cpSpace *sp) { return sp->curr_dt; }
+cpBool cpSpaceIsLocked(cpSpace *sp) { (void)sp; return cpFalse; }
+cpBool cpSpaceContainsShape(cpSpace *sp, cpShape *s) { return s->space == sp; }
+cpBool cpSpaceContainsBody(cpSpace *sp, cpBody *b) { return b->space == sp; }
+cpBool cpSpaceContainsConstraint(cpSpace *sp, cpConstraint *c) { return c->space == sp; }
+void cpGpuSetSolverMode(cpSpace *sp, int mode) { sp->mode = mode; }
+int cpGpuGetSolverMode(const cpSpace *sp) { return sp->mode; }
+
+cpBody *cpSpaceAddBody(cpSpace *sp, cpBody *b)
+{
+	/* cpSpace.c:440-451 */
+	ASSERT_HARD(b->space != sp, "You have already added this body to this space. You must not add it a second time.");
+	ASSERT_HARD(!b->space, "You have already added this body to another space. You cannot add it to a second.");
+	if(body_type_(b) == CP_BODY_TYPE_STATIC) push_((void ***)&sp->stat, &sp->nstat, &sp->capstat, b);
+	else push_((void ***)&sp->dyn, &sp->ndyn, &sp->capdyn, b);
+	b->space = sp;
+	return b;
+}
+
+cpShape *cpSpaceAddShape(cpSpace *sp, cpShape *s)
+{
+	/* cpSpace.c:417-438 */
+	ASSERT_HARD(s->space != sp, "You have already added this shape to this space. You must not add it a second time.");
+	ASSERT_HARD(!s->space, "You have already added this shape to another space. You cannot add it to a second.");
+	ASSERT_HARD(s->body, "The shape's body is not defined.");
+	ASSERT_HARD(s->body->space == sp, "The shape's body must be added to the space before the shape.");
+	cpBody *body = s->body;
+	rd(body);
+	int isStatic = (body_type_(body) == CP_BODY_TYPE_STATIC);
+	cpShape *next = body->shapeList;
+	if(next) next->prev = s;
+	s->next = next;
+	body->shapeList = s;
+	if(s->mass_m > 0.0) accumulate_mass_(body);
+	s->hashid = sp->shapeIDCounter++;
+	cpBB bb = shape_cache_(s, body->transform);
+	/* record the insertion with its add-time box and velocity */
+	if(sp->nops == sp->capops){
+		sp->capops = sp->capops ? 2*sp->capops : 256;
+		sp->ops = (cpgOp *)realloc(sp->ops, sizeof(cpgOp)*(size_t)sp->capops);
+	}
+	cpgOp *op = &sp->ops[sp->nops++];
+	memset(op, 0, sizeof(*op));
+	op->shape = (int)s->hashid;
+	op->isStatic = isStatic;
+	op->l = bb.l; op->b = bb.b; op->r = bb.r; op->t = bb.t;
+	op->vx = body->v.x; op->vy = body->v.y;
+	push_((void ***)&sp->shapes, &sp->nshapes, &sp->capshapes, s);
+	s->space = sp;
+	return s;
+}
+
+cpConstraint *cpSpaceAddConstraint(cpSpace *sp, cpConstraint *c)
+{
+	/* cpSpace.c:453-474 */
+	ASSERT_HARD(c->space != sp, "You have already added this constraint to this space. You must not add it a second time.");
+	ASSERT_HARD(!c->space, "You have already added this constraint to another space. You cannot add it to a second.");
+	ASSERT_HARD(c->a != NULL && c->b != NULL, "Constraint is attached to a NULL body.");
+	cpBody *a = c->a, *b = c->b;
+	c->index = sp->ncons;
+	push_((void ***)&sp->cons, &sp->ncons, &sp->capcons, c);
+	c->next_a = a->constraintList; a->constraintList = c;
+	c->next_b = b->constraintList; b->constraintList = c;
+	c->space = sp;
+	return c;
+}
+
+void cpSpaceEachBody(cpSpace *sp, cpSpaceBodyIteratorFunc func, void *data)
+{
+	for(int i = 0; i < sp->ndyn; i++) func(sp->dyn[i], data);
+	for(int i = 0; i < sp->nstat; i++) func(sp->stat[i], data);
+}
+
+void cpSpaceEachShape(cpSpace *sp, cpSpaceShapeIteratorFunc func, void *data)
+{
+	for(int i = 0; i < sp->nshapes; i++) func(sp->shapes[i], data);
+}
+
+void cpSpaceEachConstraint(cpSpace *sp, cpSpaceConstraintIteratorFunc func, void *data)
+{
+	for(int i = 0; i < sp->ncons; i++) func(sp->cons[i], data);
+}
+
+/* ====================================================================
+ * Arbiters: snapshot of the solve list (cpArbiter.c:54-155)
+ * ==================================================================== */
+static int space_snapshot(cpSpace *sp)
+{
+	if(sp->snapValid) return 1;
+	sp->nsnap = 0;
+	if(!sp->dev){ sp->snapValid = 1; return 1; }
+	space_pull(sp);
+	DevSet *ds = sp->dev;
+	cpgTree T;
+	d2h(&T, ds->d.tree + sp->world, sizeof(cpgTree));
+	cudaStreamSynchronize(lib_stream());
+	int n = T.narb;
+	if(n > ds->gatherCap){
+		if(ds->gather) cudaFree(ds->gather);
+		ds->gatherCap = n + n/2 + 64;
+		if(!cuda_ok(cudaMalloc((void **)&ds->gather, sizeof(cpgArb)*(size_t)ds->gatherCap), "gather")) { ds->gatherCap = 0; ds->gather = NULL; return 0; }
+	}
+	cpgArb *host = HALLOC(cpgArb, n);
+	if(n > 0){
+		cpg_launch_gather_arbs(&ds->d, sp->world, ds->gather, n, lib_stream());
+		d2h(host, ds->gather, sizeof(cpgArb)*(size_t)n);
+		cudaStreamSynchronize(lib_stream());
+	}
+	if(n > sp->capsnap){
+		sp->capsnap = n + 64;
+		sp->snap = (cpArbiter *)realloc(sp->snap, sizeof(cpArbiter)*(size_t)sp->capsnap);
+	}
+	for(int i = 0; i < n; i++){
+		cpArbiter *arb = &sp->snap[i];
+		cpgArb *g = &host[i];
+		arb->a = sp->shapes[g->a]; arb->b = sp->shapes[g->b];
+		arb->body_a = arb->a->body; arb->body_b = arb->b->body;
+		arb->count = g->count; arb->state = g->state;
+		arb->n = cpv(g->nx, g->ny); arb->surface_vr = cpv(g->svx, g->svy);
+		arb->e = g->e; arb->u = g->u; arb->swapped = cpFalse;
+		arb->c[0] = g->c[0]; arb->c[1] = g->c[1];
+	}
+	sp->nsnap = n;
+	sp->snapValid = 1;
+	free(host);
+	return 1;
+}
+
+int cpArbiterGetCount(const cpArbiter *arb) { return (arb->state < CPG_ARB_CACHED ? arb->count : 0); }
+cpFloat cpArbiterGetRestitution(const cpArbiter *arb) { return arb->e; }
+cpFloat cpArbiterGetFriction(const cpArbiter *arb) { return arb->u; }
+cpVect cpArbiterGetSurfaceVelocity(cpArbiter *arb) { return cpvmult(arb->surface_vr, arb->swapped ? -1.0 : 1.0); }
+cpBool cpArbiterIsFirstContact(const cpArbiter *arb) { return arb->state == CPG_ARB_FIRST; }
+cpVect cpArbiterGetNormal(const cpArbiter *arb) { return cpvmult(arb->n, arb->swapped ? -1.0 : 1.0); }
+
+cpVect cpArbiterGetPointA(const cpArbiter *arb, int i)
+{
+	ASSERT_HARD(0 <= i && i < cpArbiterGetCount(arb), "Index error: The specified contact index is invalid for this arbiter");
+	return cpvadd(arb->body_a->p, cpv(arb->c[i].r1x, arb->c[i].r1y));
+}
+
+cpVect cpArbiterGetPointB(const cpArbiter *arb, int i)
+{
+	ASSERT_HARD(0 <= i && i < cpArbiterGetCount(arb), "Index error: The specified contact index is invalid for this arbiter");
+	return cpvadd(arb->body_b->p, cpv(arb->c[i].r2x, arb->c[i].r2y));
+}
+
+cpFloat cpArbiterGetDepth(const cpArbiter *arb, int i)
+{
+	ASSERT_HARD(0 <= i && i < cpArbiterGetCount(arb), "Index error: The specified contact index is invalid for this arbiter");
+	const cpgContact *con = &arb->c[i];
+	return cpvdot(cpvadd(cpvsub(cpv(con->r2x, con->r2y), cpv(con->r1x, con->r1y)), cpvsub(arb->body_b->p, arb->body_a->p)), arb->n);
+}
+
+cpVect cpArbiterTotalImpulse(const cpArbiter *arb)
+{
+	cpVect n = arb->n, sum = cpvzero;
+	for(int i = 0, count = cpArbiterGetCount(arb); i < count; i++){
+		sum = cpvadd(sum, cpvrotate(n, cpv(arb->c[i].jnAcc, arb->c[i].jtAcc)));
+	}
+	return (arb->swapped ? sum : cpvneg(sum));
+}
+
+cpFloat cpArbiterTotalKE(const cpArbiter *arb)
+{
+	cpFloat eCoef = (1 - arb->e)/(1 + arb->e);
+	cpFloat sum = 0.0;
+	for(int i = 0, count = cpArbiterGetCount(arb); i < count; i++){
+		const cpgContact *con = &arb->c[i];
+		sum += eCoef*con->jnAcc*con->jnAcc/con->nMass + con->jtAcc*con->jtAcc/con->tMass;
+	}
+	return sum;
+}
+
+void cpArbiterGetShapes(const cpArbiter *arb, cpShape **a, cpShape **b)
+{
+	if(arb->swapped){ *a = arb->b; *b = arb->a; } else { *a = arb->a; *b = arb->b; }
+}
+
+void cpArbiterGetBodies(const cpArbiter *arb, cpBody **a, cpBody **b)
+{
+	cpShape *sa, *sb;
+	cpArbiterGetShapes(arb, &sa, &sb);
+	*a = sa->body; *b = sb->body;
+}
+
+cpContactPointSet cpArbiterGetContactPointSet(const cpArbiter *arb)
+{
+	cpContactPointSet set;
+	memset(&set, 0, sizeof(set));
+	set.count = cpArbiterGetCount(arb);
+	cpBool swapped = arb->swapped;
+	cpVect n = arb->n;
+	set.normal = (swapped ? cpvneg(n) : n);
+	for(int i = 0; i < set.count; i++){
+		cpVect p1 = cpvadd(arb->body_a->p, cpv(arb->c[i].r1x, arb->c[i].r1y));
+		cpVect p2 = cpvadd(arb->body_b->p, cpv(arb->c[i].r2x, arb->c[i].r2y));
+		set.points[i].pointA = (swapped ? p2 : p1);
+		set.points[i].pointB = (swapped ? p1 : p2);
+		set.points[i].distance = cpvdot(cpvsub(p2, p1), n);
+	}
+	return set;
+}
+
+/* The contact graph threads each solved arbiter onto the head of both
+ * bodies' lists (cpSpaceComponent.c:170-181), so a body sees its arbiters
+ * in reverse solve order, with `swapped` relative to it (cpBody.c:612-626). */
+void cpBodyEachArbiter(cpBody *body, cpBodyArbiterIteratorFunc func, void *data)
+{
+	cpSpace *sp = body->space;
+	if(!sp || !space_snapshot(sp)) return;
+	for(int i = sp->nsnap - 1; i >= 0; i--){
+		cpArbiter *arb = &sp->snap[i];
+		if(arb->body_a != body && arb->body_b != body) continue;
+		cpBool swapped = arb->swapped;
+		arb->swapped = (body == arb->body_b);
+		func(body, arb, data);
+		arb->swapped = swapped;
+	}
+}
+
+/* ====================================================================
+ * Debug export (shared record layouts) and per-phase timing
+ * ==================================================================== */
+int cpGpuDebugBodies(cpSpace *sp, double *out, int max)
+{
+	space_pull(sp);
+	for(int i = 0; i < sp->ndyn && i < max; i++){
+		cpBody *b = sp->dyn[i];
+		double *o = out + 18*i;
+		o[0] = b->p.x; o[1] = b->p.y; o[2] = b->v.x; o[3] = b->v.y; o[4] = b->a; o[5] = b->w;
+		o[6] = b->f.x; o[7] = b->f.y; o[8] = b->t; o[9] = b->v_bias.x; o[10] = b->v_bias.y; o[11] = b->w_bias;
+		o[12] = b->transform.a; o[13] = b->transform.b; o[14] = b->transform.c; o[15] = b->transform.d;
+		o[16] = b->transform.tx; o[17] = b->transform.ty;
+	}
+	return sp->ndyn;
+}
+
+int cpGpuDebugSetBodies(cpSpace *sp, const double *in, int count)
+{
+	space_pull(sp);
+	for(int i = 0; i < sp->ndyn && i < count; i++){
+		cpBody *b = sp->dyn[i];
+		const double *o = in + 18*i;
+		b->p = cpv(o[0], o[1]); b->v = cpv(o[2], o[3]); b->a = o[4]; b->w = o[5];
+		b->f = cpv(o[6], o[7]); b->t = o[8]; b->v_bias = cpv(o[9], o[10]); b->w_bias = o[11];
+		b->transform = cpTransformNew(o[12], o[13], o[14], o[15], o[16], o[17]);
+	}
+	sp->bodyDirty = 1;
+	return sp->ndyn;
+}
+
+int cpGpuDebugArbiters(cpSpace *sp, double *out, int max)
+{
+	if(!space_snapshot(sp)) return 0;
+	for(int i = 0; i < sp->nsnap && i < max; i++){
+		cpArbiter *arb = &sp->snap[i];
+		double *o = out + 34*i;
+		memset(o, 0, 34*sizeof(double));
+		o[0] = (double)arb->a->hashid; o[1] = (double)arb->b->hashid; o[2] = arb->count; o[3] = arb->state;
+		o[4] = arb->n.x; o[5] = arb->n.y; o[6] = arb->e; o[7] = arb->u; o[8] = arb->surface_vr.x; o[9] = arb->surface_vr.y;
+		for(int c = 0; c < arb->count; c++){
+			const cpgContact *con = &arb->c[c];
+			double *q = o + 10 + 12*c;
+			q[0] = con->r1x; q[1] = con->r1y; q[2] = con->r2x; q[3] = con->r2y;
+			q[4] = con->nMass; q[5] = con->tMass; q[6] = con->bounce; q[7] = con->jnAcc; q[8] = con->jtAcc;
+			q[9] = con->jBias; q[10] = con->bias; q[11] = (double)(con->hash & 0xffffffffffffULL);
+		}
+	}
+	return sp->nsnap;
+}
+
+int cpGpuDebugConstraints(cpSpace *sp, double *out, int max)
+{
+	for(int i = 0; i < sp->ncons && i < max; i++){
+		cpConstraint *c = sp->cons[i];
+		cons_pull_(c);
+		const cpgJoint *j = &c->rec;
+		double *o = out + 8*i;
+		o[0] = (double)c->kind;
+		if(c->kind == CPG_PIVOT){ o[1] = j->jx; o[2] = j->jy; o[7] = j->biasx; }
+		else { o[1] = j->jnAcc; o[2] = j->nMass; o[7] = j->bias; }
+		o[3] = j->r1x; o[4] = j->r1y; o[5] = j->r2x; o[6] = j->r2y;
+	}
+	return sp->ncons;
+}
+
+int cpGpuGetPhaseTimes(cpSpace *sp, double *ms, int max)
+{
+	for(int i = 0; i < 7 && i < max; i++) ms[i] = sp->phaseMs[i];
+	return 7;
+}
+
+/* The shared harness names used by the tests for every implementation. */
+int cpx_dump_bodies(cpSpace *sp, double *out, int max) { return cpGpuDebugBodies(sp, out, max); }
+int cpx_dump_arbiters(cpSpace *sp, double *out, int max) { return cpGpuDebugArbiters(sp, out, max); }
+int cpx_dump_constraints(cpSpace *sp, double *out, int max) { return cpGpuDebugConstraints(sp, out, max); }
+int cpx_set_bodies(cpSpace *sp, const double *in, int count) { return cpGpuDebugSetBodies(sp, in, count); }

@@ -1,0 +1,240 @@
+/*
+ * cpg_device.h -- device data layout shared by the C host code and the
+ * CUDA kernels of libchipmunk_gb300.
+ *
+ * A "set" holds W independent worlds (a single cpSpace is a set of one;
+ * cpGpuBatch packs thousands).  Every per-object array is the
+ * concatenation of the worlds' ranges; cpgWorld gives each world's base
+ * offsets and capacities.  All cross-references stored in device memory
+ * (body of a shape, tree node links, pair links, arbiter shapes) are
+ * world-local indices, so a world can be moved to a new base without
+ * rewriting its contents.
+ *
+ * Plain C structs only: both gcc and nvcc compile this header and must
+ * agree on every layout (all members are 4- or 8-byte scalars).
+ */
+#ifndef CPG_DEVICE_H
+#define CPG_DEVICE_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* shape kinds, in the collision-dispatch order of cpCollision.c:688-699 */
+enum { CPG_CIRCLE = 0, CPG_SEGMENT = 1, CPG_POLY = 2 };
+/* body types as cpBodyType */
+enum { CPG_DYNAMIC = 0, CPG_KINEMATIC = 1, CPG_STATIC = 2 };
+/* joint kinds */
+enum { CPG_PIVOT = 1, CPG_PIN = 2, CPG_SLIDE = 3 };
+/* arbiter states, chipmunk_structs.h:83-95 */
+enum { CPG_ARB_FIRST = 0, CPG_ARB_NORMAL = 1, CPG_ARB_IGNORE = 2, CPG_ARB_CACHED = 3 };
+/* error bits latched in cpgTree.error */
+enum { CPG_ERR_NODES = 1, CPG_ERR_PAIRS = 2, CPG_ERR_CANDS = 4, CPG_ERR_ARBS = 8, CPG_ERR_BINS = 16, CPG_ERR_LEVELS = 32 };
+
+#define CPG_KEY_EMPTY 0ull
+#define CPG_KEY_TOMB 1ull
+
+/* Per-world offsets and capacities (host-written, read-only on device). */
+typedef struct cpgWorld {
+	int bodyOff, nbodies, ndyn;   /* dynamic+kinematic bodies are [0, ndyn) */
+	int shapeOff, nshapes;
+	int vertOff, nverts;          /* polygon vertex storage */
+	int consOff, ncons;
+	int nodeOff, nodeCap;
+	int pairOff, pairCap;
+	int dbinOff, dbinCap;         /* leaf-set bins of the dynamic tree */
+	int sbinOff, sbinCap;         /* leaf-set bins of the static tree */
+	int candOff, candCap;         /* candidate pairs emitted per step */
+	int unitOff, unitCap;         /* solver units: arbiters then joints */
+	int opOff, nops;              /* pending index insertions */
+	int partOff;                  /* CSR of non-colliding joint partners */
+	int pad;
+} cpgWorld;
+
+/* Per-world step parameters (host-written each step). */
+typedef struct cpgParams {
+	double dt, dt_coef, damping, slop, biasCoef, gx, gy;
+	int iterations;
+	unsigned stamp;               /* cpSpace.stamp after the increment */
+	unsigned persistence;
+	int active;                   /* 0: world skipped this launch */
+} cpgParams;
+
+/* Per-world device-resident tree/bookkeeping state. */
+typedef struct cpgTree {
+	int dynRoot, statRoot;
+	unsigned treeStamp;           /* stamp of the dynamic (master) tree */
+	int freeNode, nodeTop;
+	int freePair, pairTop;
+	unsigned dynSize, dynEntries;
+	unsigned statSize, statEntries;
+	int ncand;                    /* candidates emitted this step */
+	int narb;                     /* arbiters in the solve list */
+	int nunits;                   /* arbiters + joints */
+	int nlevels;                  /* schedule depth of one sweep */
+	int error;
+	int pairsLive;
+	int maxChain;
+	int pad;
+} cpgTree;
+
+/* AABB-tree node (cpBBTree.c:46-60), 64 bytes. */
+typedef struct cpgNode {
+	double l, b, r, t;
+	int parent, A, B;
+	int obj;                      /* shape index for leaves, -1 internal */
+	unsigned stamp;
+	int pairs;                    /* leaves: head of the pair thread list */
+	int binNext;                  /* leaves: next leaf in the hash bin */
+	int pad;
+} cpgNode;
+
+/* Cached leaf pair (cpBBTree.c:62-72), 32 bytes. */
+typedef struct cpgPair {
+	int aPrev, aLeaf, aNext;
+	int bPrev, bLeaf, bNext;
+	unsigned id;
+	int pad;
+} cpgPair;
+
+/* Candidate emitted by the tree traversal, in solve-order. */
+typedef struct cpgCand {
+	int a, b;                     /* shapes, in the order the query passes them */
+	int pair;                     /* cached pair receiving the new GJK id, or -1 */
+	unsigned idIn;
+} cpgCand;
+
+/* Narrow-phase result for one candidate. */
+typedef struct cpgNarrow {
+	double nx, ny;
+	double p1x[2], p1y[2], p2x[2], p2y[2];
+	unsigned long long hash[2];
+	int count;                    /* 0..2 contacts */
+	int flip;                     /* 1 when info.a is the candidate's b */
+	unsigned idOut;
+	int pad;
+} cpgNarrow;
+
+typedef struct cpgContact {
+	double r1x, r1y, r2x, r2y;
+	double nMass, tMass, bounce, jnAcc, jtAcc, jBias, bias;
+	unsigned long long hash;
+} cpgContact;
+
+/* Cached arbiter (chipmunk_structs.h:124-145), one per table slot. */
+typedef struct cpgArb {
+	int a, b;                     /* shapes, info order of the last update */
+	int ba, bb;                   /* their bodies */
+	int count, state;
+	unsigned stamp;
+	int world;
+	double nx, ny, e, u, svx, svy;
+	cpgContact c[2];
+} cpgArb;
+
+/* Joint (cpPivotJoint/cpPinJoint/cpSlideJoint), one record per joint. */
+typedef struct cpgJoint {
+	int kind, a, b, pad;
+	double ax, ay, bx, by;        /* anchors in body space */
+	double maxForce, biasCoef, maxBias;
+	double dist, min, max;
+	double r1x, r1y, r2x, r2y;
+	double k11, k12, k21, k22;    /* pivot: inverse mass tensor */
+	double jx, jy;                /* pivot: accumulated impulse */
+	double biasx, biasy;          /* pivot: bias velocity */
+	double nx, ny, nMass, jnAcc, bias;  /* pin/slide */
+} cpgJoint;
+
+/* Pending tree insertion recorded by cpSpaceAddShape, with the shape's
+ * box and its body's velocity as they were at that call (the reference
+ * builds the leaf's fattened box immediately, cpBBTree.c:605-616). */
+typedef struct cpgOp {
+	int shape;
+	int isStatic;
+	int pad0, pad1;
+	double l, b, r, t;
+	double vx, vy;
+} cpgOp;
+
+/* All device arrays of a set.  Vectors are split into x/y arrays. */
+typedef struct cpgSet {
+	int nworlds;
+	int totalBodies, totalShapes, totalVerts, totalCons;
+	int totalNodes, totalPairs, totalDBins, totalSBins, totalCands, totalUnits, totalOps, totalParts;
+	int arbCap;                   /* arbiter hash table slots (power of two) */
+	int maxWorldUnits;
+
+	cpgWorld *world;              /* [nworlds] */
+	cpgParams *params;            /* [nworlds] */
+	cpgTree *tree;                /* [nworlds] */
+
+	/* bodies [totalBodies] */
+	double *px, *py, *vx, *vy, *fx, *fy, *ang, *w, *tq;
+	double *ta, *tb, *tc, *td, *ttx, *tty;   /* transform */
+	double *vbx, *vby, *wb;
+	double *m, *minv, *i, *iinv, *cogx, *cogy;
+	int *btype, *bworld;
+	int *partStart, *partCount;   /* joint partners with collideBodies off */
+	int *parts;                   /* [totalParts] */
+	int *last;                    /* schedule scratch */
+
+	/* shapes [totalShapes] */
+	int *skind, *sbody, *sleaf, *sworld, *svoff, *svcount;
+	double *sr;
+	double *s0x, *s0y, *s1x, *s1y, *snx, *sny;   /* local: circle c | seg a, b, n */
+	double *w0x, *w0y, *w1x, *w1y, *wnx, *wny;   /* world: circle tc | seg ta, tb, tn */
+	double *atx, *aty, *btx, *bty;               /* segment tangents */
+	double *bbl, *bbb, *bbr, *bbt;
+	double *se, *su, *svx, *svy;
+	unsigned long long *sgroup;
+	unsigned *scat, *smask;
+	unsigned char *ssensor;
+	unsigned long long *shash;    /* cpShape.hashid */
+
+	/* polygon planes [totalVerts]: local and world */
+	double *lvx, *lvy, *lnx, *lny, *gvx, *gvy, *gnx, *gny;
+
+	/* tree */
+	cpgNode *nodes;               /* [totalNodes] */
+	cpgPair *pairs;               /* [totalPairs] */
+	int *dbins, *sbins;
+	cpgOp *ops;                   /* [totalOps] */
+
+	/* per-step collision data [totalCands] */
+	cpgCand *cands;
+	cpgNarrow *narrow;
+	int *candArb;                 /* arbiter slot pushed to the solve list, or -1 */
+	int *arbList;                 /* solve list: arbiter slots, per world */
+	int *prevList;                /* previous step's solve list */
+	int *prevCount;               /* [nworlds] */
+
+	/* arbiter hash table [arbCap] */
+	unsigned long long *keys;
+	cpgArb *arbs;
+
+	/* joints [totalCons] */
+	cpgJoint *joints;
+	double *jbias;                /* 1 - pow(errorBias, dt), host-computed */
+
+	/* schedule [totalUnits] */
+	int *unitA, *unitB;           /* dynamic bodies touched (-1 none) */
+	int *unitLevel, *unitOrder;
+	int *levelStart;              /* [totalUnits + nworlds] */
+
+	/* stats block copied to the host after each step */
+	int *stats;
+} cpgSet;
+
+/* ---- launchers (cpg_kernels.cu) ---- */
+int cpg_launch_apply_ops(const cpgSet *s, void *stream);
+int cpg_launch_step(const cpgSet *s, const cpgSet *host_mirror, int mode, void *stream, float *phase_ms);
+int cpg_launch_gather_arbs(const cpgSet *s, int world, cpgArb *out, int n, void *stream);
+long long cpg_launch_count(int reset);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif

@@ -1,0 +1,881 @@
+/*
+ * cpg_kernels.cu -- sm_103a kernels of the cpSpaceStep pipeline and their
+ * C-callable launchers.
+ *
+ * One step of a set of worlds (src/cpSpaceStep.c:335-445) runs as:
+ *   k_reset_prev      arbiters solved last step return to NORMAL   (:351-360)
+ *   k_integrate_pos   position_func over dynamic bodies             (:364-367)
+ *   k_shape_cache     world-space shape data + AABBs                (:371)
+ *   k_tree            reference-order broadphase, 1 thread/world    (:372)
+ *   k_narrow          QueryReject + cpCollide per candidate         (:235-244)
+ *   k_arb_update      arbiter cache upsert + cpArbiterUpdate        (:246-288)
+ *   k_solve_list      order-preserving compaction -> solve list     (:274)
+ *   k_arb_filter      age out cached arbiters                       (:380)
+ *   k_schedule        exact-order level schedule of the sweep
+ *   k_prestep         cpArbiterPreStep + joint preStep              (:383-396)
+ *   k_integrate_vel   velocity_func                                 (:399-404)
+ *   k_solve           warm start + iterations, level by level       (:406-427)
+ *
+ * The solver sweep is the reference's serial Gauss-Seidel order.  Two units
+ * (arbiters or joints) that share no dynamic body commute exactly, so the
+ * schedule assigns every unit the level 1 + max(level of the previous unit
+ * touching each of its dynamic bodies); units of one level run in parallel
+ * and every body still sees its updates in the reference order, giving
+ * bit-identical results.  Static and kinematic bodies have zero inverse
+ * mass, are never written, and create no dependency.
+ *
+ * Compiled with --fmad=false: no multiply-add contraction, so every
+ * floating-point operation rounds like the reference's C code.
+ */
+#include <cstdio>
+#include <cuda_runtime.h>
+#include <math_constants.h>
+#include "cpg_device.h"
+#include "cpg_math.cuh"
+#include "cpg_tree.cuh"
+#include "cpg_narrow.cuh"
+
+static long long g_launches = 0;
+
+extern "C" long long cpg_launch_count(int reset)
+{
+	long long n = g_launches;
+	if(reset) g_launches = 0;
+	return n;
+}
+
+#define LAUNCH(...) do { __VA_ARGS__; g_launches++; } while(0)
+
+/* ------------------------------------------------------------------ */
+/* Index maintenance: pending insertions, in add order (cpSpace.c:417-438) */
+
+__device__ TreeCtx make_tree_ctx(const cpgSet *s, int w)
+{
+	const cpgWorld &W = s->world[w];
+	TreeCtx c;
+	c.nodes = s->nodes + W.nodeOff;
+	c.pairs = s->pairs + W.pairOff;
+	c.nodeCap = W.nodeCap;
+	c.pairCap = W.pairCap;
+	c.T = s->tree + w;
+	c.dbins = s->dbins + W.dbinOff;
+	c.sbins = s->sbins + W.sbinOff;
+	c.dbinCap = W.dbinCap;
+	c.sbinCap = W.sbinCap;
+	c.bbl = s->bbl + W.shapeOff; c.bbb = s->bbb + W.shapeOff;
+	c.bbr = s->bbr + W.shapeOff; c.bbt = s->bbt + W.shapeOff;
+	c.sbody = s->sbody + W.shapeOff;
+	c.shash = s->shash + W.shapeOff;
+	c.vx = s->vx + W.bodyOff; c.vy = s->vy + W.bodyOff;
+	c.cands = s->cands + W.candOff;
+	c.candCap = W.candCap;
+	c.ncand = 0;
+	c.collide = 0;
+	return c;
+}
+
+__global__ void k_apply_ops(cpgSet s)
+{
+	int w = blockIdx.x*blockDim.x + threadIdx.x;
+	if(w >= s.nworlds) return;
+	const cpgWorld &W = s.world[w];
+	if(W.nops == 0) return;
+	TreeCtx c = make_tree_ctx(&s, w);
+	for(int i = 0; i < W.nops; i++){
+		cpgOp op = s.ops[W.opOff + i];
+		tree_insert(c, op);
+	}
+}
+
+/* ------------------------------------------------------------------ */
+
+__global__ void k_reset_prev(cpgSet s)
+{
+	int w = blockIdx.x;
+	if(!s.params[w].active) return;
+	const cpgWorld &W = s.world[w];
+	int n = s.tree[w].narb;
+	for(int i = threadIdx.x; i < n; i += blockDim.x){
+		int slot = s.arbList[W.candOff + i];
+		s.arbs[slot].state = CPG_ARB_NORMAL;
+	}
+}
+
+/* cpBody.c:347-357 */
+__device__ __forceinline__ void set_transform(const cpgSet &s, int g, double px, double py, double a)
+{
+	double cx = s.cogx[g], cy = s.cogy[g];
+	double rx = cos(a), ry = sin(a);
+	s.ta[g] = rx; s.tb[g] = ry;
+	s.tc[g] = -ry; s.td[g] = rx;
+	s.ttx[g] = px - (cx*rx - cy*ry);
+	s.tty[g] = py - (cx*ry + cy*rx);
+}
+
+/* cpBody.c:511-522 over each world's dynamic-body list */
+__global__ void k_integrate_pos(cpgSet s)
+{
+	int g = blockIdx.x*blockDim.x + threadIdx.x;
+	if(g >= s.totalBodies) return;
+	int w = s.bworld[g];
+	const cpgParams &P = s.params[w];
+	if(!P.active || g - s.world[w].bodyOff >= s.world[w].ndyn) return;
+	double dt = P.dt;
+	double px = s.px[g] + (s.vx[g] + s.vbx[g])*dt;
+	double py = s.py[g] + (s.vy[g] + s.vby[g])*dt;
+	double a = s.ang[g] + (s.w[g] + s.wb[g])*dt;
+	s.px[g] = px; s.py[g] = py; s.ang[g] = a;
+	set_transform(s, g, px, py, a);
+	s.vbx[g] = 0.0; s.vby[g] = 0.0; s.wb[g] = 0.0;
+}
+
+/* Shape caches: cpShape.c:291-296 (circle), :378-405 (segment),
+ * cpPolyShape.c:39-64 (polygon).  Shapes of static bodies are skipped. */
+__device__ void cache_shape(const cpgSet &s, int g)
+{
+	int w = s.sworld[g];
+	const cpgWorld &W = s.world[w];
+	int body = W.bodyOff + s.sbody[g];
+	double ta = s.ta[body], tb = s.tb[body], tc = s.tc[body], td = s.td[body], tx = s.ttx[body], ty = s.tty[body];
+	int kind = s.skind[g];
+	double r = s.sr[g];
+	if(kind == CPG_CIRCLE){
+		double cx = s.s0x[g], cy = s.s0y[g];
+		double wx = ta*cx + tc*cy + tx, wy = tb*cx + td*cy + ty;
+		s.w0x[g] = wx; s.w0y[g] = wy;
+		s.bbl[g] = wx - r; s.bbb[g] = wy - r; s.bbr[g] = wx + r; s.bbt[g] = wy + r;
+	} else if(kind == CPG_SEGMENT){
+		double ax = s.s0x[g], ay = s.s0y[g], bx = s.s1x[g], by = s.s1y[g], nx = s.snx[g], ny = s.sny[g];
+		double tax = ta*ax + tc*ay + tx, tay = tb*ax + td*ay + ty;
+		double tbx = ta*bx + tc*by + tx, tby = tb*bx + td*by + ty;
+		s.w0x[g] = tax; s.w0y[g] = tay; s.w1x[g] = tbx; s.w1y[g] = tby;
+		s.wnx[g] = ta*nx + tc*ny; s.wny[g] = tb*nx + td*ny;
+		double l, rr, b, t;
+		if(tax < tbx){ l = tax; rr = tbx; } else { l = tbx; rr = tax; }
+		if(tay < tby){ b = tay; t = tby; } else { b = tby; t = tay; }
+		s.bbl[g] = l - r; s.bbb[g] = b - r; s.bbr[g] = rr + r; s.bbt[g] = t + r;
+	} else {
+		int off = W.vertOff + s.svoff[g];
+		int count = s.svcount[g];
+		double l = CUDART_INF, rr = -CUDART_INF, b = CUDART_INF, t = -CUDART_INF;
+		for(int i = 0; i < count; i++){
+			double vx = s.lvx[off + i], vy = s.lvy[off + i];
+			double nx = s.lnx[off + i], ny = s.lny[off + i];
+			double gx = ta*vx + tc*vy + tx, gy = tb*vx + td*vy + ty;
+			s.gvx[off + i] = gx; s.gvy[off + i] = gy;
+			s.gnx[off + i] = ta*nx + tc*ny; s.gny[off + i] = tb*nx + td*ny;
+			l = dmin(l, gx); rr = dmax(rr, gx);
+			b = dmin(b, gy); t = dmax(t, gy);
+		}
+		s.bbl[g] = l - r; s.bbb[g] = b - r; s.bbr[g] = rr + r; s.bbt[g] = t + r;
+	}
+}
+
+__global__ void k_shape_cache(cpgSet s)
+{
+	int g = blockIdx.x*blockDim.x + threadIdx.x;
+	if(g >= s.totalShapes) return;
+	int w = s.sworld[g];
+	if(!s.params[w].active) return;
+	int body = s.world[w].bodyOff + s.sbody[g];
+	if(s.btype[body] == CPG_STATIC) return;
+	cache_shape(s, g);
+}
+
+/* cpBBTree.c:638-654: one thread per world re-indexes and traverses. */
+__global__ void k_tree(cpgSet s)
+{
+	int w = blockIdx.x*blockDim.x + threadIdx.x;
+	if(w >= s.nworlds || !s.params[w].active) return;
+	TreeCtx c = make_tree_ctx(&s, w);
+	c.collide = 1;
+	tree_reindex_query(c);
+	c.T->ncand = c.ncand;
+}
+
+/* ------------------------------------------------------------------ */
+/* Narrow phase: cpSpaceStep.c:219-244 */
+
+__device__ bool query_reject(const cpgSet &s, const cpgWorld &W, int a, int b)
+{
+	int ga = W.shapeOff + a, gb = W.shapeOff + b;
+	BB ba = bbnew(s.bbl[ga], s.bbb[ga], s.bbr[ga], s.bbt[ga]);
+	BB bbb = bbnew(s.bbl[gb], s.bbb[gb], s.bbr[gb], s.bbt[gb]);
+	if(!bbintersects(ba, bbb)) return true;
+	int bodyA = s.sbody[ga], bodyB = s.sbody[gb];
+	if(bodyA == bodyB) return true;
+	/* chipmunk_private.h:144-155 */
+	unsigned long long groupA = s.sgroup[ga], groupB = s.sgroup[gb];
+	if((groupA != 0 && groupA == groupB) || (s.scat[ga] & s.smask[gb]) == 0 || (s.scat[gb] & s.smask[ga]) == 0) return true;
+	/* cpSpaceStep.c:204-217: joints with collideBodies off */
+	int gBodyA = W.bodyOff + bodyA;
+	int start = s.partStart[gBodyA], cnt = s.partCount[gBodyA];
+	for(int k = 0; k < cnt; k++) if(s.parts[W.partOff + start + k] == bodyB) return true;
+	return false;
+}
+
+__global__ void k_narrow(cpgSet s)
+{
+	int w = blockIdx.y;
+	if(!s.params[w].active) return;
+	const cpgWorld &W = s.world[w];
+	int n = s.tree[w].ncand;
+	NarrowCtx nc; nc.s = &s; nc.shapeBase = W.shapeOff; nc.bodyBase = W.bodyOff; nc.vertBase = W.vertOff;
+	for(int i = blockIdx.x*blockDim.x + threadIdx.x; i < n; i += gridDim.x*blockDim.x){
+		cpgCand cd = s.cands[W.candOff + i];
+		cpgNarrow out;
+		out.count = 0; out.flip = 0; out.idOut = cd.idIn; out.nx = 0.0; out.ny = 0.0;
+		if(!query_reject(s, W, cd.a, cd.b)){
+			ShapeView A = load_shape(nc, cd.a), B = load_shape(nc, cd.b);
+			NInfo info;
+			int flip;
+			collide(A, B, cd.idIn, info, flip);
+			out.count = info.count > 2 ? 2 : info.count;
+			out.flip = flip;
+			out.idOut = info.id;
+			out.nx = info.n.x; out.ny = info.n.y;
+			for(int k = 0; k < out.count; k++){
+				out.p1x[k] = info.p1[k].x; out.p1y[k] = info.p1[k].y;
+				out.p2x[k] = info.p2[k].x; out.p2y[k] = info.p2[k].y;
+				out.hash[k] = info.hash[k];
+			}
+		}
+		s.narrow[W.candOff + i] = out;
+		if(cd.pair >= 0) s.pairs[W.pairOff + cd.pair].id = out.idOut;
+	}
+}
+
+/* ------------------------------------------------------------------ */
+/* Arbiter cache (cpSpaceStep.c:246-288, cpArbiter.c:356-414) */
+
+__device__ __forceinline__ unsigned long long arb_key(int w, int a, int b)
+{
+	unsigned long long lo = (unsigned long long)(a < b ? a : b), hi = (unsigned long long)(a < b ? b : a);
+	return (((unsigned long long)w << 42) | (lo << 21) | hi) + 2ull;
+}
+
+__device__ __forceinline__ unsigned long long mix64(unsigned long long z)
+{
+	z = (z ^ (z >> 30)) * 0xbf58476d1ce4e5b9ull;
+	z = (z ^ (z >> 27)) * 0x94d049bb133111ebull;
+	return z ^ (z >> 31);
+}
+
+/* Returns the slot of `key`, inserting it (fresh arbiter) if absent; -1 when
+ * the table is full.  Keys are unique per step, so the only concurrent
+ * writers of a slot are inserters of different keys. */
+__device__ int arb_find_or_insert(const cpgSet &s, unsigned long long key, bool &fresh)
+{
+	unsigned mask = (unsigned)s.arbCap - 1;
+	unsigned h0 = (unsigned)mix64(key) & mask;
+	fresh = false;
+	unsigned h = h0;
+	for(int probe = 0; probe < s.arbCap; probe++, h = (h + 1) & mask){
+		unsigned long long k = *(volatile unsigned long long *)&s.keys[h];
+		if(k == key) return (int)h;
+		if(k == CPG_KEY_EMPTY) break;
+	}
+	h = h0;
+	for(int probe = 0; probe < s.arbCap; probe++, h = (h + 1) & mask){
+		unsigned long long k = *(volatile unsigned long long *)&s.keys[h];
+		while(k <= CPG_KEY_TOMB){
+			unsigned long long old = atomicCAS(&s.keys[h], k, key);
+			if(old == k){ fresh = true; return (int)h; }
+			k = old;
+		}
+	}
+	return -1;
+}
+
+__global__ void k_arb_update(cpgSet s)
+{
+	int w = blockIdx.y;
+	const cpgParams &P = s.params[w];
+	if(!P.active) return;
+	const cpgWorld &W = s.world[w];
+	int n = s.tree[w].ncand;
+	for(int i = blockIdx.x*blockDim.x + threadIdx.x; i < n; i += gridDim.x*blockDim.x){
+		const cpgNarrow nr = s.narrow[W.candOff + i];
+		if(nr.count == 0){ s.candArb[W.candOff + i] = -1; continue; }
+		cpgCand cd = s.cands[W.candOff + i];
+		int ia = nr.flip ? cd.b : cd.a, ib = nr.flip ? cd.a : cd.b;
+		bool fresh;
+		int slot = arb_find_or_insert(s, arb_key(w, ia, ib), fresh);
+		if(slot < 0){ s.tree[w].error |= CPG_ERR_ARBS; s.candArb[W.candOff + i] = -1; continue; }
+		cpgArb &arb = s.arbs[slot];
+		if(fresh){
+			/* cpArbiterInit, cpArbiter.c:260-293 */
+			arb.count = 0;
+			arb.state = CPG_ARB_FIRST;
+			arb.stamp = 0;
+			arb.world = w;
+			arb.svx = 0.0; arb.svy = 0.0; arb.e = 0.0; arb.u = 0.0;
+		}
+		int ga = W.shapeOff + ia, gb = W.shapeOff + ib;
+		int bodyA = s.sbody[ga], bodyB = s.sbody[gb];
+		int gBodyA = W.bodyOff + bodyA, gBodyB = W.bodyOff + bodyB;
+		double pax = s.px[gBodyA], pay = s.py[gBodyA], pbx = s.px[gBodyB], pby = s.py[gBodyB];
+		cpgContact nc[2];
+		int oldCount = arb.count;
+		for(int k = 0; k < nr.count; k++){
+			cpgContact &con = nc[k];
+			con.r1x = nr.p1x[k] - pax; con.r1y = nr.p1y[k] - pay;
+			con.r2x = nr.p2x[k] - pbx; con.r2y = nr.p2y[k] - pby;
+			con.hash = nr.hash[k];
+			con.jnAcc = 0.0; con.jtAcc = 0.0;
+			for(int j = 0; j < oldCount; j++){
+				if(con.hash == arb.c[j].hash){
+					con.jnAcc = arb.c[j].jnAcc;
+					con.jtAcc = arb.c[j].jtAcc;
+				}
+			}
+			con.nMass = 0.0; con.tMass = 0.0; con.bounce = 0.0; con.jBias = 0.0; con.bias = 0.0;
+		}
+		for(int k = 0; k < nr.count; k++) arb.c[k] = nc[k];
+		arb.a = ia; arb.b = ib; arb.ba = bodyA; arb.bb = bodyB;
+		arb.count = nr.count;
+		arb.nx = nr.nx; arb.ny = nr.ny;
+		arb.e = s.se[ga]*s.se[gb];
+		arb.u = s.su[ga]*s.su[gb];
+		double svx = s.svx[gb] - s.svx[ga], svy = s.svy[gb] - s.svy[ga];
+		double d = svx*nr.nx + svy*nr.ny;
+		arb.svx = svx - nr.nx*d; arb.svy = svy - nr.ny*d;
+		if(arb.state == CPG_ARB_CACHED) arb.state = CPG_ARB_FIRST;
+		bool sensor = s.ssensor[ga] || s.ssensor[gb];
+		bool infinite = (s.m[gBodyA] == CUDART_INF && s.m[gBodyB] == CUDART_INF);
+		if(arb.state != CPG_ARB_IGNORE && !sensor && !infinite){
+			s.candArb[W.candOff + i] = slot;
+		} else {
+			arb.count = 0;
+			if(arb.state != CPG_ARB_IGNORE) arb.state = CPG_ARB_NORMAL;
+			s.candArb[W.candOff + i] = -1;
+		}
+		arb.stamp = P.stamp;
+	}
+}
+
+/* Order-preserving compaction of the pushed arbiters into the solve list,
+ * then the solver units (arbiters, then joints) with their dynamic bodies. */
+__global__ void k_solve_list(cpgSet s)
+{
+	int w = blockIdx.x;
+	if(!s.params[w].active) return;
+	const cpgWorld &W = s.world[w];
+	int n = s.tree[w].ncand;
+	__shared__ int warpSums[32];
+	__shared__ int base;
+	if(threadIdx.x == 0) base = 0;
+	__syncthreads();
+	int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+	for(int c0 = 0; c0 < n; c0 += blockDim.x){
+		int i = c0 + threadIdx.x;
+		int slot = (i < n) ? s.candArb[W.candOff + i] : -1;
+		bool keep = slot >= 0;
+		unsigned ballot = __ballot_sync(0xffffffffu, keep);
+		int before = __popc(ballot & ((1u << lane) - 1u));
+		if(lane == 0) warpSums[warp] = __popc(ballot);
+		__syncthreads();
+		int off = 0, total = 0;
+		for(int k = 0; k < nwarps; k++){
+			if(k < warp) off += warpSums[k];
+			total += warpSums[k];
+		}
+		if(keep) s.arbList[W.candOff + base + off + before] = slot;
+		__syncthreads();
+		if(threadIdx.x == 0) base += total;
+		__syncthreads();
+	}
+	int narb = base;
+	int nunits = narb + W.ncons;
+	if(threadIdx.x == 0){
+		s.tree[w].narb = narb;
+		s.tree[w].nunits = nunits;
+		if(nunits > W.unitCap) s.tree[w].error |= CPG_ERR_LEVELS;
+	}
+	if(nunits > W.unitCap) return;
+	for(int u = threadIdx.x; u < nunits; u += blockDim.x){
+		int a, b;
+		if(u < narb){
+			const cpgArb &arb = s.arbs[s.arbList[W.candOff + u]];
+			a = arb.ba; b = arb.bb;
+		} else {
+			const cpgJoint &j = s.joints[W.consOff + (u - narb)];
+			a = j.a; b = j.b;
+		}
+		s.unitA[W.unitOff + u] = (s.btype[W.bodyOff + a] == CPG_DYNAMIC) ? a : -1;
+		s.unitB[W.unitOff + u] = (s.btype[W.bodyOff + b] == CPG_DYNAMIC) ? b : -1;
+	}
+}
+
+/* cpSpaceStep.c:292-325 */
+__global__ void k_arb_filter(cpgSet s)
+{
+	int i = blockIdx.x*blockDim.x + threadIdx.x;
+	if(i >= s.arbCap) return;
+	unsigned long long key = s.keys[i];
+	if(key <= CPG_KEY_TOMB) return;
+	cpgArb &arb = s.arbs[i];
+	const cpgParams &P = s.params[arb.world];
+	if(!P.active) return;
+	int bodyOff = s.world[arb.world].bodyOff;
+	unsigned ticks = P.stamp - arb.stamp;
+	if(s.btype[bodyOff + arb.ba] == CPG_STATIC && s.btype[bodyOff + arb.bb] == CPG_STATIC) return;
+	if(ticks >= 1 && arb.state != CPG_ARB_CACHED) arb.state = CPG_ARB_CACHED;
+	if(ticks >= P.persistence){
+		arb.count = 0;
+		s.keys[i] = CPG_KEY_TOMB;
+	} else {
+		atomicAdd(&s.stats[3], 1);
+	}
+}
+
+/* Level schedule of one sweep (arbiters then joints), one thread per
+ * world: level(u) = max over u's dynamic bodies of (level of the body's
+ * previous unit + 1). */
+__global__ void k_schedule(cpgSet s)
+{
+	int w = blockIdx.x*blockDim.x + threadIdx.x;
+	if(w >= s.nworlds || !s.params[w].active) return;
+	const cpgWorld &W = s.world[w];
+	cpgTree &T = s.tree[w];
+	int nunits = T.nunits;
+	if(nunits > W.unitCap){ T.nlevels = 0; return; }
+	int *last = s.last + W.bodyOff;
+	for(int b = 0; b < W.nbodies; b++) last[b] = 0;
+	int *lvl = s.unitLevel + W.unitOff;
+	const int *ua = s.unitA + W.unitOff, *ub = s.unitB + W.unitOff;
+	int nlev = 0;
+	for(int u = 0; u < nunits; u++){
+		int a = ua[u], b = ub[u];
+		int l = 0;
+		if(a >= 0 && last[a] > l) l = last[a];
+		if(b >= 0 && last[b] > l) l = last[b];
+		lvl[u] = l;
+		if(a >= 0) last[a] = l + 1;
+		if(b >= 0) last[b] = l + 1;
+		if(l + 1 > nlev) nlev = l + 1;
+	}
+	int *start = s.levelStart + W.unitOff + w;
+	for(int l = 0; l <= nlev; l++) start[l] = 0;
+	for(int u = 0; u < nunits; u++) start[lvl[u] + 1]++;
+	for(int l = 0; l < nlev; l++) start[l + 1] += start[l];
+	/* stable scatter; start[l] runs as the cursor of level l and is
+	 * shifted back afterwards */
+	int *order = s.unitOrder + W.unitOff;
+	for(int u = 0; u < nunits; u++){
+		int l = lvl[u];
+		order[start[l]++] = u;
+	}
+	for(int l = nlev; l > 0; l--) start[l] = start[l - 1];
+	start[0] = 0;
+	T.nlevels = nlev;
+	if(nlev > T.maxChain) T.maxChain = nlev;
+}
+
+/* ------------------------------------------------------------------ */
+/* Pre-step: cpArbiter.c:416-439, cpPivotJoint.c:24-39, cpPinJoint.c:24-46,
+ * cpSlideJoint.c:24-56 */
+
+__device__ __forceinline__ double k_scalar_body(const cpgSet &s, int g, double rx, double ry, double nx, double ny)
+{
+	double rcn = rx*ny - ry*nx;
+	return s.minv[g] + s.iinv[g]*rcn*rcn;
+}
+
+__global__ void k_prestep(cpgSet s)
+{
+	int w = blockIdx.y;
+	const cpgParams &P = s.params[w];
+	if(!P.active) return;
+	const cpgWorld &W = s.world[w];
+	const cpgTree &T = s.tree[w];
+	int narb = T.narb, nunits = T.nunits;
+	if(nunits > W.unitCap) return;
+	double dt = P.dt;
+	for(int u = blockIdx.x*blockDim.x + threadIdx.x; u < nunits; u += gridDim.x*blockDim.x){
+		if(u < narb){
+			cpgArb &arb = s.arbs[s.arbList[W.candOff + u]];
+			int ga = W.bodyOff + arb.ba, gb = W.bodyOff + arb.bb;
+			double nx = arb.nx, ny = arb.ny;
+			double dx = s.px[gb] - s.px[ga], dy = s.py[gb] - s.py[ga];
+			for(int k = 0; k < arb.count; k++){
+				cpgContact &con = arb.c[k];
+				double kn = k_scalar_body(s, ga, con.r1x, con.r1y, nx, ny) + k_scalar_body(s, gb, con.r2x, con.r2y, nx, ny);
+				con.nMass = 1.0/kn;
+				double kt = k_scalar_body(s, ga, con.r1x, con.r1y, -ny, nx) + k_scalar_body(s, gb, con.r2x, con.r2y, -ny, nx);
+				con.tMass = 1.0/kt;
+				double ddx = (con.r2x - con.r1x) + dx, ddy = (con.r2y - con.r1y) + dy;
+				double dist = ddx*nx + ddy*ny;
+				con.bias = -P.biasCoef*dmin(0.0, dist + P.slop)/dt;
+				con.jBias = 0.0;
+				/* relative_velocity, chipmunk_private.h:172-178 */
+				double v1x = s.vx[ga] + (-con.r1y)*s.w[ga], v1y = s.vy[ga] + con.r1x*s.w[ga];
+				double v2x = s.vx[gb] + (-con.r2y)*s.w[gb], v2y = s.vy[gb] + con.r2x*s.w[gb];
+				double vrx = v2x - v1x, vry = v2y - v1y;
+				con.bounce = (vrx*nx + vry*ny)*arb.e;
+			}
+		} else {
+			cpgJoint &j = s.joints[W.consOff + (u - narb)];
+			double biasCoef = s.jbias[W.consOff + (u - narb)];
+			int ga = W.bodyOff + j.a, gb = W.bodyOff + j.b;
+			/* r = transformVect(body, anchor - cog) */
+			double lax = j.ax - s.cogx[ga], lay = j.ay - s.cogy[ga];
+			double lbx = j.bx - s.cogx[gb], lby = j.by - s.cogy[gb];
+			j.r1x = s.ta[ga]*lax + s.tc[ga]*lay; j.r1y = s.tb[ga]*lax + s.td[ga]*lay;
+			j.r2x = s.ta[gb]*lbx + s.tc[gb]*lby; j.r2y = s.tb[gb]*lbx + s.td[gb]*lby;
+			double deltax = (s.px[gb] + j.r2x) - (s.px[ga] + j.r1x);
+			double deltay = (s.py[gb] + j.r2y) - (s.py[ga] + j.r1y);
+			if(j.kind == CPG_PIVOT){
+				/* k_tensor, chipmunk_private.h:228-262 */
+				double m_sum = s.minv[ga] + s.minv[gb];
+				double k11 = m_sum, k12 = 0.0, k21 = 0.0, k22 = m_sum;
+				double ai = s.iinv[ga];
+				double r1xsq = j.r1x*j.r1x*ai, r1ysq = j.r1y*j.r1y*ai, r1nxy = -j.r1x*j.r1y*ai;
+				k11 += r1ysq; k12 += r1nxy; k21 += r1nxy; k22 += r1xsq;
+				double bi = s.iinv[gb];
+				double r2xsq = j.r2x*j.r2x*bi, r2ysq = j.r2y*j.r2y*bi, r2nxy = -j.r2x*j.r2y*bi;
+				k11 += r2ysq; k12 += r2nxy; k21 += r2nxy; k22 += r2xsq;
+				double det = k11*k22 - k12*k21;
+				double det_inv = 1.0/det;
+				j.k11 = k22*det_inv; j.k12 = -k12*det_inv; j.k21 = -k21*det_inv; j.k22 = k11*det_inv;
+				V2 bias = vclamp(vmul(v2(deltax, deltay), -biasCoef/dt), j.maxBias);
+				j.biasx = bias.x; j.biasy = bias.y;
+			} else if(j.kind == CPG_PIN){
+				double dist = sqrt(deltax*deltax + deltay*deltay);
+				double inv = 1.0/(dist ? dist : CUDART_INF);
+				j.nx = deltax*inv; j.ny = deltay*inv;
+				double kn = k_scalar_body(s, ga, j.r1x, j.r1y, j.nx, j.ny) + k_scalar_body(s, gb, j.r2x, j.r2y, j.nx, j.ny);
+				j.nMass = 1.0/kn;
+				j.bias = dclamp(-biasCoef*(dist - j.dist)/dt, -j.maxBias, j.maxBias);
+			} else {
+				double dist = sqrt(deltax*deltax + deltay*deltay);
+				double pdist = 0.0;
+				if(dist > j.max){
+					pdist = dist - j.max;
+					V2 n = vnormalize(v2(deltax, deltay));
+					j.nx = n.x; j.ny = n.y;
+				} else if(dist < j.min){
+					pdist = j.min - dist;
+					V2 n = vneg(vnormalize(v2(deltax, deltay)));
+					j.nx = n.x; j.ny = n.y;
+				} else {
+					j.nx = 0.0; j.ny = 0.0;
+					j.jnAcc = 0.0;
+				}
+				double kn = k_scalar_body(s, ga, j.r1x, j.r1y, j.nx, j.ny) + k_scalar_body(s, gb, j.r2x, j.r2y, j.nx, j.ny);
+				j.nMass = 1.0/kn;
+				j.bias = dclamp(-biasCoef*pdist/dt, -j.maxBias, j.maxBias);
+			}
+		}
+	}
+}
+
+/* cpBody.c:493-509 */
+__global__ void k_integrate_vel(cpgSet s)
+{
+	int g = blockIdx.x*blockDim.x + threadIdx.x;
+	if(g >= s.totalBodies) return;
+	int w = s.bworld[g];
+	const cpgParams &P = s.params[w];
+	if(!P.active || g - s.world[w].bodyOff >= s.world[w].ndyn) return;
+	if(s.btype[g] == CPG_KINEMATIC) return;
+	double dt = P.dt, damping = P.damping;
+	double minv = s.minv[g];
+	s.vx[g] = s.vx[g]*damping + (P.gx + s.fx[g]*minv)*dt;
+	s.vy[g] = s.vy[g]*damping + (P.gy + s.fy[g]*minv)*dt;
+	s.w[g] = s.w[g]*damping + s.tq[g]*s.iinv[g]*dt;
+	s.fx[g] = 0.0; s.fy[g] = 0.0; s.tq[g] = 0.0;
+}
+
+/* ------------------------------------------------------------------ */
+/* Solver units: cpArbiter.c:441-498, joint applyCachedImpulse/applyImpulse.
+ * Only dynamic bodies are written; the others have zero inverse mass, so
+ * the reference's update leaves them unchanged. */
+
+struct BodyRef {
+	double vx, vy, w, vbx, vby, wb, minv, iinv;
+	int g;
+	bool dyn;
+};
+
+__device__ __forceinline__ BodyRef load_body(const cpgSet &s, int g, bool dyn)
+{
+	BodyRef b;
+	b.g = g; b.dyn = dyn;
+	b.vx = s.vx[g]; b.vy = s.vy[g]; b.w = s.w[g];
+	b.vbx = s.vbx[g]; b.vby = s.vby[g]; b.wb = s.wb[g];
+	b.minv = s.minv[g]; b.iinv = s.iinv[g];
+	return b;
+}
+
+__device__ __forceinline__ void store_body(const cpgSet &s, const BodyRef &b)
+{
+	if(!b.dyn) return;
+	s.vx[b.g] = b.vx; s.vy[b.g] = b.vy; s.w[b.g] = b.w;
+	s.vbx[b.g] = b.vbx; s.vby[b.g] = b.vby; s.wb[b.g] = b.wb;
+}
+
+/* chipmunk_private.h:193-210 */
+__device__ __forceinline__ void apply_impulse(BodyRef &b, double jx, double jy, double rx, double ry)
+{
+	b.vx = b.vx + jx*b.minv;
+	b.vy = b.vy + jy*b.minv;
+	b.w += b.iinv*(rx*jy - ry*jx);
+}
+
+__device__ __forceinline__ void apply_impulses(BodyRef &a, BodyRef &b, double r1x, double r1y, double r2x, double r2y, double jx, double jy)
+{
+	apply_impulse(a, -jx, -jy, r1x, r1y);
+	apply_impulse(b, jx, jy, r2x, r2y);
+}
+
+__device__ __forceinline__ void apply_bias_impulse(BodyRef &b, double jx, double jy, double rx, double ry)
+{
+	b.vbx = b.vbx + jx*b.minv;
+	b.vby = b.vby + jy*b.minv;
+	b.wb += b.iinv*(rx*jy - ry*jx);
+}
+
+__device__ __forceinline__ void arb_apply_cached(const cpgSet &s, cpgArb &arb, int bodyOff, double dt_coef)
+{
+	if(arb.state == CPG_ARB_FIRST) return;
+	int ga = bodyOff + arb.ba, gb = bodyOff + arb.bb;
+	BodyRef A = load_body(s, ga, s.btype[ga] == CPG_DYNAMIC);
+	BodyRef B = load_body(s, gb, s.btype[gb] == CPG_DYNAMIC);
+	double nx = arb.nx, ny = arb.ny;
+	for(int k = 0; k < arb.count; k++){
+		const cpgContact &con = arb.c[k];
+		/* j = rotate(n, (jnAcc, jtAcc)) * dt_coef */
+		double jx = nx*con.jnAcc - ny*con.jtAcc, jy = nx*con.jtAcc + ny*con.jnAcc;
+		apply_impulses(A, B, con.r1x, con.r1y, con.r2x, con.r2y, jx*dt_coef, jy*dt_coef);
+	}
+	store_body(s, A); store_body(s, B);
+}
+
+__device__ __forceinline__ void arb_apply(const cpgSet &s, cpgArb &arb, int bodyOff)
+{
+	int ga = bodyOff + arb.ba, gb = bodyOff + arb.bb;
+	BodyRef A = load_body(s, ga, s.btype[ga] == CPG_DYNAMIC);
+	BodyRef B = load_body(s, gb, s.btype[gb] == CPG_DYNAMIC);
+	double nx = arb.nx, ny = arb.ny;
+	double svx = arb.svx, svy = arb.svy;
+	double friction = arb.u;
+	for(int k = 0; k < arb.count; k++){
+		cpgContact &con = arb.c[k];
+		double nMass = con.nMass;
+		double r1x = con.r1x, r1y = con.r1y, r2x = con.r2x, r2y = con.r2y;
+		double vb1x = A.vbx + (-r1y)*A.wb, vb1y = A.vby + r1x*A.wb;
+		double vb2x = B.vbx + (-r2y)*B.wb, vb2y = B.vby + r2x*B.wb;
+		double v1x = A.vx + (-r1y)*A.w, v1y = A.vy + r1x*A.w;
+		double v2x = B.vx + (-r2y)*B.w, v2y = B.vy + r2x*B.w;
+		double vrx = (v2x - v1x) + svx, vry = (v2y - v1y) + svy;
+		double vbn = (vb2x - vb1x)*nx + (vb2y - vb1y)*ny;
+		double vrn = vrx*nx + vry*ny;
+		double vrt = vrx*(-ny) + vry*nx;
+		double jbn = (con.bias - vbn)*nMass;
+		double jbnOld = con.jBias;
+		con.jBias = dmax(jbnOld + jbn, 0.0);
+		double jn = -(con.bounce + vrn)*nMass;
+		double jnOld = con.jnAcc;
+		con.jnAcc = dmax(jnOld + jn, 0.0);
+		double jtMax = friction*con.jnAcc;
+		double jt = -vrt*con.tMass;
+		double jtOld = con.jtAcc;
+		con.jtAcc = dclamp(jtOld + jt, -jtMax, jtMax);
+		double db = con.jBias - jbnOld;
+		double bx = nx*db, by = ny*db;
+		apply_bias_impulse(A, -bx, -by, r1x, r1y);
+		apply_bias_impulse(B, bx, by, r2x, r2y);
+		double djn = con.jnAcc - jnOld, djt = con.jtAcc - jtOld;
+		double jx = nx*djn - ny*djt, jy = nx*djt + ny*djn;
+		apply_impulses(A, B, r1x, r1y, r2x, r2y, jx, jy);
+	}
+	store_body(s, A); store_body(s, B);
+}
+
+__device__ __forceinline__ void joint_apply_cached(const cpgSet &s, const cpgJoint &j, int bodyOff, double dt_coef)
+{
+	int ga = bodyOff + j.a, gb = bodyOff + j.b;
+	BodyRef A = load_body(s, ga, s.btype[ga] == CPG_DYNAMIC);
+	BodyRef B = load_body(s, gb, s.btype[gb] == CPG_DYNAMIC);
+	if(j.kind == CPG_PIVOT){
+		apply_impulses(A, B, j.r1x, j.r1y, j.r2x, j.r2y, j.jx*dt_coef, j.jy*dt_coef);
+	} else {
+		double s_ = j.jnAcc*dt_coef;
+		apply_impulses(A, B, j.r1x, j.r1y, j.r2x, j.r2y, j.nx*s_, j.ny*s_);
+	}
+	store_body(s, A); store_body(s, B);
+}
+
+__device__ __forceinline__ void joint_apply(const cpgSet &s, cpgJoint &j, int bodyOff, double dt)
+{
+	if(j.kind == CPG_SLIDE && j.nx == 0.0 && j.ny == 0.0) return;
+	int ga = bodyOff + j.a, gb = bodyOff + j.b;
+	BodyRef A = load_body(s, ga, s.btype[ga] == CPG_DYNAMIC);
+	BodyRef B = load_body(s, gb, s.btype[gb] == CPG_DYNAMIC);
+	double v1x = A.vx + (-j.r1y)*A.w, v1y = A.vy + j.r1x*A.w;
+	double v2x = B.vx + (-j.r2y)*B.w, v2y = B.vy + j.r2x*B.w;
+	double vrx = v2x - v1x, vry = v2y - v1y;
+	if(j.kind == CPG_PIVOT){
+		double ex = j.biasx - vrx, ey = j.biasy - vry;
+		double jx = ex*j.k11 + ey*j.k12, jy = ex*j.k21 + ey*j.k22;
+		double oldx = j.jx, oldy = j.jy;
+		V2 acc = vclamp(v2(j.jx + jx, j.jy + jy), j.maxForce*dt);
+		j.jx = acc.x; j.jy = acc.y;
+		apply_impulses(A, B, j.r1x, j.r1y, j.r2x, j.r2y, j.jx - oldx, j.jy - oldy);
+	} else if(j.kind == CPG_PIN){
+		double vrn = vrx*j.nx + vry*j.ny;
+		double jnMax = j.maxForce*dt;
+		double jn = (j.bias - vrn)*j.nMass;
+		double jnOld = j.jnAcc;
+		j.jnAcc = dclamp(jnOld + jn, -jnMax, jnMax);
+		jn = j.jnAcc - jnOld;
+		apply_impulses(A, B, j.r1x, j.r1y, j.r2x, j.r2y, j.nx*jn, j.ny*jn);
+	} else {
+		double vrn = vrx*j.nx + vry*j.ny;
+		double jn = (j.bias - vrn)*j.nMass;
+		double jnOld = j.jnAcc;
+		j.jnAcc = dclamp(jnOld + jn, -j.maxForce*dt, 0.0);
+		jn = j.jnAcc - jnOld;
+		apply_impulses(A, B, j.r1x, j.r1y, j.r2x, j.r2y, j.nx*jn, j.ny*jn);
+	}
+	store_body(s, A); store_body(s, B);
+}
+
+/* Warm start (pass 0) and `iterations` sweeps, level by level; one block
+ * per world.  __syncthreads() orders a level's global-memory writes before
+ * the next level's reads within the block. */
+__global__ void k_solve(cpgSet s)
+{
+	int w = blockIdx.x;
+	const cpgParams &P = s.params[w];
+	if(!P.active) return;
+	const cpgWorld &W = s.world[w];
+	const cpgTree &T = s.tree[w];
+	int narb = T.narb, nunits = T.nunits, nlev = T.nlevels;
+	if(nunits > W.unitCap) return;
+	const int *start = s.levelStart + W.unitOff + w;
+	const int *order = s.unitOrder + W.unitOff;
+	const int *list = s.arbList + W.candOff;
+	for(int pass = 0; pass <= P.iterations; pass++){
+		for(int l = 0; l < nlev; l++){
+			int e = start[l + 1];
+			for(int k = start[l] + threadIdx.x; k < e; k += blockDim.x){
+				int u = order[k];
+				if(u < narb){
+					cpgArb &arb = s.arbs[list[u]];
+					if(pass == 0) arb_apply_cached(s, arb, W.bodyOff, P.dt_coef);
+					else arb_apply(s, arb, W.bodyOff);
+				} else {
+					cpgJoint &j = s.joints[W.consOff + (u - narb)];
+					if(pass == 0) joint_apply_cached(s, j, W.bodyOff, P.dt_coef);
+					else joint_apply(s, j, W.bodyOff, P.dt);
+				}
+			}
+			__syncthreads();
+		}
+	}
+}
+
+/* Aggregate per-world bookkeeping for the host (one block). */
+__global__ void k_stats(cpgSet s)
+{
+	__shared__ int err, pairMax, nodeMax, candMax, levMax, ncand, narb;
+	if(threadIdx.x == 0){ err = 0; pairMax = 0; nodeMax = 0; candMax = 0; levMax = 0; ncand = 0; narb = 0; }
+	__syncthreads();
+	for(int w = threadIdx.x; w < s.nworlds; w += blockDim.x){
+		const cpgTree &T = s.tree[w];
+		const cpgWorld &W = s.world[w];
+		atomicOr(&err, T.error);
+		atomicMax(&pairMax, (int)((long long)T.pairTop*1000/(W.pairCap > 0 ? W.pairCap : 1)));
+		atomicMax(&nodeMax, (int)((long long)T.nodeTop*1000/(W.nodeCap > 0 ? W.nodeCap : 1)));
+		atomicMax(&candMax, (int)((long long)T.ncand*1000/(W.candCap > 0 ? W.candCap : 1)));
+		atomicMax(&levMax, T.nlevels);
+		atomicAdd(&ncand, T.ncand);
+		atomicAdd(&narb, T.narb);
+	}
+	__syncthreads();
+	if(threadIdx.x == 0){
+		s.stats[0] = err; s.stats[1] = pairMax; s.stats[2] = nodeMax; s.stats[4] = ncand;
+		s.stats[5] = narb; s.stats[6] = levMax; s.stats[7] = candMax;
+	}
+}
+
+/* Copy one world's solve list of arbiters into a contiguous buffer. */
+__global__ void k_gather_arbs(cpgSet s, int w, cpgArb *out, int n)
+{
+	int i = blockIdx.x*blockDim.x + threadIdx.x;
+	if(i >= n) return;
+	out[i] = s.arbs[s.arbList[s.world[w].candOff + i]];
+}
+
+/* ------------------------------------------------------------------ */
+/* Launchers */
+
+static inline int blocks_for(int n, int bs) { return (n + bs - 1)/bs > 0 ? (n + bs - 1)/bs : 1; }
+
+static cudaError_t check_launch(const char *what)
+{
+	cudaError_t e = cudaGetLastError();
+	if(e != cudaSuccess) fprintf(stderr, "chipmunk_gb300: launch of %s failed: %s\n", what, cudaGetErrorString(e));
+	return e;
+}
+
+extern "C" int cpg_launch_gather_arbs(const cpgSet *s, int world, cpgArb *out, int n, void *stream)
+{
+	LAUNCH(k_gather_arbs<<<blocks_for(n, 128), 128, 0, (cudaStream_t)stream>>>(*s, world, out, n));
+	return check_launch("k_gather_arbs") == cudaSuccess ? 0 : -1;
+}
+
+extern "C" int cpg_launch_apply_ops(const cpgSet *s, void *stream)
+{
+	cudaStream_t st = (cudaStream_t)stream;
+	LAUNCH(k_apply_ops<<<blocks_for(s->nworlds, 64), 64, 0, st>>>(*s));
+	return check_launch("k_apply_ops") == cudaSuccess ? 0 : -1;
+}
+
+/* `h` is the host copy of the set's sizes (same struct, host values). */
+extern "C" int cpg_launch_step(const cpgSet *s, const cpgSet *h, int mode, void *stream, float *phase_ms)
+{
+	(void)mode;
+	cudaStream_t st = (cudaStream_t)stream;
+	int W = h->nworlds;
+	cudaEvent_t ev[8];
+	bool timing = (phase_ms != NULL);
+	if(timing){
+		for(int i = 0; i < 8; i++) cudaEventCreate(&ev[i]);
+		cudaEventRecord(ev[0], st);
+	}
+	/* grid.x for per-world candidate/unit kernels: one world spans many
+	 * blocks; many worlds get one block row each */
+	int perWorldX = (W == 1) ? 152*4 : 1;
+
+	cudaMemsetAsync(s->stats, 0, 16*sizeof(int), st);
+	LAUNCH(k_reset_prev<<<W, 128, 0, st>>>(*s));
+	LAUNCH(k_integrate_pos<<<blocks_for(h->totalBodies, 128), 128, 0, st>>>(*s));
+	LAUNCH(k_shape_cache<<<blocks_for(h->totalShapes, 128), 128, 0, st>>>(*s));
+	if(timing) cudaEventRecord(ev[1], st);
+	LAUNCH(k_tree<<<blocks_for(W, 32), 32, 0, st>>>(*s));
+	if(timing) cudaEventRecord(ev[2], st);
+	LAUNCH(k_narrow<<<dim3(perWorldX, W), 128, 0, st>>>(*s));
+	if(timing) cudaEventRecord(ev[3], st);
+	LAUNCH(k_arb_update<<<dim3(perWorldX, W), 128, 0, st>>>(*s));
+	LAUNCH(k_solve_list<<<W, 256, 0, st>>>(*s));
+	LAUNCH(k_arb_filter<<<blocks_for(h->arbCap, 256), 256, 0, st>>>(*s));
+	if(timing) cudaEventRecord(ev[4], st);
+	LAUNCH(k_schedule<<<blocks_for(W, 32), 32, 0, st>>>(*s));
+	if(timing) cudaEventRecord(ev[5], st);
+	LAUNCH(k_prestep<<<dim3(perWorldX, W), 128, 0, st>>>(*s));
+	LAUNCH(k_integrate_vel<<<blocks_for(h->totalBodies, 128), 128, 0, st>>>(*s));
+	if(timing) cudaEventRecord(ev[6], st);
+	LAUNCH(k_solve<<<W, 256, 0, st>>>(*s));
+	if(timing) cudaEventRecord(ev[7], st);
+	LAUNCH(k_stats<<<1, 256, 0, st>>>(*s));
+	cudaError_t e = check_launch("step");
+	if(timing){
+		cudaEventSynchronize(ev[7]);
+		for(int i = 0; i < 7; i++) cudaEventElapsedTime(&phase_ms[i], ev[i], ev[i + 1]);
+		for(int i = 0; i < 8; i++) cudaEventDestroy(ev[i]);
+	}
+	return e == cudaSuccess ? 0 : -1;
+}

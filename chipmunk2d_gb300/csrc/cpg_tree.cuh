@@ -1,0 +1,446 @@
+/*
+ * cpg_tree.cuh -- device mirror of the reference's incremental AABB tree
+ * (src/cpBBTree.c) for one world, run by one thread.
+ *
+ * The tree, its per-leaf pair cache and the leaf hash set determine the
+ * order in which cpSpaceStep visits shape pairs, and that order is the
+ * Gauss-Seidel order of the solver.  The GPU path reproduces it exactly by
+ * keeping the same incremental structure on the device: the same insertion
+ * cost function and tie-breaks (cpBBTree.c:325-350), the same pair
+ * threading (:150-205), the same marking traversal (:418-480) and the same
+ * leaf re-index order (hash-bin order, src/cpHashSet.c:87-229).
+ * Recursion is replaced by explicit stacks; node and pair pools are
+ * world-local index ranges with LIFO free lists.
+ *
+ * The traversal only *emits* candidate pairs (cpgCand) in visit order; the
+ * narrow phase then runs on all candidates in parallel, which is exact
+ * because the reference's query callback never modifies the tree.
+ */
+#pragma once
+#include "cpg_device.h"
+#include "cpg_math.cuh"
+
+#define CPG_STACK 512
+
+struct TreeCtx {
+	cpgNode *nodes;
+	cpgPair *pairs;
+	int nodeCap, pairCap;
+	cpgTree *T;
+	int *dbins, *sbins;
+	int dbinCap, sbinCap;
+	/* shape data, world base */
+	const double *bbl, *bbb, *bbr, *bbt;
+	const int *sbody;
+	const unsigned long long *shash;
+	const double *vx, *vy;   /* body velocity, world base */
+	/* candidate output */
+	cpgCand *cands;
+	int candCap;
+	int ncand;
+	int collide;            /* 1: emit candidates; 0: the void query */
+};
+
+__device__ __forceinline__ BB node_bb(const cpgNode &n) { return bbnew(n.l, n.b, n.r, n.t); }
+__device__ __forceinline__ void set_node_bb(cpgNode &n, BB bb) { n.l = bb.l; n.b = bb.b; n.r = bb.r; n.t = bb.t; }
+__device__ __forceinline__ bool is_leaf(const TreeCtx &c, int n) { return c.nodes[n].obj >= 0; }
+
+__device__ __forceinline__ BB shape_bb(const TreeCtx &c, int s) { return bbnew(c.bbl[s], c.bbb[s], c.bbr[s], c.bbt[s]); }
+
+/* cpBBTree.c:82-98: dynamic leaves are fattened by 10% of their size plus
+ * 0.1 s of their body's velocity (both factors are the float literal 0.1f). */
+__device__ BB fatten(BB bb, V2 vel)
+{
+	const double coef = (double)0.1f;
+	double x = (bb.r - bb.l)*coef;
+	double y = (bb.t - bb.b)*coef;
+	V2 v = vmul(vel, (double)0.1f);
+	return bbnew(bb.l + dmin(-x, v.x), bb.b + dmin(-y, v.y), bb.r + dmax(x, v.x), bb.t + dmax(y, v.y));
+}
+
+__device__ BB leaf_fat_bb(const TreeCtx &c, int s)
+{
+	int body = c.sbody[s];
+	return fatten(shape_bb(c, s), v2(c.vx[body], c.vy[body]));
+}
+
+__device__ int node_alloc(TreeCtx &c)
+{
+	cpgTree *T = c.T;
+	if(T->freeNode >= 0){
+		int n = T->freeNode;
+		T->freeNode = c.nodes[n].parent;
+		return n;
+	}
+	if(T->nodeTop >= c.nodeCap){ T->error |= CPG_ERR_NODES; return -1; }
+	return T->nodeTop++;
+}
+
+__device__ __forceinline__ void node_recycle(TreeCtx &c, int n)
+{
+	c.nodes[n].parent = c.T->freeNode;
+	c.T->freeNode = n;
+}
+
+__device__ int pair_alloc(TreeCtx &c)
+{
+	cpgTree *T = c.T;
+	if(T->freePair >= 0){
+		int p = T->freePair;
+		T->freePair = c.pairs[p].aNext;
+		return p;
+	}
+	if(T->pairTop >= c.pairCap){ T->error |= CPG_ERR_PAIRS; return -1; }
+	return T->pairTop++;
+}
+
+__device__ __forceinline__ void pair_recycle(TreeCtx &c, int p)
+{
+	c.pairs[p].aNext = c.T->freePair;
+	c.T->freePair = p;
+	c.T->pairsLive--;
+}
+
+/* cpBBTree.c:150-165 */
+__device__ void thread_unlink(TreeCtx &c, int prev, int leaf, int next)
+{
+	if(next >= 0){
+		cpgPair &np = c.pairs[next];
+		if(np.aLeaf == leaf) np.aPrev = prev; else np.bPrev = prev;
+	}
+	if(prev >= 0){
+		cpgPair &pp = c.pairs[prev];
+		if(pp.aLeaf == leaf) pp.aNext = next; else pp.bNext = next;
+	} else {
+		c.nodes[leaf].pairs = next;
+	}
+}
+
+/* cpBBTree.c:167-186 */
+__device__ void pairs_clear(TreeCtx &c, int leaf)
+{
+	int p = c.nodes[leaf].pairs;
+	c.nodes[leaf].pairs = -1;
+	for(int guard = 0; p >= 0; guard++){
+		if(guard > c.pairCap){ c.T->error |= CPG_ERR_PAIRS; return; }
+		cpgPair pr = c.pairs[p];
+		int next;
+		if(pr.aLeaf == leaf){
+			next = pr.aNext;
+			thread_unlink(c, pr.bPrev, pr.bLeaf, pr.bNext);
+		} else {
+			next = pr.bNext;
+			thread_unlink(c, pr.aPrev, pr.aLeaf, pr.aNext);
+		}
+		pair_recycle(c, p);
+		p = next;
+	}
+}
+
+/* cpBBTree.c:188-205 */
+__device__ void pair_insert(TreeCtx &c, int a, int b)
+{
+	int nextA = c.nodes[a].pairs, nextB = c.nodes[b].pairs;
+	int p = pair_alloc(c);
+	if(p < 0) return;
+	c.T->pairsLive++;
+	cpgPair &pr = c.pairs[p];
+	pr.aPrev = -1; pr.aLeaf = a; pr.aNext = nextA;
+	pr.bPrev = -1; pr.bLeaf = b; pr.bNext = nextB;
+	pr.id = 0;
+	c.nodes[a].pairs = p;
+	c.nodes[b].pairs = p;
+	if(nextA >= 0){
+		cpgPair &q = c.pairs[nextA];
+		if(q.aLeaf == a) q.aPrev = p; else q.bPrev = p;
+	}
+	if(nextB >= 0){
+		cpgPair &q = c.pairs[nextB];
+		if(q.aLeaf == b) q.aPrev = p; else q.bPrev = p;
+	}
+}
+
+/* cpBBTree.c:250-267 */
+__device__ int node_new(TreeCtx &c, int a, int b)
+{
+	int n = node_alloc(c);
+	if(n < 0) return -1;
+	cpgNode &nd = c.nodes[n];
+	nd.obj = -1;
+	set_node_bb(nd, bbmerge(node_bb(c.nodes[a]), node_bb(c.nodes[b])));
+	nd.parent = -1;
+	nd.A = a; c.nodes[a].parent = n;
+	nd.B = b; c.nodes[b].parent = n;
+	nd.pairs = -1; nd.binNext = -1; nd.stamp = 0;
+	return n;
+}
+
+/* cpBBTree.c:281-299 */
+__device__ void node_replace_child(TreeCtx &c, int parent, int child, int value)
+{
+	cpgNode &pn = c.nodes[parent];
+	if(pn.A == child){
+		node_recycle(c, pn.A);
+		pn.A = value; c.nodes[value].parent = parent;
+	} else {
+		node_recycle(c, pn.B);
+		pn.B = value; c.nodes[value].parent = parent;
+	}
+	int guard = 0;
+	for(int n = parent; n >= 0; n = c.nodes[n].parent){
+		if(++guard > c.nodeCap){ c.T->error |= CPG_ERR_NODES; return; }
+		cpgNode &nd = c.nodes[n];
+		set_node_bb(nd, bbmerge(node_bb(c.nodes[nd.A]), node_bb(c.nodes[nd.B])));
+	}
+}
+
+/* cpBBTree.c:325-350, iterative.  The reference merges each visited
+ * node's box on the way back up; a node's own box is only read by its
+ * parent's cost test, which has already run, so merging on the way down
+ * gives the same tree and boxes. */
+__device__ int subtree_insert(TreeCtx &c, int root, int leaf)
+{
+	if(root < 0) return leaf;
+	if(is_leaf(c, root)) return node_new(c, leaf, root);
+	BB lbb = node_bb(c.nodes[leaf]);
+	int cur = root;
+	for(int guard = 0;; guard++){
+		if(guard > c.nodeCap){ c.T->error |= CPG_ERR_NODES; return root; }
+		cpgNode &nd = c.nodes[cur];
+		BB abb = node_bb(c.nodes[nd.A]), bbb = node_bb(c.nodes[nd.B]);
+		double cost_a = bbarea(bbb) + bbmergedarea(abb, lbb);
+		double cost_b = bbarea(abb) + bbmergedarea(bbb, lbb);
+		if(cost_a == cost_b){
+			cost_a = bbproximity(abb, lbb);
+			cost_b = bbproximity(bbb, lbb);
+		}
+		bool goB = (cost_b < cost_a);
+		int child = goB ? nd.B : nd.A;
+		set_node_bb(nd, bbmerge(node_bb(nd), lbb));
+		if(is_leaf(c, child)){
+			int nn = node_new(c, leaf, child);
+			if(nn < 0) return root;
+			if(goB) nd.B = nn; else nd.A = nn;
+			c.nodes[nn].parent = cur;
+			return root;
+		}
+		cur = child;
+	}
+}
+
+/* cpBBTree.c:397-415 */
+__device__ int subtree_remove(TreeCtx &c, int root, int leaf)
+{
+	if(leaf == root) return -1;
+	int parent = c.nodes[leaf].parent;
+	if(parent == root){
+		int other = (c.nodes[root].A == leaf ? c.nodes[root].B : c.nodes[root].A);
+		c.nodes[other].parent = c.nodes[root].parent;
+		node_recycle(c, root);
+		return other;
+	}
+	int other = (c.nodes[parent].A == leaf ? c.nodes[parent].B : c.nodes[parent].A);
+	node_replace_child(c, c.nodes[parent].parent, parent, other);
+	return root;
+}
+
+__device__ __forceinline__ void emit(TreeCtx &c, int a, int b, int pair, unsigned id)
+{
+	if(c.ncand >= c.candCap){ c.T->error |= CPG_ERR_CANDS; return; }
+	cpgCand cd; cd.a = a; cd.b = b; cd.pair = pair; cd.idIn = id;
+	c.cands[c.ncand++] = cd;
+}
+
+/* cpBBTree.c:425-441 (MarkLeafQuery), depth-first A before B. */
+__device__ void mark_leaf_query(TreeCtx &c, int subtree, int leaf, bool left)
+{
+	int stack[CPG_STACK];
+	int sp = 0;
+	stack[sp++] = subtree;
+	BB lbb = node_bb(c.nodes[leaf]);
+	while(sp > 0){
+		int n = stack[--sp];
+		const cpgNode &nd = c.nodes[n];
+		if(!bbintersects(lbb, node_bb(nd))) continue;
+		if(nd.obj >= 0){
+			if(left){
+				pair_insert(c, leaf, n);
+			} else {
+				if(nd.stamp < c.nodes[leaf].stamp) pair_insert(c, n, leaf);
+				if(c.collide) emit(c, c.nodes[leaf].obj, nd.obj, -1, 0u);
+			}
+		} else {
+			if(sp + 2 > CPG_STACK){ c.T->error |= CPG_ERR_NODES; return; }
+			stack[sp++] = nd.B;
+			stack[sp++] = nd.A;
+		}
+	}
+}
+
+/* cpBBTree.c:443-469 */
+__device__ void mark_leaf(TreeCtx &c, int leaf, int staticRoot)
+{
+	if(c.nodes[leaf].stamp == c.T->treeStamp){
+		if(staticRoot >= 0) mark_leaf_query(c, staticRoot, leaf, false);
+		int guard = 0;
+		for(int n = leaf; c.nodes[n].parent >= 0; n = c.nodes[n].parent){
+			if(++guard > c.nodeCap){ c.T->error |= CPG_ERR_NODES; return; }
+			int parent = c.nodes[n].parent;
+			if(n == c.nodes[parent].A){
+				mark_leaf_query(c, c.nodes[parent].B, leaf, true);
+			} else {
+				mark_leaf_query(c, c.nodes[parent].A, leaf, false);
+			}
+		}
+	} else {
+		int p = c.nodes[leaf].pairs;
+		for(int guard = 0; p >= 0; guard++){
+			if(guard > c.pairCap){ c.T->error |= CPG_ERR_PAIRS; return; }
+			const cpgPair &pr = c.pairs[p];
+			if(leaf == pr.bLeaf){
+				if(c.collide) emit(c, c.nodes[pr.aLeaf].obj, c.nodes[leaf].obj, p, pr.id);
+				p = pr.bNext;
+			} else {
+				p = pr.aNext;
+			}
+		}
+	}
+}
+
+/* cpBBTree.c:471-480 */
+__device__ void mark_subtree(TreeCtx &c, int root, int staticRoot)
+{
+	int stack[CPG_STACK];
+	int sp = 0;
+	stack[sp++] = root;
+	while(sp > 0){
+		int n = stack[--sp];
+		const cpgNode &nd = c.nodes[n];
+		if(nd.obj >= 0){
+			mark_leaf(c, n, staticRoot);
+		} else {
+			if(sp + 2 > CPG_STACK){ c.T->error |= CPG_ERR_NODES; return; }
+			stack[sp++] = nd.B;
+			stack[sp++] = nd.A;
+		}
+	}
+}
+
+/* src/prime.h:25-55: the leaf set's table sizes, roughly doubling primes. */
+__device__ __constant__ int cpg_primes[] = {
+	5, 13, 23, 47, 97, 193, 389, 769, 1543, 3079, 6151, 12289, 24593, 49157,
+	98317, 196613, 393241, 786433, 1572869, 3145739, 6291469, 12582917,
+	25165843, 50331653, 100663319, 201326611, 402653189, 805306457, 1610612741, 0,
+};
+
+__device__ unsigned next_prime_dev(unsigned n)
+{
+	int i = 0;
+	while(n > (unsigned)cpg_primes[i] && cpg_primes[i + 1]) i++;
+	return (unsigned)cpg_primes[i];
+}
+
+/* cpHashSet.c:87-114: rehash into next_prime(size + 1) bins, walking the
+ * old bins in order and pushing each leaf on the head of its new chain. */
+__device__ bool leafset_resize(TreeCtx &c, int *bins, int binCap, unsigned *size)
+{
+	unsigned newSize = next_prime_dev(*size + 1);
+	if((int)newSize > binCap){ c.T->error |= CPG_ERR_BINS; return false; }
+	int head = -1, tail = -1;
+	int guard = 0;
+	for(unsigned i = 0; i < *size; i++){
+		int n = bins[i];
+		while(n >= 0){
+			if(++guard > c.nodeCap){ c.T->error |= CPG_ERR_BINS; return false; }
+			int next = c.nodes[n].binNext;
+			if(tail >= 0) c.nodes[tail].binNext = n; else head = n;
+			tail = n;
+			n = next;
+		}
+	}
+	if(tail >= 0) c.nodes[tail].binNext = -1;
+	for(unsigned i = 0; i < newSize; i++) bins[i] = -1;
+	guard = 0;
+	for(int n = head; n >= 0;){
+		if(++guard > c.nodeCap){ c.T->error |= CPG_ERR_BINS; return false; }
+		int next = c.nodes[n].binNext;
+		unsigned idx = (unsigned)(c.shash[c.nodes[n].obj] % newSize);
+		c.nodes[n].binNext = bins[idx];
+		bins[idx] = n;
+		n = next;
+	}
+	*size = newSize;
+	return true;
+}
+
+/* cpBBTree.c:605-616 with LeafAddPairs (:521-537) and the leaf-set insert
+ * (cpHashSet.c:152-176). */
+__device__ void tree_insert(TreeCtx &c, const cpgOp &op)
+{
+	cpgTree *T = c.T;
+	int shape = op.shape;
+	bool isStatic = op.isStatic != 0;
+	int leaf = node_alloc(c);
+	if(leaf < 0) return;
+	cpgNode &nd = c.nodes[leaf];
+	nd.obj = shape;
+	BB bb = bbnew(op.l, op.b, op.r, op.t);
+	set_node_bb(nd, isStatic ? bb : fatten(bb, v2(op.vx, op.vy)));
+	nd.parent = -1; nd.A = -1; nd.B = -1;
+	nd.stamp = 0;
+	nd.pairs = -1;
+	int *bins = isStatic ? c.sbins : c.dbins;
+	unsigned *size = isStatic ? &T->statSize : &T->dynSize;
+	unsigned *entries = isStatic ? &T->statEntries : &T->dynEntries;
+	unsigned idx = (unsigned)(c.shash[shape] % *size);
+	nd.binNext = bins[idx];
+	bins[idx] = leaf;
+	(*entries)++;
+	if(*entries >= *size) leafset_resize(c, bins, isStatic ? c.sbinCap : c.dbinCap, size);
+
+	if(isStatic){
+		T->statRoot = subtree_insert(c, T->statRoot, leaf);
+		c.nodes[leaf].stamp = T->treeStamp;
+		if(T->dynRoot >= 0) mark_leaf_query(c, T->dynRoot, leaf, true);
+	} else {
+		T->dynRoot = subtree_insert(c, T->dynRoot, leaf);
+		c.nodes[leaf].stamp = T->treeStamp;
+		mark_leaf(c, leaf, T->statRoot);
+	}
+	T->treeStamp++;
+}
+
+/* cpBBTree.c:498-517 */
+__device__ void leaf_update(TreeCtx &c, int leaf)
+{
+	cpgTree *T = c.T;
+	int s = c.nodes[leaf].obj;
+	BB bb = shape_bb(c, s);
+	if(!bbcontains(node_bb(c.nodes[leaf]), bb)){
+		set_node_bb(c.nodes[leaf], leaf_fat_bb(c, s));
+		int root = subtree_remove(c, T->dynRoot, leaf);
+		T->dynRoot = subtree_insert(c, root, leaf);
+		pairs_clear(c, leaf);
+		c.nodes[leaf].stamp = T->treeStamp;
+	}
+}
+
+/* cpBBTree.c:638-654 */
+__device__ void tree_reindex_query(TreeCtx &c)
+{
+	cpgTree *T = c.T;
+	if(T->dynRoot < 0) return;
+	int guard = 0;
+	for(unsigned i = 0; i < T->dynSize; i++){
+		int n = c.dbins[i];
+		while(n >= 0){
+			if(++guard > c.nodeCap || T->error){ T->error |= CPG_ERR_BINS; return; }
+			int next = c.nodes[n].binNext;
+			leaf_update(c, n);
+			n = next;
+		}
+	}
+	if(T->error) return;
+	mark_subtree(c, T->dynRoot, T->statRoot);
+	T->treeStamp++;
+}

@@ -271,6 +271,8 @@ cpDataPointer cpBodyGetUserData(const cpBody *body);                 /* cpBody.h
 void cpBodySetUserData(cpBody *body, cpDataPointer userData);        /* cpBody.h:138 */
 void cpBodySetVelocityUpdateFunc(cpBody *body, cpBodyVelocityFunc f);/* cpBody.h:141 */
 void cpBodySetPositionUpdateFunc(cpBody *body, cpBodyPositionFunc f);/* cpBody.h:144 */
+void cpBodyUpdateVelocity(cpBody *body, cpVect gravity, cpFloat damping, cpFloat dt); /* cpBody.h:147 */
+void cpBodyUpdatePosition(cpBody *body, cpFloat dt);                 /* cpBody.h:149 */
 cpVect cpBodyLocalToWorld(const cpBody *body, const cpVect point);   /* cpBody.h:152 */
 cpVect cpBodyWorldToLocal(const cpBody *body, const cpVect point);   /* cpBody.h:154 */
 void cpBodyApplyForceAtWorldPoint(cpBody *body, cpVect force, cpVect point);     /* cpBody.h:157 */

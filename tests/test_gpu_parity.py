@@ -1,0 +1,168 @@
+"""GPU parity: libchipmunk_gb300 (reference-order solver) against the CPU
+oracle, through the C ABI, on the seeded workloads.
+
+Tolerance: 1e-12 relative per step, per state component, scaled by the
+component's magnitude over all bodies (max(|x|, 1)).  The device and the
+host round every +,-,*,/,sqrt identically (no FMA contraction on either
+side); the remaining source of difference is the last bit of sin/cos in
+the body transforms, which this tolerance covers.
+
+"Teacher-forced" runs copy the oracle's body state into the GPU before
+every step, so each comparison measures one step from identical inputs;
+"free" runs compare two independent rollouts.  Arbiter lists (shape pairs,
+contact counts, solve order) must match exactly.
+"""
+import numpy as np
+import pytest
+
+from chipmunk2d_gb300 import Scene
+import known_answers as ka
+
+pytestmark = pytest.mark.gpu
+
+RTOL = 1e-12
+
+
+def rel_err(a, b):
+    """Largest component error, each column scaled by max(|b|, 1)."""
+    if a.size == 0 and b.size == 0:
+        return 0.0
+    scale = np.maximum(np.abs(b).max(axis=0), 1.0)
+    return float((np.abs(a - b) / scale).max())
+
+
+def check_gpu_error(lib):
+    e = lib.cpGpuGetLastError()
+    assert e == 0, lib.cpGpuGetLastErrorString().decode()
+
+
+def compare_step(g, o, step, strict_structure=True):
+    gb, ob = g.bodies(), o.bodies()
+    ga, oa = g.arbiters(), o.arbiters()
+    assert ga.shape == oa.shape, "step %d: %d arbiters on the GPU, %d in the oracle" % (step, len(ga), len(oa))
+    np.testing.assert_array_equal(ga[:, :3], oa[:, :3], err_msg="step %d: arbiter pairs/counts/order" % step)
+    eb = rel_err(gb, ob)
+    ea = rel_err(ga[:, 4:], oa[:, 4:])
+    gj, oj = g.constraints(), o.constraints()
+    ej = rel_err(gj, oj) if len(oj) else 0.0
+    return eb, ea, ej
+
+
+CASES = [
+    ("pyramid", 1, 14, 1 / 60, 300),
+    ("circles", 2, 1500, 1 / 60, 120),
+    ("mixed", 3, 1200, 1 / 60, 80),
+    ("tumble", 4, 300, 1 / 60, 120),
+    ("adjoint", 5, 64, 1 / 120, 120),
+]
+
+
+@pytest.mark.parametrize("name,cfg,size,dt,steps", CASES, ids=[c[0] for c in CASES])
+def test_teacher_forced_per_step(gpu_lib, oracle_lib, name, cfg, size, dt, steps):
+    g = Scene(gpu_lib, cfg, size)
+    o = Scene(oracle_lib, cfg, size)
+    worst = [0.0, 0.0, 0.0]
+    try:
+        for s in range(steps):
+            g.set_bodies(o.bodies())
+            g.step(dt)
+            o.step(dt)
+            check_gpu_error(gpu_lib)
+            errs = compare_step(g, o, s)
+            worst = [max(a, b) for a, b in zip(worst, errs)]
+            assert max(errs) <= RTOL, "step %d: body %.3g arbiter %.3g joint %.3g" % ((s,) + errs)
+    finally:
+        g.free()
+        o.free()
+    print("%s: worst rel err bodies %.3g arbiters %.3g joints %.3g" % (name, *worst))
+
+
+FREE_RUN_DRIFT = 1e-9
+
+
+def test_pyramid_free_run_1000_steps(gpu_lib, oracle_lib):
+    """The full 1000-step pyramid rollout as two independent runs.  The
+    per-step contract (1e-12, teacher-forced tests above) holds; over a free
+    run, last-bit differences between the device's and the host C library's
+    sin/cos compound, so this bounds the accumulated drift instead.  The
+    arbiter lists must still agree exactly at every checkpoint."""
+    g = Scene(gpu_lib, 1, 14)
+    o = Scene(oracle_lib, 1, 14)
+    try:
+        worst = 0.0
+        for s in range(1000):
+            g.step(1 / 60)
+            o.step(1 / 60)
+            if s % 50 == 49 or s < 5:
+                check_gpu_error(gpu_lib)
+                eb, ea, _ = compare_step(g, o, s)
+                worst = max(worst, eb, ea)
+        print("pyramid free-run drift after 1000 steps: %.3g" % worst)
+        assert worst <= FREE_RUN_DRIFT, worst
+        np.testing.assert_allclose(g.impulses(), o.impulses(), rtol=0, atol=1e-7)
+    finally:
+        g.free()
+        o.free()
+
+
+def test_known_answer_time_stepping(gpu_lib):
+    assert ka.time_stepping(gpu_lib) == ka.TIME_STEPPING_EXPECTED
+
+
+def test_known_answer_resting_ball(gpu_lib):
+    y, slop = ka.resting_ball(gpu_lib)
+    assert abs(y - 2.0) <= 1.1 * slop
+
+
+@pytest.mark.parametrize("case", range(len(ka.HULL_CASES)))
+def test_known_answer_convex_hull(gpu_lib, case):
+    pts, count, expected = ka.HULL_CASES[case]
+    ka.check_hull_case(gpu_lib, pts, count, expected)
+
+
+def test_public_getters_and_impulses_match(gpu_lib, oracle_lib):
+    g = Scene(gpu_lib, 4, 200)
+    o = Scene(oracle_lib, 4, 200)
+    try:
+        for s in range(60):
+            g.set_bodies(o.bodies())
+            g.step(1 / 60)
+            o.step(1 / 60)
+        check_gpu_error(gpu_lib)
+        assert rel_err(g.public(), o.public()) <= RTOL
+        assert rel_err(g.impulses(), o.impulses()) <= 1e-10
+    finally:
+        g.free()
+        o.free()
+
+
+def test_batched_worlds_match_single_worlds(gpu_lib, oracle_lib):
+    """Uneven tumble worlds stepped together in one batch match the oracle
+    stepping each world alone."""
+    import ctypes
+    sizes = (ctypes.c_int * 24)()
+    gpu_lib.cpx_batch_sizes(24, 3, ctypes.cast(sizes, ctypes.c_void_p))
+    gs = [Scene(gpu_lib, 4, sizes[i], seed=100 + i) for i in range(24)]
+    os_ = [Scene(oracle_lib, 4, sizes[i], seed=100 + i) for i in range(24)]
+    batch = gpu_lib.cpGpuBatchNew()
+    try:
+        for g in gs:
+            assert gpu_lib.cpGpuBatchAddSpace(batch, g.space) >= 0
+        worst = 0.0
+        for s in range(60):
+            for g, o in zip(gs, os_):
+                g.set_bodies(o.bodies())
+            assert gpu_lib.cpGpuBatchStep(batch, 1 / 60, 1, 0) == 0
+            for o in os_:
+                o.step(1 / 60)
+            check_gpu_error(gpu_lib)
+            for g, o in zip(gs, os_):
+                eb, ea, _ = compare_step(g, o, s)
+                worst = max(worst, eb, ea)
+        assert worst <= RTOL, worst
+    finally:
+        gpu_lib.cpGpuBatchFree(batch)
+        for g in gs:
+            g.free()
+        for o in os_:
+            o.free()
