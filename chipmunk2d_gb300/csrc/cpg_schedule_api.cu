@@ -1,0 +1,77 @@
+/*
+ * cpg_schedule_api.cu -- standalone exact-order sweep scheduler.
+ *
+ * A sequential-impulse sweep applies its units (contacts, joints) one after
+ * the other (src/cpSpaceStep.c:418-427).  Two units that share no dynamic
+ * body commute exactly, so the sweep can run level by level: a unit's level
+ * is 1 + the level of the latest earlier unit touching any of its bodies.
+ * Every body then sees its updates in the original order and the parallel
+ * sweep reproduces the serial one bit for bit.  cpGpuSolveSchedule computes
+ * that schedule for any unit sequence given as two body indices per unit
+ * (negative = no dynamic body), entirely on the device.
+ *
+ * Scratch: the per-body "last level" array and the per-unit levels.
+ */
+#include <cstdio>
+#include <cuda_runtime.h>
+#include "../../include/chipmunk_gb300.h"
+
+/* Level of every unit; one thread walks the sequence (the recurrence is a
+ * scan in unit order).  Then the block counting-sorts units by level. */
+__device__ void schedule_levels(const int *bodyA, const int *bodyB, int nunits, int nbodies,
+                                int *last, int *level, int *levelStart, int *order, int *nlevels)
+{
+	__shared__ int nlev;
+	for(int b = threadIdx.x; b < nbodies; b += blockDim.x) last[b] = 0;
+	__syncthreads();
+	if(threadIdx.x == 0){
+		int maxl = 0;
+		for(int u = 0; u < nunits; u++){
+			int a = bodyA[u], b = bodyB[u];
+			if(a >= nbodies) a = -1;
+			if(b >= nbodies) b = -1;
+			int l = 0;
+			if(a >= 0 && last[a] > l) l = last[a];
+			if(b >= 0 && last[b] > l) l = last[b];
+			level[u] = l;
+			if(a >= 0) last[a] = l + 1;
+			if(b >= 0) last[b] = l + 1;
+			if(l + 1 > maxl) maxl = l + 1;
+		}
+		nlev = maxl;
+		for(int l = 0; l <= maxl; l++) levelStart[l] = 0;
+		for(int u = 0; u < nunits; u++) levelStart[level[u] + 1]++;
+		for(int l = 0; l < maxl; l++) levelStart[l + 1] += levelStart[l];
+		/* stable scatter with levelStart as the cursors, shifted back after */
+		for(int u = 0; u < nunits; u++){
+			int l = level[u];
+			order[levelStart[l]] = u;
+			levelStart[l]++;
+		}
+		for(int l = maxl; l > 0; l--) levelStart[l] = levelStart[l - 1];
+		levelStart[0] = 0;
+		*nlevels = maxl;
+	}
+	__syncthreads();
+}
+
+__global__ void k_schedule_api(const int *bodyA, const int *bodyB, int nunits, int nbodies,
+                               int *last, int *level, int *levelStart, int *order, int *nlevels)
+{
+	schedule_levels(bodyA, bodyB, nunits, nbodies, last, level, levelStart, order, nlevels);
+}
+
+extern "C" int cpGpuSolveSchedule(const int *bodyA, const int *bodyB, int nunits, int nbodies,
+                                  int *levelStart, int *order, int *nlevels, void *stream)
+{
+	if(nunits < 0 || nbodies < 0 || (nunits > 0 && (!bodyA || !bodyB || !levelStart || !order)) || !nlevels)
+		return CP_GPU_ERR_ARGUMENT;
+	cudaStream_t st = (cudaStream_t)stream;
+	int *scratch = NULL;
+	size_t words = (size_t)nbodies + (size_t)nunits + 1;
+	if(cudaMallocAsync((void **)&scratch, words*sizeof(int), st) != cudaSuccess) return CP_GPU_ERR_CUDA;
+	k_schedule_api<<<1, 256, 0, st>>>(bodyA, bodyB, nunits, nbodies, scratch, scratch + nbodies, levelStart, order, nlevels);
+	cudaError_t e = cudaGetLastError();
+	cudaFreeAsync(scratch, st);
+	return e == cudaSuccess ? CP_GPU_OK : CP_GPU_ERR_CUDA;
+}

@@ -440,6 +440,19 @@ int cpGpuBatchAddSpace(cpGpuBatch *batch, cpSpace *space);
  * and replayed. */
 int cpGpuBatchStep(cpGpuBatch *batch, cpFloat dt, int steps, int use_graph);
 
+/* Exact-order parallel schedule of a sequential sweep.  Unit u of the
+ * sweep touches dynamic bodies bodyA[u] and bodyB[u] (a negative index or
+ * one >= nbodies means "no dynamic body").  On return, order[levelStart[l]
+ * .. levelStart[l+1]) lists the units of level l in sweep order, and
+ * *nlevels is the number of levels.  Units of one level share no body, and
+ * running the levels in turn applies every body's updates in the original
+ * sweep order, so the result equals the serial sweep exactly.  All pointers
+ * are device pointers; levelStart holds nunits + 1 ints.  The call is
+ * stream-ordered on `stream` and returns a CP_GPU_* code; its scratch comes
+ * from cudaMallocAsync on that stream. */
+int cpGpuSolveSchedule(const int *bodyA, const int *bodyB, int nunits, int nbodies,
+                       int *levelStart, int *order, int *nlevels, void *stream);
+
 /* Debug/state export used by the parity tests.  Layouts are fixed:
  *   bodies:      18 doubles per dynamic body, in space order:
  *                p.x p.y v.x v.y a w f.x f.y t vb.x vb.y wb tf.a tf.b tf.c tf.d tf.tx tf.ty
