@@ -57,7 +57,7 @@ def check_schedule(a, b, nbodies, start, order, L):
     np.testing.assert_array_equal(order, expect)
     for l in range(L):
         units = order[start[l]:start[l + 1]]
-        touched = [x for u in units for x in (a[u], b[u]) if 0 <= x < nbodies]
+        touched = [x for u in units for x in {a[u], b[u]} if 0 <= x < nbodies]
         assert len(touched) == len(set(touched)), "level %d reuses a body" % l
 
 
