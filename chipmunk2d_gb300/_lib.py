@@ -171,6 +171,7 @@ _GPU_API = {
     "cpGpuGetPhaseTimes": (I, [P, P, I]),
     "cpGpuGetLaunchCount": (ctypes.c_longlong, [I]),
     "cpGpuSolveSchedule": (I, [P, P, I, I, P, P, P, P]),
+    "cpGpuSolveScheduleNoAlloc": (I, [P, P, I, I, P, P, P, P]),
 }
 
 BODY_REC, ARB_REC, CONS_REC = 18, 34, 8

@@ -75,3 +75,53 @@ extern "C" int cpGpuSolveSchedule(const int *bodyA, const int *bodyB, int nunits
 	cudaFreeAsync(scratch, st);
 	return e == cudaSuccess ? CP_GPU_OK : CP_GPU_ERR_CUDA;
 }
+
+/* ------------------------------------------------------------------ */
+/* Allocation-free variant.
+ *
+ * Some callers cannot allocate device memory when they need a schedule: a
+ * frame loop with a hard time budget (cudaMalloc and cudaMallocAsync may
+ * synchronise or take unbounded time), or a host application that owns
+ * every device allocation through its own memory manager and forbids
+ * libraries from allocating after start-up.  cpGpuSolveScheduleNoAlloc
+ * serves them: it runs the same kernel with its scratch in a fixed device
+ * array that is part of the library image, so the call itself allocates
+ * nothing.  The array (8 MiB) exists on every GPU that loads the library
+ * until the process exits.  Calls share it, so calls that overlap on the
+ * GPU (different streams, or different host threads) race; the kernel
+ * clears the part that must start at zero on every call.
+ */
+#define CPG_SCHEDULE_STATIC_MAX_BODIES (1 << 20)
+#define CPG_SCHEDULE_STATIC_MAX_UNITS (1 << 20)
+
+static __device__ __align__(256) int g_schedule_scratch[CPG_SCHEDULE_STATIC_MAX_BODIES + CPG_SCHEDULE_STATIC_MAX_UNITS];
+
+#define CPG_SCHEDULE_MAX_DEVICES 64
+/* Device address of g_schedule_scratch per device; host code cannot use the
+ * symbol's name as a device pointer. */
+static int *g_schedule_scratch_addr[CPG_SCHEDULE_MAX_DEVICES];
+
+extern "C" int cpGpuSolveScheduleNoAlloc(const int *bodyA, const int *bodyB, int nunits, int nbodies,
+                                         int *levelStart, int *order, int *nlevels, void *stream)
+{
+	if(nunits < 0 || nbodies < 0 || (nunits > 0 && (!bodyA || !bodyB || !levelStart || !order)) || !nlevels)
+		return CP_GPU_ERR_ARGUMENT;
+	if(nunits > CPG_SCHEDULE_STATIC_MAX_UNITS || nbodies > CPG_SCHEDULE_STATIC_MAX_BODIES){
+		fprintf(stderr, "cpGpuSolveScheduleNoAlloc: %d units / %d bodies exceed the fixed scratch (%d units, %d bodies)\n",
+			nunits, nbodies, CPG_SCHEDULE_STATIC_MAX_UNITS, CPG_SCHEDULE_STATIC_MAX_BODIES);
+		return CP_GPU_ERR_ARGUMENT;
+	}
+	int dev = 0;
+	if(cudaGetDevice(&dev) != cudaSuccess) return CP_GPU_ERR_CUDA;
+	if(dev < 0 || dev >= CPG_SCHEDULE_MAX_DEVICES) return CP_GPU_ERR_ARGUMENT;
+	if(!g_schedule_scratch_addr[dev]){
+		/* once per device, with that device current */
+		int *ptr = NULL;
+		if(cudaGetSymbolAddress((void **)&ptr, g_schedule_scratch) != cudaSuccess || ptr == NULL) return CP_GPU_ERR_CUDA;
+		g_schedule_scratch_addr[dev] = ptr;
+	}
+	int *scratch = g_schedule_scratch_addr[dev];
+	cudaStream_t st = (cudaStream_t)stream;
+	k_schedule_api<<<1, 256, 0, st>>>(bodyA, bodyB, nunits, nbodies, scratch, scratch + nbodies, levelStart, order, nlevels);
+	return cudaGetLastError() == cudaSuccess ? CP_GPU_OK : CP_GPU_ERR_CUDA;
+}

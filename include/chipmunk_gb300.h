@@ -453,6 +453,21 @@ int cpGpuBatchStep(cpGpuBatch *batch, cpFloat dt, int steps, int use_graph);
 int cpGpuSolveSchedule(const int *bodyA, const int *bodyB, int nunits, int nbodies,
                        int *levelStart, int *order, int *nlevels, void *stream);
 
+/* Same schedule as cpGpuSolveSchedule, for callers that cannot allocate
+ * device memory at the time of the call (a frame loop with a fixed time
+ * budget, or a host application whose memory manager owns every device
+ * allocation).  No counterpart in the reference.  It allocates nothing: its
+ * scratch is a fixed 8 MiB device array inside the library, present on
+ * every GPU that loads the library until exit.  Limits: nunits <= 1048576
+ * and nbodies <= 1048576; larger inputs are rejected with
+ * CP_GPU_ERR_ARGUMENT and a message on stderr.  The first call on a device
+ * looks up the array's device address (make it before any stream capture
+ * on that device).  Calls share the array: calls that overlap on the GPU
+ * race, so serialise them (one stream, or events).  Inputs and outputs are
+ * caller-provided device pointers, as for cpGpuSolveSchedule. */
+int cpGpuSolveScheduleNoAlloc(const int *bodyA, const int *bodyB, int nunits, int nbodies,
+                              int *levelStart, int *order, int *nlevels, void *stream);
+
 /* Debug/state export used by the parity tests.  Layouts are fixed:
  *   bodies:      18 doubles per dynamic body, in space order:
  *                p.x p.y v.x v.y a w f.x f.y t vb.x vb.y wb tf.a tf.b tf.c tf.d tf.tx tf.ty
