@@ -149,6 +149,7 @@ _API = {
     "cpx_dump_arbiters": (I, [P, P, I]),
     "cpx_dump_constraints": (I, [P, P, I]),
     "cpx_set_bodies": (I, [P, P, I]),
+    "cpx_dump_candidates": (I, [P, P, I]),
 }
 
 # GPU-only entry points (libchipmunk_gb300.so)
@@ -167,6 +168,7 @@ _GPU_API = {
     "cpGpuDebugArbiters": (I, [P, P, I]),
     "cpGpuDebugConstraints": (I, [P, P, I]),
     "cpGpuDebugSetBodies": (I, [P, P, I]),
+    "cpGpuDebugCandidates": (I, [P, P, I]),
     "cpGpuSetTiming": (None, [I]),
     "cpGpuGetPhaseTimes": (I, [P, P, I]),
     "cpGpuGetLaunchCount": (ctypes.c_longlong, [I]),
@@ -240,6 +242,13 @@ class Scene:
         out = np.zeros(CONS_REC * cap)
         n = self.lib.cpx_dump_constraints(self.space, out.ctypes.data, cap)
         return out[:CONS_REC * n].reshape(n, CONS_REC)
+
+    def candidates(self, cap=None):
+        cap = cap or max(16 * self.nshapes + 64, 64)
+        out = np.zeros(2 * cap, dtype=np.int32)
+        n = self.lib.cpx_dump_candidates(self.space, out.ctypes.data, cap)
+        pairs = out[:2 * min(n, cap)].reshape(-1, 2)
+        return set(map(tuple, pairs.tolist()))
 
     def public(self):
         out = np.zeros(8 * max(self.nbodies, 1))

@@ -184,6 +184,7 @@ struct cpSpace {
 	int builtBodies, builtShapes, builtCons;
 	int hostStale;                          /* device bodies newer than host */
 	int consStale;                          /* device joint records newer than host */
+	int shapesStale;                        /* device shape boxes newer than host */
 	int bodyDirty, shapeDirty, consDirty;   /* host newer than device */
 	double jointDt;                         /* dt the joint bias terms were made for */
 
@@ -307,6 +308,13 @@ static size_t carve_set(cpgSet *d, char *base, int pass)
 	CARVE(unitA, int, d->totalUnits); CARVE(unitB, int, d->totalUnits);
 	CARVE(unitLevel, int, d->totalUnits); CARVE(unitOrder, int, d->totalUnits);
 	CARVE(levelStart, int, d->totalUnits + W);
+	CARVE(dynShapes, int, NS);
+	CARVE(sortKA, unsigned, NS); CARVE(sortKB, unsigned, NS); CARVE(rkeys, unsigned, NS);
+	CARVE(sapCount, unsigned, NS + 1);
+	CARVE(rsHist, unsigned, 256*(NS/2048 + 2));
+	CARVE(sortVA, int, NS); CARVE(sortVB, int, NS);
+	CARVE(claim, unsigned long long, NB); CARVE(cmask, unsigned long long, NB);
+	CARVE(colorCursor, int, 256);
 	CARVE(stats, int, 16);
 	return total;
 }
@@ -570,6 +578,7 @@ static DevSet *devset_build(cpSpace **spaces, int nspaces)
 		W->unitOff = (int)NU; W->unitCap = W->candCap + sp->ncons;
 		W->opOff = (int)NO; W->nops = sp->nops;
 		W->partOff = (int)NPT;
+		W->dynShapeOff = (int)NS; W->ndynShapes = ndynShapes;
 		NB += nb; NS += sp->nshapes; NV += nverts; NC += sp->ncons;
 		NN += W->nodeCap; NP += W->pairCap; NDB += W->dbinCap; NSB += W->sbinCap;
 		NCD += W->candCap; NU += W->unitCap; NO += sp->nops; NPT += nparts;
@@ -645,13 +654,19 @@ static DevSet *devset_build(cpSpace **spaces, int nspaces)
 		ok &= h2d(d->partCount + W->bodyOff, pcount, sizeof(int)*(size_t)nb);
 		ok &= h2d(d->parts + W->partOff, parts, sizeof(int)*(size_t)np);
 		ok &= h2d(d->ops + W->opOff, sp->ops, sizeof(cpgOp)*(size_t)sp->nops);
+		int *dyns = HALLOC(int, sp->nshapes);
+		int nds = 0;
+		for(int i = 0; i < sp->nshapes; i++) if(body_type_(sp->shapes[i]->body) != CP_BODY_TYPE_STATIC) dyns[nds++] = i;
+		ok &= h2d(d->dynShapes + W->dynShapeOff, dyns, sizeof(int)*(size_t)nds);
 		cudaStreamSynchronize(st);
-		free(bi); free(parts);
+		free(bi); free(parts); free(dyns);
 		sp->builtBodies = world_body_count(sp); sp->builtShapes = sp->nshapes; sp->builtCons = sp->ncons;
 		sp->bodyDirty = sp->shapeDirty = sp->consDirty = 0;
 		sp->jointDt = 0.0;
 	}
 	if(!ok){ devset_free(ds); return NULL; }
+	d->hostNdyn = ds->hworld[0].ndynShapes;
+	d->hostUnitsHint = 0;
 	/* replay the recorded index insertions, then clear the logs */
 	if(cpg_launch_apply_ops(d, st) != 0){ set_error(CP_GPU_ERR_CUDA, "apply_ops launch failed"); devset_free(ds); return NULL; }
 	for(int w = 0; w < nspaces; w++){ ds->hworld[w].nops = 0; spaces[w]->nops = 0; }
@@ -679,6 +694,10 @@ static void check_stats(DevSet *ds)
 	cudaEventSynchronize(ds->statsEvent);
 	ds->statsPending = 0;
 	int err = ds->hstats[0];
+	/* whole-grid solve pays off when one sweep level is wide enough */
+	int units = ds->hstats[5] + (ds->nspaces == 1 ? ds->spaces[0]->ncons : 0);
+	int levels = ds->hstats[6] > 0 ? ds->hstats[6] : 1;
+	ds->d.hostUnitsHint = (units/levels >= 64) ? units : 0;
 	if(err){
 		set_error(CP_GPU_ERR_OVERFLOW, "device table overflow (flags 0x%x): pairs %d/1000, nodes %d/1000, candidates %d/1000",
 			err, ds->hstats[1], ds->hstats[2], ds->hstats[7]);
@@ -715,6 +734,7 @@ static int devset_step(DevSet *ds, const double *dts, cpSpace **only)
 		P->active = 1;
 		sp->hostStale = 1;
 		sp->consStale = 1;
+		sp->shapesStale = 1;
 		sp->snapValid = 0;
 	}
 	cudaStream_t st = lib_stream();
@@ -1228,18 +1248,27 @@ static cpBB shape_cache_(cpShape *s, cpTransform t)
 	return (s->bb = bb);
 }
 
+/* Device caches are current after a step: copy the space's shape boxes
+ * back in one transfer when a box is read. */
+static void shapes_pull_(cpSpace *sp)
+{
+	if(!sp || !sp->dev || !sp->shapesStale) return;
+	DevSet *ds = sp->dev;
+	int n = sp->nshapes, off = ds->hworld[sp->world].shapeOff;
+	double *buf = HALLOC(double, 4*n);
+	d2h(buf, ds->d.bbl + off, sizeof(double)*(size_t)n);
+	d2h(buf + n, ds->d.bbb + off, sizeof(double)*(size_t)n);
+	d2h(buf + 2*n, ds->d.bbr + off, sizeof(double)*(size_t)n);
+	d2h(buf + 3*n, ds->d.bbt + off, sizeof(double)*(size_t)n);
+	cuda_ok(cudaStreamSynchronize(lib_stream()), "download shape boxes");
+	for(int i = 0; i < n; i++) sp->shapes[i]->bb = cpBBNew(buf[i], buf[n + i], buf[2*n + i], buf[3*n + i]);
+	free(buf);
+	sp->shapesStale = 0;
+}
+
 static cpBB shape_bb_now_(cpShape *s)
 {
-	/* device caches are current after a step: read the box back */
-	if(s->space && s->space->dev && s->space->hostStale){
-		cpSpace *sp = s->space;
-		DevSet *ds = sp->dev;
-		int g = ds->hworld[sp->world].shapeOff + (int)s->hashid;
-		double v[4];
-		d2h(&v[0], ds->d.bbl + g, 8); d2h(&v[1], ds->d.bbb + g, 8); d2h(&v[2], ds->d.bbr + g, 8); d2h(&v[3], ds->d.bbt + g, 8);
-		cudaStreamSynchronize(lib_stream());
-		s->bb = cpBBNew(v[0], v[1], v[2], v[3]);
-	}
+	if(s->space) shapes_pull_(s->space);
 	return s->bb;
 }
 
@@ -1813,8 +1842,38 @@ int cpGpuGetPhaseTimes(cpSpace *sp, double *ms, int max)
 	return 7;
 }
 
+/* Shape-id pairs (min, max) of the last step's candidates whose boxes
+ * intersect (the pair set the broadphase handed to the narrow phase). */
+int cpGpuDebugCandidates(cpSpace *sp, int *out, int max)
+{
+	if(!sp->dev) return 0;
+	DevSet *ds = sp->dev;
+	cpgTree T;
+	d2h(&T, ds->d.tree + sp->world, sizeof(cpgTree));
+	cudaStreamSynchronize(lib_stream());
+	int n = T.ncand;
+	cpgCand *c = HALLOC(cpgCand, n);
+	d2h(c, ds->d.cands + ds->hworld[sp->world].candOff, sizeof(cpgCand)*(size_t)n);
+	cudaStreamSynchronize(lib_stream());
+	space_pull(sp);
+	int k = 0;
+	for(int i = 0; i < n; i++){
+		cpShape *a = sp->shapes[c[i].a], *b = sp->shapes[c[i].b];
+		cpBB ba = shape_bb_now_(a), bb = shape_bb_now_(b);
+		if(!cpBBIntersects(ba, bb)) continue;
+		if(k < max){
+			int x = (int)a->hashid, y = (int)b->hashid;
+			out[2*k] = x < y ? x : y; out[2*k + 1] = x < y ? y : x;
+		}
+		k++;
+	}
+	free(c);
+	return k;
+}
+
 /* The shared harness names used by the tests for every implementation. */
 int cpx_dump_bodies(cpSpace *sp, double *out, int max) { return cpGpuDebugBodies(sp, out, max); }
 int cpx_dump_arbiters(cpSpace *sp, double *out, int max) { return cpGpuDebugArbiters(sp, out, max); }
 int cpx_dump_constraints(cpSpace *sp, double *out, int max) { return cpGpuDebugConstraints(sp, out, max); }
 int cpx_set_bodies(cpSpace *sp, const double *in, int count) { return cpGpuDebugSetBodies(sp, in, count); }
+int cpx_dump_candidates(cpSpace *sp, int *out, int max) { return cpGpuDebugCandidates(sp, out, max); }

@@ -50,6 +50,7 @@ typedef struct cpgWorld {
 	int unitOff, unitCap;         /* solver units: arbiters then joints */
 	int opOff, nops;              /* pending index insertions */
 	int partOff;                  /* CSR of non-colliding joint partners */
+	int dynShapeOff, ndynShapes;  /* shapes on non-static bodies (coloured mode) */
 	int pad;
 } cpgWorld;
 
@@ -130,6 +131,8 @@ typedef struct cpgArb {
 	int count, state;
 	unsigned stamp;
 	int world;
+	unsigned gjk;                 /* last GJK feature id of the pair */
+	int pad;
 	double nx, ny, e, u, svx, svy;
 	cpgContact c[2];
 } cpgArb;
@@ -222,6 +225,15 @@ typedef struct cpgSet {
 	int *unitA, *unitB;           /* dynamic bodies touched (-1 none) */
 	int *unitLevel, *unitOrder;
 	int *levelStart;              /* [totalUnits + nworlds] */
+
+	/* coloured mode (single-world sets) */
+	int *dynShapes;               /* [totalShapes] shapes on non-static bodies */
+	unsigned *sortKA, *sortKB, *rkeys, *sapCount, *rsHist;
+	int *sortVA, *sortVB;
+	unsigned long long *claim, *cmask;   /* [totalBodies] */
+	int *colorCursor;             /* [256] */
+	int hostNdyn;                 /* dynamic shapes of world 0 (host value) */
+	int hostUnitsHint;            /* solver units of world 0 last step (host value) */
 
 	/* stats block copied to the host after each step */
 	int *stats;

@@ -34,6 +34,7 @@
 #include "cpg_math.cuh"
 #include "cpg_tree.cuh"
 #include "cpg_narrow.cuh"
+#include "cpg_colored.cuh"
 
 static long long g_launches = 0;
 
@@ -332,6 +333,7 @@ __global__ void k_arb_update(cpgSet s)
 			con.nMass = 0.0; con.tMass = 0.0; con.bounce = 0.0; con.jBias = 0.0; con.bias = 0.0;
 		}
 		for(int k = 0; k < nr.count; k++) arb.c[k] = nc[k];
+		arb.gjk = nr.idOut;
 		arb.a = ia; arb.b = ib; arb.ba = bodyA; arb.bb = bodyB;
 		arb.count = nr.count;
 		arb.nx = nr.nx; arb.ny = nr.ny;
@@ -636,12 +638,9 @@ __device__ __forceinline__ void apply_bias_impulse(BodyRef &b, double jx, double
 	b.wb += b.iinv*(rx*jy - ry*jx);
 }
 
-__device__ __forceinline__ void arb_apply_cached(const cpgSet &s, cpgArb &arb, int bodyOff, double dt_coef)
+__device__ __forceinline__ void arb_apply_cached_ref(const cpgArb &arb, BodyRef &A, BodyRef &B, double dt_coef)
 {
 	if(arb.state == CPG_ARB_FIRST) return;
-	int ga = bodyOff + arb.ba, gb = bodyOff + arb.bb;
-	BodyRef A = load_body(s, ga, s.btype[ga] == CPG_DYNAMIC);
-	BodyRef B = load_body(s, gb, s.btype[gb] == CPG_DYNAMIC);
 	double nx = arb.nx, ny = arb.ny;
 	for(int k = 0; k < arb.count; k++){
 		const cpgContact &con = arb.c[k];
@@ -649,14 +648,10 @@ __device__ __forceinline__ void arb_apply_cached(const cpgSet &s, cpgArb &arb, i
 		double jx = nx*con.jnAcc - ny*con.jtAcc, jy = nx*con.jtAcc + ny*con.jnAcc;
 		apply_impulses(A, B, con.r1x, con.r1y, con.r2x, con.r2y, jx*dt_coef, jy*dt_coef);
 	}
-	store_body(s, A); store_body(s, B);
 }
 
-__device__ __forceinline__ void arb_apply(const cpgSet &s, cpgArb &arb, int bodyOff)
+__device__ __forceinline__ void arb_apply_ref(cpgArb &arb, BodyRef &A, BodyRef &B)
 {
-	int ga = bodyOff + arb.ba, gb = bodyOff + arb.bb;
-	BodyRef A = load_body(s, ga, s.btype[ga] == CPG_DYNAMIC);
-	BodyRef B = load_body(s, gb, s.btype[gb] == CPG_DYNAMIC);
 	double nx = arb.nx, ny = arb.ny;
 	double svx = arb.svx, svy = arb.svy;
 	double friction = arb.u;
@@ -690,29 +685,21 @@ __device__ __forceinline__ void arb_apply(const cpgSet &s, cpgArb &arb, int body
 		double jx = nx*djn - ny*djt, jy = nx*djt + ny*djn;
 		apply_impulses(A, B, r1x, r1y, r2x, r2y, jx, jy);
 	}
-	store_body(s, A); store_body(s, B);
 }
 
-__device__ __forceinline__ void joint_apply_cached(const cpgSet &s, const cpgJoint &j, int bodyOff, double dt_coef)
+__device__ __forceinline__ void joint_apply_cached_ref(const cpgJoint &j, BodyRef &A, BodyRef &B, double dt_coef)
 {
-	int ga = bodyOff + j.a, gb = bodyOff + j.b;
-	BodyRef A = load_body(s, ga, s.btype[ga] == CPG_DYNAMIC);
-	BodyRef B = load_body(s, gb, s.btype[gb] == CPG_DYNAMIC);
 	if(j.kind == CPG_PIVOT){
 		apply_impulses(A, B, j.r1x, j.r1y, j.r2x, j.r2y, j.jx*dt_coef, j.jy*dt_coef);
 	} else {
 		double s_ = j.jnAcc*dt_coef;
 		apply_impulses(A, B, j.r1x, j.r1y, j.r2x, j.r2y, j.nx*s_, j.ny*s_);
 	}
-	store_body(s, A); store_body(s, B);
 }
 
-__device__ __forceinline__ void joint_apply(const cpgSet &s, cpgJoint &j, int bodyOff, double dt)
+__device__ __forceinline__ void joint_apply_ref(cpgJoint &j, BodyRef &A, BodyRef &B, double dt)
 {
 	if(j.kind == CPG_SLIDE && j.nx == 0.0 && j.ny == 0.0) return;
-	int ga = bodyOff + j.a, gb = bodyOff + j.b;
-	BodyRef A = load_body(s, ga, s.btype[ga] == CPG_DYNAMIC);
-	BodyRef B = load_body(s, gb, s.btype[gb] == CPG_DYNAMIC);
 	double v1x = A.vx + (-j.r1y)*A.w, v1y = A.vy + j.r1x*A.w;
 	double v2x = B.vx + (-j.r2y)*B.w, v2y = B.vy + j.r2x*B.w;
 	double vrx = v2x - v1x, vry = v2y - v1y;
@@ -739,6 +726,43 @@ __device__ __forceinline__ void joint_apply(const cpgSet &s, cpgJoint &j, int bo
 		jn = j.jnAcc - jnOld;
 		apply_impulses(A, B, j.r1x, j.r1y, j.r2x, j.r2y, j.nx*jn, j.ny*jn);
 	}
+}
+
+__device__ __forceinline__ void arb_apply_cached(const cpgSet &s, cpgArb &arb, int bodyOff, double dt_coef)
+{
+	if(arb.state == CPG_ARB_FIRST) return;
+	int ga = bodyOff + arb.ba, gb = bodyOff + arb.bb;
+	BodyRef A = load_body(s, ga, s.btype[ga] == CPG_DYNAMIC);
+	BodyRef B = load_body(s, gb, s.btype[gb] == CPG_DYNAMIC);
+	arb_apply_cached_ref(arb, A, B, dt_coef);
+	store_body(s, A); store_body(s, B);
+}
+
+__device__ __forceinline__ void arb_apply(const cpgSet &s, cpgArb &arb, int bodyOff)
+{
+	int ga = bodyOff + arb.ba, gb = bodyOff + arb.bb;
+	BodyRef A = load_body(s, ga, s.btype[ga] == CPG_DYNAMIC);
+	BodyRef B = load_body(s, gb, s.btype[gb] == CPG_DYNAMIC);
+	arb_apply_ref(arb, A, B);
+	store_body(s, A); store_body(s, B);
+}
+
+__device__ __forceinline__ void joint_apply_cached(const cpgSet &s, const cpgJoint &j, int bodyOff, double dt_coef)
+{
+	int ga = bodyOff + j.a, gb = bodyOff + j.b;
+	BodyRef A = load_body(s, ga, s.btype[ga] == CPG_DYNAMIC);
+	BodyRef B = load_body(s, gb, s.btype[gb] == CPG_DYNAMIC);
+	joint_apply_cached_ref(j, A, B, dt_coef);
+	store_body(s, A); store_body(s, B);
+}
+
+__device__ __forceinline__ void joint_apply(const cpgSet &s, cpgJoint &j, int bodyOff, double dt)
+{
+	if(j.kind == CPG_SLIDE && j.nx == 0.0 && j.ny == 0.0) return;
+	int ga = bodyOff + j.a, gb = bodyOff + j.b;
+	BodyRef A = load_body(s, ga, s.btype[ga] == CPG_DYNAMIC);
+	BodyRef B = load_body(s, gb, s.btype[gb] == CPG_DYNAMIC);
+	joint_apply_ref(j, A, B, dt);
 	store_body(s, A); store_body(s, B);
 }
 
@@ -810,6 +834,219 @@ __global__ void k_gather_arbs(cpgSet s, int w, cpgArb *out, int n)
 }
 
 /* ------------------------------------------------------------------ */
+/* Coloured mode (single-world sets): sweep-and-prune, colouring, solve */
+
+__global__ void k_sap_keys(cpgSet s, int w)
+{
+	const cpgWorld &W = s.world[w];
+	int k = blockIdx.x*blockDim.x + threadIdx.x;
+	if(k >= W.ndynShapes) return;
+	int sh = s.dynShapes[W.dynShapeOff + k];
+	int g = W.shapeOff + sh;
+	s.sortKA[k] = float_order_key(__double2float_rd(s.bbl[g]));
+	s.sortVA[k] = sh;
+	s.rkeys[sh] = float_order_key(__double2float_ru(s.bbr[g]));
+}
+
+__device__ int arb_find(const cpgSet &s, unsigned long long key)
+{
+	unsigned mask = (unsigned)s.arbCap - 1;
+	unsigned h = (unsigned)mix64(key) & mask;
+	for(int probe = 0; probe < s.arbCap; probe++, h = (h + 1) & mask){
+		unsigned long long k = s.keys[h];
+		if(k == key) return (int)h;
+		if(k == CPG_KEY_EMPTY) return -1;
+	}
+	return -1;
+}
+
+__global__ void k_sap_count(cpgSet s, int w)
+{
+	const cpgWorld &W = s.world[w];
+	const cpgTree &T = s.tree[w];
+	SapCtx c; c.keys = s.sortKA; c.vals = s.sortVA; c.rkeys = s.rkeys; c.n = W.ndynShapes;
+	for(int i = blockIdx.x*blockDim.x + threadIdx.x; i < c.n; i += gridDim.x*blockDim.x){
+		unsigned cnt = 0;
+		sap_visit(s, W, T, c, i, [&](int, int){ cnt++; });
+		s.sapCount[i] = cnt;
+	}
+	if(blockIdx.x == 0 && threadIdx.x == 0) s.sapCount[c.n] = 0;
+}
+
+__global__ void k_sap_emit(cpgSet s, int w)
+{
+	const cpgWorld &W = s.world[w];
+	cpgTree &T = s.tree[w];
+	SapCtx c; c.keys = s.sortKA; c.vals = s.sortVA; c.rkeys = s.rkeys; c.n = W.ndynShapes;
+	unsigned total = s.sapCount[c.n];
+	if(blockIdx.x == 0 && threadIdx.x == 0){
+		if(total > (unsigned)W.candCap){ T.error |= CPG_ERR_CANDS; T.ncand = W.candCap; }
+		else T.ncand = (int)total;
+	}
+	for(int i = blockIdx.x*blockDim.x + threadIdx.x; i < c.n; i += gridDim.x*blockDim.x){
+		unsigned pos = s.sapCount[i];
+		sap_visit(s, W, T, c, i, [&](int a, int b){
+			if(pos < (unsigned)W.candCap){
+				cpgCand cd;
+				cd.a = a < b ? a : b; cd.b = a < b ? b : a; cd.pair = -1;
+				int slot = arb_find(s, arb_key(w, cd.a, cd.b));
+				cd.idIn = (slot >= 0) ? s.arbs[slot].gjk : 0u;
+				s.cands[W.candOff + pos] = cd;
+			}
+			pos++;
+		});
+	}
+}
+
+__device__ __forceinline__ unsigned long long unit_priority(int u)
+{
+	return (mix64((unsigned long long)u + 0x9e3779b97f4a7c15ull) & 0xffffffff00000000ull) | (unsigned)u;
+}
+
+#define CPG_COLOR_ROUNDS 128
+
+/* Jones-Plassmann rounds with hashed priorities; the lowest colour free on
+ * both bodies.  Then a counting sort of units by colour. */
+__global__ void k_color_coop(cpgSet s, int w)
+{
+	cg::grid_group grid = cg::this_grid();
+	const cpgWorld &W = s.world[w];
+	cpgTree &T = s.tree[w];
+	int n = T.nunits, nb = W.nbodies;
+	int gtid = blockIdx.x*blockDim.x + threadIdx.x, gsz = gridDim.x*blockDim.x;
+	const int *ua = s.unitA + W.unitOff, *ub = s.unitB + W.unitOff;
+	int *color = s.unitLevel + W.unitOff;
+	unsigned long long *claim = s.claim + W.bodyOff, *cmask = s.cmask + W.bodyOff;
+	int *counter = s.colorCursor;   /* [0],[1]: remaining per round parity; [2]: colours */
+	for(int b = gtid; b < nb; b += gsz){ cmask[b] = 0ull; claim[b] = ~0ull; }
+	for(int u = gtid; u < n; u += gsz) color[u] = -1;
+	if(gtid == 0){ counter[0] = 0; counter[1] = 0; counter[2] = 0; }
+	grid.sync();
+	for(int round = 0; round < CPG_COLOR_ROUNDS; round++){
+		for(int u = gtid; u < n; u += gsz){
+			if(color[u] >= 0) continue;
+			unsigned long long p = unit_priority(u);
+			int a = ua[u], b = ub[u];
+			if(a >= 0) atomicMin(&claim[a], p);
+			if(b >= 0) atomicMin(&claim[b], p);
+		}
+		grid.sync();
+		int remaining = 0;
+		for(int u = gtid; u < n; u += gsz){
+			if(color[u] >= 0) continue;
+			unsigned long long p = unit_priority(u);
+			int a = ua[u], b = ub[u];
+			if((a < 0 || __ldcg(&claim[a]) == p) && (b < 0 || __ldcg(&claim[b]) == p)){
+				unsigned long long m = (a >= 0 ? __ldcg(&cmask[a]) : 0ull) | (b >= 0 ? __ldcg(&cmask[b]) : 0ull);
+				int c = (m == ~0ull) ? 64 + round : __ffsll((long long)~m) - 1;
+				color[u] = c;
+				if(c < 64){
+					/* units selected in one round share no body */
+					if(a >= 0) cmask[a] = __ldcg(&cmask[a]) | (1ull << c);
+					if(b >= 0) cmask[b] = __ldcg(&cmask[b]) | (1ull << c);
+				}
+				atomicMax(&counter[2], c + 1);
+			} else {
+				remaining++;
+			}
+		}
+		if(remaining) atomicAdd(&counter[round & 1], remaining);
+		if(gtid == 0) counter[(round + 1) & 1] = 0;
+		grid.sync();
+		int left = __ldcg(&counter[round & 1]);
+		if(left == 0) break;
+		for(int u = gtid; u < n; u += gsz){
+			if(color[u] >= 0) continue;
+			int a = ua[u], b = ub[u];
+			if(a >= 0) claim[a] = ~0ull;
+			if(b >= 0) claim[b] = ~0ull;
+		}
+		grid.sync();
+	}
+	grid.sync();
+	/* counting sort by colour (order within a colour is irrelevant: its
+	 * units share no body) */
+	int ncol = __ldcg(&counter[2]);
+	int *start = s.levelStart + W.unitOff + w;
+	int *order = s.unitOrder + W.unitOff;
+	int *cursor = s.colorCursor + 4;
+	for(int c = gtid; c <= ncol; c += gsz) start[c] = 0;
+	grid.sync();
+	for(int u = gtid; u < n; u += gsz){
+		int c = color[u];
+		if(c < 0) c = ncol - 1;    /* rounds exhausted: the error flag marks it */
+		atomicAdd(&start[c + 1], 1);
+	}
+	grid.sync();
+	if(gtid == 0){
+		int acc = 0;
+		for(int c = 0; c < ncol; c++){ acc += __ldcg(&start[c + 1]); start[c + 1] = acc; }
+		for(int c = 0; c < ncol; c++) cursor[c] = start[c];
+		T.nlevels = ncol;
+		if(ncol > T.maxChain) T.maxChain = ncol;
+	}
+	grid.sync();
+	for(int u = gtid; u < n; u += gsz){
+		int c = color[u];
+		if(c < 0){ c = ncol - 1; T.error |= CPG_ERR_LEVELS; }
+		order[atomicAdd(&cursor[c], 1)] = u;
+	}
+}
+
+/* Body state read past the L1 (other blocks write it between grid syncs). */
+__device__ __forceinline__ BodyRef load_body_cg(const cpgSet &s, int g, bool dyn)
+{
+	BodyRef b;
+	b.g = g; b.dyn = dyn;
+	b.vx = __ldcg(&s.vx[g]); b.vy = __ldcg(&s.vy[g]); b.w = __ldcg(&s.w[g]);
+	b.vbx = __ldcg(&s.vbx[g]); b.vby = __ldcg(&s.vby[g]); b.wb = __ldcg(&s.wb[g]);
+	b.minv = s.minv[g]; b.iinv = s.iinv[g];
+	return b;
+}
+
+/* Levels (ordered mode) or colours (coloured mode) of one large world,
+ * with the whole grid: grid.sync() between levels. */
+__global__ void k_solve_coop(cpgSet s, int w)
+{
+	cg::grid_group grid = cg::this_grid();
+	const cpgParams &P = s.params[w];
+	const cpgWorld &W = s.world[w];
+	const cpgTree &T = s.tree[w];
+	int narb = T.narb, nunits = T.nunits, nlev = T.nlevels;
+	if(nunits > W.unitCap) return;
+	const int *start = s.levelStart + W.unitOff + w;
+	const int *order = s.unitOrder + W.unitOff;
+	const int *list = s.arbList + W.candOff;
+	int gtid = blockIdx.x*blockDim.x + threadIdx.x, gsz = gridDim.x*blockDim.x;
+	for(int pass = 0; pass <= P.iterations; pass++){
+		for(int l = 0; l < nlev; l++){
+			int e = start[l + 1];
+			for(int k = start[l] + gtid; k < e; k += gsz){
+				int u = order[k];
+				if(u < narb){
+					cpgArb &arb = s.arbs[list[u]];
+					int ga = W.bodyOff + arb.ba, gb = W.bodyOff + arb.bb;
+					BodyRef A = load_body_cg(s, ga, s.btype[ga] == CPG_DYNAMIC);
+					BodyRef B = load_body_cg(s, gb, s.btype[gb] == CPG_DYNAMIC);
+					if(pass == 0) arb_apply_cached_ref(arb, A, B, P.dt_coef);
+					else arb_apply_ref(arb, A, B);
+					store_body(s, A); store_body(s, B);
+				} else {
+					cpgJoint &j = s.joints[W.consOff + (u - narb)];
+					int ga = W.bodyOff + j.a, gb = W.bodyOff + j.b;
+					BodyRef A = load_body_cg(s, ga, s.btype[ga] == CPG_DYNAMIC);
+					BodyRef B = load_body_cg(s, gb, s.btype[gb] == CPG_DYNAMIC);
+					if(pass == 0) joint_apply_cached_ref(j, A, B, P.dt_coef);
+					else joint_apply_ref(j, A, B, P.dt);
+					store_body(s, A); store_body(s, B);
+				}
+			}
+			grid.sync();
+		}
+	}
+}
+
+/* ------------------------------------------------------------------ */
 /* Launchers */
 
 static inline int blocks_for(int n, int bs) { return (n + bs - 1)/bs > 0 ? (n + bs - 1)/bs : 1; }
@@ -834,10 +1071,33 @@ extern "C" int cpg_launch_apply_ops(const cpgSet *s, void *stream)
 	return check_launch("k_apply_ops") == cudaSuccess ? 0 : -1;
 }
 
+static int coop_blocks(const void *kernel, int threads)
+{
+	static int sms = 0;
+	if(!sms){ int dev = 0; cudaGetDevice(&dev); cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev); }
+	int per = 0;
+	cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kernel, threads, 0);
+	if(per < 1) per = 1;
+	return sms*per;
+}
+
+static cudaError_t launch_coop(const void *kernel, int threads, cpgSet *s, int w, cudaStream_t st)
+{
+	static int blocks_solve = 0, blocks_color = 0;
+	int *cache = (kernel == (const void *)k_solve_coop) ? &blocks_solve : &blocks_color;
+	if(!*cache) *cache = coop_blocks(kernel, threads);
+	void *args[] = { (void *)s, (void *)&w };
+	g_launches++;
+	return cudaLaunchCooperativeKernel(kernel, dim3(*cache), dim3(threads), args, 0, st);
+}
+
+/* Single-world sets with at least this many solver units use the
+ * cooperative whole-grid solve; smaller ones keep one block. */
+#define CPG_COOP_UNITS 2048
+
 /* `h` is the host copy of the set's sizes (same struct, host values). */
 extern "C" int cpg_launch_step(const cpgSet *s, const cpgSet *h, int mode, void *stream, float *phase_ms)
 {
-	(void)mode;
 	cudaStream_t st = (cudaStream_t)stream;
 	int W = h->nworlds;
 	cudaEvent_t ev[8];
@@ -849,13 +1109,33 @@ extern "C" int cpg_launch_step(const cpgSet *s, const cpgSet *h, int mode, void 
 	/* grid.x for per-world candidate/unit kernels: one world spans many
 	 * blocks; many worlds get one block row each */
 	int perWorldX = (W == 1) ? 152*4 : 1;
+	bool colored = (mode == 1 && W == 1);
+	cpgSet sv = *s;
 
 	cudaMemsetAsync(s->stats, 0, 16*sizeof(int), st);
 	LAUNCH(k_reset_prev<<<W, 128, 0, st>>>(*s));
 	LAUNCH(k_integrate_pos<<<blocks_for(h->totalBodies, 128), 128, 0, st>>>(*s));
 	LAUNCH(k_shape_cache<<<blocks_for(h->totalShapes, 128), 128, 0, st>>>(*s));
 	if(timing) cudaEventRecord(ev[1], st);
-	LAUNCH(k_tree<<<blocks_for(W, 32), 32, 0, st>>>(*s));
+	if(colored){
+		int n = h->hostNdyn;
+		int nb = blocks_for(n, RS_TILE);
+		LAUNCH(k_sap_keys<<<blocks_for(n, 256), 256, 0, st>>>(*s, 0));
+		unsigned *ka = s->sortKA, *kb = s->sortKB;
+		int *va = s->sortVA, *vb = s->sortVB;
+		for(int pass = 0; pass < 4; pass++){
+			LAUNCH(k_rs_hist<<<nb, RS_THREADS, 0, st>>>(ka, n, 8*pass, s->rsHist));
+			LAUNCH(k_scan_excl<<<1, 1024, 0, st>>>(s->rsHist, 256*nb, NULL));
+			LAUNCH(k_rs_scatter<<<nb, RS_THREADS, 0, st>>>(ka, va, kb, vb, n, 8*pass, s->rsHist));
+			unsigned *tk = ka; ka = kb; kb = tk;
+			int *tv = va; va = vb; vb = tv;
+		}
+		LAUNCH(k_sap_count<<<blocks_for(n, 128), 128, 0, st>>>(*s, 0));
+		LAUNCH(k_scan_excl<<<1, 1024, 0, st>>>(s->sapCount, n + 1, NULL));
+		LAUNCH(k_sap_emit<<<blocks_for(n, 128), 128, 0, st>>>(*s, 0));
+	} else {
+		LAUNCH(k_tree<<<blocks_for(W, 32), 32, 0, st>>>(*s));
+	}
 	if(timing) cudaEventRecord(ev[2], st);
 	LAUNCH(k_narrow<<<dim3(perWorldX, W), 128, 0, st>>>(*s));
 	if(timing) cudaEventRecord(ev[3], st);
@@ -863,12 +1143,14 @@ extern "C" int cpg_launch_step(const cpgSet *s, const cpgSet *h, int mode, void 
 	LAUNCH(k_solve_list<<<W, 256, 0, st>>>(*s));
 	LAUNCH(k_arb_filter<<<blocks_for(h->arbCap, 256), 256, 0, st>>>(*s));
 	if(timing) cudaEventRecord(ev[4], st);
-	LAUNCH(k_schedule<<<blocks_for(W, 32), 32, 0, st>>>(*s));
+	if(colored) launch_coop((const void *)k_color_coop, 256, &sv, 0, st);
+	else LAUNCH(k_schedule<<<blocks_for(W, 32), 32, 0, st>>>(*s));
 	if(timing) cudaEventRecord(ev[5], st);
 	LAUNCH(k_prestep<<<dim3(perWorldX, W), 128, 0, st>>>(*s));
 	LAUNCH(k_integrate_vel<<<blocks_for(h->totalBodies, 128), 128, 0, st>>>(*s));
 	if(timing) cudaEventRecord(ev[6], st);
-	LAUNCH(k_solve<<<W, 256, 0, st>>>(*s));
+	if(W == 1 && (colored || h->hostUnitsHint >= CPG_COOP_UNITS)) launch_coop((const void *)k_solve_coop, 256, &sv, 0, st);
+	else LAUNCH(k_solve<<<W, 256, 0, st>>>(*s));
 	if(timing) cudaEventRecord(ev[7], st);
 	LAUNCH(k_stats<<<1, 256, 0, st>>>(*s));
 	cudaError_t e = check_launch("step");

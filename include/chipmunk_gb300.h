@@ -484,6 +484,9 @@ int cpGpuDebugConstraints(cpSpace *space, double *out, int max);
  * constraints' accumulated impulses; used to run one step from a state
  * taken from another implementation. */
 int cpGpuDebugSetBodies(cpSpace *space, const double *in, int count);
+/* Shape-id pairs (min, max) of the last step whose boxes intersect: the
+ * pair set the broadphase handed to the narrow phase (2 ints per pair). */
+int cpGpuDebugCandidates(cpSpace *space, int *out, int max);
 
 /* Per-phase device time of the last step of the space, in milliseconds,
  * measured with CUDA events on the launching stream (0 when timing is off).

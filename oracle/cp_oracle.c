@@ -213,6 +213,9 @@ struct cpSpace {
 	Tree dynTree, statTree;
 	cpTimestamp treeStamp;
 
+	/* pairs that passed the box test in the last step (for broadphase checks) */
+	int *candPairs; int ncand, capcand;
+
 	/* arbiters */
 	cpArbiter *arbs; int narbs, caparbs, freeArb;
 	int *freeList; int nfree, capfree;
@@ -1959,6 +1962,7 @@ void cpSpaceFree(cpSpace *sp)
 	free(sp->nodes); free(sp->pairs);
 	free(sp->dynTree.leaves.bins); free(sp->statTree.leaves.bins);
 	free(sp->arbs); free(sp->freeList); free(sp->amap.keys); free(sp->amap.slot); free(sp->active);
+	free(sp->candPairs);
 	free(sp);
 }
 
@@ -2059,6 +2063,17 @@ static cpBool filter_reject(cpShapeFilter a, cpShapeFilter b)
 	return ((a.group != 0 && a.group == b.group) || (a.categories & b.mask) == 0 || (b.categories & a.mask) == 0);
 }
 
+static void record_candidate(cpSpace *sp, cpShape *a, cpShape *b)
+{
+	if(sp->ncand + 2 > sp->capcand){
+		sp->capcand = sp->capcand ? 2*sp->capcand : 1024;
+		sp->candPairs = (int *)realloc(sp->candPairs, sizeof(int)*(size_t)sp->capcand);
+	}
+	int x = (int)a->hashid, y = (int)b->hashid;
+	sp->candPairs[sp->ncand++] = x < y ? x : y;
+	sp->candPairs[sp->ncand++] = x < y ? y : x;
+}
+
 /* cpSpaceStep.c:204-232 */
 static cpBool query_reject(cpShape *a, cpShape *b)
 {
@@ -2082,6 +2097,7 @@ static void active_push(cpSpace *sp, int slot)
 /* cpSpaceStep.c:235-289 (default handlers: begin/preSolve accept) */
 static cpCollisionID collide_shapes(cpSpace *sp, cpShape *a, cpShape *b, cpCollisionID id)
 {
+	if(cpBBIntersects(a->bb, b->bb)) record_candidate(sp, a, b);
 	if(query_reject(a, b)) return id;
 	CollisionInfo info = collide(a, b, id);
 	if(info.count == 0) return info.id;
@@ -2135,6 +2151,7 @@ void cpSpaceStep(cpSpace *sp, cpFloat dt)
 	sp->nactive = 0;
 
 	sp->locked++;
+	sp->ncand = 0;
 	for(int i = 0; i < sp->ndyn; i++){
 		cpBody *body = sp->dyn[i];
 		body->position_func(body, dt);
@@ -2326,4 +2343,14 @@ int cpx_dump_constraints(cpSpace *sp, double *out, int max)
 		o[3] = c->r1.x; o[4] = c->r1.y; o[5] = c->r2.x; o[6] = c->r2.y;
 	}
 	return sp->ncons;
+}
+
+
+/* Shape-id pairs (min, max) whose boxes intersected in the last step: the
+ * pair set the broadphase handed to the narrow phase. */
+int cpx_dump_candidates(cpSpace *sp, int *out, int max)
+{
+	int n = sp->ncand/2;
+	for(int i = 0; i < n && i < max; i++){ out[2*i] = sp->candPairs[2*i]; out[2*i + 1] = sp->candPairs[2*i + 1]; }
+	return n;
 }
