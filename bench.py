@@ -189,6 +189,121 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
+def batch_sizes(lib, count, seed=3):
+    import ctypes
+    arr = (ctypes.c_int * count)()
+    lib.cpx_batch_sizes(count, seed, ctypes.cast(arr, ctypes.c_void_p))
+    return list(arr)
+
+
+BATCH_WORLDS = 4096
+BATCH_DT = 1 / 60
+
+
+def run_batch(args):
+    """4096 tumble worlds with body counts log-uniform in [8, 512], stepped
+    together (cpGpuBatchStep, reference sweep order in every world)."""
+    import ctypes
+    import torch
+    from chipmunk2d_gb300 import load_gpu_library, Scene
+    lib = load_gpu_library()
+    stream = torch.cuda.Stream()
+    lib.cpGpuSetStream(ctypes.c_void_p(stream.cuda_stream))
+    sizes = batch_sizes(lib, BATCH_WORLDS)
+    t0 = time.perf_counter()
+    scenes = [Scene(lib, 4, sizes[i], seed=1000 + i) for i in range(BATCH_WORLDS)]
+    nb = sum(sc.nbodies for sc in scenes)
+    batch = lib.cpGpuBatchNew()
+    for sc in scenes:
+        lib.cpGpuBatchAddSpace(batch, sc.space)
+    assert lib.cpGpuBatchStep(batch, BATCH_DT, args.warmup, 0) == 0
+    torch.cuda.synchronize()
+    build_s = time.perf_counter() - t0
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+    lib.cpGpuGetLaunchCount(1)
+    clocks = ClockSampler(0)
+    clocks.start()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    for i in range(args.steps):
+        with torch.cuda.stream(stream):
+            flush.fill_(float(i))
+            ev[i][0].record(stream)
+        lib.cpGpuBatchStep(batch, BATCH_DT, 1, 0)
+        with torch.cuda.stream(stream):
+            ev[i][1].record(stream)
+    torch.cuda.synchronize()
+    launches = lib.cpGpuGetLaunchCount(1)
+    clk = clocks.stop()
+    if lib.cpGpuGetLastError():
+        raise RuntimeError(lib.cpGpuGetLastErrorString().decode())
+    total_s = sum(a.elapsed_time(b) for a, b in ev) / 1000.0
+    world_steps = BATCH_WORLDS * args.steps / total_s
+    lib.cpGpuSetTiming(1)
+    phase = np.zeros(8)
+    buf = np.zeros(8)
+    for _ in range(5):
+        lib.cpGpuBatchStep(batch, BATCH_DT, 1, 0)
+        lib.cpGpuGetPhaseTimes(scenes[0].space, buf.ctypes.data, 8)
+        phase += buf
+    lib.cpGpuSetTiming(0)
+    phase /= 5
+    lib.cpGpuBatchFree(batch)
+    for sc in scenes:
+        sc.free()
+
+    # the same worlds stepped one cpSpaceStep at a time (plain GPU step), on a sample
+    loop_n = 64
+    loop = [Scene(lib, 4, sizes[i], seed=1000 + i) for i in range(loop_n)]
+    for sc in loop:
+        sc.step(BATCH_DT, args.warmup)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    loop_steps = 5
+    for _ in range(loop_steps):
+        for sc in loop:
+            lib.cpSpaceStep(sc.space, BATCH_DT)
+    torch.cuda.synchronize()
+    loop_ws = loop_n * loop_steps / (time.perf_counter() - t0)
+    for sc in loop:
+        sc.free()
+
+    # CPU restatement, one core, on a sample of worlds
+    from chipmunk2d_gb300 import Scene as S2
+    orc = oracle_lib()
+    cpu_n = 128
+    cw = [S2(orc, 4, sizes[i], seed=1000 + i) for i in range(cpu_n)]
+    for sc in cw:
+        sc.step(BATCH_DT, args.warmup)
+    t0 = time.perf_counter()
+    cpu_steps = 5
+    for _ in range(cpu_steps):
+        for sc in cw:
+            sc.step(BATCH_DT, 1)
+    cpu_ws = cpu_n * cpu_steps / (time.perf_counter() - t0)
+    for sc in cw:
+        sc.free()
+
+    names = ["integrate+cache", "broadphase tree", "narrowphase", "arbiters", "schedule", "prestep+velocity", "solve"]
+    line = {
+        "metric": "world-steps/s", "value": world_steps, "unit": "world-steps/s", "n_gpus": 1,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000 * total_s / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": "batch", "worlds": BATCH_WORLDS, "bodies": nb,
+                   "description": "4096 tumble worlds, bodies log-uniform in [8,512], 10 it, dt 1/60, seed 3",
+                   "solver": "ordered (reference sweep order per world)", "build_s": build_s,
+                   "l2": "flushed between timed steps (256 MB fill, untimed)"},
+        "body_steps_per_s": nb * args.steps / total_s,
+        "looped_plain_gpu_world_steps_per_s": loop_ws,
+        "batched_over_looped": world_steps / loop_ws,
+        "phase_ms": dict(zip(names, [round(float(x), 4) for x in phase[:7]])),
+        "gpu_launches": int(launches),
+        "clocks": clk,
+        "cpu_baseline": {"value": cpu_ws, "unit": "world-steps/s", "cores": 1, "kind": "port",
+                         "sample": "%d worlds x %d steps" % (cpu_n, cpu_steps)},
+    }
+    print(json.dumps(line), flush=True)
+
+
 def run_ours(args):
     import ctypes
     import torch
@@ -237,6 +352,11 @@ def run_ours(args):
             ev[i][1].record(stream)
     torch.cuda.synchronize()
     launches = lib.cpGpuGetLaunchCount(1)
+    if args.profile:
+        # profiling runs (ncu) stop after the device-timed steps
+        clocks.stop()
+        sc.free()
+        return
     step_ms = [a.elapsed_time(b) for a, b in ev]
     total_s = sum(step_ms) / 1000.0
     if dist:
@@ -262,6 +382,9 @@ def run_ours(args):
         phase += buf[:7]
     lib.cpGpuSetTiming(0)
     phase /= nph
+    st = np.zeros(8, dtype=np.int32)
+    lib.cpGpuGetStepStats(sc.space, st.ctypes.data, 8)
+    sweep_levels = int(st[6])
     sc.free()
 
     # ---- end-to-end run through the public C API ----
@@ -321,6 +444,7 @@ def run_ours(args):
                      "unit": "GB/s", "frac": achieved / peak, "peak_kind": peak_kind,
                      "traffic": traffic, "algorithmic_bytes_per_launch": algo},
         "phase_ms": dict(zip(names, [round(float(x), 4) for x in phase])),
+        "sweep_levels_final": sweep_levels,
         "gpu_launches": int(launches),
         "clocks": clk,
         "cpu_baseline": {"value": cpu_v, "unit": "body-steps/s", "cores": 1, "kind": "port",
@@ -339,13 +463,17 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--mode", default="ordered", choices=["ordered", "colored"])
-    ap.add_argument("--workload", default="circles", choices=sorted(WORKLOADS))
+    ap.add_argument("--workload", default="circles", choices=sorted(WORKLOADS) + ["batch"])
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
+    ap.add_argument("--profile", action="store_true",
+                    help="run only the warm-up and device-timed steps (for ncu captures)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
     if args.impl == "reference":
         run_reference(args)
+    elif args.workload == "batch":
+        run_batch(args)
     else:
         run_ours(args)
 

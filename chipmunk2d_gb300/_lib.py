@@ -171,6 +171,7 @@ _GPU_API = {
     "cpGpuDebugCandidates": (I, [P, P, I]),
     "cpGpuSetTiming": (None, [I]),
     "cpGpuGetPhaseTimes": (I, [P, P, I]),
+    "cpGpuGetStepStats": (I, [P, P, I]),
     "cpGpuGetLaunchCount": (ctypes.c_longlong, [I]),
     "cpGpuSolveSchedule": (I, [P, P, I, I, P, P, P, P]),
     "cpGpuSolveScheduleNoAlloc": (I, [P, P, I, I, P, P, P, P]),

@@ -305,9 +305,12 @@ static size_t carve_set(cpgSet *d, char *base, int pass)
 	CARVE(prevCount, int, W);
 	CARVE(keys, unsigned long long, d->arbCap); CARVE(arbs, cpgArb, d->arbCap);
 	CARVE(joints, cpgJoint, NC); CARVE(jbias, double, NC);
-	CARVE(unitA, int, d->totalUnits); CARVE(unitB, int, d->totalUnits);
+	CARVE(unitA, int, d->totalUnits); CARVE(unitB, int, d->totalUnits); CARVE(unitKey, int, d->totalUnits);
+	CARVE(worldOrder, int, W);
 	CARVE(unitLevel, int, d->totalUnits); CARVE(unitOrder, int, d->totalUnits);
 	CARVE(levelStart, int, d->totalUnits + W);
+	CARVE(rows, cpgRow, d->totalUnits);
+	CARVE(pbody, double, 8*NB);
 	CARVE(dynShapes, int, NS);
 	CARVE(sortKA, unsigned, NS); CARVE(sortKB, unsigned, NS); CARVE(rkeys, unsigned, NS);
 	CARVE(sapCount, unsigned, NS + 1);
@@ -315,6 +318,8 @@ static size_t carve_set(cpgSet *d, char *base, int pass)
 	CARVE(sortVA, int, NS); CARVE(sortVB, int, NS);
 	CARVE(claim, unsigned long long, NB); CARVE(cmask, unsigned long long, NB);
 	CARVE(colorCursor, int, 256);
+	CARVE(sapBB, double, 4*NS);
+	CARVE(sapStats, double, 8);
 	CARVE(stats, int, 16);
 	return total;
 }
@@ -667,6 +672,27 @@ static DevSet *devset_build(cpSpace **spaces, int nspaces)
 	if(!ok){ devset_free(ds); return NULL; }
 	d->hostNdyn = ds->hworld[0].ndynShapes;
 	d->hostUnitsHint = 0;
+	d->hostMaxBodies = 0;
+	d->hostMaxNodes = 0;
+	for(int w = 0; w < nspaces; w++){
+		if(ds->hworld[w].nbodies > d->hostMaxBodies) d->hostMaxBodies = ds->hworld[w].nbodies;
+		if(ds->hworld[w].nodeCap > d->hostMaxNodes) d->hostMaxNodes = ds->hworld[w].nodeCap;
+	}
+	/* worlds by decreasing shape count: the serial tree step of the largest
+	 * worlds starts first */
+	{
+		int *ord = HALLOC(int, nspaces);
+		for(int w = 0; w < nspaces; w++) ord[w] = w;
+		/* insertion sort by key, stable, descending (counting sort would also do) */
+		for(int i = 1; i < nspaces; i++){
+			int x = ord[i], k = i;
+			while(k > 0 && ds->hworld[ord[k - 1]].nshapes < ds->hworld[x].nshapes){ ord[k] = ord[k - 1]; k--; }
+			ord[k] = x;
+		}
+		h2d(d->worldOrder, ord, sizeof(int)*(size_t)nspaces);
+		cudaStreamSynchronize(lib_stream());
+		free(ord);
+	}
 	/* replay the recorded index insertions, then clear the logs */
 	if(cpg_launch_apply_ops(d, st) != 0){ set_error(CP_GPU_ERR_CUDA, "apply_ops launch failed"); devset_free(ds); return NULL; }
 	for(int w = 0; w < nspaces; w++){ ds->hworld[w].nops = 0; spaces[w]->nops = 0; }
@@ -1834,6 +1860,19 @@ int cpGpuDebugConstraints(cpSpace *sp, double *out, int max)
 		o[3] = j->r1x; o[4] = j->r1y; o[5] = j->r2x; o[6] = j->r2y;
 	}
 	return sp->ncons;
+}
+
+int cpGpuGetStepStats(cpSpace *sp, int *out, int max)
+{
+	if(!sp || !sp->dev || max < 1) return 0;
+	DevSet *ds = sp->dev;
+	cudaStreamSynchronize(lib_stream());
+	/* the stats block of the last step: error flags, pair/node use (per
+	 * mille of capacity), live arbiters, candidates, solved arbiters,
+	 * sweep levels or colours, candidate use (per mille) */
+	int n = max < 8 ? max : 8;
+	for(int i = 0; i < n; i++) out[i] = ds->hstats[i];
+	return n;
 }
 
 int cpGpuGetPhaseTimes(cpSpace *sp, double *ms, int max)

@@ -132,6 +132,7 @@ struct SapCtx {
 	const unsigned *keys;     /* sorted left-edge keys */
 	const int *vals;          /* sorted shape indices (world-local) */
 	const unsigned *rkeys;    /* right-edge keys by shape */
+	const double4 *sbb;       /* boxes in sorted order */
 	int n;                    /* dynamic shapes */
 };
 
@@ -165,7 +166,7 @@ __device__ void sap_visit(const cpgSet &s, const cpgWorld &W, const cpgTree &T, 
 	}
 	unsigned rk = c.rkeys[sa];
 	for(int j = i + 1; j < c.n && c.keys[j] <= rk; j++){
-		int sb = c.vals[j];
-		if(bbintersects(ba, gshape_bb(s, W.shapeOff + sb))) f(sa, sb);
+		double4 bj = c.sbb[j];
+		if(bbintersects(ba, bbnew(bj.x, bj.y, bj.z, bj.w))) f(sa, c.vals[j]);
 	}
 }

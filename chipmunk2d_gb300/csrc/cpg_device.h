@@ -150,6 +150,29 @@ typedef struct cpgJoint {
 	double nx, ny, nMass, jnAcc, bias;  /* pin/slide */
 } cpgJoint;
 
+/* Solver rows: one per unit, stored in schedule order so that the threads
+ * of one level read consecutive rows.  Built by the pre-step, consumed by
+ * the warm start and the iterations, written back to the arbiters and
+ * joints at the end of the solve. */
+typedef struct cpgRowContact {
+	double r1x, r1y, r2x, r2y;
+	double nMass, tMass, bounce, bias;
+	double jnAcc, jtAcc, jBias, pad;
+} cpgRowContact;
+
+typedef struct cpgRow {
+	int a, b;                     /* world-local bodies */
+	int kind;                     /* 0: arbiter, else CPG_PIVOT/PIN/SLIDE */
+	int count;                    /* arbiter contacts */
+	int src;                      /* arbiter slot, or joint index in the world */
+	int flags;                    /* 1: first step (no warm start); 2/4: body a/b dynamic */
+	union {
+		struct { double nx, ny, u, svx, svy, pad; cpgRowContact c[2]; } arb;
+		struct { double r1x, r1y, r2x, r2y, k11, k12, k21, k22, jx, jy, biasx, biasy;
+		         double nx, ny, nMass, jnAcc, bias, maxForce; } jnt;
+	};
+} cpgRow;
+
 /* Pending tree insertion recorded by cpSpaceAddShape, with the shape's
  * box and its body's velocity as they were at that call (the reference
  * builds the leaf's fattened box immediately, cpBBTree.c:605-616). */
@@ -221,8 +244,15 @@ typedef struct cpgSet {
 	cpgJoint *joints;
 	double *jbias;                /* 1 - pow(errorBias, dt), host-computed */
 
+	/* solver rows [totalUnits] and packed body state [totalBodies*8]:
+	 * vx vy w vbx vby wb minv iinv */
+	cpgRow *rows;
+	double *pbody;
+
 	/* schedule [totalUnits] */
 	int *unitA, *unitB;           /* dynamic bodies touched (-1 none) */
+	int *unitKey;                 /* coloured mode: deterministic unit id */
+	int *worldOrder;              /* [nworlds] worlds by decreasing size */
 	int *unitLevel, *unitOrder;
 	int *levelStart;              /* [totalUnits + nworlds] */
 
@@ -232,8 +262,12 @@ typedef struct cpgSet {
 	int *sortVA, *sortVB;
 	unsigned long long *claim, *cmask;   /* [totalBodies] */
 	int *colorCursor;             /* [256] */
+	double *sapBB;                /* [4*totalShapes] boxes in sweep order */
+	double *sapStats;             /* [8] axis statistics */
 	int hostNdyn;                 /* dynamic shapes of world 0 (host value) */
 	int hostUnitsHint;            /* solver units of world 0 last step (host value) */
+	int hostMaxBodies;            /* largest world (host value) */
+	int hostMaxNodes;             /* largest world's node pool (host value) */
 
 	/* stats block copied to the host after each step */
 	int *stats;

@@ -183,15 +183,35 @@ __global__ void k_shape_cache(cpgSet s)
 	cache_shape(s, g);
 }
 
-/* cpBBTree.c:638-654: one thread per world re-indexes and traverses. */
-__global__ void k_tree(cpgSet s)
+/* cpBBTree.c:638-654: one block per world (largest worlds first); its
+ * threads stage the world's node pool in shared memory when it fits, and
+ * thread 0 re-indexes and traverses. */
+extern __shared__ cpgNode snodes[];
+
+__global__ void k_tree(cpgSet s, int stagedNodes)
 {
-	int w = blockIdx.x*blockDim.x + threadIdx.x;
-	if(w >= s.nworlds || !s.params[w].active) return;
-	TreeCtx c = make_tree_ctx(&s, w);
-	c.collide = 1;
-	tree_reindex_query(c);
-	c.T->ncand = c.ncand;
+	int w = s.worldOrder[blockIdx.x];
+	if(!s.params[w].active) return;
+	const cpgWorld &W = s.world[w];
+	int nn = s.tree[w].nodeTop;
+	bool staged = nn <= stagedNodes;
+	cpgNode *gnodes = s.nodes + W.nodeOff;
+	if(staged){
+		for(int i = threadIdx.x; i < nn; i += blockDim.x) snodes[i] = gnodes[i];
+		__syncthreads();
+	}
+	if(threadIdx.x == 0){
+		TreeCtx c = make_tree_ctx(&s, w);
+		if(staged){ c.nodes = snodes; c.nodeCap = stagedNodes < W.nodeCap ? stagedNodes : W.nodeCap; }
+		c.collide = 1;
+		tree_reindex_query(c);
+		c.T->ncand = c.ncand;
+	}
+	__syncthreads();
+	if(staged){
+		nn = s.tree[w].nodeTop;
+		for(int i = threadIdx.x; i < nn; i += blockDim.x) gnodes[i] = snodes[i];
+	}
 }
 
 /* ------------------------------------------------------------------ */
@@ -409,6 +429,53 @@ __global__ void k_solve_list(cpgSet s)
 	}
 }
 
+/* Coloured mode: the solve list in any order (one colour's units commute),
+ * compacted with warp-aggregated atomics, then the joints' units. */
+__global__ void k_solve_list_any(cpgSet s, int w)
+{
+	const cpgWorld &W = s.world[w];
+	cpgTree &T = s.tree[w];
+	int n = T.ncand;
+	int lane = threadIdx.x & 31;
+	for(int i0 = blockIdx.x*blockDim.x; i0 < n; i0 += gridDim.x*blockDim.x){
+		int i = i0 + threadIdx.x;
+		int slot = (i < n) ? s.candArb[W.candOff + i] : -1;
+		bool keep = slot >= 0;
+		unsigned ballot = __ballot_sync(0xffffffffu, keep);
+		int base = 0;
+		if(lane == 0 && ballot) base = atomicAdd(&T.narb, __popc(ballot));
+		base = __shfl_sync(0xffffffffu, base, 0);
+		if(keep){
+			int pos = base + __popc(ballot & ((1u << lane) - 1u));
+			if(pos < W.unitCap){
+				s.arbList[W.candOff + pos] = slot;
+				s.unitKey[W.unitOff + pos] = i;
+				const cpgArb &arb = s.arbs[slot];
+				s.unitA[W.unitOff + pos] = (s.btype[W.bodyOff + arb.ba] == CPG_DYNAMIC) ? arb.ba : -1;
+				s.unitB[W.unitOff + pos] = (s.btype[W.bodyOff + arb.bb] == CPG_DYNAMIC) ? arb.bb : -1;
+			}
+		}
+	}
+}
+
+__global__ void k_units_joints(cpgSet s, int w)
+{
+	const cpgWorld &W = s.world[w];
+	cpgTree &T = s.tree[w];
+	int narb = T.narb, nunits = narb + W.ncons;
+	if(blockIdx.x == 0 && threadIdx.x == 0){
+		T.nunits = nunits;
+		if(nunits > W.unitCap) T.error |= CPG_ERR_LEVELS;
+	}
+	if(nunits > W.unitCap) return;
+	for(int j = blockIdx.x*blockDim.x + threadIdx.x; j < W.ncons; j += gridDim.x*blockDim.x){
+		const cpgJoint &jr = s.joints[W.consOff + j];
+		s.unitKey[W.unitOff + narb + j] = W.candCap + j;
+		s.unitA[W.unitOff + narb + j] = (s.btype[W.bodyOff + jr.a] == CPG_DYNAMIC) ? jr.a : -1;
+		s.unitB[W.unitOff + narb + j] = (s.btype[W.bodyOff + jr.b] == CPG_DYNAMIC) ? jr.b : -1;
+	}
+}
+
 /* cpSpaceStep.c:292-325 */
 __global__ void k_arb_filter(cpgSet s)
 {
@@ -475,8 +542,13 @@ __global__ void k_schedule(cpgSet s)
 }
 
 /* ------------------------------------------------------------------ */
-/* Pre-step: cpArbiter.c:416-439, cpPivotJoint.c:24-39, cpPinJoint.c:24-46,
- * cpSlideJoint.c:24-56 */
+/* Pre-step into solver rows: cpArbiter.c:416-439, cpPivotJoint.c:24-39,
+ * cpPinJoint.c:24-46, cpSlideJoint.c:24-56.  Rows are written in schedule
+ * order (row k holds unit order[k]). */
+
+#define ROW_FIRST 1
+#define ROW_DYN_A 2
+#define ROW_DYN_B 4
 
 __device__ __forceinline__ double k_scalar_body(const cpgSet &s, int g, double rx, double ry, double nx, double ny)
 {
@@ -484,7 +556,7 @@ __device__ __forceinline__ double k_scalar_body(const cpgSet &s, int g, double r
 	return s.minv[g] + s.iinv[g]*rcn*rcn;
 }
 
-__global__ void k_prestep(cpgSet s)
+__global__ void k_build_rows(cpgSet s)
 {
 	int w = blockIdx.y;
 	const cpgParams &P = s.params[w];
@@ -494,127 +566,157 @@ __global__ void k_prestep(cpgSet s)
 	int narb = T.narb, nunits = T.nunits;
 	if(nunits > W.unitCap) return;
 	double dt = P.dt;
-	for(int u = blockIdx.x*blockDim.x + threadIdx.x; u < nunits; u += gridDim.x*blockDim.x){
+	const int *order = s.unitOrder + W.unitOff;
+	for(int k = blockIdx.x*blockDim.x + threadIdx.x; k < nunits; k += gridDim.x*blockDim.x){
+		int u = order[k];
+		cpgRow &row = s.rows[W.unitOff + k];
 		if(u < narb){
-			cpgArb &arb = s.arbs[s.arbList[W.candOff + u]];
+			int slot = s.arbList[W.candOff + u];
+			const cpgArb &arb = s.arbs[slot];
 			int ga = W.bodyOff + arb.ba, gb = W.bodyOff + arb.bb;
+			row.a = arb.ba; row.b = arb.bb; row.kind = 0; row.count = arb.count; row.src = slot;
+			row.flags = (arb.state == CPG_ARB_FIRST ? ROW_FIRST : 0)
+				| (s.btype[ga] == CPG_DYNAMIC ? ROW_DYN_A : 0) | (s.btype[gb] == CPG_DYNAMIC ? ROW_DYN_B : 0);
 			double nx = arb.nx, ny = arb.ny;
+			row.arb.nx = nx; row.arb.ny = ny; row.arb.u = arb.u; row.arb.svx = arb.svx; row.arb.svy = arb.svy;
 			double dx = s.px[gb] - s.px[ga], dy = s.py[gb] - s.py[ga];
-			for(int k = 0; k < arb.count; k++){
-				cpgContact &con = arb.c[k];
+			for(int c = 0; c < arb.count; c++){
+				const cpgContact &con = arb.c[c];
+				cpgRowContact &rc = row.arb.c[c];
+				rc.r1x = con.r1x; rc.r1y = con.r1y; rc.r2x = con.r2x; rc.r2y = con.r2y;
 				double kn = k_scalar_body(s, ga, con.r1x, con.r1y, nx, ny) + k_scalar_body(s, gb, con.r2x, con.r2y, nx, ny);
-				con.nMass = 1.0/kn;
+				rc.nMass = 1.0/kn;
 				double kt = k_scalar_body(s, ga, con.r1x, con.r1y, -ny, nx) + k_scalar_body(s, gb, con.r2x, con.r2y, -ny, nx);
-				con.tMass = 1.0/kt;
+				rc.tMass = 1.0/kt;
 				double ddx = (con.r2x - con.r1x) + dx, ddy = (con.r2y - con.r1y) + dy;
 				double dist = ddx*nx + ddy*ny;
-				con.bias = -P.biasCoef*dmin(0.0, dist + P.slop)/dt;
-				con.jBias = 0.0;
+				rc.bias = -P.biasCoef*dmin(0.0, dist + P.slop)/dt;
+				rc.jBias = 0.0;
 				/* relative_velocity, chipmunk_private.h:172-178 */
 				double v1x = s.vx[ga] + (-con.r1y)*s.w[ga], v1y = s.vy[ga] + con.r1x*s.w[ga];
 				double v2x = s.vx[gb] + (-con.r2y)*s.w[gb], v2y = s.vy[gb] + con.r2x*s.w[gb];
 				double vrx = v2x - v1x, vry = v2y - v1y;
-				con.bounce = (vrx*nx + vry*ny)*arb.e;
+				rc.bounce = (vrx*nx + vry*ny)*arb.e;
+				rc.jnAcc = con.jnAcc; rc.jtAcc = con.jtAcc;
 			}
 		} else {
-			cpgJoint &j = s.joints[W.consOff + (u - narb)];
-			double biasCoef = s.jbias[W.consOff + (u - narb)];
+			int jidx = u - narb;
+			const cpgJoint &j = s.joints[W.consOff + jidx];
+			double biasCoef = s.jbias[W.consOff + jidx];
 			int ga = W.bodyOff + j.a, gb = W.bodyOff + j.b;
+			row.a = j.a; row.b = j.b; row.kind = j.kind; row.count = 0; row.src = jidx;
+			row.flags = (s.btype[ga] == CPG_DYNAMIC ? ROW_DYN_A : 0) | (s.btype[gb] == CPG_DYNAMIC ? ROW_DYN_B : 0);
 			/* r = transformVect(body, anchor - cog) */
 			double lax = j.ax - s.cogx[ga], lay = j.ay - s.cogy[ga];
 			double lbx = j.bx - s.cogx[gb], lby = j.by - s.cogy[gb];
-			j.r1x = s.ta[ga]*lax + s.tc[ga]*lay; j.r1y = s.tb[ga]*lax + s.td[ga]*lay;
-			j.r2x = s.ta[gb]*lbx + s.tc[gb]*lby; j.r2y = s.tb[gb]*lbx + s.td[gb]*lby;
-			double deltax = (s.px[gb] + j.r2x) - (s.px[ga] + j.r1x);
-			double deltay = (s.py[gb] + j.r2y) - (s.py[ga] + j.r1y);
+			double r1x = s.ta[ga]*lax + s.tc[ga]*lay, r1y = s.tb[ga]*lax + s.td[ga]*lay;
+			double r2x = s.ta[gb]*lbx + s.tc[gb]*lby, r2y = s.tb[gb]*lbx + s.td[gb]*lby;
+			row.jnt.r1x = r1x; row.jnt.r1y = r1y; row.jnt.r2x = r2x; row.jnt.r2y = r2y;
+			row.jnt.maxForce = j.maxForce;
+			double deltax = (s.px[gb] + r2x) - (s.px[ga] + r1x);
+			double deltay = (s.py[gb] + r2y) - (s.py[ga] + r1y);
 			if(j.kind == CPG_PIVOT){
 				/* k_tensor, chipmunk_private.h:228-262 */
 				double m_sum = s.minv[ga] + s.minv[gb];
 				double k11 = m_sum, k12 = 0.0, k21 = 0.0, k22 = m_sum;
 				double ai = s.iinv[ga];
-				double r1xsq = j.r1x*j.r1x*ai, r1ysq = j.r1y*j.r1y*ai, r1nxy = -j.r1x*j.r1y*ai;
+				double r1xsq = r1x*r1x*ai, r1ysq = r1y*r1y*ai, r1nxy = -r1x*r1y*ai;
 				k11 += r1ysq; k12 += r1nxy; k21 += r1nxy; k22 += r1xsq;
 				double bi = s.iinv[gb];
-				double r2xsq = j.r2x*j.r2x*bi, r2ysq = j.r2y*j.r2y*bi, r2nxy = -j.r2x*j.r2y*bi;
+				double r2xsq = r2x*r2x*bi, r2ysq = r2y*r2y*bi, r2nxy = -r2x*r2y*bi;
 				k11 += r2ysq; k12 += r2nxy; k21 += r2nxy; k22 += r2xsq;
 				double det = k11*k22 - k12*k21;
 				double det_inv = 1.0/det;
-				j.k11 = k22*det_inv; j.k12 = -k12*det_inv; j.k21 = -k21*det_inv; j.k22 = k11*det_inv;
+				row.jnt.k11 = k22*det_inv; row.jnt.k12 = -k12*det_inv; row.jnt.k21 = -k21*det_inv; row.jnt.k22 = k11*det_inv;
 				V2 bias = vclamp(vmul(v2(deltax, deltay), -biasCoef/dt), j.maxBias);
-				j.biasx = bias.x; j.biasy = bias.y;
+				row.jnt.biasx = bias.x; row.jnt.biasy = bias.y;
+				row.jnt.jx = j.jx; row.jnt.jy = j.jy;
 			} else if(j.kind == CPG_PIN){
 				double dist = sqrt(deltax*deltax + deltay*deltay);
 				double inv = 1.0/(dist ? dist : CUDART_INF);
-				j.nx = deltax*inv; j.ny = deltay*inv;
-				double kn = k_scalar_body(s, ga, j.r1x, j.r1y, j.nx, j.ny) + k_scalar_body(s, gb, j.r2x, j.r2y, j.nx, j.ny);
-				j.nMass = 1.0/kn;
-				j.bias = dclamp(-biasCoef*(dist - j.dist)/dt, -j.maxBias, j.maxBias);
+				double nx = deltax*inv, ny = deltay*inv;
+				row.jnt.nx = nx; row.jnt.ny = ny;
+				double kn = k_scalar_body(s, ga, r1x, r1y, nx, ny) + k_scalar_body(s, gb, r2x, r2y, nx, ny);
+				row.jnt.nMass = 1.0/kn;
+				row.jnt.bias = dclamp(-biasCoef*(dist - j.dist)/dt, -j.maxBias, j.maxBias);
+				row.jnt.jnAcc = j.jnAcc;
 			} else {
 				double dist = sqrt(deltax*deltax + deltay*deltay);
-				double pdist = 0.0;
+				double pdist = 0.0, nx, ny, jn = j.jnAcc;
 				if(dist > j.max){
 					pdist = dist - j.max;
 					V2 n = vnormalize(v2(deltax, deltay));
-					j.nx = n.x; j.ny = n.y;
+					nx = n.x; ny = n.y;
 				} else if(dist < j.min){
 					pdist = j.min - dist;
 					V2 n = vneg(vnormalize(v2(deltax, deltay)));
-					j.nx = n.x; j.ny = n.y;
+					nx = n.x; ny = n.y;
 				} else {
-					j.nx = 0.0; j.ny = 0.0;
-					j.jnAcc = 0.0;
+					nx = 0.0; ny = 0.0;
+					jn = 0.0;
 				}
-				double kn = k_scalar_body(s, ga, j.r1x, j.r1y, j.nx, j.ny) + k_scalar_body(s, gb, j.r2x, j.r2y, j.nx, j.ny);
-				j.nMass = 1.0/kn;
-				j.bias = dclamp(-biasCoef*pdist/dt, -j.maxBias, j.maxBias);
+				row.jnt.nx = nx; row.jnt.ny = ny;
+				double kn = k_scalar_body(s, ga, r1x, r1y, nx, ny) + k_scalar_body(s, gb, r2x, r2y, nx, ny);
+				row.jnt.nMass = 1.0/kn;
+				row.jnt.bias = dclamp(-biasCoef*pdist/dt, -j.maxBias, j.maxBias);
+				row.jnt.jnAcc = jn;
 			}
 		}
 	}
 }
 
-/* cpBody.c:493-509 */
+/* cpBody.c:493-509, then pack every body's solver state
+ * (vx vy w vbx vby wb minv iinv, 64 bytes) */
 __global__ void k_integrate_vel(cpgSet s)
 {
 	int g = blockIdx.x*blockDim.x + threadIdx.x;
 	if(g >= s.totalBodies) return;
 	int w = s.bworld[g];
 	const cpgParams &P = s.params[w];
-	if(!P.active || g - s.world[w].bodyOff >= s.world[w].ndyn) return;
-	if(s.btype[g] == CPG_KINEMATIC) return;
-	double dt = P.dt, damping = P.damping;
-	double minv = s.minv[g];
-	s.vx[g] = s.vx[g]*damping + (P.gx + s.fx[g]*minv)*dt;
-	s.vy[g] = s.vy[g]*damping + (P.gy + s.fy[g]*minv)*dt;
-	s.w[g] = s.w[g]*damping + s.tq[g]*s.iinv[g]*dt;
-	s.fx[g] = 0.0; s.fy[g] = 0.0; s.tq[g] = 0.0;
+	if(!P.active) return;
+	double vx = s.vx[g], vy = s.vy[g], wv = s.w[g];
+	double minv = s.minv[g], iinv = s.iinv[g];
+	if(g - s.world[w].bodyOff < s.world[w].ndyn && s.btype[g] != CPG_KINEMATIC){
+		double dt = P.dt, damping = P.damping;
+		vx = vx*damping + (P.gx + s.fx[g]*minv)*dt;
+		vy = vy*damping + (P.gy + s.fy[g]*minv)*dt;
+		wv = wv*damping + s.tq[g]*iinv*dt;
+		s.vx[g] = vx; s.vy[g] = vy; s.w[g] = wv;
+		s.fx[g] = 0.0; s.fy[g] = 0.0; s.tq[g] = 0.0;
+	}
+	double2 *pb = (double2 *)(s.pbody + 8*(size_t)g);
+	pb[0] = make_double2(vx, vy);
+	pb[1] = make_double2(wv, s.vbx[g]);
+	pb[2] = make_double2(s.vby[g], s.wb[g]);
+	pb[3] = make_double2(minv, iinv);
 }
 
 /* ------------------------------------------------------------------ */
-/* Solver units: cpArbiter.c:441-498, joint applyCachedImpulse/applyImpulse.
- * Only dynamic bodies are written; the others have zero inverse mass, so
- * the reference's update leaves them unchanged. */
+/* Solver units on rows: cpArbiter.c:441-498, joint applyCachedImpulse /
+ * applyImpulse.  Bodies come from the packed state; only dynamic bodies
+ * are written back (the others have zero inverse mass, so the reference's
+ * update leaves them unchanged). */
 
-struct BodyRef {
-	double vx, vy, w, vbx, vby, wb, minv, iinv;
-	int g;
-	bool dyn;
-};
+struct BodyRef { double vx, vy, w, vbx, vby, wb, minv, iinv; };
 
-__device__ __forceinline__ BodyRef load_body(const cpgSet &s, int g, bool dyn)
+template<bool CG>
+__device__ __forceinline__ BodyRef load_pbody(const double *base, int b)
 {
-	BodyRef b;
-	b.g = g; b.dyn = dyn;
-	b.vx = s.vx[g]; b.vy = s.vy[g]; b.w = s.w[g];
-	b.vbx = s.vbx[g]; b.vby = s.vby[g]; b.wb = s.wb[g];
-	b.minv = s.minv[g]; b.iinv = s.iinv[g];
-	return b;
+	const double2 *p = (const double2 *)(base + 8*(size_t)b);
+	double2 x0, x1, x2, x3;
+	if(CG){ x0 = __ldcg(p); x1 = __ldcg(p + 1); x2 = __ldcg(p + 2); x3 = __ldcg(p + 3); }
+	else { x0 = p[0]; x1 = p[1]; x2 = p[2]; x3 = p[3]; }
+	BodyRef r;
+	r.vx = x0.x; r.vy = x0.y; r.w = x1.x; r.vbx = x1.y; r.vby = x2.x; r.wb = x2.y; r.minv = x3.x; r.iinv = x3.y;
+	return r;
 }
 
-__device__ __forceinline__ void store_body(const cpgSet &s, const BodyRef &b)
+__device__ __forceinline__ void store_pbody(double *base, int b, const BodyRef &r)
 {
-	if(!b.dyn) return;
-	s.vx[b.g] = b.vx; s.vy[b.g] = b.vy; s.w[b.g] = b.w;
-	s.vbx[b.g] = b.vbx; s.vby[b.g] = b.vby; s.wb[b.g] = b.wb;
+	double2 *p = (double2 *)(base + 8*(size_t)b);
+	p[0] = make_double2(r.vx, r.vy);
+	p[1] = make_double2(r.w, r.vbx);
+	p[2] = make_double2(r.vby, r.wb);
 }
 
 /* chipmunk_private.h:193-210 */
@@ -638,167 +740,186 @@ __device__ __forceinline__ void apply_bias_impulse(BodyRef &b, double jx, double
 	b.wb += b.iinv*(rx*jy - ry*jx);
 }
 
-__device__ __forceinline__ void arb_apply_cached_ref(const cpgArb &arb, BodyRef &A, BodyRef &B, double dt_coef)
+/* warm start: cpArbiter.c:441-455, joint applyCachedImpulse */
+__device__ __forceinline__ void row_apply_cached(const cpgRow &row, BodyRef &A, BodyRef &B, double dt_coef)
 {
-	if(arb.state == CPG_ARB_FIRST) return;
-	double nx = arb.nx, ny = arb.ny;
-	for(int k = 0; k < arb.count; k++){
-		const cpgContact &con = arb.c[k];
-		/* j = rotate(n, (jnAcc, jtAcc)) * dt_coef */
-		double jx = nx*con.jnAcc - ny*con.jtAcc, jy = nx*con.jtAcc + ny*con.jnAcc;
-		apply_impulses(A, B, con.r1x, con.r1y, con.r2x, con.r2y, jx*dt_coef, jy*dt_coef);
-	}
-}
-
-__device__ __forceinline__ void arb_apply_ref(cpgArb &arb, BodyRef &A, BodyRef &B)
-{
-	double nx = arb.nx, ny = arb.ny;
-	double svx = arb.svx, svy = arb.svy;
-	double friction = arb.u;
-	for(int k = 0; k < arb.count; k++){
-		cpgContact &con = arb.c[k];
-		double nMass = con.nMass;
-		double r1x = con.r1x, r1y = con.r1y, r2x = con.r2x, r2y = con.r2y;
-		double vb1x = A.vbx + (-r1y)*A.wb, vb1y = A.vby + r1x*A.wb;
-		double vb2x = B.vbx + (-r2y)*B.wb, vb2y = B.vby + r2x*B.wb;
-		double v1x = A.vx + (-r1y)*A.w, v1y = A.vy + r1x*A.w;
-		double v2x = B.vx + (-r2y)*B.w, v2y = B.vy + r2x*B.w;
-		double vrx = (v2x - v1x) + svx, vry = (v2y - v1y) + svy;
-		double vbn = (vb2x - vb1x)*nx + (vb2y - vb1y)*ny;
-		double vrn = vrx*nx + vry*ny;
-		double vrt = vrx*(-ny) + vry*nx;
-		double jbn = (con.bias - vbn)*nMass;
-		double jbnOld = con.jBias;
-		con.jBias = dmax(jbnOld + jbn, 0.0);
-		double jn = -(con.bounce + vrn)*nMass;
-		double jnOld = con.jnAcc;
-		con.jnAcc = dmax(jnOld + jn, 0.0);
-		double jtMax = friction*con.jnAcc;
-		double jt = -vrt*con.tMass;
-		double jtOld = con.jtAcc;
-		con.jtAcc = dclamp(jtOld + jt, -jtMax, jtMax);
-		double db = con.jBias - jbnOld;
-		double bx = nx*db, by = ny*db;
-		apply_bias_impulse(A, -bx, -by, r1x, r1y);
-		apply_bias_impulse(B, bx, by, r2x, r2y);
-		double djn = con.jnAcc - jnOld, djt = con.jtAcc - jtOld;
-		double jx = nx*djn - ny*djt, jy = nx*djt + ny*djn;
-		apply_impulses(A, B, r1x, r1y, r2x, r2y, jx, jy);
-	}
-}
-
-__device__ __forceinline__ void joint_apply_cached_ref(const cpgJoint &j, BodyRef &A, BodyRef &B, double dt_coef)
-{
-	if(j.kind == CPG_PIVOT){
-		apply_impulses(A, B, j.r1x, j.r1y, j.r2x, j.r2y, j.jx*dt_coef, j.jy*dt_coef);
+	if(row.kind == 0){
+		if(row.flags & ROW_FIRST) return;
+		double nx = row.arb.nx, ny = row.arb.ny;
+		for(int k = 0; k < row.count; k++){
+			const cpgRowContact &con = row.arb.c[k];
+			/* j = rotate(n, (jnAcc, jtAcc)) * dt_coef */
+			double jx = nx*con.jnAcc - ny*con.jtAcc, jy = nx*con.jtAcc + ny*con.jnAcc;
+			apply_impulses(A, B, con.r1x, con.r1y, con.r2x, con.r2y, jx*dt_coef, jy*dt_coef);
+		}
+	} else if(row.kind == CPG_PIVOT){
+		apply_impulses(A, B, row.jnt.r1x, row.jnt.r1y, row.jnt.r2x, row.jnt.r2y, row.jnt.jx*dt_coef, row.jnt.jy*dt_coef);
 	} else {
-		double s_ = j.jnAcc*dt_coef;
-		apply_impulses(A, B, j.r1x, j.r1y, j.r2x, j.r2y, j.nx*s_, j.ny*s_);
+		double s_ = row.jnt.jnAcc*dt_coef;
+		apply_impulses(A, B, row.jnt.r1x, row.jnt.r1y, row.jnt.r2x, row.jnt.r2y, row.jnt.nx*s_, row.jnt.ny*s_);
 	}
 }
 
-__device__ __forceinline__ void joint_apply_ref(cpgJoint &j, BodyRef &A, BodyRef &B, double dt)
+/* one iteration: cpArbiter.c:459-498, cpPivotJoint.c:47-66,
+ * cpPinJoint.c:57-75, cpSlideJoint.c:66-89 */
+__device__ __forceinline__ void row_apply(cpgRow &row, BodyRef &A, BodyRef &B, double dt)
 {
-	if(j.kind == CPG_SLIDE && j.nx == 0.0 && j.ny == 0.0) return;
-	double v1x = A.vx + (-j.r1y)*A.w, v1y = A.vy + j.r1x*A.w;
-	double v2x = B.vx + (-j.r2y)*B.w, v2y = B.vy + j.r2x*B.w;
+	if(row.kind == 0){
+		double nx = row.arb.nx, ny = row.arb.ny;
+		double svx = row.arb.svx, svy = row.arb.svy;
+		double friction = row.arb.u;
+		for(int k = 0; k < row.count; k++){
+			cpgRowContact &con = row.arb.c[k];
+			double nMass = con.nMass;
+			double r1x = con.r1x, r1y = con.r1y, r2x = con.r2x, r2y = con.r2y;
+			double vb1x = A.vbx + (-r1y)*A.wb, vb1y = A.vby + r1x*A.wb;
+			double vb2x = B.vbx + (-r2y)*B.wb, vb2y = B.vby + r2x*B.wb;
+			double v1x = A.vx + (-r1y)*A.w, v1y = A.vy + r1x*A.w;
+			double v2x = B.vx + (-r2y)*B.w, v2y = B.vy + r2x*B.w;
+			double vrx = (v2x - v1x) + svx, vry = (v2y - v1y) + svy;
+			double vbn = (vb2x - vb1x)*nx + (vb2y - vb1y)*ny;
+			double vrn = vrx*nx + vry*ny;
+			double vrt = vrx*(-ny) + vry*nx;
+			double jbn = (con.bias - vbn)*nMass;
+			double jbnOld = con.jBias;
+			con.jBias = dmax(jbnOld + jbn, 0.0);
+			double jn = -(con.bounce + vrn)*nMass;
+			double jnOld = con.jnAcc;
+			con.jnAcc = dmax(jnOld + jn, 0.0);
+			double jtMax = friction*con.jnAcc;
+			double jt = -vrt*con.tMass;
+			double jtOld = con.jtAcc;
+			con.jtAcc = dclamp(jtOld + jt, -jtMax, jtMax);
+			double db = con.jBias - jbnOld;
+			double bx = nx*db, by = ny*db;
+			apply_bias_impulse(A, -bx, -by, r1x, r1y);
+			apply_bias_impulse(B, bx, by, r2x, r2y);
+			double djn = con.jnAcc - jnOld, djt = con.jtAcc - jtOld;
+			double jx = nx*djn - ny*djt, jy = nx*djt + ny*djn;
+			apply_impulses(A, B, r1x, r1y, r2x, r2y, jx, jy);
+		}
+		return;
+	}
+	if(row.kind == CPG_SLIDE && row.jnt.nx == 0.0 && row.jnt.ny == 0.0) return;
+	double v1x = A.vx + (-row.jnt.r1y)*A.w, v1y = A.vy + row.jnt.r1x*A.w;
+	double v2x = B.vx + (-row.jnt.r2y)*B.w, v2y = B.vy + row.jnt.r2x*B.w;
 	double vrx = v2x - v1x, vry = v2y - v1y;
-	if(j.kind == CPG_PIVOT){
-		double ex = j.biasx - vrx, ey = j.biasy - vry;
-		double jx = ex*j.k11 + ey*j.k12, jy = ex*j.k21 + ey*j.k22;
-		double oldx = j.jx, oldy = j.jy;
-		V2 acc = vclamp(v2(j.jx + jx, j.jy + jy), j.maxForce*dt);
-		j.jx = acc.x; j.jy = acc.y;
-		apply_impulses(A, B, j.r1x, j.r1y, j.r2x, j.r2y, j.jx - oldx, j.jy - oldy);
-	} else if(j.kind == CPG_PIN){
-		double vrn = vrx*j.nx + vry*j.ny;
-		double jnMax = j.maxForce*dt;
-		double jn = (j.bias - vrn)*j.nMass;
-		double jnOld = j.jnAcc;
-		j.jnAcc = dclamp(jnOld + jn, -jnMax, jnMax);
-		jn = j.jnAcc - jnOld;
-		apply_impulses(A, B, j.r1x, j.r1y, j.r2x, j.r2y, j.nx*jn, j.ny*jn);
+	if(row.kind == CPG_PIVOT){
+		double ex = row.jnt.biasx - vrx, ey = row.jnt.biasy - vry;
+		double jx = ex*row.jnt.k11 + ey*row.jnt.k12, jy = ex*row.jnt.k21 + ey*row.jnt.k22;
+		double oldx = row.jnt.jx, oldy = row.jnt.jy;
+		V2 acc = vclamp(v2(row.jnt.jx + jx, row.jnt.jy + jy), row.jnt.maxForce*dt);
+		row.jnt.jx = acc.x; row.jnt.jy = acc.y;
+		apply_impulses(A, B, row.jnt.r1x, row.jnt.r1y, row.jnt.r2x, row.jnt.r2y, row.jnt.jx - oldx, row.jnt.jy - oldy);
+	} else if(row.kind == CPG_PIN){
+		double vrn = vrx*row.jnt.nx + vry*row.jnt.ny;
+		double jnMax = row.jnt.maxForce*dt;
+		double jn = (row.jnt.bias - vrn)*row.jnt.nMass;
+		double jnOld = row.jnt.jnAcc;
+		row.jnt.jnAcc = dclamp(jnOld + jn, -jnMax, jnMax);
+		jn = row.jnt.jnAcc - jnOld;
+		apply_impulses(A, B, row.jnt.r1x, row.jnt.r1y, row.jnt.r2x, row.jnt.r2y, row.jnt.nx*jn, row.jnt.ny*jn);
 	} else {
-		double vrn = vrx*j.nx + vry*j.ny;
-		double jn = (j.bias - vrn)*j.nMass;
-		double jnOld = j.jnAcc;
-		j.jnAcc = dclamp(jnOld + jn, -j.maxForce*dt, 0.0);
-		jn = j.jnAcc - jnOld;
-		apply_impulses(A, B, j.r1x, j.r1y, j.r2x, j.r2y, j.nx*jn, j.ny*jn);
+		double vrn = vrx*row.jnt.nx + vry*row.jnt.ny;
+		double jn = (row.jnt.bias - vrn)*row.jnt.nMass;
+		double jnOld = row.jnt.jnAcc;
+		row.jnt.jnAcc = dclamp(jnOld + jn, -row.jnt.maxForce*dt, 0.0);
+		jn = row.jnt.jnAcc - jnOld;
+		apply_impulses(A, B, row.jnt.r1x, row.jnt.r1y, row.jnt.r2x, row.jnt.r2y, row.jnt.nx*jn, row.jnt.ny*jn);
 	}
 }
 
-__device__ __forceinline__ void arb_apply_cached(const cpgSet &s, cpgArb &arb, int bodyOff, double dt_coef)
+template<bool CG>
+__device__ __forceinline__ void solve_row(cpgRow *rows, int k, double *bodies, int pass, double dt_coef, double dt)
 {
-	if(arb.state == CPG_ARB_FIRST) return;
-	int ga = bodyOff + arb.ba, gb = bodyOff + arb.bb;
-	BodyRef A = load_body(s, ga, s.btype[ga] == CPG_DYNAMIC);
-	BodyRef B = load_body(s, gb, s.btype[gb] == CPG_DYNAMIC);
-	arb_apply_cached_ref(arb, A, B, dt_coef);
-	store_body(s, A); store_body(s, B);
+	cpgRow &row = rows[k];
+	BodyRef A = load_pbody<CG>(bodies, row.a);
+	BodyRef B = load_pbody<CG>(bodies, row.b);
+	if(pass == 0) row_apply_cached(row, A, B, dt_coef);
+	else row_apply(row, A, B, dt);
+	if(row.flags & ROW_DYN_A) store_pbody(bodies, row.a, A);
+	if(row.flags & ROW_DYN_B) store_pbody(bodies, row.b, B);
 }
 
-__device__ __forceinline__ void arb_apply(const cpgSet &s, cpgArb &arb, int bodyOff)
-{
-	int ga = bodyOff + arb.ba, gb = bodyOff + arb.bb;
-	BodyRef A = load_body(s, ga, s.btype[ga] == CPG_DYNAMIC);
-	BodyRef B = load_body(s, gb, s.btype[gb] == CPG_DYNAMIC);
-	arb_apply_ref(arb, A, B);
-	store_body(s, A); store_body(s, B);
-}
-
-__device__ __forceinline__ void joint_apply_cached(const cpgSet &s, const cpgJoint &j, int bodyOff, double dt_coef)
-{
-	int ga = bodyOff + j.a, gb = bodyOff + j.b;
-	BodyRef A = load_body(s, ga, s.btype[ga] == CPG_DYNAMIC);
-	BodyRef B = load_body(s, gb, s.btype[gb] == CPG_DYNAMIC);
-	joint_apply_cached_ref(j, A, B, dt_coef);
-	store_body(s, A); store_body(s, B);
-}
-
-__device__ __forceinline__ void joint_apply(const cpgSet &s, cpgJoint &j, int bodyOff, double dt)
-{
-	if(j.kind == CPG_SLIDE && j.nx == 0.0 && j.ny == 0.0) return;
-	int ga = bodyOff + j.a, gb = bodyOff + j.b;
-	BodyRef A = load_body(s, ga, s.btype[ga] == CPG_DYNAMIC);
-	BodyRef B = load_body(s, gb, s.btype[gb] == CPG_DYNAMIC);
-	joint_apply_ref(j, A, B, dt);
-	store_body(s, A); store_body(s, B);
-}
+extern __shared__ double sbody[];
 
 /* Warm start (pass 0) and `iterations` sweeps, level by level; one block
- * per world.  __syncthreads() orders a level's global-memory writes before
- * the next level's reads within the block. */
-__global__ void k_solve(cpgSet s)
+ * per world.  Worlds of at most `stagedMax` bodies keep their packed body
+ * state in shared memory for the whole solve. */
+__global__ void k_solve(cpgSet s, int stagedMax)
 {
 	int w = blockIdx.x;
 	const cpgParams &P = s.params[w];
 	if(!P.active) return;
 	const cpgWorld &W = s.world[w];
 	const cpgTree &T = s.tree[w];
-	int narb = T.narb, nunits = T.nunits, nlev = T.nlevels;
+	int nunits = T.nunits, nlev = T.nlevels;
 	if(nunits > W.unitCap) return;
+	bool staged = W.nbodies <= stagedMax;
+	double *gb = s.pbody + 8*(size_t)W.bodyOff;
+	if(staged){
+		for(int i = threadIdx.x; i < 8*W.nbodies; i += blockDim.x) sbody[i] = gb[i];
+		__syncthreads();
+	}
+	double *bodies = staged ? sbody : gb;
 	const int *start = s.levelStart + W.unitOff + w;
-	const int *order = s.unitOrder + W.unitOff;
-	const int *list = s.arbList + W.candOff;
+	cpgRow *rows = s.rows + W.unitOff;
 	for(int pass = 0; pass <= P.iterations; pass++){
 		for(int l = 0; l < nlev; l++){
 			int e = start[l + 1];
-			for(int k = start[l] + threadIdx.x; k < e; k += blockDim.x){
-				int u = order[k];
-				if(u < narb){
-					cpgArb &arb = s.arbs[list[u]];
-					if(pass == 0) arb_apply_cached(s, arb, W.bodyOff, P.dt_coef);
-					else arb_apply(s, arb, W.bodyOff);
-				} else {
-					cpgJoint &j = s.joints[W.consOff + (u - narb)];
-					if(pass == 0) joint_apply_cached(s, j, W.bodyOff, P.dt_coef);
-					else joint_apply(s, j, W.bodyOff, P.dt);
-				}
-			}
+			for(int k = start[l] + threadIdx.x; k < e; k += blockDim.x)
+				solve_row<false>(rows, k, bodies, pass, P.dt_coef, P.dt);
 			__syncthreads();
 		}
 	}
+	if(staged){
+		for(int i = threadIdx.x; i < 8*W.nbodies; i += blockDim.x) gb[i] = sbody[i];
+	}
+}
+
+/* Rows back to the arbiter table and the joint records (the warm-start
+ * state of the next step), packed bodies back to the body arrays. */
+__global__ void k_writeback(cpgSet s)
+{
+	int w = blockIdx.y;
+	if(!s.params[w].active) return;
+	const cpgWorld &W = s.world[w];
+	const cpgTree &T = s.tree[w];
+	int nunits = T.nunits;
+	if(nunits > W.unitCap) return;
+	for(int k = blockIdx.x*blockDim.x + threadIdx.x; k < nunits; k += gridDim.x*blockDim.x){
+		const cpgRow &row = s.rows[W.unitOff + k];
+		if(row.kind == 0){
+			cpgArb &arb = s.arbs[row.src];
+			for(int c = 0; c < row.count; c++){
+				const cpgRowContact &rc = row.arb.c[c];
+				cpgContact &con = arb.c[c];
+				con.nMass = rc.nMass; con.tMass = rc.tMass; con.bounce = rc.bounce; con.bias = rc.bias;
+				con.jnAcc = rc.jnAcc; con.jtAcc = rc.jtAcc; con.jBias = rc.jBias;
+			}
+		} else {
+			cpgJoint &j = s.joints[W.consOff + row.src];
+			j.r1x = row.jnt.r1x; j.r1y = row.jnt.r1y; j.r2x = row.jnt.r2x; j.r2y = row.jnt.r2y;
+			if(row.kind == CPG_PIVOT){
+				j.k11 = row.jnt.k11; j.k12 = row.jnt.k12; j.k21 = row.jnt.k21; j.k22 = row.jnt.k22;
+				j.jx = row.jnt.jx; j.jy = row.jnt.jy; j.biasx = row.jnt.biasx; j.biasy = row.jnt.biasy;
+			} else {
+				j.nx = row.jnt.nx; j.ny = row.jnt.ny; j.nMass = row.jnt.nMass; j.jnAcc = row.jnt.jnAcc; j.bias = row.jnt.bias;
+			}
+		}
+	}
+}
+
+__global__ void k_unpack_bodies(cpgSet s)
+{
+	int g = blockIdx.x*blockDim.x + threadIdx.x;
+	if(g >= s.totalBodies) return;
+	int w = s.bworld[g];
+	if(!s.params[w].active || s.btype[g] != CPG_DYNAMIC) return;
+	const double2 *pb = (const double2 *)(s.pbody + 8*(size_t)g);
+	double2 x0 = pb[0], x1 = pb[1], x2 = pb[2];
+	s.vx[g] = x0.x; s.vy[g] = x0.y; s.w[g] = x1.x;
+	s.vbx[g] = x1.y; s.vby[g] = x2.x; s.wb[g] = x2.y;
 }
 
 /* Aggregate per-world bookkeeping for the host (one block). */
@@ -836,16 +957,57 @@ __global__ void k_gather_arbs(cpgSet s, int w, cpgArb *out, int n)
 /* ------------------------------------------------------------------ */
 /* Coloured mode (single-world sets): sweep-and-prune, colouring, solve */
 
+/* Sweep axis: the one along which the shape centres spread more (their
+ * variance), so that a sweep visits fewer boxes.  One block. */
+__global__ void k_sap_axis(cpgSet s, int w)
+{
+	const cpgWorld &W = s.world[w];
+	__shared__ double red[4][32];
+	double sx = 0, sxx = 0, sy = 0, syy = 0;
+	for(int k = threadIdx.x; k < W.ndynShapes; k += blockDim.x){
+		int g = W.shapeOff + s.dynShapes[W.dynShapeOff + k];
+		double cx = 0.5*(s.bbl[g] + s.bbr[g]), cy = 0.5*(s.bbb[g] + s.bbt[g]);
+		sx += cx; sxx += cx*cx; sy += cy; syy += cy*cy;
+	}
+	for(int o = 16; o > 0; o >>= 1){
+		sx += __shfl_down_sync(0xffffffffu, sx, o); sxx += __shfl_down_sync(0xffffffffu, sxx, o);
+		sy += __shfl_down_sync(0xffffffffu, sy, o); syy += __shfl_down_sync(0xffffffffu, syy, o);
+	}
+	int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+	if(lane == 0){ red[0][warp] = sx; red[1][warp] = sxx; red[2][warp] = sy; red[3][warp] = syy; }
+	__syncthreads();
+	if(threadIdx.x == 0){
+		double a = 0, b = 0, c = 0, d = 0;
+		for(int i = 0; i < (int)(blockDim.x >> 5); i++){ a += red[0][i]; b += red[1][i]; c += red[2][i]; d += red[3][i]; }
+		double n = W.ndynShapes > 0 ? (double)W.ndynShapes : 1.0;
+		double vx = b/n - (a/n)*(a/n), vy = d/n - (c/n)*(c/n);
+		s.colorCursor[8] = (vy > vx) ? 1 : 0;
+	}
+}
+
 __global__ void k_sap_keys(cpgSet s, int w)
 {
 	const cpgWorld &W = s.world[w];
 	int k = blockIdx.x*blockDim.x + threadIdx.x;
 	if(k >= W.ndynShapes) return;
+	int axis = s.colorCursor[8];
 	int sh = s.dynShapes[W.dynShapeOff + k];
 	int g = W.shapeOff + sh;
-	s.sortKA[k] = float_order_key(__double2float_rd(s.bbl[g]));
+	double lo = axis ? s.bbb[g] : s.bbl[g], hi = axis ? s.bbt[g] : s.bbr[g];
+	s.sortKA[k] = float_order_key(__double2float_rd(lo));
 	s.sortVA[k] = sh;
-	s.rkeys[sh] = float_order_key(__double2float_ru(s.bbr[g]));
+	s.rkeys[sh] = float_order_key(__double2float_ru(hi));
+}
+
+/* Boxes in sweep order, so that a sweep reads consecutive records. */
+__global__ void k_sap_gather(cpgSet s, int w)
+{
+	const cpgWorld &W = s.world[w];
+	int k = blockIdx.x*blockDim.x + threadIdx.x;
+	if(k >= W.ndynShapes) return;
+	int g = W.shapeOff + s.sortVA[k];
+	double4 b; b.x = s.bbl[g]; b.y = s.bbb[g]; b.z = s.bbr[g]; b.w = s.bbt[g];
+	((double4 *)s.sapBB)[k] = b;
 }
 
 __device__ int arb_find(const cpgSet &s, unsigned long long key)
@@ -864,7 +1026,7 @@ __global__ void k_sap_count(cpgSet s, int w)
 {
 	const cpgWorld &W = s.world[w];
 	const cpgTree &T = s.tree[w];
-	SapCtx c; c.keys = s.sortKA; c.vals = s.sortVA; c.rkeys = s.rkeys; c.n = W.ndynShapes;
+	SapCtx c; c.keys = s.sortKA; c.vals = s.sortVA; c.rkeys = s.rkeys; c.sbb = (const double4 *)s.sapBB; c.n = W.ndynShapes;
 	for(int i = blockIdx.x*blockDim.x + threadIdx.x; i < c.n; i += gridDim.x*blockDim.x){
 		unsigned cnt = 0;
 		sap_visit(s, W, T, c, i, [&](int, int){ cnt++; });
@@ -877,11 +1039,12 @@ __global__ void k_sap_emit(cpgSet s, int w)
 {
 	const cpgWorld &W = s.world[w];
 	cpgTree &T = s.tree[w];
-	SapCtx c; c.keys = s.sortKA; c.vals = s.sortVA; c.rkeys = s.rkeys; c.n = W.ndynShapes;
+	SapCtx c; c.keys = s.sortKA; c.vals = s.sortVA; c.rkeys = s.rkeys; c.sbb = (const double4 *)s.sapBB; c.n = W.ndynShapes;
 	unsigned total = s.sapCount[c.n];
 	if(blockIdx.x == 0 && threadIdx.x == 0){
 		if(total > (unsigned)W.candCap){ T.error |= CPG_ERR_CANDS; T.ncand = W.candCap; }
 		else T.ncand = (int)total;
+		T.narb = 0;   /* the unordered compaction counts from zero */
 	}
 	for(int i = blockIdx.x*blockDim.x + threadIdx.x; i < c.n; i += gridDim.x*blockDim.x){
 		unsigned pos = s.sapCount[i];
@@ -898,9 +1061,13 @@ __global__ void k_sap_emit(cpgSet s, int w)
 	}
 }
 
-__device__ __forceinline__ unsigned long long unit_priority(int u)
+/* 24 hashed priority bits above the unit's id (bits 56-63 hold the
+ * round).  The id is the unit's candidate index (joints follow the
+ * candidates), which does not depend on the order of the unordered
+ * compaction, so the colouring is the same on every run. */
+__device__ __forceinline__ unsigned long long unit_priority(int key)
 {
-	return (mix64((unsigned long long)u + 0x9e3779b97f4a7c15ull) & 0xffffffff00000000ull) | (unsigned)u;
+	return (mix64((unsigned long long)key + 0x9e3779b97f4a7c15ull) & 0x00ffffff00000000ull) | (unsigned)key;
 }
 
 #define CPG_COLOR_ROUNDS 128
@@ -915,6 +1082,7 @@ __global__ void k_color_coop(cpgSet s, int w)
 	int n = T.nunits, nb = W.nbodies;
 	int gtid = blockIdx.x*blockDim.x + threadIdx.x, gsz = gridDim.x*blockDim.x;
 	const int *ua = s.unitA + W.unitOff, *ub = s.unitB + W.unitOff;
+	const int *ukey = s.unitKey + W.unitOff;
 	int *color = s.unitLevel + W.unitOff;
 	unsigned long long *claim = s.claim + W.bodyOff, *cmask = s.cmask + W.bodyOff;
 	int *counter = s.colorCursor;   /* [0],[1]: remaining per round parity; [2]: colours */
@@ -923,9 +1091,12 @@ __global__ void k_color_coop(cpgSet s, int w)
 	if(gtid == 0){ counter[0] = 0; counter[1] = 0; counter[2] = 0; }
 	grid.sync();
 	for(int round = 0; round < CPG_COLOR_ROUNDS; round++){
+		/* claims carry the round in their top byte, newer rounds smaller,
+		 * so stale claims never need clearing */
+		unsigned long long tag = (unsigned long long)(255 - round) << 56;
 		for(int u = gtid; u < n; u += gsz){
 			if(color[u] >= 0) continue;
-			unsigned long long p = unit_priority(u);
+			unsigned long long p = tag | unit_priority(ukey[u]);
 			int a = ua[u], b = ub[u];
 			if(a >= 0) atomicMin(&claim[a], p);
 			if(b >= 0) atomicMin(&claim[b], p);
@@ -934,7 +1105,7 @@ __global__ void k_color_coop(cpgSet s, int w)
 		int remaining = 0;
 		for(int u = gtid; u < n; u += gsz){
 			if(color[u] >= 0) continue;
-			unsigned long long p = unit_priority(u);
+			unsigned long long p = tag | unit_priority(ukey[u]);
 			int a = ua[u], b = ub[u];
 			if((a < 0 || __ldcg(&claim[a]) == p) && (b < 0 || __ldcg(&claim[b]) == p)){
 				unsigned long long m = (a >= 0 ? __ldcg(&cmask[a]) : 0ull) | (b >= 0 ? __ldcg(&cmask[b]) : 0ull);
@@ -953,15 +1124,7 @@ __global__ void k_color_coop(cpgSet s, int w)
 		if(remaining) atomicAdd(&counter[round & 1], remaining);
 		if(gtid == 0) counter[(round + 1) & 1] = 0;
 		grid.sync();
-		int left = __ldcg(&counter[round & 1]);
-		if(left == 0) break;
-		for(int u = gtid; u < n; u += gsz){
-			if(color[u] >= 0) continue;
-			int a = ua[u], b = ub[u];
-			if(a >= 0) claim[a] = ~0ull;
-			if(b >= 0) claim[b] = ~0ull;
-		}
-		grid.sync();
+		if(__ldcg(&counter[round & 1]) == 0) break;
 	}
 	grid.sync();
 	/* counting sort by colour (order within a colour is irrelevant: its
@@ -993,54 +1156,28 @@ __global__ void k_color_coop(cpgSet s, int w)
 	}
 }
 
-/* Body state read past the L1 (other blocks write it between grid syncs). */
-__device__ __forceinline__ BodyRef load_body_cg(const cpgSet &s, int g, bool dyn)
-{
-	BodyRef b;
-	b.g = g; b.dyn = dyn;
-	b.vx = __ldcg(&s.vx[g]); b.vy = __ldcg(&s.vy[g]); b.w = __ldcg(&s.w[g]);
-	b.vbx = __ldcg(&s.vbx[g]); b.vby = __ldcg(&s.vby[g]); b.wb = __ldcg(&s.wb[g]);
-	b.minv = s.minv[g]; b.iinv = s.iinv[g];
-	return b;
-}
-
 /* Levels (ordered mode) or colours (coloured mode) of one large world,
- * with the whole grid: grid.sync() between levels. */
+ * with the whole grid: grid.sync() between levels.  Packed body state is
+ * read past the L1 (__ldcg), since other blocks write it between syncs;
+ * a row is always handled by the same thread, so its own updates are
+ * coherent. */
 __global__ void k_solve_coop(cpgSet s, int w)
 {
 	cg::grid_group grid = cg::this_grid();
 	const cpgParams &P = s.params[w];
 	const cpgWorld &W = s.world[w];
 	const cpgTree &T = s.tree[w];
-	int narb = T.narb, nunits = T.nunits, nlev = T.nlevels;
+	int nunits = T.nunits, nlev = T.nlevels;
 	if(nunits > W.unitCap) return;
 	const int *start = s.levelStart + W.unitOff + w;
-	const int *order = s.unitOrder + W.unitOff;
-	const int *list = s.arbList + W.candOff;
+	cpgRow *rows = s.rows + W.unitOff;
+	double *bodies = s.pbody + 8*(size_t)W.bodyOff;
 	int gtid = blockIdx.x*blockDim.x + threadIdx.x, gsz = gridDim.x*blockDim.x;
 	for(int pass = 0; pass <= P.iterations; pass++){
 		for(int l = 0; l < nlev; l++){
 			int e = start[l + 1];
-			for(int k = start[l] + gtid; k < e; k += gsz){
-				int u = order[k];
-				if(u < narb){
-					cpgArb &arb = s.arbs[list[u]];
-					int ga = W.bodyOff + arb.ba, gb = W.bodyOff + arb.bb;
-					BodyRef A = load_body_cg(s, ga, s.btype[ga] == CPG_DYNAMIC);
-					BodyRef B = load_body_cg(s, gb, s.btype[gb] == CPG_DYNAMIC);
-					if(pass == 0) arb_apply_cached_ref(arb, A, B, P.dt_coef);
-					else arb_apply_ref(arb, A, B);
-					store_body(s, A); store_body(s, B);
-				} else {
-					cpgJoint &j = s.joints[W.consOff + (u - narb)];
-					int ga = W.bodyOff + j.a, gb = W.bodyOff + j.b;
-					BodyRef A = load_body_cg(s, ga, s.btype[ga] == CPG_DYNAMIC);
-					BodyRef B = load_body_cg(s, gb, s.btype[gb] == CPG_DYNAMIC);
-					if(pass == 0) joint_apply_cached_ref(j, A, B, P.dt_coef);
-					else joint_apply_ref(j, A, B, P.dt);
-					store_body(s, A); store_body(s, B);
-				}
-			}
+			for(int k = start[l] + gtid; k < e; k += gsz)
+				solve_row<true>(rows, k, bodies, pass, P.dt_coef, P.dt);
 			grid.sync();
 		}
 	}
@@ -1083,9 +1220,17 @@ static int coop_blocks(const void *kernel, int threads)
 
 static cudaError_t launch_coop(const void *kernel, int threads, cpgSet *s, int w, cudaStream_t st)
 {
+	/* one block per SM: the fewer blocks a grid barrier waits for, the
+	 * cheaper it is, and a colour rarely has more units than threads */
 	static int blocks_solve = 0, blocks_color = 0;
 	int *cache = (kernel == (const void *)k_solve_coop) ? &blocks_solve : &blocks_color;
-	if(!*cache) *cache = coop_blocks(kernel, threads);
+	if(!*cache){
+		int most = coop_blocks(kernel, threads);
+		int sms = 0, dev = 0;
+		cudaGetDevice(&dev);
+		cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+		*cache = most < sms ? most : sms;
+	}
 	void *args[] = { (void *)s, (void *)&w };
 	g_launches++;
 	return cudaLaunchCooperativeKernel(kernel, dim3(*cache), dim3(threads), args, 0, st);
@@ -1094,6 +1239,12 @@ static cudaError_t launch_coop(const void *kernel, int threads, cpgSet *s, int w
 /* Single-world sets with at least this many solver units use the
  * cooperative whole-grid solve; smaller ones keep one block. */
 #define CPG_COOP_UNITS 2048
+/* Worlds up to this many bodies keep their solver body state in shared
+ * memory (64 bytes each, 200 KB at most). */
+#define CPG_STAGED_BODIES 3200
+/* Worlds whose tree node pool has at most this many nodes run the tree step
+ * with the pool in shared memory (64 bytes a node, 192 KB at most). */
+#define CPG_STAGED_NODES 3072
 
 /* `h` is the host copy of the set's sizes (same struct, host values). */
 extern "C" int cpg_launch_step(const cpgSet *s, const cpgSet *h, int mode, void *stream, float *phase_ms)
@@ -1120,6 +1271,7 @@ extern "C" int cpg_launch_step(const cpgSet *s, const cpgSet *h, int mode, void 
 	if(colored){
 		int n = h->hostNdyn;
 		int nb = blocks_for(n, RS_TILE);
+		LAUNCH(k_sap_axis<<<1, 1024, 0, st>>>(*s, 0));
 		LAUNCH(k_sap_keys<<<blocks_for(n, 256), 256, 0, st>>>(*s, 0));
 		unsigned *ka = s->sortKA, *kb = s->sortKB;
 		int *va = s->sortVA, *vb = s->sortVB;
@@ -1130,27 +1282,54 @@ extern "C" int cpg_launch_step(const cpgSet *s, const cpgSet *h, int mode, void 
 			unsigned *tk = ka; ka = kb; kb = tk;
 			int *tv = va; va = vb; vb = tv;
 		}
+		LAUNCH(k_sap_gather<<<blocks_for(n, 256), 256, 0, st>>>(*s, 0));
 		LAUNCH(k_sap_count<<<blocks_for(n, 128), 128, 0, st>>>(*s, 0));
 		LAUNCH(k_scan_excl<<<1, 1024, 0, st>>>(s->sapCount, n + 1, NULL));
 		LAUNCH(k_sap_emit<<<blocks_for(n, 128), 128, 0, st>>>(*s, 0));
 	} else {
-		LAUNCH(k_tree<<<blocks_for(W, 32), 32, 0, st>>>(*s));
+		/* node pools of up to CPG_STAGED_NODES nodes (64 B each) run from
+		 * shared memory; larger worlds use the global pool */
+		int staged = h->hostMaxNodes <= CPG_STAGED_NODES ? h->hostMaxNodes : 0;
+		size_t smem = (size_t)staged*sizeof(cpgNode);
+		static size_t treeSmemSet = 0;
+		if(smem > 48*1024 && smem > treeSmemSet){
+			cudaFuncSetAttribute(k_tree, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+			treeSmemSet = smem;
+		}
+		LAUNCH(k_tree<<<W, 32, smem, st>>>(*s, staged));
 	}
 	if(timing) cudaEventRecord(ev[2], st);
 	LAUNCH(k_narrow<<<dim3(perWorldX, W), 128, 0, st>>>(*s));
 	if(timing) cudaEventRecord(ev[3], st);
 	LAUNCH(k_arb_update<<<dim3(perWorldX, W), 128, 0, st>>>(*s));
-	LAUNCH(k_solve_list<<<W, 256, 0, st>>>(*s));
+	if(colored){
+		LAUNCH(k_solve_list_any<<<152*2, 256, 0, st>>>(*s, 0));
+		LAUNCH(k_units_joints<<<blocks_for(h->totalCons > 0 ? h->totalCons : 1, 128), 128, 0, st>>>(*s, 0));
+	} else {
+		LAUNCH(k_solve_list<<<W, 256, 0, st>>>(*s));
+	}
 	LAUNCH(k_arb_filter<<<blocks_for(h->arbCap, 256), 256, 0, st>>>(*s));
 	if(timing) cudaEventRecord(ev[4], st);
-	if(colored) launch_coop((const void *)k_color_coop, 256, &sv, 0, st);
+	if(colored) launch_coop((const void *)k_color_coop, 512, &sv, 0, st);
 	else LAUNCH(k_schedule<<<blocks_for(W, 32), 32, 0, st>>>(*s));
 	if(timing) cudaEventRecord(ev[5], st);
-	LAUNCH(k_prestep<<<dim3(perWorldX, W), 128, 0, st>>>(*s));
+	LAUNCH(k_build_rows<<<dim3(perWorldX, W), 128, 0, st>>>(*s));
 	LAUNCH(k_integrate_vel<<<blocks_for(h->totalBodies, 128), 128, 0, st>>>(*s));
 	if(timing) cudaEventRecord(ev[6], st);
-	if(W == 1 && (colored || h->hostUnitsHint >= CPG_COOP_UNITS)) launch_coop((const void *)k_solve_coop, 256, &sv, 0, st);
-	else LAUNCH(k_solve<<<W, 256, 0, st>>>(*s));
+	if(W == 1 && (colored || h->hostUnitsHint >= CPG_COOP_UNITS)){
+		launch_coop((const void *)k_solve_coop, 512, &sv, 0, st);
+	} else {
+		int stagedMax = h->hostMaxBodies <= CPG_STAGED_BODIES ? h->hostMaxBodies : 0;
+		size_t smem = (size_t)stagedMax*8*sizeof(double);
+		static size_t smemSet = 0;
+		if(smem > 48*1024 && smem > smemSet){
+			cudaFuncSetAttribute(k_solve, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+			smemSet = smem;
+		}
+		LAUNCH(k_solve<<<W, 256, smem, st>>>(*s, stagedMax));
+	}
+	LAUNCH(k_writeback<<<dim3(perWorldX, W), 128, 0, st>>>(*s));
+	LAUNCH(k_unpack_bodies<<<blocks_for(h->totalBodies, 128), 128, 0, st>>>(*s));
 	if(timing) cudaEventRecord(ev[7], st);
 	LAUNCH(k_stats<<<1, 256, 0, st>>>(*s));
 	cudaError_t e = check_launch("step");

@@ -493,6 +493,12 @@ int cpGpuDebugCandidates(cpSpace *space, int *out, int max);
  * Phases: 0 integrate+cache, 1 broadphase, 2 narrowphase, 3 arbiters,
  * 4 schedule, 5 prestep+warmstart, 6 solve. */
 void cpGpuSetTiming(int enabled);
+/* Bookkeeping of the last step (after it completes): [0] error flags,
+ * [1] pair-pool use and [2] node-pool use (per mille of capacity, largest
+ * world), [3] live cached arbiters, [4] candidate pairs, [5] solved
+ * arbiters, [6] levels (ordered) or colours (coloured) of one sweep,
+ * [7] candidate-buffer use (per mille).  Returns the count written. */
+int cpGpuGetStepStats(cpSpace *space, int *out, int max);
 int cpGpuGetPhaseTimes(cpSpace *space, double *ms, int max);
 /* Number of kernel launches issued by this library since the last reset. */
 long long cpGpuGetLaunchCount(int reset);
