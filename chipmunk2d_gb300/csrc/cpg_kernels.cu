@@ -92,11 +92,11 @@ __global__ void k_apply_ops(cpgSet s)
 
 __global__ void k_reset_prev(cpgSet s)
 {
-	int w = blockIdx.x;
+	int w = blockIdx.y;
 	if(!s.params[w].active) return;
 	const cpgWorld &W = s.world[w];
 	int n = s.tree[w].narb;
-	for(int i = threadIdx.x; i < n; i += blockDim.x){
+	for(int i = blockIdx.x*blockDim.x + threadIdx.x; i < n; i += gridDim.x*blockDim.x){
 		int slot = s.arbList[W.candOff + i];
 		s.arbs[slot].state = CPG_ARB_NORMAL;
 	}
@@ -1080,7 +1080,7 @@ __global__ void k_color_coop(cpgSet s, int w)
 	const cpgWorld &W = s.world[w];
 	cpgTree &T = s.tree[w];
 	int n = T.nunits, nb = W.nbodies;
-	int gtid = blockIdx.x*blockDim.x + threadIdx.x, gsz = gridDim.x*blockDim.x;
+	int gtid = threadIdx.x*gridDim.x + blockIdx.x, gsz = gridDim.x*blockDim.x;
 	const int *ua = s.unitA + W.unitOff, *ub = s.unitB + W.unitOff;
 	const int *ukey = s.unitKey + W.unitOff;
 	int *color = s.unitLevel + W.unitOff;
@@ -1172,11 +1172,15 @@ __global__ void k_solve_coop(cpgSet s, int w)
 	const int *start = s.levelStart + W.unitOff + w;
 	cpgRow *rows = s.rows + W.unitOff;
 	double *bodies = s.pbody + 8*(size_t)W.bodyOff;
-	int gtid = blockIdx.x*blockDim.x + threadIdx.x, gsz = gridDim.x*blockDim.x;
+	/* a level's units are dealt round-robin over the blocks (unit i to
+	 * block i % gridDim.x), so every SM's FP64 pipe gets a share: FP64 is
+	 * slow on this part (about 64 cycles per dependent operation) and a
+	 * level stacked on a few SMs would queue there */
+	int lane_id = threadIdx.x*gridDim.x + blockIdx.x, gsz = gridDim.x*blockDim.x;
 	for(int pass = 0; pass <= P.iterations; pass++){
 		for(int l = 0; l < nlev; l++){
 			int e = start[l + 1];
-			for(int k = start[l] + gtid; k < e; k += gsz)
+			for(int k = start[l] + lane_id; k < e; k += gsz)
 				solve_row<true>(rows, k, bodies, pass, P.dt_coef, P.dt);
 			grid.sync();
 		}
@@ -1264,7 +1268,7 @@ extern "C" int cpg_launch_step(const cpgSet *s, const cpgSet *h, int mode, void 
 	cpgSet sv = *s;
 
 	cudaMemsetAsync(s->stats, 0, 16*sizeof(int), st);
-	LAUNCH(k_reset_prev<<<W, 128, 0, st>>>(*s));
+	LAUNCH(k_reset_prev<<<dim3(perWorldX, W), 128, 0, st>>>(*s));
 	LAUNCH(k_integrate_pos<<<blocks_for(h->totalBodies, 128), 128, 0, st>>>(*s));
 	LAUNCH(k_shape_cache<<<blocks_for(h->totalShapes, 128), 128, 0, st>>>(*s));
 	if(timing) cudaEventRecord(ev[1], st);
