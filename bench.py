@@ -200,7 +200,7 @@ BATCH_WORLDS = 4096
 BATCH_DT = 1 / 60
 
 
-def run_batch(args):
+def run_batch(args, emit=True):
     """4096 tumble worlds with body counts log-uniform in [8, 512], stepped
     together (cpGpuBatchStep, reference sweep order in every world)."""
     import ctypes
@@ -301,7 +301,31 @@ def run_batch(args):
         "cpu_baseline": {"value": cpu_ws, "unit": "world-steps/s", "cores": 1, "kind": "port",
                          "sample": "%d worlds x %d steps" % (cpu_n, cpu_steps)},
     }
-    print(json.dumps(line), flush=True)
+    if emit:
+        print(json.dumps(line), flush=True)
+    return line
+
+
+def parity_mode_sample(lib, workload, steps, warmup):
+    """Device-timed steps of the exact reference-order mode (the drop-in's
+    default), for the JSON line's `ordered_mode` record."""
+    import torch
+    from chipmunk2d_gb300 import Scene
+    cfg, size, dt, desc = WORKLOADS[workload]
+    sc = Scene(lib, cfg, size)
+    for _ in range(warmup):
+        lib.cpSpaceStep(sc.space, dt)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        lib.cpSpaceStep(sc.space, dt)
+    lib.cpGpuSpaceSync(sc.space)
+    torch.cuda.synchronize()
+    secs = time.perf_counter() - t0
+    n = sc.nbodies
+    sc.free()
+    return {"workload": workload, "bodies": n, "steps": steps, "body_steps_per_s": n * steps / secs,
+            "ms_per_step": 1000 * secs / steps}
 
 
 def run_ours(args):
@@ -428,6 +452,19 @@ def run_ours(args):
 
     cpu_v, cpu_steps, cpu_s, _ = cpu_sample(args.workload, budget_s=args.cpu_seconds) if rank == 0 else (None, 0, 0, 0)
 
+    extras = {}
+    if args.extras and rank == 0 and args.workload == "circles":
+        # the exact-order mode (bit-compatible with cpSpaceStep) on the
+        # pyramid and on this workload, and the batched-world throughput
+        lib.cpGpuSetStream(ctypes.c_void_p(stream.cuda_stream))
+        extras["ordered_mode"] = [parity_mode_sample(lib, "pyramid", 300, 5),
+                                  parity_mode_sample(lib, "circles", 10, 3)]
+        b = run_batch(argparse.Namespace(steps=30, warmup=3), emit=False)
+        extras["batch"] = {k: b[k] for k in ("value", "unit", "ms_per_step", "body_steps_per_s",
+                                             "looped_plain_gpu_world_steps_per_s", "batched_over_looped",
+                                             "cpu_baseline", "phase_ms")}
+        extras["batch"]["config"] = b["config"]
+
     line = {
         "metric": "body-steps/s", "value": value, "unit": "body-steps/s", "n_gpus": world_size,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000 * total_s / args.steps,
@@ -450,6 +487,7 @@ def run_ours(args):
         "cpu_baseline": {"value": cpu_v, "unit": "body-steps/s", "cores": 1, "kind": "port",
                          "sample": "%d steps (%.1f s) of the %s workload after 5 warm-up steps" % (cpu_steps, cpu_s, args.workload)},
     }
+    line.update(extras)
     if rank == 0:
         print(json.dumps(line), flush=True)
     if dist:
@@ -459,10 +497,12 @@ def run_ours(args):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=120)
+    ap.add_argument("--steps", type=int, default=600)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--mode", default="ordered", choices=["ordered", "colored"])
+    ap.add_argument("--mode", default="colored", choices=["ordered", "colored"])
+    ap.add_argument("--no-extras", dest="extras", action="store_false",
+                    help="skip the ordered-mode and batched-world records of the default line")
     ap.add_argument("--workload", default="circles", choices=sorted(WORKLOADS) + ["batch"])
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--profile", action="store_true",
