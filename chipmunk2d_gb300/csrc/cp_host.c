@@ -204,19 +204,30 @@ static void push_(void ***arr, int *n, int *cap, void *p)
 /* ====================================================================
  * Device sets
  * ==================================================================== */
+#define CPG_STATS_INTERVAL 16
+/* The step parameters are uploaded from pinned memory by an asynchronous
+ * copy, so the host must not rewrite a block until that copy has run: the
+ * blocks rotate through a ring and each is reused only after its event. */
+#define CPG_PARAM_RING 8
+
 struct DevSet {
 	cpgSet d;                 /* device pointers; counts valid on host too */
 	cpgWorld *hworld;
-	cpgParams *hparams;       /* pinned */
+	cpgParams *hparams;       /* pinned, CPG_PARAM_RING slots of nspaces each */
+	cudaEvent_t paramEvent[CPG_PARAM_RING]; /* recorded after each slot's upload */
+	int paramRecorded[CPG_PARAM_RING];
+	int paramSlot;
 	int *hstats;              /* pinned */
 	cudaEvent_t statsEvent;
 	int statsPending;
+	int stepsSinceCheck;      /* steps enqueued since the stats were last read */
 	cpSpace **spaces;
 	int nspaces;
 	void *slab;
 	cpgArb *gather;           /* arbiter snapshot staging */
 	int gatherCap;
 };
+
 
 static cudaStream_t g_stream = NULL;
 static int g_stream_user = 0;
@@ -523,6 +534,7 @@ static void devset_free(DevSet *ds)
 	if(ds->hparams) cudaFreeHost(ds->hparams);
 	if(ds->hstats) cudaFreeHost(ds->hstats);
 	if(ds->statsEvent) cudaEventDestroy(ds->statsEvent);
+	for(int i = 0; i < CPG_PARAM_RING; i++) if(ds->paramEvent[i]) cudaEventDestroy(ds->paramEvent[i]);
 	for(int w = 0; w < ds->nspaces; w++){
 		if(ds->spaces[w]->dev == ds){ ds->spaces[w]->dev = NULL; }
 	}
@@ -608,7 +620,9 @@ static DevSet *devset_build(cpSpace **spaces, int nspaces)
 	ok &= cuda_ok(cudaMemsetAsync(ds->slab, 0, bytes, st), "memset set");
 	ok &= cuda_ok(cudaMemsetAsync(d->dbins, 0xff, sizeof(int)*(size_t)(NDB > 0 ? NDB : 1), st), "memset bins");
 	ok &= cuda_ok(cudaMemsetAsync(d->sbins, 0xff, sizeof(int)*(size_t)(NSB > 0 ? NSB : 1), st), "memset bins");
-	ok &= cuda_ok(cudaMallocHost((void **)&ds->hparams, sizeof(cpgParams)*(size_t)nspaces), "cudaMallocHost");
+	ok &= cuda_ok(cudaMallocHost((void **)&ds->hparams, sizeof(cpgParams)*(size_t)nspaces*CPG_PARAM_RING), "cudaMallocHost");
+	if(ok) memset(ds->hparams, 0, sizeof(cpgParams)*(size_t)nspaces*CPG_PARAM_RING);
+	for(int i = 0; i < CPG_PARAM_RING && ok; i++) ok &= cuda_ok(cudaEventCreateWithFlags(&ds->paramEvent[i], cudaEventDisableTiming), "event");
 	ok &= cuda_ok(cudaMallocHost((void **)&ds->hstats, sizeof(int)*16), "cudaMallocHost");
 	ok &= cuda_ok(cudaEventCreateWithFlags(&ds->statsEvent, cudaEventDisableTiming), "event");
 	if(!ok){ devset_free(ds); return NULL; }
@@ -701,11 +715,14 @@ static DevSet *devset_build(cpSpace **spaces, int nspaces)
 	return ds;
 }
 
+static void check_stats(DevSet *ds);
+
 /* Make host copies of the space's body state current. */
 static void space_pull(cpSpace *sp)
 {
 	if(!sp || !sp->dev || !sp->hostStale) return;
 	DevSet *ds = sp->dev;
+	check_stats(ds);
 	download_bodies(ds);
 	for(int w = 0; w < ds->nspaces; w++){
 		cpSpace *o = ds->spaces[w];
@@ -719,6 +736,7 @@ static void check_stats(DevSet *ds)
 	if(!ds->statsPending) return;
 	cudaEventSynchronize(ds->statsEvent);
 	ds->statsPending = 0;
+	ds->stepsSinceCheck = 0;
 	int err = ds->hstats[0];
 	/* whole-grid solve pays off when one sweep level is wide enough */
 	int units = ds->hstats[5] + (ds->nspaces == 1 ? ds->spaces[0]->ncons : 0);
@@ -734,10 +752,18 @@ static void check_stats(DevSet *ds)
 static int devset_step(DevSet *ds, const double *dts, cpSpace **only)
 {
 	cpgSet *d = &ds->d;
-	check_stats(ds);
+	/* The bookkeeping of a step (overflow flags, level counts) is read back
+	 * asynchronously; waiting for it every step would stop the host from
+	 * queueing the next step while the device runs this one.  It is checked
+	 * every CPG_STATS_INTERVAL steps and whenever the host reads state. */
+	if(ds->stepsSinceCheck >= CPG_STATS_INTERVAL) check_stats(ds);
+	int slot = ds->paramSlot;
+	ds->paramSlot = (slot + 1) % CPG_PARAM_RING;
+	if(ds->paramRecorded[slot]) cudaEventSynchronize(ds->paramEvent[slot]);
+	cpgParams *hp = ds->hparams + (size_t)slot*ds->nspaces;
 	for(int w = 0; w < ds->nspaces; w++){
 		cpSpace *sp = ds->spaces[w];
-		cpgParams *P = &ds->hparams[w];
+		cpgParams *P = &hp[w];
 		if((only && *only != sp) || dts[w] == 0.0){ P->active = 0; continue; }
 		if(sp->bodyDirty){ upload_bodies(ds, w); sp->bodyDirty = 0; }
 		if(sp->shapeDirty){ upload_shapes(ds, w); sp->shapeDirty = 0; }
@@ -764,7 +790,9 @@ static int devset_step(DevSet *ds, const double *dts, cpSpace **only)
 		sp->snapValid = 0;
 	}
 	cudaStream_t st = lib_stream();
-	if(!h2d(d->params, ds->hparams, sizeof(cpgParams)*(size_t)ds->nspaces)) return -1;
+	if(!h2d(d->params, hp, sizeof(cpgParams)*(size_t)ds->nspaces)) return -1;
+	cudaEventRecord(ds->paramEvent[slot], st);
+	ds->paramRecorded[slot] = 1;
 	float ms[8] = {0};
 	int mode = ds->spaces[0]->mode;
 	if(cpg_launch_step(d, d, mode, st, g_timing ? ms : NULL) != 0){
@@ -772,9 +800,12 @@ static int devset_step(DevSet *ds, const double *dts, cpSpace **only)
 		return -1;
 	}
 	if(g_timing) for(int w = 0; w < ds->nspaces; w++) memcpy(ds->spaces[w]->phaseMs, ms, sizeof(ms));
-	cudaMemcpyAsync(ds->hstats, d->stats, sizeof(int)*16, cudaMemcpyDeviceToHost, st);
-	cudaEventRecord(ds->statsEvent, st);
-	ds->statsPending = 1;
+	if(!ds->statsPending){
+		cudaMemcpyAsync(ds->hstats, d->stats, sizeof(int)*16, cudaMemcpyDeviceToHost, st);
+		cudaEventRecord(ds->statsEvent, st);
+		ds->statsPending = 1;
+	}
+	ds->stepsSinceCheck++;
 	return 0;
 }
 

@@ -132,41 +132,58 @@ struct SapCtx {
 	const unsigned *keys;     /* sorted left-edge keys */
 	const int *vals;          /* sorted shape indices (world-local) */
 	const unsigned *rkeys;    /* right-edge keys by shape */
-	const double4 *sbb;       /* boxes in sorted order */
+	const double4_32a *sbb;   /* boxes in sorted order */
 	int n;                    /* dynamic shapes */
 };
 
 __device__ __forceinline__ BB gshape_bb(const cpgSet &s, int g) { return bbnew(s.bbl[g], s.bbb[g], s.bbr[g], s.bbt[g]); }
 
-/* Visit every candidate of sorted shape i: static-tree hits, then sweep
- * hits.  f(a, b) receives world-local shape indices. */
+/* Static-tree hits of sorted shape i (one thread). */
 template<class F>
-__device__ void sap_visit(const cpgSet &s, const cpgWorld &W, const cpgTree &T, const SapCtx &c, int i, F f)
+__device__ void sap_static(const cpgSet &s, const cpgWorld &W, const cpgTree &T, const SapCtx &c, int i, F f)
 {
+	if(T.statRoot < 0) return;
 	int sa = c.vals[i];
-	int ga = W.shapeOff + sa;
-	BB ba = gshape_bb(s, ga);
-	/* static tree query (cpBBTree.c:352-363 SubtreeQuery), depth-first */
-	if(T.statRoot >= 0){
-		const cpgNode *nodes = s.nodes + W.nodeOff;
-		int stack[64];
-		int sp = 0;
-		stack[sp++] = T.statRoot;
-		while(sp > 0){
-			int nidx = stack[--sp];
-			const cpgNode &nd = nodes[nidx];
-			if(!bbintersects(bbnew(nd.l, nd.b, nd.r, nd.t), ba)) continue;
-			if(nd.obj >= 0){
-				if(bbintersects(ba, gshape_bb(s, W.shapeOff + nd.obj))) f(sa, nd.obj);
-			} else if(sp + 2 <= 64){
-				stack[sp++] = nd.B;
-				stack[sp++] = nd.A;
-			}
+	BB ba = gshape_bb(s, W.shapeOff + sa);
+	const cpgNode *nodes = s.nodes + W.nodeOff;
+	int stack[64];
+	int sp = 0;
+	stack[sp++] = T.statRoot;
+	while(sp > 0){
+		int nidx = stack[--sp];
+		const cpgNode &nd = nodes[nidx];
+		if(!bbintersects(bbnew(nd.l, nd.b, nd.r, nd.t), ba)) continue;
+		if(nd.obj >= 0){
+			if(bbintersects(ba, gshape_bb(s, W.shapeOff + nd.obj))) f(sa, nd.obj);
+		} else if(sp + 2 <= 64){
+			stack[sp++] = nd.B;
+			stack[sp++] = nd.A;
 		}
 	}
+}
+
+/* Sweep of sorted shape i by one warp: lane l tests box i+1+l, i+33+l, ...
+ * while keys stay <= the shape's high key (keys are sorted, so the first
+ * lane past the bound ends the sweep).  f(lane_rank, total, hit, a, b) is
+ * called once per 32-box window by every lane; hits are ranked in box
+ * order, so output positions are deterministic. */
+template<class F>
+__device__ void sap_sweep_warp(const SapCtx &c, int i, BB ba, int sa, F f)
+{
+	int lane = threadIdx.x & 31;
 	unsigned rk = c.rkeys[sa];
-	for(int j = i + 1; j < c.n && c.keys[j] <= rk; j++){
-		double4 bj = c.sbb[j];
-		if(bbintersects(ba, bbnew(bj.x, bj.y, bj.z, bj.w))) f(sa, c.vals[j]);
+	for(int j0 = i + 1; j0 < c.n; j0 += 32){
+		int j = j0 + lane;
+		bool inside = (j < c.n) && (c.keys[j] <= rk);
+		bool hit = false;
+		int sb = -1;
+		if(inside){
+			double4_32a bj = c.sbb[j];
+			hit = bbintersects(ba, bbnew(bj.x, bj.y, bj.z, bj.w));
+			if(hit) sb = c.vals[j];
+		}
+		unsigned hits = __ballot_sync(0xffffffffu, hit);
+		f(__popc(hits & ((1u << lane) - 1u)), __popc(hits), hit, sa, sb);
+		if(__ballot_sync(0xffffffffu, inside) != 0xffffffffu) break;
 	}
 }

@@ -1006,8 +1006,8 @@ __global__ void k_sap_gather(cpgSet s, int w)
 	int k = blockIdx.x*blockDim.x + threadIdx.x;
 	if(k >= W.ndynShapes) return;
 	int g = W.shapeOff + s.sortVA[k];
-	double4 b; b.x = s.bbl[g]; b.y = s.bbb[g]; b.z = s.bbr[g]; b.w = s.bbt[g];
-	((double4 *)s.sapBB)[k] = b;
+	double4_32a b; b.x = s.bbl[g]; b.y = s.bbb[g]; b.z = s.bbr[g]; b.w = s.bbt[g];
+	((double4_32a *)s.sapBB)[k] = b;
 }
 
 __device__ int arb_find(const cpgSet &s, unsigned long long key)
@@ -1022,15 +1022,24 @@ __device__ int arb_find(const cpgSet &s, unsigned long long key)
 	return -1;
 }
 
+/* One warp per sorted shape: lane 0 queries the static tree, all lanes
+ * sweep.  Count pass, then (after the scan) the emit pass writes the pairs
+ * at deterministic positions: static hits first, then sweep hits in box
+ * order. */
 __global__ void k_sap_count(cpgSet s, int w)
 {
 	const cpgWorld &W = s.world[w];
 	const cpgTree &T = s.tree[w];
-	SapCtx c; c.keys = s.sortKA; c.vals = s.sortVA; c.rkeys = s.rkeys; c.sbb = (const double4 *)s.sapBB; c.n = W.ndynShapes;
-	for(int i = blockIdx.x*blockDim.x + threadIdx.x; i < c.n; i += gridDim.x*blockDim.x){
+	SapCtx c; c.keys = s.sortKA; c.vals = s.sortVA; c.rkeys = s.rkeys; c.sbb = (const double4_32a *)s.sapBB; c.n = W.ndynShapes;
+	int lane = threadIdx.x & 31;
+	int nwarps = (gridDim.x*blockDim.x) >> 5;
+	for(int i = (blockIdx.x*blockDim.x + threadIdx.x) >> 5; i < c.n; i += nwarps){
 		unsigned cnt = 0;
-		sap_visit(s, W, T, c, i, [&](int, int){ cnt++; });
-		s.sapCount[i] = cnt;
+		if(lane == 0) sap_static(s, W, T, c, i, [&](int, int){ cnt++; });
+		int sa = c.vals[i];
+		BB ba = gshape_bb(s, W.shapeOff + sa);
+		sap_sweep_warp(c, i, ba, sa, [&](int, int total, bool, int, int){ cnt += (lane == 0) ? total : 0; });
+		if(lane == 0) s.sapCount[i] = cnt;
 	}
 	if(blockIdx.x == 0 && threadIdx.x == 0) s.sapCount[c.n] = 0;
 }
@@ -1039,32 +1048,37 @@ __global__ void k_sap_emit(cpgSet s, int w)
 {
 	const cpgWorld &W = s.world[w];
 	cpgTree &T = s.tree[w];
-	SapCtx c; c.keys = s.sortKA; c.vals = s.sortVA; c.rkeys = s.rkeys; c.sbb = (const double4 *)s.sapBB; c.n = W.ndynShapes;
+	SapCtx c; c.keys = s.sortKA; c.vals = s.sortVA; c.rkeys = s.rkeys; c.sbb = (const double4_32a *)s.sapBB; c.n = W.ndynShapes;
 	unsigned total = s.sapCount[c.n];
 	if(blockIdx.x == 0 && threadIdx.x == 0){
 		if(total > (unsigned)W.candCap){ T.error |= CPG_ERR_CANDS; T.ncand = W.candCap; }
 		else T.ncand = (int)total;
 		T.narb = 0;   /* the unordered compaction counts from zero */
 	}
-	for(int i = blockIdx.x*blockDim.x + threadIdx.x; i < c.n; i += gridDim.x*blockDim.x){
+	int lane = threadIdx.x & 31;
+	int nwarps = (gridDim.x*blockDim.x) >> 5;
+	for(int i = (blockIdx.x*blockDim.x + threadIdx.x) >> 5; i < c.n; i += nwarps){
 		unsigned pos = s.sapCount[i];
-		sap_visit(s, W, T, c, i, [&](int a, int b){
-			if(pos < (unsigned)W.candCap){
+		auto put = [&](unsigned p, int a, int b){
+			if(p < (unsigned)W.candCap){
 				cpgCand cd;
 				cd.a = a < b ? a : b; cd.b = a < b ? b : a; cd.pair = -1;
 				int slot = arb_find(s, arb_key(w, cd.a, cd.b));
 				cd.idIn = (slot >= 0) ? s.arbs[slot].gjk : 0u;
-				s.cands[W.candOff + pos] = cd;
+				s.cands[W.candOff + p] = cd;
 			}
-			pos++;
+		};
+		if(lane == 0) sap_static(s, W, s.tree[w], c, i, [&](int a, int b){ put(pos, a, b); pos++; });
+		pos = __shfl_sync(0xffffffffu, pos, 0);
+		int sa = c.vals[i];
+		BB ba = gshape_bb(s, W.shapeOff + sa);
+		sap_sweep_warp(c, i, ba, sa, [&](int rank, int tot, bool hit, int a, int b){
+			if(hit) put(pos + rank, a, b);
+			pos += tot;
 		});
 	}
 }
 
-/* 24 hashed priority bits above the unit's id (bits 56-63 hold the
- * round).  The id is the unit's candidate index (joints follow the
- * candidates), which does not depend on the order of the unordered
- * compaction, so the colouring is the same on every run. */
 __device__ __forceinline__ unsigned long long unit_priority(int key)
 {
 	return (mix64((unsigned long long)key + 0x9e3779b97f4a7c15ull) & 0x00ffffff00000000ull) | (unsigned)key;
@@ -1287,9 +1301,9 @@ extern "C" int cpg_launch_step(const cpgSet *s, const cpgSet *h, int mode, void 
 			int *tv = va; va = vb; vb = tv;
 		}
 		LAUNCH(k_sap_gather<<<blocks_for(n, 256), 256, 0, st>>>(*s, 0));
-		LAUNCH(k_sap_count<<<blocks_for(n, 128), 128, 0, st>>>(*s, 0));
+		LAUNCH(k_sap_count<<<blocks_for(32*n, 256), 256, 0, st>>>(*s, 0));
 		LAUNCH(k_scan_excl<<<1, 1024, 0, st>>>(s->sapCount, n + 1, NULL));
-		LAUNCH(k_sap_emit<<<blocks_for(n, 128), 128, 0, st>>>(*s, 0));
+		LAUNCH(k_sap_emit<<<blocks_for(32*n, 256), 256, 0, st>>>(*s, 0));
 	} else {
 		/* node pools of up to CPG_STAGED_NODES nodes (64 B each) run from
 		 * shared memory; larger worlds use the global pool */
