@@ -1611,7 +1611,14 @@ cpBool cpSpaceIsLocked(cpSpace *sp) { (void)sp; return cpFalse; }
 cpBool cpSpaceContainsShape(cpSpace *sp, cpShape *s) { return s->space == sp; }
 cpBool cpSpaceContainsBody(cpSpace *sp, cpBody *b) { return b->space == sp; }
 cpBool cpSpaceContainsConstraint(cpSpace *sp, cpConstraint *c) { return c->space == sp; }
-void cpGpuSetSolverMode(cpSpace *sp, int mode) { sp->mode = mode; }
+void cpGpuSetSolverMode(cpSpace *sp, int mode)
+{
+	if(mode < CP_GPU_SOLVER_ORDERED || mode > CP_GPU_SOLVER_COLORED){
+		set_error(CP_GPU_ERR_ARGUMENT, "unknown solver mode %d", mode);
+		return;
+	}
+	sp->mode = mode;
+}
 int cpGpuGetSolverMode(const cpSpace *sp) { return sp->mode; }
 
 cpBody *cpSpaceAddBody(cpSpace *sp, cpBody *b)

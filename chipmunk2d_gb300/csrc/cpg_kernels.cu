@@ -746,7 +746,9 @@ __device__ __forceinline__ void row_apply_cached(const cpgRow &row, BodyRef &A, 
 	if(row.kind == 0){
 		if(row.flags & ROW_FIRST) return;
 		double nx = row.arb.nx, ny = row.arb.ny;
-		for(int k = 0; k < row.count; k++){
+#pragma unroll
+		for(int k = 0; k < 2; k++){
+			if(k >= row.count) break;
 			const cpgRowContact &con = row.arb.c[k];
 			/* j = rotate(n, (jnAcc, jtAcc)) * dt_coef */
 			double jx = nx*con.jnAcc - ny*con.jtAcc, jy = nx*con.jtAcc + ny*con.jnAcc;
@@ -768,7 +770,9 @@ __device__ __forceinline__ void row_apply(cpgRow &row, BodyRef &A, BodyRef &B, d
 		double nx = row.arb.nx, ny = row.arb.ny;
 		double svx = row.arb.svx, svy = row.arb.svy;
 		double friction = row.arb.u;
-		for(int k = 0; k < row.count; k++){
+#pragma unroll
+		for(int k = 0; k < 2; k++){
+			if(k >= row.count) break;
 			cpgRowContact &con = row.arb.c[k];
 			double nMass = con.nMass;
 			double r1x = con.r1x, r1y = con.r1y, r2x = con.r2x, r2y = con.r2y;
@@ -841,6 +845,118 @@ __device__ __forceinline__ void solve_row(cpgRow *rows, int k, double *bodies, i
 	if(row.flags & ROW_DYN_B) store_pbody(bodies, row.b, B);
 }
 
+/* ---- four lanes per contact unit ----
+ * Within one contact the bias impulse reads and writes only bias
+ * velocities (v_bias, w_bias) and the normal and friction impulses only
+ * velocities (v, w) (cpArbiter.c:459-498).  A contact unit therefore splits
+ * into four independent parts, one per body and kind of velocity, and runs
+ * on four lanes: lane q of a quad takes side q & 1 (0: body a, 1: body b)
+ * and part q >> 1 (0: velocity, 1: bias velocity).  Each lane performs the
+ * reference's operations for its body and part in the reference's order;
+ * the two lanes of a part exchange contact-point velocities by shuffle;
+ * sign flips are exact (xor of the sign bit) and per-part choices are
+ * selects.  Results are bit-identical to one lane per unit.
+ *
+ * Why: FP64 issue is one warp instruction per 64 cycles per SM
+ * sub-partition whatever the number of active lanes, so a sweep level
+ * costs its FP64 instruction count per warp: about 40 per contact here
+ * against about 90 with one lane per unit.  Joint rows run on lane 0. */
+struct QuadRow {
+	int body, flags, kind, count;
+	double nx, ny, u, svx, svy;
+	double rx[2], ry[2], nMass[2], tMass[2], c[2], acc[2], jt[2];
+};
+
+__device__ __forceinline__ double dneg_if(double x, bool f)
+{
+	long long b = __double_as_longlong(x);
+	return __longlong_as_double(f ? (b ^ (long long)0x8000000000000000ull) : b);
+}
+
+__device__ __forceinline__ void quad_load(QuadRow &q, const cpgRow &row, int lane4)
+{
+	bool side = (lane4 & 1) != 0, bias = (lane4 & 2) != 0;
+	q.kind = row.kind; q.flags = row.flags; q.count = row.count;
+	q.body = side ? row.b : row.a;
+	if(q.kind != 0) return;
+	q.nx = row.arb.nx; q.ny = row.arb.ny; q.u = row.arb.u; q.svx = row.arb.svx; q.svy = row.arb.svy;
+#pragma unroll
+	for(int k = 0; k < 2; k++){
+		if(k >= q.count) break;
+		const cpgRowContact &c = row.arb.c[k];
+		q.rx[k] = side ? c.r2x : c.r1x; q.ry[k] = side ? c.r2y : c.r1y;
+		q.nMass[k] = c.nMass; q.tMass[k] = c.tMass;
+		q.c[k] = bias ? c.bias : c.bounce;
+		q.acc[k] = bias ? c.jBias : c.jnAcc;
+		q.jt[k] = c.jtAcc;
+	}
+}
+
+/* Warm start (pass 0: cpArbiter.c:441-455) or one iteration of a contact
+ * row held in registers; accumulators go back to *row. */
+template<bool CG>
+__device__ __forceinline__ void quad_apply(const QuadRow &q, cpgRow *row, double *bodies, int pass, double dt_coef, unsigned qmask, int lane4)
+{
+	bool side = (lane4 & 1) != 0, bias = (lane4 & 2) != 0;
+	if(pass == 0 && ((q.flags & ROW_FIRST) || bias)) return;
+	bool dyn = (q.flags & (side ? ROW_DYN_B : ROW_DYN_A)) != 0;
+	double *base = bodies + 8*(size_t)q.body;
+	double *bp = base + (bias ? 3 : 0);
+	double vx, vy, w, minv, iinv;
+	if(CG){ vx = __ldcg(bp); vy = __ldcg(bp + 1); w = __ldcg(bp + 2); minv = __ldcg(base + 6); iinv = __ldcg(base + 7); }
+	else { vx = bp[0]; vy = bp[1]; w = bp[2]; minv = base[6]; iinv = base[7]; }
+	double nx = q.nx, ny = q.ny;
+	if(pass == 0){
+#pragma unroll
+		for(int k = 0; k < 2; k++){
+			if(k >= q.count) break;
+			/* j = rotate(n, (jnAcc, jtAcc)) * dt_coef, negated for body a */
+			double jx = nx*q.acc[k] - ny*q.jt[k], jy = nx*q.jt[k] + ny*q.acc[k];
+			jx = dneg_if(jx*dt_coef, !side); jy = dneg_if(jy*dt_coef, !side);
+			vx = vx + jx*minv;
+			vy = vy + jy*minv;
+			w += iinv*(q.rx[k]*jy - q.ry[k]*jx);
+		}
+	} else {
+#pragma unroll
+		for(int k = 0; k < 2; k++){
+			if(k >= q.count) break;
+			double rx = q.rx[k], ry = q.ry[k];
+			/* contact-point velocity of this lane's body, then of the other */
+			double px = vx + (-ry)*w, py = vy + rx*w;
+			double ox = __shfl_xor_sync(qmask, px, 1), oy = __shfl_xor_sync(qmask, py, 1);
+			double v1x = side ? ox : px, v1y = side ? oy : py;
+			double v2x = side ? px : ox, v2y = side ? py : oy;
+			double dx = v2x - v1x, dy = v2y - v1y;
+			double sx = dx + q.svx, sy = dy + q.svy;
+			double vrx = bias ? dx : sx, vry = bias ? dy : sy;
+			double vn = vrx*nx + vry*ny;
+			double vt = vrx*(-ny) + vry*nx;
+			/* velocity: jn = -(bounce + vrn)*nMass; bias: jbn = (bias - vbn)*nMass */
+			double y = q.c[k] + dneg_if(vn, bias);
+			double j = dneg_if(y, !bias)*q.nMass[k];
+			double old = q.acc[k];
+			double acc = dmax(old + j, 0.0);
+			/* friction (used by the velocity lanes only) */
+			double jtMax = q.u*acc;
+			double jt = -vt*q.tMass[k];
+			double jtOld = q.jt[k];
+			double jtAcc = dclamp(jtOld + jt, -jtMax, jtMax);
+			double d = acc - old, djt = jtAcc - jtOld;
+			double ax = nx*d, ay = ny*d;
+			double nxj = ax - ny*djt, nyj = nx*djt + ay;
+			double jx = bias ? ax : nxj, jy = bias ? ay : nyj;
+			jx = dneg_if(jx, !side); jy = dneg_if(jy, !side);
+			vx = vx + jx*minv;
+			vy = vy + jy*minv;
+			w += iinv*(rx*jy - ry*jx);
+			if(lane4 == 0){ row->arb.c[k].jnAcc = acc; row->arb.c[k].jtAcc = jtAcc; }
+			else if(lane4 == 2){ row->arb.c[k].jBias = acc; }
+		}
+	}
+	if(dyn){ bp[0] = vx; bp[1] = vy; bp[2] = w; }
+}
+
 extern __shared__ double sbody[];
 
 /* Warm start (pass 0) and `iterations` sweeps, level by level; one block
@@ -864,11 +980,17 @@ __global__ void k_solve(cpgSet s, int stagedMax)
 	double *bodies = staged ? sbody : gb;
 	const int *start = s.levelStart + W.unitOff + w;
 	cpgRow *rows = s.rows + W.unitOff;
+	int lane4 = threadIdx.x & 3, nq = blockDim.x >> 2;
+	unsigned qmask = 0xFu << (threadIdx.x & 28);
 	for(int pass = 0; pass <= P.iterations; pass++){
 		for(int l = 0; l < nlev; l++){
 			int e = start[l + 1];
-			for(int k = start[l] + threadIdx.x; k < e; k += blockDim.x)
-				solve_row<false>(rows, k, bodies, pass, P.dt_coef, P.dt);
+			for(int k = start[l] + (threadIdx.x >> 2); k < e; k += nq){
+				QuadRow q;
+				quad_load(q, rows[k], lane4);
+				if(q.kind == 0) quad_apply<false>(q, rows + k, bodies, pass, P.dt_coef, qmask, lane4);
+				else if(lane4 == 0) solve_row<false>(rows, k, bodies, pass, P.dt_coef, P.dt);
+			}
 			__syncthreads();
 		}
 	}
@@ -1170,32 +1292,62 @@ __global__ void k_color_coop(cpgSet s, int w)
 	}
 }
 
+/* 96 quads per block: the quad-lane solve holds its next row in registers
+ * (about 170 per thread, so 384 threads fill the register file) */
+#define CPG_COOP_SOLVE_THREADS 384
+
 /* Levels (ordered mode) or colours (coloured mode) of one large world,
  * with the whole grid: grid.sync() between levels.  Packed body state is
  * read past the L1 (__ldcg), since other blocks write it between syncs;
- * a row is always handled by the same thread, so its own updates are
- * coherent. */
-__global__ void k_solve_coop(cpgSet s, int w)
+ * a row is always handled by the same quad of lanes, in one SM, so its own
+ * accumulator updates are coherent. */
+__global__ void __launch_bounds__(CPG_COOP_SOLVE_THREADS, 1) k_solve_coop(cpgSet s, int w)
 {
 	cg::grid_group grid = cg::this_grid();
 	const cpgParams &P = s.params[w];
 	const cpgWorld &W = s.world[w];
 	const cpgTree &T = s.tree[w];
 	int nunits = T.nunits, nlev = T.nlevels;
-	if(nunits > W.unitCap) return;
+	if(nunits > W.unitCap || nlev < 1) return;
 	const int *start = s.levelStart + W.unitOff + w;
 	cpgRow *rows = s.rows + W.unitOff;
 	double *bodies = s.pbody + 8*(size_t)W.bodyOff;
-	/* a level's units are dealt round-robin over the blocks (unit i to
-	 * block i % gridDim.x), so every SM's FP64 pipe gets a share: FP64 is
-	 * slow on this part (about 64 cycles per dependent operation) and a
-	 * level stacked on a few SMs would queue there */
-	int lane_id = threadIdx.x*gridDim.x + blockIdx.x, gsz = gridDim.x*blockDim.x;
-	for(int pass = 0; pass <= P.iterations; pass++){
+	int iters = P.iterations;
+	double dt_coef = P.dt_coef, dt = P.dt;
+	/* four lanes per unit; a level's units are dealt round-robin over the
+	 * blocks (unit i to block i % gridDim.x), so that every SM's FP64 pipes
+	 * take a share of each level */
+	int lane4 = threadIdx.x & 3;
+	int quad = (threadIdx.x >> 2)*gridDim.x + blockIdx.x, nq = (gridDim.x*blockDim.x) >> 2;
+	unsigned qmask = 0xFu << (threadIdx.x & 28);
+	/* the quad's first unit of the next level is read before the barrier,
+	 * so that only the body loads remain after it */
+	QuadRow q;
+	int k = start[0] + quad;
+	bool have = k < start[1];
+	if(have) quad_load(q, rows[k], lane4);
+	for(int pass = 0; pass <= iters; pass++){
 		for(int l = 0; l < nlev; l++){
 			int e = start[l + 1];
-			for(int k = start[l] + lane_id; k < e; k += gsz)
-				solve_row<true>(rows, k, bodies, pass, P.dt_coef, P.dt);
+			if(have){
+				if(q.kind == 0) quad_apply<true>(q, rows + k, bodies, pass, dt_coef, qmask, lane4);
+				else if(lane4 == 0) solve_row<true>(rows, k, bodies, pass, dt_coef, dt);
+				/* levels wider than the grid */
+				for(int k2 = k + nq; k2 < e; k2 += nq){
+					QuadRow q2;
+					quad_load(q2, rows[k2], lane4);
+					if(q2.kind == 0) quad_apply<true>(q2, rows + k2, bodies, pass, dt_coef, qmask, lane4);
+					else if(lane4 == 0) solve_row<true>(rows, k2, bodies, pass, dt_coef, dt);
+				}
+			}
+			int nl = l + 1, np = pass;
+			if(nl == nlev){ nl = 0; np++; }
+			k = start[nl] + quad;
+			have = np <= iters && k < start[nl + 1];
+			/* with a single level the next row is the one just written by
+			 * lanes 0 and 2 of this quad */
+			__syncwarp(qmask);
+			if(have) quad_load(q, rows[k], lane4);
 			grid.sync();
 		}
 	}
@@ -1240,8 +1392,13 @@ static cudaError_t launch_coop(const void *kernel, int threads, cpgSet *s, int w
 {
 	/* one block per SM: the fewer blocks a grid barrier waits for, the
 	 * cheaper it is, and a colour rarely has more units than threads */
-	static int blocks_solve = 0, blocks_color = 0;
-	int *cache = (kernel == (const void *)k_solve_coop) ? &blocks_solve : &blocks_color;
+	static const void *kernels[8];
+	static int blocks[8];
+	int slot = 0;
+	while(slot < 8 && kernels[slot] && kernels[slot] != kernel) slot++;
+	if(slot == 8) return cudaErrorInvalidValue;
+	kernels[slot] = kernel;
+	int *cache = &blocks[slot];
 	if(!*cache){
 		int most = coop_blocks(kernel, threads);
 		int sms = 0, dev = 0;
@@ -1335,7 +1492,7 @@ extern "C" int cpg_launch_step(const cpgSet *s, const cpgSet *h, int mode, void 
 	LAUNCH(k_integrate_vel<<<blocks_for(h->totalBodies, 128), 128, 0, st>>>(*s));
 	if(timing) cudaEventRecord(ev[6], st);
 	if(W == 1 && (colored || h->hostUnitsHint >= CPG_COOP_UNITS)){
-		launch_coop((const void *)k_solve_coop, 512, &sv, 0, st);
+		launch_coop((const void *)k_solve_coop, CPG_COOP_SOLVE_THREADS, &sv, 0, st);
 	} else {
 		int stagedMax = h->hostMaxBodies <= CPG_STAGED_BODIES ? h->hostMaxBodies : 0;
 		size_t smem = (size_t)stagedMax*8*sizeof(double);

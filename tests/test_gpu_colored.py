@@ -94,3 +94,14 @@ def test_colored_runs_are_deterministic(gpu_lib):
     finally:
         a.free()
         b.free()
+
+
+def test_solver_mode_rejects_unknown_values(gpu_lib):
+    sc = Scene(gpu_lib, 1, 14)
+    try:
+        gpu_lib.cpGpuGetLastError()
+        gpu_lib.cpGpuSetSolverMode(sc.space, 7)
+        assert gpu_lib.cpGpuGetLastError() == 6
+        assert gpu_lib.cpGpuGetSolverMode(sc.space) == 0
+    finally:
+        sc.free()
