@@ -328,7 +328,7 @@ static size_t carve_set(cpgSet *d, char *base, int pass)
 	CARVE(rsHist, unsigned, 256*(NS/2048 + 2));
 	CARVE(sortVA, int, NS); CARVE(sortVB, int, NS);
 	CARVE(claim, unsigned long long, NB); CARVE(cmask, unsigned long long, NB);
-	CARVE(colorCursor, int, 256);
+	CARVE(colorCursor, int, 512);
 	CARVE(sapBB, double, 4*NS);
 	CARVE(sapStats, double, 8);
 	CARVE(stats, int, 16);
@@ -1904,10 +1904,13 @@ int cpGpuGetStepStats(cpSpace *sp, int *out, int max)
 {
 	if(!sp || !sp->dev || max < 1) return 0;
 	DevSet *ds = sp->dev;
-	cudaStreamSynchronize(lib_stream());
 	/* the stats block of the last step: error flags, pair/node use (per
 	 * mille of capacity), live arbiters, candidates, solved arbiters,
-	 * sweep levels or colours, candidate use (per mille) */
+	 * sweep levels or colours, candidate use (per mille); the step's own
+	 * asynchronous read-back may be older */
+	check_stats(ds);
+	if(!d2h(ds->hstats, ds->d.stats, sizeof(int)*16)) return 0;
+	cudaStreamSynchronize(lib_stream());
 	int n = max < 8 ? max : 8;
 	for(int i = 0; i < n; i++) out[i] = ds->hstats[i];
 	return n;

@@ -132,14 +132,14 @@ typedef struct cpgArb {
 	unsigned stamp;
 	int world;
 	unsigned gjk;                 /* last GJK feature id of the pair */
-	int pad;
+	int colorTag;                 /* coloured mode: valid bit, low 23 bits of the colouring step's stamp, colour */
 	double nx, ny, e, u, svx, svy;
 	cpgContact c[2];
 } cpgArb;
 
 /* Joint (cpPivotJoint/cpPinJoint/cpSlideJoint), one record per joint. */
 typedef struct cpgJoint {
-	int kind, a, b, pad;
+	int kind, a, b, colorTag;     /* colorTag: as in cpgArb */
 	double ax, ay, bx, by;        /* anchors in body space */
 	double maxForce, biasCoef, maxBias;
 	double dist, min, max;
@@ -261,7 +261,7 @@ typedef struct cpgSet {
 	unsigned *sortKA, *sortKB, *rkeys, *sapCount, *rsHist;
 	int *sortVA, *sortVB;
 	unsigned long long *claim, *cmask;   /* [totalBodies] */
-	int *colorCursor;             /* [256] */
+	int *colorCursor;             /* [512]: [0..1] colouring round counters, [8] sweep axis, [256..511] colour counts */
 	double *sapBB;                /* [4*totalShapes] boxes in sweep order */
 	double *sapStats;             /* [8] axis statistics */
 	int hostNdyn;                 /* dynamic shapes of world 0 (host value) */

@@ -330,6 +330,7 @@ __global__ void k_arb_update(cpgSet s)
 			arb.state = CPG_ARB_FIRST;
 			arb.stamp = 0;
 			arb.world = w;
+			arb.colorTag = 0;     /* no colour yet */
 			arb.svx = 0.0; arb.svy = 0.0; arb.e = 0.0; arb.u = 0.0;
 		}
 		int ga = W.shapeOff + ia, gb = W.shapeOff + ib;
@@ -1207,24 +1208,61 @@ __device__ __forceinline__ unsigned long long unit_priority(int key)
 }
 
 #define CPG_COLOR_ROUNDS 128
+/* every this many steps all units are coloured afresh */
+#define CPG_RECOLOR_PERIOD 64
 
-/* Jones-Plassmann rounds with hashed priorities; the lowest colour free on
- * both bodies.  Then a counting sort of units by colour. */
+/* Colour tag kept in an arbiter's or joint's colorTag word: valid bit, the low
+ * 23 bits of the stamp of the step that coloured it, the colour (< 64). */
+__device__ __forceinline__ unsigned color_tag(unsigned stamp, int c)
+{
+	return 0x80000000u | ((stamp & 0x7FFFFFu) << 8) | (unsigned)c;
+}
+
+__device__ __forceinline__ int *unit_pad(const cpgSet &s, const cpgWorld &W, int narb, int u)
+{
+	return (u < narb) ? &s.arbs[s.arbList[W.candOff + u]].colorTag : &s.joints[W.consOff + (u - narb)].colorTag;
+}
+
+/* Units that were units of the previous step keep their colour (a subset
+ * of a proper colouring is proper); the others are coloured by
+ * Jones-Plassmann rounds with hashed priorities, each taking the lowest
+ * colour free on both of its bodies.  Every CPG_RECOLOR_PERIOD steps all
+ * units are coloured afresh, which bounds the drift of the colour count.
+ * Then a counting sort of units by colour (empty colours dropped), with
+ * per-block histograms so that each colour's counter takes one atomic per
+ * block. */
 __global__ void k_color_coop(cpgSet s, int w)
 {
 	cg::grid_group grid = cg::this_grid();
+	__shared__ unsigned shHist[256], shBase[256];
+	const cpgParams &P = s.params[w];
 	const cpgWorld &W = s.world[w];
 	cpgTree &T = s.tree[w];
-	int n = T.nunits, nb = W.nbodies;
+	int n = T.nunits, nb = W.nbodies, narb = T.narb;
 	int gtid = threadIdx.x*gridDim.x + blockIdx.x, gsz = gridDim.x*blockDim.x;
 	const int *ua = s.unitA + W.unitOff, *ub = s.unitB + W.unitOff;
 	const int *ukey = s.unitKey + W.unitOff;
 	int *color = s.unitLevel + W.unitOff;
 	unsigned long long *claim = s.claim + W.bodyOff, *cmask = s.cmask + W.bodyOff;
-	int *counter = s.colorCursor;   /* [0],[1]: remaining per round parity; [2]: colours */
+	int *counter = s.colorCursor;   /* [0],[1]: remaining units per round parity */
+	bool reuse = (P.stamp % CPG_RECOLOR_PERIOD) != 0;
+	unsigned prevTag = color_tag(P.stamp - 1u, 0);
 	for(int b = gtid; b < nb; b += gsz){ cmask[b] = 0ull; claim[b] = ~0ull; }
-	for(int u = gtid; u < n; u += gsz) color[u] = -1;
-	if(gtid == 0){ counter[0] = 0; counter[1] = 0; counter[2] = 0; }
+	if(gtid == 0){ counter[0] = 0; counter[1] = 0; }
+	grid.sync();
+	for(int u = gtid; u < n; u += gsz){
+		int c = -1;
+		if(reuse){
+			unsigned tag = (unsigned)*unit_pad(s, W, narb, u);
+			if((tag & 0xFFFFFF00u) == prevTag) c = (int)(tag & 0xFFu);
+		}
+		color[u] = c;
+		if(c >= 0){
+			/* kept units on one body have distinct colours */
+			if(ua[u] >= 0) atomicOr(&cmask[ua[u]], 1ull << c);
+			if(ub[u] >= 0) atomicOr(&cmask[ub[u]], 1ull << c);
+		}
+	}
 	grid.sync();
 	for(int round = 0; round < CPG_COLOR_ROUNDS; round++){
 		/* claims carry the round in their top byte, newer rounds smaller,
@@ -1252,43 +1290,65 @@ __global__ void k_color_coop(cpgSet s, int w)
 					if(a >= 0) cmask[a] = __ldcg(&cmask[a]) | (1ull << c);
 					if(b >= 0) cmask[b] = __ldcg(&cmask[b]) | (1ull << c);
 				}
-				atomicMax(&counter[2], c + 1);
 			} else {
 				remaining++;
 			}
 		}
-		if(remaining) atomicAdd(&counter[round & 1], remaining);
+		remaining = __reduce_add_sync(0xffffffffu, remaining);
+		if((threadIdx.x & 31) == 0 && remaining) atomicAdd(&counter[round & 1], remaining);
 		if(gtid == 0) counter[(round + 1) & 1] = 0;
 		grid.sync();
 		if(__ldcg(&counter[round & 1]) == 0) break;
 	}
+	/* counting sort by colour: colours past 63 come only from exhausted
+	 * masks (64 + round), 255 marks a unit the rounds left uncoloured */
+	for(int c = threadIdx.x; c < 256; c += blockDim.x) shHist[c] = 0u;
+	__syncthreads();
+	for(int u = gtid; u < n; u += gsz){
+		int c = color[u];
+		if(c < 0 || c > 255){ c = 255; atomicOr(&T.error, CPG_ERR_LEVELS); }
+		atomicAdd(&shHist[c], 1u);
+	}
+	__syncthreads();
+	unsigned *gHist = (unsigned *)s.colorCursor + 256;   /* [256] colour counts */
+	if(blockIdx.x == 0) for(int c = threadIdx.x; c < 256; c += blockDim.x) gHist[c] = 0u;
 	grid.sync();
-	/* counting sort by colour (order within a colour is irrelevant: its
-	 * units share no body) */
-	int ncol = __ldcg(&counter[2]);
+	for(int c = threadIdx.x; c < 256; c += blockDim.x)
+		shBase[c] = shHist[c] ? atomicAdd(&gHist[c], shHist[c]) : 0u;
+	grid.sync();
+	/* levels over the non-empty colours; every block derives the same
+	 * offsets from the counts */
 	int *start = s.levelStart + W.unitOff + w;
+	__shared__ int shLevel[256], shStart[256], shN;
+	if(threadIdx.x == 0){
+		int lev = 0, acc = 0;
+		for(int c = 0; c < 256; c++){
+			unsigned cnt = __ldcg(&gHist[c]);
+			if(cnt){ shLevel[c] = lev; shStart[c] = acc; acc += (int)cnt; lev++; }
+			else shLevel[c] = -1;
+		}
+		shN = lev;
+	}
+	__syncthreads();
+	int nlev = shN;
+	if(blockIdx.x == 0){
+		for(int c = threadIdx.x; c < 256; c += blockDim.x)
+			if(shLevel[c] >= 0) start[shLevel[c]] = shStart[c];
+		if(threadIdx.x == 0){
+			start[nlev] = n;
+			T.nlevels = nlev;
+			if(nlev > T.maxChain) T.maxChain = nlev;
+		}
+	}
+	for(int c = threadIdx.x; c < 256; c += blockDim.x) shHist[c] = 0u;
+	__syncthreads();
 	int *order = s.unitOrder + W.unitOff;
-	int *cursor = s.colorCursor + 4;
-	for(int c = gtid; c <= ncol; c += gsz) start[c] = 0;
-	grid.sync();
+	unsigned newTagBase = color_tag(P.stamp, 0);
 	for(int u = gtid; u < n; u += gsz){
 		int c = color[u];
-		if(c < 0) c = ncol - 1;    /* rounds exhausted: the error flag marks it */
-		atomicAdd(&start[c + 1], 1);
-	}
-	grid.sync();
-	if(gtid == 0){
-		int acc = 0;
-		for(int c = 0; c < ncol; c++){ acc += __ldcg(&start[c + 1]); start[c + 1] = acc; }
-		for(int c = 0; c < ncol; c++) cursor[c] = start[c];
-		T.nlevels = ncol;
-		if(ncol > T.maxChain) T.maxChain = ncol;
-	}
-	grid.sync();
-	for(int u = gtid; u < n; u += gsz){
-		int c = color[u];
-		if(c < 0){ c = ncol - 1; T.error |= CPG_ERR_LEVELS; }
-		order[atomicAdd(&cursor[c], 1)] = u;
+		if(c < 0 || c > 255) c = 255;
+		order[shStart[c] + shBase[c] + atomicAdd(&shHist[c], 1u)] = u;
+		*unit_pad(s, W, narb, u) = (int)(c < 64 ? (newTagBase | (unsigned)c) : 0u);
 	}
 }
 

@@ -105,3 +105,40 @@ def test_solver_mode_rejects_unknown_values(gpu_lib):
         assert gpu_lib.cpGpuGetSolverMode(sc.space) == 0
     finally:
         sc.free()
+
+
+def test_colour_reuse_stays_deterministic_across_recolouring(gpu_lib):
+    """Units that were units of the previous step keep their colour; every
+    64th step colours all units afresh.  A unit kept with a colour another
+    unit of its body also holds would race in the solve, so bit-identical
+    runs over both kinds of step show the colouring stays proper."""
+    a = colored(gpu_lib, 2, 20000)
+    b = colored(gpu_lib, 2, 20000)
+    try:
+        for chunk in range(3):
+            a.step(1 / 60, 50)
+            b.step(1 / 60, 50)
+            assert gpu_lib.cpGpuGetLastError() == 0, gpu_lib.cpGpuGetLastErrorString()
+            np.testing.assert_array_equal(a.bodies(), b.bodies(), err_msg="after %d steps" % (50 * chunk + 50))
+    finally:
+        a.free()
+        b.free()
+
+
+def test_colour_count_with_reuse_stays_near_fresh_colouring(gpu_lib):
+    sc = colored(gpu_lib, 2, 20000)
+    stats = np.zeros(8, dtype=np.int32)
+    try:
+        sc.step(1 / 60, 128)          # the 128th step colours afresh
+        gpu_lib.cpGpuGetStepStats(sc.space, stats.ctypes.data, 8)
+        fresh = int(stats[6])
+        worst = 0
+        for _ in range(40):
+            sc.step(1 / 60)
+            gpu_lib.cpGpuGetStepStats(sc.space, stats.ctypes.data, 8)
+            worst = max(worst, int(stats[6]))
+        assert gpu_lib.cpGpuGetLastError() == 0
+        assert 2 <= fresh <= 16, fresh
+        assert worst <= fresh + 3, (fresh, worst)
+    finally:
+        sc.free()
