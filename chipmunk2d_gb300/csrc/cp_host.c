@@ -325,12 +325,13 @@ static size_t carve_set(cpgSet *d, char *base, int pass)
 	CARVE(dynShapes, int, NS);
 	CARVE(sortKA, unsigned, NS); CARVE(sortKB, unsigned, NS); CARVE(rkeys, unsigned, NS);
 	CARVE(sapCount, unsigned, NS + 1);
-	CARVE(rsHist, unsigned, 256*(NS/2048 + 2));
+	CARVE(rsHist, unsigned, 256*CPG_SORT_MAX_BLOCKS + 256);
+	CARVE(sortK64, unsigned long long, NS);
 	CARVE(sortVA, int, NS); CARVE(sortVB, int, NS);
 	CARVE(claim, unsigned long long, NB); CARVE(cmask, unsigned long long, NB);
 	CARVE(colorCursor, int, 512);
-	CARVE(sapBB, double, 4*NS);
-	CARVE(sapStats, double, 8);
+	CARVE(sapBB, long long, 4*NS);
+	CARVE(sapPart, float, 4*CPG_SORT_MAX_BLOCKS);
 	CARVE(stats, int, 16);
 	return total;
 }

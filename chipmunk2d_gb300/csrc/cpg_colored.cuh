@@ -2,8 +2,9 @@
  * cpg_colored.cuh -- the graph-coloured solver mode for large spaces.
  *
  * Broadphase: sweep-and-prune over the dynamic shapes.  Each shape's AABB
- * left edge, rounded down to float, is the sort key (LSD radix sort, 8-bit
- * digits, stable multi-block).  The sweep from shape i visits the following
+ * left edge, rounded down to float, is the sort key; the order (key, shape
+ * index) is repaired from the previous step's or rebuilt by a stable radix
+ * sort (k_sap_sort).  The sweep from shape i visits the following
  * shapes while their key is <= i's right edge rounded up, and keeps the
  * pairs whose double-precision boxes intersect (cpBBIntersects, cpBB.h:47).
  * Rounding the keys outward keeps the sweep exact: a pair whose boxes
@@ -28,29 +29,10 @@
 
 namespace cg = cooperative_groups;
 
-#define RS_THREADS 256
-#define RS_ITEMS 8
-#define RS_TILE (RS_THREADS*RS_ITEMS)
-
 __device__ __forceinline__ unsigned float_order_key(float f)
 {
 	unsigned u = __float_as_uint(f);
 	return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
-}
-
-/* Per-digit counts of one tile; hist is digit-major: hist[d*nblocks + b]. */
-__global__ void k_rs_hist(const unsigned *keys, int n, int shift, unsigned *hist)
-{
-	__shared__ unsigned h[256];
-	h[threadIdx.x] = 0;
-	__syncthreads();
-	int base = blockIdx.x*RS_TILE;
-	for(int k = 0; k < RS_ITEMS; k++){
-		int i = base + k*RS_THREADS + threadIdx.x;
-		if(i < n) atomicAdd(&h[(keys[i] >> shift) & 0xFF], 1u);
-	}
-	__syncthreads();
-	hist[threadIdx.x*gridDim.x + blockIdx.x] = h[threadIdx.x];
 }
 
 /* Exclusive scan of `n` counts by one block. */
@@ -89,54 +71,43 @@ __global__ void k_scan_excl(unsigned *data, int n, unsigned *total)
 	if(threadIdx.x == 0 && total) *total = carry;
 }
 
-/* Stable scatter of one tile: item order is round-major, then thread. */
-__global__ void k_rs_scatter(const unsigned *kin, const int *vin, unsigned *kout, int *vout, int n, int shift, const unsigned *hist)
+/* ---- sweep-and-prune ----
+ *
+ * Box tests run on ordered integer images of the doubles: -0 is folded to
+ * +0 and negative values have their magnitude bits inverted, so that
+ * okey(a) <= okey(b) exactly when a <= b for every non-NaN pair.  The
+ * cpBBIntersects test (cpBB.h:47) then takes integer compares instead of
+ * FP64 compares, which issue at a small fraction of the integer rate on
+ * this part. */
+__device__ __forceinline__ long long okey(double x)
 {
-	__shared__ unsigned base[256];
-	__shared__ unsigned roundTotal[256];
-	__shared__ unsigned warpCount[RS_THREADS/32][256];
-	int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-	base[threadIdx.x] = hist[threadIdx.x*gridDim.x + blockIdx.x];
-	int tile = blockIdx.x*RS_TILE;
-	for(int k = 0; k < RS_ITEMS; k++){
-		for(int w = 0; w < RS_THREADS/32; w++) warpCount[w][threadIdx.x] = 0;
-		__syncthreads();
-		int i = tile + k*RS_THREADS + threadIdx.x;
-		bool valid = i < n;
-		unsigned key = valid ? kin[i] : 0u;
-		unsigned d = valid ? ((key >> shift) & 0xFF) : 256u;
-		unsigned peers = __match_any_sync(0xffffffffu, d);
-		unsigned rank = __popc(peers & ((1u << lane) - 1u));
-		if(valid && rank == 0) warpCount[warp][d] = __popc(peers);
-		__syncthreads();
-		{
-			unsigned s = 0;
-			for(int w = 0; w < RS_THREADS/32; w++){ unsigned t = warpCount[w][threadIdx.x]; warpCount[w][threadIdx.x] = s; s += t; }
-			roundTotal[threadIdx.x] = s;
-		}
-		__syncthreads();
-		if(valid){
-			unsigned pos = base[d] + warpCount[warp][d] + rank;
-			kout[pos] = key;
-			vout[pos] = vin[i];
-		}
-		__syncthreads();
-		base[threadIdx.x] += roundTotal[threadIdx.x];
-		__syncthreads();
-	}
+	long long b = __double_as_longlong(x);
+	if(b == (long long)0x8000000000000000ull) b = 0;
+	return b < 0 ? (b ^ 0x7FFFFFFFFFFFFFFFll) : b;
 }
 
-/* ---- sweep-and-prune ---- */
+struct KBB { long long l, b, r, t; };
+
+__device__ __forceinline__ KBB kbb(double l, double b, double r, double t)
+{
+	KBB k; k.l = okey(l); k.b = okey(b); k.r = okey(r); k.t = okey(t);
+	return k;
+}
+
+__device__ __forceinline__ bool kbb_intersects(const KBB &a, const KBB &b)
+{
+	return a.l <= b.r && b.l <= a.r && a.b <= b.t && b.b <= a.t;
+}
 
 struct SapCtx {
 	const unsigned *keys;     /* sorted left-edge keys */
 	const int *vals;          /* sorted shape indices (world-local) */
 	const unsigned *rkeys;    /* right-edge keys by shape */
-	const double4_32a *sbb;   /* boxes in sorted order */
+	const longlong4_32a *sbb; /* box keys (okey of l, b, r, t) in sorted order */
 	int n;                    /* dynamic shapes */
 };
 
-__device__ __forceinline__ BB gshape_bb(const cpgSet &s, int g) { return bbnew(s.bbl[g], s.bbb[g], s.bbr[g], s.bbt[g]); }
+__device__ __forceinline__ KBB gshape_kbb(const cpgSet &s, int g) { return kbb(s.bbl[g], s.bbb[g], s.bbr[g], s.bbt[g]); }
 
 /* Static-tree hits of sorted shape i (one thread). */
 template<class F>
@@ -144,7 +115,7 @@ __device__ void sap_static(const cpgSet &s, const cpgWorld &W, const cpgTree &T,
 {
 	if(T.statRoot < 0) return;
 	int sa = c.vals[i];
-	BB ba = gshape_bb(s, W.shapeOff + sa);
+	KBB ba = gshape_kbb(s, W.shapeOff + sa);
 	const cpgNode *nodes = s.nodes + W.nodeOff;
 	int stack[64];
 	int sp = 0;
@@ -152,9 +123,9 @@ __device__ void sap_static(const cpgSet &s, const cpgWorld &W, const cpgTree &T,
 	while(sp > 0){
 		int nidx = stack[--sp];
 		const cpgNode &nd = nodes[nidx];
-		if(!bbintersects(bbnew(nd.l, nd.b, nd.r, nd.t), ba)) continue;
+		if(!kbb_intersects(kbb(nd.l, nd.b, nd.r, nd.t), ba)) continue;
 		if(nd.obj >= 0){
-			if(bbintersects(ba, gshape_bb(s, W.shapeOff + nd.obj))) f(sa, nd.obj);
+			if(kbb_intersects(ba, gshape_kbb(s, W.shapeOff + nd.obj))) f(sa, nd.obj);
 		} else if(sp + 2 <= 64){
 			stack[sp++] = nd.B;
 			stack[sp++] = nd.A;
@@ -168,7 +139,7 @@ __device__ void sap_static(const cpgSet &s, const cpgWorld &W, const cpgTree &T,
  * called once per 32-box window by every lane; hits are ranked in box
  * order, so output positions are deterministic. */
 template<class F>
-__device__ void sap_sweep_warp(const SapCtx &c, int i, BB ba, int sa, F f)
+__device__ void sap_sweep_warp(const SapCtx &c, int i, const KBB &ba, int sa, F f)
 {
 	int lane = threadIdx.x & 31;
 	unsigned rk = c.rkeys[sa];
@@ -178,8 +149,9 @@ __device__ void sap_sweep_warp(const SapCtx &c, int i, BB ba, int sa, F f)
 		bool hit = false;
 		int sb = -1;
 		if(inside){
-			double4_32a bj = c.sbb[j];
-			hit = bbintersects(ba, bbnew(bj.x, bj.y, bj.z, bj.w));
+			longlong4_32a bj = c.sbb[j];
+			KBB kb; kb.l = bj.x; kb.b = bj.y; kb.r = bj.z; kb.t = bj.w;
+			hit = kbb_intersects(ba, kb);
 			if(hit) sb = c.vals[j];
 		}
 		unsigned hits = __ballot_sync(0xffffffffu, hit);

@@ -33,6 +33,9 @@ enum { CPG_ARB_FIRST = 0, CPG_ARB_NORMAL = 1, CPG_ARB_IGNORE = 2, CPG_ARB_CACHED
 /* error bits latched in cpgTree.error */
 enum { CPG_ERR_NODES = 1, CPG_ERR_PAIRS = 2, CPG_ERR_CANDS = 4, CPG_ERR_ARBS = 8, CPG_ERR_BINS = 16, CPG_ERR_LEVELS = 32 };
 
+/* upper bound on the blocks of the cooperative sweep-and-prune sort */
+#define CPG_SORT_MAX_BLOCKS 1024
+
 #define CPG_KEY_EMPTY 0ull
 #define CPG_KEY_TOMB 1ull
 
@@ -258,12 +261,13 @@ typedef struct cpgSet {
 
 	/* coloured mode (single-world sets) */
 	int *dynShapes;               /* [totalShapes] shapes on non-static bodies */
-	unsigned *sortKA, *sortKB, *rkeys, *sapCount, *rsHist;
+	unsigned *sortKA, *sortKB, *rkeys, *sapCount, *rsHist;   /* rsHist: [256*CPG_SORT_MAX_BLOCKS + 256] */
+	unsigned long long *sortK64;  /* [totalShapes] (key << 32 | shape) in the previous sweep order */
 	int *sortVA, *sortVB;
 	unsigned long long *claim, *cmask;   /* [totalBodies] */
-	int *colorCursor;             /* [512]: [0..1] colouring round counters, [8] sweep axis, [256..511] colour counts */
-	double *sapBB;                /* [4*totalShapes] boxes in sweep order */
-	double *sapStats;             /* [8] axis statistics */
+	int *colorCursor;             /* [512]: [0..1] colouring round counters, [8] sweep axis, [10] n+1 once a sweep order exists, [11] its axis, [16..31] transposition swap counters, [256..511] colour counts */
+	long long *sapBB;             /* [4*totalShapes] box keys in sweep order */
+	float *sapPart;               /* [4*CPG_SORT_MAX_BLOCKS] per-block centre sums for the sweep axis */
 	int hostNdyn;                 /* dynamic shapes of world 0 (host value) */
 	int hostUnitsHint;            /* solver units of world 0 last step (host value) */
 	int hostMaxBodies;            /* largest world (host value) */

@@ -1082,57 +1082,215 @@ __global__ void k_gather_arbs(cpgSet s, int w, cpgArb *out, int n)
 
 /* Sweep axis: the one along which the shape centres spread more (their
  * variance), so that a sweep visits fewer boxes.  One block. */
-__global__ void k_sap_axis(cpgSet s, int w)
+/* ---- sweep order: one cooperative launch per step ----
+ *
+ * The sweep order is the dynamic shapes sorted by (left-edge key, shape
+ * index), a unique order.  Between steps it barely changes, so the keys
+ * are first recomputed in the previous order as 64-bit (key << 32 | shape)
+ * values and repaired by odd-even transposition rounds (compare-exchange
+ * of (2i, 2i+1), then of (2i+1, 2i+2)); a round with no exchange leaves the
+ * keys sorted.  When SAP_REPAIR_ROUNDS rounds do not finish (first step,
+ * axis change, fast motion), a stable LSD radix sort by the 32-bit key from
+ * shape-index order gives the same order.  Then the boxes are gathered in
+ * sweep order, and the sweep axis for the next step is chosen: the axis
+ * along which box centres have the larger variance (FP32 sums per block
+ * in a fixed order, then over blocks in block order, so the choice is
+ * deterministic).  Any axis gives the same pair set. */
+#define SAP_THREADS 256
+#define SAP_REPAIR_ROUNDS 8
+
+__device__ __forceinline__ unsigned sap_lo_key(const cpgSet &s, int g, int axis)
 {
+	return float_order_key(__double2float_rd(axis ? s.bbb[g] : s.bbl[g]));
+}
+
+__device__ __forceinline__ unsigned sap_hi_key(const cpgSet &s, int g, int axis)
+{
+	return float_order_key(__double2float_ru(axis ? s.bbt[g] : s.bbr[g]));
+}
+
+/* One stable LSD pass over 8 bits with the whole grid: block histograms,
+ * per-digit prefixes over blocks (one warp per digit), digit bases, then a
+ * stable scatter of each block's contiguous range in sub-tiles.  Data other
+ * blocks wrote in this launch is read with __ldcg. */
+__device__ void sap_radix_pass(cg::grid_group &grid, const unsigned *kin, const int *vin, unsigned *kout, int *vout,
+	int n, int shift, unsigned *hist, unsigned *rowTot)
+{
+	__shared__ unsigned shHist[256], shBase[256], shTot[256];
+	__shared__ unsigned shWarp[SAP_THREADS/32][256];
+	int nblk = gridDim.x, b = blockIdx.x, tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+	int per = (n + nblk - 1)/nblk;
+	int lo = b*per, hi = min(n, lo + per);
+	shHist[tid] = 0u;
+	for(int w2 = 0; w2 < SAP_THREADS/32; w2++) shWarp[w2][tid] = 0u;
+	__syncthreads();
+	for(int i = lo + tid; i < hi; i += SAP_THREADS) atomicAdd(&shHist[(__ldcg(&kin[i]) >> shift) & 0xFFu], 1u);
+	__syncthreads();
+	hist[tid*nblk + b] = shHist[tid];
+	grid.sync();
+	int gw = (b*SAP_THREADS + tid) >> 5, nw = (nblk*SAP_THREADS) >> 5;
+	for(int d = gw; d < 256; d += nw){
+		unsigned carry = 0u;
+		for(int c0 = 0; c0 < nblk; c0 += 32){
+			int j = c0 + lane;
+			unsigned v = (j < nblk) ? __ldcg(&hist[d*nblk + j]) : 0u;
+			unsigned x = v;
+			for(int o = 1; o < 32; o <<= 1){
+				unsigned y = __shfl_up_sync(0xffffffffu, x, o);
+				if(lane >= o) x += y;
+			}
+			if(j < nblk) hist[d*nblk + j] = carry + x - v;
+			carry += __shfl_sync(0xffffffffu, x, 31);
+		}
+		if(lane == 0) rowTot[d] = carry;
+	}
+	grid.sync();
+	/* digit bases: exclusive scan of the 256 totals (every block) */
+	{
+		unsigned v = __ldcg(&rowTot[tid]);
+		unsigned x = v;
+		for(int o = 1; o < 32; o <<= 1){
+			unsigned y = __shfl_up_sync(0xffffffffu, x, o);
+			if(lane >= o) x += y;
+		}
+		if(lane == 31) shTot[warp] = x;
+		__syncthreads();
+		unsigned wp = 0u;
+		for(int w2 = 0; w2 < warp; w2++) wp += shTot[w2];
+		shBase[tid] = wp + x - v + __ldcg(&hist[tid*nblk + b]);
+		__syncthreads();
+	}
+	for(int t0 = lo; t0 < hi; t0 += SAP_THREADS){
+		int i = t0 + tid;
+		bool valid = i < hi;
+		unsigned key = valid ? __ldcg(&kin[i]) : 0u;
+		unsigned d = valid ? ((key >> shift) & 0xFFu) : 256u;
+		unsigned peers = __match_any_sync(0xffffffffu, d);
+		unsigned rank = __popc(peers & ((1u << lane) - 1u));
+		if(valid && rank == 0) shWarp[warp][d] = __popc(peers);
+		__syncthreads();
+		{
+			unsigned acc = 0u;
+			for(int w2 = 0; w2 < SAP_THREADS/32; w2++){ unsigned t = shWarp[w2][tid]; shWarp[w2][tid] = acc; acc += t; }
+			shTot[tid] = acc;
+		}
+		__syncthreads();
+		if(valid){
+			unsigned pos = shBase[d] + shWarp[warp][d] + rank;
+			kout[pos] = key;
+			vout[pos] = __ldcg(&vin[i]);
+		}
+		__syncthreads();
+		shBase[tid] += shTot[tid];
+		for(int w2 = 0; w2 < SAP_THREADS/32; w2++) shWarp[w2][tid] = 0u;
+		__syncthreads();
+	}
+	grid.sync();
+}
+
+__global__ void __launch_bounds__(SAP_THREADS) k_sap_sort(cpgSet s, int w)
+{
+	cg::grid_group grid = cg::this_grid();
+	__shared__ float red[4][SAP_THREADS/32];
 	const cpgWorld &W = s.world[w];
-	__shared__ double red[4][32];
-	double sx = 0, sxx = 0, sy = 0, syy = 0;
-	for(int k = threadIdx.x; k < W.ndynShapes; k += blockDim.x){
-		int g = W.shapeOff + s.dynShapes[W.dynShapeOff + k];
-		double cx = 0.5*(s.bbl[g] + s.bbr[g]), cy = 0.5*(s.bbb[g] + s.bbt[g]);
+	int n = W.ndynShapes;
+	int gtid = blockIdx.x*SAP_THREADS + threadIdx.x, gsz = gridDim.x*SAP_THREADS;
+	int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+	int *cc = s.colorCursor;
+	int axis = cc[8];
+	bool have = (cc[10] == n + 1) && (cc[11] == axis);
+	unsigned long long *K = s.sortK64;
+	unsigned *KA = s.sortKA;
+	int *VA = s.sortVA;
+	if(gtid < 2*SAP_REPAIR_ROUNDS) cc[16 + gtid] = 0;
+	grid.sync();
+	bool sorted = false;
+	if(have){
+		for(int i = gtid; i < n; i += gsz){
+			int sh = VA[i];
+			int g = W.shapeOff + sh;
+			K[i] = ((unsigned long long)sap_lo_key(s, g, axis) << 32) | (unsigned)sh;
+			s.rkeys[sh] = sap_hi_key(s, g, axis);
+		}
+		grid.sync();
+		for(int round = 0; round < SAP_REPAIR_ROUNDS && !sorted; round++){
+			for(int phase = 0; phase < 2; phase++){
+				int swaps = 0;
+				for(int j = gtid; 2*j + phase + 1 < n; j += gsz){
+					int a = 2*j + phase;
+					unsigned long long ka = __ldcg(&K[a]), kb = __ldcg(&K[a + 1]);
+					if(ka > kb){ K[a] = kb; K[a + 1] = ka; swaps++; }
+				}
+				swaps = __reduce_add_sync(0xffffffffu, swaps);
+				if(lane == 0 && swaps) atomicAdd(&cc[16 + 2*round + phase], swaps);
+				grid.sync();
+			}
+			sorted = (__ldcg(&cc[16 + 2*round]) == 0) && (__ldcg(&cc[16 + 2*round + 1]) == 0);
+		}
+		if(sorted){
+			for(int i = gtid; i < n; i += gsz){
+				unsigned long long k = __ldcg(&K[i]);
+				KA[i] = (unsigned)(k >> 32);
+				VA[i] = (int)(unsigned)(k & 0xFFFFFFFFull);
+			}
+		}
+	}
+	if(!sorted){
+		for(int k = gtid; k < n; k += gsz){
+			int sh = s.dynShapes[W.dynShapeOff + k];
+			int g = W.shapeOff + sh;
+			KA[k] = sap_lo_key(s, g, axis);
+			VA[k] = sh;
+			s.rkeys[sh] = sap_hi_key(s, g, axis);
+		}
+		grid.sync();
+		unsigned *hist = s.rsHist, *rowTot = s.rsHist + 256*CPG_SORT_MAX_BLOCKS;
+		sap_radix_pass(grid, s.sortKA, s.sortVA, s.sortKB, s.sortVB, n, 0, hist, rowTot);
+		sap_radix_pass(grid, s.sortKB, s.sortVB, s.sortKA, s.sortVA, n, 8, hist, rowTot);
+		sap_radix_pass(grid, s.sortKA, s.sortVA, s.sortKB, s.sortVB, n, 16, hist, rowTot);
+		sap_radix_pass(grid, s.sortKB, s.sortVB, s.sortKA, s.sortVA, n, 24, hist, rowTot);
+	} else {
+		grid.sync();
+	}
+	/* boxes in sweep order, and the centre sums for the next axis */
+	float sx = 0.0f, sxx = 0.0f, sy = 0.0f, syy = 0.0f;
+	for(int k = gtid; k < n; k += gsz){
+		int g = W.shapeOff + __ldcg(&VA[k]);
+		double l = s.bbl[g], b = s.bbb[g], r = s.bbr[g], t = s.bbt[g];
+		longlong4_32a kb4;
+		kb4.x = okey(l); kb4.y = okey(b); kb4.z = okey(r); kb4.w = okey(t);
+		((longlong4_32a *)s.sapBB)[k] = kb4;
+		float cx = 0.5f*((float)l + (float)r), cy = 0.5f*((float)b + (float)t);
 		sx += cx; sxx += cx*cx; sy += cy; syy += cy*cy;
 	}
 	for(int o = 16; o > 0; o >>= 1){
 		sx += __shfl_down_sync(0xffffffffu, sx, o); sxx += __shfl_down_sync(0xffffffffu, sxx, o);
 		sy += __shfl_down_sync(0xffffffffu, sy, o); syy += __shfl_down_sync(0xffffffffu, syy, o);
 	}
-	int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
 	if(lane == 0){ red[0][warp] = sx; red[1][warp] = sxx; red[2][warp] = sy; red[3][warp] = syy; }
 	__syncthreads();
 	if(threadIdx.x == 0){
-		double a = 0, b = 0, c = 0, d = 0;
-		for(int i = 0; i < (int)(blockDim.x >> 5); i++){ a += red[0][i]; b += red[1][i]; c += red[2][i]; d += red[3][i]; }
-		double n = W.ndynShapes > 0 ? (double)W.ndynShapes : 1.0;
-		double vx = b/n - (a/n)*(a/n), vy = d/n - (c/n)*(c/n);
-		s.colorCursor[8] = (vy > vx) ? 1 : 0;
+		float a = 0.0f, bb = 0.0f, c = 0.0f, d = 0.0f;
+		for(int i = 0; i < SAP_THREADS/32; i++){ a += red[0][i]; bb += red[1][i]; c += red[2][i]; d += red[3][i]; }
+		float *part = s.sapPart + 4*blockIdx.x;
+		part[0] = a; part[1] = bb; part[2] = c; part[3] = d;
+	}
+	grid.sync();
+	if(gtid == 0){
+		float a = 0.0f, bb = 0.0f, c = 0.0f, d = 0.0f;
+		for(int i = 0; i < (int)gridDim.x; i++){
+			const float *part = s.sapPart + 4*i;
+			a += __ldcg(part); bb += __ldcg(part + 1); c += __ldcg(part + 2); d += __ldcg(part + 3);
+		}
+		float nn = n > 0 ? (float)n : 1.0f;
+		float vx = bb/nn - (a/nn)*(a/nn), vy = d/nn - (c/nn)*(c/nn);
+		cc[8] = (vy > vx) ? 1 : 0;
+		cc[10] = n + 1;
+		cc[11] = axis;
 	}
 }
 
-__global__ void k_sap_keys(cpgSet s, int w)
-{
-	const cpgWorld &W = s.world[w];
-	int k = blockIdx.x*blockDim.x + threadIdx.x;
-	if(k >= W.ndynShapes) return;
-	int axis = s.colorCursor[8];
-	int sh = s.dynShapes[W.dynShapeOff + k];
-	int g = W.shapeOff + sh;
-	double lo = axis ? s.bbb[g] : s.bbl[g], hi = axis ? s.bbt[g] : s.bbr[g];
-	s.sortKA[k] = float_order_key(__double2float_rd(lo));
-	s.sortVA[k] = sh;
-	s.rkeys[sh] = float_order_key(__double2float_ru(hi));
-}
-
-/* Boxes in sweep order, so that a sweep reads consecutive records. */
-__global__ void k_sap_gather(cpgSet s, int w)
-{
-	const cpgWorld &W = s.world[w];
-	int k = blockIdx.x*blockDim.x + threadIdx.x;
-	if(k >= W.ndynShapes) return;
-	int g = W.shapeOff + s.sortVA[k];
-	double4_32a b; b.x = s.bbl[g]; b.y = s.bbb[g]; b.z = s.bbr[g]; b.w = s.bbt[g];
-	((double4_32a *)s.sapBB)[k] = b;
-}
-
+/* Slot of an arbiter key in the open-addressing table, or -1. */
 __device__ int arb_find(const cpgSet &s, unsigned long long key)
 {
 	unsigned mask = (unsigned)s.arbCap - 1;
@@ -1153,14 +1311,14 @@ __global__ void k_sap_count(cpgSet s, int w)
 {
 	const cpgWorld &W = s.world[w];
 	const cpgTree &T = s.tree[w];
-	SapCtx c; c.keys = s.sortKA; c.vals = s.sortVA; c.rkeys = s.rkeys; c.sbb = (const double4_32a *)s.sapBB; c.n = W.ndynShapes;
+	SapCtx c; c.keys = s.sortKA; c.vals = s.sortVA; c.rkeys = s.rkeys; c.sbb = (const longlong4_32a *)s.sapBB; c.n = W.ndynShapes;
 	int lane = threadIdx.x & 31;
 	int nwarps = (gridDim.x*blockDim.x) >> 5;
 	for(int i = (blockIdx.x*blockDim.x + threadIdx.x) >> 5; i < c.n; i += nwarps){
 		unsigned cnt = 0;
 		if(lane == 0) sap_static(s, W, T, c, i, [&](int, int){ cnt++; });
 		int sa = c.vals[i];
-		BB ba = gshape_bb(s, W.shapeOff + sa);
+		KBB ba = gshape_kbb(s, W.shapeOff + sa);
 		sap_sweep_warp(c, i, ba, sa, [&](int, int total, bool, int, int){ cnt += (lane == 0) ? total : 0; });
 		if(lane == 0) s.sapCount[i] = cnt;
 	}
@@ -1171,7 +1329,7 @@ __global__ void k_sap_emit(cpgSet s, int w)
 {
 	const cpgWorld &W = s.world[w];
 	cpgTree &T = s.tree[w];
-	SapCtx c; c.keys = s.sortKA; c.vals = s.sortVA; c.rkeys = s.rkeys; c.sbb = (const double4_32a *)s.sapBB; c.n = W.ndynShapes;
+	SapCtx c; c.keys = s.sortKA; c.vals = s.sortVA; c.rkeys = s.rkeys; c.sbb = (const longlong4_32a *)s.sapBB; c.n = W.ndynShapes;
 	unsigned total = s.sapCount[c.n];
 	if(blockIdx.x == 0 && threadIdx.x == 0){
 		if(total > (unsigned)W.candCap){ T.error |= CPG_ERR_CANDS; T.ncand = W.candCap; }
@@ -1194,7 +1352,7 @@ __global__ void k_sap_emit(cpgSet s, int w)
 		if(lane == 0) sap_static(s, W, s.tree[w], c, i, [&](int a, int b){ put(pos, a, b); pos++; });
 		pos = __shfl_sync(0xffffffffu, pos, 0);
 		int sa = c.vals[i];
-		BB ba = gshape_bb(s, W.shapeOff + sa);
+		KBB ba = gshape_kbb(s, W.shapeOff + sa);
 		sap_sweep_warp(c, i, ba, sa, [&](int rank, int tot, bool hit, int a, int b){
 			if(hit) put(pos + rank, a, b);
 			pos += tot;
@@ -1505,19 +1663,7 @@ extern "C" int cpg_launch_step(const cpgSet *s, const cpgSet *h, int mode, void 
 	if(timing) cudaEventRecord(ev[1], st);
 	if(colored){
 		int n = h->hostNdyn;
-		int nb = blocks_for(n, RS_TILE);
-		LAUNCH(k_sap_axis<<<1, 1024, 0, st>>>(*s, 0));
-		LAUNCH(k_sap_keys<<<blocks_for(n, 256), 256, 0, st>>>(*s, 0));
-		unsigned *ka = s->sortKA, *kb = s->sortKB;
-		int *va = s->sortVA, *vb = s->sortVB;
-		for(int pass = 0; pass < 4; pass++){
-			LAUNCH(k_rs_hist<<<nb, RS_THREADS, 0, st>>>(ka, n, 8*pass, s->rsHist));
-			LAUNCH(k_scan_excl<<<1, 1024, 0, st>>>(s->rsHist, 256*nb, NULL));
-			LAUNCH(k_rs_scatter<<<nb, RS_THREADS, 0, st>>>(ka, va, kb, vb, n, 8*pass, s->rsHist));
-			unsigned *tk = ka; ka = kb; kb = tk;
-			int *tv = va; va = vb; vb = tv;
-		}
-		LAUNCH(k_sap_gather<<<blocks_for(n, 256), 256, 0, st>>>(*s, 0));
+		launch_coop((const void *)k_sap_sort, SAP_THREADS, &sv, 0, st);
 		LAUNCH(k_sap_count<<<blocks_for(32*n, 256), 256, 0, st>>>(*s, 0));
 		LAUNCH(k_scan_excl<<<1, 1024, 0, st>>>(s->sapCount, n + 1, NULL));
 		LAUNCH(k_sap_emit<<<blocks_for(32*n, 256), 256, 0, st>>>(*s, 0));
