@@ -170,6 +170,7 @@ _GPU_API = {
     "cpGpuDebugSetBodies": (I, [P, P, I]),
     "cpGpuDebugCandidates": (I, [P, P, I]),
     "cpGpuSetTiming": (None, [I]),
+    "cpGpuDebugSetWholeGridSolve": (None, [I]),
     "cpGpuGetPhaseTimes": (I, [P, P, I]),
     "cpGpuGetStepStats": (I, [P, P, I]),
     "cpGpuGetLaunchCount": (ctypes.c_longlong, [I]),

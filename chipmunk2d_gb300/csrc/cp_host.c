@@ -218,6 +218,7 @@ struct DevSet {
 	int paramRecorded[CPG_PARAM_RING];
 	int paramSlot;
 	int *hstats;              /* pinned */
+	double *hbodies;          /* pinned staging for body downloads */
 	cudaEvent_t statsEvent;
 	int statsPending;
 	int stepsSinceCheck;      /* steps enqueued since the stats were last read */
@@ -232,6 +233,7 @@ struct DevSet {
 static cudaStream_t g_stream = NULL;
 static int g_stream_user = 0;
 static int g_timing = 0;
+static int g_whole_grid = 0;     /* 1: single-world sets always use the whole-grid solve */
 
 static cudaStream_t lib_stream(void)
 {
@@ -241,6 +243,7 @@ static cudaStream_t lib_stream(void)
 
 void cpGpuSetStream(void *stream) { g_stream = (cudaStream_t)stream; g_stream_user = (stream != NULL); }
 void cpGpuSetTiming(int enabled) { g_timing = enabled; }
+void cpGpuDebugSetWholeGridSolve(int always) { g_whole_grid = always ? 1 : 0; }
 long long cpGpuGetLaunchCount(int reset) { return cpg_launch_count(reset); }
 
 static const int kPrimes[] = {
@@ -402,13 +405,25 @@ static void download_bodies(DevSet *ds)
 {
 	cpgSet *d = &ds->d;
 	int NB = d->totalBodies;
-	double *buf = HALLOC(double, 18*NB);
-	double *f[18];
-	for(int k = 0; k < 18; k++) f[k] = buf + (size_t)k*NB;
-	double *src[18] = { d->px, d->py, d->vx, d->vy, d->fx, d->fy, d->ang, d->w, d->tq,
+	/* px .. wb are carved back to back (each padded to 256 bytes), so one
+	 * copy into the pinned staging block brings all eighteen arrays */
+	size_t stride = (size_t)(d->py - d->px);
+	size_t bytes = (size_t)((char *)(d->wb + NB) - (char *)d->px);
+	if(!ds->hbodies){
+		if(!cuda_ok(cudaMallocHost((void **)&ds->hbodies, 18*stride*sizeof(double)), "cudaMallocHost")){ ds->hbodies = NULL; return; }
+	}
+	const double *src[18] = { d->px, d->py, d->vx, d->vy, d->fx, d->fy, d->ang, d->w, d->tq,
 		d->ta, d->tb, d->tc, d->td, d->ttx, d->tty, d->vbx, d->vby, d->wb };
-	for(int k = 0; k < 18; k++) d2h(f[k], src[k], sizeof(double)*(size_t)NB);
+	int contiguous = 1;
+	for(int k = 0; k < 18; k++) contiguous &= (src[k] == d->px + (size_t)k*stride);
+	if(contiguous){
+		if(!d2h(ds->hbodies, d->px, bytes)) return;
+	} else {
+		for(int k = 0; k < 18; k++) if(!d2h(ds->hbodies + (size_t)k*stride, src[k], sizeof(double)*(size_t)NB)) return;
+	}
 	cuda_ok(cudaStreamSynchronize(lib_stream()), "download bodies");
+	const double *f[18];
+	for(int k = 0; k < 18; k++) f[k] = ds->hbodies + (size_t)k*stride;
 	for(int w = 0; w < ds->nspaces; w++){
 		cpSpace *sp = ds->spaces[w];
 		int off = ds->hworld[w].bodyOff;
@@ -421,7 +436,6 @@ static void download_bodies(DevSet *ds)
 			b->v_bias = cpv(f[15][g], f[16][g]); b->w_bias = f[17][g];
 		}
 	}
-	free(buf);
 }
 
 static int upload_shapes(DevSet *ds, int w)
@@ -534,6 +548,7 @@ static void devset_free(DevSet *ds)
 	if(ds->gather) cudaFree(ds->gather);
 	if(ds->hparams) cudaFreeHost(ds->hparams);
 	if(ds->hstats) cudaFreeHost(ds->hstats);
+	if(ds->hbodies) cudaFreeHost(ds->hbodies);
 	if(ds->statsEvent) cudaEventDestroy(ds->statsEvent);
 	for(int i = 0; i < CPG_PARAM_RING; i++) if(ds->paramEvent[i]) cudaEventDestroy(ds->paramEvent[i]);
 	for(int w = 0; w < ds->nspaces; w++){
@@ -791,6 +806,7 @@ static int devset_step(DevSet *ds, const double *dts, cpSpace **only)
 		sp->snapValid = 0;
 	}
 	cudaStream_t st = lib_stream();
+	if(g_whole_grid) d->hostUnitsHint = 0x7fffffff;
 	if(!h2d(d->params, hp, sizeof(cpgParams)*(size_t)ds->nspaces)) return -1;
 	cudaEventRecord(ds->paramEvent[slot], st);
 	ds->paramRecorded[slot] = 1;

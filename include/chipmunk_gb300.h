@@ -493,6 +493,12 @@ int cpGpuDebugCandidates(cpSpace *space, int *out, int max);
  * Phases: 0 integrate+cache, 1 broadphase, 2 narrowphase, 3 arbiters,
  * 4 schedule, 5 prestep+warmstart, 6 solve. */
 void cpGpuSetTiming(int enabled);
+/* Debug: 1 makes single-world sets always solve with the whole-grid
+ * kernel (a grid barrier between levels), 0 restores the automatic choice
+ * (whole grid when a world's levels average at least 64 units and it has
+ * at least 2048).  Both give the same results; the parity tests use this
+ * to cover the whole-grid path on small worlds. */
+void cpGpuDebugSetWholeGridSolve(int always);
 /* Bookkeeping of the last step (after it completes): [0] error flags,
  * [1] pair-pool use and [2] node-pool use (per mille of capacity, largest
  * world), [3] live cached arbiters, [4] candidate pairs, [5] solved

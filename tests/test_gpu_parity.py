@@ -80,6 +80,30 @@ def test_teacher_forced_per_step(gpu_lib, oracle_lib, name, cfg, size, dt, steps
 FREE_RUN_DRIFT = 1e-9
 
 
+@pytest.mark.parametrize("name,cfg,size,dt,steps", [CASES[0], CASES[1], CASES[2]], ids=["pyramid", "circles", "mixed"])
+def test_teacher_forced_whole_grid_solve(gpu_lib, oracle_lib, name, cfg, size, dt, steps):
+    """The whole-grid solve (four lanes per contact, a grid barrier between
+    levels), which large single worlds use, against the oracle."""
+    gpu_lib.cpGpuDebugSetWholeGridSolve(1)
+    try:
+        g = Scene(gpu_lib, cfg, size)
+        o = Scene(oracle_lib, cfg, size)
+        try:
+            worst = 0.0
+            for s in range(min(steps, 60)):
+                g.set_bodies(o.bodies())
+                g.step(dt)
+                o.step(dt)
+                check_gpu_error(gpu_lib)
+                worst = max(worst, *compare_step(g, o, s))
+            assert worst <= RTOL, worst
+        finally:
+            g.free()
+            o.free()
+    finally:
+        gpu_lib.cpGpuDebugSetWholeGridSolve(0)
+
+
 def test_pyramid_free_run_1000_steps(gpu_lib, oracle_lib):
     """The full 1000-step pyramid rollout as two independent runs.  The
     per-step contract (1e-12, teacher-forced tests above) holds; over a free
