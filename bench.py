@@ -283,7 +283,7 @@ def run_batch(args, emit=True):
     for sc in cw:
         sc.free()
 
-    names = ["integrate+cache", "broadphase tree", "narrowphase", "arbiters", "schedule", "prestep+velocity", "solve"]
+    names = PHASES
     line = {
         "metric": "world-steps/s", "value": world_steps, "unit": "world-steps/s", "n_gpus": 1,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000 * total_s / args.steps,
@@ -306,15 +306,21 @@ def run_batch(args, emit=True):
     return line
 
 
-def parity_mode_sample(lib, workload, steps, warmup):
-    """Device-timed steps of the exact reference-order mode (the drop-in's
-    default), for the JSON line's `ordered_mode` record."""
+PHASES = ["integrate+cache", "broadphase", "narrowphase", "arbiters", "schedule", "prestep+velocity", "solve"]
+
+
+def mode_sample(lib, workload, steps, warmup, mode=0, phases=False):
+    """Wall-timed steps of one workload in one solver mode (0: the exact
+    reference-order mode, the drop-in's default; 1: coloured), closed by a
+    device sync, for the JSON line's extra records."""
     import torch
     from chipmunk2d_gb300 import Scene
     cfg, size, dt, desc = WORKLOADS[workload]
     sc = Scene(lib, cfg, size)
+    lib.cpGpuSetSolverMode(sc.space, mode)
     for _ in range(warmup):
         lib.cpSpaceStep(sc.space, dt)
+    lib.cpGpuSpaceSync(sc.space)
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     for _ in range(steps):
@@ -322,10 +328,30 @@ def parity_mode_sample(lib, workload, steps, warmup):
     lib.cpGpuSpaceSync(sc.space)
     torch.cuda.synchronize()
     secs = time.perf_counter() - t0
-    n = sc.nbodies
+    err = lib.cpGpuGetLastError()
+    rec = {"workload": workload, "solver": "colored" if mode else "ordered", "bodies": sc.nbodies,
+           "shapes": sc.nshapes, "constraints": sc.nconstraints, "steps": steps, "warmup": warmup,
+           "body_steps_per_s": sc.nbodies * steps / secs, "ms_per_step": 1000 * secs / steps,
+           "description": desc}
+    if err:
+        rec["error"] = lib.cpGpuGetLastErrorString().decode()
+    if phases:
+        lib.cpGpuSetTiming(1)
+        buf, acc = np.zeros(8), np.zeros(7)
+        for _ in range(5):
+            lib.cpSpaceStep(sc.space, dt)
+            lib.cpGpuGetPhaseTimes(sc.space, buf.ctypes.data, 8)
+            acc += buf[:7]
+        lib.cpGpuSetTiming(0)
+        rec["phase_ms"] = dict(zip(PHASES, [round(float(x) / 5, 4) for x in acc]))
     sc.free()
-    return {"workload": workload, "bodies": n, "steps": steps, "body_steps_per_s": n * steps / secs,
-            "ms_per_step": 1000 * secs / steps}
+    return rec
+
+
+def parity_mode_sample(lib, workload, steps, warmup):
+    """The exact reference-order mode, for the `ordered_mode` record."""
+    rec = mode_sample(lib, workload, steps, warmup, mode=0)
+    return {k: rec[k] for k in ("workload", "bodies", "steps", "body_steps_per_s", "ms_per_step")}
 
 
 def run_ours(args):
@@ -430,7 +456,7 @@ def run_ours(args):
     e2e_value = n * e2e_steps * world_size / e2e_s
 
     # ---- roofline of the dominant phase ----
-    names = ["integrate+cache", "broadphase tree", "narrowphase", "arbiters", "schedule", "prestep+velocity", "solve"]
+    names = PHASES
     dom = int(np.argmax(phase))
     iters = 10 if cfg != 3 else 15
     algo = {
@@ -459,6 +485,9 @@ def run_ours(args):
         lib.cpGpuSetStream(ctypes.c_void_p(stream.cuda_stream))
         extras["ordered_mode"] = [parity_mode_sample(lib, "pyramid", 300, 5),
                                   parity_mode_sample(lib, "circles", 10, 3)]
+        # mixed shapes and pivot chains at full size (40,000 bodies)
+        extras["mixed"] = [mode_sample(lib, "mixed", 150, 150, mode=1, phases=True),
+                           mode_sample(lib, "mixed", 3, 2, mode=0)]
         b = run_batch(argparse.Namespace(steps=30, warmup=3), emit=False)
         extras["batch"] = {k: b[k] for k in ("value", "unit", "ms_per_step", "body_steps_per_s",
                                              "looped_plain_gpu_world_steps_per_s", "batched_over_looped",
@@ -479,7 +508,10 @@ def run_ours(args):
                 "path": "cpSpaceStep + cpBodyGetPosition/Velocity/Angle for every body (ctypes)"},
         "roofline": {"bound": "hbm", "kernel": names[dom], "achieved": achieved, "peak": peak,
                      "unit": "GB/s", "frac": achieved / peak, "peak_kind": peak_kind,
-                     "traffic": traffic, "algorithmic_bytes_per_launch": algo},
+                     "traffic": traffic, "algorithmic_bytes_per_launch": algo,
+                     "limiter": ("latency: one grid barrier, one round of L2 body loads and the dependent FP64 "
+                                 "chain per colour level; rows and bodies stay L2-resident" if names[dom] == "solve"
+                                 else "latency-bound gather")},
         "phase_ms": dict(zip(names, [round(float(x), 4) for x in phase])),
         "sweep_levels_final": sweep_levels,
         "gpu_launches": int(launches),
