@@ -200,18 +200,32 @@ BATCH_WORLDS = 4096
 BATCH_DT = 1 / 60
 
 
-def run_batch(args, emit=True):
+def run_batch(args, emit=True, sharded=True):
     """4096 tumble worlds with body counts log-uniform in [8, 512], stepped
-    together (cpGpuBatchStep, reference sweep order in every world)."""
+    together (cpGpuBatchStep, reference sweep order in every world).  Under
+    torchrun each rank steps its contiguous range of worlds (balanced on
+    body count, chipmunk2d_gb300.shard) as one batch on its own GPU: no
+    collective on the data path, a barrier around the timed steps and the
+    maximum of the ranks' times."""
     import ctypes
     import torch
     from chipmunk2d_gb300 import load_gpu_library, Scene
+    from chipmunk2d_gb300.shard import rank_range
+    world_size = int(os.environ.get("WORLD_SIZE", "1")) if sharded else 1
+    rank = int(os.environ.get("RANK", "0")) if sharded else 0
+    dist = None
+    if world_size > 1:
+        import torch.distributed as dist
+        torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+        if not dist.is_initialized():
+            dist.init_process_group("nccl")
     lib = load_gpu_library()
     stream = torch.cuda.Stream()
     lib.cpGpuSetStream(ctypes.c_void_p(stream.cuda_stream))
     sizes = batch_sizes(lib, BATCH_WORLDS)
+    lo, hi = rank_range(sizes, rank, world_size)
     t0 = time.perf_counter()
-    scenes = [Scene(lib, 4, sizes[i], seed=1000 + i) for i in range(BATCH_WORLDS)]
+    scenes = [Scene(lib, 4, sizes[i], seed=1000 + i) for i in range(lo, hi)]
     nb = sum(sc.nbodies for sc in scenes)
     batch = lib.cpGpuBatchNew()
     for sc in scenes:
@@ -221,8 +235,11 @@ def run_batch(args, emit=True):
     build_s = time.perf_counter() - t0
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
     lib.cpGpuGetLaunchCount(1)
-    clocks = ClockSampler(0)
+    clocks = ClockSampler(int(os.environ.get("LOCAL_RANK", "0")) if world_size > 1 else 0)
     clocks.start()
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
     ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
     for i in range(args.steps):
         with torch.cuda.stream(stream):
@@ -237,7 +254,22 @@ def run_batch(args, emit=True):
     if lib.cpGpuGetLastError():
         raise RuntimeError(lib.cpGpuGetLastErrorString().decode())
     total_s = sum(a.elapsed_time(b) for a, b in ev) / 1000.0
+    if dist:
+        t = torch.tensor([total_s], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total_s = float(t.item())
+        dist.barrier()
     world_steps = BATCH_WORLDS * args.steps / total_s
+    nb_total = nb
+    if dist:
+        t = torch.tensor([float(nb)], device="cuda")
+        dist.all_reduce(t)
+        nb_total = int(t.item())
+    if rank != 0:
+        lib.cpGpuBatchFree(batch)
+        for sc in scenes:
+            sc.free()
+        return None
     lib.cpGpuSetTiming(1)
     phase = np.zeros(8)
     buf = np.zeros(8)
@@ -285,14 +317,16 @@ def run_batch(args, emit=True):
 
     names = PHASES
     line = {
-        "metric": "world-steps/s", "value": world_steps, "unit": "world-steps/s", "n_gpus": 1,
+        "metric": "world-steps/s", "value": world_steps, "unit": "world-steps/s", "n_gpus": world_size,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000 * total_s / args.steps,
-        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": "batch", "worlds": BATCH_WORLDS, "bodies": nb,
+        "higher_is_better": True, "scaling": "strong", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": "batch", "worlds": BATCH_WORLDS, "bodies": nb_total,
                    "description": "4096 tumble worlds, bodies log-uniform in [8,512], 10 it, dt 1/60, seed 3",
                    "solver": "ordered (reference sweep order per world)", "build_s": build_s,
+                   "parallelism": ("worlds sharded over %d GPUs (contiguous ranges balanced on body count)" % world_size
+                                   if world_size > 1 else "single"),
                    "l2": "flushed between timed steps (256 MB fill, untimed)"},
-        "body_steps_per_s": nb * args.steps / total_s,
+        "body_steps_per_s": nb_total * args.steps / total_s,
         "looped_plain_gpu_world_steps_per_s": loop_ws,
         "batched_over_looped": world_steps / loop_ws,
         "phase_ms": dict(zip(names, [round(float(x), 4) for x in phase[:7]])),
@@ -488,7 +522,7 @@ def run_ours(args):
         # mixed shapes and pivot chains at full size (40,000 bodies)
         extras["mixed"] = [mode_sample(lib, "mixed", 150, 150, mode=1, phases=True),
                            mode_sample(lib, "mixed", 3, 2, mode=0)]
-        b = run_batch(argparse.Namespace(steps=30, warmup=3), emit=False)
+        b = run_batch(argparse.Namespace(steps=30, warmup=3), emit=False, sharded=False)
         extras["batch"] = {k: b[k] for k in ("value", "unit", "ms_per_step", "body_steps_per_s",
                                              "looped_plain_gpu_world_steps_per_s", "batched_over_looped",
                                              "cpu_baseline", "phase_ms")}
