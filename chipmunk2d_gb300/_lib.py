@@ -92,6 +92,7 @@ _API = {
     "cpBodyFree": (None, [P]),
     "cpBodyGetType": (I, [P]),
     "cpBodyGetMass": (D, [P]),
+    "cpBodySetMass": (None, [P, D]),
     "cpBodyGetMoment": (D, [P]),
     "cpBodyGetPosition": (V, [P]),
     "cpBodySetPosition": (None, [P, V]),
@@ -111,7 +112,9 @@ _API = {
     "cpShapeFree": (None, [P]),
     "cpShapeGetBB": (cpBB, [P]),
     "cpShapeSetFriction": (None, [P, D]),
+    "cpShapeGetFriction": (D, [P]),
     "cpShapeSetElasticity": (None, [P, D]),
+    "cpShapeGetElasticity": (D, [P]),
     "cpCircleShapeNew": (P, [P, D, V]),
     "cpSegmentShapeNew": (P, [P, V, V, D]),
     "cpPolyShapeNew": (P, [P, I, P, cpTransform, D]),
@@ -164,6 +167,8 @@ _GPU_API = {
     "cpGpuBatchFree": (None, [P]),
     "cpGpuBatchAddSpace": (I, [P, P]),
     "cpGpuBatchStep": (I, [P, D, I, I]),
+    "cpGpuRolloutForward": (I, [P, D, I, I]),
+    "cpGpuRolloutBackward": (I, [P, P, P, P, P, P, P]),
     "cpGpuDebugBodies": (I, [P, P, I]),
     "cpGpuDebugArbiters": (I, [P, P, I]),
     "cpGpuDebugConstraints": (I, [P, P, I]),

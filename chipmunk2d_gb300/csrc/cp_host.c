@@ -225,6 +225,7 @@ struct DevSet {
 	cpSpace **spaces;
 	int nspaces;
 	void *slab;
+	size_t slabBytes;
 	cpgArb *gather;           /* arbiter snapshot staging */
 	int gatherCap;
 };
@@ -629,6 +630,7 @@ static DevSet *devset_build(cpSpace **spaces, int nspaces)
 	d->arbCap = (int)arbCap;
 
 	size_t bytes = carve_set(d, NULL, 0);
+	ds->slabBytes = bytes;
 	if(!cuda_ok(cudaMalloc(&ds->slab, bytes), "cudaMalloc set")){ devset_free(ds); return NULL; }
 	carve_set(d, (char *)ds->slab, 1);
 	cudaStream_t st = lib_stream();
@@ -764,6 +766,15 @@ static void check_stats(DevSet *ds)
 	}
 }
 
+/* Upload what the host changed in world w since the last step. */
+static void devset_flush_space(DevSet *ds, int w)
+{
+	cpSpace *sp = ds->spaces[w];
+	if(sp->bodyDirty){ upload_bodies(ds, w); sp->bodyDirty = 0; }
+	if(sp->shapeDirty){ upload_shapes(ds, w); sp->shapeDirty = 0; }
+	if(sp->consDirty){ upload_joints(ds, w, 0); sp->consDirty = 0; sp->jointDt = 0.0; }
+}
+
 /* One step of every world of the set with per-world dt. */
 static int devset_step(DevSet *ds, const double *dts, cpSpace **only)
 {
@@ -781,9 +792,7 @@ static int devset_step(DevSet *ds, const double *dts, cpSpace **only)
 		cpSpace *sp = ds->spaces[w];
 		cpgParams *P = &hp[w];
 		if((only && *only != sp) || dts[w] == 0.0){ P->active = 0; continue; }
-		if(sp->bodyDirty){ upload_bodies(ds, w); sp->bodyDirty = 0; }
-		if(sp->shapeDirty){ upload_shapes(ds, w); sp->shapeDirty = 0; }
-		if(sp->consDirty){ upload_joints(ds, w, 0); sp->consDirty = 0; sp->jointDt = 0.0; }
+		devset_flush_space(ds, w);
 		double dt = dts[w];
 		/* cpSpaceStep.c:339-344, 384, 399, 407 */
 		sp->stamp++;
@@ -891,17 +900,37 @@ void cpGpuSpaceSync(cpSpace *sp)
 /* ====================================================================
  * Batches
  * ==================================================================== */
+/* A differentiable rollout of a batch: the forward's checkpoints. */
+typedef struct Rollout {
+	int steps, K, nckpt;
+	double dt;
+	char *ckpt;                   /* nckpt copies of the device set */
+	unsigned *stamps;             /* [nckpt][nspaces] host stamps at the checkpoints */
+	double *currDt;               /* [nckpt][nspaces] */
+	size_t rowCap;                /* tape rows the last reverse pass needed */
+} Rollout;
+
 struct cpGpuBatch {
 	cpSpace **spaces;
 	int n, cap;
 	DevSet *dev;
+	Rollout *roll;
 };
+
+static void rollout_free(Rollout *r)
+{
+	if(!r) return;
+	if(r->ckpt) cudaFree(r->ckpt);
+	free(r->stamps); free(r->currDt);
+	free(r);
+}
 
 cpGpuBatch *cpGpuBatchNew(void) { return (cpGpuBatch *)calloc(1, sizeof(cpGpuBatch)); }
 
 void cpGpuBatchFree(cpGpuBatch *b)
 {
 	if(!b) return;
+	rollout_free(b->roll);
 	if(b->dev){
 		for(int i = 0; i < b->n; i++) space_pull(b->spaces[i]);
 		devset_free(b->dev);
@@ -935,6 +964,264 @@ int cpGpuBatchStep(cpGpuBatch *b, cpFloat dt, int steps, int use_graph)
 	int rc = 0;
 	for(int s = 0; s < steps && rc == 0; s++) rc = devset_step(b->dev, dts, NULL);
 	free(dts);
+	return rc;
+}
+
+/* ====================================================================
+ * Differentiable rollout (reference-order mode)
+ * ==================================================================== */
+
+static int batch_ready(cpGpuBatch *b)
+{
+	if(!b || b->n == 0){ set_error(CP_GPU_ERR_ARGUMENT, "empty batch"); return 0; }
+	for(int i = 0; i < b->n; i++){
+		if(!space_supported(b->spaces[i])) return 0;
+		if(b->spaces[i]->mode != CP_GPU_SOLVER_ORDERED){
+			set_error(CP_GPU_ERR_UNSUPPORTED, "the differentiable rollout runs the reference-order solver");
+			return 0;
+		}
+	}
+	if(!b->dev){
+		b->dev = devset_build(b->spaces, b->n);
+		if(!b->dev) return 0;
+		for(int i = 0; i < b->n; i++) b->spaces[i]->ownsDev = 0;
+	}
+	return 1;
+}
+
+static void rollout_save(cpGpuBatch *b, int i)
+{
+	DevSet *ds = b->dev;
+	Rollout *r = b->roll;
+	for(int w = 0; w < ds->nspaces; w++) devset_flush_space(ds, w);
+	cuda_ok(cudaMemcpyAsync(r->ckpt + (size_t)i*ds->slabBytes, ds->slab, ds->slabBytes, cudaMemcpyDeviceToDevice, lib_stream()), "checkpoint");
+	for(int w = 0; w < ds->nspaces; w++){
+		r->stamps[(size_t)i*ds->nspaces + w] = ds->spaces[w]->stamp;
+		r->currDt[(size_t)i*ds->nspaces + w] = ds->spaces[w]->curr_dt;
+	}
+}
+
+static void rollout_restore_from(DevSet *ds, const char *src, const unsigned *stamps, const double *currDt)
+{
+	cuda_ok(cudaMemcpyAsync(ds->slab, src, ds->slabBytes, cudaMemcpyDeviceToDevice, lib_stream()), "restore");
+	for(int w = 0; w < ds->nspaces; w++){
+		cpSpace *sp = ds->spaces[w];
+		sp->stamp = stamps[w];
+		sp->curr_dt = currDt[w];
+		sp->hostStale = 1; sp->consStale = 1; sp->shapesStale = 1; sp->snapValid = 0;
+	}
+}
+
+int cpGpuRolloutForward(cpGpuBatch *b, cpFloat dt, int steps, int checkpoint)
+{
+	if(steps < 1 || checkpoint < 1 || !(dt > 0.0)){ set_error(CP_GPU_ERR_ARGUMENT, "rollout: steps, checkpoint and dt must be positive"); return -1; }
+	if(!batch_ready(b)) return -1;
+	DevSet *ds = b->dev;
+	rollout_free(b->roll);
+	Rollout *r = b->roll = (Rollout *)calloc(1, sizeof(Rollout));
+	r->steps = steps; r->K = checkpoint; r->dt = dt;
+	r->nckpt = (steps + checkpoint - 1)/checkpoint;
+	r->stamps = HALLOC(unsigned, (size_t)r->nckpt*ds->nspaces);
+	r->currDt = HALLOC(double, (size_t)r->nckpt*ds->nspaces);
+	if(!cuda_ok(cudaMalloc((void **)&r->ckpt, (size_t)r->nckpt*ds->slabBytes), "cudaMalloc checkpoints")){
+		r->ckpt = NULL; rollout_free(r); b->roll = NULL;
+		set_error(CP_GPU_ERR_OVERFLOW, "rollout: no device memory for %d checkpoints of %zu bytes", (steps + checkpoint - 1)/checkpoint, ds->slabBytes);
+		return -1;
+	}
+	double *dts = (double *)malloc(sizeof(double)*(size_t)b->n);
+	for(int i = 0; i < b->n; i++) dts[i] = dt;
+	int rc = 0;
+	for(int s = 0; s < steps && rc == 0; s++){
+		if(s % checkpoint == 0) rollout_save(b, s/checkpoint);
+		rc = devset_step(ds, dts, NULL);
+	}
+	free(dts);
+	return rc;
+}
+
+typedef struct TapeMem {
+	cpgTape t;
+	cpgAdj a;
+	void *block;                  /* one allocation for everything */
+} TapeMem;
+
+static size_t tape_carve(cpgSet *d, TapeMem *m, char *base, int K, size_t rowCap, int iters, int pass)
+{
+	size_t total = 0;
+#define TCARVE(ptr, type, count) do { size_t b_ = align256(sizeof(type)*(size_t)((count) > 0 ? (count) : 1)); if(pass) ptr = (type *)(base + total); total += b_; } while(0)
+	int W = d->nworlds;
+	size_t levCap = rowCap + (size_t)K*(W + 1);
+	TCARVE(m->t.body, double, (size_t)K*8*d->totalBodies);
+	TCARVE(m->t.shape, double, (size_t)K*6*d->totalShapes);
+	TCARVE(m->t.verts, double, (size_t)K*4*d->totalVerts);
+	TCARVE(m->t.params, cpgParams, (size_t)K*W);
+	TCARVE(m->t.rows, cpgRow, rowCap);
+	TCARVE(m->t.rowInfo, int, 4*rowCap);
+	TCARVE(m->t.rowOff, int, (size_t)K*(W + 1));
+	TCARVE(m->t.levels, int, levCap);
+	TCARVE(m->t.levOff, int, (size_t)K*(W + 1));
+	TCARVE(m->t.app, double, rowCap*(size_t)iters*2*14);   /* AdjApp: 14 doubles */
+	TCARVE(m->t.cursor, int, 4);
+	TCARVE(m->a.body, double, 9*(size_t)d->totalBodies);
+	TCARVE(m->a.arb, double, 4*(size_t)d->arbCap);
+	TCARVE(m->a.gMinv, double, d->totalBodies);
+	TCARVE(m->a.gE, double, d->totalShapes);
+	TCARVE(m->a.gU, double, d->totalShapes);
+	TCARVE(m->a.con, double, rowCap*2*16);
+	TCARVE(m->a.unit, double, rowCap*2);
+#undef TCARVE
+	if(pass){ m->t.K = K; m->t.rowCap = (int)rowCap; m->t.levCap = (int)levCap; }
+	return total;
+}
+
+static int tape_alloc(cpgSet *d, TapeMem *m, int K, size_t rowCap, int iters)
+{
+	memset(m, 0, sizeof(*m));
+	if(rowCap > 0x7fffffffULL/(size_t)(iters*2 + 2)){ set_error(CP_GPU_ERR_OVERFLOW, "rollout: tape too large"); return 0; }
+	size_t bytes = tape_carve(d, m, NULL, K, rowCap, iters, 0);
+	if(!cuda_ok(cudaMalloc(&m->block, bytes), "cudaMalloc rollout tape")){ m->block = NULL; return 0; }
+	tape_carve(d, m, (char *)m->block, K, rowCap, iters, 1);
+	return 1;
+}
+
+int cpGpuRolloutBackward(cpGpuBatch *b, const cpFloat *dLdp, cpFloat *dLdv0, cpFloat *dLdw0, cpFloat *dLdm, cpFloat *dLde, cpFloat *dLdu)
+{
+	if(!b || !b->dev || !b->roll){ set_error(CP_GPU_ERR_ARGUMENT, "rollout: no forward rollout to reverse"); return -1; }
+	if(!dLdp){ set_error(CP_GPU_ERR_ARGUMENT, "rollout: dLdp is required"); return -1; }
+	DevSet *ds = b->dev;
+	cpgSet *d = &ds->d;
+	Rollout *r = b->roll;
+	cudaStream_t st = lib_stream();
+	int W = ds->nspaces, K = r->K;
+	int iters = 0;
+	for(int w = 0; w < W; w++) if(ds->spaces[w]->iterations > iters) iters = ds->spaces[w]->iterations;
+	for(int w = 0; w < W; w++) if(ds->spaces[w]->iterations != iters){
+		set_error(CP_GPU_ERR_UNSUPPORTED, "rollout: all spaces of the batch need the same iteration count");
+		return -1;
+	}
+	/* the state after the forward, restored at the end */
+	char *fin = NULL;
+	if(!cuda_ok(cudaMalloc((void **)&fin, ds->slabBytes), "cudaMalloc final state")) return -1;
+	cuda_ok(cudaMemcpyAsync(fin, ds->slab, ds->slabBytes, cudaMemcpyDeviceToDevice, st), "save final state");
+	unsigned *finStamp = HALLOC(unsigned, W);
+	double *finDt = HALLOC(double, W);
+	for(int w = 0; w < W; w++){ finStamp[w] = ds->spaces[w]->stamp; finDt[w] = ds->spaces[w]->curr_dt; }
+
+	/* tape rows for K steps: twice the solved arbiters of the last step, or what a previous pass needed */
+	check_stats(ds);
+	size_t rowCap = r->rowCap ? r->rowCap : (size_t)K*(2*(size_t)(ds->hstats[5] > 0 ? ds->hstats[5] : 0) + (size_t)d->totalCons + 1024);
+	TapeMem m;
+	int rc = -1;
+	double *h = NULL;
+	if(!tape_alloc(d, &m, K, rowCap, iters)) goto done;
+
+	/* seeds: dL/dp at the end, nothing else */
+	{
+		size_t nbd = 9*(size_t)d->totalBodies;
+		h = HALLOC(double, nbd);
+		int idx = 0;
+		for(int w = 0; w < W; w++){
+			cpSpace *sp = ds->spaces[w];
+			for(int i = 0; i < sp->ndyn; i++, idx++){
+				size_t g = (size_t)ds->hworld[w].bodyOff + i;
+				h[9*g] = dLdp[2*idx]; h[9*g + 1] = dLdp[2*idx + 1];
+			}
+		}
+		cuda_ok(cudaMemcpyAsync(m.a.body, h, sizeof(double)*nbd, cudaMemcpyHostToDevice, st), "seed");
+		cudaMemsetAsync(m.a.arb, 0, sizeof(double)*4*(size_t)d->arbCap, st);
+		cudaMemsetAsync(m.a.gMinv, 0, sizeof(double)*(size_t)d->totalBodies, st);
+		cudaMemsetAsync(m.a.gE, 0, sizeof(double)*(size_t)d->totalShapes, st);
+		cudaMemsetAsync(m.a.gU, 0, sizeof(double)*(size_t)d->totalShapes, st);
+	}
+	{
+		double *dts = (double *)malloc(sizeof(double)*(size_t)W);
+		for(int i = 0; i < W; i++) dts[i] = r->dt;
+		int ok = 1;
+		for(int seg = r->nckpt - 1; seg >= 0 && ok; seg--){
+			int first = seg*K, len = (r->steps - first < K) ? r->steps - first : K;
+			for(int attempt = 0; attempt < 4; attempt++){
+				rollout_restore_from(ds, r->ckpt + (size_t)seg*ds->slabBytes, r->stamps + (size_t)seg*W, r->currDt + (size_t)seg*W);
+				cudaMemsetAsync(m.t.cursor, 0, sizeof(int)*4, st);
+				d->tape = m.t;
+				d->tape.on = 1;
+				for(int t = 0; t < len && ok; t++){
+					d->tape.step = t;
+					if(devset_step(ds, dts, NULL) != 0) ok = 0;
+				}
+				d->tape.on = 0;
+				int cur[4];
+				cuda_ok(cudaMemcpyAsync(cur, m.t.cursor, sizeof(cur), cudaMemcpyDeviceToHost, st), "tape cursor");
+				cudaStreamSynchronize(st);
+				if(!ok) break;
+				if(cur[3] & 1){ set_error(CP_GPU_ERR_UNSUPPORTED, "rollout: constraints are not differentiated"); ok = 0; break; }
+				if(!cur[2]) break;
+				/* the tape overflowed: grow it (the gradients so far are kept) and replay */
+				size_t need = (size_t)cur[0] + (size_t)cur[0]/4 + 1024;
+				TapeMem m2;
+				if(!tape_alloc(d, &m2, K, need, iters)){ ok = 0; break; }
+				cudaMemcpyAsync(m2.a.body, m.a.body, sizeof(double)*9*(size_t)d->totalBodies, cudaMemcpyDeviceToDevice, st);
+				cudaMemcpyAsync(m2.a.arb, m.a.arb, sizeof(double)*4*(size_t)d->arbCap, cudaMemcpyDeviceToDevice, st);
+				cudaMemcpyAsync(m2.a.gMinv, m.a.gMinv, sizeof(double)*(size_t)d->totalBodies, cudaMemcpyDeviceToDevice, st);
+				cudaMemcpyAsync(m2.a.gE, m.a.gE, sizeof(double)*(size_t)d->totalShapes, cudaMemcpyDeviceToDevice, st);
+				cudaMemcpyAsync(m2.a.gU, m.a.gU, sizeof(double)*(size_t)d->totalShapes, cudaMemcpyDeviceToDevice, st);
+				cudaStreamSynchronize(st);
+				cudaFree(m.block);
+				m = m2;
+				r->rowCap = need;
+				if(attempt == 3){ set_error(CP_GPU_ERR_OVERFLOW, "rollout: tape overflow"); ok = 0; }
+			}
+			if(!ok) break;
+			d->tape = m.t;
+			d->tape.on = 0;
+			for(int t = len - 1; t >= 0; t--){
+				if(cpg_launch_adjoint(d, &m.a, t, st) != 0){ set_error(CP_GPU_ERR_CUDA, "adjoint launch failed"); ok = 0; break; }
+			}
+		}
+		free(dts);
+		int cur[4] = {0, 0, 0, 0};
+		if(ok){
+			cuda_ok(cudaMemcpyAsync(cur, m.t.cursor, sizeof(cur), cudaMemcpyDeviceToHost, st), "tape cursor");
+			cudaStreamSynchronize(st);
+			if(cur[3] & 2){ set_error(CP_GPU_ERR_CUDA, "rollout: contact geometry of a replayed step did not match its rows"); ok = 0; }
+		}
+		if(ok){
+			/* gather: dL/dv0, dL/dw0 from the body adjoints, dL/dm = -dL/d(1/m) / m^2 */
+			size_t nbd = 9*(size_t)d->totalBodies;
+			double *gm = HALLOC(double, d->totalBodies), *minv = HALLOC(double, d->totalBodies);
+			double *ge = HALLOC(double, d->totalShapes), *gu = HALLOC(double, d->totalShapes);
+			ok &= cuda_ok(cudaMemcpyAsync(h, m.a.body, sizeof(double)*nbd, cudaMemcpyDeviceToHost, st), "gradients");
+			ok &= cuda_ok(cudaMemcpyAsync(gm, m.a.gMinv, sizeof(double)*(size_t)d->totalBodies, cudaMemcpyDeviceToHost, st), "gradients");
+			ok &= cuda_ok(cudaMemcpyAsync(minv, d->minv, sizeof(double)*(size_t)d->totalBodies, cudaMemcpyDeviceToHost, st), "gradients");
+			ok &= cuda_ok(cudaMemcpyAsync(ge, m.a.gE, sizeof(double)*(size_t)d->totalShapes, cudaMemcpyDeviceToHost, st), "gradients");
+			ok &= cuda_ok(cudaMemcpyAsync(gu, m.a.gU, sizeof(double)*(size_t)d->totalShapes, cudaMemcpyDeviceToHost, st), "gradients");
+			cudaStreamSynchronize(st);
+			int idx = 0, sidx = 0;
+			for(int w = 0; w < W && ok; w++){
+				cpSpace *sp = ds->spaces[w];
+				for(int i = 0; i < sp->ndyn; i++, idx++){
+					size_t g = (size_t)ds->hworld[w].bodyOff + i;
+					if(dLdv0){ dLdv0[2*idx] = h[9*g + 3]; dLdv0[2*idx + 1] = h[9*g + 4]; }
+					if(dLdw0) dLdw0[idx] = h[9*g + 5];
+					if(dLdm) dLdm[idx] = -gm[g]*minv[g]*minv[g];
+				}
+				for(int i = 0; i < sp->nshapes; i++, sidx++){
+					size_t g = (size_t)ds->hworld[w].shapeOff + i;
+					if(dLde) dLde[sidx] = ge[g];
+					if(dLdu) dLdu[sidx] = gu[g];
+				}
+			}
+			free(gm); free(minv); free(ge); free(gu);
+		}
+		rc = ok ? 0 : -1;
+	}
+done:
+	d->tape.on = 0;
+	rollout_restore_from(ds, fin, finStamp, finDt);
+	cudaStreamSynchronize(st);
+	cudaFree(fin);
+	if(m.block) cudaFree(m.block);
+	memset(&d->tape, 0, sizeof(d->tape));
+	free(finStamp); free(finDt); free(h);
 	return rc;
 }
 

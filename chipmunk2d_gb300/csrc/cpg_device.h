@@ -136,6 +136,8 @@ typedef struct cpgArb {
 	int world;
 	unsigned gjk;                 /* last GJK feature id of the pair */
 	int colorTag;                 /* coloured mode: valid bit, low 23 bits of the colouring step's stamp, colour */
+	int warmSrc;                  /* per contact k, bits 4k..4k+3: 1 + index of the old contact whose impulses it took (0: none) */
+	int pad;
 	double nx, ny, e, u, svx, svy;
 	cpgContact c[2];
 } cpgArb;
@@ -170,7 +172,7 @@ typedef struct cpgRow {
 	int src;                      /* arbiter slot, or joint index in the world */
 	int flags;                    /* 1: first step (no warm start); 2/4: body a/b dynamic */
 	union {
-		struct { double nx, ny, u, svx, svy, pad; cpgRowContact c[2]; } arb;
+		struct { double nx, ny, u, svx, svy, e; cpgRowContact c[2]; } arb;   /* e: elasticity */
 		struct { double r1x, r1y, r2x, r2y, k11, k12, k21, k22, jx, jy, biasx, biasy;
 		         double nx, ny, nMass, jnAcc, bias, maxForce; } jnt;
 	};
@@ -188,6 +190,25 @@ typedef struct cpgOp {
 } cpgOp;
 
 /* All device arrays of a set.  Vectors are split into x/y arrays. */
+/* Recording of replayed steps for the differentiable rollout. */
+typedef struct cpgTape {
+	int on;                   /* record this step */
+	int step;                 /* its index within the replayed segment */
+	int K;                    /* steps per segment */
+	int rowCap, levCap;
+	double *body;             /* [K][8][totalBodies] planes: p.x p.y a (after position integration), v.x v.y w (pre-step), cos, sin */
+	double *shape;            /* [K][6][totalShapes] planes: world p0.x p0.y p1.x p1.y n.x n.y */
+	double *verts;            /* [K][4][totalVerts] planes: world vertex x y, world normal x y */
+	cpgParams *params;        /* [K][nworlds] */
+	cpgRow *rows;             /* [rowCap] rows of all recorded steps, world by world */
+	int *rowInfo;             /* [rowCap][4]: arbiter shapes a, b; final GJK id; warm-start sources */
+	int *rowOff;              /* [K][nworlds + 1] */
+	int *levels;              /* [levCap] level starts (relative to the world's rows) */
+	int *levOff;              /* [K][nworlds + 1] */
+	double *app;              /* [rowCap][iterations][2] impulse application records (AdjApp) */
+	int *cursor;              /* [4]: rows used, levels used, overflow flag, unsupported-row flag */
+} cpgTape;
+
 typedef struct cpgSet {
 	int nworlds;
 	int totalBodies, totalShapes, totalVerts, totalCons;
@@ -275,13 +296,28 @@ typedef struct cpgSet {
 
 	/* stats block copied to the host after each step */
 	int *stats;
+
+	/* differentiable rollout: recording of a replayed step (on = 0 otherwise) */
+	cpgTape tape;
 } cpgSet;
+
+/* Adjoint state of the differentiable rollout (device arrays). */
+typedef struct cpgAdj {
+	double *body;                 /* [totalBodies][9]: adjoints of p.x p.y a v.x v.y w v_bias.x v_bias.y w_bias */
+	double *arb;                  /* [arbCap][2][2]: adjoints of the stored jnAcc, jtAcc of each arbiter contact */
+	double *gMinv;                /* [totalBodies] dL/d(1/m) */
+	double *gE, *gU;              /* [totalShapes] dL/de, dL/du */
+	double *con;                  /* [rowCap][2][16] per-contact scratch */
+	double *unit;                 /* [rowCap][2] per-unit dL/d(arbiter e), dL/d(arbiter u) */
+} cpgAdj;
 
 /* ---- launchers (cpg_kernels.cu) ---- */
 int cpg_launch_apply_ops(const cpgSet *s, void *stream);
 int cpg_launch_step(const cpgSet *s, const cpgSet *host_mirror, int mode, void *stream, float *phase_ms);
 int cpg_launch_gather_arbs(const cpgSet *s, int world, cpgArb *out, int n, void *stream);
 long long cpg_launch_count(int reset);
+int cpg_launch_tape(const cpgSet *s, void *stream);
+int cpg_launch_adjoint(const cpgSet *s, const cpgAdj *a, int step, void *stream);
 
 #ifdef __cplusplus
 }

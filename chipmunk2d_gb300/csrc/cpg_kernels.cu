@@ -35,6 +35,7 @@
 #include "cpg_tree.cuh"
 #include "cpg_narrow.cuh"
 #include "cpg_colored.cuh"
+#include "cpg_adjoint.cuh"
 
 static long long g_launches = 0;
 
@@ -339,21 +340,26 @@ __global__ void k_arb_update(cpgSet s)
 		double pax = s.px[gBodyA], pay = s.py[gBodyA], pbx = s.px[gBodyB], pby = s.py[gBodyB];
 		cpgContact nc[2];
 		int oldCount = arb.count;
+		int warmSrc = 0;
 		for(int k = 0; k < nr.count; k++){
 			cpgContact &con = nc[k];
 			con.r1x = nr.p1x[k] - pax; con.r1y = nr.p1y[k] - pay;
 			con.r2x = nr.p2x[k] - pbx; con.r2y = nr.p2y[k] - pby;
 			con.hash = nr.hash[k];
 			con.jnAcc = 0.0; con.jtAcc = 0.0;
+			int src = 0;
 			for(int j = 0; j < oldCount; j++){
 				if(con.hash == arb.c[j].hash){
 					con.jnAcc = arb.c[j].jnAcc;
 					con.jtAcc = arb.c[j].jtAcc;
+					src = j + 1;
 				}
 			}
+			warmSrc |= src << (4*k);
 			con.nMass = 0.0; con.tMass = 0.0; con.bounce = 0.0; con.jBias = 0.0; con.bias = 0.0;
 		}
 		for(int k = 0; k < nr.count; k++) arb.c[k] = nc[k];
+		arb.warmSrc = warmSrc;
 		arb.gjk = nr.idOut;
 		arb.a = ia; arb.b = ib; arb.ba = bodyA; arb.bb = bodyB;
 		arb.count = nr.count;
@@ -580,6 +586,7 @@ __global__ void k_build_rows(cpgSet s)
 				| (s.btype[ga] == CPG_DYNAMIC ? ROW_DYN_A : 0) | (s.btype[gb] == CPG_DYNAMIC ? ROW_DYN_B : 0);
 			double nx = arb.nx, ny = arb.ny;
 			row.arb.nx = nx; row.arb.ny = ny; row.arb.u = arb.u; row.arb.svx = arb.svx; row.arb.svy = arb.svy;
+			row.arb.e = arb.e;        /* for the rollout's pre-step adjoint */
 			double dx = s.px[gb] - s.px[ga], dy = s.py[gb] - s.py[ga];
 			for(int c = 0; c < arb.count; c++){
 				const cpgContact &con = arb.c[c];
@@ -899,7 +906,8 @@ __device__ __forceinline__ void quad_load(QuadRow &q, const cpgRow &row, int lan
  * the multiply-adds of an iteration: 32 FP64 instructions per contact
  * instead of 40.  Without it every operation is the reference's. */
 template<bool CG, bool FUSED>
-__device__ __forceinline__ void quad_apply(const QuadRow &q, cpgRow *row, double *bodies, int pass, double dt_coef, unsigned qmask, int lane4)
+__device__ __forceinline__ void quad_apply(const QuadRow &q, cpgRow *row, double *bodies, int pass, double dt_coef, unsigned qmask, int lane4,
+	AdjApp *rec = nullptr)
 {
 	bool side = (lane4 & 1) != 0, bias = (lane4 & 2) != 0;
 	if(pass == 0 && ((q.flags & ROW_FIRST) || bias)) return;
@@ -955,6 +963,14 @@ __device__ __forceinline__ void quad_apply(const QuadRow &q, cpgRow *row, double
 			else { nxj = ax - ny*djt; nyj = nx*djt + ay; }
 			double jx = bias ? ax : nxj, jy = bias ? ay : nyj;
 			jx = dneg_if(jx, !side); jy = dneg_if(jy, !side);
+			if(rec){
+				/* rollout recording: each lane writes its part of the record */
+				AdjApp &r = rec[k];
+				if(lane4 == 0){ r.jN0 = old; r.jN1 = acc; r.jT0 = jtOld; r.jT1 = jtAcc; r.vrx = vrx; r.vry = vry; r.wA = w; }
+				else if(lane4 == 1){ r.wB = w; }
+				else if(lane4 == 2){ r.jB0 = old; r.jB1 = acc; r.vbx = vrx; r.vby = vry; r.wbA = w; }
+				else { r.wbB = w; }
+			}
 			if(FUSED){
 				vx = __fma_rn(jx, minv, vx);
 				vy = __fma_rn(jy, minv, vy);
@@ -996,14 +1012,26 @@ __global__ void k_solve(cpgSet s, int stagedMax)
 	cpgRow *rows = s.rows + W.unitOff;
 	int lane4 = threadIdx.x & 3, nq = blockDim.x >> 2;
 	unsigned qmask = 0xFu << (threadIdx.x & 28);
+	/* rollout recording: the rows of this world in the tape */
+	AdjApp *tapeApp = nullptr;
+	if(s.tape.on){
+		const int *off = s.tape.rowOff + (size_t)s.tape.step*(s.nworlds + 1);
+		/* past the tape's capacity nothing is recorded: the host grows the
+		 * tape and replays the segment */
+		if(off[w + 1] <= s.tape.rowCap) tapeApp = (AdjApp *)s.tape.app + (size_t)off[w]*P.iterations*2;
+	}
 	for(int pass = 0; pass <= P.iterations; pass++){
 		for(int l = 0; l < nlev; l++){
 			int e = start[l + 1];
 			for(int k = start[l] + (threadIdx.x >> 2); k < e; k += nq){
 				QuadRow q;
 				quad_load(q, rows[k], lane4);
-				if(q.kind == 0) quad_apply<false, false>(q, rows + k, bodies, pass, P.dt_coef, qmask, lane4);
-				else if(lane4 == 0) solve_row<false>(rows, k, bodies, pass, P.dt_coef, P.dt);
+				AdjApp *rec = (tapeApp && pass > 0) ? tapeApp + ((size_t)k*P.iterations + (pass - 1))*2 : nullptr;
+				if(q.kind == 0) quad_apply<false, false>(q, rows + k, bodies, pass, P.dt_coef, qmask, lane4, rec);
+				else if(lane4 == 0){
+					if(tapeApp) atomicOr(&s.tape.cursor[3], 1);   /* joints are not differentiated */
+					solve_row<false>(rows, k, bodies, pass, P.dt_coef, P.dt);
+				}
 			}
 			__syncthreads();
 		}
@@ -1709,11 +1737,12 @@ extern "C" int cpg_launch_step(const cpgSet *s, const cpgSet *h, int mode, void 
 	else LAUNCH(k_schedule<<<blocks_for(W, 32), 32, 0, st>>>(*s));
 	if(timing) cudaEventRecord(ev[5], st);
 	LAUNCH(k_build_rows<<<dim3(perWorldX, W), 128, 0, st>>>(*s));
+	if(h->tape.on) cpg_launch_tape(s, st);
 	LAUNCH(k_integrate_vel<<<blocks_for(h->totalBodies, 128), 128, 0, st>>>(*s));
 	if(timing) cudaEventRecord(ev[6], st);
 	if(W == 1 && colored){
 		launch_coop((const void *)k_solve_coop<true>, CPG_COOP_SOLVE_THREADS, &sv, 0, st);
-	} else if(W == 1 && h->hostUnitsHint >= CPG_COOP_UNITS){
+	} else if(W == 1 && h->hostUnitsHint >= CPG_COOP_UNITS && !h->tape.on){
 		launch_coop((const void *)k_solve_coop<false>, CPG_COOP_SOLVE_THREADS, &sv, 0, st);
 	} else {
 		int stagedMax = h->hostMaxBodies <= CPG_STAGED_BODIES ? h->hostMaxBodies : 0;

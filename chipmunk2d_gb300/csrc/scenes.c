@@ -30,8 +30,8 @@
  *      50/50 circles r~U[1,4] and 3-6-vertex hull polys of radius U[1,4],
  *      uniform positions, v~N(0,20)/axis, density 1, u 0.7, e 0.1.
  *   5  adjoint world: `size`/2 circles r~U[1,3] and `size`/2 boxes with
- *      sides U[2,6], dropped onto a static ground segment, density 1,
- *      u 0.7, e 0.1.
+ *      sides U[2,6] at random orientations, dropped onto a static ground
+ *      segment, density 1, u 0.7, e 0.1.
  * Gravity, time step and iterations are set by the caller.
  */
 #include <stdlib.h>
@@ -341,7 +341,18 @@ static void build_adjoint(cpxScene *sc, int n, uint64_t seed)
 			add_circle(sc, p, v, rng_uniform(&rng, 1.0, 3.0), 0.7, 0.1);
 		} else {
 			double w = rng_uniform(&rng, 2.0, 6.0), h = rng_uniform(&rng, 2.0, 6.0);
-			add_box(sc, p, v, w, h, w*h, 0.7, 0.1);
+			/* a random orientation: a box dropped flat lands on a kink of
+			 * the contact geometry (tied support vertices) */
+			double ang = rng_uniform(&rng, 0.0, 6.283185307179586);
+			cpBody *body = cpBodyNew(w*h, cpMomentForBox(w*h, w, h));
+			cpBodySetPosition(body, p);
+			cpBodySetAngle(body, ang);
+			cpBodySetVelocity(body, v);
+			add_body(sc, body);
+			cpShape *s = cpBoxShapeNew(body, w, h, 0.0);
+			cpShapeSetFriction(s, 0.7);
+			cpShapeSetElasticity(s, 0.1);
+			add_shape(sc, s);
 		}
 	}
 }

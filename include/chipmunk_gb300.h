@@ -492,6 +492,24 @@ int cpGpuDebugCandidates(cpSpace *space, int *out, int max);
  * measured with CUDA events on the launching stream (0 when timing is off).
  * Phases: 0 integrate+cache, 1 broadphase, 2 narrowphase, 3 arbiters,
  * 4 schedule, 5 prestep+warmstart, 6 solve. */
+/* Differentiable rollout of a batch (reference-order solver).
+ * cpGpuRolloutForward steps every space of the batch `steps` times by dt
+ * from its current state, keeping a copy of the device state every
+ * `checkpoint` steps.  cpGpuRolloutBackward then returns the gradients of
+ * a scalar loss L of the final state, given dL/dp (2 per dynamic body, in
+ * batch order: spaces in the order they were added, each space's dynamic
+ * bodies in the order they were added), with respect to the initial
+ * velocities (dLdv0: 2 per dynamic body), initial angular velocities
+ * (dLdw0: 1 per dynamic body), masses (dLdm; the moment of inertia held
+ * fixed, as cpBodySetMass does), and each shape's elasticity and friction
+ * (dLde, dLdu: 1 per shape, all shapes of each space in order).  Any output
+ * pointer may be NULL.  It replays each checkpoint's steps with recording
+ * and runs the reverse steps on the device; the batch is left in the state
+ * the forward ended in.  Constraints and external forces are not
+ * differentiated.  Returns 0 on success, -1 with cpGpuGetLastError() set. */
+int cpGpuRolloutForward(cpGpuBatch *batch, cpFloat dt, int steps, int checkpoint);
+int cpGpuRolloutBackward(cpGpuBatch *batch, const cpFloat *dLdp, cpFloat *dLdv0, cpFloat *dLdw0,
+	cpFloat *dLdm, cpFloat *dLde, cpFloat *dLdu);
 void cpGpuSetTiming(int enabled);
 /* Debug: 1 makes single-world sets always solve with the whole-grid
  * kernel (a grid barrier between levels), 0 restores the automatic choice

@@ -1,0 +1,211 @@
+"""Differentiable rollout (cpGpuRolloutForward / cpGpuRolloutBackward).
+
+The reverse pass's gradients of L = sum |p_final - target|^2 are compared
+with central finite differences of the forward: of the GPU forward (the
+same batch stepped by cpGpuBatchStep with one parameter moved by +-h) and
+of the CPU oracle.  The scene is the rollout workload (circles and boxes
+dropped onto a ground segment, 10 iterations, dt = 1/120), with fewer
+worlds and bodies than the benchmark so that the finite differences, two
+full rollouts per parameter, stay cheap.
+"""
+import ctypes
+
+import numpy as np
+import pytest
+
+from chipmunk2d_gb300 import Scene, cpVect
+
+pytestmark = pytest.mark.gpu
+
+DT = 1 / 120
+WORLDS, SIZE = 6, 16
+
+
+def make(lib, seeds):
+    return [Scene(lib, 5, SIZE, seed=s) for s in seeds]
+
+
+def positions(scenes):
+    return np.concatenate([sc.bodies()[:, 0:2] for sc in scenes])
+
+
+def targets(n):
+    return np.random.default_rng(4).normal(0.0, 10.0, size=(n, 2))
+
+
+def loss(p, t):
+    return float(np.sum((p - t) ** 2))
+
+
+class Param:
+    """One differentiable parameter of the batch: kind, world, index, component."""
+
+    def __init__(self, kind, world, index, comp=0):
+        self.kind, self.world, self.index, self.comp = kind, world, index, comp
+
+    def apply(self, lib, scenes, h):
+        sc = scenes[self.world]
+        if self.kind in ("v", "w", "m"):
+            body = lib.cpx_scene_body(sc.h, self.index)
+            if self.kind == "v":
+                v = lib.cpBodyGetVelocity(body)
+                lib.cpBodySetVelocity(body, cpVect(v.x + (h if self.comp == 0 else 0.0), v.y + (h if self.comp == 1 else 0.0)))
+            elif self.kind == "w":
+                lib.cpBodySetAngularVelocity(body, lib.cpBodyGetAngularVelocity(body) + h)
+            else:
+                lib.cpBodySetMass(body, lib.cpBodyGetMass(body) + h)
+        else:
+            shape = lib.cpx_scene_shape(sc.h, self.index)
+            if self.kind == "e":
+                lib.cpShapeSetElasticity(shape, lib.cpShapeGetElasticity(shape) + h)
+            else:
+                lib.cpShapeSetFriction(shape, lib.cpShapeGetFriction(shape) + h)
+
+    def grad(self, g):
+        b = self.world * SIZE + self.index
+        s = self.world * (SIZE + 1) + self.index
+        return {"v": g["v0"][2 * b + self.comp], "w": g["w0"][b], "m": g["m"][b],
+                "e": g["e"][s], "u": g["u"][s]}[self.kind]
+
+
+def gpu_loss(lib, seeds, steps, t, param=None, h=0.0):
+    scenes = make(lib, seeds)
+    if param is not None:
+        param.apply(lib, scenes, h)
+    batch = lib.cpGpuBatchNew()
+    for sc in scenes:
+        lib.cpGpuBatchAddSpace(batch, sc.space)
+    assert lib.cpGpuBatchStep(batch, DT, steps, 0) == 0
+    L = loss(positions(scenes), t)
+    lib.cpGpuBatchFree(batch)
+    for sc in scenes:
+        sc.free()
+    return L
+
+
+def oracle_loss(lib, seeds, steps, t, param=None, h=0.0):
+    scenes = make(lib, seeds)
+    if param is not None:
+        param.apply(lib, scenes, h)
+    for sc in scenes:
+        sc.step(DT, steps)
+    L = loss(positions(scenes), t)
+    for sc in scenes:
+        sc.free()
+    return L
+
+
+def rollout_grads(lib, seeds, steps, K, t):
+    scenes = make(lib, seeds)
+    batch = lib.cpGpuBatchNew()
+    for sc in scenes:
+        lib.cpGpuBatchAddSpace(batch, sc.space)
+    assert lib.cpGpuRolloutForward(batch, DT, steps, K) == 0, lib.cpGpuGetLastErrorString()
+    p = positions(scenes)
+    nd = len(p)
+    ns = sum(sc.nshapes for sc in scenes)
+    dLdp = np.ascontiguousarray(2.0 * (p - t)).ravel()
+    g = {"v0": np.zeros(2 * nd), "w0": np.zeros(nd), "m": np.zeros(nd), "e": np.zeros(ns), "u": np.zeros(ns)}
+    rc = lib.cpGpuRolloutBackward(batch, dLdp.ctypes.data, g["v0"].ctypes.data, g["w0"].ctypes.data,
+                                  g["m"].ctypes.data, g["e"].ctypes.data, g["u"].ctypes.data)
+    assert rc == 0, lib.cpGpuGetLastErrorString()
+    # the batch is left in the forward's final state
+    np.testing.assert_array_equal(positions(scenes), p)
+    lib.cpGpuBatchFree(batch)
+    for sc in scenes:
+        sc.free()
+    return g, loss(p, t)
+
+
+def test_one_step_free_fall_gradient_is_exact(gpu_lib):
+    """Before the first contact, p1 = p0 + v0*dt, so dL/dv0 = 2 (p1 - t) dt."""
+    seeds = [4000 + i for i in range(WORLDS)]
+    scenes = make(gpu_lib, seeds)
+    p0 = positions(scenes)
+    v0 = np.concatenate([sc.bodies()[:, 2:4] for sc in scenes])
+    for sc in scenes:
+        sc.free()
+    t = targets(len(p0))
+    g, _ = rollout_grads(gpu_lib, seeds, 1, 1, t)
+    p1 = p0 + v0 * DT
+    np.testing.assert_allclose(g["v0"].reshape(-1, 2), 2.0 * (p1 - t) * DT, rtol=1e-12, atol=1e-12)
+
+
+def test_gradients_do_not_depend_on_the_checkpoint_interval(gpu_lib):
+    seeds = [4000 + i for i in range(WORLDS)]
+    t = targets(WORLDS * SIZE)
+    a, La = rollout_grads(gpu_lib, seeds, 60, 60, t)
+    b, Lb = rollout_grads(gpu_lib, seeds, 60, 16, t)
+    assert La == Lb
+    for k in a:
+        np.testing.assert_array_equal(a[k], b[k], err_msg=k)
+
+
+def sample_params():
+    rng = np.random.default_rng(11)
+    ps = []
+    for _ in range(16):
+        ps.append(Param("v", int(rng.integers(WORLDS)), int(rng.integers(SIZE)), int(rng.integers(2))))
+    for _ in range(6):
+        ps.append(Param("w", int(rng.integers(WORLDS)), int(rng.integers(SIZE))))
+    for _ in range(6):
+        ps.append(Param("m", int(rng.integers(WORLDS)), int(rng.integers(SIZE))))
+    for _ in range(6):
+        ps.append(Param("e", int(rng.integers(WORLDS)), int(rng.integers(SIZE + 1))))
+    for _ in range(6):
+        ps.append(Param("u", int(rng.integers(WORLDS)), int(rng.integers(SIZE + 1))))
+    return ps
+
+
+STEPS = 150
+
+
+def test_gradients_match_gpu_finite_differences(gpu_lib):
+    """Central differences at two step sizes screen out parameters whose
+    loss is not smooth at this point (a contact appearing within the step,
+    a tie between support features); for the rest the adjoint must agree
+    to 1e-5 relative."""
+    seeds = [4000 + i for i in range(WORLDS)]
+    t = targets(WORLDS * SIZE)
+    g, L0 = rollout_grads(gpu_lib, seeds, STEPS, 16, t)
+    assert gpu_loss(gpu_lib, seeds, STEPS, t) == L0
+    rows = []
+    for p in sample_params():
+        fd = []
+        for h in (1e-6, 1e-7):
+            fd.append((gpu_loss(gpu_lib, seeds, STEPS, t, p, h) - gpu_loss(gpu_lib, seeds, STEPS, t, p, -h)) / (2 * h))
+        rows.append((p, p.grad(g), fd[0], fd[1]))
+    scale = max(abs(r[2]) for r in rows)
+    floor = 1e-4 * scale
+    reliable, bad = 0, []
+    for p, adj, f6, f7 in rows:
+        smooth = abs(f6 - f7) <= 1e-6 * max(abs(f6), floor) * 10 or (abs(f6) < floor and abs(f7) < floor)
+        err = abs(adj - f6) / max(abs(f6), floor)
+        print("%s w%d i%d c%d adjoint %+.10e fd %+.10e %+.10e rel %.2e%s" % (
+            p.kind, p.world, p.index, p.comp, adj, f6, f7, err, "" if smooth else "  (not smooth)"))
+        if smooth:
+            reliable += 1
+            if err > 1e-5:
+                bad.append((p.kind, p.world, p.index, p.comp, adj, f6, f7))
+    assert reliable >= 0.75 * len(rows), reliable
+    assert not bad, bad
+
+
+def test_gradients_match_oracle_finite_differences(gpu_lib, oracle_lib):
+    """The CPU reference's forward (the oracle) gives the same finite
+    differences: the GPU forward agrees with it to ~1e-12 per step."""
+    seeds = [4000 + i for i in range(2)]
+    global WORLDS
+    saved = WORLDS
+    WORLDS = 2
+    try:
+        t = targets(WORLDS * SIZE)
+        g, L0 = rollout_grads(gpu_lib, seeds, 40, 16, t)
+        params = [Param("v", 0, 3, 0), Param("v", 1, 9, 1), Param("w", 0, 12), Param("m", 1, 2), Param("u", 0, 0), Param("e", 1, 5)]
+        for p in params:
+            h = 1e-5
+            fd = (oracle_loss(oracle_lib, seeds, 40, t, p, h) - oracle_loss(oracle_lib, seeds, 40, t, p, -h)) / (2 * h)
+            adj = p.grad(g)
+            assert abs(adj - fd) <= 1e-4 * max(abs(fd), 1.0), (p.kind, adj, fd)
+    finally:
+        WORLDS = saved
