@@ -169,6 +169,7 @@ _GPU_API = {
     "cpGpuBatchStep": (I, [P, D, I, I]),
     "cpGpuRolloutForward": (I, [P, D, I, I]),
     "cpGpuRolloutBackward": (I, [P, P, P, P, P, P, P]),
+    "cpGpuDebugRolloutTimes": (I, [P, P]),
     "cpGpuDebugBodies": (I, [P, P, I]),
     "cpGpuDebugArbiters": (I, [P, P, I]),
     "cpGpuDebugConstraints": (I, [P, P, I]),

@@ -901,13 +901,27 @@ void cpGpuSpaceSync(cpSpace *sp)
  * Batches
  * ==================================================================== */
 /* A differentiable rollout of a batch: the forward's checkpoints. */
+typedef struct TapeMem {
+	cpgTape t;
+	cpgAdj a;
+	void *block;                  /* one allocation for everything */
+} TapeMem;
+
+/* A differentiable rollout of a batch: the forward's checkpoints, and the
+ * device buffers of the reverse pass, kept for the next rollout of the
+ * same shape (a training loop calls forward and backward repeatedly). */
 typedef struct Rollout {
 	int steps, K, nckpt;
 	double dt;
-	char *ckpt;                   /* nckpt copies of the device set */
+	char *ckpt;                   /* ckptCap copies of the device set */
+	int ckptCap;
 	unsigned *stamps;             /* [nckpt][nspaces] host stamps at the checkpoints */
 	double *currDt;               /* [nckpt][nspaces] */
 	size_t rowCap;                /* tape rows the last reverse pass needed */
+	char *fin;                    /* the forward's final state during the reverse pass */
+	TapeMem tape;                 /* tape.block == NULL until the first reverse pass */
+	int tapeK, tapeIters;
+	float replayMs, adjointMs;    /* device time of the last reverse pass (with cpGpuSetTiming(1)) */
 } Rollout;
 
 struct cpGpuBatch {
@@ -921,6 +935,8 @@ static void rollout_free(Rollout *r)
 {
 	if(!r) return;
 	if(r->ckpt) cudaFree(r->ckpt);
+	if(r->fin) cudaFree(r->fin);
+	if(r->tape.block) cudaFree(r->tape.block);
 	free(r->stamps); free(r->currDt);
 	free(r);
 }
@@ -1012,21 +1028,34 @@ static void rollout_restore_from(DevSet *ds, const char *src, const unsigned *st
 	}
 }
 
+int cpGpuDebugRolloutTimes(cpGpuBatch *b, double *out)
+{
+	if(!b || !b->roll || !out) return 0;
+	out[0] = b->roll->replayMs; out[1] = b->roll->adjointMs;
+	return 2;
+}
+
 int cpGpuRolloutForward(cpGpuBatch *b, cpFloat dt, int steps, int checkpoint)
 {
 	if(steps < 1 || checkpoint < 1 || !(dt > 0.0)){ set_error(CP_GPU_ERR_ARGUMENT, "rollout: steps, checkpoint and dt must be positive"); return -1; }
 	if(!batch_ready(b)) return -1;
 	DevSet *ds = b->dev;
-	rollout_free(b->roll);
-	Rollout *r = b->roll = (Rollout *)calloc(1, sizeof(Rollout));
+	if(!b->roll) b->roll = (Rollout *)calloc(1, sizeof(Rollout));
+	Rollout *r = b->roll;
 	r->steps = steps; r->K = checkpoint; r->dt = dt;
 	r->nckpt = (steps + checkpoint - 1)/checkpoint;
+	free(r->stamps); free(r->currDt);
 	r->stamps = HALLOC(unsigned, (size_t)r->nckpt*ds->nspaces);
 	r->currDt = HALLOC(double, (size_t)r->nckpt*ds->nspaces);
-	if(!cuda_ok(cudaMalloc((void **)&r->ckpt, (size_t)r->nckpt*ds->slabBytes), "cudaMalloc checkpoints")){
-		r->ckpt = NULL; rollout_free(r); b->roll = NULL;
-		set_error(CP_GPU_ERR_OVERFLOW, "rollout: no device memory for %d checkpoints of %zu bytes", (steps + checkpoint - 1)/checkpoint, ds->slabBytes);
-		return -1;
+	if(r->ckptCap < r->nckpt){
+		if(r->ckpt) cudaFree(r->ckpt);
+		r->ckpt = NULL; r->ckptCap = 0;
+		if(!cuda_ok(cudaMalloc((void **)&r->ckpt, (size_t)r->nckpt*ds->slabBytes), "cudaMalloc checkpoints")){
+			r->ckpt = NULL;
+			set_error(CP_GPU_ERR_OVERFLOW, "rollout: no device memory for %d checkpoints of %zu bytes", r->nckpt, ds->slabBytes);
+			return -1;
+		}
+		r->ckptCap = r->nckpt;
 	}
 	double *dts = (double *)malloc(sizeof(double)*(size_t)b->n);
 	for(int i = 0; i < b->n; i++) dts[i] = dt;
@@ -1039,11 +1068,6 @@ int cpGpuRolloutForward(cpGpuBatch *b, cpFloat dt, int steps, int checkpoint)
 	return rc;
 }
 
-typedef struct TapeMem {
-	cpgTape t;
-	cpgAdj a;
-	void *block;                  /* one allocation for everything */
-} TapeMem;
 
 static size_t tape_carve(cpgSet *d, TapeMem *m, char *base, int K, size_t rowCap, int iters, int pass)
 {
@@ -1057,6 +1081,7 @@ static size_t tape_carve(cpgSet *d, TapeMem *m, char *base, int K, size_t rowCap
 	TCARVE(m->t.params, cpgParams, (size_t)K*W);
 	TCARVE(m->t.rows, cpgRow, rowCap);
 	TCARVE(m->t.rowInfo, int, 4*rowCap);
+	TCARVE(m->t.rowWorld, int, rowCap);
 	TCARVE(m->t.rowOff, int, (size_t)K*(W + 1));
 	TCARVE(m->t.levels, int, levCap);
 	TCARVE(m->t.levOff, int, (size_t)K*(W + 1));
@@ -1067,8 +1092,9 @@ static size_t tape_carve(cpgSet *d, TapeMem *m, char *base, int K, size_t rowCap
 	TCARVE(m->a.gMinv, double, d->totalBodies);
 	TCARVE(m->a.gE, double, d->totalShapes);
 	TCARVE(m->a.gU, double, d->totalShapes);
-	TCARVE(m->a.con, double, rowCap*2*16);
-	TCARVE(m->a.unit, double, rowCap*2);
+	TCARVE(m->a.con, double, rowCap*2*4*16);
+	TCARVE(m->a.unit, double, rowCap*20);
+	TCARVE(m->a.arbTmp, double, 4*(size_t)d->arbCap);
 #undef TCARVE
 	if(pass){ m->t.K = K; m->t.rowCap = (int)rowCap; m->t.levCap = (int)levCap; }
 	return total;
@@ -1100,8 +1126,8 @@ int cpGpuRolloutBackward(cpGpuBatch *b, const cpFloat *dLdp, cpFloat *dLdv0, cpF
 		return -1;
 	}
 	/* the state after the forward, restored at the end */
-	char *fin = NULL;
-	if(!cuda_ok(cudaMalloc((void **)&fin, ds->slabBytes), "cudaMalloc final state")) return -1;
+	if(!r->fin && !cuda_ok(cudaMalloc((void **)&r->fin, ds->slabBytes), "cudaMalloc final state")){ r->fin = NULL; return -1; }
+	char *fin = r->fin;
 	cuda_ok(cudaMemcpyAsync(fin, ds->slab, ds->slabBytes, cudaMemcpyDeviceToDevice, st), "save final state");
 	unsigned *finStamp = HALLOC(unsigned, W);
 	double *finDt = HALLOC(double, W);
@@ -1113,7 +1139,14 @@ int cpGpuRolloutBackward(cpGpuBatch *b, const cpFloat *dLdp, cpFloat *dLdv0, cpF
 	TapeMem m;
 	int rc = -1;
 	double *h = NULL;
-	if(!tape_alloc(d, &m, K, rowCap, iters)) goto done;
+	if(r->tape.block && r->tapeK == K && r->tapeIters == iters && (size_t)r->tape.t.rowCap >= rowCap){
+		m = r->tape;
+	} else {
+		if(r->tape.block) cudaFree(r->tape.block);
+		memset(&r->tape, 0, sizeof(r->tape));
+		if(!tape_alloc(d, &m, K, rowCap, iters)) goto done;
+		r->tape = m; r->tapeK = K; r->tapeIters = iters;
+	}
 
 	/* seeds: dL/dp at the end, nothing else */
 	{
@@ -1137,8 +1170,12 @@ int cpGpuRolloutBackward(cpGpuBatch *b, const cpFloat *dLdp, cpFloat *dLdv0, cpF
 		double *dts = (double *)malloc(sizeof(double)*(size_t)W);
 		for(int i = 0; i < W; i++) dts[i] = r->dt;
 		int ok = 1;
+		cudaEvent_t ev[3];
+		if(g_timing) for(int i = 0; i < 3; i++) cudaEventCreate(&ev[i]);
+		r->replayMs = 0.0f; r->adjointMs = 0.0f;
 		for(int seg = r->nckpt - 1; seg >= 0 && ok; seg--){
 			int first = seg*K, len = (r->steps - first < K) ? r->steps - first : K;
+			if(g_timing) cudaEventRecord(ev[0], st);
 			for(int attempt = 0; attempt < 4; attempt++){
 				rollout_restore_from(ds, r->ckpt + (size_t)seg*ds->slabBytes, r->stamps + (size_t)seg*W, r->currDt + (size_t)seg*W);
 				cudaMemsetAsync(m.t.cursor, 0, sizeof(int)*4, st);
@@ -1167,17 +1204,39 @@ int cpGpuRolloutBackward(cpGpuBatch *b, const cpFloat *dLdp, cpFloat *dLdv0, cpF
 				cudaStreamSynchronize(st);
 				cudaFree(m.block);
 				m = m2;
+				r->tape = m;
 				r->rowCap = need;
 				if(attempt == 3){ set_error(CP_GPU_ERR_OVERFLOW, "rollout: tape overflow"); ok = 0; }
 			}
 			if(!ok) break;
+			if(g_timing) cudaEventRecord(ev[1], st);
 			d->tape = m.t;
 			d->tape.on = 0;
-			for(int t = len - 1; t >= 0; t--){
-				if(cpg_launch_adjoint(d, &m.a, t, st) != 0){ set_error(CP_GPU_ERR_CUDA, "adjoint launch failed"); ok = 0; break; }
+			/* the carried impulse adjoints, in the next checkpoint's slot
+			 * numbering, move to this replay's */
+			if(seg + 1 < r->nckpt){
+				const char *next = r->ckpt + (size_t)(seg + 1)*ds->slabBytes + ((const char *)d->keys - (const char *)ds->slab);
+				if(cpg_launch_adjoint_remap(d, &m.a, next, st) != 0){ set_error(CP_GPU_ERR_CUDA, "adjoint launch failed"); ok = 0; break; }
+			}
+			int *off = HALLOC(int, (size_t)len*(W + 1));
+			cuda_ok(cudaMemcpyAsync(off, m.t.rowOff, sizeof(int)*(size_t)len*(W + 1), cudaMemcpyDeviceToHost, st), "tape offsets");
+			cudaStreamSynchronize(st);
+			for(int t = len - 1; t >= 0 && ok; t--){
+				int rows = off[(size_t)t*(W + 1) + W] - off[(size_t)t*(W + 1)];
+				if(cpg_launch_adjoint(d, &m.a, t, rows, st) != 0){ set_error(CP_GPU_ERR_CUDA, "adjoint launch failed"); ok = 0; }
+			}
+			free(off);
+			if(g_timing){
+				float a0 = 0.0f, a1 = 0.0f;
+				cudaEventRecord(ev[2], st);
+				cudaEventSynchronize(ev[2]);
+				cudaEventElapsedTime(&a0, ev[0], ev[1]);
+				cudaEventElapsedTime(&a1, ev[1], ev[2]);
+				r->replayMs += a0; r->adjointMs += a1;
 			}
 		}
 		free(dts);
+		if(g_timing) for(int i = 0; i < 3; i++) cudaEventDestroy(ev[i]);
 		int cur[4] = {0, 0, 0, 0};
 		if(ok){
 			cuda_ok(cudaMemcpyAsync(cur, m.t.cursor, sizeof(cur), cudaMemcpyDeviceToHost, st), "tape cursor");
@@ -1218,8 +1277,6 @@ done:
 	d->tape.on = 0;
 	rollout_restore_from(ds, fin, finStamp, finDt);
 	cudaStreamSynchronize(st);
-	cudaFree(fin);
-	if(m.block) cudaFree(m.block);
 	memset(&d->tape, 0, sizeof(d->tape));
 	free(finStamp); free(finDt); free(h);
 	return rc;

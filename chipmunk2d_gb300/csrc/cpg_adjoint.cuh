@@ -569,3 +569,156 @@ CPG_HD void geom_adjoint(const GContacts &g, int count, const double *r1bar, con
 		poseBar[3] -= r2bar[2*k]; poseBar[4] -= r2bar[2*k + 1];
 	}
 }
+
+/* ---------------------------------------------------------------------
+ * Four lanes per contact for the reverse of an application, as the
+ * forward solve runs it: lane q takes side q & 1 (0: body a, 1: body b)
+ * and part q >> 1 (0: velocity with the normal and friction impulse,
+ * 1: bias velocity with the bias impulse).  The two parts touch disjoint
+ * state.  Within a part, each lane computes its body's share of the
+ * impulse adjoint (phase 1); the shares are added across the pair (a
+ * shuffle on the device); both lanes then run the scalar part and update
+ * their own body (phase 2).  The constants' adjoints go to per-lane
+ * partial sums: r1 and 1/m_a on side 0, r2 and 1/m_b on side 1, the
+ * contact's scalars on side 0 only.  Summed over the four lanes they equal
+ * app_adjoint's up to the order of the additions.
+ * ------------------------------------------------------------------- */
+struct AdjLane {
+	int side, part;
+	double minv, iinv, rx, ry;    /* the lane's body: 1/m, 1/I, r1 or r2 */
+};
+
+/* Phase 1: the lane's share of the adjoint of the impulse (J for part 0,
+ * the bias impulse for part 1), from its body's adjoint (ax, ay, aw) after
+ * the application.  Partial adjoints of r and 1/m go to cb. */
+CPG_HD void quad_adj_phase1(const AdjCon &c, const AdjApp &t, const AdjLane &L, double ax, double ay, double aw,
+	double &jbx, double &jby, AdjConBar &cb)
+{
+	double nx = c.nx, ny = c.ny;
+	double Jx, Jy;
+	if(L.part == 0){
+		double dN = t.jN1 - t.jN0, dT = t.jT1 - t.jT0;
+		Jx = nx*dN - ny*dT; Jy = nx*dT + ny*dN;
+	} else {
+		double db = t.jB1 - t.jB0;
+		Jx = nx*db; Jy = ny*db;
+	}
+	double s = L.side ? 1.0 : -1.0;          /* b receives J, a receives -J */
+	jbx = s*L.minv*ax; jby = s*L.minv*ay;
+	double gm = s*(Jx*ax + Jy*ay);
+	double g = s*L.iinv*aw;
+	if(L.side){ cb.minvB += gm; cb.r2x += g*Jy; cb.r2y += -g*Jx; }
+	else { cb.minvA += gm; cb.r1x += g*Jy; cb.r1y += -g*Jx; }
+	jbx += -g*L.ry; jby += g*L.rx;
+}
+
+/* Phase 2: with the pair's total (Jbx, Jby), the scalar part (both lanes of
+ * a part compute it; side 0 keeps the constants' adjoints), then the
+ * lane's own body adjoint (ax, ay, aw) for the relative velocity.  jA, jB2
+ * are the accumulator adjoints the part carries: (jN, jT) for part 0, (jB,
+ * unused) for part 1. */
+CPG_HD void quad_adj_phase2(const AdjCon &c, const AdjApp &t, const AdjLane &L, double Jbx, double Jby,
+	double &ax, double &ay, double &aw, double &jA, double &jB2, AdjConBar &cb)
+{
+	double nx = c.nx, ny = c.ny;
+	bool keep = (L.side == 0);
+	double dbx, dby, wown;
+	if(L.part == 0){
+		double vrn = t.vrx*nx + t.vry*ny;
+		double vrt = t.vrx*(-ny) + t.vry*nx;
+		double jn = -(c.bounce + vrn)*c.nMass;
+		bool activeN = (t.jN0 + jn > 0.0);
+		double jtMax = c.u*t.jN1;
+		double jt = -vrt*c.tMass;
+		double f = t.jT0 + jt;
+		int sd = (f > -jtMax) ? 0 : 1;
+		double m = sd ? -jtMax : f;
+		if(!(m < jtMax)) sd = 2;
+		double dN = t.jN1 - t.jN0, dT = t.jT1 - t.jT0;
+		double dNbar = Jbx*nx + Jby*ny;
+		double dTbar = -Jbx*ny + Jby*nx;
+		if(keep){ cb.nx += Jbx*dN + Jby*dT; cb.ny += -Jbx*dT + Jby*dN; }
+		double jN1bar = jA + dNbar, jN0bar = -dNbar;
+		double jT1bar = jB2 + dTbar, jT0bar = -dTbar;
+		double fbar = 0.0, jtMaxbar = 0.0;
+		if(sd == 0) fbar = jT1bar; else if(sd == 1) jtMaxbar = -jT1bar; else jtMaxbar = jT1bar;
+		jT0bar += fbar;
+		double vrtbar = -fbar*c.tMass;
+		if(keep){ cb.tMass += -fbar*vrt; cb.u += jtMaxbar*t.jN1; }
+		jN1bar += jtMaxbar*c.u;
+		double jnbar = 0.0;
+		if(activeN){ jN0bar += jN1bar; jnbar = jN1bar; }
+		if(keep){ cb.bounce += -jnbar*c.nMass; cb.nMass += -jnbar*(c.bounce + vrn); }
+		double vrnbar = -jnbar*c.nMass;
+		dbx = vrnbar*nx - vrtbar*ny;
+		dby = vrnbar*ny + vrtbar*nx;
+		if(keep){ cb.nx += vrnbar*t.vrx + vrtbar*t.vry; cb.ny += vrnbar*t.vry - vrtbar*t.vrx; }
+		jA = jN0bar; jB2 = jT0bar;
+		wown = L.side ? t.wB : t.wA;
+	} else {
+		double vbn = t.vbx*nx + t.vby*ny;
+		double jbn = (c.bias - vbn)*c.nMass;
+		bool activeB = (t.jB0 + jbn > 0.0);
+		double db = t.jB1 - t.jB0;
+		double dbbar = Jbx*nx + Jby*ny;
+		if(keep){ cb.nx += Jbx*db; cb.ny += Jby*db; }
+		double jB1bar = jA + dbbar, jB0bar = -dbbar;
+		double jbnbar = 0.0;
+		if(activeB){ jB0bar += jB1bar; jbnbar = jB1bar; }
+		if(keep){ cb.bias += jbnbar*c.nMass; cb.nMass += jbnbar*(c.bias - vbn); }
+		double vbnbar = -jbnbar*c.nMass;
+		if(keep){ cb.nx += vbnbar*t.vbx; cb.ny += vbnbar*t.vby; }
+		dbx = vbnbar*nx; dby = vbnbar*ny;
+		jA = jB0bar;
+		wown = L.side ? t.wbB : t.wbA;
+	}
+	/* d = (v_b + perp(r2) w_b) - (v_a + perp(r1) w_a) */
+	if(L.side){
+		ax += dbx; ay += dby;
+		aw += -dbx*L.ry + dby*L.rx;
+		cb.r2y += -dbx*wown; cb.r2x += dby*wown;
+	} else {
+		ax -= dbx; ay -= dby;
+		aw += dbx*L.ry - dby*L.rx;
+		cb.r1y += dbx*wown; cb.r1x += -dby*wown;
+	}
+}
+
+/* Warm start on the two velocity lanes: phase 1 as for an application
+ * (with J = rotate(n, (jN, jT))*dt_coef), then this. */
+CPG_HD void quad_warm_phase2(const AdjCon &c, const AdjLane &L, double jN, double jT, double dt_coef, double Jbx, double Jby,
+	double &jNbar, double &jTbar, AdjConBar &cb)
+{
+	double nx = c.nx, ny = c.ny;
+	double jxbar = Jbx*dt_coef, jybar = Jby*dt_coef;
+	jNbar += jxbar*nx + jybar*ny;
+	jTbar += -jxbar*ny + jybar*nx;
+	if(L.side == 0){ cb.nx += jxbar*jN + jybar*jT; cb.ny += -jxbar*jT + jybar*jN; }
+}
+
+/* Phase 1 of the warm start: J = rotate(n, (jN, jT))*dt_coef. */
+CPG_HD void quad_warm_phase1(const AdjCon &c, const AdjLane &L, double jN, double jT, double dt_coef, double ax, double ay, double aw,
+	double &jbx, double &jby, AdjConBar &cb)
+{
+	double nx = c.nx, ny = c.ny;
+	double jx = nx*jN - ny*jT, jy = nx*jT + ny*jN;
+	double Jx = jx*dt_coef, Jy = jy*dt_coef;
+	double s = L.side ? 1.0 : -1.0;
+	jbx = s*L.minv*ax; jby = s*L.minv*ay;
+	double gm = s*(Jx*ax + Jy*ay);
+	double g = s*L.iinv*aw;
+	if(L.side){ cb.minvB += gm; cb.r2x += g*Jy; cb.r2y += -g*Jx; }
+	else { cb.minvA += gm; cb.r1x += g*Jy; cb.r1y += -g*Jx; }
+	jbx += -g*L.ry; jby += g*L.rx;
+}
+
+CPG_HD AdjLane adj_lane(const AdjCon &c, int q)
+{
+	AdjLane L;
+	L.side = q & 1; L.part = q >> 1;
+	L.minv = L.side ? c.minvB : c.minvA;
+	L.iinv = L.side ? c.iinvB : c.iinvA;
+	L.rx = L.side ? c.r2x : c.r1x;
+	L.ry = L.side ? c.r2y : c.r1y;
+	return L;
+}

@@ -202,6 +202,7 @@ typedef struct cpgTape {
 	cpgParams *params;        /* [K][nworlds] */
 	cpgRow *rows;             /* [rowCap] rows of all recorded steps, world by world */
 	int *rowInfo;             /* [rowCap][4]: arbiter shapes a, b; final GJK id; warm-start sources */
+	int *rowWorld;            /* [rowCap] world of the row */
 	int *rowOff;              /* [K][nworlds + 1] */
 	int *levels;              /* [levCap] level starts (relative to the world's rows) */
 	int *levOff;              /* [K][nworlds + 1] */
@@ -307,8 +308,9 @@ typedef struct cpgAdj {
 	double *arb;                  /* [arbCap][2][2]: adjoints of the stored jnAcc, jtAcc of each arbiter contact */
 	double *gMinv;                /* [totalBodies] dL/d(1/m) */
 	double *gE, *gU;              /* [totalShapes] dL/de, dL/du */
-	double *con;                  /* [rowCap][2][16] per-contact scratch */
-	double *unit;                 /* [rowCap][2] per-unit dL/d(arbiter e), dL/d(arbiter u) */
+	double *con;                  /* [rowCap][2][4][16] per contact and lane scratch */
+	double *unit;                 /* [rowCap][20] per-unit contributions of the pre-step and geometry adjoints */
+	double *arbTmp;               /* [arbCap][2][2] remapping buffer */
 } cpgAdj;
 
 /* ---- launchers (cpg_kernels.cu) ---- */
@@ -317,7 +319,8 @@ int cpg_launch_step(const cpgSet *s, const cpgSet *host_mirror, int mode, void *
 int cpg_launch_gather_arbs(const cpgSet *s, int world, cpgArb *out, int n, void *stream);
 long long cpg_launch_count(int reset);
 int cpg_launch_tape(const cpgSet *s, void *stream);
-int cpg_launch_adjoint(const cpgSet *s, const cpgAdj *a, int step, void *stream);
+int cpg_launch_adjoint(const cpgSet *s, const cpgAdj *a, int step, int rows, void *stream);
+int cpg_launch_adjoint_remap(const cpgSet *s, const cpgAdj *a, const void *oldKeys, void *stream);
 
 #ifdef __cplusplus
 }

@@ -8,10 +8,11 @@
  * velocities, world geometry, the pre-step rows with their arbiter data,
  * the level structure, and per impulse application the accumulators and
  * velocities the solver saw, written by the solve kernel itself), then
- * runs k_adj_step for the K steps in reverse.
+ * runs the K steps in reverse.
  *
- * k_adj_step, one block per world, reverses one step (cpSpaceStep.c:
- * 335-445) in the opposite order of the forward:
+ * The reverse of one step (cpSpaceStep.c:335-445) runs in the opposite
+ * order of the forward (k_adj_solve per world, k_adj_geom per unit,
+ * k_adj_accum per world):
  *   1. the adjoints of the impulses stored in the arbiters at the end of
  *      the step seed the contacts' accumulators;
  *   2. the iterations in reverse, levels in reverse (units of one level
@@ -23,7 +24,8 @@
  *   4. velocity integration (damping) and the bias velocities, which the
  *      step starts at zero;
  *   5. pre-step (prestep_adjoint) and contact geometry (geom_contacts in
- *      dual numbers, geom_adjoint) per unit, by levels;
+ *      dual numbers, geom_adjoint), one thread per unit over all worlds,
+ *      then added into the body adjoints level by level;
  *   6. position integration, which turns the pose adjoints into those of
  *      the previous step's velocities and bias velocities.
  * Parameter gradients: 1/m per body (impulses, pre-step masses), and the
@@ -130,6 +132,7 @@ __global__ void k_tape_rows(cpgSet s)
 		if(ro + k >= tp.rowCap) break;
 		const cpgRow &row = s.rows[W.unitOff + k];
 		tp.rows[ro + k] = row;
+		tp.rowWorld[ro + k] = w;
 		int *info = tp.rowInfo + 4*(size_t)(ro + k);
 		if(row.kind == 0){
 			const cpgArb &arb = s.arbs[row.src];
@@ -157,11 +160,14 @@ extern "C" int cpg_launch_tape(const cpgSet *s, void *stream)
 
 /* ---- reverse pass ---- */
 
-struct AdjScratch { AdjConBar cb; double jN, jT, jB; };
+/* Per contact and lane: the lane's partial adjoints of the contact's
+ * constants, and the accumulator adjoints its part carries (velocity
+ * lanes: jnAcc, jtAcc; bias lanes: jBias). */
+struct AdjScratch { AdjConBar cb; double jA, j2, pad; };
 
-__device__ __forceinline__ AdjScratch *con_scratch(const cpgAdj &a, size_t row, int c)
+__device__ __forceinline__ AdjScratch *con_scratch(const cpgAdj &a, size_t row, int c, int lane)
 {
-	return (AdjScratch *)(a.con + (row*2 + (size_t)c)*16);
+	return (AdjScratch *)(a.con + ((row*2 + (size_t)c)*4 + (size_t)lane)*16);
 }
 
 __device__ __forceinline__ AdjBody load_bar(const cpgAdj &a, int g)
@@ -209,7 +215,13 @@ __device__ GShape tape_gshape(const cpgSet &s, int t, int g, int bodyG, int side
 	return r;
 }
 
-__global__ void k_adj_step(cpgSet s, cpgAdj a, int t)
+/* Per-unit contributions of the pre-step and geometry adjoints (a.unit). */
+enum { U_POSE = 0, U_PA = 6, U_PB = 8, U_VA = 10, U_WA = 12, U_VB = 13, U_WB = 15, U_MA = 16, U_MB = 17, U_E = 18, U_U = 19, U_N = 20 };
+
+/* Steps 1-4 of the reverse step (one block per world, four lanes per
+ * unit as in the forward solve): the impulses stored at the end, the
+ * iterations and the warm start in reverse, velocity integration. */
+__global__ void k_adj_solve(cpgSet s, cpgAdj a, int t)
 {
 	int w = blockIdx.x;
 	const cpgTape &tp = s.tape;
@@ -226,22 +238,28 @@ __global__ void k_adj_step(cpgSet s, cpgAdj a, int t)
 	const int *info = tp.rowInfo + 4*(size_t)ro;
 	int iters = P.iterations;
 	int tid = threadIdx.x, nt = blockDim.x;
+	int lane4 = tid & 3, quad = tid >> 2, nq = nt >> 2;
+	int side = lane4 & 1, part = lane4 >> 1;
+	unsigned qmask = 0xFu << (tid & 28);
+	unsigned pmask = 0x3u << (tid & 28);     /* the quad's two velocity lanes */
 	int nbw = W.nbodies, bo = W.bodyOff;
-	int nb = s.totalBodies;
-	const double *bd = tp.body + (size_t)t*8*nb;
 
 	/* 1. adjoints of the impulses stored at the end of the step */
-	for(int k = tid; k < n; k += nt){
+	for(int k = quad; k < n; k += nq){
 		const cpgRow &row = rows[k];
 		for(int c = 0; c < 2; c++){
-			AdjScratch *sc = con_scratch(a, ro + k, c);
+			AdjScratch *sc = con_scratch(a, ro + k, c, lane4);
 			adj_zero(sc->cb);
-			sc->jN = 0.0; sc->jT = 0.0; sc->jB = 0.0;
-			if(row.kind == 0){
-				double *arb = a.arb + 4*(size_t)row.src + 2*c;
-				if(c < row.count){ sc->jN = arb[0]; sc->jT = arb[1]; }
-				arb[0] = 0.0; arb[1] = 0.0;
+			sc->jA = 0.0; sc->j2 = 0.0;
+			if(row.kind == 0 && part == 0 && c < row.count){
+				const double *arb = a.arb + 4*(size_t)row.src + 2*c;
+				sc->jA = arb[0]; sc->j2 = arb[1];
 			}
+		}
+		__syncwarp(qmask);
+		if(lane4 == 0 && row.kind == 0){
+			double *arb = a.arb + 4*(size_t)row.src;
+			arb[0] = 0.0; arb[1] = 0.0; arb[2] = 0.0; arb[3] = 0.0;
 		}
 	}
 	__syncthreads();
@@ -249,47 +267,65 @@ __global__ void k_adj_step(cpgSet s, cpgAdj a, int t)
 	/* 2. iterations in reverse */
 	for(int pass = iters; pass >= 1; pass--){
 		for(int l = nlev - 1; l >= 0; l--){
-			for(int k = start[l] + tid; k < start[l + 1]; k += nt){
+			for(int k = start[l] + quad; k < start[l + 1]; k += nq){
 				const cpgRow &row = rows[k];
 				if(row.kind != 0) continue;
 				int ga = bo + row.a, gb = bo + row.b;
-				bool da = (row.flags & ROW_DYN_A_) != 0, db = (row.flags & ROW_DYN_B_) != 0;
-				AdjBody A = {0, 0, 0, 0, 0, 0}, B = {0, 0, 0, 0, 0, 0};
-				if(da) A = load_bar(a, ga);
-				if(db) B = load_bar(a, gb);
+				int g = side ? gb : ga;
+				bool dyn = (row.flags & (side ? ROW_DYN_B_ : ROW_DYN_A_)) != 0;
+				double *bar = a.body + 9*(size_t)g + 3 + 3*part;
+				double ax = 0.0, ay = 0.0, aw = 0.0;
+				if(dyn){ ax = bar[0]; ay = bar[1]; aw = bar[2]; }
 				const AdjApp *rec = (const AdjApp *)tp.app + ((size_t)(ro + k)*iters + (pass - 1))*2;
 				for(int c = row.count - 1; c >= 0; c--){
 					AdjCon con = make_con(s, row, c, ga, gb);
-					AdjScratch *sc = con_scratch(a, ro + k, c);
-					app_adjoint(con, rec[c], A, B, sc->jN, sc->jT, sc->jB, sc->cb);
+					AdjLane L = adj_lane(con, lane4);
+					AdjScratch *sc = con_scratch(a, ro + k, c, lane4);
+					double jbx, jby;
+					quad_adj_phase1(con, rec[c], L, ax, ay, aw, jbx, jby, sc->cb);
+					jbx += __shfl_xor_sync(qmask, jbx, 1);
+					jby += __shfl_xor_sync(qmask, jby, 1);
+					quad_adj_phase2(con, rec[c], L, jbx, jby, ax, ay, aw, sc->jA, sc->j2, sc->cb);
 				}
-				if(da) store_bar(a, ga, A);
-				if(db) store_bar(a, gb, B);
+				if(dyn){ bar[0] = ax; bar[1] = ay; bar[2] = aw; }
 			}
 			__syncthreads();
 		}
 	}
 
-	/* 3. warm start (reads the body adjoints only), then the initial
-	 * accumulators' adjoints go to their source contacts */
-	for(int k = tid; k < n; k += nt){
+	/* 3. warm start on the velocity lanes (the body adjoints pass through),
+	 * then the initial accumulators' adjoints go to their source contacts */
+	for(int k = quad; k < n; k += nq){
 		const cpgRow &row = rows[k];
 		if(row.kind != 0) continue;
 		int ga = bo + row.a, gb = bo + row.b;
-		bool da = (row.flags & ROW_DYN_A_) != 0, db = (row.flags & ROW_DYN_B_) != 0;
-		AdjBody A = {0, 0, 0, 0, 0, 0}, B = {0, 0, 0, 0, 0, 0};
-		if(da) A = load_bar(a, ga);
-		if(db) B = load_bar(a, gb);
-		int src = info[4*k + 3];
-		for(int c = row.count - 1; c >= 0; c--){
-			AdjCon con = make_con(s, row, c, ga, gb);
-			AdjScratch *sc = con_scratch(a, ro + k, c);
-			if(!(row.flags & ROW_FIRST_))
-				warm_adjoint(con, row.arb.c[c].jnAcc, row.arb.c[c].jtAcc, P.dt_coef, A, B, sc->jN, sc->jT, sc->cb);
-			int j = ((src >> (4*c)) & 0xF) - 1;
-			if(j >= 0 && j < 2){
-				double *arb = a.arb + 4*(size_t)row.src + 2*j;
-				arb[0] += sc->jN; arb[1] += sc->jT;
+		if(part == 0 && !(row.flags & ROW_FIRST_)){
+			int g = side ? gb : ga;
+			bool dyn = (row.flags & (side ? ROW_DYN_B_ : ROW_DYN_A_)) != 0;
+			const double *bar = a.body + 9*(size_t)g + 3;
+			double ax = 0.0, ay = 0.0, aw = 0.0;
+			if(dyn){ ax = bar[0]; ay = bar[1]; aw = bar[2]; }
+			for(int c = row.count - 1; c >= 0; c--){
+				AdjCon con = make_con(s, row, c, ga, gb);
+				AdjLane L = adj_lane(con, lane4);
+				AdjScratch *sc = con_scratch(a, ro + k, c, lane4);
+				double jN = row.arb.c[c].jnAcc, jT = row.arb.c[c].jtAcc;
+				double jbx, jby;
+				quad_warm_phase1(con, L, jN, jT, P.dt_coef, ax, ay, aw, jbx, jby, sc->cb);
+				jbx += __shfl_xor_sync(pmask, jbx, 1);
+				jby += __shfl_xor_sync(pmask, jby, 1);
+				quad_warm_phase2(con, L, jN, jT, P.dt_coef, jbx, jby, sc->jA, sc->j2, sc->cb);
+			}
+		}
+		if(lane4 == 0){
+			int src = info[4*k + 3];
+			for(int c = 0; c < row.count && c < 2; c++){
+				int j = ((src >> (4*c)) & 0xF) - 1;
+				if(j >= 0 && j < 2){
+					const AdjScratch *sc = con_scratch(a, ro + k, c, 0);
+					double *arb = a.arb + 4*(size_t)row.src + 2*j;
+					arb[0] += sc->jA; arb[1] += sc->j2;
+				}
 			}
 		}
 	}
@@ -303,69 +339,114 @@ __global__ void k_adj_step(cpgSet s, cpgAdj a, int t)
 		b[3] *= P.damping; b[4] *= P.damping; b[5] *= P.damping;
 		b[6] = 0.0; b[7] = 0.0; b[8] = 0.0;
 	}
-	__syncthreads();
+}
 
-	/* 5. pre-step and contact geometry, by levels */
-	for(int l = nlev - 1; l >= 0; l--){
+/* Step 5a, one thread per unit of the step (all worlds): the pre-step and
+ * contact geometry adjoints of the unit, into a.unit. */
+__global__ void k_adj_geom(cpgSet s, cpgAdj a, int t)
+{
+	const cpgTape &tp = s.tape;
+	int nw = s.nworlds;
+	int r0 = tp.rowOff[(size_t)t*(nw + 1)], r1 = tp.rowOff[(size_t)t*(nw + 1) + nw];
+	int r = r0 + blockIdx.x*blockDim.x + threadIdx.x;
+	if(r >= r1) return;
+	const cpgRow &row = tp.rows[r];
+	double *u = a.unit + (size_t)U_N*r;
+	for(int i = 0; i < U_N; i++) u[i] = 0.0;
+	if(row.kind != 0) return;
+	int w = tp.rowWorld[r];
+	const cpgParams &P = tp.params[(size_t)t*nw + w];
+	const cpgWorld &W = s.world[w];
+	const int *info = tp.rowInfo + 4*(size_t)r;
+	int nb = s.totalBodies;
+	const double *bd = tp.body + (size_t)t*8*nb;
+	int ga = W.bodyOff + row.a, gb = W.bodyOff + row.b;
+	bool da = (row.flags & ROW_DYN_A_) != 0, db = (row.flags & ROW_DYN_B_) != 0;
+	double r1bar[4] = {0, 0, 0, 0}, r2bar[4] = {0, 0, 0, 0}, nbx = 0.0, nby = 0.0;
+	for(int c = 0; c < row.count && c < 2; c++){
+		const cpgRowContact &rc = row.arb.c[c];
+		AdjPre p;
+		p.r1x = rc.r1x; p.r1y = rc.r1y; p.r2x = rc.r2x; p.r2y = rc.r2y;
+		p.nx = row.arb.nx; p.ny = row.arb.ny;
+		p.pAx = bd[ga]; p.pAy = bd[nb + ga]; p.pBx = bd[gb]; p.pBy = bd[nb + gb];
+		p.vAx = bd[3*(size_t)nb + ga]; p.vAy = bd[4*(size_t)nb + ga]; p.wA = bd[5*(size_t)nb + ga];
+		p.vBx = bd[3*(size_t)nb + gb]; p.vBy = bd[4*(size_t)nb + gb]; p.wB = bd[5*(size_t)nb + gb];
+		p.minvA = s.minv[ga]; p.minvB = s.minv[gb]; p.iinvA = s.iinv[ga]; p.iinvB = s.iinv[gb];
+		p.e = row.arb.e;
+		p.biasCoef = P.biasCoef; p.slop = P.slop; p.dt = P.dt;
+		/* the four lanes' partial adjoints of the contact's constants */
+		AdjConBar cb; adj_zero(cb);
+		for(int q = 0; q < 4; q++){
+			const AdjConBar &l = con_scratch(a, r, c, q)->cb;
+			cb.r1x += l.r1x; cb.r1y += l.r1y; cb.r2x += l.r2x; cb.r2y += l.r2y;
+			cb.nx += l.nx; cb.ny += l.ny; cb.nMass += l.nMass; cb.tMass += l.tMass;
+			cb.bias += l.bias; cb.bounce += l.bounce; cb.u += l.u;
+			cb.minvA += l.minvA; cb.minvB += l.minvB;
+		}
+		const AdjConBar *scb = &cb;
+		AdjPreBar pb; adj_zero(pb);
+		prestep_adjoint(p, scb->nMass, scb->tMass, scb->bias, scb->bounce, pb);
+		r1bar[2*c] = scb->r1x + pb.r1x; r1bar[2*c + 1] = scb->r1y + pb.r1y;
+		r2bar[2*c] = scb->r2x + pb.r2x; r2bar[2*c + 1] = scb->r2y + pb.r2y;
+		nbx += scb->nx + pb.nx; nby += scb->ny + pb.ny;
+		u[U_PA] += pb.pAx; u[U_PA + 1] += pb.pAy; u[U_PB] += pb.pBx; u[U_PB + 1] += pb.pBy;
+		u[U_VA] += pb.vAx; u[U_VA + 1] += pb.vAy; u[U_WA] += pb.wA;
+		u[U_VB] += pb.vBx; u[U_VB + 1] += pb.vBy; u[U_WB] += pb.wB;
+		u[U_MA] += scb->minvA + pb.minvA; u[U_MB] += scb->minvB + pb.minvB;
+		u[U_E] += pb.e;
+		u[U_U] += scb->u;
+	}
+	/* geometry: the arbiter's shapes in the order the forward stored */
+	int sa = W.shapeOff + info[0], sb = W.shapeOff + info[1];
+	GShape SA = tape_gshape(s, t, sa, ga, da ? 0 : -1);
+	GShape SB = tape_gshape(s, t, sb, gb, db ? 1 : -1);
+	GContacts g;
+	geom_contacts(SA, SB, (unsigned)info[2], g);
+	if(g.count == row.count) geom_adjoint(g, row.count, r1bar, r2bar, nbx, nby, u + U_POSE);
+	else atomicOr(&tp.cursor[3], 2);
+}
+
+/* Steps 5b and 6 (one block per world): unit contributions into the body
+ * adjoints level by level (units of a level touch disjoint dynamic
+ * bodies), position integration, per-shape e and u in unit order. */
+__global__ void k_adj_accum(cpgSet s, cpgAdj a, int t)
+{
+	int w = blockIdx.x;
+	const cpgTape &tp = s.tape;
+	int nw = s.nworlds;
+	const cpgParams P = tp.params[(size_t)t*nw + w];
+	if(!P.active) return;
+	const cpgWorld &W = s.world[w];
+	int ro = tp.rowOff[(size_t)t*(nw + 1) + w];
+	int n = tp.rowOff[(size_t)t*(nw + 1) + w + 1] - ro;
+	int lo = tp.levOff[(size_t)t*(nw + 1) + w];
+	int nlev = tp.levOff[(size_t)t*(nw + 1) + w + 1] - lo - 1;
+	const int *start = tp.levels + lo;
+	const cpgRow *rows = tp.rows + ro;
+	const int *info = tp.rowInfo + 4*(size_t)ro;
+	int tid = threadIdx.x, nt = blockDim.x;
+	int nbw = W.nbodies, bo = W.bodyOff;
+	for(int l = 0; l < nlev; l++){
 		for(int k = start[l] + tid; k < start[l + 1]; k += nt){
 			const cpgRow &row = rows[k];
 			if(row.kind != 0) continue;
+			const double *u = a.unit + (size_t)U_N*(ro + k);
 			int ga = bo + row.a, gb = bo + row.b;
-			bool da = (row.flags & ROW_DYN_A_) != 0, db = (row.flags & ROW_DYN_B_) != 0;
-			double r1bar[4] = {0, 0, 0, 0}, r2bar[4] = {0, 0, 0, 0}, nbx = 0.0, nby = 0.0;
-			AdjPreBar tot; adj_zero(tot);
-			double uArb = 0.0, mA = 0.0, mB = 0.0;
-			for(int c = 0; c < row.count && c < 2; c++){
-				const cpgRowContact &rc = row.arb.c[c];
-				AdjPre p;
-				p.r1x = rc.r1x; p.r1y = rc.r1y; p.r2x = rc.r2x; p.r2y = rc.r2y;
-				p.nx = row.arb.nx; p.ny = row.arb.ny;
-				p.pAx = bd[ga]; p.pAy = bd[nb + ga]; p.pBx = bd[gb]; p.pBy = bd[nb + gb];
-				p.vAx = bd[3*(size_t)nb + ga]; p.vAy = bd[4*(size_t)nb + ga]; p.wA = bd[5*(size_t)nb + ga];
-				p.vBx = bd[3*(size_t)nb + gb]; p.vBy = bd[4*(size_t)nb + gb]; p.wB = bd[5*(size_t)nb + gb];
-				p.minvA = s.minv[ga]; p.minvB = s.minv[gb]; p.iinvA = s.iinv[ga]; p.iinvB = s.iinv[gb];
-				p.e = row.arb.e;
-				p.biasCoef = P.biasCoef; p.slop = P.slop; p.dt = P.dt;
-				const AdjScratch *sc = con_scratch(a, ro + k, c);
-				AdjPreBar pb; adj_zero(pb);
-				prestep_adjoint(p, sc->cb.nMass, sc->cb.tMass, sc->cb.bias, sc->cb.bounce, pb);
-				r1bar[2*c] = sc->cb.r1x + pb.r1x; r1bar[2*c + 1] = sc->cb.r1y + pb.r1y;
-				r2bar[2*c] = sc->cb.r2x + pb.r2x; r2bar[2*c + 1] = sc->cb.r2y + pb.r2y;
-				nbx += sc->cb.nx + pb.nx; nby += sc->cb.ny + pb.ny;
-				tot.pAx += pb.pAx; tot.pAy += pb.pAy; tot.pBx += pb.pBx; tot.pBy += pb.pBy;
-				tot.vAx += pb.vAx; tot.vAy += pb.vAy; tot.wA += pb.wA;
-				tot.vBx += pb.vBx; tot.vBy += pb.vBy; tot.wB += pb.wB;
-				tot.e += pb.e;
-				uArb += sc->cb.u;
-				mA += sc->cb.minvA + pb.minvA; mB += sc->cb.minvB + pb.minvB;
-			}
-			/* geometry: the arbiter's shapes in the order the forward stored */
-			int sa = W.shapeOff + info[4*k], sb = W.shapeOff + info[4*k + 1];
-			GShape SA = tape_gshape(s, t, sa, ga, da ? 0 : -1);
-			GShape SB = tape_gshape(s, t, sb, gb, db ? 1 : -1);
-			GContacts g;
-			geom_contacts(SA, SB, (unsigned)info[4*k + 2], g);
-			double pose[6] = {0, 0, 0, 0, 0, 0};
-			if(g.count == row.count) geom_adjoint(g, row.count, r1bar, r2bar, nbx, nby, pose);
-			else atomicOr(&tp.cursor[3], 2);
-			if(da){
+			if(row.flags & ROW_DYN_A_){
 				double *b = a.body + 9*(size_t)ga;
-				b[0] += pose[0] + tot.pAx; b[1] += pose[1] + tot.pAy; b[2] += pose[2];
-				b[3] += tot.vAx; b[4] += tot.vAy; b[5] += tot.wA;
-				a.gMinv[ga] += mA;
+				b[0] += u[U_POSE] + u[U_PA]; b[1] += u[U_POSE + 1] + u[U_PA + 1]; b[2] += u[U_POSE + 2];
+				b[3] += u[U_VA]; b[4] += u[U_VA + 1]; b[5] += u[U_WA];
+				a.gMinv[ga] += u[U_MA];
 			}
-			if(db){
+			if(row.flags & ROW_DYN_B_){
 				double *b = a.body + 9*(size_t)gb;
-				b[0] += pose[3] + tot.pBx; b[1] += pose[4] + tot.pBy; b[2] += pose[5];
-				b[3] += tot.vBx; b[4] += tot.vBy; b[5] += tot.wB;
-				a.gMinv[gb] += mB;
+				b[0] += u[U_POSE + 3] + u[U_PB]; b[1] += u[U_POSE + 4] + u[U_PB + 1]; b[2] += u[U_POSE + 5];
+				b[3] += u[U_VB]; b[4] += u[U_VB + 1]; b[5] += u[U_WB];
+				a.gMinv[gb] += u[U_MB];
 			}
-			a.unit[2*(size_t)(ro + k)] = tot.e;
-			a.unit[2*(size_t)(ro + k) + 1] = uArb;
 		}
 		__syncthreads();
 	}
-
 	/* 6. position integration: p' = p + (v + v_bias)*dt, a' = a + (w + w_bias)*dt */
 	for(int i = tid; i < nbw; i += nt){
 		int g = bo + i;
@@ -375,22 +456,65 @@ __global__ void k_adj_step(cpgSet s, cpgAdj a, int t)
 		b[3] += b[0]*dt; b[4] += b[1]*dt; b[5] += b[2]*dt;
 		b[6] = b[0]*dt; b[7] = b[1]*dt; b[8] = b[2]*dt;
 	}
-
-	/* per-shape elasticity and friction, in unit order */
 	if(tid == 0){
 		for(int k = 0; k < n; k++){
 			const cpgRow &row = rows[k];
 			if(row.kind != 0) continue;
 			int sa = W.shapeOff + info[4*k], sb = W.shapeOff + info[4*k + 1];
-			double eb = a.unit[2*(size_t)(ro + k)], ub = a.unit[2*(size_t)(ro + k) + 1];
-			a.gE[sa] += eb*s.se[sb]; a.gE[sb] += eb*s.se[sa];
-			a.gU[sa] += ub*s.su[sb]; a.gU[sb] += ub*s.su[sa];
+			const double *u = a.unit + (size_t)U_N*(ro + k);
+			a.gE[sa] += u[U_E]*s.se[sb]; a.gE[sb] += u[U_E]*s.se[sa];
+			a.gU[sa] += u[U_U]*s.su[sb]; a.gU[sb] += u[U_U]*s.su[sa];
 		}
 	}
 }
 
-extern "C" int cpg_launch_adjoint(const cpgSet *s, const cpgAdj *a, int step, void *stream)
+/* The adjoints of the arbiters' stored impulses follow the arbiters across
+ * a checkpoint: slots of arbiters created between checkpoints can differ
+ * between the forward and its replay (the table is filled with atomics),
+ * so the adjoints are moved by key, from the table `oldKeys` numbering to
+ * the current table's. */
+__device__ __forceinline__ unsigned long long mix64r(unsigned long long z)
 {
-	k_adj_step<<<s->nworlds, 256, 0, (cudaStream_t)stream>>>(*s, *a, step);
+	z = (z ^ (z >> 30)) * 0xbf58476d1ce4e5b9ull;
+	z = (z ^ (z >> 27)) * 0x94d049bb133111ebull;
+	return z ^ (z >> 31);
+}
+
+__global__ void k_adj_remap(cpgSet s, const unsigned long long *oldKeys, const double *oldArb, double *newArb)
+{
+	int i = blockIdx.x*blockDim.x + threadIdx.x;
+	if(i >= s.arbCap) return;
+	double *d = newArb + 4*(size_t)i;
+	d[0] = d[1] = d[2] = d[3] = 0.0;
+	unsigned long long key = s.keys[i];
+	if(key < 2ull) return;
+	unsigned mask = (unsigned)s.arbCap - 1;
+	unsigned h = (unsigned)mix64r(key) & mask;
+	for(int probe = 0; probe < s.arbCap; probe++, h = (h + 1) & mask){
+		unsigned long long k = oldKeys[h];
+		if(k == key){
+			const double *o = oldArb + 4*(size_t)h;
+			d[0] = o[0]; d[1] = o[1]; d[2] = o[2]; d[3] = o[3];
+			return;
+		}
+		if(k == 0ull) return;
+	}
+}
+
+extern "C" int cpg_launch_adjoint_remap(const cpgSet *s, const cpgAdj *a, const void *oldKeys, void *stream)
+{
+	cudaStream_t st = (cudaStream_t)stream;
+	k_adj_remap<<<blocks_of(s->arbCap, 256), 256, 0, st>>>(*s, (const unsigned long long *)oldKeys, a->arb, a->arbTmp);
+	cudaMemcpyAsync(a->arb, a->arbTmp, sizeof(double)*4*(size_t)s->arbCap, cudaMemcpyDeviceToDevice, st);
+	return cudaGetLastError() == cudaSuccess ? 0 : -1;
+}
+
+extern "C" int cpg_launch_adjoint(const cpgSet *s, const cpgAdj *a, int step, int rows, void *stream)
+{
+	cudaStream_t st = (cudaStream_t)stream;
+	/* a few units per level: two warps per world keep every world resident */
+	k_adj_solve<<<s->nworlds, 64, 0, st>>>(*s, *a, step);
+	k_adj_geom<<<blocks_of(rows, 128), 128, 0, st>>>(*s, *a, step);
+	k_adj_accum<<<s->nworlds, 64, 0, st>>>(*s, *a, step);
 	return cudaGetLastError() == cudaSuccess ? 0 : -1;
 }

@@ -508,6 +508,10 @@ int cpGpuDebugCandidates(cpSpace *space, int *out, int max);
  * the forward ended in.  Constraints and external forces are not
  * differentiated.  Returns 0 on success, -1 with cpGpuGetLastError() set. */
 int cpGpuRolloutForward(cpGpuBatch *batch, cpFloat dt, int steps, int checkpoint);
+/* Debug: device milliseconds of the last cpGpuRolloutBackward taken with
+ * cpGpuSetTiming(1): [0] replays with recording, [1] reverse steps.
+ * Returns the number of values written (2), or 0. */
+int cpGpuDebugRolloutTimes(cpGpuBatch *batch, double *out);
 int cpGpuRolloutBackward(cpGpuBatch *batch, const cpFloat *dLdp, cpFloat *dLdv0, cpFloat *dLdw0,
 	cpFloat *dLdm, cpFloat *dLde, cpFloat *dLdu);
 void cpGpuSetTiming(int enabled);

@@ -241,6 +241,86 @@ static void test_prestep()
 	printf("pre-step adjoint: %d checks\n", n);
 }
 
+
+/* ---- 1d. four lanes per contact against one lane ---- */
+static void close_to(const char *what, double a, double b)
+{
+	/* the lanes add the same terms in another order: rounding only */
+	double err = fabs(a - b)/(fabs(b) + 1e-3);
+	if(err > 1e-12){
+		if(failures < 20) printf("  FAIL %s: lanes %.17g one lane %.17g\n", what, a, b);
+		failures++;
+	}
+}
+
+static void test_quad_lanes()
+{
+	int n = 0;
+	for(int trial = 0; trial < 4000; trial++){
+		AdjCon c; St s;
+		random_contact(c, s, trial & 7);
+		AdjApp rec;
+		{ AdjCon cc = c; St ss = s; app_forward(cc, ss, &rec); }
+		double w[15];
+		for(int i = 0; i < 15; i++) w[i] = urange(-1, 1);
+		/* one lane */
+		AdjBody A = { w[0], w[1], w[2], w[3], w[4], w[5] }, B = { w[6], w[7], w[8], w[9], w[10], w[11] };
+		double jN = w[12], jT = w[13], jB = w[14];
+		AdjConBar cb; adj_zero(cb);
+		app_adjoint(c, rec, A, B, jN, jT, jB, cb);
+		/* four lanes */
+		double ax[4], ay[4], aw[4], jA[4], j2[4], jbx[4], jby[4];
+		AdjConBar cl[4];
+		for(int q = 0; q < 4; q++){
+			int side = q & 1, part = q >> 1;
+			const double *o = w + 6*side + 3*part;
+			ax[q] = o[0]; ay[q] = o[1]; aw[q] = o[2];
+			jA[q] = part ? w[14] : w[12]; j2[q] = part ? 0.0 : w[13];
+			adj_zero(cl[q]);
+			quad_adj_phase1(c, rec, adj_lane(c, q), ax[q], ay[q], aw[q], jbx[q], jby[q], cl[q]);
+		}
+		for(int q = 0; q < 4; q++){
+			double Jx = jbx[q] + jbx[q ^ 1], Jy = jby[q] + jby[q ^ 1];
+			quad_adj_phase2(c, rec, adj_lane(c, q), Jx, Jy, ax[q], ay[q], aw[q], jA[q], j2[q], cl[q]);
+		}
+		AdjConBar sum; adj_zero(sum);
+		for(int q = 0; q < 4; q++){
+			sum.r1x += cl[q].r1x; sum.r1y += cl[q].r1y; sum.r2x += cl[q].r2x; sum.r2y += cl[q].r2y;
+			sum.nx += cl[q].nx; sum.ny += cl[q].ny; sum.nMass += cl[q].nMass; sum.tMass += cl[q].tMass;
+			sum.bias += cl[q].bias; sum.bounce += cl[q].bounce; sum.u += cl[q].u;
+			sum.minvA += cl[q].minvA; sum.minvB += cl[q].minvB;
+		}
+		char nm[64];
+		double lanes[] = { ax[0], ay[0], aw[0], ax[2], ay[2], aw[2], ax[1], ay[1], aw[1], ax[3], ay[3], aw[3], jA[0], j2[0], jA[2],
+			sum.r1x, sum.r1y, sum.r2x, sum.r2y, sum.nx, sum.ny, sum.nMass, sum.tMass, sum.bias, sum.bounce, sum.u, sum.minvA, sum.minvB };
+		double one[] = { A.vx, A.vy, A.w, A.vbx, A.vby, A.wb, B.vx, B.vy, B.w, B.vbx, B.vby, B.wb, jN, jT, jB,
+			cb.r1x, cb.r1y, cb.r2x, cb.r2y, cb.nx, cb.ny, cb.nMass, cb.tMass, cb.bias, cb.bounce, cb.u, cb.minvA, cb.minvB };
+		for(int i = 0; i < 28; i++){ snprintf(nm, sizeof(nm), "lanes trial %d value %d", trial, i); close_to(nm, lanes[i], one[i]); n++; }
+		/* both lanes of a part carry the same accumulator adjoints */
+		if(jA[0] != jA[1] || j2[0] != j2[1] || jA[2] != jA[3]){ failures++; printf("  FAIL lanes trial %d: pair accumulators differ\n", trial); }
+		/* warm start */
+		AdjBody Aw = { w[0], w[1], w[2], 0, 0, 0 }, Bw = { w[6], w[7], w[8], 0, 0, 0 };
+		double wN = 0.0, wT = 0.0, dtc = urange(0.5, 1.5);
+		AdjConBar wc; adj_zero(wc);
+		warm_adjoint(c, s.jN, s.jT, dtc, Aw, Bw, wN, wT, wc);
+		double qb[2][2]; AdjConBar wl[2]; double qN[2] = {0, 0}, qT[2] = {0, 0};
+		for(int q = 0; q < 2; q++){
+			adj_zero(wl[q]);
+			const double *o = w + 6*q;
+			quad_warm_phase1(c, adj_lane(c, q), s.jN, s.jT, dtc, o[0], o[1], o[2], qb[q][0], qb[q][1], wl[q]);
+		}
+		for(int q = 0; q < 2; q++)
+			quad_warm_phase2(c, adj_lane(c, q), s.jN, s.jT, dtc, qb[q][0] + qb[q ^ 1][0], qb[q][1] + qb[q ^ 1][1], qN[q], qT[q], wl[q]);
+		snprintf(nm, sizeof(nm), "warm lanes trial %d", trial);
+		close_to(nm, qN[0], wN); close_to(nm, qT[0], wT);
+		close_to(nm, wl[0].nx + wl[1].nx, wc.nx); close_to(nm, wl[0].ny + wl[1].ny, wc.ny);
+		close_to(nm, wl[0].r1x + wl[1].r1x, wc.r1x); close_to(nm, wl[0].r2y + wl[1].r2y, wc.r2y);
+		close_to(nm, wl[0].minvA + wl[1].minvA, wc.minvA); close_to(nm, wl[0].minvB + wl[1].minvB, wc.minvB);
+		n += 8;
+	}
+	printf("four-lane adjoint: %d checks\n", n);
+}
+
 /* ---- 2. contact geometry against the narrow phase ---- */
 struct LShape {
 	int kind;
@@ -382,6 +462,7 @@ int main()
 	test_application();
 	test_warm();
 	test_prestep();
+	test_quad_lanes();
 	test_geometry();
 	printf("worst relative error %.3g, failures %d\n", worst_rel, failures);
 	return failures ? 1 : 0;

@@ -141,6 +141,25 @@ def test_gradients_do_not_depend_on_the_checkpoint_interval(gpu_lib):
         np.testing.assert_array_equal(a[k], b[k], err_msg=k)
 
 
+def test_gradients_are_deterministic_at_scale(gpu_lib):
+    """Arbiters created between checkpoints can take other table slots in
+    the replay than in the forward; the carried impulse adjoints follow
+    them by key, so two runs give identical gradients."""
+    global WORLDS, SIZE
+    saved = WORLDS, SIZE
+    WORLDS, SIZE = 256, 64
+    try:
+        seeds = [4000 + i for i in range(WORLDS)]
+        t = targets(WORLDS * SIZE)
+        a, La = rollout_grads(gpu_lib, seeds, 120, 16, t)
+        b, Lb = rollout_grads(gpu_lib, seeds, 120, 16, t)
+        assert La == Lb
+        for k in a:
+            np.testing.assert_array_equal(a[k], b[k], err_msg=k)
+    finally:
+        WORLDS, SIZE = saved
+
+
 def sample_params():
     rng = np.random.default_rng(11)
     ps = []
