@@ -922,6 +922,7 @@ typedef struct Rollout {
 	TapeMem tape;                 /* tape.block == NULL until the first reverse pass */
 	int tapeK, tapeIters;
 	float replayMs, adjointMs;    /* device time of the last reverse pass (with cpGpuSetTiming(1)) */
+	int lastTaped;                /* the forward recorded its last segment into tape */
 } Rollout;
 
 struct cpGpuBatch {
@@ -1035,40 +1036,6 @@ int cpGpuDebugRolloutTimes(cpGpuBatch *b, double *out)
 	return 2;
 }
 
-int cpGpuRolloutForward(cpGpuBatch *b, cpFloat dt, int steps, int checkpoint)
-{
-	if(steps < 1 || checkpoint < 1 || !(dt > 0.0)){ set_error(CP_GPU_ERR_ARGUMENT, "rollout: steps, checkpoint and dt must be positive"); return -1; }
-	if(!batch_ready(b)) return -1;
-	DevSet *ds = b->dev;
-	if(!b->roll) b->roll = (Rollout *)calloc(1, sizeof(Rollout));
-	Rollout *r = b->roll;
-	r->steps = steps; r->K = checkpoint; r->dt = dt;
-	r->nckpt = (steps + checkpoint - 1)/checkpoint;
-	free(r->stamps); free(r->currDt);
-	r->stamps = HALLOC(unsigned, (size_t)r->nckpt*ds->nspaces);
-	r->currDt = HALLOC(double, (size_t)r->nckpt*ds->nspaces);
-	if(r->ckptCap < r->nckpt){
-		if(r->ckpt) cudaFree(r->ckpt);
-		r->ckpt = NULL; r->ckptCap = 0;
-		if(!cuda_ok(cudaMalloc((void **)&r->ckpt, (size_t)r->nckpt*ds->slabBytes), "cudaMalloc checkpoints")){
-			r->ckpt = NULL;
-			set_error(CP_GPU_ERR_OVERFLOW, "rollout: no device memory for %d checkpoints of %zu bytes", r->nckpt, ds->slabBytes);
-			return -1;
-		}
-		r->ckptCap = r->nckpt;
-	}
-	double *dts = (double *)malloc(sizeof(double)*(size_t)b->n);
-	for(int i = 0; i < b->n; i++) dts[i] = dt;
-	int rc = 0;
-	for(int s = 0; s < steps && rc == 0; s++){
-		if(s % checkpoint == 0) rollout_save(b, s/checkpoint);
-		rc = devset_step(ds, dts, NULL);
-	}
-	free(dts);
-	return rc;
-}
-
-
 static size_t tape_carve(cpgSet *d, TapeMem *m, char *base, int K, size_t rowCap, int iters, int pass)
 {
 	size_t total = 0;
@@ -1092,7 +1059,7 @@ static size_t tape_carve(cpgSet *d, TapeMem *m, char *base, int K, size_t rowCap
 	TCARVE(m->a.gMinv, double, d->totalBodies);
 	TCARVE(m->a.gE, double, d->totalShapes);
 	TCARVE(m->a.gU, double, d->totalShapes);
-	TCARVE(m->a.con, double, rowCap*2*4*16);
+	TCARVE(m->a.con, double, rowCap*2*4*CPG_ADJ_LANE_DOUBLES);
 	TCARVE(m->a.unit, double, rowCap*20);
 	TCARVE(m->a.arbTmp, double, 4*(size_t)d->arbCap);
 #undef TCARVE
@@ -1110,6 +1077,101 @@ static int tape_alloc(cpgSet *d, TapeMem *m, int K, size_t rowCap, int iters)
 	return 1;
 }
 
+/* The iteration count shared by every space of the batch, or -1. */
+static int rollout_iterations(DevSet *ds)
+{
+	int iters = ds->nspaces ? ds->spaces[0]->iterations : 0;
+	for(int w = 1; w < ds->nspaces; w++) if(ds->spaces[w]->iterations != iters) return -1;
+	return iters;
+}
+
+/* The tape for segments of K steps and at least rowCap rows: the one kept
+ * from an earlier pass if it fits, else a new one. */
+static int rollout_tape(DevSet *ds, Rollout *r, int K, int iters, size_t rowCap)
+{
+	if(r->tape.block && r->tapeK == K && r->tapeIters == iters && (size_t)r->tape.t.rowCap >= rowCap) return 1;
+	if(r->tape.block) cudaFree(r->tape.block);
+	memset(&r->tape, 0, sizeof(r->tape));
+	r->tapeK = 0;
+	if(!tape_alloc(&ds->d, &r->tape, K, rowCap, iters)) return 0;
+	r->tapeK = K; r->tapeIters = iters;
+	return 1;
+}
+
+/* Tape rows for K steps: what a previous pass needed, else twice the
+ * solved arbiters of the latest step plus the joints. */
+static size_t rollout_row_estimate(DevSet *ds, Rollout *r, int K)
+{
+	if(r->rowCap) return r->rowCap;
+	check_stats(ds);
+	return (size_t)K*(2*(size_t)(ds->hstats[5] > 0 ? ds->hstats[5] : 0) + (size_t)ds->d.totalCons + 1024);
+}
+
+int cpGpuRolloutForward(cpGpuBatch *b, cpFloat dt, int steps, int checkpoint)
+{
+	if(steps < 1 || checkpoint < 1 || !(dt > 0.0)){ set_error(CP_GPU_ERR_ARGUMENT, "rollout: steps, checkpoint and dt must be positive"); return -1; }
+	if(!batch_ready(b)) return -1;
+	DevSet *ds = b->dev;
+	cpgSet *d = &ds->d;
+	cudaStream_t st = lib_stream();
+	if(!b->roll) b->roll = (Rollout *)calloc(1, sizeof(Rollout));
+	Rollout *r = b->roll;
+	r->steps = steps; r->K = checkpoint; r->dt = dt;
+	r->nckpt = (steps + checkpoint - 1)/checkpoint;
+	r->lastTaped = 0;
+	free(r->stamps); free(r->currDt);
+	r->stamps = HALLOC(unsigned, (size_t)r->nckpt*ds->nspaces);
+	r->currDt = HALLOC(double, (size_t)r->nckpt*ds->nspaces);
+	if(r->ckptCap < r->nckpt){
+		if(r->ckpt) cudaFree(r->ckpt);
+		r->ckpt = NULL; r->ckptCap = 0;
+		if(!cuda_ok(cudaMalloc((void **)&r->ckpt, (size_t)r->nckpt*ds->slabBytes), "cudaMalloc checkpoints")){
+			r->ckpt = NULL;
+			set_error(CP_GPU_ERR_OVERFLOW, "rollout: no device memory for %d checkpoints of %zu bytes", r->nckpt, ds->slabBytes);
+			return -1;
+		}
+		r->ckptCap = r->nckpt;
+	}
+	double *dts = (double *)malloc(sizeof(double)*(size_t)b->n);
+	for(int i = 0; i < b->n; i++) dts[i] = dt;
+	/* the last segment is recorded as it runs, so the reverse pass starts
+	 * on it without a replay; without a tape (no memory, mixed iteration
+	 * counts) or past its capacity the reverse pass replays it */
+	int last = (r->nckpt - 1)*checkpoint, iters = rollout_iterations(ds), taping = 0;
+	int rc = 0;
+	for(int s = 0; s < steps && rc == 0; s++){
+		if(s % checkpoint == 0) rollout_save(b, s/checkpoint);
+		if(s == last && iters > 0){
+			size_t rowCap = rollout_row_estimate(ds, r, checkpoint);
+			int err0 = g_error;
+			if(rollout_tape(ds, r, checkpoint, iters, rowCap)){
+				cudaMemsetAsync(r->tape.t.cursor, 0, sizeof(int)*4, st);
+				d->tape = r->tape.t;
+				d->tape.on = 1;
+				taping = 1;
+			} else {
+				/* no room: the reverse pass replays the segment */
+				(void)cudaGetLastError();
+				g_error = err0;
+			}
+		}
+		if(taping) d->tape.step = s - last;
+		rc = devset_step(ds, dts, NULL);
+	}
+	free(dts);
+	if(taping){
+		d->tape.on = 0;
+		int cur[4] = {0, 0, 0, 0};
+		if(rc == 0 && cuda_ok(cudaMemcpyAsync(cur, r->tape.t.cursor, sizeof(cur), cudaMemcpyDeviceToHost, st), "tape cursor")){
+			cudaStreamSynchronize(st);
+			if(cur[2]) r->rowCap = (size_t)cur[0] + (size_t)cur[0]/4 + 1024;
+			else if(!(cur[3] & 1)) r->lastTaped = 1;
+		}
+		memset(&d->tape, 0, sizeof(d->tape));
+	}
+	return rc;
+}
+
 int cpGpuRolloutBackward(cpGpuBatch *b, const cpFloat *dLdp, cpFloat *dLdv0, cpFloat *dLdw0, cpFloat *dLdm, cpFloat *dLde, cpFloat *dLdu)
 {
 	if(!b || !b->dev || !b->roll){ set_error(CP_GPU_ERR_ARGUMENT, "rollout: no forward rollout to reverse"); return -1; }
@@ -1119,9 +1181,8 @@ int cpGpuRolloutBackward(cpGpuBatch *b, const cpFloat *dLdp, cpFloat *dLdv0, cpF
 	Rollout *r = b->roll;
 	cudaStream_t st = lib_stream();
 	int W = ds->nspaces, K = r->K;
-	int iters = 0;
-	for(int w = 0; w < W; w++) if(ds->spaces[w]->iterations > iters) iters = ds->spaces[w]->iterations;
-	for(int w = 0; w < W; w++) if(ds->spaces[w]->iterations != iters){
+	int iters = rollout_iterations(ds);
+	if(iters < 0){
 		set_error(CP_GPU_ERR_UNSUPPORTED, "rollout: all spaces of the batch need the same iteration count");
 		return -1;
 	}
@@ -1133,20 +1194,15 @@ int cpGpuRolloutBackward(cpGpuBatch *b, const cpFloat *dLdp, cpFloat *dLdv0, cpF
 	double *finDt = HALLOC(double, W);
 	for(int w = 0; w < W; w++){ finStamp[w] = ds->spaces[w]->stamp; finDt[w] = ds->spaces[w]->curr_dt; }
 
-	/* tape rows for K steps: twice the solved arbiters of the last step, or what a previous pass needed */
-	check_stats(ds);
-	size_t rowCap = r->rowCap ? r->rowCap : (size_t)K*(2*(size_t)(ds->hstats[5] > 0 ? ds->hstats[5] : 0) + (size_t)d->totalCons + 1024);
+	/* the forward's recording of the last segment is used when the tape
+	 * is still the one it wrote */
+	int useLast = r->lastTaped && r->tape.block && r->tapeK == K && r->tapeIters == iters;
+	r->lastTaped = 0;
 	TapeMem m;
 	int rc = -1;
 	double *h = NULL;
-	if(r->tape.block && r->tapeK == K && r->tapeIters == iters && (size_t)r->tape.t.rowCap >= rowCap){
-		m = r->tape;
-	} else {
-		if(r->tape.block) cudaFree(r->tape.block);
-		memset(&r->tape, 0, sizeof(r->tape));
-		if(!tape_alloc(d, &m, K, rowCap, iters)) goto done;
-		r->tape = m; r->tapeK = K; r->tapeIters = iters;
-	}
+	if(!useLast && !rollout_tape(ds, r, K, iters, rollout_row_estimate(ds, r, K))) goto done;
+	m = r->tape;
 
 	/* seeds: dL/dp at the end, nothing else */
 	{
@@ -1176,7 +1232,7 @@ int cpGpuRolloutBackward(cpGpuBatch *b, const cpFloat *dLdp, cpFloat *dLdv0, cpF
 		for(int seg = r->nckpt - 1; seg >= 0 && ok; seg--){
 			int first = seg*K, len = (r->steps - first < K) ? r->steps - first : K;
 			if(g_timing) cudaEventRecord(ev[0], st);
-			for(int attempt = 0; attempt < 4; attempt++){
+			for(int attempt = (useLast && seg == r->nckpt - 1) ? 4 : 0; attempt < 4; attempt++){
 				rollout_restore_from(ds, r->ckpt + (size_t)seg*ds->slabBytes, r->stamps + (size_t)seg*W, r->currDt + (size_t)seg*W);
 				cudaMemsetAsync(m.t.cursor, 0, sizeof(int)*4, st);
 				d->tape = m.t;

@@ -23,6 +23,7 @@
 #pragma once
 #include <cfloat>
 #include <cmath>
+#include <cstring>
 
 #ifdef __CUDACC__
 #define CPG_HD __host__ __device__ __forceinline__
@@ -578,147 +579,193 @@ CPG_HD void geom_adjoint(const GContacts &g, int count, const double *r1bar, con
  * state.  Within a part, each lane computes its body's share of the
  * impulse adjoint (phase 1); the shares are added across the pair (a
  * shuffle on the device); both lanes then run the scalar part and update
- * their own body (phase 2).  The constants' adjoints go to per-lane
- * partial sums: r1 and 1/m_a on side 0, r2 and 1/m_b on side 1, the
- * contact's scalars on side 0 only.  Summed over the four lanes they equal
- * app_adjoint's up to the order of the additions.
+ * their own body (phase 2).
+ *
+ * Every lane runs the same instructions: the part and side pick operands
+ * (selects and sign flips of the bit pattern), never branches, because a
+ * warp that diverges on them issues both paths and each double-precision
+ * instruction is issued once per warp whatever its active lanes.  The bias
+ * part is the velocity part with no friction (its friction impulse is the
+ * constant 0).  Clamp activity is read from the recorded results: a
+ * normal or bias accumulator clamps at 0 exactly when its result is +0,
+ * and the friction clamp took the bound whose bit pattern the result
+ * carries (dclamp returns one of its operands), which is the forward's
+ * branch exactly.
+ *
+ * The constants' adjoints go to per-lane partial sums (AdjLaneBar): each
+ * lane sums 1/m and r of its own body; the contact's scalars are summed by
+ * every lane but only the side-0 lanes' sums are used (both sides compute
+ * the same values).  lane_bar_sum turns the four lanes' sums into the
+ * contact's AdjConBar, equal to app_adjoint's up to the order of the
+ * additions.
  * ------------------------------------------------------------------- */
+CPG_HD long long adj_bits(double x)
+{
+#ifdef __CUDA_ARCH__
+	return __double_as_longlong(x);
+#else
+	long long b; memcpy(&b, &x, sizeof(b)); return b;
+#endif
+}
+
+CPG_HD double adj_double(long long b)
+{
+#ifdef __CUDA_ARCH__
+	return __longlong_as_double(b);
+#else
+	double x; memcpy(&x, &b, sizeof(x)); return x;
+#endif
+}
+
+#define ADJ_SIGN ((long long)0x8000000000000000ULL)
+
+CPG_HD double adj_neg_if(double x, bool f) { return adj_double(adj_bits(x) ^ (f ? ADJ_SIGN : 0LL)); }
+
+/* The lane's constants: its body's 1/m, 1/I, r; the part's constant term
+ * (bounce for the velocity part, bias for the bias part). */
 struct AdjLane {
 	int side, part;
-	double minv, iinv, rx, ry;    /* the lane's body: 1/m, 1/I, r1 or r2 */
+	double nx, ny, minv, iinv, rx, ry, c0, nMass, tMass, u;
 };
 
-/* Phase 1: the lane's share of the adjoint of the impulse (J for part 0,
- * the bias impulse for part 1), from its body's adjoint (ax, ay, aw) after
- * the application.  Partial adjoints of r and 1/m go to cb. */
-CPG_HD void quad_adj_phase1(const AdjCon &c, const AdjApp &t, const AdjLane &L, double ax, double ay, double aw,
-	double &jbx, double &jby, AdjConBar &cb)
-{
-	double nx = c.nx, ny = c.ny;
-	double Jx, Jy;
-	if(L.part == 0){
-		double dN = t.jN1 - t.jN0, dT = t.jT1 - t.jT0;
-		Jx = nx*dN - ny*dT; Jy = nx*dT + ny*dN;
-	} else {
-		double db = t.jB1 - t.jB0;
-		Jx = nx*db; Jy = ny*db;
-	}
-	double s = L.side ? 1.0 : -1.0;          /* b receives J, a receives -J */
-	jbx = s*L.minv*ax; jby = s*L.minv*ay;
-	double gm = s*(Jx*ax + Jy*ay);
-	double g = s*L.iinv*aw;
-	if(L.side){ cb.minvB += gm; cb.r2x += g*Jy; cb.r2y += -g*Jx; }
-	else { cb.minvA += gm; cb.r1x += g*Jy; cb.r1y += -g*Jx; }
-	jbx += -g*L.ry; jby += g*L.rx;
-}
+/* The lane's view of a record: the part's accumulator before and after
+ * (J0, J1), friction before and after (T0, T1: 0 for the bias part), the
+ * part's relative velocity and the lane's body's angular velocity. */
+struct AdjLaneRec { double J0, J1, T0, T1, vrx, vry, wown; };
 
-/* Phase 2: with the pair's total (Jbx, Jby), the scalar part (both lanes of
- * a part compute it; side 0 keeps the constants' adjoints), then the
- * lane's own body adjoint (ax, ay, aw) for the relative velocity.  jA, jB2
- * are the accumulator adjoints the part carries: (jN, jT) for part 0, (jB,
- * unused) for part 1. */
-CPG_HD void quad_adj_phase2(const AdjCon &c, const AdjApp &t, const AdjLane &L, double Jbx, double Jby,
-	double &ax, double &ay, double &aw, double &jA, double &jB2, AdjConBar &cb)
-{
-	double nx = c.nx, ny = c.ny;
-	bool keep = (L.side == 0);
-	double dbx, dby, wown;
-	if(L.part == 0){
-		double vrn = t.vrx*nx + t.vry*ny;
-		double vrt = t.vrx*(-ny) + t.vry*nx;
-		double jn = -(c.bounce + vrn)*c.nMass;
-		bool activeN = (t.jN0 + jn > 0.0);
-		double jtMax = c.u*t.jN1;
-		double jt = -vrt*c.tMass;
-		double f = t.jT0 + jt;
-		int sd = (f > -jtMax) ? 0 : 1;
-		double m = sd ? -jtMax : f;
-		if(!(m < jtMax)) sd = 2;
-		double dN = t.jN1 - t.jN0, dT = t.jT1 - t.jT0;
-		double dNbar = Jbx*nx + Jby*ny;
-		double dTbar = -Jbx*ny + Jby*nx;
-		if(keep){ cb.nx += Jbx*dN + Jby*dT; cb.ny += -Jbx*dT + Jby*dN; }
-		double jN1bar = jA + dNbar, jN0bar = -dNbar;
-		double jT1bar = jB2 + dTbar, jT0bar = -dTbar;
-		double fbar = 0.0, jtMaxbar = 0.0;
-		if(sd == 0) fbar = jT1bar; else if(sd == 1) jtMaxbar = -jT1bar; else jtMaxbar = jT1bar;
-		jT0bar += fbar;
-		double vrtbar = -fbar*c.tMass;
-		if(keep){ cb.tMass += -fbar*vrt; cb.u += jtMaxbar*t.jN1; }
-		jN1bar += jtMaxbar*c.u;
-		double jnbar = 0.0;
-		if(activeN){ jN0bar += jN1bar; jnbar = jN1bar; }
-		if(keep){ cb.bounce += -jnbar*c.nMass; cb.nMass += -jnbar*(c.bounce + vrn); }
-		double vrnbar = -jnbar*c.nMass;
-		dbx = vrnbar*nx - vrtbar*ny;
-		dby = vrnbar*ny + vrtbar*nx;
-		if(keep){ cb.nx += vrnbar*t.vrx + vrtbar*t.vry; cb.ny += vrnbar*t.vry - vrtbar*t.vrx; }
-		jA = jN0bar; jB2 = jT0bar;
-		wown = L.side ? t.wB : t.wA;
-	} else {
-		double vbn = t.vbx*nx + t.vby*ny;
-		double jbn = (c.bias - vbn)*c.nMass;
-		bool activeB = (t.jB0 + jbn > 0.0);
-		double db = t.jB1 - t.jB0;
-		double dbbar = Jbx*nx + Jby*ny;
-		if(keep){ cb.nx += Jbx*db; cb.ny += Jby*db; }
-		double jB1bar = jA + dbbar, jB0bar = -dbbar;
-		double jbnbar = 0.0;
-		if(activeB){ jB0bar += jB1bar; jbnbar = jB1bar; }
-		if(keep){ cb.bias += jbnbar*c.nMass; cb.nMass += jbnbar*(c.bias - vbn); }
-		double vbnbar = -jbnbar*c.nMass;
-		if(keep){ cb.nx += vbnbar*t.vbx; cb.ny += vbnbar*t.vby; }
-		dbx = vbnbar*nx; dby = vbnbar*ny;
-		jA = jB0bar;
-		wown = L.side ? t.wbB : t.wbA;
-	}
-	/* d = (v_b + perp(r2) w_b) - (v_a + perp(r1) w_a) */
-	if(L.side){
-		ax += dbx; ay += dby;
-		aw += -dbx*L.ry + dby*L.rx;
-		cb.r2y += -dbx*wown; cb.r2x += dby*wown;
-	} else {
-		ax -= dbx; ay -= dby;
-		aw += dbx*L.ry - dby*L.rx;
-		cb.r1y += dbx*wown; cb.r1x += -dby*wown;
-	}
-}
+/* Per-lane partial sums of the contact's constants' adjoints, and the
+ * accumulator adjoints the part carries (velocity: jA = jN, j2 = jT; bias:
+ * jA = jB). */
+struct alignas(16) AdjLaneBar { double minv, rx, ry, nx, ny, tMass, u, c0, nMass, jA, j2, pad; };
 
-/* Warm start on the two velocity lanes: phase 1 as for an application
- * (with J = rotate(n, (jN, jT))*dt_coef), then this. */
-CPG_HD void quad_warm_phase2(const AdjCon &c, const AdjLane &L, double jN, double jT, double dt_coef, double Jbx, double Jby,
-	double &jNbar, double &jTbar, AdjConBar &cb)
+CPG_HD void lane_bar_zero(AdjLaneBar &b)
 {
-	double nx = c.nx, ny = c.ny;
-	double jxbar = Jbx*dt_coef, jybar = Jby*dt_coef;
-	jNbar += jxbar*nx + jybar*ny;
-	jTbar += -jxbar*ny + jybar*nx;
-	if(L.side == 0){ cb.nx += jxbar*jN + jybar*jT; cb.ny += -jxbar*jT + jybar*jN; }
-}
-
-/* Phase 1 of the warm start: J = rotate(n, (jN, jT))*dt_coef. */
-CPG_HD void quad_warm_phase1(const AdjCon &c, const AdjLane &L, double jN, double jT, double dt_coef, double ax, double ay, double aw,
-	double &jbx, double &jby, AdjConBar &cb)
-{
-	double nx = c.nx, ny = c.ny;
-	double jx = nx*jN - ny*jT, jy = nx*jT + ny*jN;
-	double Jx = jx*dt_coef, Jy = jy*dt_coef;
-	double s = L.side ? 1.0 : -1.0;
-	jbx = s*L.minv*ax; jby = s*L.minv*ay;
-	double gm = s*(Jx*ax + Jy*ay);
-	double g = s*L.iinv*aw;
-	if(L.side){ cb.minvB += gm; cb.r2x += g*Jy; cb.r2y += -g*Jx; }
-	else { cb.minvA += gm; cb.r1x += g*Jy; cb.r1y += -g*Jx; }
-	jbx += -g*L.ry; jby += g*L.rx;
+	b.minv = b.rx = b.ry = b.nx = b.ny = b.tMass = b.u = b.c0 = b.nMass = b.jA = b.j2 = b.pad = 0.0;
 }
 
 CPG_HD AdjLane adj_lane(const AdjCon &c, int q)
 {
 	AdjLane L;
 	L.side = q & 1; L.part = q >> 1;
+	L.nx = c.nx; L.ny = c.ny;
 	L.minv = L.side ? c.minvB : c.minvA;
 	L.iinv = L.side ? c.iinvB : c.iinvA;
 	L.rx = L.side ? c.r2x : c.r1x;
 	L.ry = L.side ? c.r2y : c.r1y;
+	L.c0 = L.part ? c.bias : c.bounce;
+	L.nMass = c.nMass; L.tMass = c.tMass; L.u = c.u;
 	return L;
+}
+
+CPG_HD AdjLaneRec adj_lane_rec(const AdjApp &t, int side, int part)
+{
+	const double *p = &t.jN0;     /* AdjApp is 14 consecutive doubles */
+	AdjLaneRec r;
+	r.J0 = p[part ? 2 : 0]; r.J1 = p[part ? 5 : 3];
+	r.T0 = part ? 0.0 : p[1]; r.T1 = part ? 0.0 : p[4];
+	r.vrx = p[part ? 8 : 6]; r.vry = p[part ? 9 : 7];
+	r.wown = p[10 + 2*part + side];
+	return r;
+}
+
+/* Phase 1: the lane's share (jbx, jby) of the adjoint of the part's
+ * impulse, from its body's adjoint (ax, ay, aw) after the application. */
+CPG_HD void lane_adj_phase1(const AdjLane &L, const AdjLaneRec &t, double ax, double ay, double aw,
+	double &jbx, double &jby, AdjLaneBar &b)
+{
+	double dN = t.J1 - t.J0, dT = t.T1 - t.T0;
+	double Jx = L.nx*dN - L.ny*dT, Jy = L.nx*dT + L.ny*dN;
+	bool neg = (L.side == 0);                /* b receives J, a receives -J */
+	double sminv = adj_neg_if(L.minv, neg), siinv = adj_neg_if(L.iinv, neg);
+	jbx = sminv*ax; jby = sminv*ay;
+	double gm = adj_neg_if(Jx*ax + Jy*ay, neg);
+	double g = siinv*aw;
+	b.minv += gm; b.rx += g*Jy; b.ry -= g*Jx;
+	jbx += -g*L.ry; jby += g*L.rx;
+}
+
+/* Phase 2: with the pair's total (Jbx, Jby), the scalar part, then the
+ * lane's own body adjoint (ax, ay, aw) for the relative velocity; b.jA,
+ * b.j2 are the part's accumulator adjoints, after to before. */
+CPG_HD void lane_adj_phase2(const AdjLane &L, const AdjLaneRec &t, double Jbx, double Jby,
+	double &ax, double &ay, double &aw, AdjLaneBar &b)
+{
+	double nx = L.nx, ny = L.ny;
+	bool vel = (L.part == 0);
+	double dN = t.J1 - t.J0, dT = t.T1 - t.T0;
+	double vn = t.vrx*nx + t.vry*ny;
+	double vt = t.vry*nx - t.vrx*ny;
+	double dNbar = Jbx*nx + Jby*ny;
+	double dTbar = Jby*nx - Jbx*ny;
+	b.nx += Jbx*dN + Jby*dT;
+	b.ny += Jby*dN - Jbx*dT;
+	double J1bar = b.jA + dNbar, J0bar = -dNbar;
+	double T1bar = b.j2 + dTbar, T0bar = -dTbar;
+	/* friction: dclamp(f, -jtMax, jtMax) returned f, -jtMax or jtMax */
+	double jtMax = L.u*t.J1;
+	long long bt = adj_bits(t.T1), bm = adj_bits(jtMax);
+	bool top = (bt == bm), bot = !top && (bt == (bm ^ ADJ_SIGN));
+	double fbar = (vel && !top && !bot) ? T1bar : 0.0;
+	double mbar = (vel && (top || bot)) ? adj_neg_if(T1bar, bot) : 0.0;
+	T0bar += fbar;
+	double vtbar = -fbar*L.tMass;
+	b.tMass -= fbar*vt;
+	b.u += mbar*t.J1;
+	J1bar += mbar*L.u;
+	/* normal (bias): dmax(J0 + j, 0) passed J0 + j on when the result is not +0 */
+	double jnbar = (adj_bits(t.J1) > 0) ? J1bar : 0.0;
+	J0bar += jnbar;
+	/* j = y*nMass with y = -(bounce + vn) (velocity) or bias - vn (bias) */
+	double y = adj_neg_if(L.c0 + adj_neg_if(vn, !vel), vel);
+	b.nMass += jnbar*y;
+	b.c0 += adj_neg_if(jnbar, vel)*L.nMass;
+	double vnbar = -jnbar*L.nMass;
+	double dbx = vnbar*nx - vtbar*ny, dby = vnbar*ny + vtbar*nx;
+	b.nx += vnbar*t.vrx + vtbar*t.vry;
+	b.ny += vnbar*t.vry - vtbar*t.vrx;
+	b.jA = J0bar; b.j2 = T0bar;
+	/* d = (v_b + perp(r2) w_b) - (v_a + perp(r1) w_a) */
+	bool neg = (L.side == 0);
+	double sdx = adj_neg_if(dbx, neg), sdy = adj_neg_if(dby, neg);
+	ax += sdx; ay += sdy;
+	aw += L.rx*sdy - L.ry*sdx;
+	b.ry -= sdx*t.wown; b.rx += sdy*t.wown;
+}
+
+/* Warm start on the two velocity lanes: phase 1 as for an application
+ * with J = rotate(n, (jN, jT))*dt_coef. */
+CPG_HD void lane_warm_phase1(const AdjLane &L, double jN, double jT, double dt_coef, double ax, double ay, double aw,
+	double &jbx, double &jby, AdjLaneBar &b)
+{
+	double jx = L.nx*jN - L.ny*jT, jy = L.nx*jT + L.ny*jN;
+	double Jx = jx*dt_coef, Jy = jy*dt_coef;
+	bool neg = (L.side == 0);
+	double sminv = adj_neg_if(L.minv, neg), siinv = adj_neg_if(L.iinv, neg);
+	jbx = sminv*ax; jby = sminv*ay;
+	double gm = adj_neg_if(Jx*ax + Jy*ay, neg);
+	double g = siinv*aw;
+	b.minv += gm; b.rx += g*Jy; b.ry -= g*Jx;
+	jbx += -g*L.ry; jby += g*L.rx;
+}
+
+CPG_HD void lane_warm_phase2(const AdjLane &L, double jN, double jT, double dt_coef, double Jbx, double Jby, AdjLaneBar &b)
+{
+	double jxbar = Jbx*dt_coef, jybar = Jby*dt_coef;
+	b.jA += jxbar*L.nx + jybar*L.ny;
+	b.j2 += jybar*L.nx - jxbar*L.ny;
+	b.nx += jxbar*jN + jybar*jT;
+	b.ny += jybar*jN - jxbar*jT;
+}
+
+/* The contact's constants' adjoints from its four lanes' partial sums
+ * (lanes 0, 1: velocity part, sides a, b; lanes 2, 3: bias part). */
+CPG_HD void lane_bar_sum(const AdjLaneBar *l, AdjConBar &cb)
+{
+	cb.minvA = l[0].minv + l[2].minv; cb.minvB = l[1].minv + l[3].minv;
+	cb.r1x = l[0].rx + l[2].rx; cb.r1y = l[0].ry + l[2].ry;
+	cb.r2x = l[1].rx + l[3].rx; cb.r2y = l[1].ry + l[3].ry;
+	cb.nx = l[0].nx + l[2].nx; cb.ny = l[0].ny + l[2].ny;
+	cb.nMass = l[0].nMass + l[2].nMass;
+	cb.tMass = l[0].tMass; cb.u = l[0].u;
+	cb.bounce = l[0].c0; cb.bias = l[2].c0;
 }

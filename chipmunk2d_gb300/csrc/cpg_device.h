@@ -191,6 +191,12 @@ typedef struct cpgOp {
 
 /* All device arrays of a set.  Vectors are split into x/y arrays. */
 /* Recording of replayed steps for the differentiable rollout. */
+/* Reverse solve: doubles of a contact lane's scratch (AdjLaneBar), block
+ * size, and the largest world whose body adjoints it keeps in shared memory. */
+#define CPG_ADJ_LANE_DOUBLES 12
+#define CPG_ADJ_SOLVE_THREADS 64
+#define CPG_ADJ_STAGED_BODIES 1024
+
 typedef struct cpgTape {
 	int on;                   /* record this step */
 	int step;                 /* its index within the replayed segment */

@@ -160,38 +160,25 @@ extern "C" int cpg_launch_tape(const cpgSet *s, void *stream)
 
 /* ---- reverse pass ---- */
 
-/* Per contact and lane: the lane's partial adjoints of the contact's
- * constants, and the accumulator adjoints its part carries (velocity
- * lanes: jnAcc, jtAcc; bias lanes: jBias). */
-struct AdjScratch { AdjConBar cb; double jA, j2, pad; };
-
-__device__ __forceinline__ AdjScratch *con_scratch(const cpgAdj &a, size_t row, int c, int lane)
+/* Per contact and lane: the lane's partial sums of the contact's
+ * constants' adjoints and the accumulator adjoints its part carries. */
+__device__ __forceinline__ AdjLaneBar *lane_scratch(const cpgAdj &a, size_t row, int c, int lane)
 {
-	return (AdjScratch *)(a.con + ((row*2 + (size_t)c)*4 + (size_t)lane)*16);
+	return (AdjLaneBar *)(a.con + ((row*2 + (size_t)c)*4 + (size_t)lane)*CPG_ADJ_LANE_DOUBLES);
 }
 
-__device__ __forceinline__ AdjBody load_bar(const cpgAdj &a, int g)
-{
-	const double *b = a.body + 9*(size_t)g;
-	AdjBody r; r.vx = b[3]; r.vy = b[4]; r.w = b[5]; r.vbx = b[6]; r.vby = b[7]; r.wb = b[8];
-	return r;
-}
-
-__device__ __forceinline__ void store_bar(const cpgAdj &a, int g, const AdjBody &r)
-{
-	double *b = a.body + 9*(size_t)g;
-	b[3] = r.vx; b[4] = r.vy; b[5] = r.w; b[6] = r.vbx; b[7] = r.vby; b[8] = r.wb;
-}
-
-__device__ __forceinline__ AdjCon make_con(const cpgSet &s, const cpgRow &row, int c, int ga, int gb)
+/* The lane's constants of contact c of an arbiter row (g: the lane's body). */
+__device__ __forceinline__ AdjLane row_lane(const cpgSet &s, const cpgRow &row, int c, int g, int side, int part)
 {
 	const cpgRowContact &rc = row.arb.c[c];
-	AdjCon k;
-	k.r1x = rc.r1x; k.r1y = rc.r1y; k.r2x = rc.r2x; k.r2y = rc.r2y;
-	k.nx = row.arb.nx; k.ny = row.arb.ny;
-	k.nMass = rc.nMass; k.tMass = rc.tMass; k.bias = rc.bias; k.bounce = rc.bounce; k.u = row.arb.u;
-	k.minvA = s.minv[ga]; k.minvB = s.minv[gb]; k.iinvA = s.iinv[ga]; k.iinvB = s.iinv[gb];
-	return k;
+	AdjLane L;
+	L.side = side; L.part = part;
+	L.nx = row.arb.nx; L.ny = row.arb.ny;
+	L.minv = s.minv[g]; L.iinv = s.iinv[g];
+	L.rx = side ? rc.r2x : rc.r1x; L.ry = side ? rc.r2y : rc.r1y;
+	L.c0 = part ? rc.bias : rc.bounce;
+	L.nMass = rc.nMass; L.tMass = rc.tMass; L.u = row.arb.u;
+	return L;
 }
 
 /* A shape's recorded world geometry at step t as a GShape. */
@@ -220,9 +207,12 @@ enum { U_POSE = 0, U_PA = 6, U_PB = 8, U_VA = 10, U_WA = 12, U_VB = 13, U_WB = 1
 
 /* Steps 1-4 of the reverse step (one block per world, four lanes per
  * unit as in the forward solve): the impulses stored at the end, the
- * iterations and the warm start in reverse, velocity integration. */
-__global__ void k_adj_solve(cpgSet s, cpgAdj a, int t)
+ * iterations and the warm start in reverse, velocity integration.  Worlds
+ * of at most `stagedMax` bodies keep their bodies' velocity adjoints (v, w,
+ * v_bias, w_bias) in shared memory for the whole solve. */
+__global__ void __launch_bounds__(CPG_ADJ_SOLVE_THREADS) k_adj_solve(cpgSet s, cpgAdj a, int t, int stagedMax)
 {
+	extern __shared__ double sbar[];
 	int w = blockIdx.x;
 	const cpgTape &tp = s.tape;
 	int nw = s.nworlds;
@@ -243,18 +233,23 @@ __global__ void k_adj_solve(cpgSet s, cpgAdj a, int t)
 	unsigned qmask = 0xFu << (tid & 28);
 	unsigned pmask = 0x3u << (tid & 28);     /* the quad's two velocity lanes */
 	int nbw = W.nbodies, bo = W.bodyOff;
+	bool staged = nbw <= stagedMax;
+	double *bars = staged ? sbar : a.body + 9*(size_t)bo + 3;
+	int bstride = staged ? 6 : 9;
+	if(staged)
+		for(int i = tid; i < 6*nbw; i += nt) sbar[i] = a.body[9*(size_t)(bo + i/6) + 3 + i%6];
 
 	/* 1. adjoints of the impulses stored at the end of the step */
 	for(int k = quad; k < n; k += nq){
 		const cpgRow &row = rows[k];
 		for(int c = 0; c < 2; c++){
-			AdjScratch *sc = con_scratch(a, ro + k, c, lane4);
-			adj_zero(sc->cb);
-			sc->jA = 0.0; sc->j2 = 0.0;
+			AdjLaneBar z;
+			lane_bar_zero(z);
 			if(row.kind == 0 && part == 0 && c < row.count){
 				const double *arb = a.arb + 4*(size_t)row.src + 2*c;
-				sc->jA = arb[0]; sc->j2 = arb[1];
+				z.jA = arb[0]; z.j2 = arb[1];
 			}
+			*lane_scratch(a, ro + k, c, lane4) = z;
 		}
 		__syncwarp(qmask);
 		if(lane4 == 0 && row.kind == 0){
@@ -270,22 +265,25 @@ __global__ void k_adj_solve(cpgSet s, cpgAdj a, int t)
 			for(int k = start[l] + quad; k < start[l + 1]; k += nq){
 				const cpgRow &row = rows[k];
 				if(row.kind != 0) continue;
-				int ga = bo + row.a, gb = bo + row.b;
-				int g = side ? gb : ga;
+				int lb = side ? row.b : row.a;
 				bool dyn = (row.flags & (side ? ROW_DYN_B_ : ROW_DYN_A_)) != 0;
-				double *bar = a.body + 9*(size_t)g + 3 + 3*part;
+				double *bar = bars + (size_t)bstride*lb + 3*part;
 				double ax = 0.0, ay = 0.0, aw = 0.0;
 				if(dyn){ ax = bar[0]; ay = bar[1]; aw = bar[2]; }
 				const AdjApp *rec = (const AdjApp *)tp.app + ((size_t)(ro + k)*iters + (pass - 1))*2;
-				for(int c = row.count - 1; c >= 0; c--){
-					AdjCon con = make_con(s, row, c, ga, gb);
-					AdjLane L = adj_lane(con, lane4);
-					AdjScratch *sc = con_scratch(a, ro + k, c, lane4);
+#pragma unroll
+				for(int c = 1; c >= 0; c--){
+					if(c >= row.count) continue;
+					AdjLane L = row_lane(s, row, c, bo + lb, side, part);
+					AdjLaneRec R = adj_lane_rec(rec[c], side, part);
+					AdjLaneBar *sc = lane_scratch(a, ro + k, c, lane4);
+					AdjLaneBar B = *sc;
 					double jbx, jby;
-					quad_adj_phase1(con, rec[c], L, ax, ay, aw, jbx, jby, sc->cb);
+					lane_adj_phase1(L, R, ax, ay, aw, jbx, jby, B);
 					jbx += __shfl_xor_sync(qmask, jbx, 1);
 					jby += __shfl_xor_sync(qmask, jby, 1);
-					quad_adj_phase2(con, rec[c], L, jbx, jby, ax, ay, aw, sc->jA, sc->j2, sc->cb);
+					lane_adj_phase2(L, R, jbx, jby, ax, ay, aw, B);
+					*sc = B;
 				}
 				if(dyn){ bar[0] = ax; bar[1] = ay; bar[2] = aw; }
 			}
@@ -298,23 +296,23 @@ __global__ void k_adj_solve(cpgSet s, cpgAdj a, int t)
 	for(int k = quad; k < n; k += nq){
 		const cpgRow &row = rows[k];
 		if(row.kind != 0) continue;
-		int ga = bo + row.a, gb = bo + row.b;
 		if(part == 0 && !(row.flags & ROW_FIRST_)){
-			int g = side ? gb : ga;
+			int lb = side ? row.b : row.a;
 			bool dyn = (row.flags & (side ? ROW_DYN_B_ : ROW_DYN_A_)) != 0;
-			const double *bar = a.body + 9*(size_t)g + 3;
+			const double *bar = bars + (size_t)bstride*lb;
 			double ax = 0.0, ay = 0.0, aw = 0.0;
 			if(dyn){ ax = bar[0]; ay = bar[1]; aw = bar[2]; }
 			for(int c = row.count - 1; c >= 0; c--){
-				AdjCon con = make_con(s, row, c, ga, gb);
-				AdjLane L = adj_lane(con, lane4);
-				AdjScratch *sc = con_scratch(a, ro + k, c, lane4);
+				AdjLane L = row_lane(s, row, c, bo + lb, side, 0);
+				AdjLaneBar *sc = lane_scratch(a, ro + k, c, lane4);
+				AdjLaneBar B = *sc;
 				double jN = row.arb.c[c].jnAcc, jT = row.arb.c[c].jtAcc;
 				double jbx, jby;
-				quad_warm_phase1(con, L, jN, jT, P.dt_coef, ax, ay, aw, jbx, jby, sc->cb);
+				lane_warm_phase1(L, jN, jT, P.dt_coef, ax, ay, aw, jbx, jby, B);
 				jbx += __shfl_xor_sync(pmask, jbx, 1);
 				jby += __shfl_xor_sync(pmask, jby, 1);
-				quad_warm_phase2(con, L, jN, jT, P.dt_coef, jbx, jby, sc->jA, sc->j2, sc->cb);
+				lane_warm_phase2(L, jN, jT, P.dt_coef, jbx, jby, B);
+				*sc = B;
 			}
 		}
 		if(lane4 == 0){
@@ -322,7 +320,7 @@ __global__ void k_adj_solve(cpgSet s, cpgAdj a, int t)
 			for(int c = 0; c < row.count && c < 2; c++){
 				int j = ((src >> (4*c)) & 0xF) - 1;
 				if(j >= 0 && j < 2){
-					const AdjScratch *sc = con_scratch(a, ro + k, c, 0);
+					const AdjLaneBar *sc = lane_scratch(a, ro + k, c, 0);
 					double *arb = a.arb + 4*(size_t)row.src + 2*j;
 					arb[0] += sc->jA; arb[1] += sc->j2;
 				}
@@ -336,7 +334,9 @@ __global__ void k_adj_solve(cpgSet s, cpgAdj a, int t)
 		int g = bo + i;
 		if(s.btype[g] != CPG_DYNAMIC) continue;
 		double *b = a.body + 9*(size_t)g;
-		b[3] *= P.damping; b[4] *= P.damping; b[5] *= P.damping;
+		const double *sb = bars + (size_t)bstride*i;
+		double vx = sb[0], vy = sb[1], vw = sb[2];
+		b[3] = vx*P.damping; b[4] = vy*P.damping; b[5] = vw*P.damping;
 		b[6] = 0.0; b[7] = 0.0; b[8] = 0.0;
 	}
 }
@@ -375,14 +375,10 @@ __global__ void k_adj_geom(cpgSet s, cpgAdj a, int t)
 		p.e = row.arb.e;
 		p.biasCoef = P.biasCoef; p.slop = P.slop; p.dt = P.dt;
 		/* the four lanes' partial adjoints of the contact's constants */
-		AdjConBar cb; adj_zero(cb);
-		for(int q = 0; q < 4; q++){
-			const AdjConBar &l = con_scratch(a, r, c, q)->cb;
-			cb.r1x += l.r1x; cb.r1y += l.r1y; cb.r2x += l.r2x; cb.r2y += l.r2y;
-			cb.nx += l.nx; cb.ny += l.ny; cb.nMass += l.nMass; cb.tMass += l.tMass;
-			cb.bias += l.bias; cb.bounce += l.bounce; cb.u += l.u;
-			cb.minvA += l.minvA; cb.minvB += l.minvB;
-		}
+		AdjLaneBar lb[4];
+		for(int q = 0; q < 4; q++) lb[q] = *lane_scratch(a, r, c, q);
+		AdjConBar cb;
+		lane_bar_sum(lb, cb);
 		const AdjConBar *scb = &cb;
 		AdjPreBar pb; adj_zero(pb);
 		prestep_adjoint(p, scb->nMass, scb->tMass, scb->bias, scb->bounce, pb);
@@ -513,7 +509,8 @@ extern "C" int cpg_launch_adjoint(const cpgSet *s, const cpgAdj *a, int step, in
 {
 	cudaStream_t st = (cudaStream_t)stream;
 	/* a few units per level: two warps per world keep every world resident */
-	k_adj_solve<<<s->nworlds, 64, 0, st>>>(*s, *a, step);
+	int stagedMax = s->hostMaxBodies <= CPG_ADJ_STAGED_BODIES ? s->hostMaxBodies : 0;
+	k_adj_solve<<<s->nworlds, CPG_ADJ_SOLVE_THREADS, (size_t)stagedMax*6*sizeof(double), st>>>(*s, *a, step, stagedMax);
 	k_adj_geom<<<blocks_of(rows, 128), 128, 0, st>>>(*s, *a, step);
 	k_adj_accum<<<s->nworlds, 64, 0, st>>>(*s, *a, step);
 	return cudaGetLastError() == cudaSuccess ? 0 : -1;

@@ -269,53 +269,51 @@ static void test_quad_lanes()
 		AdjConBar cb; adj_zero(cb);
 		app_adjoint(c, rec, A, B, jN, jT, jB, cb);
 		/* four lanes */
-		double ax[4], ay[4], aw[4], jA[4], j2[4], jbx[4], jby[4];
-		AdjConBar cl[4];
+		double ax[4], ay[4], aw[4], jbx[4], jby[4];
+		AdjLaneBar cl[4];
 		for(int q = 0; q < 4; q++){
 			int side = q & 1, part = q >> 1;
 			const double *o = w + 6*side + 3*part;
 			ax[q] = o[0]; ay[q] = o[1]; aw[q] = o[2];
-			jA[q] = part ? w[14] : w[12]; j2[q] = part ? 0.0 : w[13];
-			adj_zero(cl[q]);
-			quad_adj_phase1(c, rec, adj_lane(c, q), ax[q], ay[q], aw[q], jbx[q], jby[q], cl[q]);
+			lane_bar_zero(cl[q]);
+			cl[q].jA = part ? w[14] : w[12]; cl[q].j2 = part ? 0.0 : w[13];
+			lane_adj_phase1(adj_lane(c, q), adj_lane_rec(rec, side, part), ax[q], ay[q], aw[q], jbx[q], jby[q], cl[q]);
 		}
 		for(int q = 0; q < 4; q++){
 			double Jx = jbx[q] + jbx[q ^ 1], Jy = jby[q] + jby[q ^ 1];
-			quad_adj_phase2(c, rec, adj_lane(c, q), Jx, Jy, ax[q], ay[q], aw[q], jA[q], j2[q], cl[q]);
+			lane_adj_phase2(adj_lane(c, q), adj_lane_rec(rec, q & 1, q >> 1), Jx, Jy, ax[q], ay[q], aw[q], cl[q]);
 		}
-		AdjConBar sum; adj_zero(sum);
-		for(int q = 0; q < 4; q++){
-			sum.r1x += cl[q].r1x; sum.r1y += cl[q].r1y; sum.r2x += cl[q].r2x; sum.r2y += cl[q].r2y;
-			sum.nx += cl[q].nx; sum.ny += cl[q].ny; sum.nMass += cl[q].nMass; sum.tMass += cl[q].tMass;
-			sum.bias += cl[q].bias; sum.bounce += cl[q].bounce; sum.u += cl[q].u;
-			sum.minvA += cl[q].minvA; sum.minvB += cl[q].minvB;
-		}
+		AdjConBar sum;
+		lane_bar_sum(cl, sum);
 		char nm[64];
-		double lanes[] = { ax[0], ay[0], aw[0], ax[2], ay[2], aw[2], ax[1], ay[1], aw[1], ax[3], ay[3], aw[3], jA[0], j2[0], jA[2],
+		double lanes[] = { ax[0], ay[0], aw[0], ax[2], ay[2], aw[2], ax[1], ay[1], aw[1], ax[3], ay[3], aw[3], cl[0].jA, cl[0].j2, cl[2].jA,
 			sum.r1x, sum.r1y, sum.r2x, sum.r2y, sum.nx, sum.ny, sum.nMass, sum.tMass, sum.bias, sum.bounce, sum.u, sum.minvA, sum.minvB };
 		double one[] = { A.vx, A.vy, A.w, A.vbx, A.vby, A.wb, B.vx, B.vy, B.w, B.vbx, B.vby, B.wb, jN, jT, jB,
 			cb.r1x, cb.r1y, cb.r2x, cb.r2y, cb.nx, cb.ny, cb.nMass, cb.tMass, cb.bias, cb.bounce, cb.u, cb.minvA, cb.minvB };
 		for(int i = 0; i < 28; i++){ snprintf(nm, sizeof(nm), "lanes trial %d value %d", trial, i); close_to(nm, lanes[i], one[i]); n++; }
 		/* both lanes of a part carry the same accumulator adjoints */
-		if(jA[0] != jA[1] || j2[0] != j2[1] || jA[2] != jA[3]){ failures++; printf("  FAIL lanes trial %d: pair accumulators differ\n", trial); }
+		if(cl[0].jA != cl[1].jA || cl[0].j2 != cl[1].j2 || cl[2].jA != cl[3].jA){ failures++; printf("  FAIL lanes trial %d: pair accumulators differ\n", trial); }
 		/* warm start */
 		AdjBody Aw = { w[0], w[1], w[2], 0, 0, 0 }, Bw = { w[6], w[7], w[8], 0, 0, 0 };
 		double wN = 0.0, wT = 0.0, dtc = urange(0.5, 1.5);
 		AdjConBar wc; adj_zero(wc);
 		warm_adjoint(c, s.jN, s.jT, dtc, Aw, Bw, wN, wT, wc);
-		double qb[2][2]; AdjConBar wl[2]; double qN[2] = {0, 0}, qT[2] = {0, 0};
+		double qb[2][2]; AdjLaneBar wl[4];
+		for(int q = 0; q < 4; q++) lane_bar_zero(wl[q]);
 		for(int q = 0; q < 2; q++){
-			adj_zero(wl[q]);
 			const double *o = w + 6*q;
-			quad_warm_phase1(c, adj_lane(c, q), s.jN, s.jT, dtc, o[0], o[1], o[2], qb[q][0], qb[q][1], wl[q]);
+			lane_warm_phase1(adj_lane(c, q), s.jN, s.jT, dtc, o[0], o[1], o[2], qb[q][0], qb[q][1], wl[q]);
 		}
 		for(int q = 0; q < 2; q++)
-			quad_warm_phase2(c, adj_lane(c, q), s.jN, s.jT, dtc, qb[q][0] + qb[q ^ 1][0], qb[q][1] + qb[q ^ 1][1], qN[q], qT[q], wl[q]);
+			lane_warm_phase2(adj_lane(c, q), s.jN, s.jT, dtc, qb[q][0] + qb[q ^ 1][0], qb[q][1] + qb[q ^ 1][1], wl[q]);
+		AdjConBar ws;
+		lane_bar_sum(wl, ws);
+		double qN[1] = { wl[0].jA }, qT[1] = { wl[0].j2 };
 		snprintf(nm, sizeof(nm), "warm lanes trial %d", trial);
 		close_to(nm, qN[0], wN); close_to(nm, qT[0], wT);
-		close_to(nm, wl[0].nx + wl[1].nx, wc.nx); close_to(nm, wl[0].ny + wl[1].ny, wc.ny);
-		close_to(nm, wl[0].r1x + wl[1].r1x, wc.r1x); close_to(nm, wl[0].r2y + wl[1].r2y, wc.r2y);
-		close_to(nm, wl[0].minvA + wl[1].minvA, wc.minvA); close_to(nm, wl[0].minvB + wl[1].minvB, wc.minvB);
+		close_to(nm, ws.nx, wc.nx); close_to(nm, ws.ny, wc.ny);
+		close_to(nm, ws.r1x, wc.r1x); close_to(nm, ws.r2y, wc.r2y);
+		close_to(nm, ws.minvA, wc.minvA); close_to(nm, ws.minvB, wc.minvB);
 		n += 8;
 	}
 	printf("four-lane adjoint: %d checks\n", n);
