@@ -22,7 +22,7 @@ Metric: body-steps/s = dynamic bodies x timed steps / device seconds.
 and metric, and prints its own JSON line.
 
 Usage: python bench.py [--gpus N] [--steps K] [--warmup W] [--mode ordered|colored]
-                       [--impl ours|reference] [--workload circles|pyramid|mixed|batch]
+                       [--impl ours|reference] [--workload circles|pyramid|mixed|batch|rollout]
 """
 import argparse
 import json
@@ -340,6 +340,251 @@ def run_batch(args, emit=True, sharded=True):
     return line
 
 
+ROLLOUT_WORLDS, ROLLOUT_SIZE, ROLLOUT_STEPS, ROLLOUT_K, ROLLOUT_DT = 1024, 64, 240, 16, 1 / 120
+
+
+def _rollout_scenes(lib, indices):
+    from chipmunk2d_gb300 import Scene
+    return [Scene(lib, 5, ROLLOUT_SIZE, seed=4000 + i) for i in indices]
+
+
+def _positions(scenes):
+    return np.concatenate([sc.bodies()[:, 0:2] for sc in scenes])
+
+
+def _rollout_fd(lib, targets, n_params=64, seed=11):
+    """Central differences of the GPU forward for sampled parameters.  The
+    worlds are independent, so the loss terms of world i are the only ones
+    a parameter of world i moves: each difference steps that world alone
+    (cpGpuBatchStep on a one-world batch, bit-identical to its steps in the
+    full batch).  Two step sizes screen out parameters where the loss is not
+    smooth (a contact starting inside the step)."""
+    from chipmunk2d_gb300 import cpVect
+    rng = np.random.default_rng(seed)
+    kinds = ["v"] * 24 + ["w"] * 10 + ["m"] * 10 + ["e"] * 10 + ["u"] * 10
+    params = []
+    for k in kinds[:n_params]:
+        w = int(rng.integers(ROLLOUT_WORLDS))
+        idx = int(rng.integers(ROLLOUT_SIZE + (1 if k in "eu" else 0)))
+        params.append((k, w, idx, int(rng.integers(2))))
+
+    def world_loss(p, h):
+        k, w, idx, comp = p
+        (sc,) = _rollout_scenes(lib, [w])
+        if k in "vwm":
+            body = lib.cpx_scene_body(sc.h, idx)
+            if k == "v":
+                v = lib.cpBodyGetVelocity(body)
+                lib.cpBodySetVelocity(body, cpVect(v.x + (h if comp == 0 else 0.0), v.y + (h if comp == 1 else 0.0)))
+            elif k == "w":
+                lib.cpBodySetAngularVelocity(body, lib.cpBodyGetAngularVelocity(body) + h)
+            else:
+                lib.cpBodySetMass(body, lib.cpBodyGetMass(body) + h)
+        else:
+            shape = lib.cpx_scene_shape(sc.h, idx)
+            if k == "e":
+                lib.cpShapeSetElasticity(shape, lib.cpShapeGetElasticity(shape) + h)
+            else:
+                lib.cpShapeSetFriction(shape, lib.cpShapeGetFriction(shape) + h)
+        b = lib.cpGpuBatchNew()
+        lib.cpGpuBatchAddSpace(b, sc.space)
+        assert lib.cpGpuBatchStep(b, ROLLOUT_DT, ROLLOUT_STEPS, 0) == 0
+        p_ = sc.bodies()[:, 0:2]
+        lib.cpGpuBatchFree(b)
+        sc.free()
+        t = targets[w * ROLLOUT_SIZE:(w + 1) * ROLLOUT_SIZE]
+        return float(np.sum((p_ - t) ** 2))
+
+    out = []
+    for p in params:
+        fd, lw = [], 0.0
+        for h in (1e-6, 1e-7):
+            lp, lm = world_loss(p, h), world_loss(p, -h)
+            fd.append((lp - lm) / (2 * h))
+            lw = max(lw, abs(lp), abs(lm))
+        out.append((p, fd[0], fd[1], lw))
+    return out
+
+
+def run_rollout(args, emit=True, sharded=True):
+    """Differentiable rollout: 1024 worlds of 32 circles and 32 boxes over a
+    ground segment, 240 steps at dt 1/120, 10 iterations, a checkpoint every
+    16 steps; loss sum |p_final - target|^2, targets ~ N(0, 10).  Timed: the
+    plain batched forward (cpGpuBatchStep, 240 steps) and the forward with
+    checkpoints plus the reverse pass (cpGpuRolloutForward +
+    cpGpuRolloutBackward, host gradient buffers), each from the same fresh
+    worlds.  Under torchrun each rank takes its contiguous range of worlds;
+    the gradients are per world, so nothing is exchanged."""
+    import ctypes
+    import torch
+    from chipmunk2d_gb300 import load_gpu_library
+    from chipmunk2d_gb300.shard import rank_range
+    world_size = int(os.environ.get("WORLD_SIZE", "1")) if sharded else 1
+    rank = int(os.environ.get("RANK", "0")) if sharded else 0
+    dist = None
+    if world_size > 1:
+        import torch.distributed as dist
+        torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+        if not dist.is_initialized():
+            dist.init_process_group("nccl")
+    lib = load_gpu_library()
+    stream = torch.cuda.Stream()
+    lib.cpGpuSetStream(ctypes.c_void_p(stream.cuda_stream))
+    lo, hi = rank_range([ROLLOUT_SIZE] * ROLLOUT_WORLDS, rank, world_size)
+    targets = np.random.default_rng(4).normal(0.0, 10.0, size=(ROLLOUT_WORLDS * ROLLOUT_SIZE, 2))
+    my_t = targets[lo * ROLLOUT_SIZE:hi * ROLLOUT_SIZE]
+
+    def fresh():
+        scenes = _rollout_scenes(lib, range(lo, hi))
+        b = lib.cpGpuBatchNew()
+        for sc in scenes:
+            lib.cpGpuBatchAddSpace(b, sc.space)
+        assert lib.cpGpuBatchStep(b, ROLLOUT_DT, 0, 0) == 0      # uploads the worlds
+        torch.cuda.synchronize()
+        return scenes, b
+
+    def done(scenes, b):
+        lib.cpGpuBatchFree(b)
+        for sc in scenes:
+            sc.free()
+
+    def sync_all():
+        torch.cuda.synchronize()
+        if dist:
+            dist.barrier()
+
+    def plain():
+        scenes, b = fresh()
+        sync_all()
+        t0 = time.perf_counter()
+        assert lib.cpGpuBatchStep(b, ROLLOUT_DT, ROLLOUT_STEPS, 0) == 0
+        torch.cuda.synchronize()
+        dt_ = time.perf_counter() - t0
+        done(scenes, b)
+        return dt_
+
+    def rollout(timing=False):
+        scenes, b = fresh()
+        nd = sum(sc.nbodies for sc in scenes)
+        ns = sum(sc.nshapes for sc in scenes)
+        g = {"v0": np.zeros(2 * nd), "w0": np.zeros(nd), "m": np.zeros(nd), "e": np.zeros(ns), "u": np.zeros(ns)}
+        lib.cpGpuSetTiming(1 if timing else 0)
+        sync_all()
+        t0 = time.perf_counter()
+        assert lib.cpGpuRolloutForward(b, ROLLOUT_DT, ROLLOUT_STEPS, ROLLOUT_K) == 0, lib.cpGpuGetLastErrorString()
+        p = _positions(scenes)      # the final positions, read back through the C API
+        dLdp = np.ascontiguousarray(2.0 * (p - my_t)).ravel()
+        t1 = time.perf_counter()
+        rc = lib.cpGpuRolloutBackward(b, dLdp.ctypes.data, g["v0"].ctypes.data, g["w0"].ctypes.data,
+                                      g["m"].ctypes.data, g["e"].ctypes.data, g["u"].ctypes.data)
+        torch.cuda.synchronize()
+        t2 = time.perf_counter()
+        assert rc == 0, lib.cpGpuGetLastErrorString()
+        tt = np.zeros(4)
+        lib.cpGpuDebugRolloutTimes(b, tt.ctypes.data)
+        lib.cpGpuSetTiming(0)
+        L = float(np.sum((p - my_t) ** 2))
+        done(scenes, b)
+        return t1 - t0, t2 - t1, g, L, tt, nd, ns
+
+    # warm-up: one of each (allocations, tape sizing), the reverse pass with
+    # per-phase timing
+    plain()
+    _, _, _, _, phase_tt, _, _ = rollout(timing=True)
+    lib.cpGpuGetLaunchCount(1)
+    clocks = ClockSampler(int(os.environ.get("LOCAL_RANK", "0")) if world_size > 1 else 0)
+    clocks.start()
+    plain_s = min(plain() for _ in range(2))
+    runs = [rollout() for _ in range(2)]
+    launches = lib.cpGpuGetLaunchCount(1)
+    clk = clocks.stop()
+    fwd_s, bwd_s, g, L, _, nd, ns = min(runs, key=lambda r: r[0] + r[1])
+    if dist:
+        t = torch.tensor([plain_s, fwd_s, bwd_s], device="cuda", dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        plain_s, fwd_s, bwd_s = (float(x) for x in t.tolist())
+    if rank != 0:
+        if dist:
+            dist.destroy_process_group()
+        return None
+    deterministic = all(np.array_equal(runs[0][2][k], runs[1][2][k]) for k in g)
+
+    fd_rows = _rollout_fd(lib, targets) if world_size == 1 else []
+    # u = |fd(1e-6) - fd(1e-7)| bounds the differences' own error.  Resolved:
+    # u <= 1e-6 |fd|; kinked: u > 1e-2 |fd| (a contact event within the step).
+    resolved, kinked, within = [], 0, 0
+    for (k, w, idx, comp), f6, f7, lw in fd_rows:
+        b0 = (w - lo) * ROLLOUT_SIZE + idx
+        s0 = (w - lo) * (ROLLOUT_SIZE + 1) + idx
+        adj = {"v": lambda: g["v0"][2 * b0 + comp], "w": lambda: g["w0"][b0], "m": lambda: g["m"][b0],
+               "e": lambda: g["e"][s0], "u": lambda: g["u"][s0]}[k]()
+        u = abs(f6 - f7)
+        if u > 1e-2 * abs(f6):
+            kinked += 1
+            continue
+        if abs(adj - f6) <= max(1e-6 * abs(f6), u):
+            within += 1
+        if u <= 1e-6 * abs(f6):
+            resolved.append(abs(adj - f6) / abs(f6))
+
+    # CPU restatement (the oracle), one core: the plain forward of a sample of worlds
+    orc = oracle_lib()
+    cpu_n = 16
+    cw = _rollout_scenes(orc, range(cpu_n))
+    t0 = time.perf_counter()
+    for sc in cw:
+        sc.step(ROLLOUT_DT, ROLLOUT_STEPS)
+    cpu_s = time.perf_counter() - t0
+    for sc in cw:
+        sc.free()
+
+    total = fwd_s + bwd_s
+    worlds = ROLLOUT_WORLDS
+    line = {
+        "metric": "rollout steps/s (forward+adjoint)", "value": ROLLOUT_STEPS / total, "unit": "steps/s",
+        "n_gpus": world_size, "steps": ROLLOUT_STEPS, "warmup": 1,
+        "ms_per_step": 1000 * total / ROLLOUT_STEPS, "higher_is_better": True,
+        "scaling": "strong", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": "rollout", "worlds": worlds, "bodies_per_world": ROLLOUT_SIZE,
+                   "description": ("1024 worlds x (32 circles r~U[1,3] + 32 boxes sides U[2,6]) over a ground segment, "
+                                   "240 steps, dt 1/120, 10 it, checkpoint every 16, world i seeded 4000+i; "
+                                   "loss sum |p_final - target|^2, targets ~ N(0,10)"),
+                   "parallelism": ("worlds sharded over %d GPUs" % world_size if world_size > 1 else "single"),
+                   "l2": "inputs larger than L2 (tape and checkpoints)"},
+        "plain_forward_ms": 1000 * plain_s,
+        "rollout_forward_ms": 1000 * fwd_s,
+        "backward_ms": 1000 * bwd_s,
+        "fwd_adj_over_forward": total / plain_s,
+        "backward_phases_ms": {"replay_with_recording": float(phase_tt[0]), "reverse_steps": float(phase_tt[1])},
+        "device_memory_gb": {"segment_tape": float(phase_tt[2]) / 1e9, "checkpoints": float(phase_tt[3]) / 1e9},
+        "gradients_deterministic": bool(deterministic),
+        "fd_check": {"params": len(fd_rows), "kinked": kinked,
+                     "within_fd_uncertainty": within,
+                     "resolved": len(resolved),
+                     "resolved_max_rel_err": max(resolved) if resolved else None,
+                     "resolved_median_rel_err": float(np.median(resolved)) if resolved else None,
+                     "against": ("central differences of the GPU forward at h=1e-6 (error bound u = their distance "
+                                 "from h=1e-7), one world per difference; resolved: u <= 1e-6 |fd|; kinked: "
+                                 "u > 1e-2 |fd|; within: |adjoint - fd| <= max(1e-6 |fd|, u)")},
+        "e2e": {"value": ROLLOUT_STEPS / total, "unit": "steps/s",
+                "h2d_bytes_per_step": 72 * nd / ROLLOUT_STEPS,
+                "d2h_bytes_per_step": (16 * nd + 8 * nd * 2 + 8 * ns * 2 + 18 * 8 * nd) / ROLLOUT_STEPS,
+                "path": "cpGpuRolloutForward, final bodies read back, cpGpuRolloutBackward with host seed and gradient buffers"},
+        "loss": L,
+        "gpu_launches": int(launches),
+        "clocks": clk,
+        "cpu_baseline": {"value": cpu_n * ROLLOUT_STEPS * ROLLOUT_SIZE / cpu_s, "unit": "body-steps/s (forward only)",
+                         "cores": 1, "kind": "port",
+                         "sample": "%d worlds x %d steps of the forward (the reference has no adjoint)" % (cpu_n, ROLLOUT_STEPS)},
+        "gpu_forward_body_steps_per_s": worlds * ROLLOUT_SIZE * ROLLOUT_STEPS / plain_s,
+    }
+    if dist:
+        dist.destroy_process_group()
+    if emit:
+        print(json.dumps(line), flush=True)
+    return line
+
+
 PHASES = ["integrate+cache", "broadphase", "narrowphase", "arbiters", "schedule", "prestep+velocity", "solve"]
 
 
@@ -527,6 +772,12 @@ def run_ours(args):
                                              "looped_plain_gpu_world_steps_per_s", "batched_over_looped",
                                              "cpu_baseline", "phase_ms")}
         extras["batch"]["config"] = b["config"]
+        r = run_rollout(args, emit=False, sharded=False)
+        extras["rollout"] = {k: r[k] for k in ("value", "unit", "plain_forward_ms", "rollout_forward_ms", "backward_ms",
+                                               "fwd_adj_over_forward", "backward_phases_ms", "device_memory_gb",
+                                               "gradients_deterministic",
+                                               "fd_check", "cpu_baseline")}
+        extras["rollout"]["config"] = r["config"]
 
     line = {
         "metric": "body-steps/s", "value": value, "unit": "body-steps/s", "n_gpus": world_size,
@@ -569,7 +820,7 @@ def main():
     ap.add_argument("--mode", default="colored", choices=["ordered", "colored"])
     ap.add_argument("--no-extras", dest="extras", action="store_false",
                     help="skip the ordered-mode and batched-world records of the default line")
-    ap.add_argument("--workload", default="circles", choices=sorted(WORKLOADS) + ["batch"])
+    ap.add_argument("--workload", default="circles", choices=sorted(WORKLOADS) + ["batch", "rollout"])
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--profile", action="store_true",
                     help="run only the warm-up and device-timed steps (for ncu captures)")
@@ -580,6 +831,8 @@ def main():
         run_reference(args)
     elif args.workload == "batch":
         run_batch(args)
+    elif args.workload == "rollout":
+        run_rollout(args)
     else:
         run_ours(args)
 

@@ -1029,12 +1029,6 @@ static void rollout_restore_from(DevSet *ds, const char *src, const unsigned *st
 	}
 }
 
-int cpGpuDebugRolloutTimes(cpGpuBatch *b, double *out)
-{
-	if(!b || !b->roll || !out) return 0;
-	out[0] = b->roll->replayMs; out[1] = b->roll->adjointMs;
-	return 2;
-}
 
 static size_t tape_carve(cpgSet *d, TapeMem *m, char *base, int K, size_t rowCap, int iters, int pass)
 {
@@ -1075,6 +1069,16 @@ static int tape_alloc(cpgSet *d, TapeMem *m, int K, size_t rowCap, int iters)
 	if(!cuda_ok(cudaMalloc(&m->block, bytes), "cudaMalloc rollout tape")){ m->block = NULL; return 0; }
 	tape_carve(d, m, (char *)m->block, K, rowCap, iters, 1);
 	return 1;
+}
+
+int cpGpuDebugRolloutTimes(cpGpuBatch *b, double *out)
+{
+	if(!b || !b->roll || !out) return 0;
+	Rollout *r = b->roll;
+	out[0] = r->replayMs; out[1] = r->adjointMs;
+	out[2] = r->tape.block ? (double)tape_carve(&b->dev->d, &r->tape, NULL, r->tapeK, (size_t)r->tape.t.rowCap, r->tapeIters, 0) : 0.0;
+	out[3] = (double)r->ckptCap*(double)b->dev->slabBytes;
+	return 4;
 }
 
 /* The iteration count shared by every space of the batch, or -1. */

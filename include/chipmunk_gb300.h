@@ -503,17 +503,20 @@ int cpGpuDebugCandidates(cpSpace *space, int *out, int max);
  * (dLdw0: 1 per dynamic body), masses (dLdm; the moment of inertia held
  * fixed, as cpBodySetMass does), and each shape's elasticity and friction
  * (dLde, dLdu: 1 per shape, all shapes of each space in order).  Any output
- * pointer may be NULL.  It replays each checkpoint's steps with recording
- * and runs the reverse steps on the device; the batch is left in the state
- * the forward ended in.  Constraints and external forces are not
+ * pointer may be NULL.  The forward records its last segment as it runs;
+ * the backward replays each earlier checkpoint's steps with recording and
+ * runs the reverse steps on the device; the batch is left in the state the
+ * forward ended in.  The reverse pass needs the reference-order solver
+ * and one iteration count for all spaces.  Constraints and external forces are not
  * differentiated.  Returns 0 on success, -1 with cpGpuGetLastError() set. */
 int cpGpuRolloutForward(cpGpuBatch *batch, cpFloat dt, int steps, int checkpoint);
-/* Debug: device milliseconds of the last cpGpuRolloutBackward taken with
- * cpGpuSetTiming(1): [0] replays with recording, [1] reverse steps.
- * Returns the number of values written (2), or 0. */
-int cpGpuDebugRolloutTimes(cpGpuBatch *batch, double *out);
 int cpGpuRolloutBackward(cpGpuBatch *batch, const cpFloat *dLdp, cpFloat *dLdv0, cpFloat *dLdw0,
 	cpFloat *dLdm, cpFloat *dLde, cpFloat *dLdu);
+/* Debug: [0], [1] device milliseconds of the last cpGpuRolloutBackward
+ * taken with cpGpuSetTiming(1) (replays with recording, reverse steps);
+ * [2] bytes of the segment tape, [3] bytes of the checkpoints.  Returns the
+ * number of values written (4), or 0. */
+int cpGpuDebugRolloutTimes(cpGpuBatch *batch, double *out);
 void cpGpuSetTiming(int enabled);
 /* Debug: 1 makes single-world sets always solve with the whole-grid
  * kernel (a grid barrier between levels), 0 restores the automatic choice
