@@ -153,10 +153,69 @@ def cpu_sample(workload, budget_s=15.0, warm=5):
     return n * steps / el, steps, el, n
 
 
+def cpu_threads():
+    try:
+        return len(os.sched_getaffinity(0))
+    except AttributeError:
+        return os.cpu_count() or 1
+
+
+def cpu_step_worlds(scenes, dt, steps, threads):
+    """Steps independent worlds of the CPU implementation on `threads` host
+    threads (one world at a time per thread; the ctypes calls release the
+    GIL).  Returns the wall seconds."""
+    from concurrent.futures import ThreadPoolExecutor
+    t0 = time.perf_counter()
+    if threads <= 1:
+        for sc in scenes:
+            sc.step(dt, steps)
+    else:
+        with ThreadPoolExecutor(max_workers=threads) as ex:
+            list(ex.map(lambda sc: sc.step(dt, steps), scenes))
+    return time.perf_counter() - t0
+
+
+def run_reference_worlds(args):
+    """The batch (or the rollout's forward) on the CPU implementation: every
+    world of the workload, stepped on all host threads, one world per thread
+    at a time."""
+    from chipmunk2d_gb300 import Scene
+    lib = oracle_lib()
+    threads = cpu_threads()
+    if args.workload == "batch":
+        sizes = batch_sizes(lib, BATCH_WORLDS)
+        scenes = [Scene(lib, 4, sizes[i], seed=1000 + i) for i in range(BATCH_WORLDS)]
+        dt, steps = BATCH_DT, args.steps
+        desc = "4096 tumble worlds, bodies log-uniform in [8,512], 10 it, dt 1/60, seed 3"
+    else:
+        scenes = _rollout_scenes(lib, range(ROLLOUT_WORLDS))
+        dt, steps = ROLLOUT_DT, ROLLOUT_STEPS
+        desc = "forward only (the CPU implementation has no adjoint): " + ROLLOUT_DESC
+    cpu_step_worlds(scenes, dt, args.warmup, threads)
+    secs = cpu_step_worlds(scenes, dt, steps, threads)
+    nb = sum(sc.nbodies for sc in scenes)
+    for sc in scenes:
+        sc.free()
+    value = len(scenes) * steps / secs
+    line = {
+        "impl": "reference", "metric": "world-steps/s", "value": value, "unit": "world-steps/s",
+        "n_gpus": args.gpus, "steps": steps, "warmup": args.warmup, "ms_per_step": 1000 * secs / steps,
+        "higher_is_better": True, "scaling": "strong", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic", "config": {"workload": args.workload, "description": desc, "worlds": len(scenes), "bodies": nb},
+        "body_steps_per_s": nb * steps / secs,
+        "cpu_baseline": {"value": value, "unit": "world-steps/s", "cores": threads, "kind": "port",
+                         "sample": "every world, %d steps after %d warm-up steps, one world per thread" % (steps, args.warmup)},
+        "e2e": {"value": value, "unit": "world-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
 def run_reference(args):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
+    if args.workload in ("batch", "rollout"):
+        return run_reference_worlds(args)
     workload = args.workload
     cfg, size, dt, desc = WORKLOADS[workload]
     from chipmunk2d_gb300 import Scene
@@ -198,6 +257,7 @@ def batch_sizes(lib, count, seed=3):
 
 BATCH_WORLDS = 4096
 BATCH_DT = 1 / 60
+BATCH_STEPS = 300     # the workload's run length; the worlds settle into piles, so later steps cost more
 
 
 def run_batch(args, emit=True, sharded=True):
@@ -299,20 +359,22 @@ def run_batch(args, emit=True, sharded=True):
     for sc in loop:
         sc.free()
 
-    # CPU restatement, one core, on a sample of worlds
+    # CPU restatement on a sample of worlds (every 16th), the same run
+    # length: one thread, and all host threads (one world per thread)
     from chipmunk2d_gb300 import Scene as S2
     orc = oracle_lib()
-    cpu_n = 128
-    cw = [S2(orc, 4, sizes[i], seed=1000 + i) for i in range(cpu_n)]
+    sample = list(range(0, BATCH_WORLDS, 16))
+    cw = [S2(orc, 4, sizes[i], seed=1000 + i) for i in sample]
+    threads = cpu_threads()
+    cpu_step_worlds(cw, BATCH_DT, args.warmup, threads)
+    cpu_all_s = cpu_step_worlds(cw, BATCH_DT, args.steps, threads)
+    cpu_ws_all = len(cw) * args.steps / cpu_all_s
     for sc in cw:
-        sc.step(BATCH_DT, args.warmup)
-    t0 = time.perf_counter()
-    cpu_steps = 5
-    for _ in range(cpu_steps):
-        for sc in cw:
-            sc.step(BATCH_DT, 1)
-    cpu_ws = cpu_n * cpu_steps / (time.perf_counter() - t0)
-    for sc in cw:
+        sc.free()
+    c1 = [S2(orc, 4, sizes[i], seed=1000 + i) for i in sample[::8]]
+    cpu_step_worlds(c1, BATCH_DT, args.warmup, 1)
+    cpu_ws = len(c1) * args.steps / cpu_step_worlds(c1, BATCH_DT, args.steps, 1)
+    for sc in c1:
         sc.free()
 
     names = PHASES
@@ -329,11 +391,13 @@ def run_batch(args, emit=True, sharded=True):
         "body_steps_per_s": nb_total * args.steps / total_s,
         "looped_plain_gpu_world_steps_per_s": loop_ws,
         "batched_over_looped": world_steps / loop_ws,
-        "phase_ms": dict(zip(names, [round(float(x), 4) for x in phase[:7]])),
+        "phase_ms_after_run": dict(zip(names, [round(float(x), 4) for x in phase[:7]])),
         "gpu_launches": int(launches),
         "clocks": clk,
         "cpu_baseline": {"value": cpu_ws, "unit": "world-steps/s", "cores": 1, "kind": "port",
-                         "sample": "%d worlds x %d steps" % (cpu_n, cpu_steps)},
+                         "sample": "%d worlds (every 128th) x %d steps" % (len(sample[::8]), args.steps)},
+        "cpu_all_threads": {"value": cpu_ws_all, "unit": "world-steps/s", "cores": threads, "kind": "port",
+                            "sample": "%d worlds (every 16th) x %d steps, one world per thread" % (len(sample), args.steps)},
     }
     if emit:
         print(json.dumps(line), flush=True)
@@ -341,6 +405,9 @@ def run_batch(args, emit=True, sharded=True):
 
 
 ROLLOUT_WORLDS, ROLLOUT_SIZE, ROLLOUT_STEPS, ROLLOUT_K, ROLLOUT_DT = 1024, 64, 240, 16, 1 / 120
+ROLLOUT_DESC = ("1024 worlds x (32 circles r~U[1,3] + 32 boxes sides U[2,6]) over a ground segment, "
+                "240 steps, dt 1/120, 10 it, checkpoint every 16, world i seeded 4000+i; "
+                "loss sum |p_final - target|^2, targets ~ N(0,10)")
 
 
 def _rollout_scenes(lib, indices):
@@ -527,14 +594,17 @@ def run_rollout(args, emit=True, sharded=True):
         if u <= 1e-6 * abs(f6):
             resolved.append(abs(adj - f6) / abs(f6))
 
-    # CPU restatement (the oracle), one core: the plain forward of a sample of worlds
+    # CPU restatement (the oracle): the plain forward, one thread on a
+    # sample of worlds and all host threads on every world
     orc = oracle_lib()
     cpu_n = 16
     cw = _rollout_scenes(orc, range(cpu_n))
-    t0 = time.perf_counter()
+    cpu_s = cpu_step_worlds(cw, ROLLOUT_DT, ROLLOUT_STEPS, 1)
     for sc in cw:
-        sc.step(ROLLOUT_DT, ROLLOUT_STEPS)
-    cpu_s = time.perf_counter() - t0
+        sc.free()
+    threads = cpu_threads()
+    cw = _rollout_scenes(orc, range(ROLLOUT_WORLDS))
+    cpu_all_s = cpu_step_worlds(cw, ROLLOUT_DT, ROLLOUT_STEPS, threads)
     for sc in cw:
         sc.free()
 
@@ -546,9 +616,7 @@ def run_rollout(args, emit=True, sharded=True):
         "ms_per_step": 1000 * total / ROLLOUT_STEPS, "higher_is_better": True,
         "scaling": "strong", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
         "config": {"workload": "rollout", "worlds": worlds, "bodies_per_world": ROLLOUT_SIZE,
-                   "description": ("1024 worlds x (32 circles r~U[1,3] + 32 boxes sides U[2,6]) over a ground segment, "
-                                   "240 steps, dt 1/120, 10 it, checkpoint every 16, world i seeded 4000+i; "
-                                   "loss sum |p_final - target|^2, targets ~ N(0,10)"),
+                   "description": ROLLOUT_DESC,
                    "parallelism": ("worlds sharded over %d GPUs" % world_size if world_size > 1 else "single"),
                    "l2": "inputs larger than L2 (tape and checkpoints)"},
         "plain_forward_ms": 1000 * plain_s,
@@ -576,6 +644,9 @@ def run_rollout(args, emit=True, sharded=True):
         "cpu_baseline": {"value": cpu_n * ROLLOUT_STEPS * ROLLOUT_SIZE / cpu_s, "unit": "body-steps/s (forward only)",
                          "cores": 1, "kind": "port",
                          "sample": "%d worlds x %d steps of the forward (the reference has no adjoint)" % (cpu_n, ROLLOUT_STEPS)},
+        "cpu_all_threads": {"value": ROLLOUT_WORLDS * ROLLOUT_STEPS * ROLLOUT_SIZE / cpu_all_s,
+                            "unit": "body-steps/s (forward only)", "cores": threads, "kind": "port",
+                            "sample": "all %d worlds x %d steps of the forward, one world per thread" % (ROLLOUT_WORLDS, ROLLOUT_STEPS)},
         "gpu_forward_body_steps_per_s": worlds * ROLLOUT_SIZE * ROLLOUT_STEPS / plain_s,
     }
     if dist:
@@ -767,16 +838,16 @@ def run_ours(args):
         # mixed shapes and pivot chains at full size (40,000 bodies)
         extras["mixed"] = [mode_sample(lib, "mixed", 150, 150, mode=1, phases=True),
                            mode_sample(lib, "mixed", 3, 2, mode=0)]
-        b = run_batch(argparse.Namespace(steps=30, warmup=3), emit=False, sharded=False)
+        b = run_batch(argparse.Namespace(steps=BATCH_STEPS, warmup=3), emit=False, sharded=False)
         extras["batch"] = {k: b[k] for k in ("value", "unit", "ms_per_step", "body_steps_per_s",
                                              "looped_plain_gpu_world_steps_per_s", "batched_over_looped",
-                                             "cpu_baseline", "phase_ms")}
+                                             "cpu_baseline", "cpu_all_threads", "phase_ms_after_run")}
         extras["batch"]["config"] = b["config"]
         r = run_rollout(args, emit=False, sharded=False)
         extras["rollout"] = {k: r[k] for k in ("value", "unit", "plain_forward_ms", "rollout_forward_ms", "backward_ms",
                                                "fwd_adj_over_forward", "backward_phases_ms", "device_memory_gb",
                                                "gradients_deterministic",
-                                               "fd_check", "cpu_baseline")}
+                                               "fd_check", "cpu_baseline", "cpu_all_threads")}
         extras["rollout"]["config"] = r["config"]
 
     line = {
@@ -814,7 +885,8 @@ def run_ours(args):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=600)
+    ap.add_argument("--steps", type=int, default=None,
+                    help="timed steps (default: 600; the batch workload's own 300; the rollout's 240)")
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--mode", default="colored", choices=["ordered", "colored"])
@@ -827,6 +899,8 @@ def main():
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
+    if args.steps is None:
+        args.steps = BATCH_STEPS if args.workload == "batch" else 600
     if args.impl == "reference":
         run_reference(args)
     elif args.workload == "batch":

@@ -113,6 +113,7 @@ _API = {
     "cpShapeGetBB": (cpBB, [P]),
     "cpShapeSetFriction": (None, [P, D]),
     "cpShapeGetFriction": (D, [P]),
+    "cpShapeGetBody": (P, [P]),
     "cpShapeSetElasticity": (None, [P, D]),
     "cpShapeGetElasticity": (D, [P]),
     "cpCircleShapeNew": (P, [P, D, V]),
@@ -177,6 +178,8 @@ _GPU_API = {
     "cpGpuDebugCandidates": (I, [P, P, I]),
     "cpGpuSetTiming": (None, [I]),
     "cpGpuDebugSetWholeGridSolve": (None, [I]),
+    "cpGpuDebugSetTreeStaging": (None, [I]),
+    "cpGpuDebugSetSolveShape": (None, [I, I]),
     "cpGpuGetPhaseTimes": (I, [P, P, I]),
     "cpGpuGetStepStats": (I, [P, P, I]),
     "cpGpuGetLaunchCount": (ctypes.c_longlong, [I]),

@@ -234,6 +234,14 @@ struct DevSet {
 static cudaStream_t g_stream = NULL;
 static int g_stream_user = 0;
 static int g_timing = 0;
+static int g_tree_stage = -1;
+static int g_solve_threads = 0, g_solve_stage = -1;
+void cpGpuDebugSetSolveShape(int threads, int maxBodies)
+{
+	g_solve_threads = (threads == 64 || threads == 128 || threads == 256 || threads == 512) ? threads : 0;
+	g_solve_stage = maxBodies < 0 ? -1 : maxBodies;
+}
+void cpGpuDebugSetTreeStaging(int maxNodes) { g_tree_stage = maxNodes < 0 ? -1 : maxNodes; }
 static int g_whole_grid = 0;     /* 1: single-world sets always use the whole-grid solve */
 
 static cudaStream_t lib_stream(void)
@@ -706,6 +714,9 @@ static DevSet *devset_build(cpSpace **spaces, int nspaces)
 	d->hostUnitsHint = 0;
 	d->hostMaxBodies = 0;
 	d->hostMaxNodes = 0;
+	d->hostTreeStage = -1;
+	d->hostSolveThreads = 0;
+	d->hostSolveStage = -1;
 	for(int w = 0; w < nspaces; w++){
 		if(ds->hworld[w].nbodies > d->hostMaxBodies) d->hostMaxBodies = ds->hworld[w].nbodies;
 		if(ds->hworld[w].nodeCap > d->hostMaxNodes) d->hostMaxNodes = ds->hworld[w].nodeCap;
@@ -816,6 +827,9 @@ static int devset_step(DevSet *ds, const double *dts, cpSpace **only)
 	}
 	cudaStream_t st = lib_stream();
 	if(g_whole_grid) d->hostUnitsHint = 0x7fffffff;
+	d->hostTreeStage = g_tree_stage;
+	d->hostSolveThreads = g_solve_threads;
+	d->hostSolveStage = g_solve_stage;
 	if(!h2d(d->params, hp, sizeof(cpgParams)*(size_t)ds->nspaces)) return -1;
 	cudaEventRecord(ds->paramEvent[slot], st);
 	ds->paramRecorded[slot] = 1;

@@ -300,6 +300,9 @@ typedef struct cpgSet {
 	int hostUnitsHint;            /* solver units of world 0 last step (host value) */
 	int hostMaxBodies;            /* largest world (host value) */
 	int hostMaxNodes;             /* largest world's node pool (host value) */
+	int hostTreeStage;            /* worlds of at most this many nodes run the tree from shared memory; -1: all that fit */
+	int hostSolveThreads;         /* block size of the per-world solve; 0: default */
+	int hostSolveStage;           /* worlds of at most this many bodies solve from shared memory; -1: all that fit */
 
 	/* stats block copied to the host after each step */
 	int *stats;

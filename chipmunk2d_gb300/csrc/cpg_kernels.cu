@@ -1713,6 +1713,11 @@ extern "C" int cpg_launch_step(const cpgSet *s, const cpgSet *h, int mode, void 
 		/* node pools of up to CPG_STAGED_NODES nodes (64 B each) run from
 		 * shared memory; larger worlds use the global pool */
 		int staged = h->hostMaxNodes <= CPG_STAGED_NODES ? h->hostMaxNodes : 0;
+		/* the tree is one serial thread per world: many worlds gain more
+		 * from residency (a pool sized for the largest world would hold
+		 * every block's shared memory) than from shared-memory latency */
+		if(h->hostTreeStage >= 0){ if(h->hostTreeStage < staged) staged = h->hostTreeStage; }
+		else if(W > 2*152) staged = 0;
 		size_t smem = (size_t)staged*sizeof(cpgNode);
 		static size_t treeSmemSet = 0;
 		if(smem > 48*1024 && smem > treeSmemSet){
@@ -1746,13 +1751,17 @@ extern "C" int cpg_launch_step(const cpgSet *s, const cpgSet *h, int mode, void 
 		launch_coop((const void *)k_solve_coop<false>, CPG_COOP_SOLVE_THREADS, &sv, 0, st);
 	} else {
 		int stagedMax = h->hostMaxBodies <= CPG_STAGED_BODIES ? h->hostMaxBodies : 0;
+		if(h->hostSolveStage >= 0 && h->hostSolveStage < stagedMax) stagedMax = h->hostSolveStage;
 		size_t smem = (size_t)stagedMax*8*sizeof(double);
 		static size_t smemSet = 0;
 		if(smem > 48*1024 && smem > smemSet){
 			cudaFuncSetAttribute(k_solve, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
 			smemSet = smem;
 		}
-		LAUNCH(k_solve<<<W, 256, smem, st>>>(*s, stagedMax));
+		/* many worlds: small blocks keep more worlds resident (registers
+		 * limit a 256-thread block to two per SM); one world: wide levels */
+		int threads = h->hostSolveThreads > 0 ? h->hostSolveThreads : (W >= 152 ? 64 : 256);
+		LAUNCH(k_solve<<<W, threads, smem, st>>>(*s, stagedMax));
 	}
 	LAUNCH(k_writeback<<<dim3(perWorldX, W), 128, 0, st>>>(*s));
 	LAUNCH(k_unpack_bodies<<<blocks_for(h->totalBodies, 128), 128, 0, st>>>(*s));

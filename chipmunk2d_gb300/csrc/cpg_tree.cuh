@@ -41,6 +41,31 @@ struct TreeCtx {
 	int collide;            /* 1: emit candidates; 0: the void query */
 };
 
+/* Comparisons on ordered integer images of the doubles: -0 folds to +0
+ * and negative magnitudes are inverted, so tkey(a) < tkey(b) exactly when
+ * a < b for every non-NaN pair.  The tree runs on one thread per world and
+ * its box tests, min and max would each be an FP64 instruction (64 cycles
+ * of the sub-partition's FP64 pipe, shared with the other worlds' threads);
+ * as integer compares and selects they return the same values. */
+__device__ __forceinline__ long long tkey(double x)
+{
+	long long b = __double_as_longlong(x);
+	if(b == (long long)0x8000000000000000ull) b = 0;
+	return b < 0 ? (b ^ 0x7FFFFFFFFFFFFFFFll) : b;
+}
+__device__ __forceinline__ double tmin(double a, double b) { return (tkey(a) < tkey(b)) ? a : b; }
+__device__ __forceinline__ double tmax(double a, double b) { return (tkey(a) > tkey(b)) ? a : b; }
+__device__ __forceinline__ bool tintersects(BB a, BB b)
+{
+	return tkey(a.l) <= tkey(b.r) && tkey(b.l) <= tkey(a.r) && tkey(a.b) <= tkey(b.t) && tkey(b.b) <= tkey(a.t);
+}
+__device__ __forceinline__ bool tcontains(BB bb, BB o)
+{
+	return tkey(bb.l) <= tkey(o.l) && tkey(bb.r) >= tkey(o.r) && tkey(bb.b) <= tkey(o.b) && tkey(bb.t) >= tkey(o.t);
+}
+__device__ __forceinline__ BB tmerge(BB a, BB b) { return bbnew(tmin(a.l, b.l), tmin(a.b, b.b), tmax(a.r, b.r), tmax(a.t, b.t)); }
+__device__ __forceinline__ double tmergedarea(BB a, BB b) { return (tmax(a.r, b.r) - tmin(a.l, b.l))*(tmax(a.t, b.t) - tmin(a.b, b.b)); }
+
 __device__ __forceinline__ BB node_bb(const cpgNode &n) { return bbnew(n.l, n.b, n.r, n.t); }
 __device__ __forceinline__ void set_node_bb(cpgNode &n, BB bb) { n.l = bb.l; n.b = bb.b; n.r = bb.r; n.t = bb.t; }
 __device__ __forceinline__ bool is_leaf(const TreeCtx &c, int n) { return c.nodes[n].obj >= 0; }
@@ -55,7 +80,7 @@ __device__ BB fatten(BB bb, V2 vel)
 	double x = (bb.r - bb.l)*coef;
 	double y = (bb.t - bb.b)*coef;
 	V2 v = vmul(vel, (double)0.1f);
-	return bbnew(bb.l + dmin(-x, v.x), bb.b + dmin(-y, v.y), bb.r + dmax(x, v.x), bb.t + dmax(y, v.y));
+	return bbnew(bb.l + tmin(-x, v.x), bb.b + tmin(-y, v.y), bb.r + tmax(x, v.x), bb.t + tmax(y, v.y));
 }
 
 __device__ BB leaf_fat_bb(const TreeCtx &c, int s)
@@ -167,7 +192,7 @@ __device__ int node_new(TreeCtx &c, int a, int b)
 	if(n < 0) return -1;
 	cpgNode &nd = c.nodes[n];
 	nd.obj = -1;
-	set_node_bb(nd, bbmerge(node_bb(c.nodes[a]), node_bb(c.nodes[b])));
+	set_node_bb(nd, tmerge(node_bb(c.nodes[a]), node_bb(c.nodes[b])));
 	nd.parent = -1;
 	nd.A = a; c.nodes[a].parent = n;
 	nd.B = b; c.nodes[b].parent = n;
@@ -190,7 +215,7 @@ __device__ void node_replace_child(TreeCtx &c, int parent, int child, int value)
 	for(int n = parent; n >= 0; n = c.nodes[n].parent){
 		if(++guard > c.nodeCap){ c.T->error |= CPG_ERR_NODES; return; }
 		cpgNode &nd = c.nodes[n];
-		set_node_bb(nd, bbmerge(node_bb(c.nodes[nd.A]), node_bb(c.nodes[nd.B])));
+		set_node_bb(nd, tmerge(node_bb(c.nodes[nd.A]), node_bb(c.nodes[nd.B])));
 	}
 }
 
@@ -208,15 +233,15 @@ __device__ int subtree_insert(TreeCtx &c, int root, int leaf)
 		if(guard > c.nodeCap){ c.T->error |= CPG_ERR_NODES; return root; }
 		cpgNode &nd = c.nodes[cur];
 		BB abb = node_bb(c.nodes[nd.A]), bbb = node_bb(c.nodes[nd.B]);
-		double cost_a = bbarea(bbb) + bbmergedarea(abb, lbb);
-		double cost_b = bbarea(abb) + bbmergedarea(bbb, lbb);
-		if(cost_a == cost_b){
+		double cost_a = bbarea(bbb) + tmergedarea(abb, lbb);
+		double cost_b = bbarea(abb) + tmergedarea(bbb, lbb);
+		if(tkey(cost_a) == tkey(cost_b)){
 			cost_a = bbproximity(abb, lbb);
 			cost_b = bbproximity(bbb, lbb);
 		}
-		bool goB = (cost_b < cost_a);
+		bool goB = (tkey(cost_b) < tkey(cost_a));
 		int child = goB ? nd.B : nd.A;
-		set_node_bb(nd, bbmerge(node_bb(nd), lbb));
+		set_node_bb(nd, tmerge(node_bb(nd), lbb));
 		if(is_leaf(c, child)){
 			int nn = node_new(c, leaf, child);
 			if(nn < 0) return root;
@@ -261,7 +286,7 @@ __device__ void mark_leaf_query(TreeCtx &c, int subtree, int leaf, bool left)
 	while(sp > 0){
 		int n = stack[--sp];
 		const cpgNode &nd = c.nodes[n];
-		if(!bbintersects(lbb, node_bb(nd))) continue;
+		if(!tintersects(lbb, node_bb(nd))) continue;
 		if(nd.obj >= 0){
 			if(left){
 				pair_insert(c, leaf, n);
@@ -416,7 +441,7 @@ __device__ void leaf_update(TreeCtx &c, int leaf)
 	cpgTree *T = c.T;
 	int s = c.nodes[leaf].obj;
 	BB bb = shape_bb(c, s);
-	if(!bbcontains(node_bb(c.nodes[leaf]), bb)){
+	if(!tcontains(node_bb(c.nodes[leaf]), bb)){
 		set_node_bb(c.nodes[leaf], leaf_fat_bb(c, s));
 		int root = subtree_remove(c, T->dynRoot, leaf);
 		T->dynRoot = subtree_insert(c, root, leaf);

@@ -524,6 +524,13 @@ void cpGpuSetTiming(int enabled);
  * at least 2048).  Both give the same results; the parity tests use this
  * to cover the whole-grid path on small worlds. */
 void cpGpuDebugSetWholeGridSolve(int always);
+/* Debug: the ordered tree step keeps the node pools of worlds of at most
+ * maxNodes nodes in shared memory (-1: every world whose pool fits). */
+void cpGpuDebugSetTreeStaging(int maxNodes);
+/* Debug: block size of the per-world solve (64, 128, 256 or 512; anything
+ * else restores the default) and the largest world (in bodies) whose
+ * bodies it keeps in shared memory (-1: every world that fits). */
+void cpGpuDebugSetSolveShape(int threads, int maxBodies);
 /* Bookkeeping of the last step (after it completes): [0] error flags,
  * [1] pair-pool use and [2] node-pool use (per mille of capacity, largest
  * world), [3] live cached arbiters, [4] candidate pairs, [5] solved
