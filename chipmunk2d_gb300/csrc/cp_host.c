@@ -226,6 +226,7 @@ struct DevSet {
 	int nspaces;
 	void *slab;
 	size_t slabBytes;
+	void *scratch;            /* per-step scratch outside the slab (not checkpointed) */
 	cpgArb *gather;           /* arbiter snapshot staging */
 	int gatherCap;
 };
@@ -554,6 +555,7 @@ static void devset_free(DevSet *ds)
 {
 	if(!ds) return;
 	if(ds->slab) cudaFree(ds->slab);
+	if(ds->scratch) cudaFree(ds->scratch);
 	if(ds->gather) cudaFree(ds->gather);
 	if(ds->hparams) cudaFreeHost(ds->hparams);
 	if(ds->hstats) cudaFreeHost(ds->hstats);
@@ -641,6 +643,13 @@ static DevSet *devset_build(cpSpace **spaces, int nspaces)
 	ds->slabBytes = bytes;
 	if(!cuda_ok(cudaMalloc(&ds->slab, bytes), "cudaMalloc set")){ devset_free(ds); return NULL; }
 	carve_set(d, (char *)ds->slab, 1);
+	/* per-step scratch that no checkpoint needs: its own allocation */
+	{
+		size_t nb = sizeof(int)*(size_t)CPG_PAIR_TYPES*(size_t)(d->totalCands > 0 ? d->totalCands : 1);
+		if(!cuda_ok(cudaMalloc(&ds->scratch, nb + 256), "cudaMalloc narrow scratch")){ devset_free(ds); return NULL; }
+		d->nbCount = (int *)ds->scratch;
+		d->nbucket = (int *)((char *)ds->scratch + 256);
+	}
 	cudaStream_t st = lib_stream();
 	int ok = 1;
 	ok &= cuda_ok(cudaMemsetAsync(ds->slab, 0, bytes, st), "memset set");

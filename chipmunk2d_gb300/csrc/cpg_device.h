@@ -191,6 +191,8 @@ typedef struct cpgOp {
 
 /* All device arrays of a set.  Vectors are split into x/y arrays. */
 /* Recording of replayed steps for the differentiable rollout. */
+#define CPG_PAIR_TYPES 6
+
 /* Reverse solve: doubles of a contact lane's scratch (AdjLaneBar), block
  * size, and the largest world whose body adjoints it keeps in shared memory. */
 #define CPG_ADJ_LANE_DOUBLES 12
@@ -262,6 +264,11 @@ typedef struct cpgSet {
 	/* per-step collision data [totalCands] */
 	cpgCand *cands;
 	cpgNarrow *narrow;
+	/* narrow-phase scratch outside the slab: candidates that pass
+	 * QueryReject, by pair type ([CPG_PAIR_TYPES][totalCands] flat
+	 * candidate indices), and the per-type counts */
+	int *nbucket;
+	int *nbCount;
 	int *candArb;                 /* arbiter slot pushed to the solve list, or -1 */
 	int *arbList;                 /* solve list: arbiter slots, per world */
 	int *prevList;                /* previous step's solve list */

@@ -7,7 +7,8 @@
  *   k_integrate_pos   position_func over dynamic bodies             (:364-367)
  *   k_shape_cache     world-space shape data + AABBs                (:371)
  *   k_tree            reference-order broadphase, 1 thread/world    (:372)
- *   k_narrow          QueryReject + cpCollide per candidate         (:235-244)
+ *   k_narrow_classify QueryReject per candidate, buckets by pair kind (:235-244)
+ *   k_narrow_collide  cpCollide over the buckets, one kind per warp
  *   k_arb_update      arbiter cache upsert + cpArbiterUpdate        (:246-288)
  *   k_solve_list      order-preserving compaction -> solve list     (:274)
  *   k_arb_filter      age out cached arbiters                       (:380)
@@ -236,33 +237,99 @@ __device__ bool query_reject(const cpgSet &s, const cpgWorld &W, int a, int b)
 	return false;
 }
 
-__global__ void k_narrow(cpgSet s)
+/* Pair routine of two shape kinds (cpCollision.c:688-726 orders the
+ * shapes by kind): 0 circle-circle, 1 circle-segment, 2 segment-segment,
+ * 3 circle-poly, 4 segment-poly, 5 poly-poly. */
+__device__ __forceinline__ int pair_type(int ka, int kb)
+{
+	int lo = ka < kb ? ka : kb, hi = ka < kb ? kb : ka;
+	int c = lo + hi*3;
+	return c == 0 ? 0 : c == 3 ? 1 : c == 4 ? 2 : c == 6 ? 3 : c == 7 ? 4 : 5;
+}
+
+/* Pass 1, one thread per candidate: QueryReject; a rejected candidate gets
+ * its empty result here, the others are appended to their pair type's
+ * bucket (warp-aggregated atomics).  The order inside a bucket is not
+ * deterministic and need not be: every candidate's result goes to its own
+ * slot. */
+__global__ void k_narrow_classify(cpgSet s)
 {
 	int w = blockIdx.y;
 	if(!s.params[w].active) return;
 	const cpgWorld &W = s.world[w];
 	int n = s.tree[w].ncand;
-	NarrowCtx nc; nc.s = &s; nc.shapeBase = W.shapeOff; nc.bodyBase = W.bodyOff; nc.vertBase = W.vertOff;
-	for(int i = blockIdx.x*blockDim.x + threadIdx.x; i < n; i += gridDim.x*blockDim.x){
-		cpgCand cd = s.cands[W.candOff + i];
-		cpgNarrow out;
-		out.count = 0; out.flip = 0; out.idOut = cd.idIn; out.nx = 0.0; out.ny = 0.0;
-		if(!query_reject(s, W, cd.a, cd.b)){
-			ShapeView A = load_shape(nc, cd.a), B = load_shape(nc, cd.b);
-			NInfo info;
-			int flip;
-			collide(A, B, cd.idIn, info, flip);
-			out.count = info.count > 2 ? 2 : info.count;
-			out.flip = flip;
-			out.idOut = info.id;
-			out.nx = info.n.x; out.ny = info.n.y;
-			for(int k = 0; k < out.count; k++){
-				out.p1x[k] = info.p1[k].x; out.p1y[k] = info.p1[k].y;
-				out.p2x[k] = info.p2[k].x; out.p2y[k] = info.p2[k].y;
-				out.hash[k] = info.hash[k];
+	int stride = gridDim.x*blockDim.x;
+	int lane = threadIdx.x & 31;
+	for(int base = blockIdx.x*blockDim.x; base < n; base += stride){
+		int i = base + threadIdx.x;
+		int t = -1;
+		if(i < n){
+			cpgCand cd = s.cands[W.candOff + i];
+			if(query_reject(s, W, cd.a, cd.b)){
+				cpgNarrow out;
+				out.count = 0; out.flip = 0; out.idOut = cd.idIn; out.nx = 0.0; out.ny = 0.0;
+				s.narrow[W.candOff + i] = out;
+				if(cd.pair >= 0) s.pairs[W.pairOff + cd.pair].id = out.idOut;
+			} else {
+				t = pair_type(s.skind[W.shapeOff + cd.a], s.skind[W.shapeOff + cd.b]);
 			}
 		}
-		s.narrow[W.candOff + i] = out;
+		unsigned active = __ballot_sync(0xffffffffu, t >= 0);
+		if(t >= 0){
+			unsigned peers = __match_any_sync(active, t);
+			int leader = __ffs(peers) - 1;
+			int slot0 = 0;
+			if(lane == leader) slot0 = atomicAdd(&s.nbCount[t], __popc(peers));
+			slot0 = __shfl_sync(peers, slot0, leader);
+			int rank = __popc(peers & ((1u << lane) - 1u));
+			s.nbucket[(size_t)t*s.totalCands + slot0 + rank] = W.candOff + i;
+		}
+	}
+}
+
+/* The world whose candidate range holds flat candidate index c. */
+__device__ __forceinline__ int world_of_cand(const cpgSet &s, int c)
+{
+	int lo = 0, hi = s.nworlds - 1;
+	while(lo < hi){
+		int mid = (lo + hi + 1) >> 1;
+		if(s.world[mid].candOff <= c) lo = mid; else hi = mid - 1;
+	}
+	return lo;
+}
+
+/* Pass 2 (cpSpaceStep.c:219-244, cpCollision.c:701-726): the buckets one
+ * after another over the whole grid, so that a warp runs one pair routine
+ * on 32 candidates that all need it. */
+__global__ void __launch_bounds__(128) k_narrow_collide(cpgSet s)
+{
+	int cnt[CPG_PAIR_TYPES];
+	int total = 0;
+#pragma unroll
+	for(int t = 0; t < CPG_PAIR_TYPES; t++){ cnt[t] = s.nbCount[t]; total += cnt[t]; }
+	for(int e = blockIdx.x*blockDim.x + threadIdx.x; e < total; e += gridDim.x*blockDim.x){
+		int t = 0, base = 0;
+		while(t < CPG_PAIR_TYPES - 1 && e - base >= cnt[t]){ base += cnt[t]; t++; }
+		int c = s.nbucket[(size_t)t*s.totalCands + (e - base)];
+		int w = world_of_cand(s, c);
+		const cpgWorld &W = s.world[w];
+		cpgCand cd = s.cands[c];
+		NarrowCtx nc; nc.s = &s; nc.shapeBase = W.shapeOff; nc.bodyBase = W.bodyOff; nc.vertBase = W.vertOff;
+		ShapeView A = load_shape(nc, cd.a), B = load_shape(nc, cd.b);
+		NInfo info;
+		int flip;
+		collide(A, B, cd.idIn, info, flip);
+		cpgNarrow out;
+		out.count = info.count > 2 ? 2 : info.count;
+		out.flip = flip;
+		out.idOut = info.id;
+		out.nx = info.n.x; out.ny = info.n.y;
+		for(int k = 0; k < out.count; k++){
+			out.p1x[k] = info.p1[k].x; out.p1y[k] = info.p1[k].y;
+			out.p2x[k] = info.p2[k].x; out.p2y[k] = info.p2[k].y;
+			out.hash[k] = info.hash[k];
+		}
+		s.narrow[c] = out;
 		if(cd.pair >= 0) s.pairs[W.pairOff + cd.pair].id = out.idOut;
 	}
 }
@@ -1727,7 +1794,9 @@ extern "C" int cpg_launch_step(const cpgSet *s, const cpgSet *h, int mode, void 
 		LAUNCH(k_tree<<<W, 32, smem, st>>>(*s, staged));
 	}
 	if(timing) cudaEventRecord(ev[2], st);
-	LAUNCH(k_narrow<<<dim3(perWorldX, W), 128, 0, st>>>(*s));
+	cudaMemsetAsync(s->nbCount, 0, CPG_PAIR_TYPES*sizeof(int), st);
+	LAUNCH(k_narrow_classify<<<dim3(perWorldX, W), 128, 0, st>>>(*s));
+	LAUNCH(k_narrow_collide<<<152*3, 128, 0, st>>>(*s));
 	if(timing) cudaEventRecord(ev[3], st);
 	LAUNCH(k_arb_update<<<dim3(perWorldX, W), 128, 0, st>>>(*s));
 	if(colored){
