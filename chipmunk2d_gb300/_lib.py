@@ -171,6 +171,7 @@ _GPU_API = {
     "cpGpuRolloutForward": (I, [P, D, I, I]),
     "cpGpuRolloutBackward": (I, [P, P, P, P, P, P, P]),
     "cpGpuDebugRolloutTimes": (I, [P, P]),
+    "cpGpuDebugSetRolloutRecording": (None, [I]),
     "cpGpuDebugBodies": (I, [P, P, I]),
     "cpGpuDebugArbiters": (I, [P, P, I]),
     "cpGpuDebugConstraints": (I, [P, P, I]),
@@ -180,6 +181,7 @@ _GPU_API = {
     "cpGpuDebugSetWholeGridSolve": (None, [I]),
     "cpGpuDebugSetTreeStaging": (None, [I]),
     "cpGpuDebugSetSolveShape": (None, [I, I]),
+    "cpGpuDebugSetSolveLayout": (None, [I]),
     "cpGpuGetPhaseTimes": (I, [P, P, I]),
     "cpGpuGetStepStats": (I, [P, P, I]),
     "cpGpuGetLaunchCount": (ctypes.c_longlong, [I]),

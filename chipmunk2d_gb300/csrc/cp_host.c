@@ -236,12 +236,15 @@ static cudaStream_t g_stream = NULL;
 static int g_stream_user = 0;
 static int g_timing = 0;
 static int g_tree_stage = -1;
-static int g_solve_threads = 0, g_solve_stage = -1;
+static int g_rollout_record = 1;
+void cpGpuDebugSetRolloutRecording(int on) { g_rollout_record = on ? 1 : 0; }
+static int g_solve_threads = 0, g_solve_stage = -1, g_solve_layout = 0;
 void cpGpuDebugSetSolveShape(int threads, int maxBodies)
 {
-	g_solve_threads = (threads == 64 || threads == 128 || threads == 256 || threads == 512) ? threads : 0;
+	g_solve_threads = (threads == 32 || threads == 64 || threads == 128 || threads == 256 || threads == 512) ? threads : 0;
 	g_solve_stage = maxBodies < 0 ? -1 : maxBodies;
 }
+void cpGpuDebugSetSolveLayout(int policy) { g_solve_layout = (policy >= 0 && policy <= 3) ? policy : 0; }
 void cpGpuDebugSetTreeStaging(int maxNodes) { g_tree_stage = maxNodes < 0 ? -1 : maxNodes; }
 static int g_whole_grid = 0;     /* 1: single-world sets always use the whole-grid solve */
 
@@ -726,6 +729,7 @@ static DevSet *devset_build(cpSpace **spaces, int nspaces)
 	d->hostTreeStage = -1;
 	d->hostSolveThreads = 0;
 	d->hostSolveStage = -1;
+	d->solveLayout = 0;
 	for(int w = 0; w < nspaces; w++){
 		if(ds->hworld[w].nbodies > d->hostMaxBodies) d->hostMaxBodies = ds->hworld[w].nbodies;
 		if(ds->hworld[w].nodeCap > d->hostMaxNodes) d->hostMaxNodes = ds->hworld[w].nodeCap;
@@ -839,6 +843,7 @@ static int devset_step(DevSet *ds, const double *dts, cpSpace **only)
 	d->hostTreeStage = g_tree_stage;
 	d->hostSolveThreads = g_solve_threads;
 	d->hostSolveStage = g_solve_stage;
+	d->solveLayout = g_solve_layout;
 	if(!h2d(d->params, hp, sizeof(cpgParams)*(size_t)ds->nspaces)) return -1;
 	cudaEventRecord(ds->paramEvent[slot], st);
 	ds->paramRecorded[slot] = 1;
@@ -924,14 +929,30 @@ void cpGpuSpaceSync(cpSpace *sp)
  * Batches
  * ==================================================================== */
 /* A differentiable rollout of a batch: the forward's checkpoints. */
-typedef struct TapeMem {
+/* The light tape of one segment (a cpgTape whose app is NULL): recorded
+ * by the forward and kept for the reverse pass. */
+typedef struct SegTape {
 	cpgTape t;
-	cpgAdj a;
-	void *block;                  /* one allocation for everything */
-} TapeMem;
+	void *block;
+	size_t bytes;
+	int recorded;                 /* holds the forward's steps of the segment */
+	int maxStepRows;              /* the most rows of one of its steps */
+	int rowsUsed;                 /* rows of all its steps */
+} SegTape;
 
-/* A differentiable rollout of a batch: the forward's checkpoints, and the
- * device buffers of the reverse pass, kept for the next rollout of the
+/* Scratch of the reverse pass, shared by the segments: the adjoint state,
+ * the per-step contact scratch, the recomputed solves' rows and bodies and
+ * their per-iteration records. */
+typedef struct AdjMem {
+	cpgAdj a;
+	double *app;                  /* [segRows][iters][2] AdjApp */
+	void *block;
+	size_t bytes, segRows, stepRows;
+	int K, iters;
+} AdjMem;
+
+/* A differentiable rollout of a batch: the forward's checkpoints and light
+ * tapes, and the reverse pass's scratch, kept for the next rollout of the
  * same shape (a training loop calls forward and backward repeatedly). */
 typedef struct Rollout {
 	int steps, K, nckpt;
@@ -940,12 +961,12 @@ typedef struct Rollout {
 	int ckptCap;
 	unsigned *stamps;             /* [nckpt][nspaces] host stamps at the checkpoints */
 	double *currDt;               /* [nckpt][nspaces] */
-	size_t rowCap;                /* tape rows the last reverse pass needed */
+	SegTape *segs;                /* [segCap] */
+	int segCap;
+	size_t rowEst;                /* rows to provide for a segment: the largest need seen */
 	char *fin;                    /* the forward's final state during the reverse pass */
-	TapeMem tape;                 /* tape.block == NULL until the first reverse pass */
-	int tapeK, tapeIters;
+	AdjMem adj;
 	float replayMs, adjointMs;    /* device time of the last reverse pass (with cpGpuSetTiming(1)) */
-	int lastTaped;                /* the forward recorded its last segment into tape */
 } Rollout;
 
 struct cpGpuBatch {
@@ -960,7 +981,9 @@ static void rollout_free(Rollout *r)
 	if(!r) return;
 	if(r->ckpt) cudaFree(r->ckpt);
 	if(r->fin) cudaFree(r->fin);
-	if(r->tape.block) cudaFree(r->tape.block);
+	for(int i = 0; i < r->segCap; i++) if(r->segs[i].block) cudaFree(r->segs[i].block);
+	if(r->adj.block) cudaFree(r->adj.block);
+	free(r->segs);
 	free(r->stamps); free(r->currDt);
 	free(r);
 }
@@ -1053,44 +1076,92 @@ static void rollout_restore_from(DevSet *ds, const char *src, const unsigned *st
 }
 
 
-static size_t tape_carve(cpgSet *d, TapeMem *m, char *base, int K, size_t rowCap, int iters, int pass)
+/* ---- rollout memory ---- */
+
+#define RCARVE(ptr, type, count) do { size_t b_ = align256(sizeof(type)*(size_t)((count) > 0 ? (count) : 1)); if(base) ptr = (type *)(base + total); total += b_; } while(0)
+
+static size_t seg_carve(const cpgSet *d, cpgTape *t, char *base, int K, size_t rowCap)
 {
 	size_t total = 0;
-#define TCARVE(ptr, type, count) do { size_t b_ = align256(sizeof(type)*(size_t)((count) > 0 ? (count) : 1)); if(pass) ptr = (type *)(base + total); total += b_; } while(0)
 	int W = d->nworlds;
 	size_t levCap = rowCap + (size_t)K*(W + 1);
-	TCARVE(m->t.body, double, (size_t)K*8*d->totalBodies);
-	TCARVE(m->t.shape, double, (size_t)K*6*d->totalShapes);
-	TCARVE(m->t.verts, double, (size_t)K*4*d->totalVerts);
-	TCARVE(m->t.params, cpgParams, (size_t)K*W);
-	TCARVE(m->t.rows, cpgRow, rowCap);
-	TCARVE(m->t.rowInfo, int, 4*rowCap);
-	TCARVE(m->t.rowWorld, int, rowCap);
-	TCARVE(m->t.rowOff, int, (size_t)K*(W + 1));
-	TCARVE(m->t.levels, int, levCap);
-	TCARVE(m->t.levOff, int, (size_t)K*(W + 1));
-	TCARVE(m->t.app, double, rowCap*(size_t)iters*2*14);   /* AdjApp: 14 doubles */
-	TCARVE(m->t.cursor, int, 4);
-	TCARVE(m->a.body, double, 9*(size_t)d->totalBodies);
-	TCARVE(m->a.arb, double, 4*(size_t)d->arbCap);
-	TCARVE(m->a.gMinv, double, d->totalBodies);
-	TCARVE(m->a.gE, double, d->totalShapes);
-	TCARVE(m->a.gU, double, d->totalShapes);
-	TCARVE(m->a.con, double, rowCap*2*4*CPG_ADJ_LANE_DOUBLES);
-	TCARVE(m->a.unit, double, rowCap*20);
-	TCARVE(m->a.arbTmp, double, 4*(size_t)d->arbCap);
-#undef TCARVE
-	if(pass){ m->t.K = K; m->t.rowCap = (int)rowCap; m->t.levCap = (int)levCap; }
+	RCARVE(t->body, double, (size_t)K*8*d->totalBodies);
+	RCARVE(t->vel, double, (size_t)K*3*d->totalBodies);
+	RCARVE(t->shape, double, (size_t)K*6*d->totalShapes);
+	RCARVE(t->verts, double, (size_t)K*4*d->totalVerts);
+	RCARVE(t->params, cpgParams, (size_t)K*W);
+	RCARVE(t->rows, cpgRow, rowCap);
+	RCARVE(t->rowInfo, int, 4*rowCap);
+	RCARVE(t->rowWorld, int, rowCap);
+	RCARVE(t->rowOff, int, (size_t)K*(W + 1));
+	RCARVE(t->levels, int, levCap);
+	RCARVE(t->levOff, int, (size_t)K*(W + 1));
+	RCARVE(t->cursor, int, 4);
+	if(base){ t->K = K; t->rowCap = (int)rowCap; t->levCap = (int)levCap; t->app = NULL; t->on = 0; t->step = 0; }
 	return total;
 }
 
-static int tape_alloc(cpgSet *d, TapeMem *m, int K, size_t rowCap, int iters)
+static size_t adj_carve(const cpgSet *d, AdjMem *m, char *base, int K, size_t segRows, size_t stepRows, int iters)
 {
-	memset(m, 0, sizeof(*m));
-	if(rowCap > 0x7fffffffULL/(size_t)(iters*2 + 2)){ set_error(CP_GPU_ERR_OVERFLOW, "rollout: tape too large"); return 0; }
-	size_t bytes = tape_carve(d, m, NULL, K, rowCap, iters, 0);
-	if(!cuda_ok(cudaMalloc(&m->block, bytes), "cudaMalloc rollout tape")){ m->block = NULL; return 0; }
-	tape_carve(d, m, (char *)m->block, K, rowCap, iters, 1);
+	size_t total = 0;
+	size_t nb = (size_t)d->totalBodies, ns = (size_t)d->totalShapes;
+	RCARVE(m->a.body, double, 9*nb);
+	RCARVE(m->a.arb, double, 4*(size_t)d->arbCap);
+	RCARVE(m->a.gMinv, double, nb);
+	RCARVE(m->a.gE, double, ns);
+	RCARVE(m->a.gU, double, ns);
+	RCARVE(m->a.con, double, stepRows*2*4*CPG_ADJ_LANE_DOUBLES);
+	RCARVE(m->a.unit, double, stepRows*20);
+	RCARVE(m->a.arbTmp, double, 4*(size_t)d->arbCap);
+	RCARVE(m->a.srows, cpgRow, segRows);
+	RCARVE(m->a.sbodies, double, (size_t)K*nb*8);
+	RCARVE(m->app, double, segRows*(size_t)iters*2*14);     /* AdjApp: 14 doubles */
+	return total;
+}
+#undef RCARVE
+
+/* A segment tape of at least rowCap rows (the kept one if it fits). */
+static int seg_alloc(const cpgSet *d, SegTape *sg, int K, size_t rowCap)
+{
+	if(sg->block && sg->t.K == K && (size_t)sg->t.rowCap >= rowCap) return 1;
+	if(rowCap > 0x7fffffffULL/4){ set_error(CP_GPU_ERR_OVERFLOW, "rollout: tape too large"); return 0; }
+	if(sg->block) cudaFree(sg->block);
+	memset(sg, 0, sizeof(*sg));
+	size_t bytes = seg_carve(d, &sg->t, NULL, K, rowCap);
+	if(!cuda_ok(cudaMalloc(&sg->block, bytes), "cudaMalloc rollout tape")){ sg->block = NULL; return 0; }
+	seg_carve(d, &sg->t, (char *)sg->block, K, rowCap);
+	sg->bytes = bytes;
+	return 1;
+}
+
+/* The reverse pass's scratch, at least segRows x stepRows; `keep` copies
+ * the adjoint state of a pass in progress into a larger one. */
+static int adj_ensure(const cpgSet *d, AdjMem *m, int K, size_t segRows, size_t stepRows, int iters, int keep)
+{
+	if(m->block && m->K == K && m->iters == iters && m->segRows >= segRows && m->stepRows >= stepRows) return 1;
+	if(segRows < m->segRows) segRows = m->segRows;
+	if(stepRows < m->stepRows) stepRows = m->stepRows;
+	if(segRows > 0x7fffffffULL/(size_t)(2*iters + 2)){ set_error(CP_GPU_ERR_OVERFLOW, "rollout: tape too large"); return 0; }
+	AdjMem n;
+	memset(&n, 0, sizeof(n));
+	size_t bytes = adj_carve(d, &n, NULL, K, segRows, stepRows, iters);
+	if(!cuda_ok(cudaMalloc(&n.block, bytes), "cudaMalloc rollout scratch")) return 0;
+	adj_carve(d, &n, (char *)n.block, K, segRows, stepRows, iters);
+	n.bytes = bytes; n.segRows = segRows; n.stepRows = stepRows; n.K = K; n.iters = iters;
+	if(m->block){
+		if(keep){
+			cudaStream_t st = lib_stream();
+			size_t nb = (size_t)d->totalBodies, ns = (size_t)d->totalShapes;
+			cudaMemcpyAsync(n.a.body, m->a.body, sizeof(double)*9*nb, cudaMemcpyDeviceToDevice, st);
+			cudaMemcpyAsync(n.a.arb, m->a.arb, sizeof(double)*4*(size_t)d->arbCap, cudaMemcpyDeviceToDevice, st);
+			cudaMemcpyAsync(n.a.gMinv, m->a.gMinv, sizeof(double)*nb, cudaMemcpyDeviceToDevice, st);
+			cudaMemcpyAsync(n.a.gE, m->a.gE, sizeof(double)*ns, cudaMemcpyDeviceToDevice, st);
+			cudaMemcpyAsync(n.a.gU, m->a.gU, sizeof(double)*ns, cudaMemcpyDeviceToDevice, st);
+			cudaStreamSynchronize(st);
+		}
+		cudaFree(m->block);
+	}
+	*m = n;
 	return 1;
 }
 
@@ -1098,8 +1169,10 @@ int cpGpuDebugRolloutTimes(cpGpuBatch *b, double *out)
 {
 	if(!b || !b->roll || !out) return 0;
 	Rollout *r = b->roll;
+	double tape = (double)r->adj.bytes;
+	for(int i = 0; i < r->segCap; i++) tape += (double)r->segs[i].bytes;
 	out[0] = r->replayMs; out[1] = r->adjointMs;
-	out[2] = r->tape.block ? (double)tape_carve(&b->dev->d, &r->tape, NULL, r->tapeK, (size_t)r->tape.t.rowCap, r->tapeIters, 0) : 0.0;
+	out[2] = tape;
 	out[3] = (double)r->ckptCap*(double)b->dev->slabBytes;
 	return 4;
 }
@@ -1112,26 +1185,63 @@ static int rollout_iterations(DevSet *ds)
 	return iters;
 }
 
-/* The tape for segments of K steps and at least rowCap rows: the one kept
- * from an earlier pass if it fits, else a new one. */
-static int rollout_tape(DevSet *ds, Rollout *r, int K, int iters, size_t rowCap)
-{
-	if(r->tape.block && r->tapeK == K && r->tapeIters == iters && (size_t)r->tape.t.rowCap >= rowCap) return 1;
-	if(r->tape.block) cudaFree(r->tape.block);
-	memset(&r->tape, 0, sizeof(r->tape));
-	r->tapeK = 0;
-	if(!tape_alloc(&ds->d, &r->tape, K, rowCap, iters)) return 0;
-	r->tapeK = K; r->tapeIters = iters;
-	return 1;
-}
-
-/* Tape rows for K steps: what a previous pass needed, else twice the
- * solved arbiters of the latest step plus the joints. */
+/* Rows to provide for K steps: the largest need seen, or twice the solved
+ * arbiters of the latest step plus the joints plus one per shape. */
 static size_t rollout_row_estimate(DevSet *ds, Rollout *r, int K)
 {
-	if(r->rowCap) return r->rowCap;
 	check_stats(ds);
-	return (size_t)K*(2*(size_t)(ds->hstats[5] > 0 ? ds->hstats[5] : 0) + (size_t)ds->d.totalCons + 1024);
+	size_t est = (size_t)K*(2*(size_t)(ds->hstats[5] > 0 ? ds->hstats[5] : 0) + (size_t)ds->d.totalCons +
+		(size_t)ds->d.totalShapes + 1024);
+	return r->rowEst > est ? r->rowEst : est;
+}
+
+/* Start recording segment `seg` of the forward into its light tape. */
+static void seg_begin(DevSet *ds, Rollout *r, int seg)
+{
+	cpgSet *d = &ds->d;
+	SegTape *sg = &r->segs[seg];
+	sg->recorded = 0;
+	int err0 = g_error;
+	if(!seg_alloc(d, sg, r->K, rollout_row_estimate(ds, r, r->K))){
+		/* no room: the reverse pass replays the segment from its checkpoint */
+		(void)cudaGetLastError();
+		g_error = err0;
+		return;
+	}
+	cudaMemsetAsync(sg->t.cursor, 0, sizeof(int)*4, lib_stream());
+	d->tape = sg->t;
+	d->tape.on = 1;
+}
+
+/* End of a segment's recording: it is kept unless it overflowed (then the
+ * reverse pass replays it, into a larger tape) or holds joints. */
+static void seg_finish(DevSet *ds, Rollout *r, int seg, int len)
+{
+	cpgSet *d = &ds->d;
+	if(!d->tape.on) return;
+	d->tape.on = 0;
+	SegTape *sg = &r->segs[seg];
+	cudaStream_t st = lib_stream();
+	int W = ds->nspaces;
+	int cur[4] = {0, 0, 0, 0};
+	int *off = HALLOC(int, (size_t)len*(W + 1));
+	int ok = cuda_ok(cudaMemcpyAsync(cur, sg->t.cursor, sizeof(cur), cudaMemcpyDeviceToHost, st), "tape cursor");
+	ok &= cuda_ok(cudaMemcpyAsync(off, sg->t.rowOff, sizeof(int)*(size_t)len*(W + 1), cudaMemcpyDeviceToHost, st), "tape offsets");
+	cudaStreamSynchronize(st);
+	size_t need = (size_t)cur[0] + (size_t)cur[0]/4 + 1024;
+	if(need > r->rowEst) r->rowEst = need;
+	if(ok && !cur[2] && !(cur[3] & 1)){
+		int mx = 0;
+		for(int t = 0; t < len; t++){
+			int rows = off[(size_t)t*(W + 1) + W] - off[(size_t)t*(W + 1)];
+			if(rows > mx) mx = rows;
+		}
+		sg->maxStepRows = mx;
+		sg->rowsUsed = cur[0];
+		sg->recorded = 1;
+	}
+	free(off);
+	memset(&d->tape, 0, sizeof(d->tape));
 }
 
 int cpGpuRolloutForward(cpGpuBatch *b, cpFloat dt, int steps, int checkpoint)
@@ -1139,13 +1249,11 @@ int cpGpuRolloutForward(cpGpuBatch *b, cpFloat dt, int steps, int checkpoint)
 	if(steps < 1 || checkpoint < 1 || !(dt > 0.0)){ set_error(CP_GPU_ERR_ARGUMENT, "rollout: steps, checkpoint and dt must be positive"); return -1; }
 	if(!batch_ready(b)) return -1;
 	DevSet *ds = b->dev;
-	cpgSet *d = &ds->d;
-	cudaStream_t st = lib_stream();
 	if(!b->roll) b->roll = (Rollout *)calloc(1, sizeof(Rollout));
 	Rollout *r = b->roll;
+	if(r->K != checkpoint) r->rowEst = 0;
 	r->steps = steps; r->K = checkpoint; r->dt = dt;
 	r->nckpt = (steps + checkpoint - 1)/checkpoint;
-	r->lastTaped = 0;
 	free(r->stamps); free(r->currDt);
 	r->stamps = HALLOC(unsigned, (size_t)r->nckpt*ds->nspaces);
 	r->currDt = HALLOC(double, (size_t)r->nckpt*ds->nspaces);
@@ -1159,49 +1267,75 @@ int cpGpuRolloutForward(cpGpuBatch *b, cpFloat dt, int steps, int checkpoint)
 		}
 		r->ckptCap = r->nckpt;
 	}
+	if(r->segCap < r->nckpt){
+		SegTape *ns = (SegTape *)calloc((size_t)r->nckpt, sizeof(SegTape));
+		if(r->segs) memcpy(ns, r->segs, sizeof(SegTape)*(size_t)r->segCap);
+		free(r->segs);
+		r->segs = ns;
+		r->segCap = r->nckpt;
+	}
+	for(int i = 0; i < r->segCap; i++) r->segs[i].recorded = 0;
 	double *dts = (double *)malloc(sizeof(double)*(size_t)b->n);
 	for(int i = 0; i < b->n; i++) dts[i] = dt;
-	/* the last segment is recorded as it runs, so the reverse pass starts
-	 * on it without a replay; without a tape (no memory, mixed iteration
-	 * counts) or past its capacity the reverse pass replays it */
-	int last = (r->nckpt - 1)*checkpoint, iters = rollout_iterations(ds), taping = 0;
-	int rc = 0;
+	int record = rollout_iterations(ds) > 0 && g_rollout_record;
+	int rc = 0, seg = -1;
 	for(int s = 0; s < steps && rc == 0; s++){
-		if(s % checkpoint == 0) rollout_save(b, s/checkpoint);
-		if(s == last && iters > 0){
-			size_t rowCap = rollout_row_estimate(ds, r, checkpoint);
-			int err0 = g_error;
-			if(rollout_tape(ds, r, checkpoint, iters, rowCap)){
-				cudaMemsetAsync(r->tape.t.cursor, 0, sizeof(int)*4, st);
-				d->tape = r->tape.t;
-				d->tape.on = 1;
-				taping = 1;
-			} else {
-				/* no room: the reverse pass replays the segment */
-				(void)cudaGetLastError();
-				g_error = err0;
-			}
+		if(s % checkpoint == 0){
+			if(seg >= 0) seg_finish(ds, r, seg, checkpoint);
+			seg = s/checkpoint;
+			rollout_save(b, seg);
+			if(record) seg_begin(ds, r, seg);
 		}
-		if(taping) d->tape.step = s - last;
+		if(ds->d.tape.on) ds->d.tape.step = s - seg*checkpoint;
 		rc = devset_step(ds, dts, NULL);
 	}
-	free(dts);
-	if(taping){
-		d->tape.on = 0;
-		int cur[4] = {0, 0, 0, 0};
-		if(rc == 0 && cuda_ok(cudaMemcpyAsync(cur, r->tape.t.cursor, sizeof(cur), cudaMemcpyDeviceToHost, st), "tape cursor")){
-			cudaStreamSynchronize(st);
-			if(cur[2]) r->rowCap = (size_t)cur[0] + (size_t)cur[0]/4 + 1024;
-			else if(!(cur[3] & 1)) r->lastTaped = 1;
-		}
-		memset(&d->tape, 0, sizeof(d->tape));
+	if(seg >= 0){
+		if(rc == 0) seg_finish(ds, r, seg, steps - seg*checkpoint);
+		else { ds->d.tape.on = 0; memset(&ds->d.tape, 0, sizeof(ds->d.tape)); }
 	}
+	free(dts);
 	return rc;
+}
+
+/* Replays segment `seg` from its checkpoint with full recording (the light
+ * tape and the per-iteration records), growing the tape on overflow. */
+static int seg_replay(DevSet *ds, Rollout *r, int seg, int len, const double *dts, int iters)
+{
+	cpgSet *d = &ds->d;
+	cudaStream_t st = lib_stream();
+	int W = ds->nspaces;
+	SegTape *sg = &r->segs[seg];
+	for(int attempt = 0; attempt < 4; attempt++){
+		size_t rowCap = rollout_row_estimate(ds, r, r->K);
+		if(!seg_alloc(d, sg, r->K, rowCap)) return 0;
+		if(!adj_ensure(d, &r->adj, r->K, (size_t)sg->t.rowCap, (size_t)sg->t.rowCap, iters, 1)) return 0;
+		rollout_restore_from(ds, r->ckpt + (size_t)seg*ds->slabBytes, r->stamps + (size_t)seg*W, r->currDt + (size_t)seg*W);
+		cudaMemsetAsync(sg->t.cursor, 0, sizeof(int)*4, st);
+		d->tape = sg->t;
+		d->tape.app = r->adj.app;
+		d->tape.on = 1;
+		int ok = 1;
+		for(int t = 0; t < len && ok; t++){
+			d->tape.step = t;
+			if(devset_step(ds, dts, NULL) != 0) ok = 0;
+		}
+		d->tape.on = 0;
+		if(!ok) return 0;
+		int cur[4];
+		cuda_ok(cudaMemcpyAsync(cur, sg->t.cursor, sizeof(cur), cudaMemcpyDeviceToHost, st), "tape cursor");
+		cudaStreamSynchronize(st);
+		if(cur[3] & 1){ set_error(CP_GPU_ERR_UNSUPPORTED, "rollout: constraints are not differentiated"); return 0; }
+		size_t need = (size_t)cur[0] + (size_t)cur[0]/4 + 1024;
+		if(!cur[2]) return 1;
+		if(need > r->rowEst) r->rowEst = need;
+	}
+	set_error(CP_GPU_ERR_OVERFLOW, "rollout: tape overflow");
+	return 0;
 }
 
 int cpGpuRolloutBackward(cpGpuBatch *b, const cpFloat *dLdp, cpFloat *dLdv0, cpFloat *dLdw0, cpFloat *dLdm, cpFloat *dLde, cpFloat *dLdu)
 {
-	if(!b || !b->dev || !b->roll){ set_error(CP_GPU_ERR_ARGUMENT, "rollout: no forward rollout to reverse"); return -1; }
+	if(!b || !b->dev || !b->roll || !b->roll->segs){ set_error(CP_GPU_ERR_ARGUMENT, "rollout: no forward rollout to reverse"); return -1; }
 	if(!dLdp){ set_error(CP_GPU_ERR_ARGUMENT, "rollout: dLdp is required"); return -1; }
 	DevSet *ds = b->dev;
 	cpgSet *d = &ds->d;
@@ -1213,7 +1347,7 @@ int cpGpuRolloutBackward(cpGpuBatch *b, const cpFloat *dLdp, cpFloat *dLdv0, cpF
 		set_error(CP_GPU_ERR_UNSUPPORTED, "rollout: all spaces of the batch need the same iteration count");
 		return -1;
 	}
-	/* the state after the forward, restored at the end */
+	/* the state after the forward, restored at the end (replays move it) */
 	if(!r->fin && !cuda_ok(cudaMalloc((void **)&r->fin, ds->slabBytes), "cudaMalloc final state")){ r->fin = NULL; return -1; }
 	char *fin = r->fin;
 	cuda_ok(cudaMemcpyAsync(fin, ds->slab, ds->slabBytes, cudaMemcpyDeviceToDevice, st), "save final state");
@@ -1221,18 +1355,28 @@ int cpGpuRolloutBackward(cpGpuBatch *b, const cpFloat *dLdp, cpFloat *dLdv0, cpF
 	double *finDt = HALLOC(double, W);
 	for(int w = 0; w < W; w++){ finStamp[w] = ds->spaces[w]->stamp; finDt[w] = ds->spaces[w]->curr_dt; }
 
-	/* the forward's recording of the last segment is used when the tape
-	 * is still the one it wrote */
-	int useLast = r->lastTaped && r->tape.block && r->tapeK == K && r->tapeIters == iters;
-	r->lastTaped = 0;
-	TapeMem m;
+	/* scratch for the largest segment and step */
+	size_t segRows = 0, stepRows = 0;
+	int missing = 0;
+	for(int i = 0; i < r->nckpt; i++){
+		SegTape *sg = &r->segs[i];
+		if(sg->recorded){
+			if((size_t)sg->rowsUsed > segRows) segRows = (size_t)sg->rowsUsed;
+			if((size_t)sg->maxStepRows > stepRows) stepRows = (size_t)sg->maxStepRows;
+		} else missing = 1;
+	}
+	if(missing){
+		size_t est = rollout_row_estimate(ds, r, K);
+		if(est > segRows) segRows = est;
+		stepRows = segRows;
+	}
 	int rc = -1;
 	double *h = NULL;
-	if(!useLast && !rollout_tape(ds, r, K, iters, rollout_row_estimate(ds, r, K))) goto done;
-	m = r->tape;
+	if(!adj_ensure(d, &r->adj, K, segRows, stepRows, iters, 0)) goto done;
 
 	/* seeds: dL/dp at the end, nothing else */
 	{
+		cpgAdj *A = &r->adj.a;
 		size_t nbd = 9*(size_t)d->totalBodies;
 		h = HALLOC(double, nbd);
 		int idx = 0;
@@ -1243,11 +1387,11 @@ int cpGpuRolloutBackward(cpGpuBatch *b, const cpFloat *dLdp, cpFloat *dLdv0, cpF
 				h[9*g] = dLdp[2*idx]; h[9*g + 1] = dLdp[2*idx + 1];
 			}
 		}
-		cuda_ok(cudaMemcpyAsync(m.a.body, h, sizeof(double)*nbd, cudaMemcpyHostToDevice, st), "seed");
-		cudaMemsetAsync(m.a.arb, 0, sizeof(double)*4*(size_t)d->arbCap, st);
-		cudaMemsetAsync(m.a.gMinv, 0, sizeof(double)*(size_t)d->totalBodies, st);
-		cudaMemsetAsync(m.a.gE, 0, sizeof(double)*(size_t)d->totalShapes, st);
-		cudaMemsetAsync(m.a.gU, 0, sizeof(double)*(size_t)d->totalShapes, st);
+		cuda_ok(cudaMemcpyAsync(A->body, h, sizeof(double)*nbd, cudaMemcpyHostToDevice, st), "seed");
+		cudaMemsetAsync(A->arb, 0, sizeof(double)*4*(size_t)d->arbCap, st);
+		cudaMemsetAsync(A->gMinv, 0, sizeof(double)*(size_t)d->totalBodies, st);
+		cudaMemsetAsync(A->gE, 0, sizeof(double)*(size_t)d->totalShapes, st);
+		cudaMemsetAsync(A->gU, 0, sizeof(double)*(size_t)d->totalShapes, st);
 	}
 	{
 		double *dts = (double *)malloc(sizeof(double)*(size_t)W);
@@ -1256,59 +1400,47 @@ int cpGpuRolloutBackward(cpGpuBatch *b, const cpFloat *dLdp, cpFloat *dLdv0, cpF
 		cudaEvent_t ev[3];
 		if(g_timing) for(int i = 0; i < 3; i++) cudaEventCreate(&ev[i]);
 		r->replayMs = 0.0f; r->adjointMs = 0.0f;
+		int *off = HALLOC(int, (size_t)K*(W + 1));
 		for(int seg = r->nckpt - 1; seg >= 0 && ok; seg--){
 			int first = seg*K, len = (r->steps - first < K) ? r->steps - first : K;
+			SegTape *sg = &r->segs[seg];
 			if(g_timing) cudaEventRecord(ev[0], st);
-			for(int attempt = (useLast && seg == r->nckpt - 1) ? 4 : 0; attempt < 4; attempt++){
-				rollout_restore_from(ds, r->ckpt + (size_t)seg*ds->slabBytes, r->stamps + (size_t)seg*W, r->currDt + (size_t)seg*W);
-				cudaMemsetAsync(m.t.cursor, 0, sizeof(int)*4, st);
-				d->tape = m.t;
-				d->tape.on = 1;
-				for(int t = 0; t < len && ok; t++){
-					d->tape.step = t;
-					if(devset_step(ds, dts, NULL) != 0) ok = 0;
-				}
+			int replayed = 0;
+			if(!sg->recorded){
+				if(!seg_replay(ds, r, seg, len, dts, iters)){ ok = 0; break; }
+				replayed = 1;
+			} else {
+				/* the solver iterations of the segment's steps, from the
+				 * forward's recording, in one launch */
+				d->tape = sg->t;
+				d->tape.app = r->adj.app;
 				d->tape.on = 0;
-				int cur[4];
-				cuda_ok(cudaMemcpyAsync(cur, m.t.cursor, sizeof(cur), cudaMemcpyDeviceToHost, st), "tape cursor");
-				cudaStreamSynchronize(st);
-				if(!ok) break;
-				if(cur[3] & 1){ set_error(CP_GPU_ERR_UNSUPPORTED, "rollout: constraints are not differentiated"); ok = 0; break; }
-				if(!cur[2]) break;
-				/* the tape overflowed: grow it (the gradients so far are kept) and replay */
-				size_t need = (size_t)cur[0] + (size_t)cur[0]/4 + 1024;
-				TapeMem m2;
-				if(!tape_alloc(d, &m2, K, need, iters)){ ok = 0; break; }
-				cudaMemcpyAsync(m2.a.body, m.a.body, sizeof(double)*9*(size_t)d->totalBodies, cudaMemcpyDeviceToDevice, st);
-				cudaMemcpyAsync(m2.a.arb, m.a.arb, sizeof(double)*4*(size_t)d->arbCap, cudaMemcpyDeviceToDevice, st);
-				cudaMemcpyAsync(m2.a.gMinv, m.a.gMinv, sizeof(double)*(size_t)d->totalBodies, cudaMemcpyDeviceToDevice, st);
-				cudaMemcpyAsync(m2.a.gE, m.a.gE, sizeof(double)*(size_t)d->totalShapes, cudaMemcpyDeviceToDevice, st);
-				cudaMemcpyAsync(m2.a.gU, m.a.gU, sizeof(double)*(size_t)d->totalShapes, cudaMemcpyDeviceToDevice, st);
-				cudaStreamSynchronize(st);
-				cudaFree(m.block);
-				m = m2;
-				r->tape = m;
-				r->rowCap = need;
-				if(attempt == 3){ set_error(CP_GPU_ERR_OVERFLOW, "rollout: tape overflow"); ok = 0; }
+				if(cpg_launch_replay_solve(d, &r->adj.a, len, st) != 0){ set_error(CP_GPU_ERR_CUDA, "replay solve launch failed"); ok = 0; break; }
 			}
-			if(!ok) break;
 			if(g_timing) cudaEventRecord(ev[1], st);
-			d->tape = m.t;
+			d->tape = sg->t;
+			d->tape.app = r->adj.app;
 			d->tape.on = 0;
-			/* the carried impulse adjoints, in the next checkpoint's slot
-			 * numbering, move to this replay's */
-			if(seg + 1 < r->nckpt){
+			/* a replay claims table slots of its own for the arbiters it
+			 * creates: the carried impulse adjoints, in the next
+			 * checkpoint's (the forward's) numbering, move to the replay's */
+			if(replayed && seg + 1 < r->nckpt){
 				const char *next = r->ckpt + (size_t)(seg + 1)*ds->slabBytes + ((const char *)d->keys - (const char *)ds->slab);
-				if(cpg_launch_adjoint_remap(d, &m.a, next, st) != 0){ set_error(CP_GPU_ERR_CUDA, "adjoint launch failed"); ok = 0; break; }
+				if(cpg_launch_adjoint_remap(d, &r->adj.a, next, st) != 0){ set_error(CP_GPU_ERR_CUDA, "adjoint launch failed"); ok = 0; break; }
 			}
-			int *off = HALLOC(int, (size_t)len*(W + 1));
-			cuda_ok(cudaMemcpyAsync(off, m.t.rowOff, sizeof(int)*(size_t)len*(W + 1), cudaMemcpyDeviceToHost, st), "tape offsets");
+			cuda_ok(cudaMemcpyAsync(off, sg->t.rowOff, sizeof(int)*(size_t)len*(W + 1), cudaMemcpyDeviceToHost, st), "tape offsets");
 			cudaStreamSynchronize(st);
 			for(int t = len - 1; t >= 0 && ok; t--){
 				int rows = off[(size_t)t*(W + 1) + W] - off[(size_t)t*(W + 1)];
-				if(cpg_launch_adjoint(d, &m.a, t, rows, st) != 0){ set_error(CP_GPU_ERR_CUDA, "adjoint launch failed"); ok = 0; }
+				if((size_t)rows > r->adj.stepRows){ set_error(CP_GPU_ERR_OVERFLOW, "rollout: step scratch too small"); ok = 0; break; }
+				if(cpg_launch_adjoint(d, &r->adj.a, t, rows, st) != 0){ set_error(CP_GPU_ERR_CUDA, "adjoint launch failed"); ok = 0; }
 			}
-			free(off);
+			if(ok){
+				int cur[4] = {0, 0, 0, 0};
+				cuda_ok(cudaMemcpyAsync(cur, sg->t.cursor, sizeof(cur), cudaMemcpyDeviceToHost, st), "tape cursor");
+				cudaStreamSynchronize(st);
+				if(cur[3] & 2){ set_error(CP_GPU_ERR_CUDA, "rollout: contact geometry of a recorded step did not match its rows"); ok = 0; }
+			}
 			if(g_timing){
 				float a0 = 0.0f, a1 = 0.0f;
 				cudaEventRecord(ev[2], st);
@@ -1317,25 +1449,23 @@ int cpGpuRolloutBackward(cpGpuBatch *b, const cpFloat *dLdp, cpFloat *dLdv0, cpF
 				cudaEventElapsedTime(&a1, ev[1], ev[2]);
 				r->replayMs += a0; r->adjointMs += a1;
 			}
+			/* a replayed tape is not the forward's any more */
+			if(replayed) sg->recorded = 0;
 		}
+		free(off);
 		free(dts);
 		if(g_timing) for(int i = 0; i < 3; i++) cudaEventDestroy(ev[i]);
-		int cur[4] = {0, 0, 0, 0};
-		if(ok){
-			cuda_ok(cudaMemcpyAsync(cur, m.t.cursor, sizeof(cur), cudaMemcpyDeviceToHost, st), "tape cursor");
-			cudaStreamSynchronize(st);
-			if(cur[3] & 2){ set_error(CP_GPU_ERR_CUDA, "rollout: contact geometry of a replayed step did not match its rows"); ok = 0; }
-		}
 		if(ok){
 			/* gather: dL/dv0, dL/dw0 from the body adjoints, dL/dm = -dL/d(1/m) / m^2 */
+			cpgAdj *A = &r->adj.a;
 			size_t nbd = 9*(size_t)d->totalBodies;
 			double *gm = HALLOC(double, d->totalBodies), *minv = HALLOC(double, d->totalBodies);
 			double *ge = HALLOC(double, d->totalShapes), *gu = HALLOC(double, d->totalShapes);
-			ok &= cuda_ok(cudaMemcpyAsync(h, m.a.body, sizeof(double)*nbd, cudaMemcpyDeviceToHost, st), "gradients");
-			ok &= cuda_ok(cudaMemcpyAsync(gm, m.a.gMinv, sizeof(double)*(size_t)d->totalBodies, cudaMemcpyDeviceToHost, st), "gradients");
+			ok &= cuda_ok(cudaMemcpyAsync(h, A->body, sizeof(double)*nbd, cudaMemcpyDeviceToHost, st), "gradients");
+			ok &= cuda_ok(cudaMemcpyAsync(gm, A->gMinv, sizeof(double)*(size_t)d->totalBodies, cudaMemcpyDeviceToHost, st), "gradients");
 			ok &= cuda_ok(cudaMemcpyAsync(minv, d->minv, sizeof(double)*(size_t)d->totalBodies, cudaMemcpyDeviceToHost, st), "gradients");
-			ok &= cuda_ok(cudaMemcpyAsync(ge, m.a.gE, sizeof(double)*(size_t)d->totalShapes, cudaMemcpyDeviceToHost, st), "gradients");
-			ok &= cuda_ok(cudaMemcpyAsync(gu, m.a.gU, sizeof(double)*(size_t)d->totalShapes, cudaMemcpyDeviceToHost, st), "gradients");
+			ok &= cuda_ok(cudaMemcpyAsync(ge, A->gE, sizeof(double)*(size_t)d->totalShapes, cudaMemcpyDeviceToHost, st), "gradients");
+			ok &= cuda_ok(cudaMemcpyAsync(gu, A->gU, sizeof(double)*(size_t)d->totalShapes, cudaMemcpyDeviceToHost, st), "gradients");
 			cudaStreamSynchronize(st);
 			int idx = 0, sidx = 0;
 			for(int w = 0; w < W && ok; w++){

@@ -199,12 +199,17 @@ typedef struct cpgOp {
 #define CPG_ADJ_SOLVE_THREADS 64
 #define CPG_ADJ_STAGED_BODIES 1024
 
+/* What a rollout records of one segment of K steps.  The forward fills
+ * everything but `app` (the light tape); the solver's per-iteration records
+ * are recomputed from it by the reverse pass, or recorded together with the
+ * rest when a segment is replayed from its checkpoint. */
 typedef struct cpgTape {
 	int on;                   /* record this step */
-	int step;                 /* its index within the replayed segment */
+	int step;                 /* its index within the segment */
 	int K;                    /* steps per segment */
 	int rowCap, levCap;
 	double *body;             /* [K][8][totalBodies] planes: p.x p.y a (after position integration), v.x v.y w (pre-step), cos, sin */
+	double *vel;              /* [K][3][totalBodies] planes: v.x v.y w after velocity integration (the solve's input) */
 	double *shape;            /* [K][6][totalShapes] planes: world p0.x p0.y p1.x p1.y n.x n.y */
 	double *verts;            /* [K][4][totalVerts] planes: world vertex x y, world normal x y */
 	cpgParams *params;        /* [K][nworlds] */
@@ -214,7 +219,7 @@ typedef struct cpgTape {
 	int *rowOff;              /* [K][nworlds + 1] */
 	int *levels;              /* [levCap] level starts (relative to the world's rows) */
 	int *levOff;              /* [K][nworlds + 1] */
-	double *app;              /* [rowCap][iterations][2] impulse application records (AdjApp) */
+	double *app;              /* [rowCap][iterations][2] impulse application records (AdjApp); NULL: not recorded */
 	int *cursor;              /* [4]: rows used, levels used, overflow flag, unsupported-row flag */
 } cpgTape;
 
@@ -310,6 +315,7 @@ typedef struct cpgSet {
 	int hostTreeStage;            /* worlds of at most this many nodes run the tree from shared memory; -1: all that fit */
 	int hostSolveThreads;         /* block size of the per-world solve; 0: default */
 	int hostSolveStage;           /* worlds of at most this many bodies solve from shared memory; -1: all that fit */
+	int solveLayout;              /* per-level lane layout: 0 automatic, 1 fewest instructions, 2 shortest chain, 3 four lanes only */
 
 	/* stats block copied to the host after each step */
 	int *stats;
@@ -324,9 +330,11 @@ typedef struct cpgAdj {
 	double *arb;                  /* [arbCap][2][2]: adjoints of the stored jnAcc, jtAcc of each arbiter contact */
 	double *gMinv;                /* [totalBodies] dL/d(1/m) */
 	double *gE, *gU;              /* [totalShapes] dL/de, dL/du */
-	double *con;                  /* [rowCap][2][4][16] per contact and lane scratch */
-	double *unit;                 /* [rowCap][20] per-unit contributions of the pre-step and geometry adjoints */
+	double *con;                  /* [rows of one step][2][4][CPG_ADJ_LANE_DOUBLES] per contact and lane scratch */
+	double *unit;                 /* [rows of one step][20] per-unit contributions of the pre-step and geometry adjoints */
 	double *arbTmp;               /* [arbCap][2][2] remapping buffer */
+	cpgRow *srows;                /* [rows of one segment] rows the recomputed solves run on */
+	double *sbodies;              /* [K][totalBodies][8] packed bodies of the recomputed solves (worlds too large for shared memory) */
 } cpgAdj;
 
 /* ---- launchers (cpg_kernels.cu) ---- */
@@ -337,6 +345,8 @@ long long cpg_launch_count(int reset);
 int cpg_launch_tape(const cpgSet *s, void *stream);
 int cpg_launch_adjoint(const cpgSet *s, const cpgAdj *a, int step, int rows, void *stream);
 int cpg_launch_adjoint_remap(const cpgSet *s, const cpgAdj *a, const void *oldKeys, void *stream);
+int cpg_launch_tape_vel(const cpgSet *s, void *stream);
+int cpg_launch_replay_solve(const cpgSet *s, const cpgAdj *a, int nsteps, void *stream);
 
 #ifdef __cplusplus
 }

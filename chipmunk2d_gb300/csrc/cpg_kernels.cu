@@ -1054,14 +1054,144 @@ __device__ __forceinline__ void quad_apply(const QuadRow &q, cpgRow *row, double
 	if(dyn){ bp[0] = vx; bp[1] = vy; bp[2] = w; }
 }
 
+/* ---- two lanes per contact unit ----
+ * Lane p of a pair takes part p (0: velocity with the normal and friction
+ * impulses, 1: bias velocity with the bias impulse) for both bodies: it
+ * computes both contact-point velocities and applies the impulse to both
+ * bodies, with the reference's operations in the reference's order, as
+ * quad_apply does for one body.  About 53 FP64 instructions per contact
+ * lane against 40 on four lanes, but twice the units per warp, so levels
+ * of 9 to 16 units (and colours wider than the grid's quads) cost fewer
+ * instructions.  Results are bit-identical to the other two layouts. */
+struct PairRow {
+	int a, b, flags, kind, count;
+	double nx, ny, u, svx, svy;
+	double r1x[2], r1y[2], r2x[2], r2y[2], nMass[2], tMass[2], c[2], acc[2], jt[2];
+};
+
+__device__ __forceinline__ void pair_load(PairRow &q, const cpgRow &row, bool bias)
+{
+	q.kind = row.kind; q.flags = row.flags; q.count = row.count;
+	q.a = row.a; q.b = row.b;
+	if(q.kind != 0) return;
+	q.nx = row.arb.nx; q.ny = row.arb.ny; q.u = row.arb.u; q.svx = row.arb.svx; q.svy = row.arb.svy;
+#pragma unroll
+	for(int k = 0; k < 2; k++){
+		if(k >= q.count) break;
+		const cpgRowContact &c = row.arb.c[k];
+		q.r1x[k] = c.r1x; q.r1y[k] = c.r1y; q.r2x[k] = c.r2x; q.r2y[k] = c.r2y;
+		q.nMass[k] = c.nMass; q.tMass[k] = c.tMass;
+		q.c[k] = bias ? c.bias : c.bounce;
+		q.acc[k] = bias ? c.jBias : c.jnAcc;
+		q.jt[k] = c.jtAcc;
+	}
+}
+
+template<bool CG, bool FUSED>
+__device__ __forceinline__ void pair_apply(const PairRow &q, cpgRow *row, double *bodies, int pass, double dt_coef, bool bias)
+{
+	if(pass == 0 && ((q.flags & ROW_FIRST) || bias)) return;
+	double *ba = bodies + 8*(size_t)q.a, *bb = bodies + 8*(size_t)q.b;
+	double *pa = ba + (bias ? 3 : 0), *pb = bb + (bias ? 3 : 0);
+	double avx, avy, aw, am, ai, bvx, bvy, bw, bm, bi;
+	if(CG){
+		avx = __ldcg(pa); avy = __ldcg(pa + 1); aw = __ldcg(pa + 2); am = __ldcg(ba + 6); ai = __ldcg(ba + 7);
+		bvx = __ldcg(pb); bvy = __ldcg(pb + 1); bw = __ldcg(pb + 2); bm = __ldcg(bb + 6); bi = __ldcg(bb + 7);
+	} else {
+		avx = pa[0]; avy = pa[1]; aw = pa[2]; am = ba[6]; ai = ba[7];
+		bvx = pb[0]; bvy = pb[1]; bw = pb[2]; bm = bb[6]; bi = bb[7];
+	}
+	double nx = q.nx, ny = q.ny;
+	if(pass == 0){
+#pragma unroll
+		for(int k = 0; k < 2; k++){
+			if(k >= q.count) break;
+			double jx = nx*q.acc[k] - ny*q.jt[k], jy = nx*q.jt[k] + ny*q.acc[k];
+			jx = jx*dt_coef; jy = jy*dt_coef;
+			avx = avx + (-jx)*am; avy = avy + (-jy)*am;
+			aw += ai*(q.r1x[k]*(-jy) - q.r1y[k]*(-jx));
+			bvx = bvx + jx*bm; bvy = bvy + jy*bm;
+			bw += bi*(q.r2x[k]*jy - q.r2y[k]*jx);
+		}
+	} else {
+#pragma unroll
+		for(int k = 0; k < 2; k++){
+			if(k >= q.count) break;
+			double r1x = q.r1x[k], r1y = q.r1y[k], r2x = q.r2x[k], r2y = q.r2y[k];
+			double v1x, v1y, v2x, v2y, vn, vt, nxj, nyj;
+			if(FUSED){
+				v1x = __fma_rn(-r1y, aw, avx); v1y = __fma_rn(r1x, aw, avy);
+				v2x = __fma_rn(-r2y, bw, bvx); v2y = __fma_rn(r2x, bw, bvy);
+			} else {
+				v1x = avx + (-r1y)*aw; v1y = avy + r1x*aw;
+				v2x = bvx + (-r2y)*bw; v2y = bvy + r2x*bw;
+			}
+			double dx = v2x - v1x, dy = v2y - v1y;
+			double sx = dx + q.svx, sy = dy + q.svy;
+			double vrx = bias ? dx : sx, vry = bias ? dy : sy;
+			if(FUSED){ vn = __fma_rn(vrx, nx, vry*ny); vt = __fma_rn(vry, nx, -(vrx*ny)); }
+			else { vn = vrx*nx + vry*ny; vt = vrx*(-ny) + vry*nx; }
+			double y = q.c[k] + dneg_if(vn, bias);
+			double j = dneg_if(y, !bias)*q.nMass[k];
+			double old = q.acc[k];
+			double acc = dmax(old + j, 0.0);
+			double jtMax = q.u*acc;
+			double jt = -vt*q.tMass[k];
+			double jtOld = q.jt[k];
+			double jtAcc = dclamp(jtOld + jt, -jtMax, jtMax);
+			double d = acc - old, djt = jtAcc - jtOld;
+			double ax = nx*d, ay = ny*d;
+			if(FUSED){ nxj = __fma_rn(-ny, djt, ax); nyj = __fma_rn(nx, djt, ay); }
+			else { nxj = ax - ny*djt; nyj = nx*djt + ay; }
+			double jx = bias ? ax : nxj, jy = bias ? ay : nyj;
+			if(FUSED){
+				avx = __fma_rn(-jx, am, avx); avy = __fma_rn(-jy, am, avy);
+				aw = __fma_rn(ai, __fma_rn(r1x, -jy, -(r1y*(-jx))), aw);
+				bvx = __fma_rn(jx, bm, bvx); bvy = __fma_rn(jy, bm, bvy);
+				bw = __fma_rn(bi, __fma_rn(r2x, jy, -(r2y*jx)), bw);
+			} else {
+				avx = avx + (-jx)*am; avy = avy + (-jy)*am;
+				aw += ai*(r1x*(-jy) - r1y*(-jx));
+				bvx = bvx + jx*bm; bvy = bvy + jy*bm;
+				bw += bi*(r2x*jy - r2y*jx);
+			}
+			if(!bias){ row->arb.c[k].jnAcc = acc; row->arb.c[k].jtAcc = jtAcc; }
+			else row->arb.c[k].jBias = acc;
+		}
+	}
+	if(q.flags & ROW_DYN_A){ pa[0] = avx; pa[1] = avy; pa[2] = aw; }
+	if(q.flags & ROW_DYN_B){ pb[0] = bvx; pb[1] = bvy; pb[2] = bw; }
+}
+
+/* Layout of a level of U units for a block of `nt` threads: the cheapest
+ * in FP64 warp instructions per contact of four lanes (40 per round of
+ * nt/4 units), two lanes (53 per round of nt/2) and one lane (93 per
+ * round of nt).  0: four, 1: two, 2: one. */
+__device__ __forceinline__ int level_layout(int U, int nt, bool many)
+{
+	int w4 = (4*U + 31) >> 5, w2 = (2*U + 31) >> 5, w1 = (U + 31) >> 5;
+	int r4 = (4*U + nt - 1)/nt, r2 = (2*U + nt - 1)/nt, r1 = (U + nt - 1)/nt;
+	long c4, c2, c1;
+	if(many){
+		/* many worlds share each sub-partition's FP64 pipe: fewest warp
+		 * instructions (ties: fewest rounds) */
+		c4 = (long)w4*40*1024 + r4; c2 = (long)w2*53*1024 + r2; c1 = (long)w1*93*1024 + r1;
+	} else {
+		/* few worlds: the level's dependent chain, rounds x per-lane count */
+		c4 = (long)r4*40*1024 + w4; c2 = (long)r2*53*1024 + w2; c1 = (long)r1*93*1024 + w1;
+	}
+	return (c4 <= c2 && c4 <= c1) ? 0 : (c2 <= c1 ? 1 : 2);
+}
+
 extern __shared__ double sbody[];
 
 /* Warm start (pass 0) and `iterations` sweeps, level by level; one block
  * per world.  Worlds of at most `stagedMax` bodies keep their packed body
  * state in shared memory for the whole solve. */
-__global__ void k_solve(cpgSet s, int stagedMax)
+__global__ void __launch_bounds__(256, 2) k_solve(cpgSet s, int stagedMax)
 {
-	int w = blockIdx.x;
+	/* largest worlds first: their long level chains start at once */
+	int w = s.worldOrder[blockIdx.x];
 	const cpgParams &P = s.params[w];
 	if(!P.active) return;
 	const cpgWorld &W = s.world[w];
@@ -1081,30 +1211,100 @@ __global__ void k_solve(cpgSet s, int stagedMax)
 	unsigned qmask = 0xFu << (threadIdx.x & 28);
 	/* rollout recording: the rows of this world in the tape */
 	AdjApp *tapeApp = nullptr;
-	if(s.tape.on){
+	if(s.tape.on && s.tape.app){
 		const int *off = s.tape.rowOff + (size_t)s.tape.step*(s.nworlds + 1);
 		/* past the tape's capacity nothing is recorded: the host grows the
 		 * tape and replays the segment */
 		if(off[w + 1] <= s.tape.rowCap) tapeApp = (AdjApp *)s.tape.app + (size_t)off[w]*P.iterations*2;
 	}
+	int nt = blockDim.x;
+	bool many = s.solveLayout == 1 || (s.solveLayout == 0 && s.nworlds >= 152);
+	bool recording = (s.tape.on && s.tape.app) || s.solveLayout == 3;
 	for(int pass = 0; pass <= P.iterations; pass++){
 		for(int l = 0; l < nlev; l++){
-			int e = start[l + 1];
-			for(int k = start[l] + (threadIdx.x >> 2); k < e; k += nq){
-				QuadRow q;
-				quad_load(q, rows[k], lane4);
-				AdjApp *rec = (tapeApp && pass > 0) ? tapeApp + ((size_t)k*P.iterations + (pass - 1))*2 : nullptr;
-				if(q.kind == 0) quad_apply<false, false>(q, rows + k, bodies, pass, P.dt_coef, qmask, lane4, rec);
-				else if(lane4 == 0){
-					if(tapeApp) atomicOr(&s.tape.cursor[3], 1);   /* joints are not differentiated */
-					solve_row<false>(rows, k, bodies, pass, P.dt_coef, P.dt);
+			int b0 = start[l], e = start[l + 1];
+			/* the recording pass writes its records from four lanes */
+			int lay = recording ? 0 : level_layout(e - b0, nt, many);
+			if(lay == 0){
+				for(int k = b0 + (threadIdx.x >> 2); k < e; k += nq){
+					QuadRow q;
+					quad_load(q, rows[k], lane4);
+					AdjApp *rec = (tapeApp && pass > 0) ? tapeApp + ((size_t)k*P.iterations + (pass - 1))*2 : nullptr;
+					if(q.kind == 0) quad_apply<false, false>(q, rows + k, bodies, pass, P.dt_coef, qmask, lane4, rec);
+					else if(lane4 == 0){
+						if(tapeApp) atomicOr(&s.tape.cursor[3], 1);   /* joints are not differentiated */
+						solve_row<false>(rows, k, bodies, pass, P.dt_coef, P.dt);
+					}
 				}
+			} else if(lay == 1){
+				bool bias = (threadIdx.x & 1) != 0;
+				for(int k = b0 + (threadIdx.x >> 1); k < e; k += nt >> 1){
+					PairRow q;
+					pair_load(q, rows[k], bias);
+					if(q.kind == 0) pair_apply<false, false>(q, rows + k, bodies, pass, P.dt_coef, bias);
+					else if(!bias) solve_row<false>(rows, k, bodies, pass, P.dt_coef, P.dt);
+				}
+			} else {
+				for(int k = b0 + threadIdx.x; k < e; k += nt) solve_row<false>(rows, k, bodies, pass, P.dt_coef, P.dt);
 			}
 			__syncthreads();
 		}
 	}
 	if(staged){
 		for(int i = threadIdx.x; i < 8*W.nbodies; i += blockDim.x) gb[i] = sbody[i];
+	}
+}
+
+/* The solver iterations of recorded steps, recomputed for the rollout's
+ * reverse pass (one block per world and step of a segment: the steps are
+ * independent given what the forward recorded).  Each block starts from
+ * the step's recorded solver input, the velocities after integration and
+ * the pre-step rows, runs the same four-lane sweep as k_solve (bit for bit
+ * the forward's solve) and writes the per-iteration application records.
+ * The rows it updates are a copy; bodies are staged like k_solve's. */
+__global__ void __launch_bounds__(256, 2) k_replay_solve(cpgSet s, cpgAdj a, int stagedMax)
+{
+	int w = s.worldOrder[blockIdx.x], t = blockIdx.y;
+	const cpgTape &tp = s.tape;
+	int nw = s.nworlds;
+	const cpgParams P = tp.params[(size_t)t*nw + w];
+	if(!P.active) return;
+	const cpgWorld &W = s.world[w];
+	int ro = tp.rowOff[(size_t)t*(nw + 1) + w];
+	int n = tp.rowOff[(size_t)t*(nw + 1) + w + 1] - ro;
+	int lo = tp.levOff[(size_t)t*(nw + 1) + w];
+	int nlev = tp.levOff[(size_t)t*(nw + 1) + w + 1] - lo - 1;
+	if(ro + n > tp.rowCap || nlev < 0) return;
+	const int *start = tp.levels + lo;
+	cpgRow *rows = a.srows + ro;
+	int nbw = W.nbodies, bo = W.bodyOff, nb = s.totalBodies;
+	bool staged = nbw <= stagedMax;
+	double *bodies = staged ? sbody : a.sbodies + 8*((size_t)t*nb + bo);
+	const double *vel = tp.vel + (size_t)t*3*nb;
+	for(int k = threadIdx.x; k < n; k += blockDim.x) rows[k] = tp.rows[ro + k];
+	for(int i = threadIdx.x; i < nbw; i += blockDim.x){
+		int g = bo + i;
+		double *b = bodies + 8*(size_t)i;
+		b[0] = vel[g]; b[1] = vel[nb + g]; b[2] = vel[2*(size_t)nb + g];
+		b[3] = 0.0; b[4] = 0.0; b[5] = 0.0;
+		b[6] = s.minv[g]; b[7] = s.iinv[g];
+	}
+	__syncthreads();
+	AdjApp *tapeApp = (AdjApp *)tp.app + (size_t)ro*P.iterations*2;
+	int lane4 = threadIdx.x & 3, nq = blockDim.x >> 2;
+	unsigned qmask = 0xFu << (threadIdx.x & 28);
+	for(int pass = 0; pass <= P.iterations; pass++){
+		for(int l = 0; l < nlev; l++){
+			int e = start[l + 1];
+			for(int k = start[l] + (threadIdx.x >> 2); k < e; k += nq){
+				QuadRow q;
+				quad_load(q, rows[k], lane4);
+				AdjApp *rec = pass > 0 ? tapeApp + ((size_t)k*P.iterations + (pass - 1))*2 : nullptr;
+				if(q.kind == 0) quad_apply<false, false>(q, rows + k, bodies, pass, P.dt_coef, qmask, lane4, rec);
+				else if(lane4 == 0) solve_row<false>(rows, k, bodies, pass, P.dt_coef, P.dt);
+			}
+			__syncthreads();
+		}
 	}
 }
 
@@ -1749,6 +1949,21 @@ static cudaError_t launch_coop(const void *kernel, int threads, cpgSet *s, int w
 #define CPG_STAGED_NODES 3072
 
 /* `h` is the host copy of the set's sizes (same struct, host values). */
+extern "C" int cpg_launch_replay_solve(const cpgSet *s, const cpgAdj *a, int nsteps, void *stream)
+{
+	cudaStream_t st = (cudaStream_t)stream;
+	int stagedMax = s->hostMaxBodies <= CPG_STAGED_BODIES ? s->hostMaxBodies : 0;
+	size_t smem = (size_t)stagedMax*8*sizeof(double);
+	static size_t smemSet = 0;
+	if(smem > 48*1024 && smem > smemSet){
+		cudaFuncSetAttribute(k_replay_solve, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+		smemSet = smem;
+	}
+	int threads = s->nworlds*nsteps >= 152 ? 128 : 256;
+	LAUNCH(k_replay_solve<<<dim3(s->nworlds, nsteps), threads, smem, st>>>(*s, *a, stagedMax));
+	return check_launch("k_replay_solve") == cudaSuccess ? 0 : -1;
+}
+
 extern "C" int cpg_launch_step(const cpgSet *s, const cpgSet *h, int mode, void *stream, float *phase_ms)
 {
 	cudaStream_t st = (cudaStream_t)stream;
@@ -1784,7 +1999,7 @@ extern "C" int cpg_launch_step(const cpgSet *s, const cpgSet *h, int mode, void 
 		 * from residency (a pool sized for the largest world would hold
 		 * every block's shared memory) than from shared-memory latency */
 		if(h->hostTreeStage >= 0){ if(h->hostTreeStage < staged) staged = h->hostTreeStage; }
-		else if(W > 2*152) staged = 0;
+		else if(W > 2*152 && staged > 384) staged = 0;
 		size_t smem = (size_t)staged*sizeof(cpgNode);
 		static size_t treeSmemSet = 0;
 		if(smem > 48*1024 && smem > treeSmemSet){
@@ -1813,6 +2028,7 @@ extern "C" int cpg_launch_step(const cpgSet *s, const cpgSet *h, int mode, void 
 	LAUNCH(k_build_rows<<<dim3(perWorldX, W), 128, 0, st>>>(*s));
 	if(h->tape.on) cpg_launch_tape(s, st);
 	LAUNCH(k_integrate_vel<<<blocks_for(h->totalBodies, 128), 128, 0, st>>>(*s));
+	if(h->tape.on) cpg_launch_tape_vel(s, st);
 	if(timing) cudaEventRecord(ev[6], st);
 	if(W == 1 && colored){
 		launch_coop((const void *)k_solve_coop<true>, CPG_COOP_SOLVE_THREADS, &sv, 0, st);
@@ -1829,7 +2045,7 @@ extern "C" int cpg_launch_step(const cpgSet *s, const cpgSet *h, int mode, void 
 		}
 		/* many worlds: small blocks keep more worlds resident (registers
 		 * limit a 256-thread block to two per SM); one world: wide levels */
-		int threads = h->hostSolveThreads > 0 ? h->hostSolveThreads : (W >= 152 ? 64 : 256);
+		int threads = h->hostSolveThreads > 0 ? h->hostSolveThreads : (W >= 152 ? 128 : 256);
 		LAUNCH(k_solve<<<W, threads, smem, st>>>(*s, stagedMax));
 	}
 	LAUNCH(k_writeback<<<dim3(perWorldX, W), 128, 0, st>>>(*s));

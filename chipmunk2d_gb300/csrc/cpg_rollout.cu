@@ -102,6 +102,16 @@ __global__ void k_tape_bodies(cpgSet s)
 	b[6*(size_t)nb + g] = s.ta[g]; b[7*(size_t)nb + g] = s.tb[g];
 }
 
+/* The solve's input: velocities after velocity integration. */
+__global__ void k_tape_vel(cpgSet s)
+{
+	int g = blockIdx.x*blockDim.x + threadIdx.x;
+	int nb = s.totalBodies;
+	if(g >= nb) return;
+	double *v = s.tape.vel + (size_t)s.tape.step*3*nb;
+	v[g] = s.vx[g]; v[nb + g] = s.vy[g]; v[2*(size_t)nb + g] = s.w[g];
+}
+
 __global__ void k_tape_shapes(cpgSet s)
 {
 	int g = blockIdx.x*blockDim.x + threadIdx.x;
@@ -139,6 +149,7 @@ __global__ void k_tape_rows(cpgSet s)
 			info[0] = arb.a; info[1] = arb.b; info[2] = (int)arb.gjk; info[3] = arb.warmSrc;
 		} else {
 			info[0] = -1; info[1] = -1; info[2] = 0; info[3] = 0;
+			atomicOr(&tp.cursor[3], 1);      /* joints are not differentiated */
 		}
 	}
 	for(int l = blockIdx.x*blockDim.x + threadIdx.x; l < nl; l += gridDim.x*blockDim.x)
@@ -146,6 +157,12 @@ __global__ void k_tape_rows(cpgSet s)
 }
 
 static inline int blocks_of(int n, int bs) { return (n + bs - 1)/bs > 0 ? (n + bs - 1)/bs : 1; }
+
+extern "C" int cpg_launch_tape_vel(const cpgSet *s, void *stream)
+{
+	k_tape_vel<<<blocks_of(s->totalBodies, 256), 256, 0, (cudaStream_t)stream>>>(*s);
+	return cudaGetLastError() == cudaSuccess ? 0 : -1;
+}
 
 extern "C" int cpg_launch_tape(const cpgSet *s, void *stream)
 {
@@ -233,6 +250,8 @@ __global__ void __launch_bounds__(CPG_ADJ_SOLVE_THREADS) k_adj_solve(cpgSet s, c
 	unsigned qmask = 0xFu << (tid & 28);
 	unsigned pmask = 0x3u << (tid & 28);     /* the quad's two velocity lanes */
 	int nbw = W.nbodies, bo = W.bodyOff;
+	/* the contact scratch holds one step's rows */
+	int rs = ro - tp.rowOff[(size_t)t*(nw + 1)];
 	bool staged = nbw <= stagedMax;
 	double *bars = staged ? sbar : a.body + 9*(size_t)bo + 3;
 	int bstride = staged ? 6 : 9;
@@ -249,7 +268,7 @@ __global__ void __launch_bounds__(CPG_ADJ_SOLVE_THREADS) k_adj_solve(cpgSet s, c
 				const double *arb = a.arb + 4*(size_t)row.src + 2*c;
 				z.jA = arb[0]; z.j2 = arb[1];
 			}
-			*lane_scratch(a, ro + k, c, lane4) = z;
+			*lane_scratch(a, rs + k, c, lane4) = z;
 		}
 		__syncwarp(qmask);
 		if(lane4 == 0 && row.kind == 0){
@@ -276,7 +295,7 @@ __global__ void __launch_bounds__(CPG_ADJ_SOLVE_THREADS) k_adj_solve(cpgSet s, c
 					if(c >= row.count) continue;
 					AdjLane L = row_lane(s, row, c, bo + lb, side, part);
 					AdjLaneRec R = adj_lane_rec(rec[c], side, part);
-					AdjLaneBar *sc = lane_scratch(a, ro + k, c, lane4);
+					AdjLaneBar *sc = lane_scratch(a, rs + k, c, lane4);
 					AdjLaneBar B = *sc;
 					double jbx, jby;
 					lane_adj_phase1(L, R, ax, ay, aw, jbx, jby, B);
@@ -304,7 +323,7 @@ __global__ void __launch_bounds__(CPG_ADJ_SOLVE_THREADS) k_adj_solve(cpgSet s, c
 			if(dyn){ ax = bar[0]; ay = bar[1]; aw = bar[2]; }
 			for(int c = row.count - 1; c >= 0; c--){
 				AdjLane L = row_lane(s, row, c, bo + lb, side, 0);
-				AdjLaneBar *sc = lane_scratch(a, ro + k, c, lane4);
+				AdjLaneBar *sc = lane_scratch(a, rs + k, c, lane4);
 				AdjLaneBar B = *sc;
 				double jN = row.arb.c[c].jnAcc, jT = row.arb.c[c].jtAcc;
 				double jbx, jby;
@@ -320,7 +339,7 @@ __global__ void __launch_bounds__(CPG_ADJ_SOLVE_THREADS) k_adj_solve(cpgSet s, c
 			for(int c = 0; c < row.count && c < 2; c++){
 				int j = ((src >> (4*c)) & 0xF) - 1;
 				if(j >= 0 && j < 2){
-					const AdjLaneBar *sc = lane_scratch(a, ro + k, c, 0);
+					const AdjLaneBar *sc = lane_scratch(a, rs + k, c, 0);
 					double *arb = a.arb + 4*(size_t)row.src + 2*j;
 					arb[0] += sc->jA; arb[1] += sc->j2;
 				}
@@ -351,7 +370,7 @@ __global__ void k_adj_geom(cpgSet s, cpgAdj a, int t)
 	int r = r0 + blockIdx.x*blockDim.x + threadIdx.x;
 	if(r >= r1) return;
 	const cpgRow &row = tp.rows[r];
-	double *u = a.unit + (size_t)U_N*r;
+	double *u = a.unit + (size_t)U_N*(r - r0);
 	for(int i = 0; i < U_N; i++) u[i] = 0.0;
 	if(row.kind != 0) return;
 	int w = tp.rowWorld[r];
@@ -376,7 +395,7 @@ __global__ void k_adj_geom(cpgSet s, cpgAdj a, int t)
 		p.biasCoef = P.biasCoef; p.slop = P.slop; p.dt = P.dt;
 		/* the four lanes' partial adjoints of the contact's constants */
 		AdjLaneBar lb[4];
-		for(int q = 0; q < 4; q++) lb[q] = *lane_scratch(a, r, c, q);
+		for(int q = 0; q < 4; q++) lb[q] = *lane_scratch(a, r - r0, c, q);
 		AdjConBar cb;
 		lane_bar_sum(lb, cb);
 		const AdjConBar *scb = &cb;
@@ -422,11 +441,12 @@ __global__ void k_adj_accum(cpgSet s, cpgAdj a, int t)
 	const int *info = tp.rowInfo + 4*(size_t)ro;
 	int tid = threadIdx.x, nt = blockDim.x;
 	int nbw = W.nbodies, bo = W.bodyOff;
+	int r0 = tp.rowOff[(size_t)t*(nw + 1)];
 	for(int l = 0; l < nlev; l++){
 		for(int k = start[l] + tid; k < start[l + 1]; k += nt){
 			const cpgRow &row = rows[k];
 			if(row.kind != 0) continue;
-			const double *u = a.unit + (size_t)U_N*(ro + k);
+			const double *u = a.unit + (size_t)U_N*(ro - r0 + k);
 			int ga = bo + row.a, gb = bo + row.b;
 			if(row.flags & ROW_DYN_A_){
 				double *b = a.body + 9*(size_t)ga;
@@ -457,7 +477,7 @@ __global__ void k_adj_accum(cpgSet s, cpgAdj a, int t)
 			const cpgRow &row = rows[k];
 			if(row.kind != 0) continue;
 			int sa = W.shapeOff + info[4*k], sb = W.shapeOff + info[4*k + 1];
-			const double *u = a.unit + (size_t)U_N*(ro + k);
+			const double *u = a.unit + (size_t)U_N*(ro - r0 + k);
 			a.gE[sa] += u[U_E]*s.se[sb]; a.gE[sb] += u[U_E]*s.se[sa];
 			a.gU[sa] += u[U_U]*s.su[sb]; a.gU[sb] += u[U_U]*s.su[sa];
 		}
@@ -508,7 +528,7 @@ extern "C" int cpg_launch_adjoint_remap(const cpgSet *s, const cpgAdj *a, const 
 extern "C" int cpg_launch_adjoint(const cpgSet *s, const cpgAdj *a, int step, int rows, void *stream)
 {
 	cudaStream_t st = (cudaStream_t)stream;
-	/* a few units per level: two warps per world keep every world resident */
+	/* two warps per world: 16 units of a level per round */
 	int stagedMax = s->hostMaxBodies <= CPG_ADJ_STAGED_BODIES ? s->hostMaxBodies : 0;
 	k_adj_solve<<<s->nworlds, CPG_ADJ_SOLVE_THREADS, (size_t)stagedMax*6*sizeof(double), st>>>(*s, *a, step, stagedMax);
 	k_adj_geom<<<blocks_of(rows, 128), 128, 0, st>>>(*s, *a, step);

@@ -503,8 +503,10 @@ int cpGpuDebugCandidates(cpSpace *space, int *out, int max);
  * (dLdw0: 1 per dynamic body), masses (dLdm; the moment of inertia held
  * fixed, as cpBodySetMass does), and each shape's elasticity and friction
  * (dLde, dLdu: 1 per shape, all shapes of each space in order).  Any output
- * pointer may be NULL.  The forward records its last segment as it runs;
- * the backward replays each earlier checkpoint's steps with recording and
+ * pointer may be NULL.  The forward records, per segment of `checkpoint`
+ * steps, the solver's inputs (rows, levels, poses, velocities, geometry);
+ * the backward recomputes each segment's solver iterations from them (a
+ * segment whose recording did not fit is replayed from its checkpoint) and
  * runs the reverse steps on the device; the batch is left in the state the
  * forward ended in.  The reverse pass needs the reference-order solver
  * and one iteration count for all spaces.  Constraints and external forces are not
@@ -517,6 +519,10 @@ int cpGpuRolloutBackward(cpGpuBatch *batch, const cpFloat *dLdp, cpFloat *dLdv0,
  * [2] bytes of the segment tape, [3] bytes of the checkpoints.  Returns the
  * number of values written (4), or 0. */
 int cpGpuDebugRolloutTimes(cpGpuBatch *batch, double *out);
+/* Debug: 0 makes cpGpuRolloutForward record nothing, so that the reverse
+ * pass replays every segment from its checkpoint; 1 (the default) records.
+ * Both give the same gradients. */
+void cpGpuDebugSetRolloutRecording(int on);
 void cpGpuSetTiming(int enabled);
 /* Debug: 1 makes single-world sets always solve with the whole-grid
  * kernel (a grid barrier between levels), 0 restores the automatic choice
@@ -527,10 +533,14 @@ void cpGpuDebugSetWholeGridSolve(int always);
 /* Debug: the ordered tree step keeps the node pools of worlds of at most
  * maxNodes nodes in shared memory (-1: every world whose pool fits). */
 void cpGpuDebugSetTreeStaging(int maxNodes);
-/* Debug: block size of the per-world solve (64, 128, 256 or 512; anything
+/* Debug: block size of the per-world solve (32, 64, 128, 256 or 512; anything
  * else restores the default) and the largest world (in bodies) whose
  * bodies it keeps in shared memory (-1: every world that fits). */
 void cpGpuDebugSetSolveShape(int threads, int maxBodies);
+/* Debug: lane layout of the per-world solve's levels: 0 automatic, 1 the
+ * fewest FP64 warp instructions, 2 the shortest dependent chain, 3 four
+ * lanes per contact only.  All give the same results. */
+void cpGpuDebugSetSolveLayout(int policy);
 /* Bookkeeping of the last step (after it completes): [0] error flags,
  * [1] pair-pool use and [2] node-pool use (per mille of capacity, largest
  * world), [3] live cached arbiters, [4] candidate pairs, [5] solved

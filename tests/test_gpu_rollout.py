@@ -141,6 +141,23 @@ def test_gradients_do_not_depend_on_the_checkpoint_interval(gpu_lib):
         np.testing.assert_array_equal(a[k], b[k], err_msg=k)
 
 
+def test_recorded_and_replayed_segments_give_the_same_gradients(gpu_lib):
+    """The reverse pass recomputes a segment's solver iterations from what
+    the forward recorded, or replays the segment from its checkpoint when
+    nothing was recorded; the gradients are bit-identical."""
+    seeds = [4000 + i for i in range(WORLDS)]
+    t = targets(WORLDS * SIZE)
+    a, La = rollout_grads(gpu_lib, seeds, 60, 16, t)
+    gpu_lib.cpGpuDebugSetRolloutRecording(0)
+    try:
+        b, Lb = rollout_grads(gpu_lib, seeds, 60, 16, t)
+    finally:
+        gpu_lib.cpGpuDebugSetRolloutRecording(1)
+    assert La == Lb
+    for k in a:
+        np.testing.assert_array_equal(a[k], b[k], err_msg=k)
+
+
 def test_gradients_are_deterministic_at_scale(gpu_lib):
     """Arbiters created between checkpoints can take other table slots in
     the replay than in the forward; the carried impulse adjoints follow
