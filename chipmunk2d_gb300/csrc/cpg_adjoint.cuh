@@ -684,11 +684,12 @@ CPG_HD void lane_adj_phase1(const AdjLane &L, const AdjLaneRec &t, double ax, do
 	jbx += -g*L.ry; jby += g*L.rx;
 }
 
-/* Phase 2: with the pair's total (Jbx, Jby), the scalar part, then the
- * lane's own body adjoint (ax, ay, aw) for the relative velocity; b.jA,
- * b.j2 are the part's accumulator adjoints, after to before. */
-CPG_HD void lane_adj_phase2(const AdjLane &L, const AdjLaneRec &t, double Jbx, double Jby,
-	double &ax, double &ay, double &aw, AdjLaneBar &b)
+/* Phase 2, scalar part: with the pair's total (Jbx, Jby), the adjoints of
+ * the part's accumulators (b.jA, b.j2, after to before) and of the
+ * contact's scalars, and the adjoint (dbx, dby) of the part's relative
+ * velocity. */
+CPG_HD void lane_adj_scalar(const AdjLane &L, const AdjLaneRec &t, double Jbx, double Jby,
+	double &dbx, double &dby, AdjLaneBar &b)
 {
 	double nx = L.nx, ny = L.ny;
 	bool vel = (L.part == 0);
@@ -720,16 +721,59 @@ CPG_HD void lane_adj_phase2(const AdjLane &L, const AdjLaneRec &t, double Jbx, d
 	b.nMass += jnbar*y;
 	b.c0 += adj_neg_if(jnbar, vel)*L.nMass;
 	double vnbar = -jnbar*L.nMass;
-	double dbx = vnbar*nx - vtbar*ny, dby = vnbar*ny + vtbar*nx;
+	dbx = vnbar*nx - vtbar*ny; dby = vnbar*ny + vtbar*nx;
 	b.nx += vnbar*t.vrx + vtbar*t.vry;
 	b.ny += vnbar*t.vry - vtbar*t.vrx;
 	b.jA = J0bar; b.j2 = T0bar;
-	/* d = (v_b + perp(r2) w_b) - (v_a + perp(r1) w_a) */
-	bool neg = (L.side == 0);
+}
+
+/* Phase 2, body part: the adjoint of one body's velocity through the
+ * relative velocity d = (v_b + perp(r2) w_b) - (v_a + perp(r1) w_a), and
+ * of its r. */
+CPG_HD void lane_adj_body(int side, double rx, double ry, double wown, double dbx, double dby,
+	double &ax, double &ay, double &aw, AdjLaneBar &b)
+{
+	bool neg = (side == 0);
 	double sdx = adj_neg_if(dbx, neg), sdy = adj_neg_if(dby, neg);
 	ax += sdx; ay += sdy;
-	aw += L.rx*sdy - L.ry*sdx;
-	b.ry -= sdx*t.wown; b.rx += sdy*t.wown;
+	aw += rx*sdy - ry*sdx;
+	b.ry -= sdx*wown; b.rx += sdy*wown;
+}
+
+/* Phase 2 on a four-lane quad: the scalar part (both lanes of a part
+ * compute it; side 0's sums are the ones used), then the lane's own body. */
+CPG_HD void lane_adj_phase2(const AdjLane &L, const AdjLaneRec &t, double Jbx, double Jby,
+	double &ax, double &ay, double &aw, AdjLaneBar &b)
+{
+	double dbx, dby;
+	lane_adj_scalar(L, t, Jbx, Jby, dbx, dby, b);
+	lane_adj_body(L.side, L.rx, L.ry, t.wown, dbx, dby, ax, ay, aw, b);
+}
+
+/* Two lanes per contact: lane p takes part p for both bodies (La, Lb:
+ * the part's side-0 and side-1 lanes' constants, wa, wb: the bodies'
+ * recorded angular velocities of the part).  Ba collects the contact's
+ * scalars and the part's accumulator adjoints like a side-0 lane, Bb the
+ * side-1 body's 1/m and r; the other fields of Bb are not used. */
+CPG_HD void pair_adj_apply(const AdjLane &La, const AdjLane &Lb, const AdjLaneRec &t, double wa, double wb,
+	double &ax, double &ay, double &aw, double &bx, double &by, double &bw, AdjLaneBar &Ba, AdjLaneBar &Bb)
+{
+	double dN = t.J1 - t.J0, dT = t.T1 - t.T0;
+	double Jx = La.nx*dN - La.ny*dT, Jy = La.nx*dT + La.ny*dN;
+	double gmJ_a = Jx*ax + Jy*ay, gmJ_b = Jx*bx + Jy*by;
+	/* side a receives -J, side b receives J */
+	double ga = -(La.iinv*aw), gb = Lb.iinv*bw;
+	double jbx = (-La.minv)*ax + Lb.minv*bx;
+	double jby = (-La.minv)*ay + Lb.minv*by;
+	Ba.minv -= gmJ_a; Bb.minv += gmJ_b;
+	Ba.rx += ga*Jy; Ba.ry -= ga*Jx;
+	Bb.rx += gb*Jy; Bb.ry -= gb*Jx;
+	jbx += -ga*La.ry - gb*Lb.ry;
+	jby += ga*La.rx + gb*Lb.rx;
+	double dbx, dby;
+	lane_adj_scalar(La, t, jbx, jby, dbx, dby, Ba);
+	lane_adj_body(0, La.rx, La.ry, wa, dbx, dby, ax, ay, aw, Ba);
+	lane_adj_body(1, Lb.rx, Lb.ry, wb, dbx, dby, bx, by, bw, Bb);
 }
 
 /* Warm start on the two velocity lanes: phase 1 as for an application

@@ -293,6 +293,25 @@ static void test_quad_lanes()
 		for(int i = 0; i < 28; i++){ snprintf(nm, sizeof(nm), "lanes trial %d value %d", trial, i); close_to(nm, lanes[i], one[i]); n++; }
 		/* both lanes of a part carry the same accumulator adjoints */
 		if(cl[0].jA != cl[1].jA || cl[0].j2 != cl[1].j2 || cl[2].jA != cl[3].jA){ failures++; printf("  FAIL lanes trial %d: pair accumulators differ\n", trial); }
+		/* two lanes: lane p takes part p for both bodies */
+		{
+			double pa[2][3], pb[2][3];
+			AdjLaneBar pl[4];
+			for(int q = 0; q < 4; q++) lane_bar_zero(pl[q]);
+			for(int p = 0; p < 2; p++){
+				for(int i = 0; i < 3; i++){ pa[p][i] = w[3*p + i]; pb[p][i] = w[6 + 3*p + i]; }
+				pl[2*p].jA = p ? w[14] : w[12]; pl[2*p].j2 = p ? 0.0 : w[13];
+				AdjLaneRec ra = adj_lane_rec(rec, 0, p), rb = adj_lane_rec(rec, 1, p);
+				pair_adj_apply(adj_lane(c, 2*p), adj_lane(c, 2*p + 1), ra, ra.wown, rb.wown,
+					pa[p][0], pa[p][1], pa[p][2], pb[p][0], pb[p][1], pb[p][2], pl[2*p], pl[2*p + 1]);
+			}
+			AdjConBar ps;
+			lane_bar_sum(pl, ps);
+			double pairs[] = { pa[0][0], pa[0][1], pa[0][2], pa[1][0], pa[1][1], pa[1][2], pb[0][0], pb[0][1], pb[0][2], pb[1][0], pb[1][1], pb[1][2],
+				pl[0].jA, pl[0].j2, pl[2].jA,
+				ps.r1x, ps.r1y, ps.r2x, ps.r2y, ps.nx, ps.ny, ps.nMass, ps.tMass, ps.bias, ps.bounce, ps.u, ps.minvA, ps.minvB };
+			for(int i = 0; i < 28; i++){ snprintf(nm, sizeof(nm), "pair lanes trial %d value %d", trial, i); close_to(nm, pairs[i], one[i]); n++; }
+		}
 		/* warm start */
 		AdjBody Aw = { w[0], w[1], w[2], 0, 0, 0 }, Bw = { w[6], w[7], w[8], 0, 0, 0 };
 		double wN = 0.0, wT = 0.0, dtc = urange(0.5, 1.5);
@@ -316,7 +335,7 @@ static void test_quad_lanes()
 		close_to(nm, ws.minvA, wc.minvA); close_to(nm, ws.minvB, wc.minvB);
 		n += 8;
 	}
-	printf("four-lane adjoint: %d checks\n", n);
+	printf("four- and two-lane adjoint: %d checks\n", n);
 }
 
 /* ---- 2. contact geometry against the narrow phase ---- */
