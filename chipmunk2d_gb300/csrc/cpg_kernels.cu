@@ -1820,13 +1820,24 @@ __global__ void k_color_coop(cpgSet s, int w)
 
 /* 96 quads per block: the quad-lane solve holds its next row in registers
  * (about 170 per thread, so 384 threads fill the register file) */
-#define CPG_COOP_SOLVE_THREADS 384
+#define CPG_COOP_SOLVE_THREADS 256
 
 /* Levels (ordered mode) or colours (coloured mode) of one large world,
  * with the whole grid: grid.sync() between levels.  Packed body state is
  * read past the L1 (__ldcg), since other blocks write it between syncs;
  * a row is always handled by the same quad of lanes, in one SM, so its own
  * accumulator updates are coherent. */
+/* Whether a level of U units, dealt round-robin over `blocks` blocks of
+ * the whole-grid solve, takes fewer FP64 instructions on the busiest
+ * sub-partition on two lanes per contact (~42 per lane, fused) than on
+ * four (~32): a block's warps go round-robin to its four sub-partitions. */
+__device__ __forceinline__ bool coop_two_lanes(int U, int blocks)
+{
+	int ub = (U + blocks - 1)/blocks;
+	int w4 = (4*ub + 31) >> 5, w2 = (2*ub + 31) >> 5;
+	return ((w2 + 3) >> 2)*42 < ((w4 + 3) >> 2)*32;
+}
+
 template<bool FUSED>
 __global__ void __launch_bounds__(CPG_COOP_SOLVE_THREADS, 1) k_solve_coop(cpgSet s, int w)
 {
@@ -1849,14 +1860,27 @@ __global__ void __launch_bounds__(CPG_COOP_SOLVE_THREADS, 1) k_solve_coop(cpgSet
 	unsigned qmask = 0xFu << (threadIdx.x & 28);
 	/* the quad's first unit of the next level is read before the barrier,
 	 * so that only the body loads remain after it */
+	/* a level whose units fill more than one warp per sub-partition on four
+	 * lanes runs on two (one lane per part, both bodies): half the warps,
+	 * each with ~1.3x the instructions */
+	int pair = (threadIdx.x >> 1)*gridDim.x + blockIdx.x, np2 = (gridDim.x*blockDim.x) >> 1;
+	bool bias = (threadIdx.x & 1) != 0;
 	QuadRow q;
 	int k = start[0] + quad;
-	bool have = k < start[1];
+	bool two = coop_two_lanes(start[1] - start[0], gridDim.x);
+	bool have = !two && k < start[1];
 	if(have) quad_load(q, rows[k], lane4);
 	for(int pass = 0; pass <= iters; pass++){
 		for(int l = 0; l < nlev; l++){
 			int e = start[l + 1];
-			if(have){
+			if(two){
+				for(int k2 = start[l] + pair; k2 < e; k2 += np2){
+					PairRow pr;
+					pair_load(pr, rows[k2], bias);
+					if(pr.kind == 0) pair_apply<true, FUSED>(pr, rows + k2, bodies, pass, dt_coef, bias);
+					else if(!bias) solve_row<true>(rows, k2, bodies, pass, dt_coef, dt);
+				}
+			} else if(have){
 				if(q.kind == 0) quad_apply<true, FUSED>(q, rows + k, bodies, pass, dt_coef, qmask, lane4);
 				else if(lane4 == 0) solve_row<true>(rows, k, bodies, pass, dt_coef, dt);
 				/* levels wider than the grid */
@@ -1867,13 +1891,14 @@ __global__ void __launch_bounds__(CPG_COOP_SOLVE_THREADS, 1) k_solve_coop(cpgSet
 					else if(lane4 == 0) solve_row<true>(rows, k2, bodies, pass, dt_coef, dt);
 				}
 			}
-			int nl = l + 1, np = pass;
-			if(nl == nlev){ nl = 0; np++; }
+			int nl = l + 1, npass = pass;
+			if(nl == nlev){ nl = 0; npass++; }
 			k = start[nl] + quad;
-			have = np <= iters && k < start[nl + 1];
+			two = coop_two_lanes(start[nl + 1] - start[nl], gridDim.x);
+			have = !two && npass <= iters && k < start[nl + 1];
 			/* with a single level the next row is the one just written by
 			 * lanes 0 and 2 of this quad */
-			__syncwarp(qmask);
+			__syncthreads();
 			if(have) quad_load(q, rows[k], lane4);
 			grid.sync();
 		}
