@@ -305,7 +305,7 @@ def run_batch(args, emit=True, sharded=True):
         with torch.cuda.stream(stream):
             flush.fill_(float(i))
             ev[i][0].record(stream)
-        lib.cpGpuBatchStep(batch, BATCH_DT, 1, 0)
+        lib.cpGpuBatchStep(batch, BATCH_DT, 1, 1)
         with torch.cuda.stream(stream):
             ev[i][1].record(stream)
     torch.cuda.synchronize()
@@ -313,6 +313,8 @@ def run_batch(args, emit=True, sharded=True):
     clk = clocks.stop()
     if lib.cpGpuGetLastError():
         raise RuntimeError(lib.cpGpuGetLastErrorString().decode())
+    tune = (ctypes.c_int * 2)()
+    lib.cpGpuBatchGetTuning(batch, ctypes.cast(tune, ctypes.c_void_p))
     total_s = sum(a.elapsed_time(b) for a, b in ev) / 1000.0
     if dist:
         t = torch.tensor([total_s], device="cuda")
@@ -389,6 +391,7 @@ def run_batch(args, emit=True, sharded=True):
                                    if world_size > 1 else "single"),
                    "l2": "flushed between timed steps (256 MB fill, untimed)"},
         "body_steps_per_s": nb_total * args.steps / total_s,
+        "launch": {"cuda_graph": True, "tuned_solve_threads": tune[0], "tuned_tree_staging": tune[1]},
         "looped_plain_gpu_world_steps_per_s": loop_ws,
         "batched_over_looped": world_steps / loop_ws,
         "phase_ms_after_run": dict(zip(names, [round(float(x), 4) for x in phase[:7]])),
@@ -840,7 +843,7 @@ def run_ours(args):
                            mode_sample(lib, "mixed", 3, 2, mode=0)]
         b = run_batch(argparse.Namespace(steps=BATCH_STEPS, warmup=3), emit=False, sharded=False)
         extras["batch"] = {k: b[k] for k in ("value", "unit", "ms_per_step", "body_steps_per_s",
-                                             "looped_plain_gpu_world_steps_per_s", "batched_over_looped",
+                                             "looped_plain_gpu_world_steps_per_s", "batched_over_looped", "launch",
                                              "cpu_baseline", "cpu_all_threads", "phase_ms_after_run")}
         extras["batch"]["config"] = b["config"]
         r = run_rollout(args, emit=False, sharded=False)

@@ -168,6 +168,8 @@ _GPU_API = {
     "cpGpuBatchFree": (None, [P]),
     "cpGpuBatchAddSpace": (I, [P, P]),
     "cpGpuBatchStep": (I, [P, D, I, I]),
+    "cpGpuBatchGetTuning": (I, [P, P]),
+    "cpGpuSetAutotune": (None, [I]),
     "cpGpuRolloutForward": (I, [P, D, I, I]),
     "cpGpuRolloutBackward": (I, [P, P, P, P, P, P, P]),
     "cpGpuDebugRolloutTimes": (I, [P, P]),

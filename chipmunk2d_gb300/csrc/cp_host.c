@@ -210,6 +210,15 @@ static void push_(void ***arr, int *n, int *cap, void *p)
  * blocks rotate through a ring and each is reused only after its event. */
 #define CPG_PARAM_RING 8
 
+/* Launch-shape candidates of the online tuner: solve block size and
+ * whether the tree step may stage node pools in shared memory. */
+#define CPG_TUNE_CANDIDATES 6
+#define CPG_TUNE_ROUNDS 2
+#define CPG_TUNE_PERIOD 256
+#define CPG_TUNE_FIRST 32
+static const int tune_threads[CPG_TUNE_CANDIDATES] = { 64, 128, 256, 64, 128, 256 };
+static const int tune_tree[CPG_TUNE_CANDIDATES] = { -1, -1, -1, 0, 0, 0 };
+
 struct DevSet {
 	cpgSet d;                 /* device pointers; counts valid on host too */
 	cpgWorld *hworld;
@@ -229,6 +238,15 @@ struct DevSet {
 	void *scratch;            /* per-step scratch outside the slab (not checkpointed) */
 	cpgArb *gather;           /* arbiter snapshot staging */
 	int gatherCap;
+	void *graph;              /* the step's launches as a CUDA graph (cpgStepGraph) */
+	int useGraph;             /* this call's steps replay the graph */
+	long long stepCount;      /* steps launched */
+	/* online tuning of many-world sets (launch shapes that give the same
+	 * results): candidates timed on interleaved steps, then the fastest */
+	long long tuneNext;       /* step at which the next tuning window opens */
+	int tuneIdx;              /* position in the open window */
+	double tuneMs[CPG_TUNE_CANDIDATES];
+	int tuneBest;             /* chosen candidate, -1 before the first window */
 };
 
 
@@ -236,6 +254,8 @@ static cudaStream_t g_stream = NULL;
 static int g_stream_user = 0;
 static int g_timing = 0;
 static int g_tree_stage = -1;
+static int g_autotune = 1;
+void cpGpuSetAutotune(int on) { g_autotune = on ? 1 : 0; }
 static int g_rollout_record = 1;
 void cpGpuDebugSetRolloutRecording(int on) { g_rollout_record = on ? 1 : 0; }
 static int g_solve_threads = 0, g_solve_stage = -1, g_solve_layout = 0;
@@ -559,6 +579,7 @@ static void devset_free(DevSet *ds)
 	if(!ds) return;
 	if(ds->slab) cudaFree(ds->slab);
 	if(ds->scratch) cudaFree(ds->scratch);
+	if(ds->graph) cpg_step_graph_free(ds->graph);
 	if(ds->gather) cudaFree(ds->gather);
 	if(ds->hparams) cudaFreeHost(ds->hparams);
 	if(ds->hstats) cudaFreeHost(ds->hstats);
@@ -727,6 +748,8 @@ static DevSet *devset_build(cpSpace **spaces, int nspaces)
 	d->hostMaxBodies = 0;
 	d->hostMaxNodes = 0;
 	d->hostTreeStage = -1;
+	ds->tuneNext = CPG_TUNE_FIRST;
+	ds->tuneBest = -1;
 	d->hostSolveThreads = 0;
 	d->hostSolveStage = -1;
 	d->solveLayout = 0;
@@ -783,7 +806,7 @@ static void check_stats(DevSet *ds)
 	/* whole-grid solve pays off when one sweep level is wide enough */
 	int units = ds->hstats[5] + (ds->nspaces == 1 ? ds->spaces[0]->ncons : 0);
 	int levels = ds->hstats[6] > 0 ? ds->hstats[6] : 1;
-	ds->d.hostUnitsHint = (units/levels >= 64) ? units : 0;
+	ds->d.hostUnitsHint = (ds->nspaces == 1 && units/levels >= 64) ? units : 0;
 	if(err){
 		set_error(CP_GPU_ERR_OVERFLOW, "device table overflow (flags 0x%x): pairs %d/1000, nodes %d/1000, candidates %d/1000",
 			err, ds->hstats[1], ds->hstats[2], ds->hstats[7]);
@@ -844,16 +867,51 @@ static int devset_step(DevSet *ds, const double *dts, cpSpace **only)
 	d->hostSolveThreads = g_solve_threads;
 	d->hostSolveStage = g_solve_stage;
 	d->solveLayout = g_solve_layout;
+	/* launch shapes of many-world sets: the tuner's candidates on the steps
+	 * of a tuning window, its choice after it (debug settings win) */
+	int tuning = -1;
+	if(ds->nspaces >= 152 && g_autotune && g_solve_threads == 0 && g_tree_stage < 0 && !d->tape.on){
+		if(ds->stepCount >= ds->tuneNext){
+			/* candidates in palindromic order: every candidate's steps sit
+			 * at the same mean time, so a workload that grows or settles
+			 * does not favour the ones timed first */
+			int i = ds->tuneIdx, r = i/CPG_TUNE_CANDIDATES, j = i % CPG_TUNE_CANDIDATES;
+			tuning = (r & 1) ? CPG_TUNE_CANDIDATES - 1 - j : j;
+			d->hostSolveThreads = tune_threads[tuning];
+			d->hostTreeStage = tune_tree[tuning];
+		} else if(ds->tuneBest >= 0){
+			d->hostSolveThreads = tune_threads[ds->tuneBest];
+			d->hostTreeStage = tune_tree[ds->tuneBest];
+		}
+	}
 	if(!h2d(d->params, hp, sizeof(cpgParams)*(size_t)ds->nspaces)) return -1;
 	cudaEventRecord(ds->paramEvent[slot], st);
 	ds->paramRecorded[slot] = 1;
 	float ms[8] = {0};
 	int mode = ds->spaces[0]->mode;
-	if(cpg_launch_step(d, d, mode, st, g_timing ? ms : NULL) != 0){
+	int timed = g_timing || tuning >= 0;
+	int lrc;
+	/* many-world sets launch no cooperative kernels and keep their launch
+	 * arguments from step to step: their step replays as one CUDA graph */
+	if(ds->useGraph && !timed && !d->tape.on && ds->nspaces > 1) lrc = cpg_launch_step_graph(d, mode, st, &ds->graph);
+	else lrc = cpg_launch_step(d, d, mode, st, timed ? ms : NULL);
+	if(lrc != 0){
 		set_error(CP_GPU_ERR_CUDA, "step launch failed");
 		return -1;
 	}
 	if(g_timing) for(int w = 0; w < ds->nspaces; w++) memcpy(ds->spaces[w]->phaseMs, ms, sizeof(ms));
+	if(tuning >= 0){
+		ds->tuneMs[tuning] += (double)ms[1] + (double)ms[6];
+		if(++ds->tuneIdx == CPG_TUNE_CANDIDATES*CPG_TUNE_ROUNDS){
+			int best = 0;
+			for(int c = 1; c < CPG_TUNE_CANDIDATES; c++) if(ds->tuneMs[c] < ds->tuneMs[best]) best = c;
+			ds->tuneBest = best;
+			for(int c = 0; c < CPG_TUNE_CANDIDATES; c++) ds->tuneMs[c] = 0.0;
+			ds->tuneIdx = 0;
+			ds->tuneNext = ds->stepCount + CPG_TUNE_PERIOD;
+		}
+	}
+	ds->stepCount++;
 	if(!ds->statsPending){
 		cudaMemcpyAsync(ds->hstats, d->stats, sizeof(int)*16, cudaMemcpyDeviceToHost, st);
 		cudaEventRecord(ds->statsEvent, st);
@@ -1012,9 +1070,17 @@ int cpGpuBatchAddSpace(cpGpuBatch *b, cpSpace *sp)
 	return b->n - 1;
 }
 
+int cpGpuBatchGetTuning(cpGpuBatch *b, int *out)
+{
+	if(!b || !b->dev || !out) return 0;
+	DevSet *ds = b->dev;
+	out[0] = ds->tuneBest >= 0 ? tune_threads[ds->tuneBest] : 0;
+	out[1] = ds->tuneBest >= 0 ? tune_tree[ds->tuneBest] : -1;
+	return 2;
+}
+
 int cpGpuBatchStep(cpGpuBatch *b, cpFloat dt, int steps, int use_graph)
 {
-	(void)use_graph;
 	if(!b || b->n == 0) return -1;
 	for(int i = 0; i < b->n; i++) if(!space_supported(b->spaces[i])) return -1;
 	if(!b->dev){
@@ -1025,7 +1091,9 @@ int cpGpuBatchStep(cpGpuBatch *b, cpFloat dt, int steps, int use_graph)
 	double *dts = (double *)malloc(sizeof(double)*(size_t)b->n);
 	for(int i = 0; i < b->n; i++) dts[i] = dt;
 	int rc = 0;
+	b->dev->useGraph = use_graph ? 1 : 0;
 	for(int s = 0; s < steps && rc == 0; s++) rc = devset_step(b->dev, dts, NULL);
+	b->dev->useGraph = 0;
 	free(dts);
 	return rc;
 }

@@ -346,6 +346,8 @@ int cpg_launch_tape(const cpgSet *s, void *stream);
 int cpg_launch_adjoint(const cpgSet *s, const cpgAdj *a, int step, int rows, void *stream);
 int cpg_launch_adjoint_remap(const cpgSet *s, const cpgAdj *a, const void *oldKeys, void *stream);
 int cpg_launch_tape_vel(const cpgSet *s, void *stream);
+int cpg_launch_step_graph(const cpgSet *s, int mode, void *stream, void **cache);
+void cpg_step_graph_free(void *cache);
 int cpg_launch_replay_solve(const cpgSet *s, const cpgAdj *a, int nsteps, void *stream);
 
 #ifdef __cplusplus

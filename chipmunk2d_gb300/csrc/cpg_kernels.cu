@@ -1974,6 +1974,66 @@ static cudaError_t launch_coop(const void *kernel, int threads, cpgSet *s, int w
 #define CPG_STAGED_NODES 3072
 
 /* `h` is the host copy of the set's sizes (same struct, host values). */
+/* A many-world step as a CUDA graph: captured from cpg_launch_step, and
+ * captured again when the launch arguments (the set as the host holds it,
+ * the mode) change. */
+struct cpgStepGraph {
+	cudaGraphExec_t exec;
+	cpgSet key;
+	int mode;
+	long long launches;
+	int valid;
+};
+
+extern "C" void cpg_step_graph_free(void *cache)
+{
+	cpgStepGraph *g = (cpgStepGraph *)cache;
+	if(!g) return;
+	if(g->valid) cudaGraphExecDestroy(g->exec);
+	free(g);
+}
+
+extern "C" int cpg_launch_step(const cpgSet *s, const cpgSet *h, int mode, void *stream, float *phase_ms);
+
+extern "C" int cpg_launch_step_graph(const cpgSet *s, int mode, void *stream, void **cache)
+{
+	cudaStream_t st = (cudaStream_t)stream;
+	cpgStepGraph *g = (cpgStepGraph *)*cache;
+	if(!g){
+		g = (cpgStepGraph *)calloc(1, sizeof(cpgStepGraph));
+		if(!g) return cpg_launch_step(s, s, mode, stream, NULL);
+		*cache = g;
+	}
+	if(!g->valid || g->mode != mode || memcmp(&g->key, s, sizeof(cpgSet)) != 0){
+		if(g->valid){ cudaGraphExecDestroy(g->exec); g->valid = 0; }
+		long long before = g_launches;
+		if(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal) != cudaSuccess){
+			cudaGetLastError();
+			return cpg_launch_step(s, s, mode, stream, NULL);
+		}
+		int rc = cpg_launch_step(s, s, mode, stream, NULL);
+		cudaGraph_t graph = NULL;
+		cudaError_t e = cudaStreamEndCapture(st, &graph);
+		long long n = g_launches - before;
+		g_launches = before;
+		if(rc != 0 || e != cudaSuccess || !graph){
+			if(graph) cudaGraphDestroy(graph);
+			cudaGetLastError();
+			return cpg_launch_step(s, s, mode, stream, NULL);
+		}
+		e = cudaGraphInstantiate(&g->exec, graph, 0);
+		cudaGraphDestroy(graph);
+		if(e != cudaSuccess){
+			cudaGetLastError();
+			return cpg_launch_step(s, s, mode, stream, NULL);
+		}
+		g->key = *s; g->mode = mode; g->launches = n; g->valid = 1;
+	}
+	if(cudaGraphLaunch(g->exec, st) != cudaSuccess) return -1;
+	g_launches += g->launches;
+	return 0;
+}
+
 extern "C" int cpg_launch_replay_solve(const cpgSet *s, const cpgAdj *a, int nsteps, void *stream)
 {
 	cudaStream_t st = (cudaStream_t)stream;

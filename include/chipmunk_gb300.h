@@ -437,8 +437,17 @@ void cpGpuBatchFree(cpGpuBatch *batch);
 int cpGpuBatchAddSpace(cpGpuBatch *batch, cpSpace *space);
 /* Step every space of the batch `steps` times with time step dt.  With
  * use_graph != 0 the per-step launches are captured once in a CUDA graph
- * and replayed. */
+ * and replayed (captured again when a launch argument changes).  Batches of
+ * 152 or more spaces tune their launch shapes online: on a window of 12
+ * steps every 256 (the first at step 32, once the scene has contacts)
+ * candidate solve block sizes and tree staging choices run on interleaved
+ * steps and the fastest is kept.  All candidates give the same results. */
 int cpGpuBatchStep(cpGpuBatch *batch, cpFloat dt, int steps, int use_graph);
+/* The tuner's choice: [0] solve block size (0 before the first window),
+ * [1] tree staging (-1 automatic, 0 off).  Returns the count written. */
+int cpGpuBatchGetTuning(cpGpuBatch *batch, int *out);
+/* 0 turns the online tuner off (defaults are used), 1 (default) on. */
+void cpGpuSetAutotune(int on);
 
 /* Exact-order parallel schedule of a sequential sweep.  Unit u of the
  * sweep touches dynamic bodies bodyA[u] and bodyB[u] (a negative index or

@@ -190,3 +190,38 @@ def test_batched_worlds_match_single_worlds(gpu_lib, oracle_lib):
             g.free()
         for o in os_:
             o.free()
+
+
+def _batch_run(lib, n, steps, use_graph, autotune):
+    import ctypes
+    sizes = (ctypes.c_int * n)()
+    lib.cpx_batch_sizes(n, 3, ctypes.cast(sizes, ctypes.c_void_p))
+    gs = [Scene(lib, 4, min(sizes[i], 96), seed=300 + i) for i in range(n)]
+    batch = lib.cpGpuBatchNew()
+    lib.cpGpuSetAutotune(autotune)
+    try:
+        for g in gs:
+            assert lib.cpGpuBatchAddSpace(batch, g.space) >= 0
+        for _ in range(steps // 4):
+            assert lib.cpGpuBatchStep(batch, 1 / 60, 4, use_graph) == 0
+        check_gpu_error(lib)
+        tune = (ctypes.c_int * 2)()
+        lib.cpGpuBatchGetTuning(batch, ctypes.cast(tune, ctypes.c_void_p))
+        return [g.bodies() for g in gs], (tune[0], tune[1])
+    finally:
+        lib.cpGpuSetAutotune(1)
+        lib.cpGpuBatchFree(batch)
+        for g in gs:
+            g.free()
+
+
+def test_graph_replay_and_online_tuning_do_not_change_results(gpu_lib):
+    """A many-world batch stepped through its CUDA graph, with the online
+    tuner trying launch shapes on the way, ends bit-identical to plain
+    launches with the default shapes."""
+    base, t0 = _batch_run(gpu_lib, 160, 40, 0, 0)
+    graph, t1 = _batch_run(gpu_lib, 160, 40, 1, 1)
+    assert t0 == (0, -1)
+    assert t1[0] in (64, 128, 256) and t1[1] in (-1, 0)
+    for a, b in zip(base, graph):
+        np.testing.assert_array_equal(a, b)
