@@ -870,7 +870,7 @@ static int devset_step(DevSet *ds, const double *dts, cpSpace **only)
 	/* launch shapes of many-world sets: the tuner's candidates on the steps
 	 * of a tuning window, its choice after it (debug settings win) */
 	int tuning = -1;
-	if(ds->nspaces >= 152 && g_autotune && g_solve_threads == 0 && g_tree_stage < 0 && !d->tape.on){
+	if(ds->nspaces >= 152 && g_autotune && g_solve_threads == 0 && g_tree_stage < 0){
 		if(ds->stepCount >= ds->tuneNext){
 			/* candidates in palindromic order: every candidate's steps sit
 			 * at the same mean time, so a workload that grows or settles

@@ -593,11 +593,12 @@ CPG_HD void geom_adjoint(const GContacts &g, int count, const double *r1bar, con
  * branch exactly.
  *
  * The constants' adjoints go to per-lane partial sums (AdjLaneBar): each
- * lane sums 1/m and r of its own body; the contact's scalars are summed by
- * every lane but only the side-0 lanes' sums are used (both sides compute
- * the same values).  lane_bar_sum turns the four lanes' sums into the
- * contact's AdjConBar, equal to app_adjoint's up to the order of the
- * additions.
+ * lane sums 1/m and r of its own body; the contact's scalars, which both
+ * lanes of a part could compute, are split between them (side 0: n.x,
+ * tMass and the constant term; side 1: n.y, u and nMass), so each lane
+ * issues half of those operations.  lane_bar_sum turns the four lanes'
+ * sums into the contact's AdjConBar, equal to app_adjoint's up to the
+ * order of the additions.
  * ------------------------------------------------------------------- */
 CPG_HD long long adj_bits(double x)
 {
@@ -633,9 +634,10 @@ struct AdjLane {
  * part's relative velocity and the lane's body's angular velocity. */
 struct AdjLaneRec { double J0, J1, T0, T1, vrx, vry, wown; };
 
-/* Per-lane partial sums of the contact's constants' adjoints, and the
- * accumulator adjoints the part carries (velocity: jA = jN, j2 = jT; bias:
- * jA = jB). */
+/* Per-lane partial sums of the contact's constants' adjoints (1/m and r of
+ * the lane's body; the scalars split by side: n.x, tMass, c0 on side 0,
+ * n.y, u, nMass on side 1), and the accumulator adjoints the part carries
+ * (velocity: jA = jN, j2 = jT; bias: jA = jB). */
 struct alignas(16) AdjLaneBar { double minv, rx, ry, nx, ny, tMass, u, c0, nMass, jA, j2, pad; };
 
 CPG_HD void lane_bar_zero(AdjLaneBar &b)
@@ -687,19 +689,22 @@ CPG_HD void lane_adj_phase1(const AdjLane &L, const AdjLaneRec &t, double ax, do
 /* Phase 2, scalar part: with the pair's total (Jbx, Jby), the adjoints of
  * the part's accumulators (b.jA, b.j2, after to before) and of the
  * contact's scalars, and the adjoint (dbx, dby) of the part's relative
- * velocity. */
-CPG_HD void lane_adj_scalar(const AdjLane &L, const AdjLaneRec &t, double Jbx, double Jby,
-	double &dbx, double &dby, AdjLaneBar &b)
+ * velocity.  The scalars' partial sums are split by side: a side-0 lane
+ * sums n.x, tMass and the constant term (bounce or bias), a side-1 lane
+ * n.y, u and nMass.  With BOTH (one lane for both sides) the side-1 sums
+ * go to *b1. */
+template<bool BOTH>
+CPG_HD void lane_adj_scalar_t(const AdjLane &L, const AdjLaneRec &t, double Jbx, double Jby,
+	double &dbx, double &dby, AdjLaneBar &b, AdjLaneBar *b1)
 {
 	double nx = L.nx, ny = L.ny;
 	bool vel = (L.part == 0);
+	bool s1 = !BOTH && L.side == 1;
 	double dN = t.J1 - t.J0, dT = t.T1 - t.T0;
 	double vn = t.vrx*nx + t.vry*ny;
 	double vt = t.vry*nx - t.vrx*ny;
 	double dNbar = Jbx*nx + Jby*ny;
 	double dTbar = Jby*nx - Jbx*ny;
-	b.nx += Jbx*dN + Jby*dT;
-	b.ny += Jby*dN - Jbx*dT;
 	double J1bar = b.jA + dNbar, J0bar = -dNbar;
 	double T1bar = b.j2 + dTbar, T0bar = -dTbar;
 	/* friction: dclamp(f, -jtMax, jtMax) returned f, -jtMax or jtMax */
@@ -710,21 +715,42 @@ CPG_HD void lane_adj_scalar(const AdjLane &L, const AdjLaneRec &t, double Jbx, d
 	double mbar = (vel && (top || bot)) ? adj_neg_if(T1bar, bot) : 0.0;
 	T0bar += fbar;
 	double vtbar = -fbar*L.tMass;
-	b.tMass -= fbar*vt;
-	b.u += mbar*t.J1;
 	J1bar += mbar*L.u;
 	/* normal (bias): dmax(J0 + j, 0) passed J0 + j on when the result is not +0 */
 	double jnbar = (adj_bits(t.J1) > 0) ? J1bar : 0.0;
 	J0bar += jnbar;
 	/* j = y*nMass with y = -(bounce + vn) (velocity) or bias - vn (bias) */
 	double y = adj_neg_if(L.c0 + adj_neg_if(vn, !vel), vel);
-	b.nMass += jnbar*y;
-	b.c0 += adj_neg_if(jnbar, vel)*L.nMass;
 	double vnbar = -jnbar*L.nMass;
 	dbx = vnbar*nx - vtbar*ny; dby = vnbar*ny + vtbar*nx;
-	b.nx += vnbar*t.vrx + vtbar*t.vry;
-	b.ny += vnbar*t.vry - vtbar*t.vrx;
+	/* n.x: Jb.(dN, dT) rotated + vnbar vr + vtbar perp; n.y likewise */
+	if(BOTH){
+		b.nx += Jbx*dN + Jby*dT;
+		b.nx += vnbar*t.vrx + vtbar*t.vry;
+		b.tMass -= fbar*vt;
+		b.c0 += adj_neg_if(jnbar, vel)*L.nMass;
+		b1->ny += Jby*dN - Jbx*dT;
+		b1->ny += vnbar*t.vry - vtbar*t.vrx;
+		b1->u += mbar*t.J1;
+		b1->nMass += jnbar*y;
+	} else {
+		double n = s1 ? b.ny : b.nx;
+		n += (s1 ? Jby : Jbx)*dN + (s1 ? -Jbx : Jby)*dT;
+		n += vnbar*(s1 ? t.vry : t.vrx) + vtbar*(s1 ? -t.vrx : t.vry);
+		double tu = s1 ? b.u : b.tMass;
+		tu += (s1 ? mbar : -fbar)*(s1 ? t.J1 : vt);
+		double cn = s1 ? b.nMass : b.c0;
+		cn += (s1 ? jnbar : adj_neg_if(jnbar, vel))*(s1 ? y : L.nMass);
+		if(s1){ b.ny = n; b.u = tu; b.nMass = cn; }
+		else { b.nx = n; b.tMass = tu; b.c0 = cn; }
+	}
 	b.jA = J0bar; b.j2 = T0bar;
+}
+
+CPG_HD void lane_adj_scalar(const AdjLane &L, const AdjLaneRec &t, double Jbx, double Jby,
+	double &dbx, double &dby, AdjLaneBar &b)
+{
+	lane_adj_scalar_t<false>(L, t, Jbx, Jby, dbx, dby, b, nullptr);
 }
 
 /* Phase 2, body part: the adjoint of one body's velocity through the
@@ -771,7 +797,7 @@ CPG_HD void pair_adj_apply(const AdjLane &La, const AdjLane &Lb, const AdjLaneRe
 	jbx += -ga*La.ry - gb*Lb.ry;
 	jby += ga*La.rx + gb*Lb.rx;
 	double dbx, dby;
-	lane_adj_scalar(La, t, jbx, jby, dbx, dby, Ba);
+	lane_adj_scalar_t<true>(La, t, jbx, jby, dbx, dby, Ba, &Bb);
 	lane_adj_body(0, La.rx, La.ry, wa, dbx, dby, ax, ay, aw, Ba);
 	lane_adj_body(1, Lb.rx, Lb.ry, wb, dbx, dby, bx, by, bw, Bb);
 }
@@ -797,8 +823,11 @@ CPG_HD void lane_warm_phase2(const AdjLane &L, double jN, double jT, double dt_c
 	double jxbar = Jbx*dt_coef, jybar = Jby*dt_coef;
 	b.jA += jxbar*L.nx + jybar*L.ny;
 	b.j2 += jybar*L.nx - jxbar*L.ny;
-	b.nx += jxbar*jN + jybar*jT;
-	b.ny += jybar*jN - jxbar*jT;
+	/* side 0 sums n.x, side 1 n.y */
+	bool s1 = L.side == 1;
+	double n = s1 ? b.ny : b.nx;
+	n += (s1 ? jybar : jxbar)*jN + (s1 ? -jxbar : jybar)*jT;
+	if(s1) b.ny = n; else b.nx = n;
 }
 
 /* The contact's constants' adjoints from its four lanes' partial sums
@@ -808,8 +837,8 @@ CPG_HD void lane_bar_sum(const AdjLaneBar *l, AdjConBar &cb)
 	cb.minvA = l[0].minv + l[2].minv; cb.minvB = l[1].minv + l[3].minv;
 	cb.r1x = l[0].rx + l[2].rx; cb.r1y = l[0].ry + l[2].ry;
 	cb.r2x = l[1].rx + l[3].rx; cb.r2y = l[1].ry + l[3].ry;
-	cb.nx = l[0].nx + l[2].nx; cb.ny = l[0].ny + l[2].ny;
-	cb.nMass = l[0].nMass + l[2].nMass;
-	cb.tMass = l[0].tMass; cb.u = l[0].u;
+	cb.nx = l[0].nx + l[2].nx; cb.ny = l[1].ny + l[3].ny;
+	cb.nMass = l[1].nMass + l[3].nMass;
+	cb.tMass = l[0].tMass; cb.u = l[1].u;
 	cb.bounce = l[0].c0; cb.bias = l[2].c0;
 }

@@ -2044,7 +2044,8 @@ extern "C" int cpg_launch_replay_solve(const cpgSet *s, const cpgAdj *a, int nst
 		cudaFuncSetAttribute(k_replay_solve, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
 		smemSet = smem;
 	}
-	int threads = s->nworlds*nsteps >= 152 ? 128 : 256;
+	/* the forward's (tuned) solve block size */
+	int threads = s->hostSolveThreads > 0 ? s->hostSolveThreads : (s->nworlds*nsteps >= 152 ? 128 : 256);
 	LAUNCH(k_replay_solve<<<dim3(s->nworlds, nsteps), threads, smem, st>>>(*s, *a, stagedMax));
 	return check_launch("k_replay_solve") == cudaSuccess ? 0 : -1;
 }
