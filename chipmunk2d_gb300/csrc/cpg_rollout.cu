@@ -2,13 +2,15 @@
  * cpg_rollout.cu -- recording and reverse pass of the differentiable
  * rollout (reference-order mode, batched worlds).
  *
- * The forward rollout keeps a copy of the whole device set every K steps.
- * The reverse pass restores each checkpoint, replays its K steps with
- * recording on (k_tape_*: positions after integration, pre-step
- * velocities, world geometry, the pre-step rows with their arbiter data,
- * the level structure, and per impulse application the accumulators and
- * velocities the solver saw, written by the solve kernel itself), then
- * runs the K steps in reverse.
+ * The forward rollout records, per segment of K steps, the solver's inputs
+ * (k_tape_*: positions after integration, pre-step velocities, velocities
+ * after integration, world geometry, the pre-step rows with their arbiter
+ * data, the level structure).  The reverse pass recomputes a segment's
+ * solver iterations from them (k_replay_solve, in cpg_kernels.cu), which
+ * writes per impulse application the accumulators and velocities the
+ * solver saw, then runs the segment's steps in reverse.  A segment that
+ * was not recorded is restored from its checkpoint and replayed with the
+ * same recording plus the application records.
  *
  * The reverse of one step (cpSpaceStep.c:335-445) runs in the opposite
  * order of the forward (k_adj_solve per world, k_adj_geom per unit,
@@ -17,8 +19,9 @@
  *      the step seed the contacts' accumulators;
  *   2. the iterations in reverse, levels in reverse (units of one level
  *      touch disjoint dynamic bodies, so they run in parallel without
- *      conflicts), contacts of a unit in reverse (app_adjoint);
- *   3. the warm start (warm_adjoint); the adjoints of the initial
+ *      conflicts), contacts of a unit in reverse, on four or two lanes per
+ *      contact (lane_adj_phase1/2, pair_adj_apply);
+ *   3. the warm start (lane_warm_phase1/2); the adjoints of the initial
  *      accumulators go to the arbiter contacts they were copied from
  *      (cpArbiterUpdate's hash match);
  *   4. velocity integration (damping) and the bias velocities, which the
