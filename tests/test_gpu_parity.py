@@ -219,8 +219,9 @@ def test_graph_replay_and_online_tuning_do_not_change_results(gpu_lib):
     """A many-world batch stepped through its CUDA graph, with the online
     tuner trying launch shapes on the way, ends bit-identical to plain
     launches with the default shapes."""
-    base, t0 = _batch_run(gpu_lib, 160, 40, 0, 0)
-    graph, t1 = _batch_run(gpu_lib, 160, 40, 1, 1)
+    # the first tuning window opens at step 32 and takes 12 steps
+    base, t0 = _batch_run(gpu_lib, 160, 48, 0, 0)
+    graph, t1 = _batch_run(gpu_lib, 160, 48, 1, 1)
     assert t0 == (0, -1)
     assert t1[0] in (64, 128, 256) and t1[1] in (-1, 0)
     for a, b in zip(base, graph):
