@@ -132,13 +132,16 @@ def oracle_lib():
     return bind(so)
 
 
-def cpu_sample(workload, budget_s=15.0, warm=5):
+def cpu_sample(workload, budget_s=15.0, warm=5, hasty=False):
     """Times the CPU restatement on the workload: `warm` untimed steps, then
-    steps until about budget_s seconds of CPU time have been spent."""
+    steps until about budget_s seconds of CPU time have been spent.  With
+    `hasty` the solver runs on two threads as cpHastySpace's does."""
     from chipmunk2d_gb300 import Scene
     cfg, size, dt, _ = WORKLOADS[workload]
     lib = oracle_lib()
     sc = Scene(lib, cfg, size)
+    if hasty:
+        lib.cpx_space_set_hasty(sc.space, 2)
     sc.step(dt, warm)
     steps = 0
     t0 = time.perf_counter()
@@ -222,6 +225,9 @@ def run_reference(args):
     lib = oracle_lib()
     sc = Scene(lib, cfg, size)
     n = sc.nbodies
+    # the reference's threaded space (cpHastySpace) solves on at most two
+    # threads; its restatement in the oracle does the same
+    threads = lib.cpx_space_set_hasty(sc.space, 2)
     sc.step(dt, args.warmup)
     # each timed step is a bounded sample: the whole run stays within minutes
     per_step = []
@@ -241,8 +247,9 @@ def run_reference(args):
         "n_gpus": args.gpus, "steps": k, "warmup": args.warmup, "ms_per_step": 1000 * secs / k,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
         "data": "synthetic", "config": {"workload": workload, "description": desc, "bodies": n},
-        "cpu_baseline": {"value": value, "unit": "body-steps/s", "cores": 1, "kind": "port",
-                         "sample": "%d steps of the %s workload after %d warm-up steps" % (k, workload, args.warmup)},
+        "cpu_baseline": {"value": value, "unit": "body-steps/s", "cores": threads, "kind": "port",
+                         "sample": "%d steps of the %s workload after %d warm-up steps, solver on %d threads as cpHastySpace's"
+                                   % (k, workload, args.warmup, threads)},
         "e2e": {"value": value, "unit": "body-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -843,6 +850,8 @@ def run_ours(args):
             traffic = json.load(f).get(args.workload, {}).get(names[dom])
 
     cpu_v, cpu_steps, cpu_s, _ = cpu_sample(args.workload, budget_s=args.cpu_seconds) if rank == 0 else (None, 0, 0, 0)
+    hv, h_steps, h_s, _ = (cpu_sample(args.workload, budget_s=min(args.cpu_seconds, 8.0), hasty=True)
+                           if rank == 0 else (None, 0, 0, 0))
 
     extras = {}
     if args.extras and rank == 0 and args.workload == "circles":
@@ -890,6 +899,9 @@ def run_ours(args):
         "clocks": clk,
         "cpu_baseline": {"value": cpu_v, "unit": "body-steps/s", "cores": 1, "kind": "port",
                          "sample": "%d steps (%.1f s) of the %s workload after 5 warm-up steps" % (cpu_steps, cpu_s, args.workload)},
+        "cpu_hasty": {"value": hv, "unit": "body-steps/s", "cores": 2, "kind": "port",
+                      "sample": ("cpHastySpace's two-thread solver restated in the oracle, %d steps (%.1f s) after 5 warm-up steps"
+                                 % (h_steps, h_s))},
     }
     line.update(extras)
     if rank == 0:

@@ -146,6 +146,7 @@ _API = {
     "cpx_scene_dump_public": (I, [P, P]),
     "cpx_scene_dump_impulses": (I, [P, P]),
     "cpx_scene_step": (None, [P, D, I]),
+    "cpx_space_set_hasty": (I, [P, I]),
     "cpx_scene_free": (None, [P]),
     "cpx_batch_sizes": (None, [I, ctypes.c_ulonglong, P]),
     # state export (shared record layouts)

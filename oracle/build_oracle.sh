@@ -10,6 +10,6 @@ REPO=$(cd "$HERE/.." && pwd)
 OUT="$HERE/_build"
 mkdir -p "$OUT"
 gcc -std=gnu11 -O2 -fPIC -ffp-contract=off -Wall -Wno-unused-function -shared \
-	-o "$OUT/liboracle.so.tmp" "$HERE/cp_oracle.c" "$REPO/chipmunk2d_gb300/csrc/scenes.c" -lm
+	-o "$OUT/liboracle.so.tmp" "$HERE/cp_oracle.c" "$REPO/chipmunk2d_gb300/csrc/scenes.c" -lm -lpthread
 mv "$OUT/liboracle.so.tmp" "$OUT/liboracle.so"
 echo "$OUT/liboracle.so"

@@ -23,6 +23,7 @@
 #include <stdlib.h>
 #include <string.h>
 #include <stdarg.h>
+#include <pthread.h>
 #include "../include/chipmunk_gb300.h"
 
 #define ORC_INF ((cpFloat)INFINITY)
@@ -223,6 +224,7 @@ struct cpSpace {
 	int *active; int nactive, capactive;   /* space->arbiters: slot indices */
 
 	cpBody staticBody;
+	struct Hasty *hasty;                   /* the threaded solver (cpx_space_set_hasty), or NULL */
 };
 
 /* ========================================================================
@@ -1955,9 +1957,12 @@ cpSpace *cpSpaceNew(void)
 	return sp;
 }
 
+static void hasty_stop(cpSpace *sp);
+
 void cpSpaceFree(cpSpace *sp)
 {
 	if(!sp) return;
+	hasty_stop(sp);
 	free(sp->dyn); free(sp->stat); free(sp->cons);
 	free(sp->nodes); free(sp->pairs);
 	free(sp->dynTree.leaves.bins); free(sp->statTree.leaves.bins);
@@ -2140,6 +2145,103 @@ static void filter_arbiters(cpSpace *sp)
 }
 
 /* cpSpaceStep.c:335-445 */
+/* ========================================================================
+ * The threaded solver of src/cpHastySpace.c:387-548, 471-497, 679-682, for
+ * the CPU baseline only: with two threads each runs half of the
+ * iterations (rounded up) over every arbiter and constraint at the same
+ * time, updating the shared bodies without synchronisation, as the
+ * reference does.  Its results are not deterministic; nothing checks
+ * them.  A persistent worker thread waits on a condition variable between
+ * steps (the reference's WorkerThreadLoop / RunWorkers).
+ * ====================================================================== */
+#define HASTY_THRESHOLD 50
+
+struct Hasty {
+	pthread_t thread;
+	pthread_mutex_t mutex;
+	pthread_cond_t work, done;
+	int pending, quit, started;
+	cpSpace *sp;
+	cpFloat dt;
+};
+
+static void hasty_iterations(cpSpace *sp, cpFloat dt, int iters)
+{
+	for(int it = 0; it < iters; it++){
+		for(int i = 0; i < sp->nactive; i++) arb_apply(&sp->arbs[sp->active[i]]);
+		for(int i = 0; i < sp->ncons; i++) joint_apply(sp->cons[i], dt);
+	}
+}
+
+static void *hasty_worker(void *arg)
+{
+	struct Hasty *h = (struct Hasty *)arg;
+	pthread_mutex_lock(&h->mutex);
+	for(;;){
+		while(!h->pending && !h->quit) pthread_cond_wait(&h->work, &h->mutex);
+		if(h->quit) break;
+		pthread_mutex_unlock(&h->mutex);
+		hasty_iterations(h->sp, h->dt, (h->sp->iterations + 1)/2);
+		pthread_mutex_lock(&h->mutex);
+		h->pending = 0;
+		pthread_cond_signal(&h->done);
+	}
+	pthread_mutex_unlock(&h->mutex);
+	return NULL;
+}
+
+static void hasty_solve(cpSpace *sp, cpFloat dt)
+{
+	struct Hasty *h = sp->hasty;
+	pthread_mutex_lock(&h->mutex);
+	h->dt = dt;
+	h->pending = 1;
+	pthread_cond_signal(&h->work);
+	pthread_mutex_unlock(&h->mutex);
+	hasty_iterations(sp, dt, (sp->iterations + 1)/2);
+	pthread_mutex_lock(&h->mutex);
+	while(h->pending) pthread_cond_wait(&h->done, &h->mutex);
+	pthread_mutex_unlock(&h->mutex);
+}
+
+static void hasty_stop(cpSpace *sp)
+{
+	struct Hasty *h = sp->hasty;
+	if(!h) return;
+	if(h->started){
+		pthread_mutex_lock(&h->mutex);
+		h->quit = 1;
+		pthread_cond_signal(&h->work);
+		pthread_mutex_unlock(&h->mutex);
+		pthread_join(h->thread, NULL);
+	}
+	pthread_mutex_destroy(&h->mutex);
+	pthread_cond_destroy(&h->work);
+	pthread_cond_destroy(&h->done);
+	free(h);
+	sp->hasty = NULL;
+}
+
+/* Test infrastructure: 2 runs the solver on two threads like cpHastySpace
+ * (cpHastySpaceSetThreads caps it at 2), 1 restores the serial solver.
+ * Returns the thread count in effect. */
+int cpx_space_set_hasty(cpSpace *sp, int threads)
+{
+	if(!sp) return 0;
+	if(threads < 2){ hasty_stop(sp); return 1; }
+	if(sp->hasty) return 2;
+	struct Hasty *h = (struct Hasty *)calloc(1, sizeof(struct Hasty));
+	if(!h) return 1;
+	h->sp = sp;
+	pthread_mutex_init(&h->mutex, NULL);
+	pthread_cond_init(&h->work, NULL);
+	pthread_cond_init(&h->done, NULL);
+	sp->hasty = h;
+	if(pthread_create(&h->thread, NULL, hasty_worker, h) != 0){ hasty_stop(sp); return 1; }
+	h->started = 1;
+	return 2;
+}
+
 void cpSpaceStep(cpSpace *sp, cpFloat dt)
 {
 	if(dt == 0.0) return;
@@ -2187,7 +2289,8 @@ void cpSpaceStep(cpSpace *sp, cpFloat dt)
 	for(int i = 0; i < sp->nactive; i++) arb_apply_cached(&sp->arbs[sp->active[i]], dt_coef);
 	for(int i = 0; i < sp->ncons; i++) joint_apply_cached(sp->cons[i], dt_coef);
 
-	for(int it = 0; it < sp->iterations; it++){
+	if(sp->hasty && sp->nactive + sp->ncons > HASTY_THRESHOLD) hasty_solve(sp, dt);
+	else for(int it = 0; it < sp->iterations; it++){
 		for(int i = 0; i < sp->nactive; i++) arb_apply(&sp->arbs[sp->active[i]]);
 		for(int i = 0; i < sp->ncons; i++) joint_apply(sp->cons[i], dt);
 	}
