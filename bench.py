@@ -723,8 +723,8 @@ def mode_sample(lib, workload, steps, warmup, mode=0, phases=False):
 
 def parity_mode_sample(lib, workload, steps, warmup):
     """The exact reference-order mode, for the `ordered_mode` record."""
-    rec = mode_sample(lib, workload, steps, warmup, mode=0)
-    return {k: rec[k] for k in ("workload", "bodies", "steps", "body_steps_per_s", "ms_per_step")}
+    rec = mode_sample(lib, workload, steps, warmup, mode=0, phases=True)
+    return {k: rec[k] for k in ("workload", "bodies", "steps", "body_steps_per_s", "ms_per_step", "phase_ms")}
 
 
 def run_ours(args):
