@@ -173,6 +173,7 @@ _GPU_API = {
     "cpGpuSetAutotune": (None, [I]),
     "cpGpuRolloutForward": (I, [P, D, I, I]),
     "cpGpuRolloutBackward": (I, [P, P, P, P, P, P, P]),
+    "cpGpuRolloutBackwardFull": (I, [P] * 12),
     "cpGpuDebugRolloutTimes": (I, [P, P]),
     "cpGpuDebugSetRolloutRecording": (None, [I]),
     "cpGpuDebugBodies": (I, [P, P, I]),

@@ -1403,8 +1403,14 @@ static int seg_replay(DevSet *ds, Rollout *r, int seg, int len, const double *dt
 
 int cpGpuRolloutBackward(cpGpuBatch *b, const cpFloat *dLdp, cpFloat *dLdv0, cpFloat *dLdw0, cpFloat *dLdm, cpFloat *dLde, cpFloat *dLdu)
 {
-	if(!b || !b->dev || !b->roll || !b->roll->segs){ set_error(CP_GPU_ERR_ARGUMENT, "rollout: no forward rollout to reverse"); return -1; }
 	if(!dLdp){ set_error(CP_GPU_ERR_ARGUMENT, "rollout: dLdp is required"); return -1; }
+	return cpGpuRolloutBackwardFull(b, dLdp, NULL, NULL, NULL, NULL, NULL, dLdv0, dLdw0, dLdm, dLde, dLdu);
+}
+
+int cpGpuRolloutBackwardFull(cpGpuBatch *b, const cpFloat *dLdp, const cpFloat *dLda, const cpFloat *dLdv, const cpFloat *dLdw,
+	cpFloat *dLdp0, cpFloat *dLda0, cpFloat *dLdv0, cpFloat *dLdw0, cpFloat *dLdm, cpFloat *dLde, cpFloat *dLdu)
+{
+	if(!b || !b->dev || !b->roll || !b->roll->segs){ set_error(CP_GPU_ERR_ARGUMENT, "rollout: no forward rollout to reverse"); return -1; }
 	DevSet *ds = b->dev;
 	cpgSet *d = &ds->d;
 	Rollout *r = b->roll;
@@ -1442,7 +1448,8 @@ int cpGpuRolloutBackward(cpGpuBatch *b, const cpFloat *dLdp, cpFloat *dLdv0, cpF
 	double *h = NULL;
 	if(!adj_ensure(d, &r->adj, K, segRows, stepRows, iters, 0)) goto done;
 
-	/* seeds: dL/dp at the end, nothing else */
+	/* seeds: the loss's gradient with respect to the final state (absent
+	 * arrays are zero); the bias velocities end every step at zero */
 	{
 		cpgAdj *A = &r->adj.a;
 		size_t nbd = 9*(size_t)d->totalBodies;
@@ -1452,7 +1459,10 @@ int cpGpuRolloutBackward(cpGpuBatch *b, const cpFloat *dLdp, cpFloat *dLdv0, cpF
 			cpSpace *sp = ds->spaces[w];
 			for(int i = 0; i < sp->ndyn; i++, idx++){
 				size_t g = (size_t)ds->hworld[w].bodyOff + i;
-				h[9*g] = dLdp[2*idx]; h[9*g + 1] = dLdp[2*idx + 1];
+				if(dLdp){ h[9*g] = dLdp[2*idx]; h[9*g + 1] = dLdp[2*idx + 1]; }
+				if(dLda) h[9*g + 2] = dLda[idx];
+				if(dLdv){ h[9*g + 3] = dLdv[2*idx]; h[9*g + 4] = dLdv[2*idx + 1]; }
+				if(dLdw) h[9*g + 5] = dLdw[idx];
 			}
 		}
 		cuda_ok(cudaMemcpyAsync(A->body, h, sizeof(double)*nbd, cudaMemcpyHostToDevice, st), "seed");
@@ -1540,6 +1550,8 @@ int cpGpuRolloutBackward(cpGpuBatch *b, const cpFloat *dLdp, cpFloat *dLdv0, cpF
 				cpSpace *sp = ds->spaces[w];
 				for(int i = 0; i < sp->ndyn; i++, idx++){
 					size_t g = (size_t)ds->hworld[w].bodyOff + i;
+					if(dLdp0){ dLdp0[2*idx] = h[9*g]; dLdp0[2*idx + 1] = h[9*g + 1]; }
+					if(dLda0) dLda0[idx] = h[9*g + 2];
 					if(dLdv0){ dLdv0[2*idx] = h[9*g + 3]; dLdv0[2*idx + 1] = h[9*g + 4]; }
 					if(dLdw0) dLdw0[idx] = h[9*g + 5];
 					if(dLdm) dLdm[idx] = -gm[g]*minv[g]*minv[g];

@@ -523,6 +523,16 @@ int cpGpuDebugCandidates(cpSpace *space, int *out, int max);
 int cpGpuRolloutForward(cpGpuBatch *batch, cpFloat dt, int steps, int checkpoint);
 int cpGpuRolloutBackward(cpGpuBatch *batch, const cpFloat *dLdp, cpFloat *dLdv0, cpFloat *dLdw0,
 	cpFloat *dLdm, cpFloat *dLde, cpFloat *dLdu);
+/* The general form: the loss's gradient with respect to the final
+ * positions (dLdp, 2 per dynamic body), angles (dLda, 1), velocities
+ * (dLdv, 2) and angular velocities (dLdw, 1) in; its gradient with respect
+ * to the initial positions (dLdp0), angles (dLda0), velocities (dLdv0),
+ * angular velocities (dLdw0), masses (dLdm) and each shape's elasticity
+ * and friction (dLde, dLdu) out.  Any pointer may be NULL (an absent seed
+ * is zero).  cpGpuRolloutBackward(b, dLdp, ...) is this call with only the
+ * position seed. */
+int cpGpuRolloutBackwardFull(cpGpuBatch *batch, const cpFloat *dLdp, const cpFloat *dLda, const cpFloat *dLdv, const cpFloat *dLdw,
+	cpFloat *dLdp0, cpFloat *dLda0, cpFloat *dLdv0, cpFloat *dLdw0, cpFloat *dLdm, cpFloat *dLde, cpFloat *dLdu);
 /* Debug: [0], [1] device milliseconds of the last cpGpuRolloutBackward
  * taken with cpGpuSetTiming(1) (replays with recording, reverse steps);
  * [2] bytes of the segment tape, [3] bytes of the checkpoints.  Returns the

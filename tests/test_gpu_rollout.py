@@ -251,3 +251,92 @@ def test_gradients_match_oracle_finite_differences(gpu_lib, oracle_lib):
             assert abs(adj - fd) <= 1e-4 * max(abs(fd), 1.0), (p.kind, adj, fd)
     finally:
         WORLDS = saved
+
+
+CV, CA = 0.5, 100.0
+
+
+def full_loss(scenes, t):
+    b = np.concatenate([sc.bodies() for sc in scenes])
+    p, v, a = b[:, 0:2], b[:, 2:4], b[:, 4]
+    return float(np.sum((p - t) ** 2) + CV*np.sum(v ** 2) + CA*np.sum(a ** 2))
+
+
+def apply_pose(lib, scenes, kind, world, index, comp, h):
+    body = lib.cpx_scene_body(scenes[world].h, index)
+    if kind == "p":
+        q = lib.cpBodyGetPosition(body)
+        lib.cpBodySetPosition(body, cpVect(q.x + (h if comp == 0 else 0.0), q.y + (h if comp == 1 else 0.0)))
+    elif kind == "a":
+        lib.cpBodySetAngle(body, lib.cpBodyGetAngle(body) + h)
+    else:
+        Param(kind, world, index, comp).apply(lib, scenes, h)
+
+
+def gpu_full_loss(lib, seeds, steps, t, p=None, h=0.0):
+    scenes = make(lib, seeds)
+    if p is not None:
+        apply_pose(lib, scenes, *p, h)
+    batch = lib.cpGpuBatchNew()
+    for sc in scenes:
+        lib.cpGpuBatchAddSpace(batch, sc.space)
+    assert lib.cpGpuBatchStep(batch, DT, steps, 0) == 0
+    L = full_loss(scenes, t)
+    lib.cpGpuBatchFree(batch)
+    for sc in scenes:
+        sc.free()
+    return L
+
+
+def test_full_gradients_match_gpu_finite_differences(gpu_lib):
+    """cpGpuRolloutBackwardFull with seeds on the final positions, angles and
+    velocities (L = sum |p - t|^2 + 0.5 |v|^2 + 100 a^2): the gradients with
+    respect to the initial positions, angles, velocities and angular
+    velocities agree with central differences of the GPU forward, with the
+    same screening as the position-only test."""
+    seeds = [4000 + i for i in range(WORLDS)]
+    t = targets(WORLDS * SIZE)
+    scenes = make(gpu_lib, seeds)
+    batch = gpu_lib.cpGpuBatchNew()
+    for sc in scenes:
+        gpu_lib.cpGpuBatchAddSpace(batch, sc.space)
+    assert gpu_lib.cpGpuRolloutForward(batch, DT, STEPS, 16) == 0, gpu_lib.cpGpuGetLastErrorString()
+    L0 = full_loss(scenes, t)
+    b = np.concatenate([sc.bodies() for sc in scenes])
+    n = len(b)
+    sp = np.ascontiguousarray(2.0 * (b[:, 0:2] - t)).ravel()
+    sv = np.ascontiguousarray(2.0 * CV * b[:, 2:4]).ravel()
+    sa = np.ascontiguousarray(2.0 * CA * b[:, 4])
+    g = {k: np.zeros(s) for k, s in (("p", 2 * n), ("a", n), ("v", 2 * n), ("w", n))}
+    rc = gpu_lib.cpGpuRolloutBackwardFull(batch, sp.ctypes.data, sa.ctypes.data, sv.ctypes.data, None,
+                                          g["p"].ctypes.data, g["a"].ctypes.data, g["v"].ctypes.data, g["w"].ctypes.data,
+                                          None, None, None)
+    assert rc == 0, gpu_lib.cpGpuGetLastErrorString()
+    gpu_lib.cpGpuBatchFree(batch)
+    for sc in scenes:
+        sc.free()
+    assert gpu_full_loss(gpu_lib, seeds, STEPS, t) == L0
+    rng = np.random.default_rng(23)
+    params = [(k, int(rng.integers(WORLDS)), int(rng.integers(SIZE)), int(rng.integers(2)))
+              for k in ["p"] * 10 + ["a"] * 8 + ["v"] * 6 + ["w"] * 6]
+    smooth, resolved, bad = 0, 0, []
+    for kind, w, i, c in params:
+        fd = [(gpu_full_loss(gpu_lib, seeds, STEPS, t, (kind, w, i, c), h) -
+               gpu_full_loss(gpu_lib, seeds, STEPS, t, (kind, w, i, c), -h)) / (2 * h) for h in (1e-6, 1e-7)]
+        k = w * SIZE + i
+        adj = g[kind][2 * k + c] if kind in ("p", "v") else g[kind][k]
+        u = abs(fd[0] - fd[1])
+        kink = u > 1e-2 * abs(fd[0])
+        print("%s w%d i%d c%d adjoint %+.10e fd %+.10e %+.10e%s" % (kind, w, i, c, adj, fd[0], fd[1], "  (contact event)" if kink else ""))
+        if kink:
+            continue
+        smooth += 1
+        if abs(adj - fd[0]) > max(1e-6 * abs(fd[0]), u):
+            bad.append((kind, w, i, c, adj, fd[0], fd[1]))
+        if u <= 1e-6 * abs(fd[0]) and fd[0] != 0.0:
+            resolved += 1
+            if abs(adj - fd[0]) > 1e-6 * abs(fd[0]):
+                bad.append(("resolved", kind, w, i, c, adj, fd[0], fd[1]))
+    assert smooth >= 0.7 * len(params), smooth
+    assert resolved >= 4, resolved
+    assert not bad, bad
