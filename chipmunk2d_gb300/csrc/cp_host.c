@@ -1081,7 +1081,7 @@ int cpGpuBatchGetTuning(cpGpuBatch *b, int *out)
 
 int cpGpuBatchStep(cpGpuBatch *b, cpFloat dt, int steps, int use_graph)
 {
-	if(!b || b->n == 0) return -1;
+	if(!b || b->n <= 0) return -1;
 	for(int i = 0; i < b->n; i++) if(!space_supported(b->spaces[i])) return -1;
 	if(!b->dev){
 		b->dev = devset_build(b->spaces, b->n);

@@ -21,7 +21,6 @@
 __device__ void schedule_levels(const int *bodyA, const int *bodyB, int nunits, int nbodies,
                                 int *last, int *level, int *levelStart, int *order, int *nlevels)
 {
-	__shared__ int nlev;
 	for(int b = threadIdx.x; b < nbodies; b += blockDim.x) last[b] = 0;
 	__syncthreads();
 	if(threadIdx.x == 0){
@@ -38,7 +37,6 @@ __device__ void schedule_levels(const int *bodyA, const int *bodyB, int nunits, 
 			if(b >= 0) last[b] = l + 1;
 			if(l + 1 > maxl) maxl = l + 1;
 		}
-		nlev = maxl;
 		for(int l = 0; l <= maxl; l++) levelStart[l] = 0;
 		for(int u = 0; u < nunits; u++) levelStart[level[u] + 1]++;
 		for(int l = 0; l < maxl; l++) levelStart[l + 1] += levelStart[l];
