@@ -832,15 +832,19 @@ def run_ours(args):
     names = PHASES
     dom = int(np.argmax(phase))
     iters = 10 if cfg != 3 else 15
-    algo = {
+    algo_all = {
         0: n * (BYTES_PER_BODY_POS + BYTES_PER_CIRCLE_CACHE),
-        1: 32 * sc.nshapes,
+        1: 32 * sc.nshapes + 8 * contacts,
         2: contacts * (24 * 2 + 4 + 16 + 40 + 8),
         3: contacts * 104,
         4: 16 * len(arbs),
         5: contacts * BYTES_PER_CONTACT_PRESTEP + n * BYTES_PER_BODY_VEL,
         6: contacts * BYTES_PER_CONTACT_ITER * (iters + 1),
-    }[dom]
+    }
+    algo = algo_all[dom]
+    # achieved HBM GB/s of every phase (algorithmic bytes / event-timed duration)
+    phase_gbs = {names[i]: round(algo_all[i] / (phase[i] / 1000.0) / 1e9, 2) if phase[i] > 0 else None
+                 for i in range(len(names))}
     peak, peak_kind = measured_peaks()
     achieved = algo / (phase[dom] / 1000.0) / 1e9 if phase[dom] > 0 else 0.0
     traffic = None
@@ -894,6 +898,7 @@ def run_ours(args):
                                  "chain per colour level; rows and bodies stay L2-resident" if names[dom] == "solve"
                                  else "latency-bound gather")},
         "phase_ms": dict(zip(names, [round(float(x), 4) for x in phase])),
+        "phase_achieved_gbs": phase_gbs,
         "sweep_levels_final": sweep_levels,
         "gpu_launches": int(launches),
         "clocks": clk,
