@@ -1676,6 +1676,8 @@ __device__ __forceinline__ unsigned long long unit_priority(int key)
 #define CPG_COLOR_ROUNDS 128
 /* every this many steps all units are coloured afresh */
 #define CPG_RECOLOR_PERIOD 64
+/* passes that try to empty the highest colour */
+#define CPG_COLOR_SQUEEZE 4
 
 /* Colour tag kept in an arbiter's or joint's colorTag word: valid bit, the low
  * 23 bits of the stamp of the step that coloured it, the colour (< 64). */
@@ -1714,7 +1716,7 @@ __global__ void k_color_coop(cpgSet s, int w)
 	bool reuse = (P.stamp % CPG_RECOLOR_PERIOD) != 0;
 	unsigned prevTag = color_tag(P.stamp - 1u, 0);
 	for(int b = gtid; b < nb; b += gsz){ cmask[b] = 0ull; claim[b] = ~0ull; }
-	if(gtid == 0){ counter[0] = 0; counter[1] = 0; }
+	if(gtid == 0){ counter[0] = 0; counter[1] = 0; counter[4] = -1; counter[5] = 0; counter[6] = -1; counter[7] = 0; }
 	grid.sync();
 	for(int u = gtid; u < n; u += gsz){
 		int c = -1;
@@ -1765,6 +1767,49 @@ __global__ void k_color_coop(cpgSet s, int w)
 		if(gtid == 0) counter[(round + 1) & 1] = 0;
 		grid.sync();
 		if(__ldcg(&counter[round & 1]) == 0) break;
+	}
+	/* fewer colours, so fewer levels: every unit of the highest colour moves
+	 * to the lowest colour free on both of its bodies.  Units of one colour
+	 * share no body, so they move at once without conflicts and the
+	 * colouring stays proper; the passes go on while the highest colour
+	 * empties (the counters alternate between two pairs of slots, one
+	 * reset while the other is in use).  A colouring of units that conflict
+	 * through a shared body is an edge colouring of the body graph, so it
+	 * needs at least the most units on one body; on dense piles the greedy
+	 * colouring is already there and nothing moves. */
+	int lane = threadIdx.x & 31;
+	/* only when every unit was coloured afresh: kept colours keep the
+	 * result of the last squeeze */
+	for(int pass = 0; pass < (reuse ? 0 : CPG_COLOR_SQUEEZE); pass++){
+		int slot = 4 + 2*(pass & 1);
+		int mx = -1;
+		for(int u = gtid; u < n; u += gsz){ int c = color[u]; if(c < 64 && c > mx) mx = c; }
+		mx = __reduce_max_sync(0xffffffffu, mx);
+		if(lane == 0 && mx >= 0) atomicMax(&counter[slot], mx);
+		if(gtid == 0){ counter[slot ^ 2] = -1; counter[(slot ^ 2) + 1] = 0; }
+		grid.sync();
+		int top = __ldcg(&counter[slot]);
+		if(top <= 0) break;
+		unsigned long long lower = (1ull << top) - 1ull, topBit = 1ull << top;
+		int stuck = 0;
+		for(int u = gtid; u < n; u += gsz){
+			if(color[u] != top) continue;
+			int a = ua[u], b = ub[u];
+			unsigned long long m = (a >= 0 ? __ldcg(&cmask[a]) : 0ull) | (b >= 0 ? __ldcg(&cmask[b]) : 0ull);
+			unsigned long long fr = ~m & lower;
+			if(fr){
+				int c = __ffsll((long long)fr) - 1;
+				color[u] = c;
+				if(a >= 0) cmask[a] = (__ldcg(&cmask[a]) & ~topBit) | (1ull << c);
+				if(b >= 0) cmask[b] = (__ldcg(&cmask[b]) & ~topBit) | (1ull << c);
+			} else {
+				stuck++;
+			}
+		}
+		stuck = __reduce_add_sync(0xffffffffu, stuck);
+		if(lane == 0 && stuck) atomicAdd(&counter[slot + 1], stuck);
+		grid.sync();
+		if(__ldcg(&counter[slot + 1]) > 0) break;
 	}
 	/* counting sort by colour: colours past 63 come only from exhausted
 	 * masks (64 + round), 255 marks a unit the rounds left uncoloured */
