@@ -238,6 +238,8 @@ struct DevSet {
 	void *scratch;            /* per-step scratch outside the slab (not checkpointed) */
 	cpgArb *gather;           /* arbiter snapshot staging */
 	int gatherCap;
+	int structStale;          /* the staging block holds body state the body structs do not have yet */
+	size_t hstride;           /* doubles between two arrays of the staging block */
 	void *graph;              /* the step's launches as a CUDA graph (cpgStepGraph) */
 	int useGraph;             /* this call's steps replay the graph */
 	long long stepCount;      /* steps launched */
@@ -434,7 +436,9 @@ static int upload_bodies(DevSet *ds, int w)
 	return ok;
 }
 
-static void download_bodies(DevSet *ds)
+/* The bodies' device state into the pinned staging block.  Returns 0 when
+ * it could not be brought. */
+static int download_bodies_raw(DevSet *ds)
 {
 	cpgSet *d = &ds->d;
 	int NB = d->totalBodies;
@@ -443,18 +447,26 @@ static void download_bodies(DevSet *ds)
 	size_t stride = (size_t)(d->py - d->px);
 	size_t bytes = (size_t)((char *)(d->wb + NB) - (char *)d->px);
 	if(!ds->hbodies){
-		if(!cuda_ok(cudaMallocHost((void **)&ds->hbodies, 18*stride*sizeof(double)), "cudaMallocHost")){ ds->hbodies = NULL; return; }
+		if(!cuda_ok(cudaMallocHost((void **)&ds->hbodies, 18*stride*sizeof(double)), "cudaMallocHost")){ ds->hbodies = NULL; return 0; }
 	}
+	ds->hstride = stride;
 	const double *src[18] = { d->px, d->py, d->vx, d->vy, d->fx, d->fy, d->ang, d->w, d->tq,
 		d->ta, d->tb, d->tc, d->td, d->ttx, d->tty, d->vbx, d->vby, d->wb };
 	int contiguous = 1;
 	for(int k = 0; k < 18; k++) contiguous &= (src[k] == d->px + (size_t)k*stride);
 	if(contiguous){
-		if(!d2h(ds->hbodies, d->px, bytes)) return;
+		if(!d2h(ds->hbodies, d->px, bytes)) return 0;
 	} else {
-		for(int k = 0; k < 18; k++) if(!d2h(ds->hbodies + (size_t)k*stride, src[k], sizeof(double)*(size_t)NB)) return;
+		for(int k = 0; k < 18; k++) if(!d2h(ds->hbodies + (size_t)k*stride, src[k], sizeof(double)*(size_t)NB)) return 0;
 	}
-	cuda_ok(cudaStreamSynchronize(lib_stream()), "download bodies");
+	return cuda_ok(cudaStreamSynchronize(lib_stream()), "download bodies");
+}
+
+/* The staging block into the dynamic bodies' structs. */
+static void unpack_bodies(DevSet *ds)
+{
+	if(!ds->hbodies) return;
+	size_t stride = ds->hstride;
 	const double *f[18];
 	for(int k = 0; k < 18; k++) f[k] = ds->hbodies + (size_t)k*stride;
 	for(int w = 0; w < ds->nspaces; w++){
@@ -783,16 +795,31 @@ static DevSet *devset_build(cpSpace **spaces, int nspaces)
 static void check_stats(DevSet *ds);
 
 /* Make host copies of the space's body state current. */
-static void space_pull(cpSpace *sp)
+/* After a step: the device's body state into the staging block (the body
+ * structs are unpacked from it only when something needs them). */
+static void space_download(cpSpace *sp)
 {
 	if(!sp || !sp->dev || !sp->hostStale) return;
 	DevSet *ds = sp->dev;
 	check_stats(ds);
-	download_bodies(ds);
+	if(!download_bodies_raw(ds)) return;
 	for(int w = 0; w < ds->nspaces; w++){
 		cpSpace *o = ds->spaces[w];
 		o->hostStale = 0;
 		o->snapValid = 0;
+	}
+	ds->structStale = 1;
+}
+
+/* The bodies' current state into their structs. */
+static void space_pull(cpSpace *sp)
+{
+	if(!sp || !sp->dev) return;
+	space_download(sp);
+	DevSet *ds = sp->dev;
+	if(ds->structStale){
+		unpack_bodies(ds);
+		ds->structStale = 0;
 	}
 }
 
@@ -2230,6 +2257,8 @@ void cpSpaceFree(cpSpace *sp)
 {
 	if(!sp) return;
 	if(sp->dev && sp->ownsDev){
+		/* the bodies outlive the space: they keep its last step's state */
+		space_pull(sp);
 		cudaStreamSynchronize(lib_stream());
 		devset_free(sp->dev);
 	}
