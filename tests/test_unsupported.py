@@ -1,0 +1,72 @@
+"""Features the GPU step does not run are refused, not run elsewhere: the
+step reports CP_GPU_ERR_UNSUPPORTED through cpGpuGetLastError and leaves
+the space unstepped (no CPU fallback).  The checks happen on the host
+before any device work, so these run without a GPU."""
+import ctypes
+import os
+
+import pytest
+
+from chipmunk2d_gb300 import cpVect
+from chipmunk2d_gb300._lib import LIB_PATH, bind
+
+CP_GPU_ERR_UNSUPPORTED = 3
+
+P, D = ctypes.c_void_p, ctypes.c_double
+VELOCITY_FUNC = ctypes.CFUNCTYPE(None, P, cpVect, D, D)
+PRESOLVE_FUNC = ctypes.CFUNCTYPE(None, P, P)
+
+
+@pytest.fixture(scope="module")
+def lib():
+    if not os.path.exists(LIB_PATH):
+        from chipmunk2d_gb300.build import build
+        build()
+    lib = bind(LIB_PATH, gpu=True)
+    lib.cpSpaceSetSleepTimeThreshold.argtypes = [P, D]
+    lib.cpBodySetVelocityUpdateFunc.argtypes = [P, VELOCITY_FUNC]
+    lib.cpConstraintSetPreSolveFunc.argtypes = [P, PRESOLVE_FUNC]
+    return lib
+
+
+def one_body_space(lib):
+    sp = lib.cpSpaceNew()
+    lib.cpSpaceSetGravity(sp, cpVect(0, -100))
+    b = lib.cpSpaceAddBody(sp, lib.cpBodyNew(1.0, 1.0))
+    return sp, b
+
+
+def refused(lib, sp, b):
+    lib.cpGpuGetLastError()                          # clear
+    p0 = lib.cpBodyGetPosition(b)
+    lib.cpSpaceStep(sp, 1 / 60)
+    err = lib.cpGpuGetLastError()
+    p1 = lib.cpBodyGetPosition(b)
+    return err, (p0.x, p0.y) == (p1.x, p1.y)
+
+
+def test_sleeping_is_refused(lib):
+    sp, b = one_body_space(lib)
+    lib.cpSpaceSetSleepTimeThreshold(sp, 0.5)
+    err, unmoved = refused(lib, sp, b)
+    assert err == CP_GPU_ERR_UNSUPPORTED and unmoved
+    lib.cpSpaceFree(sp); lib.cpBodyFree(b)
+
+
+def test_custom_velocity_integration_is_refused(lib):
+    sp, b = one_body_space(lib)
+    cb = VELOCITY_FUNC(lambda body, g, damping, dt: None)
+    lib.cpBodySetVelocityUpdateFunc(b, cb)
+    err, unmoved = refused(lib, sp, b)
+    assert err == CP_GPU_ERR_UNSUPPORTED and unmoved
+    lib.cpSpaceFree(sp); lib.cpBodyFree(b)
+
+
+def test_constraint_callbacks_are_refused(lib):
+    sp, b = one_body_space(lib)
+    c = lib.cpSpaceAddConstraint(sp, lib.cpPivotJointNew(lib.cpSpaceGetStaticBody(sp), b, cpVect(0, 0)))
+    cb = PRESOLVE_FUNC(lambda con, space: None)
+    lib.cpConstraintSetPreSolveFunc(c, cb)
+    err, unmoved = refused(lib, sp, b)
+    assert err == CP_GPU_ERR_UNSUPPORTED and unmoved
+    lib.cpSpaceFree(sp); lib.cpConstraintFree(c); lib.cpBodyFree(b)
