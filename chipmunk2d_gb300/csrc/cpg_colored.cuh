@@ -35,40 +35,41 @@ __device__ __forceinline__ unsigned float_order_key(float f)
 	return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
 }
 
-/* Exclusive scan of `n` counts by one block. */
+/* Exclusive scan of `n` counts by one block.  Each thread takes a
+ * contiguous run of ceil(n / blockDim) counts: it sums them, the block
+ * scans the per-thread sums once, and the thread writes its run's
+ * prefixes.  Two block barriers in all, whatever n. */
 __global__ void k_scan_excl(unsigned *data, int n, unsigned *total)
 {
 	__shared__ unsigned warpSums[32];
-	__shared__ unsigned carry;
-	if(threadIdx.x == 0) carry = 0;
-	__syncthreads();
-	int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
-	for(int c0 = 0; c0 < n; c0 += blockDim.x){
-		int i = c0 + threadIdx.x;
-		unsigned v = (i < n) ? data[i] : 0u;
-		unsigned x = v;
-		for(int o = 1; o < 32; o <<= 1){
-			unsigned y = __shfl_up_sync(0xffffffffu, x, o);
-			if(lane >= o) x += y;
-		}
-		if(lane == 31) warpSums[warp] = x;
-		__syncthreads();
-		if(warp == 0){
-			unsigned s = (lane < nwarps) ? warpSums[lane] : 0u;
-			for(int o = 1; o < 32; o <<= 1){
-				unsigned y = __shfl_up_sync(0xffffffffu, s, o);
-				if(lane >= o) s += y;
-			}
-			if(lane < nwarps) warpSums[lane] = s;
-		}
-		__syncthreads();
-		unsigned warpPrefix = (warp > 0) ? warpSums[warp - 1] : 0u;
-		if(i < n) data[i] = carry + warpPrefix + x - v;
-		__syncthreads();
-		if(threadIdx.x == 0) carry += warpSums[nwarps - 1];
-		__syncthreads();
+	int t = threadIdx.x, lane = t & 31, warp = t >> 5, nwarps = blockDim.x >> 5;
+	int per = (n + (int)blockDim.x - 1)/(int)blockDim.x;
+	int i0 = min(n, t*per), i1 = min(n, i0 + per);
+	unsigned sum = 0;
+	for(int i = i0; i < i1; i++) sum += data[i];
+	unsigned x = sum;
+	for(int o = 1; o < 32; o <<= 1){
+		unsigned y = __shfl_up_sync(0xffffffffu, x, o);
+		if(lane >= o) x += y;
 	}
-	if(threadIdx.x == 0 && total) *total = carry;
+	if(lane == 31) warpSums[warp] = x;
+	__syncthreads();
+	if(warp == 0){
+		unsigned s = (lane < nwarps) ? warpSums[lane] : 0u;
+		for(int o = 1; o < 32; o <<= 1){
+			unsigned y = __shfl_up_sync(0xffffffffu, s, o);
+			if(lane >= o) s += y;
+		}
+		if(lane < nwarps) warpSums[lane] = s;
+	}
+	__syncthreads();
+	unsigned run = ((warp > 0) ? warpSums[warp - 1] : 0u) + x - sum;
+	for(int i = i0; i < i1; i++){
+		unsigned v = data[i];
+		data[i] = run;
+		run += v;
+	}
+	if(t == (int)blockDim.x - 1 && total) *total = run;
 }
 
 /* ---- sweep-and-prune ----

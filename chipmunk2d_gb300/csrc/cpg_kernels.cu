@@ -861,14 +861,14 @@ __device__ __forceinline__ void row_apply(cpgRow &row, BodyRef &A, BodyRef &B, d
 			double vrt = vrx*(-ny) + vry*nx;
 			double jbn = (con.bias - vbn)*nMass;
 			double jbnOld = con.jBias;
-			con.jBias = dmax(jbnOld + jbn, 0.0);
+			con.jBias = dmax0(jbnOld + jbn);
 			double jn = -(con.bounce + vrn)*nMass;
 			double jnOld = con.jnAcc;
-			con.jnAcc = dmax(jnOld + jn, 0.0);
+			con.jnAcc = dmax0(jnOld + jn);
 			double jtMax = friction*con.jnAcc;
 			double jt = -vrt*con.tMass;
 			double jtOld = con.jtAcc;
-			con.jtAcc = dclamp(jtOld + jt, -jtMax, jtMax);
+			con.jtAcc = dclamp_sym(jtOld + jt, jtMax);
 			double db = con.jBias - jbnOld;
 			double bx = nx*db, by = ny*db;
 			apply_bias_impulse(A, -bx, -by, r1x, r1y);
@@ -895,7 +895,7 @@ __device__ __forceinline__ void row_apply(cpgRow &row, BodyRef &A, BodyRef &B, d
 		double jnMax = row.jnt.maxForce*dt;
 		double jn = (row.jnt.bias - vrn)*row.jnt.nMass;
 		double jnOld = row.jnt.jnAcc;
-		row.jnt.jnAcc = dclamp(jnOld + jn, -jnMax, jnMax);
+		row.jnt.jnAcc = dclamp_sym(jnOld + jn, jnMax);
 		jn = row.jnt.jnAcc - jnOld;
 		apply_impulses(A, B, row.jnt.r1x, row.jnt.r1y, row.jnt.r2x, row.jnt.r2y, row.jnt.nx*jn, row.jnt.ny*jn);
 	} else {
@@ -934,8 +934,10 @@ __device__ __forceinline__ void solve_row(cpgRow *rows, int k, double *bodies, i
  *
  * Why: FP64 issue is one warp instruction per 64 cycles per SM
  * sub-partition whatever the number of active lanes, so a sweep level
- * costs its FP64 instruction count per warp: about 40 per contact here
- * against about 90 with one lane per unit.  Joint rows run on lane 0. */
+ * costs its FP64 instruction count per warp: about 37 per contact here
+ * against about 90 with one lane per unit.  The clamps of the accumulated
+ * impulses are integer compares on the bit patterns (dmax0, dclamp_sym),
+ * not FP64 ones.  Joint rows run on lane 0. */
 struct QuadRow {
 	int body, flags, kind, count;
 	double nx, ny, u, svx, svy;
@@ -970,8 +972,9 @@ __device__ __forceinline__ void quad_load(QuadRow &q, const cpgRow &row, int lan
 /* Warm start (pass 0: cpArbiter.c:441-455) or one iteration of a contact
  * row held in registers; accumulators go back to *row.  FUSED (coloured
  * mode, whose sweep order already differs from the reference's) contracts
- * the multiply-adds of an iteration: 32 FP64 instructions per contact
- * instead of 40.  Without it every operation is the reference's. */
+ * the multiply-adds of an iteration, the accumulations of the normal and
+ * friction impulses included: about 25 FP64 instructions per contact
+ * instead of 37.  Without it every operation is the reference's. */
 template<bool CG, bool FUSED>
 __device__ __forceinline__ void quad_apply(const QuadRow &q, cpgRow *row, double *bodies, int pass, double dt_coef, unsigned qmask, int lane4,
 	AdjApp *rec = nullptr)
@@ -1016,14 +1019,19 @@ __device__ __forceinline__ void quad_apply(const QuadRow &q, cpgRow *row, double
 			else { vn = vrx*nx + vry*ny; vt = vrx*(-ny) + vry*nx; }
 			/* velocity: jn = -(bounce + vrn)*nMass; bias: jbn = (bias - vbn)*nMass */
 			double y = q.c[k] + dneg_if(vn, bias);
-			double j = dneg_if(y, !bias)*q.nMass[k];
-			double old = q.acc[k];
-			double acc = dmax(old + j, 0.0);
-			/* friction (used by the velocity lanes only) */
-			double jtMax = q.u*acc;
-			double jt = -vt*q.tMass[k];
-			double jtOld = q.jt[k];
-			double jtAcc = dclamp(jtOld + jt, -jtMax, jtMax);
+			double old = q.acc[k], jtOld = q.jt[k];
+			double acc, jtAcc;
+			if(FUSED){
+				acc = dmax0(__fma_rn(dneg_if(y, !bias), q.nMass[k], old));
+				jtAcc = dclamp_sym(__fma_rn(-vt, q.tMass[k], jtOld), q.u*acc);
+			} else {
+				double j = dneg_if(y, !bias)*q.nMass[k];
+				acc = dmax0(old + j);
+				/* friction (used by the velocity lanes only) */
+				double jtMax = q.u*acc;
+				double jt = -vt*q.tMass[k];
+				jtAcc = dclamp_sym(jtOld + jt, jtMax);
+			}
 			double d = acc - old, djt = jtAcc - jtOld;
 			double ax = nx*d, ay = ny*d;
 			if(FUSED){ nxj = __fma_rn(-ny, djt, ax); nyj = __fma_rn(nx, djt, ay); }
@@ -1059,8 +1067,8 @@ __device__ __forceinline__ void quad_apply(const QuadRow &q, cpgRow *row, double
  * impulses, 1: bias velocity with the bias impulse) for both bodies: it
  * computes both contact-point velocities and applies the impulse to both
  * bodies, with the reference's operations in the reference's order, as
- * quad_apply does for one body.  About 53 FP64 instructions per contact
- * lane against 40 on four lanes, but twice the units per warp, so levels
+ * quad_apply does for one body.  About 50 FP64 instructions per contact
+ * lane against 37 on four lanes, but twice the units per warp, so levels
  * of 9 to 16 units (and colours wider than the grid's quads) cost fewer
  * instructions.  Results are bit-identical to the other two layouts. */
 struct PairRow {
@@ -1132,13 +1140,18 @@ __device__ __forceinline__ void pair_apply(const PairRow &q, cpgRow *row, double
 			if(FUSED){ vn = __fma_rn(vrx, nx, vry*ny); vt = __fma_rn(vry, nx, -(vrx*ny)); }
 			else { vn = vrx*nx + vry*ny; vt = vrx*(-ny) + vry*nx; }
 			double y = q.c[k] + dneg_if(vn, bias);
-			double j = dneg_if(y, !bias)*q.nMass[k];
-			double old = q.acc[k];
-			double acc = dmax(old + j, 0.0);
-			double jtMax = q.u*acc;
-			double jt = -vt*q.tMass[k];
-			double jtOld = q.jt[k];
-			double jtAcc = dclamp(jtOld + jt, -jtMax, jtMax);
+			double old = q.acc[k], jtOld = q.jt[k];
+			double acc, jtAcc;
+			if(FUSED){
+				acc = dmax0(__fma_rn(dneg_if(y, !bias), q.nMass[k], old));
+				jtAcc = dclamp_sym(__fma_rn(-vt, q.tMass[k], jtOld), q.u*acc);
+			} else {
+				double j = dneg_if(y, !bias)*q.nMass[k];
+				acc = dmax0(old + j);
+				double jtMax = q.u*acc;
+				double jt = -vt*q.tMass[k];
+				jtAcc = dclamp_sym(jtOld + jt, jtMax);
+			}
 			double d = acc - old, djt = jtAcc - jtOld;
 			double ax = nx*d, ay = ny*d;
 			if(FUSED){ nxj = __fma_rn(-ny, djt, ax); nyj = __fma_rn(nx, djt, ay); }
@@ -1164,8 +1177,8 @@ __device__ __forceinline__ void pair_apply(const PairRow &q, cpgRow *row, double
 }
 
 /* Layout of a level of U units for a block of `nt` threads: the cheapest
- * in FP64 warp instructions per contact of four lanes (40 per round of
- * nt/4 units), two lanes (53 per round of nt/2) and one lane (93 per
+ * in FP64 warp instructions per contact of four lanes (37 per round of
+ * nt/4 units), two lanes (50 per round of nt/2) and one lane (90 per
  * round of nt).  0: four, 1: two, 2: one. */
 __device__ __forceinline__ int level_layout(int U, int nt, bool many)
 {
@@ -1175,10 +1188,10 @@ __device__ __forceinline__ int level_layout(int U, int nt, bool many)
 	if(many){
 		/* many worlds share each sub-partition's FP64 pipe: fewest warp
 		 * instructions (ties: fewest rounds) */
-		c4 = (long)w4*40*1024 + r4; c2 = (long)w2*53*1024 + r2; c1 = (long)w1*93*1024 + r1;
+		c4 = (long)w4*37*1024 + r4; c2 = (long)w2*50*1024 + r2; c1 = (long)w1*90*1024 + r1;
 	} else {
 		/* few worlds: the level's dependent chain, rounds x per-lane count */
-		c4 = (long)r4*40*1024 + w4; c2 = (long)r2*53*1024 + w2; c1 = (long)r1*93*1024 + w1;
+		c4 = (long)r4*37*1024 + w4; c2 = (long)r2*50*1024 + w2; c1 = (long)r1*90*1024 + w1;
 	}
 	return (c4 <= c2 && c4 <= c1) ? 0 : (c2 <= c1 ? 1 : 2);
 }
@@ -1874,13 +1887,15 @@ __global__ void k_color_coop(cpgSet s, int w)
  * accumulator updates are coherent. */
 /* Whether a level of U units, dealt round-robin over `blocks` blocks of
  * the whole-grid solve, takes fewer FP64 instructions on the busiest
- * sub-partition on two lanes per contact (~42 per lane, fused) than on
- * four (~32): a block's warps go round-robin to its four sub-partitions. */
+ * sub-partition on two lanes per contact (~33 per lane fused, ~50 exact)
+ * than on four (~25, ~37): a block's warps go round-robin to its four
+ * sub-partitions. */
+template<bool FUSED>
 __device__ __forceinline__ bool coop_two_lanes(int U, int blocks)
 {
 	int ub = (U + blocks - 1)/blocks;
 	int w4 = (4*ub + 31) >> 5, w2 = (2*ub + 31) >> 5;
-	return ((w2 + 3) >> 2)*42 < ((w4 + 3) >> 2)*32;
+	return ((w2 + 3) >> 2)*(FUSED ? 33 : 50) < ((w4 + 3) >> 2)*(FUSED ? 25 : 37);
 }
 
 template<bool FUSED>
@@ -1912,7 +1927,7 @@ __global__ void __launch_bounds__(CPG_COOP_SOLVE_THREADS, 1) k_solve_coop(cpgSet
 	bool bias = (threadIdx.x & 1) != 0;
 	QuadRow q;
 	int k = start[0] + quad;
-	bool two = coop_two_lanes(start[1] - start[0], gridDim.x);
+	bool two = coop_two_lanes<FUSED>(start[1] - start[0], gridDim.x);
 	bool have = !two && k < start[1];
 	if(have) quad_load(q, rows[k], lane4);
 	for(int pass = 0; pass <= iters; pass++){
@@ -1939,7 +1954,7 @@ __global__ void __launch_bounds__(CPG_COOP_SOLVE_THREADS, 1) k_solve_coop(cpgSet
 			int nl = l + 1, npass = pass;
 			if(nl == nlev){ nl = 0; npass++; }
 			k = start[nl] + quad;
-			two = coop_two_lanes(start[nl + 1] - start[nl], gridDim.x);
+			two = coop_two_lanes<FUSED>(start[nl + 1] - start[nl], gridDim.x);
 			have = !two && npass <= iters && k < start[nl + 1];
 			/* with a single level the next row is the one just written by
 			 * lanes 0 and 2 of this quad */

@@ -9,6 +9,7 @@
  */
 #pragma once
 #include <cfloat>
+#include <cstring>
 
 struct V2 { double x, y; };
 
@@ -34,6 +35,69 @@ __device__ __forceinline__ double dabs(double f) { return (f < 0) ? -f : f; }
 __device__ __forceinline__ double dclamp(double f, double lo, double hi) { return dmin(dmax(f, lo), hi); }
 __device__ __forceinline__ double dclamp01(double f) { return dmax(0.0, dmin(f, 1.0)); }
 __device__ __forceinline__ V2 vclamp(V2 v, double len) { return (vdot(v, v) > len*len) ? vmul(vnormalize(v), len) : v; }
+
+/* ---- the solver's clamps on the bit patterns ----
+ * A DSETP takes the FP64 pipe like a multiply, and the contact iteration
+ * needs three per contact (cpfmax(jn, 0) and the friction cone's
+ * cpfclamp, cpArbiter.c:486-492).  These return what the compares return,
+ * for every input including NaN and signed zeros, with integer compares
+ * and selects only. */
+__device__ __forceinline__ long long dbits(double x)
+{
+#ifdef __CUDA_ARCH__
+	return __double_as_longlong(x);
+#else
+	long long b; memcpy(&b, &x, sizeof(b)); return b;
+#endif
+}
+__device__ __forceinline__ double dfrombits(long long b)
+{
+#ifdef __CUDA_ARCH__
+	return __longlong_as_double(b);
+#else
+	double x; memcpy(&x, &b, sizeof(x)); return x;
+#endif
+}
+#define CPG_DBL_SIGN ((long long)0x8000000000000000ull)
+#define CPG_DBL_INF 0x7FF0000000000000ll
+
+/* a > b as IEEE compares it: false when either is NaN, -0 equal to +0.
+ * Ordered images: -0 folds to +0, negative magnitudes are inverted. */
+__device__ __forceinline__ bool dgt_bits(double a, double b)
+{
+	long long x = dbits(a), y = dbits(b);
+	bool nan = ((x & ~CPG_DBL_SIGN) > CPG_DBL_INF) || ((y & ~CPG_DBL_SIGN) > CPG_DBL_INF);
+	if(x == CPG_DBL_SIGN) x = 0;
+	if(y == CPG_DBL_SIGN) y = 0;
+	x = (x < 0) ? (x ^ ~CPG_DBL_SIGN) : x;
+	y = (y < 0) ? (y ^ ~CPG_DBL_SIGN) : y;
+	return !nan && x > y;
+}
+
+/* cpfmax(x, 0.0): x when x > 0, else +0.  The doubles above zero (NaN
+ * excluded) are exactly the bit patterns in (0, +inf]. */
+__device__ __forceinline__ double dmax0(double x)
+{
+	long long b = dbits(x);
+	return (b > 0 && b <= CPG_DBL_INF) ? x : 0.0;
+}
+
+/* cpfclamp(f, -m, m) = cpfmin(cpfmax(f, -m), m).  For m in [+0, +inf]:
+ * f when |f| < m; otherwise m, or -m when m > 0 and f is negative or NaN
+ * (NaN fails f > -m).  Any other m takes the general compares. */
+__device__ __forceinline__ double dclamp_sym(double f, double m)
+{
+	long long mb = dbits(m), fb = dbits(f);
+	double negm = dfrombits(mb ^ CPG_DBL_SIGN);
+	if(mb < 0 || mb > CPG_DBL_INF){
+		double t = dgt_bits(f, negm) ? f : negm;
+		return dgt_bits(m, t) ? t : m;
+	}
+	long long fmag = fb & ~CPG_DBL_SIGN;
+	if(fmag < mb) return f;
+	bool low = (fb < 0) || (fmag > CPG_DBL_INF);
+	return (mb != 0 && low) ? negm : m;
+}
 
 struct BB { double l, b, r, t; };
 __device__ __forceinline__ BB bbnew(double l, double b, double r, double t) { BB o; o.l = l; o.b = b; o.r = r; o.t = t; return o; }
