@@ -186,6 +186,7 @@ _GPU_API = {
     "cpGpuDebugSetTreeStaging": (None, [I]),
     "cpGpuDebugSetSolveShape": (None, [I, I]),
     "cpGpuDebugSetSolveLayout": (None, [I]),
+    "cpGpuDebugSetFlowSolve": (None, [I]),
     "cpGpuGetPhaseTimes": (I, [P, P, I]),
     "cpGpuGetStepStats": (I, [P, P, I]),
     "cpGpuGetLaunchCount": (ctypes.c_longlong, [I]),

@@ -31,7 +31,7 @@ enum { CPG_PIVOT = 1, CPG_PIN = 2, CPG_SLIDE = 3 };
 /* arbiter states, chipmunk_structs.h:83-95 */
 enum { CPG_ARB_FIRST = 0, CPG_ARB_NORMAL = 1, CPG_ARB_IGNORE = 2, CPG_ARB_CACHED = 3 };
 /* error bits latched in cpgTree.error */
-enum { CPG_ERR_NODES = 1, CPG_ERR_PAIRS = 2, CPG_ERR_CANDS = 4, CPG_ERR_ARBS = 8, CPG_ERR_BINS = 16, CPG_ERR_LEVELS = 32 };
+enum { CPG_ERR_NODES = 1, CPG_ERR_PAIRS = 2, CPG_ERR_CANDS = 4, CPG_ERR_ARBS = 8, CPG_ERR_BINS = 16, CPG_ERR_LEVELS = 32, CPG_ERR_FLOW = 64 };
 
 /* upper bound on the blocks of the cooperative sweep-and-prune sort */
 #define CPG_SORT_MAX_BLOCKS 1024
@@ -305,8 +305,14 @@ typedef struct cpgSet {
 	unsigned long long *sortK64;  /* [totalShapes] (key << 32 | shape) in the previous sweep order */
 	int *sortVA, *sortVB;
 	unsigned long long *claim, *cmask;   /* [totalBodies] */
-	int *colorCursor;             /* [512]: [0..1] colouring round counters, [8] sweep axis, [10] n+1 once a sweep order exists, [11] its axis, [16..31] transposition swap counters, [256..511] colour counts */
+	int *colorCursor;             /* [512]: [0..1] colouring round counters, [8] sweep axis, [10] n+1 once a sweep order exists, [11] its axis, [12] dataflow wait gave up, [13] no dataflow this step (a colour past 63), [16..31] transposition swap counters, [256..511] colour counts */
 	long long *sapBB;             /* [4*totalShapes] box keys in sweep order */
+	/* dataflow sweep of the coloured mode: each unit waits for the units
+	 * before it on its two bodies instead of a grid barrier per colour */
+	int *flowPred;                /* [2*totalUnits] per unit (schedule position) and body: predecessor position << 1 | previous pass, -1 none */
+	int *flowDone;                /* [totalUnits] passes the unit has finished */
+	int *flowPos;                 /* [64*totalBodies] schedule position of the unit of colour c on body b */
+	int flowSolve;                /* 1: coloured solve by dataflow (host value) */
 	float *sapPart;               /* [4*CPG_SORT_MAX_BLOCKS] per-block centre sums for the sweep axis */
 	int hostNdyn;                 /* dynamic shapes of world 0 (host value) */
 	int hostUnitsHint;            /* solver units of world 0 last step (host value) */

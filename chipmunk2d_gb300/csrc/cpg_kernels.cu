@@ -1720,6 +1720,7 @@ __global__ void k_color_coop(cpgSet s, int w)
 	const cpgWorld &W = s.world[w];
 	cpgTree &T = s.tree[w];
 	int n = T.nunits, nb = W.nbodies, narb = T.narb;
+	if(n > W.unitCap) return;
 	int gtid = threadIdx.x*gridDim.x + blockIdx.x, gsz = gridDim.x*blockDim.x;
 	const int *ua = s.unitA + W.unitOff, *ub = s.unitB + W.unitOff;
 	const int *ukey = s.unitKey + W.unitOff;
@@ -1729,7 +1730,7 @@ __global__ void k_color_coop(cpgSet s, int w)
 	bool reuse = (P.stamp % CPG_RECOLOR_PERIOD) != 0;
 	unsigned prevTag = color_tag(P.stamp - 1u, 0);
 	for(int b = gtid; b < nb; b += gsz){ cmask[b] = 0ull; claim[b] = ~0ull; }
-	if(gtid == 0){ counter[0] = 0; counter[1] = 0; counter[4] = -1; counter[5] = 0; counter[6] = -1; counter[7] = 0; }
+	if(gtid == 0){ counter[0] = 0; counter[1] = 0; counter[4] = -1; counter[5] = 0; counter[6] = -1; counter[7] = 0; counter[12] = 0; counter[13] = 0; }
 	grid.sync();
 	for(int u = gtid; u < n; u += gsz){
 		int c = -1;
@@ -1868,11 +1869,51 @@ __global__ void k_color_coop(cpgSet s, int w)
 	__syncthreads();
 	int *order = s.unitOrder + W.unitOff;
 	unsigned newTagBase = color_tag(P.stamp, 0);
+	bool flow = s.flowSolve != 0;
+	int *fpos = s.flowPos + 64*(size_t)W.bodyOff;
 	for(int u = gtid; u < n; u += gsz){
 		int c = color[u];
 		if(c < 0 || c > 255) c = 255;
-		order[shStart[c] + shBase[c] + atomicAdd(&shHist[c], 1u)] = u;
+		int pos = shStart[c] + shBase[c] + atomicAdd(&shHist[c], 1u);
+		order[pos] = u;
 		*unit_pad(s, W, narb, u) = (int)(c < 64 ? (newTagBase | (unsigned)c) : 0u);
+		if(flow){
+			s.flowDone[W.unitOff + u] = 0;
+			if(c < 64){
+				if(ua[u] >= 0) fpos[64*ua[u] + c] = pos;
+				if(ub[u] >= 0) fpos[64*ub[u] + c] = pos;
+			} else {
+				counter[13] = 1;
+			}
+		}
+	}
+	if(!flow) return;
+	grid.sync();
+	if(__ldcg(&counter[13])) return;
+	/* predecessors of the dataflow sweep: on each body, the unit of the
+	 * next lower colour in the same pass, or, for the body's lowest colour,
+	 * the unit of its highest colour in the previous pass (none when that
+	 * is the unit itself) */
+	int *pred = s.flowPred + 2*(size_t)W.unitOff;
+	for(int k = gtid; k < n; k += gsz){
+		int u = __ldcg(&order[k]);
+		int c = __ldcg(&color[u]);
+#pragma unroll
+		for(int side = 0; side < 2; side++){
+			int x = side ? ub[u] : ua[u];
+			int pr = -1;
+			if(x >= 0){
+				unsigned long long m = __ldcg(&cmask[x]);
+				unsigned long long lower = m & ((1ull << c) - 1ull);
+				if(lower){
+					pr = __ldcg(&fpos[64*x + 63 - __clzll((long long)lower)]) << 1;
+				} else {
+					int q = __ldcg(&fpos[64*x + 63 - __clzll((long long)m)]);
+					pr = (q == k) ? -1 : ((q << 1) | 1);
+				}
+			}
+			pred[2*k + side] = pr;
+		}
 	}
 }
 
@@ -1880,11 +1921,6 @@ __global__ void k_color_coop(cpgSet s, int w)
  * (about 170 per thread, so 384 threads fill the register file) */
 #define CPG_COOP_SOLVE_THREADS 256
 
-/* Levels (ordered mode) or colours (coloured mode) of one large world,
- * with the whole grid: grid.sync() between levels.  Packed body state is
- * read past the L1 (__ldcg), since other blocks write it between syncs;
- * a row is always handled by the same quad of lanes, in one SM, so its own
- * accumulator updates are coherent. */
 /* Whether a level of U units, dealt round-robin over `blocks` blocks of
  * the whole-grid solve, takes fewer FP64 instructions on the busiest
  * sub-partition on two lanes per contact (~33 per lane fused, ~50 exact)
@@ -1898,13 +1934,83 @@ __device__ __forceinline__ bool coop_two_lanes(int U, int blocks)
 	return ((w2 + 3) >> 2)*(FUSED ? 33 : 50) < ((w4 + 3) >> 2)*(FUSED ? 25 : 37);
 }
 
+/* ---- dataflow sweep (coloured mode) ----
+ * Instead of a grid barrier after every colour, each unit waits for the
+ * units before it in the sweep on its two bodies (flowPred, from the
+ * colouring) and then marks its pass done (flowDone = pass + 1).  Every
+ * body still sees its updates in the same order, so the results are the
+ * barrier sweep's bit for bit.  Warps take their units in (pass, colour)
+ * order and wait only for smaller ones, and a cooperative launch keeps
+ * every block resident, so the waits always end; they are bounded all the
+ * same: past CPG_FLOW_SPIN polls the sweep latches CPG_ERR_FLOW, raises
+ * the abort word and stops waiting.  A warp waits for all of its units
+ * together, so its lanes stay converged for the FP64 work.
+ * Measured on 20,000 settled circles it is slower than the barrier sweep
+ * (0.77 against 0.51 ms): the longest chain of dependent units still
+ * crosses every colour of every pass, and each link pays a release, a
+ * poll and the body loads, more than one grid barrier per colour costs.
+ * It is kept as an option (cpGpuDebugSetFlowSolve). */
+#define CPG_FLOW_SPIN (1 << 20)
+
+__device__ __forceinline__ int ld_acquire_gpu(const int *p)
+{
+	int v;
+	asm volatile("ld.acquire.gpu.global.b32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+	return v;
+}
+
+__device__ __forceinline__ void st_release_gpu(int *p, int v)
+{
+	asm volatile("st.release.gpu.global.b32 [%0], %1;" :: "l"(p), "r"(v) : "memory");
+}
+
+/* Whole warp: wait until the predecessors of this lane's unit k (or none,
+ * k < 0) have finished the passes this one needs. */
+__device__ __forceinline__ void flow_wait(const int *pred, const int *done, int *abortWord, int *err, int k, int pass)
+{
+	int f0 = -1, t0 = 0, f1 = -1, t1 = 0;
+	if(k >= 0){
+		int p0 = pred[2*k], p1 = pred[2*k + 1];
+		if(p0 >= 0){ t0 = pass + ((p0 & 1) ? 0 : 1); if(t0 > 0) f0 = p0 >> 1; }
+		if(p1 >= 0){ t1 = pass + ((p1 & 1) ? 0 : 1); if(t1 > 0) f1 = p1 >> 1; }
+	}
+	bool ready = false;
+	for(int it = 0;; it++){
+		if(!ready) ready = (f0 < 0 || ld_acquire_gpu(done + f0) >= t0) && (f1 < 0 || ld_acquire_gpu(done + f1) >= t1);
+		if(__all_sync(0xffffffffu, ready)) return;
+		if((it & 31) == 31){
+			if(__any_sync(0xffffffffu, ld_acquire_gpu(abortWord) != 0)) return;
+			if(it >= CPG_FLOW_SPIN){
+				if((threadIdx.x & 31) == 0){ atomicOr(err, CPG_ERR_FLOW); atomicExch(abortWord, 1); }
+				return;
+			}
+		}
+	}
+}
+
+/* Whole warp: this lane's unit k (leader lanes only) has finished `pass`;
+ * every lane's body and row stores are made visible first. */
+__device__ __forceinline__ void flow_done(int *done, int k, int pass, bool leader)
+{
+	asm volatile("fence.acq_rel.gpu;" ::: "memory");
+	__syncwarp();
+	if(leader && k >= 0) st_release_gpu(done + k, pass + 1);
+}
+
+/* Levels (ordered mode) or colours (coloured mode) of one large world,
+ * with the whole grid: grid.sync() between levels, or, in the coloured
+ * mode, the dataflow waits above.  Packed body state is read past the L1
+ * (__ldcg), since other blocks write it; a row is always handled by the
+ * same lanes, in one SM, so its own accumulator updates are coherent.
+ * Each warp walks a level's units in warp-uniform steps, so that the
+ * dataflow waits are whole-warp. */
 template<bool FUSED>
 __global__ void __launch_bounds__(CPG_COOP_SOLVE_THREADS, 1) k_solve_coop(cpgSet s, int w)
 {
 	cg::grid_group grid = cg::this_grid();
 	const cpgParams &P = s.params[w];
 	const cpgWorld &W = s.world[w];
-	const cpgTree &T = s.tree[w];
+	cpgTree &T = s.tree[w];
 	int nunits = T.nunits, nlev = T.nlevels;
 	if(nunits > W.unitCap || nlev < 1) return;
 	const int *start = s.levelStart + W.unitOff + w;
@@ -1912,6 +2018,10 @@ __global__ void __launch_bounds__(CPG_COOP_SOLVE_THREADS, 1) k_solve_coop(cpgSet
 	double *bodies = s.pbody + 8*(size_t)W.bodyOff;
 	int iters = P.iterations;
 	double dt_coef = P.dt_coef, dt = P.dt;
+	bool flow = FUSED && s.flowSolve && s.colorCursor[13] == 0;
+	const int *pred = s.flowPred + 2*(size_t)W.unitOff;
+	int *done = s.flowDone + W.unitOff;
+	int *abortWord = s.colorCursor + 12;
 	/* four lanes per unit; a level's units are dealt round-robin over the
 	 * blocks (unit i to block i % gridDim.x), so that every SM's FP64 pipes
 	 * take a share of each level */
@@ -1934,21 +2044,28 @@ __global__ void __launch_bounds__(CPG_COOP_SOLVE_THREADS, 1) k_solve_coop(cpgSet
 		for(int l = 0; l < nlev; l++){
 			int e = start[l + 1];
 			if(two){
-				for(int k2 = start[l] + pair; k2 < e; k2 += np2){
+				for(int k2 = start[l] + pair; __any_sync(0xffffffffu, k2 < e); k2 += np2){
+					bool has = k2 < e;
 					PairRow pr;
-					pair_load(pr, rows[k2], bias);
-					if(pr.kind == 0) pair_apply<true, FUSED>(pr, rows + k2, bodies, pass, dt_coef, bias);
-					else if(!bias) solve_row<true>(rows, k2, bodies, pass, dt_coef, dt);
+					if(has) pair_load(pr, rows[k2], bias);
+					if(flow) flow_wait(pred, done, abortWord, &T.error, has ? k2 : -1, pass);
+					if(has){
+						if(pr.kind == 0) pair_apply<true, FUSED>(pr, rows + k2, bodies, pass, dt_coef, bias);
+						else if(!bias) solve_row<true>(rows, k2, bodies, pass, dt_coef, dt);
+					}
+					if(flow) flow_done(done, has ? k2 : -1, pass, !bias);
 				}
-			} else if(have){
-				if(q.kind == 0) quad_apply<true, FUSED>(q, rows + k, bodies, pass, dt_coef, qmask, lane4);
-				else if(lane4 == 0) solve_row<true>(rows, k, bodies, pass, dt_coef, dt);
-				/* levels wider than the grid */
-				for(int k2 = k + nq; k2 < e; k2 += nq){
-					QuadRow q2;
-					quad_load(q2, rows[k2], lane4);
-					if(q2.kind == 0) quad_apply<true, FUSED>(q2, rows + k2, bodies, pass, dt_coef, qmask, lane4);
-					else if(lane4 == 0) solve_row<true>(rows, k2, bodies, pass, dt_coef, dt);
+			} else {
+				/* levels wider than the grid take several rounds */
+				for(int k2 = k; __any_sync(0xffffffffu, k2 < e); k2 += nq){
+					bool has = k2 < e;
+					if(has && k2 != k) quad_load(q, rows[k2], lane4);
+					if(flow) flow_wait(pred, done, abortWord, &T.error, has ? k2 : -1, pass);
+					if(has){
+						if(q.kind == 0) quad_apply<true, FUSED>(q, rows + k2, bodies, pass, dt_coef, qmask, lane4);
+						else if(lane4 == 0) solve_row<true>(rows, k2, bodies, pass, dt_coef, dt);
+					}
+					if(flow) flow_done(done, has ? k2 : -1, pass, lane4 == 0);
 				}
 			}
 			int nl = l + 1, npass = pass;
@@ -1956,11 +2073,17 @@ __global__ void __launch_bounds__(CPG_COOP_SOLVE_THREADS, 1) k_solve_coop(cpgSet
 			k = start[nl] + quad;
 			two = coop_two_lanes<FUSED>(start[nl + 1] - start[nl], gridDim.x);
 			have = !two && npass <= iters && k < start[nl + 1];
-			/* with a single level the next row is the one just written by
-			 * lanes 0 and 2 of this quad */
-			__syncthreads();
-			if(have) quad_load(q, rows[k], lane4);
-			grid.sync();
+			if(flow){
+				/* the warp synchronised after its last unit, so a row this
+				 * quad just wrote (a single level) reads back current */
+				if(have) quad_load(q, rows[k], lane4);
+			} else {
+				/* with a single level the next row is the one just written
+				 * by lanes 0 and 2 of this quad */
+				__syncthreads();
+				if(have) quad_load(q, rows[k], lane4);
+				grid.sync();
+			}
 		}
 	}
 }

@@ -560,6 +560,10 @@ void cpGpuDebugSetSolveShape(int threads, int maxBodies);
  * fewest FP64 warp instructions, 2 the shortest dependent chain, 3 four
  * lanes per contact only.  All give the same results. */
 void cpGpuDebugSetSolveLayout(int policy);
+/* Debug: the coloured mode's sweep by dataflow (1: each unit waits for the
+ * units before it on its two bodies) or with a grid barrier after every
+ * colour (0, default: faster on this part).  Both give the same results. */
+void cpGpuDebugSetFlowSolve(int on);
 /* Bookkeeping of the last step (after it completes): [0] error flags,
  * [1] pair-pool use and [2] node-pool use (per mille of capacity, largest
  * world), [3] live cached arbiters, [4] candidate pairs, [5] solved
