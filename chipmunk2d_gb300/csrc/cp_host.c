@@ -105,6 +105,7 @@ struct cpBody {
 	cpDataPointer userData;
 	cpSpace *space;
 	int index;                 /* world-local device index */
+	unsigned long long pullGen; /* download whose state this struct holds */
 	cpShape *shapeList;
 	cpConstraint *constraintList;
 };
@@ -239,6 +240,7 @@ struct DevSet {
 	cpgArb *gather;           /* arbiter snapshot staging */
 	int gatherCap;
 	int structStale;          /* the staging block holds body state the body structs do not have yet */
+	unsigned long long pullGen; /* id of the download in the staging block (unique across sets) */
 	size_t hstride;           /* doubles between two arrays of the staging block */
 	void *graph;              /* the step's launches as a CUDA graph (cpgStepGraph) */
 	int useGraph;             /* this call's steps replay the graph */
@@ -491,8 +493,26 @@ static void unpack_bodies(DevSet *ds)
 			b->a = f[6][g]; b->w = f[7][g]; b->t = f[8][g];
 			b->transform = cpTransformNew(f[9][g], f[10][g], f[11][g], f[12][g], f[13][g], f[14][g]);
 			b->v_bias = cpv(f[15][g], f[16][g]); b->w_bias = f[17][g];
+			b->pullGen = ds->pullGen;
 		}
 	}
+}
+
+/* One body's state from the staging block: a getter that reads every body
+ * after a step touches each struct once, instead of a pass that unpacks
+ * them all and a second pass that reads them. */
+static int unpack_one(DevSet *ds, cpSpace *sp, cpBody *b)
+{
+	int i = b->index;
+	if(!ds->hbodies || i < 0 || i >= sp->ndyn || sp->dyn[i] != b) return 0;
+	size_t stride = ds->hstride;
+	const double *f = ds->hbodies + ds->hworld[sp->world].bodyOff + i;
+	b->p = cpv(f[0], f[stride]); b->v = cpv(f[2*stride], f[3*stride]); b->f = cpv(f[4*stride], f[5*stride]);
+	b->a = f[6*stride]; b->w = f[7*stride]; b->t = f[8*stride];
+	b->transform = cpTransformNew(f[9*stride], f[10*stride], f[11*stride], f[12*stride], f[13*stride], f[14*stride]);
+	b->v_bias = cpv(f[15*stride], f[16*stride]); b->w_bias = f[17*stride];
+	b->pullGen = ds->pullGen;
+	return 1;
 }
 
 static int upload_shapes(DevSet *ds, int w)
@@ -806,20 +826,25 @@ static DevSet *devset_build(cpSpace **spaces, int nspaces)
 
 static void check_stats(DevSet *ds);
 
-/* Make host copies of the space's body state current. */
+/* Downloads so far: identifies the state in a staging block. */
+static unsigned long long g_pull_gen = 0;
+
 /* After a step: the device's body state into the staging block (the body
  * structs are unpacked from it only when something needs them). */
 static void space_download(cpSpace *sp)
 {
 	if(!sp || !sp->dev || !sp->hostStale) return;
 	DevSet *ds = sp->dev;
+	/* the copy queues behind the step; once it is done so are the stats */
+	int ok = download_bodies_raw(ds);
 	check_stats(ds);
-	if(!download_bodies_raw(ds)) return;
+	if(!ok) return;
 	for(int w = 0; w < ds->nspaces; w++){
 		cpSpace *o = ds->spaces[w];
 		o->hostStale = 0;
 		o->snapValid = 0;
 	}
+	ds->pullGen = ++g_pull_gen;
 	ds->structStale = 1;
 }
 
@@ -1752,8 +1777,18 @@ static void set_transform_(cpBody *b, cpVect p, cpFloat a)
 		rot.y, rot.x, p.y - (c.x*rot.y + c.y*rot.x));
 }
 
-/* Read access: make the host copy current first. */
-static inline const cpBody *rd(const cpBody *b) { if(b->space) space_pull(b->space); return b; }
+/* Read access: make the host copy current first.  After a step only this
+ * body is unpacked from the staging block (when it is one of the space's
+ * device bodies); anything else brings all of them. */
+static inline const cpBody *rd(const cpBody *b)
+{
+	cpSpace *sp = b->space;
+	if(!sp || !sp->dev) return b;
+	if(sp->hostStale) space_download(sp);
+	DevSet *ds = sp->dev;
+	if(ds->structStale && b->pullGen != ds->pullGen && !unpack_one(ds, sp, (cpBody *)b)) space_pull(sp);
+	return b;
+}
 /* Write access: pull, then mark the space's bodies for upload. */
 static inline cpBody *wr(cpBody *b)
 {
