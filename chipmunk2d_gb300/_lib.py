@@ -187,6 +187,7 @@ _GPU_API = {
     "cpGpuDebugSetSolveShape": (None, [I, I]),
     "cpGpuDebugSetSolveLayout": (None, [I]),
     "cpGpuDebugSetFlowSolve": (None, [I]),
+    "cpGpuDebugSetWarmStartGather": (None, [I]),
     "cpGpuGetPhaseTimes": (I, [P, P, I]),
     "cpGpuGetStepStats": (I, [P, P, I]),
     "cpGpuGetLaunchCount": (ctypes.c_longlong, [I]),

@@ -274,6 +274,11 @@ void cpGpuDebugSetSolveLayout(int policy) { g_solve_layout = (policy >= 0 && pol
  * off unless asked for */
 static int g_flow_solve = 0;
 void cpGpuDebugSetFlowSolve(int on) { g_flow_solve = on ? 1 : 0; }
+/* measured neutral on 20,000 settled circles (the solve lost 26 us of
+ * barrier-bound levels, the velocity kernel gained 23 us of gathers), so
+ * off unless asked for */
+static int g_warm_gather = 0;
+void cpGpuDebugSetWarmStartGather(int on) { g_warm_gather = on ? 1 : 0; }
 void cpGpuDebugSetTreeStaging(int maxNodes) { g_tree_stage = maxNodes < 0 ? -1 : maxNodes; }
 static int g_whole_grid = 0;     /* 1: single-world sets always use the whole-grid solve */
 
@@ -934,6 +939,7 @@ static int devset_step(DevSet *ds, const double *dts, cpSpace **only)
 	d->hostSolveStage = g_solve_stage;
 	d->solveLayout = g_solve_layout;
 	d->flowSolve = g_flow_solve;
+	d->warmGather = g_warm_gather;
 	/* launch shapes of many-world sets: the tuner's candidates on the steps
 	 * of a tuning window, its choice after it (debug settings win) */
 	int tuning = -1;

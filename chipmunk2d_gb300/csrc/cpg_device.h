@@ -313,6 +313,7 @@ typedef struct cpgSet {
 	int *flowDone;                /* [totalUnits] passes the unit has finished */
 	int *flowPos;                 /* [64*totalBodies] schedule position of the unit of colour c on body b */
 	int flowSolve;                /* 1: coloured solve by dataflow (host value) */
+	int warmGather;               /* 1: coloured mode applies the cached impulses per body in k_integrate_vel (host value) */
 	float *sapPart;               /* [4*CPG_SORT_MAX_BLOCKS] per-block centre sums for the sweep axis */
 	int hostNdyn;                 /* dynamic shapes of world 0 (host value) */
 	int hostUnitsHint;            /* solver units of world 0 last step (host value) */

@@ -742,6 +742,8 @@ __global__ void k_build_rows(cpgSet s)
 
 /* cpBody.c:493-509, then pack every body's solver state
  * (vx vy w vbx vby wb minv iinv, 64 bytes) */
+__device__ void warm_gather(const cpgSet &s, int w, int x, double &vx, double &vy, double &wv, double minv, double iinv);
+
 __global__ void k_integrate_vel(cpgSet s)
 {
 	int g = blockIdx.x*blockDim.x + threadIdx.x;
@@ -758,6 +760,8 @@ __global__ void k_integrate_vel(cpgSet s)
 		wv = wv*damping + s.tq[g]*iinv*dt;
 		s.vx[g] = vx; s.vy[g] = vy; s.w[g] = wv;
 		s.fx[g] = 0.0; s.fy[g] = 0.0; s.tq[g] = 0.0;
+		if(s.warmGather && s.btype[g] == CPG_DYNAMIC && s.colorCursor[13] == 0)
+			warm_gather(s, w, g - s.world[w].bodyOff, vx, vy, wv, minv, iinv);
 	}
 	double2 *pb = (double2 *)(s.pbody + 8*(size_t)g);
 	pb[0] = make_double2(vx, vy);
@@ -835,6 +839,51 @@ __device__ __forceinline__ void row_apply_cached(const cpgRow &row, BodyRef &A, 
 		double s_ = row.jnt.jnAcc*dt_coef;
 		apply_impulses(A, B, row.jnt.r1x, row.jnt.r1y, row.jnt.r2x, row.jnt.r2y, row.jnt.nx*s_, row.jnt.ny*s_);
 	}
+}
+
+/* Coloured mode, one thread per dynamic body: the warm start (the sweep's
+ * first pass) as a gather.  The body takes the cached impulses of its
+ * units in colour order, which is the order the coloured sweep applies
+ * them to it, with the same operations as row_apply_cached: the result is
+ * the sweep's bit for bit, without its twelve or so grid barriers.  The
+ * colouring's table gives the unit of each colour on the body. */
+__device__ void warm_gather(const cpgSet &s, int w, int x, double &vx, double &vy, double &wv, double minv, double iinv)
+{
+	const cpgWorld &W = s.world[w];
+	double dt_coef = s.params[w].dt_coef;
+	unsigned long long m = s.cmask[W.bodyOff + x];
+	const int *pos = s.flowPos + 64*(size_t)(W.bodyOff + x);
+	const cpgRow *rows = s.rows + W.unitOff;
+	BodyRef B;
+	B.vx = vx; B.vy = vy; B.w = wv; B.vbx = 0.0; B.vby = 0.0; B.wb = 0.0; B.minv = minv; B.iinv = iinv;
+	while(m){
+		int c = __ffsll((long long)m) - 1;
+		m &= m - 1ull;
+		int k = pos[c];
+		if(k < 0 || k >= s.tree[w].nunits || k >= W.unitCap) continue;
+		const cpgRow &row = rows[k];
+		bool isA = (row.a == x), isB = (row.b == x);
+		if(row.kind == 0){
+			if(row.flags & ROW_FIRST) continue;
+			double nx = row.arb.nx, ny = row.arb.ny;
+#pragma unroll
+			for(int j = 0; j < 2; j++){
+				if(j >= row.count) break;
+				const cpgRowContact &con = row.arb.c[j];
+				double jx = nx*con.jnAcc - ny*con.jtAcc, jy = nx*con.jtAcc + ny*con.jnAcc;
+				jx = jx*dt_coef; jy = jy*dt_coef;
+				if(isA) apply_impulse(B, -jx, -jy, con.r1x, con.r1y);
+				if(isB) apply_impulse(B, jx, jy, con.r2x, con.r2y);
+			}
+		} else {
+			double jx, jy;
+			if(row.kind == CPG_PIVOT){ jx = row.jnt.jx*dt_coef; jy = row.jnt.jy*dt_coef; }
+			else { double s_ = row.jnt.jnAcc*dt_coef; jx = row.jnt.nx*s_; jy = row.jnt.ny*s_; }
+			if(isA) apply_impulse(B, -jx, -jy, row.jnt.r1x, row.jnt.r1y);
+			if(isB) apply_impulse(B, jx, jy, row.jnt.r2x, row.jnt.r2y);
+		}
+	}
+	vx = B.vx; vy = B.vy; wv = B.w;
 }
 
 /* one iteration: cpArbiter.c:459-498, cpPivotJoint.c:47-66,
@@ -1720,8 +1769,12 @@ __global__ void k_color_coop(cpgSet s, int w)
 	const cpgWorld &W = s.world[w];
 	cpgTree &T = s.tree[w];
 	int n = T.nunits, nb = W.nbodies, narb = T.narb;
-	if(n > W.unitCap) return;
 	int gtid = threadIdx.x*gridDim.x + blockIdx.x, gsz = gridDim.x*blockDim.x;
+	if(n > W.unitCap){
+		/* no colouring, so no per-body unit table this step */
+		if(gtid == 0) s.colorCursor[13] = 1;
+		return;
+	}
 	const int *ua = s.unitA + W.unitOff, *ub = s.unitB + W.unitOff;
 	const int *ukey = s.unitKey + W.unitOff;
 	int *color = s.unitLevel + W.unitOff;
@@ -1869,7 +1922,9 @@ __global__ void k_color_coop(cpgSet s, int w)
 	__syncthreads();
 	int *order = s.unitOrder + W.unitOff;
 	unsigned newTagBase = color_tag(P.stamp, 0);
-	bool flow = s.flowSolve != 0;
+	/* the per-body unit table serves the dataflow sweep and the per-body
+	 * warm start (which also counts as the sweep's pass 0 done) */
+	bool flow = s.flowSolve != 0, table = flow || s.warmGather;
 	int *fpos = s.flowPos + 64*(size_t)W.bodyOff;
 	for(int u = gtid; u < n; u += gsz){
 		int c = color[u];
@@ -1877,8 +1932,8 @@ __global__ void k_color_coop(cpgSet s, int w)
 		int pos = shStart[c] + shBase[c] + atomicAdd(&shHist[c], 1u);
 		order[pos] = u;
 		*unit_pad(s, W, narb, u) = (int)(c < 64 ? (newTagBase | (unsigned)c) : 0u);
-		if(flow){
-			s.flowDone[W.unitOff + u] = 0;
+		if(table){
+			if(flow) s.flowDone[W.unitOff + u] = s.warmGather ? 1 : 0;
 			if(c < 64){
 				if(ua[u] >= 0) fpos[64*ua[u] + c] = pos;
 				if(ub[u] >= 0) fpos[64*ub[u] + c] = pos;
@@ -2019,6 +2074,8 @@ __global__ void __launch_bounds__(CPG_COOP_SOLVE_THREADS, 1) k_solve_coop(cpgSet
 	int iters = P.iterations;
 	double dt_coef = P.dt_coef, dt = P.dt;
 	bool flow = FUSED && s.flowSolve && s.colorCursor[13] == 0;
+	/* coloured mode: k_integrate_vel has applied the cached impulses */
+	int pass0 = (FUSED && s.warmGather && s.colorCursor[13] == 0) ? 1 : 0;
 	const int *pred = s.flowPred + 2*(size_t)W.unitOff;
 	int *done = s.flowDone + W.unitOff;
 	int *abortWord = s.colorCursor + 12;
@@ -2040,7 +2097,7 @@ __global__ void __launch_bounds__(CPG_COOP_SOLVE_THREADS, 1) k_solve_coop(cpgSet
 	bool two = coop_two_lanes<FUSED>(start[1] - start[0], gridDim.x);
 	bool have = !two && k < start[1];
 	if(have) quad_load(q, rows[k], lane4);
-	for(int pass = 0; pass <= iters; pass++){
+	for(int pass = pass0; pass <= iters; pass++){
 		for(int l = 0; l < nlev; l++){
 			int e = start[l + 1];
 			if(two){
@@ -2248,6 +2305,8 @@ extern "C" int cpg_launch_step(const cpgSet *s, const cpgSet *h, int mode, void 
 	int perWorldX = (W == 1) ? 152*4 : 1;
 	bool colored = (mode == 1 && W == 1);
 	cpgSet sv = *s;
+	/* the per-body warm start needs the colouring's per-body unit table */
+	sv.warmGather = (colored && !h->tape.on && s->warmGather) ? 1 : 0;
 
 	cudaMemsetAsync(s->stats, 0, 16*sizeof(int), st);
 	LAUNCH(k_reset_prev<<<dim3(perWorldX, W), 128, 0, st>>>(*s));
@@ -2296,7 +2355,7 @@ extern "C" int cpg_launch_step(const cpgSet *s, const cpgSet *h, int mode, void 
 	if(timing) cudaEventRecord(ev[5], st);
 	LAUNCH(k_build_rows<<<dim3(perWorldX, W), 128, 0, st>>>(*s));
 	if(h->tape.on) cpg_launch_tape(s, st);
-	LAUNCH(k_integrate_vel<<<blocks_for(h->totalBodies, 128), 128, 0, st>>>(*s));
+	LAUNCH(k_integrate_vel<<<blocks_for(h->totalBodies, 128), 128, 0, st>>>(sv));
 	if(h->tape.on) cpg_launch_tape_vel(s, st);
 	if(timing) cudaEventRecord(ev[6], st);
 	if(W == 1 && colored){

@@ -564,6 +564,10 @@ void cpGpuDebugSetSolveLayout(int policy);
  * units before it on its two bodies) or with a grid barrier after every
  * colour (0, default: faster on this part).  Both give the same results. */
 void cpGpuDebugSetFlowSolve(int on);
+/* Debug: the coloured mode's warm start (the sweep's first pass) as a
+ * per-body gather of the cached impulses in colour order (1) or as colour
+ * levels of the sweep (0, default).  Both give the same results. */
+void cpGpuDebugSetWarmStartGather(int on);
 /* Bookkeeping of the last step (after it completes): [0] error flags,
  * [1] pair-pool use and [2] node-pool use (per mille of capacity, largest
  * world), [3] live cached arbiters, [4] candidate pairs, [5] solved

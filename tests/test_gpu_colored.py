@@ -167,3 +167,27 @@ def test_dataflow_sweep_matches_barrier_sweep(gpu_lib, cfg, size, steps):
         gpu_lib.cpGpuDebugSetFlowSolve(0)
         a.free()
         b.free()
+
+
+@pytest.mark.parametrize("cfg,size,steps,flow", [(2, 20000, 130, 0), (3, 3000, 60, 0), (3, 3000, 30, 1)])
+def test_warm_start_gather_matches_sweep(gpu_lib, cfg, size, steps, flow):
+    """The coloured mode's warm start as a per-body gather of the cached
+    impulses in colour order gives every body the same updates in the same
+    order as the sweep's first pass: bit-identical results, with joints
+    (mixed scene) and under the dataflow sweep too."""
+    a = colored(gpu_lib, cfg, size)
+    b = colored(gpu_lib, cfg, size)
+    gpu_lib.cpGpuDebugSetFlowSolve(flow)
+    try:
+        for chunk in range(0, steps, 10):
+            gpu_lib.cpGpuDebugSetWarmStartGather(1)
+            a.step(1 / 60, 10)
+            gpu_lib.cpGpuDebugSetWarmStartGather(0)
+            b.step(1 / 60, 10)
+            assert gpu_lib.cpGpuGetLastError() == 0, gpu_lib.cpGpuGetLastErrorString()
+            np.testing.assert_array_equal(a.bodies(), b.bodies(), err_msg="after %d steps" % (chunk + 10))
+    finally:
+        gpu_lib.cpGpuDebugSetWarmStartGather(0)
+        gpu_lib.cpGpuDebugSetFlowSolve(0)
+        a.free()
+        b.free()
