@@ -1558,7 +1558,7 @@ __device__ void sap_radix_pass(cg::grid_group &grid, const unsigned *kin, const 
 	grid.sync();
 }
 
-__global__ void __launch_bounds__(SAP_THREADS) k_sap_sort(cpgSet s, int w)
+__global__ void __launch_bounds__(SAP_THREADS, 1) k_sap_sort(cpgSet s, int w)
 {
 	cg::grid_group grid = cg::this_grid();
 	__shared__ float red[4][SAP_THREADS/32];
