@@ -202,12 +202,12 @@ __global__ void k_tree(cpgSet s, int stagedNodes)
 		for(int i = threadIdx.x; i < nn; i += blockDim.x) snodes[i] = gnodes[i];
 		__syncthreads();
 	}
-	if(threadIdx.x == 0){
+	{
 		TreeCtx c = make_tree_ctx(&s, w);
 		if(staged){ c.nodes = snodes; c.nodeCap = stagedNodes < W.nodeCap ? stagedNodes : W.nodeCap; }
 		c.collide = 1;
-		tree_reindex_query(c);
-		c.T->ncand = c.ncand;
+		tree_reindex_query_block(c);
+		if(threadIdx.x == 0) c.T->ncand = c.ncand;
 	}
 	__syncthreads();
 	if(staged){
@@ -2334,7 +2334,9 @@ extern "C" int cpg_launch_step(const cpgSet *s, const cpgSet *h, int mode, void 
 			cudaFuncSetAttribute(k_tree, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
 			treeSmemSet = smem;
 		}
-		LAUNCH(k_tree<<<W, 32, smem, st>>>(*s, staged));
+		/* one warp per world in a batch; a single world's leaf scan takes
+		 * 256 threads (thread 0 alone reinserts and marks) */
+		LAUNCH(k_tree<<<W, W == 1 ? 256 : 32, smem, st>>>(*s, staged));
 	}
 	if(timing) cudaEventRecord(ev[2], st);
 	cudaMemsetAsync(s->nbCount, 0, CPG_PAIR_TYPES*sizeof(int), st);

@@ -435,19 +435,25 @@ __device__ void tree_insert(TreeCtx &c, const cpgOp &op)
 	T->treeStamp++;
 }
 
-/* cpBBTree.c:498-517 */
-__device__ void leaf_update(TreeCtx &c, int leaf)
+/* cpBBTree.c:498-517: a leaf whose shape left its fattened box */
+__device__ __forceinline__ bool leaf_moved(const TreeCtx &c, int leaf)
+{
+	return !tcontains(node_bb(c.nodes[leaf]), shape_bb(c, c.nodes[leaf].obj));
+}
+
+__device__ void leaf_reinsert(TreeCtx &c, int leaf)
 {
 	cpgTree *T = c.T;
-	int s = c.nodes[leaf].obj;
-	BB bb = shape_bb(c, s);
-	if(!tcontains(node_bb(c.nodes[leaf]), bb)){
-		set_node_bb(c.nodes[leaf], leaf_fat_bb(c, s));
-		int root = subtree_remove(c, T->dynRoot, leaf);
-		T->dynRoot = subtree_insert(c, root, leaf);
-		pairs_clear(c, leaf);
-		c.nodes[leaf].stamp = T->treeStamp;
-	}
+	set_node_bb(c.nodes[leaf], leaf_fat_bb(c, c.nodes[leaf].obj));
+	int root = subtree_remove(c, T->dynRoot, leaf);
+	T->dynRoot = subtree_insert(c, root, leaf);
+	pairs_clear(c, leaf);
+	c.nodes[leaf].stamp = T->treeStamp;
+}
+
+__device__ void leaf_update(TreeCtx &c, int leaf)
+{
+	if(leaf_moved(c, leaf)) leaf_reinsert(c, leaf);
 }
 
 /* cpBBTree.c:638-654 */
@@ -468,4 +474,77 @@ __device__ void tree_reindex_query(TreeCtx &c)
 	if(T->error) return;
 	mark_subtree(c, T->dynRoot, T->statRoot);
 	T->treeStamp++;
+}
+
+/* tree_reindex_query with the leaf scan spread over the block.  A leaf's
+ * containment test reads only its own box and its shape's, and the
+ * reinsertion of another leaf changes neither, so the threads first test
+ * every hash bin and list the leaves that moved, in hash-bin order; thread
+ * 0 then reinserts them in that order, exactly as the serial loop does,
+ * and marks the tree.  The list lives in the candidate buffer, which
+ * marking fills only afterwards (its capacity, 4 ints per candidate, is
+ * far above the leaf count).  The whole scan runs before the first
+ * reinsertion, so its loads do not evict the tree's top nodes from thread
+ * 0's L1 between reinsertions.  Every thread of the block calls it. */
+__device__ void tree_reindex_query_block(TreeCtx &c)
+{
+	__shared__ int warpTot[32];
+	__shared__ int carry, stop;
+	cpgTree *T = c.T;
+	int tid = threadIdx.x, nt = blockDim.x, lane = tid & 31, warp = tid >> 5, nw = (nt + 31) >> 5;
+	int *list = (int *)c.cands;
+	long long listCap = 4ll*(long long)c.candCap;
+	if(tid == 0){ stop = (T->dynRoot < 0) || (T->error != 0); carry = 0; }
+	__syncthreads();
+	if(stop){
+		if(tid == 0 && T->dynRoot >= 0) T->error |= CPG_ERR_BINS;
+		return;
+	}
+	unsigned size = T->dynSize;
+	for(unsigned base = 0; base < size; base += (unsigned)nt){
+		unsigned i = base + (unsigned)tid;
+		int cnt = 0;
+		if(i < size){
+			int guard = 0;
+			for(int n = c.dbins[i]; n >= 0; n = c.nodes[n].binNext){
+				if(++guard > c.nodeCap){ atomicOr(&T->error, CPG_ERR_BINS); break; }
+				if(leaf_moved(c, n)) cnt++;
+			}
+		}
+		/* exclusive block scan of the moved counts, after the running total */
+		int x = cnt;
+		for(int o = 1; o < 32; o <<= 1){
+			int y = __shfl_up_sync(0xffffffffu, x, o);
+			if(lane >= o) x += y;
+		}
+		if(lane == 31) warpTot[warp] = x;
+		__syncthreads();
+		if(tid == 0){
+			int acc = carry;
+			for(int k = 0; k < nw; k++){ int t = warpTot[k]; warpTot[k] = acc; acc += t; }
+			carry = acc;
+		}
+		__syncthreads();
+		if(cnt > 0){
+			long long off = (long long)warpTot[warp] + x - cnt;
+			int guard = 0;
+			for(int n = c.dbins[i]; n >= 0; n = c.nodes[n].binNext){
+				if(++guard > c.nodeCap) break;
+				if(leaf_moved(c, n)){
+					if(off < listCap) list[off] = n;
+					off++;
+				}
+			}
+		}
+		__syncthreads();
+	}
+	if(tid == 0){
+		int moved = carry;
+		if((long long)moved > listCap) T->error |= CPG_ERR_CANDS;
+		for(int k = 0; k < moved && !T->error; k++) leaf_reinsert(c, list[k]);
+		if(!T->error){
+			mark_subtree(c, T->dynRoot, T->statRoot);
+			T->treeStamp++;
+		}
+	}
 }
