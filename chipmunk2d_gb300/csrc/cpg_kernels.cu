@@ -186,8 +186,9 @@ __global__ void k_shape_cache(cpgSet s)
 }
 
 /* cpBBTree.c:638-654: one block per world (largest worlds first); its
- * threads stage the world's node pool in shared memory when it fits, and
- * thread 0 re-indexes and traverses. */
+ * threads stage the world's node pool in shared memory when it fits and
+ * scan the leaves for the ones that moved; thread 0 reinserts those and
+ * traverses. */
 extern __shared__ cpgNode snodes[];
 
 __global__ void k_tree(cpgSet s, int stagedNodes)

@@ -1,6 +1,7 @@
 /*
  * cpg_tree.cuh -- device mirror of the reference's incremental AABB tree
- * (src/cpBBTree.c) for one world, run by one thread.
+ * (src/cpBBTree.c) for one world, run by one thread (the containment
+ * scan of the leaves, which has no order to keep, by the whole block).
  *
  * The tree, its per-leaf pair cache and the leaf hash set determine the
  * order in which cpSpaceStep visits shape pairs, and that order is the
