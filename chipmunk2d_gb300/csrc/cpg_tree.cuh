@@ -452,37 +452,14 @@ __device__ void leaf_reinsert(TreeCtx &c, int leaf)
 	c.nodes[leaf].stamp = T->treeStamp;
 }
 
-__device__ void leaf_update(TreeCtx &c, int leaf)
-{
-	if(leaf_moved(c, leaf)) leaf_reinsert(c, leaf);
-}
-
-/* cpBBTree.c:638-654 */
-__device__ void tree_reindex_query(TreeCtx &c)
-{
-	cpgTree *T = c.T;
-	if(T->dynRoot < 0) return;
-	int guard = 0;
-	for(unsigned i = 0; i < T->dynSize; i++){
-		int n = c.dbins[i];
-		while(n >= 0){
-			if(++guard > c.nodeCap || T->error){ T->error |= CPG_ERR_BINS; return; }
-			int next = c.nodes[n].binNext;
-			leaf_update(c, n);
-			n = next;
-		}
-	}
-	if(T->error) return;
-	mark_subtree(c, T->dynRoot, T->statRoot);
-	T->treeStamp++;
-}
-
-/* tree_reindex_query with the leaf scan spread over the block.  A leaf's
- * containment test reads only its own box and its shape's, and the
- * reinsertion of another leaf changes neither, so the threads first test
- * every hash bin and list the leaves that moved, in hash-bin order; thread
- * 0 then reinserts them in that order, exactly as the serial loop does,
- * and marks the tree.  The list lives in the candidate buffer, which
+/* cpBBTree.c:638-654 (cpBBTreeReindexQuery): every leaf of the hash set,
+ * in bin order, is updated (reinserted when its shape left its box), then
+ * the tree is marked and the stamp advanced.  A leaf's containment test
+ * reads only its own box and its shape's, and the reinsertion of another
+ * leaf changes neither, so the threads first test every hash bin and list
+ * the leaves that moved, in hash-bin order; thread 0 then reinserts them
+ * in that order, which is the serial loop's sequence of tree changes, and
+ * marks the tree.  The list lives in the candidate buffer, which
  * marking fills only afterwards (its capacity, 4 ints per candidate, is
  * far above the leaf count).  The whole scan runs before the first
  * reinsertion, so its loads do not evict the tree's top nodes from thread
