@@ -120,8 +120,10 @@ __device__ int pair_alloc(TreeCtx &c)
 	return T->pairTop++;
 }
 
+/* pad marks a pool slot live (1) or free (0) */
 __device__ __forceinline__ void pair_recycle(TreeCtx &c, int p)
 {
+	c.pairs[p].pad = 0;
 	c.pairs[p].aNext = c.T->freePair;
 	c.T->freePair = p;
 	c.T->pairsLive--;
@@ -174,6 +176,7 @@ __device__ void pair_insert(TreeCtx &c, int a, int b)
 	pr.aPrev = -1; pr.aLeaf = a; pr.aNext = nextA;
 	pr.bPrev = -1; pr.bLeaf = b; pr.bNext = nextB;
 	pr.id = 0;
+	pr.pad = 1;
 	c.nodes[a].pairs = p;
 	c.nodes[b].pairs = p;
 	if(nextA >= 0){
@@ -442,16 +445,19 @@ __device__ __forceinline__ bool leaf_moved(const TreeCtx &c, int leaf)
 	return !tcontains(node_bb(c.nodes[leaf]), shape_bb(c, c.nodes[leaf].obj));
 }
 
-__device__ void leaf_reinsert(TreeCtx &c, int leaf)
+/* clearPairs false: the pairs stay threaded; the parallel marking drops
+ * those of every moved leaf at once (cpg_mark.cuh) */
+__device__ void leaf_reinsert(TreeCtx &c, int leaf, bool clearPairs = true)
 {
 	cpgTree *T = c.T;
 	set_node_bb(c.nodes[leaf], leaf_fat_bb(c, c.nodes[leaf].obj));
 	int root = subtree_remove(c, T->dynRoot, leaf);
 	T->dynRoot = subtree_insert(c, root, leaf);
-	pairs_clear(c, leaf);
+	if(clearPairs) pairs_clear(c, leaf);
 	c.nodes[leaf].stamp = T->treeStamp;
 }
 
+#ifdef __CUDACC__
 /* cpBBTree.c:638-654 (cpBBTreeReindexQuery): every leaf of the hash set,
  * in bin order, is updated (reinserted when its shape left its box), then
  * the tree is marked and the stamp advanced.  A leaf's containment test
@@ -526,3 +532,4 @@ __device__ void tree_reindex_query_block(TreeCtx &c)
 		}
 	}
 }
+#endif
