@@ -188,6 +188,7 @@ _GPU_API = {
     "cpGpuDebugSetSolveLayout": (None, [I]),
     "cpGpuDebugSetFlowSolve": (None, [I]),
     "cpGpuDebugSetWarmStartGather": (None, [I]),
+    "cpGpuDebugSetParallelMarking": (None, [I]),
     "cpGpuGetPhaseTimes": (I, [P, P, I]),
     "cpGpuGetStepStats": (I, [P, P, I]),
     "cpGpuGetLaunchCount": (ctypes.c_longlong, [I]),

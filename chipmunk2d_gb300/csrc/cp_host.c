@@ -279,6 +279,8 @@ void cpGpuDebugSetFlowSolve(int on) { g_flow_solve = on ? 1 : 0; }
  * off unless asked for */
 static int g_warm_gather = 0;
 void cpGpuDebugSetWarmStartGather(int on) { g_warm_gather = on ? 1 : 0; }
+static int g_par_mark = 0;
+void cpGpuDebugSetParallelMarking(int on) { g_par_mark = on ? 1 : 0; }
 void cpGpuDebugSetTreeStaging(int maxNodes) { g_tree_stage = maxNodes < 0 ? -1 : maxNodes; }
 static int g_whole_grid = 0;     /* 1: single-world sets always use the whole-grid solve */
 
@@ -387,6 +389,10 @@ static size_t carve_set(cpgSet *d, char *base, int pass)
 		CARVE(flowPred, int, one ? 2*d->totalUnits : 1);
 		CARVE(flowDone, int, one ? d->totalUnits : 1);
 		CARVE(flowPos, int, one ? 64*NB : 1);
+		/* the parallel marking's scratch: 9 arrays per node, 2 per pair
+		 * slot, 2 incidences of 2 ints per pair slot, block sums */
+		size_t nn1 = (size_t)d->totalNodes + 1, np1 = (size_t)d->totalPairs + 1;
+		CARVE(markScratch, int, one ? (9*nn1 + 2*np1 + 4*(size_t)d->totalPairs + 1025) : 1);
 	}
 	CARVE(sapPart, float, 4*CPG_SORT_MAX_BLOCKS);
 	CARVE(stats, int, 16);
@@ -940,6 +946,7 @@ static int devset_step(DevSet *ds, const double *dts, cpSpace **only)
 	d->solveLayout = g_solve_layout;
 	d->flowSolve = g_flow_solve;
 	d->warmGather = g_warm_gather;
+	d->parMark = g_par_mark;
 	/* launch shapes of many-world sets: the tuner's candidates on the steps
 	 * of a tuning window, its choice after it (debug settings win) */
 	int tuning = -1;

@@ -314,6 +314,8 @@ typedef struct cpgSet {
 	int *flowPos;                 /* [64*totalBodies] schedule position of the unit of colour c on body b */
 	int flowSolve;                /* 1: coloured solve by dataflow (host value) */
 	int warmGather;               /* 1: coloured mode applies the cached impulses per body in k_integrate_vel (host value) */
+	int parMark;                  /* 1: a single world's tree is marked by k_tree_mark's parallel phases (host value) */
+	int *markScratch;             /* single-world sets: the parallel marking's scratch (mark_scratch in cpg_kernels.cu) */
 	float *sapPart;               /* [4*CPG_SORT_MAX_BLOCKS] per-block centre sums for the sweep axis */
 	int hostNdyn;                 /* dynamic shapes of world 0 (host value) */
 	int hostUnitsHint;            /* solver units of world 0 last step (host value) */

@@ -37,6 +37,7 @@
 #include "cpg_narrow.cuh"
 #include "cpg_colored.cuh"
 #include "cpg_adjoint.cuh"
+#include "cpg_mark.cuh"
 
 static long long g_launches = 0;
 
@@ -207,13 +208,171 @@ __global__ void k_tree(cpgSet s, int stagedNodes)
 		TreeCtx c = make_tree_ctx(&s, w);
 		if(staged){ c.nodes = snodes; c.nodeCap = stagedNodes < W.nodeCap ? stagedNodes : W.nodeCap; }
 		c.collide = 1;
-		tree_reindex_query_block(c);
+		tree_reindex_query_block(c, s.parMark != 0);
 		if(threadIdx.x == 0) c.T->ncand = c.ncand;
 	}
 	__syncthreads();
 	if(staged){
 		nn = s.tree[w].nodeTop;
 		for(int i = threadIdx.x; i < nn; i += blockDim.x) gnodes[i] = snodes[i];
+	}
+}
+
+/* ---- parallel marking of a single world's tree (cpg_mark.cuh) ----
+ * One cooperative launch after k_tree has reinserted the moved leaves with
+ * their pairs kept: the marking phases over the leaves (threads take hash
+ * bins and walk their chains) and the pair slots, with grid barriers
+ * between phases and grid-wide prefix sums.  Candidates, pair lists and
+ * slot choice are deterministic. */
+#define CPG_MARK_THREADS 256
+
+/* the scratch of cpgSet.markScratch, in the order carve_set sizes it:
+ * 9 arrays of nodeCap + 1, 2 of pairCap + 1, incidences, block sums */
+__device__ __forceinline__ MarkScratch mark_scratch(const cpgSet &s, const cpgWorld &W, int **freeFlag, int **blockSum)
+{
+	MarkScratch m;
+	int n1 = W.nodeCap + 1, p1 = W.pairCap + 1;
+	int *q = s.markScratch;
+	m.cnt = q; q += n1;
+	m.arrive = q; q += n1;
+	m.rank = q; q += n1;
+	m.oldB = q; q += n1;
+	m.inc = q; q += n1;
+	m.incid = q; q += n1;
+	m.incCur = q; q += n1;
+	m.emit = q; q += n1;
+	m.ins = q; q += n1;
+	m.freeSlot = q; q += p1;
+	*freeFlag = q; q += p1;
+	m.incEnt = q; q += 4*(size_t)W.pairCap;
+	*blockSum = q;
+	m.nFree = 0; m.pairTop = 0; m.incCap = 2*W.pairCap; m.rankCap = n1;
+	return m;
+}
+
+/* Exclusive scan of a[0, len) by one block: each thread sums a contiguous
+ * run, the block scans the run sums, each thread writes its run's
+ * prefixes.  Returns the total to every thread. */
+__device__ int block_excl_scan(int *a, int len)
+{
+	__shared__ int wsum[32];
+	__shared__ int btot;
+	int t = threadIdx.x, lane = t & 31, warp = t >> 5, nw = blockDim.x >> 5;
+	int per = (len + (int)blockDim.x - 1)/(int)blockDim.x;
+	int i0 = min(len, t*per), i1 = min(len, i0 + per);
+	int sum = 0;
+	for(int i = i0; i < i1; i++) sum += __ldcg(&a[i]);
+	int x = sum;
+	for(int o = 1; o < 32; o <<= 1){ int y = __shfl_up_sync(0xffffffffu, x, o); if(lane >= o) x += y; }
+	if(lane == 31) wsum[warp] = x;
+	__syncthreads();
+	if(t == 0){ int acc = 0; for(int k = 0; k < nw; k++){ int v = wsum[k]; wsum[k] = acc; acc += v; } btot = acc; }
+	__syncthreads();
+	int run = wsum[warp] + x - sum;
+	for(int i = i0; i < i1; i++){ int v = __ldcg(&a[i]); a[i] = run; run += v; }
+	int tot = btot;
+	__syncthreads();
+	return tot;
+}
+
+/* Exclusive scan of a[0, n) by the whole grid; returns the total. */
+__device__ int grid_excl_scan(cg::grid_group &grid, int *a, int n, int *blockSum)
+{
+	int nb = gridDim.x, b = blockIdx.x;
+	int per = (n + nb - 1)/nb;
+	int lo = min(n, b*per), hi = min(n, lo + per);
+	int tot = block_excl_scan(a + lo, hi - lo);
+	if(threadIdx.x == 0) blockSum[b] = tot;
+	grid.sync();
+	if(b == 0 && threadIdx.x == 0){
+		int acc = 0;
+		for(int k = 0; k < nb; k++){ int v = __ldcg(&blockSum[k]); blockSum[k] = acc; acc += v; }
+		blockSum[nb] = acc;
+	}
+	grid.sync();
+	int base = __ldcg(&blockSum[b]);
+	if(base) for(int i = lo + (int)threadIdx.x; i < hi; i += blockDim.x) a[i] += base;
+	int total = __ldcg(&blockSum[nb]);
+	grid.sync();
+	return total;
+}
+
+/* The phases, in order (each loop over leaves takes hash bins with the
+ * same bin-to-thread mapping, so a leaf's own writes are read back by the
+ * thread that made them). */
+#define MARK_DYN_LEAVES(n) for(unsigned i_ = gtid; i_ < dsize; i_ += gsz) for(int n = c.dbins[i_], g_ = 0; n >= 0 && g_ <= c.nodeCap; n = c.nodes[n].binNext, g_++)
+#define MARK_STAT_LEAVES(n) for(unsigned i_ = gtid; i_ < ssize; i_ += gsz) for(int n = c.sbins[i_], g_ = 0; n >= 0 && g_ <= c.nodeCap; n = c.nodes[n].binNext, g_++)
+
+__global__ void __launch_bounds__(CPG_MARK_THREADS, 1) k_tree_mark(cpgSet s, int w)
+{
+	cg::grid_group grid = cg::this_grid();
+	const cpgWorld &W = s.world[w];
+	TreeCtx c = make_tree_ctx(&s, w);
+	c.collide = 1;
+	cpgTree *T = c.T;
+	if(T->dynRoot < 0 || T->error) return;
+	unsigned gtid = blockIdx.x*blockDim.x + threadIdx.x, gsz = gridDim.x*blockDim.x;
+	int *freeFlag, *blockSum;
+	MarkScratch m = mark_scratch(s, W, &freeFlag, &blockSum);
+	int nodeTop = T->nodeTop, pairTop = T->pairTop, nLeaves = (int)T->dynEntries, statRoot = T->statRoot;
+	if(nLeaves > m.rankCap || nodeTop > W.nodeCap || pairTop > W.pairCap){
+		if(gtid == 0) T->error |= CPG_ERR_NODES;
+		return;
+	}
+	unsigned dsize = T->dynSize, ssize = T->statSize;
+	for(int i = gtid; i <= nodeTop; i += gsz){ m.arrive[i] = 0; m.inc[i] = 0; m.incid[i] = 0; m.incCur[i] = 0; }
+	grid.sync();
+	/* 1: the moved leaves' pairs out of every list */
+	MARK_DYN_LEAVES(n) mark_filter_list(c, m, n);
+	MARK_STAT_LEAVES(n) mark_filter_list(c, m, n);
+	grid.sync();
+	/* the pool's free slots; leaf counts bottom up */
+	for(int p = gtid; p < pairTop; p += gsz) freeFlag[p] = (__ldcg(&c.pairs[p].pad) == 0) ? 1 : 0;
+	MARK_DYN_LEAVES(n) mark_count_up(c, m, n);
+	grid.sync();
+	/* 2: ranks (the scan's barriers follow) */
+	MARK_DYN_LEAVES(n) mark_rank(c, m, n);
+	int nFree = grid_excl_scan(grid, freeFlag, pairTop, blockSum);
+	for(int p = gtid; p < pairTop; p += gsz) if(__ldcg(&c.pairs[p].pad) == 0) m.freeSlot[__ldcg(&freeFlag[p])] = p;
+	/* 3: counts, every moved leaf's before the others' */
+	MARK_DYN_LEAVES(n) if(mark_moved(c, n)) mark_count_moved(c, m, n, statRoot);
+	grid.sync();
+	MARK_DYN_LEAVES(n) if(!mark_moved(c, n)) mark_count_still(c, m, n);
+	grid.sync();
+	/* 4: offsets */
+	int ne = grid_excl_scan(grid, m.emit, nLeaves, blockSum);
+	int ni = grid_excl_scan(grid, m.ins, nLeaves, blockSum);
+	int nin = grid_excl_scan(grid, m.incid, nodeTop, blockSum);
+	m.nFree = nFree; m.pairTop = pairTop;
+	int fresh = ni > nFree ? ni - nFree : 0;
+	if(ne > c.candCap || pairTop + fresh > c.pairCap || nin > m.incCap){
+		if(gtid == 0) T->error |= (ne > c.candCap) ? CPG_ERR_CANDS : CPG_ERR_PAIRS;
+		return;
+	}
+	/* 5: the moved leaves' candidates and new pairs */
+	MARK_DYN_LEAVES(n) if(mark_moved(c, n)) mark_write_moved(c, m, n, statRoot);
+	grid.sync();
+	/* 6, 7: new pairs in front of every list, then the other leaves emit */
+	MARK_DYN_LEAVES(n){
+		mark_link(c, m, n);
+		if(!mark_moved(c, n)) mark_emit_still(c, m, n);
+	}
+	MARK_STAT_LEAVES(n) mark_link(c, m, n);
+	/* the unused free slots back into the pool's list */
+	int left = nFree > ni ? nFree - ni : 0;
+	for(int k = gtid; k < left; k += gsz){
+		int p = __ldcg(&m.freeSlot[ni + k]);
+		c.pairs[p].aNext = (k + 1 < left) ? __ldcg(&m.freeSlot[ni + k + 1]) : -1;
+	}
+	/* every thread is done with mark_moved, which reads the tree's stamp,
+	 * before thread 0 advances it */
+	grid.sync();
+	if(gtid == 0){
+		T->freePair = left > 0 ? __ldcg(&m.freeSlot[ni]) : -1;
+		T->pairTop = pairTop + fresh;
+		T->pairsLive = T->pairTop - left;
+		T->ncand = ne;
+		T->treeStamp++;
 	}
 }
 
@@ -2308,6 +2467,7 @@ extern "C" int cpg_launch_step(const cpgSet *s, const cpgSet *h, int mode, void 
 	cpgSet sv = *s;
 	/* the per-body warm start needs the colouring's per-body unit table */
 	sv.warmGather = (colored && !h->tape.on && s->warmGather) ? 1 : 0;
+	sv.parMark = (!colored && W == 1 && s->parMark) ? 1 : 0;
 
 	cudaMemsetAsync(s->stats, 0, 16*sizeof(int), st);
 	LAUNCH(k_reset_prev<<<dim3(perWorldX, W), 128, 0, st>>>(*s));
@@ -2337,7 +2497,8 @@ extern "C" int cpg_launch_step(const cpgSet *s, const cpgSet *h, int mode, void 
 		}
 		/* one warp per world in a batch; a single world's leaf scan takes
 		 * 256 threads (thread 0 alone reinserts and marks) */
-		LAUNCH(k_tree<<<W, W == 1 ? 256 : 32, smem, st>>>(*s, staged));
+		LAUNCH(k_tree<<<W, W == 1 ? 256 : 32, smem, st>>>(sv, staged));
+		if(sv.parMark) launch_coop((const void *)k_tree_mark, CPG_MARK_THREADS, &sv, 0, st);
 	}
 	if(timing) cudaEventRecord(ev[2], st);
 	cudaMemsetAsync(s->nbCount, 0, CPG_PAIR_TYPES*sizeof(int), st);

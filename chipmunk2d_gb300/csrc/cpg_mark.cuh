@@ -60,7 +60,16 @@ struct MarkScratch {
 	int nFree;      /* free slots below pairTop */
 	int pairTop;    /* pairTop before the new pairs */
 	int incCap;     /* incidences incEnt holds */
+	int rankCap;    /* entries of emit and ins */
 };
+
+/* a leaf's rank, or -1 (with the error latched) when out of range */
+__device__ __forceinline__ int mark_rank_of(const TreeCtx &c, const MarkScratch &m, int leaf)
+{
+	int r = m.rank[leaf];
+	if(r < 0 || r >= m.rankCap){ c.T->error |= CPG_ERR_NODES; return -1; }
+	return r;
+}
 
 __device__ __forceinline__ bool mark_moved(const TreeCtx &c, int leaf)
 {
@@ -70,7 +79,7 @@ __device__ __forceinline__ bool mark_moved(const TreeCtx &c, int leaf)
 /* Own side of a pair for leaf x: the prev / next links x's list uses. */
 __device__ __forceinline__ void mark_set_links(cpgPair &pr, int x, int prev, int next)
 {
-	if(pr.aLeaf == x){ pr.aPrev = prev; pr.aNext = next; }
+	if(MARK_LOAD(&pr.aLeaf) == x){ pr.aPrev = prev; pr.aNext = next; }
 	else { pr.bPrev = prev; pr.bNext = next; }
 }
 
@@ -86,16 +95,17 @@ __device__ void mark_filter_list(TreeCtx &c, MarkScratch &m, int x)
 	for(int guard = 0; p >= 0; guard++){
 		if(guard > c.pairCap){ c.T->error |= CPG_ERR_PAIRS; break; }
 		cpgPair &pr = c.pairs[p];
-		bool isA = (pr.aLeaf == x);
-		int next = isA ? pr.aNext : pr.bNext;
-		int other = isA ? pr.bLeaf : pr.aLeaf;
+		int pa = MARK_LOAD(&pr.aLeaf), pb = MARK_LOAD(&pr.bLeaf);
+		bool isA = (pa == x);
+		int next = isA ? MARK_LOAD(&pr.aNext) : MARK_LOAD(&pr.bNext);
+		int other = isA ? pb : pa;
 		if(xm || mark_moved(c, other)){
 			pr.pad = 0;
 		} else {
 			if(isA) pr.aPrev = prev; else pr.bPrev = prev;
 			if(prev >= 0){
 				cpgPair &pp = c.pairs[prev];
-				if(pp.aLeaf == x) pp.aNext = p; else pp.bNext = p;
+				if(MARK_LOAD(&pp.aLeaf) == x) pp.aNext = p; else pp.bNext = p;
 			} else {
 				head = p;
 			}
@@ -106,7 +116,7 @@ __device__ void mark_filter_list(TreeCtx &c, MarkScratch &m, int x)
 	}
 	if(prev >= 0){
 		cpgPair &pp = c.pairs[prev];
-		if(pp.aLeaf == x) pp.aNext = -1; else pp.bNext = -1;
+		if(MARK_LOAD(&pp.aLeaf) == x) pp.aNext = -1; else pp.bNext = -1;
 	}
 	c.nodes[x].pairs = head;
 	m.oldB[x] = ob;
@@ -216,7 +226,8 @@ __device__ void mark_count_moved(const TreeCtx &c, MarkScratch &m, int leaf, int
 	f.c = &c; f.m = &m; f.leaf = leaf; f.ne = 0; f.ni = 0;
 	mark_hits(c, leaf, staticRoot, f);
 	if(f.ni) MARK_ADD(&m.incid[leaf], f.ni);
-	int r = m.rank[leaf];
+	int r = mark_rank_of(c, m, leaf);
+	if(r < 0) return;
 	m.emit[r] = f.ne;
 	m.ins[r] = f.ni;
 }
@@ -225,7 +236,8 @@ __device__ void mark_count_moved(const TreeCtx &c, MarkScratch &m, int leaf, int
  * where it is second, then its surviving ones. */
 __device__ void mark_count_still(const TreeCtx &c, MarkScratch &m, int leaf)
 {
-	int r = m.rank[leaf];
+	int r = mark_rank_of(c, m, leaf);
+	if(r < 0) return;
 	m.emit[r] = MARK_LOAD(&m.inc[leaf]) + m.oldB[leaf];
 	m.ins[r] = 0;
 }
@@ -234,12 +246,12 @@ __device__ void mark_count_still(const TreeCtx &c, MarkScratch &m, int leaf)
  * old pairTop in ascending order, then fresh ones. */
 __device__ __forceinline__ int mark_slot(const MarkScratch &m, int g)
 {
-	return g < m.nFree ? m.freeSlot[g] : m.pairTop + (g - m.nFree);
+	return g < m.nFree ? MARK_LOAD(&m.freeSlot[g]) : m.pairTop + (g - m.nFree);
 }
 
 __device__ __forceinline__ void mark_incidence(MarkScratch &m, int x, int g, int slot)
 {
-	int k = m.incid[x] + MARK_ADD(&m.incCur[x], 1);
+	int k = MARK_LOAD(&m.incid[x]) + MARK_ADD(&m.incCur[x], 1);
 	if(k < m.incCap){ m.incEnt[2*k] = g; m.incEnt[2*k + 1] = slot; }
 }
 
@@ -279,8 +291,9 @@ struct MarkWriter {
 __device__ void mark_write_moved(TreeCtx &c, MarkScratch &m, int leaf, int staticRoot)
 {
 	MarkWriter f;
-	int r = m.rank[leaf];
-	f.c = &c; f.m = &m; f.leaf = leaf; f.e = m.emit[r]; f.g = m.ins[r];
+	int r = mark_rank_of(c, m, leaf);
+	if(r < 0) return;
+	f.c = &c; f.m = &m; f.leaf = leaf; f.e = MARK_LOAD(&m.emit[r]); f.g = MARK_LOAD(&m.ins[r]);
 	mark_hits(c, leaf, staticRoot, f);
 }
 
@@ -289,10 +302,13 @@ __device__ void mark_write_moved(TreeCtx &c, MarkScratch &m, int leaf, int stati
  * them. */
 __device__ void mark_link(TreeCtx &c, MarkScratch &m, int x)
 {
-	int lo = m.incid[x], k = MARK_LOAD(&m.incCur[x]);
+	int k = MARK_LOAD(&m.incCur[x]);
 	if(k <= 0) return;
+	int lo = MARK_LOAD(&m.incid[x]);
 	if(lo + k > m.incCap){ c.T->error |= CPG_ERR_PAIRS; return; }
 	int *ent = m.incEnt + 2*lo;
+	/* written by other leaves' threads: read past the L1 once */
+	for(int i = 0; i < 2*k; i++) ent[i] = MARK_LOAD(&ent[i]);
 	/* insertion sort by creation number, descending (lists are short) */
 	for(int i = 1; i < k; i++){
 		int g = ent[2*i], s = ent[2*i + 1], j = i - 1;
@@ -307,7 +323,7 @@ __device__ void mark_link(TreeCtx &c, MarkScratch &m, int x)
 	}
 	if(oldHead >= 0){
 		cpgPair &oh = c.pairs[oldHead];
-		if(oh.aLeaf == x) oh.aPrev = ent[2*k - 1]; else oh.bPrev = ent[2*k - 1];
+		if(MARK_LOAD(&oh.aLeaf) == x) oh.aPrev = ent[2*k - 1]; else oh.bPrev = ent[2*k - 1];
 	}
 	c.nodes[x].pairs = ent[1];
 }
@@ -316,20 +332,23 @@ __device__ void mark_link(TreeCtx &c, MarkScratch &m, int x)
  * (cpBBTree.c:459-468), at its offset. */
 __device__ void mark_emit_still(TreeCtx &c, const MarkScratch &m, int leaf)
 {
-	int e = m.emit[m.rank[leaf]];
+	int r = mark_rank_of(c, m, leaf);
+	if(r < 0) return;
+	int e = MARK_LOAD(&m.emit[r]);
 	int p = c.nodes[leaf].pairs;
 	for(int guard = 0; p >= 0; guard++){
 		if(guard > c.pairCap){ c.T->error |= CPG_ERR_PAIRS; return; }
 		const cpgPair &pr = c.pairs[p];
-		if(pr.bLeaf == leaf){
+		int pa = MARK_LOAD(&pr.aLeaf), pb = MARK_LOAD(&pr.bLeaf);
+		if(pb == leaf){
 			if(e < c.candCap){
-				cpgCand cd; cd.a = c.nodes[pr.aLeaf].obj; cd.b = c.nodes[leaf].obj; cd.pair = p; cd.idIn = pr.id;
+				cpgCand cd; cd.a = c.nodes[pa].obj; cd.b = c.nodes[leaf].obj; cd.pair = p; cd.idIn = MARK_LOAD(&pr.id);
 				c.cands[e] = cd;
 			}
 			e++;
-			p = pr.bNext;
+			p = MARK_LOAD(&pr.bNext);
 		} else {
-			p = pr.aNext;
+			p = MARK_LOAD(&pr.aNext);
 		}
 	}
 }

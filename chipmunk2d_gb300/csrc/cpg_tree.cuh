@@ -470,7 +470,7 @@ __device__ void leaf_reinsert(TreeCtx &c, int leaf, bool clearPairs = true)
  * far above the leaf count).  The whole scan runs before the first
  * reinsertion, so its loads do not evict the tree's top nodes from thread
  * 0's L1 between reinsertions.  Every thread of the block calls it. */
-__device__ void tree_reindex_query_block(TreeCtx &c)
+__device__ void tree_reindex_query_block(TreeCtx &c, bool parallelMark = false)
 {
 	__shared__ int warpTot[32];
 	__shared__ int carry, stop;
@@ -525,8 +525,10 @@ __device__ void tree_reindex_query_block(TreeCtx &c)
 	if(tid == 0){
 		int moved = carry;
 		if((long long)moved > listCap) T->error |= CPG_ERR_CANDS;
-		for(int k = 0; k < moved && !T->error; k++) leaf_reinsert(c, list[k]);
-		if(!T->error){
+		/* with parallelMark the pairs of moved leaves stay threaded and
+		 * k_tree_mark marks the tree (cpg_mark.cuh) */
+		for(int k = 0; k < moved && !T->error; k++) leaf_reinsert(c, list[k], !parallelMark);
+		if(!T->error && !parallelMark){
 			mark_subtree(c, T->dynRoot, T->statRoot);
 			T->treeStamp++;
 		}

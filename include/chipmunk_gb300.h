@@ -568,6 +568,10 @@ void cpGpuDebugSetFlowSolve(int on);
  * per-body gather of the cached impulses in colour order (1) or as colour
  * levels of the sweep (0, default).  Both give the same results. */
 void cpGpuDebugSetWarmStartGather(int on);
+/* Debug: a single space's exact-order tree marked by parallel phases (1)
+ * instead of one device thread (0, default).  Both give the same
+ * candidates, pair lists and results. */
+void cpGpuDebugSetParallelMarking(int on);
 /* Bookkeeping of the last step (after it completes): [0] error flags,
  * [1] pair-pool use and [2] node-pool use (per mille of capacity, largest
  * world), [3] live cached arbiters, [4] candidate pairs, [5] solved

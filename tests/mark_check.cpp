@@ -119,6 +119,7 @@ static void parallel_step(TreeCtx &c)
 	m.cnt = cnt.data(); m.arrive = arrive.data(); m.rank = rank.data(); m.oldB = oldB.data(); m.inc = inc.data();
 	m.incid = incid.data(); m.incCur = incCur.data(); m.emit = emit.data(); m.ins = ins.data();
 	m.freeSlot = freeSlot.data();
+	m.rankCap = (int)dyn.size() + 1;
 
 	/* 1: drop the moved leaves' pairs from every list */
 	for(int n : dyn) mark_filter_list(c, m, n);
