@@ -194,7 +194,7 @@ static void write_ids(TreeCtx &c, int step)
 	}
 }
 
-static int run(int ndyn, int nstat, int steps, double speed, unsigned long long seed)
+static int run(int ndyn, int nstat, int steps, double speed, unsigned long long seed, double gravity = 0.0)
 {
 	rng = seed;
 	Shapes sh;
@@ -252,9 +252,14 @@ static int run(int ndyn, int nstat, int steps, double speed, unsigned long long 
 			if(u < 0.05){ sh.vx[i] = 0.0; sh.vy[i] = 0.0; }
 			else if(u < 0.10){ sh.vx[i] = 4.0*speed*(urand() - 0.5); sh.vy[i] = 4.0*speed*(urand() - 0.5); }
 			else { sh.vx[i] += 0.2*speed*(urand() - 0.5); sh.vy[i] += 0.2*speed*(urand() - 0.5); }
+			sh.vy[i] -= gravity*0.1;
 			sh.cx[i] += sh.vx[i]*0.1; sh.cy[i] += sh.vy[i]*0.1;
 			if(sh.cx[i] < 0.0 || sh.cx[i] > side) sh.vx[i] = -sh.vx[i];
-			if(sh.cy[i] < 0.0 || sh.cy[i] > side) sh.vy[i] = -sh.vy[i];
+			if(gravity > 0.0 && sh.cy[i] < 1.0 + sh.hh[i]){
+				/* a pile on the floor: resting boxes keep still */
+				sh.cy[i] = 1.0 + sh.hh[i]; sh.vy[i] = 0.0; sh.vx[i] *= 0.5;
+				if(urand() < 0.9){ sh.vx[i] = 0.0; }
+			} else if(sh.cy[i] < 0.0 || sh.cy[i] > side) sh.vy[i] = -sh.vy[i];
 			set_box(sh, i);
 		}
 		TreeCtx ca = ctx(A, sh), cb = ctx(B, sh);
@@ -292,6 +297,7 @@ int main()
 	bad |= run(2000, 5, 40, 6.0, 2);
 	bad |= run(800, 0, 40, 1.0, 3);
 	bad |= run(1500, 10, 30, 20.0, 4);
+	bad |= run(3000, 5, 80, 3.0, 5, 2.0);
 	printf("parallel marking: %ld mismatches\n", mismatches);
 	return (bad || mismatches) ? 1 : 0;
 }
