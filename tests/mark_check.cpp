@@ -99,8 +99,21 @@ static void excl_scan(int *a, int n, int *total)
 	if(total) *total = acc;
 }
 
+/* the items of a phase in a random order: the phases claim their items are
+ * independent, so any order (as threads would run them) gives the same */
+static std::vector<int> shuffled(std::vector<int> v)
+{
+	for(size_t i = v.size(); i > 1; i--){
+		size_t j = (size_t)(urand()*(double)i);
+		if(j >= i) j = i - 1;
+		int t = v[i - 1]; v[i - 1] = v[j]; v[j] = t;
+	}
+	return v;
+}
+
 /* the same step with the moved leaves' pairs kept through the reinsertions
- * and the parallel marking phases run as loops, in phase order */
+ * and the parallel marking phases run as loops, in phase order, each over
+ * its items in a fresh random order */
 static void parallel_step(TreeCtx &c)
 {
 	cpgTree *T = c.T;
@@ -122,17 +135,17 @@ static void parallel_step(TreeCtx &c)
 	m.rankCap = (int)dyn.size() + 1;
 
 	/* 1: drop the moved leaves' pairs from every list */
-	for(int n : dyn) mark_filter_list(c, m, n);
-	for(int n : stat) mark_filter_list(c, m, n);
+	for(int n : shuffled(dyn)) mark_filter_list(c, m, n);
+	for(int n : shuffled(stat)) mark_filter_list(c, m, n);
 	/* free slots below pairTop, ascending */
 	m.nFree = 0; m.pairTop = T->pairTop;
 	for(int p = 0; p < T->pairTop; p++) if(c.pairs[p].pad == 0) freeSlot[m.nFree++] = p;
 	/* 2: depth-first ranks */
-	for(int n : dyn) mark_count_up(c, m, n);
-	for(int n : dyn) mark_rank(c, m, n);
+	for(int n : shuffled(dyn)) mark_count_up(c, m, n);
+	for(int n : shuffled(dyn)) mark_rank(c, m, n);
 	/* 3: counts (every moved leaf before any leaf that did not move) */
-	for(int n : moved) mark_count_moved(c, m, n, T->statRoot);
-	for(int n : dyn) if(!mark_moved(c, n)) mark_count_still(c, m, n);
+	for(int n : shuffled(moved)) mark_count_moved(c, m, n, T->statRoot);
+	for(int n : shuffled(dyn)) if(!mark_moved(c, n)) mark_count_still(c, m, n);
 	/* 4: prefix sums */
 	int ne = 0, ni = 0, nin = 0;
 	excl_scan(emit.data(), (int)dyn.size(), &ne);
@@ -143,12 +156,14 @@ static void parallel_step(TreeCtx &c)
 	int fresh = ni > m.nFree ? ni - m.nFree : 0;
 	if(ne > c.candCap || T->pairTop + fresh > pairCap){ T->error |= CPG_ERR_CANDS; return; }
 	/* 5: candidates and new pairs of the moved leaves */
-	for(int n : moved) mark_write_moved(c, m, n, T->statRoot);
-	/* 6: new pairs in front of every list */
-	for(int n : dyn) mark_link(c, m, n);
-	for(int n : stat) mark_link(c, m, n);
-	/* 7: the leaves that did not move emit */
-	for(int n : dyn) if(!mark_moved(c, n)) mark_emit_still(c, m, n);
+	for(int n : shuffled(moved)) mark_write_moved(c, m, n, T->statRoot);
+	/* 6, 7: new pairs in front of every list, then the leaves that did not
+	 * move emit (one phase on the device: a leaf links, then emits) */
+	for(int n : shuffled(dyn)){
+		mark_link(c, m, n);
+		if(!mark_moved(c, n)) mark_emit_still(c, m, n);
+	}
+	for(int n : shuffled(stat)) mark_link(c, m, n);
 	/* the pool: slots past the used free ones stay free, in a list again */
 	int left = m.nFree > ni ? m.nFree - ni : 0;
 	for(int k = 0; k < left; k++){
