@@ -15,6 +15,8 @@ import numpy as np
 PKG_DIR = os.path.dirname(os.path.abspath(__file__))
 REPO_DIR = os.path.dirname(PKG_DIR)
 LIB_PATH = os.path.join(PKG_DIR, "_build", "libchipmunk_gb300.so")
+# the seeded workloads (csrc/scenes.c), linked against the product library
+SCENES_PATH = os.path.join(PKG_DIR, "_build", "libcpx_scenes.so")
 HEADER = os.path.join(REPO_DIR, "include", "chipmunk_gb300.h")
 
 
@@ -180,6 +182,7 @@ _GPU_API = {
     "cpGpuDebugArbiters": (I, [P, P, I]),
     "cpGpuDebugConstraints": (I, [P, P, I]),
     "cpGpuDebugSetBodies": (I, [P, P, I]),
+    "cpGpuDebugSetImpulses": (I, [P, P, I, P, I]),
     "cpGpuDebugCandidates": (I, [P, P, I]),
     "cpGpuSetTiming": (None, [I]),
     "cpGpuDebugSetWholeGridSolve": (None, [I]),
@@ -215,11 +218,28 @@ def bind(path, gpu=False):
 
 
 def load_gpu_library():
-    """Load the in-tree GPU drop-in.  Raises if it has not been built."""
+    """Load the in-tree GPU drop-in together with the seeded workloads.
+
+    The workloads live in libcpx_scenes.so, which links against
+    libchipmunk_gb300.so; symbol lookup through its handle also searches the
+    product library it depends on, so one handle serves both.  Raises if
+    they have not been built."""
+    for path in (LIB_PATH, SCENES_PATH):
+        if not os.path.exists(path):
+            raise RuntimeError(
+                "%s is not built; run "
+                "`python -c 'import __graft_entry__ as g; g.build()'`" % os.path.basename(path))
+    # RTLD_LOCAL (ctypes' default): with the product in the global scope,
+    # another implementation of the API loaded later (the oracle) would
+    # bind its own calls to the product's symbols
+    return bind(SCENES_PATH, gpu=True)
+
+
+def load_product_library():
+    """The product library alone (libchipmunk_gb300.so), for checks of what
+    it exports."""
     if not os.path.exists(LIB_PATH):
-        raise RuntimeError(
-            "libchipmunk_gb300.so is not built; run "
-            "`python -c 'import __graft_entry__ as g; g.build()'`")
+        raise RuntimeError("libchipmunk_gb300.so is not built")
     return bind(LIB_PATH, gpu=True)
 
 
@@ -247,6 +267,15 @@ class Scene:
     def set_bodies(self, arr):
         arr = np.ascontiguousarray(arr, dtype=np.float64)
         return self.lib.cpx_set_bodies(self.space, arr.ctypes.data, arr.shape[0])
+
+    def set_impulses(self, arbs, cons):
+        """Warm-start state (GPU library only): accumulated impulses of the
+        last solve list's arbiters and of the constraints, from another
+        implementation's dumps.  Returns the count of skipped records."""
+        arbs = np.ascontiguousarray(arbs, dtype=np.float64)
+        cons = np.ascontiguousarray(cons, dtype=np.float64)
+        return self.lib.cpGpuDebugSetImpulses(self.space, arbs.ctypes.data, arbs.shape[0],
+                                              cons.ctypes.data, cons.shape[0])
 
     def arbiters(self, cap=None):
         cap = cap or max(4 * self.nshapes + 16, 64)

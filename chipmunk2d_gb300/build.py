@@ -20,7 +20,11 @@ NVCC = os.path.join(CUDA_HOME, "bin", "nvcc") if os.path.exists(os.path.join(CUD
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 CU_SOURCES = ["cpg_kernels.cu", "cpg_schedule_api.cu", "cpg_rollout.cu"]
-C_SOURCES = ["cp_host.c", "scenes.c"]
+C_SOURCES = ["cp_host.c"]
+# The seeded workloads the tests and the benchmark build through the public
+# API: a library of their own that links against the product, so the
+# product exports nothing but the API.
+SCENE_SOURCES = ["scenes.c", "scene_export_gpu.c"]
 
 
 def _run(cmd):
@@ -43,12 +47,13 @@ def build(verbose=False, ptxas_info=False):
             cmd += ["-Xptxas", "-v"]
         jobs.append(cmd)
         objs.append(obj)
-    for f in C_SOURCES:
+    for f in C_SOURCES + SCENE_SOURCES:
         obj = os.path.join(OUT, f + ".o")
         cmd = ["gcc", "-std=gnu11", "-O2", "-fPIC", "-ffp-contract=off", "-Wall", "-Wno-unused-function",
                "-c", os.path.join(SRC, f), "-o", obj] + inc
         jobs.append(cmd)
-        objs.append(obj)
+        if f in C_SOURCES:
+            objs.append(obj)
     with ThreadPoolExecutor(max_workers=len(jobs)) as ex:
         outs = list(ex.map(_run, jobs))
     if verbose or ptxas_info:
@@ -59,6 +64,10 @@ def build(verbose=False, ptxas_info=False):
     tmp = lib + ".tmp"
     _run([NVCC] + ARCH + ["-shared", "-o", tmp] + objs + ["-lm"])
     shutil.move(tmp, lib)
+    scenes = os.path.join(OUT, "libcpx_scenes.so")
+    _run(["gcc", "-shared", "-o", scenes + ".tmp"] + [os.path.join(OUT, f + ".o") for f in SCENE_SOURCES] +
+         ["-L" + OUT, "-lchipmunk_gb300", "-Wl,-rpath,$ORIGIN", "-lm"])
+    shutil.move(scenes + ".tmp", scenes)
     return lib
 
 

@@ -279,8 +279,12 @@ void cpGpuDebugSetFlowSolve(int on) { g_flow_solve = on ? 1 : 0; }
  * off unless asked for */
 static int g_warm_gather = 0;
 void cpGpuDebugSetWarmStartGather(int on) { g_warm_gather = on ? 1 : 0; }
-static int g_par_mark = 0;
-void cpGpuDebugSetParallelMarking(int on) { g_par_mark = on ? 1 : 0; }
+/* marking of a single space's exact tree: -1 automatic (the parallel
+ * phases from CPG_PAR_MARK_MIN dynamic shapes up, where they beat one
+ * thread), 0 always serial, 1 always parallel */
+static int g_par_mark = -1;
+#define CPG_PAR_MARK_MIN 1024
+void cpGpuDebugSetParallelMarking(int on) { g_par_mark = on < 0 ? -1 : (on ? 1 : 0); }
 void cpGpuDebugSetTreeStaging(int maxNodes) { g_tree_stage = maxNodes < 0 ? -1 : maxNodes; }
 static int g_whole_grid = 0;     /* 1: single-world sets always use the whole-grid solve */
 
@@ -946,7 +950,7 @@ static int devset_step(DevSet *ds, const double *dts, cpSpace **only)
 	d->solveLayout = g_solve_layout;
 	d->flowSolve = g_flow_solve;
 	d->warmGather = g_warm_gather;
-	d->parMark = g_par_mark;
+	d->parMark = g_par_mark >= 0 ? g_par_mark : (d->hostNdyn >= CPG_PAR_MARK_MIN);
 	/* launch shapes of many-world sets: the tuner's candidates on the steps
 	 * of a tuning window, its choice after it (debug settings win) */
 	int tuning = -1;
@@ -2611,6 +2615,45 @@ int cpGpuDebugSetBodies(cpSpace *sp, const double *in, int count)
 	return sp->ndyn;
 }
 
+int cpGpuDebugSetImpulses(cpSpace *sp, const double *arbs, int narb, const double *cons, int ncons)
+{
+	int bad = 0;
+	if(sp->dev && narb > 0){
+		DevSet *ds = sp->dev;
+		space_pull(sp);
+		double *himp = HALLOC(double, 4*narb);
+		int *hpair = HALLOC(int, 2*narb);
+		for(int i = 0; i < narb; i++){
+			const double *o = arbs + 34*i;
+			hpair[2*i] = (int)o[0]; hpair[2*i + 1] = (int)o[1];
+			himp[4*i] = o[17]; himp[4*i + 1] = o[18]; himp[4*i + 2] = o[29]; himp[4*i + 3] = o[30];
+		}
+		char *buf = NULL;
+		size_t bi = sizeof(double)*4*(size_t)narb, bp = sizeof(int)*2*(size_t)narb;
+		if(cuda_ok(cudaMalloc((void **)&buf, bi + bp + 16), "debug impulses")){
+			cudaStream_t st = lib_stream();
+			int *mis = (int *)(buf + bi + bp);
+			int ok = h2d(buf, himp, bi) && h2d(buf + bi, hpair, bp) &&
+				cuda_ok(cudaMemsetAsync(mis, 0, sizeof(int), st), "memset");
+			if(ok && cpg_launch_set_arb_impulses(&ds->d, sp->world, (const double *)buf, (const int *)(buf + bi), narb, mis, st) == 0)
+				d2h(&bad, mis, sizeof(int));
+			cudaStreamSynchronize(st);
+			cudaFree(buf);
+		}
+		free(himp); free(hpair);
+		sp->snapValid = 0;
+	}
+	for(int i = 0; i < sp->ncons && i < ncons; i++){
+		cpConstraint *c = sp->cons[i];
+		const double *o = cons + 8*i;
+		cons_pull_(c);
+		if(c->kind == CPG_PIVOT){ c->rec.jx = o[1]; c->rec.jy = o[2]; }
+		else c->rec.jnAcc = o[1];
+		sp->consDirty = 1;
+	}
+	return bad;
+}
+
 int cpGpuDebugArbiters(cpSpace *sp, double *out, int max)
 {
 	if(!space_snapshot(sp)) return 0;
@@ -2697,9 +2740,3 @@ int cpGpuDebugCandidates(cpSpace *sp, int *out, int max)
 	return k;
 }
 
-/* The shared harness names used by the tests for every implementation. */
-int cpx_dump_bodies(cpSpace *sp, double *out, int max) { return cpGpuDebugBodies(sp, out, max); }
-int cpx_dump_arbiters(cpSpace *sp, double *out, int max) { return cpGpuDebugArbiters(sp, out, max); }
-int cpx_dump_constraints(cpSpace *sp, double *out, int max) { return cpGpuDebugConstraints(sp, out, max); }
-int cpx_set_bodies(cpSpace *sp, const double *in, int count) { return cpGpuDebugSetBodies(sp, in, count); }
-int cpx_dump_candidates(cpSpace *sp, int *out, int max) { return cpGpuDebugCandidates(sp, out, max); }

@@ -358,6 +358,7 @@ int cpg_launch_tape_vel(const cpgSet *s, void *stream);
 int cpg_launch_step_graph(const cpgSet *s, int mode, void *stream, void **cache);
 void cpg_step_graph_free(void *cache);
 int cpg_launch_replay_solve(const cpgSet *s, const cpgAdj *a, int nsteps, void *stream);
+int cpg_launch_set_arb_impulses(const cpgSet *s, int w, const double *imp, const int *pairs, int n, int *mismatch, void *stream);
 
 #ifdef __cplusplus
 }

@@ -300,8 +300,16 @@ __device__ int grid_excl_scan(cg::grid_group &grid, int *a, int n, int *blockSum
 /* The phases, in order (each loop over leaves takes hash bins with the
  * same bin-to-thread mapping, so a leaf's own writes are read back by the
  * thread that made them). */
-#define MARK_DYN_LEAVES(n) for(unsigned i_ = gtid; i_ < dsize; i_ += gsz) for(int n = c.dbins[i_], g_ = 0; n >= 0 && g_ <= c.nodeCap; n = c.nodes[n].binNext, g_++)
-#define MARK_STAT_LEAVES(n) for(unsigned i_ = gtid; i_ < ssize; i_ += gsz) for(int n = c.sbins[i_], g_ = 0; n >= 0 && g_ <= c.nodeCap; n = c.nodes[n].binNext, g_++)
+/* A bin chain longer than the node pool is corrupt (a cycle): the walk
+ * stops there and latches CPG_ERR_BINS, as the serial re-index scan does. */
+__device__ __forceinline__ bool mark_bin_ok(const TreeCtx &c, int n, int g)
+{
+	if(n < 0) return false;
+	if(g > c.nodeCap){ atomicOr(&c.T->error, CPG_ERR_BINS); return false; }
+	return true;
+}
+#define MARK_DYN_LEAVES(n) for(unsigned i_ = gtid; i_ < dsize; i_ += gsz) for(int n = c.dbins[i_], g_ = 0; mark_bin_ok(c, n, g_); n = c.nodes[n].binNext, g_++)
+#define MARK_STAT_LEAVES(n) for(unsigned i_ = gtid; i_ < ssize; i_ += gsz) for(int n = c.sbins[i_], g_ = 0; mark_bin_ok(c, n, g_); n = c.nodes[n].binNext, g_++)
 
 __global__ void __launch_bounds__(CPG_MARK_THREADS, 1) k_tree_mark(cpgSet s, int w)
 {
@@ -1599,6 +1607,30 @@ __global__ void k_stats(cpgSet s)
 	}
 }
 
+/* Overwrite the accumulated impulses of one world's last solve list with
+ * records in its order (4 doubles each: jnAcc, jtAcc of contacts 0, 1;
+ * 2 ints each: the shapes the record belongs to).  A record whose shapes
+ * differ from the listed arbiter's is skipped and counted in *mismatch. */
+__global__ void k_set_arb_impulses(cpgSet s, int w, const double *imp, const int *pairs, int n, int *mismatch)
+{
+	int i = blockIdx.x*blockDim.x + threadIdx.x;
+	const cpgTree &T = s.tree[w];
+	if(i >= n || i >= T.narb) return;
+	cpgArb &arb = s.arbs[s.arbList[s.world[w].candOff + i]];
+	if(arb.a != pairs[2*i] || arb.b != pairs[2*i + 1]){ atomicAdd(mismatch, 1); return; }
+	for(int k = 0; k < arb.count && k < 2; k++){
+		arb.c[k].jnAcc = imp[4*i + 2*k];
+		arb.c[k].jtAcc = imp[4*i + 2*k + 1];
+	}
+}
+
+extern "C" int cpg_launch_set_arb_impulses(const cpgSet *s, int w, const double *imp, const int *pairs, int n, int *mismatch, void *stream)
+{
+	if(n <= 0) return 0;
+	LAUNCH(k_set_arb_impulses<<<(n + 127)/128, 128, 0, (cudaStream_t)stream>>>(*s, w, imp, pairs, n, mismatch));
+	return cudaGetLastError() == cudaSuccess ? 0 : -1;
+}
+
 /* Copy one world's solve list of arbiters into a contiguous buffer. */
 __global__ void k_gather_arbs(cpgSet s, int w, cpgArb *out, int n)
 {
@@ -2469,6 +2501,10 @@ extern "C" int cpg_launch_step(const cpgSet *s, const cpgSet *h, int mode, void 
 	sv.warmGather = (colored && !h->tape.on && s->warmGather) ? 1 : 0;
 	sv.parMark = (!colored && W == 1 && s->parMark) ? 1 : 0;
 
+	/* a refused cooperative launch (occupancy, an unsupported context)
+	 * fails the step: the kernels after it would run on a half-done step */
+	cudaError_t coop = cudaSuccess;
+#define COOP(kernel, threads) do { cudaError_t e_ = launch_coop((const void *)(kernel), (threads), &sv, 0, st); if(e_ != cudaSuccess && coop == cudaSuccess) coop = e_; } while(0)
 	cudaMemsetAsync(s->stats, 0, 16*sizeof(int), st);
 	LAUNCH(k_reset_prev<<<dim3(perWorldX, W), 128, 0, st>>>(*s));
 	LAUNCH(k_integrate_pos<<<blocks_for(h->totalBodies, 128), 128, 0, st>>>(*s));
@@ -2476,7 +2512,7 @@ extern "C" int cpg_launch_step(const cpgSet *s, const cpgSet *h, int mode, void 
 	if(timing) cudaEventRecord(ev[1], st);
 	if(colored){
 		int n = h->hostNdyn;
-		launch_coop((const void *)k_sap_sort, SAP_THREADS, &sv, 0, st);
+		COOP(k_sap_sort, SAP_THREADS);
 		LAUNCH(k_sap_count<<<blocks_for(32*n, 256), 256, 0, st>>>(*s, 0));
 		LAUNCH(k_scan_excl<<<1, 1024, 0, st>>>(s->sapCount, n + 1, NULL));
 		LAUNCH(k_sap_emit<<<blocks_for(32*n, 256), 256, 0, st>>>(*s, 0));
@@ -2498,7 +2534,7 @@ extern "C" int cpg_launch_step(const cpgSet *s, const cpgSet *h, int mode, void 
 		/* one warp per world in a batch; a single world's leaf scan takes
 		 * 256 threads (thread 0 alone reinserts and marks) */
 		LAUNCH(k_tree<<<W, W == 1 ? 256 : 32, smem, st>>>(sv, staged));
-		if(sv.parMark) launch_coop((const void *)k_tree_mark, CPG_MARK_THREADS, &sv, 0, st);
+		if(sv.parMark) COOP(k_tree_mark, CPG_MARK_THREADS);
 	}
 	if(timing) cudaEventRecord(ev[2], st);
 	cudaMemsetAsync(s->nbCount, 0, CPG_PAIR_TYPES*sizeof(int), st);
@@ -2514,7 +2550,7 @@ extern "C" int cpg_launch_step(const cpgSet *s, const cpgSet *h, int mode, void 
 	}
 	LAUNCH(k_arb_filter<<<blocks_for(h->arbCap, 256), 256, 0, st>>>(*s));
 	if(timing) cudaEventRecord(ev[4], st);
-	if(colored) launch_coop((const void *)k_color_coop, 512, &sv, 0, st);
+	if(colored) COOP(k_color_coop, 512);
 	else LAUNCH(k_schedule<<<blocks_for(W, 32), 32, 0, st>>>(*s));
 	if(timing) cudaEventRecord(ev[5], st);
 	LAUNCH(k_build_rows<<<dim3(perWorldX, W), 128, 0, st>>>(*s));
@@ -2523,9 +2559,9 @@ extern "C" int cpg_launch_step(const cpgSet *s, const cpgSet *h, int mode, void 
 	if(h->tape.on) cpg_launch_tape_vel(s, st);
 	if(timing) cudaEventRecord(ev[6], st);
 	if(W == 1 && colored){
-		launch_coop((const void *)k_solve_coop<true>, CPG_COOP_SOLVE_THREADS, &sv, 0, st);
+		COOP(k_solve_coop<true>, CPG_COOP_SOLVE_THREADS);
 	} else if(W == 1 && h->hostUnitsHint >= CPG_COOP_UNITS && !h->tape.on){
-		launch_coop((const void *)k_solve_coop<false>, CPG_COOP_SOLVE_THREADS, &sv, 0, st);
+		COOP(k_solve_coop<false>, CPG_COOP_SOLVE_THREADS);
 	} else {
 		int stagedMax = h->hostMaxBodies <= CPG_STAGED_BODIES ? h->hostMaxBodies : 0;
 		if(h->hostSolveStage >= 0 && h->hostSolveStage < stagedMax) stagedMax = h->hostSolveStage;
@@ -2544,7 +2580,12 @@ extern "C" int cpg_launch_step(const cpgSet *s, const cpgSet *h, int mode, void 
 	LAUNCH(k_unpack_bodies<<<blocks_for(h->totalBodies, 128), 128, 0, st>>>(*s));
 	if(timing) cudaEventRecord(ev[7], st);
 	LAUNCH(k_stats<<<1, 256, 0, st>>>(*s));
+#undef COOP
 	cudaError_t e = check_launch("step");
+	if(coop != cudaSuccess){
+		fprintf(stderr, "chipmunk_gb300: a cooperative launch was refused: %s\n", cudaGetErrorString(coop));
+		e = coop;
+	}
 	if(timing){
 		cudaEventSynchronize(ev[7]);
 		for(int i = 0; i < 7; i++) cudaEventElapsedTime(&phase_ms[i], ev[i], ev[i + 1]);

@@ -59,11 +59,21 @@ __global__ void k_schedule_api(const int *bodyA, const int *bodyB, int nunits, i
 	schedule_levels(bodyA, bodyB, nunits, nbodies, last, level, levelStart, order, nlevels);
 }
 
+/* levelStart always receives levelStart[0] = 0, even for an empty
+ * sequence, so it must be a device array of nunits + 1 ints whatever
+ * nunits is; order and the body arrays are only touched when nunits > 0. */
+static bool schedule_args_ok(const int *bodyA, const int *bodyB, int nunits, int nbodies,
+                             const int *levelStart, const int *order, const int *nlevels)
+{
+	if(nunits < 0 || nbodies < 0 || !levelStart || !nlevels) return false;
+	if(nunits > 0 && (!bodyA || !bodyB || !order)) return false;
+	return true;
+}
+
 extern "C" int cpGpuSolveSchedule(const int *bodyA, const int *bodyB, int nunits, int nbodies,
                                   int *levelStart, int *order, int *nlevels, void *stream)
 {
-	if(nunits < 0 || nbodies < 0 || (nunits > 0 && (!bodyA || !bodyB || !levelStart || !order)) || !nlevels)
-		return CP_GPU_ERR_ARGUMENT;
+	if(!schedule_args_ok(bodyA, bodyB, nunits, nbodies, levelStart, order, nlevels)) return CP_GPU_ERR_ARGUMENT;
 	cudaStream_t st = (cudaStream_t)stream;
 	int *scratch = NULL;
 	size_t words = (size_t)nbodies + (size_t)nunits + 1;
@@ -102,8 +112,7 @@ static int *g_schedule_scratch_addr[CPG_SCHEDULE_MAX_DEVICES];
 extern "C" int cpGpuSolveScheduleNoAlloc(const int *bodyA, const int *bodyB, int nunits, int nbodies,
                                          int *levelStart, int *order, int *nlevels, void *stream)
 {
-	if(nunits < 0 || nbodies < 0 || (nunits > 0 && (!bodyA || !bodyB || !levelStart || !order)) || !nlevels)
-		return CP_GPU_ERR_ARGUMENT;
+	if(!schedule_args_ok(bodyA, bodyB, nunits, nbodies, levelStart, order, nlevels)) return CP_GPU_ERR_ARGUMENT;
 	if(nunits > CPG_SCHEDULE_STATIC_MAX_UNITS || nbodies > CPG_SCHEDULE_STATIC_MAX_BODIES){
 		fprintf(stderr, "cpGpuSolveScheduleNoAlloc: %d units / %d bodies exceed the fixed scratch (%d units, %d bodies)\n",
 			nunits, nbodies, CPG_SCHEDULE_STATIC_MAX_UNITS, CPG_SCHEDULE_STATIC_MAX_BODIES);

@@ -32,7 +32,10 @@
  *   5  adjoint world: `size`/2 circles r~U[1,3] and `size`/2 boxes with
  *      sides U[2,6] at random orientations, dropped onto a static ground
  *      segment, density 1, u 0.7, e 0.1.
- * Gravity, time step and iterations are set by the caller.
+ *   6  joints and filters: pin-joint chains, slide-joint pairs and ropes,
+ *      filtered free bodies (build_joints below).
+ * Gravity is (0,-100); iterations are set per workload; the time step is
+ * the caller's.
  */
 #include <stdlib.h>
 #include <string.h>
@@ -357,6 +360,119 @@ static void build_adjoint(cpxScene *sc, int n, uint64_t seed)
 	}
 }
 
+/* Workload 6, joints and filters: pin-joint chains, slide-joint pairs and
+ * ropes, and free bodies sorted into collision categories.
+ *   - size/40 chains [1] of 8 boxes 1 x 3 (mass 1) joined by pin joints
+ *     between anchors 1.25 from their centres, 2.75 apart, so neighbouring
+ *     links overlap by 0.25 and only their shared filter group keeps them
+ *     from colliding; each chain hangs by a pin joint from a static anchor;
+ *     every third chain's joints have a finite maxForce (the
+ *     impulse clamp binds) and a finite maxBias; chains start swinging.
+ *   - size/8 pairs of circles r~U[1,2] joined by a slide joint (min 3,
+ *     max 6) at a separation U[1.5,8], so joints start below min, inside
+ *     the band (n = 0) or beyond max, with v~N(0,15)/axis; every fourth has
+ *     a finite maxForce; collideBodies off on every other pair.
+ *   - size/8 circles hung from static anchors by slide joints (min 0,
+ *     max U[4,12]), the anchors at the circles' start, so each rope is
+ *     slack until the fall takes it past max.
+ *   - `size` free bodies, circles r~U[1,3] and hull polys of radius U[1,3],
+ *     category 1 << (i % 3); mask all categories, except every fifth body,
+ *     which masks out the next category ((i + 1) % 3).
+ * Container: square of half-size 60 sqrt(size/40) of 4 static segments r 1;
+ * u~U[0.3,1], e~U[0,0.3], v~N(0,5)/axis unless stated; density 1. */
+static void build_joints(cpxScene *sc, int n, uint64_t seed)
+{
+	Rng rng; rng_seed(&rng, seed);
+	double half = 60.0*sqrt((double)n/40.0);
+	if(half < 40.0) half = 40.0;
+	add_box_walls(sc, half, half, 1.0, 0.7, 0.1);
+	cpBody *ground = cpSpaceGetStaticBody(sc->space);
+	double top = half - 4.0;
+
+	int chains = n/40;
+	if(chains < 1) chains = 1;
+	for(int c = 0; c < chains; c++){
+		double x = -half + ((double)c + 0.5)*(2.0*half/(double)chains);
+		cpShapeFilter f = { (cpGroup)(uintptr_t)(c + 1), CP_ALL_CATEGORIES, CP_ALL_CATEGORIES };
+		cpBody *prev = ground;
+		cpVect prevAnchor = cpv(x, top);
+		double vx0 = 10.0*rng_normal(&rng);
+		for(int l = 0; l < 8; l++){
+			double cy = top - 0.25 - 1.25 - 2.75*(double)l;
+			cpBody *link = cpBodyNew(1.0, cpMomentForBox(1.0, 1.0, 3.0));
+			cpBodySetPosition(link, cpv(x, cy));
+			cpBodySetVelocity(link, cpv(vx0*(double)(l + 1)/8.0, 0.0));
+			add_body(sc, link);
+			cpShape *s = cpBoxShapeNew(link, 1.0, 3.0, 0.0);
+			cpShapeSetFriction(s, rng_uniform(&rng, 0.3, 1.0));
+			cpShapeSetElasticity(s, rng_uniform(&rng, 0.0, 0.3));
+			cpShapeSetFilter(s, f);
+			add_shape(sc, s);
+			cpConstraint *j = cpPinJointNew(prev, link, prevAnchor, cpv(0.0, 1.25));
+			if(c % 3 == 2){
+				cpConstraintSetMaxForce(j, 3000.0);
+				cpConstraintSetMaxBias(j, 40.0);
+			}
+			add_constraint(sc, j);
+			prev = link;
+			prevAnchor = cpv(0.0, -1.25);
+		}
+	}
+
+	double lo = -half + 6.0, hi = half - 6.0;
+	double ylo = -half + 6.0, yhi = top - 32.0;
+	int pairs = n/8;
+	for(int i = 0; i < pairs; i++){
+		cpVect p = cpv(rng_uniform(&rng, lo, hi), rng_uniform(&rng, ylo, yhi));
+		cpVect d = rng_direction(&rng);
+		double sep = rng_uniform(&rng, 1.5, 8.0);
+		cpBody *bb[2];
+		for(int k = 0; k < 2; k++){
+			double r = rng_uniform(&rng, 1.0, 2.0), m = 3.14159265358979323846*r*r;
+			cpBody *body = cpBodyNew(m, cpMomentForCircle(m, 0.0, r, cpvzero));
+			cpBodySetPosition(body, cpvadd(p, cpvmult(d, k ? 0.5*sep : -0.5*sep)));
+			cpBodySetVelocity(body, cpv(15.0*rng_normal(&rng), 15.0*rng_normal(&rng)));
+			add_body(sc, body);
+			cpShape *s = cpCircleShapeNew(body, r, cpvzero);
+			cpShapeSetFriction(s, rng_uniform(&rng, 0.3, 1.0));
+			cpShapeSetElasticity(s, rng_uniform(&rng, 0.0, 0.3));
+			add_shape(sc, s);
+			bb[k] = body;
+		}
+		cpConstraint *j = cpSlideJointNew(bb[0], bb[1], cpvzero, cpvzero, 3.0, 6.0);
+		if(i % 4 == 3) cpConstraintSetMaxForce(j, 5000.0);
+		if(i % 2 == 1) cpConstraintSetCollideBodies(j, cpFalse);
+		add_constraint(sc, j);
+	}
+
+	int ropes = n/8;
+	for(int i = 0; i < ropes; i++){
+		cpVect p = cpv(rng_uniform(&rng, lo, hi), rng_uniform(&rng, ylo, yhi));
+		double r = rng_uniform(&rng, 1.0, 2.0), m = 3.14159265358979323846*r*r;
+		cpBody *body = cpBodyNew(m, cpMomentForCircle(m, 0.0, r, cpvzero));
+		cpBodySetPosition(body, p);
+		cpBodySetVelocity(body, cpv(5.0*rng_normal(&rng), 5.0*rng_normal(&rng)));
+		add_body(sc, body);
+		cpShape *s = cpCircleShapeNew(body, r, cpvzero);
+		cpShapeSetFriction(s, rng_uniform(&rng, 0.3, 1.0));
+		cpShapeSetElasticity(s, rng_uniform(&rng, 0.0, 0.3));
+		add_shape(sc, s);
+		add_constraint(sc, cpSlideJointNew(ground, body, p, cpvzero, 0.0, rng_uniform(&rng, 4.0, 12.0)));
+	}
+
+	for(int i = 0; i < n; i++){
+		cpVect p = cpv(rng_uniform(&rng, lo, hi), rng_uniform(&rng, ylo, yhi));
+		cpVect v = cpv(5.0*rng_normal(&rng), 5.0*rng_normal(&rng));
+		double u = rng_uniform(&rng, 0.3, 1.0), e = rng_uniform(&rng, 0.0, 0.3);
+		if(i & 1) add_random_poly(sc, &rng, p, v, rng_int(&rng, 3, 6), rng_uniform(&rng, 1.0, 3.0), u, e);
+		else add_circle(sc, p, v, rng_uniform(&rng, 1.0, 3.0), u, e);
+		cpBitmask cat = (cpBitmask)1u << (i % 3);
+		cpBitmask mask = (i % 5 == 0) ? (CP_ALL_CATEGORIES & ~((cpBitmask)1u << ((i + 1) % 3))) : CP_ALL_CATEGORIES;
+		cpShapeFilter f = { CP_NO_GROUP, cat, mask };
+		cpShapeSetFilter(sc->shapes[sc->nshapes - 1], f);
+	}
+}
+
 /* ---- exported harness entry points (cpx_ prefix: workload plumbing, not
  * part of the Chipmunk2D API) ---- */
 
@@ -371,6 +487,7 @@ void *cpx_scene_build(int config, int size, unsigned long long seed)
 		case 3: build_mixed(sc, size > 0 ? size : 30000, seed); cpSpaceSetIterations(sc->space, 15); break;
 		case 4: build_tumble(sc, size > 0 ? size : 121, seed); cpSpaceSetIterations(sc->space, 10); break;
 		case 5: build_adjoint(sc, size > 0 ? size : 64, seed); cpSpaceSetIterations(sc->space, 10); break;
+		case 6: build_joints(sc, size > 0 ? size : 400, seed); cpSpaceSetIterations(sc->space, 10); break;
 		default: cpSpaceFree(sc->space); free(sc); return NULL;
 	}
 	return sc;

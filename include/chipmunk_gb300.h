@@ -456,7 +456,9 @@ void cpGpuSetAutotune(int on);
  * *nlevels is the number of levels.  Units of one level share no body, and
  * running the levels in turn applies every body's updates in the original
  * sweep order, so the result equals the serial sweep exactly.  All pointers
- * are device pointers; levelStart holds nunits + 1 ints.  The call is
+ * are device pointers; levelStart holds nunits + 1 ints and must be given
+ * even when nunits is 0 (levelStart[0] is always written); order and the
+ * body arrays may be NULL only when nunits is 0.  The call is
  * stream-ordered on `stream` and returns a CP_GPU_* code; its scratch comes
  * from cudaMallocAsync on that stream. */
 int cpGpuSolveSchedule(const int *bodyA, const int *bodyB, int nunits, int nbodies,
@@ -470,10 +472,19 @@ int cpGpuSolveSchedule(const int *bodyA, const int *bodyB, int nunits, int nbodi
  * every GPU that loads the library until exit.  Limits: nunits <= 1048576
  * and nbodies <= 1048576; larger inputs are rejected with
  * CP_GPU_ERR_ARGUMENT and a message on stderr.  The first call on a device
- * looks up the array's device address (make it before any stream capture
- * on that device).  Calls share the array: calls that overlap on the GPU
- * race, so serialise them (one stream, or events).  Inputs and outputs are
- * caller-provided device pointers, as for cpGpuSolveSchedule. */
+ * does a one-time set-up with that device current: it looks up the array's
+ * device address, and with CUDA's default lazy module loading that lookup
+ * is also what loads this part of the library onto the device, which is
+ * when the 8 MiB array is created (an allocation by the driver, and it may
+ * synchronise).  So make the first call during start-up, before any frame
+ * loop and before any stream capture on that device (a call with nunits =
+ * 0 and a one-int levelStart does it), or run the process with
+ * CUDA_MODULE_LOADING=EAGER.  Every later call allocates nothing.  The
+ * cached address belongs to the device's primary context: after
+ * cudaDeviceReset the library must be reloaded.  Calls share the array:
+ * calls that overlap on the GPU race, so serialise them (one stream, or
+ * events).  Inputs and outputs are caller-provided device pointers, as for
+ * cpGpuSolveSchedule, with the same argument rules. */
 int cpGpuSolveScheduleNoAlloc(const int *bodyA, const int *bodyB, int nunits, int nbodies,
                               int *levelStart, int *order, int *nlevels, void *stream);
 
@@ -493,6 +504,15 @@ int cpGpuDebugConstraints(cpSpace *space, double *out, int max);
  * constraints' accumulated impulses; used to run one step from a state
  * taken from another implementation. */
 int cpGpuDebugSetBodies(cpSpace *space, const double *in, int count);
+/* Overwrite the warm-start state the next step starts from: the
+ * accumulated contact impulses of the arbiters of the last solve list (in
+ * the arbiters layout above, in solve order; records whose shape pair
+ * differs from the listed arbiter's are skipped) and the constraints'
+ * accumulated impulses (constraints layout, j0 and j1 of pivots, j0 of
+ * pin and slide joints).  Returns the number of skipped arbiter records.
+ * Used with cpGpuDebugSetBodies to run one step from another
+ * implementation's complete state. */
+int cpGpuDebugSetImpulses(cpSpace *space, const double *arbs, int narb, const double *cons, int ncons);
 /* Shape-id pairs (min, max) of the last step whose boxes intersect: the
  * pair set the broadphase handed to the narrow phase (2 ints per pair). */
 int cpGpuDebugCandidates(cpSpace *space, int *out, int max);
@@ -568,9 +588,10 @@ void cpGpuDebugSetFlowSolve(int on);
  * per-body gather of the cached impulses in colour order (1) or as colour
  * levels of the sweep (0, default).  Both give the same results. */
 void cpGpuDebugSetWarmStartGather(int on);
-/* Debug: a single space's exact-order tree marked by parallel phases (1)
- * instead of one device thread (0, default).  Both give the same
- * candidates, pair lists and results. */
+/* Debug: how a single space's exact-order tree is marked: by parallel
+ * phases (1), by one device thread (0), or automatically (-1, default:
+ * parallel from 1024 dynamic shapes up).  All give the same candidates,
+ * pair lists and results. */
 void cpGpuDebugSetParallelMarking(int on);
 /* Bookkeeping of the last step (after it completes): [0] error flags,
  * [1] pair-pool use and [2] node-pool use (per mille of capacity, largest

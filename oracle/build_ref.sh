@@ -10,9 +10,14 @@
 # spins forever under gcc 13), so this recipe builds with strict IEEE
 # semantics and no FMA contraction (GNU C contracts by default on aarch64).
 #
-# Usage: oracle/build_ref.sh [REFERENCE_ROOT]   (default /root/reference)
+# Usage: oracle/build_ref.sh REFERENCE_ROOT
+#    or: CHIPMUNK_REF_ROOT=... oracle/build_ref.sh
 set -e
-REF=${1:-/root/reference}
+REF=${1:-$CHIPMUNK_REF_ROOT}
+if [ -z "$REF" ]; then
+	echo "usage: $0 REFERENCE_ROOT (or set CHIPMUNK_REF_ROOT)" >&2
+	exit 2
+fi
 HERE=$(cd "$(dirname "$0")" && pwd)
 REPO=$(cd "$HERE/.." && pwd)
 OUT="$HERE/_ref"

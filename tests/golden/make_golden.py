@@ -6,7 +6,7 @@ seeded workloads and records the full state (bodies, arbiters in solve
 order, joints) at a few checkpoints.  The fixtures travel with the
 repository, so the oracle stays pinned where the reference cannot be built.
 
-Usage:  python tests/golden/make_golden.py
+Usage:  python tests/golden/make_golden.py [fixture names]
 """
 import os
 import sys
@@ -26,12 +26,15 @@ FIXTURES = [
     ("mixed", 3, 600, 1 / 60, [1, 5, 40]),
     ("tumble", 4, 150, 1 / 60, [1, 5, 60]),
     ("adjoint", 5, 64, 1 / 120, [1, 5, 120]),
+    ("joints", 6, 120, 1 / 60, [1, 5, 60, 200]),
 ]
 
 
-def main():
+def main(only=None):
     lib = bind(os.path.join(REPO, "oracle", "_ref", "libcpref.so"))
     for name, cfg, size, dt, checkpoints in FIXTURES:
+        if only and name not in only:
+            continue
         sc = Scene(lib, cfg, size)
         data = {"config": np.array([cfg, size]), "dt": np.array(dt), "checkpoints": np.array(checkpoints)}
         done = 0
@@ -50,4 +53,4 @@ def main():
 
 
 if __name__ == "__main__":
-    main()
+    main(sys.argv[1:])

@@ -38,3 +38,10 @@ def test_header_declares_the_step_api():
 def test_library_exports_every_declared_symbol(lib):
     missing = [n for n in declared_functions() if not hasattr(lib, n)]
     assert not missing, missing
+
+
+def test_product_exports_no_test_scaffolding(lib):
+    """The seeded workloads and the state-export names live in the
+    test-side libcpx_scenes.so, not in the product library."""
+    for n in ("cpx_scene_build", "cpx_batch_sizes", "cpx_scene_dump_public", "cpx_dump_bodies"):
+        assert not hasattr(lib, n), n

@@ -7,10 +7,12 @@ host round every +,-,*,/,sqrt identically (no FMA contraction on either
 side); the remaining source of difference is the last bit of sin/cos in
 the body transforms, which this tolerance covers.
 
-"Teacher-forced" runs copy the oracle's body state into the GPU before
-every step, so each comparison measures one step from identical inputs;
-"free" runs compare two independent rollouts.  Arbiter lists (shape pairs,
-contact counts, solve order) must match exactly.
+"Teacher-forced" runs copy the oracle's complete state into the GPU before
+every step -- the bodies and the warm-start impulses the step begins from
+(every arbiter of the last solve list and every joint) -- so each
+comparison measures one step from identical inputs; "free" runs compare two
+independent rollouts.  Arbiter lists (shape pairs, contact counts, solve
+order) must match exactly.
 """
 import numpy as np
 import pytest
@@ -36,6 +38,13 @@ def check_gpu_error(lib):
     assert e == 0, lib.cpGpuGetLastErrorString().decode()
 
 
+def force(g, o):
+    """The oracle's state into the GPU space: bodies, then the accumulated
+    impulses of the arbiters and joints (same solve list on both sides)."""
+    g.set_bodies(o.bodies())
+    assert g.set_impulses(o.arbiters(), o.constraints()) == 0
+
+
 def compare_step(g, o, step, strict_structure=True):
     gb, ob = g.bodies(), o.bodies()
     ga, oa = g.arbiters(), o.arbiters()
@@ -54,6 +63,7 @@ CASES = [
     ("mixed", 3, 1200, 1 / 60, 80),
     ("tumble", 4, 300, 1 / 60, 120),
     ("adjoint", 5, 64, 1 / 120, 120),
+    ("joints", 6, 200, 1 / 60, 200),
 ]
 
 
@@ -64,7 +74,7 @@ def test_teacher_forced_per_step(gpu_lib, oracle_lib, name, cfg, size, dt, steps
     worst = [0.0, 0.0, 0.0]
     try:
         for s in range(steps):
-            g.set_bodies(o.bodies())
+            force(g, o)
             g.step(dt)
             o.step(dt)
             check_gpu_error(gpu_lib)
@@ -80,7 +90,8 @@ def test_teacher_forced_per_step(gpu_lib, oracle_lib, name, cfg, size, dt, steps
 FREE_RUN_DRIFT = 1e-9
 
 
-@pytest.mark.parametrize("name,cfg,size,dt,steps", [CASES[0], CASES[1], CASES[2]], ids=["pyramid", "circles", "mixed"])
+@pytest.mark.parametrize("name,cfg,size,dt,steps", [CASES[0], CASES[1], CASES[2], CASES[5]],
+                         ids=["pyramid", "circles", "mixed", "joints"])
 def test_teacher_forced_whole_grid_solve(gpu_lib, oracle_lib, name, cfg, size, dt, steps):
     """The whole-grid solve (four lanes per contact, a grid barrier between
     levels), which large single worlds use, against the oracle."""
@@ -91,7 +102,7 @@ def test_teacher_forced_whole_grid_solve(gpu_lib, oracle_lib, name, cfg, size, d
         try:
             worst = 0.0
             for s in range(min(steps, 60)):
-                g.set_bodies(o.bodies())
+                force(g, o)
                 g.step(dt)
                 o.step(dt)
                 check_gpu_error(gpu_lib)
@@ -149,7 +160,7 @@ def test_public_getters_and_impulses_match(gpu_lib, oracle_lib):
     o = Scene(oracle_lib, 4, 200)
     try:
         for s in range(60):
-            g.set_bodies(o.bodies())
+            force(g, o)
             g.step(1 / 60)
             o.step(1 / 60)
         check_gpu_error(gpu_lib)
@@ -160,14 +171,18 @@ def test_public_getters_and_impulses_match(gpu_lib, oracle_lib):
         o.free()
 
 
-def test_batched_worlds_match_single_worlds(gpu_lib, oracle_lib):
-    """Uneven tumble worlds stepped together in one batch match the oracle
-    stepping each world alone."""
+@pytest.mark.parametrize("cfg", [4, 6], ids=["tumble", "joints"])
+def test_batched_worlds_match_single_worlds(gpu_lib, oracle_lib, cfg):
+    """Uneven worlds stepped together in one batch match the oracle stepping
+    each world alone: tumble worlds, and worlds of pin and slide joints with
+    filtered shapes."""
     import ctypes
     sizes = (ctypes.c_int * 24)()
     gpu_lib.cpx_batch_sizes(24, 3, ctypes.cast(sizes, ctypes.c_void_p))
-    gs = [Scene(gpu_lib, 4, sizes[i], seed=100 + i) for i in range(24)]
-    os_ = [Scene(oracle_lib, 4, sizes[i], seed=100 + i) for i in range(24)]
+    if cfg == 6:
+        sizes = [40 + (sizes[i] * 160) // 512 for i in range(24)]
+    gs = [Scene(gpu_lib, cfg, sizes[i], seed=100 + i) for i in range(24)]
+    os_ = [Scene(oracle_lib, cfg, sizes[i], seed=100 + i) for i in range(24)]
     batch = gpu_lib.cpGpuBatchNew()
     try:
         for g in gs:
@@ -175,7 +190,7 @@ def test_batched_worlds_match_single_worlds(gpu_lib, oracle_lib):
         worst = 0.0
         for s in range(60):
             for g, o in zip(gs, os_):
-                g.set_bodies(o.bodies())
+                force(g, o)
             assert gpu_lib.cpGpuBatchStep(batch, 1 / 60, 1, 0) == 0
             for o in os_:
                 o.step(1 / 60)

@@ -71,3 +71,7 @@ def test_schedule_matches_recurrence(gpu_lib, nunits, nbodies, seed):
 
 def test_schedule_rejects_bad_arguments(gpu_lib):
     assert gpu_lib.cpGpuSolveSchedule(None, None, -1, 4, None, None, None, None) != 0
+    # levelStart is written even for an empty sequence, so it is required
+    # whatever nunits is (refused on the host, before any launch)
+    for fn in ("cpGpuSolveSchedule", "cpGpuSolveScheduleNoAlloc"):
+        assert getattr(gpu_lib, fn)(None, None, 0, 0, None, None, ctypes.c_void_p(8), None) != 0

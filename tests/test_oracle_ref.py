@@ -20,6 +20,7 @@ CASES = [
     (3, 900, 120, 1 / 60),
     (4, 300, 200, 1 / 60),
     (5, 64, 240, 1 / 120),
+    (6, 200, 300, 1 / 60),
 ]
 
 
