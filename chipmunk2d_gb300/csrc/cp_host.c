@@ -105,6 +105,7 @@ struct cpBody {
 	cpDataPointer userData;
 	cpSpace *space;
 	int index;                 /* world-local device index */
+	DevSet *devOwner;          /* the device set `index` refers to */
 	unsigned long long pullGen; /* download whose state this struct holds */
 	cpShape *shapeList;
 	cpConstraint *constraintList;
@@ -174,7 +175,10 @@ struct cpSpace {
 
 	cpBody **dyn; int ndyn, capdyn;
 	cpBody **stat; int nstat, capstat;
+	/* shapes by hash id: a removed shape leaves its slot NULL, so the
+	 * device index of a shape (its hash id) never changes */
 	cpShape **shapes; int nshapes, capshapes;
+	int nlive;                              /* shapes in the space */
 	cpConstraint **cons; int ncons, capcons;
 	cpgOp *ops; int nops, capops;           /* insertions not yet on the device */
 	cpBody staticBody;
@@ -187,6 +191,8 @@ struct cpSpace {
 	int consStale;                          /* device joint records newer than host */
 	int shapesStale;                        /* device shape boxes newer than host */
 	int bodyDirty, shapeDirty, consDirty;   /* host newer than device */
+	int structDirty;                        /* objects added or removed since the device set was built:
+	                                           the host holds the state until the next step rebuilds it */
 	double jointDt;                         /* dt the joint bias terms were made for */
 
 	cpArbiter *snap; int nsnap, capsnap; int snapValid;
@@ -447,6 +453,7 @@ static int upload_bodies(DevSet *ds, int w)
 	for(int i = 0; i < n; i++){
 		cpBody *b = world_body(sp, i);
 		b->index = i;
+		b->devOwner = ds;
 		f[0][i] = b->p.x; f[1][i] = b->p.y; f[2][i] = b->v.x; f[3][i] = b->v.y;
 		f[4][i] = b->f.x; f[5][i] = b->f.y; f[6][i] = b->a; f[7][i] = b->w; f[8][i] = b->t;
 		f[9][i] = b->transform.a; f[10][i] = b->transform.b; f[11][i] = b->transform.c; f[12][i] = b->transform.d;
@@ -544,8 +551,16 @@ static int upload_shapes(DevSet *ds, int w)
 	unsigned *cm = HALLOC(unsigned, 2*n), *cat = cm, *msk = cm + n;
 	unsigned char *sens = HALLOC(unsigned char, n);
 	int nv = 0;
+	int staticIndex = world_body_count(sp) - 1;
 	for(int i = 0; i < n; i++){
 		cpShape *s = sp->shapes[i];
+		if(!s){
+			/* the slot of a removed shape: on the space's static body, in no
+			 * index, so no kernel reads it (buffers are zeroed) */
+			kind[i] = CPG_CIRCLE; body[i] = staticIndex; wld[i] = w;
+			hsh[i] = (unsigned long long)i; voff[i] = nv; vcount[i] = 0;
+			continue;
+		}
 		kind[i] = s->kind; body[i] = s->body->index; wld[i] = w;
 		f[0][i] = s->r;
 		cpVect l0 = s->kind == CPG_CIRCLE ? s->c : s->sa, l1 = s->sb, ln = s->sn;
@@ -563,6 +578,7 @@ static int upload_shapes(DevSet *ds, int w)
 	double *vb = HALLOC(double, 8*nv);
 	for(int i = 0, k = 0; i < n; i++){
 		cpShape *s = sp->shapes[i];
+		if(!s) continue;
 		for(int j = 0; j < s->count; j++, k++){
 			vb[k] = s->lv[j].x; vb[nv + k] = s->lv[j].y; vb[2*nv + k] = s->ln[j].x; vb[3*nv + k] = s->ln[j].y;
 			vb[4*nv + k] = s->gv[j].x; vb[5*nv + k] = s->gv[j].y; vb[6*nv + k] = s->gn[j].x; vb[7*nv + k] = s->gn[j].y;
@@ -669,8 +685,11 @@ static int device_available(void)
 	return 1;
 }
 
-/* Build a device set holding `spaces` (each becomes one world). */
-static DevSet *devset_build(cpSpace **spaces, int nspaces)
+/* Build a device set holding `spaces` (each becomes one world).  With
+ * `from` (a single space's previous set), the tree, pair cache, leaf sets
+ * and arbiter cache carry over from it instead of starting empty, and the
+ * index edits recorded since it was built replay on top. */
+static DevSet *devset_build(cpSpace **spaces, int nspaces, DevSet *from)
 {
 	if(!device_available()) return NULL;
 	DevSet *ds = (DevSet *)calloc(1, sizeof(DevSet));
@@ -688,6 +707,7 @@ static DevSet *devset_build(cpSpace **spaces, int nspaces)
 		int nverts = 0, ndynShapes = 0, nstatShapes = 0;
 		for(int i = 0; i < sp->nshapes; i++){
 			cpShape *s = sp->shapes[i];
+			if(!s) continue;
 			nverts += s->count;
 			if(body_type_(s->body) == CP_BODY_TYPE_STATIC) nstatShapes++; else ndynShapes++;
 		}
@@ -697,10 +717,21 @@ static DevSet *devset_build(cpSpace **spaces, int nspaces)
 		W->shapeOff = (int)NS; W->nshapes = sp->nshapes;
 		W->vertOff = (int)NV; W->nverts = nverts;
 		W->consOff = (int)NC; W->ncons = sp->ncons;
-		W->nodeOff = (int)NN; W->nodeCap = 2*(ndynShapes + nstatShapes) + 4;
+		/* capacities by shape slots (removed shapes keep theirs), so a set
+		 * rebuilt after removals holds at least what its predecessor held */
+		int churn = (sp->nshapes != ndynShapes + nstatShapes) || from;
+		W->nodeOff = (int)NN; W->nodeCap = 2*sp->nshapes + 4;
 		W->pairOff = (int)NP; W->pairCap = 16*sp->nshapes + 256;
-		W->dbinOff = (int)NDB; W->dbinCap = bins_for(ndynShapes);
-		W->sbinOff = (int)NSB; W->sbinCap = bins_for(nstatShapes);
+		W->dbinOff = (int)NDB; W->dbinCap = bins_for(churn ? sp->nshapes : ndynShapes);
+		W->sbinOff = (int)NSB; W->sbinCap = bins_for(churn ? sp->nshapes : nstatShapes);
+		if(from){
+			/* never below the predecessor's pools, whose contents move over */
+			const cpgWorld *O = &from->hworld[0];
+			if(W->nodeCap < O->nodeCap) W->nodeCap = O->nodeCap;
+			if(W->pairCap < O->pairCap) W->pairCap = O->pairCap;
+			if(W->dbinCap < O->dbinCap) W->dbinCap = O->dbinCap;
+			if(W->sbinCap < O->sbinCap) W->sbinCap = O->sbinCap;
+		}
 		W->candOff = (int)NCD; W->candCap = W->pairCap;
 		W->unitOff = (int)NU; W->unitCap = W->candCap + sp->ncons;
 		W->opOff = (int)NO; W->nops = sp->nops;
@@ -720,6 +751,7 @@ static DevSet *devset_build(cpSpace **spaces, int nspaces)
 	d->totalCands = (int)NCD; d->totalUnits = (int)NU; d->totalOps = (int)NO; d->totalParts = (int)NPT;
 	long long arbCap = 1024;
 	while(arbCap < 8*NS + 1024) arbCap *= 2;
+	if(from && arbCap < from->d.arbCap) arbCap = from->d.arbCap;
 	d->arbCap = (int)arbCap;
 
 	size_t bytes = carve_set(d, NULL, 0);
@@ -746,6 +778,20 @@ static DevSet *devset_build(cpSpace **spaces, int nspaces)
 	if(!ok){ devset_free(ds); return NULL; }
 
 	ok &= h2d(d->world, ds->hworld, sizeof(cpgWorld)*(size_t)nspaces);
+	/* bodies of the predecessor set by their new index (read before the
+	 * uploads below renumber them) */
+	int *bodyMap = NULL;
+	if(from){
+		int oldNB = from->hworld[0].nbodies;
+		bodyMap = HALLOC(int, oldNB);
+		for(int i = 0; i < oldNB; i++) bodyMap[i] = -1;
+		cpSpace *sp = spaces[0];
+		int nb = world_body_count(sp);
+		for(int i = 0; i < nb; i++){
+			cpBody *b = world_body(sp, i);
+			if(b->devOwner == from && b->index >= 0 && b->index < oldNB) bodyMap[b->index] = i;
+		}
+	}
 	cpgTree *trees = HALLOC(cpgTree, nspaces);
 	for(int w = 0; w < nspaces; w++){
 		cpgTree *T = &trees[w];
@@ -793,12 +839,12 @@ static DevSet *devset_build(cpSpace **spaces, int nspaces)
 		ok &= h2d(d->ops + W->opOff, sp->ops, sizeof(cpgOp)*(size_t)sp->nops);
 		int *dyns = HALLOC(int, sp->nshapes);
 		int nds = 0;
-		for(int i = 0; i < sp->nshapes; i++) if(body_type_(sp->shapes[i]->body) != CP_BODY_TYPE_STATIC) dyns[nds++] = i;
+		for(int i = 0; i < sp->nshapes; i++) if(sp->shapes[i] && body_type_(sp->shapes[i]->body) != CP_BODY_TYPE_STATIC) dyns[nds++] = i;
 		ok &= h2d(d->dynShapes + W->dynShapeOff, dyns, sizeof(int)*(size_t)nds);
 		cudaStreamSynchronize(st);
 		free(bi); free(parts); free(dyns);
 		sp->builtBodies = world_body_count(sp); sp->builtShapes = sp->nshapes; sp->builtCons = sp->ncons;
-		sp->bodyDirty = sp->shapeDirty = sp->consDirty = 0;
+		sp->bodyDirty = sp->shapeDirty = sp->consDirty = sp->structDirty = 0;
 		sp->jointDt = 0.0;
 	}
 	if(!ok){ devset_free(ds); return NULL; }
@@ -831,7 +877,30 @@ static DevSet *devset_build(cpSpace **spaces, int nspaces)
 		cudaStreamSynchronize(lib_stream());
 		free(ord);
 	}
-	/* replay the recorded index insertions, then clear the logs */
+	if(from){
+		/* the predecessor's tree and arbiter cache, bodies renumbered and
+		 * the arbiters of removed shapes dropped */
+		cpSpace *sp = spaces[0];
+		int oldNB = from->hworld[0].nbodies, oldNS = from->hworld[0].nshapes;
+		size_t bm = align256(sizeof(int)*(size_t)(oldNB > 0 ? oldNB : 1));
+		size_t dm = align256((size_t)(oldNS > 0 ? oldNS : 1));
+		size_t sm = sizeof(int)*(size_t)from->d.arbCap;
+		unsigned char *dead = HALLOC(unsigned char, oldNS);
+		for(int i = 0; i < oldNS; i++) dead[i] = (i >= sp->nshapes || sp->shapes[i] == NULL);
+		char *tmp = NULL;
+		int tok = cuda_ok(cudaMalloc((void **)&tmp, bm + dm + sm), "cudaMalloc transfer");
+		if(tok){
+			tok &= h2d(tmp, bodyMap, sizeof(int)*(size_t)oldNB);
+			tok &= h2d(tmp + bm, dead, (size_t)oldNS);
+			tok &= (cpg_launch_transfer(d, &from->d, (const int *)tmp, (const unsigned char *)(tmp + bm), (int *)(tmp + bm + dm), st) == 0);
+			tok &= cuda_ok(cudaStreamSynchronize(st), "transfer");
+			cudaFree(tmp);
+		}
+		free(dead);
+		if(!tok){ free(bodyMap); set_error(CP_GPU_ERR_CUDA, "device state transfer failed"); devset_free(ds); return NULL; }
+	}
+	free(bodyMap);
+	/* replay the recorded index edits, then clear the logs */
 	if(cpg_launch_apply_ops(d, st) != 0){ set_error(CP_GPU_ERR_CUDA, "apply_ops launch failed"); devset_free(ds); return NULL; }
 	for(int w = 0; w < nspaces; w++){ ds->hworld[w].nops = 0; spaces[w]->nops = 0; }
 	h2d(d->world, ds->hworld, sizeof(cpgWorld)*(size_t)nspaces);
@@ -840,6 +909,7 @@ static DevSet *devset_build(cpSpace **spaces, int nspaces)
 }
 
 static void check_stats(DevSet *ds);
+static void space_detach(cpSpace *sp);
 
 /* Downloads so far: identifies the state in a staging block. */
 static unsigned long long g_pull_gen = 0;
@@ -1041,17 +1111,25 @@ void cpSpaceStep(cpSpace *sp, cpFloat dt)
 		set_error(CP_GPU_ERR_UNSUPPORTED, "space belongs to a cpGpuBatch; step it with cpGpuBatchStep");
 		return;
 	}
-	if(space_structure_changed(sp)){
-		/* Objects were added after the space went to the device: bring the
-		 * state home and rebuild.  The device tree and arbiter cache are
-		 * rebuilt from the insertion history, which is exact only while
-		 * nothing has been stepped; report it otherwise. */
-		set_error(CP_GPU_ERR_UNSUPPORTED, "adding objects to a space after its first step is not supported");
-		return;
+	if(sp->dev && (sp->structDirty || space_structure_changed(sp))){
+		/* Objects were added or removed since the set was built: the host
+		 * holds the whole state (space_detach), so build a new set from it,
+		 * carrying the device tree and arbiter cache over, and replay the
+		 * index edits recorded since, in call order. */
+		DevSet *old = sp->dev;
+		space_detach(sp);
+		cpSpace *one[1] = { sp };
+		DevSet *ds = devset_build(one, 1, old);
+		if(!ds){
+			sp->dev = old; sp->world = 0; sp->structDirty = 1;
+			return;
+		}
+		devset_free(old);
+		sp->ownsDev = 1;
 	}
 	if(!sp->dev){
 		cpSpace *one[1] = { sp };
-		DevSet *ds = devset_build(one, 1);
+		DevSet *ds = devset_build(one, 1, NULL);
 		if(!ds) return;
 		sp->ownsDev = 1;
 	}
@@ -1168,7 +1246,7 @@ int cpGpuBatchStep(cpGpuBatch *b, cpFloat dt, int steps, int use_graph)
 	if(!b || b->n <= 0) return -1;
 	for(int i = 0; i < b->n; i++) if(!space_supported(b->spaces[i])) return -1;
 	if(!b->dev){
-		b->dev = devset_build(b->spaces, b->n);
+		b->dev = devset_build(b->spaces, b->n, NULL);
 		if(!b->dev) return -1;
 		for(int i = 0; i < b->n; i++) b->spaces[i]->ownsDev = 0;
 	}
@@ -1197,7 +1275,7 @@ static int batch_ready(cpGpuBatch *b)
 		}
 	}
 	if(!b->dev){
-		b->dev = devset_build(b->spaces, b->n);
+		b->dev = devset_build(b->spaces, b->n, NULL);
 		if(!b->dev) return 0;
 		for(int i = 0; i < b->n; i++) b->spaces[i]->ownsDev = 0;
 	}
@@ -2066,7 +2144,7 @@ static void shapes_pull_(cpSpace *sp)
 	d2h(buf + 2*n, ds->d.bbr + off, sizeof(double)*(size_t)n);
 	d2h(buf + 3*n, ds->d.bbt + off, sizeof(double)*(size_t)n);
 	cuda_ok(cudaStreamSynchronize(lib_stream()), "download shape boxes");
-	for(int i = 0; i < n; i++) sp->shapes[i]->bb = cpBBNew(buf[i], buf[n + i], buf[2*n + i], buf[3*n + i]);
+	for(int i = 0; i < n; i++) if(sp->shapes[i]) sp->shapes[i]->bb = cpBBNew(buf[i], buf[n + i], buf[2*n + i], buf[3*n + i]);
 	free(buf);
 	sp->shapesStale = 0;
 }
@@ -2331,7 +2409,7 @@ void cpSpaceFree(cpSpace *sp)
 	}
 	for(int i = 0; i < sp->ndyn; i++) if(sp->dyn[i]->space == sp) sp->dyn[i]->space = NULL;
 	for(int i = 0; i < sp->nstat; i++) if(sp->stat[i]->space == sp) sp->stat[i]->space = NULL;
-	for(int i = 0; i < sp->nshapes; i++) if(sp->shapes[i]->space == sp) sp->shapes[i]->space = NULL;
+	for(int i = 0; i < sp->nshapes; i++) if(sp->shapes[i] && sp->shapes[i]->space == sp) sp->shapes[i]->space = NULL;
 	for(int i = 0; i < sp->ncons; i++) if(sp->cons[i]->space == sp) sp->cons[i]->space = NULL;
 	free(sp->dyn); free(sp->stat); free(sp->shapes); free(sp->cons); free(sp->ops); free(sp->snap);
 	free(sp);
@@ -2371,11 +2449,70 @@ void cpGpuSetSolverMode(cpSpace *sp, int mode)
 }
 int cpGpuGetSolverMode(const cpSpace *sp) { return sp->mode; }
 
+/* Objects are about to be added or removed while the space's state is on
+ * the device: bring it home (bodies, joint accumulators, shape boxes), so
+ * the host holds the whole state until the next step rebuilds the set. */
+static void space_detach(cpSpace *sp)
+{
+	if(!sp || !sp->dev || sp->structDirty || !sp->ownsDev) return;
+	space_pull(sp);
+	joints_pull_(sp);
+	shapes_pull_(sp);
+	sp->structDirty = 1;
+	sp->snapValid = 0;
+}
+
+/* Whether the space's objects may change now.  A space stepped in a batch
+ * keeps the objects it joined with. */
+static int space_edit_ok(cpSpace *sp)
+{
+	if(sp->dev && !sp->ownsDev){
+		set_error(CP_GPU_ERR_UNSUPPORTED, "a space stepped in a cpGpuBatch cannot gain or lose objects");
+		return 0;
+	}
+	space_detach(sp);
+	return 1;
+}
+
+/* cpArrayDeleteObj (cpArray.c:76-88): the last element takes the hole. */
+static int array_delete_(void **arr, int *n, void *obj)
+{
+	for(int i = 0; i < *n; i++){
+		if(arr[i] == obj){
+			(*n)--;
+			arr[i] = arr[*n];
+			arr[*n] = NULL;
+			return i;
+		}
+	}
+	return -1;
+}
+
+static void record_op_(cpSpace *sp, int kind, cpShape *s, int isStatic)
+{
+	if(sp->nops == sp->capops){
+		sp->capops = sp->capops ? 2*sp->capops : 256;
+		sp->ops = (cpgOp *)realloc(sp->ops, sizeof(cpgOp)*(size_t)sp->capops);
+	}
+	cpgOp *op = &sp->ops[sp->nops++];
+	memset(op, 0, sizeof(*op));
+	op->shape = (int)s->hashid;
+	op->isStatic = isStatic;
+	op->kind = kind;
+	if(kind == CPG_OP_INSERT){
+		/* the box as cached now and the body's velocity now: the leaf's
+		 * fattened box is made at this call (cpBBTree.c:82-98, 605-616) */
+		op->l = s->bb.l; op->b = s->bb.b; op->r = s->bb.r; op->t = s->bb.t;
+		op->vx = s->body->v.x; op->vy = s->body->v.y;
+	}
+}
+
 cpBody *cpSpaceAddBody(cpSpace *sp, cpBody *b)
 {
 	/* cpSpace.c:440-451 */
 	ASSERT_HARD(b->space != sp, "You have already added this body to this space. You must not add it a second time.");
 	ASSERT_HARD(!b->space, "You have already added this body to another space. You cannot add it to a second.");
+	if(!space_edit_ok(sp)) return b;
 	if(body_type_(b) == CP_BODY_TYPE_STATIC) push_((void ***)&sp->stat, &sp->nstat, &sp->capstat, b);
 	else push_((void ***)&sp->dyn, &sp->ndyn, &sp->capdyn, b);
 	b->space = sp;
@@ -2389,6 +2526,7 @@ cpShape *cpSpaceAddShape(cpSpace *sp, cpShape *s)
 	ASSERT_HARD(!s->space, "You have already added this shape to another space. You cannot add it to a second.");
 	ASSERT_HARD(s->body, "The shape's body is not defined.");
 	ASSERT_HARD(s->body->space == sp, "The shape's body must be added to the space before the shape.");
+	if(!space_edit_ok(sp)) return s;
 	cpBody *body = s->body;
 	rd(body);
 	int isStatic = (body_type_(body) == CP_BODY_TYPE_STATIC);
@@ -2397,20 +2535,12 @@ cpShape *cpSpaceAddShape(cpSpace *sp, cpShape *s)
 	s->next = next;
 	body->shapeList = s;
 	if(s->mass_m > 0.0) accumulate_mass_(body);
+	/* the hash id is the shape's slot: ids are never reused */
 	s->hashid = sp->shapeIDCounter++;
-	cpBB bb = shape_cache_(s, body->transform);
-	/* record the insertion with its add-time box and velocity */
-	if(sp->nops == sp->capops){
-		sp->capops = sp->capops ? 2*sp->capops : 256;
-		sp->ops = (cpgOp *)realloc(sp->ops, sizeof(cpgOp)*(size_t)sp->capops);
-	}
-	cpgOp *op = &sp->ops[sp->nops++];
-	memset(op, 0, sizeof(*op));
-	op->shape = (int)s->hashid;
-	op->isStatic = isStatic;
-	op->l = bb.l; op->b = bb.b; op->r = bb.r; op->t = bb.t;
-	op->vx = body->v.x; op->vy = body->v.y;
+	shape_cache_(s, body->transform);
+	record_op_(sp, CPG_OP_INSERT, s, isStatic);
 	push_((void ***)&sp->shapes, &sp->nshapes, &sp->capshapes, s);
+	sp->nlive++;
 	s->space = sp;
 	return s;
 }
@@ -2421,6 +2551,7 @@ cpConstraint *cpSpaceAddConstraint(cpSpace *sp, cpConstraint *c)
 	ASSERT_HARD(c->space != sp, "You have already added this constraint to this space. You must not add it a second time.");
 	ASSERT_HARD(!c->space, "You have already added this constraint to another space. You cannot add it to a second.");
 	ASSERT_HARD(c->a != NULL && c->b != NULL, "Constraint is attached to a NULL body.");
+	if(!space_edit_ok(sp)) return c;
 	cpBody *a = c->a, *b = c->b;
 	c->index = sp->ncons;
 	push_((void ***)&sp->cons, &sp->ncons, &sp->capcons, c);
@@ -2428,6 +2559,65 @@ cpConstraint *cpSpaceAddConstraint(cpSpace *sp, cpConstraint *c)
 	c->next_b = b->constraintList; b->constraintList = c;
 	c->space = sp;
 	return c;
+}
+
+void cpSpaceRemoveShape(cpSpace *sp, cpShape *s)
+{
+	/* cpSpace.c:523-545 */
+	ASSERT_HARD(cpSpaceContainsShape(sp, s), "Cannot remove a shape that was not added to the space. (Removed twice maybe?)");
+	if(!space_edit_ok(sp)) return;
+	cpBody *body = s->body;
+	int isStatic = (body_type_(body) == CP_BODY_TYPE_STATIC);
+	/* cpBodyRemoveShape, cpBody.c:306-327 */
+	if(s->prev) s->prev->next = s->next; else body->shapeList = s->next;
+	if(s->next) s->next->prev = s->prev;
+	s->prev = s->next = NULL;
+	if(body_type_(body) == CP_BODY_TYPE_DYNAMIC && s->mass_m > 0.0) accumulate_mass_(body);
+	/* its arbiters go when the set is rebuilt (cpSpaceFilterArbiters), its
+	 * leaf when the edit replays (cpSpatialIndexRemove) */
+	record_op_(sp, CPG_OP_REMOVE, s, isStatic);
+	sp->shapes[s->hashid] = NULL;
+	sp->nlive--;
+	s->space = NULL;
+	s->hashid = 0;
+}
+
+void cpSpaceRemoveBody(cpSpace *sp, cpBody *b)
+{
+	/* cpSpace.c:547-562 */
+	ASSERT_HARD(b != cpSpaceGetStaticBody(sp), "Cannot remove the designated static body for the space.");
+	ASSERT_HARD(cpSpaceContainsBody(sp, b), "Cannot remove a body that was not added to the space. (Removed twice maybe?)");
+	if(!space_edit_ok(sp)) return;
+	if(body_type_(b) == CP_BODY_TYPE_STATIC) array_delete_((void **)sp->stat, &sp->nstat, b);
+	else array_delete_((void **)sp->dyn, &sp->ndyn, b);
+	b->space = NULL;
+}
+
+/* cpBody.c:272-287 (filterConstraints), iteratively */
+static void body_remove_constraint_(cpBody *body, cpConstraint *c)
+{
+	cpConstraint **link = &body->constraintList;
+	int guard = 0;
+	while(*link && guard++ < (1 << 30)){
+		cpConstraint *node = *link;
+		if(node == c){ *link = cons_next_(node, body); return; }
+		link = (node->a == body) ? &node->next_a : &node->next_b;
+	}
+}
+
+void cpSpaceRemoveConstraint(cpSpace *sp, cpConstraint *c)
+{
+	/* cpSpace.c:564-577: the constraint array loses it like
+	 * cpArrayDeleteObj, so the last constraint takes its place in the
+	 * solve order */
+	ASSERT_HARD(cpSpaceContainsConstraint(sp, c), "Cannot remove a constraint that was not added to the space. (Removed twice maybe?)");
+	if(!space_edit_ok(sp)) return;
+	int i = array_delete_((void **)sp->cons, &sp->ncons, c);
+	if(i >= 0 && i < sp->ncons) sp->cons[i]->index = i;
+	body_remove_constraint_(c->a, c);
+	body_remove_constraint_(c->b, c);
+	c->space = NULL;
+	c->index = -1;
 }
 
 void cpSpaceEachBody(cpSpace *sp, cpSpaceBodyIteratorFunc func, void *data)
@@ -2438,7 +2628,7 @@ void cpSpaceEachBody(cpSpace *sp, cpSpaceBodyIteratorFunc func, void *data)
 
 void cpSpaceEachShape(cpSpace *sp, cpSpaceShapeIteratorFunc func, void *data)
 {
-	for(int i = 0; i < sp->nshapes; i++) func(sp->shapes[i], data);
+	for(int i = 0; i < sp->nshapes; i++) if(sp->shapes[i]) func(sp->shapes[i], data);
 }
 
 void cpSpaceEachConstraint(cpSpace *sp, cpSpaceConstraintIteratorFunc func, void *data)
@@ -2652,6 +2842,28 @@ int cpGpuDebugSetImpulses(cpSpace *sp, const double *arbs, int narb, const doubl
 		sp->consDirty = 1;
 	}
 	return bad;
+}
+
+int cpGpuDebugNarrowIds(cpSpace *sp, int *out, int max)
+{
+	if(!sp || !sp->dev) return 0;
+	DevSet *ds = sp->dev;
+	space_pull(sp);
+	cpgTree T;
+	d2h(&T, ds->d.tree + sp->world, sizeof(cpgTree));
+	cudaStreamSynchronize(lib_stream());
+	int n = T.ncand;
+	cpgCand *c = HALLOC(cpgCand, n);
+	cpgNarrow *r = HALLOC(cpgNarrow, n);
+	int off = ds->hworld[sp->world].candOff;
+	d2h(c, ds->d.cands + off, sizeof(cpgCand)*(size_t)n);
+	d2h(r, ds->d.narrow + off, sizeof(cpgNarrow)*(size_t)n);
+	cudaStreamSynchronize(lib_stream());
+	for(int i = 0; i < n && i < max; i++){
+		out[4*i] = c[i].a; out[4*i + 1] = c[i].b; out[4*i + 2] = (int)c[i].idIn; out[4*i + 3] = (int)r[i].idOut;
+	}
+	free(c); free(r);
+	return n;
 }
 
 int cpGpuDebugArbiters(cpSpace *sp, double *out, int max)

@@ -178,13 +178,18 @@ typedef struct cpgRow {
 	};
 } cpgRow;
 
-/* Pending tree insertion recorded by cpSpaceAddShape, with the shape's
- * box and its body's velocity as they were at that call (the reference
- * builds the leaf's fattened box immediately, cpBBTree.c:605-616). */
+/* Pending index edit, replayed on the device in call order before the
+ * next step.  An insertion (cpSpaceAddShape, cpBodySetType) carries the
+ * shape's box and its body's velocity as they were at that call (the
+ * reference builds the leaf's fattened box immediately,
+ * cpBBTree.c:605-616); a removal (cpSpaceRemoveShape, cpBodySetType)
+ * names the shape and the index it leaves (cpBBTree.c:619-630). */
+enum { CPG_OP_INSERT = 0, CPG_OP_REMOVE = 1 };
 typedef struct cpgOp {
 	int shape;
 	int isStatic;
-	int pad0, pad1;
+	int kind;                     /* CPG_OP_INSERT or CPG_OP_REMOVE */
+	int pad1;
 	double l, b, r, t;
 	double vx, vy;
 } cpgOp;
@@ -358,6 +363,8 @@ int cpg_launch_tape_vel(const cpgSet *s, void *stream);
 int cpg_launch_step_graph(const cpgSet *s, int mode, void *stream, void **cache);
 void cpg_step_graph_free(void *cache);
 int cpg_launch_replay_solve(const cpgSet *s, const cpgAdj *a, int nsteps, void *stream);
+int cpg_launch_transfer(const cpgSet *to, const cpgSet *from, const int *bodyMap, const unsigned char *deadShape,
+                        int *slotMap, void *stream);
 int cpg_launch_set_arb_impulses(const cpgSet *s, int w, const double *imp, const int *pairs, int n, int *mismatch, void *stream);
 
 #ifdef __cplusplus

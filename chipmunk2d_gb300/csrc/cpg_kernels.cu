@@ -87,8 +87,77 @@ __global__ void k_apply_ops(cpgSet s)
 	TreeCtx c = make_tree_ctx(&s, w);
 	for(int i = 0; i < W.nops; i++){
 		cpgOp op = s.ops[W.opOff + i];
-		tree_insert(c, op);
+		if(op.kind == CPG_OP_REMOVE) tree_remove(c, op);
+		else tree_insert(c, op);
 	}
+}
+
+/* A single space's set rebuilt between steps because objects were added
+ * or removed: the tree with its pair cache and leaf sets, and the arbiter
+ * cache, carry over into the new set, whose pools are at least as large.
+ * Shape indices are the shapes' hash ids, which never change (a removed
+ * shape leaves an unused index); body indices are remapped (bodyMap[old]
+ * = new, -1 for a body that left).  Arbiters of removed shapes or bodies
+ * are dropped, as cpSpaceFilterArbiters drops them (cpSpace.c:481-521).
+ * Colours are cleared, so the coloured mode colours afresh. */
+__global__ void k_transfer_pools(cpgSet to, cpgSet from)
+{
+	const cpgWorld &WO = from.world[0], &WN = to.world[0];
+	int i0 = blockIdx.x*blockDim.x + threadIdx.x, n = gridDim.x*blockDim.x;
+	for(int k = i0; k < WO.nodeCap; k += n) to.nodes[WN.nodeOff + k] = from.nodes[WO.nodeOff + k];
+	for(int k = i0; k < WO.pairCap; k += n) to.pairs[WN.pairOff + k] = from.pairs[WO.pairOff + k];
+	for(int k = i0; k < WO.dbinCap; k += n) to.dbins[WN.dbinOff + k] = from.dbins[WO.dbinOff + k];
+	for(int k = i0; k < WO.sbinCap; k += n) to.sbins[WN.sbinOff + k] = from.sbins[WO.sbinOff + k];
+	if(i0 == 0) to.tree[0] = from.tree[0];
+}
+
+__device__ int arb_find_or_insert(const cpgSet &s, unsigned long long key, bool &fresh);
+
+__global__ void k_transfer_arbs(cpgSet to, cpgSet from, const int *bodyMap, const unsigned char *deadShape, int *slotMap)
+{
+	bool same = (to.arbCap == from.arbCap);
+	int oldBodies = from.world[0].nbodies, oldShapes = from.world[0].nshapes;
+	for(int k = blockIdx.x*blockDim.x + threadIdx.x; k < from.arbCap; k += gridDim.x*blockDim.x){
+		unsigned long long key = from.keys[k];
+		slotMap[k] = -1;
+		if(key <= CPG_KEY_TOMB){
+			if(same) to.keys[k] = key;
+			continue;
+		}
+		cpgArb a = from.arbs[k];
+		bool bad = a.ba < 0 || a.ba >= oldBodies || a.bb < 0 || a.bb >= oldBodies ||
+			a.a < 0 || a.a >= oldShapes || a.b < 0 || a.b >= oldShapes;
+		int ba = bad ? -1 : bodyMap[a.ba], bb = bad ? -1 : bodyMap[a.bb];
+		if(ba < 0 || bb < 0 || deadShape[a.a] || deadShape[a.b]){
+			if(same) to.keys[k] = CPG_KEY_TOMB;
+			continue;
+		}
+		a.ba = ba; a.bb = bb; a.colorTag = 0;
+		int slot = k;
+		if(same) to.keys[k] = key;
+		else {
+			bool fresh;
+			slot = arb_find_or_insert(to, key, fresh);
+			if(slot < 0){ atomicOr(&to.tree[0].error, CPG_ERR_ARBS); continue; }
+		}
+		to.arbs[slot] = a;
+		slotMap[k] = slot;
+	}
+}
+
+/* the last solve list (reset by the next step, cpSpaceStep.c:351-360) in
+ * its order, without the dropped arbiters */
+__global__ void k_transfer_list(cpgSet to, cpgSet from, const int *slotMap)
+{
+	if(blockIdx.x != 0 || threadIdx.x != 0) return;
+	int n = from.tree[0].narb, m = 0;
+	for(int i = 0; i < n; i++){
+		int slot = slotMap[from.arbList[from.world[0].candOff + i]];
+		if(slot >= 0) to.arbList[to.world[0].candOff + m++] = slot;
+	}
+	to.tree[0].narb = m;
+	to.tree[0].ncand = 0;
+	to.tree[0].nunits = 0;
 }
 
 /* ------------------------------------------------------------------ */
@@ -2360,6 +2429,16 @@ extern "C" int cpg_launch_apply_ops(const cpgSet *s, void *stream)
 	cudaStream_t st = (cudaStream_t)stream;
 	LAUNCH(k_apply_ops<<<blocks_for(s->nworlds, 64), 64, 0, st>>>(*s));
 	return check_launch("k_apply_ops") == cudaSuccess ? 0 : -1;
+}
+
+extern "C" int cpg_launch_transfer(const cpgSet *to, const cpgSet *from, const int *bodyMap, const unsigned char *deadShape,
+                                   int *slotMap, void *stream)
+{
+	cudaStream_t st = (cudaStream_t)stream;
+	LAUNCH(k_transfer_pools<<<152*2, 256, 0, st>>>(*to, *from));
+	LAUNCH(k_transfer_arbs<<<blocks_for(from->arbCap, 256), 256, 0, st>>>(*to, *from, bodyMap, deadShape, slotMap));
+	LAUNCH(k_transfer_list<<<1, 32, 0, st>>>(*to, *from, slotMap));
+	return check_launch("k_transfer") == cudaSuccess ? 0 : -1;
 }
 
 static int coop_blocks(const void *kernel, int threads)

@@ -439,6 +439,36 @@ __device__ void tree_insert(TreeCtx &c, const cpgOp &op)
 	T->treeStamp++;
 }
 
+/* cpBBTree.c:619-630 (cpBBTreeRemove): the leaf leaves the hash set
+ * (cpHashSet.c:209-233: unlinked from its bin, the other leaves keep
+ * their order), then the tree, then every pair list, and is recycled. */
+__device__ void tree_remove(TreeCtx &c, const cpgOp &op)
+{
+	cpgTree *T = c.T;
+	int shape = op.shape;
+	bool isStatic = op.isStatic != 0;
+	int *bins = isStatic ? c.sbins : c.dbins;
+	unsigned size = isStatic ? T->statSize : T->dynSize;
+	unsigned *entries = isStatic ? &T->statEntries : &T->dynEntries;
+	if(size == 0){ T->error |= CPG_ERR_BINS; return; }
+	unsigned idx = (unsigned)(c.shash[shape] % size);
+	int prev = -1, leaf = bins[idx];
+	for(int guard = 0; leaf >= 0; guard++){
+		if(guard > c.nodeCap){ T->error |= CPG_ERR_BINS; return; }
+		if(c.nodes[leaf].obj == shape) break;
+		prev = leaf;
+		leaf = c.nodes[leaf].binNext;
+	}
+	if(leaf < 0){ T->error |= CPG_ERR_BINS; return; }
+	if(prev >= 0) c.nodes[prev].binNext = c.nodes[leaf].binNext;
+	else bins[idx] = c.nodes[leaf].binNext;
+	(*entries)--;
+	if(isStatic) T->statRoot = subtree_remove(c, T->statRoot, leaf);
+	else T->dynRoot = subtree_remove(c, T->dynRoot, leaf);
+	pairs_clear(c, leaf);
+	node_recycle(c, leaf);
+}
+
 /* cpBBTree.c:498-517: a leaf whose shape left its fattened box */
 __device__ __forceinline__ bool leaf_moved(const TreeCtx &c, int leaf)
 {

@@ -89,6 +89,25 @@ static double rng_normal(Rng *r)
 	return s - 6.0;
 }
 
+/* A point uniform in [xlo,xhi) x [ylo,yhi), and a vector of normal
+ * variates scaled by s.  The y coordinate is drawn first: C leaves the
+ * order of two calls in one argument list unspecified (gcc evaluates them
+ * right to left on x86-64 and left to right on AArch64), and the scenes
+ * were first generated with y first, so every draw is sequenced here. */
+static cpVect rng_point(Rng *r, double xlo, double xhi, double ylo, double yhi)
+{
+	double y = rng_uniform(r, ylo, yhi);
+	double x = rng_uniform(r, xlo, xhi);
+	return cpv(x, y);
+}
+
+static cpVect rng_normal2(Rng *r, double s)
+{
+	double y = s*rng_normal(r);
+	double x = s*rng_normal(r);
+	return cpv(x, y);
+}
+
 /* Point uniform in the disk of radius R by rejection from the square. */
 static cpVect rng_in_disk(Rng *r, double R)
 {
@@ -252,8 +271,8 @@ static void build_circles(cpxScene *sc, int n, uint64_t seed)
 	add_box_walls(sc, hw, hh, 1.0, 0.7, 0.1);
 	for(int i = 0; i < n; i++){
 		double r = rng_uniform(&rng, 0.5, 2.0);
-		cpVect p = cpv(rng_uniform(&rng, -hw + 3.0, hw - 3.0), rng_uniform(&rng, -hh + 3.0, hh - 3.0));
-		cpVect v = cpv(5.0*rng_normal(&rng), 5.0*rng_normal(&rng));
+		cpVect p = rng_point(&rng, -hw + 3.0, hw - 3.0, -hh + 3.0, hh - 3.0);
+		cpVect v = rng_normal2(&rng, 5.0);
 		add_circle(sc, p, v, r, 0.7, 0.1);
 	}
 }
@@ -289,8 +308,8 @@ static void build_mixed(cpxScene *sc, int n, uint64_t seed)
 
 	double ylo = -half + 5.0, yhi = top - 45.0;
 	for(int i = 0; i < n; i++){
-		cpVect p = cpv(rng_uniform(&rng, -half + 5.0, half - 5.0), rng_uniform(&rng, ylo, yhi));
-		cpVect v = cpv(5.0*rng_normal(&rng), 5.0*rng_normal(&rng));
+		cpVect p = rng_point(&rng, -half + 5.0, half - 5.0, ylo, yhi);
+		cpVect v = rng_normal2(&rng, 5.0);
 		double u = rng_uniform(&rng, 0.3, 1.0);
 		double e = rng_uniform(&rng, 0.0, 0.3);
 		int kind = i % 3;
@@ -321,8 +340,8 @@ static void build_tumble(cpxScene *sc, int n, uint64_t seed)
 	Rng rng; rng_seed(&rng, seed);
 	add_box_walls(sc, 100.0, 100.0, 1.0, 0.7, 0.1);
 	for(int i = 0; i < n; i++){
-		cpVect p = cpv(rng_uniform(&rng, -94.0, 94.0), rng_uniform(&rng, -94.0, 94.0));
-		cpVect v = cpv(20.0*rng_normal(&rng), 20.0*rng_normal(&rng));
+		cpVect p = rng_point(&rng, -94.0, 94.0, -94.0, 94.0);
+		cpVect v = rng_normal2(&rng, 20.0);
 		if(rng_u01(&rng) < 0.5){
 			add_circle(sc, p, v, rng_uniform(&rng, 1.0, 4.0), 0.7, 0.1);
 		} else {
@@ -338,8 +357,8 @@ static void build_adjoint(cpxScene *sc, int n, uint64_t seed)
 	add_wall(sc, cpv(-120.0, 0.0), cpv(120.0, 0.0), 0.0, 0.7, 0.1);
 	int half = n/2;
 	for(int i = 0; i < n; i++){
-		cpVect p = cpv(rng_uniform(&rng, -60.0, 60.0), rng_uniform(&rng, 8.0, 120.0));
-		cpVect v = cpv(rng_normal(&rng), rng_normal(&rng));
+		cpVect p = rng_point(&rng, -60.0, 60.0, 8.0, 120.0);
+		cpVect v = rng_normal2(&rng, 1.0);
 		if(i < half){
 			add_circle(sc, p, v, rng_uniform(&rng, 1.0, 3.0), 0.7, 0.1);
 		} else {
@@ -423,7 +442,7 @@ static void build_joints(cpxScene *sc, int n, uint64_t seed)
 	double ylo = -half + 6.0, yhi = top - 32.0;
 	int pairs = n/8;
 	for(int i = 0; i < pairs; i++){
-		cpVect p = cpv(rng_uniform(&rng, lo, hi), rng_uniform(&rng, ylo, yhi));
+		cpVect p = rng_point(&rng, lo, hi, ylo, yhi);
 		cpVect d = rng_direction(&rng);
 		double sep = rng_uniform(&rng, 1.5, 8.0);
 		cpBody *bb[2];
@@ -431,7 +450,7 @@ static void build_joints(cpxScene *sc, int n, uint64_t seed)
 			double r = rng_uniform(&rng, 1.0, 2.0), m = 3.14159265358979323846*r*r;
 			cpBody *body = cpBodyNew(m, cpMomentForCircle(m, 0.0, r, cpvzero));
 			cpBodySetPosition(body, cpvadd(p, cpvmult(d, k ? 0.5*sep : -0.5*sep)));
-			cpBodySetVelocity(body, cpv(15.0*rng_normal(&rng), 15.0*rng_normal(&rng)));
+			cpBodySetVelocity(body, rng_normal2(&rng, 15.0));
 			add_body(sc, body);
 			cpShape *s = cpCircleShapeNew(body, r, cpvzero);
 			cpShapeSetFriction(s, rng_uniform(&rng, 0.3, 1.0));
@@ -447,11 +466,11 @@ static void build_joints(cpxScene *sc, int n, uint64_t seed)
 
 	int ropes = n/8;
 	for(int i = 0; i < ropes; i++){
-		cpVect p = cpv(rng_uniform(&rng, lo, hi), rng_uniform(&rng, ylo, yhi));
+		cpVect p = rng_point(&rng, lo, hi, ylo, yhi);
 		double r = rng_uniform(&rng, 1.0, 2.0), m = 3.14159265358979323846*r*r;
 		cpBody *body = cpBodyNew(m, cpMomentForCircle(m, 0.0, r, cpvzero));
 		cpBodySetPosition(body, p);
-		cpBodySetVelocity(body, cpv(5.0*rng_normal(&rng), 5.0*rng_normal(&rng)));
+		cpBodySetVelocity(body, rng_normal2(&rng, 5.0));
 		add_body(sc, body);
 		cpShape *s = cpCircleShapeNew(body, r, cpvzero);
 		cpShapeSetFriction(s, rng_uniform(&rng, 0.3, 1.0));
@@ -461,10 +480,13 @@ static void build_joints(cpxScene *sc, int n, uint64_t seed)
 	}
 
 	for(int i = 0; i < n; i++){
-		cpVect p = cpv(rng_uniform(&rng, lo, hi), rng_uniform(&rng, ylo, yhi));
-		cpVect v = cpv(5.0*rng_normal(&rng), 5.0*rng_normal(&rng));
+		cpVect p = rng_point(&rng, lo, hi, ylo, yhi);
+		cpVect v = rng_normal2(&rng, 5.0);
 		double u = rng_uniform(&rng, 0.3, 1.0), e = rng_uniform(&rng, 0.0, 0.3);
-		if(i & 1) add_random_poly(sc, &rng, p, v, rng_int(&rng, 3, 6), rng_uniform(&rng, 1.0, 3.0), u, e);
+		if(i & 1){
+			double R = rng_uniform(&rng, 1.0, 3.0);
+			add_random_poly(sc, &rng, p, v, rng_int(&rng, 3, 6), R, u, e);
+		}
 		else add_circle(sc, p, v, rng_uniform(&rng, 1.0, 3.0), u, e);
 		cpBitmask cat = (cpBitmask)1u << (i % 3);
 		cpBitmask mask = (i % 5 == 0) ? (CP_ALL_CATEGORIES & ~((cpBitmask)1u << ((i + 1) % 3))) : CP_ALL_CATEGORIES;

@@ -513,6 +513,10 @@ int cpGpuDebugSetBodies(cpSpace *space, const double *in, int count);
  * Used with cpGpuDebugSetBodies to run one step from another
  * implementation's complete state. */
 int cpGpuDebugSetImpulses(cpSpace *space, const double *arbs, int narb, const double *cons, int ncons);
+/* The last step's candidates in traversal order, 4 ints each: the two
+ * shapes as the query passed them, the GJK feature id passed in (the pair
+ * cache's) and the one the narrow phase returned. */
+int cpGpuDebugNarrowIds(cpSpace *space, int *out, int max);
 /* Shape-id pairs (min, max) of the last step whose boxes intersect: the
  * pair set the broadphase handed to the narrow phase (2 ints per pair). */
 int cpGpuDebugCandidates(cpSpace *space, int *out, int max);

@@ -1801,6 +1801,9 @@ typedef struct MarkCtx {
 	int collide;      /* 1: run cpSpaceCollideShapes, 0: the void query */
 } MarkCtx;
 
+/* debug trace of GJK ids (cpx_dump_narrow_ids) */
+static int *g_nid = NULL, g_nid_n = 0, g_nid_cap = 0;
+static const cpSpace *g_nid_space = NULL;
 static cpCollisionID collide_shapes(cpSpace *sp, cpShape *a, cpShape *b, cpCollisionID id);
 
 static void mark_leaf_query(cpSpace *sp, int subtree, int leaf, int left, MarkCtx *ctx)
@@ -2100,7 +2103,38 @@ static void active_push(cpSpace *sp, int slot)
 }
 
 /* cpSpaceStep.c:235-289 (default handlers: begin/preSolve accept) */
+/* Debug record of every query-callback call of the last step: shapes, the
+ * GJK id passed in and the one returned (cpx_dump_narrow_ids). */
+static void record_narrow_id(const cpSpace *sp, const cpShape *a, const cpShape *b, cpCollisionID in, cpCollisionID out)
+{
+	if(g_nid_space != sp) return;
+	if(g_nid_n + 4 > g_nid_cap){
+		g_nid_cap = g_nid_cap ? 2*g_nid_cap : 4096;
+		g_nid = (int *)realloc(g_nid, sizeof(int)*(size_t)g_nid_cap);
+	}
+	g_nid[g_nid_n++] = (int)a->hashid; g_nid[g_nid_n++] = (int)b->hashid;
+	g_nid[g_nid_n++] = (int)in; g_nid[g_nid_n++] = (int)out;
+}
+
+static cpCollisionID collide_shapes_(cpSpace *sp, cpShape *a, cpShape *b, cpCollisionID id);
 static cpCollisionID collide_shapes(cpSpace *sp, cpShape *a, cpShape *b, cpCollisionID id)
+{
+	cpCollisionID out = collide_shapes_(sp, a, b, id);
+	record_narrow_id(sp, a, b, id, out);
+	return out;
+}
+
+/* Records (a, b, id in, id out) of the space's last step, 4 ints each, once
+ * cpx_trace_narrow_ids(space) has selected the space (one at a time). */
+void cpx_trace_narrow_ids(cpSpace *sp) { g_nid_space = sp; g_nid_n = 0; }
+int cpx_dump_narrow_ids(cpSpace *sp, int *out, int max)
+{
+	int n = (g_nid_space == sp) ? g_nid_n/4 : 0;
+	for(int i = 0; i < n && i < max; i++) for(int k = 0; k < 4; k++) out[4*i + k] = g_nid[4*i + k];
+	return n;
+}
+
+static cpCollisionID collide_shapes_(cpSpace *sp, cpShape *a, cpShape *b, cpCollisionID id)
 {
 	if(cpBBIntersects(a->bb, b->bb)) record_candidate(sp, a, b);
 	if(query_reject(a, b)) return id;
@@ -2254,6 +2288,7 @@ void cpSpaceStep(cpSpace *sp, cpFloat dt)
 
 	sp->locked++;
 	sp->ncand = 0;
+	if(g_nid_space == sp) g_nid_n = 0;
 	for(int i = 0; i < sp->ndyn; i++){
 		cpBody *body = sp->dyn[i];
 		body->position_func(body, dt);

@@ -23,6 +23,15 @@ import known_answers as ka
 pytestmark = pytest.mark.gpu
 
 RTOL = 1e-12
+# Bias velocities (v_bias, w_bias: the position-correction pseudo-velocity
+# a step leaves for the next position update) carry the contact normals'
+# conditioning: a 2 cm polygon edge at 60 units from the origin turns the
+# one-ulp sin/cos difference of a body's rotation into one ulp of 60 in its
+# world vertices and 3e-13 in that edge's normal (measured on the joints
+# workload, where positions, velocities and impulses stayed within 3e-14).
+# They are held to 1e-11; every other component to RTOL.
+BIAS_COLS = [9, 10, 11]
+RTOL_BIAS = 1e-11
 
 
 def rel_err(a, b):
@@ -45,11 +54,16 @@ def force(g, o):
     assert g.set_impulses(o.arbiters(), o.constraints()) == 0
 
 
-def compare_step(g, o, step, strict_structure=True):
+def compare_step(g, o, step, bias_tol=RTOL_BIAS):
     gb, ob = g.bodies(), o.bodies()
     ga, oa = g.arbiters(), o.arbiters()
     assert ga.shape == oa.shape, "step %d: %d arbiters on the GPU, %d in the oracle" % (step, len(ga), len(oa))
     np.testing.assert_array_equal(ga[:, :3], oa[:, :3], err_msg="step %d: arbiter pairs/counts/order" % step)
+    if len(ob):
+        eb_bias = rel_err(gb[:, BIAS_COLS], ob[:, BIAS_COLS])
+        assert eb_bias <= bias_tol, "step %d: bias velocities differ by %.3g" % (step, eb_bias)
+        keep = [c for c in range(gb.shape[1]) if c not in BIAS_COLS]
+        gb, ob = gb[:, keep], ob[:, keep]
     eb = rel_err(gb, ob)
     ea = rel_err(ga[:, 4:], oa[:, 4:])
     gj, oj = g.constraints(), o.constraints()
@@ -130,7 +144,7 @@ def test_pyramid_free_run_1000_steps(gpu_lib, oracle_lib):
             o.step(1 / 60)
             if s % 50 == 49 or s < 5:
                 check_gpu_error(gpu_lib)
-                eb, ea, _ = compare_step(g, o, s)
+                eb, ea, _ = compare_step(g, o, s, bias_tol=FREE_RUN_DRIFT)
                 worst = max(worst, eb, ea)
         print("pyramid free-run drift after 1000 steps: %.3g" % worst)
         assert worst <= FREE_RUN_DRIFT, worst
