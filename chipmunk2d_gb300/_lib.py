@@ -150,6 +150,7 @@ _API = {
     "cpx_scene_step": (None, [P, D, I]),
     "cpx_space_set_hasty": (I, [P, I]),
     "cpx_scene_free": (None, [P]),
+    "cpx_scene_edit": (I, [P, I, ctypes.c_ulonglong]),
     "cpx_batch_sizes": (None, [I, ctypes.c_ulonglong, P]),
     # state export (shared record layouts)
     "cpx_dump_bodies": (I, [P, P, I]),
@@ -260,9 +261,20 @@ class Scene:
         self.lib.cpx_scene_step(self.h, dt, steps)
 
     def bodies(self):
-        out = np.zeros(BODY_REC * max(self.nbodies, 1))
-        n = self.lib.cpx_dump_bodies(self.space, out.ctypes.data, self.nbodies)
+        # the space's dynamic bodies now (objects may have been added or removed)
+        cap = self.lib.cpx_dump_bodies(self.space, None, 0)
+        out = np.zeros(BODY_REC * max(cap, 1))
+        n = self.lib.cpx_dump_bodies(self.space, out.ctypes.data, cap)
         return out[:BODY_REC * n].reshape(n, BODY_REC)
+
+    def edit(self, round_, seed):
+        """One round of deterministic edits between steps (cpx_scene_edit):
+        removals, additions, constraint churn and body-type changes."""
+        n = self.lib.cpx_scene_edit(self.h, round_, seed)
+        self.nbodies = self.lib.cpx_scene_body_count(self.h)
+        self.nshapes = self.lib.cpx_scene_shape_count(self.h)
+        self.nconstraints = self.lib.cpx_scene_constraint_count(self.h)
+        return n
 
     def set_bodies(self, arr):
         arr = np.ascontiguousarray(arr, dtype=np.float64)
@@ -287,8 +299,8 @@ class Scene:
             cap = n
 
     def constraints(self):
-        cap = max(self.nconstraints, 1)
-        out = np.zeros(CONS_REC * cap)
+        cap = self.lib.cpx_dump_constraints(self.space, None, 0)
+        out = np.zeros(CONS_REC * max(cap, 1))
         n = self.lib.cpx_dump_constraints(self.space, out.ctypes.data, cap)
         return out[:CONS_REC * n].reshape(n, CONS_REC)
 

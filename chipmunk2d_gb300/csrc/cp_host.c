@@ -1718,10 +1718,12 @@ int cpGpuRolloutBackwardFull(cpGpuBatch *b, const cpFloat *dLdp, const cpFloat *
 					if(dLdw0) dLdw0[idx] = h[9*g + 5];
 					if(dLdm) dLdm[idx] = -gm[g]*minv[g]*minv[g];
 				}
-				for(int i = 0; i < sp->nshapes; i++, sidx++){
+				for(int i = 0; i < sp->nshapes; i++){
+					if(!sp->shapes[i]) continue;      /* a removed shape's slot */
 					size_t g = (size_t)ds->hworld[w].shapeOff + i;
 					if(dLde) dLde[sidx] = ge[g];
 					if(dLdu) dLdu[sidx] = gu[g];
+					sidx++;
 				}
 			}
 			free(gm); free(minv); free(ge); free(gu);
@@ -1933,6 +1935,49 @@ void cpBodyFree(cpBody *b) { free(b); }
 void cpBodyActivate(cpBody *b) { (void)b; }
 cpBool cpBodyIsSleeping(const cpBody *b) { (void)b; return cpFalse; }
 cpBodyType cpBodyGetType(cpBody *b) { return (cpBodyType)body_type_(b); }
+static int space_edit_ok(cpSpace *sp);
+static int array_delete_(void **arr, int *n, void *obj);
+static void record_op_(cpSpace *sp, int kind, cpShape *s, int isStatic);
+static void accumulate_mass_(cpBody *b);
+
+void cpBodySetType(cpBody *b, cpBodyType type)
+{
+	/* cpBody.c:157-205 */
+	int oldType = body_type_(b);
+	if(oldType == (int)type) return;
+	cpSpace *sp = b->space;
+	if(sp && !space_edit_ok(sp)) return;
+	if(sp) sp->bodyDirty = 1;
+	b->idleTime = (type == CP_BODY_TYPE_STATIC ? INF_ : 0.0);
+	if(type == CP_BODY_TYPE_DYNAMIC){
+		b->m = b->i = 0.0;
+		b->m_inv = b->i_inv = INF_;
+		accumulate_mass_(b);
+	} else {
+		b->m = b->i = INF_;
+		b->m_inv = b->i_inv = 0.0;
+		b->v = cpvzero;
+		b->w = 0.0;
+	}
+	if(!sp) return;
+	/* the body changes array (dynamic and kinematic bodies share one), and
+	 * its shapes change index: each leaves one tree and enters the other
+	 * with its cached box, in shape-list order */
+	int fromStatic = (oldType == CP_BODY_TYPE_STATIC), toStatic = (type == CP_BODY_TYPE_STATIC);
+	if(fromStatic != toStatic){
+		if(fromStatic){
+			array_delete_((void **)sp->stat, &sp->nstat, b);
+			push_((void ***)&sp->dyn, &sp->ndyn, &sp->capdyn, b);
+		} else {
+			array_delete_((void **)sp->dyn, &sp->ndyn, b);
+			push_((void ***)&sp->stat, &sp->nstat, &sp->capstat, b);
+		}
+		for(cpShape *s = b->shapeList; s; s = s->next){
+			record_op_(sp, CPG_OP_REMOVE, s, fromStatic);
+			record_op_(sp, CPG_OP_INSERT, s, toStatic);
+		}
+	}
+}
 cpSpace *cpBodyGetSpace(const cpBody *b) { return b->space; }
 cpFloat cpBodyGetMass(const cpBody *b) { return b->m; }
 cpFloat cpBodyGetMoment(const cpBody *b) { return b->i; }
@@ -2147,6 +2192,47 @@ static void shapes_pull_(cpSpace *sp)
 	for(int i = 0; i < n; i++) if(sp->shapes[i]) sp->shapes[i]->bb = cpBBNew(buf[i], buf[n + i], buf[2*n + i], buf[3*n + i]);
 	free(buf);
 	sp->shapesStale = 0;
+}
+
+/* The device's whole shape caches (boxes and world geometry) into the
+ * host structs, before a rebuild uploads them again: a shape whose body
+ * turns static keeps the caches of its last step (the reference updates
+ * only dynamic shapes, cpSpaceStep.c:380-382). */
+static void shapes_pull_all_(cpSpace *sp)
+{
+	if(!sp || !sp->dev) return;
+	DevSet *ds = sp->dev;
+	shapes_pull_(sp);
+	const cpgWorld *W = &ds->hworld[sp->world];
+	int n = W->nshapes, nv = W->nverts;
+	if(n > sp->nshapes) n = sp->nshapes;
+	double *buf = HALLOC(double, 6*(size_t)W->nshapes + 4*(size_t)nv);
+	const double *src[6] = { ds->d.w0x, ds->d.w0y, ds->d.w1x, ds->d.w1y, ds->d.wnx, ds->d.wny };
+	for(int k = 0; k < 6; k++) d2h(buf + (size_t)k*W->nshapes, src[k] + W->shapeOff, sizeof(double)*(size_t)W->nshapes);
+	double *vb = buf + 6*(size_t)W->nshapes;
+	const double *vsrc[4] = { ds->d.gvx, ds->d.gvy, ds->d.gnx, ds->d.gny };
+	for(int k = 0; k < 4; k++) d2h(vb + (size_t)k*nv, vsrc[k] + W->vertOff, sizeof(double)*(size_t)nv);
+	int *voff = HALLOC(int, W->nshapes);
+	d2h(voff, ds->d.svoff + W->shapeOff, sizeof(int)*(size_t)W->nshapes);
+	if(!cuda_ok(cudaStreamSynchronize(lib_stream()), "download shape caches")){ free(buf); free(voff); return; }
+	size_t S = (size_t)W->nshapes;
+	for(int i = 0; i < n; i++){
+		cpShape *sh = sp->shapes[i];
+		if(!sh) continue;
+		cpVect g0 = cpv(buf[i], buf[S + i]), g1 = cpv(buf[2*S + i], buf[3*S + i]), gn = cpv(buf[4*S + i], buf[5*S + i]);
+		if(sh->kind == CPG_CIRCLE){
+			sh->tc = g0;
+		} else if(sh->kind == CPG_SEGMENT){
+			sh->ta = g0; sh->tb = g1; sh->tn = gn;
+		} else {
+			for(int j = 0; j < sh->count && voff[i] + j < nv; j++){
+				size_t v = (size_t)voff[i] + j;
+				sh->gv[j] = cpv(vb[v], vb[nv + v]);
+				sh->gn[j] = cpv(vb[2*(size_t)nv + v], vb[3*(size_t)nv + v]);
+			}
+		}
+	}
+	free(buf); free(voff);
 }
 
 static cpBB shape_bb_now_(cpShape *s)
@@ -2370,6 +2456,17 @@ cpVect cpSlideJointGetAnchorA(const cpConstraint *c) { return c->anchorA; }
 cpVect cpSlideJointGetAnchorB(const cpConstraint *c) { return c->anchorB; }
 cpFloat cpSlideJointGetMin(const cpConstraint *c) { return c->min; }
 cpFloat cpSlideJointGetMax(const cpConstraint *c) { return c->max; }
+/* setters: cpPivotJoint.c:145-165, cpPinJoint.c:148-180, cpSlideJoint.c:158-201
+ * (the reference also wakes the bodies; there is no sleeping here) */
+void cpPivotJointSetAnchorA(cpConstraint *c, cpVect v) { ASSERT_HARD(c->kind == CPG_PIVOT, "Constraint is not a pivot joint."); cwr(c)->anchorA = v; }
+void cpPivotJointSetAnchorB(cpConstraint *c, cpVect v) { ASSERT_HARD(c->kind == CPG_PIVOT, "Constraint is not a pivot joint."); cwr(c)->anchorB = v; }
+void cpPinJointSetAnchorA(cpConstraint *c, cpVect v) { ASSERT_HARD(c->kind == CPG_PIN, "Constraint is not a pin joint."); cwr(c)->anchorA = v; }
+void cpPinJointSetAnchorB(cpConstraint *c, cpVect v) { ASSERT_HARD(c->kind == CPG_PIN, "Constraint is not a pin joint."); cwr(c)->anchorB = v; }
+void cpPinJointSetDist(cpConstraint *c, cpFloat d) { ASSERT_HARD(c->kind == CPG_PIN, "Constraint is not a pin joint."); cwr(c)->dist = d; }
+void cpSlideJointSetAnchorA(cpConstraint *c, cpVect v) { ASSERT_HARD(c->kind == CPG_SLIDE, "Constraint is not a slide joint."); cwr(c)->anchorA = v; }
+void cpSlideJointSetAnchorB(cpConstraint *c, cpVect v) { ASSERT_HARD(c->kind == CPG_SLIDE, "Constraint is not a slide joint."); cwr(c)->anchorB = v; }
+void cpSlideJointSetMin(cpConstraint *c, cpFloat v) { ASSERT_HARD(c->kind == CPG_SLIDE, "Constraint is not a slide joint."); cwr(c)->min = v; }
+void cpSlideJointSetMax(cpConstraint *c, cpFloat v) { ASSERT_HARD(c->kind == CPG_SLIDE, "Constraint is not a slide joint."); cwr(c)->max = v; }
 
 cpFloat cpConstraintGetImpulse(cpConstraint *c)
 {
@@ -2457,7 +2554,7 @@ static void space_detach(cpSpace *sp)
 	if(!sp || !sp->dev || sp->structDirty || !sp->ownsDev) return;
 	space_pull(sp);
 	joints_pull_(sp);
-	shapes_pull_(sp);
+	shapes_pull_all_(sp);
 	sp->structDirty = 1;
 	sp->snapValid = 0;
 }
@@ -2665,9 +2762,13 @@ static int space_snapshot(cpSpace *sp)
 		sp->capsnap = n + 64;
 		sp->snap = (cpArbiter *)realloc(sp->snap, sizeof(cpArbiter)*(size_t)sp->capsnap);
 	}
+	int kept = 0;
 	for(int i = 0; i < n; i++){
-		cpArbiter *arb = &sp->snap[i];
 		cpgArb *g = &host[i];
+		/* a shape removed since the step: its arbiters are gone too
+		 * (cpSpaceFilterArbiters) */
+		if(g->a < 0 || g->a >= sp->nshapes || g->b < 0 || g->b >= sp->nshapes || !sp->shapes[g->a] || !sp->shapes[g->b]) continue;
+		cpArbiter *arb = &sp->snap[kept++];
 		arb->a = sp->shapes[g->a]; arb->b = sp->shapes[g->b];
 		arb->body_a = arb->a->body; arb->body_b = arb->b->body;
 		arb->count = g->count; arb->state = g->state;
@@ -2675,7 +2776,7 @@ static int space_snapshot(cpSpace *sp)
 		arb->e = g->e; arb->u = g->u; arb->swapped = cpFalse;
 		arb->c[0] = g->c[0]; arb->c[1] = g->c[1];
 	}
-	sp->nsnap = n;
+	sp->nsnap = kept;
 	sp->snapValid = 1;
 	free(host);
 	return 1;
@@ -2940,6 +3041,7 @@ int cpGpuDebugCandidates(cpSpace *sp, int *out, int max)
 	int k = 0;
 	for(int i = 0; i < n; i++){
 		cpShape *a = sp->shapes[c[i].a], *b = sp->shapes[c[i].b];
+		if(!a || !b) continue;
 		cpBB ba = shape_bb_now_(a), bb = shape_bb_now_(b);
 		if(!cpBBIntersects(ba, bb)) continue;
 		if(k < max){

@@ -153,6 +153,11 @@ typedef struct cpxScene {
 	cpShape **shapes;         /* every shape (static ones included), add order */
 	int nconstraints, cap_constraints;
 	cpConstraint **constraints;
+	/* bodies whose type an edit round changed, with the mass and moment
+	 * they get back when they turn dynamic again */
+	cpBody *changed[4];
+	double changedM[4], changedI[4];
+	int nchanged;
 } cpxScene;
 
 static void push_ptr(void ***arr, int *n, int *cap, void *p)
@@ -513,6 +518,168 @@ void *cpx_scene_build(int config, int size, unsigned long long seed)
 		default: cpSpaceFree(sc->space); free(sc); return NULL;
 	}
 	return sc;
+}
+
+/* Whether one of b's shapes is within `margin` of a static shape's box.
+ * A body that turns static while it touches a static body keeps that
+ * arbiter forever (static pairs never age, cpSpaceStep.c:292-325); the
+ * reference leaves its contacts in a contact buffer that is recycled after
+ * the persistence window and, if the body turns dynamic again, warm-starts
+ * from whatever that memory then holds.  The edit rounds keep clear of that
+ * case. */
+static int near_static(cpxScene *sc, cpBody *b, double margin)
+{
+	cpSpace *sp = sc->space;
+	for(int k = 0; k < sc->nshapes; k++){
+		cpShape *s = sc->shapes[k];
+		if(cpShapeGetBody(s) != b || cpShapeGetSpace(s) != sp) continue;
+		cpBB bb = cpShapeGetBB(s);
+		bb.l -= margin; bb.b -= margin; bb.r += margin; bb.t += margin;
+		for(int q = 0; q < sc->nshapes; q++){
+			cpShape *o = sc->shapes[q];
+			if(cpShapeGetSpace(o) != sp || cpBodyGetType(cpShapeGetBody(o)) != CP_BODY_TYPE_STATIC) continue;
+			cpBB ob = cpShapeGetBB(o);
+			if(bb.l <= ob.r && ob.l <= bb.r && bb.b <= ob.t && ob.b <= bb.t) return 1;
+		}
+	}
+	return 0;
+}
+
+/* One round of edits between steps, the same calls in every
+ * implementation (seeded by `seed` and `round`):
+ *   - 1 in 16 single-shape dynamic bodies without constraints leave the
+ *     space (shape first, then body);
+ *   - as many new circles and polys (radius U[1,3]) enter near the top with
+ *     v~N(0,10)/axis, plus one more;
+ *   - one constraint (if any) leaves, and a pin joint joins a random
+ *     dynamic body to its nearest dynamic neighbour (collideBodies off on
+ *     odd rounds);
+ *   - one dynamic body with shapes and no constraints, clear of static
+ *     shapes (near_static), turns static and, on the next round, dynamic
+ *     again with its mass and moment; one turns kinematic with a velocity,
+ *     and dynamic on the next round.
+ * Returns the number of edits. */
+int cpx_scene_edit(void *h, int round, unsigned long long seed)
+{
+	cpxScene *sc = (cpxScene *)h;
+	cpSpace *sp = sc->space;
+	Rng rng; rng_seed(&rng, seed*1000003ull + (unsigned long long)round);
+	int edits = 0;
+	/* bodies that changed type last round go back to dynamic, with their
+	 * mass and moment (cpBodySetType recomputes them from the shapes, and
+	 * these shapes carry none) */
+	for(int k = 0; k < sc->nchanged; k++){
+		cpBody *b = sc->changed[k];
+		if(cpBodyGetSpace(b) != sp) continue;
+		cpBodySetType(b, CP_BODY_TYPE_DYNAMIC);
+		cpBodySetMass(b, sc->changedM[k]);
+		cpBodySetMoment(b, sc->changedI[k]);
+		edits++;
+	}
+	sc->nchanged = 0;
+	/* removals */
+	int nb0 = sc->nbodies;
+	for(int i = 0; i < nb0; i++){
+		cpBody *b = sc->bodies[i];
+		if(cpBodyGetSpace(b) != sp || rng_int(&rng, 0, 15) != 0) continue;
+		cpShape *only = NULL; int nshape = 0, ncons = 0;
+		for(int k = 0; k < sc->nshapes; k++) if(cpShapeGetBody(sc->shapes[k]) == b && cpShapeGetSpace(sc->shapes[k]) == sp){ only = sc->shapes[k]; nshape++; }
+		for(int k = 0; k < sc->nconstraints; k++){
+			cpConstraint *c = sc->constraints[k];
+			if(cpConstraintGetSpace(c) == sp && (cpConstraintGetBodyA(c) == b || cpConstraintGetBodyB(c) == b)) ncons++;
+		}
+		if(nshape != 1 || ncons != 0) continue;
+		cpSpaceRemoveShape(sp, only);
+		cpSpaceRemoveBody(sp, b);
+		edits += 2;
+	}
+	/* additions, dropped near the top of the scene's box of bodies */
+	double lo = 1e30, hi = -1e30, top = -1e30;
+	for(int i = 0; i < sc->nbodies; i++){
+		cpBody *b = sc->bodies[i];
+		if(cpBodyGetSpace(b) != sp) continue;
+		cpVect p = cpBodyGetPosition(b);
+		if(p.x < lo) lo = p.x;
+		if(p.x > hi) hi = p.x;
+		if(p.y > top) top = p.y;
+	}
+	if(lo > hi){ lo = -10.0; hi = 10.0; top = 0.0; }
+	int adds = edits/2 + 1;
+	for(int i = 0; i < adds; i++){
+		cpVect p = rng_point(&rng, lo, hi, top + 4.0, top + 12.0);
+		cpVect v = rng_normal2(&rng, 10.0);
+		double u = rng_uniform(&rng, 0.3, 1.0), e = rng_uniform(&rng, 0.0, 0.3);
+		if(i & 1){
+			double R = rng_uniform(&rng, 1.0, 3.0);
+			add_random_poly(sc, &rng, p, v, rng_int(&rng, 3, 6), R, u, e);
+		} else {
+			add_circle(sc, p, v, rng_uniform(&rng, 1.0, 3.0), u, e);
+		}
+		edits++;
+	}
+	/* constraints */
+	int live = 0;
+	for(int k = 0; k < sc->nconstraints; k++) live += (cpConstraintGetSpace(sc->constraints[k]) == sp);
+	if(live > 0){
+		int pick = rng_int(&rng, 0, live - 1);
+		for(int k = 0; k < sc->nconstraints; k++){
+			cpConstraint *c = sc->constraints[k];
+			if(cpConstraintGetSpace(c) != sp) continue;
+			if(pick-- == 0){ cpSpaceRemoveConstraint(sp, c); edits++; break; }
+		}
+	}
+	/* the pin joint links a random dynamic body to its nearest dynamic
+	 * neighbour, at their centres */
+	cpBody *pa = NULL, *pb = NULL;
+	for(int tries = 0; tries < 64 && !pa; tries++){
+		cpBody *b = sc->bodies[rng_int(&rng, 0, sc->nbodies - 1)];
+		if(cpBodyGetSpace(b) == sp && cpBodyGetType(b) == CP_BODY_TYPE_DYNAMIC) pa = b;
+	}
+	if(pa){
+		cpVect q = cpBodyGetPosition(pa);
+		double best = 1e300;
+		for(int i = 0; i < sc->nbodies; i++){
+			cpBody *b = sc->bodies[i];
+			if(b == pa || cpBodyGetSpace(b) != sp || cpBodyGetType(b) != CP_BODY_TYPE_DYNAMIC) continue;
+			double d = cpvdistsq(cpBodyGetPosition(b), q);
+			if(d < best){ best = d; pb = b; }
+		}
+	}
+	if(pa && pb){
+		cpConstraint *j = cpPinJointNew(pa, pb, cpvzero, cpvzero);
+		if(round & 1) cpConstraintSetCollideBodies(j, cpFalse);
+		add_constraint(sc, j);
+		edits++;
+	}
+	/* type changes: dynamic bodies in the space with shapes and without
+	 * constraints (a joint between two bodies of infinite mass has no
+	 * finite impulse) */
+	for(int which = 0; which < 2; which++){
+		for(int tries = 0; tries < 64; tries++){
+			cpBody *b = sc->bodies[rng_int(&rng, 0, sc->nbodies - 1)];
+			if(cpBodyGetSpace(b) != sp || cpBodyGetType(b) != CP_BODY_TYPE_DYNAMIC) continue;
+			int has = 0, cons = 0;
+			for(int k = 0; k < sc->nshapes && !has; k++) has = (cpShapeGetBody(sc->shapes[k]) == b && cpShapeGetSpace(sc->shapes[k]) == sp);
+			for(int k = 0; k < sc->nconstraints; k++){
+				cpConstraint *c = sc->constraints[k];
+				cons += (cpConstraintGetSpace(c) == sp && (cpConstraintGetBodyA(c) == b || cpConstraintGetBodyB(c) == b));
+			}
+			if(!has || cons || (which == 0 && near_static(sc, b, 4.0))) continue;
+			sc->changed[sc->nchanged] = b;
+			sc->changedM[sc->nchanged] = cpBodyGetMass(b);
+			sc->changedI[sc->nchanged] = cpBodyGetMoment(b);
+			sc->nchanged++;
+			if(which == 0){
+				cpBodySetType(b, CP_BODY_TYPE_STATIC);
+			} else {
+				cpBodySetType(b, CP_BODY_TYPE_KINEMATIC);
+				cpBodySetVelocity(b, rng_normal2(&rng, 3.0));
+			}
+			edits++;
+			break;
+		}
+	}
+	return edits;
 }
 
 cpSpace *cpx_scene_space(void *h) { return ((cpxScene *)h)->space; }

@@ -229,6 +229,13 @@ cpBool cpSpaceIsLocked(cpSpace *space);                              /* cpSpace.
 cpShape *cpSpaceAddShape(cpSpace *space, cpShape *shape);            /* cpSpace.h:159 */
 cpBody *cpSpaceAddBody(cpSpace *space, cpBody *body);                /* cpSpace.h:161 */
 cpConstraint *cpSpaceAddConstraint(cpSpace *space, cpConstraint *c); /* cpSpace.h:163 */
+/* Removal (and addition) between steps: the next cpSpaceStep rebuilds the
+ * device set, carrying the tree, pair cache and arbiter cache over, and
+ * replays the index edits in call order; removal order follows the
+ * reference's arrays (the last element takes the hole). */
+void cpSpaceRemoveShape(cpSpace *space, cpShape *shape);              /* cpSpace.h:166 */
+void cpSpaceRemoveBody(cpSpace *space, cpBody *body);                 /* cpSpace.h:168 */
+void cpSpaceRemoveConstraint(cpSpace *space, cpConstraint *constraint); /* cpSpace.h:170 */
 cpBool cpSpaceContainsShape(cpSpace *space, cpShape *shape);         /* cpSpace.h:173 */
 cpBool cpSpaceContainsBody(cpSpace *space, cpBody *body);            /* cpSpace.h:175 */
 cpBool cpSpaceContainsConstraint(cpSpace *space, cpConstraint *c);   /* cpSpace.h:177 */
@@ -247,6 +254,7 @@ void cpBodyFree(cpBody *body);                                       /* cpBody.h
 void cpBodyActivate(cpBody *body);                                   /* cpBody.h:67  */
 cpBool cpBodyIsSleeping(const cpBody *body);                         /* cpBody.h:77  */
 cpBodyType cpBodyGetType(cpBody *body);                              /* cpBody.h:80  */
+void cpBodySetType(cpBody *body, cpBodyType type);                    /* cpBody.h:82  */
 cpSpace *cpBodyGetSpace(const cpBody *body);                         /* cpBody.h:85  */
 cpFloat cpBodyGetMass(const cpBody *body);                           /* cpBody.h:88  */
 void cpBodySetMass(cpBody *body, cpFloat m);                         /* cpBody.h:90  */
@@ -359,12 +367,17 @@ cpConstraint *cpPivotJointNew(cpBody *a, cpBody *b, cpVect pivot);           /* 
 cpConstraint *cpPivotJointNew2(cpBody *a, cpBody *b, cpVect anchorA, cpVect anchorB); /* cpPivotJoint.h:35 */
 cpVect cpPivotJointGetAnchorA(const cpConstraint *constraint);               /* cpPivotJoint.h:38 */
 cpVect cpPivotJointGetAnchorB(const cpConstraint *constraint);               /* cpPivotJoint.h:43 */
+void cpPivotJointSetAnchorA(cpConstraint *constraint, cpVect anchorA);       /* cpPivotJoint.h:40 */
+void cpPivotJointSetAnchorB(cpConstraint *constraint, cpVect anchorB);       /* cpPivotJoint.h:45 */
 
 cpBool cpConstraintIsPinJoint(const cpConstraint *constraint);               /* cpPinJoint.h:26 */
 cpConstraint *cpPinJointNew(cpBody *a, cpBody *b, cpVect anchorA, cpVect anchorB);    /* cpPinJoint.h:33 */
 cpVect cpPinJointGetAnchorA(const cpConstraint *constraint);                 /* cpPinJoint.h:36 */
 cpVect cpPinJointGetAnchorB(const cpConstraint *constraint);                 /* cpPinJoint.h:41 */
 cpFloat cpPinJointGetDist(const cpConstraint *constraint);                   /* cpPinJoint.h:46 */
+void cpPinJointSetAnchorA(cpConstraint *constraint, cpVect anchorA);         /* cpPinJoint.h:38 */
+void cpPinJointSetAnchorB(cpConstraint *constraint, cpVect anchorB);         /* cpPinJoint.h:43 */
+void cpPinJointSetDist(cpConstraint *constraint, cpFloat dist);              /* cpPinJoint.h:48 */
 
 cpBool cpConstraintIsSlideJoint(const cpConstraint *constraint);             /* cpSlideJoint.h:26 */
 cpConstraint *cpSlideJointNew(cpBody *a, cpBody *b, cpVect anchorA, cpVect anchorB, cpFloat min, cpFloat max); /* cpSlideJoint.h:33 */
@@ -372,6 +385,10 @@ cpVect cpSlideJointGetAnchorA(const cpConstraint *constraint);               /* 
 cpVect cpSlideJointGetAnchorB(const cpConstraint *constraint);               /* cpSlideJoint.h:41 */
 cpFloat cpSlideJointGetMin(const cpConstraint *constraint);                  /* cpSlideJoint.h:46 */
 cpFloat cpSlideJointGetMax(const cpConstraint *constraint);                  /* cpSlideJoint.h:51 */
+void cpSlideJointSetAnchorA(cpConstraint *constraint, cpVect anchorA);       /* cpSlideJoint.h:38 */
+void cpSlideJointSetAnchorB(cpConstraint *constraint, cpVect anchorB);       /* cpSlideJoint.h:43 */
+void cpSlideJointSetMin(cpConstraint *constraint, cpFloat min);              /* cpSlideJoint.h:48 */
+void cpSlideJointSetMax(cpConstraint *constraint, cpFloat max);              /* cpSlideJoint.h:53 */
 
 /* ------------------------------------------------------------------------
  * Arbiters: cpArbiter.h:32-119.  Arbiter handles are valid from the

@@ -2041,6 +2041,135 @@ cpConstraint *cpSpaceAddConstraint(cpSpace *sp, cpConstraint *c)
 	return c;
 }
 
+/* cpBBTree.c:619-630 (cpBBTreeRemove): the leaf leaves the leaf set
+ * (cpHashSet.c:209-233: unlinked from its bin, the others keep their
+ * order), the tree and every pair list, and is recycled. */
+static void tree_remove(cpSpace *sp, Tree *tree, cpShape *s)
+{
+	LeafSet *set = &tree->leaves;
+	unsigned idx = (unsigned)(s->hashid % set->size);
+	int prev = -1, leaf = set->bins[idx];
+	while(leaf >= 0 && sp->nodes[leaf].obj != s){ prev = leaf; leaf = sp->nodes[leaf].binNext; }
+	ORC_ASSERT(leaf >= 0, "shape missing from its index");
+	if(prev >= 0) sp->nodes[prev].binNext = sp->nodes[leaf].binNext;
+	else set->bins[idx] = sp->nodes[leaf].binNext;
+	set->entries--;
+	tree->root = subtree_remove(sp, tree->root, leaf);
+	pairs_clear(sp, leaf);
+	node_recycle(sp, leaf);
+	s->leaf = -1;
+}
+
+/* cpArrayDeleteObj (cpArray.c:76-88): the last element takes the hole. */
+static int array_delete_(void **arr, int *n, void *obj)
+{
+	for(int i = 0; i < *n; i++){
+		if(arr[i] == obj){ (*n)--; arr[i] = arr[*n]; arr[*n] = NULL; return i; }
+	}
+	return -1;
+}
+
+/* cpSpace.c:481-521 (cpSpaceFilterArbiters with a shape): every cached
+ * arbiter of the shape is dropped.  The reference also deletes it from the
+ * last step's arbiter array, whose order then depends on the hash set's
+ * pointer hashes; here the array keeps its order (the next step rebuilds
+ * it from scratch either way). */
+static void filter_arbiters_of(cpSpace *sp, cpShape *s)
+{
+	ArbMap *m = &sp->amap;
+	for(int h = 0; h < m->cap; h++){
+		if(m->keys[h] <= 1) continue;
+		int slot = m->slot[h];
+		cpArbiter *arb = &sp->arbs[slot];
+		if(arb->a != s && arb->b != s) continue;
+		m->keys[h] = 1;
+		arb_free(sp, slot);
+		int k = 0;
+		for(int i = 0; i < sp->nactive; i++) if(sp->active[i] != slot) sp->active[k++] = sp->active[i];
+		sp->nactive = k;
+	}
+}
+
+void cpSpaceRemoveShape(cpSpace *sp, cpShape *s)
+{
+	/* cpSpace.c:523-545 */
+	ORC_ASSERT(s->space == sp, "Cannot remove a shape that was not added to the space.");
+	cpBody *body = s->body;
+	int isStatic = (body_type(body) == CP_BODY_TYPE_STATIC);
+	/* cpBodyRemoveShape, cpBody.c:306-327 */
+	if(s->prev) s->prev->next = s->next; else body->shapeList = s->next;
+	if(s->next) s->next->prev = s->prev;
+	s->prev = s->next = NULL;
+	if(body_type(body) == CP_BODY_TYPE_DYNAMIC && s->mass_m > 0.0) body_accumulate_mass(body);
+	filter_arbiters_of(sp, s);
+	tree_remove(sp, isStatic ? &sp->statTree : &sp->dynTree, s);
+	s->space = NULL;
+	s->hashid = 0;
+}
+
+void cpSpaceRemoveBody(cpSpace *sp, cpBody *body)
+{
+	/* cpSpace.c:547-562 */
+	ORC_ASSERT(body != &sp->staticBody, "Cannot remove the designated static body for the space.");
+	ORC_ASSERT(body->space == sp, "Cannot remove a body that was not added to the space.");
+	if(body_type(body) == CP_BODY_TYPE_STATIC) array_delete_((void **)sp->stat, &sp->nstat, body);
+	else array_delete_((void **)sp->dyn, &sp->ndyn, body);
+	body->space = NULL;
+}
+
+/* cpBody.c:272-287 (filterConstraints) */
+static cpConstraint *filter_constraints_(cpConstraint *node, cpBody *body, cpConstraint *filter)
+{
+	if(node == filter) return constraint_next_(node, body);
+	if(node->a == body) node->next_a = filter_constraints_(node->next_a, body, filter);
+	else node->next_b = filter_constraints_(node->next_b, body, filter);
+	return node;
+}
+
+void cpSpaceRemoveConstraint(cpSpace *sp, cpConstraint *c)
+{
+	/* cpSpace.c:564-577 */
+	ORC_ASSERT(c->space == sp, "Cannot remove a constraint that was not added to the space.");
+	array_delete_((void **)sp->cons, &sp->ncons, c);
+	c->a->constraintList = filter_constraints_(c->a->constraintList, c->a, c);
+	c->b->constraintList = filter_constraints_(c->b->constraintList, c->b, c);
+	c->space = NULL;
+}
+
+void cpBodySetType(cpBody *body, cpBodyType type)
+{
+	/* cpBody.c:157-205 */
+	cpBodyType oldType = body_type(body);
+	if(oldType == type) return;
+	body->idleTime = (type == CP_BODY_TYPE_STATIC ? ORC_INF : 0.0);
+	if(type == CP_BODY_TYPE_DYNAMIC){
+		body->m = body->i = 0.0;
+		body->m_inv = body->i_inv = ORC_INF;
+		body_accumulate_mass(body);
+	} else {
+		body->m = body->i = ORC_INF;
+		body->m_inv = body->i_inv = 0.0;
+		body->v = cpvzero;
+		body->w = 0.0;
+	}
+	cpSpace *sp = body->space;
+	if(!sp) return;
+	int fromStatic = (oldType == CP_BODY_TYPE_STATIC), toStatic = (type == CP_BODY_TYPE_STATIC);
+	if(fromStatic != toStatic){
+		if(fromStatic){
+			array_delete_((void **)sp->stat, &sp->nstat, body);
+			push_ptr_((void ***)&sp->dyn, &sp->ndyn, &sp->capdyn, body);
+		} else {
+			array_delete_((void **)sp->dyn, &sp->ndyn, body);
+			push_ptr_((void ***)&sp->stat, &sp->nstat, &sp->capstat, body);
+		}
+		for(cpShape *s = body->shapeList; s; s = s->next){
+			tree_remove(sp, fromStatic ? &sp->statTree : &sp->dynTree, s);
+			tree_insert(sp, toStatic ? &sp->statTree : &sp->dynTree, s);
+		}
+	}
+}
+
 void cpSpaceEachBody(cpSpace *sp, cpSpaceBodyIteratorFunc func, void *data)
 {
 	for(int i = 0; i < sp->ndyn; i++) func(sp->dyn[i], data);

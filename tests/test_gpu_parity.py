@@ -101,6 +101,39 @@ def test_teacher_forced_per_step(gpu_lib, oracle_lib, name, cfg, size, dt, steps
     print("%s: worst rel err bodies %.3g arbiters %.3g joints %.3g" % (name, *worst))
 
 
+@pytest.mark.parametrize("cfg,size", [(6, 200), (3, 600), (1, 14), (4, 150)], ids=["joints", "mixed", "pyramid", "tumble"])
+def test_teacher_forced_with_objects_added_and_removed(gpu_lib, oracle_lib, cfg, size):
+    """Objects added and removed between steps (cpx_scene_edit every 10
+    steps: removals, additions, constraint churn, body-type changes).  The
+    GPU rebuilds its set at the next step, carrying the tree and arbiter
+    cache over, and must stay on the oracle's per-step results: same
+    arbiter lists, bodies and joints within the per-step bounds.  On an
+    edit step only the bodies are forced (the arbiter lists of the two
+    sides are compared after the step)."""
+    g = Scene(gpu_lib, cfg, size)
+    o = Scene(oracle_lib, cfg, size)
+    worst = 0.0
+    try:
+        for s in range(150):
+            edited = (s % 10 == 5)
+            if edited:
+                assert g.edit(s // 10, 7) == o.edit(s // 10, 7)
+                g.set_bodies(o.bodies())
+            else:
+                force(g, o)
+            g.step(1 / 60)
+            o.step(1 / 60)
+            check_gpu_error(gpu_lib)
+            assert g.bodies().shape == o.bodies().shape
+            errs = compare_step(g, o, s)
+            worst = max(worst, *errs)
+            assert max(errs) <= RTOL, "step %d: body %.3g arbiter %.3g joint %.3g" % ((s,) + errs)
+    finally:
+        g.free()
+        o.free()
+    print("edits, workload %d: worst rel err %.3g" % (cfg, worst))
+
+
 FREE_RUN_DRIFT = 1e-9
 
 

@@ -43,6 +43,30 @@ def test_oracle_bit_exact_per_step(ref_lib, oracle_lib, cfg, size, steps, dt):
         o.free()
 
 
+@pytest.mark.parametrize("cfg,size", [(6, 120), (4, 150), (3, 300), (1, 14)])
+def test_oracle_bit_exact_with_objects_added_and_removed(ref_lib, oracle_lib, cfg, size):
+    """Every 10 steps a round of edits between steps (cpx_scene_edit): shapes
+    and bodies leave, new ones enter, a constraint leaves and a pin joint
+    joins, bodies turn static or kinematic and back.  The state after every
+    step must stay bit-identical to the reference's."""
+    r = Scene(ref_lib, cfg, size)
+    o = Scene(oracle_lib, cfg, size)
+    eq = lambda x, y: np.array_equal(x, y, equal_nan=True)
+    try:
+        for s in range(200):
+            if s % 10 == 5:
+                assert r.edit(s // 10, 7) == o.edit(s // 10, 7)
+            r.step(1 / 60)
+            o.step(1 / 60)
+            assert eq(o.bodies(), r.bodies()), "bodies, step %d" % s
+            assert eq(o.arbiters(), r.arbiters()), "arbiters, step %d" % s
+            assert eq(o.constraints(), r.constraints()), "joints, step %d" % s
+        assert eq(o.public(), r.public())
+    finally:
+        r.free()
+        o.free()
+
+
 @pytest.mark.parametrize("which", ["ref", "oracle"])
 def test_time_stepping_known_answer(request, which):
     lib = request.getfixturevalue(which + "_lib")
