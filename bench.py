@@ -441,7 +441,10 @@ def _rollout_fd(lib, targets, n_params=64, seed=11):
     a parameter of world i moves: each difference steps that world alone
     (cpGpuBatchStep on a one-world batch, bit-identical to its steps in the
     full batch).  Two step sizes screen out parameters where the loss is not
-    smooth (a contact starting inside the step)."""
+    smooth (a contact starting inside the step).  Each difference is formed
+    from the final positions, L(+h) - L(-h) = sum (p+ - p-)(p+ + p- - 2t),
+    so the rounding of the ~1e5 loss itself does not enter, at three step
+    sizes whose spread bounds the differences' own error."""
     from chipmunk2d_gb300 import cpVect
     rng = np.random.default_rng(seed)
     kinds = ["v"] * 24 + ["w"] * 10 + ["m"] * 10 + ["e"] * 10 + ["u"] * 10
@@ -451,7 +454,7 @@ def _rollout_fd(lib, targets, n_params=64, seed=11):
         idx = int(rng.integers(ROLLOUT_SIZE + (1 if k in "eu" else 0)))
         params.append((k, w, idx, int(rng.integers(2))))
 
-    def world_loss(p, h):
+    def world_final(p, h):
         k, w, idx, comp = p
         (sc,) = _rollout_scenes(lib, [w])
         if k in "vwm":
@@ -475,18 +478,20 @@ def _rollout_fd(lib, targets, n_params=64, seed=11):
         p_ = sc.bodies()[:, 0:2]
         lib.cpGpuBatchFree(b)
         sc.free()
-        t = targets[w * ROLLOUT_SIZE:(w + 1) * ROLLOUT_SIZE]
-        return float(np.sum((p_ - t) ** 2))
+        return p_
 
     out = []
     for p in params:
-        fd, lw = [], 0.0
-        for h in (1e-6, 1e-7):
-            lp, lm = world_loss(p, h), world_loss(p, -h)
-            fd.append((lp - lm) / (2 * h))
-            lw = max(lw, abs(lp), abs(lm))
-        out.append((p, fd[0], fd[1], lw))
+        t = targets[p[1] * ROLLOUT_SIZE:(p[1] + 1) * ROLLOUT_SIZE]
+        fd = []
+        for h in ROLLOUT_FD_STEPS:
+            pp, pm = world_final(p, h), world_final(p, -h)
+            fd.append(float(np.sum((pp - pm) * (pp + pm - 2.0 * t))) / (2 * h))
+        out.append((p, fd))
     return out
+
+
+ROLLOUT_FD_STEPS = (1e-5, 1e-6, 1e-7)
 
 
 def run_rollout(args, emit=True, sharded=True):
@@ -600,21 +605,25 @@ def run_rollout(args, emit=True, sharded=True):
     deterministic = all(np.array_equal(runs[0][2][k], runs[1][2][k]) for k in g)
 
     fd_rows = _rollout_fd(lib, targets) if world_size == 1 else []
-    # u = |fd(1e-6) - fd(1e-7)| bounds the differences' own error.  Resolved:
-    # u <= 1e-6 |fd|; kinked: u > 1e-2 |fd| (a contact event within the step).
-    resolved, kinked, within = [], 0, 0
-    for (k, w, idx, comp), f6, f7, lw in fd_rows:
+    # u = the spread of the differences at the three step sizes bounds
+    # their own error.  Resolved: u <= 1e-6 |fd|; kinked: the two smaller
+    # sizes differ by more than 1e-2 |fd| (a contact event within the step).
+    resolved, kinked, within, outside = [], 0, 0, []
+    for (k, w, idx, comp), (f5, f6, f7) in fd_rows:
         b0 = (w - lo) * ROLLOUT_SIZE + idx
         s0 = (w - lo) * (ROLLOUT_SIZE + 1) + idx
         adj = {"v": lambda: g["v0"][2 * b0 + comp], "w": lambda: g["w0"][b0], "m": lambda: g["m"][b0],
                "e": lambda: g["e"][s0], "u": lambda: g["u"][s0]}[k]()
-        u = abs(f6 - f7)
-        if u > 1e-2 * abs(f6):
+        if abs(f6 - f7) > 1e-2 * abs(f6):
             kinked += 1
             continue
+        u = max(abs(f5 - f6), abs(f6 - f7), abs(f5 - f7))
         if abs(adj - f6) <= max(1e-6 * abs(f6), u):
             within += 1
-        if u <= 1e-6 * abs(f6):
+        else:
+            outside.append({"param": "%s world %d index %d comp %d" % (k, w, idx, comp), "adjoint": float(adj),
+                            "fd": [f5, f6, f7], "rel_err": abs(adj - f6) / max(abs(f6), 1e-300)})
+        if f6 != 0.0 and u <= 1e-6 * abs(f6):
             resolved.append(abs(adj - f6) / abs(f6))
 
     # CPU restatement (the oracle): the plain forward, one thread on a
@@ -651,12 +660,14 @@ def run_rollout(args, emit=True, sharded=True):
         "gradients_deterministic": bool(deterministic),
         "fd_check": {"params": len(fd_rows), "kinked": kinked,
                      "within_fd_uncertainty": within,
+                     "outside": outside,
                      "resolved": len(resolved),
                      "resolved_max_rel_err": max(resolved) if resolved else None,
                      "resolved_median_rel_err": float(np.median(resolved)) if resolved else None,
-                     "against": ("central differences of the GPU forward at h=1e-6 (error bound u = their distance "
-                                 "from h=1e-7), one world per difference; resolved: u <= 1e-6 |fd|; kinked: "
-                                 "u > 1e-2 |fd|; within: |adjoint - fd| <= max(1e-6 |fd|, u)")},
+                     "against": ("central differences of the GPU forward at h = 1e-5, 1e-6, 1e-7, formed from the "
+                                 "final positions (sum (p+ - p-)(p+ + p- - 2t)), one world per difference; u = their "
+                                 "spread; resolved: u <= 1e-6 |fd|; kinked: fd(1e-6), fd(1e-7) differ by > 1e-2; "
+                                 "within: |adjoint - fd(1e-6)| <= max(1e-6 |fd|, u)")},
         "e2e": {"value": ROLLOUT_STEPS / total, "unit": "steps/s",
                 "h2d_bytes_per_step": 72 * nd / ROLLOUT_STEPS,
                 "d2h_bytes_per_step": (16 * nd + 8 * nd * 2 + 8 * ns * 2 + 18 * 8 * nd) / ROLLOUT_STEPS,

@@ -68,7 +68,8 @@ class Param:
                 "e": g["e"][s], "u": g["u"][s]}[self.kind]
 
 
-def gpu_loss(lib, seeds, steps, t, param=None, h=0.0):
+def gpu_final(lib, seeds, steps, param=None, h=0.0):
+    """Final body records of the GPU forward with one parameter moved by h."""
     scenes = make(lib, seeds)
     if param is not None:
         param.apply(lib, scenes, h)
@@ -76,11 +77,51 @@ def gpu_loss(lib, seeds, steps, t, param=None, h=0.0):
     for sc in scenes:
         lib.cpGpuBatchAddSpace(batch, sc.space)
     assert lib.cpGpuBatchStep(batch, DT, steps, 0) == 0
-    L = loss(positions(scenes), t)
+    b = np.concatenate([sc.bodies() for sc in scenes])
     lib.cpGpuBatchFree(batch)
     for sc in scenes:
         sc.free()
-    return L
+    return b
+
+
+def gpu_loss(lib, seeds, steps, t, param=None, h=0.0):
+    return loss(gpu_final(lib, seeds, steps, param, h)[:, 0:2], t)
+
+
+# Central differences of L = sum |p - t|^2 formed from the state itself:
+# L(+h) - L(-h) = sum (p+ - p-) (p+ + p- - 2t), so the rounding of a loss of
+# ~1e5 (one unit in the last place is ~3e-11, i.e. ~1e-5 absolute in a
+# difference at h = 1e-6) does not enter.  Three step sizes bound the
+# differences' own error by their spread u (two sizes can agree by chance).
+FD_STEPS = (1e-5, 1e-6, 1e-7)
+
+
+def central_difference(final_of, t, extra=None):
+    """final_of(h) -> final records.  Returns the central differences at
+    FD_STEPS of sum |p - t|^2, plus extra(plus, minus), the difference of
+    any further loss terms."""
+    out = []
+    for h in FD_STEPS:
+        bp, bm = final_of(h), final_of(-h)
+        pp, pm = bp[:, 0:2], bm[:, 0:2]
+        dl = float(np.sum((pp - pm) * (pp + pm - 2.0 * t)))
+        if extra is not None:
+            dl += extra(bp, bm)
+        out.append(dl / (2 * h))
+    return out
+
+
+def fd_verdict(adj, fds):
+    """(kink, resolved, ok, u): a contact event inside the step when the two
+    smaller sizes disagree by more than 1e-2; otherwise the adjoint must lie
+    within max(1e-6 |fd|, u) of the h = 1e-6 difference, u being the spread
+    of the three; 'resolved' when u <= 1e-6 |fd|."""
+    f5, f6, f7 = fds
+    kink = abs(f6 - f7) > 1e-2 * abs(f6)
+    u = max(abs(f5 - f6), abs(f6 - f7), abs(f5 - f7))
+    resolved = (not kink) and f6 != 0.0 and u <= 1e-6 * abs(f6)
+    ok = kink or abs(adj - f6) <= max(1e-6 * abs(f6), u)
+    return kink, resolved, ok, u
 
 
 def oracle_loss(lib, seeds, steps, t, param=None, h=0.0):
@@ -197,58 +238,77 @@ STEPS = 150
 
 
 def test_gradients_match_gpu_finite_differences(gpu_lib):
-    """Central differences at h = 1e-6 and 1e-7: their distance u bounds
-    the differences' own error.  Where u > 1e-2 |fd| a contact event lies
+    """Central differences at three step sizes (FD_STEPS, fd_verdict): where
+    the two smaller ones disagree by more than 1e-2 a contact event lies
     within the step and the loss is not smooth there (skipped).  Elsewhere
-    the adjoint must agree within max(1e-6 |fd|, u), and where the
-    differences are resolved to 1e-6 (u <= 1e-6 |fd|) to 1e-6 relative."""
+    the adjoint must agree within max(1e-6 |fd|, u), u the differences'
+    spread, and to 1e-6 relative where they are resolved to 1e-6."""
     seeds = [4000 + i for i in range(WORLDS)]
     t = targets(WORLDS * SIZE)
     g, L0 = rollout_grads(gpu_lib, seeds, STEPS, 16, t)
     assert gpu_loss(gpu_lib, seeds, STEPS, t) == L0
-    rows = []
-    for p in sample_params():
-        fd = []
-        for h in (1e-6, 1e-7):
-            fd.append((gpu_loss(gpu_lib, seeds, STEPS, t, p, h) - gpu_loss(gpu_lib, seeds, STEPS, t, p, -h)) / (2 * h))
-        rows.append((p, p.grad(g), fd[0], fd[1]))
     smooth, resolved, bad = 0, 0, []
-    for p, adj, f6, f7 in rows:
-        u = abs(f6 - f7)
-        kink = u > 1e-2 * abs(f6)
-        err = abs(adj - f6) / max(abs(f6), 1e-300)
-        print("%s w%d i%d c%d adjoint %+.10e fd %+.10e %+.10e rel %.2e%s" % (
-            p.kind, p.world, p.index, p.comp, adj, f6, f7, err, "  (contact event)" if kink else ""))
-        if kink:
-            continue
-        smooth += 1
-        if abs(adj - f6) > max(1e-6 * abs(f6), u):
-            bad.append((p.kind, p.world, p.index, p.comp, adj, f6, f7))
-        if u <= 1e-6 * abs(f6) and f6 != 0.0:
-            resolved += 1
-            if err > 1e-6:
-                bad.append(("resolved", p.kind, p.world, p.index, p.comp, adj, f6, f7))
-    assert smooth >= 0.75 * len(rows), smooth
+    params = sample_params()
+    for p in params:
+        adj = p.grad(g)
+        fds = central_difference(lambda h: gpu_final(gpu_lib, seeds, STEPS, p, h), t)
+        kink, res, ok, u = fd_verdict(adj, fds)
+        err = abs(adj - fds[1]) / max(abs(fds[1]), 1e-300)
+        print("%s w%d i%d c%d adjoint %+.10e fd %+.10e %+.10e %+.10e rel %.2e u %.1e%s" % (
+            p.kind, p.world, p.index, p.comp, adj, *fds, err, u / max(abs(fds[1]), 1e-300), "  (contact event)" if kink else ""))
+        smooth += not kink
+        resolved += res
+        if not ok:
+            bad.append((p.kind, p.world, p.index, p.comp, adj, fds))
+    assert smooth >= 0.75 * len(params), smooth
     assert resolved >= 5, resolved
     assert not bad, bad
 
 
 def test_gradients_match_oracle_finite_differences(gpu_lib, oracle_lib):
     """The CPU reference's forward (the oracle) gives the same finite
-    differences: the GPU forward agrees with it to ~1e-12 per step."""
-    seeds = [4000 + i for i in range(2)]
+    differences as the GPU's: the GPU adjoint agrees with central
+    differences of the oracle under the same rule (fd_verdict: 1e-6
+    relative where the differences are resolved to 1e-6), on 18 parameters
+    of 3 worlds over 60 steps."""
     global WORLDS
     saved = WORLDS
-    WORLDS = 2
+    WORLDS = 3
+    steps = 60
     try:
+        seeds = [4000 + i for i in range(WORLDS)]
         t = targets(WORLDS * SIZE)
-        g, L0 = rollout_grads(gpu_lib, seeds, 40, 16, t)
-        params = [Param("v", 0, 3, 0), Param("v", 1, 9, 1), Param("w", 0, 12), Param("m", 1, 2), Param("u", 0, 0), Param("e", 1, 5)]
+        g, L0 = rollout_grads(gpu_lib, seeds, steps, 16, t)
+        rng = np.random.default_rng(29)
+        params = [Param(k, int(rng.integers(WORLDS)), int(rng.integers(SIZE + (k in "eu"))), int(rng.integers(2)))
+                  for k in ["v"] * 6 + ["w"] * 3 + ["m"] * 3 + ["u"] * 3 + ["e"] * 3]
+
+        def final_of(p):
+            def run(h):
+                scenes = make(oracle_lib, seeds)
+                p.apply(oracle_lib, scenes, h)
+                for sc in scenes:
+                    sc.step(DT, steps)
+                b = np.concatenate([sc.bodies() for sc in scenes])
+                for sc in scenes:
+                    sc.free()
+                return b
+            return run
+
+        smooth, resolved, bad = 0, 0, []
         for p in params:
-            h = 1e-5
-            fd = (oracle_loss(oracle_lib, seeds, 40, t, p, h) - oracle_loss(oracle_lib, seeds, 40, t, p, -h)) / (2 * h)
             adj = p.grad(g)
-            assert abs(adj - fd) <= 1e-4 * max(abs(fd), 1.0), (p.kind, adj, fd)
+            fds = central_difference(final_of(p), t)
+            kink, res, ok, u = fd_verdict(adj, fds)
+            print("%s w%d i%d c%d adjoint %+.10e oracle fd %+.10e %+.10e %+.10e u %.1e%s" % (
+                p.kind, p.world, p.index, p.comp, adj, *fds, u / max(abs(fds[1]), 1e-300), "  (contact event)" if kink else ""))
+            smooth += not kink
+            resolved += res
+            if not ok:
+                bad.append((p.kind, p.world, p.index, p.comp, adj, fds))
+        assert smooth >= 0.7 * len(params), smooth
+        assert resolved >= 4, resolved
+        assert not bad, bad
     finally:
         WORLDS = saved
 
@@ -319,24 +379,39 @@ def test_full_gradients_match_gpu_finite_differences(gpu_lib):
     rng = np.random.default_rng(23)
     params = [(k, int(rng.integers(WORLDS)), int(rng.integers(SIZE)), int(rng.integers(2)))
               for k in ["p"] * 10 + ["a"] * 8 + ["v"] * 6 + ["w"] * 6]
+
+    def extra(bp, bm):
+        # the velocity and angle terms of L, in the same difference form
+        vp, vm, ap, am = bp[:, 2:4], bm[:, 2:4], bp[:, 4], bm[:, 4]
+        return float(CV * np.sum((vp - vm) * (vp + vm)) + CA * np.sum((ap - am) * (ap + am)))
+
+    def final_of(p):
+        def run(h):
+            scenes = make(gpu_lib, seeds)
+            apply_pose(gpu_lib, scenes, *p, h)
+            batch = gpu_lib.cpGpuBatchNew()
+            for sc in scenes:
+                gpu_lib.cpGpuBatchAddSpace(batch, sc.space)
+            assert gpu_lib.cpGpuBatchStep(batch, DT, STEPS, 0) == 0
+            b = np.concatenate([sc.bodies() for sc in scenes])
+            gpu_lib.cpGpuBatchFree(batch)
+            for sc in scenes:
+                sc.free()
+            return b
+        return run
+
     smooth, resolved, bad = 0, 0, []
     for kind, w, i, c in params:
-        fd = [(gpu_full_loss(gpu_lib, seeds, STEPS, t, (kind, w, i, c), h) -
-               gpu_full_loss(gpu_lib, seeds, STEPS, t, (kind, w, i, c), -h)) / (2 * h) for h in (1e-6, 1e-7)]
         k = w * SIZE + i
         adj = g[kind][2 * k + c] if kind in ("p", "v") else g[kind][k]
-        u = abs(fd[0] - fd[1])
-        kink = u > 1e-2 * abs(fd[0])
-        print("%s w%d i%d c%d adjoint %+.10e fd %+.10e %+.10e%s" % (kind, w, i, c, adj, fd[0], fd[1], "  (contact event)" if kink else ""))
-        if kink:
-            continue
-        smooth += 1
-        if abs(adj - fd[0]) > max(1e-6 * abs(fd[0]), u):
-            bad.append((kind, w, i, c, adj, fd[0], fd[1]))
-        if u <= 1e-6 * abs(fd[0]) and fd[0] != 0.0:
-            resolved += 1
-            if abs(adj - fd[0]) > 1e-6 * abs(fd[0]):
-                bad.append(("resolved", kind, w, i, c, adj, fd[0], fd[1]))
+        fds = central_difference(final_of((kind, w, i, c)), t, extra)
+        kink, res, ok, u = fd_verdict(adj, fds)
+        print("%s w%d i%d c%d adjoint %+.10e fd %+.10e %+.10e %+.10e u %.1e%s" % (
+            kind, w, i, c, adj, *fds, u / max(abs(fds[1]), 1e-300), "  (contact event)" if kink else ""))
+        smooth += not kink
+        resolved += res
+        if not ok:
+            bad.append((kind, w, i, c, adj, fds))
     assert smooth >= 0.7 * len(params), smooth
     assert resolved >= 4, resolved
     assert not bad, bad
