@@ -191,6 +191,8 @@ _GPU_API = {
     "cpGpuDebugSetSolveShape": (None, [I, I]),
     "cpGpuDebugSetSolveLayout": (None, [I]),
     "cpGpuDebugSetFlowSolve": (None, [I]),
+    "cpGpuDebugSetFlowWaitLimit": (None, [I, I]),
+    "cpGpuDebugSetCapacities": (None, [I, I, I, I]),
     "cpGpuDebugSetWarmStartGather": (None, [I]),
     "cpGpuDebugSetParallelMarking": (None, [I]),
     "cpGpuGetPhaseTimes": (I, [P, P, I]),

@@ -280,6 +280,21 @@ void cpGpuDebugSetSolveLayout(int policy) { g_solve_layout = (policy >= 0 && pol
  * off unless asked for */
 static int g_flow_solve = 0;
 void cpGpuDebugSetFlowSolve(int on) { g_flow_solve = on ? 1 : 0; }
+static int g_flow_spin = 0, g_flow_withhold = 0;
+void cpGpuDebugSetFlowWaitLimit(int polls, int withhold)
+{
+	g_flow_spin = polls > 0 ? polls : 0;
+	g_flow_withhold = withhold ? 1 : 0;
+}
+/* capacity overrides for tests of the overflow latches (0: the defaults) */
+static int g_cap_pairs_per_shape = 0, g_cap_pairs_extra = -1, g_cap_arbs = 0, g_cap_nodes = 0;
+void cpGpuDebugSetCapacities(int pairsPerShape, int pairsExtra, int arbiterSlots, int nodes)
+{
+	g_cap_pairs_per_shape = pairsPerShape > 0 ? pairsPerShape : 0;
+	g_cap_pairs_extra = pairsExtra >= 0 ? pairsExtra : -1;
+	g_cap_arbs = arbiterSlots > 0 ? arbiterSlots : 0;
+	g_cap_nodes = nodes > 0 ? nodes : 0;
+}
 /* measured neutral on 20,000 settled circles (the solve lost 26 us of
  * barrier-bound levels, the velocity kernel gained 23 us of gathers), so
  * off unless asked for */
@@ -722,6 +737,9 @@ static DevSet *devset_build(cpSpace **spaces, int nspaces, DevSet *from)
 		int churn = (sp->nshapes != ndynShapes + nstatShapes) || from;
 		W->nodeOff = (int)NN; W->nodeCap = 2*sp->nshapes + 4;
 		W->pairOff = (int)NP; W->pairCap = 16*sp->nshapes + 256;
+		if(g_cap_pairs_per_shape || g_cap_pairs_extra >= 0)
+			W->pairCap = (g_cap_pairs_per_shape ? g_cap_pairs_per_shape : 16)*sp->nshapes + (g_cap_pairs_extra >= 0 ? g_cap_pairs_extra : 256);
+		if(g_cap_nodes && g_cap_nodes < W->nodeCap) W->nodeCap = g_cap_nodes;
 		W->dbinOff = (int)NDB; W->dbinCap = bins_for(churn ? sp->nshapes : ndynShapes);
 		W->sbinOff = (int)NSB; W->sbinCap = bins_for(churn ? sp->nshapes : nstatShapes);
 		if(from){
@@ -751,6 +769,7 @@ static DevSet *devset_build(cpSpace **spaces, int nspaces, DevSet *from)
 	d->totalCands = (int)NCD; d->totalUnits = (int)NU; d->totalOps = (int)NO; d->totalParts = (int)NPT;
 	long long arbCap = 1024;
 	while(arbCap < 8*NS + 1024) arbCap *= 2;
+	if(g_cap_arbs){ arbCap = 1; while(arbCap < g_cap_arbs) arbCap *= 2; }
 	if(from && arbCap < from->d.arbCap) arbCap = from->d.arbCap;
 	d->arbCap = (int)arbCap;
 
@@ -1019,6 +1038,8 @@ static int devset_step(DevSet *ds, const double *dts, cpSpace **only)
 	d->hostSolveStage = g_solve_stage;
 	d->solveLayout = g_solve_layout;
 	d->flowSolve = g_flow_solve;
+	d->flowSpin = g_flow_spin;
+	d->flowWithhold = g_flow_withhold;
 	d->warmGather = g_warm_gather;
 	d->parMark = g_par_mark >= 0 ? g_par_mark : (d->hostNdyn >= CPG_PAR_MARK_MIN);
 	/* launch shapes of many-world sets: the tuner's candidates on the steps

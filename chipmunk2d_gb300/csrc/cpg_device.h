@@ -318,6 +318,8 @@ typedef struct cpgSet {
 	int *flowDone;                /* [totalUnits] passes the unit has finished */
 	int *flowPos;                 /* [64*totalBodies] schedule position of the unit of colour c on body b */
 	int flowSolve;                /* 1: coloured solve by dataflow (host value) */
+	int flowSpin;                 /* polls before a dataflow wait gives up; 0: the default (host value) */
+	int flowWithhold;             /* test of the wait limit: completions are not published (host value) */
 	int warmGather;               /* 1: coloured mode applies the cached impulses per body in k_integrate_vel (host value) */
 	int parMark;                  /* 1: a single world's tree is marked by k_tree_mark's parallel phases (host value) */
 	int *markScratch;             /* single-world sets: the parallel marking's scratch (mark_scratch in cpg_kernels.cu) */

@@ -86,6 +86,9 @@ __global__ void k_apply_ops(cpgSet s)
 	if(W.nops == 0) return;
 	TreeCtx c = make_tree_ctx(&s, w);
 	for(int i = 0; i < W.nops; i++){
+		/* a latched error (a pool ran out mid-insertion) stops the replay,
+		 * as it stops the tree step: the tree may hold a half-made leaf */
+		if(c.T->error) break;
 		cpgOp op = s.ops[W.opOff + i];
 		if(op.kind == CPG_OP_REMOVE) tree_remove(c, op);
 		else tree_insert(c, op);
@@ -2282,7 +2285,7 @@ __device__ __forceinline__ void st_release_gpu(int *p, int v)
 
 /* Whole warp: wait until the predecessors of this lane's unit k (or none,
  * k < 0) have finished the passes this one needs. */
-__device__ __forceinline__ void flow_wait(const int *pred, const int *done, int *abortWord, int *err, int k, int pass)
+__device__ __forceinline__ void flow_wait(const int *pred, const int *done, int *abortWord, int *err, int k, int pass, int limit)
 {
 	int f0 = -1, t0 = 0, f1 = -1, t1 = 0;
 	if(k >= 0){
@@ -2296,7 +2299,7 @@ __device__ __forceinline__ void flow_wait(const int *pred, const int *done, int 
 		if(__all_sync(0xffffffffu, ready)) return;
 		if((it & 31) == 31){
 			if(__any_sync(0xffffffffu, ld_acquire_gpu(abortWord) != 0)) return;
-			if(it >= CPG_FLOW_SPIN){
+			if(it >= limit){
 				if((threadIdx.x & 31) == 0){ atomicOr(err, CPG_ERR_FLOW); atomicExch(abortWord, 1); }
 				return;
 			}
@@ -2335,6 +2338,10 @@ __global__ void __launch_bounds__(CPG_COOP_SOLVE_THREADS, 1) k_solve_coop(cpgSet
 	int iters = P.iterations;
 	double dt_coef = P.dt_coef, dt = P.dt;
 	bool flow = FUSED && s.flowSolve && s.colorCursor[13] == 0;
+	/* the waits' poll limit, and (a test of the limit) completions that
+	 * are never published, so that every wait with a predecessor runs out */
+	int flowLimit = s.flowSpin > 0 ? s.flowSpin : CPG_FLOW_SPIN;
+	bool publish = !s.flowWithhold;
 	/* coloured mode: k_integrate_vel has applied the cached impulses */
 	int pass0 = (FUSED && s.warmGather && s.colorCursor[13] == 0) ? 1 : 0;
 	const int *pred = s.flowPred + 2*(size_t)W.unitOff;
@@ -2366,24 +2373,24 @@ __global__ void __launch_bounds__(CPG_COOP_SOLVE_THREADS, 1) k_solve_coop(cpgSet
 					bool has = k2 < e;
 					PairRow pr;
 					if(has) pair_load(pr, rows[k2], bias);
-					if(flow) flow_wait(pred, done, abortWord, &T.error, has ? k2 : -1, pass);
+					if(flow) flow_wait(pred, done, abortWord, &T.error, has ? k2 : -1, pass, flowLimit);
 					if(has){
 						if(pr.kind == 0) pair_apply<true, FUSED>(pr, rows + k2, bodies, pass, dt_coef, bias);
 						else if(!bias) solve_row<true>(rows, k2, bodies, pass, dt_coef, dt);
 					}
-					if(flow) flow_done(done, has ? k2 : -1, pass, !bias);
+					if(flow) flow_done(done, has ? k2 : -1, pass, !bias && publish);
 				}
 			} else {
 				/* levels wider than the grid take several rounds */
 				for(int k2 = k; __any_sync(0xffffffffu, k2 < e); k2 += nq){
 					bool has = k2 < e;
 					if(has && k2 != k) quad_load(q, rows[k2], lane4);
-					if(flow) flow_wait(pred, done, abortWord, &T.error, has ? k2 : -1, pass);
+					if(flow) flow_wait(pred, done, abortWord, &T.error, has ? k2 : -1, pass, flowLimit);
 					if(has){
 						if(q.kind == 0) quad_apply<true, FUSED>(q, rows + k2, bodies, pass, dt_coef, qmask, lane4);
 						else if(lane4 == 0) solve_row<true>(rows, k2, bodies, pass, dt_coef, dt);
 					}
-					if(flow) flow_done(done, has ? k2 : -1, pass, lane4 == 0);
+					if(flow) flow_done(done, has ? k2 : -1, pass, lane4 == 0 && publish);
 				}
 			}
 			int nl = l + 1, npass = pass;

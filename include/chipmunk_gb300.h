@@ -609,6 +609,19 @@ void cpGpuDebugSetFlowSolve(int on);
  * per-body gather of the cached impulses in colour order (1) or as colour
  * levels of the sweep (0, default).  Both give the same results. */
 void cpGpuDebugSetWarmStartGather(int on);
+/* Debug, tests of the bounded waits: the coloured dataflow sweep's waits
+ * give up after `polls` polls (0: the default, 2^20) and then latch an
+ * error that cpGpuGetLastError() reports as CP_GPU_ERR_TIMEOUT; with
+ * `withhold` set the sweep publishes no completions, so every wait that
+ * has a predecessor runs out (the step's results are then not defined). */
+void cpGpuDebugSetFlowWaitLimit(int polls, int withhold);
+/* Debug, tests of the overflow latches: capacities of the sets built from
+ * now on -- candidate pairs per world (pairsPerShape * shapes +
+ * pairsExtra), arbiter table slots (rounded up to a power of two) and tree
+ * nodes per world; 0 (or -1 for pairsExtra) keeps a default.  A table that
+ * runs out latches an error that cpGpuGetLastError() reports as
+ * CP_GPU_ERR_OVERFLOW; nothing is written past it. */
+void cpGpuDebugSetCapacities(int pairsPerShape, int pairsExtra, int arbiterSlots, int nodes);
 /* Debug: how a single space's exact-order tree is marked: by parallel
  * phases (1), by one device thread (0), or automatically (-1, default:
  * parallel from 1024 dynamic shapes up).  All give the same candidates,
