@@ -38,6 +38,41 @@ import numpy as np
 REPO = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, REPO)
 
+# the configured run length of each single-space workload (steps)
+RUN_STEPS = {"circles": 600, "pyramid": 1000, "mixed": 600}
+
+
+def window_start(workload, warmup, steps):
+    """First timed step: a K-step sample of a longer configured run is taken
+    from its middle (untimed lead-in steps, the W warm-up steps among them),
+    so that it costs what the run costs on average rather than its free-fall
+    start; a run of K >= the configured length starts after the warm-up."""
+    total = RUN_STEPS.get(workload, steps)
+    return warmup if steps >= total else max(warmup, (total - steps)//2)
+
+
+def host_cpu():
+    """The host CPU model (lscpu, else /proc/cpuinfo) and its usable threads."""
+    model = None
+    try:
+        out = subprocess.run(["lscpu"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True, timeout=10).stdout
+        for ln in out.splitlines():
+            if ln.startswith("Model name:"):
+                model = ln.split(":", 1)[1].strip()
+                break
+    except (OSError, subprocess.SubprocessError):
+        pass
+    if model is None:
+        try:
+            for ln in open("/proc/cpuinfo"):
+                if ln.lower().startswith(("model name", "cpu model")):
+                    model = ln.split(":", 1)[1].strip()
+                    break
+        except OSError:
+            pass
+    return {"model": model, "threads": cpu_threads()}
+
+
 WORKLOADS = {
     # name: (scene config, size, dt, description)
     "circles": (2, 20000, 1 / 60, "20000 circles r~U[0.5,2] in a 1000x2000 box, 10 it, dt 1/60, seed 1"),
@@ -132,28 +167,36 @@ def oracle_lib():
     return bind(so)
 
 
-def cpu_sample(workload, budget_s=15.0, warm=5, hasty=False):
-    """Times the CPU restatement on the workload: `warm` untimed steps, then
-    steps until about budget_s seconds of CPU time have been spent.  With
-    `hasty` the solver runs on two threads as cpHastySpace's does."""
+def cpu_sample(workload, budget_s=15.0, warm=5, hasty_s=0.0):
+    """Times the CPU restatement on the workload: `warm` untimed lead-in
+    steps, then steps on one thread until about budget_s seconds have been
+    spent, then (hasty_s > 0) steps with the solver on two threads as
+    cpHastySpace's for about hasty_s seconds.  Returns ((value, steps,
+    seconds) one thread, (value, steps, seconds) two threads or None, bodies)."""
     from chipmunk2d_gb300 import Scene
     cfg, size, dt, _ = WORKLOADS[workload]
     lib = oracle_lib()
     sc = Scene(lib, cfg, size)
-    if hasty:
-        lib.cpx_space_set_hasty(sc.space, 2)
     sc.step(dt, warm)
-    steps = 0
-    t0 = time.perf_counter()
-    while True:
-        sc.step(dt, 1)
-        steps += 1
-        el = time.perf_counter() - t0
-        if el >= budget_s or steps >= 2000:
-            break
     n = sc.nbodies
+
+    def timed(budget):
+        steps = 0
+        t0 = time.perf_counter()
+        while True:
+            sc.step(dt, 1)
+            steps += 1
+            el = time.perf_counter() - t0
+            if el >= budget or steps >= 2000:
+                return n * steps / el, steps, el
+
+    one = timed(budget_s)
+    two = None
+    if hasty_s > 0:
+        lib.cpx_space_set_hasty(sc.space, 2)
+        two = timed(hasty_s)
     sc.free()
-    return n * steps / el, steps, el, n
+    return one, two, n
 
 
 def cpu_threads():
@@ -228,7 +271,10 @@ def run_reference(args):
     # the reference's threaded space (cpHastySpace) solves on at most two
     # threads; its restatement in the oracle does the same
     threads = lib.cpx_space_set_hasty(sc.space, 2)
-    sc.step(dt, args.warmup)
+    # the same timed window as the GPU arm: an untimed lead-in to the
+    # middle of the configured run
+    start = window_start(workload, args.warmup, args.steps)
+    sc.step(dt, start)
     # each timed step is a bounded sample: the whole run stays within minutes
     per_step = []
     t_all = time.perf_counter()
@@ -246,10 +292,12 @@ def run_reference(args):
         "impl": "reference", "metric": "body-steps/s", "value": value, "unit": "body-steps/s",
         "n_gpus": args.gpus, "steps": k, "warmup": args.warmup, "ms_per_step": 1000 * secs / k,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-        "data": "synthetic", "config": {"workload": workload, "description": desc, "bodies": n},
+        "data": "synthetic", "config": {"workload": workload, "description": desc, "bodies": n,
+                                        "timed_window": [start, start + k], "lead_in_untimed": start},
+        "host_cpu": host_cpu(),
         "cpu_baseline": {"value": value, "unit": "body-steps/s", "cores": threads, "kind": "port",
-                         "sample": "%d steps of the %s workload after %d warm-up steps, solver on %d threads as cpHastySpace's"
-                                   % (k, workload, args.warmup, threads)},
+                         "sample": "steps %d-%d of the %s workload (untimed lead-in before), solver on %d threads as cpHastySpace's"
+                                   % (start, start + k, workload, threads)},
         "e2e": {"value": value, "unit": "body-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -693,10 +741,13 @@ def run_rollout(args, emit=True, sharded=True):
 PHASES = ["integrate+cache", "broadphase", "narrowphase", "arbiters", "schedule", "prestep+velocity", "solve"]
 
 
-def mode_sample(lib, workload, steps, warmup, mode=0, phases=False):
+def mode_sample(lib, workload, steps, warmup, mode=0, phases=False, e2e=False):
     """Wall-timed steps of one workload in one solver mode (0: the exact
     reference-order mode, the drop-in's default; 1: coloured), closed by a
-    device sync, for the JSON line's extra records."""
+    device sync, for the JSON line's extra records; `warmup` untimed steps
+    lead in.  With e2e, as many further steps are timed through the public
+    API as a program uses it: cpSpaceStep, then every body's position,
+    velocity and angle (cpBodyGet*)."""
     import torch
     from chipmunk2d_gb300 import Scene
     cfg, size, dt, desc = WORKLOADS[workload]
@@ -715,8 +766,18 @@ def mode_sample(lib, workload, steps, warmup, mode=0, phases=False):
     err = lib.cpGpuGetLastError()
     rec = {"workload": workload, "solver": "colored" if mode else "ordered", "bodies": sc.nbodies,
            "shapes": sc.nshapes, "constraints": sc.nconstraints, "steps": steps, "warmup": warmup,
+           "timed_window": [warmup, warmup + steps],
            "body_steps_per_s": sc.nbodies * steps / secs, "ms_per_step": 1000 * secs / steps,
            "description": desc}
+    if e2e:
+        out = np.zeros(8 * sc.nbodies)
+        t0 = time.perf_counter()
+        for _ in range(steps):
+            lib.cpSpaceStep(sc.space, dt)
+            lib.cpx_scene_dump_public(sc.h, out.ctypes.data)
+        es = time.perf_counter() - t0
+        rec["e2e"] = {"value": sc.nbodies * steps / es, "unit": "body-steps/s", "timed_window": [warmup + steps, warmup + 2 * steps],
+                      "path": "cpSpaceStep + cpBodyGetPosition/Velocity/Angle for every body (ctypes)"}
     if err:
         rec["error"] = lib.cpGpuGetLastErrorString().decode()
     if phases:
@@ -732,10 +793,28 @@ def mode_sample(lib, workload, steps, warmup, mode=0, phases=False):
     return rec
 
 
-def parity_mode_sample(lib, workload, steps, warmup):
+def parity_mode_sample(lib, workload, steps, warmup, e2e=False):
     """The exact reference-order mode, for the `ordered_mode` record."""
-    rec = mode_sample(lib, workload, steps, warmup, mode=0, phases=True)
-    return {k: rec[k] for k in ("workload", "bodies", "steps", "body_steps_per_s", "ms_per_step", "phase_ms")}
+    rec = mode_sample(lib, workload, steps, warmup, mode=0, phases=True, e2e=e2e)
+    return {k: rec[k] for k in ("workload", "bodies", "steps", "timed_window", "body_steps_per_s", "ms_per_step",
+                                "phase_ms", "e2e") if k in rec}
+
+
+def solver_quality(lib, sc, dt, iters):
+    """cpGpuSolverQuality from the space's current state, both solver modes:
+    per iteration the RMS normal and friction residuals and the largest
+    penetration."""
+    out = {}
+    for mode, name in ((0, "ordered"), (1, "colored")):
+        q = np.zeros(3 * iters)
+        if lib.cpGpuSolverQuality(sc.space, mode, dt, iters, q.ctypes.data) != 0:
+            out[name] = {"error": lib.cpGpuGetLastErrorString().decode()}
+            continue
+        q = q.reshape(iters, 3)
+        out[name] = {"normal_residual_rms": [float(x) for x in q[:, 0]],
+                     "friction_residual_rms": [float(x) for x in q[:, 1]],
+                     "max_penetration": [float(x) for x in q[:, 2]]}
+    return out
 
 
 def run_ours(args):
@@ -764,11 +843,14 @@ def run_ours(args):
         return sc
 
     # ---- device-timed run (state resident in HBM) ----
+    start = window_start(args.workload, args.warmup, args.steps)
     sc = make()
     n = sc.nbodies
-    for _ in range(args.warmup):
+    for _ in range(start):
         lib.cpSpaceStep(sc.space, dt)
     torch.cuda.synchronize()
+    arbs0 = sc.arbiters()
+    contacts0 = int(arbs0[:, 2].sum()) if len(arbs0) else 0
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
     lib.cpGpuGetLaunchCount(1)
     clocks = ClockSampler(local_rank)
@@ -804,6 +886,8 @@ def run_ours(args):
         raise RuntimeError("GPU step failed: %s" % lib.cpGpuGetLastErrorString().decode())
     arbs = sc.arbiters()
     contacts = int(arbs[:, 2].sum()) if len(arbs) else 0
+    # solver quality at the end of the window, both modes from this state
+    quality = solver_quality(lib, sc, dt, 15 if cfg == 3 else 10) if rank == 0 and args.extras else None
 
     # ---- per-phase timing pass (phase events, separate run) ----
     lib.cpGpuSetTiming(1)
@@ -821,19 +905,24 @@ def run_ours(args):
     sweep_levels = int(st[6])
     sc.free()
 
-    # ---- end-to-end run through the public C API ----
+    # ---- end-to-end run through the public C API, same window ----
     sc = make()
-    for _ in range(args.warmup):
+    for _ in range(start):
         lib.cpSpaceStep(sc.space, dt)
     out = np.zeros(8 * n)
     sc.public()
     torch.cuda.synchronize()
-    t0 = time.perf_counter()
     e2e_steps = min(args.steps, 200)
+    e2e_s = 0.0
+    arb_per_step = []
+    stats = np.zeros(8, dtype=np.int32)
     for _ in range(e2e_steps):
+        t0 = time.perf_counter()
         lib.cpSpaceStep(sc.space, dt)
         lib.cpx_scene_dump_public(sc.h, out.ctypes.data)
-    e2e_s = time.perf_counter() - t0
+        e2e_s += time.perf_counter() - t0
+        lib.cpGpuGetStepStats(sc.space, stats.ctypes.data, 8)      # untimed: arbiters solved this step
+        arb_per_step.append(int(stats[5]))
     sc.free()
 
     value = n * args.steps * world_size / total_s
@@ -858,23 +947,30 @@ def run_ours(args):
                  for i in range(len(names))}
     peak, peak_kind = measured_peaks()
     achieved = algo / (phase[dom] / 1000.0) / 1e9 if phase[dom] > 0 else 0.0
-    traffic = None
+    # DRAM bytes of one launch of the dominant kernel, from an ncu capture
+    # of the same timed window (profiles/traffic.json records the window)
+    traffic, traffic_note = None, "no capture of this window"
     tpath = os.path.join(REPO, "profiles", "traffic.json")
     if os.path.exists(tpath):
         with open(tpath) as f:
-            traffic = json.load(f).get(args.workload, {}).get(names[dom])
+            rec = json.load(f).get(args.workload, {})
+        if rec.get("window") == [start, start + args.steps] and names[dom] in rec:
+            traffic = rec[names[dom]]
+            traffic_note = rec.get("how", "")
 
-    cpu_v, cpu_steps, cpu_s, _ = cpu_sample(args.workload, budget_s=args.cpu_seconds) if rank == 0 else (None, 0, 0, 0)
-    hv, h_steps, h_s, _ = (cpu_sample(args.workload, budget_s=min(args.cpu_seconds, 8.0), hasty=True)
-                           if rank == 0 else (None, 0, 0, 0))
+    if rank == 0:
+        (cpu_v, cpu_steps, cpu_s), (hv, h_steps, h_s), _ = cpu_sample(
+            args.workload, budget_s=args.cpu_seconds, warm=start, hasty_s=min(args.cpu_seconds, 8.0))
+    else:
+        cpu_v, cpu_steps, cpu_s, hv, h_steps, h_s = None, 0, 0, None, 0, 0
 
     extras = {}
     if args.extras and rank == 0 and args.workload == "circles":
         # the exact-order mode (bit-compatible with cpSpaceStep) on the
         # pyramid and on this workload, and the batched-world throughput
         lib.cpGpuSetStream(ctypes.c_void_p(stream.cuda_stream))
-        extras["ordered_mode"] = [parity_mode_sample(lib, "pyramid", 300, 5),
-                                  parity_mode_sample(lib, "circles", 10, 3)]
+        extras["ordered_mode"] = [parity_mode_sample(lib, "pyramid", 300, window_start("pyramid", 5, 300)),
+                                  parity_mode_sample(lib, "circles", 10, window_start("circles", 5, 10), e2e=True)]
         # mixed shapes and pivot chains at full size (40,000 bodies)
         extras["mixed"] = [mode_sample(lib, "mixed", 150, 150, mode=1, phases=True),
                            mode_sample(lib, "mixed", 3, 2, mode=0)]
@@ -896,7 +992,10 @@ def run_ours(args):
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
         "data": "synthetic",
         "config": {"workload": args.workload, "description": desc, "bodies": n, "solver": args.mode,
-                   "arbiters_final": int(len(arbs)), "contacts_final": contacts,
+                   "timed_window": [start, start + args.steps], "lead_in_untimed": start,
+                   "run_length": RUN_STEPS.get(args.workload),
+                   "contacts_window_start": contacts0, "contacts_window_end": contacts,
+                   "arbiters_per_timed_step": arb_per_step,
                    "l2": "flushed between timed steps (256 MB fill, untimed)",
                    "parallelism": "replicas" if world_size > 1 else "single"},
         "e2e": {"value": e2e_value, "unit": "body-steps/s", "h2d_bytes_per_step": 88,
@@ -904,7 +1003,7 @@ def run_ours(args):
                 "path": "cpSpaceStep + cpBodyGetPosition/Velocity/Angle for every body (ctypes)"},
         "roofline": {"bound": "hbm", "kernel": names[dom], "achieved": achieved, "peak": peak,
                      "unit": "GB/s", "frac": achieved / peak, "peak_kind": peak_kind,
-                     "traffic": traffic, "algorithmic_bytes_per_launch": algo,
+                     "traffic": traffic, "traffic_capture": traffic_note, "algorithmic_bytes_per_launch": algo,
                      "limiter": ("latency: one grid barrier, one round of L2 body loads and the dependent FP64 "
                                  "chain per colour level; rows and bodies stay L2-resident" if names[dom] == "solve"
                                  else "latency-bound gather")},
@@ -914,10 +1013,13 @@ def run_ours(args):
         "gpu_launches": int(launches),
         "clocks": clk,
         "cpu_baseline": {"value": cpu_v, "unit": "body-steps/s", "cores": 1, "kind": "port",
-                         "sample": "%d steps (%.1f s) of the %s workload after 5 warm-up steps" % (cpu_steps, cpu_s, args.workload)},
+                         "sample": "%d steps (%.1f s) of the %s workload from step %d (the timed window's start)" % (cpu_steps, cpu_s, args.workload, start)},
         "cpu_hasty": {"value": hv, "unit": "body-steps/s", "cores": 2, "kind": "port",
-                      "sample": ("cpHastySpace's two-thread solver restated in the oracle, %d steps (%.1f s) after 5 warm-up steps"
+                      "sample": ("cpHastySpace's two-thread solver restated in the oracle, %d steps (%.1f s) following those"
                                  % (h_steps, h_s))},
+        "host_cpu": host_cpu(),
+        "solver_quality": ({"state": "after step %d, both solvers from the same state" % (start + args.steps), **quality}
+                           if quality else None),
     }
     line.update(extras)
     if rank == 0:

@@ -196,6 +196,7 @@ _GPU_API = {
     "cpGpuDebugSetWarmStartGather": (None, [I]),
     "cpGpuDebugSetParallelMarking": (None, [I]),
     "cpGpuGetPhaseTimes": (I, [P, P, I]),
+    "cpGpuSolverQuality": (I, [P, I, D, I, P]),
     "cpGpuGetStepStats": (I, [P, P, I]),
     "cpGpuGetLaunchCount": (ctypes.c_longlong, [I]),
     "cpGpuSolveSchedule": (I, [P, P, I, I, P, P, P, P]),

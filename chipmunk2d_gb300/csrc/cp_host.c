@@ -146,6 +146,13 @@ struct cpConstraint {
 	cpDataPointer userData;
 	cpVect anchorA, anchorB;
 	cpFloat dist, min, max;
+	/* groove, springs, rotary joints (the ratchet's angle, a state the
+	 * step updates, lives in rec) */
+	cpVect grv_a, grv_b, grv_n;
+	cpFloat restLength, restAngle, stiffness, damping;
+	cpFloat phase, ratchet, ratio, ratio_inv, rate;
+	cpDampedSpringForceFunc springForceFunc;
+	cpDampedRotarySpringTorqueFunc springTorqueFunc;
 	int index;
 	cpgJoint rec;                          /* last downloaded device record */
 };
@@ -371,6 +378,7 @@ static size_t carve_set(cpgSet *d, char *base, int pass)
 	CARVE(cogx, double, NB); CARVE(cogy, double, NB);
 	CARVE(btype, int, NB); CARVE(bworld, int, NB); CARVE(partStart, int, NB); CARVE(partCount, int, NB);
 	CARVE(parts, int, d->totalParts); CARVE(last, int, NB);
+	CARVE(springStart, int, NB); CARVE(springCount, int, NB); CARVE(springs, int, d->totalSprings);
 	CARVE(skind, int, NS); CARVE(sbody, int, NS); CARVE(sleaf, int, NS); CARVE(sworld, int, NS);
 	CARVE(svoff, int, NS); CARVE(svcount, int, NS);
 	CARVE(sr, double, NS);
@@ -636,6 +644,11 @@ static int upload_joints(DevSet *ds, int w, int params_only)
 			j->ax = c->anchorA.x; j->ay = c->anchorA.y; j->bx = c->anchorB.x; j->by = c->anchorB.y;
 			j->maxForce = c->maxForce; j->maxBias = c->maxBias;
 			j->dist = c->dist; j->min = c->min; j->max = c->max;
+			j->gax = c->grv_a.x; j->gay = c->grv_a.y; j->gbx = c->grv_b.x; j->gby = c->grv_b.y;
+			j->gnx = c->grv_n.x; j->gny = c->grv_n.y;
+			j->restLength = (c->kind == CPG_DRSPRING) ? c->restAngle : c->restLength;
+			j->stiffness = c->stiffness; j->damping = c->damping;
+			j->phase = c->phase; j->ratchet = c->ratchet; j->ratio = c->ratio; j->ratioInv = c->ratio_inv; j->rate = c->rate;
 		}
 		ok &= h2d(d->joints + off, rec, sizeof(cpgJoint)*(size_t)n);
 		cudaStreamSynchronize(lib_stream());
@@ -714,7 +727,7 @@ static DevSet *devset_build(cpSpace **spaces, int nspaces, DevSet *from)
 	ds->hworld = HALLOC(cpgWorld, nspaces);
 	cpgSet *d = &ds->d;
 	d->nworlds = nspaces;
-	long long NB = 0, NS = 0, NV = 0, NC = 0, NN = 0, NP = 0, NDB = 0, NSB = 0, NCD = 0, NU = 0, NO = 0, NPT = 0;
+	long long NB = 0, NS = 0, NV = 0, NC = 0, NN = 0, NP = 0, NDB = 0, NSB = 0, NCD = 0, NU = 0, NO = 0, NPT = 0, NSP = 0;
 	for(int w = 0; w < nspaces; w++){
 		cpSpace *sp = spaces[w];
 		cpgWorld *W = &ds->hworld[w];
@@ -726,8 +739,11 @@ static DevSet *devset_build(cpSpace **spaces, int nspaces, DevSet *from)
 			nverts += s->count;
 			if(body_type_(s->body) == CP_BODY_TYPE_STATIC) nstatShapes++; else ndynShapes++;
 		}
-		int nparts = 0;
-		for(int i = 0; i < sp->ncons; i++) if(!sp->cons[i]->collideBodies) nparts += 2;
+		int nparts = 0, nsprings = 0;
+		for(int i = 0; i < sp->ncons; i++){
+			if(!sp->cons[i]->collideBodies) nparts += 2;
+			if(sp->cons[i]->kind == CPG_DSPRING || sp->cons[i]->kind == CPG_DRSPRING) nsprings += 2;
+		}
 		W->bodyOff = (int)NB; W->nbodies = nb; W->ndyn = sp->ndyn;
 		W->shapeOff = (int)NS; W->nshapes = sp->nshapes;
 		W->vertOff = (int)NV; W->nverts = nverts;
@@ -754,10 +770,11 @@ static DevSet *devset_build(cpSpace **spaces, int nspaces, DevSet *from)
 		W->unitOff = (int)NU; W->unitCap = W->candCap + sp->ncons;
 		W->opOff = (int)NO; W->nops = sp->nops;
 		W->partOff = (int)NPT;
+		W->springOff = (int)NSP;
 		W->dynShapeOff = (int)NS; W->ndynShapes = ndynShapes;
 		NB += nb; NS += sp->nshapes; NV += nverts; NC += sp->ncons;
 		NN += W->nodeCap; NP += W->pairCap; NDB += W->dbinCap; NSB += W->sbinCap;
-		NCD += W->candCap; NU += W->unitCap; NO += sp->nops; NPT += nparts;
+		NCD += W->candCap; NU += W->unitCap; NO += sp->nops; NPT += nparts; NSP += nsprings;
 	}
 	if(NB > 0x7fffffffLL || NCD > 0x7fffffffLL || NU > 0x7fffffffLL){
 		set_error(CP_GPU_ERR_OVERFLOW, "set too large");
@@ -767,6 +784,7 @@ static DevSet *devset_build(cpSpace **spaces, int nspaces, DevSet *from)
 	d->totalBodies = (int)NB; d->totalShapes = (int)NS; d->totalVerts = (int)NV; d->totalCons = (int)NC;
 	d->totalNodes = (int)NN; d->totalPairs = (int)NP; d->totalDBins = (int)NDB; d->totalSBins = (int)NSB;
 	d->totalCands = (int)NCD; d->totalUnits = (int)NU; d->totalOps = (int)NO; d->totalParts = (int)NPT;
+	d->totalSprings = (int)NSP;
 	long long arbCap = 1024;
 	while(arbCap < 8*NS + 1024) arbCap *= 2;
 	if(g_cap_arbs){ arbCap = 1; while(arbCap < g_cap_arbs) arbCap *= 2; }
@@ -855,6 +873,30 @@ static DevSet *devset_build(cpSpace **spaces, int nspaces, DevSet *from)
 		ok &= h2d(d->partStart + W->bodyOff, pstart, sizeof(int)*(size_t)nb);
 		ok &= h2d(d->partCount + W->bodyOff, pcount, sizeof(int)*(size_t)nb);
 		ok &= h2d(d->parts + W->partOff, parts, sizeof(int)*(size_t)np);
+		/* the springs on each body, in constraint order */
+		{
+			int *ss = HALLOC(int, 2*nb), *sstart = ss, *scount = ss + nb;
+			int nsp = 0;
+			for(int i = 0; i < sp->ncons; i++){
+				cpConstraint *c = sp->cons[i];
+				if(c->kind != CPG_DSPRING && c->kind != CPG_DRSPRING) continue;
+				scount[c->a->index]++; scount[c->b->index]++; nsp += 2;
+			}
+			for(int i = 0, acc = 0; i < nb; i++){ sstart[i] = acc; acc += scount[i]; scount[i] = 0; }
+			int *sl = HALLOC(int, nsp);
+			for(int i = 0; i < sp->ncons; i++){
+				cpConstraint *c = sp->cons[i];
+				if(c->kind != CPG_DSPRING && c->kind != CPG_DRSPRING) continue;
+				int a = c->a->index, b = c->b->index;
+				sl[sstart[a] + scount[a]++] = i;
+				sl[sstart[b] + scount[b]++] = i;
+			}
+			ok &= h2d(d->springStart + W->bodyOff, sstart, sizeof(int)*(size_t)nb);
+			ok &= h2d(d->springCount + W->bodyOff, scount, sizeof(int)*(size_t)nb);
+			ok &= h2d(d->springs + W->springOff, sl, sizeof(int)*(size_t)nsp);
+			cudaStreamSynchronize(st);
+			free(ss); free(sl);
+		}
 		ok &= h2d(d->ops + W->opOff, sp->ops, sizeof(cpgOp)*(size_t)sp->nops);
 		int *dyns = HALLOC(int, sp->nshapes);
 		int nds = 0;
@@ -929,6 +971,8 @@ static DevSet *devset_build(cpSpace **spaces, int nspaces, DevSet *from)
 
 static void check_stats(DevSet *ds);
 static void space_detach(cpSpace *sp);
+static cpFloat default_spring_force_(cpConstraint *c, cpFloat dist);
+static cpFloat default_spring_torque_(cpConstraint *c, cpFloat relativeAngle);
 
 /* Downloads so far: identifies the state in a staging block. */
 static unsigned long long g_pull_gen = 0;
@@ -1110,8 +1154,14 @@ static int space_supported(cpSpace *sp)
 		}
 	}
 	for(int i = 0; i < sp->ncons; i++){
-		if(sp->cons[i]->preSolve || sp->cons[i]->postSolve){
+		cpConstraint *c = sp->cons[i];
+		if(c->preSolve || c->postSolve){
 			set_error(CP_GPU_ERR_UNSUPPORTED, "constraint pre/post-solve callbacks are not run on the GPU");
+			return 0;
+		}
+		if((c->kind == CPG_DSPRING && c->springForceFunc != (cpDampedSpringForceFunc)default_spring_force_) ||
+		   (c->kind == CPG_DRSPRING && c->springTorqueFunc != (cpDampedRotarySpringTorqueFunc)default_spring_torque_)){
+			set_error(CP_GPU_ERR_UNSUPPORTED, "custom spring force or torque functions are not run on the GPU");
 			return 0;
 		}
 	}
@@ -2492,9 +2542,127 @@ void cpSlideJointSetMax(cpConstraint *c, cpFloat v) { ASSERT_HARD(c->kind == CPG
 cpFloat cpConstraintGetImpulse(cpConstraint *c)
 {
 	cons_pull_(c);
-	if(c->kind == CPG_PIVOT) return cpvlength(cpv(c->rec.jx, c->rec.jy));
+	if(c->kind == CPG_PIVOT || c->kind == CPG_GROOVE) return cpvlength(cpv(c->rec.jx, c->rec.jy));
+	/* the springs report their signed accumulated impulse
+	 * (cpDampedSpring.c:79-83, cpDampedRotarySpring.c:74-78) */
+	if(c->kind == CPG_DSPRING || c->kind == CPG_DRSPRING) return c->rec.jnAcc;
 	return habs(c->rec.jnAcc);
 }
+
+/* The remaining joints (constructors: cpGrooveJoint.c:119-132,
+ * cpDampedSpring.c:124-140, cpDampedRotarySpring.c:100-115,
+ * cpRotaryLimitJoint.c:108-119, cpRatchetJoint.c:111-123,
+ * cpGearJoint.c:91-102, cpSimpleMotor.c:87-96) */
+static cpFloat default_spring_force_(cpConstraint *c, cpFloat dist) { return (c->restLength - dist)*c->stiffness; }
+static cpFloat default_spring_torque_(cpConstraint *c, cpFloat relativeAngle) { return (relativeAngle - c->restAngle)*c->stiffness; }
+
+cpConstraint *cpGrooveJointNew(cpBody *a, cpBody *b, cpVect groove_a, cpVect groove_b, cpVect anchorB)
+{
+	cpConstraint *c = cons_new_(CPG_GROOVE, a, b);
+	c->grv_a = groove_a; c->grv_b = groove_b;
+	c->grv_n = cpvperp(cpvnormalize(cpvsub(groove_b, groove_a)));
+	c->anchorB = anchorB;
+	return c;
+}
+cpConstraint *cpDampedSpringNew(cpBody *a, cpBody *b, cpVect anchorA, cpVect anchorB, cpFloat restLength, cpFloat stiffness, cpFloat damping)
+{
+	cpConstraint *c = cons_new_(CPG_DSPRING, a, b);
+	c->anchorA = anchorA; c->anchorB = anchorB;
+	c->restLength = restLength; c->stiffness = stiffness; c->damping = damping;
+	c->springForceFunc = (cpDampedSpringForceFunc)default_spring_force_;
+	return c;
+}
+cpConstraint *cpDampedRotarySpringNew(cpBody *a, cpBody *b, cpFloat restAngle, cpFloat stiffness, cpFloat damping)
+{
+	cpConstraint *c = cons_new_(CPG_DRSPRING, a, b);
+	c->restAngle = restAngle; c->stiffness = stiffness; c->damping = damping;
+	c->springTorqueFunc = (cpDampedRotarySpringTorqueFunc)default_spring_torque_;
+	return c;
+}
+cpConstraint *cpRotaryLimitJointNew(cpBody *a, cpBody *b, cpFloat min, cpFloat max)
+{
+	cpConstraint *c = cons_new_(CPG_ROTLIMIT, a, b);
+	c->min = min; c->max = max;
+	return c;
+}
+cpConstraint *cpRatchetJointNew(cpBody *a, cpBody *b, cpFloat phase, cpFloat ratchet)
+{
+	cpConstraint *c = cons_new_(CPG_RATCHET, a, b);
+	c->phase = phase; c->ratchet = ratchet;
+	c->rec.angle = (b ? rd(b)->a : 0.0) - (a ? rd(a)->a : 0.0);
+	return c;
+}
+cpConstraint *cpGearJointNew(cpBody *a, cpBody *b, cpFloat phase, cpFloat ratio)
+{
+	cpConstraint *c = cons_new_(CPG_GEAR, a, b);
+	c->phase = phase; c->ratio = ratio; c->ratio_inv = 1.0/ratio;
+	return c;
+}
+cpConstraint *cpSimpleMotorNew(cpBody *a, cpBody *b, cpFloat rate)
+{
+	cpConstraint *c = cons_new_(CPG_MOTOR, a, b);
+	c->rate = rate;
+	return c;
+}
+
+#define KIND_CHECK(c, k, what) ASSERT_HARD((c)->kind == (k), "Constraint is not a " what ".")
+cpBool cpConstraintIsGrooveJoint(const cpConstraint *c) { return c->kind == CPG_GROOVE; }
+cpBool cpConstraintIsDampedSpring(const cpConstraint *c) { return c->kind == CPG_DSPRING; }
+cpBool cpConstraintIsDampedRotarySpring(const cpConstraint *c) { return c->kind == CPG_DRSPRING; }
+cpBool cpConstraintIsRotaryLimitJoint(const cpConstraint *c) { return c->kind == CPG_ROTLIMIT; }
+cpBool cpConstraintIsRatchetJoint(const cpConstraint *c) { return c->kind == CPG_RATCHET; }
+cpBool cpConstraintIsGearJoint(const cpConstraint *c) { return c->kind == CPG_GEAR; }
+cpBool cpConstraintIsSimpleMotor(const cpConstraint *c) { return c->kind == CPG_MOTOR; }
+cpVect cpGrooveJointGetGrooveA(const cpConstraint *c) { KIND_CHECK(c, CPG_GROOVE, "groove joint"); return c->grv_a; }
+void cpGrooveJointSetGrooveA(cpConstraint *c, cpVect v)
+{
+	KIND_CHECK(c, CPG_GROOVE, "groove joint");
+	cwr(c)->grv_a = v; c->grv_n = cpvperp(cpvnormalize(cpvsub(c->grv_b, v)));
+}
+cpVect cpGrooveJointGetGrooveB(const cpConstraint *c) { KIND_CHECK(c, CPG_GROOVE, "groove joint"); return c->grv_b; }
+void cpGrooveJointSetGrooveB(cpConstraint *c, cpVect v)
+{
+	KIND_CHECK(c, CPG_GROOVE, "groove joint");
+	cwr(c)->grv_b = v; c->grv_n = cpvperp(cpvnormalize(cpvsub(v, c->grv_a)));
+}
+cpVect cpGrooveJointGetAnchorB(const cpConstraint *c) { KIND_CHECK(c, CPG_GROOVE, "groove joint"); return c->anchorB; }
+void cpGrooveJointSetAnchorB(cpConstraint *c, cpVect v) { KIND_CHECK(c, CPG_GROOVE, "groove joint"); cwr(c)->anchorB = v; }
+cpVect cpDampedSpringGetAnchorA(const cpConstraint *c) { KIND_CHECK(c, CPG_DSPRING, "damped spring"); return c->anchorA; }
+void cpDampedSpringSetAnchorA(cpConstraint *c, cpVect v) { KIND_CHECK(c, CPG_DSPRING, "damped spring"); cwr(c)->anchorA = v; }
+cpVect cpDampedSpringGetAnchorB(const cpConstraint *c) { KIND_CHECK(c, CPG_DSPRING, "damped spring"); return c->anchorB; }
+void cpDampedSpringSetAnchorB(cpConstraint *c, cpVect v) { KIND_CHECK(c, CPG_DSPRING, "damped spring"); cwr(c)->anchorB = v; }
+cpFloat cpDampedSpringGetRestLength(const cpConstraint *c) { KIND_CHECK(c, CPG_DSPRING, "damped spring"); return c->restLength; }
+void cpDampedSpringSetRestLength(cpConstraint *c, cpFloat v) { KIND_CHECK(c, CPG_DSPRING, "damped spring"); cwr(c)->restLength = v; }
+cpFloat cpDampedSpringGetStiffness(const cpConstraint *c) { KIND_CHECK(c, CPG_DSPRING, "damped spring"); return c->stiffness; }
+void cpDampedSpringSetStiffness(cpConstraint *c, cpFloat v) { KIND_CHECK(c, CPG_DSPRING, "damped spring"); cwr(c)->stiffness = v; }
+cpFloat cpDampedSpringGetDamping(const cpConstraint *c) { KIND_CHECK(c, CPG_DSPRING, "damped spring"); return c->damping; }
+void cpDampedSpringSetDamping(cpConstraint *c, cpFloat v) { KIND_CHECK(c, CPG_DSPRING, "damped spring"); cwr(c)->damping = v; }
+cpDampedSpringForceFunc cpDampedSpringGetSpringForceFunc(const cpConstraint *c) { KIND_CHECK(c, CPG_DSPRING, "damped spring"); return c->springForceFunc; }
+void cpDampedSpringSetSpringForceFunc(cpConstraint *c, cpDampedSpringForceFunc f) { KIND_CHECK(c, CPG_DSPRING, "damped spring"); cwr(c)->springForceFunc = f; }
+cpFloat cpDampedRotarySpringGetRestAngle(const cpConstraint *c) { KIND_CHECK(c, CPG_DRSPRING, "damped rotary spring"); return c->restAngle; }
+void cpDampedRotarySpringSetRestAngle(cpConstraint *c, cpFloat v) { KIND_CHECK(c, CPG_DRSPRING, "damped rotary spring"); cwr(c)->restAngle = v; }
+cpFloat cpDampedRotarySpringGetStiffness(const cpConstraint *c) { KIND_CHECK(c, CPG_DRSPRING, "damped rotary spring"); return c->stiffness; }
+void cpDampedRotarySpringSetStiffness(cpConstraint *c, cpFloat v) { KIND_CHECK(c, CPG_DRSPRING, "damped rotary spring"); cwr(c)->stiffness = v; }
+cpFloat cpDampedRotarySpringGetDamping(const cpConstraint *c) { KIND_CHECK(c, CPG_DRSPRING, "damped rotary spring"); return c->damping; }
+void cpDampedRotarySpringSetDamping(cpConstraint *c, cpFloat v) { KIND_CHECK(c, CPG_DRSPRING, "damped rotary spring"); cwr(c)->damping = v; }
+cpDampedRotarySpringTorqueFunc cpDampedRotarySpringGetSpringTorqueFunc(const cpConstraint *c) { KIND_CHECK(c, CPG_DRSPRING, "damped rotary spring"); return c->springTorqueFunc; }
+void cpDampedRotarySpringSetSpringTorqueFunc(cpConstraint *c, cpDampedRotarySpringTorqueFunc f) { KIND_CHECK(c, CPG_DRSPRING, "damped rotary spring"); cwr(c)->springTorqueFunc = f; }
+cpFloat cpRotaryLimitJointGetMin(const cpConstraint *c) { KIND_CHECK(c, CPG_ROTLIMIT, "rotary limit joint"); return c->min; }
+void cpRotaryLimitJointSetMin(cpConstraint *c, cpFloat v) { KIND_CHECK(c, CPG_ROTLIMIT, "rotary limit joint"); cwr(c)->min = v; }
+cpFloat cpRotaryLimitJointGetMax(const cpConstraint *c) { KIND_CHECK(c, CPG_ROTLIMIT, "rotary limit joint"); return c->max; }
+void cpRotaryLimitJointSetMax(cpConstraint *c, cpFloat v) { KIND_CHECK(c, CPG_ROTLIMIT, "rotary limit joint"); cwr(c)->max = v; }
+cpFloat cpRatchetJointGetAngle(const cpConstraint *c) { KIND_CHECK(c, CPG_RATCHET, "ratchet joint"); cons_pull_((cpConstraint *)c); return c->rec.angle; }
+void cpRatchetJointSetAngle(cpConstraint *c, cpFloat v) { KIND_CHECK(c, CPG_RATCHET, "ratchet joint"); cwr(c)->rec.angle = v; }
+cpFloat cpRatchetJointGetPhase(const cpConstraint *c) { KIND_CHECK(c, CPG_RATCHET, "ratchet joint"); return c->phase; }
+void cpRatchetJointSetPhase(cpConstraint *c, cpFloat v) { KIND_CHECK(c, CPG_RATCHET, "ratchet joint"); cwr(c)->phase = v; }
+cpFloat cpRatchetJointGetRatchet(const cpConstraint *c) { KIND_CHECK(c, CPG_RATCHET, "ratchet joint"); return c->ratchet; }
+void cpRatchetJointSetRatchet(cpConstraint *c, cpFloat v) { KIND_CHECK(c, CPG_RATCHET, "ratchet joint"); cwr(c)->ratchet = v; }
+cpFloat cpGearJointGetPhase(const cpConstraint *c) { KIND_CHECK(c, CPG_GEAR, "gear joint"); return c->phase; }
+void cpGearJointSetPhase(cpConstraint *c, cpFloat v) { KIND_CHECK(c, CPG_GEAR, "gear joint"); cwr(c)->phase = v; }
+cpFloat cpGearJointGetRatio(const cpConstraint *c) { KIND_CHECK(c, CPG_GEAR, "gear joint"); return c->ratio; }
+void cpGearJointSetRatio(cpConstraint *c, cpFloat v) { KIND_CHECK(c, CPG_GEAR, "gear joint"); cwr(c)->ratio = v; c->ratio_inv = 1.0/v; }
+cpFloat cpSimpleMotorGetRate(const cpConstraint *c) { KIND_CHECK(c, CPG_MOTOR, "simple motor"); return c->rate; }
+void cpSimpleMotorSetRate(cpConstraint *c, cpFloat v) { KIND_CHECK(c, CPG_MOTOR, "simple motor"); cwr(c)->rate = v; }
 
 /* ====================================================================
  * Space
@@ -2959,11 +3127,65 @@ int cpGpuDebugSetImpulses(cpSpace *sp, const double *arbs, int narb, const doubl
 		cpConstraint *c = sp->cons[i];
 		const double *o = cons + 8*i;
 		cons_pull_(c);
-		if(c->kind == CPG_PIVOT){ c->rec.jx = o[1]; c->rec.jy = o[2]; }
+		if(c->kind == CPG_PIVOT || c->kind == CPG_GROOVE){ c->rec.jx = o[1]; c->rec.jy = o[2]; }
 		else c->rec.jnAcc = o[1];
+		if(c->kind == CPG_RATCHET) c->rec.angle = o[3];
 		sp->consDirty = 1;
 	}
 	return bad;
+}
+
+/* Solver quality from the space's current state: the next step is run
+ * from a saved copy of the device state once per iteration count k = 1 ..
+ * maxIters (the first k iterations of a sweep do not depend on how many
+ * follow), with solver mode `mode`; after each run the contacts' RMS normal
+ * and friction residuals and the largest penetration are measured
+ * (k_contact_quality), and the state is put back, so the space is left as
+ * it was. */
+int cpGpuSolverQuality(cpSpace *sp, int mode, cpFloat dt, int maxIters, double *out)
+{
+	if(!sp || !sp->dev || !sp->ownsDev || sp->structDirty || maxIters < 1 || !out || !(dt > 0.0) ||
+	   mode < CP_GPU_SOLVER_ORDERED || mode > CP_GPU_SOLVER_COLORED){
+		set_error(CP_GPU_ERR_ARGUMENT, "solver quality: a stepped standalone space, iterations >= 1 and dt > 0 are needed");
+		return -1;
+	}
+	DevSet *ds = sp->dev;
+	cudaStream_t st = lib_stream();
+	devset_flush_space(ds, 0);
+	char *saved = NULL;
+	double *acc = NULL;
+	if(!cuda_ok(cudaMalloc((void **)&saved, ds->slabBytes), "cudaMalloc quality state")) return -1;
+	if(!cuda_ok(cudaMalloc((void **)&acc, 4*sizeof(double)), "cudaMalloc quality")){ cudaFree(saved); return -1; }
+	cuda_ok(cudaMemcpyAsync(saved, ds->slab, ds->slabBytes, cudaMemcpyDeviceToDevice, st), "save state");
+	unsigned stamp = sp->stamp;
+	double currDt = sp->curr_dt, jointDt = sp->jointDt;
+	int iters = sp->iterations, oldMode = sp->mode, rc = 0;
+	for(int k = 1; k <= maxIters && rc == 0; k++){
+		if(k > 1) rollout_restore_from(ds, saved, &stamp, &currDt);
+		sp->jointDt = jointDt;
+		sp->iterations = k;
+		sp->mode = mode;
+		double dts[1] = { dt };
+		double h[4] = { 0.0, 0.0, 0.0, 0.0 };
+		rc = devset_step(ds, dts, NULL);
+		if(rc == 0 && cpg_launch_contact_quality(&ds->d, 0, dt, acc, st) != 0) rc = -1;
+		if(rc == 0 && !d2h(h, acc, sizeof(h))) rc = -1;
+		if(rc == 0 && !cuda_ok(cudaStreamSynchronize(st), "quality")) rc = -1;
+		double n = h[2] > 0.0 ? h[2] : 1.0, pen;
+		memcpy(&pen, &h[3], sizeof(pen));
+		out[3*(k - 1)] = sqrt(h[0]/n);
+		out[3*(k - 1) + 1] = sqrt(h[1]/n);
+		out[3*(k - 1) + 2] = pen;
+	}
+	rollout_restore_from(ds, saved, &stamp, &currDt);
+	sp->jointDt = jointDt;
+	sp->iterations = iters;
+	sp->mode = oldMode;
+	cudaStreamSynchronize(st);
+	check_stats(ds);
+	cudaFree(saved);
+	cudaFree(acc);
+	return rc;
 }
 
 int cpGpuDebugNarrowIds(cpSpace *sp, int *out, int max)
@@ -3015,10 +3237,18 @@ int cpGpuDebugConstraints(cpSpace *sp, double *out, int max)
 		cons_pull_(c);
 		const cpgJoint *j = &c->rec;
 		double *o = out + 8*i;
+		memset(o, 0, 8*sizeof(double));
 		o[0] = (double)c->kind;
-		if(c->kind == CPG_PIVOT){ o[1] = j->jx; o[2] = j->jy; o[7] = j->biasx; }
-		else { o[1] = j->jnAcc; o[2] = j->nMass; o[7] = j->bias; }
-		o[3] = j->r1x; o[4] = j->r1y; o[5] = j->r2x; o[6] = j->r2y;
+		switch(c->kind){
+		case CPG_PIVOT: case CPG_GROOVE: o[1] = j->jx; o[2] = j->jy; o[7] = j->biasx; break;
+		case CPG_PIN: case CPG_SLIDE: o[1] = j->jnAcc; o[2] = j->nMass; o[7] = j->bias; break;
+		case CPG_DSPRING: o[1] = j->jnAcc; o[2] = j->nMass; o[7] = j->coef; break;
+		case CPG_DRSPRING: o[1] = j->jnAcc; o[2] = j->nMass; o[3] = j->coef; o[7] = j->bias; break;
+		case CPG_RATCHET: o[1] = j->jnAcc; o[2] = j->nMass; o[3] = j->angle; o[7] = j->bias; break;
+		case CPG_ROTLIMIT: case CPG_GEAR: o[1] = j->jnAcc; o[2] = j->nMass; o[7] = j->bias; break;
+		default: o[1] = j->jnAcc; o[2] = j->nMass; break;
+		}
+		if(c->kind <= CPG_DSPRING){ o[3] = j->r1x; o[4] = j->r1y; o[5] = j->r2x; o[6] = j->r2y; }
 	}
 	return sp->ncons;
 }

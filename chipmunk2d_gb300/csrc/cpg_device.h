@@ -27,7 +27,8 @@ enum { CPG_CIRCLE = 0, CPG_SEGMENT = 1, CPG_POLY = 2 };
 /* body types as cpBodyType */
 enum { CPG_DYNAMIC = 0, CPG_KINEMATIC = 1, CPG_STATIC = 2 };
 /* joint kinds */
-enum { CPG_PIVOT = 1, CPG_PIN = 2, CPG_SLIDE = 3 };
+enum { CPG_PIVOT = 1, CPG_PIN = 2, CPG_SLIDE = 3, CPG_GROOVE = 4, CPG_DSPRING = 5, CPG_DRSPRING = 6,
+       CPG_ROTLIMIT = 7, CPG_RATCHET = 8, CPG_GEAR = 9, CPG_MOTOR = 10 };
 /* arbiter states, chipmunk_structs.h:83-95 */
 enum { CPG_ARB_FIRST = 0, CPG_ARB_NORMAL = 1, CPG_ARB_IGNORE = 2, CPG_ARB_CACHED = 3 };
 /* error bits latched in cpgTree.error */
@@ -54,7 +55,7 @@ typedef struct cpgWorld {
 	int opOff, nops;              /* pending index insertions */
 	int partOff;                  /* CSR of non-colliding joint partners */
 	int dynShapeOff, ndynShapes;  /* shapes on non-static bodies (coloured mode) */
-	int pad;
+	int springOff;                /* CSR of the springs on each body */
 } cpgWorld;
 
 /* Per-world step parameters (host-written each step). */
@@ -152,7 +153,13 @@ typedef struct cpgJoint {
 	double k11, k12, k21, k22;    /* pivot: inverse mass tensor */
 	double jx, jy;                /* pivot: accumulated impulse */
 	double biasx, biasy;          /* pivot: bias velocity */
-	double nx, ny, nMass, jnAcc, bias;  /* pin/slide */
+	double nx, ny, nMass, jnAcc, bias;  /* pin/slide; nMass holds iSum and bias the
+	                                     * spring's target velocity for the other kinds */
+	double gax, gay, gbx, gby, gnx, gny; /* groove: ends and normal in body a's space */
+	double restLength, stiffness, damping; /* springs (rotary spring: restLength is the rest angle) */
+	double phase, ratchet, angle, ratio, ratioInv, rate; /* ratchet, gear, motor */
+	double coef, clamp;                  /* spring damping coefficient, groove clamp (pre-step) */
+	double preJx, preJy;                 /* the springs' pre-step impulse (rotary: preJx) */
 } cpgJoint;
 
 /* Solver rows: one per unit, stored in schedule order so that the threads
@@ -174,7 +181,8 @@ typedef struct cpgRow {
 	union {
 		struct { double nx, ny, u, svx, svy, e; cpgRowContact c[2]; } arb;   /* e: elasticity */
 		struct { double r1x, r1y, r2x, r2y, k11, k12, k21, k22, jx, jy, biasx, biasy;
-		         double nx, ny, nMass, jnAcc, bias, maxForce; } jnt;
+		         double nx, ny, nMass, jnAcc, bias, maxForce;
+		         double clamp, coef, aux1, aux2; } jnt;   /* groove clamp; spring coefficient; ratchet / gear ratios */
 	};
 } cpgRow;
 
@@ -231,7 +239,7 @@ typedef struct cpgTape {
 typedef struct cpgSet {
 	int nworlds;
 	int totalBodies, totalShapes, totalVerts, totalCons;
-	int totalNodes, totalPairs, totalDBins, totalSBins, totalCands, totalUnits, totalOps, totalParts;
+	int totalNodes, totalPairs, totalDBins, totalSBins, totalCands, totalUnits, totalOps, totalParts, totalSprings;
 	int arbCap;                   /* arbiter hash table slots (power of two) */
 	int maxWorldUnits;
 
@@ -247,6 +255,8 @@ typedef struct cpgSet {
 	int *btype, *bworld;
 	int *partStart, *partCount;   /* joint partners with collideBodies off */
 	int *parts;                   /* [totalParts] */
+	int *springStart, *springCount; /* damped springs (linear and rotary) on each body, */
+	int *springs;                 /* [totalSprings] their world-local joint indices in constraint order */
 	int *last;                    /* schedule scratch */
 
 	/* shapes [totalShapes] */
@@ -367,6 +377,7 @@ void cpg_step_graph_free(void *cache);
 int cpg_launch_replay_solve(const cpgSet *s, const cpgAdj *a, int nsteps, void *stream);
 int cpg_launch_transfer(const cpgSet *to, const cpgSet *from, const int *bodyMap, const unsigned char *deadShape,
                         int *slotMap, void *stream);
+int cpg_launch_contact_quality(const cpgSet *s, int w, double dt, double *acc, void *stream);
 int cpg_launch_set_arb_impulses(const cpgSet *s, int w, const double *imp, const int *pairs, int n, int *mismatch, void *stream);
 
 #ifdef __cplusplus

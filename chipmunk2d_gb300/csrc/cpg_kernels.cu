@@ -870,6 +870,131 @@ __device__ __forceinline__ double k_scalar_body(const cpgSet &s, int g, double r
 	return s.minv[g] + s.iinv[g]*rcn*rcn;
 }
 
+/* k_tensor, chipmunk_private.h:228-262: the inverse of the 2x2 effective
+ * mass of a point constraint, into the row */
+__device__ __forceinline__ void row_k_tensor(const cpgSet &s, int ga, int gb, double r1x, double r1y, double r2x, double r2y, cpgRow &row)
+{
+	double m_sum = s.minv[ga] + s.minv[gb];
+	double k11 = m_sum, k12 = 0.0, k21 = 0.0, k22 = m_sum;
+	double ai = s.iinv[ga];
+	double r1xsq = r1x*r1x*ai, r1ysq = r1y*r1y*ai, r1nxy = -r1x*r1y*ai;
+	k11 += r1ysq; k12 += r1nxy; k21 += r1nxy; k22 += r1xsq;
+	double bi = s.iinv[gb];
+	double r2xsq = r2x*r2x*bi, r2ysq = r2y*r2y*bi, r2nxy = -r2x*r2y*bi;
+	k11 += r2ysq; k12 += r2nxy; k21 += r2nxy; k22 += r2xsq;
+	double det = k11*k22 - k12*k21;
+	double det_inv = 1.0/det;
+	row.jnt.k11 = k22*det_inv; row.jnt.k12 = -k12*det_inv; row.jnt.k21 = -k21*det_inv; row.jnt.k22 = k11*det_inv;
+}
+
+/* Pre-steps of the groove, damped spring, damped rotary spring, rotary
+ * limit, ratchet, gear and simple motor (cpGrooveJoint.c:24-59,
+ * cpDampedSpring.c:29-53, cpDampedRotarySpring.c:29-49,
+ * cpRotaryLimitJoint.c:24-46, cpRatchetJoint.c:24-52, cpGearJoint.c:24-35,
+ * cpSimpleMotor.c:24-31).  The springs' own impulses are not applied here:
+ * they go into the joint record (preJx, preJy) and k_integrate_vel applies
+ * them to each body in constraint order, before the velocity update, as
+ * the reference's pre-step loop does; the ratchet's angle, a state kept
+ * from step to step, is written back to the record. */
+__device__ void joint_prestep_more(const cpgSet &s, cpgJoint &jrec, cpgRow &row, int ga, int gb,
+                                   double r1x, double r1y, double r2x, double r2y, double biasCoef, double dt)
+{
+	const cpgJoint &j = jrec;
+	double iSum = 0.0;
+	switch(j.kind){
+	case CPG_GROOVE: {
+		double ta_ = s.ta[ga], tb_ = s.tb[ga], tc_ = s.tc[ga], td_ = s.td[ga], tx = s.ttx[ga], ty = s.tty[ga];
+		V2 tA = v2(ta_*j.gax + tc_*j.gay + tx, tb_*j.gax + td_*j.gay + ty);
+		V2 tB = v2(ta_*j.gbx + tc_*j.gby + tx, tb_*j.gbx + td_*j.gby + ty);
+		V2 n = v2(ta_*j.gnx + tc_*j.gny, tb_*j.gnx + td_*j.gny);
+		double d = vdot(tA, n);
+		V2 pa = v2(s.px[ga], s.py[ga]), pb = v2(s.px[gb], s.py[gb]);
+		double tdist = vcross(vadd(pb, v2(r2x, r2y)), n);
+		double clamp;
+		V2 r1;
+		if(tdist <= vcross(tA, n)){ clamp = 1.0; r1 = vsub(tA, pa); }
+		else if(tdist >= vcross(tB, n)){ clamp = -1.0; r1 = vsub(tB, pa); }
+		else { clamp = 0.0; r1 = vsub(vadd(vmul(vperp(n), -tdist), vmul(n, d)), pa); }
+		row.jnt.r1x = r1.x; row.jnt.r1y = r1.y;
+		row_k_tensor(s, ga, gb, r1.x, r1.y, r2x, r2y, row);
+		V2 delta = vsub(vadd(pb, v2(r2x, r2y)), vadd(pa, r1));
+		V2 bias = vclamp(vmul(delta, -biasCoef/dt), j.maxBias);
+		row.jnt.biasx = bias.x; row.jnt.biasy = bias.y;
+		row.jnt.nx = n.x; row.jnt.ny = n.y;
+		row.jnt.clamp = clamp;
+		row.jnt.jx = j.jx; row.jnt.jy = j.jy;
+		return;
+	}
+	case CPG_DSPRING: {
+		double deltax = (s.px[gb] + r2x) - (s.px[ga] + r1x);
+		double deltay = (s.py[gb] + r2y) - (s.py[ga] + r1y);
+		double dist = sqrt(deltax*deltax + deltay*deltay);
+		double inv = 1.0/(dist ? dist : CUDART_INF);
+		double nx = deltax*inv, ny = deltay*inv;
+		double k = k_scalar_body(s, ga, r1x, r1y, nx, ny) + k_scalar_body(s, gb, r2x, r2y, nx, ny);
+		row.jnt.nx = nx; row.jnt.ny = ny;
+		row.jnt.nMass = 1.0/k;
+		row.jnt.bias = 0.0;                                  /* target_vrn */
+		row.jnt.coef = 1.0 - exp(-j.damping*dt*k);           /* v_coef */
+		double j_spring = ((j.restLength - dist)*j.stiffness)*dt;
+		row.jnt.jnAcc = j_spring;
+		jrec.preJx = nx*j_spring; jrec.preJy = ny*j_spring;
+		jrec.r1x = r1x; jrec.r1y = r1y; jrec.r2x = r2x; jrec.r2y = r2y;
+		return;
+	}
+	case CPG_DRSPRING: {
+		double moment = s.iinv[ga] + s.iinv[gb];
+		row.jnt.nMass = 1.0/moment;                          /* iSum */
+		row.jnt.coef = 1.0 - exp(-j.damping*dt*moment);      /* w_coef */
+		row.jnt.bias = 0.0;                                  /* target_wrn */
+		double j_spring = (((s.ang[ga] - s.ang[gb]) - j.restLength)*j.stiffness)*dt;
+		row.jnt.jnAcc = j_spring;
+		jrec.preJx = j_spring;
+		return;
+	}
+	case CPG_ROTLIMIT: {
+		double dist = s.ang[gb] - s.ang[ga];
+		double pdist = 0.0;
+		if(dist > j.max) pdist = j.max - dist;
+		else if(dist < j.min) pdist = j.min - dist;
+		iSum = 1.0/(s.iinv[ga] + s.iinv[gb]);
+		row.jnt.nMass = iSum;
+		double bias = dclamp(-biasCoef*pdist/dt, -j.maxBias, j.maxBias);
+		row.jnt.bias = bias;
+		row.jnt.jnAcc = bias ? j.jnAcc : 0.0;
+		return;
+	}
+	case CPG_RATCHET: {
+		double angle = j.angle, phase = j.phase, ratchet = j.ratchet;
+		double delta = s.ang[gb] - s.ang[ga];
+		double diff = angle - delta;
+		double pdist = 0.0;
+		if(diff*ratchet > 0.0) pdist = diff;
+		else jrec.angle = floor((delta - phase)/ratchet)*ratchet + phase;
+		iSum = 1.0/(s.iinv[ga] + s.iinv[gb]);
+		row.jnt.nMass = iSum;
+		double bias = dclamp(-biasCoef*pdist/dt, -j.maxBias, j.maxBias);
+		row.jnt.bias = bias;
+		row.jnt.jnAcc = bias ? j.jnAcc : 0.0;
+		row.jnt.aux1 = ratchet;
+		return;
+	}
+	case CPG_GEAR: {
+		iSum = 1.0/(s.iinv[ga]*j.ratioInv + j.ratio*s.iinv[gb]);
+		row.jnt.nMass = iSum;
+		row.jnt.bias = dclamp(-biasCoef*((s.ang[gb]*j.ratio - s.ang[ga]) - j.phase)/dt, -j.maxBias, j.maxBias);
+		row.jnt.jnAcc = j.jnAcc;
+		row.jnt.aux1 = j.ratio; row.jnt.aux2 = j.ratioInv;
+		return;
+	}
+	default: /* CPG_MOTOR */
+		row.jnt.nMass = 1.0/(s.iinv[ga] + s.iinv[gb]);
+		row.jnt.bias = j.rate;
+		row.jnt.jnAcc = j.jnAcc;
+		return;
+	}
+}
+
 __global__ void k_build_rows(cpgSet s)
 {
 	int w = blockIdx.y;
@@ -916,7 +1041,8 @@ __global__ void k_build_rows(cpgSet s)
 			}
 		} else {
 			int jidx = u - narb;
-			const cpgJoint &j = s.joints[W.consOff + jidx];
+			cpgJoint &jrec = s.joints[W.consOff + jidx];
+			const cpgJoint &j = jrec;
 			double biasCoef = s.jbias[W.consOff + jidx];
 			int ga = W.bodyOff + j.a, gb = W.bodyOff + j.b;
 			row.a = j.a; row.b = j.b; row.kind = j.kind; row.count = 0; row.src = jidx;
@@ -931,18 +1057,7 @@ __global__ void k_build_rows(cpgSet s)
 			double deltax = (s.px[gb] + r2x) - (s.px[ga] + r1x);
 			double deltay = (s.py[gb] + r2y) - (s.py[ga] + r1y);
 			if(j.kind == CPG_PIVOT){
-				/* k_tensor, chipmunk_private.h:228-262 */
-				double m_sum = s.minv[ga] + s.minv[gb];
-				double k11 = m_sum, k12 = 0.0, k21 = 0.0, k22 = m_sum;
-				double ai = s.iinv[ga];
-				double r1xsq = r1x*r1x*ai, r1ysq = r1y*r1y*ai, r1nxy = -r1x*r1y*ai;
-				k11 += r1ysq; k12 += r1nxy; k21 += r1nxy; k22 += r1xsq;
-				double bi = s.iinv[gb];
-				double r2xsq = r2x*r2x*bi, r2ysq = r2y*r2y*bi, r2nxy = -r2x*r2y*bi;
-				k11 += r2ysq; k12 += r2nxy; k21 += r2nxy; k22 += r2xsq;
-				double det = k11*k22 - k12*k21;
-				double det_inv = 1.0/det;
-				row.jnt.k11 = k22*det_inv; row.jnt.k12 = -k12*det_inv; row.jnt.k21 = -k21*det_inv; row.jnt.k22 = k11*det_inv;
+				row_k_tensor(s, ga, gb, r1x, r1y, r2x, r2y, row);
 				V2 bias = vclamp(vmul(v2(deltax, deltay), -biasCoef/dt), j.maxBias);
 				row.jnt.biasx = bias.x; row.jnt.biasy = bias.y;
 				row.jnt.jx = j.jx; row.jnt.jy = j.jy;
@@ -955,7 +1070,7 @@ __global__ void k_build_rows(cpgSet s)
 				row.jnt.nMass = 1.0/kn;
 				row.jnt.bias = dclamp(-biasCoef*(dist - j.dist)/dt, -j.maxBias, j.maxBias);
 				row.jnt.jnAcc = j.jnAcc;
-			} else {
+			} else if(j.kind == CPG_SLIDE){
 				double dist = sqrt(deltax*deltax + deltay*deltay);
 				double pdist = 0.0, nx, ny, jn = j.jnAcc;
 				if(dist > j.max){
@@ -975,6 +1090,8 @@ __global__ void k_build_rows(cpgSet s)
 				row.jnt.nMass = 1.0/kn;
 				row.jnt.bias = dclamp(-biasCoef*pdist/dt, -j.maxBias, j.maxBias);
 				row.jnt.jnAcc = jn;
+			} else {
+				joint_prestep_more(s, jrec, row, ga, gb, r1x, r1y, r2x, r2y, biasCoef, dt);
 			}
 		}
 	}
@@ -995,6 +1112,27 @@ __global__ void k_integrate_vel(cpgSet s)
 	double minv = s.minv[g], iinv = s.iinv[g];
 	if(g - s.world[w].bodyOff < s.world[w].ndyn && s.btype[g] != CPG_KINEMATIC){
 		double dt = P.dt, damping = P.damping;
+		/* the springs' pre-step impulses, in constraint order
+		 * (cpDampedSpring.c:51, cpDampedRotarySpring.c:46-47), before the
+		 * velocity update that follows the pre-steps (cpSpaceStep.c:395-403) */
+		const cpgWorld &W = s.world[w];
+		int x = g - W.bodyOff;
+		for(int k = 0, n = s.springCount[g]; k < n; k++){
+			const cpgJoint &jr = s.joints[W.consOff + s.springs[W.springOff + s.springStart[g] + k]];
+			if(jr.kind == CPG_DSPRING){
+				if(jr.a == x){
+					vx = vx + (-jr.preJx)*minv; vy = vy + (-jr.preJy)*minv;
+					wv += iinv*(jr.r1x*(-jr.preJy) - jr.r1y*(-jr.preJx));
+				}
+				if(jr.b == x){
+					vx = vx + jr.preJx*minv; vy = vy + jr.preJy*minv;
+					wv += iinv*(jr.r2x*jr.preJy - jr.r2y*jr.preJx);
+				}
+			} else {
+				if(jr.a == x) wv -= jr.preJx*iinv;
+				if(jr.b == x) wv += jr.preJx*iinv;
+			}
+		}
 		vx = vx*damping + (P.gx + s.fx[g]*minv)*dt;
 		vy = vy*damping + (P.gy + s.fy[g]*minv)*dt;
 		wv = wv*damping + s.tq[g]*iinv*dt;
@@ -1073,11 +1211,106 @@ __device__ __forceinline__ void row_apply_cached(const cpgRow &row, BodyRef &A, 
 			double jx = nx*con.jnAcc - ny*con.jtAcc, jy = nx*con.jtAcc + ny*con.jnAcc;
 			apply_impulses(A, B, con.r1x, con.r1y, con.r2x, con.r2y, jx*dt_coef, jy*dt_coef);
 		}
-	} else if(row.kind == CPG_PIVOT){
+	} else if(row.kind == CPG_PIVOT || row.kind == CPG_GROOVE){
 		apply_impulses(A, B, row.jnt.r1x, row.jnt.r1y, row.jnt.r2x, row.jnt.r2y, row.jnt.jx*dt_coef, row.jnt.jy*dt_coef);
-	} else {
+	} else if(row.kind == CPG_PIN || row.kind == CPG_SLIDE){
 		double s_ = row.jnt.jnAcc*dt_coef;
 		apply_impulses(A, B, row.jnt.r1x, row.jnt.r1y, row.jnt.r2x, row.jnt.r2y, row.jnt.nx*s_, row.jnt.ny*s_);
+	} else if(row.kind == CPG_ROTLIMIT || row.kind == CPG_RATCHET || row.kind == CPG_MOTOR || row.kind == CPG_GEAR){
+		/* cpRotaryLimitJoint.c:48-57, cpRatchetJoint.c:54-62, cpGearJoint.c:37-46, cpSimpleMotor.c:33-41 */
+		double j = row.jnt.jnAcc*dt_coef;
+		A.w -= (row.kind == CPG_GEAR) ? j*A.iinv*row.jnt.aux2 : j*A.iinv;
+		B.w += j*B.iinv;
+	}
+	/* the springs keep no cached impulse (cpDampedSpring.c:55, cpDampedRotarySpring.c:51) */
+}
+
+/* One iteration of the groove, springs and rotary joints:
+ * cpGrooveJoint.c:61-94, cpDampedSpring.c:57-77, cpDampedRotarySpring.c:53-72,
+ * cpRotaryLimitJoint.c:59-85, cpRatchetJoint.c:64-87, cpGearJoint.c:48-67,
+ * cpSimpleMotor.c:43-61 */
+__device__ __noinline__ void row_apply_more(cpgRow &row, BodyRef &A, BodyRef &B, double dt)
+{
+	switch(row.kind){
+	case CPG_GROOVE: {
+		double v1x = A.vx + (-row.jnt.r1y)*A.w, v1y = A.vy + row.jnt.r1x*A.w;
+		double v2x = B.vx + (-row.jnt.r2y)*B.w, v2y = B.vy + row.jnt.r2x*B.w;
+		double vrx = v2x - v1x, vry = v2y - v1y;
+		double ex = row.jnt.biasx - vrx, ey = row.jnt.biasy - vry;
+		double jx = ex*row.jnt.k11 + ey*row.jnt.k12, jy = ex*row.jnt.k21 + ey*row.jnt.k22;
+		double oldx = row.jnt.jx, oldy = row.jnt.jy;
+		V2 acc = v2(oldx + jx, oldy + jy);
+		V2 n = v2(row.jnt.nx, row.jnt.ny);
+		/* grooveConstrain: inside the groove's ends only the normal part, at
+		 * an end also the part pushing back in */
+		V2 jc = (row.jnt.clamp*vcross(acc, n) > 0.0) ? acc : vmul(n, vdot(acc, n)/vdot(n, n));
+		acc = vclamp(jc, row.jnt.maxForce*dt);
+		row.jnt.jx = acc.x; row.jnt.jy = acc.y;
+		apply_impulses(A, B, row.jnt.r1x, row.jnt.r1y, row.jnt.r2x, row.jnt.r2y, acc.x - oldx, acc.y - oldy);
+		return;
+	}
+	case CPG_DSPRING: {
+		double v1x = A.vx + (-row.jnt.r1y)*A.w, v1y = A.vy + row.jnt.r1x*A.w;
+		double v2x = B.vx + (-row.jnt.r2y)*B.w, v2y = B.vy + row.jnt.r2x*B.w;
+		double vrn = (v2x - v1x)*row.jnt.nx + (v2y - v1y)*row.jnt.ny;
+		double v_damp = (row.jnt.bias - vrn)*row.jnt.coef;
+		row.jnt.bias = vrn + v_damp;
+		double j_damp = v_damp*row.jnt.nMass;
+		row.jnt.jnAcc += j_damp;
+		apply_impulses(A, B, row.jnt.r1x, row.jnt.r1y, row.jnt.r2x, row.jnt.r2y, row.jnt.nx*j_damp, row.jnt.ny*j_damp);
+		return;
+	}
+	case CPG_DRSPRING: {
+		double wrn = A.w - B.w;
+		double w_damp = (row.jnt.bias - wrn)*row.jnt.coef;
+		row.jnt.bias = wrn + w_damp;
+		double j_damp = w_damp*row.jnt.nMass;
+		row.jnt.jnAcc += j_damp;
+		A.w += j_damp*A.iinv;
+		B.w -= j_damp*B.iinv;
+		return;
+	}
+	case CPG_ROTLIMIT: case CPG_RATCHET: {
+		if(!row.jnt.bias) return;
+		double wr = B.w - A.w;
+		double jMax = row.jnt.maxForce*dt;
+		double j = -(row.jnt.bias + wr)*row.jnt.nMass;
+		double jOld = row.jnt.jnAcc;
+		if(row.kind == CPG_RATCHET){
+			double ratchet = row.jnt.aux1;
+			row.jnt.jnAcc = dclamp((jOld + j)*ratchet, 0.0, jMax*dabs(ratchet))/ratchet;
+		} else if(row.jnt.bias < 0.0){
+			row.jnt.jnAcc = dclamp(jOld + j, 0.0, jMax);
+		} else {
+			row.jnt.jnAcc = dclamp(jOld + j, -jMax, 0.0);
+		}
+		j = row.jnt.jnAcc - jOld;
+		A.w -= j*A.iinv;
+		B.w += j*B.iinv;
+		return;
+	}
+	case CPG_GEAR: {
+		double wr = B.w*row.jnt.aux1 - A.w;
+		double jMax = row.jnt.maxForce*dt;
+		double j = (row.jnt.bias - wr)*row.jnt.nMass;
+		double jOld = row.jnt.jnAcc;
+		row.jnt.jnAcc = dclamp(jOld + j, -jMax, jMax);
+		j = row.jnt.jnAcc - jOld;
+		A.w -= j*A.iinv*row.jnt.aux2;
+		B.w += j*B.iinv;
+		return;
+	}
+	default: { /* CPG_MOTOR */
+		double wr = B.w - A.w + row.jnt.bias;
+		double jMax = row.jnt.maxForce*dt;
+		double j = -wr*row.jnt.nMass;
+		double jOld = row.jnt.jnAcc;
+		row.jnt.jnAcc = dclamp(jOld + j, -jMax, jMax);
+		j = row.jnt.jnAcc - jOld;
+		A.w -= j*A.iinv;
+		B.w += j*B.iinv;
+		return;
+	}
 	}
 }
 
@@ -1115,9 +1348,16 @@ __device__ void warm_gather(const cpgSet &s, int w, int x, double &vx, double &v
 				if(isA) apply_impulse(B, -jx, -jy, con.r1x, con.r1y);
 				if(isB) apply_impulse(B, jx, jy, con.r2x, con.r2y);
 			}
+		} else if(row.kind == CPG_DSPRING || row.kind == CPG_DRSPRING){
+			continue;
+		} else if(row.kind > CPG_SLIDE && row.kind != CPG_GROOVE){
+			/* rotary joints: angular impulses only, as row_apply_cached */
+			double j = row.jnt.jnAcc*dt_coef;
+			if(isA) B.w -= (row.kind == CPG_GEAR) ? j*B.iinv*row.jnt.aux2 : j*B.iinv;
+			if(isB) B.w += j*B.iinv;
 		} else {
 			double jx, jy;
-			if(row.kind == CPG_PIVOT){ jx = row.jnt.jx*dt_coef; jy = row.jnt.jy*dt_coef; }
+			if(row.kind == CPG_PIVOT || row.kind == CPG_GROOVE){ jx = row.jnt.jx*dt_coef; jy = row.jnt.jy*dt_coef; }
 			else { double s_ = row.jnt.jnAcc*dt_coef; jx = row.jnt.nx*s_; jy = row.jnt.ny*s_; }
 			if(isA) apply_impulse(B, -jx, -jy, row.jnt.r1x, row.jnt.r1y);
 			if(isB) apply_impulse(B, jx, jy, row.jnt.r2x, row.jnt.r2y);
@@ -1168,6 +1408,7 @@ __device__ __forceinline__ void row_apply(cpgRow &row, BodyRef &A, BodyRef &B, d
 		}
 		return;
 	}
+	if(row.kind > CPG_SLIDE){ row_apply_more(row, A, B, dt); return; }
 	if(row.kind == CPG_SLIDE && row.jnt.nx == 0.0 && row.jnt.ny == 0.0) return;
 	double v1x = A.vx + (-row.jnt.r1y)*A.w, v1y = A.vy + row.jnt.r1x*A.w;
 	double v2x = B.vx + (-row.jnt.r2y)*B.w, v2y = B.vy + row.jnt.r2x*B.w;
@@ -1633,11 +1874,13 @@ __global__ void k_writeback(cpgSet s)
 		} else {
 			cpgJoint &j = s.joints[W.consOff + row.src];
 			j.r1x = row.jnt.r1x; j.r1y = row.jnt.r1y; j.r2x = row.jnt.r2x; j.r2y = row.jnt.r2y;
-			if(row.kind == CPG_PIVOT){
+			if(row.kind == CPG_PIVOT || row.kind == CPG_GROOVE){
 				j.k11 = row.jnt.k11; j.k12 = row.jnt.k12; j.k21 = row.jnt.k21; j.k22 = row.jnt.k22;
 				j.jx = row.jnt.jx; j.jy = row.jnt.jy; j.biasx = row.jnt.biasx; j.biasy = row.jnt.biasy;
+				j.nx = row.jnt.nx; j.ny = row.jnt.ny; j.clamp = row.jnt.clamp;
 			} else {
 				j.nx = row.jnt.nx; j.ny = row.jnt.ny; j.nMass = row.jnt.nMass; j.jnAcc = row.jnt.jnAcc; j.bias = row.jnt.bias;
+				j.coef = row.jnt.coef;
 			}
 		}
 	}
@@ -1700,6 +1943,72 @@ extern "C" int cpg_launch_set_arb_impulses(const cpgSet *s, int w, const double 
 {
 	if(n <= 0) return 0;
 	LAUNCH(k_set_arb_impulses<<<(n + 127)/128, 128, 0, (cudaStream_t)stream>>>(*s, w, imp, pairs, n, mismatch));
+	return cudaGetLastError() == cudaSuccess ? 0 : -1;
+}
+
+/* Contact quality of one world after a step, from its solver rows and
+ * final velocities (all contacts of all arbiter rows):
+ *   normal residual: |vn + bounce| where the accumulated normal impulse is
+ *     positive, else the approach speed max(0, -(vn + bounce)) -- the
+ *     complementarity the sequential impulses converge to
+ *     (cpArbiter.c:459-498);
+ *   friction residual: |vt| for a contact inside the friction cone
+ *     (|jt| < u jn), else the slip along the friction impulse
+ *     max(0, vt sign(jt)) (friction must oppose sliding);
+ *   penetration: max(0, -d'), d' the contact's separation along n after
+ *     the next position update, d + dt (vn + vbn): d at the step's
+ *     positions (cpArbiterGetDepth, cpArbiter.c:90-98), vn and vbn the
+ *     relative normal velocity and bias velocity the solve left.
+ * acc: [0] sum of squared normal residuals, [1] of friction residuals,
+ * [2] contacts, [3] largest penetration (as the bits of a non-negative
+ * double, so that integer max orders them). */
+__global__ void k_contact_quality(cpgSet s, int w, double dt, double *acc)
+{
+	const cpgWorld &W = s.world[w];
+	const cpgTree &T = s.tree[w];
+	int nunits = T.nunits;
+	if(nunits > W.unitCap) return;
+	double sn = 0.0, stt = 0.0, cnt = 0.0, pen = 0.0;
+	for(int k = blockIdx.x*blockDim.x + threadIdx.x; k < nunits; k += gridDim.x*blockDim.x){
+		const cpgRow &row = s.rows[W.unitOff + k];
+		if(row.kind != 0) continue;
+		int ga = W.bodyOff + row.a, gb = W.bodyOff + row.b;
+		double nx = row.arb.nx, ny = row.arb.ny, u = row.arb.u;
+		for(int c = 0; c < row.count && c < 2; c++){
+			const cpgRowContact &rc = row.arb.c[c];
+			double v1x = s.vx[ga] + (-rc.r1y)*s.w[ga], v1y = s.vy[ga] + rc.r1x*s.w[ga];
+			double v2x = s.vx[gb] + (-rc.r2y)*s.w[gb], v2y = s.vy[gb] + rc.r2x*s.w[gb];
+			double vrx = (v2x - v1x) + row.arb.svx, vry = (v2y - v1y) + row.arb.svy;
+			double vn = vrx*nx + vry*ny, vt = vrx*(-ny) + vry*nx;
+			double rn = vn + rc.bounce;
+			double resn = rc.jnAcc > 0.0 ? fabs(rn) : fmax(0.0, -rn);
+			double rest = fabs(rc.jtAcc) < u*rc.jnAcc ? fabs(vt) : fmax(0.0, rc.jtAcc > 0.0 ? vt : (rc.jtAcc < 0.0 ? -vt : 0.0));
+			double dx = (rc.r2x - rc.r1x) + (s.px[gb] - s.px[ga]), dy = (rc.r2y - rc.r1y) + (s.py[gb] - s.py[ga]);
+			double b1x = s.vbx[ga] + (-rc.r1y)*s.wb[ga], b1y = s.vby[ga] + rc.r1x*s.wb[ga];
+			double b2x = s.vbx[gb] + (-rc.r2y)*s.wb[gb], b2y = s.vby[gb] + rc.r2x*s.wb[gb];
+			double vbn = (b2x - b1x)*nx + (b2y - b1y)*ny;
+			double d = (dx*nx + dy*ny) + dt*(((v2x - v1x)*nx + (v2y - v1y)*ny) + vbn);
+			sn += resn*resn; stt += rest*rest; cnt += 1.0;
+			pen = fmax(pen, -d);
+		}
+	}
+	for(int o = 16; o > 0; o >>= 1){
+		sn += __shfl_down_sync(0xffffffffu, sn, o);
+		stt += __shfl_down_sync(0xffffffffu, stt, o);
+		cnt += __shfl_down_sync(0xffffffffu, cnt, o);
+		pen = fmax(pen, __shfl_down_sync(0xffffffffu, pen, o));
+	}
+	if((threadIdx.x & 31) == 0 && cnt > 0.0){
+		atomicAdd(&acc[0], sn); atomicAdd(&acc[1], stt); atomicAdd(&acc[2], cnt);
+		atomicMax((unsigned long long *)&acc[3], (unsigned long long)__double_as_longlong(fmax(pen, 0.0)));
+	}
+}
+
+extern "C" int cpg_launch_contact_quality(const cpgSet *s, int w, double dt, double *acc, void *stream)
+{
+	cudaStream_t st = (cudaStream_t)stream;
+	cudaMemsetAsync(acc, 0, 4*sizeof(double), st);
+	LAUNCH(k_contact_quality<<<152*2, 256, 0, st>>>(*s, w, dt, acc));
 	return cudaGetLastError() == cudaSuccess ? 0 : -1;
 }
 

@@ -34,6 +34,8 @@
  *      segment, density 1, u 0.7, e 0.1.
  *   6  joints and filters: pin-joint chains, slide-joint pairs and ropes,
  *      filtered free bodies (build_joints below).
+ *   7  machines: motors, gears, ratchets, rotary springs and limits,
+ *      grooves and damped springs (build_machines below).
  * Gravity is (0,-100); iterations are set per workload; the time step is
  * the caller's.
  */
@@ -503,6 +505,8 @@ static void build_joints(cpxScene *sc, int n, uint64_t seed)
 /* ---- exported harness entry points (cpx_ prefix: workload plumbing, not
  * part of the Chipmunk2D API) ---- */
 
+static void build_machines(cpxScene *sc, int n, uint64_t seed);
+
 void *cpx_scene_build(int config, int size, unsigned long long seed)
 {
 	cpxScene *sc = (cpxScene *)calloc(1, sizeof(cpxScene));
@@ -515,9 +519,89 @@ void *cpx_scene_build(int config, int size, unsigned long long seed)
 		case 4: build_tumble(sc, size > 0 ? size : 121, seed); cpSpaceSetIterations(sc->space, 10); break;
 		case 5: build_adjoint(sc, size > 0 ? size : 64, seed); cpSpaceSetIterations(sc->space, 10); break;
 		case 6: build_joints(sc, size > 0 ? size : 400, seed); cpSpaceSetIterations(sc->space, 10); break;
+		case 7: build_machines(sc, size > 0 ? size : 40, seed); cpSpaceSetIterations(sc->space, 10); break;
 		default: cpSpaceFree(sc->space); free(sc); return NULL;
 	}
 	return sc;
+}
+
+/* Workload 7, machines: `size` [40] mechanisms on a grid, each built from
+ * the remaining joints, with debris falling on them:
+ *   - wheel W1 (circle r 2) on a pivot to the static body at its centre,
+ *     driven by a simple motor (rate +-U[1,4]; maxForce 5e4 on odd
+ *     mechanisms);
+ *   - wheel W2 (circle r 1.5) on a pivot, geared to W1 (ratio U[0.5,2],
+ *     phase 0) and held by a ratchet to the static body (ratchet 0.4);
+ *   - bar B (8 x 1 box) on a pivot at one end, tied to W2 by a damped
+ *     rotary spring (rest angle 0.3, stiffness 3000, damping 60) and to the
+ *     static body by a rotary limit (-0.6, 0.9);
+ *   - slider S (circle r 1) in a groove along B (x in [-3.5, 3.5] of B);
+ *   - weight M (2 x 2 box) hanging from S by a damped spring (rest 5,
+ *     stiffness 200, damping 8).
+ * A mechanism's shapes share a filter group.  size/2 debris circles
+ * r~U[0.5,1.5] fall from above with v~N(0,5)/axis; a ground segment and
+ * side walls close the scene.  Friction 0.7, elasticity 0.1, density 1
+ * except where masses are given. */
+static void build_machines(cpxScene *sc, int n, uint64_t seed)
+{
+	Rng rng; rng_seed(&rng, seed);
+	cpSpace *sp = sc->space;
+	cpBody *ground = cpSpaceGetStaticBody(sp);
+	int cols = (int)sqrt((double)n) + 1;
+	double cell = 24.0;
+	double half = 0.5*cell*(double)cols + 10.0;
+	int rows = (n + cols - 1)/cols;
+	double top = cell*(double)rows + 20.0;
+	add_wall(sc, cpv(-half, 0.0), cpv(half, 0.0), 1.0, 0.7, 0.1);
+	add_wall(sc, cpv(-half, 0.0), cpv(-half, top + 40.0), 1.0, 0.7, 0.1);
+	add_wall(sc, cpv(half, 0.0), cpv(half, top + 40.0), 1.0, 0.7, 0.1);
+	for(int i = 0; i < n; i++){
+		double cx = -half + 10.0 + cell*((double)(i % cols) + 0.5);
+		double cy = 12.0 + cell*(double)(i/cols);
+		cpShapeFilter f = { (cpGroup)(uintptr_t)(1000 + i), CP_ALL_CATEGORIES, CP_ALL_CATEGORIES };
+		cpShape *s;
+		/* W1 */
+		double m1 = 3.14159265358979323846*4.0;
+		cpBody *w1 = add_body(sc, cpBodyNew(m1, cpMomentForCircle(m1, 0.0, 2.0, cpvzero)));
+		cpBodySetPosition(w1, cpv(cx - 6.0, cy));
+		s = add_shape(sc, cpCircleShapeNew(w1, 2.0, cpvzero)); cpShapeSetFriction(s, 0.7); cpShapeSetElasticity(s, 0.1); cpShapeSetFilter(s, f);
+		add_constraint(sc, cpPivotJointNew(ground, w1, cpv(cx - 6.0, cy)));
+		double rate = rng_uniform(&rng, 1.0, 4.0)*((i & 2) ? -1.0 : 1.0);
+		cpConstraint *motor = add_constraint(sc, cpSimpleMotorNew(ground, w1, rate));
+		if(i & 1) cpConstraintSetMaxForce(motor, 5e4);
+		/* W2 */
+		double m2 = 3.14159265358979323846*2.25;
+		cpBody *w2 = add_body(sc, cpBodyNew(m2, cpMomentForCircle(m2, 0.0, 1.5, cpvzero)));
+		cpBodySetPosition(w2, cpv(cx - 2.0, cy));
+		s = add_shape(sc, cpCircleShapeNew(w2, 1.5, cpvzero)); cpShapeSetFriction(s, 0.7); cpShapeSetElasticity(s, 0.1); cpShapeSetFilter(s, f);
+		add_constraint(sc, cpPivotJointNew(ground, w2, cpv(cx - 2.0, cy)));
+		add_constraint(sc, cpGearJointNew(w1, w2, 0.0, rng_uniform(&rng, 0.5, 2.0)));
+		add_constraint(sc, cpRatchetJointNew(ground, w2, 0.0, 0.4));
+		/* B */
+		cpBody *bar = add_body(sc, cpBodyNew(8.0, cpMomentForBox(8.0, 8.0, 1.0)));
+		cpBodySetPosition(bar, cpv(cx + 4.0, cy + 2.0));
+		s = add_shape(sc, cpBoxShapeNew(bar, 8.0, 1.0, 0.0)); cpShapeSetFriction(s, 0.7); cpShapeSetElasticity(s, 0.1); cpShapeSetFilter(s, f);
+		add_constraint(sc, cpPivotJointNew(ground, bar, cpv(cx, cy + 2.0)));
+		add_constraint(sc, cpDampedRotarySpringNew(w2, bar, 0.3, 3000.0, 60.0));
+		add_constraint(sc, cpRotaryLimitJointNew(ground, bar, -0.6, 0.9));
+		/* S */
+		double ms = 3.14159265358979323846;
+		cpBody *sl = add_body(sc, cpBodyNew(ms, cpMomentForCircle(ms, 0.0, 1.0, cpvzero)));
+		cpBodySetPosition(sl, cpv(cx + 4.0 + rng_uniform(&rng, -3.0, 3.0), cy + 2.0));
+		s = add_shape(sc, cpCircleShapeNew(sl, 1.0, cpvzero)); cpShapeSetFriction(s, 0.7); cpShapeSetElasticity(s, 0.1); cpShapeSetFilter(s, f);
+		add_constraint(sc, cpGrooveJointNew(bar, sl, cpv(-3.5, 0.0), cpv(3.5, 0.0), cpvzero));
+		/* M */
+		cpBody *wt = add_body(sc, cpBodyNew(4.0, cpMomentForBox(4.0, 2.0, 2.0)));
+		cpVect sp0 = cpBodyGetPosition(sl);
+		cpBodySetPosition(wt, cpv(sp0.x, sp0.y - 5.0));
+		s = add_shape(sc, cpBoxShapeNew(wt, 2.0, 2.0, 0.0)); cpShapeSetFriction(s, 0.7); cpShapeSetElasticity(s, 0.1); cpShapeSetFilter(s, f);
+		add_constraint(sc, cpDampedSpringNew(sl, wt, cpvzero, cpvzero, 5.0, 200.0, 8.0));
+	}
+	for(int i = 0; i < n/2; i++){
+		cpVect p = rng_point(&rng, -half + 3.0, half - 3.0, top, top + 30.0);
+		cpVect v = rng_normal2(&rng, 5.0);
+		add_circle(sc, p, v, rng_uniform(&rng, 0.5, 1.5), 0.7, 0.1);
+	}
 }
 
 /* Whether one of b's shapes is within `margin` of a static shape's box.

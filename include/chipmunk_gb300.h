@@ -155,6 +155,8 @@ static inline cpFloat cpvdot(const cpVect a, const cpVect b) { return a.x*b.x + 
 static inline cpFloat cpvcross(const cpVect a, const cpVect b) { return a.x*b.y - a.y*b.x; }
 static inline cpVect cpvperp(const cpVect a) { return cpv(-a.y, a.x); }
 static inline cpVect cpvrperp(const cpVect a) { return cpv(a.y, -a.x); }
+/* cpVect.h:98-101 */
+static inline cpVect cpvproject(const cpVect v1, const cpVect v2) { return cpvmult(v2, cpvdot(v1, v2)/cpvdot(v2, v2)); }
 static inline cpVect cpvrotate(const cpVect a, const cpVect b) { return cpv(a.x*b.x - a.y*b.y, a.x*b.y + a.y*b.x); }
 static inline cpVect cpvunrotate(const cpVect a, const cpVect b) { return cpv(a.x*b.x + a.y*b.y, a.y*b.x - a.x*b.y); }
 static inline cpFloat cpvlengthsq(const cpVect a) { return cpvdot(a, a); }
@@ -390,6 +392,70 @@ void cpSlideJointSetAnchorB(cpConstraint *constraint, cpVect anchorB);       /* 
 void cpSlideJointSetMin(cpConstraint *constraint, cpFloat min);              /* cpSlideJoint.h:48 */
 void cpSlideJointSetMax(cpConstraint *constraint, cpFloat max);              /* cpSlideJoint.h:53 */
 
+/* The remaining joints: cpGrooveJoint.h, cpDampedSpring.h,
+ * cpDampedRotarySpring.h, cpRotaryLimitJoint.h, cpRatchetJoint.h,
+ * cpGearJoint.h, cpSimpleMotor.h.  A space whose spring uses a force or
+ * torque function other than the default is refused at the step
+ * (CP_GPU_ERR_UNSUPPORTED): callbacks are host code. */
+typedef cpFloat (*cpDampedSpringForceFunc)(cpConstraint *spring, cpFloat dist);                 /* cpDampedSpring.h:29 */
+typedef cpFloat (*cpDampedRotarySpringTorqueFunc)(cpConstraint *spring, cpFloat relativeAngle); /* cpDampedRotarySpring.h:29 */
+cpBool cpConstraintIsGrooveJoint(const cpConstraint *constraint);            /* cpGrooveJoint.h:26 */
+cpConstraint *cpGrooveJointNew(cpBody *a, cpBody *b, cpVect groove_a, cpVect groove_b, cpVect anchorB); /* cpGrooveJoint.h:33 */
+cpVect cpGrooveJointGetGrooveA(const cpConstraint *constraint);              /* cpGrooveJoint.h:36 */
+void cpGrooveJointSetGrooveA(cpConstraint *constraint, cpVect grooveA);      /* cpGrooveJoint.h:38 */
+cpVect cpGrooveJointGetGrooveB(const cpConstraint *constraint);              /* cpGrooveJoint.h:41 */
+void cpGrooveJointSetGrooveB(cpConstraint *constraint, cpVect grooveB);      /* cpGrooveJoint.h:43 */
+cpVect cpGrooveJointGetAnchorB(const cpConstraint *constraint);              /* cpGrooveJoint.h:46 */
+void cpGrooveJointSetAnchorB(cpConstraint *constraint, cpVect anchorB);      /* cpGrooveJoint.h:48 */
+cpBool cpConstraintIsDampedSpring(const cpConstraint *constraint);           /* cpDampedSpring.h:26 */
+cpConstraint *cpDampedSpringNew(cpBody *a, cpBody *b, cpVect anchorA, cpVect anchorB, cpFloat restLength, cpFloat stiffness, cpFloat damping); /* cpDampedSpring.h:36 */
+cpVect cpDampedSpringGetAnchorA(const cpConstraint *constraint);             /* cpDampedSpring.h:39 */
+void cpDampedSpringSetAnchorA(cpConstraint *constraint, cpVect anchorA);     /* cpDampedSpring.h:41 */
+cpVect cpDampedSpringGetAnchorB(const cpConstraint *constraint);             /* cpDampedSpring.h:44 */
+void cpDampedSpringSetAnchorB(cpConstraint *constraint, cpVect anchorB);     /* cpDampedSpring.h:46 */
+cpFloat cpDampedSpringGetRestLength(const cpConstraint *constraint);         /* cpDampedSpring.h:49 */
+void cpDampedSpringSetRestLength(cpConstraint *constraint, cpFloat restLength); /* cpDampedSpring.h:51 */
+cpFloat cpDampedSpringGetStiffness(const cpConstraint *constraint);          /* cpDampedSpring.h:54 */
+void cpDampedSpringSetStiffness(cpConstraint *constraint, cpFloat stiffness); /* cpDampedSpring.h:56 */
+cpFloat cpDampedSpringGetDamping(const cpConstraint *constraint);            /* cpDampedSpring.h:59 */
+void cpDampedSpringSetDamping(cpConstraint *constraint, cpFloat damping);    /* cpDampedSpring.h:61 */
+cpDampedSpringForceFunc cpDampedSpringGetSpringForceFunc(const cpConstraint *constraint);               /* cpDampedSpring.h:64 */
+void cpDampedSpringSetSpringForceFunc(cpConstraint *constraint, cpDampedSpringForceFunc springForceFunc); /* cpDampedSpring.h:66 */
+cpBool cpConstraintIsDampedRotarySpring(const cpConstraint *constraint);     /* cpDampedRotarySpring.h:26 */
+cpConstraint *cpDampedRotarySpringNew(cpBody *a, cpBody *b, cpFloat restAngle, cpFloat stiffness, cpFloat damping); /* cpDampedRotarySpring.h:36 */
+cpFloat cpDampedRotarySpringGetRestAngle(const cpConstraint *constraint);    /* cpDampedRotarySpring.h:39 */
+void cpDampedRotarySpringSetRestAngle(cpConstraint *constraint, cpFloat restAngle); /* cpDampedRotarySpring.h:41 */
+cpFloat cpDampedRotarySpringGetStiffness(const cpConstraint *constraint);    /* cpDampedRotarySpring.h:44 */
+void cpDampedRotarySpringSetStiffness(cpConstraint *constraint, cpFloat stiffness); /* cpDampedRotarySpring.h:46 */
+cpFloat cpDampedRotarySpringGetDamping(const cpConstraint *constraint);      /* cpDampedRotarySpring.h:49 */
+void cpDampedRotarySpringSetDamping(cpConstraint *constraint, cpFloat damping); /* cpDampedRotarySpring.h:51 */
+cpDampedRotarySpringTorqueFunc cpDampedRotarySpringGetSpringTorqueFunc(const cpConstraint *constraint);                /* cpDampedRotarySpring.h:54 */
+void cpDampedRotarySpringSetSpringTorqueFunc(cpConstraint *constraint, cpDampedRotarySpringTorqueFunc springTorqueFunc); /* cpDampedRotarySpring.h:56 */
+cpBool cpConstraintIsRotaryLimitJoint(const cpConstraint *constraint);       /* cpRotaryLimitJoint.h:26 */
+cpConstraint *cpRotaryLimitJointNew(cpBody *a, cpBody *b, cpFloat min, cpFloat max); /* cpRotaryLimitJoint.h:33 */
+cpFloat cpRotaryLimitJointGetMin(const cpConstraint *constraint);            /* cpRotaryLimitJoint.h:36 */
+void cpRotaryLimitJointSetMin(cpConstraint *constraint, cpFloat min);        /* cpRotaryLimitJoint.h:38 */
+cpFloat cpRotaryLimitJointGetMax(const cpConstraint *constraint);            /* cpRotaryLimitJoint.h:41 */
+void cpRotaryLimitJointSetMax(cpConstraint *constraint, cpFloat max);        /* cpRotaryLimitJoint.h:43 */
+cpBool cpConstraintIsRatchetJoint(const cpConstraint *constraint);           /* cpRatchetJoint.h:26 */
+cpConstraint *cpRatchetJointNew(cpBody *a, cpBody *b, cpFloat phase, cpFloat ratchet); /* cpRatchetJoint.h:33 */
+cpFloat cpRatchetJointGetAngle(const cpConstraint *constraint);              /* cpRatchetJoint.h:36 */
+void cpRatchetJointSetAngle(cpConstraint *constraint, cpFloat angle);        /* cpRatchetJoint.h:38 */
+cpFloat cpRatchetJointGetPhase(const cpConstraint *constraint);              /* cpRatchetJoint.h:41 */
+void cpRatchetJointSetPhase(cpConstraint *constraint, cpFloat phase);        /* cpRatchetJoint.h:43 */
+cpFloat cpRatchetJointGetRatchet(const cpConstraint *constraint);            /* cpRatchetJoint.h:46 */
+void cpRatchetJointSetRatchet(cpConstraint *constraint, cpFloat ratchet);    /* cpRatchetJoint.h:48 */
+cpBool cpConstraintIsGearJoint(const cpConstraint *constraint);              /* cpGearJoint.h:26 */
+cpConstraint *cpGearJointNew(cpBody *a, cpBody *b, cpFloat phase, cpFloat ratio); /* cpGearJoint.h:33 */
+cpFloat cpGearJointGetPhase(const cpConstraint *constraint);                 /* cpGearJoint.h:36 */
+void cpGearJointSetPhase(cpConstraint *constraint, cpFloat phase);           /* cpGearJoint.h:38 */
+cpFloat cpGearJointGetRatio(const cpConstraint *constraint);                 /* cpGearJoint.h:41 */
+void cpGearJointSetRatio(cpConstraint *constraint, cpFloat ratio);           /* cpGearJoint.h:43 */
+cpBool cpConstraintIsSimpleMotor(const cpConstraint *constraint);            /* cpSimpleMotor.h:29 */
+cpConstraint *cpSimpleMotorNew(cpBody *a, cpBody *b, cpFloat rate);          /* cpSimpleMotor.h:36 */
+cpFloat cpSimpleMotorGetRate(const cpConstraint *constraint);                /* cpSimpleMotor.h:39 */
+void cpSimpleMotorSetRate(cpConstraint *constraint, cpFloat rate);           /* cpSimpleMotor.h:41 */
+
 /* ------------------------------------------------------------------------
  * Arbiters: cpArbiter.h:32-119.  Arbiter handles are valid from the
  * cpBodyEachArbiter callback until the next cpSpaceStep, as in the reference.
@@ -465,6 +531,20 @@ int cpGpuBatchStep(cpGpuBatch *batch, cpFloat dt, int steps, int use_graph);
 int cpGpuBatchGetTuning(cpGpuBatch *batch, int *out);
 /* 0 turns the online tuner off (defaults are used), 1 (default) on. */
 void cpGpuSetAutotune(int on);
+
+/* Solver quality (no reference counterpart): from the space's current
+ * state, the next step of time dt is run once per iteration count k = 1 ..
+ * maxIters with solver `mode` (CP_GPU_SOLVER_*), and after each run out[3k-3
+ * .. 3k-1] receive the RMS over all contacts of the normal residual
+ * (|vn + bounce| where the accumulated normal impulse is positive, else the
+ * approach speed), the RMS friction residual (|vt| inside the friction
+ * cone, else slip along the friction impulse) and the largest penetration
+ * (the deepest contact's overlap along its normal after the next position
+ * update, from the velocities and bias velocities the solve left).  The
+ * space's state is
+ * restored afterwards.  Needs a standalone space stepped at least once;
+ * returns 0 or -1 (with cpGpuGetLastError() set). */
+int cpGpuSolverQuality(cpSpace *space, int mode, cpFloat dt, int maxIters, double *out);
 
 /* Exact-order parallel schedule of a sequential sweep.  Unit u of the
  * sweep touches dynamic bodies bodyA[u] and bodyB[u] (a negative index or

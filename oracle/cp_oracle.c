@@ -72,7 +72,8 @@ static inline cpVect mat2_mul_(cpMat2x2 m, cpVect v) { return cpv(v.x*m.a + v.y*
  * Object layouts (oracle-private)
  * ====================================================================== */
 enum { SHAPE_CIRCLE = 0, SHAPE_SEGMENT = 1, SHAPE_POLY = 2 };
-enum { JOINT_PIVOT = 1, JOINT_PIN = 2, JOINT_SLIDE = 3 };
+enum { JOINT_PIVOT = 1, JOINT_PIN = 2, JOINT_SLIDE = 3, JOINT_GROOVE = 4, JOINT_DSPRING = 5, JOINT_DRSPRING = 6,
+       JOINT_ROTLIMIT = 7, JOINT_RATCHET = 8, JOINT_GEAR = 9, JOINT_MOTOR = 10 };
 enum { ARB_FIRST = 0, ARB_NORMAL = 1, ARB_IGNORE = 2, ARB_CACHED = 3, ARB_INVALID = 4 };
 
 typedef struct Contact {
@@ -153,8 +154,18 @@ struct cpConstraint {
 	cpVect r1, r2;
 	cpMat2x2 k;                 /* pivot */
 	cpVect jAcc, biasv;         /* pivot */
-	cpVect n;                   /* pin, slide */
-	cpFloat nMass, jnAcc, bias; /* pin, slide */
+	cpVect n;                   /* pin, slide, damped spring */
+	cpFloat nMass, jnAcc, bias; /* pin, slide; jnAcc is the scalar jAcc of the other kinds */
+	/* groove (chipmunk_structs.h:307-318) */
+	cpVect grv_n, grv_a, grv_b, grv_tn;
+	cpFloat clamp;
+	/* springs (chipmunk_structs.h:320-345) */
+	cpFloat restLength, stiffness, damping, target_vrn, v_coef;
+	cpFloat restAngle, target_wrn, w_coef;
+	cpDampedSpringForceFunc springForceFunc;
+	cpDampedRotarySpringTorqueFunc springTorqueFunc;
+	/* rotary limit, ratchet, gear, motor (chipmunk_structs.h:347-385) */
+	cpFloat iSum, angle, phase, ratchet, ratio, ratio_inv, rate;
 };
 
 /* ---- AABB tree: index-based nodes and pairs (src/cpBBTree.c:32-72) ---- */
@@ -861,6 +872,127 @@ cpConstraint *cpSlideJointNew(cpBody *a, cpBody *b, cpVect anchorA, cpVect ancho
 	return c;
 }
 
+/* cpGrooveJoint.c:119-132 */
+cpConstraint *cpGrooveJointNew(cpBody *a, cpBody *b, cpVect groove_a, cpVect groove_b, cpVect anchorB)
+{
+	cpConstraint *c = constraint_new(JOINT_GROOVE, a, b);
+	c->grv_a = groove_a; c->grv_b = groove_b;
+	c->grv_n = cpvperp(cpvnormalize(cpvsub(groove_b, groove_a)));
+	c->anchorB = anchorB;
+	c->jAcc = cpvzero;
+	return c;
+}
+
+/* cpDampedSpring.c:24-27 (default force), 124-140 */
+static cpFloat default_spring_force(cpConstraint *c, cpFloat dist) { return (c->restLength - dist)*c->stiffness; }
+cpConstraint *cpDampedSpringNew(cpBody *a, cpBody *b, cpVect anchorA, cpVect anchorB, cpFloat restLength, cpFloat stiffness, cpFloat damping)
+{
+	cpConstraint *c = constraint_new(JOINT_DSPRING, a, b);
+	c->anchorA = anchorA; c->anchorB = anchorB;
+	c->restLength = restLength; c->stiffness = stiffness; c->damping = damping;
+	c->springForceFunc = default_spring_force;
+	c->jnAcc = 0.0;
+	return c;
+}
+
+/* cpDampedRotarySpring.c:24-27 (default torque), 100-115 */
+static cpFloat default_spring_torque(cpConstraint *c, cpFloat relativeAngle) { return (relativeAngle - c->restAngle)*c->stiffness; }
+cpConstraint *cpDampedRotarySpringNew(cpBody *a, cpBody *b, cpFloat restAngle, cpFloat stiffness, cpFloat damping)
+{
+	cpConstraint *c = constraint_new(JOINT_DRSPRING, a, b);
+	c->restAngle = restAngle; c->stiffness = stiffness; c->damping = damping;
+	c->springTorqueFunc = default_spring_torque;
+	c->jnAcc = 0.0;
+	return c;
+}
+
+/* cpRotaryLimitJoint.c:108-119 */
+cpConstraint *cpRotaryLimitJointNew(cpBody *a, cpBody *b, cpFloat min, cpFloat max)
+{
+	cpConstraint *c = constraint_new(JOINT_ROTLIMIT, a, b);
+	c->min = min; c->max = max;
+	c->jnAcc = 0.0;
+	return c;
+}
+
+/* cpRatchetJoint.c:111-123 */
+cpConstraint *cpRatchetJointNew(cpBody *a, cpBody *b, cpFloat phase, cpFloat ratchet)
+{
+	cpConstraint *c = constraint_new(JOINT_RATCHET, a, b);
+	c->angle = 0.0;
+	c->phase = phase; c->ratchet = ratchet;
+	c->angle = (b ? b->a : 0.0) - (a ? a->a : 0.0);
+	return c;
+}
+
+/* cpGearJoint.c:91-102 */
+cpConstraint *cpGearJointNew(cpBody *a, cpBody *b, cpFloat phase, cpFloat ratio)
+{
+	cpConstraint *c = constraint_new(JOINT_GEAR, a, b);
+	c->phase = phase; c->ratio = ratio; c->ratio_inv = 1.0/ratio;
+	c->jnAcc = 0.0;
+	return c;
+}
+
+/* cpSimpleMotor.c:87-96 */
+cpConstraint *cpSimpleMotorNew(cpBody *a, cpBody *b, cpFloat rate)
+{
+	cpConstraint *c = constraint_new(JOINT_MOTOR, a, b);
+	c->rate = rate;
+	c->jnAcc = 0.0;
+	return c;
+}
+
+cpBool cpConstraintIsGrooveJoint(const cpConstraint *c) { return c->kind == JOINT_GROOVE; }
+cpBool cpConstraintIsDampedSpring(const cpConstraint *c) { return c->kind == JOINT_DSPRING; }
+cpBool cpConstraintIsDampedRotarySpring(const cpConstraint *c) { return c->kind == JOINT_DRSPRING; }
+cpBool cpConstraintIsRotaryLimitJoint(const cpConstraint *c) { return c->kind == JOINT_ROTLIMIT; }
+cpBool cpConstraintIsRatchetJoint(const cpConstraint *c) { return c->kind == JOINT_RATCHET; }
+cpBool cpConstraintIsGearJoint(const cpConstraint *c) { return c->kind == JOINT_GEAR; }
+cpBool cpConstraintIsSimpleMotor(const cpConstraint *c) { return c->kind == JOINT_MOTOR; }
+cpVect cpGrooveJointGetGrooveA(const cpConstraint *c) { return c->grv_a; }
+void cpGrooveJointSetGrooveA(cpConstraint *c, cpVect v) { c->grv_a = v; c->grv_n = cpvperp(cpvnormalize(cpvsub(c->grv_b, v))); }
+cpVect cpGrooveJointGetGrooveB(const cpConstraint *c) { return c->grv_b; }
+void cpGrooveJointSetGrooveB(cpConstraint *c, cpVect v) { c->grv_b = v; c->grv_n = cpvperp(cpvnormalize(cpvsub(v, c->grv_a))); }
+cpVect cpGrooveJointGetAnchorB(const cpConstraint *c) { return c->anchorB; }
+void cpGrooveJointSetAnchorB(cpConstraint *c, cpVect v) { c->anchorB = v; }
+cpVect cpDampedSpringGetAnchorA(const cpConstraint *c) { return c->anchorA; }
+void cpDampedSpringSetAnchorA(cpConstraint *c, cpVect v) { c->anchorA = v; }
+cpVect cpDampedSpringGetAnchorB(const cpConstraint *c) { return c->anchorB; }
+void cpDampedSpringSetAnchorB(cpConstraint *c, cpVect v) { c->anchorB = v; }
+cpFloat cpDampedSpringGetRestLength(const cpConstraint *c) { return c->restLength; }
+void cpDampedSpringSetRestLength(cpConstraint *c, cpFloat v) { c->restLength = v; }
+cpFloat cpDampedSpringGetStiffness(const cpConstraint *c) { return c->stiffness; }
+void cpDampedSpringSetStiffness(cpConstraint *c, cpFloat v) { c->stiffness = v; }
+cpFloat cpDampedSpringGetDamping(const cpConstraint *c) { return c->damping; }
+void cpDampedSpringSetDamping(cpConstraint *c, cpFloat v) { c->damping = v; }
+cpDampedSpringForceFunc cpDampedSpringGetSpringForceFunc(const cpConstraint *c) { return c->springForceFunc; }
+void cpDampedSpringSetSpringForceFunc(cpConstraint *c, cpDampedSpringForceFunc f) { c->springForceFunc = f; }
+cpFloat cpDampedRotarySpringGetRestAngle(const cpConstraint *c) { return c->restAngle; }
+void cpDampedRotarySpringSetRestAngle(cpConstraint *c, cpFloat v) { c->restAngle = v; }
+cpFloat cpDampedRotarySpringGetStiffness(const cpConstraint *c) { return c->stiffness; }
+void cpDampedRotarySpringSetStiffness(cpConstraint *c, cpFloat v) { c->stiffness = v; }
+cpFloat cpDampedRotarySpringGetDamping(const cpConstraint *c) { return c->damping; }
+void cpDampedRotarySpringSetDamping(cpConstraint *c, cpFloat v) { c->damping = v; }
+cpDampedRotarySpringTorqueFunc cpDampedRotarySpringGetSpringTorqueFunc(const cpConstraint *c) { return c->springTorqueFunc; }
+void cpDampedRotarySpringSetSpringTorqueFunc(cpConstraint *c, cpDampedRotarySpringTorqueFunc f) { c->springTorqueFunc = f; }
+cpFloat cpRotaryLimitJointGetMin(const cpConstraint *c) { return c->min; }
+void cpRotaryLimitJointSetMin(cpConstraint *c, cpFloat v) { c->min = v; }
+cpFloat cpRotaryLimitJointGetMax(const cpConstraint *c) { return c->max; }
+void cpRotaryLimitJointSetMax(cpConstraint *c, cpFloat v) { c->max = v; }
+cpFloat cpRatchetJointGetAngle(const cpConstraint *c) { return c->angle; }
+void cpRatchetJointSetAngle(cpConstraint *c, cpFloat v) { c->angle = v; }
+cpFloat cpRatchetJointGetPhase(const cpConstraint *c) { return c->phase; }
+void cpRatchetJointSetPhase(cpConstraint *c, cpFloat v) { c->phase = v; }
+cpFloat cpRatchetJointGetRatchet(const cpConstraint *c) { return c->ratchet; }
+void cpRatchetJointSetRatchet(cpConstraint *c, cpFloat v) { c->ratchet = v; }
+cpFloat cpGearJointGetPhase(const cpConstraint *c) { return c->phase; }
+void cpGearJointSetPhase(cpConstraint *c, cpFloat v) { c->phase = v; }
+cpFloat cpGearJointGetRatio(const cpConstraint *c) { return c->ratio; }
+void cpGearJointSetRatio(cpConstraint *c, cpFloat v) { c->ratio = v; c->ratio_inv = 1.0/v; }
+cpFloat cpSimpleMotorGetRate(const cpConstraint *c) { return c->rate; }
+void cpSimpleMotorSetRate(cpConstraint *c, cpFloat v) { c->rate = v; }
+
 void cpConstraintFree(cpConstraint *c) { free(c); }
 cpSpace *cpConstraintGetSpace(const cpConstraint *c) { return c->space; }
 cpBody *cpConstraintGetBodyA(const cpConstraint *c) { return c->a; }
@@ -893,12 +1025,104 @@ cpFloat cpSlideJointGetMax(const cpConstraint *c) { return c->max; }
 cpFloat cpConstraintGetImpulse(cpConstraint *c)
 {
 	switch(c->kind){
-		case JOINT_PIVOT: return cpvlength(c->jAcc);
+		case JOINT_PIVOT: case JOINT_GROOVE: return cpvlength(c->jAcc);
+		case JOINT_DSPRING: case JOINT_DRSPRING: return c->jnAcc;
 		default: return fabs_(c->jnAcc);
 	}
 }
 
 static inline cpFloat bias_coef_(cpFloat errorBias, cpFloat dt) { return 1.0 - pow(errorBias, dt); }
+
+/* cpGrooveJoint.c:24-59, cpDampedSpring.c:29-53, cpDampedRotarySpring.c:29-49,
+ * cpRotaryLimitJoint.c:24-46, cpRatchetJoint.c:24-52, cpGearJoint.c:24-35,
+ * cpSimpleMotor.c:24-31 (r1 and r2 of the groove and spring are set by the
+ * caller only for the spring; the groove computes its own) */
+static void joint_prestep_more(cpConstraint *c, cpFloat dt)
+{
+	cpBody *a = c->a, *b = c->b;
+	switch(c->kind){
+	case JOINT_GROOVE: {
+		cpVect ta = cpTransformPoint(a->transform, c->grv_a);
+		cpVect tb = cpTransformPoint(a->transform, c->grv_b);
+		cpVect n = cpTransformVect(a->transform, c->grv_n);
+		cpFloat d = cpvdot(ta, n);
+		c->grv_tn = n;
+		c->r2 = cpTransformVect(b->transform, cpvsub(c->anchorB, b->cog));
+		cpFloat td = cpvcross(cpvadd(b->p, c->r2), n);
+		if(td <= cpvcross(ta, n)){
+			c->clamp = 1.0;
+			c->r1 = cpvsub(ta, a->p);
+		} else if(td >= cpvcross(tb, n)){
+			c->clamp = -1.0;
+			c->r1 = cpvsub(tb, a->p);
+		} else {
+			c->clamp = 0.0;
+			c->r1 = cpvsub(cpvadd(cpvmult(cpvperp(n), -td), cpvmult(n, d)), a->p);
+		}
+		c->k = k_tensor_(a, b, c->r1, c->r2);
+		cpVect delta = cpvsub(cpvadd(b->p, c->r2), cpvadd(a->p, c->r1));
+		c->biasv = vclamp_(cpvmult(delta, -bias_coef_(c->errorBias, dt)/dt), c->maxBias);
+		break;
+	}
+	case JOINT_DSPRING: {
+		cpVect delta = cpvsub(cpvadd(b->p, c->r2), cpvadd(a->p, c->r1));
+		cpFloat dist = cpvlength(delta);
+		c->n = cpvmult(delta, 1.0/(dist ? dist : ORC_INF));
+		cpFloat k = k_scalar_(a, b, c->r1, c->r2, c->n);
+		c->nMass = 1.0/k;
+		c->target_vrn = 0.0;
+		c->v_coef = 1.0 - exp(-c->damping*dt*k);
+		cpFloat f_spring = c->springForceFunc(c, dist);
+		cpFloat j_spring = c->jnAcc = f_spring*dt;
+		apply_impulses_(a, b, c->r1, c->r2, cpvmult(c->n, j_spring));
+		break;
+	}
+	case JOINT_DRSPRING: {
+		cpFloat moment = a->i_inv + b->i_inv;
+		c->iSum = 1.0/moment;
+		c->w_coef = 1.0 - exp(-c->damping*dt*moment);
+		c->target_wrn = 0.0;
+		cpFloat j_spring = c->springTorqueFunc(c, a->a - b->a)*dt;
+		c->jnAcc = j_spring;
+		a->w -= j_spring*a->i_inv;
+		b->w += j_spring*b->i_inv;
+		break;
+	}
+	case JOINT_ROTLIMIT: {
+		cpFloat dist = b->a - a->a;
+		cpFloat pdist = 0.0;
+		if(dist > c->max) pdist = c->max - dist;
+		else if(dist < c->min) pdist = c->min - dist;
+		c->iSum = 1.0/(a->i_inv + b->i_inv);
+		cpFloat maxBias = c->maxBias;
+		c->bias = fclamp_(-bias_coef_(c->errorBias, dt)*pdist/dt, -maxBias, maxBias);
+		if(!c->bias) c->jnAcc = 0.0;
+		break;
+	}
+	case JOINT_RATCHET: {
+		cpFloat angle = c->angle, phase = c->phase, ratchet = c->ratchet;
+		cpFloat delta = b->a - a->a;
+		cpFloat diff = angle - delta;
+		cpFloat pdist = 0.0;
+		if(diff*ratchet > 0.0) pdist = diff;
+		else c->angle = floor((delta - phase)/ratchet)*ratchet + phase;
+		c->iSum = 1.0/(a->i_inv + b->i_inv);
+		cpFloat maxBias = c->maxBias;
+		c->bias = fclamp_(-bias_coef_(c->errorBias, dt)*pdist/dt, -maxBias, maxBias);
+		if(!c->bias) c->jnAcc = 0.0;
+		break;
+	}
+	case JOINT_GEAR: {
+		c->iSum = 1.0/(a->i_inv*c->ratio_inv + c->ratio*b->i_inv);
+		cpFloat maxBias = c->maxBias;
+		c->bias = fclamp_(-bias_coef_(c->errorBias, dt)*(b->a*c->ratio - a->a - c->phase)/dt, -maxBias, maxBias);
+		break;
+	}
+	default: /* JOINT_MOTOR */
+		c->iSum = 1.0/(a->i_inv + b->i_inv);
+		break;
+	}
+}
 
 /* cpPivotJoint.c:24-39, cpPinJoint.c:24-46, cpSlideJoint.c:24-56 */
 static void joint_prestep(cpConstraint *c, cpFloat dt)
@@ -917,7 +1141,7 @@ static void joint_prestep(cpConstraint *c, cpFloat dt)
 		c->nMass = 1.0/k_scalar_(a, b, c->r1, c->r2, c->n);
 		cpFloat maxBias = c->maxBias;
 		c->bias = fclamp_(-bias_coef_(c->errorBias, dt)*(dist - c->dist)/dt, -maxBias, maxBias);
-	} else {
+	} else if(c->kind == JOINT_SLIDE){
 		cpVect delta = cpvsub(cpvadd(b->p, c->r2), cpvadd(a->p, c->r1));
 		cpFloat dist = cpvlength(delta);
 		cpFloat pdist = 0.0;
@@ -934,12 +1158,32 @@ static void joint_prestep(cpConstraint *c, cpFloat dt)
 		c->nMass = 1.0/k_scalar_(a, b, c->r1, c->r2, c->n);
 		cpFloat maxBias = c->maxBias;
 		c->bias = fclamp_(-bias_coef_(c->errorBias, dt)*pdist/dt, -maxBias, maxBias);
+	} else {
+		joint_prestep_more(c, dt);
 	}
 }
 
 static void joint_apply_cached(cpConstraint *c, cpFloat dt_coef)
 {
-	if(c->kind == JOINT_PIVOT){
+	cpBody *a = c->a, *b = c->b;
+	switch(c->kind){
+	case JOINT_DSPRING: case JOINT_DRSPRING:
+		return;      /* cpDampedSpring.c:55, cpDampedRotarySpring.c:51 */
+	case JOINT_ROTLIMIT: case JOINT_RATCHET: case JOINT_MOTOR: {
+		cpFloat j = c->jnAcc*dt_coef;
+		a->w -= j*a->i_inv;
+		b->w += j*b->i_inv;
+		return;
+	}
+	case JOINT_GEAR: {
+		cpFloat j = c->jnAcc*dt_coef;
+		a->w -= j*a->i_inv*c->ratio_inv;
+		b->w += j*b->i_inv;
+		return;
+	}
+	default: break;
+	}
+	if(c->kind == JOINT_PIVOT || c->kind == JOINT_GROOVE){
 		apply_impulses_(c->a, c->b, c->r1, c->r2, cpvmult(c->jAcc, dt_coef));
 	} else {
 		cpVect j = cpvmult(c->n, c->jnAcc*dt_coef);
@@ -967,6 +1211,74 @@ static void joint_apply(cpConstraint *c, cpFloat dt)
 		c->jnAcc = fclamp_(jnOld + jn, -jnMax, jnMax);
 		jn = c->jnAcc - jnOld;
 		apply_impulses_(a, b, c->r1, c->r2, cpvmult(n, jn));
+	} else if(c->kind == JOINT_GROOVE){
+		/* cpGrooveJoint.c:70-94 */
+		cpVect r1 = c->r1, r2 = c->r2;
+		cpVect vr = relative_velocity_(a, b, r1, r2);
+		cpVect j = mat2_mul_(c->k, cpvsub(c->biasv, vr));
+		cpVect jOld = c->jAcc;
+		cpVect jn = cpvadd(jOld, j);
+		cpVect tn = c->grv_tn;
+		cpVect jClamp = (c->clamp*cpvcross(jn, tn) > 0.0) ? jn : cpvproject(jn, tn);
+		c->jAcc = vclamp_(jClamp, c->maxForce*dt);
+		j = cpvsub(c->jAcc, jOld);
+		apply_impulses_(a, b, c->r1, c->r2, j);
+	} else if(c->kind == JOINT_DSPRING){
+		/* cpDampedSpring.c:57-77 */
+		cpVect n = c->n, r1 = c->r1, r2 = c->r2;
+		cpFloat vrn = cpvdot(relative_velocity_(a, b, r1, r2), n);
+		cpFloat v_damp = (c->target_vrn - vrn)*c->v_coef;
+		c->target_vrn = vrn + v_damp;
+		cpFloat j_damp = v_damp*c->nMass;
+		c->jnAcc += j_damp;
+		apply_impulses_(a, b, c->r1, c->r2, cpvmult(c->n, j_damp));
+	} else if(c->kind == JOINT_DRSPRING){
+		/* cpDampedRotarySpring.c:53-72 */
+		cpFloat wrn = a->w - b->w;
+		cpFloat w_damp = (c->target_wrn - wrn)*c->w_coef;
+		c->target_wrn = wrn + w_damp;
+		cpFloat j_damp = w_damp*c->iSum;
+		c->jnAcc += j_damp;
+		a->w += j_damp*a->i_inv;
+		b->w -= j_damp*b->i_inv;
+	} else if(c->kind == JOINT_ROTLIMIT || c->kind == JOINT_RATCHET){
+		/* cpRotaryLimitJoint.c:59-85, cpRatchetJoint.c:64-87 */
+		if(!c->bias) return;
+		cpFloat wr = b->w - a->w;
+		cpFloat jMax = c->maxForce*dt;
+		cpFloat j = -(c->bias + wr)*c->iSum;
+		cpFloat jOld = c->jnAcc;
+		if(c->kind == JOINT_RATCHET){
+			cpFloat ratchet = c->ratchet;
+			c->jnAcc = fclamp_((jOld + j)*ratchet, 0.0, jMax*fabs_(ratchet))/ratchet;
+		} else if(c->bias < 0.0){
+			c->jnAcc = fclamp_(jOld + j, 0.0, jMax);
+		} else {
+			c->jnAcc = fclamp_(jOld + j, -jMax, 0.0);
+		}
+		j = c->jnAcc - jOld;
+		a->w -= j*a->i_inv;
+		b->w += j*b->i_inv;
+	} else if(c->kind == JOINT_GEAR){
+		/* cpGearJoint.c:48-67 */
+		cpFloat wr = b->w*c->ratio - a->w;
+		cpFloat jMax = c->maxForce*dt;
+		cpFloat j = (c->bias - wr)*c->iSum;
+		cpFloat jOld = c->jnAcc;
+		c->jnAcc = fclamp_(jOld + j, -jMax, jMax);
+		j = c->jnAcc - jOld;
+		a->w -= j*a->i_inv*c->ratio_inv;
+		b->w += j*b->i_inv;
+	} else if(c->kind == JOINT_MOTOR){
+		/* cpSimpleMotor.c:43-61 */
+		cpFloat wr = b->w - a->w + c->rate;
+		cpFloat jMax = c->maxForce*dt;
+		cpFloat j = -wr*c->iSum;
+		cpFloat jOld = c->jnAcc;
+		c->jnAcc = fclamp_(jOld + j, -jMax, jMax);
+		j = c->jnAcc - jOld;
+		a->w -= j*a->i_inv;
+		b->w += j*b->i_inv;
 	} else {
 		if(cpveql(c->n, cpvzero)) return;
 		cpVect n = c->n, r1 = c->r1, r2 = c->r2;
@@ -2604,10 +2916,18 @@ int cpx_dump_constraints(cpSpace *sp, double *out, int max)
 	for(int i = 0; i < sp->ncons && i < max; i++){
 		cpConstraint *c = sp->cons[i];
 		double *o = out + 8*i;
+		memset(o, 0, 8*sizeof(double));
 		o[0] = (double)c->kind;
-		if(c->kind == JOINT_PIVOT){ o[1] = c->jAcc.x; o[2] = c->jAcc.y; o[7] = c->biasv.x; }
-		else { o[1] = c->jnAcc; o[2] = c->nMass; o[7] = c->bias; }
-		o[3] = c->r1.x; o[4] = c->r1.y; o[5] = c->r2.x; o[6] = c->r2.y;
+		switch(c->kind){
+		case JOINT_PIVOT: case JOINT_GROOVE: o[1] = c->jAcc.x; o[2] = c->jAcc.y; o[7] = c->biasv.x; break;
+		case JOINT_PIN: case JOINT_SLIDE: o[1] = c->jnAcc; o[2] = c->nMass; o[7] = c->bias; break;
+		case JOINT_DSPRING: o[1] = c->jnAcc; o[2] = c->nMass; o[7] = c->v_coef; break;
+		case JOINT_DRSPRING: o[1] = c->jnAcc; o[2] = c->iSum; o[3] = c->w_coef; o[7] = c->target_wrn; break;
+		case JOINT_RATCHET: o[1] = c->jnAcc; o[2] = c->iSum; o[3] = c->angle; o[7] = c->bias; break;
+		case JOINT_ROTLIMIT: case JOINT_GEAR: o[1] = c->jnAcc; o[2] = c->iSum; o[7] = c->bias; break;
+		default: o[1] = c->jnAcc; o[2] = c->iSum; break;
+		}
+		if(c->kind <= JOINT_DSPRING){ o[3] = c->r1.x; o[4] = c->r1.y; o[5] = c->r2.x; o[6] = c->r2.y; }
 	}
 	return sp->ncons;
 }

@@ -86,6 +86,29 @@ int cpx_dump_constraints(cpSpace *space, double *out, int max)
 			cpSlideJoint *j = (cpSlideJoint *)c;
 			o[0] = KIND_SLIDE; o[1] = j->jnAcc; o[2] = j->nMass;
 			o[3] = j->r1.x; o[4] = j->r1.y; o[5] = j->r2.x; o[6] = j->r2.y; o[7] = j->bias;
+		} else if(cpConstraintIsGrooveJoint(c)){
+			cpGrooveJoint *j = (cpGrooveJoint *)c;
+			o[0] = 4; o[1] = j->jAcc.x; o[2] = j->jAcc.y;
+			o[3] = j->r1.x; o[4] = j->r1.y; o[5] = j->r2.x; o[6] = j->r2.y; o[7] = j->bias.x;
+		} else if(cpConstraintIsDampedSpring(c)){
+			cpDampedSpring *j = (cpDampedSpring *)c;
+			o[0] = 5; o[1] = j->jAcc; o[2] = j->nMass;
+			o[3] = j->r1.x; o[4] = j->r1.y; o[5] = j->r2.x; o[6] = j->r2.y; o[7] = j->v_coef;
+		} else if(cpConstraintIsDampedRotarySpring(c)){
+			cpDampedRotarySpring *j = (cpDampedRotarySpring *)c;
+			o[0] = 6; o[1] = j->jAcc; o[2] = j->iSum; o[3] = j->w_coef; o[7] = j->target_wrn;
+		} else if(cpConstraintIsRotaryLimitJoint(c)){
+			cpRotaryLimitJoint *j = (cpRotaryLimitJoint *)c;
+			o[0] = 7; o[1] = j->jAcc; o[2] = j->iSum; o[7] = j->bias;
+		} else if(cpConstraintIsRatchetJoint(c)){
+			cpRatchetJoint *j = (cpRatchetJoint *)c;
+			o[0] = 8; o[1] = j->jAcc; o[2] = j->iSum; o[3] = j->angle; o[7] = j->bias;
+		} else if(cpConstraintIsGearJoint(c)){
+			cpGearJoint *j = (cpGearJoint *)c;
+			o[0] = 9; o[1] = j->jAcc; o[2] = j->iSum; o[7] = j->bias;
+		} else if(cpConstraintIsSimpleMotor(c)){
+			cpSimpleMotor *j = (cpSimpleMotor *)c;
+			o[0] = 10; o[1] = j->jAcc; o[2] = j->iSum;
 		}
 	}
 	return constraints->num;

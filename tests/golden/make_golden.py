@@ -27,6 +27,7 @@ FIXTURES = [
     ("tumble", 4, 150, 1 / 60, [1, 5, 60]),
     ("adjoint", 5, 64, 1 / 120, [1, 5, 120]),
     ("joints", 6, 120, 1 / 60, [1, 5, 60, 200]),
+    ("machines", 7, 12, 1 / 60, [1, 5, 60, 200]),
 ]
 
 

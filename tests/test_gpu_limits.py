@@ -63,13 +63,13 @@ def test_dataflow_wait_runs_out_and_reports_a_timeout(gpu_lib, oracle_lib):
     still_in_parity(gpu_lib, oracle_lib)
 
 
-@pytest.mark.parametrize("caps", [(1, 0, 0, 0), (0, -1, 16, 0), (0, -1, 0, 40)],
+@pytest.mark.parametrize("caps", [(1, 0, 0, 0), (0, -1, 4, 0), (0, -1, 0, 40)],
                          ids=["pairs", "arbiters", "nodes"])
 def test_table_overflow_is_latched_and_reported(gpu_lib, oracle_lib, caps):
     gpu_lib.cpGpuDebugSetCapacities(*caps)
     sc = Scene(gpu_lib, 4, 300)
     try:
-        err = run_until_error(gpu_lib, sc, 30)
+        err = run_until_error(gpu_lib, sc, 90)
     finally:
         gpu_lib.cpGpuDebugSetCapacities(0, -1, 0, 0)
         sc.free()

@@ -78,6 +78,7 @@ CASES = [
     ("tumble", 4, 300, 1 / 60, 120),
     ("adjoint", 5, 64, 1 / 120, 120),
     ("joints", 6, 200, 1 / 60, 200),
+    ("machines", 7, 40, 1 / 60, 300),
 ]
 
 
@@ -137,8 +138,8 @@ def test_teacher_forced_with_objects_added_and_removed(gpu_lib, oracle_lib, cfg,
 FREE_RUN_DRIFT = 1e-9
 
 
-@pytest.mark.parametrize("name,cfg,size,dt,steps", [CASES[0], CASES[1], CASES[2], CASES[5]],
-                         ids=["pyramid", "circles", "mixed", "joints"])
+@pytest.mark.parametrize("name,cfg,size,dt,steps", [CASES[0], CASES[1], CASES[2], CASES[5], CASES[6]],
+                         ids=["pyramid", "circles", "mixed", "joints", "machines"])
 def test_teacher_forced_whole_grid_solve(gpu_lib, oracle_lib, name, cfg, size, dt, steps):
     """The whole-grid solve (four lanes per contact, a grid barrier between
     levels), which large single worlds use, against the oracle."""
@@ -218,7 +219,7 @@ def test_public_getters_and_impulses_match(gpu_lib, oracle_lib):
         o.free()
 
 
-@pytest.mark.parametrize("cfg", [4, 6], ids=["tumble", "joints"])
+@pytest.mark.parametrize("cfg", [4, 6, 7], ids=["tumble", "joints", "machines"])
 def test_batched_worlds_match_single_worlds(gpu_lib, oracle_lib, cfg):
     """Uneven worlds stepped together in one batch match the oracle stepping
     each world alone: tumble worlds, and worlds of pin and slide joints with
@@ -228,6 +229,8 @@ def test_batched_worlds_match_single_worlds(gpu_lib, oracle_lib, cfg):
     gpu_lib.cpx_batch_sizes(24, 3, ctypes.cast(sizes, ctypes.c_void_p))
     if cfg == 6:
         sizes = [40 + (sizes[i] * 160) // 512 for i in range(24)]
+    elif cfg == 7:
+        sizes = [2 + (sizes[i] * 30) // 512 for i in range(24)]
     gs = [Scene(gpu_lib, cfg, sizes[i], seed=100 + i) for i in range(24)]
     os_ = [Scene(oracle_lib, cfg, sizes[i], seed=100 + i) for i in range(24)]
     batch = gpu_lib.cpGpuBatchNew()

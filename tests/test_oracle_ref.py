@@ -21,6 +21,7 @@ CASES = [
     (4, 300, 200, 1 / 60),
     (5, 64, 240, 1 / 120),
     (6, 200, 300, 1 / 60),
+    (7, 40, 400, 1 / 60),
 ]
 
 

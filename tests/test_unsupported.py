@@ -70,3 +70,21 @@ def test_constraint_callbacks_are_refused(lib):
     err, unmoved = refused(lib, sp, b)
     assert err == CP_GPU_ERR_UNSUPPORTED and unmoved
     lib.cpSpaceFree(sp); lib.cpConstraintFree(c); lib.cpBodyFree(b)
+
+
+SPRING_FORCE = ctypes.CFUNCTYPE(D, P, D)
+
+
+def test_custom_spring_force_is_refused(lib):
+    """A damped spring with its own force function (host code) is refused;
+    the default force runs on the GPU."""
+    lib.cpDampedSpringNew.restype = P
+    lib.cpDampedSpringNew.argtypes = [P, P, cpVect, cpVect, D, D, D]
+    lib.cpDampedSpringSetSpringForceFunc.argtypes = [P, SPRING_FORCE]
+    sp, b = one_body_space(lib)
+    c = lib.cpSpaceAddConstraint(sp, lib.cpDampedSpringNew(lib.cpSpaceGetStaticBody(sp), b, cpVect(0, 0), cpVect(0, 0), 5.0, 10.0, 1.0))
+    cb = SPRING_FORCE(lambda spring, dist: 0.0)
+    lib.cpDampedSpringSetSpringForceFunc(c, cb)
+    err, unmoved = refused(lib, sp, b)
+    assert err == CP_GPU_ERR_UNSUPPORTED and unmoved
+    lib.cpSpaceFree(sp); lib.cpConstraintFree(c); lib.cpBodyFree(b)
