@@ -3259,12 +3259,13 @@ int cpGpuGetStepStats(cpSpace *sp, int *out, int max)
 	DevSet *ds = sp->dev;
 	/* the stats block of the last step: error flags, pair/node use (per
 	 * mille of capacity), live arbiters, candidates, solved arbiters,
-	 * sweep levels or colours, candidate use (per mille); the step's own
-	 * asynchronous read-back may be older */
+	 * sweep levels or colours, candidate use (per mille), leaves
+	 * reinserted in the exact-order tree; the step's own asynchronous
+	 * read-back may be older */
 	check_stats(ds);
 	if(!d2h(ds->hstats, ds->d.stats, sizeof(int)*16)) return 0;
 	cudaStreamSynchronize(lib_stream());
-	int n = max < 8 ? max : 8;
+	int n = max < 9 ? max : 9;
 	for(int i = 0; i < n; i++) out[i] = ds->hstats[i];
 	return n;
 }

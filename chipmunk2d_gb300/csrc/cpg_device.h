@@ -82,7 +82,7 @@ typedef struct cpgTree {
 	int error;
 	int pairsLive;
 	int maxChain;
-	int pad;
+	int moved;                    /* leaves reinserted this step */
 } cpgTree;
 
 /* AABB-tree node (cpBBTree.c:46-60), 64 bytes. */

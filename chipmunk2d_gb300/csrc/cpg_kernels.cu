@@ -855,6 +855,158 @@ __global__ void k_schedule(cpgSet s)
 	if(nlev > T.maxChain) T.maxChain = nlev;
 }
 
+/* In-place exclusive scan of a[0, len) by one block: each thread sums a
+ * contiguous run, warp 0 scans the warps' totals, each thread rewrites its
+ * run.  blockDim.x is a multiple of 32, at most 1024. */
+__device__ void block_exscan_inplace(int *a, int len)
+{
+	__shared__ int wsum[32];
+	int nt = blockDim.x, tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+	int per = (len + nt - 1)/nt;
+	int lo = min(len, tid*per), hi = min(len, lo + per);
+	int sum = 0;
+	for(int i = lo; i < hi; i++) sum += a[i];
+	int x = sum;
+	for(int o = 1; o < 32; o <<= 1){
+		int y = __shfl_up_sync(0xffffffffu, x, o);
+		if(lane >= o) x += y;
+	}
+	if(lane == 31) wsum[warp] = x;
+	__syncthreads();
+	if(warp == 0){
+		int v = (lane < (nt >> 5)) ? wsum[lane] : 0;
+		int z = v;
+		for(int o = 1; o < 32; o <<= 1){
+			int y = __shfl_up_sync(0xffffffffu, z, o);
+			if(lane >= o) z += y;
+		}
+		wsum[lane] = z - v;
+	}
+	__syncthreads();
+	int run = wsum[warp] + x - sum;
+	for(int i = lo; i < hi; i++){ int t = a[i]; a[i] = run; run += t; }
+	__syncthreads();
+}
+
+/* The level schedule of k_schedule for one large world, by one block of
+ * 1024 threads.  The recurrence is a scan in unit order and stays on one
+ * thread, but its per-body "last level" array sits in shared memory (a
+ * dependent shared load and store per unit instead of two L2 round trips)
+ * and the units' body indices are loaded a batch ahead.  The block then
+ * counts the units of every level, scans the counts into levelStart and
+ * warp 0 scatters the units 32 at a time in unit order (ranks within a
+ * warp by __match_any_sync), which is the serial stable scatter's order.
+ * Arrays that do not fit in the shared scratch (sh, shInts ints) stay in
+ * global memory.  Returns the level count to every thread. */
+#define CPG_SCHED_THREADS 1024
+#define CPG_SCHED_SMEM_INTS (56*1024)
+#define CPG_SCHED_BATCH 16
+__device__ int schedule_block(const int *ua, const int *ub, int nunits, int nbodies,
+                              int *lastG, int *level, int *levelStart, int *order, int *sh, int shInts)
+{
+	__shared__ int nlevSh;
+	int tid = threadIdx.x, nt = blockDim.x;
+	int *last = (nbodies <= shInts) ? sh : lastG;
+	for(int b = tid; b < nbodies; b += nt) last[b] = 0;
+	__syncthreads();
+	if(tid == 0){
+		int nlev = 0;
+		int na[CPG_SCHED_BATCH], nb[CPG_SCHED_BATCH];
+#pragma unroll
+		for(int k = 0; k < CPG_SCHED_BATCH; k++){
+			na[k] = (k < nunits) ? ua[k] : -1;
+			nb[k] = (k < nunits) ? ub[k] : -1;
+		}
+		for(int u0 = 0; u0 < nunits; u0 += CPG_SCHED_BATCH){
+			int ca[CPG_SCHED_BATCH], cb[CPG_SCHED_BATCH];
+#pragma unroll
+			for(int k = 0; k < CPG_SCHED_BATCH; k++){
+				ca[k] = na[k]; cb[k] = nb[k];
+				int u = u0 + CPG_SCHED_BATCH + k;
+				na[k] = (u < nunits) ? ua[u] : -1;
+				nb[k] = (u < nunits) ? ub[u] : -1;
+			}
+#pragma unroll
+			for(int k = 0; k < CPG_SCHED_BATCH; k++){
+				int u = u0 + k;
+				if(u < nunits){
+					int a = ca[k], b = cb[k];
+					if(a >= nbodies) a = -1;
+					if(b >= nbodies) b = -1;
+					int l = 0;
+					if(a >= 0 && last[a] > l) l = last[a];
+					if(b >= 0 && last[b] > l) l = last[b];
+					level[u] = l;
+					if(a >= 0) last[a] = l + 1;
+					if(b >= 0) last[b] = l + 1;
+					if(l + 1 > nlev) nlev = l + 1;
+				}
+			}
+		}
+		nlevSh = nlev;
+	}
+	__syncthreads();
+	int nlev = nlevSh;
+	/* counts of every level, scanned into the level starts */
+	int *cnt = (nlev + 1 <= shInts) ? sh : levelStart;
+	for(int l = tid; l <= nlev; l += nt) cnt[l] = 0;
+	__syncthreads();
+	for(int u = tid; u < nunits; u += nt) atomicAdd(&cnt[level[u]], 1);
+	__syncthreads();
+	block_exscan_inplace(cnt, nlev + 1);
+	if(cnt != levelStart){
+		for(int l = tid; l <= nlev; l += nt) levelStart[l] = cnt[l];
+	}
+	__syncthreads();
+	/* stable scatter; cnt[l] runs as level l's cursor */
+	if(tid < 32){
+		for(int u0 = 0; u0 < nunits; u0 += 32){
+			int u = u0 + tid;
+			int l = (u < nunits) ? level[u] : -1;
+			unsigned peers = __match_any_sync(0xffffffffu, l);
+			int rank = __popc(peers & ((1u << tid) - 1u));
+			int lead = __ffs(peers) - 1;
+			int base = 0;
+			if(u < nunits && rank == 0){ base = cnt[l]; cnt[l] = base + __popc(peers); }
+			base = __shfl_sync(0xffffffffu, base, lead);
+			if(u < nunits) order[base + rank] = u;
+			__syncwarp();
+		}
+	}
+	__syncthreads();
+	if(cnt == levelStart){
+		/* the cursors ended at the next level's start: shift them back */
+		if(tid == 0){
+			for(int l = nlev; l > 0; l--) levelStart[l] = levelStart[l - 1];
+			levelStart[0] = 0;
+		}
+		__syncthreads();
+	}
+	return nlev;
+}
+
+/* k_schedule for a set of one world (the large single spaces). */
+__global__ void __launch_bounds__(CPG_SCHED_THREADS, 1) k_schedule_one(cpgSet s)
+{
+	extern __shared__ int schedSh[];
+	const int w = 0;
+	if(!s.params[w].active) return;
+	const cpgWorld &W = s.world[w];
+	cpgTree &T = s.tree[w];
+	int nunits = T.nunits;
+	if(nunits > W.unitCap){
+		if(threadIdx.x == 0) T.nlevels = 0;
+		return;
+	}
+	int nlev = schedule_block(s.unitA + W.unitOff, s.unitB + W.unitOff, nunits, W.nbodies,
+	                          s.last + W.bodyOff, s.unitLevel + W.unitOff, s.levelStart + W.unitOff + w,
+	                          s.unitOrder + W.unitOff, schedSh, CPG_SCHED_SMEM_INTS);
+	if(threadIdx.x == 0){
+		T.nlevels = nlev;
+		if(nlev > T.maxChain) T.maxChain = nlev;
+	}
+}
+
 /* ------------------------------------------------------------------ */
 /* Pre-step into solver rows: cpArbiter.c:416-439, cpPivotJoint.c:24-39,
  * cpPinJoint.c:24-46, cpSlideJoint.c:24-56.  Rows are written in schedule
@@ -1901,8 +2053,8 @@ __global__ void k_unpack_bodies(cpgSet s)
 /* Aggregate per-world bookkeeping for the host (one block). */
 __global__ void k_stats(cpgSet s)
 {
-	__shared__ int err, pairMax, nodeMax, candMax, levMax, ncand, narb;
-	if(threadIdx.x == 0){ err = 0; pairMax = 0; nodeMax = 0; candMax = 0; levMax = 0; ncand = 0; narb = 0; }
+	__shared__ int err, pairMax, nodeMax, candMax, levMax, ncand, narb, moved;
+	if(threadIdx.x == 0){ err = 0; pairMax = 0; nodeMax = 0; candMax = 0; levMax = 0; ncand = 0; narb = 0; moved = 0; }
 	__syncthreads();
 	for(int w = threadIdx.x; w < s.nworlds; w += blockDim.x){
 		const cpgTree &T = s.tree[w];
@@ -1914,11 +2066,12 @@ __global__ void k_stats(cpgSet s)
 		atomicMax(&levMax, T.nlevels);
 		atomicAdd(&ncand, T.ncand);
 		atomicAdd(&narb, T.narb);
+		atomicAdd(&moved, T.moved);
 	}
 	__syncthreads();
 	if(threadIdx.x == 0){
 		s.stats[0] = err; s.stats[1] = pairMax; s.stats[2] = nodeMax; s.stats[4] = ncand;
-		s.stats[5] = narb; s.stats[6] = levMax; s.stats[7] = candMax;
+		s.stats[5] = narb; s.stats[6] = levMax; s.stats[7] = candMax; s.stats[8] = moved;
 	}
 }
 
@@ -2946,6 +3099,14 @@ extern "C" int cpg_launch_step(const cpgSet *s, const cpgSet *h, int mode, void 
 	LAUNCH(k_arb_filter<<<blocks_for(h->arbCap, 256), 256, 0, st>>>(*s));
 	if(timing) cudaEventRecord(ev[4], st);
 	if(colored) COOP(k_color_coop, 512);
+	else if(W == 1){
+		static bool schedSmemSet = false;
+		if(!schedSmemSet){
+			cudaFuncSetAttribute(k_schedule_one, cudaFuncAttributeMaxDynamicSharedMemorySize, CPG_SCHED_SMEM_INTS*(int)sizeof(int));
+			schedSmemSet = true;
+		}
+		LAUNCH(k_schedule_one<<<1, CPG_SCHED_THREADS, CPG_SCHED_SMEM_INTS*sizeof(int), st>>>(*s));
+	}
 	else LAUNCH(k_schedule<<<blocks_for(W, 32), 32, 0, st>>>(*s));
 	if(timing) cudaEventRecord(ev[5], st);
 	LAUNCH(k_build_rows<<<dim3(perWorldX, W), 128, 0, st>>>(*s));

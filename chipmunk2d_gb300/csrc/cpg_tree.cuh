@@ -189,14 +189,29 @@ __device__ void pair_insert(TreeCtx &c, int a, int b)
 	}
 }
 
-/* cpBBTree.c:250-267 */
-__device__ int node_new(TreeCtx &c, int a, int b)
+/* A node's box and links in registers. */
+struct NodeRec {
+	BB bb;
+	int parent, A, B, obj;
+};
+
+__device__ __forceinline__ NodeRec node_rec(const TreeCtx &c, int n)
+{
+	const cpgNode &nd = c.nodes[n];
+	NodeRec r;
+	r.bb = node_bb(nd);
+	r.parent = nd.parent; r.A = nd.A; r.B = nd.B; r.obj = nd.obj;
+	return r;
+}
+
+/* cpBBTree.c:250-267, with the children's boxes passed in */
+__device__ int node_new_bb(TreeCtx &c, int a, BB abb, int b, BB bbb)
 {
 	int n = node_alloc(c);
 	if(n < 0) return -1;
 	cpgNode &nd = c.nodes[n];
 	nd.obj = -1;
-	set_node_bb(nd, tmerge(node_bb(c.nodes[a]), node_bb(c.nodes[b])));
+	set_node_bb(nd, tmerge(abb, bbb));
 	nd.parent = -1;
 	nd.A = a; c.nodes[a].parent = n;
 	nd.B = b; c.nodes[b].parent = n;
@@ -204,10 +219,19 @@ __device__ int node_new(TreeCtx &c, int a, int b)
 	return n;
 }
 
-/* cpBBTree.c:281-299 */
+__device__ int node_new(TreeCtx &c, int a, int b)
+{
+	return node_new_bb(c, a, node_bb(c.nodes[a]), b, node_bb(c.nodes[b]));
+}
+
+/* cpBBTree.c:281-299.  The refit from the parent up to the root is one
+ * round of dependent loads per level: the child just refitted is known,
+ * so a level loads its sibling's box and the next parent's links at once
+ * (merged in the reference's A, B order). */
 __device__ void node_replace_child(TreeCtx &c, int parent, int child, int value)
 {
 	cpgNode &pn = c.nodes[parent];
+	BB fromBB = node_bb(c.nodes[value]);
 	if(pn.A == child){
 		node_recycle(c, pn.A);
 		pn.A = value; c.nodes[value].parent = parent;
@@ -215,28 +239,42 @@ __device__ void node_replace_child(TreeCtx &c, int parent, int child, int value)
 		node_recycle(c, pn.B);
 		pn.B = value; c.nodes[value].parent = parent;
 	}
-	int guard = 0;
-	for(int n = parent; n >= 0; n = c.nodes[n].parent){
-		if(++guard > c.nodeCap){ c.T->error |= CPG_ERR_NODES; return; }
-		cpgNode &nd = c.nodes[n];
-		set_node_bb(nd, tmerge(node_bb(c.nodes[nd.A]), node_bb(c.nodes[nd.B])));
+	int from = value, n = parent;
+	int a = pn.A, b = pn.B, up = pn.parent;
+	for(int guard = 0;; guard++){
+		if(guard > c.nodeCap){ c.T->error |= CPG_ERR_NODES; return; }
+		bool fromA = (a == from);
+		BB sbb = node_bb(c.nodes[fromA ? b : a]);
+		int na = -1, nb = -1, nup = -1;
+		if(up >= 0){
+			const cpgNode &un = c.nodes[up];
+			na = un.A; nb = un.B; nup = un.parent;
+		}
+		BB m = fromA ? tmerge(fromBB, sbb) : tmerge(sbb, fromBB);
+		set_node_bb(c.nodes[n], m);
+		if(up < 0) return;
+		from = n; fromBB = m; n = up;
+		a = na; b = nb; up = nup;
 	}
 }
 
 /* cpBBTree.c:325-350, iterative.  The reference merges each visited
  * node's box on the way back up; a node's own box is only read by its
  * parent's cost test, which has already run, so merging on the way down
- * gives the same tree and boxes. */
+ * gives the same tree and boxes.  Both children's records are loaded at
+ * each level, so the chosen child's links are already in registers and
+ * the descent costs one round of dependent loads per level. */
 __device__ int subtree_insert(TreeCtx &c, int root, int leaf)
 {
 	if(root < 0) return leaf;
-	if(is_leaf(c, root)) return node_new(c, leaf, root);
+	NodeRec nd = node_rec(c, root);
+	if(nd.obj >= 0) return node_new(c, leaf, root);
 	BB lbb = node_bb(c.nodes[leaf]);
 	int cur = root;
 	for(int guard = 0;; guard++){
 		if(guard > c.nodeCap){ c.T->error |= CPG_ERR_NODES; return root; }
-		cpgNode &nd = c.nodes[cur];
-		BB abb = node_bb(c.nodes[nd.A]), bbb = node_bb(c.nodes[nd.B]);
+		NodeRec ra = node_rec(c, nd.A), rb = node_rec(c, nd.B);
+		BB abb = ra.bb, bbb = rb.bb;
 		double cost_a = bbarea(bbb) + tmergedarea(abb, lbb);
 		double cost_b = bbarea(abb) + tmergedarea(bbb, lbb);
 		if(tkey(cost_a) == tkey(cost_b)){
@@ -245,15 +283,17 @@ __device__ int subtree_insert(TreeCtx &c, int root, int leaf)
 		}
 		bool goB = (tkey(cost_b) < tkey(cost_a));
 		int child = goB ? nd.B : nd.A;
-		set_node_bb(nd, tmerge(node_bb(nd), lbb));
-		if(is_leaf(c, child)){
-			int nn = node_new(c, leaf, child);
+		NodeRec rc = goB ? rb : ra;
+		set_node_bb(c.nodes[cur], tmerge(nd.bb, lbb));
+		if(rc.obj >= 0){
+			int nn = node_new_bb(c, leaf, lbb, child, rc.bb);
 			if(nn < 0) return root;
-			if(goB) nd.B = nn; else nd.A = nn;
+			if(goB) c.nodes[cur].B = nn; else c.nodes[cur].A = nn;
 			c.nodes[nn].parent = cur;
 			return root;
 		}
 		cur = child;
+		nd = rc;
 	}
 }
 
@@ -504,6 +544,7 @@ __device__ void tree_reindex_query_block(TreeCtx &c, bool parallelMark = false)
 {
 	__shared__ int warpTot[32];
 	__shared__ int carry, stop;
+	__shared__ cpgTree hdr;
 	cpgTree *T = c.T;
 	int tid = threadIdx.x, nt = blockDim.x, lane = tid & 31, warp = tid >> 5, nw = (nt + 31) >> 5;
 	int *list = (int *)c.cands;
@@ -553,15 +594,22 @@ __device__ void tree_reindex_query_block(TreeCtx &c, bool parallelMark = false)
 		__syncthreads();
 	}
 	if(tid == 0){
+		/* thread 0 reads and writes the tree header at every reinsertion
+		 * and node or pair allocation: it works on a shared-memory copy */
+		hdr = *T;
+		c.T = &hdr;
 		int moved = carry;
-		if((long long)moved > listCap) T->error |= CPG_ERR_CANDS;
+		hdr.moved = moved;
+		if((long long)moved > listCap) hdr.error |= CPG_ERR_CANDS;
 		/* with parallelMark the pairs of moved leaves stay threaded and
 		 * k_tree_mark marks the tree (cpg_mark.cuh) */
-		for(int k = 0; k < moved && !T->error; k++) leaf_reinsert(c, list[k], !parallelMark);
-		if(!T->error && !parallelMark){
-			mark_subtree(c, T->dynRoot, T->statRoot);
-			T->treeStamp++;
+		for(int k = 0; k < moved && !hdr.error; k++) leaf_reinsert(c, list[k], !parallelMark);
+		if(!hdr.error && !parallelMark){
+			mark_subtree(c, hdr.dynRoot, hdr.statRoot);
+			hdr.treeStamp++;
 		}
+		*T = hdr;
+		c.T = T;
 	}
 }
 #endif

@@ -711,7 +711,8 @@ void cpGpuDebugSetParallelMarking(int on);
  * [1] pair-pool use and [2] node-pool use (per mille of capacity, largest
  * world), [3] live cached arbiters, [4] candidate pairs, [5] solved
  * arbiters, [6] levels (ordered) or colours (coloured) of one sweep,
- * [7] candidate-buffer use (per mille).  Returns the count written. */
+ * [7] candidate-buffer use (per mille), [8] leaves reinserted in the
+ * exact-order tree (all worlds).  Returns the count written. */
 int cpGpuGetStepStats(cpSpace *space, int *out, int max);
 int cpGpuGetPhaseTimes(cpSpace *space, double *ms, int max);
 /* Number of kernel launches issued by this library since the last reset. */
