@@ -151,6 +151,7 @@ _API = {
     "cpx_space_set_hasty": (I, [P, I]),
     "cpx_scene_free": (None, [P]),
     "cpx_scene_edit": (I, [P, I, ctypes.c_ulonglong]),
+    "cpx_scene_queries": (I, [P, I, I, P, I]),
     "cpx_batch_sizes": (None, [I, ctypes.c_ulonglong, P]),
     # state export (shared record layouts)
     "cpx_dump_bodies": (I, [P, P, I]),
@@ -313,6 +314,17 @@ class Scene:
         n = self.lib.cpx_dump_candidates(self.space, out.ctypes.data, cap)
         pairs = out[:2 * min(n, cap)].reshape(-1, 2)
         return set(map(tuple, pairs.tolist()))
+
+    def queries(self, seed, nq):
+        """nq seeded spatial queries through the public API (scenes.c,
+        cpx_scene_queries): one row of 8 per callback or result."""
+        cap = 64 * nq + 64
+        while True:
+            out = np.zeros(8 * cap)
+            n = self.lib.cpx_scene_queries(self.h, seed, nq, out.ctypes.data, cap)
+            if n <= cap:
+                return out[:8 * n].reshape(n, 8)
+            cap = n
 
     def public(self):
         out = np.zeros(8 * max(self.nbodies, 1))

@@ -19,7 +19,7 @@ CUDA_HOME = os.environ.get("CUDA_HOME", "/usr/local/cuda")
 NVCC = os.path.join(CUDA_HOME, "bin", "nvcc") if os.path.exists(os.path.join(CUDA_HOME, "bin", "nvcc")) else "nvcc"
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
-CU_SOURCES = ["cpg_kernels.cu", "cpg_schedule_api.cu", "cpg_rollout.cu"]
+CU_SOURCES = ["cpg_kernels.cu", "cpg_schedule_api.cu", "cpg_rollout.cu", "cpg_query.cu"]
 C_SOURCES = ["cp_host.c"]
 # The seeded workloads the tests and the benchmark build through the public
 # API: a library of their own that links against the product, so the

@@ -264,6 +264,8 @@ struct DevSet {
 	int tuneIdx;              /* position in the open window */
 	double tuneMs[CPG_TUNE_CANDIDATES];
 	int tuneBest;             /* chosen candidate, -1 before the first window */
+	void *qbuf;               /* spatial queries: queries, hits, counts, status */
+	size_t qbytes;
 };
 
 
@@ -684,6 +686,7 @@ static void devset_free(DevSet *ds)
 	if(ds->scratch) cudaFree(ds->scratch);
 	if(ds->graph) cpg_step_graph_free(ds->graph);
 	if(ds->gather) cudaFree(ds->gather);
+	if(ds->qbuf) cudaFree(ds->qbuf);
 	if(ds->hparams) cudaFreeHost(ds->hparams);
 	if(ds->hstats) cudaFreeHost(ds->hstats);
 	if(ds->hbodies) cudaFreeHost(ds->hbodies);
@@ -1174,6 +1177,34 @@ static int space_structure_changed(cpSpace *sp)
 }
 
 /* cpSpaceStep.c:335-445 */
+/* A space's own device set, current with the host's structure: built at
+ * first use; rebuilt when objects were added or removed since, the host
+ * holding the whole state (space_detach), carrying the device tree and
+ * arbiter cache over and replaying the index edits recorded since, in
+ * call order.  Returns 0 (error set) when no set could be built. */
+static int space_device_ready_(cpSpace *sp)
+{
+	if(sp->dev && (sp->structDirty || space_structure_changed(sp))){
+		DevSet *old = sp->dev;
+		space_detach(sp);
+		cpSpace *one[1] = { sp };
+		DevSet *ds = devset_build(one, 1, old);
+		if(!ds){
+			sp->dev = old; sp->world = 0; sp->structDirty = 1;
+			return 0;
+		}
+		devset_free(old);
+		sp->ownsDev = 1;
+	}
+	if(!sp->dev){
+		cpSpace *one[1] = { sp };
+		DevSet *ds = devset_build(one, 1, NULL);
+		if(!ds) return 0;
+		sp->ownsDev = 1;
+	}
+	return 1;
+}
+
 void cpSpaceStep(cpSpace *sp, cpFloat dt)
 {
 	if(dt == 0.0) return;
@@ -1182,30 +1213,255 @@ void cpSpaceStep(cpSpace *sp, cpFloat dt)
 		set_error(CP_GPU_ERR_UNSUPPORTED, "space belongs to a cpGpuBatch; step it with cpGpuBatchStep");
 		return;
 	}
-	if(sp->dev && (sp->structDirty || space_structure_changed(sp))){
-		/* Objects were added or removed since the set was built: the host
-		 * holds the whole state (space_detach), so build a new set from it,
-		 * carrying the device tree and arbiter cache over, and replay the
-		 * index edits recorded since, in call order. */
-		DevSet *old = sp->dev;
-		space_detach(sp);
-		cpSpace *one[1] = { sp };
-		DevSet *ds = devset_build(one, 1, old);
-		if(!ds){
-			sp->dev = old; sp->world = 0; sp->structDirty = 1;
-			return;
-		}
-		devset_free(old);
-		sp->ownsDev = 1;
-	}
-	if(!sp->dev){
-		cpSpace *one[1] = { sp };
-		DevSet *ds = devset_build(one, 1, NULL);
-		if(!ds) return;
-		sp->ownsDev = 1;
-	}
+	if(!space_device_ready_(sp)) return;
 	double dts[1] = { dt };
 	devset_step(sp->dev, dts, NULL);
+}
+
+/* ====================================================================
+ * Spatial queries (cpSpaceQuery.c:48-204, cpShape.c:222-256): answered on
+ * the device by cpg_query.cu, which walks the space's trees in the
+ * reference's order; the callbacks then run here, in that order.
+ * ==================================================================== */
+#define CPG_QUERY_HITS0 64
+
+static cpgQuery query_new_(int kind, double ax, double ay, double bx, double by, double r, cpShapeFilter f)
+{
+	cpgQuery q;
+	memset(&q, 0, sizeof(q));
+	q.kind = kind; q.ax = ax; q.ay = ay; q.bx = bx; q.by = by; q.r = r;
+	q.group = (unsigned long long)f.group; q.cat = f.categories; q.mask = f.mask;
+	return q;
+}
+
+/* Runs nq queries on the space's device set.  On success *hits holds cap
+ * records per query and *counts the number of each (all-hits queries) or
+ * 0/1 (nearest and first-hit queries); both are malloc'd. */
+static int run_queries_(cpSpace *sp, const cpgQuery *q, int nq, cpgHit **hitsOut, int **countsOut, int *capOut)
+{
+	*hitsOut = NULL; *countsOut = NULL; *capOut = 0;
+	if(!sp || nq < 0 || (nq > 0 && !q)){ set_error(CP_GPU_ERR_ARGUMENT, "query: null space or queries"); return 0; }
+	if(sp->dev && !sp->ownsDev){
+		if(sp->structDirty || space_structure_changed(sp)){
+			set_error(CP_GPU_ERR_UNSUPPORTED, "query: objects were added to or removed from a space of a cpGpuBatch");
+			return 0;
+		}
+	} else if(!space_device_ready_(sp)) return 0;
+	DevSet *ds = sp->dev;
+	devset_flush_space(ds, sp->world);
+	cudaStream_t st = lib_stream();
+	int brute = (sp->mode == CP_GPU_SOLVER_COLORED);
+	int cap = CPG_QUERY_HITS0;
+	int *counts = HALLOC(int, nq + 1);
+	for(int attempt = 0; attempt < 2; attempt++){
+		size_t qb = align256(sizeof(cpgQuery)*(size_t)(nq > 0 ? nq : 1));
+		size_t hb = align256(sizeof(cpgHit)*(size_t)(nq > 0 ? nq : 1)*(size_t)cap);
+		size_t cb = align256(sizeof(int)*(size_t)(nq + 1));
+		size_t need = qb + hb + cb;
+		if(ds->qbytes < need){
+			if(ds->qbuf) cudaFree(ds->qbuf);
+			ds->qbuf = NULL; ds->qbytes = 0;
+			if(!cuda_ok(cudaMalloc(&ds->qbuf, need), "cudaMalloc queries")){ free(counts); return 0; }
+			ds->qbytes = need;
+		}
+		char *base = (char *)ds->qbuf;
+		cpgQuery *dq = (cpgQuery *)base;
+		cpgHit *dh = (cpgHit *)(base + qb);
+		int *dc = (int *)(base + qb + hb);
+		int ok = h2d(dq, q, sizeof(cpgQuery)*(size_t)nq);
+		ok &= cuda_ok(cudaMemsetAsync(dc + nq, 0, sizeof(int), st), "query status");
+		ok &= (cpg_launch_query(&ds->d, sp->world, dq, nq, dh, cap, dc, brute, dc + nq, st) == 0);
+		ok &= d2h(counts, dc, sizeof(int)*(size_t)(nq + 1));
+		ok &= cuda_ok(cudaStreamSynchronize(st), "query");
+		if(!ok){ set_error(CP_GPU_ERR_CUDA, "query launch failed"); free(counts); return 0; }
+		if(counts[nq]){
+			set_error(CP_GPU_ERR_OVERFLOW, "query: tree walk stack or guard exceeded");
+			free(counts); return 0;
+		}
+		int most = 0;
+		for(int i = 0; i < nq; i++) if(counts[i] > most) most = counts[i];
+		if(most > cap && attempt == 0){ cap = most; continue; }
+		cpgHit *hits = HALLOC(cpgHit, (size_t)(nq > 0 ? nq : 1)*(size_t)cap);
+		if(!d2h(hits, dh, sizeof(cpgHit)*(size_t)nq*(size_t)cap) || !cuda_ok(cudaStreamSynchronize(st), "query results")){
+			free(hits); free(counts); return 0;
+		}
+		*hitsOut = hits; *countsOut = counts; *capOut = cap;
+		return 1;
+	}
+	set_error(CP_GPU_ERR_OVERFLOW, "query: hit lists kept growing");
+	free(counts);
+	return 0;
+}
+
+static cpShape *slot_shape_(cpSpace *sp, int slot)
+{
+	return (slot >= 0 && slot < sp->nshapes) ? sp->shapes[slot] : NULL;
+}
+
+void cpSpacePointQuery(cpSpace *sp, cpVect point, cpFloat maxDistance, cpShapeFilter filter, cpSpacePointQueryFunc func, void *data)
+{
+	cpgQuery q = query_new_(CPG_Q_POINT, point.x, point.y, 0.0, 0.0, maxDistance, filter);
+	cpgHit *h; int *c, cap;
+	if(!run_queries_(sp, &q, 1, &h, &c, &cap)) return;
+	for(int k = 0; k < c[0] && k < cap; k++){
+		cpShape *shape = slot_shape_(sp, h[k].shape);
+		if(shape && func) func(shape, cpv(h[k].px, h[k].py), h[k].d, cpv(h[k].gx, h[k].gy), data);
+	}
+	free(h); free(c);
+}
+
+cpShape *cpSpacePointQueryNearest(cpSpace *sp, cpVect point, cpFloat maxDistance, cpShapeFilter filter, cpPointQueryInfo *out)
+{
+	cpPointQueryInfo info = {NULL, cpvzero, maxDistance, cpvzero};
+	if(out) *out = info; else out = &info;
+	cpgQuery q = query_new_(CPG_Q_POINT_NEAREST, point.x, point.y, 0.0, 0.0, maxDistance, filter);
+	cpgHit *h; int *c, cap;
+	if(!run_queries_(sp, &q, 1, &h, &c, &cap)) return NULL;
+	if(c[0] && slot_shape_(sp, h[0].shape)){
+		out->shape = slot_shape_(sp, h[0].shape);
+		out->point = cpv(h[0].px, h[0].py);
+		out->distance = h[0].d;
+		out->gradient = cpv(h[0].gx, h[0].gy);
+	}
+	free(h); free(c);
+	return (cpShape *)out->shape;
+}
+
+void cpSpaceSegmentQuery(cpSpace *sp, cpVect start, cpVect end, cpFloat radius, cpShapeFilter filter, cpSpaceSegmentQueryFunc func, void *data)
+{
+	cpgQuery q = query_new_(CPG_Q_SEGMENT, start.x, start.y, end.x, end.y, radius, filter);
+	cpgHit *h; int *c, cap;
+	if(!run_queries_(sp, &q, 1, &h, &c, &cap)) return;
+	for(int k = 0; k < c[0] && k < cap; k++){
+		cpShape *shape = slot_shape_(sp, h[k].shape);
+		if(shape && func) func(shape, cpv(h[k].px, h[k].py), cpv(h[k].gx, h[k].gy), h[k].d, data);
+	}
+	free(h); free(c);
+}
+
+cpShape *cpSpaceSegmentQueryFirst(cpSpace *sp, cpVect start, cpVect end, cpFloat radius, cpShapeFilter filter, cpSegmentQueryInfo *out)
+{
+	cpSegmentQueryInfo info = {NULL, end, cpvzero, 1.0};
+	if(out) *out = info; else out = &info;
+	cpgQuery q = query_new_(CPG_Q_SEGMENT_FIRST, start.x, start.y, end.x, end.y, radius, filter);
+	cpgHit *h; int *c, cap;
+	if(!run_queries_(sp, &q, 1, &h, &c, &cap)) return NULL;
+	if(c[0] && slot_shape_(sp, h[0].shape)){
+		out->shape = slot_shape_(sp, h[0].shape);
+		out->point = cpv(h[0].px, h[0].py);
+		out->normal = cpv(h[0].gx, h[0].gy);
+		out->alpha = h[0].d;
+	}
+	free(h); free(c);
+	return (cpShape *)out->shape;
+}
+
+void cpSpaceBBQuery(cpSpace *sp, cpBB bb, cpShapeFilter filter, cpSpaceBBQueryFunc func, void *data)
+{
+	cpgQuery q = query_new_(CPG_Q_BB, bb.l, bb.b, bb.r, bb.t, 0.0, filter);
+	cpgHit *h; int *c, cap;
+	if(!run_queries_(sp, &q, 1, &h, &c, &cap)) return;
+	for(int k = 0; k < c[0] && k < cap; k++){
+		cpShape *shape = slot_shape_(sp, h[k].shape);
+		if(shape && func) func(shape, data);
+	}
+	free(h); free(c);
+}
+
+/* The slot of a shape in its space, or -1 (error set) when it is in none. */
+static int shape_slot_(const cpShape *shape)
+{
+	cpSpace *sp = shape ? shape->space : NULL;
+	if(!sp){
+		set_error(CP_GPU_ERR_UNSUPPORTED, "shape query: the shape is in no space (its geometry lives on the device)");
+		return -1;
+	}
+	for(int i = 0; i < sp->nshapes; i++) if(sp->shapes[i] == shape) return i;
+	set_error(CP_GPU_ERR_ARGUMENT, "shape query: shape not found in its space");
+	return -1;
+}
+
+cpFloat cpShapePointQuery(const cpShape *shape, cpVect p, cpPointQueryInfo *out)
+{
+	cpPointQueryInfo blank = {NULL, cpvzero, INFINITY, cpvzero};
+	if(out) *out = blank; else out = &blank;
+	int slot = shape_slot_(shape);
+	if(slot < 0) return out->distance;
+	cpgQuery q = query_new_(CPG_Q_SHAPE_POINT, p.x, p.y, 0.0, 0.0, 0.0, CP_SHAPE_FILTER_ALL);
+	q.pad = slot;
+	cpgHit *h; int *c, cap;
+	if(!run_queries_(shape->space, &q, 1, &h, &c, &cap)) return out->distance;
+	if(c[0]){
+		out->shape = shape;
+		out->point = cpv(h[0].px, h[0].py);
+		out->distance = h[0].d;
+		out->gradient = cpv(h[0].gx, h[0].gy);
+	}
+	free(h); free(c);
+	return out->distance;
+}
+
+cpBool cpShapeSegmentQuery(const cpShape *shape, cpVect a, cpVect b, cpFloat radius, cpSegmentQueryInfo *info)
+{
+	cpSegmentQueryInfo blank = {NULL, b, cpvzero, 1.0};
+	if(info) *info = blank; else info = &blank;
+	int slot = shape_slot_(shape);
+	if(slot < 0) return cpFalse;
+	cpgQuery q = query_new_(CPG_Q_SHAPE_SEGMENT, a.x, a.y, b.x, b.y, radius, CP_SHAPE_FILTER_ALL);
+	q.pad = slot;
+	cpgHit *h; int *c, cap;
+	if(!run_queries_(shape->space, &q, 1, &h, &c, &cap)) return cpFalse;
+	if(c[0]){
+		info->shape = shape;
+		info->point = cpv(h[0].px, h[0].py);
+		info->normal = cpv(h[0].gx, h[0].gy);
+		info->alpha = h[0].d;
+	}
+	free(h); free(c);
+	return info->shape != NULL;
+}
+
+/* Many nearest-point or first-hit queries in one launch, one thread each. */
+int cpGpuSpacePointQueryNearestBatch(cpSpace *sp, int n, const cpVect *points, cpFloat maxDistance,
+                                     cpShapeFilter filter, cpPointQueryInfo *out)
+{
+	if(n < 0 || (n > 0 && (!points || !out))){ set_error(CP_GPU_ERR_ARGUMENT, "query batch: bad arguments"); return CP_GPU_ERR_ARGUMENT; }
+	cpgQuery *q = HALLOC(cpgQuery, n);
+	for(int i = 0; i < n; i++) q[i] = query_new_(CPG_Q_POINT_NEAREST, points[i].x, points[i].y, 0.0, 0.0, maxDistance, filter);
+	cpgHit *h; int *c, cap;
+	if(!run_queries_(sp, q, n, &h, &c, &cap)){ free(q); return g_error ? g_error : CP_GPU_ERR_CUDA; }
+	for(int i = 0; i < n; i++){
+		cpPointQueryInfo info = {NULL, cpvzero, maxDistance, cpvzero};
+		const cpgHit *r = h + (size_t)i*cap;
+		if(c[i] && slot_shape_(sp, r->shape)){
+			info.shape = slot_shape_(sp, r->shape);
+			info.point = cpv(r->px, r->py); info.distance = r->d; info.gradient = cpv(r->gx, r->gy);
+		}
+		out[i] = info;
+	}
+	free(h); free(c); free(q);
+	return CP_GPU_OK;
+}
+
+int cpGpuSpaceSegmentQueryFirstBatch(cpSpace *sp, int n, const cpVect *starts, const cpVect *ends, cpFloat radius,
+                                     cpShapeFilter filter, cpSegmentQueryInfo *out)
+{
+	if(n < 0 || (n > 0 && (!starts || !ends || !out))){ set_error(CP_GPU_ERR_ARGUMENT, "query batch: bad arguments"); return CP_GPU_ERR_ARGUMENT; }
+	cpgQuery *q = HALLOC(cpgQuery, n);
+	for(int i = 0; i < n; i++) q[i] = query_new_(CPG_Q_SEGMENT_FIRST, starts[i].x, starts[i].y, ends[i].x, ends[i].y, radius, filter);
+	cpgHit *h; int *c, cap;
+	if(!run_queries_(sp, q, n, &h, &c, &cap)){ free(q); return g_error ? g_error : CP_GPU_ERR_CUDA; }
+	for(int i = 0; i < n; i++){
+		cpSegmentQueryInfo info = {NULL, ends[i], cpvzero, 1.0};
+		const cpgHit *r = h + (size_t)i*cap;
+		if(c[i] && slot_shape_(sp, r->shape)){
+			info.shape = slot_shape_(sp, r->shape);
+			info.point = cpv(r->px, r->py); info.normal = cpv(r->gx, r->gy); info.alpha = r->d;
+		}
+		out[i] = info;
+	}
+	free(h); free(c); free(q);
+	return CP_GPU_OK;
 }
 
 void cpGpuSpaceSync(cpSpace *sp)

@@ -85,9 +85,12 @@ typedef struct cpgTree {
 	int moved;                    /* leaves reinserted this step */
 } cpgTree;
 
-/* AABB-tree node (cpBBTree.c:46-60), 64 bytes. */
+/* AABB-tree node (cpBBTree.c:46-60), 96 bytes.  Each box coordinate x
+ * is also kept as the pair of floats rounded down and up from it
+ * (xlo <= x <= xhi), maintained by every box write in cpg_tree.cuh. */
 typedef struct cpgNode {
 	double l, b, r, t;
+	float llo, lhi, blo, bhi, rlo, rhi, tlo, thi;
 	int parent, A, B;
 	int obj;                      /* shape index for leaves, -1 internal */
 	unsigned stamp;
@@ -201,6 +204,25 @@ typedef struct cpgOp {
 	double l, b, r, t;
 	double vx, vy;
 } cpgOp;
+
+/* A spatial query (cpSpaceQuery.c) and one of its results. */
+enum { CPG_Q_POINT = 0, CPG_Q_POINT_NEAREST = 1, CPG_Q_SEGMENT = 2, CPG_Q_SEGMENT_FIRST = 3, CPG_Q_BB = 4,
+       CPG_Q_SHAPE_POINT = 5, CPG_Q_SHAPE_SEGMENT = 6 };   /* the last two: one shape, slot in pad */
+typedef struct cpgQuery {
+	double ax, ay, bx, by;        /* point | segment start, end | box l, b, r, t */
+	double r;                     /* maximum distance | segment radius */
+	unsigned long long group;     /* the query's cpShapeFilter */
+	unsigned cat, mask;
+	int kind;
+	int pad;
+} cpgQuery;
+typedef struct cpgHit {
+	int shape;                    /* world-local shape slot, -1 none */
+	int pad;
+	double px, py;                /* point */
+	double d;                     /* distance | alpha */
+	double gx, gy;                /* gradient | normal */
+} cpgHit;
 
 /* All device arrays of a set.  Vectors are split into x/y arrays. */
 /* Recording of replayed steps for the differentiable rollout. */
@@ -378,6 +400,8 @@ int cpg_launch_replay_solve(const cpgSet *s, const cpgAdj *a, int nsteps, void *
 int cpg_launch_transfer(const cpgSet *to, const cpgSet *from, const int *bodyMap, const unsigned char *deadShape,
                         int *slotMap, void *stream);
 int cpg_launch_contact_quality(const cpgSet *s, int w, double dt, double *acc, void *stream);
+int cpg_launch_query(const cpgSet *s, int world, const cpgQuery *queries, int nq, cpgHit *hits, int cap,
+                     int *counts, int brute, int *status, void *stream);
 int cpg_launch_set_arb_impulses(const cpgSet *s, int w, const double *imp, const int *pairs, int n, int *mismatch, void *stream);
 
 #ifdef __cplusplus

@@ -2951,7 +2951,7 @@ static cudaError_t launch_coop(const void *kernel, int threads, cpgSet *s, int w
 #define CPG_STAGED_BODIES 3200
 /* Worlds whose tree node pool has at most this many nodes run the tree step
  * with the pool in shared memory (64 bytes a node, 192 KB at most). */
-#define CPG_STAGED_NODES 3072
+#define CPG_STAGED_NODES 2048
 
 /* `h` is the host copy of the set's sizes (same struct, host values). */
 /* A many-world step as a CUDA graph: captured from cpg_launch_step, and
@@ -3065,7 +3065,7 @@ extern "C" int cpg_launch_step(const cpgSet *s, const cpgSet *h, int mode, void 
 		LAUNCH(k_scan_excl<<<1, 1024, 0, st>>>(s->sapCount, n + 1, NULL));
 		LAUNCH(k_sap_emit<<<blocks_for(32*n, 256), 256, 0, st>>>(*s, 0));
 	} else {
-		/* node pools of up to CPG_STAGED_NODES nodes (64 B each) run from
+		/* node pools of up to CPG_STAGED_NODES nodes (96 B each) run from
 		 * shared memory; larger worlds use the global pool */
 		int staged = h->hostMaxNodes <= CPG_STAGED_NODES ? h->hostMaxNodes : 0;
 		/* the tree is one serial thread per world: many worlds gain more

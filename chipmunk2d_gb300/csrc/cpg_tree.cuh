@@ -67,8 +67,120 @@ __device__ __forceinline__ bool tcontains(BB bb, BB o)
 __device__ __forceinline__ BB tmerge(BB a, BB b) { return bbnew(tmin(a.l, b.l), tmin(a.b, b.b), tmax(a.r, b.r), tmax(a.t, b.t)); }
 __device__ __forceinline__ double tmergedarea(BB a, BB b) { return (tmax(a.r, b.r) - tmin(a.l, b.l))*(tmax(a.t, b.t) - tmin(a.b, b.b)); }
 
+/* ---- float brackets of the boxes ----
+ * A node keeps, beside each double coordinate x, the floats rounded down
+ * and up from it (lo <= x <= hi, equal when x is a float).  Rounding is
+ * monotone, so lo(min(a, b)) = min(lo(a), lo(b)) and likewise for hi and
+ * max: a merged box's brackets are min/max of its children's, with no
+ * conversion.  The brackets decide most comparisons and the insertion
+ * cost test in FP32 (full rate), and only near-ties fall back to the exact
+ * doubles.  The decisions are the exact ones: a_hi < b_lo implies a < b;
+ * and a cost computed in doubles, each operation rounded to nearest,
+ * lies inside the FP32 interval computed with the rounding directed
+ * outwards, because a double rounded to nearest stays between any two
+ * floats that bracket the exact value. */
+struct FBox { float llo, lhi, blo, bhi, rlo, rhi, tlo, thi; };
+
 __device__ __forceinline__ BB node_bb(const cpgNode &n) { return bbnew(n.l, n.b, n.r, n.t); }
-__device__ __forceinline__ void set_node_bb(cpgNode &n, BB bb) { n.l = bb.l; n.b = bb.b; n.r = bb.r; n.t = bb.t; }
+__device__ __forceinline__ FBox node_fbox(const cpgNode &n)
+{
+	FBox f;
+	f.llo = n.llo; f.lhi = n.lhi; f.blo = n.blo; f.bhi = n.bhi;
+	f.rlo = n.rlo; f.rhi = n.rhi; f.tlo = n.tlo; f.thi = n.thi;
+	return f;
+}
+__device__ __forceinline__ void set_node_box(cpgNode &n, BB bb, FBox f)
+{
+	n.l = bb.l; n.b = bb.b; n.r = bb.r; n.t = bb.t;
+	n.llo = f.llo; n.lhi = f.lhi; n.blo = f.blo; n.bhi = f.bhi;
+	n.rlo = f.rlo; n.rhi = f.rhi; n.tlo = f.tlo; n.thi = f.thi;
+}
+
+/* x rounded down (lo) and up (hi) to floats.  In the normal float range
+ * by bit arithmetic: the truncated mantissa is the magnitude rounded
+ * towards zero, and one more unit in its last place (a carry runs into
+ * the exponent) the magnitude rounded away from zero; elsewhere (zero,
+ * float-subnormal, out of range, NaN) by the conversion intrinsics. */
+__device__ __forceinline__ void f32_bracket(double x, float &lo, float &hi)
+{
+	unsigned long long u = (unsigned long long)__double_as_longlong(x);
+	unsigned h = (unsigned)(u >> 32);
+	int e = (int)((h >> 20) & 0x7FFu);
+	if(e < 1023 - 126 || e > 1023 + 127){
+		lo = __double2float_rd(x);
+		hi = __double2float_ru(x);
+		return;
+	}
+	unsigned sign = h & 0x80000000u;
+	unsigned mag = ((unsigned)(e - 1023 + 127) << 23) | (unsigned)((u >> 29) & 0x7FFFFFu);
+	float tz = __uint_as_float(sign | mag);
+	if((u & 0x1FFFFFFFull) == 0ull){ lo = hi = tz; return; }
+	float away = __uint_as_float(sign | (mag + 1u));
+	if(sign){ lo = away; hi = tz; } else { lo = tz; hi = away; }
+}
+
+__device__ __forceinline__ FBox fbox_of(BB bb)
+{
+	FBox f;
+	f32_bracket(bb.l, f.llo, f.lhi); f32_bracket(bb.b, f.blo, f.bhi);
+	f32_bracket(bb.r, f.rlo, f.rhi); f32_bracket(bb.t, f.tlo, f.thi);
+	return f;
+}
+
+__device__ __forceinline__ void set_node_bb(cpgNode &n, BB bb) { set_node_box(n, bb, fbox_of(bb)); }
+
+/* tmin/tmax decided by the brackets when they are apart */
+__device__ __forceinline__ double bmin(double a, float alo, float ahi, double b, float blo, float bhi)
+{
+	if(ahi < blo) return a;
+	if(bhi < alo) return b;
+	return tmin(a, b);
+}
+__device__ __forceinline__ double bmax(double a, float alo, float ahi, double b, float blo, float bhi)
+{
+	if(alo > bhi) return a;
+	if(blo > ahi) return b;
+	return tmax(a, b);
+}
+
+/* tmerge(a, b) and the merged brackets */
+__device__ __forceinline__ void bmerge(BB a, const FBox &fa, BB b, const FBox &fb, BB &m, FBox &fm)
+{
+	m.l = bmin(a.l, fa.llo, fa.lhi, b.l, fb.llo, fb.lhi);
+	m.b = bmin(a.b, fa.blo, fa.bhi, b.b, fb.blo, fb.bhi);
+	m.r = bmax(a.r, fa.rlo, fa.rhi, b.r, fb.rlo, fb.rhi);
+	m.t = bmax(a.t, fa.tlo, fa.thi, b.t, fb.tlo, fb.thi);
+	fm.llo = fminf(fa.llo, fb.llo); fm.lhi = fminf(fa.lhi, fb.lhi);
+	fm.blo = fminf(fa.blo, fb.blo); fm.bhi = fminf(fa.bhi, fb.bhi);
+	fm.rlo = fmaxf(fa.rlo, fb.rlo); fm.rhi = fmaxf(fa.rhi, fb.rhi);
+	fm.tlo = fmaxf(fa.tlo, fb.tlo); fm.thi = fmaxf(fa.thi, fb.thi);
+}
+
+/* Interval of bbarea over a box's brackets.  A box whose width or height
+ * may be negative gets the unbounded interval (its cost test then runs
+ * in doubles). */
+__device__ __forceinline__ void farea(float llo, float lhi, float blo, float bhi,
+                                      float rlo, float rhi, float tlo, float thi, float &lo, float &hi)
+{
+	float wlo = __fsub_rd(rlo, lhi), whi = __fsub_ru(rhi, llo);
+	float hlo = __fsub_rd(tlo, bhi), hhi = __fsub_ru(thi, blo);
+	if(wlo >= 0.0f && hlo >= 0.0f){
+		lo = __fmul_rd(wlo, hlo);
+		hi = __fmul_ru(whi, hhi);
+	} else {
+		lo = -INFINITY; hi = INFINITY;
+	}
+}
+__device__ __forceinline__ void fbox_area(const FBox &f, float &lo, float &hi)
+{
+	farea(f.llo, f.lhi, f.blo, f.bhi, f.rlo, f.rhi, f.tlo, f.thi, lo, hi);
+}
+/* interval of tmergedarea(a, b) */
+__device__ __forceinline__ void fmerged_area(const FBox &a, const FBox &b, float &lo, float &hi)
+{
+	farea(fminf(a.llo, b.llo), fminf(a.lhi, b.lhi), fminf(a.blo, b.blo), fminf(a.bhi, b.bhi),
+	      fmaxf(a.rlo, b.rlo), fmaxf(a.rhi, b.rhi), fmaxf(a.tlo, b.tlo), fmaxf(a.thi, b.thi), lo, hi);
+}
 __device__ __forceinline__ bool is_leaf(const TreeCtx &c, int n) { return c.nodes[n].obj >= 0; }
 
 __device__ __forceinline__ BB shape_bb(const TreeCtx &c, int s) { return bbnew(c.bbl[s], c.bbb[s], c.bbr[s], c.bbt[s]); }
@@ -192,6 +304,7 @@ __device__ void pair_insert(TreeCtx &c, int a, int b)
 /* A node's box and links in registers. */
 struct NodeRec {
 	BB bb;
+	FBox f;
 	int parent, A, B, obj;
 };
 
@@ -200,18 +313,21 @@ __device__ __forceinline__ NodeRec node_rec(const TreeCtx &c, int n)
 	const cpgNode &nd = c.nodes[n];
 	NodeRec r;
 	r.bb = node_bb(nd);
+	r.f = node_fbox(nd);
 	r.parent = nd.parent; r.A = nd.A; r.B = nd.B; r.obj = nd.obj;
 	return r;
 }
 
 /* cpBBTree.c:250-267, with the children's boxes passed in */
-__device__ int node_new_bb(TreeCtx &c, int a, BB abb, int b, BB bbb)
+__device__ int node_new_bb(TreeCtx &c, int a, BB abb, const FBox &fa, int b, BB bbb, const FBox &fb)
 {
 	int n = node_alloc(c);
 	if(n < 0) return -1;
 	cpgNode &nd = c.nodes[n];
 	nd.obj = -1;
-	set_node_bb(nd, tmerge(abb, bbb));
+	BB m; FBox fm;
+	bmerge(abb, fa, bbb, fb, m, fm);
+	set_node_box(nd, m, fm);
 	nd.parent = -1;
 	nd.A = a; c.nodes[a].parent = n;
 	nd.B = b; c.nodes[b].parent = n;
@@ -221,7 +337,8 @@ __device__ int node_new_bb(TreeCtx &c, int a, BB abb, int b, BB bbb)
 
 __device__ int node_new(TreeCtx &c, int a, int b)
 {
-	return node_new_bb(c, a, node_bb(c.nodes[a]), b, node_bb(c.nodes[b]));
+	const cpgNode &na = c.nodes[a], &nb = c.nodes[b];
+	return node_new_bb(c, a, node_bb(na), node_fbox(na), b, node_bb(nb), node_fbox(nb));
 }
 
 /* cpBBTree.c:281-299.  The refit from the parent up to the root is one
@@ -232,6 +349,7 @@ __device__ void node_replace_child(TreeCtx &c, int parent, int child, int value)
 {
 	cpgNode &pn = c.nodes[parent];
 	BB fromBB = node_bb(c.nodes[value]);
+	FBox fromF = node_fbox(c.nodes[value]);
 	if(pn.A == child){
 		node_recycle(c, pn.A);
 		pn.A = value; c.nodes[value].parent = parent;
@@ -244,16 +362,20 @@ __device__ void node_replace_child(TreeCtx &c, int parent, int child, int value)
 	for(int guard = 0;; guard++){
 		if(guard > c.nodeCap){ c.T->error |= CPG_ERR_NODES; return; }
 		bool fromA = (a == from);
-		BB sbb = node_bb(c.nodes[fromA ? b : a]);
+		const cpgNode &sn = c.nodes[fromA ? b : a];
+		BB sbb = node_bb(sn);
+		FBox sf = node_fbox(sn);
 		int na = -1, nb = -1, nup = -1;
 		if(up >= 0){
 			const cpgNode &un = c.nodes[up];
 			na = un.A; nb = un.B; nup = un.parent;
 		}
-		BB m = fromA ? tmerge(fromBB, sbb) : tmerge(sbb, fromBB);
-		set_node_bb(c.nodes[n], m);
+		BB m; FBox fm;
+		if(fromA) bmerge(fromBB, fromF, sbb, sf, m, fm);
+		else bmerge(sbb, sf, fromBB, fromF, m, fm);
+		set_node_box(c.nodes[n], m, fm);
 		if(up < 0) return;
-		from = n; fromBB = m; n = up;
+		from = n; fromBB = m; fromF = fm; n = up;
 		a = na; b = nb; up = nup;
 	}
 }
@@ -269,24 +391,41 @@ __device__ int subtree_insert(TreeCtx &c, int root, int leaf)
 	if(root < 0) return leaf;
 	NodeRec nd = node_rec(c, root);
 	if(nd.obj >= 0) return node_new(c, leaf, root);
-	BB lbb = node_bb(c.nodes[leaf]);
+	const cpgNode &ln = c.nodes[leaf];
+	BB lbb = node_bb(ln);
+	FBox lf = node_fbox(ln);
 	int cur = root;
 	for(int guard = 0;; guard++){
 		if(guard > c.nodeCap){ c.T->error |= CPG_ERR_NODES; return root; }
 		NodeRec ra = node_rec(c, nd.A), rb = node_rec(c, nd.B);
-		BB abb = ra.bb, bbb = rb.bb;
-		double cost_a = bbarea(bbb) + tmergedarea(abb, lbb);
-		double cost_b = bbarea(abb) + tmergedarea(bbb, lbb);
-		if(tkey(cost_a) == tkey(cost_b)){
-			cost_a = bbproximity(abb, lbb);
-			cost_b = bbproximity(bbb, lbb);
+		/* the cost test on intervals; doubles only when they overlap */
+		float aLo, aHi, bLo, bHi, maLo, maHi, mbLo, mbHi;
+		fbox_area(ra.f, aLo, aHi);
+		fbox_area(rb.f, bLo, bHi);
+		fmerged_area(ra.f, lf, maLo, maHi);
+		fmerged_area(rb.f, lf, mbLo, mbHi);
+		float caLo = __fadd_rd(bLo, maLo), caHi = __fadd_ru(bHi, maHi);
+		float cbLo = __fadd_rd(aLo, mbLo), cbHi = __fadd_ru(aHi, mbHi);
+		bool goB;
+		if(cbHi < caLo) goB = true;
+		else if(caHi < cbLo) goB = false;
+		else {
+			BB abb = ra.bb, bbb = rb.bb;
+			double cost_a = bbarea(bbb) + tmergedarea(abb, lbb);
+			double cost_b = bbarea(abb) + tmergedarea(bbb, lbb);
+			if(tkey(cost_a) == tkey(cost_b)){
+				cost_a = bbproximity(abb, lbb);
+				cost_b = bbproximity(bbb, lbb);
+			}
+			goB = (tkey(cost_b) < tkey(cost_a));
 		}
-		bool goB = (tkey(cost_b) < tkey(cost_a));
 		int child = goB ? nd.B : nd.A;
 		NodeRec rc = goB ? rb : ra;
-		set_node_bb(c.nodes[cur], tmerge(nd.bb, lbb));
+		BB m; FBox fm;
+		bmerge(nd.bb, nd.f, lbb, lf, m, fm);
+		set_node_box(c.nodes[cur], m, fm);
 		if(rc.obj >= 0){
-			int nn = node_new_bb(c, leaf, lbb, child, rc.bb);
+			int nn = node_new_bb(c, leaf, lbb, lf, child, rc.bb, rc.f);
 			if(nn < 0) return root;
 			if(goB) c.nodes[cur].B = nn; else c.nodes[cur].A = nn;
 			c.nodes[nn].parent = cur;

@@ -774,6 +774,116 @@ cpBody *cpx_scene_body(void *h, int i) { return ((cpxScene *)h)->bodies[i]; }
 cpShape *cpx_scene_shape(void *h, int i) { return ((cpxScene *)h)->shapes[i]; }
 cpConstraint *cpx_scene_constraint(void *h, int i) { return ((cpxScene *)h)->constraints[i]; }
 
+/* ---- spatial queries through the public API ----
+ * nq seeded queries over the scene's extent, cycling through the kinds:
+ * 0 cpSpacePointQuery, 1 cpSpacePointQueryNearest, 2 cpSpaceSegmentQuery,
+ * 3 cpSpaceSegmentQueryFirst, 4 cpSpaceBBQuery, 5 cpShapePointQuery,
+ * 6 cpShapeSegmentQuery.  Every callback and every result is one record
+ * of 8 doubles: query, kind, shape (its index in the scene, -1 none),
+ * point x, y, distance or alpha, gradient or normal x, y.  Returns the
+ * record count (records past cap are counted, not written). */
+typedef struct QRec { double *out; int cap, n, qi, kind; } QRec;
+
+static int shape_index_(const cpShape *s) { return s ? (int)(intptr_t)cpShapeGetUserData(s) - 1 : -1; }
+
+static void q_put(QRec *r, int shape, cpVect p, double d, cpVect g)
+{
+	if(r->n < r->cap){
+		double *o = r->out + 8*(size_t)r->n;
+		o[0] = r->qi; o[1] = r->kind; o[2] = shape; o[3] = p.x; o[4] = p.y; o[5] = d; o[6] = g.x; o[7] = g.y;
+	}
+	r->n++;
+}
+static void q_point_cb(cpShape *s, cpVect p, cpFloat d, cpVect g, void *data) { q_put((QRec *)data, shape_index_(s), p, d, g); }
+static void q_seg_cb(cpShape *s, cpVect p, cpVect n, cpFloat a, void *data) { q_put((QRec *)data, shape_index_(s), p, a, n); }
+static void q_bb_cb(cpShape *s, void *data) { q_put((QRec *)data, shape_index_(s), cpvzero, 0.0, cpvzero); }
+
+int cpx_scene_queries(void *h, int seed, int nq, double *out, int cap)
+{
+	cpxScene *sc = (cpxScene *)h;
+	cpSpace *sp = sc->space;
+	int *live = (int *)malloc(sizeof(int)*(size_t)(sc->nshapes > 0 ? sc->nshapes : 1));
+	int nlive = 0;
+	cpBB ext = cpBBNew(0.0, 0.0, 0.0, 0.0);
+	for(int i = 0; i < sc->nshapes; i++){
+		cpShape *s = sc->shapes[i];
+		cpShapeSetUserData(s, (cpDataPointer)(intptr_t)(i + 1));
+		if(cpShapeGetSpace(s) != sp) continue;
+		cpBB bb = cpShapeGetBB(s);
+		ext = nlive ? cpBBNew(bb.l < ext.l ? bb.l : ext.l, bb.b < ext.b ? bb.b : ext.b,
+		                      bb.r > ext.r ? bb.r : ext.r, bb.t > ext.t ? bb.t : ext.t) : bb;
+		live[nlive++] = i;
+	}
+	QRec rec = {out, cap, 0, 0, 0};
+	Rng rng;
+	rng_seed(&rng, (uint64_t)seed*0x9e3779b97f4a7c15ULL + 17u);
+	double size = (ext.r - ext.l) > (ext.t - ext.b) ? (ext.r - ext.l) : (ext.t - ext.b);
+	for(int qi = 0; qi < nq && nlive > 0; qi++){
+		int kind = qi % 7;
+		rec.qi = qi; rec.kind = kind;
+		/* near a shape half of the time, anywhere in the extent otherwise */
+		cpShape *target = sc->shapes[live[rng_int(&rng, 0, nlive - 1)]];
+		cpBB tb = cpShapeGetBB(target);
+		int nearShape = rng_int(&rng, 0, 1);
+		double x0 = rng_uniform(&rng, ext.l, ext.r);
+		double y0 = rng_uniform(&rng, ext.b, ext.t);
+		cpVect p = nearShape ? cpv(0.5*(tb.l + tb.r) + rng_uniform(&rng, -2.0, 2.0), 0.5*(tb.b + tb.t) + rng_uniform(&rng, -2.0, 2.0)) : cpv(x0, y0);
+		cpShapeFilter filter = CP_SHAPE_FILTER_ALL;
+		if(rng_int(&rng, 0, 3) == 0){
+			cpGroup grp = (cpGroup)rng_int(&rng, 0, 3);
+			cpBitmask cat = (cpBitmask)1u << rng_int(&rng, 0, 3);
+			cpBitmask mask = (cpBitmask)rng_int(&rng, 1, 15);
+			filter = cpShapeFilterNew(grp, cat, mask);
+		}
+		double len = rng_uniform(&rng, 2.0, 0.25*size + 2.0);
+		cpVect dir = rng_direction(&rng);
+		cpVect q = cpvadd(p, cpvmult(dir, len));
+		double r = rng_int(&rng, 0, 2) == 0 ? 0.0 : rng_uniform(&rng, 0.0, 1.5);
+		switch(kind){
+		case 0: {
+			double md = rng_int(&rng, 0, 4) == 0 ? -0.25 : rng_uniform(&rng, 0.0, 4.0);
+			cpSpacePointQuery(sp, p, md, filter, q_point_cb, &rec);
+			break;
+		}
+		case 1: {
+			cpPointQueryInfo info;
+			double md = rng_uniform(&rng, 0.5, 20.0);
+			cpShape *s = cpSpacePointQueryNearest(sp, p, md, filter, &info);
+			q_put(&rec, s ? shape_index_(s) : -1, info.point, info.distance, info.gradient);
+			break;
+		}
+		case 2:
+			cpSpaceSegmentQuery(sp, p, q, r, filter, q_seg_cb, &rec);
+			break;
+		case 3: {
+			cpSegmentQueryInfo info;
+			cpShape *s = cpSpaceSegmentQueryFirst(sp, p, q, r, filter, &info);
+			q_put(&rec, s ? shape_index_(s) : -1, info.point, info.alpha, info.normal);
+			break;
+		}
+		case 4: {
+			double hw = rng_uniform(&rng, 1.0, 30.0), hh = rng_uniform(&rng, 1.0, 30.0);
+			cpSpaceBBQuery(sp, cpBBNew(p.x - hw, p.y - hh, p.x + hw, p.y + hh), filter, q_bb_cb, &rec);
+			break;
+		}
+		case 5: {
+			cpPointQueryInfo info;
+			double d = cpShapePointQuery(target, p, &info);
+			q_put(&rec, shape_index_(target), info.point, d, info.gradient);
+			break;
+		}
+		default: {
+			cpSegmentQueryInfo info;
+			cpBool hit = cpShapeSegmentQuery(target, p, q, r, &info);
+			q_put(&rec, hit ? shape_index_(target) : -1, info.point, info.alpha, info.normal);
+			break;
+		}
+		}
+	}
+	free(live);
+	return rec.n;
+}
+
 /* Public-getter view of every dynamic body: position (transform origin),
  * velocity, angle, angular velocity, rotation -- 8 doubles per body. */
 int cpx_scene_dump_public(void *h, double *out)

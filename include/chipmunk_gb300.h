@@ -134,6 +134,11 @@ typedef void (*cpSpaceBodyIteratorFunc)(cpBody *body, void *data);
 typedef void (*cpSpaceShapeIteratorFunc)(cpShape *shape, void *data);
 typedef void (*cpSpaceConstraintIteratorFunc)(cpConstraint *constraint, void *data);
 
+/* Query callbacks: cpSpace.h:196-210 */
+typedef void (*cpSpacePointQueryFunc)(cpShape *shape, cpVect point, cpFloat distance, cpVect gradient, void *data);
+typedef void (*cpSpaceSegmentQueryFunc)(cpShape *shape, cpVect point, cpVect normal, cpFloat alpha, void *data);
+typedef void (*cpSpaceBBQueryFunc)(cpShape *shape, void *data);
+
 /* cpConstraint.h:25-29 */
 typedef void (*cpConstraintPreSolveFunc)(cpConstraint *constraint, cpSpace *space);
 typedef void (*cpConstraintPostSolveFunc)(cpConstraint *constraint, cpSpace *space);
@@ -245,6 +250,23 @@ void cpSpaceEachBody(cpSpace *space, cpSpaceBodyIteratorFunc func, void *data); 
 void cpSpaceEachShape(cpSpace *space, cpSpaceShapeIteratorFunc func, void *data);           /* cpSpace.h:231 */
 void cpSpaceEachConstraint(cpSpace *space, cpSpaceConstraintIteratorFunc func, void *data); /* cpSpace.h:236 */
 void cpSpaceStep(cpSpace *space, cpFloat dt);                        /* cpSpace.h:255 */
+/* Spatial queries (cpSpaceQuery.c:49-212).  They run on the device, over
+ * the space's own trees in the exact-order mode (the reference's visit
+ * order: dynamic then static shapes for point and box queries, static
+ * then dynamic for segment queries), and the callbacks are then called
+ * on the host in that order.  Objects added or removed since the last
+ * step are indexed first.  In the coloured mode the dynamic tree is not
+ * kept current, so every shape is tested and callbacks come in the
+ * space's shape order. */
+void cpSpacePointQuery(cpSpace *space, cpVect point, cpFloat maxDistance, cpShapeFilter filter,
+                       cpSpacePointQueryFunc func, void *data);                                    /* cpSpace.h:198 */
+cpShape *cpSpacePointQueryNearest(cpSpace *space, cpVect point, cpFloat maxDistance, cpShapeFilter filter,
+                                  cpPointQueryInfo *out);                                          /* cpSpace.h:200 */
+void cpSpaceSegmentQuery(cpSpace *space, cpVect start, cpVect end, cpFloat radius, cpShapeFilter filter,
+                         cpSpaceSegmentQueryFunc func, void *data);                                /* cpSpace.h:205 */
+cpShape *cpSpaceSegmentQueryFirst(cpSpace *space, cpVect start, cpVect end, cpFloat radius, cpShapeFilter filter,
+                                  cpSegmentQueryInfo *out);                                        /* cpSpace.h:207 */
+void cpSpaceBBQuery(cpSpace *space, cpBB bb, cpShapeFilter filter, cpSpaceBBQueryFunc func, void *data); /* cpSpace.h:212 */
 
 /* ------------------------------------------------------------------------
  * Body: cpBody.h:49-187
@@ -325,6 +347,10 @@ cpCollisionType cpShapeGetCollisionType(const cpShape *shape);       /* cpShape.
 void cpShapeSetCollisionType(cpShape *shape, cpCollisionType t);     /* cpShape.h:154 */
 cpShapeFilter cpShapeGetFilter(const cpShape *shape);                /* cpShape.h:157 */
 void cpShapeSetFilter(cpShape *shape, cpShapeFilter filter);         /* cpShape.h:159 */
+/* One shape against a point or a segment, on its world geometry of the
+ * last step (cpShape.c:222-256). */
+cpFloat cpShapePointQuery(const cpShape *shape, cpVect p, cpPointQueryInfo *out);                  /* cpShape.h:89 */
+cpBool cpShapeSegmentQuery(const cpShape *shape, cpVect a, cpVect b, cpFloat radius, cpSegmentQueryInfo *info); /* cpShape.h:92 */
 cpShape *cpCircleShapeNew(cpBody *body, cpFloat radius, cpVect offset);      /* cpShape.h:170 */
 cpVect cpCircleShapeGetOffset(const cpShape *shape);                         /* cpShape.h:173 */
 cpFloat cpCircleShapeGetRadius(const cpShape *shape);                        /* cpShape.h:175 */

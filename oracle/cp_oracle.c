@@ -2941,3 +2941,354 @@ int cpx_dump_candidates(cpSpace *sp, int *out, int max)
 	for(int i = 0; i < n && i < max; i++){ out[2*i] = sp->candPairs[2*i]; out[2*i + 1] = sp->candPairs[2*i + 1]; }
 	return n;
 }
+
+/* ========================================================================
+ * Spatial queries: cpSpaceQuery.c:49-212 over the two trees (cpBBTree.c
+ * SubtreeQuery :355-365, SubtreeSegmentQuery :367-385), with the shapes'
+ * point and segment queries (cpShape.c:222-256, 298-318, 407-468,
+ * cpPolyShape.c:66-149, chipmunk_private.h:120-142).
+ * ====================================================================== */
+#define ORC_MAGIC_EPSILON 1e-5
+
+static int filter_reject_(cpShapeFilter a, cpShapeFilter b)
+{
+	return (a.group != 0 && a.group == b.group) || (a.categories & b.mask) == 0 || (b.categories & a.mask) == 0;
+}
+
+/* chipmunk.h:183-188 */
+static cpVect closest_on_segment_(cpVect p, cpVect a, cpVect b)
+{
+	cpVect delta = cpvsub(a, b);
+	cpFloat t = fclamp01_(cpvdot(delta, cpvsub(p, b))/cpvlengthsq(delta));
+	return cpvadd(b, cpvmult(delta, t));
+}
+
+/* chipmunk_private.h:120-142 */
+static void circle_segment_query_(const cpShape *shape, cpVect center, cpFloat r1, cpVect a, cpVect b, cpFloat r2, cpSegmentQueryInfo *info)
+{
+	cpVect da = cpvsub(a, center);
+	cpVect db = cpvsub(b, center);
+	cpFloat rsum = r1 + r2;
+	cpFloat qa = cpvdot(da, da) - 2.0*cpvdot(da, db) + cpvdot(db, db);
+	cpFloat qb = cpvdot(da, db) - cpvdot(da, da);
+	cpFloat det = qb*qb - qa*(cpvdot(da, da) - rsum*rsum);
+	if(det >= 0.0){
+		cpFloat t = (-qb - sqrt(det))/(qa);
+		if(0.0 <= t && t <= 1.0){
+			cpVect n = cpvnormalize(cpvlerp(da, db, t));
+			info->shape = shape;
+			info->point = cpvsub(cpvlerp(a, b, t), cpvmult(n, r2));
+			info->normal = n;
+			info->alpha = t;
+		}
+	}
+}
+
+static void shape_point_query_(const cpShape *s, cpVect p, cpPointQueryInfo *info)
+{
+	if(s->kind == SHAPE_CIRCLE){
+		/* cpShape.c:298-312 */
+		cpVect delta = cpvsub(p, s->tc);
+		cpFloat d = cpvlength(delta);
+		cpFloat r = s->r;
+		info->shape = s;
+		cpFloat r_over_d = d > 0.0 ? r/d : r;
+		info->point = cpvadd(s->tc, cpvmult(delta, r_over_d));
+		info->distance = d - r;
+		info->gradient = (d > ORC_MAGIC_EPSILON ? cpvmult(delta, 1.0/d) : cpv(0.0, 1.0));
+	} else if(s->kind == SHAPE_SEGMENT){
+		/* cpShape.c:407-423; the small-distance gradient is the local normal */
+		cpVect closest = closest_on_segment_(p, s->ta, s->tb);
+		cpVect delta = cpvsub(p, closest);
+		cpFloat d = cpvlength(delta);
+		cpFloat r = s->r;
+		cpVect g = cpvmult(delta, 1.0/d);
+		info->shape = s;
+		info->point = (d ? cpvadd(closest, cpvmult(g, r)) : closest);
+		info->distance = d - r;
+		info->gradient = (d > ORC_MAGIC_EPSILON ? g : s->sn);
+	} else {
+		/* cpPolyShape.c:66-103 */
+		int count = s->count;
+		cpFloat r = s->r;
+		cpVect v0 = s->pv[count - 1];
+		cpFloat minDist = ORC_INF;
+		cpVect closestPoint = cpvzero, closestNormal = cpvzero;
+		cpBool outside = cpFalse;
+		for(int i = 0; i < count; i++){
+			cpVect v1 = s->pv[i];
+			outside = outside || (cpvdot(s->pn[i], cpvsub(p, v1)) > 0.0);
+			cpVect closest = closest_on_segment_(p, v0, v1);
+			cpFloat dist = cpvdist(p, closest);
+			if(dist < minDist){
+				minDist = dist;
+				closestPoint = closest;
+				closestNormal = s->pn[i];
+			}
+			v0 = v1;
+		}
+		cpFloat dist = (outside ? minDist : -minDist);
+		cpVect g = cpvmult(cpvsub(p, closestPoint), 1.0/dist);
+		info->shape = s;
+		info->point = cpvadd(closestPoint, cpvmult(g, r));
+		info->distance = dist - r;
+		info->gradient = (minDist > ORC_MAGIC_EPSILON ? g : closestNormal);
+	}
+}
+
+static void shape_segment_query_(const cpShape *s, cpVect a, cpVect b, cpFloat r2, cpSegmentQueryInfo *info)
+{
+	if(s->kind == SHAPE_CIRCLE){
+		circle_segment_query_(s, s->tc, s->r, a, b, r2, info);
+	} else if(s->kind == SHAPE_SEGMENT){
+		/* cpShape.c:425-468 */
+		cpVect n = s->tn;
+		cpFloat d = cpvdot(cpvsub(s->ta, a), n);
+		cpFloat r = s->r + r2;
+		cpVect flipped_n = (d > 0.0 ? cpvneg(n) : n);
+		cpVect seg_offset = cpvsub(cpvmult(flipped_n, r), a);
+		cpVect seg_a = cpvadd(s->ta, seg_offset);
+		cpVect seg_b = cpvadd(s->tb, seg_offset);
+		cpVect delta = cpvsub(b, a);
+		if(cpvcross(delta, seg_a)*cpvcross(delta, seg_b) <= 0.0){
+			cpFloat d_offset = d + (d > 0.0 ? -r : r);
+			cpFloat ad = -d_offset;
+			cpFloat bd = cpvdot(delta, n) - d_offset;
+			if(ad*bd < 0.0){
+				cpFloat t = ad/(ad - bd);
+				info->shape = s;
+				info->point = cpvsub(cpvlerp(a, b, t), cpvmult(flipped_n, r2));
+				info->normal = flipped_n;
+				info->alpha = t;
+			}
+		} else if(r != 0.0){
+			cpSegmentQueryInfo info1 = {NULL, b, cpvzero, 1.0};
+			cpSegmentQueryInfo info2 = {NULL, b, cpvzero, 1.0};
+			circle_segment_query_(s, s->ta, s->r, a, b, r2, &info1);
+			circle_segment_query_(s, s->tb, s->r, a, b, r2, &info2);
+			if(info1.alpha < info2.alpha) *info = info1; else *info = info2;
+		}
+	} else {
+		/* cpPolyShape.c:105-149 */
+		int count = s->count;
+		cpFloat r = s->r;
+		cpFloat rsum = r + r2;
+		for(int i = 0; i < count; i++){
+			cpVect n = s->pn[i];
+			cpFloat an = cpvdot(a, n);
+			cpFloat d = an - cpvdot(s->pv[i], n) - rsum;
+			if(d < 0.0) continue;
+			cpFloat bn = cpvdot(b, n);
+			cpFloat t = d/fmax_(an - bn, DBL_MIN);
+			if(t < 0.0 || 1.0 < t) continue;
+			cpVect point = cpvlerp(a, b, t);
+			cpFloat dt = cpvcross(n, point);
+			cpFloat dtMin = cpvcross(n, s->pv[(i - 1 + count)%count]);
+			cpFloat dtMax = cpvcross(n, s->pv[i]);
+			if(dtMin <= dt && dt <= dtMax){
+				info->shape = s;
+				info->point = cpvsub(cpvlerp(a, b, t), cpvmult(n, r2));
+				info->normal = n;
+				info->alpha = t;
+			}
+		}
+		if(rsum > 0.0){
+			for(int i = 0; i < count; i++){
+				cpSegmentQueryInfo circle_info = {NULL, b, cpvzero, 1.0};
+				circle_segment_query_(s, s->pv[i], r, a, b, r2, &circle_info);
+				if(circle_info.alpha < info->alpha) *info = circle_info;
+			}
+		}
+	}
+}
+
+/* cpShape.c:222-235 */
+cpFloat cpShapePointQuery(const cpShape *shape, cpVect p, cpPointQueryInfo *info)
+{
+	cpPointQueryInfo blank = {NULL, cpvzero, ORC_INF, cpvzero};
+	if(info) *info = blank; else info = &blank;
+	shape_point_query_(shape, p, info);
+	return info->distance;
+}
+
+/* cpShape.c:238-256 */
+cpBool cpShapeSegmentQuery(const cpShape *shape, cpVect a, cpVect b, cpFloat radius, cpSegmentQueryInfo *info)
+{
+	cpSegmentQueryInfo blank = {NULL, b, cpvzero, 1.0};
+	if(info) *info = blank; else info = &blank;
+	cpPointQueryInfo nearest;
+	shape_point_query_(shape, a, &nearest);
+	if(nearest.distance <= radius){
+		info->shape = shape;
+		info->alpha = 0.0;
+		info->normal = cpvnormalize(cpvsub(a, nearest.point));
+	} else {
+		shape_segment_query_(shape, a, b, radius, info);
+	}
+	return (info->shape != NULL);
+}
+
+/* cpBB.h:115-143 */
+static cpFloat bb_segment_query_(cpBB bb, cpVect a, cpVect b)
+{
+	cpVect delta = cpvsub(b, a);
+	cpFloat tmin = -ORC_INF, tmax = ORC_INF;
+	if(delta.x == 0.0){
+		if(a.x < bb.l || bb.r < a.x) return ORC_INF;
+	} else {
+		cpFloat t1 = (bb.l - a.x)/delta.x;
+		cpFloat t2 = (bb.r - a.x)/delta.x;
+		tmin = fmax_(tmin, fmin_(t1, t2));
+		tmax = fmin_(tmax, fmax_(t1, t2));
+	}
+	if(delta.y == 0.0){
+		if(a.y < bb.b || bb.t < a.y) return ORC_INF;
+	} else {
+		cpFloat t1 = (bb.b - a.y)/delta.y;
+		cpFloat t2 = (bb.t - a.y)/delta.y;
+		tmin = fmax_(tmin, fmin_(t1, t2));
+		tmax = fmin_(tmax, fmax_(t1, t2));
+	}
+	if(tmin <= tmax && 0.0 <= tmax && tmin <= 1.0) return fmax_(tmin, 0.0);
+	return ORC_INF;
+}
+
+typedef struct QueryCtx {
+	int kind;                 /* 0 point, 1 nearest, 2 segment, 3 first, 4 box */
+	cpVect a, b;
+	cpFloat r;
+	cpBB bb;
+	cpShapeFilter filter;
+	void *func, *data;
+	cpPointQueryInfo *pout;
+	cpSegmentQueryInfo *sout;
+} QueryCtx;
+
+/* the leaf callbacks of cpSpaceQuery.c: NearestPointQuery :33-46,
+ * NearestPointQueryNearest :61-74, SegmentQuery :105-121, SegmentQueryFirst
+ * :138-152 (returns the running best alpha), BBQuery :183-193 */
+static cpFloat query_leaf_(QueryCtx *q, cpShape *shape)
+{
+	if(filter_reject_(shape->filter, q->filter)) return (q->kind == 3) ? q->sout->alpha : 1.0;
+	switch(q->kind){
+	case 0: {
+		cpPointQueryInfo info;
+		cpShapePointQuery(shape, q->a, &info);
+		if(info.shape && info.distance < q->r)
+			((cpSpacePointQueryFunc)q->func)(shape, info.point, info.distance, info.gradient, q->data);
+		return 1.0;
+	}
+	case 1:
+		if(!shape->sensor){
+			cpPointQueryInfo info;
+			cpShapePointQuery(shape, q->a, &info);
+			if(info.distance < q->pout->distance) *q->pout = info;
+		}
+		return 1.0;
+	case 2: {
+		cpSegmentQueryInfo info;
+		if(cpShapeSegmentQuery(shape, q->a, q->b, q->r, &info))
+			((cpSpaceSegmentQueryFunc)q->func)(shape, info.point, info.normal, info.alpha, q->data);
+		return 1.0;
+	}
+	case 3: {
+		cpSegmentQueryInfo info;
+		if(!shape->sensor && cpShapeSegmentQuery(shape, q->a, q->b, q->r, &info) && info.alpha < q->sout->alpha)
+			*q->sout = info;
+		return q->sout->alpha;
+	}
+	default:
+		if(cpBBIntersects(q->bb, shape->bb)) ((cpSpaceBBQueryFunc)q->func)(shape, q->data);
+		return 1.0;
+	}
+}
+
+/* cpBBTree.c:355-365 */
+static void subtree_query_(cpSpace *sp, int n, QueryCtx *q)
+{
+	Node *nd = &sp->nodes[n];
+	if(cpBBIntersects(nd->bb, q->bb)){
+		if(nd->obj) query_leaf_(q, nd->obj);
+		else {
+			subtree_query_(sp, nd->A, q);
+			subtree_query_(sp, sp->nodes[n].B, q);
+		}
+	}
+}
+
+/* cpBBTree.c:367-385 */
+static cpFloat subtree_segment_query_(cpSpace *sp, int n, QueryCtx *q, cpFloat t_exit)
+{
+	Node *nd = &sp->nodes[n];
+	if(nd->obj) return query_leaf_(q, nd->obj);
+	int A = nd->A, B = nd->B;
+	cpFloat t_a = bb_segment_query_(sp->nodes[A].bb, q->a, q->b);
+	cpFloat t_b = bb_segment_query_(sp->nodes[B].bb, q->a, q->b);
+	if(t_a < t_b){
+		if(t_a < t_exit) t_exit = fmin_(t_exit, subtree_segment_query_(sp, A, q, t_exit));
+		if(t_b < t_exit) t_exit = fmin_(t_exit, subtree_segment_query_(sp, B, q, t_exit));
+	} else {
+		if(t_b < t_exit) t_exit = fmin_(t_exit, subtree_segment_query_(sp, B, q, t_exit));
+		if(t_a < t_exit) t_exit = fmin_(t_exit, subtree_segment_query_(sp, A, q, t_exit));
+	}
+	return t_exit;
+}
+
+static void tree_query_(cpSpace *sp, Tree *t, QueryCtx *q) { if(t->root >= 0) subtree_query_(sp, t->root, q); }
+static void tree_segment_query_(cpSpace *sp, Tree *t, QueryCtx *q, cpFloat t_exit)
+{
+	if(t->root >= 0) subtree_segment_query_(sp, t->root, q, t_exit);
+}
+
+/* cpSpaceQuery.c:48-57 */
+void cpSpacePointQuery(cpSpace *sp, cpVect point, cpFloat maxDistance, cpShapeFilter filter, cpSpacePointQueryFunc func, void *data)
+{
+	QueryCtx q = {0};
+	q.kind = 0; q.a = point; q.r = maxDistance; q.filter = filter; q.func = (void *)func; q.data = data;
+	q.bb = cpBBNewForCircle(point, fmax_(maxDistance, 0.0));
+	tree_query_(sp, &sp->dynTree, &q);
+	tree_query_(sp, &sp->statTree, &q);
+}
+
+/* cpSpaceQuery.c:76-98 */
+cpShape *cpSpacePointQueryNearest(cpSpace *sp, cpVect point, cpFloat maxDistance, cpShapeFilter filter, cpPointQueryInfo *out)
+{
+	cpPointQueryInfo info = {NULL, cpvzero, maxDistance, cpvzero};
+	if(out) *out = info; else out = &info;
+	QueryCtx q = {0};
+	q.kind = 1; q.a = point; q.r = maxDistance; q.filter = filter; q.pout = out;
+	q.bb = cpBBNewForCircle(point, fmax_(maxDistance, 0.0));
+	tree_query_(sp, &sp->dynTree, &q);
+	tree_query_(sp, &sp->statTree, &q);
+	return (cpShape *)out->shape;
+}
+
+/* cpSpaceQuery.c:123-136 */
+void cpSpaceSegmentQuery(cpSpace *sp, cpVect start, cpVect end, cpFloat radius, cpShapeFilter filter, cpSpaceSegmentQueryFunc func, void *data)
+{
+	QueryCtx q = {0};
+	q.kind = 2; q.a = start; q.b = end; q.r = radius; q.filter = filter; q.func = (void *)func; q.data = data;
+	tree_segment_query_(sp, &sp->statTree, &q, 1.0);
+	tree_segment_query_(sp, &sp->dynTree, &q, 1.0);
+}
+
+/* cpSpaceQuery.c:154-175 */
+cpShape *cpSpaceSegmentQueryFirst(cpSpace *sp, cpVect start, cpVect end, cpFloat radius, cpShapeFilter filter, cpSegmentQueryInfo *out)
+{
+	cpSegmentQueryInfo info = {NULL, end, cpvzero, 1.0};
+	if(out) *out = info; else out = &info;
+	QueryCtx q = {0};
+	q.kind = 3; q.a = start; q.b = end; q.r = radius; q.filter = filter; q.sout = out;
+	tree_segment_query_(sp, &sp->statTree, &q, 1.0);
+	tree_segment_query_(sp, &sp->dynTree, &q, out->alpha);
+	return (cpShape *)out->shape;
+}
+
+/* cpSpaceQuery.c:195-204 */
+void cpSpaceBBQuery(cpSpace *sp, cpBB bb, cpShapeFilter filter, cpSpaceBBQueryFunc func, void *data)
+{
+	QueryCtx q = {0};
+	q.kind = 4; q.bb = bb; q.filter = filter; q.func = (void *)func; q.data = data;
+	tree_query_(sp, &sp->dynTree, &q);
+	tree_query_(sp, &sp->statTree, &q);
+}

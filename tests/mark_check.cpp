@@ -7,16 +7,10 @@
 // step the candidates (shape pair and cached id, in order) and every leaf's
 // pair list (as shape pairs and ids, in order) must be identical; pair slot
 // numbers may differ.  Prints one line and exits non-zero on a mismatch.
-#define __device__
-#define __host__
-#define __forceinline__ inline
-#define __constant__
-#include <cmath>
 #include <cstdio>
 #include <cstdlib>
-#include <cstring>
 #include <vector>
-static inline long long __double_as_longlong(double x) { long long b; memcpy(&b, &x, sizeof(b)); return b; }
+#include "host_cuda_shims.h"
 #include "cpg_mark.cuh"
 
 static unsigned long long rng = 0x9E3779B97F4A7C15ull;

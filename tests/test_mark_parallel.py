@@ -22,10 +22,27 @@ def test_parallel_marking_matches_serial_marking(tmp_path):
     if gxx is None:
         pytest.skip("no C++ compiler")
     exe = str(tmp_path / "mark_check")
-    subprocess.check_call([gxx, "-std=c++17", "-O2", "-ffp-contract=off",
+    subprocess.check_call([gxx, "-std=c++17", "-O2", "-ffp-contract=off", "-frounding-math",
                            "-I", os.path.join(REPO, "chipmunk2d_gb300", "csrc"),
                            os.path.join(REPO, "tests", "mark_check.cpp"), "-o", exe])
     r = subprocess.run([exe], stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True, timeout=600)
     print(r.stdout)
     assert r.returncode == 0, r.stdout
     assert " 0 mismatches" in r.stdout
+
+
+def test_tree_box_brackets_decide_exactly(tmp_path):
+    """The tree's float brackets (cpg_tree.cuh): every comparison, merge and
+    insertion-cost decision they settle must be the one the doubles give,
+    on random boxes, near-ties, signed zeros and large magnitudes."""
+    gxx = shutil.which("g++")
+    if gxx is None:
+        pytest.skip("no C++ compiler")
+    exe = str(tmp_path / "tree_bracket_check")
+    subprocess.check_call([gxx, "-std=c++17", "-O2", "-ffp-contract=off", "-frounding-math",
+                           "-I", os.path.join(REPO, "chipmunk2d_gb300", "csrc"),
+                           os.path.join(REPO, "tests", "tree_bracket_check.cpp"), "-o", exe])
+    r = subprocess.run([exe], stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True, timeout=600)
+    print(r.stdout)
+    assert r.returncode == 0, r.stdout
+    assert " 0 wrong" in r.stdout

@@ -92,3 +92,27 @@ def test_convex_hull_known_answer(request, which, case):
 def test_random_hulls_match_reference(ref_lib, oracle_lib):
     for n, seed in ((100, 1), (1000, 2), (10000, 3)):
         assert ka.random_hull_fixed_point(oracle_lib, n, seed) == ka.random_hull_fixed_point(ref_lib, n, seed)
+
+
+@pytest.mark.parametrize("cfg,size,steps", [(1, 14, 60), (2, 600, 150), (3, 600, 80), (6, 150, 100), (7, 30, 100)])
+def test_oracle_spatial_queries_bit_exact(ref_lib, oracle_lib, cfg, size, steps):
+    """Point, nearest-point, segment, first-hit, box and single-shape queries
+    (cpSpaceQuery.c, cpShape.c) on the seeded scenes before the first step,
+    after some steps and after edits: every callback, in order, and every
+    result must be bit-identical to the reference's."""
+    r = Scene(ref_lib, cfg, size)
+    o = Scene(oracle_lib, cfg, size)
+    try:
+        np.testing.assert_array_equal(o.queries(1, 140), r.queries(1, 140), err_msg="before the first step")
+        for s in range(steps):
+            r.step(1 / 60)
+            o.step(1 / 60)
+        qo, qr = o.queries(2, 700), r.queries(2, 700)
+        assert len(qr) > 700
+        np.testing.assert_array_equal(qo, qr, err_msg="after %d steps" % steps)
+        if cfg in (1, 3, 6):
+            assert r.edit(0, 7) == o.edit(0, 7)
+            np.testing.assert_array_equal(o.queries(3, 140), r.queries(3, 140), err_msg="after edits")
+    finally:
+        r.free()
+        o.free()
