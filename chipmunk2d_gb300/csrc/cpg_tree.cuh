@@ -143,6 +143,12 @@ __device__ __forceinline__ double bmax(double a, float alo, float ahi, double b,
 	return tmax(a, b);
 }
 
+__device__ __forceinline__ bool same_box_bits(BB a, BB b)
+{
+	return __double_as_longlong(a.l) == __double_as_longlong(b.l) && __double_as_longlong(a.b) == __double_as_longlong(b.b) &&
+	       __double_as_longlong(a.r) == __double_as_longlong(b.r) && __double_as_longlong(a.t) == __double_as_longlong(b.t);
+}
+
 /* tmerge(a, b) and the merged brackets */
 __device__ __forceinline__ void bmerge(BB a, const FBox &fa, BB b, const FBox &fb, BB &m, FBox &fm)
 {
@@ -359,6 +365,7 @@ __device__ void node_replace_child(TreeCtx &c, int parent, int child, int value)
 	}
 	int from = value, n = parent;
 	int a = pn.A, b = pn.B, up = pn.parent;
+	BB cur = node_bb(pn);
 	for(int guard = 0;; guard++){
 		if(guard > c.nodeCap){ c.T->error |= CPG_ERR_NODES; return; }
 		bool fromA = (a == from);
@@ -366,17 +373,27 @@ __device__ void node_replace_child(TreeCtx &c, int parent, int child, int value)
 		BB sbb = node_bb(sn);
 		FBox sf = node_fbox(sn);
 		int na = -1, nb = -1, nup = -1;
+		BB ncur = cur;
 		if(up >= 0){
 			const cpgNode &un = c.nodes[up];
 			na = un.A; nb = un.B; nup = un.parent;
+			ncur = node_bb(un);
 		}
 		BB m; FBox fm;
 		if(fromA) bmerge(fromBB, fromF, sbb, sf, m, fm);
 		else bmerge(sbb, sf, fromBB, fromF, m, fm);
+		/* A box the refit leaves as it was ends the walk: every node's box
+		 * is the merge of its children's (insertion merges the leaf into
+		 * each box on its path, a refit recomputes it), so the ancestors'
+		 * recomputed boxes equal their present ones.  Equal in value; the
+		 * bits could differ only in the sign of a zero coordinate, which
+		 * the comparisons fold and no cost, area or proximity turns into
+		 * a different decision. */
+		if(same_box_bits(m, cur)) return;
 		set_node_box(c.nodes[n], m, fm);
 		if(up < 0) return;
 		from = n; fromBB = m; fromF = fm; n = up;
-		a = na; b = nb; up = nup;
+		a = na; b = nb; up = nup; cur = ncur;
 	}
 }
 
@@ -423,7 +440,7 @@ __device__ int subtree_insert(TreeCtx &c, int root, int leaf)
 		NodeRec rc = goB ? rb : ra;
 		BB m; FBox fm;
 		bmerge(nd.bb, nd.f, lbb, lf, m, fm);
-		set_node_box(c.nodes[cur], m, fm);
+		if(!same_box_bits(m, nd.bb)) set_node_box(c.nodes[cur], m, fm);
 		if(rc.obj >= 0){
 			int nn = node_new_bb(c, leaf, lbb, lf, child, rc.bb, rc.f);
 			if(nn < 0) return root;

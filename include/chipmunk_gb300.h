@@ -572,6 +572,17 @@ void cpGpuSetAutotune(int on);
  * returns 0 or -1 (with cpGpuGetLastError() set). */
 int cpGpuSolverQuality(cpSpace *space, int mode, cpFloat dt, int maxIters, double *out);
 
+/* Many queries against one space in one device launch, one thread each:
+ * the nearest shape within maxDistance of each point
+ * (cpSpacePointQueryNearest for every point) and the first shape hit by
+ * each segment (cpSpaceSegmentQueryFirst for every start/end pair).  Host
+ * arrays of n entries; out[i] is what the single query returns in its
+ * info argument.  Returns CP_GPU_OK or an error code. */
+int cpGpuSpacePointQueryNearestBatch(cpSpace *space, int n, const cpVect *points, cpFloat maxDistance,
+                                     cpShapeFilter filter, cpPointQueryInfo *out);
+int cpGpuSpaceSegmentQueryFirstBatch(cpSpace *space, int n, const cpVect *starts, const cpVect *ends, cpFloat radius,
+                                     cpShapeFilter filter, cpSegmentQueryInfo *out);
+
 /* Exact-order parallel schedule of a sequential sweep.  Unit u of the
  * sweep touches dynamic bodies bodyA[u] and bodyB[u] (a negative index or
  * one >= nbodies means "no dynamic body").  On return, order[levelStart[l]
