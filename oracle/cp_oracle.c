@@ -1019,6 +1019,18 @@ cpVect cpPinJointGetAnchorB(const cpConstraint *c) { return c->anchorB; }
 cpFloat cpPinJointGetDist(const cpConstraint *c) { return c->dist; }
 cpVect cpSlideJointGetAnchorA(const cpConstraint *c) { return c->anchorA; }
 cpVect cpSlideJointGetAnchorB(const cpConstraint *c) { return c->anchorB; }
+/* cpPivotJoint.c:133-155, cpPinJoint.c:109-142, cpSlideJoint.c:127-172:
+ * the setters store the value (they also wake the bodies, and no body
+ * sleeps here) */
+void cpPivotJointSetAnchorA(cpConstraint *c, cpVect v) { c->anchorA = v; }
+void cpPivotJointSetAnchorB(cpConstraint *c, cpVect v) { c->anchorB = v; }
+void cpPinJointSetAnchorA(cpConstraint *c, cpVect v) { c->anchorA = v; }
+void cpPinJointSetAnchorB(cpConstraint *c, cpVect v) { c->anchorB = v; }
+void cpPinJointSetDist(cpConstraint *c, cpFloat v) { c->dist = v; }
+void cpSlideJointSetAnchorA(cpConstraint *c, cpVect v) { c->anchorA = v; }
+void cpSlideJointSetAnchorB(cpConstraint *c, cpVect v) { c->anchorB = v; }
+void cpSlideJointSetMin(cpConstraint *c, cpFloat v) { c->min = v; }
+void cpSlideJointSetMax(cpConstraint *c, cpFloat v) { c->max = v; }
 cpFloat cpSlideJointGetMin(const cpConstraint *c) { return c->min; }
 cpFloat cpSlideJointGetMax(const cpConstraint *c) { return c->max; }
 
