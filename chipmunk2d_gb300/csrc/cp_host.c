@@ -201,6 +201,7 @@ struct cpSpace {
 	int structDirty;                        /* objects added or removed since the device set was built:
 	                                           the host holds the state until the next step rebuilds it */
 	double jointDt;                         /* dt the joint bias terms were made for */
+	unsigned long long editGen;             /* counts object edits through the setters */
 
 	cpArbiter *snap; int nsnap, capsnap; int snapValid;
 	float phaseMs[8];
@@ -1219,6 +1220,72 @@ void cpSpaceStep(cpSpace *sp, cpFloat dt)
 }
 
 /* ====================================================================
+ * Saved states of a space: a device copy of its whole set (bodies, shape
+ * caches, the trees and pair caches, the arbiter table and contacts,
+ * joints with their accumulated impulses) and the host counters that go
+ * with it (timestamp, last dt, the dt the joint bias terms were made for).
+ * The same copy is what the differentiable rollout keeps per segment.
+ * ==================================================================== */
+struct cpGpuSpaceState {
+	cpSpace *space;
+	DevSet *ds;
+	unsigned long long editGen;
+	void *slab;
+	size_t bytes;
+	cpTimestamp stamp;
+	cpFloat currDt, jointDt;
+};
+
+cpGpuSpaceState *cpGpuSpaceSaveState(cpSpace *sp)
+{
+	if(!sp){ set_error(CP_GPU_ERR_ARGUMENT, "save state: null space"); return NULL; }
+	if(sp->dev && !sp->ownsDev){ set_error(CP_GPU_ERR_UNSUPPORTED, "save state: the space belongs to a cpGpuBatch"); return NULL; }
+	if(!space_device_ready_(sp)) return NULL;
+	DevSet *ds = sp->dev;
+	devset_flush_space(ds, sp->world);
+	check_stats(ds);
+	cpGpuSpaceState *st = (cpGpuSpaceState *)calloc(1, sizeof(cpGpuSpaceState));
+	if(!st) return NULL;
+	if(!cuda_ok(cudaMalloc(&st->slab, ds->slabBytes), "cudaMalloc saved state")){ free(st); return NULL; }
+	st->bytes = ds->slabBytes;
+	if(!cuda_ok(cudaMemcpyAsync(st->slab, ds->slab, ds->slabBytes, cudaMemcpyDeviceToDevice, lib_stream()), "save state") ||
+	   !cuda_ok(cudaStreamSynchronize(lib_stream()), "save state")){
+		cudaFree(st->slab); free(st); return NULL;
+	}
+	st->space = sp; st->ds = ds; st->editGen = sp->editGen;
+	st->stamp = sp->stamp; st->currDt = sp->curr_dt; st->jointDt = sp->jointDt;
+	return st;
+}
+
+int cpGpuSpaceRestoreState(cpSpace *sp, const cpGpuSpaceState *st)
+{
+	if(!sp || !st){ set_error(CP_GPU_ERR_ARGUMENT, "restore state: null argument"); return CP_GPU_ERR_ARGUMENT; }
+	if(st->space != sp || sp->dev != st->ds || sp->structDirty || space_structure_changed(sp) || st->bytes != sp->dev->slabBytes){
+		set_error(CP_GPU_ERR_UNSUPPORTED, "restore state: the space's objects were added or removed since the save");
+		return CP_GPU_ERR_UNSUPPORTED;
+	}
+	if(sp->editGen != st->editGen){
+		set_error(CP_GPU_ERR_UNSUPPORTED, "restore state: objects of the space were edited since the save");
+		return CP_GPU_ERR_UNSUPPORTED;
+	}
+	DevSet *ds = sp->dev;
+	check_stats(ds);
+	if(!cuda_ok(cudaMemcpyAsync(ds->slab, st->slab, st->bytes, cudaMemcpyDeviceToDevice, lib_stream()), "restore state") ||
+	   !cuda_ok(cudaStreamSynchronize(lib_stream()), "restore state"))
+		return CP_GPU_ERR_CUDA;
+	sp->stamp = st->stamp; sp->curr_dt = st->currDt; sp->jointDt = st->jointDt;
+	sp->hostStale = 1; sp->consStale = 1; sp->shapesStale = 1; sp->snapValid = 0;
+	return CP_GPU_OK;
+}
+
+void cpGpuSpaceStateFree(cpGpuSpaceState *st)
+{
+	if(!st) return;
+	if(st->slab) cudaFree(st->slab);
+	free(st);
+}
+
+/* ====================================================================
  * Spatial queries (cpSpaceQuery.c:48-204, cpShape.c:222-256): answered on
  * the device by cpg_query.cu, which walks the space's trees in the
  * reference's order; the callbacks then run here, in that order.
@@ -2216,7 +2283,7 @@ static inline const cpBody *rd(const cpBody *b)
 /* Write access: pull, then mark the space's bodies for upload. */
 static inline cpBody *wr(cpBody *b)
 {
-	if(b->space){ space_pull(b->space); b->space->bodyDirty = 1; }
+	if(b->space){ space_pull(b->space); b->space->bodyDirty = 1; b->space->editGen++; }
 	return b;
 }
 
@@ -2638,7 +2705,7 @@ cpShape *cpBoxShapeNew(cpBody *body, cpFloat width, cpFloat height, cpFloat radi
 
 void cpShapeFree(cpShape *s) { if(s){ free(s->lv); free(s); } }
 
-static inline cpShape *swr(cpShape *s) { if(s->space) s->space->shapeDirty = 1; return s; }
+static inline cpShape *swr(cpShape *s) { if(s->space){ s->space->shapeDirty = 1; s->space->editGen++; } return s; }
 
 cpSpace *cpShapeGetSpace(const cpShape *s) { return s->space; }
 cpBody *cpShapeGetBody(const cpShape *s) { return s->body; }
@@ -2747,6 +2814,7 @@ static inline cpConstraint *cwr(cpConstraint *c)
 	if(c->space){
 		joints_pull_(c->space);   /* keep the device-side accumulators */
 		c->space->consDirty = 1;
+		c->space->editGen++;
 	}
 	return c;
 }

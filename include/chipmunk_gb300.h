@@ -572,6 +572,21 @@ void cpGpuSetAutotune(int on);
  * returns 0 or -1 (with cpGpuGetLastError() set). */
 int cpGpuSolverQuality(cpSpace *space, int mode, cpFloat dt, int maxIters, double *out);
 
+/* Saved states.  cpGpuSpaceSaveState copies a standalone space's whole
+ * simulation state on the device (bodies, shape caches, trees and pair
+ * caches, arbiters with their contacts and impulses, joints with their
+ * accumulated impulses, the timestamp and last dt); a later
+ * cpGpuSpaceRestoreState puts it back, and steps from there repeat the
+ * steps from the save bit for bit.  Restoring is refused
+ * (CP_GPU_ERR_UNSUPPORTED) once objects were added, removed or edited
+ * through a setter since the save; stepping, queries, reads and the
+ * space's own settings (gravity, iterations, ...) are not part of it.
+ * Returns NULL (error set) when the copy could not be made. */
+typedef struct cpGpuSpaceState cpGpuSpaceState;
+cpGpuSpaceState *cpGpuSpaceSaveState(cpSpace *space);
+int cpGpuSpaceRestoreState(cpSpace *space, const cpGpuSpaceState *state);
+void cpGpuSpaceStateFree(cpGpuSpaceState *state);
+
 /* Many queries against one space in one device launch, one thread each:
  * the nearest shape within maxDistance of each point
  * (cpSpacePointQueryNearest for every point) and the first shape hit by
