@@ -42,6 +42,18 @@ sys.path.insert(0, REPO)
 RUN_STEPS = {"circles": 600, "pyramid": 1000, "mixed": 600}
 
 
+_PINNED = []
+
+
+def pinned_doubles(n):
+    """A numpy view of n doubles of page-locked host memory (the tensor
+    that owns it is kept for the life of the run)."""
+    import torch
+    t = torch.empty(max(n, 1), dtype=torch.float64, pin_memory=True)
+    _PINNED.append(t)
+    return t.numpy()
+
+
 def window_start(workload, warmup, steps):
     """First timed step: a K-step sample of a longer configured run is taken
     from its middle (untimed lead-in steps, the W warm-up steps among them),
@@ -770,14 +782,15 @@ def mode_sample(lib, workload, steps, warmup, mode=0, phases=False, e2e=False):
            "body_steps_per_s": sc.nbodies * steps / secs, "ms_per_step": 1000 * secs / steps,
            "description": desc}
     if e2e:
-        out = np.zeros(8 * sc.nbodies)
+        out = pinned_doubles(8 * sc.nbodies)
         t0 = time.perf_counter()
         for _ in range(steps):
             lib.cpSpaceStep(sc.space, dt)
-            lib.cpx_scene_dump_public(sc.h, out.ctypes.data)
+            assert lib.cpGpuSpaceGetBodyStates(sc.space, out.ctypes.data, sc.nbodies) == sc.nbodies
         es = time.perf_counter() - t0
         rec["e2e"] = {"value": sc.nbodies * steps / es, "unit": "body-steps/s", "timed_window": [warmup + steps, warmup + 2 * steps],
-                      "path": "cpSpaceStep + cpBodyGetPosition/Velocity/Angle for every body (ctypes)"}
+                      "d2h_bytes_per_step": 64 * sc.nbodies,
+                      "path": "cpSpaceStep + cpGpuSpaceGetBodyStates (every body's position, velocity, angle, angular velocity, rotation)"}
     if err:
         rec["error"] = lib.cpGpuGetLastErrorString().decode()
     if phases:
@@ -909,7 +922,7 @@ def run_ours(args):
     sc = make()
     for _ in range(start):
         lib.cpSpaceStep(sc.space, dt)
-    out = np.zeros(8 * n)
+    out = pinned_doubles(8 * n)
     sc.public()
     torch.cuda.synchronize()
     e2e_steps = min(args.steps, 200)
@@ -919,10 +932,19 @@ def run_ours(args):
     for _ in range(e2e_steps):
         t0 = time.perf_counter()
         lib.cpSpaceStep(sc.space, dt)
-        lib.cpx_scene_dump_public(sc.h, out.ctypes.data)
+        got = lib.cpGpuSpaceGetBodyStates(sc.space, out.ctypes.data, n)
         e2e_s += time.perf_counter() - t0
+        assert got == n, got
         lib.cpGpuGetStepStats(sc.space, stats.ctypes.data, 8)      # untimed: arbiters solved this step
         arb_per_step.append(int(stats[5]))
+    # the same window read through one getter call per value instead
+    getter_s = 0.0
+    for _ in range(min(e2e_steps, 20)):
+        t0 = time.perf_counter()
+        lib.cpSpaceStep(sc.space, dt)
+        lib.cpx_scene_dump_public(sc.h, out.ctypes.data)
+        getter_s += time.perf_counter() - t0
+    getter_value = n * min(e2e_steps, 20) * world_size / getter_s
     sc.free()
 
     value = n * args.steps * world_size / total_s
@@ -999,8 +1021,10 @@ def run_ours(args):
                    "l2": "flushed between timed steps (256 MB fill, untimed)",
                    "parallelism": "replicas" if world_size > 1 else "single"},
         "e2e": {"value": e2e_value, "unit": "body-steps/s", "h2d_bytes_per_step": 88,
-                "d2h_bytes_per_step": 18 * 8 * (n + 5) + 64, "steps": e2e_steps,
-                "path": "cpSpaceStep + cpBodyGetPosition/Velocity/Angle for every body (ctypes)"},
+                "d2h_bytes_per_step": 64 * n + 64, "steps": e2e_steps,
+                "path": "cpSpaceStep + cpGpuSpaceGetBodyStates (every body's position, velocity, angle, angular velocity, rotation into pinned host memory)",
+                "per_body_getters": {"value": getter_value, "steps": min(e2e_steps, 20),
+                                     "path": "cpSpaceStep + cpBodyGetPosition/Velocity/Angle/AngularVelocity/Rotation for every body (one C call each)"}},
         "roofline": {"bound": "hbm", "kernel": names[dom], "achieved": achieved, "peak": peak,
                      "unit": "GB/s", "frac": achieved / peak, "peak_kind": peak_kind,
                      "traffic": traffic, "traffic_capture": traffic_note, "algorithmic_bytes_per_launch": algo,

@@ -198,6 +198,7 @@ _GPU_API = {
     "cpGpuDebugSetParallelMarking": (None, [I]),
     "cpGpuGetPhaseTimes": (I, [P, P, I]),
     "cpGpuSolverQuality": (I, [P, I, D, I, P]),
+    "cpGpuSpaceGetBodyStates": (I, [P, P, I]),
     "cpGpuGetStepStats": (I, [P, P, I]),
     "cpGpuGetLaunchCount": (ctypes.c_longlong, [I]),
     "cpGpuSolveSchedule": (I, [P, P, I, I, P, P, P, P]),

@@ -267,6 +267,8 @@ struct DevSet {
 	int tuneBest;             /* chosen candidate, -1 before the first window */
 	void *qbuf;               /* spatial queries: queries, hits, counts, status */
 	size_t qbytes;
+	double *bstates;          /* cpGpuSpaceGetBodyStates: device staging */
+	int bstatesCap;
 };
 
 
@@ -688,6 +690,7 @@ static void devset_free(DevSet *ds)
 	if(ds->graph) cpg_step_graph_free(ds->graph);
 	if(ds->gather) cudaFree(ds->gather);
 	if(ds->qbuf) cudaFree(ds->qbuf);
+	if(ds->bstates) cudaFree(ds->bstates);
 	if(ds->hparams) cudaFreeHost(ds->hparams);
 	if(ds->hstats) cudaFreeHost(ds->hstats);
 	if(ds->hbodies) cudaFreeHost(ds->hbodies);
@@ -1217,6 +1220,42 @@ void cpSpaceStep(cpSpace *sp, cpFloat dt)
 	if(!space_device_ready_(sp)) return;
 	double dts[1] = { dt };
 	devset_step(sp->dev, dts, NULL);
+}
+
+static inline const cpBody *rd(const cpBody *b);
+
+/* Every dynamic body's public state in one read: 8 doubles per body in
+ * the space's body order (position, velocity, angle, angular velocity,
+ * rotation), the values the getters return.  After a step they are
+ * gathered on the device and copied in one transfer. */
+int cpGpuSpaceGetBodyStates(cpSpace *sp, double *out, int max)
+{
+	if(!sp || (max > 0 && !out)){ set_error(CP_GPU_ERR_ARGUMENT, "body states: null argument"); return -1; }
+	int n = sp->ndyn < max ? sp->ndyn : max;
+	if(n <= 0) return 0;
+	if(!sp->dev || sp->bodyDirty || sp->structDirty || !sp->hostStale){
+		/* the host structs hold the current state */
+		for(int i = 0; i < n; i++){
+			const cpBody *b = rd(sp->dyn[i]);
+			double *o = out + 8*(size_t)i;
+			cpVect p = cpTransformPoint(b->transform, cpvzero);
+			o[0] = p.x; o[1] = p.y; o[2] = b->v.x; o[3] = b->v.y;
+			o[4] = b->a; o[5] = b->w; o[6] = b->transform.a; o[7] = b->transform.b;
+		}
+		return n;
+	}
+	DevSet *ds = sp->dev;
+	if(ds->bstatesCap < n){
+		if(ds->bstates) cudaFree(ds->bstates);
+		ds->bstates = NULL; ds->bstatesCap = 0;
+		if(!cuda_ok(cudaMalloc((void **)&ds->bstates, sizeof(double)*8*(size_t)n), "cudaMalloc body states")) return -1;
+		ds->bstatesCap = n;
+	}
+	cudaStream_t st = lib_stream();
+	if(cpg_launch_body_states(&ds->d, sp->world, ds->bstates, n, st) != 0){ set_error(CP_GPU_ERR_CUDA, "body states launch failed"); return -1; }
+	if(!d2h(out, ds->bstates, sizeof(double)*8*(size_t)n) || !cuda_ok(cudaStreamSynchronize(st), "body states")) return -1;
+	check_stats(ds);
+	return n;
 }
 
 /* ====================================================================

@@ -400,6 +400,7 @@ int cpg_launch_replay_solve(const cpgSet *s, const cpgAdj *a, int nsteps, void *
 int cpg_launch_transfer(const cpgSet *to, const cpgSet *from, const int *bodyMap, const unsigned char *deadShape,
                         int *slotMap, void *stream);
 int cpg_launch_contact_quality(const cpgSet *s, int w, double dt, double *acc, void *stream);
+int cpg_launch_body_states(const cpgSet *s, int w, double *out, int n, void *stream);
 int cpg_launch_query(const cpgSet *s, int world, const cpgQuery *queries, int nq, cpgHit *hits, int cap,
                      int *counts, int brute, int *status, void *stream);
 int cpg_launch_set_arb_impulses(const cpgSet *s, int w, const double *imp, const int *pairs, int n, int *mismatch, void *stream);

@@ -2157,6 +2157,24 @@ __global__ void k_contact_quality(cpgSet s, int w, double dt, double *acc)
 	}
 }
 
+/* The public view of world w's first n bodies, 8 doubles each, as the
+ * getters compute it (cpBody.c): position cpTransformPoint(transform,
+ * cpvzero), velocity, angle, angular velocity, rotation (transform.a,
+ * transform.b). */
+__global__ void k_body_states(cpgSet s, int w, double *out, int n)
+{
+	int i = blockIdx.x*blockDim.x + threadIdx.x;
+	if(i >= n) return;
+	int g = s.world[w].bodyOff + i;
+	double ta = s.ta[g], tb = s.tb[g], tc = s.tc[g], td = s.td[g];
+	double *o = out + 8*(size_t)i;
+	o[0] = ta*0.0 + tc*0.0 + s.ttx[g];
+	o[1] = tb*0.0 + td*0.0 + s.tty[g];
+	o[2] = s.vx[g]; o[3] = s.vy[g];
+	o[4] = s.ang[g]; o[5] = s.w[g];
+	o[6] = ta; o[7] = tb;
+}
+
 extern "C" int cpg_launch_contact_quality(const cpgSet *s, int w, double dt, double *acc, void *stream)
 {
 	cudaStream_t st = (cudaStream_t)stream;
@@ -2891,6 +2909,13 @@ extern "C" int cpg_launch_gather_arbs(const cpgSet *s, int world, cpgArb *out, i
 {
 	LAUNCH(k_gather_arbs<<<blocks_for(n, 128), 128, 0, (cudaStream_t)stream>>>(*s, world, out, n));
 	return check_launch("k_gather_arbs") == cudaSuccess ? 0 : -1;
+}
+
+extern "C" int cpg_launch_body_states(const cpgSet *s, int w, double *out, int n, void *stream)
+{
+	if(n <= 0) return 0;
+	LAUNCH(k_body_states<<<blocks_for(n, 256), 256, 0, (cudaStream_t)stream>>>(*s, w, out, n));
+	return check_launch("k_body_states") == cudaSuccess ? 0 : -1;
 }
 
 extern "C" int cpg_launch_apply_ops(const cpgSet *s, void *stream)

@@ -572,6 +572,15 @@ void cpGpuSetAutotune(int on);
  * returns 0 or -1 (with cpGpuGetLastError() set). */
 int cpGpuSolverQuality(cpSpace *space, int mode, cpFloat dt, int maxIters, double *out);
 
+/* Every dynamic body's public state in one read (the results of a step
+ * without a getter call per value): 8 doubles per body, in the order the
+ * bodies were added -- position (cpBodyGetPosition), velocity, angle,
+ * angular velocity, rotation (cpBodyGetRotation) -- the getters' values
+ * bit for bit.  After a step they are gathered on the device and copied
+ * in one transfer.  Returns the number of bodies written (at most max),
+ * or -1 (error set). */
+int cpGpuSpaceGetBodyStates(cpSpace *space, double *out, int max);
+
 /* Saved states.  cpGpuSpaceSaveState copies a standalone space's whole
  * simulation state on the device (bodies, shape caches, trees and pair
  * caches, arbiters with their contacts and impulses, joints with their
