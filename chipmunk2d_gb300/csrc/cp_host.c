@@ -1527,6 +1527,159 @@ cpBool cpShapeSegmentQuery(const cpShape *shape, cpVect a, cpVect b, cpFloat rad
 	return info->shape != NULL;
 }
 
+static cpBB shape_cache_(cpShape *s, cpTransform t);
+static void shapes_pull_all_(cpSpace *sp);
+
+/* A shape's host cache as a probe; its polygon planes go to planes (four
+ * arrays of n) from voff on. */
+static void probe_fill_(const cpShape *s, cpgProbe *p, double *planes, int n, int voff)
+{
+	memset(p, 0, sizeof(*p));
+	p->kind = s->kind; p->r = s->r;
+	cpVect g0 = (s->kind == CPG_CIRCLE) ? s->tc : s->ta;
+	p->p0x = g0.x; p->p0y = g0.y; p->p1x = s->tb.x; p->p1y = s->tb.y; p->nx = s->tn.x; p->ny = s->tn.y;
+	p->atx = s->a_tangent.x; p->aty = s->a_tangent.y; p->btx = s->b_tangent.x; p->bty = s->b_tangent.y;
+	p->rotx = s->body ? s->body->transform.a : 1.0;
+	p->roty = s->body ? s->body->transform.b : 0.0;
+	p->bbl = s->bb.l; p->bbb = s->bb.b; p->bbr = s->bb.r; p->bbt = s->bb.t;
+	p->hashid = (unsigned long long)s->hashid;
+	p->group = (unsigned long long)s->filter.group; p->cat = s->filter.categories; p->mask = s->filter.mask;
+	p->sensor = s->sensor ? 1 : 0;
+	p->count = (s->kind == CPG_POLY) ? s->count : 0;
+	p->voff = voff;
+	p->slot = -1;
+	for(int i = 0; i < p->count; i++){
+		planes[voff + i] = s->gv[i].x; planes[n + voff + i] = s->gv[i].y;
+		planes[2*n + voff + i] = s->gn[i].x; planes[3*n + voff + i] = s->gn[i].y;
+	}
+}
+
+static cpContactPointSet point_set_(const cpgShapeHit *h)
+{
+	cpContactPointSet set;
+	memset(&set, 0, sizeof(set));
+	set.count = h->count;
+	set.normal = cpv(h->nx, h->ny);
+	for(int i = 0; i < h->count && i < CP_MAX_CONTACTS_PER_ARBITER; i++){
+		set.points[i].pointA = cpv(h->ax[i], h->ay[i]);
+		set.points[i].pointB = cpv(h->bx[i], h->by[i]);
+		set.points[i].distance = h->dist[i];
+	}
+	return set;
+}
+
+/* cpSpaceQuery.c:230-246: the shape's cache is brought to its body's
+ * transform here, as cpShapeUpdate does there; the device walks the trees
+ * with it. */
+cpBool cpSpaceShapeQuery(cpSpace *sp, cpShape *shape, cpSpaceShapeQueryFunc func, void *data)
+{
+	if(!sp || !shape){ set_error(CP_GPU_ERR_ARGUMENT, "shape query: null argument"); return cpFalse; }
+	if(shape->body){
+		rd(shape->body);
+		shape_cache_(shape, shape->body->transform);
+	} else if(shape->space){
+		shapes_pull_all_(shape->space);
+	}
+	if(sp->dev && !sp->ownsDev){
+		if(sp->structDirty || space_structure_changed(sp)){
+			set_error(CP_GPU_ERR_UNSUPPORTED, "query: objects were added to or removed from a space of a cpGpuBatch");
+			return cpFalse;
+		}
+	} else if(!space_device_ready_(sp)) return cpFalse;
+	DevSet *ds = sp->dev;
+	devset_flush_space(ds, sp->world);
+	cudaStream_t st = lib_stream();
+	int nplanes = (shape->kind == CPG_POLY) ? shape->count : 0;
+	double *hplanes = HALLOC(double, 4*(size_t)(nplanes > 0 ? nplanes : 1));
+	cpgProbe probe;
+	probe_fill_(shape, &probe, hplanes, nplanes, 0);
+	if(shape->space == sp) for(int i = 0; i < sp->nshapes; i++) if(sp->shapes[i] == shape){ probe.slot = i; break; }
+	int brute = (sp->mode == CP_GPU_SOLVER_COLORED);
+	int cap = CPG_QUERY_HITS0, counts[3] = {0, 0, 0};
+	cpgShapeHit *hits = NULL;
+	cpBool any = cpFalse;
+	for(int attempt = 0; attempt < 2; attempt++){
+		size_t pb = align256(sizeof(double)*4*(size_t)(nplanes > 0 ? nplanes : 1));
+		size_t hb = align256(sizeof(cpgShapeHit)*(size_t)cap);
+		size_t need = pb + hb + 256;
+		if(ds->qbytes < need){
+			if(ds->qbuf) cudaFree(ds->qbuf);
+			ds->qbuf = NULL; ds->qbytes = 0;
+			if(!cuda_ok(cudaMalloc(&ds->qbuf, need), "cudaMalloc queries")){ free(hplanes); return cpFalse; }
+			ds->qbytes = need;
+		}
+		char *base = (char *)ds->qbuf;
+		double *dplanes = (double *)base;
+		cpgShapeHit *dh = (cpgShapeHit *)(base + pb);
+		int *dc = (int *)(base + pb + hb);
+		int ok = h2d(dplanes, hplanes, sizeof(double)*4*(size_t)nplanes);
+		ok &= (cpg_launch_shape_query(&ds->d, sp->world, &probe, dplanes, nplanes, brute, dh, cap, dc, st) == 0);
+		ok &= d2h(counts, dc, sizeof(int)*3);
+		ok &= cuda_ok(cudaStreamSynchronize(st), "shape query");
+		if(!ok){ set_error(CP_GPU_ERR_CUDA, "shape query launch failed"); free(hplanes); return cpFalse; }
+		if(counts[2]){ set_error(CP_GPU_ERR_OVERFLOW, "shape query: tree walk stack or guard exceeded"); free(hplanes); return cpFalse; }
+		if(counts[0] > cap && attempt == 0){ cap = counts[0]; continue; }
+		hits = HALLOC(cpgShapeHit, cap);
+		if(!d2h(hits, dh, sizeof(cpgShapeHit)*(size_t)cap) || !cuda_ok(cudaStreamSynchronize(st), "shape query results")){
+			free(hits); free(hplanes); return cpFalse;
+		}
+		break;
+	}
+	free(hplanes);
+	if(!hits) return cpFalse;
+	int n = counts[0] < cap ? counts[0] : cap;
+	for(int k = 0; k < n; k++){
+		cpShape *other = slot_shape_(sp, hits[k].shape);
+		if(!other) continue;
+		cpContactPointSet set = point_set_(&hits[k]);
+		if(func) func(other, &set, data);
+	}
+	any = counts[1] ? cpTrue : cpFalse;
+	free(hits);
+	return any;
+}
+
+/* cpShape.c:258-283 on the shapes' caches as they are */
+cpContactPointSet cpShapesCollide(const cpShape *a, const cpShape *b)
+{
+	cpContactPointSet set;
+	memset(&set, 0, sizeof(set));
+	if(!a || !b){ set_error(CP_GPU_ERR_ARGUMENT, "cpShapesCollide: null shape"); return set; }
+	if(!device_available()) return set;
+	if(a->space) shapes_pull_all_(a->space);
+	if(b->space && b->space != a->space) shapes_pull_all_(b->space);
+	static void *buf = NULL;
+	static size_t bufBytes = 0;
+	int na = (a->kind == CPG_POLY) ? a->count : 0, nb = (b->kind == CPG_POLY) ? b->count : 0;
+	int n = na + nb;
+	double *hplanes = HALLOC(double, 4*(size_t)(n > 0 ? n : 1));
+	cpgProbe probes[2];
+	probe_fill_(a, &probes[0], hplanes, n, 0);
+	probe_fill_(b, &probes[1], hplanes, n, na);
+	size_t pb = align256(sizeof(cpgProbe)*2), lb = align256(sizeof(double)*4*(size_t)(n > 0 ? n : 1));
+	size_t need = pb + lb + align256(sizeof(cpgShapeHit)) + 256;
+	if(bufBytes < need){
+		if(buf) cudaFree(buf);
+		buf = NULL; bufBytes = 0;
+		if(!cuda_ok(cudaMalloc(&buf, need), "cudaMalloc cpShapesCollide")){ free(hplanes); return set; }
+		bufBytes = need;
+	}
+	char *base = (char *)buf;
+	cpgProbe *dp = (cpgProbe *)base;
+	double *dl = (double *)(base + pb);
+	cpgShapeHit *dh = (cpgShapeHit *)(base + pb + lb);
+	int *dc = (int *)(base + pb + lb + align256(sizeof(cpgShapeHit)));
+	cudaStream_t st = lib_stream();
+	cpgShapeHit h;
+	int cnt = 0;
+	int ok = h2d(dp, probes, sizeof(probes)) && h2d(dl, hplanes, sizeof(double)*4*(size_t)n);
+	ok = ok && cpg_launch_shape_pair(dp, dl, n, dh, dc, st) == 0;
+	ok = ok && d2h(&h, dh, sizeof(h)) && d2h(&cnt, dc, sizeof(int)) && cuda_ok(cudaStreamSynchronize(st), "cpShapesCollide");
+	free(hplanes);
+	if(!ok){ set_error(CP_GPU_ERR_CUDA, "cpShapesCollide launch failed"); return set; }
+	return point_set_(&h);
+}
+
 /* Many nearest-point or first-hit queries in one launch, one thread each. */
 int cpGpuSpacePointQueryNearestBatch(cpSpace *sp, int n, const cpVect *points, cpFloat maxDistance,
                                      cpShapeFilter filter, cpPointQueryInfo *out)

@@ -216,6 +216,26 @@ typedef struct cpgQuery {
 	int kind;
 	int pad;
 } cpgQuery;
+/* A shape given to a shape query or to cpShapesCollide by value: its
+ * world-space cache (circle tc | segment ta, tb, tn; polygon planes at
+ * voff of the query's plane array), the segment tangents in body space,
+ * its body's rotation, box, filter and sensor flag; slot is its place in
+ * the queried world, -1 when it is not one of its shapes. */
+typedef struct cpgProbe {
+	double r, p0x, p0y, p1x, p1y, nx, ny, atx, aty, btx, bty, rotx, roty;
+	double bbl, bbb, bbr, bbt;
+	unsigned long long hashid, group;
+	unsigned cat, mask;
+	int kind, count, voff, slot, sensor, pad;
+} cpgProbe;
+/* One shape found by a shape query, with its contact point set
+ * (cpShape.c:258-283). */
+typedef struct cpgShapeHit {
+	int shape, count, sensor, pad;
+	double nx, ny;
+	double ax[2], ay[2], bx[2], by[2], dist[2];
+} cpgShapeHit;
+
 typedef struct cpgHit {
 	int shape;                    /* world-local shape slot, -1 none */
 	int pad;
@@ -401,6 +421,10 @@ int cpg_launch_transfer(const cpgSet *to, const cpgSet *from, const int *bodyMap
                         int *slotMap, void *stream);
 int cpg_launch_contact_quality(const cpgSet *s, int w, double dt, double *acc, void *stream);
 int cpg_launch_body_states(const cpgSet *s, int w, double *out, int n, void *stream);
+int cpg_launch_shape_query(const cpgSet *s, int world, const cpgProbe *probe, const double *planes, int nplanes,
+                           int brute, cpgShapeHit *hits, int cap, int *counts, void *stream);
+int cpg_launch_shape_pair(const cpgProbe *probes, const double *planes, int nplanes, cpgShapeHit *hit,
+                          int *counts, void *stream);
 int cpg_launch_query(const cpgSet *s, int world, const cpgQuery *queries, int nq, cpgHit *hits, int cap,
                      int *counts, int brute, int *status, void *stream);
 int cpg_launch_set_arb_impulses(const cpgSet *s, int w, const double *imp, const int *pairs, int n, int *mismatch, void *stream);

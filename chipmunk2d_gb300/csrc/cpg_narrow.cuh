@@ -9,6 +9,9 @@
  * produced with the reference's arithmetic, in the same order.
  */
 #pragma once
+#ifdef __CUDACC__
+#include <math_constants.h>
+#endif
 #include "cpg_device.h"
 #include "cpg_math.cuh"
 
@@ -30,7 +33,7 @@ struct NarrowCtx {
 	int shapeBase, bodyBase, vertBase;
 };
 
-__device__ ShapeView load_shape(const NarrowCtx &c, int shape)
+static __device__ ShapeView load_shape(const NarrowCtx &c, int shape)
 {
 	const cpgSet *s = c.s;
 	int g = c.shapeBase + shape;
@@ -86,7 +89,7 @@ struct SPt { V2 p; unsigned index; };
 struct MPt { V2 a, b, ab; unsigned id; };
 
 /* cpCollision.c:62-76 */
-__device__ int poly_support_index(const ShapeView &s, V2 n)
+static __device__ int poly_support_index(const ShapeView &s, V2 n)
 {
 	double max = -CUDART_INF;
 	int index = 0;
@@ -98,7 +101,7 @@ __device__ int poly_support_index(const ShapeView &s, V2 n)
 }
 
 /* cpCollision.c:86-110 */
-__device__ SPt support_point(const ShapeView &s, V2 n)
+static __device__ SPt support_point(const ShapeView &s, V2 n)
 {
 	SPt sp;
 	if(s.kind == CPG_CIRCLE){
@@ -129,7 +132,7 @@ struct EdgePt { V2 p; unsigned long long hash; };
 struct Edge { EdgePt a, b; double r; V2 n; };
 
 /* cpCollision.c:163-182 */
-__device__ Edge support_edge_poly(const ShapeView &poly, V2 n)
+static __device__ Edge support_edge_poly(const ShapeView &poly, V2 n)
 {
 	int count = poly.count;
 	int i1 = poly_support_index(poly, n);
@@ -150,7 +153,7 @@ __device__ Edge support_edge_poly(const ShapeView &poly, V2 n)
 }
 
 /* cpCollision.c:184-195 */
-__device__ Edge support_edge_segment(const ShapeView &seg, V2 n)
+static __device__ Edge support_edge_segment(const ShapeView &seg, V2 n)
 {
 	Edge e;
 	if(vdot(seg.n, n) > 0.0){
@@ -181,7 +184,7 @@ __device__ __forceinline__ V2 lerp_t(V2 a, V2 b, double t)
 struct CPts { V2 a, b, n; double d; unsigned id; };
 
 /* cpCollision.c:227-258 */
-__device__ CPts closest_points(const MPt &v0, const MPt &v1)
+static __device__ CPts closest_points(const MPt &v0, const MPt &v1)
 {
 	double t = closest_t(v0.ab, v1.ab);
 	V2 p = lerp_t(v0.ab, v1.ab, t);
@@ -211,7 +214,7 @@ __device__ __forceinline__ double closest_dist(V2 v0, V2 v1)
 #define CPG_GJK_MAX 30
 
 /* EPA as a bounded loop (cpCollision.c:270-343). */
-__device__ CPts epa(const ShapeView &s1, const ShapeView &s2, MPt v0, MPt v1, MPt v2)
+static __device__ CPts epa(const ShapeView &s1, const ShapeView &s2, MPt v0, MPt v1, MPt v2)
 {
 	MPt hull[CPG_EPA_MAX + 4], hull2[CPG_EPA_MAX + 4];
 	int count = 3;
@@ -249,7 +252,7 @@ __device__ CPts epa(const ShapeView &s1, const ShapeView &s2, MPt v0, MPt v1, MP
 }
 
 /* GJK as a bounded loop (cpCollision.c:348-392). */
-__device__ CPts gjk_loop(const ShapeView &s1, const ShapeView &s2, MPt v0, MPt v1)
+static __device__ CPts gjk_loop(const ShapeView &s1, const ShapeView &s2, MPt v0, MPt v1)
 {
 	int iteration = 1;
 	for(int guard = 0; guard < 4*CPG_GJK_MAX + 8; guard++){
@@ -272,7 +275,7 @@ __device__ CPts gjk_loop(const ShapeView &s1, const ShapeView &s2, MPt v0, MPt v
 }
 
 /* cpCollision.c:395-415 */
-__device__ SPt shape_point(const ShapeView &s, int i)
+static __device__ SPt shape_point(const ShapeView &s, int i)
 {
 	SPt sp;
 	if(s.kind == CPG_CIRCLE){ sp.p = s.p0; sp.index = 0; }
@@ -285,7 +288,7 @@ __device__ SPt shape_point(const ShapeView &s, int i)
 }
 
 /* cpCollision.c:416-472 */
-__device__ CPts gjk(const ShapeView &s1, const ShapeView &s2, unsigned &id)
+static __device__ CPts gjk(const ShapeView &s1, const ShapeView &s2, unsigned &id)
 {
 	MPt v0, v1;
 	if(id){
@@ -302,7 +305,7 @@ __device__ CPts gjk(const ShapeView &s1, const ShapeView &s2, unsigned &id)
 }
 
 /* cpCollision.c:477-518 */
-__device__ void contact_points(const Edge &e1, const Edge &e2, const CPts &pts, NInfo &info)
+static __device__ void contact_points(const Edge &e1, const Edge &e2, const CPts &pts, NInfo &info)
 {
 	double mindist = e1.r + e2.r;
 	if(pts.d <= mindist){
@@ -328,7 +331,7 @@ __device__ void contact_points(const Edge &e1, const Edge &e2, const CPts &pts, 
 }
 
 /* cpCollision.c:525-537 */
-__device__ void circle_circle(const ShapeView &c1, const ShapeView &c2, NInfo &info)
+static __device__ void circle_circle(const ShapeView &c1, const ShapeView &c2, NInfo &info)
 {
 	double mindist = c1.r + c2.r;
 	V2 delta = vsub(c2.p0, c1.p0);
@@ -341,7 +344,7 @@ __device__ void circle_circle(const ShapeView &c1, const ShapeView &c2, NInfo &i
 }
 
 /* cpCollision.c:539-569 */
-__device__ void circle_segment(const ShapeView &circle, const ShapeView &seg, NInfo &info)
+static __device__ void circle_segment(const ShapeView &circle, const ShapeView &seg, NInfo &info)
 {
 	V2 seg_a = seg.p0, seg_b = seg.p1, center = circle.p0;
 	V2 seg_delta = vsub(seg_b, seg_a);
@@ -362,7 +365,7 @@ __device__ void circle_segment(const ShapeView &circle, const ShapeView &seg, NI
 }
 
 /* cpCollision.c:571-604 */
-__device__ void segment_segment(const ShapeView &s1, const ShapeView &s2, NInfo &info)
+static __device__ void segment_segment(const ShapeView &s1, const ShapeView &s2, NInfo &info)
 {
 	CPts pts = gjk(s1, s2, info.id);
 	V2 n = pts.n;
@@ -377,7 +380,7 @@ __device__ void segment_segment(const ShapeView &s1, const ShapeView &s2, NInfo 
 }
 
 /* cpCollision.c:606-627 */
-__device__ void poly_poly(const ShapeView &p1, const ShapeView &p2, NInfo &info)
+static __device__ void poly_poly(const ShapeView &p1, const ShapeView &p2, NInfo &info)
 {
 	CPts pts = gjk(p1, p2, info.id);
 	if(pts.d - p1.r - p2.r <= 0.0){
@@ -386,7 +389,7 @@ __device__ void poly_poly(const ShapeView &p1, const ShapeView &p2, NInfo &info)
 }
 
 /* cpCollision.c:629-659 */
-__device__ void segment_poly(const ShapeView &seg, const ShapeView &poly, NInfo &info)
+static __device__ void segment_poly(const ShapeView &seg, const ShapeView &poly, NInfo &info)
 {
 	CPts pts = gjk(seg, poly, info.id);
 	V2 n = pts.n;
@@ -399,7 +402,7 @@ __device__ void segment_poly(const ShapeView &seg, const ShapeView &poly, NInfo 
 }
 
 /* cpCollision.c:661-679 */
-__device__ void circle_poly(const ShapeView &circle, const ShapeView &poly, NInfo &info)
+static __device__ void circle_poly(const ShapeView &circle, const ShapeView &poly, NInfo &info)
 {
 	CPts pts = gjk(circle, poly, info.id);
 	if(pts.d <= circle.r + poly.r){
@@ -410,7 +413,7 @@ __device__ void circle_poly(const ShapeView &circle, const ShapeView &poly, NInf
 
 /* cpCollision.c:701-726.  Returns info for (a, b) after ordering by kind;
  * `flip` tells whether info.a is the second argument. */
-__device__ void collide(const ShapeView &a, const ShapeView &b, unsigned idIn, NInfo &info, int &flip)
+static __device__ void collide(const ShapeView &a, const ShapeView &b, unsigned idIn, NInfo &info, int &flip)
 {
 	info.n = v2(0.0, 0.0);
 	info.count = 0;

@@ -32,6 +32,7 @@
 #include <cuda_runtime.h>
 #include "cpg_device.h"
 #include "cpg_math.cuh"
+#include "cpg_narrow.cuh"
 
 #define CPG_QUERY_STACK 256
 #define MAGIC_EPSILON 1e-5
@@ -426,5 +427,140 @@ extern "C" int cpg_launch_query(const cpgSet *s, int world, const cpgQuery *quer
 {
 	if(nq <= 0) return 0;
 	k_query<<<(nq + 127)/128, 128, 0, (cudaStream_t)stream>>>(*s, world, queries, nq, hits, cap, counts, brute, status);
+	return cudaGetLastError() == cudaSuccess ? 0 : -1;
+}
+
+/* ---- shape queries (cpSpaceQuery.c:214-246) and cpShapesCollide ---- */
+
+/* A probe's view for the narrow phase; planes holds its polygon planes as
+ * four arrays of n (x, y of the points, then of the normals). */
+__device__ ShapeView probe_view(const cpgProbe &p, const double *planes, int n)
+{
+	ShapeView v;
+	v.kind = p.kind;
+	v.r = p.r;
+	v.p0 = v2(p.p0x, p.p0y); v.p1 = v2(p.p1x, p.p1y); v.n = v2(p.nx, p.ny);
+	v.atan = v2(p.atx, p.aty); v.btan = v2(p.btx, p.bty);
+	v.rot = v2(p.rotx, p.roty);
+	v.bb = bbnew(p.bbl, p.bbb, p.bbr, p.bbt);
+	v.hashid = p.hashid;
+	v.count = p.count;
+	v.vx = planes + p.voff; v.vy = planes + n + p.voff;
+	v.nx = planes + 2*n + p.voff; v.ny = planes + 3*n + p.voff;
+	return v;
+}
+
+/* cpShapesCollide(a, b): the contact set with a's side first */
+__device__ void shapes_collide(const ShapeView &a, const ShapeView &b, cpgShapeHit &h)
+{
+	NInfo info;
+	int flip;
+	collide(a, b, 0u, info, flip);
+	int count = info.count < 2 ? info.count : 2;
+	h.count = count;
+	V2 n = flip ? vneg(info.n) : info.n;
+	h.nx = n.x; h.ny = n.y;
+	for(int i = 0; i < 2; i++){
+		h.ax[i] = h.ay[i] = h.bx[i] = h.by[i] = h.dist[i] = 0.0;
+	}
+	for(int i = 0; i < count; i++){
+		V2 p1 = info.p1[i], p2 = info.p2[i];
+		V2 pa = flip ? p2 : p1, pb = flip ? p1 : p2;
+		h.ax[i] = pa.x; h.ay[i] = pa.y; h.bx[i] = pb.x; h.by[i] = pb.y;
+		h.dist[i] = vdot(vsub(p2, p1), n);
+	}
+}
+
+struct SQOut { cpgShapeHit *hits; int cap, n, any; };
+
+/* ShapeQuery (cpSpaceQuery.c:214-228) on one leaf */
+__device__ void shape_query_leaf(const cpgSet &s, const cpgWorld &W, const cpgProbe &p, const ShapeView &a, int shape, SQOut &o)
+{
+	int g = W.shapeOff + shape;
+	unsigned long long grp = s.sgroup[g];
+	bool reject = (p.group != 0ull && p.group == grp) || (p.cat & s.smask[g]) == 0u || (s.scat[g] & p.mask) == 0u;
+	if(reject || shape == p.slot) return;
+	NarrowCtx nc; nc.s = &s; nc.shapeBase = W.shapeOff; nc.bodyBase = W.bodyOff; nc.vertBase = W.vertOff;
+	ShapeView b = load_shape(nc, shape);
+	cpgShapeHit h;
+	shapes_collide(a, b, h);
+	if(h.count){
+		h.shape = shape; h.sensor = s.ssensor[g]; h.pad = 0;
+		if(o.n < o.cap) o.hits[o.n] = h;
+		o.n++;
+		o.any = !(p.sensor || s.ssensor[g]);
+	}
+}
+
+__global__ void k_shape_query(cpgSet s, int w, cpgProbe p, const double *planes, int nplanes, int brute,
+                              cpgShapeHit *hits, int cap, int *counts)
+{
+	if(blockIdx.x != 0 || threadIdx.x != 0) return;
+	const cpgWorld &W = s.world[w];
+	const cpgTree &T = s.tree[w];
+	const cpgNode *nodes = s.nodes + W.nodeOff;
+	ShapeView a = probe_view(p, planes, nplanes);
+	BB qb = bbnew(p.bbl, p.bbb, p.bbr, p.bbt);
+	SQOut o; o.hits = hits; o.cap = cap; o.n = 0; o.any = 0;
+	bool ok = true;
+	if(brute){
+		for(int pass = 0; pass < 2; pass++){
+			for(int k = 0; k < W.nshapes; k++){
+				int g = W.shapeOff + k;
+				bool isStatic = s.btype[W.bodyOff + s.sbody[g]] == CPG_STATIC;
+				if(isStatic != (pass == 1)) continue;
+				if(!bbintersects(bbnew(s.bbl[g], s.bbb[g], s.bbr[g], s.bbt[g]), qb)) continue;
+				shape_query_leaf(s, W, p, a, k, o);
+			}
+		}
+	} else {
+		int roots[2] = { T.dynRoot, T.statRoot };
+		for(int t = 0; t < 2 && ok; t++){
+			if(roots[t] < 0) continue;
+			int stack[CPG_QUERY_STACK];
+			int sp = 0;
+			stack[sp++] = roots[t];
+			for(int guard = 0; sp > 0; guard++){
+				if(guard > 2*W.nodeCap + 2){ ok = false; break; }
+				int n = stack[--sp];
+				const cpgNode &nd = nodes[n];
+				if(!bbintersects(q_node_bb(nd), qb)) continue;
+				if(nd.obj >= 0){
+					shape_query_leaf(s, W, p, a, nd.obj, o);
+				} else {
+					if(sp + 2 > CPG_QUERY_STACK){ ok = false; break; }
+					stack[sp++] = nd.B;
+					stack[sp++] = nd.A;
+				}
+			}
+		}
+	}
+	counts[0] = o.n;
+	counts[1] = o.any;
+	counts[2] = ok ? 0 : 1;
+}
+
+__global__ void k_shape_pair(const cpgProbe *probes, const double *planes, int nplanes, cpgShapeHit *hit, int *counts)
+{
+	if(blockIdx.x != 0 || threadIdx.x != 0) return;
+	ShapeView a = probe_view(probes[0], planes, nplanes), b = probe_view(probes[1], planes, nplanes);
+	cpgShapeHit h;
+	shapes_collide(a, b, h);
+	h.shape = -1; h.sensor = 0; h.pad = 0;
+	*hit = h;
+	counts[0] = h.count;
+}
+
+extern "C" int cpg_launch_shape_query(const cpgSet *s, int world, const cpgProbe *probe, const double *planes, int nplanes,
+                                      int brute, cpgShapeHit *hits, int cap, int *counts, void *stream)
+{
+	k_shape_query<<<1, 32, 0, (cudaStream_t)stream>>>(*s, world, *probe, planes, nplanes, brute, hits, cap, counts);
+	return cudaGetLastError() == cudaSuccess ? 0 : -1;
+}
+
+extern "C" int cpg_launch_shape_pair(const cpgProbe *probes, const double *planes, int nplanes, cpgShapeHit *hit,
+                                     int *counts, void *stream)
+{
+	k_shape_pair<<<1, 32, 0, (cudaStream_t)stream>>>(probes, planes, nplanes, hit, counts);
 	return cudaGetLastError() == cudaSuccess ? 0 : -1;
 }

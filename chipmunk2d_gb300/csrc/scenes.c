@@ -778,10 +778,15 @@ cpConstraint *cpx_scene_constraint(void *h, int i) { return ((cpxScene *)h)->con
  * nq seeded queries over the scene's extent, cycling through the kinds:
  * 0 cpSpacePointQuery, 1 cpSpacePointQueryNearest, 2 cpSpaceSegmentQuery,
  * 3 cpSpaceSegmentQueryFirst, 4 cpSpaceBBQuery, 5 cpShapePointQuery,
- * 6 cpShapeSegmentQuery.  Every callback and every result is one record
- * of 8 doubles: query, kind, shape (its index in the scene, -1 none),
- * point x, y, distance or alpha, gradient or normal x, y.  Returns the
- * record count (records past cap are counted, not written). */
+ * 6 cpShapeSegmentQuery, 7 cpSpaceShapeQuery.  Every callback and every
+ * result is one record of 8 doubles: query, kind, shape (its index in the
+ * scene, -1 none), point x, y, distance or alpha, gradient or normal x, y.
+ * A shape query's callback gives [query, 7, shape, count, normal x, y, 0,
+ * 0] and a record [query, 8, shape, pointA x, y, pointB x, y, distance]
+ * per contact point; the query ends with [query, 9, its result, 0...].
+ * Its probe is a scene shape or, every other time, a circle, box or
+ * segment on a body of its own that is in no space.  Returns the record
+ * count (records past cap are counted, not written). */
 typedef struct QRec { double *out; int cap, n, qi, kind; } QRec;
 
 static int shape_index_(const cpShape *s) { return s ? (int)(intptr_t)cpShapeGetUserData(s) - 1 : -1; }
@@ -797,6 +802,17 @@ static void q_put(QRec *r, int shape, cpVect p, double d, cpVect g)
 static void q_point_cb(cpShape *s, cpVect p, cpFloat d, cpVect g, void *data) { q_put((QRec *)data, shape_index_(s), p, d, g); }
 static void q_seg_cb(cpShape *s, cpVect p, cpVect n, cpFloat a, void *data) { q_put((QRec *)data, shape_index_(s), p, a, n); }
 static void q_bb_cb(cpShape *s, void *data) { q_put((QRec *)data, shape_index_(s), cpvzero, 0.0, cpvzero); }
+static void q_shape_cb(cpShape *s, cpContactPointSet *set, void *data)
+{
+	QRec *r = (QRec *)data;
+	int idx = shape_index_(s);
+	q_put(r, idx, cpv((double)set->count, set->normal.x), set->normal.y, cpvzero);
+	int kind = r->kind;
+	r->kind = 8;
+	for(int i = 0; i < set->count; i++)
+		q_put(r, idx, set->points[i].pointA, set->points[i].pointB.x, cpv(set->points[i].pointB.y, set->points[i].distance));
+	r->kind = kind;
+}
 
 int cpx_scene_queries(void *h, int seed, int nq, double *out, int cap)
 {
@@ -819,7 +835,7 @@ int cpx_scene_queries(void *h, int seed, int nq, double *out, int cap)
 	rng_seed(&rng, (uint64_t)seed*0x9e3779b97f4a7c15ULL + 17u);
 	double size = (ext.r - ext.l) > (ext.t - ext.b) ? (ext.r - ext.l) : (ext.t - ext.b);
 	for(int qi = 0; qi < nq && nlive > 0; qi++){
-		int kind = qi % 7;
+		int kind = qi % 8;
 		rec.qi = qi; rec.kind = kind;
 		/* near a shape half of the time, anywhere in the extent otherwise */
 		cpShape *target = sc->shapes[live[rng_int(&rng, 0, nlive - 1)]];
@@ -872,10 +888,33 @@ int cpx_scene_queries(void *h, int seed, int nq, double *out, int cap)
 			q_put(&rec, shape_index_(target), info.point, d, info.gradient);
 			break;
 		}
-		default: {
+		case 6: {
 			cpSegmentQueryInfo info;
 			cpBool hit = cpShapeSegmentQuery(target, p, q, r, &info);
 			q_put(&rec, hit ? shape_index_(target) : -1, info.point, info.alpha, info.normal);
+			break;
+		}
+		default: {
+			cpBool any;
+			if((qi/8) % 2 == 0){
+				/* a scene shape against the others */
+				any = cpSpaceShapeQuery(sp, target, q_shape_cb, &rec);
+			} else {
+				cpBody *pb = cpBodyNew(1.0, 1.0);
+				cpBodySetPosition(pb, p);
+				cpBodySetAngle(pb, rng_uniform(&rng, 0.0, 6.0));
+				cpShape *probe;
+				int pk = (qi/16) % 3;
+				if(pk == 0) probe = cpCircleShapeNew(pb, rng_uniform(&rng, 1.0, 6.0), cpvzero);
+				else if(pk == 1) probe = cpBoxShapeNew(pb, rng_uniform(&rng, 2.0, 12.0), rng_uniform(&rng, 2.0, 12.0), rng_uniform(&rng, 0.0, 0.5));
+				else probe = cpSegmentShapeNew(pb, cpv(-rng_uniform(&rng, 1.0, 8.0), 0.0), cpv(rng_uniform(&rng, 1.0, 8.0), 0.0), rng_uniform(&rng, 0.0, 1.0));
+				cpShapeSetFilter(probe, filter);
+				any = cpSpaceShapeQuery(sp, probe, q_shape_cb, &rec);
+				cpShapeFree(probe);
+				cpBodyFree(pb);
+			}
+			rec.kind = 9;
+			q_put(&rec, (int)any, cpvzero, 0.0, cpvzero);
 			break;
 		}
 		}

@@ -138,6 +138,7 @@ typedef void (*cpSpaceConstraintIteratorFunc)(cpConstraint *constraint, void *da
 typedef void (*cpSpacePointQueryFunc)(cpShape *shape, cpVect point, cpFloat distance, cpVect gradient, void *data);
 typedef void (*cpSpaceSegmentQueryFunc)(cpShape *shape, cpVect point, cpVect normal, cpFloat alpha, void *data);
 typedef void (*cpSpaceBBQueryFunc)(cpShape *shape, void *data);
+typedef void (*cpSpaceShapeQueryFunc)(cpShape *shape, cpContactPointSet *points, void *data);
 
 /* cpConstraint.h:25-29 */
 typedef void (*cpConstraintPreSolveFunc)(cpConstraint *constraint, cpSpace *space);
@@ -267,6 +268,10 @@ void cpSpaceSegmentQuery(cpSpace *space, cpVect start, cpVect end, cpFloat radiu
 cpShape *cpSpaceSegmentQueryFirst(cpSpace *space, cpVect start, cpVect end, cpFloat radius, cpShapeFilter filter,
                                   cpSegmentQueryInfo *out);                                        /* cpSpace.h:207 */
 void cpSpaceBBQuery(cpSpace *space, cpBB bb, cpShapeFilter filter, cpSpaceBBQueryFunc func, void *data); /* cpSpace.h:212 */
+/* Shapes overlapping a shape (cpSpaceQuery.c:214-246): its cache is
+ * brought to its body's transform, as the reference does, and each
+ * overlapping shape comes with its contact point set. */
+cpBool cpSpaceShapeQuery(cpSpace *space, cpShape *shape, cpSpaceShapeQueryFunc func, void *data);     /* cpSpace.h:217 */
 
 /* ------------------------------------------------------------------------
  * Body: cpBody.h:49-187
@@ -351,6 +356,8 @@ void cpShapeSetFilter(cpShape *shape, cpShapeFilter filter);         /* cpShape.
  * last step (cpShape.c:222-256). */
 cpFloat cpShapePointQuery(const cpShape *shape, cpVect p, cpPointQueryInfo *out);                  /* cpShape.h:89 */
 cpBool cpShapeSegmentQuery(const cpShape *shape, cpVect a, cpVect b, cpFloat radius, cpSegmentQueryInfo *info); /* cpShape.h:92 */
+/* The contact points of two shapes at their cached positions (cpShape.c:258-283). */
+cpContactPointSet cpShapesCollide(const cpShape *a, const cpShape *b);                              /* cpShape.h:95 */
 cpShape *cpCircleShapeNew(cpBody *body, cpFloat radius, cpVect offset);      /* cpShape.h:170 */
 cpVect cpCircleShapeGetOffset(const cpShape *shape);                         /* cpShape.h:173 */
 cpFloat cpCircleShapeGetRadius(const cpShape *shape);                        /* cpShape.h:175 */

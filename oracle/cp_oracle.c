@@ -3304,3 +3304,55 @@ void cpSpaceBBQuery(cpSpace *sp, cpBB bb, cpShapeFilter filter, cpSpaceBBQueryFu
 	tree_query_(sp, &sp->dynTree, &q);
 	tree_query_(sp, &sp->statTree, &q);
 }
+
+
+/* cpShape.c:258-283 */
+cpContactPointSet cpShapesCollide(const cpShape *a, const cpShape *b)
+{
+	CollisionInfo info = collide((cpShape *)a, (cpShape *)b, 0);
+	cpContactPointSet set;
+	memset(&set, 0, sizeof(set));
+	set.count = info.count;
+	cpBool swapped = (a != info.a);
+	set.normal = (swapped ? cpvneg(info.n) : info.n);
+	for(int i = 0; i < info.count; i++){
+		cpVect p1 = info.arr[i].r1, p2 = info.arr[i].r2;
+		set.points[i].pointA = (swapped ? p2 : p1);
+		set.points[i].pointB = (swapped ? p1 : p2);
+		set.points[i].distance = cpvdot(cpvsub(p2, p1), set.normal);
+	}
+	return set;
+}
+
+typedef struct ShapeQueryCtx { cpShape *shape; cpSpaceShapeQueryFunc func; void *data; cpBool anyCollision; } ShapeQueryCtx;
+
+/* cpSpaceQuery.c:214-228 (ShapeQuery) over cpBBTree.c:355-365 */
+static void subtree_shape_query_(cpSpace *sp, int n, cpBB bb, ShapeQueryCtx *q)
+{
+	Node *nd = &sp->nodes[n];
+	if(!cpBBIntersects(nd->bb, bb)) return;
+	if(nd->obj){
+		cpShape *a = q->shape, *b = nd->obj;
+		if(filter_reject_(a->filter, b->filter) || a == b) return;
+		cpContactPointSet set = cpShapesCollide(a, b);
+		if(set.count){
+			if(q->func) q->func(b, &set, q->data);
+			q->anyCollision = !(a->sensor || b->sensor);
+		}
+	} else {
+		int B = nd->B;
+		subtree_shape_query_(sp, nd->A, bb, q);
+		subtree_shape_query_(sp, B, bb, q);
+	}
+}
+
+/* cpSpaceQuery.c:230-246 */
+cpBool cpSpaceShapeQuery(cpSpace *sp, cpShape *shape, cpSpaceShapeQueryFunc func, void *data)
+{
+	cpBody *body = shape->body;
+	cpBB bb = (body ? shape_update(shape, body->transform) : shape->bb);
+	ShapeQueryCtx q = {shape, func, data, cpFalse};
+	if(sp->dynTree.root >= 0) subtree_shape_query_(sp, sp->dynTree.root, bb, &q);
+	if(sp->statTree.root >= 0) subtree_shape_query_(sp, sp->statTree.root, bb, &q);
+	return q.anyCollision;
+}
