@@ -1022,6 +1022,7 @@ def run_ours(args):
                    "parallelism": "replicas" if world_size > 1 else "single"},
         "e2e": {"value": e2e_value, "unit": "body-steps/s", "h2d_bytes_per_step": 88,
                 "d2h_bytes_per_step": 64 * n + 64, "steps": e2e_steps,
+                "l2": "not flushed: consecutive steps as a program runs them (the device-timed value flushes L2 before every step)",
                 "path": "cpSpaceStep + cpGpuSpaceGetBodyStates (every body's position, velocity, angle, angular velocity, rotation into pinned host memory)",
                 "per_body_getters": {"value": getter_value, "steps": min(e2e_steps, 20),
                                      "path": "cpSpaceStep + cpBodyGetPosition/Velocity/Angle/AngularVelocity/Rotation for every body (one C call each)"}},
