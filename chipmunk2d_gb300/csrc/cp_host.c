@@ -202,6 +202,7 @@ struct cpSpace {
 	                                           the host holds the state until the next step rebuilds it */
 	double jointDt;                         /* dt the joint bias terms were made for */
 	unsigned long long editGen;             /* counts object edits through the setters */
+	unsigned long hastyThreads;             /* cpHastySpaceSetThreads */
 
 	cpArbiter *snap; int nsnap, capsnap; int snapValid;
 	float phaseMs[8];
@@ -2896,6 +2897,7 @@ cpShape *cpBoxShapeNew(cpBody *body, cpFloat width, cpFloat height, cpFloat radi
 }
 
 void cpShapeFree(cpShape *s) { if(s){ free(s->lv); free(s); } }
+void cpShapeDestroy(cpShape *s);
 
 static inline cpShape *swr(cpShape *s) { if(s->space){ s->space->shapeDirty = 1; s->space->editGen++; } return s; }
 
@@ -3200,7 +3202,7 @@ cpSpace *cpSpaceNew(void)
 	return sp;
 }
 
-void cpSpaceFree(cpSpace *sp)
+void cpSpaceDestroy(cpSpace *sp)
 {
 	if(!sp) return;
 	if(sp->dev && sp->ownsDev){
@@ -3214,8 +3216,99 @@ void cpSpaceFree(cpSpace *sp)
 	for(int i = 0; i < sp->nshapes; i++) if(sp->shapes[i] && sp->shapes[i]->space == sp) sp->shapes[i]->space = NULL;
 	for(int i = 0; i < sp->ncons; i++) if(sp->cons[i]->space == sp) sp->cons[i]->space = NULL;
 	free(sp->dyn); free(sp->stat); free(sp->shapes); free(sp->cons); free(sp->ops); free(sp->snap);
+	sp->dyn = NULL; sp->stat = NULL; sp->shapes = NULL; sp->cons = NULL; sp->ops = NULL; sp->snap = NULL;
+	sp->dev = NULL;
+}
+
+void cpSpaceFree(cpSpace *sp)
+{
+	if(!sp) return;
+	cpSpaceDestroy(sp);
 	free(sp);
 }
+
+/* ---- caller-placed objects: the New functions' objects moved into the
+ * caller's memory (no object refers to its own address except a space's
+ * static body, re-pointed here) ---- */
+static void *adopt_(void *mem, void *fresh, size_t bytes)
+{
+	if(mem && fresh) memcpy(mem, fresh, bytes);
+	free(fresh);
+	return mem;
+}
+
+cpSpace *cpSpaceAlloc(void) { return (cpSpace *)calloc(1, sizeof(cpSpace)); }
+cpSpace *cpSpaceInit(cpSpace *sp)
+{
+	adopt_(sp, cpSpaceNew(), sizeof(cpSpace));
+	sp->staticBody.space = sp;
+	return sp;
+}
+cpBody *cpBodyAlloc(void) { return (cpBody *)calloc(1, sizeof(cpBody)); }
+cpBody *cpBodyInit(cpBody *b, cpFloat mass, cpFloat moment) { return (cpBody *)adopt_(b, cpBodyNew(mass, moment), sizeof(cpBody)); }
+void cpBodyDestroy(cpBody *b) { (void)b; }
+void cpShapeDestroy(cpShape *s) { if(s){ free(s->lv); s->lv = s->ln = s->gv = s->gn = NULL; } }
+void cpConstraintDestroy(cpConstraint *c) { (void)c; }
+
+#define CPG_SHAPE_ALLOC(T) T *T##Alloc(void) { return (T *)calloc(1, sizeof(cpShape)); }
+#define CPG_JOINT_ALLOC(T) T *T##Alloc(void) { return (T *)calloc(1, sizeof(cpConstraint)); }
+CPG_SHAPE_ALLOC(cpCircleShape)
+CPG_SHAPE_ALLOC(cpSegmentShape)
+CPG_SHAPE_ALLOC(cpPolyShape)
+CPG_JOINT_ALLOC(cpPivotJoint)
+CPG_JOINT_ALLOC(cpPinJoint)
+CPG_JOINT_ALLOC(cpSlideJoint)
+CPG_JOINT_ALLOC(cpGrooveJoint)
+CPG_JOINT_ALLOC(cpDampedSpring)
+CPG_JOINT_ALLOC(cpDampedRotarySpring)
+CPG_JOINT_ALLOC(cpRotaryLimitJoint)
+CPG_JOINT_ALLOC(cpRatchetJoint)
+CPG_JOINT_ALLOC(cpGearJoint)
+CPG_JOINT_ALLOC(cpSimpleMotor)
+
+cpCircleShape *cpCircleShapeInit(cpCircleShape *m, cpBody *body, cpFloat radius, cpVect offset)
+{ return (cpCircleShape *)adopt_(m, cpCircleShapeNew(body, radius, offset), sizeof(cpShape)); }
+cpSegmentShape *cpSegmentShapeInit(cpSegmentShape *m, cpBody *body, cpVect a, cpVect b, cpFloat radius)
+{ return (cpSegmentShape *)adopt_(m, cpSegmentShapeNew(body, a, b, radius), sizeof(cpShape)); }
+cpPolyShape *cpPolyShapeInit(cpPolyShape *m, cpBody *body, int count, const cpVect *verts, cpTransform transform, cpFloat radius)
+{ return (cpPolyShape *)adopt_(m, cpPolyShapeNew(body, count, verts, transform, radius), sizeof(cpShape)); }
+cpPolyShape *cpPolyShapeInitRaw(cpPolyShape *m, cpBody *body, int count, const cpVect *verts, cpFloat radius)
+{ return (cpPolyShape *)adopt_(m, cpPolyShapeNewRaw(body, count, verts, radius), sizeof(cpShape)); }
+cpPolyShape *cpBoxShapeInit(cpPolyShape *m, cpBody *body, cpFloat width, cpFloat height, cpFloat radius)
+{ return (cpPolyShape *)adopt_(m, cpBoxShapeNew(body, width, height, radius), sizeof(cpShape)); }
+cpPolyShape *cpBoxShapeInit2(cpPolyShape *m, cpBody *body, cpBB box, cpFloat radius)
+{ return (cpPolyShape *)adopt_(m, cpBoxShapeNew2(body, box, radius), sizeof(cpShape)); }
+
+cpPivotJoint *cpPivotJointInit(cpPivotJoint *m, cpBody *a, cpBody *b, cpVect anchorA, cpVect anchorB)
+{ return (cpPivotJoint *)adopt_(m, cpPivotJointNew2(a, b, anchorA, anchorB), sizeof(cpConstraint)); }
+cpPinJoint *cpPinJointInit(cpPinJoint *m, cpBody *a, cpBody *b, cpVect anchorA, cpVect anchorB)
+{ return (cpPinJoint *)adopt_(m, cpPinJointNew(a, b, anchorA, anchorB), sizeof(cpConstraint)); }
+cpSlideJoint *cpSlideJointInit(cpSlideJoint *m, cpBody *a, cpBody *b, cpVect anchorA, cpVect anchorB, cpFloat min, cpFloat max)
+{ return (cpSlideJoint *)adopt_(m, cpSlideJointNew(a, b, anchorA, anchorB, min, max), sizeof(cpConstraint)); }
+cpGrooveJoint *cpGrooveJointInit(cpGrooveJoint *m, cpBody *a, cpBody *b, cpVect groove_a, cpVect groove_b, cpVect anchorB)
+{ return (cpGrooveJoint *)adopt_(m, cpGrooveJointNew(a, b, groove_a, groove_b, anchorB), sizeof(cpConstraint)); }
+cpDampedSpring *cpDampedSpringInit(cpDampedSpring *m, cpBody *a, cpBody *b, cpVect anchorA, cpVect anchorB,
+                                   cpFloat restLength, cpFloat stiffness, cpFloat damping)
+{ return (cpDampedSpring *)adopt_(m, cpDampedSpringNew(a, b, anchorA, anchorB, restLength, stiffness, damping), sizeof(cpConstraint)); }
+cpDampedRotarySpring *cpDampedRotarySpringInit(cpDampedRotarySpring *m, cpBody *a, cpBody *b, cpFloat restAngle,
+                                               cpFloat stiffness, cpFloat damping)
+{ return (cpDampedRotarySpring *)adopt_(m, cpDampedRotarySpringNew(a, b, restAngle, stiffness, damping), sizeof(cpConstraint)); }
+cpRotaryLimitJoint *cpRotaryLimitJointInit(cpRotaryLimitJoint *m, cpBody *a, cpBody *b, cpFloat min, cpFloat max)
+{ return (cpRotaryLimitJoint *)adopt_(m, cpRotaryLimitJointNew(a, b, min, max), sizeof(cpConstraint)); }
+cpRatchetJoint *cpRatchetJointInit(cpRatchetJoint *m, cpBody *a, cpBody *b, cpFloat phase, cpFloat ratchet)
+{ return (cpRatchetJoint *)adopt_(m, cpRatchetJointNew(a, b, phase, ratchet), sizeof(cpConstraint)); }
+cpGearJoint *cpGearJointInit(cpGearJoint *m, cpBody *a, cpBody *b, cpFloat phase, cpFloat ratio)
+{ return (cpGearJoint *)adopt_(m, cpGearJointNew(a, b, phase, ratio), sizeof(cpConstraint)); }
+cpSimpleMotor *cpSimpleMotorInit(cpSimpleMotor *m, cpBody *a, cpBody *b, cpFloat rate)
+{ return (cpSimpleMotor *)adopt_(m, cpSimpleMotorNew(a, b, rate), sizeof(cpConstraint)); }
+
+/* cpHastySpace.c:453-548: the threaded space, here a space (the device
+ * runs the solver); the thread count is stored and reported */
+cpSpace *cpHastySpaceNew(void) { return cpSpaceNew(); }
+void cpHastySpaceFree(cpSpace *sp) { cpSpaceFree(sp); }
+void cpHastySpaceSetThreads(cpSpace *sp, unsigned long threads) { if(sp) sp->hastyThreads = threads; }
+unsigned long cpHastySpaceGetThreads(cpSpace *sp) { return (sp && sp->hastyThreads) ? sp->hastyThreads : 1ul; }
+void cpHastySpaceStep(cpSpace *sp, cpFloat dt) { cpSpaceStep(sp, dt); }
 
 int cpSpaceGetIterations(const cpSpace *sp) { return sp->iterations; }
 void cpSpaceSetIterations(cpSpace *sp, int it) { ASSERT_HARD(it > 0, "Iterations must be positive and non-zero."); sp->iterations = it; }

@@ -65,6 +65,13 @@ typedef struct cpConstraint cpConstraint;
 typedef struct cpPinJoint cpPinJoint;
 typedef struct cpSlideJoint cpSlideJoint;
 typedef struct cpPivotJoint cpPivotJoint;
+typedef struct cpGrooveJoint cpGrooveJoint;
+typedef struct cpDampedSpring cpDampedSpring;
+typedef struct cpDampedRotarySpring cpDampedRotarySpring;
+typedef struct cpRotaryLimitJoint cpRotaryLimitJoint;
+typedef struct cpRatchetJoint cpRatchetJoint;
+typedef struct cpGearJoint cpGearJoint;
+typedef struct cpSimpleMotor cpSimpleMotor;
 typedef struct cpArbiter cpArbiter;
 typedef struct cpSpace cpSpace;
 typedef struct cpCollisionHandler cpCollisionHandler;
@@ -251,6 +258,60 @@ void cpSpaceEachBody(cpSpace *space, cpSpaceBodyIteratorFunc func, void *data); 
 void cpSpaceEachShape(cpSpace *space, cpSpaceShapeIteratorFunc func, void *data);           /* cpSpace.h:231 */
 void cpSpaceEachConstraint(cpSpace *space, cpSpaceConstraintIteratorFunc func, void *data); /* cpSpace.h:236 */
 void cpSpaceStep(cpSpace *space, cpFloat dt);                        /* cpSpace.h:255 */
+/* Caller-placed objects (cpSpace.h:80-88, cpBody.h:49-58, cpShape.h:78-84,
+ * 161-197, cpPolyShape.h:26-40, cpConstraint.h:61, the joints' headers):
+ * cp*Alloc returns zeroed memory of the object's size, cp*Init
+ * initialises it as the matching cp*New does and returns it, cp*Destroy
+ * releases what an object holds without freeing the object itself. */
+cpSpace *cpSpaceAlloc(void);
+cpSpace *cpSpaceInit(cpSpace *space);
+void cpSpaceDestroy(cpSpace *space);
+cpBody *cpBodyAlloc(void);
+cpBody *cpBodyInit(cpBody *body, cpFloat mass, cpFloat moment);
+void cpBodyDestroy(cpBody *body);
+void cpShapeDestroy(cpShape *shape);
+cpCircleShape *cpCircleShapeAlloc(void);
+cpCircleShape *cpCircleShapeInit(cpCircleShape *circle, cpBody *body, cpFloat radius, cpVect offset);
+cpSegmentShape *cpSegmentShapeAlloc(void);
+cpSegmentShape *cpSegmentShapeInit(cpSegmentShape *seg, cpBody *body, cpVect a, cpVect b, cpFloat radius);
+cpPolyShape *cpPolyShapeAlloc(void);
+cpPolyShape *cpPolyShapeInit(cpPolyShape *poly, cpBody *body, int count, const cpVect *verts, cpTransform transform, cpFloat radius);
+cpPolyShape *cpPolyShapeInitRaw(cpPolyShape *poly, cpBody *body, int count, const cpVect *verts, cpFloat radius);
+cpPolyShape *cpBoxShapeInit(cpPolyShape *poly, cpBody *body, cpFloat width, cpFloat height, cpFloat radius);
+cpPolyShape *cpBoxShapeInit2(cpPolyShape *poly, cpBody *body, cpBB box, cpFloat radius);
+void cpConstraintDestroy(cpConstraint *constraint);
+cpPivotJoint *cpPivotJointAlloc(void);
+cpPivotJoint *cpPivotJointInit(cpPivotJoint *joint, cpBody *a, cpBody *b, cpVect anchorA, cpVect anchorB);
+cpPinJoint *cpPinJointAlloc(void);
+cpPinJoint *cpPinJointInit(cpPinJoint *joint, cpBody *a, cpBody *b, cpVect anchorA, cpVect anchorB);
+cpSlideJoint *cpSlideJointAlloc(void);
+cpSlideJoint *cpSlideJointInit(cpSlideJoint *joint, cpBody *a, cpBody *b, cpVect anchorA, cpVect anchorB, cpFloat min, cpFloat max);
+cpGrooveJoint *cpGrooveJointAlloc(void);
+cpGrooveJoint *cpGrooveJointInit(cpGrooveJoint *joint, cpBody *a, cpBody *b, cpVect groove_a, cpVect groove_b, cpVect anchorB);
+cpDampedSpring *cpDampedSpringAlloc(void);
+cpDampedSpring *cpDampedSpringInit(cpDampedSpring *joint, cpBody *a, cpBody *b, cpVect anchorA, cpVect anchorB,
+                                   cpFloat restLength, cpFloat stiffness, cpFloat damping);
+cpDampedRotarySpring *cpDampedRotarySpringAlloc(void);
+cpDampedRotarySpring *cpDampedRotarySpringInit(cpDampedRotarySpring *joint, cpBody *a, cpBody *b, cpFloat restAngle,
+                                               cpFloat stiffness, cpFloat damping);
+cpRotaryLimitJoint *cpRotaryLimitJointAlloc(void);
+cpRotaryLimitJoint *cpRotaryLimitJointInit(cpRotaryLimitJoint *joint, cpBody *a, cpBody *b, cpFloat min, cpFloat max);
+cpRatchetJoint *cpRatchetJointAlloc(void);
+cpRatchetJoint *cpRatchetJointInit(cpRatchetJoint *joint, cpBody *a, cpBody *b, cpFloat phase, cpFloat ratchet);
+cpGearJoint *cpGearJointAlloc(void);
+cpGearJoint *cpGearJointInit(cpGearJoint *joint, cpBody *a, cpBody *b, cpFloat phase, cpFloat ratio);
+cpSimpleMotor *cpSimpleMotorAlloc(void);
+cpSimpleMotor *cpSimpleMotorInit(cpSimpleMotor *joint, cpBody *a, cpBody *b, cpFloat rate);
+
+/* cpHastySpace.h:6-27: the threaded space's entry points.  The device
+ * step is the solver here, so a hasty space is a space; the thread count
+ * is kept and reported. */
+cpSpace *cpHastySpaceNew(void);
+void cpHastySpaceFree(cpSpace *space);
+void cpHastySpaceSetThreads(cpSpace *space, unsigned long threads);
+unsigned long cpHastySpaceGetThreads(cpSpace *space);
+void cpHastySpaceStep(cpSpace *space, cpFloat dt);
+
 /* Spatial queries (cpSpaceQuery.c:49-212).  They run on the device, over
  * the space's own trees in the exact-order mode (the reference's visit
  * order: dynamic then static shapes for point and box queries, static

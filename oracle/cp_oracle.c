@@ -2286,7 +2286,8 @@ cpSpace *cpSpaceNew(void)
 
 static void hasty_stop(cpSpace *sp);
 
-void cpSpaceFree(cpSpace *sp)
+/* cpSpace.c:180-205 (cpSpaceDestroy / cpSpaceFree) */
+void cpSpaceDestroy(cpSpace *sp)
 {
 	if(!sp) return;
 	hasty_stop(sp);
@@ -2295,6 +2296,16 @@ void cpSpaceFree(cpSpace *sp)
 	free(sp->dynTree.leaves.bins); free(sp->statTree.leaves.bins);
 	free(sp->arbs); free(sp->freeList); free(sp->amap.keys); free(sp->amap.slot); free(sp->active);
 	free(sp->candPairs);
+	sp->dyn = sp->stat = NULL; sp->cons = NULL; sp->nodes = NULL; sp->pairs = NULL;
+	sp->dynTree.leaves.bins = sp->statTree.leaves.bins = NULL;
+	sp->arbs = NULL; sp->freeList = NULL; sp->amap.keys = NULL; sp->amap.slot = NULL; sp->active = NULL;
+	sp->candPairs = NULL;
+}
+
+void cpSpaceFree(cpSpace *sp)
+{
+	if(!sp) return;
+	cpSpaceDestroy(sp);
 	free(sp);
 }
 
@@ -3356,3 +3367,82 @@ cpBool cpSpaceShapeQuery(cpSpace *sp, cpShape *shape, cpSpaceShapeQueryFunc func
 	if(sp->statTree.root >= 0) subtree_shape_query_(sp, sp->statTree.root, bb, &q);
 	return q.anyCollision;
 }
+
+
+/* ---- caller-placed objects (the *Alloc / *Init / *Destroy functions of
+ * cpSpace.c, cpBody.c, cpShape.c, cpPolyShape.c and the joints): the New
+ * functions' objects moved into the caller's memory; only a space's
+ * static body refers back to its owner ---- */
+static void *adopt_(void *mem, void *fresh, size_t bytes)
+{
+	if(mem && fresh) memcpy(mem, fresh, bytes);
+	free(fresh);
+	return mem;
+}
+
+cpSpace *cpSpaceAlloc(void) { return (cpSpace *)calloc(1, sizeof(cpSpace)); }
+cpSpace *cpSpaceInit(cpSpace *sp) { adopt_(sp, cpSpaceNew(), sizeof(cpSpace)); sp->staticBody.space = sp; return sp; }
+cpBody *cpBodyAlloc(void) { return (cpBody *)calloc(1, sizeof(cpBody)); }
+cpBody *cpBodyInit(cpBody *b, cpFloat m, cpFloat i) { return (cpBody *)adopt_(b, cpBodyNew(m, i), sizeof(cpBody)); }
+void cpBodyDestroy(cpBody *b) { (void)b; }
+void cpShapeDestroy(cpShape *s) { if(s){ free(s->pv); free(s->pn); s->pv = s->pn = NULL; } }
+void cpConstraintDestroy(cpConstraint *c) { (void)c; }
+
+#define ORC_SHAPE_ALLOC(T) T *T##Alloc(void) { return (T *)calloc(1, sizeof(cpShape)); }
+#define ORC_JOINT_ALLOC(T) T *T##Alloc(void) { return (T *)calloc(1, sizeof(cpConstraint)); }
+ORC_SHAPE_ALLOC(cpCircleShape)
+ORC_SHAPE_ALLOC(cpSegmentShape)
+ORC_SHAPE_ALLOC(cpPolyShape)
+ORC_JOINT_ALLOC(cpPivotJoint)
+ORC_JOINT_ALLOC(cpPinJoint)
+ORC_JOINT_ALLOC(cpSlideJoint)
+ORC_JOINT_ALLOC(cpGrooveJoint)
+ORC_JOINT_ALLOC(cpDampedSpring)
+ORC_JOINT_ALLOC(cpDampedRotarySpring)
+ORC_JOINT_ALLOC(cpRotaryLimitJoint)
+ORC_JOINT_ALLOC(cpRatchetJoint)
+ORC_JOINT_ALLOC(cpGearJoint)
+ORC_JOINT_ALLOC(cpSimpleMotor)
+
+cpCircleShape *cpCircleShapeInit(cpCircleShape *m, cpBody *body, cpFloat radius, cpVect offset)
+{ return (cpCircleShape *)adopt_(m, cpCircleShapeNew(body, radius, offset), sizeof(cpShape)); }
+cpSegmentShape *cpSegmentShapeInit(cpSegmentShape *m, cpBody *body, cpVect a, cpVect b, cpFloat radius)
+{ return (cpSegmentShape *)adopt_(m, cpSegmentShapeNew(body, a, b, radius), sizeof(cpShape)); }
+cpPolyShape *cpPolyShapeInit(cpPolyShape *m, cpBody *body, int count, const cpVect *verts, cpTransform transform, cpFloat radius)
+{ return (cpPolyShape *)adopt_(m, cpPolyShapeNew(body, count, verts, transform, radius), sizeof(cpShape)); }
+cpPolyShape *cpPolyShapeInitRaw(cpPolyShape *m, cpBody *body, int count, const cpVect *verts, cpFloat radius)
+{ return (cpPolyShape *)adopt_(m, cpPolyShapeNewRaw(body, count, verts, radius), sizeof(cpShape)); }
+cpPolyShape *cpBoxShapeInit(cpPolyShape *m, cpBody *body, cpFloat width, cpFloat height, cpFloat radius)
+{ return (cpPolyShape *)adopt_(m, cpBoxShapeNew(body, width, height, radius), sizeof(cpShape)); }
+cpPolyShape *cpBoxShapeInit2(cpPolyShape *m, cpBody *body, cpBB box, cpFloat radius)
+{ return (cpPolyShape *)adopt_(m, cpBoxShapeNew2(body, box, radius), sizeof(cpShape)); }
+cpPivotJoint *cpPivotJointInit(cpPivotJoint *m, cpBody *a, cpBody *b, cpVect anchorA, cpVect anchorB)
+{ return (cpPivotJoint *)adopt_(m, cpPivotJointNew2(a, b, anchorA, anchorB), sizeof(cpConstraint)); }
+cpPinJoint *cpPinJointInit(cpPinJoint *m, cpBody *a, cpBody *b, cpVect anchorA, cpVect anchorB)
+{ return (cpPinJoint *)adopt_(m, cpPinJointNew(a, b, anchorA, anchorB), sizeof(cpConstraint)); }
+cpSlideJoint *cpSlideJointInit(cpSlideJoint *m, cpBody *a, cpBody *b, cpVect anchorA, cpVect anchorB, cpFloat min, cpFloat max)
+{ return (cpSlideJoint *)adopt_(m, cpSlideJointNew(a, b, anchorA, anchorB, min, max), sizeof(cpConstraint)); }
+cpGrooveJoint *cpGrooveJointInit(cpGrooveJoint *m, cpBody *a, cpBody *b, cpVect groove_a, cpVect groove_b, cpVect anchorB)
+{ return (cpGrooveJoint *)adopt_(m, cpGrooveJointNew(a, b, groove_a, groove_b, anchorB), sizeof(cpConstraint)); }
+cpDampedSpring *cpDampedSpringInit(cpDampedSpring *m, cpBody *a, cpBody *b, cpVect anchorA, cpVect anchorB,
+                                   cpFloat restLength, cpFloat stiffness, cpFloat damping)
+{ return (cpDampedSpring *)adopt_(m, cpDampedSpringNew(a, b, anchorA, anchorB, restLength, stiffness, damping), sizeof(cpConstraint)); }
+cpDampedRotarySpring *cpDampedRotarySpringInit(cpDampedRotarySpring *m, cpBody *a, cpBody *b, cpFloat restAngle,
+                                               cpFloat stiffness, cpFloat damping)
+{ return (cpDampedRotarySpring *)adopt_(m, cpDampedRotarySpringNew(a, b, restAngle, stiffness, damping), sizeof(cpConstraint)); }
+cpRotaryLimitJoint *cpRotaryLimitJointInit(cpRotaryLimitJoint *m, cpBody *a, cpBody *b, cpFloat min, cpFloat max)
+{ return (cpRotaryLimitJoint *)adopt_(m, cpRotaryLimitJointNew(a, b, min, max), sizeof(cpConstraint)); }
+cpRatchetJoint *cpRatchetJointInit(cpRatchetJoint *m, cpBody *a, cpBody *b, cpFloat phase, cpFloat ratchet)
+{ return (cpRatchetJoint *)adopt_(m, cpRatchetJointNew(a, b, phase, ratchet), sizeof(cpConstraint)); }
+cpGearJoint *cpGearJointInit(cpGearJoint *m, cpBody *a, cpBody *b, cpFloat phase, cpFloat ratio)
+{ return (cpGearJoint *)adopt_(m, cpGearJointNew(a, b, phase, ratio), sizeof(cpConstraint)); }
+cpSimpleMotor *cpSimpleMotorInit(cpSimpleMotor *m, cpBody *a, cpBody *b, cpFloat rate)
+{ return (cpSimpleMotor *)adopt_(m, cpSimpleMotorNew(a, b, rate), sizeof(cpConstraint)); }
+
+/* the threaded space's names on the serial space (the oracle's checked
+ * results are the serial solver's) */
+cpSpace *cpHastySpaceNew(void) { return cpSpaceNew(); }
+void cpHastySpaceFree(cpSpace *sp) { cpSpaceFree(sp); }
+void cpHastySpaceSetThreads(cpSpace *sp, unsigned long threads) { (void)sp; (void)threads; }
+unsigned long cpHastySpaceGetThreads(cpSpace *sp) { (void)sp; return 1ul; }
+void cpHastySpaceStep(cpSpace *sp, cpFloat dt) { cpSpaceStep(sp, dt); }

@@ -12,7 +12,7 @@ import numpy as np
 import pytest
 
 REPO = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
-SRC = os.path.join(REPO, "tests", "relink_program.c")
+PROGRAMS = ["relink_program.c", "relink_program2.c"]
 GPU_DIR = os.path.join(REPO, "chipmunk2d_gb300", "_build")
 ORACLE_DIR = os.path.join(REPO, "oracle", "_build")
 REF_DIR = os.path.join(REPO, "oracle", "_ref")
@@ -24,7 +24,7 @@ def reference_headers():
     return inc if os.path.exists(os.path.join(inc, "chipmunk", "chipmunk.h")) else None
 
 
-def build(tmp_path, name, libdir, lib, ref_headers=None):
+def build(tmp_path, name, libdir, lib, ref_headers=None, program="relink_program.c"):
     gcc = shutil.which("gcc")
     if gcc is None:
         pytest.skip("no C compiler")
@@ -34,20 +34,25 @@ def build(tmp_path, name, libdir, lib, ref_headers=None):
         cmd += ["-DRELINK_REFERENCE_HEADERS", "-I", ref_headers]
     else:
         cmd += ["-I", os.path.join(REPO, "include")]
-    cmd += [SRC, "-o", exe, "-L", libdir, "-l" + lib, "-Wl,-rpath," + libdir, "-lm"]
+    cmd += [os.path.join(REPO, "tests", program), "-o", exe, "-L", libdir, "-l" + lib, "-Wl,-rpath," + libdir, "-lm"]
     subprocess.check_call(cmd)
     return exe
 
 
 def run(exe):
+    """(row labels, values) of the program's output: one row per body and
+    per query result, the values printed as hexadecimal floats."""
     out = subprocess.run([exe], stdout=subprocess.PIPE, stderr=subprocess.PIPE, text=True, timeout=300, check=True).stdout
     rows = [ln.split() for ln in out.strip().splitlines()]
-    ids = [int(r[0]) for r in rows]
-    vals = np.array([[float.fromhex(x) for x in r[1:]] for r in rows])
+    ids = [r[0] for r in rows]
+    width = max(len(r) for r in rows)
+    vals = np.array([[float.fromhex(x) if x.startswith(("0x", "-0x")) else float(x) for x in r[1:]] + [0.0] * (width - len(r))
+                     for r in rows])
     return ids, vals
 
 
-def test_builds_against_the_reference_headers_and_links_the_gpu_library(tmp_path):
+@pytest.mark.parametrize("program", PROGRAMS)
+def test_builds_against_the_reference_headers_and_links_the_gpu_library(tmp_path, program):
     """Source and link compatibility: the program compiled with the
     reference's own headers links against libchipmunk_gb300.so."""
     inc = reference_headers()
@@ -55,29 +60,32 @@ def test_builds_against_the_reference_headers_and_links_the_gpu_library(tmp_path
         pytest.skip("reference headers not present on this machine")
     if not os.path.exists(os.path.join(GPU_DIR, "libchipmunk_gb300.so")):
         pytest.skip("libchipmunk_gb300.so not built")
-    build(tmp_path, "relink_ref_headers", GPU_DIR, "chipmunk_gb300", ref_headers=inc)
+    build(tmp_path, "relink_ref_headers", GPU_DIR, "chipmunk_gb300", ref_headers=inc, program=program)
 
 
-def test_oracle_matches_the_reference_on_the_program(tmp_path, oracle_lib):
+@pytest.mark.parametrize("program", PROGRAMS)
+def test_oracle_matches_the_reference_on_the_program(tmp_path, oracle_lib, program):
     """The same program on the reference library and on the oracle: bit for
-    bit, through removals and additions mid-run."""
+    bit, through removals and additions mid-run, caller-placed objects,
+    every joint kind and the queries."""
     if not os.path.exists(os.path.join(REF_DIR, "libcpref.so")):
         pytest.skip("reference library not built on this machine")
-    ids_r, ref = run(build(tmp_path, "relink_ref", REF_DIR, "cpref"))
-    ids_o, orc = run(build(tmp_path, "relink_oracle", ORACLE_DIR, "oracle"))
-    assert ids_r == ids_o and len(ids_r) > 30
+    ids_r, ref = run(build(tmp_path, "relink_ref", REF_DIR, "cpref", program=program))
+    ids_o, orc = run(build(tmp_path, "relink_oracle", ORACLE_DIR, "oracle", program=program))
+    assert ids_r == ids_o and len(ids_r) > 20
     np.testing.assert_array_equal(orc, ref)
 
 
 @pytest.mark.gpu
-def test_gpu_library_runs_the_program_like_the_oracle(tmp_path, oracle_lib):
+@pytest.mark.parametrize("program", PROGRAMS)
+def test_gpu_library_runs_the_program_like_the_oracle(tmp_path, oracle_lib, program):
     """The program linked against libchipmunk_gb300.so runs on the GPU and
     ends where the oracle does.  Two free runs (no state copied between
     them): the last-bit differences of sin/cos compound over the 180 steps,
     so positions and velocities are held to 1e-9 of their magnitude, as in
     the free-run pyramid test."""
-    ids_o, orc = run(build(tmp_path, "relink_oracle", ORACLE_DIR, "oracle"))
-    ids_g, gpu = run(build(tmp_path, "relink_gpu", GPU_DIR, "chipmunk_gb300"))
+    ids_o, orc = run(build(tmp_path, "relink_oracle", ORACLE_DIR, "oracle", program=program))
+    ids_g, gpu = run(build(tmp_path, "relink_gpu", GPU_DIR, "chipmunk_gb300", program=program))
     assert ids_g == ids_o
     scale = np.maximum(np.abs(orc).max(axis=0), 1.0)
     err = float((np.abs(gpu - orc) / scale).max())
