@@ -1883,8 +1883,7 @@ extern __shared__ double sbody[];
 /* Warm start (pass 0) and `iterations` sweeps, level by level; one block
  * per world.  Worlds of at most `stagedMax` bodies keep their packed body
  * state in shared memory for the whole solve. */
-template <bool PREFETCH>
-__global__ void __launch_bounds__(256, PREFETCH ? 1 : 2) k_solve(cpgSet s, int stagedMax)
+__global__ void __launch_bounds__(256, 2) k_solve(cpgSet s, int stagedMax)
 {
 	/* largest worlds first: their long level chains start at once */
 	int w = s.worldOrder[blockIdx.x];
@@ -1916,14 +1915,6 @@ __global__ void __launch_bounds__(256, PREFETCH ? 1 : 2) k_solve(cpgSet s, int s
 	int nt = blockDim.x;
 	bool many = s.solveLayout == 1 || (s.solveLayout == 0 && s.nworlds >= 152);
 	bool recording = (s.tape.on && s.tape.app) || s.solveLayout == 3;
-	/* PREFETCH (sets of one world, whose solve is a chain of levels): a
-	 * quad's first row of the next four-lane level is read before the
-	 * level's barrier, so that the row's L2 latency overlaps the wait;
-	 * rows are written only by the quad that applies them, and with one
-	 * level the quad re-reads its own row after __syncwarp.  Many-world
-	 * sets keep the registers. */
-	QuadRow qn;
-	int kn = -1;
 	for(int pass = 0; pass <= P.iterations; pass++){
 		for(int l = 0; l < nlev; l++){
 			int b0 = start[l], e = start[l + 1];
@@ -1932,8 +1923,7 @@ __global__ void __launch_bounds__(256, PREFETCH ? 1 : 2) k_solve(cpgSet s, int s
 			if(lay == 0){
 				for(int k = b0 + (threadIdx.x >> 2); k < e; k += nq){
 					QuadRow q;
-					if(PREFETCH && k == kn) q = qn;
-					else quad_load(q, rows[k], lane4);
+					quad_load(q, rows[k], lane4);
 					AdjApp *rec = (tapeApp && pass > 0) ? tapeApp + ((size_t)k*P.iterations + (pass - 1))*2 : nullptr;
 					if(q.kind == 0) quad_apply<false, false>(q, rows + k, bodies, pass, P.dt_coef, qmask, lane4, rec);
 					else if(lane4 == 0){
@@ -1951,18 +1941,6 @@ __global__ void __launch_bounds__(256, PREFETCH ? 1 : 2) k_solve(cpgSet s, int s
 				}
 			} else {
 				for(int k = b0 + threadIdx.x; k < e; k += nt) solve_row<false>(rows, k, bodies, pass, P.dt_coef, P.dt);
-			}
-			int nl = l + 1, npass = pass;
-			if(nl == nlev){ nl = 0; npass++; }
-			kn = -1;
-			if(PREFETCH && npass <= P.iterations){
-				int nb0 = start[nl], ne = start[nl + 1];
-				int k2 = nb0 + (threadIdx.x >> 2);
-				if(k2 < ne && (recording || level_layout(ne - nb0, nt, many) == 0)){
-					__syncwarp(qmask);
-					quad_load(qn, rows[k2], lane4);
-					kn = k2;
-				}
 			}
 			__syncthreads();
 		}
@@ -3171,15 +3149,13 @@ extern "C" int cpg_launch_step(const cpgSet *s, const cpgSet *h, int mode, void 
 		size_t smem = (size_t)stagedMax*8*sizeof(double);
 		static size_t smemSet = 0;
 		if(smem > 48*1024 && smem > smemSet){
-			cudaFuncSetAttribute(k_solve<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-			cudaFuncSetAttribute(k_solve<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+			cudaFuncSetAttribute(k_solve, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
 			smemSet = smem;
 		}
 		/* many worlds: small blocks keep more worlds resident (registers
 		 * limit a 256-thread block to two per SM); one world: wide levels */
 		int threads = h->hostSolveThreads > 0 ? h->hostSolveThreads : (W >= 152 ? 128 : 256);
-		if(W == 1) LAUNCH(k_solve<true><<<W, threads, smem, st>>>(*s, stagedMax));
-		else LAUNCH(k_solve<false><<<W, threads, smem, st>>>(*s, stagedMax));
+		LAUNCH(k_solve<<<W, threads, smem, st>>>(*s, stagedMax));
 	}
 	LAUNCH(k_writeback<<<dim3(perWorldX, W), 128, 0, st>>>(*s));
 	LAUNCH(k_unpack_bodies<<<blocks_for(h->totalBodies, 128), 128, 0, st>>>(*s));
