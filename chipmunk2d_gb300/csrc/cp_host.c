@@ -203,10 +203,14 @@ struct cpSpace {
 	double jointDt;                         /* dt the joint bias terms were made for */
 	unsigned long long editGen;             /* counts object edits through the setters */
 	unsigned long hastyThreads;             /* cpHastySpaceSetThreads */
+	struct PostStep *post; int npost, cappost, postRunning;   /* cpSpaceAddPostStepCallback */
 
 	cpArbiter *snap; int nsnap, capsnap; int snapValid;
 	float phaseMs[8];
 };
+
+static void run_post_step_(cpSpace *sp);
+static cpShape *slot_shape_(cpSpace *sp, int slot);
 
 static void push_(void ***arr, int *n, int *cap, void *p)
 {
@@ -1221,6 +1225,7 @@ void cpSpaceStep(cpSpace *sp, cpFloat dt)
 	if(!space_device_ready_(sp)) return;
 	double dts[1] = { dt };
 	devset_step(sp->dev, dts, NULL);
+	run_post_step_(sp);
 }
 
 static inline const cpBody *rd(const cpBody *b);
@@ -1414,7 +1419,7 @@ void cpSpacePointQuery(cpSpace *sp, cpVect point, cpFloat maxDistance, cpShapeFi
 		cpShape *shape = slot_shape_(sp, h[k].shape);
 		if(shape && func) func(shape, cpv(h[k].px, h[k].py), h[k].d, cpv(h[k].gx, h[k].gy), data);
 	}
-	free(h); free(c);
+	free(h); free(c);	run_post_step_(sp);
 }
 
 cpShape *cpSpacePointQueryNearest(cpSpace *sp, cpVect point, cpFloat maxDistance, cpShapeFilter filter, cpPointQueryInfo *out)
@@ -1443,7 +1448,7 @@ void cpSpaceSegmentQuery(cpSpace *sp, cpVect start, cpVect end, cpFloat radius, 
 		cpShape *shape = slot_shape_(sp, h[k].shape);
 		if(shape && func) func(shape, cpv(h[k].px, h[k].py), cpv(h[k].gx, h[k].gy), h[k].d, data);
 	}
-	free(h); free(c);
+	free(h); free(c);	run_post_step_(sp);
 }
 
 cpShape *cpSpaceSegmentQueryFirst(cpSpace *sp, cpVect start, cpVect end, cpFloat radius, cpShapeFilter filter, cpSegmentQueryInfo *out)
@@ -1472,7 +1477,7 @@ void cpSpaceBBQuery(cpSpace *sp, cpBB bb, cpShapeFilter filter, cpSpaceBBQueryFu
 		cpShape *shape = slot_shape_(sp, h[k].shape);
 		if(shape && func) func(shape, data);
 	}
-	free(h); free(c);
+	free(h); free(c);	run_post_step_(sp);
 }
 
 /* The slot of a shape in its space, or -1 (error set) when it is in none. */
@@ -1637,6 +1642,7 @@ cpBool cpSpaceShapeQuery(cpSpace *sp, cpShape *shape, cpSpaceShapeQueryFunc func
 	}
 	any = counts[1] ? cpTrue : cpFalse;
 	free(hits);
+	run_post_step_(sp);
 	return any;
 }
 
@@ -3215,8 +3221,8 @@ void cpSpaceDestroy(cpSpace *sp)
 	for(int i = 0; i < sp->nstat; i++) if(sp->stat[i]->space == sp) sp->stat[i]->space = NULL;
 	for(int i = 0; i < sp->nshapes; i++) if(sp->shapes[i] && sp->shapes[i]->space == sp) sp->shapes[i]->space = NULL;
 	for(int i = 0; i < sp->ncons; i++) if(sp->cons[i]->space == sp) sp->cons[i]->space = NULL;
-	free(sp->dyn); free(sp->stat); free(sp->shapes); free(sp->cons); free(sp->ops); free(sp->snap);
-	sp->dyn = NULL; sp->stat = NULL; sp->shapes = NULL; sp->cons = NULL; sp->ops = NULL; sp->snap = NULL;
+	free(sp->dyn); free(sp->stat); free(sp->shapes); free(sp->cons); free(sp->ops); free(sp->snap); free(sp->post);
+	sp->dyn = NULL; sp->stat = NULL; sp->shapes = NULL; sp->cons = NULL; sp->ops = NULL; sp->snap = NULL; sp->post = NULL;
 	sp->dev = NULL;
 }
 
@@ -3519,16 +3525,91 @@ void cpSpaceEachBody(cpSpace *sp, cpSpaceBodyIteratorFunc func, void *data)
 {
 	for(int i = 0; i < sp->ndyn; i++) func(sp->dyn[i], data);
 	for(int i = 0; i < sp->nstat; i++) func(sp->stat[i], data);
+	run_post_step_(sp);
 }
 
+/* cpSpace.c:621-629: the dynamic then the static index's leaves, each in
+ * its leaf hash set's order (bins, then each bin's chain: cpHashSet.c),
+ * which the device sets keep as the reference's do. */
 void cpSpaceEachShape(cpSpace *sp, cpSpaceShapeIteratorFunc func, void *data)
 {
+	if(!sp) return;
+	if(sp->nshapes > 0 && !(sp->dev && !sp->ownsDev && (sp->structDirty || space_structure_changed(sp))) &&
+	   (sp->dev && !sp->ownsDev ? 1 : space_device_ready_(sp))){
+		DevSet *ds = sp->dev;
+		const cpgWorld *W = &ds->hworld[sp->world];
+		cpgTree T;
+		int nn = W->nodeCap;
+		int *bins = HALLOC(int, (size_t)W->dbinCap + (size_t)W->sbinCap);
+		cpgNode *nodes = HALLOC(cpgNode, nn);
+		int ok = d2h(&T, ds->d.tree + sp->world, sizeof(cpgTree));
+		ok &= d2h(bins, ds->d.dbins + W->dbinOff, sizeof(int)*(size_t)W->dbinCap);
+		ok &= d2h(bins + W->dbinCap, ds->d.sbins + W->sbinOff, sizeof(int)*(size_t)W->sbinCap);
+		ok &= d2h(nodes, ds->d.nodes + W->nodeOff, sizeof(cpgNode)*(size_t)nn);
+		ok &= cuda_ok(cudaStreamSynchronize(lib_stream()), "shape iteration");
+		if(ok){
+			int nshapes = sp->nshapes;
+			cpShape **order = HALLOC(cpShape *, nshapes);
+			int n = 0;
+			for(int set = 0; set < 2; set++){
+				const int *b = set ? bins + W->dbinCap : bins;
+				unsigned size = set ? T.statSize : T.dynSize;
+				int cap = set ? W->sbinCap : W->dbinCap;
+				for(unsigned i = 0; i < size && (int)i < cap; i++){
+					int guard = 0;
+					for(int k = b[i]; k >= 0 && k < nn && guard <= nn; k = nodes[k].binNext, guard++){
+						cpShape *shape = slot_shape_(sp, nodes[k].obj);
+						if(shape && n < nshapes) order[n++] = shape;
+					}
+				}
+			}
+			/* callbacks may edit the space: iterate a copy */
+			for(int i = 0; i < n; i++) func(order[i], data);
+			free(order);
+			free(bins); free(nodes);
+			run_post_step_(sp);
+			return;
+		}
+		free(bins); free(nodes);
+	}
 	for(int i = 0; i < sp->nshapes; i++) if(sp->shapes[i]) func(sp->shapes[i], data);
+	run_post_step_(sp);
 }
 
 void cpSpaceEachConstraint(cpSpace *sp, cpSpaceConstraintIteratorFunc func, void *data)
 {
 	for(int i = 0; i < sp->ncons; i++) func(sp->cons[i], data);
+	run_post_step_(sp);
+}
+
+/* cpSpaceStep.c:26-58, 84-103: post-step callbacks, one per key, run in
+ * the order added when the step (or an iteration or query) ends; a
+ * callback added by one of them runs in the same round. */
+typedef struct PostStep { cpPostStepFunc func; void *key, *data; } PostStep;
+
+cpBool cpSpaceAddPostStepCallback(cpSpace *sp, cpPostStepFunc func, void *key, void *data)
+{
+	for(int i = 0; i < sp->npost; i++) if(sp->post[i].key == key) return cpFalse;
+	if(sp->npost == sp->cappost){
+		sp->cappost = sp->cappost ? 2*sp->cappost : 8;
+		sp->post = (PostStep *)realloc(sp->post, sizeof(PostStep)*(size_t)sp->cappost);
+	}
+	PostStep *cb = &sp->post[sp->npost++];
+	cb->func = func; cb->key = key; cb->data = data;
+	return cpTrue;
+}
+
+static void run_post_step_(cpSpace *sp)
+{
+	if(!sp || sp->postRunning || sp->npost == 0) return;
+	sp->postRunning = 1;
+	for(int i = 0; i < sp->npost; i++){
+		PostStep cb = sp->post[i];
+		sp->post[i].func = NULL;
+		if(cb.func) cb.func(sp, cb.key, cb.data);
+	}
+	sp->npost = 0;
+	sp->postRunning = 0;
 }
 
 /* ====================================================================

@@ -2840,15 +2840,34 @@ __global__ void __launch_bounds__(CPG_COOP_SOLVE_THREADS, 1) k_solve_coop(cpgSet
 	 * each with ~1.3x the instructions */
 	int pair = (threadIdx.x >> 1)*gridDim.x + blockIdx.x, np2 = (gridDim.x*blockDim.x) >> 1;
 	bool bias = (threadIdx.x & 1) != 0;
+	/* exact order: a level of at most two rounds of one block's quads runs
+	 * on block 0 alone, and a run of such levels needs a grid barrier only
+	 * after its last level (a block barrier between its levels).  A level's
+	 * units share no body, so which quads apply them changes no result. */
+	const int narrowMax = FUSED ? 0 : 2*(blockDim.x >> 2);
 	QuadRow q;
 	int k = start[0] + quad;
 	bool two = coop_two_lanes<FUSED>(start[1] - start[0], gridDim.x);
-	bool have = !two && k < start[1];
+	bool have = !two && k < start[1] && (FUSED || (start[1] - start[0]) > narrowMax);
 	if(have) quad_load(q, rows[k], lane4);
 	for(int pass = pass0; pass <= iters; pass++){
 		for(int l = 0; l < nlev; l++){
 			int e = start[l + 1];
-			if(two){
+			bool narrow = !FUSED && (e - start[l]) <= narrowMax;
+			if(narrow){
+				if(blockIdx.x == 0){
+					for(int k2 = start[l] + (threadIdx.x >> 2); __any_sync(0xffffffffu, k2 < e); k2 += blockDim.x >> 2){
+						bool has = k2 < e;
+						QuadRow qq;
+						if(has) quad_load(qq, rows[k2], lane4);
+						if(has){
+							if(qq.kind == 0) quad_apply<true, FUSED>(qq, rows + k2, bodies, pass, dt_coef, qmask, lane4);
+							else if(lane4 == 0) solve_row<true>(rows, k2, bodies, pass, dt_coef, dt);
+						}
+					}
+					__syncthreads();
+				}
+			} else if(two){
 				for(int k2 = start[l] + pair; __any_sync(0xffffffffu, k2 < e); k2 += np2){
 					bool has = k2 < e;
 					PairRow pr;
@@ -2875,9 +2894,11 @@ __global__ void __launch_bounds__(CPG_COOP_SOLVE_THREADS, 1) k_solve_coop(cpgSet
 			}
 			int nl = l + 1, npass = pass;
 			if(nl == nlev){ nl = 0; npass++; }
+			bool nextNarrow = !FUSED && npass <= iters && (start[nl + 1] - start[nl]) <= narrowMax;
+			if(narrow && nextNarrow) continue;
 			k = start[nl] + quad;
 			two = coop_two_lanes<FUSED>(start[nl + 1] - start[nl], gridDim.x);
-			have = !two && npass <= iters && k < start[nl + 1];
+			have = !two && !nextNarrow && npass <= iters && k < start[nl + 1];
 			if(flow){
 				/* the warp synchronised after its last unit, so a row this
 				 * quad just wrote (a single level) reads back current */

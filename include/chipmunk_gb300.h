@@ -146,6 +146,7 @@ typedef void (*cpSpacePointQueryFunc)(cpShape *shape, cpVect point, cpFloat dist
 typedef void (*cpSpaceSegmentQueryFunc)(cpShape *shape, cpVect point, cpVect normal, cpFloat alpha, void *data);
 typedef void (*cpSpaceBBQueryFunc)(cpShape *shape, void *data);
 typedef void (*cpSpaceShapeQueryFunc)(cpShape *shape, cpContactPointSet *points, void *data);
+typedef void (*cpPostStepFunc)(cpSpace *space, void *key, void *data);               /* cpSpace.h:182 */
 
 /* cpConstraint.h:25-29 */
 typedef void (*cpConstraintPreSolveFunc)(cpConstraint *constraint, cpSpace *space);
@@ -258,6 +259,10 @@ void cpSpaceEachBody(cpSpace *space, cpSpaceBodyIteratorFunc func, void *data); 
 void cpSpaceEachShape(cpSpace *space, cpSpaceShapeIteratorFunc func, void *data);           /* cpSpace.h:231 */
 void cpSpaceEachConstraint(cpSpace *space, cpSpaceConstraintIteratorFunc func, void *data); /* cpSpace.h:236 */
 void cpSpaceStep(cpSpace *space, cpFloat dt);                        /* cpSpace.h:255 */
+/* A callback run once when the current (or next) step, body/shape/
+ * constraint iteration or point/segment/box/shape query ends, one per key;
+ * returns cpFalse when the key is already registered. */
+cpBool cpSpaceAddPostStepCallback(cpSpace *space, cpPostStepFunc func, void *key, void *data);     /* cpSpace.h:187 */
 /* Caller-placed objects (cpSpace.h:80-88, cpBody.h:49-58, cpShape.h:78-84,
  * 161-197, cpPolyShape.h:26-40, cpConstraint.h:61, the joints' headers):
  * cp*Alloc returns zeroed memory of the object's size, cp*Init

@@ -236,7 +236,10 @@ struct cpSpace {
 
 	cpBody staticBody;
 	struct Hasty *hasty;                   /* the threaded solver (cpx_space_set_hasty), or NULL */
+	struct PostStep *post; int npost, cappost, postRunning;   /* post-step callbacks */
 };
+
+static void run_post_step_(cpSpace *sp);
 
 /* ========================================================================
  * Creation-time math: src/chipmunk.c:63-171, 250-274
@@ -2300,6 +2303,7 @@ void cpSpaceDestroy(cpSpace *sp)
 	sp->dynTree.leaves.bins = sp->statTree.leaves.bins = NULL;
 	sp->arbs = NULL; sp->freeList = NULL; sp->amap.keys = NULL; sp->amap.slot = NULL; sp->active = NULL;
 	sp->candPairs = NULL;
+	free(sp->post); sp->post = NULL; sp->npost = sp->cappost = 0;
 }
 
 void cpSpaceFree(cpSpace *sp)
@@ -2509,6 +2513,7 @@ void cpSpaceEachBody(cpSpace *sp, cpSpaceBodyIteratorFunc func, void *data)
 {
 	for(int i = 0; i < sp->ndyn; i++) func(sp->dyn[i], data);
 	for(int i = 0; i < sp->nstat; i++) func(sp->stat[i], data);
+	run_post_step_(sp);
 }
 
 static void each_leaf(cpSpace *sp, LeafSet *set, cpSpaceShapeIteratorFunc func, void *data)
@@ -2522,11 +2527,13 @@ void cpSpaceEachShape(cpSpace *sp, cpSpaceShapeIteratorFunc func, void *data)
 {
 	each_leaf(sp, &sp->dynTree.leaves, func, data);
 	each_leaf(sp, &sp->statTree.leaves, func, data);
+	run_post_step_(sp);
 }
 
 void cpSpaceEachConstraint(cpSpace *sp, cpSpaceConstraintIteratorFunc func, void *data)
 {
 	for(int i = 0; i < sp->ncons; i++) func(sp->cons[i], data);
+	run_post_step_(sp);
 }
 
 /* cpShape filter test: chipmunk_private.h:144-155 */
@@ -2799,6 +2806,7 @@ void cpSpaceStep(cpSpace *sp, cpFloat dt)
 		if(c->postSolve) c->postSolve(c, sp);
 	}
 	sp->locked--;
+	run_post_step_(sp);
 }
 
 /* ========================================================================
@@ -3271,6 +3279,7 @@ void cpSpacePointQuery(cpSpace *sp, cpVect point, cpFloat maxDistance, cpShapeFi
 	q.bb = cpBBNewForCircle(point, fmax_(maxDistance, 0.0));
 	tree_query_(sp, &sp->dynTree, &q);
 	tree_query_(sp, &sp->statTree, &q);
+	run_post_step_(sp);
 }
 
 /* cpSpaceQuery.c:76-98 */
@@ -3293,6 +3302,7 @@ void cpSpaceSegmentQuery(cpSpace *sp, cpVect start, cpVect end, cpFloat radius, 
 	q.kind = 2; q.a = start; q.b = end; q.r = radius; q.filter = filter; q.func = (void *)func; q.data = data;
 	tree_segment_query_(sp, &sp->statTree, &q, 1.0);
 	tree_segment_query_(sp, &sp->dynTree, &q, 1.0);
+	run_post_step_(sp);
 }
 
 /* cpSpaceQuery.c:154-175 */
@@ -3314,6 +3324,7 @@ void cpSpaceBBQuery(cpSpace *sp, cpBB bb, cpShapeFilter filter, cpSpaceBBQueryFu
 	q.kind = 4; q.bb = bb; q.filter = filter; q.func = (void *)func; q.data = data;
 	tree_query_(sp, &sp->dynTree, &q);
 	tree_query_(sp, &sp->statTree, &q);
+	run_post_step_(sp);
 }
 
 
@@ -3365,6 +3376,7 @@ cpBool cpSpaceShapeQuery(cpSpace *sp, cpShape *shape, cpSpaceShapeQueryFunc func
 	ShapeQueryCtx q = {shape, func, data, cpFalse};
 	if(sp->dynTree.root >= 0) subtree_shape_query_(sp, sp->dynTree.root, bb, &q);
 	if(sp->statTree.root >= 0) subtree_shape_query_(sp, sp->statTree.root, bb, &q);
+	run_post_step_(sp);
 	return q.anyCollision;
 }
 
@@ -3446,3 +3458,33 @@ void cpHastySpaceFree(cpSpace *sp) { cpSpaceFree(sp); }
 void cpHastySpaceSetThreads(cpSpace *sp, unsigned long threads) { (void)sp; (void)threads; }
 unsigned long cpHastySpaceGetThreads(cpSpace *sp) { (void)sp; return 1ul; }
 void cpHastySpaceStep(cpSpace *sp, cpFloat dt) { cpSpaceStep(sp, dt); }
+
+
+/* cpSpaceStep.c:26-58 (cpSpaceAddPostStepCallback), 84-103 (run when the
+ * space unlocks after a step, an iteration or a query) */
+typedef struct PostStep { cpPostStepFunc func; void *key, *data; } PostStep;
+
+cpBool cpSpaceAddPostStepCallback(cpSpace *sp, cpPostStepFunc func, void *key, void *data)
+{
+	for(int i = 0; i < sp->npost; i++) if(sp->post[i].key == key) return cpFalse;
+	if(sp->npost == sp->cappost){
+		sp->cappost = sp->cappost ? 2*sp->cappost : 8;
+		sp->post = (PostStep *)realloc(sp->post, sizeof(PostStep)*(size_t)sp->cappost);
+	}
+	PostStep *cb = &sp->post[sp->npost++];
+	cb->func = func; cb->key = key; cb->data = data;
+	return cpTrue;
+}
+
+static void run_post_step_(cpSpace *sp)
+{
+	if(!sp || sp->postRunning || sp->npost == 0) return;
+	sp->postRunning = 1;
+	for(int i = 0; i < sp->npost; i++){
+		PostStep cb = sp->post[i];
+		sp->post[i].func = NULL;
+		if(cb.func) cb.func(sp, cb.key, cb.data);
+	}
+	sp->npost = 0;
+	sp->postRunning = 0;
+}

@@ -2,9 +2,10 @@
  * relink_program2.c -- an ordinary Chipmunk2D program (reference public API
  * only) that places its objects in memory it asks the library for
  * (cp*Alloc / cp*Init / cp*Destroy), uses the threaded space's entry
- * points (cpHastySpace.h), every joint kind, and the space and shape
- * queries, then prints every body's state and the queries' results as
- * hexadecimal floats.  Built like relink_program.c.
+ * points (cpHastySpace.h), every joint kind, the space queries, a
+ * post-step callback that removes a body, and the shape iteration order,
+ * then prints every body's state and the queries' results as hexadecimal
+ * floats.  Built like relink_program.c.
  */
 #include <stdio.h>
 #include <stdlib.h>
@@ -16,6 +17,25 @@
 #endif
 
 #define NB 24
+
+static cpBody *bodies[NB];
+static cpShape *shapes[NB];
+
+/* a post-step callback that takes a body and its shape out of the space */
+static void remove_later(cpSpace *space, void *key, void *data)
+{
+	int i = (int)(size_t)data;
+	(void)key;
+	cpSpaceRemoveShape(space, shapes[i]); cpShapeDestroy(shapes[i]); free(shapes[i]);
+	cpSpaceRemoveBody(space, bodies[i]); cpBodyDestroy(bodies[i]); free(bodies[i]);
+	bodies[i] = NULL; shapes[i] = NULL;
+}
+
+static void print_shape(cpShape *shape, void *data)
+{
+	(void)data;
+	printf(" %d", (int)(size_t)cpShapeGetUserData(shape));
+}
 
 static void print_nearest(cpSpace *space, cpVect p)
 {
@@ -43,8 +63,6 @@ int main(void)
 	cpShapeSetFriction(ground, 1.0);
 	cpSpaceAddShape(space, ground);
 
-	cpBody *bodies[NB];
-	cpShape *shapes[NB];
 	for(int i = 0; i < NB; i++){
 		cpBody *b = cpBodyInit(cpBodyAlloc(), 1.0 + 0.1*i, 1.0);
 		cpShape *s;
@@ -61,6 +79,7 @@ int main(void)
 		}
 		cpBodySetPosition(b, cpv(-120.0 + 22.0*(i % 12), 20.0 + 30.0*(i/12)));
 		cpShapeSetFriction(s, 0.6);
+		cpShapeSetUserData(s, (cpDataPointer)(size_t)(i + 1));
 		cpSpaceAddBody(space, b);
 		cpSpaceAddShape(space, s);
 		bodies[i] = b; shapes[i] = s;
@@ -84,9 +103,19 @@ int main(void)
 			print_nearest(space, cpv(-100.0, 10.0));
 			print_ray(space, cpv(-200.0, 15.0), cpv(200.0, 15.0));
 		}
+		if(step == 100){
+			/* runs when the next step ends; a second callback on the same key is refused */
+			cpBool first = cpSpaceAddPostStepCallback(space, remove_later, bodies + 21, (void *)(size_t)21);
+			cpBool again = cpSpaceAddPostStepCallback(space, remove_later, bodies + 21, (void *)(size_t)21);
+			printf("poststep %d %d\n", (int)first, (int)again);
+		}
 	}
+	printf("order");
+	cpSpaceEachShape(space, print_shape, NULL);
+	printf("\n");
 	printf("threads %lu\n", cpHastySpaceGetThreads(space) > 0 ? 1ul : 0ul);
 	for(int i = 0; i < NB; i++){
+		if(!bodies[i]) continue;
 		cpVect p = cpBodyGetPosition(bodies[i]), v = cpBodyGetVelocity(bodies[i]);
 		printf("%d %a %a %a %a %a %a\n", i, p.x, p.y, v.x, v.y, cpBodyGetAngle(bodies[i]), cpBodyGetAngularVelocity(bodies[i]));
 	}
@@ -95,6 +124,7 @@ int main(void)
 
 	for(int k = 0; k < 10; k++){ cpSpaceRemoveConstraint(space, joints[k]); cpConstraintDestroy(joints[k]); free(joints[k]); }
 	for(int i = 0; i < NB; i++){
+		if(!bodies[i]) continue;
 		cpSpaceRemoveShape(space, shapes[i]); cpShapeDestroy(shapes[i]); free(shapes[i]);
 		cpSpaceRemoveBody(space, bodies[i]); cpBodyDestroy(bodies[i]); free(bodies[i]);
 	}

@@ -44,6 +44,8 @@ def run(exe):
     per query result, the values printed as hexadecimal floats."""
     out = subprocess.run([exe], stdout=subprocess.PIPE, stderr=subprocess.PIPE, text=True, timeout=300, check=True).stdout
     rows = [ln.split() for ln in out.strip().splitlines()]
+    # the shape iteration order must agree exactly: it goes into the labels
+    rows = [[" ".join(r)] if r[0] in ("order", "poststep") else r for r in rows]
     ids = [r[0] for r in rows]
     width = max(len(r) for r in rows)
     vals = np.array([[float.fromhex(x) if x.startswith(("0x", "-0x")) else float(x) for x in r[1:]] + [0.0] * (width - len(r))
