@@ -2840,11 +2840,14 @@ __global__ void __launch_bounds__(CPG_COOP_SOLVE_THREADS, 1) k_solve_coop(cpgSet
 	 * each with ~1.3x the instructions */
 	int pair = (threadIdx.x >> 1)*gridDim.x + blockIdx.x, np2 = (gridDim.x*blockDim.x) >> 1;
 	bool bias = (threadIdx.x & 1) != 0;
-	/* exact order: a level of at most two rounds of one block's quads runs
-	 * on block 0 alone, and a run of such levels needs a grid barrier only
-	 * after its last level (a block barrier between its levels).  A level's
-	 * units share no body, so which quads apply them changes no result. */
-	const int narrowMax = FUSED ? 0 : 2*(blockDim.x >> 2);
+	/* exact order: a level no wider than one block's quads runs on block 0
+	 * alone, and a run of such levels needs a grid barrier only after its
+	 * last level (a block barrier between its levels, the next level's row
+	 * read before it).  A level's units share no body, so which quads
+	 * apply them changes no result. */
+	const int narrowMax = FUSED ? 0 : (blockDim.x >> 2);
+	QuadRow qn;
+	bool haveN = false;
 	QuadRow q;
 	int k = start[0] + quad;
 	bool two = coop_two_lanes<FUSED>(start[1] - start[0], gridDim.x);
@@ -2856,15 +2859,20 @@ __global__ void __launch_bounds__(CPG_COOP_SOLVE_THREADS, 1) k_solve_coop(cpgSet
 			bool narrow = !FUSED && (e - start[l]) <= narrowMax;
 			if(narrow){
 				if(blockIdx.x == 0){
-					for(int k2 = start[l] + (threadIdx.x >> 2); __any_sync(0xffffffffu, k2 < e); k2 += blockDim.x >> 2){
-						bool has = k2 < e;
-						QuadRow qq;
-						if(has) quad_load(qq, rows[k2], lane4);
-						if(has){
-							if(qq.kind == 0) quad_apply<true, FUSED>(qq, rows + k2, bodies, pass, dt_coef, qmask, lane4);
-							else if(lane4 == 0) solve_row<true>(rows, k2, bodies, pass, dt_coef, dt);
-						}
+					int k2 = start[l] + (threadIdx.x >> 2);
+					if(k2 < e){
+						if(!haveN) quad_load(qn, rows[k2], lane4);
+						if(qn.kind == 0) quad_apply<true, FUSED>(qn, rows + k2, bodies, pass, dt_coef, qmask, lane4);
+						else if(lane4 == 0) solve_row<true>(rows, k2, bodies, pass, dt_coef, dt);
 					}
+					/* the next narrow level's row, before the block barrier
+					 * (a single level re-reads the row this quad wrote) */
+					int nl2 = l + 1, np2 = pass;
+					if(nl2 == nlev){ nl2 = 0; np2++; }
+					int kq = start[nl2] + (threadIdx.x >> 2);
+					haveN = np2 <= iters && (start[nl2 + 1] - start[nl2]) <= narrowMax && kq < start[nl2 + 1];
+					__syncwarp(qmask);
+					if(haveN) quad_load(qn, rows[kq], lane4);
 					__syncthreads();
 				}
 			} else if(two){
