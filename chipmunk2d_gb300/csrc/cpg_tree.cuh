@@ -438,9 +438,14 @@ __device__ int subtree_insert(TreeCtx &c, int root, int leaf)
 		}
 		int child = goB ? nd.B : nd.A;
 		NodeRec rc = goB ? rb : ra;
-		BB m; FBox fm;
-		bmerge(nd.bb, nd.f, lbb, lf, m, fm);
-		if(!same_box_bits(m, nd.bb)) set_node_box(c.nodes[cur], m, fm);
+		/* a box whose brackets already hold the leaf's strictly inside is
+		 * its own merge with the leaf: nothing to compute or store */
+		bool inside = nd.f.lhi < lf.llo && nd.f.bhi < lf.blo && nd.f.rlo > lf.rhi && nd.f.tlo > lf.thi;
+		if(!inside){
+			BB m; FBox fm;
+			bmerge(nd.bb, nd.f, lbb, lf, m, fm);
+			if(!same_box_bits(m, nd.bb)) set_node_box(c.nodes[cur], m, fm);
+		}
 		if(rc.obj >= 0){
 			int nn = node_new_bb(c, leaf, lbb, lf, child, rc.bb, rc.f);
 			if(nn < 0) return root;
