@@ -3400,12 +3400,60 @@ static void record_op_(cpSpace *sp, int kind, cpShape *s, int isStatic)
 	op->shape = (int)s->hashid;
 	op->isStatic = isStatic;
 	op->kind = kind;
-	if(kind == CPG_OP_INSERT){
+	if(kind == CPG_OP_INSERT || kind == CPG_OP_REINDEX){
 		/* the box as cached now and the body's velocity now: the leaf's
 		 * fattened box is made at this call (cpBBTree.c:82-98, 605-616) */
 		op->l = s->bb.l; op->b = s->bb.b; op->r = s->bb.r; op->t = s->bb.t;
 		op->vx = s->body->v.x; op->vy = s->body->v.y;
 	}
+}
+
+/* cpSpace.c:662-678: the shape's cache brought to its body's transform,
+ * then its leaf re-indexed (cpBBTreeReindexObject, replayed on the device
+ * before the next step or query with the box and velocity of this call). */
+void cpSpaceReindexShape(cpSpace *sp, cpShape *s)
+{
+	if(s->space != sp){
+		/* not in this space: the reference finds no leaf and only caches */
+		cpShapeCacheBB(s);
+		return;
+	}
+	/* the whole state comes home first (space_detach): the new cache is
+	 * what the rebuild uploads */
+	if(!space_edit_ok(sp)) return;
+	rd(s->body);
+	shape_cache_(s, s->body->transform);
+	record_op_(sp, CPG_OP_REINDEX, s, body_type_(s->body) == CP_BODY_TYPE_STATIC);
+	sp->structDirty = 1;
+	sp->editGen++;
+}
+
+void cpSpaceReindexShapesForBody(cpSpace *sp, cpBody *body)
+{
+	/* cpSpace.c:674-678, in the body's shape-list order */
+	for(cpShape *s = body->shapeList; s; s = s->next) cpSpaceReindexShape(sp, s);
+}
+
+/* cpSpace.c:654-660: every static shape's cache updated, then the static
+ * tree re-indexed as a whole (replayed on the device). */
+void cpSpaceReindexStatic(cpSpace *sp)
+{
+	if(!space_edit_ok(sp)) return;
+	for(int i = 0; i < sp->nshapes; i++){
+		cpShape *s = sp->shapes[i];
+		if(!s || body_type_(s->body) != CP_BODY_TYPE_STATIC) continue;
+		shape_cache_(s, s->body->transform);
+	}
+	if(sp->nops == sp->capops){
+		sp->capops = sp->capops ? 2*sp->capops : 256;
+		sp->ops = (cpgOp *)realloc(sp->ops, sizeof(cpgOp)*(size_t)sp->capops);
+	}
+	cpgOp *op = &sp->ops[sp->nops++];
+	memset(op, 0, sizeof(*op));
+	op->kind = CPG_OP_REINDEX_STATIC;
+	op->isStatic = 1;
+	sp->structDirty = 1;
+	sp->editGen++;
 }
 
 cpBody *cpSpaceAddBody(cpSpace *sp, cpBody *b)

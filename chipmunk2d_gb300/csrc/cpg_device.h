@@ -195,7 +195,10 @@ typedef struct cpgRow {
  * reference builds the leaf's fattened box immediately,
  * cpBBTree.c:605-616); a removal (cpSpaceRemoveShape, cpBodySetType)
  * names the shape and the index it leaves (cpBBTree.c:619-630). */
-enum { CPG_OP_INSERT = 0, CPG_OP_REMOVE = 1 };
+enum { CPG_OP_INSERT = 0, CPG_OP_REMOVE = 1, CPG_OP_REINDEX = 2, CPG_OP_REINDEX_STATIC = 3 };
+/* CPG_OP_REINDEX (cpSpaceReindexShape) carries the shape's new cached box
+ * and its body's velocity; CPG_OP_REINDEX_STATIC (cpSpaceReindexStatic)
+ * re-indexes every static leaf against the shapes' uploaded boxes. */
 typedef struct cpgOp {
 	int shape;
 	int isStatic;

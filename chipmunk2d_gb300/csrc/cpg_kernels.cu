@@ -91,6 +91,8 @@ __global__ void k_apply_ops(cpgSet s)
 		if(c.T->error) break;
 		cpgOp op = s.ops[W.opOff + i];
 		if(op.kind == CPG_OP_REMOVE) tree_remove(c, op);
+		else if(op.kind == CPG_OP_REINDEX) tree_reindex(c, op);
+		else if(op.kind == CPG_OP_REINDEX_STATIC) tree_reindex_static(c);
 		else tree_insert(c, op);
 	}
 }

@@ -670,6 +670,82 @@ __device__ void tree_remove(TreeCtx &c, const cpgOp &op)
 	node_recycle(c, leaf);
 }
 
+/* The leaf of `shape` in the dynamic or the static leaf set, -1 when it
+ * is not there (cpHashSetFind). */
+__device__ int leaf_find(const TreeCtx &c, int shape, bool isStatic)
+{
+	const int *bins = isStatic ? c.sbins : c.dbins;
+	unsigned size = isStatic ? c.T->statSize : c.T->dynSize;
+	if(size == 0) return -1;
+	int leaf = bins[(unsigned)(c.shash[shape] % size)];
+	for(int guard = 0; leaf >= 0; guard++){
+		if(guard > c.nodeCap){ c.T->error |= CPG_ERR_BINS; return -1; }
+		if(c.nodes[leaf].obj == shape) return leaf;
+		leaf = c.nodes[leaf].binNext;
+	}
+	return -1;
+}
+
+/* LeafUpdate (cpBBTree.c:498-517) against a given box: a leaf whose box
+ * no longer holds it is given the new (fattened when dynamic) box and
+ * reinserted, its pairs dropped and its stamp set. */
+__device__ bool leaf_update_to(TreeCtx &c, int leaf, BB bb, bool isStatic, V2 vel)
+{
+	cpgTree *T = c.T;
+	if(tcontains(node_bb(c.nodes[leaf]), bb)) return false;
+	set_node_bb(c.nodes[leaf], isStatic ? bb : fatten(bb, vel));
+	if(isStatic){
+		int root = subtree_remove(c, T->statRoot, leaf);
+		T->statRoot = subtree_insert(c, root, leaf);
+	} else {
+		int root = subtree_remove(c, T->dynRoot, leaf);
+		T->dynRoot = subtree_insert(c, root, leaf);
+	}
+	pairs_clear(c, leaf);
+	c.nodes[leaf].stamp = T->treeStamp;
+	return true;
+}
+
+/* cpBBTreeReindexObject (cpBBTree.c:676-684) for cpSpaceReindexShape: an
+ * updated leaf gets its pairs back (LeafAddPairs, :521-537), and the
+ * stamp advances whenever the leaf is found. */
+__device__ void tree_reindex(TreeCtx &c, const cpgOp &op)
+{
+	cpgTree *T = c.T;
+	bool isStatic = op.isStatic != 0;
+	int leaf = leaf_find(c, op.shape, isStatic);
+	if(leaf < 0) return;
+	if(leaf_update_to(c, leaf, bbnew(op.l, op.b, op.r, op.t), isStatic, v2(op.vx, op.vy))){
+		if(isStatic){
+			if(T->dynRoot >= 0) mark_leaf_query(c, T->dynRoot, leaf, true);
+		} else {
+			mark_leaf(c, leaf, T->statRoot);
+		}
+	}
+	T->treeStamp++;
+}
+
+/* cpSpaceReindexStatic (cpSpace.c:654-660): the static tree's
+ * cpBBTreeReindexQuery with the void query (cpBBTree.c:638-654): every
+ * static leaf, in hash-bin order, updated to its shape's box, then the
+ * static tree marked (no static root of its own) and the stamp advanced. */
+__device__ void tree_reindex_static(TreeCtx &c)
+{
+	cpgTree *T = c.T;
+	if(T->statRoot < 0) return;
+	for(unsigned i = 0; i < T->statSize && (int)i < c.sbinCap; i++){
+		int guard = 0;
+		for(int n = c.sbins[i]; n >= 0; guard++){
+			if(guard > c.nodeCap){ T->error |= CPG_ERR_BINS; return; }
+			int next = c.nodes[n].binNext;
+			leaf_update_to(c, n, shape_bb(c, c.nodes[n].obj), true, v2(0.0, 0.0));
+			n = next;
+		}
+	}
+	mark_subtree(c, T->statRoot, -1);
+	T->treeStamp++;
+}
+
 /* cpBBTree.c:498-517: a leaf whose shape left its fattened box */
 __device__ __forceinline__ bool leaf_moved(const TreeCtx &c, int leaf)
 {

@@ -259,6 +259,12 @@ void cpSpaceEachBody(cpSpace *space, cpSpaceBodyIteratorFunc func, void *data); 
 void cpSpaceEachShape(cpSpace *space, cpSpaceShapeIteratorFunc func, void *data);           /* cpSpace.h:231 */
 void cpSpaceEachConstraint(cpSpace *space, cpSpaceConstraintIteratorFunc func, void *data); /* cpSpace.h:236 */
 void cpSpaceStep(cpSpace *space, cpFloat dt);                        /* cpSpace.h:255 */
+/* Re-indexing moved shapes (cpSpace.h:240-246): the caches are brought to
+ * the bodies' transforms at the call and the trees updated as the
+ * reference's are, before the next step or query. */
+void cpSpaceReindexStatic(cpSpace *space);                           /* cpSpace.h:240 */
+void cpSpaceReindexShape(cpSpace *space, cpShape *shape);            /* cpSpace.h:242 */
+void cpSpaceReindexShapesForBody(cpSpace *space, cpBody *body);      /* cpSpace.h:244 */
 /* A callback run once when the current (or next) step, body/shape/
  * constraint iteration or point/segment/box/shape query ends, one per key;
  * returns cpFalse when the key is already registered. */

@@ -2368,6 +2368,59 @@ cpShape *cpSpaceAddShape(cpSpace *sp, cpShape *s)
 	return s;
 }
 
+/* cpSpace.c:662-672 with cpBBTreeReindexObject (cpBBTree.c:676-684): the
+ * shape's cache is brought to its body's transform; its leaf, when the
+ * space holds one, is updated (LeafUpdate) and given its pairs back
+ * (LeafAddPairs, cpBBTree.c:521-537), and the stamp advances. */
+void cpSpaceReindexShape(cpSpace *sp, cpShape *s)
+{
+	cpShapeCacheBB(s);
+	if(s->space != sp || s->leaf < 0) return;
+	int isStatic = (body_type(s->body) == CP_BODY_TYPE_STATIC);
+	Tree *tree = isStatic ? &sp->statTree : &sp->dynTree;
+	int leaf = s->leaf;
+	if(leaf_update(sp, tree, leaf)){
+		if(!isStatic){
+			MarkCtx ctx = { sp->statTree.root, 0 };
+			mark_leaf(sp, leaf, &ctx);
+		} else if(sp->dynTree.root >= 0){
+			MarkCtx ctx = { -1, 0 };
+			mark_leaf_query(sp, sp->dynTree.root, leaf, 1, &ctx);
+		}
+	}
+	sp->treeStamp++;
+}
+
+/* cpSpace.c:674-678, in the body's shape-list order */
+void cpSpaceReindexShapesForBody(cpSpace *sp, cpBody *body)
+{
+	for(cpShape *s = body->shapeList; s; s = s->next) cpSpaceReindexShape(sp, s);
+}
+
+/* cpSpace.c:654-660: every static shape's cache updated (cpShapeUpdateFunc
+ * over the leaf set), then cpBBTreeReindex of the static tree
+ * (cpBBTree.c:638-654 with the void query and no static root): each leaf,
+ * in bin order, updated; the tree marked; the stamp advanced. */
+void cpSpaceReindexStatic(cpSpace *sp)
+{
+	Tree *tree = &sp->statTree;
+	LeafSet *set = &tree->leaves;
+	for(unsigned i = 0; i < set->size; i++)
+		for(int n = set->bins[i]; n >= 0; n = sp->nodes[n].binNext) cpShapeCacheBB(sp->nodes[n].obj);
+	if(tree->root < 0) return;
+	for(unsigned i = 0; i < set->size; i++){
+		int n = set->bins[i];
+		while(n >= 0){
+			int next = sp->nodes[n].binNext;
+			leaf_update(sp, tree, n);
+			n = next;
+		}
+	}
+	MarkCtx ctx = { -1, 0 };
+	mark_subtree(sp, tree->root, &ctx);
+	sp->treeStamp++;
+}
+
 cpConstraint *cpSpaceAddConstraint(cpSpace *sp, cpConstraint *c)
 {
 	/* cpSpace.c:453-474 */
