@@ -353,6 +353,9 @@ cpBody *cpBodyNewKinematic(void);                                    /* cpBody.h
 cpBody *cpBodyNewStatic(void);                                       /* cpBody.h:58  */
 void cpBodyFree(cpBody *body);                                       /* cpBody.h:63  */
 void cpBodyActivate(cpBody *body);                                   /* cpBody.h:67  */
+void cpBodyActivateStatic(cpBody *body, cpShape *filter);            /* cpBody.h:69  */
+void cpBodySleep(cpBody *body);                                      /* cpBody.h:72  */
+void cpBodySleepWithGroup(cpBody *body, cpBody *group);              /* cpBody.h:74  */
 cpBool cpBodyIsSleeping(const cpBody *body);                         /* cpBody.h:77  */
 cpBodyType cpBodyGetType(cpBody *body);                              /* cpBody.h:80  */
 void cpBodySetType(cpBody *body, cpBodyType type);                    /* cpBody.h:82  */

@@ -94,6 +94,9 @@ struct cpArbiter {
 	cpTimestamp stamp;
 	int state;
 	int live;   /* slot in use in the cache */
+	/* the contact graph (cpArbiterThread, chipmunk_structs.h:176-179):
+	 * body_a's and body_b's list links, as slot + 1 (0 = none) */
+	int prevA, nextA, prevB, nextB;
 };
 
 struct cpBody {
@@ -110,6 +113,10 @@ struct cpBody {
 	cpShape *shapeList;
 	cpConstraint *constraintList;
 	cpFloat idleTime;
+	/* sleeping (chipmunk_structs.h:90-94): the component root and next
+	 * body; the head of the body's arbiter list, as slot + 1 (0 = none) */
+	cpBody *sleepRoot, *sleepNext;
+	int arbList;
 };
 
 struct cpShape {
@@ -234,12 +241,21 @@ struct cpSpace {
 	ArbMap amap;
 	int *active; int nactive, capactive;   /* space->arbiters: slot indices */
 
+	/* sleeping components (their roots) and bodies woken while locked */
+	cpBody **sleeping; int nsleeping, capsleeping;
+	cpBody **roused; int nroused, caproused;
+
 	cpBody staticBody;
 	struct Hasty *hasty;                   /* the threaded solver (cpx_space_set_hasty), or NULL */
 	struct PostStep *post; int npost, cappost, postRunning;   /* post-step callbacks */
 };
 
 static void run_post_step_(cpSpace *sp);
+static void arb_unthread_(cpSpace *sp, int slot);
+static void space_unlock_(cpSpace *sp);
+
+/* cpConstraintActivateBodies (chipmunk_private.h:165-170) */
+static void activate_bodies_(cpConstraint *c) { cpBodyActivate(c->a); cpBodyActivate(c->b); }
 
 /* ========================================================================
  * Creation-time math: src/chipmunk.c:63-171, 250-274
@@ -456,36 +472,36 @@ cpBody *cpBodyNewKinematic(void)
 }
 
 void cpBodyFree(cpBody *body) { free(body); }
-void cpBodyActivate(cpBody *body) { (void)body; }
-cpBool cpBodyIsSleeping(const cpBody *body) { (void)body; return cpFalse; }
+cpBool cpBodyIsSleeping(const cpBody *body) { return body->sleepRoot != NULL; }
 cpBodyType cpBodyGetType(cpBody *body) { return body_type(body); }
 cpSpace *cpBodyGetSpace(const cpBody *body) { return body->space; }
 cpFloat cpBodyGetMass(const cpBody *body) { return body->m; }
-void cpBodySetMass(cpBody *body, cpFloat mass) { body->m = mass; body->m_inv = (mass == 0.0 ? ORC_INF : 1.0/mass); }
+void cpBodySetMass(cpBody *body, cpFloat mass) { cpBodyActivate(body); body->m = mass; body->m_inv = (mass == 0.0 ? ORC_INF : 1.0/mass); }
 cpFloat cpBodyGetMoment(const cpBody *body) { return body->i; }
-void cpBodySetMoment(cpBody *body, cpFloat i) { body->i = i; body->i_inv = (i == 0.0 ? ORC_INF : 1.0/i); }
+void cpBodySetMoment(cpBody *body, cpFloat i) { cpBodyActivate(body); body->i = i; body->i_inv = (i == 0.0 ? ORC_INF : 1.0/i); }
 cpVect cpBodyGetRotation(const cpBody *body) { return cpv(body->transform.a, body->transform.b); }
 cpVect cpBodyGetPosition(const cpBody *body) { return cpTransformPoint(body->transform, cpvzero); }
 
 void cpBodySetPosition(cpBody *body, cpVect position)
 {
 	/* cpBody.c:374-382 */
+	cpBodyActivate(body);
 	cpVect p = body->p = cpvadd(cpTransformVect(body->transform, body->cog), position);
 	body_set_transform(body, p, body->a);
 }
 
 cpVect cpBodyGetCenterOfGravity(const cpBody *body) { return body->cog; }
-void cpBodySetCenterOfGravity(cpBody *body, cpVect cog) { body->cog = cog; }
+void cpBodySetCenterOfGravity(cpBody *body, cpVect cog) { cpBodyActivate(body); body->cog = cog; }
 cpVect cpBodyGetVelocity(const cpBody *body) { return body->v; }
-void cpBodySetVelocity(cpBody *body, cpVect v) { body->v = v; }
+void cpBodySetVelocity(cpBody *body, cpVect v) { cpBodyActivate(body); body->v = v; }
 cpVect cpBodyGetForce(const cpBody *body) { return body->f; }
-void cpBodySetForce(cpBody *body, cpVect f) { body->f = f; }
+void cpBodySetForce(cpBody *body, cpVect f) { cpBodyActivate(body); body->f = f; }
 cpFloat cpBodyGetAngle(const cpBody *body) { return body->a; }
-void cpBodySetAngle(cpBody *body, cpFloat a) { body->a = a; body_set_transform(body, body->p, a); }
+void cpBodySetAngle(cpBody *body, cpFloat a) { cpBodyActivate(body); body->a = a; body_set_transform(body, body->p, a); }
 cpFloat cpBodyGetAngularVelocity(const cpBody *body) { return body->w; }
-void cpBodySetAngularVelocity(cpBody *body, cpFloat w) { body->w = w; }
+void cpBodySetAngularVelocity(cpBody *body, cpFloat w) { cpBodyActivate(body); body->w = w; }
 cpFloat cpBodyGetTorque(const cpBody *body) { return body->t; }
-void cpBodySetTorque(cpBody *body, cpFloat t) { body->t = t; }
+void cpBodySetTorque(cpBody *body, cpFloat t) { cpBodyActivate(body); body->t = t; }
 cpDataPointer cpBodyGetUserData(const cpBody *body) { return body->userData; }
 void cpBodySetUserData(cpBody *body, cpDataPointer d) { body->userData = d; }
 void cpBodySetVelocityUpdateFunc(cpBody *body, cpBodyVelocityFunc f) { body->velocity_func = f; }
@@ -495,6 +511,7 @@ cpVect cpBodyWorldToLocal(const cpBody *body, const cpVect point) { return cpTra
 
 void cpBodyApplyForceAtWorldPoint(cpBody *body, cpVect force, cpVect point)
 {
+	cpBodyActivate(body);
 	body->f = cpvadd(body->f, force);
 	cpVect r = cpvsub(point, cpTransformPoint(body->transform, body->cog));
 	body->t += cpvcross(r, force);
@@ -579,6 +596,7 @@ cpVect cpBodyGetVelocityAtLocalPoint(const cpBody *body, cpVect point)
 
 void cpBodyApplyImpulseAtWorldPoint(cpBody *body, cpVect impulse, cpVect point)
 {
+	cpBodyActivate(body);
 	cpVect r = cpvsub(point, cpTransformPoint(body->transform, body->cog));
 	apply_impulse_(body, impulse, r);
 }
@@ -790,7 +808,7 @@ void cpShapeFree(cpShape *s)
 cpSpace *cpShapeGetSpace(const cpShape *s) { return s->space; }
 cpBody *cpShapeGetBody(const cpShape *s) { return s->body; }
 cpFloat cpShapeGetMass(cpShape *s) { return s->mass_m; }
-void cpShapeSetMass(cpShape *s, cpFloat mass) { s->mass_m = mass; body_accumulate_mass(s->body); }
+void cpShapeSetMass(cpShape *s, cpFloat mass) { cpBodyActivate(s->body); s->mass_m = mass; body_accumulate_mass(s->body); }
 cpFloat cpShapeGetDensity(cpShape *s) { return s->mass_m/s->mass_area; }
 void cpShapeSetDensity(cpShape *s, cpFloat d) { cpShapeSetMass(s, d*s->mass_area); }
 cpFloat cpShapeGetMoment(cpShape *s) { return s->mass_m*s->mass_i; }
@@ -798,19 +816,19 @@ cpFloat cpShapeGetArea(cpShape *s) { return s->mass_area; }
 cpVect cpShapeGetCenterOfGravity(cpShape *s) { return s->mass_cog; }
 cpBB cpShapeGetBB(const cpShape *s) { return s->bb; }
 cpBool cpShapeGetSensor(const cpShape *s) { return s->sensor; }
-void cpShapeSetSensor(cpShape *s, cpBool v) { s->sensor = v; }
+void cpShapeSetSensor(cpShape *s, cpBool v) { cpBodyActivate(s->body); s->sensor = v; }
 cpFloat cpShapeGetElasticity(const cpShape *s) { return s->e; }
-void cpShapeSetElasticity(cpShape *s, cpFloat e) { ORC_ASSERT(e >= 0.0, "Elasticity must be positive."); s->e = e; }
+void cpShapeSetElasticity(cpShape *s, cpFloat e) { ORC_ASSERT(e >= 0.0, "Elasticity must be positive."); cpBodyActivate(s->body); s->e = e; }
 cpFloat cpShapeGetFriction(const cpShape *s) { return s->u; }
-void cpShapeSetFriction(cpShape *s, cpFloat u) { ORC_ASSERT(u >= 0.0, "Friction must be postive."); s->u = u; }
+void cpShapeSetFriction(cpShape *s, cpFloat u) { ORC_ASSERT(u >= 0.0, "Friction must be postive."); cpBodyActivate(s->body); s->u = u; }
 cpVect cpShapeGetSurfaceVelocity(const cpShape *s) { return s->surfaceV; }
-void cpShapeSetSurfaceVelocity(cpShape *s, cpVect v) { s->surfaceV = v; }
+void cpShapeSetSurfaceVelocity(cpShape *s, cpVect v) { cpBodyActivate(s->body); s->surfaceV = v; }
 cpDataPointer cpShapeGetUserData(const cpShape *s) { return s->userData; }
 void cpShapeSetUserData(cpShape *s, cpDataPointer d) { s->userData = d; }
 cpCollisionType cpShapeGetCollisionType(const cpShape *s) { return s->type; }
-void cpShapeSetCollisionType(cpShape *s, cpCollisionType t) { s->type = t; }
+void cpShapeSetCollisionType(cpShape *s, cpCollisionType t) { cpBodyActivate(s->body); s->type = t; }
 cpShapeFilter cpShapeGetFilter(const cpShape *s) { return s->filter; }
-void cpShapeSetFilter(cpShape *s, cpShapeFilter f) { s->filter = f; }
+void cpShapeSetFilter(cpShape *s, cpShapeFilter f) { cpBodyActivate(s->body); s->filter = f; }
 cpVect cpCircleShapeGetOffset(const cpShape *s) { return s->c; }
 cpFloat cpCircleShapeGetRadius(const cpShape *s) { return s->r; }
 cpVect cpSegmentShapeGetA(const cpShape *s) { return s->sa; }
@@ -954,60 +972,60 @@ cpBool cpConstraintIsRatchetJoint(const cpConstraint *c) { return c->kind == JOI
 cpBool cpConstraintIsGearJoint(const cpConstraint *c) { return c->kind == JOINT_GEAR; }
 cpBool cpConstraintIsSimpleMotor(const cpConstraint *c) { return c->kind == JOINT_MOTOR; }
 cpVect cpGrooveJointGetGrooveA(const cpConstraint *c) { return c->grv_a; }
-void cpGrooveJointSetGrooveA(cpConstraint *c, cpVect v) { c->grv_a = v; c->grv_n = cpvperp(cpvnormalize(cpvsub(c->grv_b, v))); }
+void cpGrooveJointSetGrooveA(cpConstraint *c, cpVect v) { activate_bodies_(c); c->grv_a = v; c->grv_n = cpvperp(cpvnormalize(cpvsub(c->grv_b, v))); }
 cpVect cpGrooveJointGetGrooveB(const cpConstraint *c) { return c->grv_b; }
-void cpGrooveJointSetGrooveB(cpConstraint *c, cpVect v) { c->grv_b = v; c->grv_n = cpvperp(cpvnormalize(cpvsub(v, c->grv_a))); }
+void cpGrooveJointSetGrooveB(cpConstraint *c, cpVect v) { activate_bodies_(c); c->grv_b = v; c->grv_n = cpvperp(cpvnormalize(cpvsub(v, c->grv_a))); }
 cpVect cpGrooveJointGetAnchorB(const cpConstraint *c) { return c->anchorB; }
-void cpGrooveJointSetAnchorB(cpConstraint *c, cpVect v) { c->anchorB = v; }
+void cpGrooveJointSetAnchorB(cpConstraint *c, cpVect v) { activate_bodies_(c); c->anchorB = v; }
 cpVect cpDampedSpringGetAnchorA(const cpConstraint *c) { return c->anchorA; }
-void cpDampedSpringSetAnchorA(cpConstraint *c, cpVect v) { c->anchorA = v; }
+void cpDampedSpringSetAnchorA(cpConstraint *c, cpVect v) { activate_bodies_(c); c->anchorA = v; }
 cpVect cpDampedSpringGetAnchorB(const cpConstraint *c) { return c->anchorB; }
-void cpDampedSpringSetAnchorB(cpConstraint *c, cpVect v) { c->anchorB = v; }
+void cpDampedSpringSetAnchorB(cpConstraint *c, cpVect v) { activate_bodies_(c); c->anchorB = v; }
 cpFloat cpDampedSpringGetRestLength(const cpConstraint *c) { return c->restLength; }
-void cpDampedSpringSetRestLength(cpConstraint *c, cpFloat v) { c->restLength = v; }
+void cpDampedSpringSetRestLength(cpConstraint *c, cpFloat v) { activate_bodies_(c); c->restLength = v; }
 cpFloat cpDampedSpringGetStiffness(const cpConstraint *c) { return c->stiffness; }
-void cpDampedSpringSetStiffness(cpConstraint *c, cpFloat v) { c->stiffness = v; }
+void cpDampedSpringSetStiffness(cpConstraint *c, cpFloat v) { activate_bodies_(c); c->stiffness = v; }
 cpFloat cpDampedSpringGetDamping(const cpConstraint *c) { return c->damping; }
-void cpDampedSpringSetDamping(cpConstraint *c, cpFloat v) { c->damping = v; }
+void cpDampedSpringSetDamping(cpConstraint *c, cpFloat v) { activate_bodies_(c); c->damping = v; }
 cpDampedSpringForceFunc cpDampedSpringGetSpringForceFunc(const cpConstraint *c) { return c->springForceFunc; }
-void cpDampedSpringSetSpringForceFunc(cpConstraint *c, cpDampedSpringForceFunc f) { c->springForceFunc = f; }
+void cpDampedSpringSetSpringForceFunc(cpConstraint *c, cpDampedSpringForceFunc f) { activate_bodies_(c); c->springForceFunc = f; }
 cpFloat cpDampedRotarySpringGetRestAngle(const cpConstraint *c) { return c->restAngle; }
-void cpDampedRotarySpringSetRestAngle(cpConstraint *c, cpFloat v) { c->restAngle = v; }
+void cpDampedRotarySpringSetRestAngle(cpConstraint *c, cpFloat v) { activate_bodies_(c); c->restAngle = v; }
 cpFloat cpDampedRotarySpringGetStiffness(const cpConstraint *c) { return c->stiffness; }
-void cpDampedRotarySpringSetStiffness(cpConstraint *c, cpFloat v) { c->stiffness = v; }
+void cpDampedRotarySpringSetStiffness(cpConstraint *c, cpFloat v) { activate_bodies_(c); c->stiffness = v; }
 cpFloat cpDampedRotarySpringGetDamping(const cpConstraint *c) { return c->damping; }
-void cpDampedRotarySpringSetDamping(cpConstraint *c, cpFloat v) { c->damping = v; }
+void cpDampedRotarySpringSetDamping(cpConstraint *c, cpFloat v) { activate_bodies_(c); c->damping = v; }
 cpDampedRotarySpringTorqueFunc cpDampedRotarySpringGetSpringTorqueFunc(const cpConstraint *c) { return c->springTorqueFunc; }
-void cpDampedRotarySpringSetSpringTorqueFunc(cpConstraint *c, cpDampedRotarySpringTorqueFunc f) { c->springTorqueFunc = f; }
+void cpDampedRotarySpringSetSpringTorqueFunc(cpConstraint *c, cpDampedRotarySpringTorqueFunc f) { activate_bodies_(c); c->springTorqueFunc = f; }
 cpFloat cpRotaryLimitJointGetMin(const cpConstraint *c) { return c->min; }
-void cpRotaryLimitJointSetMin(cpConstraint *c, cpFloat v) { c->min = v; }
+void cpRotaryLimitJointSetMin(cpConstraint *c, cpFloat v) { activate_bodies_(c); c->min = v; }
 cpFloat cpRotaryLimitJointGetMax(const cpConstraint *c) { return c->max; }
-void cpRotaryLimitJointSetMax(cpConstraint *c, cpFloat v) { c->max = v; }
+void cpRotaryLimitJointSetMax(cpConstraint *c, cpFloat v) { activate_bodies_(c); c->max = v; }
 cpFloat cpRatchetJointGetAngle(const cpConstraint *c) { return c->angle; }
-void cpRatchetJointSetAngle(cpConstraint *c, cpFloat v) { c->angle = v; }
+void cpRatchetJointSetAngle(cpConstraint *c, cpFloat v) { activate_bodies_(c); c->angle = v; }
 cpFloat cpRatchetJointGetPhase(const cpConstraint *c) { return c->phase; }
-void cpRatchetJointSetPhase(cpConstraint *c, cpFloat v) { c->phase = v; }
+void cpRatchetJointSetPhase(cpConstraint *c, cpFloat v) { activate_bodies_(c); c->phase = v; }
 cpFloat cpRatchetJointGetRatchet(const cpConstraint *c) { return c->ratchet; }
-void cpRatchetJointSetRatchet(cpConstraint *c, cpFloat v) { c->ratchet = v; }
+void cpRatchetJointSetRatchet(cpConstraint *c, cpFloat v) { activate_bodies_(c); c->ratchet = v; }
 cpFloat cpGearJointGetPhase(const cpConstraint *c) { return c->phase; }
-void cpGearJointSetPhase(cpConstraint *c, cpFloat v) { c->phase = v; }
+void cpGearJointSetPhase(cpConstraint *c, cpFloat v) { activate_bodies_(c); c->phase = v; }
 cpFloat cpGearJointGetRatio(const cpConstraint *c) { return c->ratio; }
-void cpGearJointSetRatio(cpConstraint *c, cpFloat v) { c->ratio = v; c->ratio_inv = 1.0/v; }
+void cpGearJointSetRatio(cpConstraint *c, cpFloat v) { activate_bodies_(c); c->ratio = v; c->ratio_inv = 1.0/v; }
 cpFloat cpSimpleMotorGetRate(const cpConstraint *c) { return c->rate; }
-void cpSimpleMotorSetRate(cpConstraint *c, cpFloat v) { c->rate = v; }
+void cpSimpleMotorSetRate(cpConstraint *c, cpFloat v) { activate_bodies_(c); c->rate = v; }
 
 void cpConstraintFree(cpConstraint *c) { free(c); }
 cpSpace *cpConstraintGetSpace(const cpConstraint *c) { return c->space; }
 cpBody *cpConstraintGetBodyA(const cpConstraint *c) { return c->a; }
 cpBody *cpConstraintGetBodyB(const cpConstraint *c) { return c->b; }
 cpFloat cpConstraintGetMaxForce(const cpConstraint *c) { return c->maxForce; }
-void cpConstraintSetMaxForce(cpConstraint *c, cpFloat v) { c->maxForce = v; }
+void cpConstraintSetMaxForce(cpConstraint *c, cpFloat v) { activate_bodies_(c); c->maxForce = v; }
 cpFloat cpConstraintGetErrorBias(const cpConstraint *c) { return c->errorBias; }
-void cpConstraintSetErrorBias(cpConstraint *c, cpFloat v) { c->errorBias = v; }
+void cpConstraintSetErrorBias(cpConstraint *c, cpFloat v) { activate_bodies_(c); c->errorBias = v; }
 cpFloat cpConstraintGetMaxBias(const cpConstraint *c) { return c->maxBias; }
-void cpConstraintSetMaxBias(cpConstraint *c, cpFloat v) { c->maxBias = v; }
+void cpConstraintSetMaxBias(cpConstraint *c, cpFloat v) { activate_bodies_(c); c->maxBias = v; }
 cpBool cpConstraintGetCollideBodies(const cpConstraint *c) { return c->collideBodies; }
-void cpConstraintSetCollideBodies(cpConstraint *c, cpBool v) { c->collideBodies = v; }
+void cpConstraintSetCollideBodies(cpConstraint *c, cpBool v) { activate_bodies_(c); c->collideBodies = v; }
 void cpConstraintSetPreSolveFunc(cpConstraint *c, cpConstraintPreSolveFunc f) { c->preSolve = f; }
 void cpConstraintSetPostSolveFunc(cpConstraint *c, cpConstraintPostSolveFunc f) { c->postSolve = f; }
 cpDataPointer cpConstraintGetUserData(const cpConstraint *c) { return c->userData; }
@@ -1025,15 +1043,15 @@ cpVect cpSlideJointGetAnchorB(const cpConstraint *c) { return c->anchorB; }
 /* cpPivotJoint.c:133-155, cpPinJoint.c:109-142, cpSlideJoint.c:127-172:
  * the setters store the value (they also wake the bodies, and no body
  * sleeps here) */
-void cpPivotJointSetAnchorA(cpConstraint *c, cpVect v) { c->anchorA = v; }
-void cpPivotJointSetAnchorB(cpConstraint *c, cpVect v) { c->anchorB = v; }
-void cpPinJointSetAnchorA(cpConstraint *c, cpVect v) { c->anchorA = v; }
-void cpPinJointSetAnchorB(cpConstraint *c, cpVect v) { c->anchorB = v; }
-void cpPinJointSetDist(cpConstraint *c, cpFloat v) { c->dist = v; }
-void cpSlideJointSetAnchorA(cpConstraint *c, cpVect v) { c->anchorA = v; }
-void cpSlideJointSetAnchorB(cpConstraint *c, cpVect v) { c->anchorB = v; }
-void cpSlideJointSetMin(cpConstraint *c, cpFloat v) { c->min = v; }
-void cpSlideJointSetMax(cpConstraint *c, cpFloat v) { c->max = v; }
+void cpPivotJointSetAnchorA(cpConstraint *c, cpVect v) { activate_bodies_(c); c->anchorA = v; }
+void cpPivotJointSetAnchorB(cpConstraint *c, cpVect v) { activate_bodies_(c); c->anchorB = v; }
+void cpPinJointSetAnchorA(cpConstraint *c, cpVect v) { activate_bodies_(c); c->anchorA = v; }
+void cpPinJointSetAnchorB(cpConstraint *c, cpVect v) { activate_bodies_(c); c->anchorB = v; }
+void cpPinJointSetDist(cpConstraint *c, cpFloat v) { activate_bodies_(c); c->dist = v; }
+void cpSlideJointSetAnchorA(cpConstraint *c, cpVect v) { activate_bodies_(c); c->anchorA = v; }
+void cpSlideJointSetAnchorB(cpConstraint *c, cpVect v) { activate_bodies_(c); c->anchorB = v; }
+void cpSlideJointSetMin(cpConstraint *c, cpFloat v) { activate_bodies_(c); c->min = v; }
+void cpSlideJointSetMax(cpConstraint *c, cpFloat v) { activate_bodies_(c); c->max = v; }
 cpFloat cpSlideJointGetMin(const cpConstraint *c) { return c->min; }
 cpFloat cpSlideJointGetMax(const cpConstraint *c) { return c->max; }
 
@@ -2290,9 +2308,12 @@ cpSpace *cpSpaceNew(void)
 static void hasty_stop(cpSpace *sp);
 
 /* cpSpace.c:180-205 (cpSpaceDestroy / cpSpaceFree) */
+static void activate_wrap_(cpBody *body, void *unused) { (void)unused; cpBodyActivate(body); }
+
 void cpSpaceDestroy(cpSpace *sp)
 {
 	if(!sp) return;
+	cpSpaceEachBody(sp, activate_wrap_, NULL);
 	hasty_stop(sp);
 	free(sp->dyn); free(sp->stat); free(sp->cons);
 	free(sp->nodes); free(sp->pairs);
@@ -2304,6 +2325,8 @@ void cpSpaceDestroy(cpSpace *sp)
 	sp->arbs = NULL; sp->freeList = NULL; sp->amap.keys = NULL; sp->amap.slot = NULL; sp->active = NULL;
 	sp->candPairs = NULL;
 	free(sp->post); sp->post = NULL; sp->npost = sp->cappost = 0;
+	free(sp->sleeping); free(sp->roused); sp->sleeping = sp->roused = NULL;
+	sp->nsleeping = sp->capsleeping = sp->nroused = sp->caproused = 0;
 }
 
 void cpSpaceFree(cpSpace *sp)
@@ -2316,7 +2339,13 @@ void cpSpaceFree(cpSpace *sp)
 int cpSpaceGetIterations(const cpSpace *sp) { return sp->iterations; }
 void cpSpaceSetIterations(cpSpace *sp, int it) { ORC_ASSERT(it > 0, "Iterations must be positive and non-zero."); sp->iterations = it; }
 cpVect cpSpaceGetGravity(const cpSpace *sp) { return sp->gravity; }
-void cpSpaceSetGravity(cpSpace *sp, cpVect g) { sp->gravity = g; }
+/* cpSpace.c:253-263: the sleeping components are woken as the reference
+ * wakes them, walking the array that each activation shrinks */
+void cpSpaceSetGravity(cpSpace *sp, cpVect g)
+{
+	sp->gravity = g;
+	for(int i = 0; i < sp->nsleeping; i++) cpBodyActivate(sp->sleeping[i]);
+}
 cpFloat cpSpaceGetDamping(const cpSpace *sp) { return sp->damping; }
 void cpSpaceSetDamping(cpSpace *sp, cpFloat d) { sp->damping = d; }
 cpFloat cpSpaceGetIdleSpeedThreshold(const cpSpace *sp) { return sp->idleSpeedThreshold; }
@@ -2355,6 +2384,7 @@ cpShape *cpSpaceAddShape(cpSpace *sp, cpShape *s)
 	cpBody *body = s->body;
 	ORC_ASSERT(body->space == sp, "The shape's body must be added to the space before the shape.");
 	int isStatic = (body_type(body) == CP_BODY_TYPE_STATIC);
+	if(!isStatic) cpBodyActivate(body);
 	/* cpBody.c:182-194: push on the body's shape list */
 	cpShape *next = body->shapeList;
 	if(next) next->prev = s;
@@ -2376,7 +2406,8 @@ void cpSpaceReindexShape(cpSpace *sp, cpShape *s)
 {
 	cpShapeCacheBB(s);
 	if(s->space != sp || s->leaf < 0) return;
-	int isStatic = (body_type(s->body) == CP_BODY_TYPE_STATIC);
+	/* a sleeping body's shapes are in the static index */
+	int isStatic = (body_type(s->body) == CP_BODY_TYPE_STATIC || cpBodyIsSleeping(s->body));
 	Tree *tree = isStatic ? &sp->statTree : &sp->dynTree;
 	int leaf = s->leaf;
 	if(leaf_update(sp, tree, leaf)){
@@ -2426,6 +2457,8 @@ cpConstraint *cpSpaceAddConstraint(cpSpace *sp, cpConstraint *c)
 	/* cpSpace.c:453-474 */
 	ORC_ASSERT(!c->space, "You have already added this constraint to a space.");
 	cpBody *a = c->a, *b = c->b;
+	cpBodyActivate(a);
+	cpBodyActivate(b);
 	push_ptr_((void ***)&sp->cons, &sp->ncons, &sp->capcons, c);
 	c->next_a = a->constraintList; a->constraintList = c;
 	c->next_b = b->constraintList; b->constraintList = c;
@@ -2462,10 +2495,11 @@ static int array_delete_(void **arr, int *n, void *obj)
 }
 
 /* cpSpace.c:481-521 (cpSpaceFilterArbiters with a shape): every cached
- * arbiter of the shape is dropped.  The reference also deletes it from the
- * last step's arbiter array, whose order then depends on the hash set's
- * pointer hashes; here the array keeps its order (the next step rebuilds
- * it from scratch either way). */
+ * arbiter of the shape leaves the contact graph and is dropped.  The
+ * reference also deletes it from the last step's arbiter array, whose
+ * order then depends on the hash set's pointer hashes; here the array
+ * keeps its order (the next step empties it, and nothing reads its order
+ * before then). */
 static void filter_arbiters_of(cpSpace *sp, cpShape *s)
 {
 	ArbMap *m = &sp->amap;
@@ -2475,6 +2509,7 @@ static void filter_arbiters_of(cpSpace *sp, cpShape *s)
 		cpArbiter *arb = &sp->arbs[slot];
 		if(arb->a != s && arb->b != s) continue;
 		m->keys[h] = 1;
+		arb_unthread_(sp, slot);
 		arb_free(sp, slot);
 		int k = 0;
 		for(int i = 0; i < sp->nactive; i++) if(sp->active[i] != slot) sp->active[k++] = sp->active[i];
@@ -2488,6 +2523,8 @@ void cpSpaceRemoveShape(cpSpace *sp, cpShape *s)
 	ORC_ASSERT(s->space == sp, "Cannot remove a shape that was not added to the space.");
 	cpBody *body = s->body;
 	int isStatic = (body_type(body) == CP_BODY_TYPE_STATIC);
+	if(isStatic) cpBodyActivateStatic(body, s);
+	else cpBodyActivate(body);
 	/* cpBodyRemoveShape, cpBody.c:306-327 */
 	if(s->prev) s->prev->next = s->next; else body->shapeList = s->next;
 	if(s->next) s->next->prev = s->prev;
@@ -2504,6 +2541,7 @@ void cpSpaceRemoveBody(cpSpace *sp, cpBody *body)
 	/* cpSpace.c:547-562 */
 	ORC_ASSERT(body != &sp->staticBody, "Cannot remove the designated static body for the space.");
 	ORC_ASSERT(body->space == sp, "Cannot remove a body that was not added to the space.");
+	cpBodyActivate(body);
 	if(body_type(body) == CP_BODY_TYPE_STATIC) array_delete_((void **)sp->stat, &sp->nstat, body);
 	else array_delete_((void **)sp->dyn, &sp->ndyn, body);
 	body->space = NULL;
@@ -2522,6 +2560,8 @@ void cpSpaceRemoveConstraint(cpSpace *sp, cpConstraint *c)
 {
 	/* cpSpace.c:564-577 */
 	ORC_ASSERT(c->space == sp, "Cannot remove a constraint that was not added to the space.");
+	cpBodyActivate(c->a);
+	cpBodyActivate(c->b);
 	array_delete_((void **)sp->cons, &sp->ncons, c);
 	c->a->constraintList = filter_constraints_(c->a->constraintList, c->a, c);
 	c->b->constraintList = filter_constraints_(c->b->constraintList, c->b, c);
@@ -2546,6 +2586,8 @@ void cpBodySetType(cpBody *body, cpBodyType type)
 	}
 	cpSpace *sp = body->space;
 	if(!sp) return;
+	/* activated with its new type (a no-op unless it turned dynamic) */
+	if(oldType != CP_BODY_TYPE_STATIC) cpBodyActivate(body);
 	int fromStatic = (oldType == CP_BODY_TYPE_STATIC), toStatic = (type == CP_BODY_TYPE_STATIC);
 	if(fromStatic != toStatic){
 		if(fromStatic){
@@ -2562,10 +2604,22 @@ void cpBodySetType(cpBody *body, cpBodyType type)
 	}
 }
 
+/* cpSpace.c:589-617: the dynamic array, the static array, then each
+ * sleeping component from its root */
 void cpSpaceEachBody(cpSpace *sp, cpSpaceBodyIteratorFunc func, void *data)
 {
+	sp->locked++;
 	for(int i = 0; i < sp->ndyn; i++) func(sp->dyn[i], data);
 	for(int i = 0; i < sp->nstat; i++) func(sp->stat[i], data);
+	for(int i = 0; i < sp->nsleeping; i++){
+		cpBody *b = sp->sleeping[i];
+		while(b){
+			cpBody *next = b->sleepNext;
+			func(b, data);
+			b = next;
+		}
+	}
+	space_unlock_(sp);
 	run_post_step_(sp);
 }
 
@@ -2683,6 +2737,261 @@ static cpCollisionID collide_shapes_(cpSpace *sp, cpShape *a, cpShape *b, cpColl
 	return info.id;
 }
 
+/* ========================================================================
+ * The contact graph and sleeping: src/cpSpaceComponent.c, cpArbiter.c:222-247
+ * ====================================================================== */
+#define ARB_AT_(sp, k) (&(sp)->arbs[(k) - 1])   /* k: slot + 1 */
+
+/* cpArbiterThreadForBody (chipmunk_private.h:178-181) */
+static int *thread_prev_(cpArbiter *arb, const cpBody *body) { return (arb->body_a == body) ? &arb->prevA : &arb->prevB; }
+static int *thread_next_(cpArbiter *arb, const cpBody *body) { return (arb->body_a == body) ? &arb->nextA : &arb->nextB; }
+
+/* cpBodyPushArbiter (cpSpaceComponent.c:168-181) */
+static void body_push_arbiter_(cpSpace *sp, cpBody *body, int slot)
+{
+	int next = body->arbList;
+	*thread_next_(&sp->arbs[slot], body) = next;
+	if(next) *thread_prev_(ARB_AT_(sp, next), body) = slot + 1;
+	body->arbList = slot + 1;
+}
+
+/* unthreadHelper (cpArbiter.c:222-241) */
+static void unthread_helper_(cpSpace *sp, int slot, cpBody *body)
+{
+	cpArbiter *arb = &sp->arbs[slot];
+	int prev = *thread_prev_(arb, body), next = *thread_next_(arb, body);
+	if(prev) *thread_next_(ARB_AT_(sp, prev), body) = next;
+	else if(body->arbList == slot + 1) body->arbList = next;
+	if(next) *thread_prev_(ARB_AT_(sp, next), body) = prev;
+	*thread_prev_(arb, body) = 0;
+	*thread_next_(arb, body) = 0;
+}
+
+/* cpArbiterUnthread (cpArbiter.c:243-247) */
+static void arb_unthread_(cpSpace *sp, int slot)
+{
+	unthread_helper_(sp, slot, sp->arbs[slot].body_a);
+	unthread_helper_(sp, slot, sp->arbs[slot].body_b);
+}
+
+/* cpArbiterNext (chipmunk_private.h:183-186), as slot + 1 */
+static int arb_next_(cpSpace *sp, int k, const cpBody *body) { return *thread_next_(ARB_AT_(sp, k), body); }
+
+/* cpArrayDeleteObj (cpArray.c:76-88) on the arbiter list */
+static void active_delete_(cpSpace *sp, int slot)
+{
+	for(int i = 0; i < sp->nactive; i++){
+		if(sp->active[i] == slot){ sp->active[i] = sp->active[--sp->nactive]; return; }
+	}
+}
+
+/* cpSpaceActivateBody (cpSpaceComponent.c:28-79): the body goes back on
+ * the dynamic array, its shapes from the static to the dynamic index, the
+ * arbiters it owns back into the cache and onto the arbiter list, and the
+ * constraints it owns back onto the constraint array.  While the space is
+ * locked the body waits on the roused list. */
+static void space_activate_body_(cpSpace *sp, cpBody *body)
+{
+	ORC_ASSERT(body_type(body) == CP_BODY_TYPE_DYNAMIC, "Internal error: Attempting to activate a non-dynamic body.");
+	if(sp->locked){
+		for(int i = 0; i < sp->nroused; i++) if(sp->roused[i] == body) return;
+		push_ptr_((void ***)&sp->roused, &sp->nroused, &sp->caproused, body);
+		return;
+	}
+	push_ptr_((void ***)&sp->dyn, &sp->ndyn, &sp->capdyn, body);
+	for(cpShape *s = body->shapeList; s; s = s->next){
+		tree_remove(sp, &sp->statTree, s);
+		tree_insert(sp, &sp->dynTree, s);
+	}
+	for(int k = body->arbList; k; k = arb_next_(sp, k, body)){
+		cpArbiter *arb = ARB_AT_(sp, k);
+		cpBody *bodyA = arb->body_a;
+		if(body == bodyA || body_type(bodyA) == CP_BODY_TYPE_STATIC){
+			amap_insert(sp, arb_key(arb->a, arb->b), k - 1);
+			arb->stamp = sp->stamp;
+			active_push(sp, k - 1);
+		}
+	}
+	for(cpConstraint *c = body->constraintList; c; c = constraint_next_(c, body)){
+		cpBody *bodyA = c->a;
+		if(body == bodyA || body_type(bodyA) == CP_BODY_TYPE_STATIC) push_ptr_((void ***)&sp->cons, &sp->ncons, &sp->capcons, c);
+	}
+}
+
+/* cpSpaceDeactivateBody (cpSpaceComponent.c:81-112); the arbiters keep
+ * their contacts in their slots */
+static void space_deactivate_body_(cpSpace *sp, cpBody *body)
+{
+	ORC_ASSERT(body_type(body) == CP_BODY_TYPE_DYNAMIC, "Internal error: Attempting to deactivate a non-dynamic body.");
+	array_delete_((void **)sp->dyn, &sp->ndyn, body);
+	for(cpShape *s = body->shapeList; s; s = s->next){
+		tree_remove(sp, &sp->dynTree, s);
+		tree_insert(sp, &sp->statTree, s);
+	}
+	for(int k = body->arbList; k; k = arb_next_(sp, k, body)){
+		cpArbiter *arb = ARB_AT_(sp, k);
+		cpBody *bodyA = arb->body_a;
+		if(body == bodyA || body_type(bodyA) == CP_BODY_TYPE_STATIC){
+			/* cpSpaceUncacheArbiter (cpSpaceStep.c:223-230) */
+			amap_remove(sp, arb_key(arb->a, arb->b));
+			active_delete_(sp, k - 1);
+		}
+	}
+	for(cpConstraint *c = body->constraintList; c; c = constraint_next_(c, body)){
+		cpBody *bodyA = c->a;
+		if(body == bodyA || body_type(bodyA) == CP_BODY_TYPE_STATIC) array_delete_((void **)sp->cons, &sp->ncons, c);
+	}
+}
+
+/* cpSpaceComponent.c:120-153 */
+void cpBodyActivate(cpBody *body)
+{
+	if(body == NULL || body_type(body) != CP_BODY_TYPE_DYNAMIC) return;
+	body->idleTime = 0.0;
+	cpBody *root = body->sleepRoot;
+	if(root && cpBodyIsSleeping(root)){
+		cpSpace *sp = root->space;
+		cpBody *b = root;
+		while(b){
+			cpBody *next = b->sleepNext;
+			b->idleTime = 0.0;
+			b->sleepRoot = NULL;
+			b->sleepNext = NULL;
+			space_activate_body_(sp, b);
+			b = next;
+		}
+		array_delete_((void **)sp->sleeping, &sp->nsleeping, root);
+	}
+	cpSpace *sp = body->space;
+	if(!sp) return;
+	for(int k = body->arbList; k; k = arb_next_(sp, k, body)){
+		cpArbiter *arb = ARB_AT_(sp, k);
+		cpBody *other = (arb->body_a == body ? arb->body_b : arb->body_a);
+		if(body_type(other) != CP_BODY_TYPE_STATIC) other->idleTime = 0.0;
+	}
+}
+
+/* cpSpaceComponent.c:155-166 */
+void cpBodyActivateStatic(cpBody *body, cpShape *filter)
+{
+	ORC_ASSERT(body_type(body) == CP_BODY_TYPE_STATIC, "cpBodyActivateStatic() called on a non-static body.");
+	cpSpace *sp = body->space;
+	if(!sp) return;
+	for(int k = body->arbList; k; k = arb_next_(sp, k, body)){
+		cpArbiter *arb = ARB_AT_(sp, k);
+		if(!filter || filter == arb->a || filter == arb->b) cpBodyActivate(arb->body_a == body ? arb->body_b : arb->body_a);
+	}
+}
+
+/* FloodFillComponent with ComponentAdd (cpSpaceComponent.c:183-212) */
+static void flood_fill_(cpSpace *sp, cpBody *root, cpBody *body)
+{
+	if(body_type(body) != CP_BODY_TYPE_DYNAMIC || body->sleepRoot != NULL) return;
+	body->sleepRoot = root;
+	if(body != root){
+		body->sleepNext = root->sleepNext;
+		root->sleepNext = body;
+	}
+	for(int k = body->arbList; k; k = arb_next_(sp, k, body)){
+		cpArbiter *arb = ARB_AT_(sp, k);
+		flood_fill_(sp, root, body == arb->body_a ? arb->body_b : arb->body_a);
+	}
+	for(cpConstraint *c = body->constraintList; c; c = constraint_next_(c, body)) flood_fill_(sp, root, body == c->a ? c->b : c->a);
+}
+
+/* cpSpaceProcessComponents (cpSpaceComponent.c:224-307): idle times, the
+ * contact graph rebuilt from the arbiter list, bodies woken by contacts
+ * with kinematic or sleeping bodies, and components whose bodies have all
+ * idled past the threshold put to sleep. */
+static void process_components_(cpSpace *sp, cpFloat dt)
+{
+	int sleep = (sp->sleepTimeThreshold != ORC_INF);
+	if(sleep){
+		cpFloat dv = sp->idleSpeedThreshold;
+		cpFloat dvsq = (dv ? dv*dv : cpvlengthsq(sp->gravity)*dt*dt);
+		for(int i = 0; i < sp->ndyn; i++){
+			cpBody *body = sp->dyn[i];
+			if(body_type(body) != CP_BODY_TYPE_DYNAMIC) continue;
+			cpFloat keThreshold = (dvsq ? body->m*dvsq : 0.0);
+			body->idleTime = (cpBodyKineticEnergy(body) > keThreshold ? 0.0 : body->idleTime + dt);
+		}
+	}
+	for(int i = 0, count = sp->nactive; i < count; i++){
+		int slot = sp->active[i];
+		cpBody *a = sp->arbs[slot].body_a, *b = sp->arbs[slot].body_b;
+		if(sleep){
+			if(body_type(b) == CP_BODY_TYPE_KINEMATIC || cpBodyIsSleeping(a)) cpBodyActivate(a);
+			if(body_type(a) == CP_BODY_TYPE_KINEMATIC || cpBodyIsSleeping(b)) cpBodyActivate(b);
+		}
+		body_push_arbiter_(sp, a, slot);
+		body_push_arbiter_(sp, b, slot);
+	}
+	if(!sleep) return;
+	for(int i = 0; i < sp->ncons; i++){
+		cpBody *a = sp->cons[i]->a, *b = sp->cons[i]->b;
+		if(body_type(b) == CP_BODY_TYPE_KINEMATIC) cpBodyActivate(a);
+		if(body_type(a) == CP_BODY_TYPE_KINEMATIC) cpBodyActivate(b);
+	}
+	for(int i = 0; i < sp->ndyn;){
+		cpBody *body = sp->dyn[i];
+		if(body->sleepRoot == NULL){
+			flood_fill_(sp, body, body);
+			/* ComponentActive (cpSpaceComponent.c:214-222) */
+			int active = 0;
+			for(cpBody *o = body; o; o = o->sleepNext) if(o->idleTime < sp->sleepTimeThreshold){ active = 1; break; }
+			if(!active){
+				push_ptr_((void ***)&sp->sleeping, &sp->nsleeping, &sp->capsleeping, body);
+				for(cpBody *o = body; o; o = o->sleepNext) space_deactivate_body_(sp, o);
+				continue;
+			}
+		}
+		i++;
+		body->sleepRoot = NULL;
+		body->sleepNext = NULL;
+	}
+}
+
+/* cpSpaceUnlock (cpSpaceStep.c:68-103) without the post-step callbacks:
+ * bodies woken while the space was locked are activated */
+static void space_unlock_(cpSpace *sp)
+{
+	sp->locked--;
+	if(sp->locked) return;
+	for(int i = 0, count = sp->nroused; i < count; i++) space_activate_body_(sp, sp->roused[i]);
+	sp->nroused = 0;
+}
+
+void cpBodySleep(cpBody *body) { cpBodySleepWithGroup(body, NULL); }
+
+/* cpSpaceComponent.c:315-350 */
+void cpBodySleepWithGroup(cpBody *body, cpBody *group)
+{
+	ORC_ASSERT(body_type(body) == CP_BODY_TYPE_DYNAMIC, "Non-dynamic bodies cannot be put to sleep.");
+	cpSpace *sp = body->space;
+	ORC_ASSERT(!sp->locked, "Bodies cannot be put to sleep during a query or a call to cpSpaceStep(). Put these calls into a post-step callback.");
+	ORC_ASSERT(sp->sleepTimeThreshold < ORC_INF, "Sleeping is not enabled on the space. You cannot sleep a body without setting a sleep time threshold on the space.");
+	ORC_ASSERT(group == NULL || cpBodyIsSleeping(group), "Cannot use a non-sleeping body as a group identifier.");
+	if(cpBodyIsSleeping(body)){
+		ORC_ASSERT(body->sleepRoot == (group ? group->sleepRoot : NULL), "The body is already sleeping and it's group cannot be reassigned.");
+		return;
+	}
+	for(cpShape *s = body->shapeList; s; s = s->next) cpShapeCacheBB(s);
+	space_deactivate_body_(sp, body);
+	if(group){
+		cpBody *root = group->sleepRoot;
+		body->sleepRoot = root;
+		body->sleepNext = root->sleepNext;
+		body->idleTime = 0.0;
+		root->sleepNext = body;
+	} else {
+		body->sleepRoot = body;
+		body->sleepNext = NULL;
+		body->idleTime = 0.0;
+		push_ptr_((void ***)&sp->sleeping, &sp->nsleeping, &sp->capsleeping, body);
+	}
+	array_delete_((void **)sp->dyn, &sp->ndyn, body);
+}
+
 /* cpSpaceStep.c:292-325 */
 static void filter_arbiters(cpSpace *sp)
 {
@@ -2692,7 +3001,8 @@ static void filter_arbiters(cpSpace *sp)
 		int slot = m->slot[h];
 		cpArbiter *arb = &sp->arbs[slot];
 		cpTimestamp ticks = sp->stamp - arb->stamp;
-		if(body_type(arb->body_a) == CP_BODY_TYPE_STATIC && body_type(arb->body_b) == CP_BODY_TYPE_STATIC) continue;
+		cpBody *a = arb->body_a, *b = arb->body_b;
+		if((body_type(a) == CP_BODY_TYPE_STATIC || cpBodyIsSleeping(a)) && (body_type(b) == CP_BODY_TYPE_STATIC || cpBodyIsSleeping(b))) continue;
 		if(ticks >= 1 && arb->state != ARB_CACHED) arb->state = ARB_CACHED;
 		if(ticks >= sp->collisionPersistence){
 			arb->count = 0;
@@ -2807,7 +3117,14 @@ void cpSpaceStep(cpSpace *sp, cpFloat dt)
 	cpFloat prev_dt = sp->curr_dt;
 	sp->curr_dt = dt;
 
-	for(int i = 0; i < sp->nactive; i++) sp->arbs[sp->active[i]].state = ARB_NORMAL;
+	/* cpSpaceStep.c:351-360: the arbiters of awake bodies leave the
+	 * contact graph */
+	for(int i = 0; i < sp->nactive; i++){
+		int slot = sp->active[i];
+		cpArbiter *arb = &sp->arbs[slot];
+		arb->state = ARB_NORMAL;
+		if(!cpBodyIsSleeping(arb->body_a) && !cpBodyIsSleeping(arb->body_b)) arb_unthread_(sp, slot);
+	}
 	sp->nactive = 0;
 
 	sp->locked++;
@@ -2823,7 +3140,9 @@ void cpSpaceStep(cpSpace *sp, cpFloat dt)
 		for(int n = set->bins[i]; n >= 0; n = sp->nodes[n].binNext) cpShapeCacheBB(sp->nodes[n].obj);
 	}
 	tree_reindex_query(sp);
-	sp->locked--;
+	space_unlock_(sp);
+
+	process_components_(sp, dt);
 
 	sp->locked++;
 	filter_arbiters(sp);
@@ -2858,7 +3177,7 @@ void cpSpaceStep(cpSpace *sp, cpFloat dt)
 		cpConstraint *c = sp->cons[i];
 		if(c->postSolve) c->postSolve(c, sp);
 	}
-	sp->locked--;
+	space_unlock_(sp);
 	run_post_step_(sp);
 }
 
@@ -2930,20 +3249,20 @@ cpContactPointSet cpArbiterGetContactPointSet(const cpArbiter *arb)
 	return set;
 }
 
-/* The contact graph pushes each solved arbiter on the head of both bodies'
- * lists (cpSpaceComponent.c:170-181), so a body sees its arbiters in
- * reverse solve order; swapped is set relative to the body (cpBody.c:612-626). */
+/* cpBody.c:612-626: the body's list in the contact graph; swapped is set
+ * relative to the body */
 void cpBodyEachArbiter(cpBody *body, cpBodyArbiterIteratorFunc func, void *data)
 {
 	cpSpace *sp = body->space;
 	if(!sp) return;
-	for(int i = sp->nactive - 1; i >= 0; i--){
-		cpArbiter *arb = &sp->arbs[sp->active[i]];
-		if(arb->body_a != body && arb->body_b != body) continue;
+	for(int k = body->arbList; k;){
+		cpArbiter *arb = ARB_AT_(sp, k);
+		int next = arb_next_(sp, k, body);
 		cpBool swapped = arb->swapped;
 		arb->swapped = (body == arb->body_b);
 		func(body, arb, data);
 		arb->swapped = swapped;
+		k = next;
 	}
 }
 
