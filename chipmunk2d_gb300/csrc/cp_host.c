@@ -109,6 +109,11 @@ struct cpBody {
 	unsigned long long pullGen; /* download whose state this struct holds */
 	cpShape *shapeList;
 	cpConstraint *constraintList;
+	/* sleeping (chipmunk_structs.h:90-94): the component root and next
+	 * body; the head of the body's list in the contact graph, as an index
+	 * of the space's graph pool + 1 (0 = none) */
+	cpBody *sleepRoot, *sleepNext;
+	int arbList;
 };
 
 struct cpShape {
@@ -166,6 +171,12 @@ struct cpArbiter {
 	cpFloat e, u;
 	cpBool swapped;
 	cpgContact c[2];
+	/* contact-graph entries only: the device table key, body_a's and
+	 * body_b's list links (graph index + 1, 0 = none) and the position in
+	 * the arbiter list (-1: not on it) */
+	unsigned long long key;
+	int prevA, nextA, prevB, nextB;
+	int listPos;
 };
 
 struct cpSpace {
@@ -207,6 +218,24 @@ struct cpSpace {
 
 	cpArbiter *snap; int nsnap, capsnap; int snapValid;
 	float phaseMs[8];
+
+	/* sleeping (cpSpaceComponent.c): bodies asleep, in device order after
+	 * the dynamic array; the sleeping components' roots; bodies woken while
+	 * the space was locked */
+	cpBody **slp; int nslp, capslp;
+	cpBody **sleeping; int nsleeping, capsleeping;
+	cpBody **roused; int nroused, caproused;
+	int locked;
+	/* the contact graph, kept while sleeping is on: a pool of arbiter
+	 * records with their list links, and the arbiter list (pool indices) */
+	int graphOn, graphFresh;
+	cpArbiter *garb; int ngarb, capgarb;
+	int *gfree; int ngfree, capgfree;
+	int *glist; int nglist, capglist;
+	/* cache edits for the device (key, 1 = out of the cache, stamp) */
+	unsigned long long *sedKey; int *sedOp; unsigned *sedStamp; int nsed, capsed;
+	int sleepMutated;
+	double prevDt;
 };
 
 static void run_post_step_(cpSpace *sp);
@@ -465,12 +494,18 @@ static int d2h(void *dst, const void *src, size_t bytes)
 	return cuda_ok(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, lib_stream()), "download");
 }
 
-static int world_body_count(const cpSpace *sp) { return sp->ndyn + sp->nstat + 1; }
+/* A world's bodies on the device: the dynamic array (awake dynamic and
+ * kinematic bodies), the sleeping bodies, the static array, the space's
+ * static body. */
+static int world_body_count(const cpSpace *sp) { return sp->ndyn + sp->nslp + sp->nstat + 1; }
 
 static cpBody *world_body(cpSpace *sp, int i)
 {
 	if(i < sp->ndyn) return sp->dyn[i];
-	if(i < sp->ndyn + sp->nstat) return sp->stat[i - sp->ndyn];
+	i -= sp->ndyn;
+	if(i < sp->nslp) return sp->slp[i];
+	i -= sp->nslp;
+	if(i < sp->nstat) return sp->stat[i];
 	return &sp->staticBody;
 }
 
@@ -762,7 +797,7 @@ static DevSet *devset_build(cpSpace **spaces, int nspaces, DevSet *from)
 		W->consOff = (int)NC; W->ncons = sp->ncons;
 		/* capacities by shape slots (removed shapes keep theirs), so a set
 		 * rebuilt after removals holds at least what its predecessor held */
-		int churn = (sp->nshapes != ndynShapes + nstatShapes) || from;
+		int churn = (sp->nshapes != ndynShapes + nstatShapes) || from || sp->nslp > 0;
 		W->nodeOff = (int)NN; W->nodeCap = 2*sp->nshapes + 4;
 		W->pairOff = (int)NP; W->pairCap = 16*sp->nshapes + 256;
 		if(g_cap_pairs_per_shape || g_cap_pairs_extra >= 0)
@@ -1049,7 +1084,10 @@ static void devset_flush_space(DevSet *ds, int w)
 }
 
 /* One step of every world of the set with per-world dt. */
-static int devset_step(DevSet *ds, const double *dts, cpSpace **only)
+/* part 0: the whole step; 1: up to the arbiter list; 2: the rest of the
+ * step begun by part 1 (a single space; its set may have been rebuilt in
+ * between, so the parameters go up again without advancing the stamp). */
+static int devset_step_part(DevSet *ds, const double *dts, cpSpace **only, int part)
 {
 	cpgSet *d = &ds->d;
 	/* The bookkeeping of a step (overflow flags, level counts) is read back
@@ -1068,9 +1106,13 @@ static int devset_step(DevSet *ds, const double *dts, cpSpace **only)
 		devset_flush_space(ds, w);
 		double dt = dts[w];
 		/* cpSpaceStep.c:339-344, 384, 399, 407 */
-		sp->stamp++;
-		cpFloat prev_dt = sp->curr_dt;
-		sp->curr_dt = dt;
+		cpFloat prev_dt;
+		if(part == 2) prev_dt = sp->prevDt;
+		else {
+			sp->stamp++;
+			prev_dt = sp->prevDt = sp->curr_dt;
+			sp->curr_dt = dt;
+		}
 		if(sp->jointDt != dt){ upload_joint_bias(ds, w, dt); sp->jointDt = dt; }
 		P->dt = dt;
 		P->dt_coef = (prev_dt == 0.0 ? 0.0 : dt/prev_dt);
@@ -1124,12 +1166,14 @@ static int devset_step(DevSet *ds, const double *dts, cpSpace **only)
 	int lrc;
 	/* many-world sets launch no cooperative kernels and keep their launch
 	 * arguments from step to step: their step replays as one CUDA graph */
-	if(ds->useGraph && !timed && !d->tape.on && ds->nspaces > 1) lrc = cpg_launch_step_graph(d, mode, st, &ds->graph);
+	if(part != 0) lrc = cpg_launch_step_part(d, d, mode, st, NULL, part);
+	else if(ds->useGraph && !timed && !d->tape.on && ds->nspaces > 1) lrc = cpg_launch_step_graph(d, mode, st, &ds->graph);
 	else lrc = cpg_launch_step(d, d, mode, st, timed ? ms : NULL);
 	if(lrc != 0){
 		set_error(CP_GPU_ERR_CUDA, "step launch failed");
 		return -1;
 	}
+	if(part == 1) return 0;
 	if(g_timing) for(int w = 0; w < ds->nspaces; w++) memcpy(ds->spaces[w]->phaseMs, ms, sizeof(ms));
 	if(tuning >= 0){
 		ds->tuneMs[tuning] += (double)ms[1] + (double)ms[6];
@@ -1152,10 +1196,18 @@ static int devset_step(DevSet *ds, const double *dts, cpSpace **only)
 	return 0;
 }
 
+static int devset_step(DevSet *ds, const double *dts, cpSpace **only) { return devset_step_part(ds, dts, only, 0); }
+
+static int sleep_mode_(const cpSpace *sp);
+static int sleep_apply_edits_(cpSpace *sp);
+static void graph_start_(cpSpace *sp);
+static void graph_stop_(cpSpace *sp);
+static int sleep_sync_(cpSpace *sp, cpFloat dt);
+
 static int space_supported(cpSpace *sp)
 {
-	if(sp->sleepTimeThreshold != INF_){
-		set_error(CP_GPU_ERR_UNSUPPORTED, "sleeping (cpSpaceSetSleepTimeThreshold) is not run on the GPU");
+	if(sleep_mode_(sp) && (sp->mode != CP_GPU_SOLVER_ORDERED || (sp->dev && !sp->ownsDev))){
+		set_error(CP_GPU_ERR_UNSUPPORTED, "sleeping runs in the exact-order mode of a standalone space");
 		return 0;
 	}
 	for(int i = 0; i < sp->ndyn; i++){
@@ -1204,12 +1256,14 @@ static int space_device_ready_(cpSpace *sp)
 		}
 		devset_free(old);
 		sp->ownsDev = 1;
+		if(!sleep_apply_edits_(sp)) return 0;
 	}
 	if(!sp->dev){
 		cpSpace *one[1] = { sp };
 		DevSet *ds = devset_build(one, 1, NULL);
 		if(!ds) return 0;
 		sp->ownsDev = 1;
+		if(!sleep_apply_edits_(sp)) return 0;
 	}
 	return 1;
 }
@@ -1224,7 +1278,16 @@ void cpSpaceStep(cpSpace *sp, cpFloat dt)
 	}
 	if(!space_device_ready_(sp)) return;
 	double dts[1] = { dt };
-	devset_step(sp->dev, dts, NULL);
+	if(sleep_mode_(sp)){
+		/* cpSpaceStep.c:375: cpSpaceProcessComponents between the halves */
+		graph_start_(sp);
+		if(devset_step_part(sp->dev, dts, NULL, 1) != 0 || !sleep_sync_(sp, dt)) return;
+		devset_step_part(sp->dev, dts, NULL, 2);
+		sp->hostStale = 1; sp->consStale = 1; sp->shapesStale = 1; sp->snapValid = 0;
+	} else {
+		graph_stop_(sp);
+		devset_step(sp->dev, dts, NULL);
+	}
 	run_post_step_(sp);
 }
 
@@ -1285,6 +1348,7 @@ cpGpuSpaceState *cpGpuSpaceSaveState(cpSpace *sp)
 {
 	if(!sp){ set_error(CP_GPU_ERR_ARGUMENT, "save state: null space"); return NULL; }
 	if(sp->dev && !sp->ownsDev){ set_error(CP_GPU_ERR_UNSUPPORTED, "save state: the space belongs to a cpGpuBatch"); return NULL; }
+	if(sleep_mode_(sp)){ set_error(CP_GPU_ERR_UNSUPPORTED, "save state: sleeping keeps host state that is not saved"); return NULL; }
 	if(!space_device_ready_(sp)) return NULL;
 	DevSet *ds = sp->dev;
 	devset_flush_space(ds, sp->world);
@@ -1837,7 +1901,10 @@ int cpGpuBatchGetTuning(cpGpuBatch *b, int *out)
 int cpGpuBatchStep(cpGpuBatch *b, cpFloat dt, int steps, int use_graph)
 {
 	if(!b || b->n <= 0) return -1;
-	for(int i = 0; i < b->n; i++) if(!space_supported(b->spaces[i])) return -1;
+	for(int i = 0; i < b->n; i++){
+		if(!space_supported(b->spaces[i])) return -1;
+		if(sleep_mode_(b->spaces[i])){ set_error(CP_GPU_ERR_UNSUPPORTED, "sleeping runs in a standalone space, not in a cpGpuBatch"); return -1; }
+	}
 	if(!b->dev){
 		b->dev = devset_build(b->spaces, b->n, NULL);
 		if(!b->dev) return -1;
@@ -1862,6 +1929,7 @@ static int batch_ready(cpGpuBatch *b)
 	if(!b || b->n == 0){ set_error(CP_GPU_ERR_ARGUMENT, "empty batch"); return 0; }
 	for(int i = 0; i < b->n; i++){
 		if(!space_supported(b->spaces[i])) return 0;
+		if(sleep_mode_(b->spaces[i])){ set_error(CP_GPU_ERR_UNSUPPORTED, "the differentiable rollout does not run sleeping"); return 0; }
 		if(b->spaces[i]->mode != CP_GPU_SOLVER_ORDERED){
 			set_error(CP_GPU_ERR_UNSUPPORTED, "the differentiable rollout runs the reference-order solver");
 			return 0;
@@ -2525,8 +2593,6 @@ cpBody *cpBodyNewKinematic(void)
 }
 
 void cpBodyFree(cpBody *b) { free(b); }
-void cpBodyActivate(cpBody *b) { (void)b; }
-cpBool cpBodyIsSleeping(const cpBody *b) { (void)b; return cpFalse; }
 cpBodyType cpBodyGetType(cpBody *b) { return (cpBodyType)body_type_(b); }
 static int space_edit_ok(cpSpace *sp);
 static int array_delete_(void **arr, int *n, void *obj);
@@ -2553,6 +2619,8 @@ void cpBodySetType(cpBody *b, cpBodyType type)
 		b->w = 0.0;
 	}
 	if(!sp) return;
+	/* activated with its new type (a no-op unless it turned dynamic) */
+	if(oldType != CP_BODY_TYPE_STATIC) cpBodyActivate(b);
 	/* the body changes array (dynamic and kinematic bodies share one), and
 	 * its shapes change index: each leaves one tree and enters the other
 	 * with its cached box, in shape-list order */
@@ -2579,12 +2647,14 @@ void cpBodySetMass(cpBody *b, cpFloat m)
 {
 	ASSERT_HARD(body_type_(b) == CP_BODY_TYPE_DYNAMIC, "You cannot set the mass of kinematic or static bodies.");
 	ASSERT_HARD(0.0 <= m && m < INF_, "Mass must be positive and finite.");
+	cpBodyActivate(b);
 	wr(b); b->m = m; b->m_inv = (m == 0.0 ? INF_ : 1.0/m);
 }
 
 void cpBodySetMoment(cpBody *b, cpFloat i)
 {
 	ASSERT_HARD(i >= 0.0, "Moment of Inertia must be positive.");
+	cpBodyActivate(b);
 	wr(b); b->i = i; b->i_inv = (i == 0.0 ? INF_ : 1.0/i);
 }
 
@@ -2594,23 +2664,24 @@ cpVect cpBodyGetPosition(const cpBody *b) { rd(b); return cpTransformPoint(b->tr
 void cpBodySetPosition(cpBody *b, cpVect pos)
 {
 	/* cpBody.c:374-382 */
+	cpBodyActivate(b);
 	wr(b);
 	cpVect p = b->p = cpvadd(cpTransformVect(b->transform, b->cog), pos);
 	set_transform_(b, p, b->a);
 }
 
 cpVect cpBodyGetCenterOfGravity(const cpBody *b) { return b->cog; }
-void cpBodySetCenterOfGravity(cpBody *b, cpVect cog) { wr(b); b->cog = cog; }
+void cpBodySetCenterOfGravity(cpBody *b, cpVect cog) { cpBodyActivate(b); wr(b); b->cog = cog; }
 cpVect cpBodyGetVelocity(const cpBody *b) { rd(b); return b->v; }
-void cpBodySetVelocity(cpBody *b, cpVect v) { wr(b); b->v = v; }
+void cpBodySetVelocity(cpBody *b, cpVect v) { cpBodyActivate(b); wr(b); b->v = v; }
 cpVect cpBodyGetForce(const cpBody *b) { rd(b); return b->f; }
-void cpBodySetForce(cpBody *b, cpVect f) { wr(b); b->f = f; }
+void cpBodySetForce(cpBody *b, cpVect f) { cpBodyActivate(b); wr(b); b->f = f; }
 cpFloat cpBodyGetAngle(const cpBody *b) { rd(b); return b->a; }
-void cpBodySetAngle(cpBody *b, cpFloat a) { wr(b); b->a = a; set_transform_(b, b->p, a); }
+void cpBodySetAngle(cpBody *b, cpFloat a) { cpBodyActivate(b); wr(b); b->a = a; set_transform_(b, b->p, a); }
 cpFloat cpBodyGetAngularVelocity(const cpBody *b) { rd(b); return b->w; }
-void cpBodySetAngularVelocity(cpBody *b, cpFloat w) { wr(b); b->w = w; }
+void cpBodySetAngularVelocity(cpBody *b, cpFloat w) { cpBodyActivate(b); wr(b); b->w = w; }
 cpFloat cpBodyGetTorque(const cpBody *b) { rd(b); return b->t; }
-void cpBodySetTorque(cpBody *b, cpFloat t) { wr(b); b->t = t; }
+void cpBodySetTorque(cpBody *b, cpFloat t) { cpBodyActivate(b); wr(b); b->t = t; }
 cpDataPointer cpBodyGetUserData(const cpBody *b) { return b->userData; }
 void cpBodySetUserData(cpBody *b, cpDataPointer d) { b->userData = d; }
 void cpBodySetVelocityUpdateFunc(cpBody *b, cpBodyVelocityFunc f) { b->velocity_func = f; }
@@ -2620,6 +2691,7 @@ cpVect cpBodyWorldToLocal(const cpBody *b, const cpVect p) { rd(b); return cpTra
 
 void cpBodyApplyForceAtWorldPoint(cpBody *b, cpVect force, cpVect point)
 {
+	cpBodyActivate(b);
 	wr(b);
 	b->f = cpvadd(b->f, force);
 	cpVect r = cpvsub(point, cpTransformPoint(b->transform, b->cog));
@@ -2634,6 +2706,7 @@ void cpBodyApplyForceAtLocalPoint(cpBody *b, cpVect force, cpVect point)
 
 void cpBodyApplyImpulseAtWorldPoint(cpBody *b, cpVect j, cpVect point)
 {
+	cpBodyActivate(b);
 	wr(b);
 	cpVect r = cpvsub(point, cpTransformPoint(b->transform, b->cog));
 	b->v = cpvadd(b->v, cpvmult(j, b->m_inv));
@@ -2905,12 +2978,12 @@ cpShape *cpBoxShapeNew(cpBody *body, cpFloat width, cpFloat height, cpFloat radi
 void cpShapeFree(cpShape *s) { if(s){ free(s->lv); free(s); } }
 void cpShapeDestroy(cpShape *s);
 
-static inline cpShape *swr(cpShape *s) { if(s->space){ s->space->shapeDirty = 1; s->space->editGen++; } return s; }
+static inline cpShape *swr(cpShape *s) { cpBodyActivate(s->body); if(s->space){ s->space->shapeDirty = 1; s->space->editGen++; } return s; }
 
 cpSpace *cpShapeGetSpace(const cpShape *s) { return s->space; }
 cpBody *cpShapeGetBody(const cpShape *s) { return s->body; }
 cpFloat cpShapeGetMass(cpShape *s) { return s->mass_m; }
-void cpShapeSetMass(cpShape *s, cpFloat mass) { s->mass_m = mass; accumulate_mass_(s->body); }
+void cpShapeSetMass(cpShape *s, cpFloat mass) { cpBodyActivate(s->body); s->mass_m = mass; accumulate_mass_(s->body); }
 cpFloat cpShapeGetDensity(cpShape *s) { return s->mass_m/s->mass_area; }
 void cpShapeSetDensity(cpShape *s, cpFloat d) { cpShapeSetMass(s, d*s->mass_area); }
 cpFloat cpShapeGetMoment(cpShape *s) { return s->mass_m*s->mass_i; }
@@ -2927,7 +3000,7 @@ void cpShapeSetSurfaceVelocity(cpShape *s, cpVect v) { swr(s)->surfaceV = v; }
 cpDataPointer cpShapeGetUserData(const cpShape *s) { return s->userData; }
 void cpShapeSetUserData(cpShape *s, cpDataPointer d) { s->userData = d; }
 cpCollisionType cpShapeGetCollisionType(const cpShape *s) { return s->ctype; }
-void cpShapeSetCollisionType(cpShape *s, cpCollisionType t) { s->ctype = t; }
+void cpShapeSetCollisionType(cpShape *s, cpCollisionType t) { cpBodyActivate(s->body); s->ctype = t; }
 cpShapeFilter cpShapeGetFilter(const cpShape *s) { return s->filter; }
 void cpShapeSetFilter(cpShape *s, cpShapeFilter f) { swr(s)->filter = f; }
 cpVect cpCircleShapeGetOffset(const cpShape *s) { return s->c; }
@@ -3009,8 +3082,12 @@ static void joints_pull_(cpSpace *sp)
 
 static void cons_pull_(cpConstraint *c) { if(c->space) joints_pull_(c->space); }
 
+/* A joint setter's write access; the setters wake both bodies
+ * (cpConstraintActivateBodies, chipmunk_private.h:165-170). */
 static inline cpConstraint *cwr(cpConstraint *c)
 {
+	cpBodyActivate(c->a);
+	cpBodyActivate(c->b);
 	if(c->space){
 		joints_pull_(c->space);   /* keep the device-side accumulators */
 		c->space->consDirty = 1;
@@ -3033,6 +3110,8 @@ cpBool cpConstraintGetCollideBodies(const cpConstraint *c) { return c->collideBo
 void cpConstraintSetCollideBodies(cpConstraint *c, cpBool v)
 {
 	ASSERT_HARD(!c->space || !c->space->dev, "collideBodies must be set before the space is first stepped");
+	cpBodyActivate(c->a);
+	cpBodyActivate(c->b);
 	c->collideBodies = v;
 }
 void cpConstraintSetPreSolveFunc(cpConstraint *c, cpConstraintPreSolveFunc f) { c->preSolve = f; }
@@ -3217,6 +3296,20 @@ void cpSpaceDestroy(cpSpace *sp)
 		cudaStreamSynchronize(lib_stream());
 		devset_free(sp->dev);
 	}
+	/* cpSpace.c:186-191: every body is woken; here the sleeping ones are
+	 * only let go of their components */
+	for(int i = 0; i < sp->nslp; i++){
+		cpBody *b = sp->slp[i];
+		b->sleepRoot = b->sleepNext = NULL;
+		b->idleTime = 0.0;
+		if(b->space == sp) b->space = NULL;
+	}
+	graph_stop_(sp);
+	free(sp->slp); free(sp->sleeping); free(sp->roused); free(sp->garb); free(sp->gfree); free(sp->glist);
+	free(sp->sedKey); free(sp->sedOp); free(sp->sedStamp);
+	sp->slp = sp->sleeping = sp->roused = NULL; sp->garb = NULL; sp->gfree = sp->glist = NULL;
+	sp->sedKey = NULL; sp->sedOp = NULL; sp->sedStamp = NULL;
+	sp->nslp = sp->nsleeping = sp->nroused = 0;
 	for(int i = 0; i < sp->ndyn; i++) if(sp->dyn[i]->space == sp) sp->dyn[i]->space = NULL;
 	for(int i = 0; i < sp->nstat; i++) if(sp->stat[i]->space == sp) sp->stat[i]->space = NULL;
 	for(int i = 0; i < sp->nshapes; i++) if(sp->shapes[i] && sp->shapes[i]->space == sp) sp->shapes[i]->space = NULL;
@@ -3319,13 +3412,24 @@ void cpHastySpaceStep(cpSpace *sp, cpFloat dt) { cpSpaceStep(sp, dt); }
 int cpSpaceGetIterations(const cpSpace *sp) { return sp->iterations; }
 void cpSpaceSetIterations(cpSpace *sp, int it) { ASSERT_HARD(it > 0, "Iterations must be positive and non-zero."); sp->iterations = it; }
 cpVect cpSpaceGetGravity(const cpSpace *sp) { return sp->gravity; }
-void cpSpaceSetGravity(cpSpace *sp, cpVect g) { sp->gravity = g; }
+/* cpSpace.c:253-263: the sleeping components are woken as the reference
+ * wakes them, walking the array that each activation shrinks */
+void cpSpaceSetGravity(cpSpace *sp, cpVect g)
+{
+	sp->gravity = g;
+	for(int i = 0; i < sp->nsleeping; i++) cpBodyActivate(sp->sleeping[i]);
+}
 cpFloat cpSpaceGetDamping(const cpSpace *sp) { return sp->damping; }
 void cpSpaceSetDamping(cpSpace *sp, cpFloat d) { ASSERT_HARD(d >= 0.0, "Damping must be positive."); sp->damping = d; }
 cpFloat cpSpaceGetIdleSpeedThreshold(const cpSpace *sp) { return sp->idleSpeedThreshold; }
 void cpSpaceSetIdleSpeedThreshold(cpSpace *sp, cpFloat v) { sp->idleSpeedThreshold = v; }
 cpFloat cpSpaceGetSleepTimeThreshold(const cpSpace *sp) { return sp->sleepTimeThreshold; }
-void cpSpaceSetSleepTimeThreshold(cpSpace *sp, cpFloat t) { sp->sleepTimeThreshold = t; }
+void cpSpaceSetSleepTimeThreshold(cpSpace *sp, cpFloat t)
+{
+	sp->sleepTimeThreshold = t;
+	/* the contact graph is kept from now on */
+	if(t != INF_) graph_start_(sp);
+}
 cpFloat cpSpaceGetCollisionSlop(const cpSpace *sp) { return sp->collisionSlop; }
 void cpSpaceSetCollisionSlop(cpSpace *sp, cpFloat v) { sp->collisionSlop = v; }
 cpFloat cpSpaceGetCollisionBias(const cpSpace *sp) { return sp->collisionBias; }
@@ -3408,6 +3512,504 @@ static void record_op_(cpSpace *sp, int kind, cpShape *s, int isStatic)
 	}
 }
 
+/* ====================================================================
+ * Sleeping and the contact graph (src/cpSpaceComponent.c)
+ *
+ * While sleeping is on (a finite sleep time threshold, or bodies still
+ * asleep) a step stops once its arbiter list is built.  The host reads
+ * the list and the bodies, rebuilds the contact graph and runs
+ * cpSpaceProcessComponents on its own objects: idle times, bodies woken
+ * by contacts, components put to sleep.  A step where no body wakes or
+ * falls asleep goes straight on to the solve.  A step where some do edits
+ * the host's arrays as the reference does (the dynamic and constraint
+ * arrays, the arbiter list, the shapes' indices), rebuilds the device set
+ * with the index edits replayed, marks the arbiters that left or rejoined
+ * the cache, writes the new arbiter list, and then solves.  A sleeping
+ * body stays on the device past the dynamic array, so it is neither
+ * integrated nor re-indexed; its shapes sit in the static index.
+ * ==================================================================== */
+static int sleep_mode_(const cpSpace *sp) { return sp->sleepTimeThreshold != INF_ || sp->nsleeping > 0; }
+
+/* the device table's key of a shape pair (world 0) */
+static inline unsigned long long garb_key_(int a, int b)
+{
+	unsigned long long lo = (unsigned long long)(a < b ? a : b), hi = (unsigned long long)(a < b ? b : a);
+	return ((lo << 21) | hi) + 2ull;
+}
+
+#define GARB_AT_(sp, k) (&(sp)->garb[(k) - 1])   /* k: pool index + 1 */
+
+static int garb_alloc_(cpSpace *sp)
+{
+	int g;
+	if(sp->ngfree > 0) g = sp->gfree[--sp->ngfree];
+	else {
+		if(sp->ngarb == sp->capgarb){
+			sp->capgarb = sp->capgarb ? 2*sp->capgarb : 256;
+			sp->garb = (cpArbiter *)realloc(sp->garb, sizeof(cpArbiter)*(size_t)sp->capgarb);
+		}
+		g = sp->ngarb++;
+	}
+	memset(&sp->garb[g], 0, sizeof(cpArbiter));
+	sp->garb[g].listPos = -1;
+	return g;
+}
+
+static void garb_release_(cpSpace *sp, int g)
+{
+	if(sp->ngfree == sp->capgfree){
+		sp->capgfree = sp->capgfree ? 2*sp->capgfree : 256;
+		sp->gfree = (int *)realloc(sp->gfree, sizeof(int)*(size_t)sp->capgfree);
+	}
+	sp->garb[g].a = sp->garb[g].b = NULL;
+	sp->gfree[sp->ngfree++] = g;
+}
+
+/* cpArbiterThreadForBody (chipmunk_private.h:178-181) */
+static int *gprev_(cpArbiter *arb, const cpBody *body) { return (arb->body_a == body) ? &arb->prevA : &arb->prevB; }
+static int *gnext_(cpArbiter *arb, const cpBody *body) { return (arb->body_a == body) ? &arb->nextA : &arb->nextB; }
+static int garb_next_(cpSpace *sp, int k, const cpBody *body) { return *gnext_(GARB_AT_(sp, k), body); }
+
+/* cpBodyPushArbiter (cpSpaceComponent.c:168-181) */
+static void gpush_(cpSpace *sp, cpBody *body, int g)
+{
+	int next = body->arbList;
+	*gnext_(&sp->garb[g], body) = next;
+	if(next) *gprev_(GARB_AT_(sp, next), body) = g + 1;
+	body->arbList = g + 1;
+}
+
+/* unthreadHelper / cpArbiterUnthread (cpArbiter.c:222-247) */
+static void gunthread_body_(cpSpace *sp, int g, cpBody *body)
+{
+	cpArbiter *arb = &sp->garb[g];
+	int prev = *gprev_(arb, body), next = *gnext_(arb, body);
+	if(prev) *gnext_(GARB_AT_(sp, prev), body) = next;
+	else if(body->arbList == g + 1) body->arbList = next;
+	if(next) *gprev_(GARB_AT_(sp, next), body) = prev;
+	*gprev_(arb, body) = 0;
+	*gnext_(arb, body) = 0;
+}
+
+static void gunthread_(cpSpace *sp, int g)
+{
+	gunthread_body_(sp, g, sp->garb[g].body_a);
+	gunthread_body_(sp, g, sp->garb[g].body_b);
+}
+
+static int gthreaded_(const cpSpace *sp, int g)
+{
+	const cpArbiter *arb = &sp->garb[g];
+	return arb->prevA || arb->nextA || arb->prevB || arb->nextB ||
+		arb->body_a->arbList == g + 1 || arb->body_b->arbList == g + 1;
+}
+
+static void glist_push_(cpSpace *sp, int g)
+{
+	if(sp->nglist == sp->capglist){
+		sp->capglist = sp->capglist ? 2*sp->capglist : 256;
+		sp->glist = (int *)realloc(sp->glist, sizeof(int)*(size_t)sp->capglist);
+	}
+	sp->garb[g].listPos = sp->nglist;
+	sp->glist[sp->nglist++] = g;
+}
+
+/* cpArrayDeleteObj (cpArray.c:76-88) on the arbiter list */
+static void glist_delete_(cpSpace *sp, int g)
+{
+	int i = sp->garb[g].listPos;
+	if(i < 0) return;
+	int last = sp->glist[--sp->nglist];
+	sp->glist[i] = last;
+	sp->garb[last].listPos = i;
+	sp->garb[g].listPos = -1;
+}
+
+/* a device arbiter record into a graph entry (links kept) */
+static void garb_fill_(cpSpace *sp, cpArbiter *arb, const cpgArb *g)
+{
+	arb->a = sp->shapes[g->a]; arb->b = sp->shapes[g->b];
+	arb->body_a = arb->a->body; arb->body_b = arb->b->body;
+	arb->count = g->count; arb->state = g->state;
+	arb->n = cpv(g->nx, g->ny); arb->surface_vr = cpv(g->svx, g->svy);
+	arb->e = g->e; arb->u = g->u; arb->swapped = cpFalse;
+	arb->c[0] = g->c[0]; arb->c[1] = g->c[1];
+	arb->key = garb_key_(g->a, g->b);
+}
+
+/* The device's arbiter list (n records), or NULL. */
+static cpgArb *gather_list_(cpSpace *sp, int *count)
+{
+	DevSet *ds = sp->dev;
+	cpgTree T;
+	*count = 0;
+	if(!d2h(&T, ds->d.tree + sp->world, sizeof(cpgTree)) || !cuda_ok(cudaStreamSynchronize(lib_stream()), "list")) return NULL;
+	int n = T.narb;
+	if(n > ds->gatherCap){
+		if(ds->gather) cudaFree(ds->gather);
+		ds->gatherCap = n + n/2 + 64;
+		if(!cuda_ok(cudaMalloc((void **)&ds->gather, sizeof(cpgArb)*(size_t)ds->gatherCap), "gather")){ ds->gatherCap = 0; ds->gather = NULL; return NULL; }
+	}
+	cpgArb *host = HALLOC(cpgArb, n);
+	if(n > 0){
+		cpg_launch_gather_arbs(&ds->d, sp->world, ds->gather, n, lib_stream());
+		d2h(host, ds->gather, sizeof(cpgArb)*(size_t)n);
+		if(!cuda_ok(cudaStreamSynchronize(lib_stream()), "list")){ free(host); return NULL; }
+	}
+	*count = n;
+	return host;
+}
+
+/* The graph entries of the arbiter list brought to the device's records
+ * (after a solve: accumulated impulses for cpBodyEachArbiter). */
+static void graph_refresh_(cpSpace *sp)
+{
+	if(sp->graphFresh || !sp->dev || sp->structDirty || !sp->ownsDev) return;
+	int n = 0;
+	cpgArb *recs = gather_list_(sp, &n);
+	if(!recs) return;
+	for(int i = 0; i < n && i < sp->nglist; i++){
+		cpArbiter *arb = &sp->garb[sp->glist[i]];
+		unsigned long long key = arb->key;
+		int pa = arb->prevA, na = arb->nextA, pb = arb->prevB, nb = arb->nextB, lp = arb->listPos;
+		garb_fill_(sp, arb, &recs[i]);
+		arb->key = key; arb->prevA = pa; arb->nextA = na; arb->prevB = pb; arb->nextB = nb; arb->listPos = lp;
+	}
+	free(recs);
+	sp->graphFresh = 1;
+}
+
+/* The graph starts from the last step's list, threaded in list order as
+ * cpSpaceProcessComponents threads it on every step. */
+static void graph_start_(cpSpace *sp)
+{
+	if(sp->graphOn) return;
+	sp->graphOn = 1;
+	sp->graphFresh = 1;
+	if(!sp->dev || !sp->ownsDev) return;
+	int n = 0;
+	cpgArb *recs = gather_list_(sp, &n);
+	if(!recs) return;
+	for(int i = 0; i < n; i++){
+		const cpgArb *r = &recs[i];
+		if(r->a < 0 || r->a >= sp->nshapes || r->b < 0 || r->b >= sp->nshapes || !sp->shapes[r->a] || !sp->shapes[r->b]) continue;
+		int g = garb_alloc_(sp);
+		garb_fill_(sp, &sp->garb[g], r);
+		glist_push_(sp, g);
+		gpush_(sp, sp->garb[g].body_a, g);
+		gpush_(sp, sp->garb[g].body_b, g);
+	}
+	free(recs);
+}
+
+static void graph_stop_(cpSpace *sp)
+{
+	if(!sp->graphOn) return;
+	for(int g = 0; g < sp->ngarb; g++){
+		cpArbiter *arb = &sp->garb[g];
+		if(arb->a){ arb->body_a->arbList = 0; arb->body_b->arbList = 0; }
+	}
+	sp->ngarb = sp->ngfree = sp->nglist = sp->nsed = 0;
+	sp->graphOn = 0;
+}
+
+static void sed_push_(cpSpace *sp, unsigned long long key, int op)
+{
+	if(sp->nsed == sp->capsed){
+		sp->capsed = sp->capsed ? 2*sp->capsed : 64;
+		sp->sedKey = (unsigned long long *)realloc(sp->sedKey, sizeof(unsigned long long)*(size_t)sp->capsed);
+		sp->sedOp = (int *)realloc(sp->sedOp, sizeof(int)*(size_t)sp->capsed);
+		sp->sedStamp = (unsigned *)realloc(sp->sedStamp, sizeof(unsigned)*(size_t)sp->capsed);
+	}
+	sp->sedKey[sp->nsed] = key; sp->sedOp[sp->nsed] = op; sp->sedStamp[sp->nsed] = (unsigned)sp->stamp;
+	sp->nsed++;
+}
+
+/* After a rebuild: the cache edits in call order and the arbiter list. */
+static int sleep_apply_edits_(cpSpace *sp)
+{
+	if(!sp->graphOn || !sp->dev) return 1;
+	DevSet *ds = sp->dev;
+	size_t kb = align256(sizeof(unsigned long long)*(size_t)(sp->nsed + 1));
+	size_t ob = align256(sizeof(int)*(size_t)(sp->nsed + 1));
+	size_t sb = align256(sizeof(unsigned)*(size_t)(sp->nsed + 1));
+	size_t lb = align256(sizeof(unsigned long long)*(size_t)(sp->nglist + 1));
+	size_t need = kb + ob + sb + lb;
+	if(ds->qbytes < need){
+		if(ds->qbuf) cudaFree(ds->qbuf);
+		ds->qbuf = NULL; ds->qbytes = 0;
+		if(!cuda_ok(cudaMalloc(&ds->qbuf, need), "cudaMalloc sleeping edits")) return 0;
+		ds->qbytes = need;
+	}
+	char *base = (char *)ds->qbuf;
+	unsigned long long *lkeys = HALLOC(unsigned long long, sp->nglist);
+	for(int i = 0; i < sp->nglist; i++) lkeys[i] = sp->garb[sp->glist[i]].key;
+	int ok = 1;
+	if(sp->nsed > 0){
+		ok &= h2d(base, sp->sedKey, sizeof(unsigned long long)*(size_t)sp->nsed);
+		ok &= h2d(base + kb, sp->sedOp, sizeof(int)*(size_t)sp->nsed);
+		ok &= h2d(base + kb + ob, sp->sedStamp, sizeof(unsigned)*(size_t)sp->nsed);
+	}
+	if(sp->nglist > 0) ok &= h2d(base + kb + ob + sb, lkeys, sizeof(unsigned long long)*(size_t)sp->nglist);
+	ok &= cpg_launch_sleep_edits(&ds->d, (const unsigned long long *)base, (const int *)(base + kb), (const unsigned *)(base + kb + ob),
+	                             sp->nsed, (const unsigned long long *)(base + kb + ob + sb), sp->nglist, lib_stream()) == 0;
+	/* the pageable copies above must finish before lkeys goes */
+	ok &= cuda_ok(cudaStreamSynchronize(lib_stream()), "sleeping edits");
+	free(lkeys);
+	sp->nsed = 0;
+	return ok;
+}
+
+/* Before the first array edit of a wake or a sleep: the state comes home
+ * (space_detach), so the next step or query rebuilds the set. */
+static void sleep_mutate_(cpSpace *sp)
+{
+	space_detach(sp);
+	if(sp->dev) sp->structDirty = 1;
+	sp->sleepMutated = 1;
+	sp->snapValid = 0;
+}
+
+static void space_unlock_(cpSpace *sp);
+
+/* cpSpaceActivateBody (cpSpaceComponent.c:28-79) */
+static void space_activate_body_(cpSpace *sp, cpBody *body)
+{
+	if(sp->locked){
+		for(int i = 0; i < sp->nroused; i++) if(sp->roused[i] == body) return;
+		push_((void ***)&sp->roused, &sp->nroused, &sp->caproused, body);
+		return;
+	}
+	sleep_mutate_(sp);
+	array_delete_((void **)sp->slp, &sp->nslp, body);
+	push_((void ***)&sp->dyn, &sp->ndyn, &sp->capdyn, body);
+	for(cpShape *s = body->shapeList; s; s = s->next){
+		record_op_(sp, CPG_OP_REMOVE, s, 1);
+		record_op_(sp, CPG_OP_INSERT, s, 0);
+	}
+	for(int k = body->arbList; k; k = garb_next_(sp, k, body)){
+		cpArbiter *arb = GARB_AT_(sp, k);
+		if(body == arb->body_a || body_type_(arb->body_a) == CP_BODY_TYPE_STATIC){
+			sed_push_(sp, arb->key, 0);
+			glist_push_(sp, k - 1);
+		}
+	}
+	for(cpConstraint *c = body->constraintList; c; c = cons_next_(c, body)){
+		if(body == c->a || body_type_(c->a) == CP_BODY_TYPE_STATIC){
+			c->index = sp->ncons;
+			push_((void ***)&sp->cons, &sp->ncons, &sp->capcons, c);
+		}
+	}
+}
+
+/* cpSpaceDeactivateBody (cpSpaceComponent.c:81-112) */
+static void space_deactivate_body_(cpSpace *sp, cpBody *body)
+{
+	sleep_mutate_(sp);
+	array_delete_((void **)sp->dyn, &sp->ndyn, body);
+	push_((void ***)&sp->slp, &sp->nslp, &sp->capslp, body);
+	for(cpShape *s = body->shapeList; s; s = s->next){
+		record_op_(sp, CPG_OP_REMOVE, s, 0);
+		record_op_(sp, CPG_OP_INSERT, s, 1);
+	}
+	for(int k = body->arbList; k; k = garb_next_(sp, k, body)){
+		cpArbiter *arb = GARB_AT_(sp, k);
+		if(body == arb->body_a || body_type_(arb->body_a) == CP_BODY_TYPE_STATIC){
+			sed_push_(sp, arb->key, 1);
+			glist_delete_(sp, k - 1);
+		}
+	}
+	for(cpConstraint *c = body->constraintList; c; c = cons_next_(c, body)){
+		if(body == c->a || body_type_(c->a) == CP_BODY_TYPE_STATIC){
+			int i = array_delete_((void **)sp->cons, &sp->ncons, c);
+			if(i >= 0 && i < sp->ncons) sp->cons[i]->index = i;
+		}
+	}
+}
+
+cpBool cpBodyIsSleeping(const cpBody *b) { return b->sleepRoot != NULL; }
+
+/* cpSpaceComponent.c:120-153 */
+void cpBodyActivate(cpBody *body)
+{
+	if(body == NULL || body_type_(body) != CP_BODY_TYPE_DYNAMIC) return;
+	body->idleTime = 0.0;
+	cpBody *root = body->sleepRoot;
+	if(root && cpBodyIsSleeping(root)){
+		cpSpace *sp = root->space;
+		cpBody *b = root;
+		while(b){
+			cpBody *next = b->sleepNext;
+			b->idleTime = 0.0;
+			b->sleepRoot = NULL;
+			b->sleepNext = NULL;
+			space_activate_body_(sp, b);
+			b = next;
+		}
+		array_delete_((void **)sp->sleeping, &sp->nsleeping, root);
+	}
+	cpSpace *sp = body->space;
+	if(!sp || !sp->graphOn) return;
+	for(int k = body->arbList; k; k = garb_next_(sp, k, body)){
+		cpArbiter *arb = GARB_AT_(sp, k);
+		cpBody *other = (arb->body_a == body ? arb->body_b : arb->body_a);
+		if(body_type_(other) != CP_BODY_TYPE_STATIC) other->idleTime = 0.0;
+	}
+}
+
+/* cpSpaceComponent.c:155-166 */
+void cpBodyActivateStatic(cpBody *body, cpShape *filter)
+{
+	ASSERT_HARD(body_type_(body) == CP_BODY_TYPE_STATIC, "cpBodyActivateStatic() called on a non-static body.");
+	cpSpace *sp = body->space;
+	if(!sp || !sp->graphOn) return;
+	for(int k = body->arbList; k; k = garb_next_(sp, k, body)){
+		cpArbiter *arb = GARB_AT_(sp, k);
+		if(!filter || filter == arb->a || filter == arb->b) cpBodyActivate(arb->body_a == body ? arb->body_b : arb->body_a);
+	}
+}
+
+/* FloodFillComponent with ComponentAdd (cpSpaceComponent.c:183-212) */
+static void flood_fill_(cpSpace *sp, cpBody *root, cpBody *body)
+{
+	if(body_type_(body) != CP_BODY_TYPE_DYNAMIC || body->sleepRoot != NULL) return;
+	body->sleepRoot = root;
+	if(body != root){
+		body->sleepNext = root->sleepNext;
+		root->sleepNext = body;
+	}
+	for(int k = body->arbList; k; k = garb_next_(sp, k, body)){
+		cpArbiter *arb = GARB_AT_(sp, k);
+		flood_fill_(sp, root, body == arb->body_a ? arb->body_b : arb->body_a);
+	}
+	for(cpConstraint *c = body->constraintList; c; c = cons_next_(c, body)) flood_fill_(sp, root, body == c->a ? c->b : c->a);
+}
+
+/* cpSpaceProcessComponents (cpSpaceComponent.c:224-307) on the host's
+ * objects; the bodies hold the state of this step's position update. */
+static void process_components_(cpSpace *sp, cpFloat dt)
+{
+	int sleep = (sp->sleepTimeThreshold != INF_);
+	if(sleep){
+		cpFloat dv = sp->idleSpeedThreshold;
+		cpFloat dvsq = (dv ? dv*dv : cpvlengthsq(sp->gravity)*dt*dt);
+		for(int i = 0; i < sp->ndyn; i++){
+			cpBody *body = sp->dyn[i];
+			if(body_type_(body) != CP_BODY_TYPE_DYNAMIC) continue;
+			cpFloat keThreshold = (dvsq ? body->m*dvsq : 0.0);
+			/* cpBodyKineticEnergy (cpBody.c:581-588) */
+			cpFloat vsq = cpvdot(body->v, body->v), wsq = body->w*body->w;
+			cpFloat ke = (vsq ? vsq*body->m : 0.0) + (wsq ? wsq*body->i : 0.0);
+			body->idleTime = (ke > keThreshold ? 0.0 : body->idleTime + dt);
+		}
+	}
+	for(int i = 0, count = sp->nglist; i < count; i++){
+		int g = sp->glist[i];
+		cpBody *a = sp->garb[g].body_a, *b = sp->garb[g].body_b;
+		if(sleep){
+			if(body_type_(b) == CP_BODY_TYPE_KINEMATIC || cpBodyIsSleeping(a)) cpBodyActivate(a);
+			if(body_type_(a) == CP_BODY_TYPE_KINEMATIC || cpBodyIsSleeping(b)) cpBodyActivate(b);
+		}
+		gpush_(sp, a, g);
+		gpush_(sp, b, g);
+	}
+	if(!sleep) return;
+	for(int i = 0; i < sp->ncons; i++){
+		cpBody *a = sp->cons[i]->a, *b = sp->cons[i]->b;
+		if(body_type_(b) == CP_BODY_TYPE_KINEMATIC) cpBodyActivate(a);
+		if(body_type_(a) == CP_BODY_TYPE_KINEMATIC) cpBodyActivate(b);
+	}
+	for(int i = 0; i < sp->ndyn;){
+		cpBody *body = sp->dyn[i];
+		if(body->sleepRoot == NULL){
+			flood_fill_(sp, body, body);
+			/* ComponentActive (cpSpaceComponent.c:214-222) */
+			int active = 0;
+			for(cpBody *o = body; o; o = o->sleepNext) if(o->idleTime < sp->sleepTimeThreshold){ active = 1; break; }
+			if(!active){
+				push_((void ***)&sp->sleeping, &sp->nsleeping, &sp->capsleeping, body);
+				for(cpBody *o = body; o; o = o->sleepNext) space_deactivate_body_(sp, o);
+				continue;
+			}
+		}
+		i++;
+		body->sleepRoot = NULL;
+		body->sleepNext = NULL;
+	}
+}
+
+/* The host half of a sleeping step, between the device's two halves:
+ * cpSpaceStep.c:351-360 (the last list leaves the graph) and :375. */
+static int sleep_sync_(cpSpace *sp, cpFloat dt)
+{
+	int n = 0;
+	cpgArb *recs = gather_list_(sp, &n);
+	if(!recs) return 0;
+	space_pull(sp);
+	for(int i = 0; i < sp->nglist; i++){
+		int g = sp->glist[i];
+		cpArbiter *arb = &sp->garb[g];
+		arb->listPos = -1;
+		if(!cpBodyIsSleeping(arb->body_a) && !cpBodyIsSleeping(arb->body_b)) gunthread_(sp, g);
+	}
+	for(int i = 0; i < sp->nglist; i++) if(!gthreaded_(sp, sp->glist[i])) garb_release_(sp, sp->glist[i]);
+	sp->nglist = 0;
+	for(int i = 0; i < n; i++){
+		int g = garb_alloc_(sp);
+		garb_fill_(sp, &sp->garb[g], &recs[i]);
+		glist_push_(sp, g);
+	}
+	free(recs);
+	sp->sleepMutated = 0;
+	process_components_(sp, dt);
+	sp->graphFresh = 0;
+	if(sp->sleepMutated && !space_device_ready_(sp)) return 0;
+	return 1;
+}
+
+/* cpSpaceUnlock (cpSpaceStep.c:68-103): bodies woken while the space was
+ * locked are activated */
+static void space_unlock_(cpSpace *sp)
+{
+	sp->locked--;
+	if(sp->locked) return;
+	for(int i = 0, count = sp->nroused; i < count; i++) space_activate_body_(sp, sp->roused[i]);
+	sp->nroused = 0;
+}
+
+void cpBodySleep(cpBody *body) { cpBodySleepWithGroup(body, NULL); }
+
+/* cpSpaceComponent.c:315-350 */
+void cpBodySleepWithGroup(cpBody *body, cpBody *group)
+{
+	ASSERT_HARD(body_type_(body) == CP_BODY_TYPE_DYNAMIC, "Non-dynamic bodies cannot be put to sleep.");
+	cpSpace *sp = body->space;
+	ASSERT_HARD(!sp->locked, "Bodies cannot be put to sleep during a query or a call to cpSpaceStep(). Put these calls into a post-step callback.");
+	ASSERT_HARD(sp->sleepTimeThreshold < INF_, "Sleeping is not enabled on the space. You cannot sleep a body without setting a sleep time threshold on the space.");
+	ASSERT_HARD(group == NULL || cpBodyIsSleeping(group), "Cannot use a non-sleeping body as a group identifier.");
+	if(cpBodyIsSleeping(body)){
+		ASSERT_HARD(body->sleepRoot == (group ? group->sleepRoot : NULL), "The body is already sleeping and it's group cannot be reassigned.");
+		return;
+	}
+	if(!space_edit_ok(sp)) return;
+	for(cpShape *s = body->shapeList; s; s = s->next) cpShapeCacheBB(s);
+	space_deactivate_body_(sp, body);
+	if(group){
+		cpBody *root = group->sleepRoot;
+		body->sleepRoot = root;
+		body->sleepNext = root->sleepNext;
+		body->idleTime = 0.0;
+		root->sleepNext = body;
+	} else {
+		body->sleepRoot = body;
+		body->sleepNext = NULL;
+		body->idleTime = 0.0;
+		push_((void ***)&sp->sleeping, &sp->nsleeping, &sp->capsleeping, body);
+	}
+	/* cpSpaceComponent.c:349: a second delete, of a body no longer there */
+	array_delete_((void **)sp->dyn, &sp->ndyn, body);
+}
+
 /* cpSpace.c:662-678: the shape's cache brought to its body's transform,
  * then its leaf re-indexed (cpBBTreeReindexObject, replayed on the device
  * before the next step or query with the box and velocity of this call). */
@@ -3423,7 +4025,8 @@ void cpSpaceReindexShape(cpSpace *sp, cpShape *s)
 	if(!space_edit_ok(sp)) return;
 	rd(s->body);
 	shape_cache_(s, s->body->transform);
-	record_op_(sp, CPG_OP_REINDEX, s, body_type_(s->body) == CP_BODY_TYPE_STATIC);
+	/* a sleeping body's shapes are in the static index */
+	record_op_(sp, CPG_OP_REINDEX, s, body_type_(s->body) == CP_BODY_TYPE_STATIC || cpBodyIsSleeping(s->body));
 	sp->structDirty = 1;
 	sp->editGen++;
 }
@@ -3479,6 +4082,7 @@ cpShape *cpSpaceAddShape(cpSpace *sp, cpShape *s)
 	cpBody *body = s->body;
 	rd(body);
 	int isStatic = (body_type_(body) == CP_BODY_TYPE_STATIC);
+	if(!isStatic) cpBodyActivate(body);
 	cpShape *next = body->shapeList;
 	if(next) next->prev = s;
 	s->next = next;
@@ -3502,6 +4106,8 @@ cpConstraint *cpSpaceAddConstraint(cpSpace *sp, cpConstraint *c)
 	ASSERT_HARD(c->a != NULL && c->b != NULL, "Constraint is attached to a NULL body.");
 	if(!space_edit_ok(sp)) return c;
 	cpBody *a = c->a, *b = c->b;
+	cpBodyActivate(a);
+	cpBodyActivate(b);
 	c->index = sp->ncons;
 	push_((void ***)&sp->cons, &sp->ncons, &sp->capcons, c);
 	c->next_a = a->constraintList; a->constraintList = c;
@@ -3517,6 +4123,26 @@ void cpSpaceRemoveShape(cpSpace *sp, cpShape *s)
 	if(!space_edit_ok(sp)) return;
 	cpBody *body = s->body;
 	int isStatic = (body_type_(body) == CP_BODY_TYPE_STATIC);
+	if(isStatic) cpBodyActivateStatic(body, s);
+	else cpBodyActivate(body);
+	/* the shape's arbiters leave the contact graph and the list
+	 * (cachedArbitersFilter, cpSpace.c:481-512) */
+	if(sp->graphOn){
+		for(int g = 0; g < sp->ngarb; g++){
+			cpArbiter *arb = &sp->garb[g];
+			if(!arb->a || (arb->a != s && arb->b != s)) continue;
+			/* its pending cache edits go with it */
+			int k = 0;
+			for(int i = 0; i < sp->nsed; i++){
+				if(sp->sedKey[i] == arb->key) continue;
+				sp->sedKey[k] = sp->sedKey[i]; sp->sedOp[k] = sp->sedOp[i]; sp->sedStamp[k] = sp->sedStamp[i]; k++;
+			}
+			sp->nsed = k;
+			gunthread_(sp, g);
+			glist_delete_(sp, g);
+			garb_release_(sp, g);
+		}
+	}
 	/* cpBodyRemoveShape, cpBody.c:306-327 */
 	if(s->prev) s->prev->next = s->next; else body->shapeList = s->next;
 	if(s->next) s->next->prev = s->prev;
@@ -3537,6 +4163,7 @@ void cpSpaceRemoveBody(cpSpace *sp, cpBody *b)
 	ASSERT_HARD(b != cpSpaceGetStaticBody(sp), "Cannot remove the designated static body for the space.");
 	ASSERT_HARD(cpSpaceContainsBody(sp, b), "Cannot remove a body that was not added to the space. (Removed twice maybe?)");
 	if(!space_edit_ok(sp)) return;
+	cpBodyActivate(b);
 	if(body_type_(b) == CP_BODY_TYPE_STATIC) array_delete_((void **)sp->stat, &sp->nstat, b);
 	else array_delete_((void **)sp->dyn, &sp->ndyn, b);
 	b->space = NULL;
@@ -3561,6 +4188,8 @@ void cpSpaceRemoveConstraint(cpSpace *sp, cpConstraint *c)
 	 * solve order */
 	ASSERT_HARD(cpSpaceContainsConstraint(sp, c), "Cannot remove a constraint that was not added to the space. (Removed twice maybe?)");
 	if(!space_edit_ok(sp)) return;
+	cpBodyActivate(c->a);
+	cpBodyActivate(c->b);
 	int i = array_delete_((void **)sp->cons, &sp->ncons, c);
 	if(i >= 0 && i < sp->ncons) sp->cons[i]->index = i;
 	body_remove_constraint_(c->a, c);
@@ -3569,10 +4198,22 @@ void cpSpaceRemoveConstraint(cpSpace *sp, cpConstraint *c)
 	c->index = -1;
 }
 
+/* cpSpace.c:589-617: the dynamic array, the static array, then each
+ * sleeping component from its root */
 void cpSpaceEachBody(cpSpace *sp, cpSpaceBodyIteratorFunc func, void *data)
 {
+	sp->locked++;
 	for(int i = 0; i < sp->ndyn; i++) func(sp->dyn[i], data);
 	for(int i = 0; i < sp->nstat; i++) func(sp->stat[i], data);
+	for(int i = 0; i < sp->nsleeping; i++){
+		cpBody *b = sp->sleeping[i];
+		while(b){
+			cpBody *next = b->sleepNext;
+			func(b, data);
+			b = next;
+		}
+	}
+	space_unlock_(sp);
 	run_post_step_(sp);
 }
 
@@ -3791,6 +4432,20 @@ cpContactPointSet cpArbiterGetContactPointSet(const cpArbiter *arb)
 void cpBodyEachArbiter(cpBody *body, cpBodyArbiterIteratorFunc func, void *data)
 {
 	cpSpace *sp = body->space;
+	if(sp && sp->graphOn){
+		/* cpBody.c:612-626 over the contact graph */
+		graph_refresh_(sp);
+		for(int k = body->arbList; k;){
+			cpArbiter *arb = GARB_AT_(sp, k);
+			int next = garb_next_(sp, k, body);
+			cpBool swapped = arb->swapped;
+			arb->swapped = (body == arb->body_b);
+			func(body, arb, data);
+			arb->swapped = swapped;
+			k = next;
+		}
+		return;
+	}
 	if(!sp || !space_snapshot(sp)) return;
 	for(int i = sp->nsnap - 1; i >= 0; i--){
 		cpArbiter *arb = &sp->snap[i];

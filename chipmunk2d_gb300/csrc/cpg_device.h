@@ -31,6 +31,8 @@ enum { CPG_PIVOT = 1, CPG_PIN = 2, CPG_SLIDE = 3, CPG_GROOVE = 4, CPG_DSPRING = 
        CPG_ROTLIMIT = 7, CPG_RATCHET = 8, CPG_GEAR = 9, CPG_MOTOR = 10 };
 /* arbiter states, chipmunk_structs.h:83-95 */
 enum { CPG_ARB_FIRST = 0, CPG_ARB_NORMAL = 1, CPG_ARB_IGNORE = 2, CPG_ARB_CACHED = 3 };
+/* cpgArb.pad bit: the arbiter is held by a sleeping body, out of the cache */
+#define CPG_ARB_ASLEEP 1
 /* error bits latched in cpgTree.error */
 enum { CPG_ERR_NODES = 1, CPG_ERR_PAIRS = 2, CPG_ERR_CANDS = 4, CPG_ERR_ARBS = 8, CPG_ERR_BINS = 16, CPG_ERR_LEVELS = 32, CPG_ERR_FLOW = 64 };
 
@@ -412,6 +414,9 @@ typedef struct cpgAdj {
 int cpg_launch_apply_ops(const cpgSet *s, void *stream);
 int cpg_launch_step(const cpgSet *s, const cpgSet *host_mirror, int mode, void *stream, float *phase_ms);
 int cpg_launch_gather_arbs(const cpgSet *s, int world, cpgArb *out, int n, void *stream);
+int cpg_launch_step_part(const cpgSet *s, const cpgSet *h, int mode, void *stream, float *phase_ms, int part);
+int cpg_launch_sleep_edits(const cpgSet *s, const unsigned long long *keys, const int *ops, const unsigned *stamps, int n,
+                           const unsigned long long *listKeys, int nlist, void *stream);
 long long cpg_launch_count(int reset);
 int cpg_launch_tape(const cpgSet *s, void *stream);
 int cpg_launch_adjoint(const cpgSet *s, const cpgAdj *a, int step, int rows, void *stream);

@@ -618,6 +618,68 @@ __device__ int arb_find_or_insert(const cpgSet &s, unsigned long long key, bool 
 	return -1;
 }
 
+/* Slot of an arbiter key in the open-addressing table, or -1. */
+__device__ int arb_find(const cpgSet &s, unsigned long long key)
+{
+	unsigned mask = (unsigned)s.arbCap - 1;
+	unsigned h = (unsigned)mix64(key) & mask;
+	for(int probe = 0; probe < s.arbCap; probe++, h = (h + 1) & mask){
+		unsigned long long k = s.keys[h];
+		if(k == key) return (int)h;
+		if(k == CPG_KEY_EMPTY) break;
+	}
+	return -1;
+}
+
+/* Sleeping edits of a single space, in call order: an arbiter leaves the
+ * cache when its body falls asleep (cpSpaceUncacheArbiter,
+ * cpSpaceComponent.c:92-101) and rejoins it with the stamp of the call when
+ * the body wakes (:50-70).  The arbiter keeps its slot and contacts.  An
+ * arbiter whose shape left the space since the edit is gone already. */
+__global__ void k_sleep_flags(cpgSet s, const unsigned long long *keys, const int *ops, const unsigned *stamps, int n)
+{
+	if(blockIdx.x != 0 || threadIdx.x != 0) return;
+	for(int i = 0; i < n; i++){
+		int slot = arb_find(s, keys[i]);
+		if(slot < 0) continue;
+		cpgArb &arb = s.arbs[slot];
+		if(ops[i]) arb.pad |= CPG_ARB_ASLEEP;
+		else { arb.pad &= ~CPG_ARB_ASLEEP; arb.stamp = stamps[i]; }
+	}
+}
+
+/* The arbiter list of a single space written from its keys, as
+ * cpSpaceProcessComponents left it (deletions and appended wakers), and
+ * the solver units made from it as k_solve_list makes them.  One block. */
+__global__ void k_set_list(cpgSet s, const unsigned long long *keys, int n)
+{
+	const cpgWorld &W = s.world[0];
+	int nunits = n + W.ncons;
+	if(n > W.candCap || nunits > W.unitCap){
+		if(threadIdx.x == 0){ s.tree[0].error |= CPG_ERR_LEVELS; s.tree[0].narb = 0; s.tree[0].nunits = 0; }
+		return;
+	}
+	for(int i = threadIdx.x; i < n; i += blockDim.x){
+		int slot = arb_find(s, keys[i]);
+		if(slot < 0){ s.tree[0].error |= CPG_ERR_ARBS; slot = 0; }
+		s.arbList[W.candOff + i] = slot;
+	}
+	__syncthreads();
+	if(threadIdx.x == 0){ s.tree[0].narb = n; s.tree[0].nunits = nunits; }
+	for(int u = threadIdx.x; u < nunits; u += blockDim.x){
+		int a, b;
+		if(u < n){
+			const cpgArb &arb = s.arbs[s.arbList[W.candOff + u]];
+			a = arb.ba; b = arb.bb;
+		} else {
+			const cpgJoint &j = s.joints[W.consOff + (u - n)];
+			a = j.a; b = j.b;
+		}
+		s.unitA[W.unitOff + u] = (s.btype[W.bodyOff + a] == CPG_DYNAMIC) ? a : -1;
+		s.unitB[W.unitOff + u] = (s.btype[W.bodyOff + b] == CPG_DYNAMIC) ? b : -1;
+	}
+}
+
 __global__ void k_arb_update(cpgSet s)
 {
 	int w = blockIdx.y;
@@ -641,6 +703,7 @@ __global__ void k_arb_update(cpgSet s)
 			arb.stamp = 0;
 			arb.world = w;
 			arb.colorTag = 0;     /* no colour yet */
+			arb.pad = 0;
 			arb.svx = 0.0; arb.svy = 0.0; arb.e = 0.0; arb.u = 0.0;
 		}
 		int ga = W.shapeOff + ia, gb = W.shapeOff + ib;
@@ -802,9 +865,13 @@ __global__ void k_arb_filter(cpgSet s)
 	cpgArb &arb = s.arbs[i];
 	const cpgParams &P = s.params[arb.world];
 	if(!P.active) return;
-	int bodyOff = s.world[arb.world].bodyOff;
+	/* an arbiter a sleeping body holds is out of the cache (cpSpaceUncacheArbiter) */
+	if(arb.pad & CPG_ARB_ASLEEP) return;
 	unsigned ticks = P.stamp - arb.stamp;
-	if(s.btype[bodyOff + arb.ba] == CPG_STATIC && s.btype[bodyOff + arb.bb] == CPG_STATIC) return;
+	/* both bodies static or asleep: the bodies past the world's dynamic
+	 * array (sleeping bodies, then static ones) */
+	int ndyn = s.world[arb.world].ndyn;
+	if(arb.ba >= ndyn && arb.bb >= ndyn) return;
 	if(ticks >= 1 && arb.state != CPG_ARB_CACHED) arb.state = CPG_ARB_CACHED;
 	if(ticks >= P.persistence){
 		arb.count = 0;
@@ -2406,19 +2473,6 @@ __global__ void __launch_bounds__(SAP_THREADS, 1) k_sap_sort(cpgSet s, int w)
 	}
 }
 
-/* Slot of an arbiter key in the open-addressing table, or -1. */
-__device__ int arb_find(const cpgSet &s, unsigned long long key)
-{
-	unsigned mask = (unsigned)s.arbCap - 1;
-	unsigned h = (unsigned)mix64(key) & mask;
-	for(int probe = 0; probe < s.arbCap; probe++, h = (h + 1) & mask){
-		unsigned long long k = s.keys[h];
-		if(k == key) return (int)h;
-		if(k == CPG_KEY_EMPTY) return -1;
-	}
-	return -1;
-}
-
 /* One warp per sorted shape: lane 0 queries the static tree, all lanes
  * sweep.  Count pass, then (after the scan) the emit pass writes the pairs
  * at deterministic positions: static hits first, then sweep hits in box
@@ -2936,6 +2990,15 @@ static cudaError_t check_launch(const char *what)
 	return e;
 }
 
+extern "C" int cpg_launch_sleep_edits(const cpgSet *s, const unsigned long long *keys, const int *ops, const unsigned *stamps, int n,
+                                      const unsigned long long *listKeys, int nlist, void *stream)
+{
+	cudaStream_t st = (cudaStream_t)stream;
+	if(n > 0) LAUNCH(k_sleep_flags<<<1, 1, 0, st>>>(*s, keys, ops, stamps, n));
+	if(nlist >= 0) LAUNCH(k_set_list<<<1, 1024, 0, st>>>(*s, listKeys, nlist));
+	return check_launch("k_sleep_edits") == cudaSuccess ? 0 : -1;
+}
+
 extern "C" int cpg_launch_gather_arbs(const cpgSet *s, int world, cpgArb *out, int n, void *stream)
 {
 	LAUNCH(k_gather_arbs<<<blocks_for(n, 128), 128, 0, (cudaStream_t)stream>>>(*s, world, out, n));
@@ -3029,7 +3092,11 @@ extern "C" void cpg_step_graph_free(void *cache)
 	free(g);
 }
 
-extern "C" int cpg_launch_step(const cpgSet *s, const cpgSet *h, int mode, void *stream, float *phase_ms);
+extern "C" int cpg_launch_step_part(const cpgSet *s, const cpgSet *h, int mode, void *stream, float *phase_ms, int part);
+extern "C" int cpg_launch_step(const cpgSet *s, const cpgSet *h, int mode, void *stream, float *phase_ms)
+{
+	return cpg_launch_step_part(s, h, mode, stream, phase_ms, 0);
+}
 
 extern "C" int cpg_launch_step_graph(const cpgSet *s, int mode, void *stream, void **cache)
 {
@@ -3086,9 +3153,13 @@ extern "C" int cpg_launch_replay_solve(const cpgSet *s, const cpgAdj *a, int nst
 	return check_launch("k_replay_solve") == cudaSuccess ? 0 : -1;
 }
 
-extern "C" int cpg_launch_step(const cpgSet *s, const cpgSet *h, int mode, void *stream, float *phase_ms)
+/* part 0: the whole step; part 1: up to the arbiter list (cpSpaceStep.c
+ * up to :372); part 2: the rest, from the cache filter on (:378-445).
+ * Between the two the host runs cpSpaceProcessComponents. */
+extern "C" int cpg_launch_step_part(const cpgSet *s, const cpgSet *h, int mode, void *stream, float *phase_ms, int part)
 {
 	cudaStream_t st = (cudaStream_t)stream;
+	if(part != 0) phase_ms = NULL;
 	int W = h->nworlds;
 	cudaEvent_t ev[8];
 	bool timing = (phase_ms != NULL);
@@ -3109,6 +3180,7 @@ extern "C" int cpg_launch_step(const cpgSet *s, const cpgSet *h, int mode, void 
 	 * fails the step: the kernels after it would run on a half-done step */
 	cudaError_t coop = cudaSuccess;
 #define COOP(kernel, threads) do { cudaError_t e_ = launch_coop((const void *)(kernel), (threads), &sv, 0, st); if(e_ != cudaSuccess && coop == cudaSuccess) coop = e_; } while(0)
+	if(part == 2) goto second;
 	cudaMemsetAsync(s->stats, 0, 16*sizeof(int), st);
 	LAUNCH(k_reset_prev<<<dim3(perWorldX, W), 128, 0, st>>>(*s));
 	LAUNCH(k_integrate_pos<<<blocks_for(h->totalBodies, 128), 128, 0, st>>>(*s));
@@ -3152,6 +3224,8 @@ extern "C" int cpg_launch_step(const cpgSet *s, const cpgSet *h, int mode, void 
 	} else {
 		LAUNCH(k_solve_list<<<W, 256, 0, st>>>(*s));
 	}
+	if(part == 1) goto done;
+second:
 	LAUNCH(k_arb_filter<<<blocks_for(h->arbCap, 256), 256, 0, st>>>(*s));
 	if(timing) cudaEventRecord(ev[4], st);
 	if(colored) COOP(k_color_coop, 512);
@@ -3192,6 +3266,7 @@ extern "C" int cpg_launch_step(const cpgSet *s, const cpgSet *h, int mode, void 
 	LAUNCH(k_unpack_bodies<<<blocks_for(h->totalBodies, 128), 128, 0, st>>>(*s));
 	if(timing) cudaEventRecord(ev[7], st);
 	LAUNCH(k_stats<<<1, 256, 0, st>>>(*s));
+done:
 #undef COOP
 	cudaError_t e = check_launch("step");
 	if(coop != cudaSuccess){

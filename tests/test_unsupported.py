@@ -45,8 +45,11 @@ def refused(lib, sp, b):
     return err, (p0.x, p0.y) == (p1.x, p1.y)
 
 
-def test_sleeping_is_refused(lib):
+def test_sleeping_in_the_coloured_mode_is_refused(lib):
+    """Sleeping runs in the exact-order mode, whose arbiter list order the
+    sleeping edits follow."""
     sp, b = one_body_space(lib)
+    lib.cpGpuSetSolverMode(sp, 1)
     lib.cpSpaceSetSleepTimeThreshold(sp, 0.5)
     err, unmoved = refused(lib, sp, b)
     assert err == CP_GPU_ERR_UNSUPPORTED and unmoved
