@@ -806,6 +806,37 @@ def mode_sample(lib, workload, steps, warmup, mode=0, phases=False, e2e=False):
     return rec
 
 
+def sleep_sample(lib, olib, workload="pyramid", threshold=0.5, n=300):
+    """The exact-order mode with sleeping on (cpSpaceSetSleepTimeThreshold):
+    each step wall-timed with a device sync, on the GPU and on the oracle
+    (one core); the awake window before the pile settles and the window
+    after it fell asleep."""
+    import torch
+    from chipmunk2d_gb300 import Scene
+    cfg, size, dt, desc = WORKLOADS[workload]
+    rec = {"workload": workload, "threshold_s": threshold, "steps": n,
+           "windows": {"awake": [10, 100], "asleep": [n - 100, n]}}
+    for name, L in (("gpu", lib), ("oracle_1core", olib)):
+        sc = Scene(L, cfg, size)
+        L.cpSpaceSetSleepTimeThreshold(sc.space, threshold)
+        times = []
+        for _ in range(n):
+            t0 = time.perf_counter()
+            L.cpSpaceStep(sc.space, dt)
+            if name == "gpu":
+                L.cpGpuSpaceSync(sc.space)
+                torch.cuda.synchronize()
+            times.append(time.perf_counter() - t0)
+        asleep = sum(L.cpBodyIsSleeping(L.cpx_scene_body(sc.h, i)) for i in range(sc.nbodies))
+        rec[name] = {"ms_per_step_awake": 1000 * float(np.mean(times[10:100])),
+                     "ms_per_step_asleep": 1000 * float(np.mean(times[-100:])),
+                     "bodies": sc.nbodies, "asleep_at_end": int(asleep)}
+        if name == "gpu" and L.cpGpuGetLastError():
+            rec[name]["error"] = L.cpGpuGetLastErrorString().decode()
+        sc.free()
+    return rec
+
+
 def parity_mode_sample(lib, workload, steps, warmup, e2e=False):
     """The exact reference-order mode, for the `ordered_mode` record."""
     rec = mode_sample(lib, workload, steps, warmup, mode=0, phases=True, e2e=e2e)
@@ -993,6 +1024,7 @@ def run_ours(args):
         lib.cpGpuSetStream(ctypes.c_void_p(stream.cuda_stream))
         extras["ordered_mode"] = [parity_mode_sample(lib, "pyramid", 300, window_start("pyramid", 5, 300)),
                                   parity_mode_sample(lib, "circles", 10, window_start("circles", 5, 10), e2e=True)]
+        extras["sleeping"] = sleep_sample(lib, oracle_lib())
         # mixed shapes and pivot chains at full size (40,000 bodies)
         extras["mixed"] = [mode_sample(lib, "mixed", 150, 150, mode=1, phases=True),
                            mode_sample(lib, "mixed", 3, 2, mode=0)]

@@ -125,6 +125,13 @@ _API = {
     "cpBoxShapeNew": (P, [P, D, D, D]),
     "cpPolyShapeGetCount": (I, [P]),
     "cpPolyShapeGetVert": (V, [P, I]),
+    # sleeping
+    "cpSpaceSetSleepTimeThreshold": (None, [P, D]),
+    "cpSpaceGetSleepTimeThreshold": (D, [P]),
+    "cpSpaceSetIdleSpeedThreshold": (None, [P, D]),
+    "cpBodyIsSleeping": (ctypes.c_ubyte, [P]),
+    "cpBodyActivate": (None, [P]),
+    "cpBodySleep": (None, [P]),
     # constraints
     "cpConstraintFree": (None, [P]),
     "cpConstraintGetImpulse": (D, [P]),
