@@ -583,6 +583,29 @@ cpVect cpArbiterGetPointA(const cpArbiter *arb, int i);              /* cpArbite
 cpVect cpArbiterGetPointB(const cpArbiter *arb, int i);              /* cpArbiter.h:117 */
 cpFloat cpArbiterGetDepth(const cpArbiter *arb, int i);              /* cpArbiter.h:119 */
 
+/* Inside collision-handler callbacks (cpArbiter.h:34-143, cpSpace.h:144-152).
+ * The callbacks run on the host between the halves of the device step, in
+ * the reference's order; the arbiter's changes go back to the device. */
+void cpArbiterSetRestitution(cpArbiter *arb, cpFloat restitution);   /* cpArbiter.h:34  */
+void cpArbiterSetFriction(cpArbiter *arb, cpFloat friction);         /* cpArbiter.h:38  */
+void cpArbiterSetSurfaceVelocity(cpArbiter *arb, cpVect vr);         /* cpArbiter.h:45  */
+cpDataPointer cpArbiterGetUserData(const cpArbiter *arb);            /* cpArbiter.h:48  */
+void cpArbiterSetUserData(cpArbiter *arb, cpDataPointer userData);   /* cpArbiter.h:51  */
+cpBool cpArbiterIgnore(cpArbiter *arb);                              /* cpArbiter.h:62  */
+void cpArbiterSetContactPointSet(cpArbiter *arb, cpContactPointSet *set); /* cpArbiter.h:103 */
+cpBool cpArbiterIsRemoval(const cpArbiter *arb);                     /* cpArbiter.h:108 */
+cpBool cpArbiterCallWildcardBeginA(cpArbiter *arb, cpSpace *space);  /* cpArbiter.h:123 */
+cpBool cpArbiterCallWildcardBeginB(cpArbiter *arb, cpSpace *space);  /* cpArbiter.h:126 */
+cpBool cpArbiterCallWildcardPreSolveA(cpArbiter *arb, cpSpace *space); /* cpArbiter.h:130 */
+cpBool cpArbiterCallWildcardPreSolveB(cpArbiter *arb, cpSpace *space); /* cpArbiter.h:133 */
+void cpArbiterCallWildcardPostSolveA(cpArbiter *arb, cpSpace *space); /* cpArbiter.h:136 */
+void cpArbiterCallWildcardPostSolveB(cpArbiter *arb, cpSpace *space); /* cpArbiter.h:138 */
+void cpArbiterCallWildcardSeparateA(cpArbiter *arb, cpSpace *space); /* cpArbiter.h:141 */
+void cpArbiterCallWildcardSeparateB(cpArbiter *arb, cpSpace *space); /* cpArbiter.h:143 */
+cpCollisionHandler *cpSpaceAddDefaultCollisionHandler(cpSpace *space); /* cpSpace.h:147 */
+cpCollisionHandler *cpSpaceAddCollisionHandler(cpSpace *space, cpCollisionType a, cpCollisionType b); /* cpSpace.h:150 */
+cpCollisionHandler *cpSpaceAddWildcardHandler(cpSpace *space, cpCollisionType type); /* cpSpace.h:152 */
+
 /* ------------------------------------------------------------------------
  * GPU-only additions (no counterpart in the reference).
  * ---------------------------------------------------------------------- */

@@ -97,6 +97,9 @@ struct cpArbiter {
 	/* the contact graph (cpArbiterThread, chipmunk_structs.h:176-179):
 	 * body_a's and body_b's list links, as slot + 1 (0 = none) */
 	int prevA, nextA, prevB, nextB;
+	/* collision handlers of the last update (chipmunk_structs.h:210-214) */
+	cpCollisionHandler *handler, *handlerA, *handlerB;
+	cpDataPointer data;
 };
 
 struct cpBody {
@@ -240,6 +243,12 @@ struct cpSpace {
 	int *freeList; int nfree, capfree;
 	ArbMap amap;
 	int *active; int nactive, capactive;   /* space->arbiters: slot indices */
+
+	/* collision handlers (cpSpace.c:65-103, 378-413): the default one and
+	 * the registered ones, each on the heap */
+	cpCollisionHandler defaultHandler;
+	int usesWildcards;
+	cpCollisionHandler **handlers; int nhandlers, caphandlers;
 
 	/* sleeping components (their roots) and bodies woken while locked */
 	cpBody **sleeping; int nsleeping, capsleeping;
@@ -1817,7 +1826,10 @@ static void arb_init(cpArbiter *arb, cpShape *a, cpShape *b)
 }
 
 /* cpArbiter.c:356-414 (default collision handler: no swap) */
-static void arb_update(cpArbiter *arb, CollisionInfo *info)
+static cpCollisionHandler *lookup_handler_(cpSpace *sp, cpCollisionType a, cpCollisionType b, cpCollisionHandler *def);
+extern cpCollisionHandler orc_handler_do_nothing_;
+
+static void arb_update(cpSpace *sp, cpArbiter *arb, CollisionInfo *info)
 {
 	cpShape *a = info->a, *b = info->b;
 	arb->a = a; arb->body_a = a->body;
@@ -1842,7 +1854,16 @@ static void arb_update(cpArbiter *arb, CollisionInfo *info)
 	arb->u = a->u * b->u;
 	cpVect surface_vr = cpvsub(b->surfaceV, a->surfaceV);
 	arb->surface_vr = cpvsub(surface_vr, cpvmult(info->n, cpvdot(surface_vr, info->n)));
-	arb->swapped = cpFalse;
+	/* cpArbiter.c:399-410: the handler of the types in info order; swapped
+	 * when they are the other way round from the handler's */
+	cpCollisionType typeA = a->type, typeB = b->type;
+	cpCollisionHandler *defaultHandler = &sp->defaultHandler;
+	cpCollisionHandler *handler = arb->handler = lookup_handler_(sp, typeA, typeB, defaultHandler);
+	cpBool swapped = arb->swapped = (typeA != handler->typeA && handler->typeA != CP_WILDCARD_COLLISION_TYPE);
+	if(handler != defaultHandler || sp->usesWildcards){
+		arb->handlerA = lookup_handler_(sp, (swapped ? typeB : typeA), CP_WILDCARD_COLLISION_TYPE, &orc_handler_do_nothing_);
+		arb->handlerB = lookup_handler_(sp, (swapped ? typeA : typeB), CP_WILDCARD_COLLISION_TYPE, &orc_handler_do_nothing_);
+	}
 	if(arb->state == ARB_CACHED) arb->state = ARB_FIRST;
 }
 
@@ -2295,6 +2316,7 @@ cpSpace *cpSpaceNew(void)
 	sp->collisionBias = pow((cpFloat)(1.0f - 0.1f), 60.0);
 	sp->collisionPersistence = 3;
 	sp->sleepTimeThreshold = ORC_INF;
+	memcpy(&sp->defaultHandler, &orc_handler_do_nothing_, sizeof(cpCollisionHandler));
 	sp->freeNode = -1;
 	sp->freePair = -1;
 	sp->dynTree.root = -1; sp->dynTree.isDynamic = 1; leafset_init(&sp->dynTree.leaves);
@@ -2326,6 +2348,8 @@ void cpSpaceDestroy(cpSpace *sp)
 	sp->candPairs = NULL;
 	free(sp->post); sp->post = NULL; sp->npost = sp->cappost = 0;
 	free(sp->sleeping); free(sp->roused); sp->sleeping = sp->roused = NULL;
+	for(int i = 0; i < sp->nhandlers; i++) free(sp->handlers[i]);
+	free(sp->handlers); sp->handlers = NULL; sp->nhandlers = sp->caphandlers = 0;
 	sp->nsleeping = sp->capsleeping = sp->nroused = sp->caproused = 0;
 }
 
@@ -2508,6 +2532,12 @@ static void filter_arbiters_of(cpSpace *sp, cpShape *s)
 		int slot = m->slot[h];
 		cpArbiter *arb = &sp->arbs[slot];
 		if(arb->a != s && arb->b != s) continue;
+		if(arb->state != ARB_CACHED){
+			/* the arbiter is invalidated: one of its shapes left */
+			arb->state = ARB_INVALID;
+			cpCollisionHandler *handler = arb->handler;
+			handler->separateFunc(arb, sp, handler->userData);
+		}
 		m->keys[h] = 1;
 		arb_unthread_(sp, slot);
 		arb_free(sp, slot);
@@ -2726,8 +2756,13 @@ static cpCollisionID collide_shapes_(cpSpace *sp, cpShape *a, cpShape *b, cpColl
 		amap_insert(sp, key, slot);
 	}
 	cpArbiter *arb = &sp->arbs[slot];
-	arb_update(arb, &info);
-	if(arb->state != ARB_IGNORE && !(a->sensor || b->sensor) && !(a->body->m == ORC_INF && b->body->m == ORC_INF)){
+	arb_update(sp, arb, &info);
+	/* cpSpaceStep.c:259-283: begin on the first step of a collision (false:
+	 * ignored until separation), then pre-solve */
+	cpCollisionHandler *handler = arb->handler;
+	if(arb->state == ARB_FIRST && !handler->beginFunc(arb, sp, handler->userData)) cpArbiterIgnore(arb);
+	if(arb->state != ARB_IGNORE && handler->preSolveFunc(arb, sp, handler->userData) && arb->state != ARB_IGNORE &&
+	   !(a->sensor || b->sensor) && !(a->body->m == ORC_INF && b->body->m == ORC_INF)){
 		active_push(sp, slot);
 	} else {
 		arb->count = 0;
@@ -3003,7 +3038,11 @@ static void filter_arbiters(cpSpace *sp)
 		cpTimestamp ticks = sp->stamp - arb->stamp;
 		cpBody *a = arb->body_a, *b = arb->body_b;
 		if((body_type(a) == CP_BODY_TYPE_STATIC || cpBodyIsSleeping(a)) && (body_type(b) == CP_BODY_TYPE_STATIC || cpBodyIsSleeping(b))) continue;
-		if(ticks >= 1 && arb->state != ARB_CACHED) arb->state = ARB_CACHED;
+		if(ticks >= 1 && arb->state != ARB_CACHED){
+			arb->state = ARB_CACHED;
+			cpCollisionHandler *handler = arb->handler;
+			handler->separateFunc(arb, sp, handler->userData);
+		}
 		if(ticks >= sp->collisionPersistence){
 			arb->count = 0;
 			m->keys[h] = 1;
@@ -3177,8 +3216,191 @@ void cpSpaceStep(cpSpace *sp, cpFloat dt)
 		cpConstraint *c = sp->cons[i];
 		if(c->postSolve) c->postSolve(c, sp);
 	}
+	/* cpSpaceStep.c:439-444 */
+	for(int i = 0; i < sp->nactive; i++){
+		cpArbiter *arb = &sp->arbs[sp->active[i]];
+		cpCollisionHandler *handler = arb->handler;
+		handler->postSolveFunc(arb, sp, handler->userData);
+	}
 	space_unlock_(sp);
 	run_post_step_(sp);
+}
+
+/* ========================================================================
+ * Collision handlers: src/cpSpace.c:62-103, 378-413, src/cpArbiter.c:249-356
+ * ====================================================================== */
+cpBool cpArbiterCallWildcardBeginA(cpArbiter *arb, cpSpace *space)
+{
+	cpCollisionHandler *handler = arb->handlerA;
+	return handler->beginFunc(arb, space, handler->userData);
+}
+
+cpBool cpArbiterCallWildcardBeginB(cpArbiter *arb, cpSpace *space)
+{
+	cpCollisionHandler *handler = arb->handlerB;
+	arb->swapped = !arb->swapped;
+	cpBool retval = handler->beginFunc(arb, space, handler->userData);
+	arb->swapped = !arb->swapped;
+	return retval;
+}
+
+cpBool cpArbiterCallWildcardPreSolveA(cpArbiter *arb, cpSpace *space)
+{
+	cpCollisionHandler *handler = arb->handlerA;
+	return handler->preSolveFunc(arb, space, handler->userData);
+}
+
+cpBool cpArbiterCallWildcardPreSolveB(cpArbiter *arb, cpSpace *space)
+{
+	cpCollisionHandler *handler = arb->handlerB;
+	arb->swapped = !arb->swapped;
+	cpBool retval = handler->preSolveFunc(arb, space, handler->userData);
+	arb->swapped = !arb->swapped;
+	return retval;
+}
+
+void cpArbiterCallWildcardPostSolveA(cpArbiter *arb, cpSpace *space)
+{
+	cpCollisionHandler *handler = arb->handlerA;
+	handler->postSolveFunc(arb, space, handler->userData);
+}
+
+void cpArbiterCallWildcardPostSolveB(cpArbiter *arb, cpSpace *space)
+{
+	cpCollisionHandler *handler = arb->handlerB;
+	arb->swapped = !arb->swapped;
+	handler->postSolveFunc(arb, space, handler->userData);
+	arb->swapped = !arb->swapped;
+}
+
+void cpArbiterCallWildcardSeparateA(cpArbiter *arb, cpSpace *space)
+{
+	cpCollisionHandler *handler = arb->handlerA;
+	handler->separateFunc(arb, space, handler->userData);
+}
+
+void cpArbiterCallWildcardSeparateB(cpArbiter *arb, cpSpace *space)
+{
+	cpCollisionHandler *handler = arb->handlerB;
+	arb->swapped = !arb->swapped;
+	handler->separateFunc(arb, space, handler->userData);
+	arb->swapped = !arb->swapped;
+}
+
+static cpBool default_begin_(cpArbiter *arb, cpSpace *space, cpDataPointer data)
+{
+	(void)data;
+	cpBool retA = cpArbiterCallWildcardBeginA(arb, space);
+	cpBool retB = cpArbiterCallWildcardBeginB(arb, space);
+	return retA && retB;
+}
+
+static cpBool default_pre_solve_(cpArbiter *arb, cpSpace *space, cpDataPointer data)
+{
+	(void)data;
+	cpBool retA = cpArbiterCallWildcardPreSolveA(arb, space);
+	cpBool retB = cpArbiterCallWildcardPreSolveB(arb, space);
+	return retA && retB;
+}
+
+static void default_post_solve_(cpArbiter *arb, cpSpace *space, cpDataPointer data)
+{
+	(void)data;
+	cpArbiterCallWildcardPostSolveA(arb, space);
+	cpArbiterCallWildcardPostSolveB(arb, space);
+}
+
+static void default_separate_(cpArbiter *arb, cpSpace *space, cpDataPointer data)
+{
+	(void)data;
+	cpArbiterCallWildcardSeparateA(arb, space);
+	cpArbiterCallWildcardSeparateB(arb, space);
+}
+
+static cpBool always_collide_(cpArbiter *arb, cpSpace *space, cpDataPointer data) { (void)arb; (void)space; (void)data; return cpTrue; }
+static void do_nothing_(cpArbiter *arb, cpSpace *space, cpDataPointer data) { (void)arb; (void)space; (void)data; }
+
+/* the default handler of a space that uses wildcards, and the do-nothing
+ * handler of one that does not (cpSpace.c:90-103) */
+static cpCollisionHandler orc_handler_default_ = {
+	CP_WILDCARD_COLLISION_TYPE, CP_WILDCARD_COLLISION_TYPE,
+	default_begin_, default_pre_solve_, default_post_solve_, default_separate_, NULL
+};
+cpCollisionHandler orc_handler_do_nothing_ = {
+	CP_WILDCARD_COLLISION_TYPE, CP_WILDCARD_COLLISION_TYPE,
+	always_collide_, always_collide_, do_nothing_, do_nothing_, NULL
+};
+
+/* cpSpaceLookupHandler (cpArbiter.c:348-354): the handler registered for
+ * the unordered pair of types */
+static cpCollisionHandler *lookup_handler_(cpSpace *sp, cpCollisionType a, cpCollisionType b, cpCollisionHandler *def)
+{
+	for(int i = 0; i < sp->nhandlers; i++){
+		cpCollisionHandler *h = sp->handlers[i];
+		if((h->typeA == a && h->typeB == b) || (h->typeB == a && h->typeA == b)) return h;
+	}
+	return def;
+}
+
+static cpCollisionHandler *add_handler_(cpSpace *sp, const cpCollisionHandler *proto)
+{
+	cpCollisionHandler *h = lookup_handler_(sp, proto->typeA, proto->typeB, NULL);
+	if(h) return h;
+	h = (cpCollisionHandler *)malloc(sizeof(cpCollisionHandler));
+	memcpy(h, proto, sizeof(cpCollisionHandler));
+	push_ptr_((void ***)&sp->handlers, &sp->nhandlers, &sp->caphandlers, h);
+	return h;
+}
+
+static void use_wildcard_default_(cpSpace *sp)
+{
+	if(!sp->usesWildcards){
+		sp->usesWildcards = 1;
+		memcpy(&sp->defaultHandler, &orc_handler_default_, sizeof(cpCollisionHandler));
+	}
+}
+
+cpCollisionHandler *cpSpaceAddDefaultCollisionHandler(cpSpace *sp)
+{
+	use_wildcard_default_(sp);
+	return &sp->defaultHandler;
+}
+
+cpCollisionHandler *cpSpaceAddCollisionHandler(cpSpace *sp, cpCollisionType a, cpCollisionType b)
+{
+	cpCollisionHandler proto = { a, b, default_begin_, default_pre_solve_, default_post_solve_, default_separate_, NULL };
+	return add_handler_(sp, &proto);
+}
+
+cpCollisionHandler *cpSpaceAddWildcardHandler(cpSpace *sp, cpCollisionType type)
+{
+	use_wildcard_default_(sp);
+	cpCollisionHandler proto = { type, CP_WILDCARD_COLLISION_TYPE, always_collide_, always_collide_, do_nothing_, do_nothing_, NULL };
+	return add_handler_(sp, &proto);
+}
+
+/* cpArbiter.c:174-238 */
+cpBool cpArbiterIgnore(cpArbiter *arb) { arb->state = ARB_IGNORE; return cpFalse; }
+void cpArbiterSetRestitution(cpArbiter *arb, cpFloat e) { arb->e = e; }
+void cpArbiterSetFriction(cpArbiter *arb, cpFloat u) { arb->u = u; }
+void cpArbiterSetSurfaceVelocity(cpArbiter *arb, cpVect vr) { arb->surface_vr = cpvmult(vr, arb->swapped ? -1.0 : 1.0); }
+cpDataPointer cpArbiterGetUserData(const cpArbiter *arb) { return arb->data; }
+void cpArbiterSetUserData(cpArbiter *arb, cpDataPointer data) { arb->data = data; }
+cpBool cpArbiterIsRemoval(const cpArbiter *arb) { return arb->state == ARB_INVALID; }
+
+/* cpArbiter.c:122-139 */
+void cpArbiterSetContactPointSet(cpArbiter *arb, cpContactPointSet *set)
+{
+	int count = set->count;
+	ORC_ASSERT(count == arb->count, "The number of contact points cannot be changed.");
+	cpBool swapped = arb->swapped;
+	arb->n = (swapped ? cpvneg(set->normal) : set->normal);
+	for(int i = 0; i < count; i++){
+		cpVect p1 = set->points[i].pointA;
+		cpVect p2 = set->points[i].pointB;
+		arb->contacts[i].r1 = cpvsub(swapped ? p2 : p1, arb->body_a->p);
+		arb->contacts[i].r2 = cpvsub(swapped ? p1 : p2, arb->body_b->p);
+	}
 }
 
 /* ========================================================================

@@ -65,7 +65,7 @@ def test_builds_against_the_reference_headers_and_links_the_gpu_library(tmp_path
     build(tmp_path, "relink_ref_headers", GPU_DIR, "chipmunk_gb300", ref_headers=inc, program=program)
 
 
-@pytest.mark.parametrize("program", PROGRAMS)
+@pytest.mark.parametrize("program", PROGRAMS + ["relink_program5.c"])
 def test_oracle_matches_the_reference_on_the_program(tmp_path, oracle_lib, program):
     """The same program on the reference library and on the oracle: bit for
     bit, through removals and additions mid-run, caller-placed objects,
