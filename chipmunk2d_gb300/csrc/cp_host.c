@@ -177,6 +177,11 @@ struct cpArbiter {
 	unsigned long long key;
 	int prevA, nextA, prevB, nextB;
 	int listPos;
+	/* collision handlers (chipmunk_structs.h:210-214): those of the last
+	 * update, the user data, the device slot of the record */
+	cpCollisionHandler *handler, *handlerA, *handlerB;
+	cpDataPointer data;
+	int slot;
 };
 
 struct cpSpace {
@@ -236,6 +241,14 @@ struct cpSpace {
 	unsigned long long *sedKey; int *sedOp; unsigned *sedStamp; int nsed, capsed;
 	int sleepMutated;
 	double prevDt;
+
+	/* collision handlers (cpSpace.c:62-103, 378-413): once any is added,
+	 * the step runs the callbacks on the host between its device halves */
+	cpCollisionHandler defaultHandler;
+	int usesWildcards, handlersOn;
+	cpCollisionHandler **handlers; int nhandlers, caphandlers;
+	cpArbiter *harb; int capharb;            /* the arbiters of one round of callbacks */
+	unsigned long long *udKey; cpDataPointer *udVal; int udCap, udUsed;   /* arbiter user data by key */
 };
 
 static void run_post_step_(cpSpace *sp);
@@ -286,6 +299,8 @@ struct DevSet {
 	size_t slabBytes;
 	void *scratch;            /* per-step scratch outside the slab (not checkpointed) */
 	cpgArb *gather;           /* arbiter snapshot staging */
+	int *bridgeBuf;           /* collision handlers: separated slots (arbCap + 1 ints), slot lists */
+	int bridgeCap;
 	int gatherCap;
 	int structStale;          /* the staging block holds body state the body structs do not have yet */
 	unsigned long long pullGen; /* id of the download in the staging block (unique across sets) */
@@ -729,6 +744,7 @@ static void devset_free(DevSet *ds)
 	if(ds->scratch) cudaFree(ds->scratch);
 	if(ds->graph) cpg_step_graph_free(ds->graph);
 	if(ds->gather) cudaFree(ds->gather);
+	if(ds->bridgeBuf) cudaFree(ds->bridgeBuf);
 	if(ds->qbuf) cudaFree(ds->qbuf);
 	if(ds->bstates) cudaFree(ds->bstates);
 	if(ds->hparams) cudaFreeHost(ds->hparams);
@@ -1084,6 +1100,8 @@ static void devset_flush_space(DevSet *ds, int w)
 }
 
 /* One step of every world of the set with per-world dt. */
+static int bridge_buf_(DevSet *ds, int n);
+
 /* part 0: the whole step; 1: up to the arbiter list; 2: the rest of the
  * step begun by part 1 (a single space; its set may have been rebuilt in
  * between, so the parameters go up again without advancing the stamp). */
@@ -1107,7 +1125,7 @@ static int devset_step_part(DevSet *ds, const double *dts, cpSpace **only, int p
 		double dt = dts[w];
 		/* cpSpaceStep.c:339-344, 384, 399, 407 */
 		cpFloat prev_dt;
-		if(part == 2) prev_dt = sp->prevDt;
+		if(part >= 2) prev_dt = sp->prevDt;
 		else {
 			sp->stamp++;
 			prev_dt = sp->prevDt = sp->curr_dt;
@@ -1140,6 +1158,14 @@ static int devset_step_part(DevSet *ds, const double *dts, cpSpace **only, int p
 	d->flowWithhold = g_flow_withhold;
 	d->warmGather = g_warm_gather;
 	d->parMark = g_par_mark >= 0 ? g_par_mark : (d->hostNdyn >= CPG_PAR_MARK_MIN);
+	/* collision handlers: the separations of the filter go to the host */
+	d->bridge = (ds->nspaces == 1 && ds->spaces[0]->handlersOn && part != 0);
+	d->sepSlots = d->sepCount = NULL;
+	if(d->bridge){
+		if(!bridge_buf_(ds, d->arbCap + 1)) return -1;
+		d->sepSlots = ds->bridgeBuf;
+		d->sepCount = ds->bridgeBuf + d->arbCap;
+	}
 	/* launch shapes of many-world sets: the tuner's candidates on the steps
 	 * of a tuning window, its choice after it (debug settings win) */
 	int tuning = -1;
@@ -1173,7 +1199,7 @@ static int devset_step_part(DevSet *ds, const double *dts, cpSpace **only, int p
 		set_error(CP_GPU_ERR_CUDA, "step launch failed");
 		return -1;
 	}
-	if(part == 1) return 0;
+	if(part == 1 || part == 3) return 0;
 	if(g_timing) for(int w = 0; w < ds->nspaces; w++) memcpy(ds->spaces[w]->phaseMs, ms, sizeof(ms));
 	if(tuning >= 0){
 		ds->tuneMs[tuning] += (double)ms[1] + (double)ms[6];
@@ -1199,6 +1225,10 @@ static int devset_step_part(DevSet *ds, const double *dts, cpSpace **only, int p
 static int devset_step(DevSet *ds, const double *dts, cpSpace **only) { return devset_step_part(ds, dts, only, 0); }
 
 static int sleep_mode_(const cpSpace *sp);
+static cpCollisionHandler handler_do_nothing_;
+static int handlers_collide_(cpSpace *sp);
+static int handlers_separate_(cpSpace *sp);
+static int handlers_post_solve_(cpSpace *sp);
 static int sleep_apply_edits_(cpSpace *sp);
 static void graph_start_(cpSpace *sp);
 static void graph_stop_(cpSpace *sp);
@@ -1208,6 +1238,10 @@ static int space_supported(cpSpace *sp)
 {
 	if(sleep_mode_(sp) && (sp->mode != CP_GPU_SOLVER_ORDERED || (sp->dev && !sp->ownsDev))){
 		set_error(CP_GPU_ERR_UNSUPPORTED, "sleeping runs in the exact-order mode of a standalone space");
+		return 0;
+	}
+	if(sp->handlersOn && (sp->mode != CP_GPU_SOLVER_ORDERED || (sp->dev && !sp->ownsDev))){
+		set_error(CP_GPU_ERR_UNSUPPORTED, "collision handlers run in the exact-order mode of a standalone space");
 		return 0;
 	}
 	for(int i = 0; i < sp->ndyn; i++){
@@ -1278,12 +1312,22 @@ void cpSpaceStep(cpSpace *sp, cpFloat dt)
 	}
 	if(!space_device_ready_(sp)) return;
 	double dts[1] = { dt };
-	if(sleep_mode_(sp)){
-		/* cpSpaceStep.c:375: cpSpaceProcessComponents between the halves */
-		graph_start_(sp);
-		if(devset_step_part(sp->dev, dts, NULL, 1) != 0 || !sleep_sync_(sp, dt)) return;
-		devset_step_part(sp->dev, dts, NULL, 2);
-		sp->hostStale = 1; sp->consStale = 1; sp->shapesStale = 1; sp->snapValid = 0;
+	int sleep = sleep_mode_(sp), bridge = sp->handlersOn;
+	if(sleep || bridge){
+		/* the host's parts of the step between the device's: the handlers'
+		 * begin and pre-solve (cpSpaceStep.c:259-286), cpSpaceProcessComponents
+		 * (:375), separate (:307-313), post-solve (:439-444) */
+		if(sleep) graph_start_(sp); else graph_stop_(sp);
+		sp->sleepMutated = 0;
+		if(devset_step_part(sp->dev, dts, NULL, 1) != 0) return;
+		if(bridge && !handlers_collide_(sp)) return;
+		if(sleep && !sleep_sync_(sp, dt)) return;
+		if(bridge){
+			if(devset_step_part(sp->dev, dts, NULL, 3) != 0 || !handlers_separate_(sp)) return;
+			if(devset_step_part(sp->dev, dts, NULL, 4) != 0 || !handlers_post_solve_(sp)) return;
+		} else {
+			devset_step_part(sp->dev, dts, NULL, 2);
+		}
 	} else {
 		graph_stop_(sp);
 		devset_step(sp->dev, dts, NULL);
@@ -3280,6 +3324,7 @@ cpSpace *cpSpaceNew(void)
 	sp->collisionBias = pow((cpFloat)(1.0f - 0.1f), 60.0);
 	sp->collisionPersistence = 3;
 	sp->sleepTimeThreshold = INF_;
+	memcpy(&sp->defaultHandler, &handler_do_nothing_, sizeof(cpCollisionHandler));
 	sp->mode = CP_GPU_SOLVER_ORDERED;
 	body_init_(&sp->staticBody, 0.0, 0.0);
 	make_static_(&sp->staticBody);
@@ -3310,6 +3355,10 @@ void cpSpaceDestroy(cpSpace *sp)
 	sp->slp = sp->sleeping = sp->roused = NULL; sp->garb = NULL; sp->gfree = sp->glist = NULL;
 	sp->sedKey = NULL; sp->sedOp = NULL; sp->sedStamp = NULL;
 	sp->nslp = sp->nsleeping = sp->nroused = 0;
+	for(int i = 0; i < sp->nhandlers; i++) free(sp->handlers[i]);
+	free(sp->handlers); free(sp->harb); free(sp->udKey); free(sp->udVal);
+	sp->handlers = NULL; sp->harb = NULL; sp->udKey = NULL; sp->udVal = NULL;
+	sp->nhandlers = sp->caphandlers = sp->capharb = sp->udCap = sp->udUsed = 0;
 	for(int i = 0; i < sp->ndyn; i++) if(sp->dyn[i]->space == sp) sp->dyn[i]->space = NULL;
 	for(int i = 0; i < sp->nstat; i++) if(sp->stat[i]->space == sp) sp->stat[i]->space = NULL;
 	for(int i = 0; i < sp->nshapes; i++) if(sp->shapes[i] && sp->shapes[i]->space == sp) sp->shapes[i]->space = NULL;
@@ -3960,7 +4009,6 @@ static int sleep_sync_(cpSpace *sp, cpFloat dt)
 		glist_push_(sp, g);
 	}
 	free(recs);
-	sp->sleepMutated = 0;
 	process_components_(sp, dt);
 	sp->graphFresh = 0;
 	if(sp->sleepMutated && !space_device_ready_(sp)) return 0;
@@ -4008,6 +4056,451 @@ void cpBodySleepWithGroup(cpBody *body, cpBody *group)
 	}
 	/* cpSpaceComponent.c:349: a second delete, of a body no longer there */
 	array_delete_((void **)sp->dyn, &sp->ndyn, body);
+}
+
+/* ====================================================================
+ * Collision handlers (src/cpSpace.c:62-103, 378-413, src/cpArbiter.c)
+ *
+ * Once a handler is added, a step stops after the arbiter cache update:
+ * every colliding arbiter is on the list in the reference's collision
+ * order, with its sensor and ignore rule left to the host.  The host runs
+ * begin and pre-solve on each (cpSpaceStep.c:259-283), applies the rule,
+ * writes the changed records back and the list of the arbiters that stay.
+ * The cache filter runs next on its own, and the host calls separate on
+ * the arbiters it moved to the cached state; then the solve, and the host
+ * calls post-solve on the list with the solved impulses.
+ * ==================================================================== */
+cpBool cpArbiterCallWildcardBeginA(cpArbiter *arb, cpSpace *space)
+{
+	cpCollisionHandler *handler = arb->handlerA;
+	return handler->beginFunc(arb, space, handler->userData);
+}
+
+cpBool cpArbiterCallWildcardBeginB(cpArbiter *arb, cpSpace *space)
+{
+	cpCollisionHandler *handler = arb->handlerB;
+	arb->swapped = !arb->swapped;
+	cpBool retval = handler->beginFunc(arb, space, handler->userData);
+	arb->swapped = !arb->swapped;
+	return retval;
+}
+
+cpBool cpArbiterCallWildcardPreSolveA(cpArbiter *arb, cpSpace *space)
+{
+	cpCollisionHandler *handler = arb->handlerA;
+	return handler->preSolveFunc(arb, space, handler->userData);
+}
+
+cpBool cpArbiterCallWildcardPreSolveB(cpArbiter *arb, cpSpace *space)
+{
+	cpCollisionHandler *handler = arb->handlerB;
+	arb->swapped = !arb->swapped;
+	cpBool retval = handler->preSolveFunc(arb, space, handler->userData);
+	arb->swapped = !arb->swapped;
+	return retval;
+}
+
+void cpArbiterCallWildcardPostSolveA(cpArbiter *arb, cpSpace *space)
+{
+	cpCollisionHandler *handler = arb->handlerA;
+	handler->postSolveFunc(arb, space, handler->userData);
+}
+
+void cpArbiterCallWildcardPostSolveB(cpArbiter *arb, cpSpace *space)
+{
+	cpCollisionHandler *handler = arb->handlerB;
+	arb->swapped = !arb->swapped;
+	handler->postSolveFunc(arb, space, handler->userData);
+	arb->swapped = !arb->swapped;
+}
+
+void cpArbiterCallWildcardSeparateA(cpArbiter *arb, cpSpace *space)
+{
+	cpCollisionHandler *handler = arb->handlerA;
+	handler->separateFunc(arb, space, handler->userData);
+}
+
+void cpArbiterCallWildcardSeparateB(cpArbiter *arb, cpSpace *space)
+{
+	cpCollisionHandler *handler = arb->handlerB;
+	arb->swapped = !arb->swapped;
+	handler->separateFunc(arb, space, handler->userData);
+	arb->swapped = !arb->swapped;
+}
+
+static cpBool default_begin_(cpArbiter *arb, cpSpace *space, cpDataPointer data)
+{
+	(void)data;
+	cpBool retA = cpArbiterCallWildcardBeginA(arb, space);
+	cpBool retB = cpArbiterCallWildcardBeginB(arb, space);
+	return retA && retB;
+}
+
+static cpBool default_pre_solve_(cpArbiter *arb, cpSpace *space, cpDataPointer data)
+{
+	(void)data;
+	cpBool retA = cpArbiterCallWildcardPreSolveA(arb, space);
+	cpBool retB = cpArbiterCallWildcardPreSolveB(arb, space);
+	return retA && retB;
+}
+
+static void default_post_solve_(cpArbiter *arb, cpSpace *space, cpDataPointer data)
+{
+	(void)data;
+	cpArbiterCallWildcardPostSolveA(arb, space);
+	cpArbiterCallWildcardPostSolveB(arb, space);
+}
+
+static void default_separate_(cpArbiter *arb, cpSpace *space, cpDataPointer data)
+{
+	(void)data;
+	cpArbiterCallWildcardSeparateA(arb, space);
+	cpArbiterCallWildcardSeparateB(arb, space);
+}
+
+static cpBool always_collide_(cpArbiter *arb, cpSpace *space, cpDataPointer data) { (void)arb; (void)space; (void)data; return cpTrue; }
+static void do_nothing_(cpArbiter *arb, cpSpace *space, cpDataPointer data) { (void)arb; (void)space; (void)data; }
+
+static cpCollisionHandler handler_default_ = {
+	CP_WILDCARD_COLLISION_TYPE, CP_WILDCARD_COLLISION_TYPE,
+	default_begin_, default_pre_solve_, default_post_solve_, default_separate_, NULL
+};
+static cpCollisionHandler handler_do_nothing_ = {
+	CP_WILDCARD_COLLISION_TYPE, CP_WILDCARD_COLLISION_TYPE,
+	always_collide_, always_collide_, do_nothing_, do_nothing_, NULL
+};
+
+/* cpSpaceLookupHandler (cpArbiter.c:348-354) */
+static cpCollisionHandler *lookup_handler_(cpSpace *sp, cpCollisionType a, cpCollisionType b, cpCollisionHandler *def)
+{
+	for(int i = 0; i < sp->nhandlers; i++){
+		cpCollisionHandler *h = sp->handlers[i];
+		if((h->typeA == a && h->typeB == b) || (h->typeB == a && h->typeA == b)) return h;
+	}
+	return def;
+}
+
+static cpCollisionHandler *add_handler_(cpSpace *sp, const cpCollisionHandler *proto)
+{
+	sp->handlersOn = 1;
+	cpCollisionHandler *h = lookup_handler_(sp, proto->typeA, proto->typeB, NULL);
+	if(h) return h;
+	h = (cpCollisionHandler *)malloc(sizeof(cpCollisionHandler));
+	memcpy(h, proto, sizeof(cpCollisionHandler));
+	push_((void ***)&sp->handlers, &sp->nhandlers, &sp->caphandlers, h);
+	return h;
+}
+
+static void use_wildcard_default_(cpSpace *sp)
+{
+	if(!sp->usesWildcards){
+		sp->usesWildcards = 1;
+		memcpy(&sp->defaultHandler, &handler_default_, sizeof(cpCollisionHandler));
+	}
+}
+
+cpCollisionHandler *cpSpaceAddDefaultCollisionHandler(cpSpace *sp)
+{
+	use_wildcard_default_(sp);
+	sp->handlersOn = 1;
+	return &sp->defaultHandler;
+}
+
+cpCollisionHandler *cpSpaceAddCollisionHandler(cpSpace *sp, cpCollisionType a, cpCollisionType b)
+{
+	cpCollisionHandler proto = { a, b, default_begin_, default_pre_solve_, default_post_solve_, default_separate_, NULL };
+	return add_handler_(sp, &proto);
+}
+
+cpCollisionHandler *cpSpaceAddWildcardHandler(cpSpace *sp, cpCollisionType type)
+{
+	use_wildcard_default_(sp);
+	cpCollisionHandler proto = { type, CP_WILDCARD_COLLISION_TYPE, always_collide_, always_collide_, do_nothing_, do_nothing_, NULL };
+	return add_handler_(sp, &proto);
+}
+
+/* cpArbiter.c:122-139, 174-238 */
+cpBool cpArbiterIgnore(cpArbiter *arb) { arb->state = CPG_ARB_IGNORE; return cpFalse; }
+void cpArbiterSetRestitution(cpArbiter *arb, cpFloat e) { arb->e = e; }
+void cpArbiterSetFriction(cpArbiter *arb, cpFloat u) { arb->u = u; }
+void cpArbiterSetSurfaceVelocity(cpArbiter *arb, cpVect vr) { arb->surface_vr = cpvmult(vr, arb->swapped ? -1.0 : 1.0); }
+cpDataPointer cpArbiterGetUserData(const cpArbiter *arb) { return arb->data; }
+void cpArbiterSetUserData(cpArbiter *arb, cpDataPointer data) { arb->data = data; }
+cpBool cpArbiterIsRemoval(const cpArbiter *arb) { return arb->state == CPG_ARB_INVALIDATED; }
+
+void cpArbiterSetContactPointSet(cpArbiter *arb, cpContactPointSet *set)
+{
+	int count = set->count;
+	ASSERT_HARD(count == arb->count, "The number of contact points cannot be changed.");
+	cpBool swapped = arb->swapped;
+	arb->n = (swapped ? cpvneg(set->normal) : set->normal);
+	for(int i = 0; i < count; i++){
+		cpVect p1 = set->points[i].pointA, p2 = set->points[i].pointB;
+		cpVect r1 = cpvsub(swapped ? p2 : p1, arb->body_a->p), r2 = cpvsub(swapped ? p1 : p2, arb->body_b->p);
+		arb->c[i].r1x = r1.x; arb->c[i].r1y = r1.y;
+		arb->c[i].r2x = r2.x; arb->c[i].r2y = r2.y;
+	}
+}
+
+/* user data of the arbiters, by device key: an arbiter keeps its data
+ * from update to update and a fresh one starts with none
+ * (cpArbiter.c:343) */
+static cpDataPointer *ud_slot_(cpSpace *sp, unsigned long long key, int insert)
+{
+	if(insert && 2*(sp->udUsed + 1) > sp->udCap){
+		int oldCap = sp->udCap;
+		unsigned long long *ok = sp->udKey;
+		cpDataPointer *ov = sp->udVal;
+		sp->udCap = oldCap ? 2*oldCap : 256;
+		sp->udKey = (unsigned long long *)calloc((size_t)sp->udCap, sizeof(unsigned long long));
+		sp->udVal = (cpDataPointer *)calloc((size_t)sp->udCap, sizeof(cpDataPointer));
+		sp->udUsed = 0;
+		for(int i = 0; i < oldCap; i++) if(ok[i]) *ud_slot_(sp, ok[i], 1) = ov[i];
+		free(ok); free(ov);
+	}
+	if(sp->udCap == 0) return NULL;
+	unsigned mask = (unsigned)sp->udCap - 1;
+	unsigned h = (unsigned)((key*0x9e3779b97f4a7c15ull) >> 40) & mask;
+	while(sp->udKey[h] && sp->udKey[h] != key) h = (h + 1) & mask;
+	if(!sp->udKey[h]){
+		if(!insert) return NULL;
+		sp->udKey[h] = key;
+		sp->udUsed++;
+	}
+	return &sp->udVal[h];
+}
+
+/* A device record as the callbacks' arbiter, with the handlers of its
+ * types in update order (cpArbiter.c:399-410). */
+/* fresh: the record is this step's update, where a new arbiter starts
+ * without user data */
+static void harb_fill_(cpSpace *sp, cpArbiter *arb, const cpgArb *g, int slot, int fresh)
+{
+	memset(arb, 0, sizeof(*arb));
+	arb->a = sp->shapes[g->a]; arb->b = sp->shapes[g->b];
+	arb->body_a = arb->a->body; arb->body_b = arb->b->body;
+	arb->count = g->count; arb->state = g->state;
+	arb->n = cpv(g->nx, g->ny); arb->surface_vr = cpv(g->svx, g->svy);
+	arb->e = g->e; arb->u = g->u;
+	arb->c[0] = g->c[0]; arb->c[1] = g->c[1];
+	arb->key = garb_key_(g->a, g->b);
+	arb->slot = slot;
+	arb->listPos = -1;
+	cpCollisionType typeA = arb->a->ctype, typeB = arb->b->ctype;
+	cpCollisionHandler *defaultHandler = &sp->defaultHandler;
+	cpCollisionHandler *handler = arb->handler = lookup_handler_(sp, typeA, typeB, defaultHandler);
+	cpBool swapped = arb->swapped = (typeA != handler->typeA && handler->typeA != CP_WILDCARD_COLLISION_TYPE);
+	arb->handlerA = arb->handlerB = &handler_do_nothing_;
+	if(handler != defaultHandler || sp->usesWildcards){
+		arb->handlerA = lookup_handler_(sp, (swapped ? typeB : typeA), CP_WILDCARD_COLLISION_TYPE, &handler_do_nothing_);
+		arb->handlerB = lookup_handler_(sp, (swapped ? typeA : typeB), CP_WILDCARD_COLLISION_TYPE, &handler_do_nothing_);
+	}
+	if(fresh && (g->pad & CPG_ARB_FRESH)){
+		cpDataPointer *ud = ud_slot_(sp, arb->key, 0);
+		if(ud) *ud = NULL;
+	} else {
+		cpDataPointer *ud = ud_slot_(sp, arb->key, 0);
+		arb->data = ud ? *ud : NULL;
+	}
+}
+
+static void harb_keep_data_(cpSpace *sp, const cpArbiter *arb)
+{
+	cpDataPointer *ud = ud_slot_(sp, arb->key, arb->data != NULL);
+	if(ud) *ud = arb->data;
+}
+
+static void harb_reserve_(cpSpace *sp, int n)
+{
+	if(n > sp->capharb){
+		sp->capharb = n + n/2 + 16;
+		sp->harb = (cpArbiter *)realloc(sp->harb, sizeof(cpArbiter)*(size_t)sp->capharb);
+	}
+}
+
+static int bridge_buf_(DevSet *ds, int n)
+{
+	if(ds->bridgeCap >= n) return 1;
+	if(ds->bridgeBuf) cudaFree(ds->bridgeBuf);
+	ds->bridgeBuf = NULL; ds->bridgeCap = 0;
+	if(!cuda_ok(cudaMalloc((void **)&ds->bridgeBuf, sizeof(int)*(size_t)n), "cudaMalloc handler buffers")) return 0;
+	ds->bridgeCap = n;
+	return 1;
+}
+
+/* Records by slot from the device. */
+static cpgArb *gather_slots_(DevSet *ds, const int *hslots, int n)
+{
+	cpgArb *recs = HALLOC(cpgArb, n);
+	if(n == 0) return recs;
+	if(n > ds->gatherCap){
+		if(ds->gather) cudaFree(ds->gather);
+		ds->gatherCap = n + n/2 + 64;
+		if(!cuda_ok(cudaMalloc((void **)&ds->gather, sizeof(cpgArb)*(size_t)ds->gatherCap), "gather")){ ds->gatherCap = 0; ds->gather = NULL; free(recs); return NULL; }
+	}
+	if(!bridge_buf_(ds, ds->d.arbCap + n + 1)){ free(recs); return NULL; }
+	int *dslots = ds->bridgeBuf + ds->d.arbCap + 1;
+	int ok = h2d(dslots, hslots, sizeof(int)*(size_t)n);
+	ok &= cpg_launch_gather_slots(&ds->d, dslots, ds->gather, n, lib_stream()) == 0;
+	ok &= d2h(recs, ds->gather, sizeof(cpgArb)*(size_t)n);
+	ok &= cuda_ok(cudaStreamSynchronize(lib_stream()), "gather slots");
+	if(!ok){ free(recs); return NULL; }
+	return recs;
+}
+
+static void cpgarb_from_(cpgArb *g, const cpArbiter *arb)
+{
+	g->count = arb->count; g->state = arb->state;
+	g->nx = arb->n.x; g->ny = arb->n.y;
+	g->svx = arb->surface_vr.x; g->svy = arb->surface_vr.y;
+	g->e = arb->e; g->u = arb->u;
+	g->c[0] = arb->c[0]; g->c[1] = arb->c[1];
+}
+
+/* begin and pre-solve on the step's colliding arbiters, in order
+ * (cpSpaceStep.c:259-286); the rule; the records and the list back. */
+static int handlers_collide_(cpSpace *sp)
+{
+	DevSet *ds = sp->dev;
+	const cpgWorld *W = &ds->hworld[sp->world];
+	int n = 0;
+	cpgArb *recs = gather_list_(sp, &n);
+	if(!recs) return 0;
+	int *slots = HALLOC(int, n);
+	if(n > 0 && (!d2h(slots, ds->d.arbList + W->candOff, sizeof(int)*(size_t)n) ||
+	             !cuda_ok(cudaStreamSynchronize(lib_stream()), "list slots"))){ free(recs); free(slots); return 0; }
+	space_pull(sp);
+	harb_reserve_(sp, n);
+	unsigned long long *keep = HALLOC(unsigned long long, n);
+	int nkeep = 0;
+	sp->locked++;
+	for(int i = 0; i < n; i++){
+		cpArbiter *arb = &sp->harb[i];
+		harb_fill_(sp, arb, &recs[i], slots[i], 1);
+		cpCollisionHandler *handler = arb->handler;
+		if(arb->state == CPG_ARB_FIRST && !handler->beginFunc(arb, sp, handler->userData)) cpArbiterIgnore(arb);
+		cpShape *a = arb->a, *b = arb->b;
+		if(arb->state != CPG_ARB_IGNORE && handler->preSolveFunc(arb, sp, handler->userData) && arb->state != CPG_ARB_IGNORE &&
+		   !(a->sensor || b->sensor) && !(a->body->m == INF_ && b->body->m == INF_)){
+			keep[nkeep++] = arb->key;
+		} else {
+			arb->count = 0;
+			if(arb->state != CPG_ARB_IGNORE) arb->state = CPG_ARB_NORMAL;
+		}
+		harb_keep_data_(sp, arb);
+		cpgarb_from_(&recs[i], arb);
+	}
+	/* the records back, then the list */
+	int ok = 1;
+	if(n > 0){
+		if(!bridge_buf_(ds, ds->d.arbCap + n + 1)) ok = 0;
+		else {
+			int *dslots = ds->bridgeBuf + ds->d.arbCap + 1;
+			ok &= h2d(dslots, slots, sizeof(int)*(size_t)n);
+			ok &= h2d(ds->gather, recs, sizeof(cpgArb)*(size_t)n);
+			ok &= cpg_launch_put_arbs(&ds->d, dslots, ds->gather, n, lib_stream()) == 0;
+		}
+	}
+	if(ok){
+		size_t lb = align256(sizeof(unsigned long long)*(size_t)(nkeep + 1));
+		if(ds->qbytes < lb){
+			if(ds->qbuf) cudaFree(ds->qbuf);
+			ds->qbuf = NULL; ds->qbytes = 0;
+			ok = cuda_ok(cudaMalloc(&ds->qbuf, lb), "cudaMalloc handler list");
+			if(ok) ds->qbytes = lb;
+		}
+		if(ok){
+			if(nkeep > 0) ok &= h2d(ds->qbuf, keep, sizeof(unsigned long long)*(size_t)nkeep);
+			ok &= cpg_launch_sleep_edits(&ds->d, NULL, NULL, NULL, 0, (const unsigned long long *)ds->qbuf, nkeep, lib_stream()) == 0;
+			ok &= cuda_ok(cudaStreamSynchronize(lib_stream()), "handler list");
+		}
+	}
+	free(recs); free(slots); free(keep);
+	/* cpSpaceStep.c:373 */
+	space_unlock_(sp);
+	return ok;
+}
+
+/* separate on the arbiters the cache filter moved to the cached state
+ * (cpSpaceStep.c:307-313), in slot order (the reference's is its hash
+ * set's). */
+static int cmp_int_(const void *x, const void *y) { int a = *(const int *)x, b = *(const int *)y; return (a > b) - (a < b); }
+
+static int handlers_separate_(cpSpace *sp)
+{
+	DevSet *ds = sp->dev;
+	int n = 0;
+	if(!d2h(&n, ds->bridgeBuf + ds->d.arbCap, sizeof(int)) || !cuda_ok(cudaStreamSynchronize(lib_stream()), "separations")) return 0;
+	if(n > ds->d.arbCap) n = ds->d.arbCap;
+	if(n == 0) return 1;
+	int *slots = HALLOC(int, n);
+	if(!d2h(slots, ds->bridgeBuf, sizeof(int)*(size_t)n) || !cuda_ok(cudaStreamSynchronize(lib_stream()), "separations")){ free(slots); return 0; }
+	qsort(slots, (size_t)n, sizeof(int), cmp_int_);
+	cpgArb *recs = gather_slots_(ds, slots, n);
+	if(!recs){ free(slots); return 0; }
+	harb_reserve_(sp, n);
+	sp->locked++;
+	for(int i = 0; i < n; i++){
+		if(recs[i].a < 0 || recs[i].a >= sp->nshapes || recs[i].b < 0 || recs[i].b >= sp->nshapes || !sp->shapes[recs[i].a] || !sp->shapes[recs[i].b]) continue;
+		cpArbiter *arb = &sp->harb[i];
+		harb_fill_(sp, arb, &recs[i], slots[i], 0);
+		arb->handler->separateFunc(arb, sp, arb->handler->userData);
+		harb_keep_data_(sp, arb);
+	}
+	space_unlock_(sp);
+	free(recs); free(slots);
+	return 1;
+}
+
+/* post-solve on the list with the solved impulses (cpSpaceStep.c:439-444) */
+static int handlers_post_solve_(cpSpace *sp)
+{
+	int n = 0;
+	cpgArb *recs = gather_list_(sp, &n);
+	if(!recs) return 0;
+	space_pull(sp);
+	harb_reserve_(sp, n);
+	sp->locked++;
+	for(int i = 0; i < n; i++){
+		cpArbiter *arb = &sp->harb[i];
+		harb_fill_(sp, arb, &recs[i], -1, 0);
+		arb->handler->postSolveFunc(arb, sp, arb->handler->userData);
+		harb_keep_data_(sp, arb);
+	}
+	space_unlock_(sp);
+	free(recs);
+	return 1;
+}
+
+/* cpSpace.c:490-503 on removal: the shape's cached arbiters, unless
+ * already separated, are invalidated and separated. */
+static void handlers_remove_shape_(cpSpace *sp, cpShape *s)
+{
+	if(!sp->handlersOn || !sp->dev || !sp->ownsDev) return;
+	DevSet *ds = sp->dev;
+	if(!bridge_buf_(ds, 2*(ds->d.arbCap + 1))) return;
+	int *dslots = ds->bridgeBuf + ds->d.arbCap + 1, n = 0;
+	if(cpg_launch_shape_arbs(&ds->d, (int)s->hashid, dslots, ds->bridgeBuf + ds->d.arbCap, ds->d.arbCap, lib_stream()) != 0) return;
+	if(!d2h(&n, ds->bridgeBuf + ds->d.arbCap, sizeof(int)) || !cuda_ok(cudaStreamSynchronize(lib_stream()), "shape arbiters")) return;
+	if(n > ds->d.arbCap) n = ds->d.arbCap;
+	if(n == 0) return;
+	int *slots = HALLOC(int, n);
+	if(!d2h(slots, dslots, sizeof(int)*(size_t)n) || !cuda_ok(cudaStreamSynchronize(lib_stream()), "shape arbiters")){ free(slots); return; }
+	qsort(slots, (size_t)n, sizeof(int), cmp_int_);
+	cpgArb *recs = gather_slots_(ds, slots, n);
+	if(!recs){ free(slots); return; }
+	harb_reserve_(sp, n);
+	sp->locked++;
+	for(int i = 0; i < n; i++){
+		if(recs[i].state == CPG_ARB_CACHED) continue;
+		if(recs[i].a < 0 || recs[i].a >= sp->nshapes || recs[i].b < 0 || recs[i].b >= sp->nshapes || !sp->shapes[recs[i].a] || !sp->shapes[recs[i].b]) continue;
+		cpArbiter *arb = &sp->harb[i];
+		harb_fill_(sp, arb, &recs[i], slots[i], 0);
+		arb->state = CPG_ARB_INVALIDATED;
+		arb->handler->separateFunc(arb, sp, arb->handler->userData);
+	}
+	space_unlock_(sp);
+	free(recs); free(slots);
 }
 
 /* cpSpace.c:662-678: the shape's cache brought to its body's transform,
@@ -4125,6 +4618,7 @@ void cpSpaceRemoveShape(cpSpace *sp, cpShape *s)
 	int isStatic = (body_type_(body) == CP_BODY_TYPE_STATIC);
 	if(isStatic) cpBodyActivateStatic(body, s);
 	else cpBodyActivate(body);
+	handlers_remove_shape_(sp, s);
 	/* the shape's arbiters leave the contact graph and the list
 	 * (cachedArbitersFilter, cpSpace.c:481-512) */
 	if(sp->graphOn){

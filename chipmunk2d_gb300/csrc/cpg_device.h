@@ -30,9 +30,11 @@ enum { CPG_DYNAMIC = 0, CPG_KINEMATIC = 1, CPG_STATIC = 2 };
 enum { CPG_PIVOT = 1, CPG_PIN = 2, CPG_SLIDE = 3, CPG_GROOVE = 4, CPG_DSPRING = 5, CPG_DRSPRING = 6,
        CPG_ROTLIMIT = 7, CPG_RATCHET = 8, CPG_GEAR = 9, CPG_MOTOR = 10 };
 /* arbiter states, chipmunk_structs.h:83-95 */
-enum { CPG_ARB_FIRST = 0, CPG_ARB_NORMAL = 1, CPG_ARB_IGNORE = 2, CPG_ARB_CACHED = 3 };
+enum { CPG_ARB_FIRST = 0, CPG_ARB_NORMAL = 1, CPG_ARB_IGNORE = 2, CPG_ARB_CACHED = 3, CPG_ARB_INVALIDATED = 4 };
 /* cpgArb.pad bit: the arbiter is held by a sleeping body, out of the cache */
 #define CPG_ARB_ASLEEP 1
+/* cpgArb.pad bit: the arbiter was created by this step's update (cpArbiterInit) */
+#define CPG_ARB_FRESH 2
 /* error bits latched in cpgTree.error */
 enum { CPG_ERR_NODES = 1, CPG_ERR_PAIRS = 2, CPG_ERR_CANDS = 4, CPG_ERR_ARBS = 8, CPG_ERR_BINS = 16, CPG_ERR_LEVELS = 32, CPG_ERR_FLOW = 64 };
 
@@ -379,6 +381,9 @@ typedef struct cpgSet {
 	int flowWithhold;             /* test of the wait limit: completions are not published (host value) */
 	int warmGather;               /* 1: coloured mode applies the cached impulses per body in k_integrate_vel (host value) */
 	int parMark;                  /* 1: a single world's tree is marked by k_tree_mark's parallel phases (host value) */
+	int bridge;                   /* 1: collision handlers run on the host (a single world): k_arb_update lists every
+	                                 colliding arbiter and leaves the sensor/ignore rule to the host (host value) */
+	int *sepSlots, *sepCount;     /* bridge: slots of the arbiters the cache filter separates this step */
 	int *markScratch;             /* single-world sets: the parallel marking's scratch (mark_scratch in cpg_kernels.cu) */
 	float *sapPart;               /* [4*CPG_SORT_MAX_BLOCKS] per-block centre sums for the sweep axis */
 	int hostNdyn;                 /* dynamic shapes of world 0 (host value) */
@@ -415,6 +420,9 @@ int cpg_launch_apply_ops(const cpgSet *s, void *stream);
 int cpg_launch_step(const cpgSet *s, const cpgSet *host_mirror, int mode, void *stream, float *phase_ms);
 int cpg_launch_gather_arbs(const cpgSet *s, int world, cpgArb *out, int n, void *stream);
 int cpg_launch_step_part(const cpgSet *s, const cpgSet *h, int mode, void *stream, float *phase_ms, int part);
+int cpg_launch_gather_slots(const cpgSet *s, const int *slots, cpgArb *out, int n, void *stream);
+int cpg_launch_put_arbs(const cpgSet *s, const int *slots, const cpgArb *recs, int n, void *stream);
+int cpg_launch_shape_arbs(const cpgSet *s, int shape, int *slots, int *count, int cap, void *stream);
 int cpg_launch_sleep_edits(const cpgSet *s, const unsigned long long *keys, const int *ops, const unsigned *stamps, int n,
                            const unsigned long long *listKeys, int nlist, void *stream);
 long long cpg_launch_count(int reset);

@@ -744,7 +744,12 @@ __global__ void k_arb_update(cpgSet s)
 		if(arb.state == CPG_ARB_CACHED) arb.state = CPG_ARB_FIRST;
 		bool sensor = s.ssensor[ga] || s.ssensor[gb];
 		bool infinite = (s.m[gBodyA] == CUDART_INF && s.m[gBodyB] == CUDART_INF);
-		if(arb.state != CPG_ARB_IGNORE && !sensor && !infinite){
+		if(s.bridge){
+			/* the host runs begin and pre-solve on every colliding
+			 * arbiter, then applies the rule below (cpSpaceStep.c:259-283) */
+			arb.pad = fresh ? (arb.pad | CPG_ARB_FRESH) : (arb.pad & ~CPG_ARB_FRESH);
+			s.candArb[W.candOff + i] = slot;
+		} else if(arb.state != CPG_ARB_IGNORE && !sensor && !infinite){
 			s.candArb[W.candOff + i] = slot;
 		} else {
 			arb.count = 0;
@@ -872,7 +877,14 @@ __global__ void k_arb_filter(cpgSet s)
 	 * array (sleeping bodies, then static ones) */
 	int ndyn = s.world[arb.world].ndyn;
 	if(arb.ba >= ndyn && arb.bb >= ndyn) return;
-	if(ticks >= 1 && arb.state != CPG_ARB_CACHED) arb.state = CPG_ARB_CACHED;
+	if(ticks >= 1 && arb.state != CPG_ARB_CACHED){
+		arb.state = CPG_ARB_CACHED;
+		/* the host calls the separate callbacks */
+		if(s.sepSlots){
+			int k = atomicAdd(s.sepCount, 1);
+			if(k < s.arbCap) s.sepSlots[k] = i;
+		}
+	}
 	if(ticks >= P.persistence){
 		arb.count = 0;
 		s.keys[i] = CPG_KEY_TOMB;
@@ -2253,6 +2265,31 @@ extern "C" int cpg_launch_contact_quality(const cpgSet *s, int w, double dt, dou
 }
 
 /* Copy one world's solve list of arbiters into a contiguous buffer. */
+/* Arbiter records by table slot (host callbacks of collision handlers). */
+__global__ void k_gather_slots(cpgSet s, const int *slots, cpgArb *out, int n)
+{
+	for(int i = blockIdx.x*blockDim.x + threadIdx.x; i < n; i += gridDim.x*blockDim.x) out[i] = s.arbs[slots[i]];
+}
+
+/* Records changed by the host's callbacks back into their slots. */
+__global__ void k_put_arbs(cpgSet s, const int *slots, const cpgArb *recs, int n)
+{
+	for(int i = blockIdx.x*blockDim.x + threadIdx.x; i < n; i += gridDim.x*blockDim.x) s.arbs[slots[i]] = recs[i];
+}
+
+/* Slots of the cached arbiters of one shape of world 0 (cpSpaceFilterArbiters
+ * on removal, cpSpace.c:481-521); the count may pass cap. */
+__global__ void k_shape_arbs(cpgSet s, int shape, int *slots, int *count, int cap)
+{
+	for(int i = blockIdx.x*blockDim.x + threadIdx.x; i < s.arbCap; i += gridDim.x*blockDim.x){
+		if(s.keys[i] <= CPG_KEY_TOMB) continue;
+		const cpgArb &a = s.arbs[i];
+		if(a.world != 0 || (a.a != shape && a.b != shape) || (a.pad & CPG_ARB_ASLEEP)) continue;
+		int k = atomicAdd(count, 1);
+		if(k < cap) slots[k] = i;
+	}
+}
+
 __global__ void k_gather_arbs(cpgSet s, int w, cpgArb *out, int n)
 {
 	int i = blockIdx.x*blockDim.x + threadIdx.x;
@@ -2999,6 +3036,28 @@ extern "C" int cpg_launch_sleep_edits(const cpgSet *s, const unsigned long long 
 	return check_launch("k_sleep_edits") == cudaSuccess ? 0 : -1;
 }
 
+extern "C" int cpg_launch_gather_slots(const cpgSet *s, const int *slots, cpgArb *out, int n, void *stream)
+{
+	if(n <= 0) return 0;
+	LAUNCH(k_gather_slots<<<blocks_for(n, 128), 128, 0, (cudaStream_t)stream>>>(*s, slots, out, n));
+	return check_launch("k_gather_slots") == cudaSuccess ? 0 : -1;
+}
+
+extern "C" int cpg_launch_put_arbs(const cpgSet *s, const int *slots, const cpgArb *recs, int n, void *stream)
+{
+	if(n <= 0) return 0;
+	LAUNCH(k_put_arbs<<<blocks_for(n, 128), 128, 0, (cudaStream_t)stream>>>(*s, slots, recs, n));
+	return check_launch("k_put_arbs") == cudaSuccess ? 0 : -1;
+}
+
+extern "C" int cpg_launch_shape_arbs(const cpgSet *s, int shape, int *slots, int *count, int cap, void *stream)
+{
+	cudaStream_t st = (cudaStream_t)stream;
+	cudaMemsetAsync(count, 0, sizeof(int), st);
+	LAUNCH(k_shape_arbs<<<blocks_for(s->arbCap, 256), 256, 0, st>>>(*s, shape, slots, count, cap));
+	return check_launch("k_shape_arbs") == cudaSuccess ? 0 : -1;
+}
+
 extern "C" int cpg_launch_gather_arbs(const cpgSet *s, int world, cpgArb *out, int n, void *stream)
 {
 	LAUNCH(k_gather_arbs<<<blocks_for(n, 128), 128, 0, (cudaStream_t)stream>>>(*s, world, out, n));
@@ -3154,8 +3213,9 @@ extern "C" int cpg_launch_replay_solve(const cpgSet *s, const cpgAdj *a, int nst
 }
 
 /* part 0: the whole step; part 1: up to the arbiter list (cpSpaceStep.c
- * up to :372); part 2: the rest, from the cache filter on (:378-445).
- * Between the two the host runs cpSpaceProcessComponents. */
+ * up to :372); part 2: the rest, from the cache filter on (:378-445);
+ * parts 3 and 4 split part 2 after the filter.  Between the parts the host
+ * runs cpSpaceProcessComponents and the collision-handler callbacks. */
 extern "C" int cpg_launch_step_part(const cpgSet *s, const cpgSet *h, int mode, void *stream, float *phase_ms, int part)
 {
 	cudaStream_t st = (cudaStream_t)stream;
@@ -3180,7 +3240,7 @@ extern "C" int cpg_launch_step_part(const cpgSet *s, const cpgSet *h, int mode, 
 	 * fails the step: the kernels after it would run on a half-done step */
 	cudaError_t coop = cudaSuccess;
 #define COOP(kernel, threads) do { cudaError_t e_ = launch_coop((const void *)(kernel), (threads), &sv, 0, st); if(e_ != cudaSuccess && coop == cudaSuccess) coop = e_; } while(0)
-	if(part == 2) goto second;
+	if(part >= 2) goto second;
 	cudaMemsetAsync(s->stats, 0, 16*sizeof(int), st);
 	LAUNCH(k_reset_prev<<<dim3(perWorldX, W), 128, 0, st>>>(*s));
 	LAUNCH(k_integrate_pos<<<blocks_for(h->totalBodies, 128), 128, 0, st>>>(*s));
@@ -3226,7 +3286,11 @@ extern "C" int cpg_launch_step_part(const cpgSet *s, const cpgSet *h, int mode, 
 	}
 	if(part == 1) goto done;
 second:
-	LAUNCH(k_arb_filter<<<blocks_for(h->arbCap, 256), 256, 0, st>>>(*s));
+	if(part != 4){
+		if(s->sepCount) cudaMemsetAsync(s->sepCount, 0, sizeof(int), st);
+		LAUNCH(k_arb_filter<<<blocks_for(h->arbCap, 256), 256, 0, st>>>(*s));
+	}
+	if(part == 3) goto done;
 	if(timing) cudaEventRecord(ev[4], st);
 	if(colored) COOP(k_color_coop, 512);
 	else if(W == 1){

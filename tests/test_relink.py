@@ -12,7 +12,7 @@ import numpy as np
 import pytest
 
 REPO = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
-PROGRAMS = ["relink_program.c", "relink_program2.c", "relink_program3.c", "relink_program4.c"]
+PROGRAMS = ["relink_program.c", "relink_program2.c", "relink_program3.c", "relink_program4.c", "relink_program5.c"]
 GPU_DIR = os.path.join(REPO, "chipmunk2d_gb300", "_build")
 ORACLE_DIR = os.path.join(REPO, "oracle", "_build")
 REF_DIR = os.path.join(REPO, "oracle", "_ref")
@@ -65,7 +65,7 @@ def test_builds_against_the_reference_headers_and_links_the_gpu_library(tmp_path
     build(tmp_path, "relink_ref_headers", GPU_DIR, "chipmunk_gb300", ref_headers=inc, program=program)
 
 
-@pytest.mark.parametrize("program", PROGRAMS + ["relink_program5.c"])
+@pytest.mark.parametrize("program", PROGRAMS)
 def test_oracle_matches_the_reference_on_the_program(tmp_path, oracle_lib, program):
     """The same program on the reference library and on the oracle: bit for
     bit, through removals and additions mid-run, caller-placed objects,
