@@ -248,6 +248,9 @@ struct cpSpace {
 	int usesWildcards, handlersOn;
 	cpCollisionHandler **handlers; int nhandlers, caphandlers;
 	cpArbiter *harb; int capharb;            /* the arbiters of one round of callbacks */
+	/* cpSpaceUseSpatialHash: both indices are spatial hashes */
+	int useHash, hashCells;
+	cpFloat hashDim;
 	unsigned long long *udKey; cpDataPointer *udVal; int udCap, udUsed;   /* arbiter user data by key */
 };
 
@@ -482,6 +485,8 @@ static size_t carve_set(cpgSet *d, char *base, int pass)
 		CARVE(markScratch, int, one ? (9*nn1 + 2*np1 + 4*(size_t)d->totalPairs + 1025) : 1);
 	}
 	CARVE(sapPart, float, 4*CPG_SORT_MAX_BLOCKS);
+	CARVE(gcells, int, 2*d->numcells);
+	CARVE(gbinHandle, int, 2*d->gbinCap); CARVE(gbinNext, int, 2*d->gbinCap);
 	CARVE(stats, int, 16);
 	return total;
 }
@@ -853,6 +858,28 @@ static DevSet *devset_build(cpSpace **spaces, int nspaces, DevSet *from)
 	if(g_cap_arbs){ arbCap = 1; while(arbCap < g_cap_arbs) arbCap *= 2; }
 	if(from && arbCap < from->d.arbCap) arbCap = from->d.arbCap;
 	d->arbCap = (int)arbCap;
+	/* a single space on the spatial hash: its grids and bin pools, the
+	 * pools sized from the shapes' boxes now with room to grow */
+	d->useHash = 0; d->numcells = 0; d->gbinCap = 0; d->celldim = 0.0;
+	if(nspaces == 1 && spaces[0]->useHash){
+		cpSpace *sp = spaces[0];
+		d->useHash = 1;
+		d->numcells = sp->hashCells;
+		d->celldim = sp->hashDim;
+		long long bins = 0;
+		for(int i = 0; i < sp->nshapes; i++){
+			cpShape *sh = sp->shapes[i];
+			if(!sh) continue;
+			double w = floor(sh->bb.r/sp->hashDim) - floor(sh->bb.l/sp->hashDim) + 1.0;
+			double h = floor(sh->bb.t/sp->hashDim) - floor(sh->bb.b/sp->hashDim) + 1.0;
+			double cells = (w > 0.0 && h > 0.0) ? w*h : 1.0;
+			bins += cells < (double)sp->hashCells ? (long long)cells : sp->hashCells;
+		}
+		long long cap = 4*bins + 16LL*sp->nshapes + 1024;
+		if(from && from->d.useHash && cap < from->d.gbinCap) cap = from->d.gbinCap;
+		if(cap > 0x3fffffffLL) cap = 0x3fffffffLL;
+		d->gbinCap = (int)cap;
+	}
 
 	size_t bytes = carve_set(d, NULL, 0);
 	ds->slabBytes = bytes;
@@ -870,6 +897,7 @@ static DevSet *devset_build(cpSpace **spaces, int nspaces, DevSet *from)
 	ok &= cuda_ok(cudaMemsetAsync(ds->slab, 0, bytes, st), "memset set");
 	ok &= cuda_ok(cudaMemsetAsync(d->dbins, 0xff, sizeof(int)*(size_t)(NDB > 0 ? NDB : 1), st), "memset bins");
 	ok &= cuda_ok(cudaMemsetAsync(d->sbins, 0xff, sizeof(int)*(size_t)(NSB > 0 ? NSB : 1), st), "memset bins");
+	if(d->useHash) ok &= cuda_ok(cudaMemsetAsync(d->gcells, 0xff, sizeof(int)*2*(size_t)d->numcells, st), "memset cells");
 	ok &= cuda_ok(cudaMallocHost((void **)&ds->hparams, sizeof(cpgParams)*(size_t)nspaces*CPG_PARAM_RING), "cudaMallocHost");
 	if(ok) memset(ds->hparams, 0, sizeof(cpgParams)*(size_t)nspaces*CPG_PARAM_RING);
 	for(int i = 0; i < CPG_PARAM_RING && ok; i++) ok &= cuda_ok(cudaEventCreateWithFlags(&ds->paramEvent[i], cudaEventDisableTiming), "event");
@@ -896,6 +924,8 @@ static DevSet *devset_build(cpSpace **spaces, int nspaces, DevSet *from)
 	for(int w = 0; w < nspaces; w++){
 		cpgTree *T = &trees[w];
 		T->dynRoot = -1; T->statRoot = -1; T->treeStamp = 0;
+		T->gbinTop[0] = T->gbinTop[1] = 0; T->gbinFree[0] = T->gbinFree[1] = -1;
+		T->gstamp[0] = T->gstamp[1] = 1;
 		T->freeNode = -1; T->freePair = -1;
 		T->dynSize = next_prime(0); T->statSize = next_prime(0);
 	}
@@ -1238,6 +1268,10 @@ static int space_supported(cpSpace *sp)
 {
 	if(sleep_mode_(sp) && (sp->mode != CP_GPU_SOLVER_ORDERED || (sp->dev && !sp->ownsDev))){
 		set_error(CP_GPU_ERR_UNSUPPORTED, "sleeping runs in the exact-order mode of a standalone space");
+		return 0;
+	}
+	if(sp->useHash && (sp->mode != CP_GPU_SOLVER_ORDERED || (sp->dev && !sp->ownsDev))){
+		set_error(CP_GPU_ERR_UNSUPPORTED, "the spatial hash runs in the exact-order mode of a standalone space");
 		return 0;
 	}
 	if(sp->handlersOn && (sp->mode != CP_GPU_SOLVER_ORDERED || (sp->dev && !sp->ownsDev))){
@@ -1948,6 +1982,7 @@ int cpGpuBatchStep(cpGpuBatch *b, cpFloat dt, int steps, int use_graph)
 	for(int i = 0; i < b->n; i++){
 		if(!space_supported(b->spaces[i])) return -1;
 		if(sleep_mode_(b->spaces[i])){ set_error(CP_GPU_ERR_UNSUPPORTED, "sleeping runs in a standalone space, not in a cpGpuBatch"); return -1; }
+		if(b->spaces[i]->useHash || b->spaces[i]->handlersOn){ set_error(CP_GPU_ERR_UNSUPPORTED, "the spatial hash and collision handlers run in a standalone space, not in a cpGpuBatch"); return -1; }
 	}
 	if(!b->dev){
 		b->dev = devset_build(b->spaces, b->n, NULL);
@@ -4548,6 +4583,26 @@ void cpSpaceReindexStatic(cpSpace *sp)
 	memset(op, 0, sizeof(*op));
 	op->kind = CPG_OP_REINDEX_STATIC;
 	op->isStatic = 1;
+	sp->structDirty = 1;
+	sp->editGen++;
+}
+
+/* cpSpace.c:687-701: both indices become spatial hashes of cells of size
+ * dim, next_prime(count) cells each, holding the same shapes (replayed on
+ * the device as one edit, in call order with the others). */
+void cpSpaceUseSpatialHash(cpSpace *sp, cpFloat dim, int count)
+{
+	if(!space_edit_ok(sp)) return;
+	sp->useHash = 1;
+	sp->hashDim = dim;
+	sp->hashCells = (int)next_prime((unsigned)count);
+	if(sp->nops == sp->capops){
+		sp->capops = sp->capops ? 2*sp->capops : 256;
+		sp->ops = (cpgOp *)realloc(sp->ops, sizeof(cpgOp)*(size_t)sp->capops);
+	}
+	cpgOp *op = &sp->ops[sp->nops++];
+	memset(op, 0, sizeof(*op));
+	op->kind = CPG_OP_USE_HASH;
 	sp->structDirty = 1;
 	sp->editGen++;
 }

@@ -36,7 +36,8 @@ enum { CPG_ARB_FIRST = 0, CPG_ARB_NORMAL = 1, CPG_ARB_IGNORE = 2, CPG_ARB_CACHED
 /* cpgArb.pad bit: the arbiter was created by this step's update (cpArbiterInit) */
 #define CPG_ARB_FRESH 2
 /* error bits latched in cpgTree.error */
-enum { CPG_ERR_NODES = 1, CPG_ERR_PAIRS = 2, CPG_ERR_CANDS = 4, CPG_ERR_ARBS = 8, CPG_ERR_BINS = 16, CPG_ERR_LEVELS = 32, CPG_ERR_FLOW = 64 };
+enum { CPG_ERR_NODES = 1, CPG_ERR_PAIRS = 2, CPG_ERR_CANDS = 4, CPG_ERR_ARBS = 8, CPG_ERR_BINS = 16, CPG_ERR_LEVELS = 32, CPG_ERR_FLOW = 64,
+       CPG_ERR_HASH = 128 };
 
 /* upper bound on the blocks of the cooperative sweep-and-prune sort */
 #define CPG_SORT_MAX_BLOCKS 1024
@@ -87,6 +88,10 @@ typedef struct cpgTree {
 	int pairsLive;
 	int maxChain;
 	int moved;                    /* leaves reinserted this step */
+	/* spatial hash (a single world): bin pool tops and free lists of the
+	 * dynamic and static grids, the grids' stamps (cpSpaceHash.stamp) */
+	int gbinTop[2], gbinFree[2];
+	unsigned gstamp[2];
 } cpgTree;
 
 /* AABB-tree node (cpBBTree.c:46-60), 96 bytes.  Each box coordinate x
@@ -199,7 +204,7 @@ typedef struct cpgRow {
  * reference builds the leaf's fattened box immediately,
  * cpBBTree.c:605-616); a removal (cpSpaceRemoveShape, cpBodySetType)
  * names the shape and the index it leaves (cpBBTree.c:619-630). */
-enum { CPG_OP_INSERT = 0, CPG_OP_REMOVE = 1, CPG_OP_REINDEX = 2, CPG_OP_REINDEX_STATIC = 3 };
+enum { CPG_OP_INSERT = 0, CPG_OP_REMOVE = 1, CPG_OP_REINDEX = 2, CPG_OP_REINDEX_STATIC = 3, CPG_OP_USE_HASH = 4 };
 /* CPG_OP_REINDEX (cpSpaceReindexShape) carries the shape's new cached box
  * and its body's velocity; CPG_OP_REINDEX_STATIC (cpSpaceReindexStatic)
  * re-indexes every static leaf against the shapes' uploaded boxes. */
@@ -384,6 +389,12 @@ typedef struct cpgSet {
 	int bridge;                   /* 1: collision handlers run on the host (a single world): k_arb_update lists every
 	                                 colliding arbiter and leaves the sensor/ignore rule to the host (host value) */
 	int *sepSlots, *sepCount;     /* bridge: slots of the arbiters the cache filter separates this step */
+	/* spatial hash (cpSpaceUseSpatialHash, a single world): the handle sets
+	 * are the leaf sets, the handles nodes; cells of the dynamic then the
+	 * static grid, and a bin pool for each (gbinCap bins each) */
+	int useHash, numcells, gbinCap;
+	double celldim;
+	int *gcells, *gbinHandle, *gbinNext;
 	int *markScratch;             /* single-world sets: the parallel marking's scratch (mark_scratch in cpg_kernels.cu) */
 	float *sapPart;               /* [4*CPG_SORT_MAX_BLOCKS] per-block centre sums for the sweep axis */
 	int hostNdyn;                 /* dynamic shapes of world 0 (host value) */

@@ -90,6 +90,11 @@ __global__ void k_apply_ops(cpgSet s)
 		 * as it stops the tree step: the tree may hold a half-made leaf */
 		if(c.T->error) break;
 		cpgOp op = s.ops[W.opOff + i];
+		if(s.useHash){
+			if(op.kind == CPG_OP_USE_HASH) hash_switch(c, s);
+			else hash_apply_op(c, s, op);
+			continue;
+		}
 		if(op.kind == CPG_OP_REMOVE) tree_remove(c, op);
 		else if(op.kind == CPG_OP_REINDEX) tree_reindex(c, op);
 		else if(op.kind == CPG_OP_REINDEX_STATIC) tree_reindex_static(c);
@@ -113,6 +118,17 @@ __global__ void k_transfer_pools(cpgSet to, cpgSet from)
 	for(int k = i0; k < WO.pairCap; k += n) to.pairs[WN.pairOff + k] = from.pairs[WO.pairOff + k];
 	for(int k = i0; k < WO.dbinCap; k += n) to.dbins[WN.dbinOff + k] = from.dbins[WO.dbinOff + k];
 	for(int k = i0; k < WO.sbinCap; k += n) to.sbins[WN.sbinOff + k] = from.sbins[WO.sbinOff + k];
+	/* spatial hash grids: the cells and the bin pools carry over (a set
+	 * rebuilt from a tree set has fresh grids, made by the switch edit) */
+	if(to.useHash && from.useHash && to.numcells == from.numcells){
+		for(int k = i0; k < 2*from.numcells; k += n) to.gcells[k] = from.gcells[k];
+		for(int w = 0; w < 2; w++){
+			for(int k = i0; k < from.gbinCap; k += n){
+				to.gbinHandle[(size_t)w*to.gbinCap + k] = from.gbinHandle[(size_t)w*from.gbinCap + k];
+				to.gbinNext[(size_t)w*to.gbinCap + k] = from.gbinNext[(size_t)w*from.gbinCap + k];
+			}
+		}
+	}
 	if(i0 == 0) to.tree[0] = from.tree[0];
 }
 
@@ -290,6 +306,18 @@ __global__ void k_tree(cpgSet s, int stagedNodes)
 		nn = s.tree[w].nodeTop;
 		for(int i = threadIdx.x; i < nn; i += blockDim.x) gnodes[i] = snodes[i];
 	}
+}
+
+/* cpSpaceHashReindexQuery for a space on the spatial hash: one thread, in
+ * the reference's order (the hash's stamps make each pair's test depend
+ * on the handles before it). */
+__global__ void k_hash_step(cpgSet s)
+{
+	if(blockIdx.x != 0 || threadIdx.x != 0 || !s.params[0].active) return;
+	TreeCtx c = make_tree_ctx(&s, 0);
+	c.collide = 1;
+	if(!c.T->error) hash_reindex_query(c, s);
+	c.T->ncand = c.ncand;
 }
 
 /* ---- parallel marking of a single world's tree (cpg_mark.cuh) ----
@@ -3269,8 +3297,11 @@ extern "C" int cpg_launch_step_part(const cpgSet *s, const cpgSet *h, int mode, 
 		}
 		/* one warp per world in a batch; a single world's leaf scan takes
 		 * 256 threads (thread 0 alone reinserts and marks) */
-		LAUNCH(k_tree<<<W, W == 1 ? 256 : 32, smem, st>>>(sv, staged));
-		if(sv.parMark) COOP(k_tree_mark, CPG_MARK_THREADS);
+		if(h->useHash) LAUNCH(k_hash_step<<<1, 32, 0, st>>>(*s));
+		else {
+			LAUNCH(k_tree<<<W, W == 1 ? 256 : 32, smem, st>>>(sv, staged));
+			if(sv.parMark) COOP(k_tree_mark, CPG_MARK_THREADS);
+		}
 	}
 	if(timing) cudaEventRecord(ev[2], st);
 	cudaMemsetAsync(s->nbCount, 0, CPG_PAIR_TYPES*sizeof(int), st);

@@ -347,11 +347,103 @@ __device__ bool q_tree_segment(const cpgSet &s, const cpgWorld &W, const cpgNode
 	return true;
 }
 
+/* ---- the spatial hash's queries (cpSpaceHash.c:353-525), for a space on
+ * cpSpaceUseSpatialHash: the cells of the box, each handle once by the
+ * grid's stamp; the segment walks the cells it crosses in order ---- */
+static __device__ __forceinline__ int qh_cell(int x, int y, int n)
+{
+	unsigned long long hx = (unsigned long long)(long long)x, hy = (unsigned long long)(long long)y;
+	return (int)((hx*1640531513ull ^ hy*2654435789ull) % (unsigned long long)n);
+}
+
+static __device__ __forceinline__ int qh_floor(double f)
+{
+	int i = (int)f;
+	return (f < 0.0 && f != (double)i) ? i - 1 : i;
+}
+
+/* which: 0 the dynamic grid, 1 the static one; skip: a shape passed over
+ * without a stamp (the querying shape), -1 for none */
+template <typename Leaf>
+static __device__ void q_hash(const cpgSet &s, cpgNode *nodes, int which, BB qb, int skip, Leaf leaf)
+{
+	cpgTree &T = s.tree[0];
+	const int *cells = s.gcells + (size_t)which*s.numcells;
+	const int *bh = s.gbinHandle + (size_t)which*s.gbinCap, *bn = s.gbinNext + (size_t)which*s.gbinCap;
+	unsigned stamp = T.gstamp[which];
+	double dim = s.celldim;
+	int l = qh_floor(qb.l/dim), r = qh_floor(qb.r/dim), b = qh_floor(qb.b/dim), t = qh_floor(qb.t/dim);
+	for(int i = l; i <= r; i++){
+		for(int j = b; j <= t; j++){
+			int guard = 0;
+			for(int k = cells[qh_cell(i, j, s.numcells)]; k >= 0 && guard <= s.gbinCap; k = bn[k], guard++){
+				cpgNode &nd = nodes[bh[k]];
+				if(nd.stamp == stamp || nd.obj == skip) continue;
+				leaf(nd.obj);
+				nd.stamp = stamp;
+			}
+		}
+	}
+	T.gstamp[which] = stamp + 1;
+}
+
+static __device__ double q_hash_segment(const cpgSet &s, const cpgWorld &W, cpgNode *nodes, int which, const cpgQuery &q,
+                                        double t_exit, QOut &o)
+{
+	cpgTree &T = s.tree[0];
+	const int *cells = s.gcells + (size_t)which*s.numcells;
+	const int *bh = s.gbinHandle + (size_t)which*s.gbinCap, *bn = s.gbinNext + (size_t)which*s.gbinCap;
+	unsigned stamp = T.gstamp[which];
+	double inv = 1.0/s.celldim;
+	V2 a = v2(q.ax*inv, q.ay*inv), b = v2(q.bx*inv, q.by*inv);
+	int cell_x = qh_floor(a.x), cell_y = qh_floor(a.y);
+	double t = 0.0;
+	int x_inc, y_inc;
+	double temp_v, temp_h;
+	if(b.x > a.x){ x_inc = 1; temp_h = (floor(a.x + 1.0) - a.x); } else { x_inc = -1; temp_h = (a.x - floor(a.x)); }
+	if(b.y > a.y){ y_inc = 1; temp_v = (floor(a.y + 1.0) - a.y); } else { y_inc = -1; temp_v = (a.y - floor(a.y)); }
+	double dx = fabs(b.x - a.x), dy = fabs(b.y - a.y);
+	double dt_dx = (dx != 0.0 ? 1.0/dx : CUDART_INF), dt_dy = (dy != 0.0 ? 1.0/dy : CUDART_INF);
+	double next_h = (temp_h != 0.0 ? temp_h*dt_dx : dt_dx);
+	double next_v = (temp_v != 0.0 ? temp_v*dt_dy : dt_dy);
+	for(int guard = 0; t < t_exit; guard++){
+		if(guard > (1 << 24)) break;
+		double tc = 1.0;
+		int bguard = 0;
+		for(int k = cells[qh_cell(cell_x, cell_y, s.numcells)]; k >= 0 && bguard <= s.gbinCap; k = bn[k], bguard++){
+			cpgNode &nd = nodes[bh[k]];
+			if(nd.stamp == stamp) continue;
+			tc = dmin(tc, q_leaf(s, W, q, nd.obj, o));
+			nd.stamp = stamp;
+		}
+		t_exit = dmin(t_exit, tc);
+		if(next_v < next_h){ cell_y += y_inc; t = next_v; next_v += dt_dy; }
+		else { cell_x += x_inc; t = next_h; next_h += dt_dx; }
+	}
+	T.gstamp[which] = stamp + 1;
+	return t_exit;
+}
+
+__device__ void query_one(const cpgSet &s, int w, const cpgQuery *queries, int i, cpgHit *hits, int cap,
+                          int *counts, int brute, int *status);
+
 __global__ void k_query(cpgSet s, int w, const cpgQuery *queries, int nq, cpgHit *hits, int cap,
                         int *counts, int brute, int *status)
 {
+	if(s.useHash){
+		/* the grids' stamps order the queries: one thread, in call order */
+		if(blockIdx.x != 0 || threadIdx.x != 0) return;
+		for(int i = 0; i < nq; i++) query_one(s, w, queries, i, hits, cap, counts, brute, status);
+		return;
+	}
 	int i = blockIdx.x*blockDim.x + threadIdx.x;
 	if(i >= nq) return;
+	query_one(s, w, queries, i, hits, cap, counts, brute, status);
+}
+
+__device__ void query_one(const cpgSet &s, int w, const cpgQuery *queries, int i, cpgHit *hits, int cap,
+                          int *counts, int brute, int *status)
+{
 	const cpgWorld &W = s.world[w];
 	const cpgTree &T = s.tree[w];
 	const cpgNode *nodes = s.nodes + W.nodeOff;
@@ -403,6 +495,17 @@ __global__ void k_query(cpgSet s, int w, const cpgQuery *queries, int nq, cpgHit
 				} else if(!bbintersects(sb, qb)) continue;
 				q_leaf(s, W, q, k, o);
 			}
+		}
+	} else if(s.useHash){
+		cpgNode *hn = s.nodes + W.nodeOff;
+		if(q.kind == CPG_Q_SEGMENT || q.kind == CPG_Q_SEGMENT_FIRST){
+			q_hash_segment(s, W, hn, 1, q, 1.0, o);
+			q_hash_segment(s, W, hn, 0, q, q.kind == CPG_Q_SEGMENT_FIRST ? o.best.d : 1.0, o);
+		} else {
+			BB qb = (q.kind == CPG_Q_BB) ? bbnew(q.ax, q.ay, q.bx, q.by)
+			        : bbnew(q.ax - dmax(q.r, 0.0), q.ay - dmax(q.r, 0.0), q.ax + dmax(q.r, 0.0), q.ay + dmax(q.r, 0.0));
+			for(int which = 0; which < 2; which++)
+				q_hash(s, hn, which, qb, -1, [&](int shape){ q_leaf(s, W, q, shape, o); });
 		}
 	} else if(q.kind == CPG_Q_SEGMENT || q.kind == CPG_Q_SEGMENT_FIRST){
 		ok = q_tree_segment(s, W, nodes, T.statRoot, q, 1.0, o);
@@ -503,7 +606,11 @@ __global__ void k_shape_query(cpgSet s, int w, cpgProbe p, const double *planes,
 	BB qb = bbnew(p.bbl, p.bbb, p.bbr, p.bbt);
 	SQOut o; o.hits = hits; o.cap = cap; o.n = 0; o.any = 0;
 	bool ok = true;
-	if(brute){
+	if(s.useHash){
+		cpgNode *hn = s.nodes + W.nodeOff;
+		for(int which = 0; which < 2; which++)
+			q_hash(s, hn, which, qb, p.slot, [&](int shape){ shape_query_leaf(s, W, p, a, shape, o); });
+	} else if(brute){
 		for(int pass = 0; pass < 2; pass++){
 			for(int k = 0; k < W.nshapes; k++){
 				int g = W.shapeOff + k;

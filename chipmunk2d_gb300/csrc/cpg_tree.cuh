@@ -746,6 +746,277 @@ __device__ void tree_reindex_static(TreeCtx &c)
 	T->treeStamp++;
 }
 
+/* ------------------------------------------------------------------ */
+/* Spatial hash (src/cpSpaceHash.c) for a space that called
+ * cpSpaceUseSpatialHash: a single world.  Handles are nodes of the pool
+ * and the handle sets are the leaf sets; each grid's cells hold lists of
+ * bins (head insertion) from the grid's own bin pool. */
+struct GridCtx {
+	int *cells;
+	int *bh, *bn;           /* bin handle, bin next */
+	int cap;
+	int *top, *freeBin;
+	unsigned *stamp;
+	int numcells;
+	double celldim;
+};
+
+__device__ __forceinline__ GridCtx grid_ctx(const cpgSet &s, cpgTree *T, int which)
+{
+	GridCtx g;
+	g.cells = s.gcells + (size_t)which*s.numcells;
+	g.bh = s.gbinHandle + (size_t)which*s.gbinCap;
+	g.bn = s.gbinNext + (size_t)which*s.gbinCap;
+	g.cap = s.gbinCap;
+	g.top = &T->gbinTop[which]; g.freeBin = &T->gbinFree[which];
+	g.stamp = &T->gstamp[which];
+	g.numcells = s.numcells;
+	g.celldim = s.celldim;
+	return g;
+}
+
+/* hash_func (cpSpaceHash.c:223-227) over cpHashValue */
+__device__ __forceinline__ int hash_cell(int x, int y, int n)
+{
+	unsigned long long hx = (unsigned long long)(long long)x, hy = (unsigned long long)(long long)y;
+	return (int)((hx*1640531513ull ^ hy*2654435789ull) % (unsigned long long)n);
+}
+
+/* floor_int (cpSpaceHash.c:229-235) */
+__device__ __forceinline__ int floor_int(double f)
+{
+	int i = (int)f;
+	return (f < 0.0 && f != (double)i) ? i - 1 : i;
+}
+
+__device__ __forceinline__ void grid_clear(GridCtx &g)
+{
+	for(int i = 0; i < g.numcells; i++) g.cells[i] = -1;
+	*g.top = 0; *g.freeBin = -1;
+}
+
+__device__ __forceinline__ bool grid_contains(const GridCtx &g, int cell, int hand, int guardMax)
+{
+	int guard = 0;
+	for(int b = g.cells[cell]; b >= 0 && guard <= guardMax; b = g.bn[b], guard++) if(g.bh[b] == hand) return true;
+	return false;
+}
+
+__device__ __forceinline__ bool grid_push(GridCtx &g, cpgTree *T, int cell, int hand)
+{
+	int b;
+	if(*g.freeBin >= 0){ b = *g.freeBin; *g.freeBin = g.bn[b]; }
+	else if(*g.top < g.cap) b = (*g.top)++;
+	else { T->error |= CPG_ERR_HASH; return false; }
+	g.bh[b] = hand;
+	g.bn[b] = g.cells[cell];
+	g.cells[cell] = b;
+	return true;
+}
+
+/* hashHandle (cpSpaceHash.c:237-265) */
+__device__ void grid_hash_handle(GridCtx &g, cpgTree *T, int hand, BB bb)
+{
+	double dim = g.celldim;
+	int l = floor_int(bb.l/dim), r = floor_int(bb.r/dim);
+	int b = floor_int(bb.b/dim), t = floor_int(bb.t/dim);
+	for(int i = l; i <= r; i++){
+		for(int j = b; j <= t; j++){
+			int cell = hash_cell(i, j, g.numcells);
+			if(grid_contains(g, cell, hand, g.cap)) continue;
+			if(!grid_push(g, T, cell, hand)) return;
+		}
+	}
+}
+
+/* A removed handle's bins leave every cell (the reference leaves them as
+ * orphans that the next query through the cell unlinks,
+ * cpSpaceHash.c:330-349; the other bins keep their order either way). */
+__device__ void grid_unlink(GridCtx &g, int hand)
+{
+	for(int i = 0; i < g.numcells; i++){
+		int prev = -1;
+		int guard = 0;
+		for(int b = g.cells[i]; b >= 0 && guard <= g.cap; guard++){
+			int next = g.bn[b];
+			if(g.bh[b] == hand){
+				if(prev >= 0) g.bn[prev] = next; else g.cells[i] = next;
+				g.bn[b] = *g.freeBin; *g.freeBin = b;
+			} else prev = b;
+			b = next;
+		}
+	}
+}
+
+/* cpSpaceHashInsert (cpSpaceHash.c:269-274): a new handle at the head of
+ * its bin in the handle set, hashed into the cells of the shape's box */
+__device__ void hash_insert(TreeCtx &c, const cpgSet &s, int shape, bool isStatic, BB bb)
+{
+	cpgTree *T = c.T;
+	int hand = node_alloc(c);
+	if(hand < 0) return;
+	cpgNode &nd = c.nodes[hand];
+	nd.obj = shape;
+	set_node_bb(nd, bb);
+	nd.parent = -1; nd.A = -1; nd.B = -1;
+	nd.stamp = 0;
+	nd.pairs = -1;
+	int *bins = isStatic ? c.sbins : c.dbins;
+	unsigned *size = isStatic ? &T->statSize : &T->dynSize;
+	unsigned *entries = isStatic ? &T->statEntries : &T->dynEntries;
+	unsigned idx = (unsigned)(c.shash[shape] % *size);
+	nd.binNext = bins[idx];
+	bins[idx] = hand;
+	(*entries)++;
+	if(*entries >= *size) leafset_resize(c, bins, isStatic ? c.sbinCap : c.dbinCap, size);
+	GridCtx g = grid_ctx(s, T, isStatic ? 1 : 0);
+	grid_hash_handle(g, T, hand, bb);
+}
+
+/* cpSpaceHashRemove (cpSpaceHash.c:300-309); returns whether found */
+__device__ bool hash_remove(TreeCtx &c, const cpgSet &s, int shape, bool isStatic)
+{
+	cpgTree *T = c.T;
+	int *bins = isStatic ? c.sbins : c.dbins;
+	unsigned size = isStatic ? T->statSize : T->dynSize;
+	unsigned *entries = isStatic ? &T->statEntries : &T->dynEntries;
+	if(size == 0) return false;
+	unsigned idx = (unsigned)(c.shash[shape] % size);
+	int prev = -1, hand = bins[idx];
+	for(int guard = 0; hand >= 0; guard++){
+		if(guard > c.nodeCap){ T->error |= CPG_ERR_BINS; return false; }
+		if(c.nodes[hand].obj == shape) break;
+		prev = hand;
+		hand = c.nodes[hand].binNext;
+	}
+	if(hand < 0) return false;
+	if(prev >= 0) c.nodes[prev].binNext = c.nodes[hand].binNext;
+	else bins[idx] = c.nodes[hand].binNext;
+	(*entries)--;
+	GridCtx g = grid_ctx(s, T, isStatic ? 1 : 0);
+	grid_unlink(g, hand);
+	node_recycle(c, hand);
+	return true;
+}
+
+/* cpSpaceHashRehash (cpSpaceHash.c:282-287) of the static grid, each
+ * handle hashed again in handle-set order with its shape's box */
+__device__ void hash_rehash_static(TreeCtx &c, const cpgSet &s)
+{
+	cpgTree *T = c.T;
+	GridCtx g = grid_ctx(s, T, 1);
+	grid_clear(g);
+	for(unsigned i = 0; i < T->statSize && (int)i < c.sbinCap; i++){
+		int guard = 0;
+		for(int n = c.sbins[i]; n >= 0; n = c.nodes[n].binNext){
+			if(++guard > c.nodeCap){ T->error |= CPG_ERR_BINS; return; }
+			BB bb = shape_bb(c, c.nodes[n].obj);
+			set_node_bb(c.nodes[n], bb);
+			grid_hash_handle(g, T, n, bb);
+		}
+	}
+}
+
+/* The index edits of a space on the spatial hash (k_apply_ops). */
+__device__ void hash_apply_op(TreeCtx &c, const cpgSet &s, const cpgOp &op)
+{
+	bool isStatic = op.isStatic != 0;
+	BB bb = bbnew(op.l, op.b, op.r, op.t);
+	if(op.kind == CPG_OP_INSERT) hash_insert(c, s, op.shape, isStatic, bb);
+	else if(op.kind == CPG_OP_REMOVE){ if(!hash_remove(c, s, op.shape, isStatic)) c.T->error |= CPG_ERR_BINS; }
+	else if(op.kind == CPG_OP_REINDEX){
+		/* cpSpaceHashRehashObject (cpSpaceHash.c:276-286): a new handle */
+		if(hash_remove(c, s, op.shape, isStatic)) hash_insert(c, s, op.shape, isStatic, bb);
+	}
+	else if(op.kind == CPG_OP_REINDEX_STATIC) hash_rehash_static(c, s);
+}
+
+/* cpSpaceUseSpatialHash (cpSpace.c:687-701): the trees give way to two
+ * hashes holding the same shapes, the static ones first, each in its leaf
+ * set's order.  The order is kept in the candidate buffer meanwhile. */
+__device__ void hash_switch(TreeCtx &c, const cpgSet &s)
+{
+	cpgTree *T = c.T;
+	int *order = (int *)c.cands;
+	int cap = c.candCap*(int)(sizeof(cpgCand)/sizeof(int));
+	int n = 0, nstat = 0;
+	for(int pass = 0; pass < 2; pass++){
+		const int *bins = pass == 0 ? c.sbins : c.dbins;
+		unsigned size = pass == 0 ? T->statSize : T->dynSize;
+		int binCap = pass == 0 ? c.sbinCap : c.dbinCap;
+		for(unsigned i = 0; i < size && (int)i < binCap; i++){
+			int guard = 0;
+			for(int l = bins[i]; l >= 0; l = c.nodes[l].binNext){
+				if(++guard > c.nodeCap || n >= cap){ T->error |= CPG_ERR_BINS; return; }
+				order[n++] = c.nodes[l].obj;
+			}
+		}
+		if(pass == 0) nstat = n;
+	}
+	/* fresh pools, sets and grids */
+	T->dynRoot = T->statRoot = -1;
+	T->freeNode = -1; T->nodeTop = 0;
+	T->freePair = -1; T->pairTop = 0;
+	T->dynSize = T->statSize = (unsigned)cpg_primes[0];
+	T->dynEntries = T->statEntries = 0;
+	for(int i = 0; i < c.dbinCap; i++) c.dbins[i] = -1;
+	for(int i = 0; i < c.sbinCap; i++) c.sbins[i] = -1;
+	for(int w = 0; w < 2; w++){
+		GridCtx g = grid_ctx(s, T, w);
+		grid_clear(g);
+		T->gstamp[w] = 1;
+	}
+	for(int k = 0; k < n; k++){
+		int shape = order[k];
+		hash_insert(c, s, shape, k < nstat, shape_bb(c, shape));
+	}
+}
+
+#ifdef __CUDACC__
+/* cpSpaceHashReindexQuery (cpSpaceHash.c:394-441) with cpSpaceCollideShapes
+ * as the candidate emitter: each dynamic handle in handle-set order meets
+ * the handles already in the cells it covers, then joins them; then each
+ * queries the static grid (cpSpatialIndexCollideStatic).  Collision ids
+ * start at 0: the hash keeps none. */
+__device__ void hash_reindex_query(TreeCtx &c, const cpgSet &s)
+{
+	cpgTree *T = c.T;
+	GridCtx g = grid_ctx(s, T, 0), sg = grid_ctx(s, T, 1);
+	grid_clear(g);
+	for(int pass = 0; pass < 2; pass++){
+		if(pass == 1 && T->statEntries == 0) break;
+		for(unsigned i = 0; i < T->dynSize && (int)i < c.dbinCap; i++){
+			int guard = 0;
+			for(int hand = c.dbins[i]; hand >= 0; hand = c.nodes[hand].binNext){
+				if(++guard > c.nodeCap){ T->error |= CPG_ERR_BINS; return; }
+				int obj = c.nodes[hand].obj;
+				BB bb = shape_bb(c, obj);
+				GridCtx &q = pass == 0 ? g : sg;
+				double dim = q.celldim;
+				int l = floor_int(bb.l/dim), r = floor_int(bb.r/dim);
+				int b = floor_int(bb.b/dim), t = floor_int(bb.t/dim);
+				for(int ci = l; ci <= r; ci++){
+					for(int cj = b; cj <= t; cj++){
+						int cell = hash_cell(ci, cj, q.numcells);
+						if(pass == 0 && grid_contains(q, cell, hand, q.cap)) continue;
+						int bguard = 0;
+						for(int bn = q.cells[cell]; bn >= 0; bn = q.bn[bn]){
+							if(++bguard > q.cap){ T->error |= CPG_ERR_HASH; return; }
+							int other = q.bh[bn];
+							if(c.nodes[other].stamp == *q.stamp || c.nodes[other].obj == obj) continue;
+							emit(c, obj, c.nodes[other].obj, -1, 0u);
+							c.nodes[other].stamp = *q.stamp;
+						}
+						if(pass == 0 && !grid_push(q, T, cell, hand)) return;
+					}
+				}
+				(*q.stamp)++;
+			}
+		}
+	}
+}
+#endif
+
 /* cpBBTree.c:498-517: a leaf whose shape left its fattened box */
 __device__ __forceinline__ bool leaf_moved(const TreeCtx &c, int leaf)
 {

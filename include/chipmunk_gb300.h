@@ -263,6 +263,9 @@ void cpSpaceStep(cpSpace *space, cpFloat dt);                        /* cpSpace.
  * the bodies' transforms at the call and the trees updated as the
  * reference's are, before the next step or query. */
 void cpSpaceReindexStatic(cpSpace *space);                           /* cpSpace.h:240 */
+/* The spatial hash as both indices (cpSpace.h:249): the broadphase then
+ * visits pairs in the hash's order, as the reference's does. */
+void cpSpaceUseSpatialHash(cpSpace *space, cpFloat dim, int count);   /* cpSpace.h:249 */
 void cpSpaceReindexShape(cpSpace *space, cpShape *shape);            /* cpSpace.h:242 */
 void cpSpaceReindexShapesForBody(cpSpace *space, cpBody *body);      /* cpSpace.h:244 */
 /* A callback run once when the current (or next) step, body/shape/

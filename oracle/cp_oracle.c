@@ -206,6 +206,18 @@ typedef struct Tree {
 	int isDynamic;       /* dynamic tree: fattened boxes, owns the stamp */
 } Tree;
 
+/* The cells of a spatial hash (src/cpSpaceHash.c:28-43, 99-115): each cell
+ * a list of bins (head insertion) naming a handle.  A handle is a node of
+ * the index's pool whose leaf set is the hash's handle set; its stamp is
+ * the handle's stamp. */
+typedef struct HashGrid {
+	int numcells;
+	cpFloat celldim;
+	int *cells;                          /* first bin of each cell, -1 */
+	int *binHandle, *binNext; int nbins, capbins, freeBin;
+	cpTimestamp stamp;
+} HashGrid;
+
 typedef struct ArbMap {
 	int cap;             /* power of two */
 	int used;            /* live + tombstones */
@@ -234,6 +246,10 @@ struct cpSpace {
 	Pair *pairs; int npairs, cappairs, freePair;
 	Tree dynTree, statTree;
 	cpTimestamp treeStamp;
+	/* cpSpaceUseSpatialHash: both indices are spatial hashes; the trees'
+	 * leaf sets are the handle sets */
+	int useHash;
+	HashGrid dynGrid, statGrid;
 
 	/* pairs that passed the box test in the last step (for broadphase checks) */
 	int *candPairs; int ncand, capcand;
@@ -2243,8 +2259,13 @@ static int leaf_update(cpSpace *sp, Tree *tree, int leaf)
 }
 
 /* cpBBTree.c:605-616 with LeafAddPairs (:521-537) */
+static void hash_insert_(cpSpace *sp, Tree *tree, cpShape *s);
+static void hash_remove_(cpSpace *sp, Tree *tree, cpShape *s);
+static void hash_rehash_(cpSpace *sp, Tree *tree);
+
 static void tree_insert(cpSpace *sp, Tree *tree, cpShape *s)
 {
+	if(sp->useHash){ hash_insert_(sp, tree, s); return; }
 	LeafSet *set = &tree->leaves;
 	int leaf = node_alloc(sp);
 	Node *nd = &sp->nodes[leaf];
@@ -2348,6 +2369,8 @@ void cpSpaceDestroy(cpSpace *sp)
 	sp->candPairs = NULL;
 	free(sp->post); sp->post = NULL; sp->npost = sp->cappost = 0;
 	free(sp->sleeping); free(sp->roused); sp->sleeping = sp->roused = NULL;
+	HashGrid *grids[2] = { &sp->dynGrid, &sp->statGrid };
+	for(int i = 0; i < 2; i++){ free(grids[i]->cells); free(grids[i]->binHandle); free(grids[i]->binNext); memset(grids[i], 0, sizeof(HashGrid)); }
 	for(int i = 0; i < sp->nhandlers; i++) free(sp->handlers[i]);
 	free(sp->handlers); sp->handlers = NULL; sp->nhandlers = sp->caphandlers = 0;
 	sp->nsleeping = sp->capsleeping = sp->nroused = sp->caproused = 0;
@@ -2433,6 +2456,12 @@ void cpSpaceReindexShape(cpSpace *sp, cpShape *s)
 	/* a sleeping body's shapes are in the static index */
 	int isStatic = (body_type(s->body) == CP_BODY_TYPE_STATIC || cpBodyIsSleeping(s->body));
 	Tree *tree = isStatic ? &sp->statTree : &sp->dynTree;
+	if(sp->useHash){
+		/* cpSpaceHashRehashObject (cpSpaceHash.c:276-286): a new handle */
+		hash_remove_(sp, tree, s);
+		hash_insert_(sp, tree, s);
+		return;
+	}
 	int leaf = s->leaf;
 	if(leaf_update(sp, tree, leaf)){
 		if(!isStatic){
@@ -2462,6 +2491,7 @@ void cpSpaceReindexStatic(cpSpace *sp)
 	LeafSet *set = &tree->leaves;
 	for(unsigned i = 0; i < set->size; i++)
 		for(int n = set->bins[i]; n >= 0; n = sp->nodes[n].binNext) cpShapeCacheBB(sp->nodes[n].obj);
+	if(sp->useHash){ hash_rehash_(sp, tree); return; }
 	if(tree->root < 0) return;
 	for(unsigned i = 0; i < set->size; i++){
 		int n = set->bins[i];
@@ -2495,6 +2525,7 @@ cpConstraint *cpSpaceAddConstraint(cpSpace *sp, cpConstraint *c)
  * order), the tree and every pair list, and is recycled. */
 static void tree_remove(cpSpace *sp, Tree *tree, cpShape *s)
 {
+	if(sp->useHash){ hash_remove_(sp, tree, s); return; }
 	LeafSet *set = &tree->leaves;
 	unsigned idx = (unsigned)(s->hashid % set->size);
 	int prev = -1, leaf = set->bins[idx];
@@ -2507,6 +2538,230 @@ static void tree_remove(cpSpace *sp, Tree *tree, cpShape *s)
 	pairs_clear(sp, leaf);
 	node_recycle(sp, leaf);
 	s->leaf = -1;
+}
+
+/* ========================================================================
+ * Spatial hash: src/cpSpaceHash.c (cpSpaceUseSpatialHash, cpSpace.c:687-701)
+ * ====================================================================== */
+/* hash_func (cpSpaceHash.c:223-227): the cell coordinates as cpHashValue */
+static unsigned hash_cell_(int x, int y, int n)
+{
+	return (unsigned)((((cpHashValue)x)*1640531513ul ^ ((cpHashValue)y)*2654435789ul) % (cpHashValue)n);
+}
+
+/* floor_int (cpSpaceHash.c:229-235) */
+static int floor_int_(cpFloat f)
+{
+	int i = (int)f;
+	return (f < 0.0f && f != i ? i - 1 : i);
+}
+
+static void grid_init_(HashGrid *g, cpFloat celldim, int numcells)
+{
+	free(g->cells); free(g->binHandle); free(g->binNext);
+	memset(g, 0, sizeof(*g));
+	g->numcells = numcells;
+	g->celldim = celldim;
+	g->cells = (int *)malloc(sizeof(int)*(size_t)numcells);
+	for(int i = 0; i < numcells; i++) g->cells[i] = -1;
+	g->freeBin = -1;
+	g->stamp = 1;
+}
+
+static int grid_bin_(HashGrid *g)
+{
+	if(g->freeBin >= 0){ int b = g->freeBin; g->freeBin = g->binNext[b]; return b; }
+	if(g->nbins == g->capbins){
+		g->capbins = g->capbins ? 2*g->capbins : 256;
+		g->binHandle = (int *)realloc(g->binHandle, sizeof(int)*(size_t)g->capbins);
+		g->binNext = (int *)realloc(g->binNext, sizeof(int)*(size_t)g->capbins);
+	}
+	return g->nbins++;
+}
+
+/* clearTable (cpSpaceHash.c:126-130) */
+static void grid_clear_(HashGrid *g)
+{
+	for(int i = 0; i < g->numcells; i++){
+		int b = g->cells[i];
+		while(b >= 0){ int next = g->binNext[b]; g->binNext[b] = g->freeBin; g->freeBin = b; b = next; }
+		g->cells[i] = -1;
+	}
+}
+
+static int grid_contains_(const HashGrid *g, int cell, int hand)
+{
+	for(int b = g->cells[cell]; b >= 0; b = g->binNext[b]) if(g->binHandle[b] == hand) return 1;
+	return 0;
+}
+
+static void grid_push_(HashGrid *g, int cell, int hand)
+{
+	int b = grid_bin_(g);
+	g->binHandle[b] = hand;
+	g->binNext[b] = g->cells[cell];
+	g->cells[cell] = b;
+}
+
+/* hashHandle (cpSpaceHash.c:237-265) */
+static void grid_hash_handle_(HashGrid *g, int hand, cpBB bb)
+{
+	cpFloat dim = g->celldim;
+	int l = floor_int_(bb.l/dim), r = floor_int_(bb.r/dim);
+	int b = floor_int_(bb.b/dim), t = floor_int_(bb.t/dim);
+	for(int i = l; i <= r; i++){
+		for(int j = b; j <= t; j++){
+			unsigned idx = hash_cell_(i, j, g->numcells);
+			if(grid_contains_(g, (int)idx, hand)) continue;
+			grid_push_(g, (int)idx, hand);
+		}
+	}
+}
+
+/* A removed handle's bins leave every cell.  The reference unlinks them
+ * when a query next walks the cell (remove_orphaned_handles,
+ * cpSpaceHash.c:330-349); the other bins keep their order either way. */
+static void grid_unlink_(HashGrid *g, int hand)
+{
+	for(int i = 0; i < g->numcells; i++){
+		int *link = &g->cells[i];
+		while(*link >= 0){
+			int b = *link;
+			if(g->binHandle[b] == hand){ *link = g->binNext[b]; g->binNext[b] = g->freeBin; g->freeBin = b; }
+			else link = &g->binNext[b];
+		}
+	}
+}
+
+/* cpSpaceHashInsert (cpSpaceHash.c:269-274): a new handle at the head of
+ * its bin in the handle set, then hashed into the cells of the shape's box */
+static void hash_insert_(cpSpace *sp, Tree *tree, cpShape *s)
+{
+	LeafSet *set = &tree->leaves;
+	int hand = node_alloc(sp);
+	Node *nd = &sp->nodes[hand];
+	memset(nd, 0, sizeof(*nd));
+	nd->obj = s;
+	nd->parent = -1; nd->A = nd->B = -1; nd->pairs = -1;
+	nd->stamp = 0;
+	unsigned idx = (unsigned)(s->hashid % set->size);
+	nd->binNext = set->bins[idx];
+	set->bins[idx] = hand;
+	set->entries++;
+	if(set->entries >= set->size) leafset_resize(sp, set);
+	s->leaf = hand;
+	grid_hash_handle_(tree->isDynamic ? &sp->dynGrid : &sp->statGrid, hand, s->bb);
+}
+
+/* cpSpaceHashRemove (cpSpaceHash.c:300-309) */
+static void hash_remove_(cpSpace *sp, Tree *tree, cpShape *s)
+{
+	LeafSet *set = &tree->leaves;
+	unsigned idx = (unsigned)(s->hashid % set->size);
+	int prev = -1, hand = set->bins[idx];
+	while(hand >= 0 && sp->nodes[hand].obj != s){ prev = hand; hand = sp->nodes[hand].binNext; }
+	ORC_ASSERT(hand >= 0, "shape missing from its index");
+	if(prev >= 0) sp->nodes[prev].binNext = sp->nodes[hand].binNext;
+	else set->bins[idx] = sp->nodes[hand].binNext;
+	set->entries--;
+	grid_unlink_(tree->isDynamic ? &sp->dynGrid : &sp->statGrid, hand);
+	node_recycle(sp, hand);
+	s->leaf = -1;
+}
+
+/* cpSpaceHashRehash (cpSpaceHash.c:282-287): every handle hashed again,
+ * in handle-set order */
+static void hash_rehash_(cpSpace *sp, Tree *tree)
+{
+	HashGrid *g = tree->isDynamic ? &sp->dynGrid : &sp->statGrid;
+	grid_clear_(g);
+	LeafSet *set = &tree->leaves;
+	for(unsigned i = 0; i < set->size; i++)
+		for(int n = set->bins[i]; n >= 0; n = sp->nodes[n].binNext) grid_hash_handle_(g, n, sp->nodes[n].obj->bb);
+}
+
+/* cpSpaceHashReindexQuery (cpSpaceHash.c:432-441) with cpSpaceCollideShapes:
+ * each dynamic handle, in handle-set order, meets the handles already in
+ * the cells it covers, then joins them (queryRehash_helper, :394-430);
+ * then each queries the static hash (cpSpatialIndexCollideStatic). */
+static void hash_reindex_query_(cpSpace *sp)
+{
+	HashGrid *g = &sp->dynGrid, *sg = &sp->statGrid;
+	LeafSet *set = &sp->dynTree.leaves;
+	grid_clear_(g);
+	for(unsigned i = 0; i < set->size; i++){
+		for(int hand = set->bins[i]; hand >= 0; hand = sp->nodes[hand].binNext){
+			cpShape *obj = sp->nodes[hand].obj;
+			cpBB bb = obj->bb;
+			cpFloat dim = g->celldim;
+			int l = floor_int_(bb.l/dim), r = floor_int_(bb.r/dim);
+			int b = floor_int_(bb.b/dim), t = floor_int_(bb.t/dim);
+			for(int ci = l; ci <= r; ci++){
+				for(int cj = b; cj <= t; cj++){
+					int cell = (int)hash_cell_(ci, cj, g->numcells);
+					if(grid_contains_(g, cell, hand)) continue;
+					/* query_helper (cpSpaceHash.c:353-372) */
+					for(int bn = g->cells[cell]; bn >= 0; bn = g->binNext[bn]){
+						int other = g->binHandle[bn];
+						if(sp->nodes[other].stamp == g->stamp || sp->nodes[other].obj == obj) continue;
+						collide_shapes(sp, obj, sp->nodes[other].obj, 0);
+						sp->nodes[other].stamp = g->stamp;
+					}
+					grid_push_(g, cell, hand);
+				}
+			}
+			g->stamp++;
+		}
+	}
+	if(sp->statTree.leaves.entries == 0) return;
+	for(unsigned i = 0; i < set->size; i++){
+		for(int hand = set->bins[i]; hand >= 0; hand = sp->nodes[hand].binNext){
+			/* cpSpaceHashQuery (cpSpaceHash.c:374-392) on the static hash */
+			cpShape *obj = sp->nodes[hand].obj;
+			cpBB bb = obj->bb;
+			cpFloat dim = sg->celldim;
+			int l = floor_int_(bb.l/dim), r = floor_int_(bb.r/dim);
+			int b = floor_int_(bb.b/dim), t = floor_int_(bb.t/dim);
+			for(int ci = l; ci <= r; ci++){
+				for(int cj = b; cj <= t; cj++){
+					int cell = (int)hash_cell_(ci, cj, sg->numcells);
+					for(int bn = sg->cells[cell]; bn >= 0; bn = sg->binNext[bn]){
+						int other = sg->binHandle[bn];
+						if(sp->nodes[other].stamp == sg->stamp || sp->nodes[other].obj == obj) continue;
+						collide_shapes(sp, obj, sp->nodes[other].obj, 0);
+						sp->nodes[other].stamp = sg->stamp;
+					}
+				}
+			}
+			sg->stamp++;
+		}
+	}
+}
+
+/* cpSpace.c:687-701: both indices become spatial hashes holding the same
+ * shapes, the static ones copied first, each in its old index's order */
+void cpSpaceUseSpatialHash(cpSpace *sp, cpFloat dim, int count)
+{
+	int nstat = (int)sp->statTree.leaves.entries, ndyn = (int)sp->dynTree.leaves.entries;
+	cpShape **order = (cpShape **)malloc(sizeof(cpShape *)*(size_t)(nstat + ndyn + 1));
+	int k = 0;
+	Tree *trees[2] = { &sp->statTree, &sp->dynTree };
+	for(int t = 0; t < 2; t++){
+		LeafSet *set = &trees[t]->leaves;
+		for(unsigned i = 0; i < set->size; i++)
+			for(int n = set->bins[i]; n >= 0; n = sp->nodes[n].binNext) order[k++] = sp->nodes[n].obj;
+	}
+	/* a fresh pool: the trees and their pair cache go */
+	sp->nnodes = 0; sp->freeNode = -1;
+	sp->npairs = 0; sp->freePair = -1;
+	free(sp->dynTree.leaves.bins); free(sp->statTree.leaves.bins);
+	sp->dynTree.root = -1; leafset_init(&sp->dynTree.leaves);
+	sp->statTree.root = -1; leafset_init(&sp->statTree.leaves);
+	sp->useHash = 1;
+	grid_init_(&sp->statGrid, dim, (int)next_prime((unsigned)count));
+	grid_init_(&sp->dynGrid, dim, (int)next_prime((unsigned)count));
+	for(int i = 0; i < k; i++) hash_insert_(sp, i < nstat ? &sp->statTree : &sp->dynTree, order[i]);
+	free(order);
 }
 
 /* cpArrayDeleteObj (cpArray.c:76-88): the last element takes the hole. */
@@ -3178,7 +3433,8 @@ void cpSpaceStep(cpSpace *sp, cpFloat dt)
 	for(unsigned i = 0; i < set->size; i++){
 		for(int n = set->bins[i]; n >= 0; n = sp->nodes[n].binNext) cpShapeCacheBB(sp->nodes[n].obj);
 	}
-	tree_reindex_query(sp);
+	if(sp->useHash) hash_reindex_query_(sp);
+	else tree_reindex_query(sp);
 	space_unlock_(sp);
 
 	process_components_(sp, dt);
@@ -3859,9 +4115,68 @@ static cpFloat subtree_segment_query_(cpSpace *sp, int n, QueryCtx *q, cpFloat t
 	return t_exit;
 }
 
-static void tree_query_(cpSpace *sp, Tree *t, QueryCtx *q) { if(t->root >= 0) subtree_query_(sp, t->root, q); }
+/* cpSpaceHashQuery (cpSpaceHash.c:353-392): the cells of the box, each
+ * handle once (its stamp) */
+static void hash_query_(cpSpace *sp, HashGrid *g, QueryCtx *q)
+{
+	cpBB bb = q->bb;
+	cpFloat dim = g->celldim;
+	int l = floor_int_(bb.l/dim), r = floor_int_(bb.r/dim);
+	int b = floor_int_(bb.b/dim), t = floor_int_(bb.t/dim);
+	for(int i = l; i <= r; i++){
+		for(int j = b; j <= t; j++){
+			int cell = (int)hash_cell_(i, j, g->numcells);
+			for(int bn = g->cells[cell]; bn >= 0; bn = g->binNext[bn]){
+				int other = g->binHandle[bn];
+				if(sp->nodes[other].stamp == g->stamp) continue;
+				query_leaf_(q, sp->nodes[other].obj);
+				sp->nodes[other].stamp = g->stamp;
+			}
+		}
+	}
+	g->stamp++;
+}
+
+/* cpSpaceHashSegmentQuery (cpSpaceHash.c:443-525): the cells along the
+ * segment in order, a grid walk */
+static void hash_segment_query_(cpSpace *sp, HashGrid *g, QueryCtx *q, cpFloat t_exit)
+{
+	cpVect a = cpvmult(q->a, 1.0f/g->celldim), b = cpvmult(q->b, 1.0f/g->celldim);
+	int cell_x = floor_int_(a.x), cell_y = floor_int_(a.y);
+	cpFloat t = 0;
+	int x_inc, y_inc;
+	cpFloat temp_v, temp_h;
+	if(b.x > a.x){ x_inc = 1; temp_h = (floor(a.x + 1.0f) - a.x); } else { x_inc = -1; temp_h = (a.x - floor(a.x)); }
+	if(b.y > a.y){ y_inc = 1; temp_v = (floor(a.y + 1.0f) - a.y); } else { y_inc = -1; temp_v = (a.y - floor(a.y)); }
+	cpFloat dx = fabs_(b.x - a.x), dy = fabs_(b.y - a.y);
+	cpFloat dt_dx = (dx ? 1.0f/dx : ORC_INF), dt_dy = (dy ? 1.0f/dy : ORC_INF);
+	cpFloat next_h = (temp_h ? temp_h*dt_dx : dt_dx);
+	cpFloat next_v = (temp_v ? temp_v*dt_dy : dt_dy);
+	while(t < t_exit){
+		int cell = (int)hash_cell_(cell_x, cell_y, g->numcells);
+		/* segmentQuery_helper (:395-418) */
+		cpFloat tc = 1.0f;
+		for(int bn = g->cells[cell]; bn >= 0; bn = g->binNext[bn]){
+			int other = g->binHandle[bn];
+			if(sp->nodes[other].stamp == g->stamp) continue;
+			tc = fmin_(tc, query_leaf_(q, sp->nodes[other].obj));
+			sp->nodes[other].stamp = g->stamp;
+		}
+		t_exit = fmin_(t_exit, tc);
+		if(next_v < next_h){ cell_y += y_inc; t = next_v; next_v += dt_dy; }
+		else { cell_x += x_inc; t = next_h; next_h += dt_dx; }
+	}
+	g->stamp++;
+}
+
+static void tree_query_(cpSpace *sp, Tree *t, QueryCtx *q)
+{
+	if(sp->useHash){ hash_query_(sp, t->isDynamic ? &sp->dynGrid : &sp->statGrid, q); return; }
+	if(t->root >= 0) subtree_query_(sp, t->root, q);
+}
 static void tree_segment_query_(cpSpace *sp, Tree *t, QueryCtx *q, cpFloat t_exit)
 {
+	if(sp->useHash){ hash_segment_query_(sp, t->isDynamic ? &sp->dynGrid : &sp->statGrid, q, t_exit); return; }
 	if(t->root >= 0) subtree_segment_query_(sp, t->root, q, t_exit);
 }
 
@@ -3962,12 +4277,46 @@ static void subtree_shape_query_(cpSpace *sp, int n, cpBB bb, ShapeQueryCtx *q)
 	}
 }
 
+/* ShapeQuery over cpSpaceHashQuery (cpSpaceHash.c:353-392) */
+static void hash_shape_query_(cpSpace *sp, HashGrid *g, cpBB bb, ShapeQueryCtx *q)
+{
+	cpFloat dim = g->celldim;
+	int l = floor_int_(bb.l/dim), r = floor_int_(bb.r/dim);
+	int b = floor_int_(bb.b/dim), t = floor_int_(bb.t/dim);
+	for(int i = l; i <= r; i++){
+		for(int j = b; j <= t; j++){
+			int cell = (int)hash_cell_(i, j, g->numcells);
+			for(int bn = g->cells[cell]; bn >= 0; bn = g->binNext[bn]){
+				int other = g->binHandle[bn];
+				cpShape *sb = sp->nodes[other].obj;
+				if(sp->nodes[other].stamp == g->stamp || sb == q->shape) continue;
+				cpShape *sa = q->shape;
+				if(!filter_reject_(sa->filter, sb->filter)){
+					cpContactPointSet set = cpShapesCollide(sa, sb);
+					if(set.count){
+						if(q->func) q->func(sb, &set, q->data);
+						q->anyCollision = !(sa->sensor || sb->sensor);
+					}
+				}
+				sp->nodes[other].stamp = g->stamp;
+			}
+		}
+	}
+	g->stamp++;
+}
+
 /* cpSpaceQuery.c:230-246 */
 cpBool cpSpaceShapeQuery(cpSpace *sp, cpShape *shape, cpSpaceShapeQueryFunc func, void *data)
 {
 	cpBody *body = shape->body;
 	cpBB bb = (body ? shape_update(shape, body->transform) : shape->bb);
 	ShapeQueryCtx q = {shape, func, data, cpFalse};
+	if(sp->useHash){
+		hash_shape_query_(sp, &sp->dynGrid, bb, &q);
+		hash_shape_query_(sp, &sp->statGrid, bb, &q);
+		run_post_step_(sp);
+		return q.anyCollision;
+	}
 	if(sp->dynTree.root >= 0) subtree_shape_query_(sp, sp->dynTree.root, bb, &q);
 	if(sp->statTree.root >= 0) subtree_shape_query_(sp, sp->statTree.root, bb, &q);
 	run_post_step_(sp);
