@@ -3744,23 +3744,73 @@ static cpgArb *gather_list_(cpSpace *sp, int *count)
 	return host;
 }
 
-/* The graph entries of the arbiter list brought to the device's records
- * (after a solve: accumulated impulses for cpBodyEachArbiter). */
+/* A graph entry's record fields from the device's record (links kept). */
+static void graph_fill_keep_(cpSpace *sp, cpArbiter *arb, const cpgArb *g)
+{
+	unsigned long long key = arb->key;
+	int pa = arb->prevA, na = arb->nextA, pb = arb->prevB, nb = arb->nextB, lp = arb->listPos;
+	garb_fill_(sp, arb, g);
+	arb->key = key; arb->prevA = pa; arb->nextA = na; arb->prevB = pb; arb->nextB = nb; arb->listPos = lp;
+}
+
+/* The graph entries brought to the device's records for cpBodyEachArbiter:
+ * the list's (after a solve: accumulated impulses) and, by key, the ones
+ * sleeping bodies hold. */
 static void graph_refresh_(cpSpace *sp)
 {
 	if(sp->graphFresh || !sp->dev || sp->structDirty || !sp->ownsDev) return;
 	int n = 0;
 	cpgArb *recs = gather_list_(sp, &n);
 	if(!recs) return;
-	for(int i = 0; i < n && i < sp->nglist; i++){
-		cpArbiter *arb = &sp->garb[sp->glist[i]];
-		unsigned long long key = arb->key;
-		int pa = arb->prevA, na = arb->nextA, pb = arb->prevB, nb = arb->nextB, lp = arb->listPos;
-		garb_fill_(sp, arb, &recs[i]);
-		arb->key = key; arb->prevA = pa; arb->nextA = na; arb->prevB = pb; arb->nextB = nb; arb->listPos = lp;
-	}
+	for(int i = 0; i < n && i < sp->nglist; i++) graph_fill_keep_(sp, &sp->garb[sp->glist[i]], &recs[i]);
 	free(recs);
+	int m = 0;
+	int *idx = HALLOC(int, sp->ngarb);
+	unsigned long long *keys = HALLOC(unsigned long long, sp->ngarb);
+	for(int g = 0; g < sp->ngarb; g++){
+		if(sp->garb[g].a && sp->garb[g].listPos < 0){ idx[m] = g; keys[m] = sp->garb[g].key; m++; }
+	}
+	DevSet *ds = sp->dev;
+	if(m > 0 && m <= ds->gatherCap){
+		size_t kb = sizeof(unsigned long long)*(size_t)m;
+		if(ds->qbytes < kb){
+			if(ds->qbuf) cudaFree(ds->qbuf);
+			ds->qbuf = NULL; ds->qbytes = 0;
+			if(cuda_ok(cudaMalloc(&ds->qbuf, kb), "cudaMalloc graph keys")) ds->qbytes = kb;
+		}
+		cpgArb *out = HALLOC(cpgArb, m);
+		if(ds->qbytes >= kb && h2d(ds->qbuf, keys, kb) &&
+		   cpg_launch_gather_keys(&ds->d, (const unsigned long long *)ds->qbuf, ds->gather, m, lib_stream()) == 0 &&
+		   d2h(out, ds->gather, sizeof(cpgArb)*(size_t)m) && cuda_ok(cudaStreamSynchronize(lib_stream()), "graph records")){
+			for(int i = 0; i < m; i++) if(out[i].a >= 0) graph_fill_keep_(sp, &sp->garb[idx[i]], &out[i]);
+		}
+		free(out);
+	}
+	free(idx); free(keys);
 	sp->graphFresh = 1;
+}
+
+/* The shape pairs of the device's arbiter list, 2 ints each, or NULL. */
+static int *gather_pairs_(cpSpace *sp, int *count)
+{
+	DevSet *ds = sp->dev;
+	cpgTree T;
+	*count = 0;
+	if(!d2h(&T, ds->d.tree + sp->world, sizeof(cpgTree)) || !cuda_ok(cudaStreamSynchronize(lib_stream()), "list")) return NULL;
+	int n = T.narb;
+	if(n > ds->gatherCap){
+		if(ds->gather) cudaFree(ds->gather);
+		ds->gatherCap = n + n/2 + 64;
+		if(!cuda_ok(cudaMalloc((void **)&ds->gather, sizeof(cpgArb)*(size_t)ds->gatherCap), "gather")){ ds->gatherCap = 0; ds->gather = NULL; return NULL; }
+	}
+	int *host = HALLOC(int, 2*n);
+	if(n > 0){
+		cpg_launch_gather_pairs(&ds->d, sp->world, (int *)ds->gather, n, lib_stream());
+		d2h(host, ds->gather, sizeof(int)*2*(size_t)n);
+		if(!cuda_ok(cudaStreamSynchronize(lib_stream()), "list pairs")){ free(host); return NULL; }
+	}
+	*count = n;
+	return host;
 }
 
 /* The graph starts from the last step's list, threaded in list order as
@@ -4027,8 +4077,8 @@ static void process_components_(cpSpace *sp, cpFloat dt)
 static int sleep_sync_(cpSpace *sp, cpFloat dt)
 {
 	int n = 0;
-	cpgArb *recs = gather_list_(sp, &n);
-	if(!recs) return 0;
+	int *pairs = gather_pairs_(sp, &n);
+	if(!pairs) return 0;
 	space_pull(sp);
 	for(int i = 0; i < sp->nglist; i++){
 		int g = sp->glist[i];
@@ -4040,10 +4090,14 @@ static int sleep_sync_(cpSpace *sp, cpFloat dt)
 	sp->nglist = 0;
 	for(int i = 0; i < n; i++){
 		int g = garb_alloc_(sp);
-		garb_fill_(sp, &sp->garb[g], &recs[i]);
+		cpArbiter *arb = &sp->garb[g];
+		/* the shapes and key now; the rest when cpBodyEachArbiter asks */
+		arb->a = sp->shapes[pairs[2*i]]; arb->b = sp->shapes[pairs[2*i + 1]];
+		arb->body_a = arb->a->body; arb->body_b = arb->b->body;
+		arb->key = garb_key_(pairs[2*i], pairs[2*i + 1]);
 		glist_push_(sp, g);
 	}
-	free(recs);
+	free(pairs);
 	process_components_(sp, dt);
 	sp->graphFresh = 0;
 	if(sp->sleepMutated && !space_device_ready_(sp)) return 0;

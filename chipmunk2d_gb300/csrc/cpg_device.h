@@ -432,6 +432,8 @@ int cpg_launch_step(const cpgSet *s, const cpgSet *host_mirror, int mode, void *
 int cpg_launch_gather_arbs(const cpgSet *s, int world, cpgArb *out, int n, void *stream);
 int cpg_launch_step_part(const cpgSet *s, const cpgSet *h, int mode, void *stream, float *phase_ms, int part);
 int cpg_launch_gather_slots(const cpgSet *s, const int *slots, cpgArb *out, int n, void *stream);
+int cpg_launch_gather_pairs(const cpgSet *s, int world, int *out, int n, void *stream);
+int cpg_launch_gather_keys(const cpgSet *s, const unsigned long long *keys, cpgArb *out, int n, void *stream);
 int cpg_launch_put_arbs(const cpgSet *s, const int *slots, const cpgArb *recs, int n, void *stream);
 int cpg_launch_shape_arbs(const cpgSet *s, int shape, int *slots, int *count, int cap, void *stream);
 int cpg_launch_sleep_edits(const cpgSet *s, const unsigned long long *keys, const int *ops, const unsigned *stamps, int n,

@@ -2325,6 +2325,27 @@ __global__ void k_gather_arbs(cpgSet s, int w, cpgArb *out, int n)
 	out[i] = s.arbs[s.arbList[s.world[w].candOff + i]];
 }
 
+/* The shape pairs of a world's arbiter list, in info order (the contact
+ * graph's needs: 8 bytes per arbiter instead of the whole record). */
+__global__ void k_gather_pairs(cpgSet s, int w, int2 *out, int n)
+{
+	int i = blockIdx.x*blockDim.x + threadIdx.x;
+	if(i >= n) return;
+	const cpgArb &a = s.arbs[s.arbList[s.world[w].candOff + i]];
+	out[i] = make_int2(a.a, a.b);
+}
+
+/* Whole records by table key (arbiters out of the list: those held by
+ * sleeping bodies); a missing key gives a record with shape -1. */
+__global__ void k_gather_keys(cpgSet s, const unsigned long long *keys, cpgArb *out, int n)
+{
+	int i = blockIdx.x*blockDim.x + threadIdx.x;
+	if(i >= n) return;
+	int slot = arb_find(s, keys[i]);
+	if(slot >= 0) out[i] = s.arbs[slot];
+	else { out[i].a = -1; out[i].b = -1; }
+}
+
 /* ------------------------------------------------------------------ */
 /* Coloured mode (single-world sets): sweep-and-prune, colouring, solve */
 
@@ -3084,6 +3105,20 @@ extern "C" int cpg_launch_shape_arbs(const cpgSet *s, int shape, int *slots, int
 	cudaMemsetAsync(count, 0, sizeof(int), st);
 	LAUNCH(k_shape_arbs<<<blocks_for(s->arbCap, 256), 256, 0, st>>>(*s, shape, slots, count, cap));
 	return check_launch("k_shape_arbs") == cudaSuccess ? 0 : -1;
+}
+
+extern "C" int cpg_launch_gather_pairs(const cpgSet *s, int world, int *out, int n, void *stream)
+{
+	if(n <= 0) return 0;
+	LAUNCH(k_gather_pairs<<<blocks_for(n, 256), 256, 0, (cudaStream_t)stream>>>(*s, world, (int2 *)out, n));
+	return check_launch("k_gather_pairs") == cudaSuccess ? 0 : -1;
+}
+
+extern "C" int cpg_launch_gather_keys(const cpgSet *s, const unsigned long long *keys, cpgArb *out, int n, void *stream)
+{
+	if(n <= 0) return 0;
+	LAUNCH(k_gather_keys<<<blocks_for(n, 128), 128, 0, (cudaStream_t)stream>>>(*s, keys, out, n));
+	return check_launch("k_gather_keys") == cudaSuccess ? 0 : -1;
 }
 
 extern "C" int cpg_launch_gather_arbs(const cpgSet *s, int world, cpgArb *out, int n, void *stream)
