@@ -8,8 +8,9 @@
  * they separate); a sensor that counts what passes through it; wildcard
  * handlers for boxes that change the friction and surface velocity; the
  * default handler summing contact counts and kinetic energy; and a shape
- * removed while it touches (a separation that is a removal).  It prints the
- * counters, the sums and every body's state.  Built like relink_program.c.
+ * removed while it touches (a separation that is a removal), with sleeping
+ * on.  It prints the counters, the sums and every body's state.  Built like
+ * relink_program.c.
  */
 #include <stdio.h>
 #include <stdlib.h>
@@ -180,6 +181,8 @@ int main(void)
 	cpSpace *space = cpSpaceNew();
 	cpSpaceSetIterations(space, 10);
 	cpSpaceSetGravity(space, cpv(0.0, -100.0));
+	/* resting piles fall asleep; the handlers see them wake */
+	cpSpaceSetSleepTimeThreshold(space, 0.5);
 
 	cpBody *sb = cpSpaceGetStaticBody(space);
 	cpShape *ground = cpSpaceAddShape(space, cpSegmentShapeNew(sb, cpv(-300.0, 0.0), cpv(300.0, 0.0), 0.0));
