@@ -837,6 +837,44 @@ def sleep_sample(lib, olib, workload="pyramid", threshold=0.5, n=300):
     return rec
 
 
+def variant_sample(lib, workload="pyramid", n=200, lead=300):
+    """The exact-order step with the host-side parts of the reference on:
+    the spatial hash as the broadphase, collision handlers (the default
+    handler functions, registered for every type pair the workload uses,
+    so their host calls are all the bridge adds), and sleeping; each step
+    wall-timed with a device sync, after `lead` untimed steps."""
+    import ctypes
+    import torch
+    from chipmunk2d_gb300 import Scene
+    cfg, size, dt, desc = WORKLOADS[workload]
+    lib.cpSpaceUseSpatialHash.argtypes = [ctypes.c_void_p, ctypes.c_double, ctypes.c_int]
+    lib.cpSpaceAddCollisionHandler.restype = ctypes.c_void_p
+    lib.cpSpaceAddCollisionHandler.argtypes = [ctypes.c_void_p, ctypes.c_size_t, ctypes.c_size_t]
+    rec = {"workload": workload, "steps": n, "timed_window": [lead, lead + n]}
+    for name in ("plain", "spatial_hash", "handlers", "sleeping"):
+        sc = Scene(lib, cfg, size)
+        if name == "spatial_hash":
+            lib.cpSpaceUseSpatialHash(sc.space, 40.0, 1000)
+        elif name == "handlers":
+            lib.cpSpaceAddCollisionHandler(sc.space, 0, 0)
+        elif name == "sleeping":
+            lib.cpSpaceSetSleepTimeThreshold(sc.space, 1e9)   # the sleeping path, nothing falls asleep
+        for _ in range(lead):
+            lib.cpSpaceStep(sc.space, dt)
+        lib.cpGpuSpaceSync(sc.space)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(n):
+            lib.cpSpaceStep(sc.space, dt)
+            lib.cpGpuSpaceSync(sc.space)
+        torch.cuda.synchronize()
+        rec[name + "_ms_per_step"] = 1000 * (time.perf_counter() - t0) / n
+        if lib.cpGpuGetLastError():
+            rec[name + "_error"] = lib.cpGpuGetLastErrorString().decode()
+        sc.free()
+    return rec
+
+
 def parity_mode_sample(lib, workload, steps, warmup, e2e=False):
     """The exact reference-order mode, for the `ordered_mode` record."""
     rec = mode_sample(lib, workload, steps, warmup, mode=0, phases=True, e2e=e2e)
@@ -1025,6 +1063,7 @@ def run_ours(args):
         extras["ordered_mode"] = [parity_mode_sample(lib, "pyramid", 300, window_start("pyramid", 5, 300)),
                                   parity_mode_sample(lib, "circles", 10, window_start("circles", 5, 10), e2e=True)]
         extras["sleeping"] = sleep_sample(lib, oracle_lib())
+        extras["host_parts"] = variant_sample(lib)
         # mixed shapes and pivot chains at full size (40,000 bodies)
         extras["mixed"] = [mode_sample(lib, "mixed", 150, 150, mode=1, phases=True),
                            mode_sample(lib, "mixed", 3, 2, mode=0)]
