@@ -310,14 +310,72 @@ __global__ void k_tree(cpgSet s, int stagedNodes)
 
 /* cpSpaceHashReindexQuery for a space on the spatial hash: one thread, in
  * the reference's order (the hash's stamps make each pair's test depend
- * on the handles before it). */
-__global__ void k_hash_step(cpgSet s)
+ * on the handles before it).  When the grids and the handles' fields fit,
+ * the block stages them in shared memory first (the walk is a chain of
+ * dependent loads) and writes back what the step changed: the dynamic
+ * grid and the stamps. */
+extern __shared__ int hsmem[];
+
+__global__ void k_hash_step(cpgSet s, int staged)
 {
-	if(blockIdx.x != 0 || threadIdx.x != 0 || !s.params[0].active) return;
-	TreeCtx c = make_tree_ctx(&s, 0);
-	c.collide = 1;
-	if(!c.T->error) hash_reindex_query(c, s);
-	c.T->ncand = c.ncand;
+	if(blockIdx.x != 0 || !s.params[0].active) return;
+	cpgTree *T = &s.tree[0];
+	const cpgWorld &W = s.world[0];
+	int nc = s.numcells, cap = s.gbinCap, nn = T->nodeTop;
+	cpgNode *gnodes = s.nodes + W.nodeOff;
+	int *cells = hsmem, *bh = cells + 2*nc, *bn = bh + 2*cap, *no = bn + 2*cap, *nx = no + nn;
+	unsigned *st = (unsigned *)(nx + nn);
+	int *rg = (int *)(st + nn);
+	if(staged){
+		/* the static grid and every handle (the dynamic grid starts empty) */
+		int stTop = T->gbinTop[1];
+		for(int i = threadIdx.x; i < nc; i += blockDim.x) cells[nc + i] = s.gcells[nc + i];
+		for(int i = threadIdx.x; i < stTop; i += blockDim.x){
+			bh[cap + i] = s.gbinHandle[cap + i];
+			bn[cap + i] = s.gbinNext[cap + i];
+		}
+		for(int i = threadIdx.x; i < nn; i += blockDim.x){
+			int obj = gnodes[i].obj;
+			no[i] = obj; nx[i] = gnodes[i].binNext; st[i] = gnodes[i].stamp;
+			/* each handle's cell range (cpSpaceHash.c:409-415), exact divisions */
+			if(obj >= 0 && obj < W.nshapes){
+				int g = W.shapeOff + obj;
+				double dim = s.celldim;
+				rg[4*i] = floor_int(s.bbl[g]/dim); rg[4*i + 1] = floor_int(s.bbr[g]/dim);
+				rg[4*i + 2] = floor_int(s.bbb[g]/dim); rg[4*i + 3] = floor_int(s.bbt[g]/dim);
+			} else {
+				rg[4*i] = 0; rg[4*i + 1] = -1; rg[4*i + 2] = 0; rg[4*i + 3] = -1;
+			}
+		}
+		__syncthreads();
+	}
+	if(threadIdx.x == 0){
+		TreeCtx c = make_tree_ctx(&s, 0);
+		c.collide = 1;
+		if(!c.T->error){
+			GridCtx g = grid_ctx(s, T, 0), sg = grid_ctx(s, T, 1);
+			if(staged){
+				g.cells = cells; g.bh = bh; g.bn = bn;
+				sg.cells = cells + nc; sg.bh = bh + cap; sg.bn = bn + cap;
+				StagedNodes v; v.o = no; v.nx = nx; v.st = st; v.rg = rg;
+				hash_reindex_query(c, g, sg, v);
+			} else {
+				PoolNodes v; v.n = gnodes;
+				hash_reindex_query(c, g, sg, v);
+			}
+		}
+		c.T->ncand = c.ncand;
+	}
+	if(staged){
+		__syncthreads();
+		int dynTop = T->gbinTop[0];
+		for(int i = threadIdx.x; i < nc; i += blockDim.x) s.gcells[i] = cells[i];
+		for(int i = threadIdx.x; i < dynTop; i += blockDim.x){
+			s.gbinHandle[i] = bh[i];
+			s.gbinNext[i] = bn[i];
+		}
+		for(int i = threadIdx.x; i < nn; i += blockDim.x) gnodes[i].stamp = st[i];
+	}
 }
 
 /* ---- parallel marking of a single world's tree (cpg_mark.cuh) ----
@@ -3332,7 +3390,18 @@ extern "C" int cpg_launch_step_part(const cpgSet *s, const cpgSet *h, int mode, 
 		}
 		/* one warp per world in a batch; a single world's leaf scan takes
 		 * 256 threads (thread 0 alone reinserts and marks) */
-		if(h->useHash) LAUNCH(k_hash_step<<<1, 32, 0, st>>>(*s));
+		if(h->useHash){
+			/* the grids (two cell arrays, two bin pools) and three ints per
+			 * node in shared memory when they fit */
+			size_t hbytes = sizeof(int)*(2*(size_t)h->numcells + 4*(size_t)h->gbinCap + 7*(size_t)h->totalNodes);
+			int hstaged = hbytes <= 200*1024;
+			static size_t hashSmemSet = 0;
+			if(hstaged && hbytes > 48*1024 && hbytes > hashSmemSet){
+				cudaFuncSetAttribute(k_hash_step, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)hbytes);
+				hashSmemSet = hbytes;
+			}
+			LAUNCH(k_hash_step<<<1, 256, hstaged ? hbytes : 0, st>>>(*s, hstaged));
+		}
 		else {
 			LAUNCH(k_tree<<<W, W == 1 ? 256 : 32, smem, st>>>(sv, staged));
 			if(sv.parMark) COOP(k_tree_mark, CPG_MARK_THREADS);

@@ -973,28 +973,58 @@ __device__ void hash_switch(TreeCtx &c, const cpgSet &s)
 }
 
 #ifdef __CUDACC__
+/* The nodes' handle fields as the hash step reads them: in the pool, or
+ * staged in shared memory as three arrays. */
+struct PoolNodes {
+	cpgNode *n;
+	__device__ __forceinline__ int obj(int i) const { return n[i].obj; }
+	__device__ __forceinline__ int next(int i) const { return n[i].binNext; }
+	__device__ __forceinline__ unsigned &stamp(int i) const { return n[i].stamp; }
+	/* the cell range of a handle's box, computed here */
+	__device__ __forceinline__ void range(const TreeCtx &c, int i, double dim, int &l, int &r, int &b, int &t) const
+	{
+		BB bb = shape_bb(c, n[i].obj);
+		l = floor_int(bb.l/dim); r = floor_int(bb.r/dim);
+		b = floor_int(bb.b/dim); t = floor_int(bb.t/dim);
+	}
+};
+/* Staged: the ranges were computed by the whole block beforehand (the
+ * divisions are the serial walk's slowest part on the FP64 pipe). */
+struct StagedNodes {
+	int *o, *nx;
+	unsigned *st;
+	int *rg;                /* 4 per node: l, r, b, t */
+	__device__ __forceinline__ int obj(int i) const { return o[i]; }
+	__device__ __forceinline__ int next(int i) const { return nx[i]; }
+	__device__ __forceinline__ unsigned &stamp(int i) const { return st[i]; }
+	__device__ __forceinline__ void range(const TreeCtx &c, int i, double dim, int &l, int &r, int &b, int &t) const
+	{
+		(void)c; (void)dim;
+		l = rg[4*i]; r = rg[4*i + 1]; b = rg[4*i + 2]; t = rg[4*i + 3];
+	}
+};
+
 /* cpSpaceHashReindexQuery (cpSpaceHash.c:394-441) with cpSpaceCollideShapes
  * as the candidate emitter: each dynamic handle in handle-set order meets
  * the handles already in the cells it covers, then joins them; then each
  * queries the static grid (cpSpatialIndexCollideStatic).  Collision ids
- * start at 0: the hash keeps none. */
-__device__ void hash_reindex_query(TreeCtx &c, const cpgSet &s)
+ * start at 0: the hash keeps none.  g and sg are the two grids, wherever
+ * their cells and bins are held. */
+template <typename Nodes>
+__device__ void hash_reindex_query(TreeCtx &c, GridCtx &g, GridCtx &sg, const Nodes &nodes)
 {
 	cpgTree *T = c.T;
-	GridCtx g = grid_ctx(s, T, 0), sg = grid_ctx(s, T, 1);
 	grid_clear(g);
 	for(int pass = 0; pass < 2; pass++){
 		if(pass == 1 && T->statEntries == 0) break;
+		GridCtx &q = pass == 0 ? g : sg;
 		for(unsigned i = 0; i < T->dynSize && (int)i < c.dbinCap; i++){
 			int guard = 0;
-			for(int hand = c.dbins[i]; hand >= 0; hand = c.nodes[hand].binNext){
+			for(int hand = c.dbins[i]; hand >= 0; hand = nodes.next(hand)){
 				if(++guard > c.nodeCap){ T->error |= CPG_ERR_BINS; return; }
-				int obj = c.nodes[hand].obj;
-				BB bb = shape_bb(c, obj);
-				GridCtx &q = pass == 0 ? g : sg;
-				double dim = q.celldim;
-				int l = floor_int(bb.l/dim), r = floor_int(bb.r/dim);
-				int b = floor_int(bb.b/dim), t = floor_int(bb.t/dim);
+				int obj = nodes.obj(hand);
+				int l, r, b, t;
+				nodes.range(c, hand, q.celldim, l, r, b, t);
 				for(int ci = l; ci <= r; ci++){
 					for(int cj = b; cj <= t; cj++){
 						int cell = hash_cell(ci, cj, q.numcells);
@@ -1003,9 +1033,9 @@ __device__ void hash_reindex_query(TreeCtx &c, const cpgSet &s)
 						for(int bn = q.cells[cell]; bn >= 0; bn = q.bn[bn]){
 							if(++bguard > q.cap){ T->error |= CPG_ERR_HASH; return; }
 							int other = q.bh[bn];
-							if(c.nodes[other].stamp == *q.stamp || c.nodes[other].obj == obj) continue;
-							emit(c, obj, c.nodes[other].obj, -1, 0u);
-							c.nodes[other].stamp = *q.stamp;
+							if(nodes.stamp(other) == *q.stamp || nodes.obj(other) == obj) continue;
+							emit(c, obj, nodes.obj(other), -1, 0u);
+							nodes.stamp(other) = *q.stamp;
 						}
 						if(pass == 0 && !grid_push(q, T, cell, hand)) return;
 					}
