@@ -406,6 +406,8 @@ void cpBodyEachArbiter(cpBody *body, cpBodyArbiterIteratorFunc func, void *data)
  * ---------------------------------------------------------------------- */
 void cpShapeFree(cpShape *shape);                                    /* cpShape.h:80  */
 cpBB cpShapeCacheBB(cpShape *shape);                                 /* cpShape.h:83  */
+cpBB cpShapeUpdate(cpShape *shape, cpTransform transform);           /* cpShape.h:85  */
+void cpShapeSetBody(cpShape *shape, cpBody *body);                   /* cpShape.h:104 */
 cpSpace *cpShapeGetSpace(const cpShape *shape);                      /* cpShape.h:98  */
 cpBody *cpShapeGetBody(const cpShape *shape);                        /* cpShape.h:101 */
 cpFloat cpShapeGetMass(cpShape *shape);                              /* cpShape.h:107 */
@@ -441,6 +443,16 @@ cpVect cpCircleShapeGetOffset(const cpShape *shape);                         /* 
 cpFloat cpCircleShapeGetRadius(const cpShape *shape);                        /* cpShape.h:175 */
 cpShape *cpSegmentShapeNew(cpBody *body, cpVect a, cpVect b, cpFloat radius);/* cpShape.h:185 */
 void cpSegmentShapeSetNeighbors(cpShape *shape, cpVect prev, cpVect next);   /* cpShape.h:188 */
+
+/* chipmunk_unsafe.h:47-63: shapes changed in place (the space's set is
+ * rebuilt with the new geometry before its next step) */
+void cpCircleShapeSetRadius(cpShape *shape, cpFloat radius);         /* chipmunk_unsafe.h:47 */
+void cpCircleShapeSetOffset(cpShape *shape, cpVect offset);          /* chipmunk_unsafe.h:49 */
+void cpSegmentShapeSetEndpoints(cpShape *shape, cpVect a, cpVect b); /* chipmunk_unsafe.h:52 */
+void cpSegmentShapeSetRadius(cpShape *shape, cpFloat radius);        /* chipmunk_unsafe.h:54 */
+void cpPolyShapeSetVerts(cpShape *shape, int count, cpVect *verts, cpTransform transform); /* chipmunk_unsafe.h:57 */
+void cpPolyShapeSetVertsRaw(cpShape *shape, int count, cpVect *verts); /* chipmunk_unsafe.h:58 */
+void cpPolyShapeSetRadius(cpShape *shape, cpFloat radius);           /* chipmunk_unsafe.h:60 */
 cpVect cpSegmentShapeGetA(const cpShape *shape);                             /* cpShape.h:191 */
 cpVect cpSegmentShapeGetB(const cpShape *shape);                             /* cpShape.h:193 */
 cpVect cpSegmentShapeGetNormal(const cpShape *shape);                        /* cpShape.h:195 */
@@ -470,6 +482,8 @@ void cpConstraintSetMaxBias(cpConstraint *constraint, cpFloat maxBias);      /* 
 cpBool cpConstraintGetCollideBodies(const cpConstraint *constraint);         /* cpConstraint.h:62 */
 void cpConstraintSetCollideBodies(cpConstraint *constraint, cpBool collideBodies); /* cpConstraint.h:64 */
 void cpConstraintSetPreSolveFunc(cpConstraint *constraint, cpConstraintPreSolveFunc f);   /* cpConstraint.h:69 */
+cpConstraintPreSolveFunc cpConstraintGetPreSolveFunc(const cpConstraint *constraint);     /* cpConstraint.h:67 */
+cpConstraintPostSolveFunc cpConstraintGetPostSolveFunc(const cpConstraint *constraint);   /* cpConstraint.h:72 */
 void cpConstraintSetPostSolveFunc(cpConstraint *constraint, cpConstraintPostSolveFunc f); /* cpConstraint.h:74 */
 cpDataPointer cpConstraintGetUserData(const cpConstraint *constraint);       /* cpConstraint.h:77 */
 void cpConstraintSetUserData(cpConstraint *constraint, cpDataPointer data);  /* cpConstraint.h:79 */

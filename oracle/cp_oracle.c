@@ -801,6 +801,92 @@ cpShape *cpPolyShapeNewRaw(cpBody *body, int count, const cpVect *verts, cpFloat
 	return s;
 }
 
+/* chipmunk_unsafe.h: shapes changed in place (cpShape.c:553-604,
+ * cpPolyShape.c:287-324).  The caches update at the next cpShapeUpdate. */
+void cpCircleShapeSetRadius(cpShape *s, cpFloat radius)
+{
+	ORC_ASSERT(s->kind == SHAPE_CIRCLE, "Shape is not a circle shape.");
+	s->r = radius;
+	cpFloat mass = s->mass_m;
+	s->mass_i = cpMomentForCircle(1.0, 0.0, s->r, cpvzero); s->mass_cog = s->c; s->mass_area = cpAreaForCircle(0.0, s->r);
+	if(mass > 0.0) body_accumulate_mass(s->body);
+}
+
+void cpCircleShapeSetOffset(cpShape *s, cpVect offset)
+{
+	ORC_ASSERT(s->kind == SHAPE_CIRCLE, "Shape is not a circle shape.");
+	s->c = offset;
+	cpFloat mass = s->mass_m;
+	s->mass_i = cpMomentForCircle(1.0, 0.0, s->r, cpvzero); s->mass_cog = s->c; s->mass_area = cpAreaForCircle(0.0, s->r);
+	if(mass > 0.0) body_accumulate_mass(s->body);
+}
+
+/* the normal is cpvperp here, not the constructor's cpvrperp (cpShape.c:586) */
+void cpSegmentShapeSetEndpoints(cpShape *s, cpVect a, cpVect b)
+{
+	ORC_ASSERT(s->kind == SHAPE_SEGMENT, "Shape is not a segment shape.");
+	s->sa = a; s->sb = b;
+	s->sn = cpvperp(cpvnormalize(cpvsub(b, a)));
+	cpFloat mass = s->mass_m;
+	s->mass_i = cpMomentForBox(1.0, cpvdist(s->sa, s->sb) + 2.0*s->r, 2.0*s->r);
+	s->mass_cog = cpvlerp(s->sa, s->sb, 0.5); s->mass_area = cpAreaForSegment(s->sa, s->sb, s->r);
+	if(mass > 0.0) body_accumulate_mass(s->body);
+}
+
+void cpSegmentShapeSetRadius(cpShape *s, cpFloat radius)
+{
+	ORC_ASSERT(s->kind == SHAPE_SEGMENT, "Shape is not a segment shape.");
+	s->r = radius;
+	cpFloat mass = s->mass_m;
+	s->mass_i = cpMomentForBox(1.0, cpvdist(s->sa, s->sb) + 2.0*s->r, 2.0*s->r);
+	s->mass_cog = cpvlerp(s->sa, s->sb, 0.5); s->mass_area = cpAreaForSegment(s->sa, s->sb, s->r);
+	if(mass > 0.0) body_accumulate_mass(s->body);
+}
+
+void cpPolyShapeSetVertsRaw(cpShape *s, int count, cpVect *verts)
+{
+	ORC_ASSERT(s->kind == SHAPE_POLY, "Shape is not a poly shape.");
+	free(s->pv); free(s->pn);
+	s->count = count;
+	s->pv = (cpVect *)calloc((size_t)(2*count), sizeof(cpVect));
+	s->pn = (cpVect *)calloc((size_t)(2*count), sizeof(cpVect));
+	for(int i = 0; i < count; i++){
+		cpVect a = verts[(i - 1 + count)%count], b = verts[i];
+		s->pv[count + i] = b;
+		s->pn[count + i] = cpvnormalize(cpvrperp(cpvsub(b, a)));
+	}
+	cpFloat mass = s->mass_m;
+	cpVect centroid = cpCentroidForPoly(count, verts);
+	s->mass_i = cpMomentForPoly(1.0, count, verts, cpvneg(centroid), s->r);
+	s->mass_cog = centroid; s->mass_area = cpAreaForPoly(count, verts, s->r);
+	if(mass > 0.0) body_accumulate_mass(s->body);
+}
+
+void cpPolyShapeSetVerts(cpShape *s, int count, cpVect *verts, cpTransform transform)
+{
+	cpVect *hull = (cpVect *)malloc((size_t)(count > 0 ? count : 1)*sizeof(cpVect));
+	for(int i = 0; i < count; i++) hull[i] = cpTransformPoint(transform, verts[i]);
+	int n = cpConvexHull(count, hull, hull, NULL, 0.0);
+	cpPolyShapeSetVertsRaw(s, n, hull);
+	free(hull);
+}
+
+/* the radius alone: the reference leaves the mass properties (cpPolyShape.c:313-324) */
+void cpPolyShapeSetRadius(cpShape *s, cpFloat radius)
+{
+	ORC_ASSERT(s->kind == SHAPE_POLY, "Shape is not a poly shape.");
+	s->r = radius;
+}
+
+/* cpShape.c:87-92, 216-220 */
+void cpShapeSetBody(cpShape *s, cpBody *body)
+{
+	ORC_ASSERT(!(s->prev || (s->body && s->body->shapeList == s)), "You cannot change the body on an active shape. You must remove the shape from the space before changing the body.");
+	s->body = body;
+}
+
+cpBB cpShapeUpdate(cpShape *s, cpTransform transform) { return shape_update(s, transform); }
+
 cpShape *cpPolyShapeNew(cpBody *body, int count, const cpVect *verts, cpTransform transform, cpFloat radius)
 {
 	cpVect *hull = (cpVect *)malloc((size_t)count*sizeof(cpVect));
@@ -1052,6 +1138,8 @@ void cpConstraintSetMaxBias(cpConstraint *c, cpFloat v) { activate_bodies_(c); c
 cpBool cpConstraintGetCollideBodies(const cpConstraint *c) { return c->collideBodies; }
 void cpConstraintSetCollideBodies(cpConstraint *c, cpBool v) { activate_bodies_(c); c->collideBodies = v; }
 void cpConstraintSetPreSolveFunc(cpConstraint *c, cpConstraintPreSolveFunc f) { c->preSolve = f; }
+cpConstraintPreSolveFunc cpConstraintGetPreSolveFunc(const cpConstraint *c) { return c->preSolve; }
+cpConstraintPostSolveFunc cpConstraintGetPostSolveFunc(const cpConstraint *c) { return c->postSolve; }
 void cpConstraintSetPostSolveFunc(cpConstraint *c, cpConstraintPostSolveFunc f) { c->postSolve = f; }
 cpDataPointer cpConstraintGetUserData(const cpConstraint *c) { return c->userData; }
 void cpConstraintSetUserData(cpConstraint *c, cpDataPointer d) { c->userData = d; }

@@ -4,16 +4,18 @@
  * static platform body moved and turned (cpSpaceReindexStatic), a single
  * static shape's body moved (cpSpaceReindexShape), dynamic bodies
  * teleported (cpSpaceReindexShapesForBody, one of them with two shapes),
- * a shape given a large velocity before its re-index, and a re-index of a
- * shape the space no longer holds.  Queries run right after the re-indexes,
- * before the next step, so they see the trees as re-indexed.  It prints
- * every body's state, the queries' results and visit orders, and some
- * shapes' boxes.  Built like relink_program.c.
+ * a shape given a large velocity before its re-index, a re-index of a
+ * shape the space no longer holds, and shapes changed in place
+ * (chipmunk_unsafe.h: radius, offset, endpoints, vertices).  Queries run
+ * right after the re-indexes, before the next step, so they see the trees
+ * as re-indexed.  It prints every body's state, the queries' results and
+ * visit orders, and some shapes' boxes.  Built like relink_program.c.
  */
 #include <stdio.h>
 #include <stdlib.h>
 #ifdef RELINK_REFERENCE_HEADERS
 #include "chipmunk/chipmunk.h"
+#include "chipmunk/chipmunk_unsafe.h"
 #else
 #include "chipmunk_gb300.h"
 #endif
@@ -155,6 +157,19 @@ int main(void)
 			cpSpaceReindexShape(space, gone);
 			print_bb("bbgone", gone);
 			cpSpaceReindexShapesForBody(space, bodies[6]);
+		}
+		if(step == 145){
+			/* shapes changed in place, a static one re-indexed after */
+			cpCircleShapeSetRadius(shapes[0], 6.0);
+			cpCircleShapeSetOffset(shapes[2], cpv(1.0, 0.5));
+			cpVect tri[4] = { cpv(-5.0, -4.0), cpv(6.0, -3.0), cpv(0.0, 5.0), cpv(-1.0, 0.0) };
+			cpPolyShapeSetVerts(shapes[1], 4, tri, cpTransformIdentity);
+			cpPolyShapeSetRadius(shapes[3], 0.5);
+			cpSegmentShapeSetEndpoints(deck, cpv(-45.0, -1.0), cpv(48.0, 2.0));
+			cpSegmentShapeSetRadius(deck, 2.5);
+			cpSpaceReindexStatic(space);
+			print_bb("bbdeck2", deck);
+			print_box(space, cpBBNew(-60.0, 0.0, 60.0, 60.0));
 		}
 		if(step == 159){
 			/* the platform back down, turned the other way */
