@@ -840,9 +840,10 @@ def sleep_sample(lib, olib, workload="pyramid", threshold=0.5, n=300):
 def variant_sample(lib, workload="pyramid", n=200, lead=300):
     """The exact-order step with the host-side parts of the reference on:
     the spatial hash as the broadphase, collision handlers (the default
-    handler functions, registered for every type pair the workload uses,
-    so their host calls are all the bridge adds), and sleeping; each step
-    wall-timed with a device sync, after `lead` untimed steps."""
+    handler functions, registered for the type every shape has, so their
+    host calls are all the bridge adds; then for types no shape has, so
+    the arbiters stay on the device), and sleeping; each step wall-timed
+    with a device sync, after `lead` untimed steps."""
     import ctypes
     import torch
     from chipmunk2d_gb300 import Scene
@@ -851,12 +852,15 @@ def variant_sample(lib, workload="pyramid", n=200, lead=300):
     lib.cpSpaceAddCollisionHandler.restype = ctypes.c_void_p
     lib.cpSpaceAddCollisionHandler.argtypes = [ctypes.c_void_p, ctypes.c_size_t, ctypes.c_size_t]
     rec = {"workload": workload, "steps": n, "timed_window": [lead, lead + n]}
-    for name in ("plain", "spatial_hash", "handlers", "sleeping"):
+    for name in ("plain", "spatial_hash", "handlers", "handlers_other_types", "sleeping"):
         sc = Scene(lib, cfg, size)
         if name == "spatial_hash":
             lib.cpSpaceUseSpatialHash(sc.space, 40.0, 1000)
         elif name == "handlers":
             lib.cpSpaceAddCollisionHandler(sc.space, 0, 0)
+        elif name == "handlers_other_types":
+            # a handler for types no shape has: every arbiter stays on the device
+            lib.cpSpaceAddCollisionHandler(sc.space, 1, 2)
         elif name == "sleeping":
             lib.cpSpaceSetSleepTimeThreshold(sc.space, 1e9)   # the sleeping path, nothing falls asleep
         for _ in range(lead):

@@ -245,7 +245,7 @@ struct cpSpace {
 	/* collision handlers (cpSpace.c:62-103, 378-413): once any is added,
 	 * the step runs the callbacks on the host between its device halves */
 	cpCollisionHandler defaultHandler;
-	int usesWildcards, handlersOn;
+	int usesWildcards, handlersOn, defaultTouched;
 	cpCollisionHandler **handlers; int nhandlers, caphandlers;
 	cpArbiter *harb; int capharb;            /* the arbiters of one round of callbacks */
 	/* cpSpaceUseSpatialHash: both indices are spatial hashes */
@@ -447,7 +447,7 @@ static size_t carve_set(cpgSet *d, char *base, int pass)
 	CARVE(bbl, double, NS); CARVE(bbb, double, NS); CARVE(bbr, double, NS); CARVE(bbt, double, NS);
 	CARVE(se, double, NS); CARVE(su, double, NS); CARVE(svx, double, NS); CARVE(svy, double, NS);
 	CARVE(sgroup, unsigned long long, NS); CARVE(scat, unsigned, NS); CARVE(smask, unsigned, NS);
-	CARVE(ssensor, unsigned char, NS); CARVE(shash, unsigned long long, NS);
+	CARVE(ssensor, unsigned char, NS); CARVE(shost, unsigned char, NS); CARVE(shash, unsigned long long, NS);
 	CARVE(lvx, double, NV); CARVE(lvy, double, NV); CARVE(lnx, double, NV); CARVE(lny, double, NV);
 	CARVE(gvx, double, NV); CARVE(gvy, double, NV); CARVE(gnx, double, NV); CARVE(gny, double, NV);
 	CARVE(nodes, cpgNode, d->totalNodes); CARVE(pairs, cpgPair, d->totalPairs);
@@ -625,6 +625,21 @@ static int unpack_one(DevSet *ds, cpSpace *sp, cpBody *b)
 	return 1;
 }
 
+/* Whether a shape's arbiters need the host's callbacks: the default
+ * handler was asked for, or its collision type has a handler of its own
+ * (typed or wildcard).  Others meet only do-nothing handlers, whose rule
+ * the device applies itself. */
+static int shape_needs_host_(const cpSpace *sp, const cpShape *s)
+{
+	if(!sp->handlersOn) return 0;
+	if(sp->defaultTouched) return 1;
+	for(int i = 0; i < sp->nhandlers; i++){
+		const cpCollisionHandler *h = sp->handlers[i];
+		if(h->typeA == s->ctype || h->typeB == s->ctype) return 1;
+	}
+	return 0;
+}
+
 static int upload_shapes(DevSet *ds, int w)
 {
 	cpSpace *sp = ds->spaces[w];
@@ -638,6 +653,7 @@ static int upload_shapes(DevSet *ds, int w)
 	unsigned long long *grp = HALLOC(unsigned long long, 2*n), *hsh = grp + n;
 	unsigned *cm = HALLOC(unsigned, 2*n), *cat = cm, *msk = cm + n;
 	unsigned char *sens = HALLOC(unsigned char, n);
+	unsigned char *hflag = HALLOC(unsigned char, n);
 	int nv = 0;
 	int staticIndex = world_body_count(sp) - 1;
 	for(int i = 0; i < n; i++){
@@ -660,6 +676,7 @@ static int upload_shapes(DevSet *ds, int w)
 		f[21][i] = s->e; f[22][i] = s->u; f[23][i] = s->surfaceV.x; f[24][i] = s->surfaceV.y;
 		grp[i] = (unsigned long long)s->filter.group; cat[i] = s->filter.categories; msk[i] = s->filter.mask;
 		sens[i] = s->sensor; hsh[i] = (unsigned long long)s->hashid;
+		hflag[i] = (unsigned char)shape_needs_host_(sp, s);
 		voff[i] = nv; vcount[i] = s->count;
 		nv += s->count;
 	}
@@ -684,11 +701,12 @@ static int upload_shapes(DevSet *ds, int w)
 	ok &= h2d(d->scat + off, cat, sizeof(unsigned)*(size_t)n);
 	ok &= h2d(d->smask + off, msk, sizeof(unsigned)*(size_t)n);
 	ok &= h2d(d->ssensor + off, sens, (size_t)n);
+	ok &= h2d(d->shost + off, hflag, (size_t)n);
 	int voffw = ds->hworld[w].vertOff;
 	double *vdst[8] = { d->lvx, d->lvy, d->lnx, d->lny, d->gvx, d->gvy, d->gnx, d->gny };
 	for(int k = 0; k < 8; k++) ok &= h2d(vdst[k] + voffw, vb + (size_t)k*nv, sizeof(double)*(size_t)nv);
 	cudaStreamSynchronize(lib_stream());
-	free(buf); free(ib); free(grp); free(cm); free(sens); free(vb);
+	free(buf); free(ib); free(grp); free(cm); free(sens); free(hflag); free(vb);
 	return ok;
 }
 
@@ -3178,7 +3196,7 @@ void cpShapeSetSurfaceVelocity(cpShape *s, cpVect v) { swr(s)->surfaceV = v; }
 cpDataPointer cpShapeGetUserData(const cpShape *s) { return s->userData; }
 void cpShapeSetUserData(cpShape *s, cpDataPointer d) { s->userData = d; }
 cpCollisionType cpShapeGetCollisionType(const cpShape *s) { return s->ctype; }
-void cpShapeSetCollisionType(cpShape *s, cpCollisionType t) { cpBodyActivate(s->body); s->ctype = t; }
+void cpShapeSetCollisionType(cpShape *s, cpCollisionType t) { cpBodyActivate(s->body); s->ctype = t; if(s->space) s->space->shapeDirty = 1; }
 cpShapeFilter cpShapeGetFilter(const cpShape *s) { return s->filter; }
 void cpShapeSetFilter(cpShape *s, cpShapeFilter f) { swr(s)->filter = f; }
 cpVect cpCircleShapeGetOffset(const cpShape *s) { return s->c; }
@@ -4373,6 +4391,7 @@ static cpCollisionHandler *lookup_handler_(cpSpace *sp, cpCollisionType a, cpCol
 static cpCollisionHandler *add_handler_(cpSpace *sp, const cpCollisionHandler *proto)
 {
 	sp->handlersOn = 1;
+	sp->shapeDirty = 1;
 	cpCollisionHandler *h = lookup_handler_(sp, proto->typeA, proto->typeB, NULL);
 	if(h) return h;
 	h = (cpCollisionHandler *)malloc(sizeof(cpCollisionHandler));
@@ -4393,6 +4412,8 @@ cpCollisionHandler *cpSpaceAddDefaultCollisionHandler(cpSpace *sp)
 {
 	use_wildcard_default_(sp);
 	sp->handlersOn = 1;
+	sp->defaultTouched = 1;
+	sp->shapeDirty = 1;
 	return &sp->defaultHandler;
 }
 
@@ -4547,48 +4568,60 @@ static void cpgarb_from_(cpgArb *g, const cpArbiter *arb)
 	g->c[0] = arb->c[0]; g->c[1] = arb->c[1];
 }
 
-/* begin and pre-solve on the step's colliding arbiters, in order
- * (cpSpaceStep.c:259-286); the rule; the records and the list back. */
+/* begin and pre-solve on the step's colliding arbiters of handled types,
+ * in order (cpSpaceStep.c:259-286); the rule; the records and the list
+ * back.  The list holds them among the arbiters the device kept by the
+ * rule alone (their handlers do nothing). */
 static int handlers_collide_(cpSpace *sp)
 {
 	DevSet *ds = sp->dev;
 	const cpgWorld *W = &ds->hworld[sp->world];
 	int n = 0;
-	cpgArb *recs = gather_list_(sp, &n);
-	if(!recs) return 0;
+	int *pairs = gather_pairs_(sp, &n);
+	if(!pairs) return 0;
 	int *slots = HALLOC(int, n);
 	if(n > 0 && (!d2h(slots, ds->d.arbList + W->candOff, sizeof(int)*(size_t)n) ||
-	             !cuda_ok(cudaStreamSynchronize(lib_stream()), "list slots"))){ free(recs); free(slots); return 0; }
-	space_pull(sp);
-	harb_reserve_(sp, n);
-	unsigned long long *keep = HALLOC(unsigned long long, n);
-	int nkeep = 0;
-	sp->locked++;
+	             !cuda_ok(cudaStreamSynchronize(lib_stream()), "list slots"))){ free(pairs); free(slots); return 0; }
+	/* the entries whose types have handlers */
+	int *hidx = HALLOC(int, n), *hslots = HALLOC(int, n);
+	int nh = 0;
 	for(int i = 0; i < n; i++){
-		cpArbiter *arb = &sp->harb[i];
-		harb_fill_(sp, arb, &recs[i], slots[i], 1);
+		cpShape *a = sp->shapes[pairs[2*i]], *b = sp->shapes[pairs[2*i + 1]];
+		if(shape_needs_host_(sp, a) || shape_needs_host_(sp, b)){ hidx[nh] = i; hslots[nh] = slots[i]; nh++; }
+	}
+	cpgArb *recs = gather_slots_(ds, hslots, nh);
+	if(!recs){ free(pairs); free(slots); free(hidx); free(hslots); return 0; }
+	space_pull(sp);
+	harb_reserve_(sp, nh);
+	unsigned char *drop = HALLOC(unsigned char, n);
+	sp->locked++;
+	for(int k = 0; k < nh; k++){
+		cpArbiter *arb = &sp->harb[k];
+		harb_fill_(sp, arb, &recs[k], hslots[k], 1);
 		cpCollisionHandler *handler = arb->handler;
 		if(arb->state == CPG_ARB_FIRST && !handler->beginFunc(arb, sp, handler->userData)) cpArbiterIgnore(arb);
 		cpShape *a = arb->a, *b = arb->b;
-		if(arb->state != CPG_ARB_IGNORE && handler->preSolveFunc(arb, sp, handler->userData) && arb->state != CPG_ARB_IGNORE &&
-		   !(a->sensor || b->sensor) && !(a->body->m == INF_ && b->body->m == INF_)){
-			keep[nkeep++] = arb->key;
-		} else {
+		if(!(arb->state != CPG_ARB_IGNORE && handler->preSolveFunc(arb, sp, handler->userData) && arb->state != CPG_ARB_IGNORE &&
+		     !(a->sensor || b->sensor) && !(a->body->m == INF_ && b->body->m == INF_))){
 			arb->count = 0;
 			if(arb->state != CPG_ARB_IGNORE) arb->state = CPG_ARB_NORMAL;
+			drop[hidx[k]] = 1;
 		}
 		harb_keep_data_(sp, arb);
-		cpgarb_from_(&recs[i], arb);
+		cpgarb_from_(&recs[k], arb);
 	}
 	/* the records back, then the list */
+	unsigned long long *keep = HALLOC(unsigned long long, n);
+	int nkeep = 0;
+	for(int i = 0; i < n; i++) if(!drop[i]) keep[nkeep++] = garb_key_(pairs[2*i], pairs[2*i + 1]);
 	int ok = 1;
-	if(n > 0){
-		if(!bridge_buf_(ds, ds->d.arbCap + n + 1)) ok = 0;
+	if(nh > 0){
+		if(!bridge_buf_(ds, ds->d.arbCap + nh + 1)) ok = 0;
 		else {
 			int *dslots = ds->bridgeBuf + ds->d.arbCap + 1;
-			ok &= h2d(dslots, slots, sizeof(int)*(size_t)n);
-			ok &= h2d(ds->gather, recs, sizeof(cpgArb)*(size_t)n);
-			ok &= cpg_launch_put_arbs(&ds->d, dslots, ds->gather, n, lib_stream()) == 0;
+			ok &= h2d(dslots, hslots, sizeof(int)*(size_t)nh);
+			ok &= h2d(ds->gather, recs, sizeof(cpgArb)*(size_t)nh);
+			ok &= cpg_launch_put_arbs(&ds->d, dslots, ds->gather, nh, lib_stream()) == 0;
 		}
 	}
 	if(ok){
@@ -4605,7 +4638,7 @@ static int handlers_collide_(cpSpace *sp)
 			ok &= cuda_ok(cudaStreamSynchronize(lib_stream()), "handler list");
 		}
 	}
-	free(recs); free(slots); free(keep);
+	free(recs); free(pairs); free(slots); free(hidx); free(hslots); free(keep); free(drop);
 	/* cpSpaceStep.c:373 */
 	space_unlock_(sp);
 	return ok;
@@ -4632,6 +4665,7 @@ static int handlers_separate_(cpSpace *sp)
 	sp->locked++;
 	for(int i = 0; i < n; i++){
 		if(recs[i].a < 0 || recs[i].a >= sp->nshapes || recs[i].b < 0 || recs[i].b >= sp->nshapes || !sp->shapes[recs[i].a] || !sp->shapes[recs[i].b]) continue;
+		if(!shape_needs_host_(sp, sp->shapes[recs[i].a]) && !shape_needs_host_(sp, sp->shapes[recs[i].b])) continue;
 		cpArbiter *arb = &sp->harb[i];
 		harb_fill_(sp, arb, &recs[i], slots[i], 0);
 		arb->handler->separateFunc(arb, sp, arb->handler->userData);
@@ -4645,20 +4679,33 @@ static int handlers_separate_(cpSpace *sp)
 /* post-solve on the list with the solved impulses (cpSpaceStep.c:439-444) */
 static int handlers_post_solve_(cpSpace *sp)
 {
+	DevSet *ds = sp->dev;
+	const cpgWorld *W = &ds->hworld[sp->world];
 	int n = 0;
-	cpgArb *recs = gather_list_(sp, &n);
-	if(!recs) return 0;
-	space_pull(sp);
-	harb_reserve_(sp, n);
-	sp->locked++;
+	int *pairs = gather_pairs_(sp, &n);
+	if(!pairs) return 0;
+	int *slots = HALLOC(int, n);
+	if(n > 0 && (!d2h(slots, ds->d.arbList + W->candOff, sizeof(int)*(size_t)n) ||
+	             !cuda_ok(cudaStreamSynchronize(lib_stream()), "list slots"))){ free(pairs); free(slots); return 0; }
+	int nh = 0;
 	for(int i = 0; i < n; i++){
+		cpShape *a = sp->shapes[pairs[2*i]], *b = sp->shapes[pairs[2*i + 1]];
+		if(shape_needs_host_(sp, a) || shape_needs_host_(sp, b)) slots[nh++] = slots[i];
+	}
+	free(pairs);
+	cpgArb *recs = gather_slots_(ds, slots, nh);
+	if(!recs){ free(slots); return 0; }
+	space_pull(sp);
+	harb_reserve_(sp, nh);
+	sp->locked++;
+	for(int i = 0; i < nh; i++){
 		cpArbiter *arb = &sp->harb[i];
 		harb_fill_(sp, arb, &recs[i], -1, 0);
 		arb->handler->postSolveFunc(arb, sp, arb->handler->userData);
 		harb_keep_data_(sp, arb);
 	}
 	space_unlock_(sp);
-	free(recs);
+	free(recs); free(slots);
 	return 1;
 }
 

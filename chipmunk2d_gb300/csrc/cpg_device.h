@@ -324,6 +324,7 @@ typedef struct cpgSet {
 	unsigned long long *sgroup;
 	unsigned *scat, *smask;
 	unsigned char *ssensor;
+	unsigned char *shost;         /* 1: the shape's collision type has a handler (its arbiters go to the host) */
 	unsigned long long *shash;    /* cpShape.hashid */
 
 	/* polygon planes [totalVerts]: local and world */

@@ -831,9 +831,12 @@ __global__ void k_arb_update(cpgSet s)
 		bool sensor = s.ssensor[ga] || s.ssensor[gb];
 		bool infinite = (s.m[gBodyA] == CUDART_INF && s.m[gBodyB] == CUDART_INF);
 		if(s.bridge){
-			/* the host runs begin and pre-solve on every colliding
-			 * arbiter, then applies the rule below (cpSpaceStep.c:259-283) */
+			/* the record is new this step, or kept (user data) */
 			arb.pad = fresh ? (arb.pad | CPG_ARB_FRESH) : (arb.pad & ~CPG_ARB_FRESH);
+		}
+		if(s.bridge && (s.shost[ga] || s.shost[gb])){
+			/* a handler's type: the host runs begin and pre-solve, then
+			 * applies the rule below (cpSpaceStep.c:259-283) */
 			s.candArb[W.candOff + i] = slot;
 		} else if(arb.state != CPG_ARB_IGNORE && !sensor && !infinite){
 			s.candArb[W.candOff + i] = slot;
