@@ -203,6 +203,7 @@ _GPU_API = {
     "cpGpuDebugSetCapacities": (None, [I, I, I, I]),
     "cpGpuDebugSetWarmStartGather": (None, [I]),
     "cpGpuDebugSetParallelMarking": (None, [I]),
+    "cpGpuDebugSetCoopBlocks": (None, [I]),
     "cpGpuGetPhaseTimes": (I, [P, P, I]),
     "cpGpuSolverQuality": (I, [P, I, D, I, P]),
     "cpGpuSpaceGetBodyStates": (I, [P, P, I]),

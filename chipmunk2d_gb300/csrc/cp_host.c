@@ -370,6 +370,10 @@ void cpGpuDebugSetWarmStartGather(int on) { g_warm_gather = on ? 1 : 0; }
 static int g_par_mark = -1;
 #define CPG_PAR_MARK_MIN 1024
 void cpGpuDebugSetParallelMarking(int on) { g_par_mark = on < 0 ? -1 : (on ? 1 : 0); }
+static int g_coop_blocks = 0;
+/* At most n blocks in the cooperative kernels (0: one per SM): a launch
+ * shape for measurements; every shape gives the same results. */
+void cpGpuDebugSetCoopBlocks(int n) { g_coop_blocks = n > 0 ? n : 0; }
 void cpGpuDebugSetTreeStaging(int maxNodes) { g_tree_stage = maxNodes < 0 ? -1 : maxNodes; }
 static int g_whole_grid = 0;     /* 1: single-world sets always use the whole-grid solve */
 
@@ -1205,6 +1209,7 @@ static int devset_step_part(DevSet *ds, const double *dts, cpSpace **only, int p
 	d->flowSpin = g_flow_spin;
 	d->flowWithhold = g_flow_withhold;
 	d->warmGather = g_warm_gather;
+	d->hostCoopBlocks = g_coop_blocks;
 	d->parMark = g_par_mark >= 0 ? g_par_mark : (d->hostNdyn >= CPG_PAR_MARK_MIN);
 	/* collision handlers: the separations of the filter go to the host */
 	d->bridge = (ds->nspaces == 1 && ds->spaces[0]->handlersOn && part != 0);

@@ -387,6 +387,7 @@ typedef struct cpgSet {
 	int flowWithhold;             /* test of the wait limit: completions are not published (host value) */
 	int warmGather;               /* 1: coloured mode applies the cached impulses per body in k_integrate_vel (host value) */
 	int parMark;                  /* 1: a single world's tree is marked by k_tree_mark's parallel phases (host value) */
+	int hostCoopBlocks;           /* > 0: at most this many blocks in the cooperative kernels (host value) */
 	int bridge;                   /* 1: collision handlers run on the host (a single world): k_arb_update lists every
 	                                 colliding arbiter and leaves the sensor/ignore rule to the host (host value) */
 	int *sepSlots, *sepCount;     /* bridge: slots of the arbiters the cache filter separates this step */

@@ -3242,7 +3242,9 @@ static cudaError_t launch_coop(const void *kernel, int threads, cpgSet *s, int w
 	}
 	void *args[] = { (void *)s, (void *)&w };
 	g_launches++;
-	return cudaLaunchCooperativeKernel(kernel, dim3(*cache), dim3(threads), args, 0, st);
+	int nb = *cache;
+	if(s->hostCoopBlocks > 0 && s->hostCoopBlocks < nb) nb = s->hostCoopBlocks;
+	return cudaLaunchCooperativeKernel(kernel, dim3(nb), dim3(threads), args, 0, st);
 }
 
 /* Single-world sets with at least this many solver units use the

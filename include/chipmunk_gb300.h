@@ -890,6 +890,7 @@ void cpGpuDebugSetCapacities(int pairsPerShape, int pairsExtra, int arbiterSlots
  * parallel from 1024 dynamic shapes up).  All give the same candidates,
  * pair lists and results. */
 void cpGpuDebugSetParallelMarking(int on);
+void cpGpuDebugSetCoopBlocks(int n);
 /* Bookkeeping of the last step (after it completes): [0] error flags,
  * [1] pair-pool use and [2] node-pool use (per mille of capacity, largest
  * world), [3] live cached arbiters, [4] candidate pairs, [5] solved
