@@ -91,3 +91,38 @@ def test_custom_spring_force_is_refused(lib):
     err, unmoved = refused(lib, sp, b)
     assert err == CP_GPU_ERR_UNSUPPORTED and unmoved
     lib.cpSpaceFree(sp); lib.cpConstraintFree(c); lib.cpBodyFree(b)
+
+
+def test_handlers_and_the_hash_in_the_coloured_mode_are_refused(lib):
+    """Collision handlers and the spatial hash follow the exact order's
+    arbiter list and pair order; the coloured mode refuses both."""
+    lib.cpSpaceAddCollisionHandler.restype = P
+    lib.cpSpaceAddCollisionHandler.argtypes = [P, ctypes.c_size_t, ctypes.c_size_t]
+    lib.cpSpaceUseSpatialHash.argtypes = [P, D, ctypes.c_int]
+    for setup in (lambda sp: lib.cpSpaceAddCollisionHandler(sp, 1, 2), lambda sp: lib.cpSpaceUseSpatialHash(sp, 10.0, 100)):
+        sp, b = one_body_space(lib)
+        lib.cpGpuSetSolverMode(sp, 1)
+        setup(sp)
+        err, unmoved = refused(lib, sp, b)
+        assert err == CP_GPU_ERR_UNSUPPORTED and unmoved
+        lib.cpSpaceFree(sp); lib.cpBodyFree(b)
+
+
+def test_sleeping_and_handlers_in_a_batch_are_refused(lib):
+    """A batch steps its spaces without the host's parts of the step."""
+    lib.cpGpuBatchNew.restype = P
+    lib.cpGpuBatchAddSpace.argtypes = [P, P]
+    lib.cpGpuBatchStep.argtypes = [P, D, ctypes.c_int, ctypes.c_int]
+    lib.cpGpuBatchFree.argtypes = [P]
+    lib.cpSpaceAddCollisionHandler.restype = P
+    lib.cpSpaceAddCollisionHandler.argtypes = [P, ctypes.c_size_t, ctypes.c_size_t]
+    for setup in (lambda sp: lib.cpSpaceSetSleepTimeThreshold(sp, 0.5), lambda sp: lib.cpSpaceAddCollisionHandler(sp, 1, 2)):
+        sp, b = one_body_space(lib)
+        setup(sp)
+        batch = lib.cpGpuBatchNew()
+        lib.cpGpuBatchAddSpace(batch, sp)
+        lib.cpGpuGetLastError()
+        assert lib.cpGpuBatchStep(batch, 1 / 60, 1, 0) == -1
+        assert lib.cpGpuGetLastError() == CP_GPU_ERR_UNSUPPORTED
+        lib.cpGpuBatchFree(batch)
+        lib.cpSpaceFree(sp); lib.cpBodyFree(b)
