@@ -255,6 +255,7 @@ struct cpSpace {
 };
 
 static void run_post_step_(cpSpace *sp);
+static void space_unlock_(cpSpace *sp);
 static cpShape *slot_shape_(cpSpace *sp, int slot);
 
 static void push_(void ***arr, int *n, int *cap, void *p)
@@ -1580,11 +1581,14 @@ void cpSpacePointQuery(cpSpace *sp, cpVect point, cpFloat maxDistance, cpShapeFi
 	cpgQuery q = query_new_(CPG_Q_POINT, point.x, point.y, 0.0, 0.0, maxDistance, filter);
 	cpgHit *h; int *c, cap;
 	if(!run_queries_(sp, &q, 1, &h, &c, &cap)) return;
+	sp->locked++;
 	for(int k = 0; k < c[0] && k < cap; k++){
 		cpShape *shape = slot_shape_(sp, h[k].shape);
 		if(shape && func) func(shape, cpv(h[k].px, h[k].py), h[k].d, cpv(h[k].gx, h[k].gy), data);
 	}
-	free(h); free(c);	run_post_step_(sp);
+	free(h); free(c);
+	space_unlock_(sp);
+	run_post_step_(sp);
 }
 
 cpShape *cpSpacePointQueryNearest(cpSpace *sp, cpVect point, cpFloat maxDistance, cpShapeFilter filter, cpPointQueryInfo *out)
@@ -1609,11 +1613,14 @@ void cpSpaceSegmentQuery(cpSpace *sp, cpVect start, cpVect end, cpFloat radius, 
 	cpgQuery q = query_new_(CPG_Q_SEGMENT, start.x, start.y, end.x, end.y, radius, filter);
 	cpgHit *h; int *c, cap;
 	if(!run_queries_(sp, &q, 1, &h, &c, &cap)) return;
+	sp->locked++;
 	for(int k = 0; k < c[0] && k < cap; k++){
 		cpShape *shape = slot_shape_(sp, h[k].shape);
 		if(shape && func) func(shape, cpv(h[k].px, h[k].py), cpv(h[k].gx, h[k].gy), h[k].d, data);
 	}
-	free(h); free(c);	run_post_step_(sp);
+	free(h); free(c);
+	space_unlock_(sp);
+	run_post_step_(sp);
 }
 
 cpShape *cpSpaceSegmentQueryFirst(cpSpace *sp, cpVect start, cpVect end, cpFloat radius, cpShapeFilter filter, cpSegmentQueryInfo *out)
@@ -1638,11 +1645,14 @@ void cpSpaceBBQuery(cpSpace *sp, cpBB bb, cpShapeFilter filter, cpSpaceBBQueryFu
 	cpgQuery q = query_new_(CPG_Q_BB, bb.l, bb.b, bb.r, bb.t, 0.0, filter);
 	cpgHit *h; int *c, cap;
 	if(!run_queries_(sp, &q, 1, &h, &c, &cap)) return;
+	sp->locked++;
 	for(int k = 0; k < c[0] && k < cap; k++){
 		cpShape *shape = slot_shape_(sp, h[k].shape);
 		if(shape && func) func(shape, data);
 	}
-	free(h); free(c);	run_post_step_(sp);
+	free(h); free(c);
+	space_unlock_(sp);
+	run_post_step_(sp);
 }
 
 /* The slot of a shape in its space, or -1 (error set) when it is in none. */
@@ -1799,12 +1809,14 @@ cpBool cpSpaceShapeQuery(cpSpace *sp, cpShape *shape, cpSpaceShapeQueryFunc func
 	free(hplanes);
 	if(!hits) return cpFalse;
 	int n = counts[0] < cap ? counts[0] : cap;
+	sp->locked++;
 	for(int k = 0; k < n; k++){
 		cpShape *other = slot_shape_(sp, hits[k].shape);
 		if(!other) continue;
 		cpContactPointSet set = point_set_(&hits[k]);
 		if(func) func(other, &set, data);
 	}
+	space_unlock_(sp);
 	any = counts[1] ? cpTrue : cpFalse;
 	free(hits);
 	run_post_step_(sp);
@@ -2707,6 +2719,7 @@ void cpBodySetType(cpBody *b, cpBodyType type)
 	int oldType = body_type_(b);
 	if(oldType == (int)type) return;
 	cpSpace *sp = b->space;
+	if(sp) ASSERT_HARD(!sp->locked, "This operation cannot be done safely during a call to cpSpaceStep() or during a query. Put these calls into a post-step callback.");
 	if(sp && !space_edit_ok(sp)) return;
 	if(sp) sp->bodyDirty = 1;
 	b->idleTime = (type == CP_BODY_TYPE_STATIC ? INF_ : 0.0);
@@ -3648,7 +3661,8 @@ cpDataPointer cpSpaceGetUserData(const cpSpace *sp) { return sp->userData; }
 void cpSpaceSetUserData(cpSpace *sp, cpDataPointer d) { sp->userData = d; }
 cpBody *cpSpaceGetStaticBody(const cpSpace *sp) { return (cpBody *)&sp->staticBody; }
 cpFloat cpSpaceGetCurrentTimeStep(const cpSpace *sp) { return sp->curr_dt; }
-cpBool cpSpaceIsLocked(cpSpace *sp) { (void)sp; return cpFalse; }
+/* locked while queries, iterations and the step's callbacks run */
+cpBool cpSpaceIsLocked(cpSpace *sp) { return sp->locked > 0; }
 cpBool cpSpaceContainsShape(cpSpace *sp, cpShape *s) { return s->space == sp; }
 cpBool cpSpaceContainsBody(cpSpace *sp, cpBody *b) { return b->space == sp; }
 cpBool cpSpaceContainsConstraint(cpSpace *sp, cpConstraint *c) { return c->space == sp; }
@@ -4817,6 +4831,7 @@ void cpSpaceUseSpatialHash(cpSpace *sp, cpFloat dim, int count)
 cpBody *cpSpaceAddBody(cpSpace *sp, cpBody *b)
 {
 	/* cpSpace.c:440-451 */
+	ASSERT_HARD(!sp->locked, "This operation cannot be done safely during a call to cpSpaceStep() or during a query. Put these calls into a post-step callback.");
 	ASSERT_HARD(b->space != sp, "You have already added this body to this space. You must not add it a second time.");
 	ASSERT_HARD(!b->space, "You have already added this body to another space. You cannot add it to a second.");
 	if(!space_edit_ok(sp)) return b;
@@ -4829,6 +4844,7 @@ cpBody *cpSpaceAddBody(cpSpace *sp, cpBody *b)
 cpShape *cpSpaceAddShape(cpSpace *sp, cpShape *s)
 {
 	/* cpSpace.c:417-438 */
+	ASSERT_HARD(!sp->locked, "This operation cannot be done safely during a call to cpSpaceStep() or during a query. Put these calls into a post-step callback.");
 	ASSERT_HARD(s->space != sp, "You have already added this shape to this space. You must not add it a second time.");
 	ASSERT_HARD(!s->space, "You have already added this shape to another space. You cannot add it to a second.");
 	ASSERT_HARD(s->body, "The shape's body is not defined.");
@@ -4856,6 +4872,7 @@ cpShape *cpSpaceAddShape(cpSpace *sp, cpShape *s)
 cpConstraint *cpSpaceAddConstraint(cpSpace *sp, cpConstraint *c)
 {
 	/* cpSpace.c:453-474 */
+	ASSERT_HARD(!sp->locked, "This operation cannot be done safely during a call to cpSpaceStep() or during a query. Put these calls into a post-step callback.");
 	ASSERT_HARD(c->space != sp, "You have already added this constraint to this space. You must not add it a second time.");
 	ASSERT_HARD(!c->space, "You have already added this constraint to another space. You cannot add it to a second.");
 	ASSERT_HARD(c->a != NULL && c->b != NULL, "Constraint is attached to a NULL body.");
@@ -4874,6 +4891,7 @@ cpConstraint *cpSpaceAddConstraint(cpSpace *sp, cpConstraint *c)
 void cpSpaceRemoveShape(cpSpace *sp, cpShape *s)
 {
 	/* cpSpace.c:523-545 */
+	ASSERT_HARD(!sp->locked, "This operation cannot be done safely during a call to cpSpaceStep() or during a query. Put these calls into a post-step callback.");
 	ASSERT_HARD(cpSpaceContainsShape(sp, s), "Cannot remove a shape that was not added to the space. (Removed twice maybe?)");
 	if(!space_edit_ok(sp)) return;
 	cpBody *body = s->body;
@@ -4916,6 +4934,7 @@ void cpSpaceRemoveShape(cpSpace *sp, cpShape *s)
 void cpSpaceRemoveBody(cpSpace *sp, cpBody *b)
 {
 	/* cpSpace.c:547-562 */
+	ASSERT_HARD(!sp->locked, "This operation cannot be done safely during a call to cpSpaceStep() or during a query. Put these calls into a post-step callback.");
 	ASSERT_HARD(b != cpSpaceGetStaticBody(sp), "Cannot remove the designated static body for the space.");
 	ASSERT_HARD(cpSpaceContainsBody(sp, b), "Cannot remove a body that was not added to the space. (Removed twice maybe?)");
 	if(!space_edit_ok(sp)) return;
@@ -4942,6 +4961,7 @@ void cpSpaceRemoveConstraint(cpSpace *sp, cpConstraint *c)
 	/* cpSpace.c:564-577: the constraint array loses it like
 	 * cpArrayDeleteObj, so the last constraint takes its place in the
 	 * solve order */
+	ASSERT_HARD(!sp->locked, "This operation cannot be done safely during a call to cpSpaceStep() or during a query. Put these calls into a post-step callback.");
 	ASSERT_HARD(cpSpaceContainsConstraint(sp, c), "Cannot remove a constraint that was not added to the space. (Removed twice maybe?)");
 	if(!space_edit_ok(sp)) return;
 	cpBodyActivate(c->a);
@@ -5008,8 +5028,10 @@ void cpSpaceEachShape(cpSpace *sp, cpSpaceShapeIteratorFunc func, void *data)
 					}
 				}
 			}
-			/* callbacks may edit the space: iterate a copy */
+			/* iterate a copy taken before the first callback */
+			sp->locked++;
 			for(int i = 0; i < n; i++) func(order[i], data);
+			space_unlock_(sp);
 			free(order);
 			free(bins); free(nodes);
 			run_post_step_(sp);
@@ -5017,13 +5039,17 @@ void cpSpaceEachShape(cpSpace *sp, cpSpaceShapeIteratorFunc func, void *data)
 		}
 		free(bins); free(nodes);
 	}
+	sp->locked++;
 	for(int i = 0; i < sp->nshapes; i++) if(sp->shapes[i]) func(sp->shapes[i], data);
+	space_unlock_(sp);
 	run_post_step_(sp);
 }
 
 void cpSpaceEachConstraint(cpSpace *sp, cpSpaceConstraintIteratorFunc func, void *data)
 {
+	sp->locked++;
 	for(int i = 0; i < sp->ncons; i++) func(sp->cons[i], data);
+	space_unlock_(sp);
 	run_post_step_(sp);
 }
 

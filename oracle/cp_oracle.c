@@ -2505,6 +2505,7 @@ cpBool cpSpaceContainsConstraint(cpSpace *sp, cpConstraint *c) { return c->space
 cpBody *cpSpaceAddBody(cpSpace *sp, cpBody *body)
 {
 	/* cpSpace.c:440-451 */
+	ORC_ASSERT(!sp->locked, "This operation cannot be done safely during a call to cpSpaceStep() or during a query. Put these calls into a post-step callback.");
 	ORC_ASSERT(!body->space, "You have already added this body to a space.");
 	if(body_type(body) == CP_BODY_TYPE_STATIC) push_ptr_((void ***)&sp->stat, &sp->nstat, &sp->capstat, body);
 	else push_ptr_((void ***)&sp->dyn, &sp->ndyn, &sp->capdyn, body);
@@ -2515,6 +2516,7 @@ cpBody *cpSpaceAddBody(cpSpace *sp, cpBody *body)
 cpShape *cpSpaceAddShape(cpSpace *sp, cpShape *s)
 {
 	/* cpSpace.c:417-438 */
+	ORC_ASSERT(!sp->locked, "This operation cannot be done safely during a call to cpSpaceStep() or during a query. Put these calls into a post-step callback.");
 	ORC_ASSERT(!s->space, "You have already added this shape to a space.");
 	cpBody *body = s->body;
 	ORC_ASSERT(body->space == sp, "The shape's body must be added to the space before the shape.");
@@ -2597,6 +2599,7 @@ void cpSpaceReindexStatic(cpSpace *sp)
 cpConstraint *cpSpaceAddConstraint(cpSpace *sp, cpConstraint *c)
 {
 	/* cpSpace.c:453-474 */
+	ORC_ASSERT(!sp->locked, "This operation cannot be done safely during a call to cpSpaceStep() or during a query. Put these calls into a post-step callback.");
 	ORC_ASSERT(!c->space, "You have already added this constraint to a space.");
 	cpBody *a = c->a, *b = c->b;
 	cpBodyActivate(a);
@@ -2893,6 +2896,7 @@ static void filter_arbiters_of(cpSpace *sp, cpShape *s)
 void cpSpaceRemoveShape(cpSpace *sp, cpShape *s)
 {
 	/* cpSpace.c:523-545 */
+	ORC_ASSERT(!sp->locked, "This operation cannot be done safely during a call to cpSpaceStep() or during a query. Put these calls into a post-step callback.");
 	ORC_ASSERT(s->space == sp, "Cannot remove a shape that was not added to the space.");
 	cpBody *body = s->body;
 	int isStatic = (body_type(body) == CP_BODY_TYPE_STATIC);
@@ -2912,6 +2916,7 @@ void cpSpaceRemoveShape(cpSpace *sp, cpShape *s)
 void cpSpaceRemoveBody(cpSpace *sp, cpBody *body)
 {
 	/* cpSpace.c:547-562 */
+	ORC_ASSERT(!sp->locked, "This operation cannot be done safely during a call to cpSpaceStep() or during a query. Put these calls into a post-step callback.");
 	ORC_ASSERT(body != &sp->staticBody, "Cannot remove the designated static body for the space.");
 	ORC_ASSERT(body->space == sp, "Cannot remove a body that was not added to the space.");
 	cpBodyActivate(body);
@@ -2932,6 +2937,7 @@ static cpConstraint *filter_constraints_(cpConstraint *node, cpBody *body, cpCon
 void cpSpaceRemoveConstraint(cpSpace *sp, cpConstraint *c)
 {
 	/* cpSpace.c:564-577 */
+	ORC_ASSERT(!sp->locked, "This operation cannot be done safely during a call to cpSpaceStep() or during a query. Put these calls into a post-step callback.");
 	ORC_ASSERT(c->space == sp, "Cannot remove a constraint that was not added to the space.");
 	cpBodyActivate(c->a);
 	cpBodyActivate(c->b);
@@ -2946,6 +2952,7 @@ void cpBodySetType(cpBody *body, cpBodyType type)
 	/* cpBody.c:157-205 */
 	cpBodyType oldType = body_type(body);
 	if(oldType == type) return;
+	if(body->space) ORC_ASSERT(!body->space->locked, "This operation cannot be done safely during a call to cpSpaceStep() or during a query. Put these calls into a post-step callback.");
 	body->idleTime = (type == CP_BODY_TYPE_STATIC ? ORC_INF : 0.0);
 	if(type == CP_BODY_TYPE_DYNAMIC){
 		body->m = body->i = 0.0;
@@ -3005,14 +3012,18 @@ static void each_leaf(cpSpace *sp, LeafSet *set, cpSpaceShapeIteratorFunc func, 
 
 void cpSpaceEachShape(cpSpace *sp, cpSpaceShapeIteratorFunc func, void *data)
 {
+	sp->locked++;
 	each_leaf(sp, &sp->dynTree.leaves, func, data);
 	each_leaf(sp, &sp->statTree.leaves, func, data);
+	space_unlock_(sp);
 	run_post_step_(sp);
 }
 
 void cpSpaceEachConstraint(cpSpace *sp, cpSpaceConstraintIteratorFunc func, void *data)
 {
+	sp->locked++;
 	for(int i = 0; i < sp->ncons; i++) func(sp->cons[i], data);
+	space_unlock_(sp);
 	run_post_step_(sp);
 }
 
@@ -4274,8 +4285,10 @@ void cpSpacePointQuery(cpSpace *sp, cpVect point, cpFloat maxDistance, cpShapeFi
 	QueryCtx q = {0};
 	q.kind = 0; q.a = point; q.r = maxDistance; q.filter = filter; q.func = (void *)func; q.data = data;
 	q.bb = cpBBNewForCircle(point, fmax_(maxDistance, 0.0));
+	sp->locked++;
 	tree_query_(sp, &sp->dynTree, &q);
 	tree_query_(sp, &sp->statTree, &q);
+	space_unlock_(sp);
 	run_post_step_(sp);
 }
 
@@ -4297,8 +4310,10 @@ void cpSpaceSegmentQuery(cpSpace *sp, cpVect start, cpVect end, cpFloat radius, 
 {
 	QueryCtx q = {0};
 	q.kind = 2; q.a = start; q.b = end; q.r = radius; q.filter = filter; q.func = (void *)func; q.data = data;
+	sp->locked++;
 	tree_segment_query_(sp, &sp->statTree, &q, 1.0);
 	tree_segment_query_(sp, &sp->dynTree, &q, 1.0);
+	space_unlock_(sp);
 	run_post_step_(sp);
 }
 
@@ -4319,8 +4334,10 @@ void cpSpaceBBQuery(cpSpace *sp, cpBB bb, cpShapeFilter filter, cpSpaceBBQueryFu
 {
 	QueryCtx q = {0};
 	q.kind = 4; q.bb = bb; q.filter = filter; q.func = (void *)func; q.data = data;
+	sp->locked++;
 	tree_query_(sp, &sp->dynTree, &q);
 	tree_query_(sp, &sp->statTree, &q);
+	space_unlock_(sp);
 	run_post_step_(sp);
 }
 
@@ -4399,14 +4416,15 @@ cpBool cpSpaceShapeQuery(cpSpace *sp, cpShape *shape, cpSpaceShapeQueryFunc func
 	cpBody *body = shape->body;
 	cpBB bb = (body ? shape_update(shape, body->transform) : shape->bb);
 	ShapeQueryCtx q = {shape, func, data, cpFalse};
+	sp->locked++;
 	if(sp->useHash){
 		hash_shape_query_(sp, &sp->dynGrid, bb, &q);
 		hash_shape_query_(sp, &sp->statGrid, bb, &q);
-		run_post_step_(sp);
-		return q.anyCollision;
+	} else {
+		if(sp->dynTree.root >= 0) subtree_shape_query_(sp, sp->dynTree.root, bb, &q);
+		if(sp->statTree.root >= 0) subtree_shape_query_(sp, sp->statTree.root, bb, &q);
 	}
-	if(sp->dynTree.root >= 0) subtree_shape_query_(sp, sp->dynTree.root, bb, &q);
-	if(sp->statTree.root >= 0) subtree_shape_query_(sp, sp->statTree.root, bb, &q);
+	space_unlock_(sp);
 	run_post_step_(sp);
 	return q.anyCollision;
 }

@@ -24,11 +24,14 @@
 
 static cpBody *bodies[NB + 1];
 static cpShape *shapes[NB + 2];
+static cpSpace *the_space;
 
+/* a visit prints the shape and whether the space is locked (it is, in
+ * queries and iterations: cpSpaceQuery.c:204, cpSpace.c:632) */
 static void print_visit(cpShape *shape, void *data)
 {
 	(void)data;
-	printf(" %d", (int)(size_t)cpShapeGetUserData(shape));
+	printf(" %d%s", (int)(size_t)cpShapeGetUserData(shape), cpSpaceIsLocked(the_space) ? "" : "u");
 }
 
 static void print_nearest(cpSpace *space, cpVect p)
@@ -63,6 +66,7 @@ static void print_bb(const char *label, cpShape *s)
 int main(void)
 {
 	cpSpace *space = cpSpaceNew();
+	the_space = space;
 	cpSpaceSetIterations(space, 10);
 	cpSpaceSetGravity(space, cpv(0.0, -100.0));
 
@@ -182,6 +186,7 @@ int main(void)
 	printf("order each");
 	cpSpaceEachShape(space, print_visit, NULL);
 	printf("\n");
+	printf("locked %d\n", (int)cpSpaceIsLocked(space));
 	for(int i = 0; i <= NB; i++){
 		cpVect p = cpBodyGetPosition(bodies[i]), v = cpBodyGetVelocity(bodies[i]);
 		printf("%d %a %a %a %a %a %a\n", i, p.x, p.y, v.x, v.y, cpBodyGetAngle(bodies[i]), cpBodyGetAngularVelocity(bodies[i]));
