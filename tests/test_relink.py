@@ -93,3 +93,43 @@ def test_gpu_library_runs_the_program_like_the_oracle(tmp_path, oracle_lib, prog
     err = float((np.abs(gpu - orc) / scale).max())
     print("relinked program: GPU against oracle, worst rel err %.3g" % err)
     assert err <= 1e-9, err
+
+
+LOCKED_MODES = ["none", "add", "remove", "type", "sleep"]
+
+
+def run_locked(exe, mode):
+    """(exit status, stdout, the first line of stderr) of relink_locked.c."""
+    p = subprocess.run([exe, mode], stdout=subprocess.PIPE, stderr=subprocess.PIPE, text=True, timeout=300)
+    err = p.stderr.strip().splitlines()
+    return p.returncode, p.stdout, err[0] if err else ""
+
+
+def check_locked(got, want, mode):
+    assert got == want
+    status, out, err = got
+    assert "locked 1" in out and out.strip().endswith(("after locked 0", "locked 1"))
+    if mode == "none":
+        assert status == 0 and "after locked 0" in out
+    else:
+        assert status != 0 and err.startswith("Aborting due to Chipmunk error: "), got
+
+
+@pytest.mark.parametrize("mode", LOCKED_MODES)
+def test_oracle_refuses_edits_while_locked_like_the_reference(tmp_path, oracle_lib, mode):
+    """Queries and iterations lock the space (cpSpaceIsLocked reads true in
+    their callbacks); an add, a removal, a type change or a sleep made
+    there aborts with the reference's message."""
+    if not os.path.exists(os.path.join(REF_DIR, "libcpref.so")):
+        pytest.skip("reference library not built on this machine")
+    ref = run_locked(build(tmp_path, "locked_ref", REF_DIR, "cpref", program="relink_locked.c"), mode)
+    orc = run_locked(build(tmp_path, "locked_oracle", ORACLE_DIR, "oracle", program="relink_locked.c"), mode)
+    check_locked(orc, ref, mode)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("mode", LOCKED_MODES)
+def test_gpu_library_refuses_edits_while_locked(tmp_path, oracle_lib, mode):
+    orc = run_locked(build(tmp_path, "locked_oracle", ORACLE_DIR, "oracle", program="relink_locked.c"), mode)
+    gpu = run_locked(build(tmp_path, "locked_gpu", GPU_DIR, "chipmunk_gb300", program="relink_locked.c"), mode)
+    check_locked(gpu, orc, mode)
