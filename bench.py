@@ -1043,15 +1043,16 @@ def run_ours(args):
     peak, peak_kind = measured_peaks()
     achieved = algo / (phase[dom] / 1000.0) / 1e9 if phase[dom] > 0 else 0.0
     # DRAM bytes of one launch of the dominant kernel, from an ncu capture
-    # of the same timed window (profiles/traffic.json records the window)
+    # of the same timed window (profiles/traffic.json records each window)
     traffic, traffic_note = None, "no capture of this window"
     tpath = os.path.join(REPO, "profiles", "traffic.json")
     if os.path.exists(tpath):
         with open(tpath) as f:
-            rec = json.load(f).get(args.workload, {})
-        if rec.get("window") == [start, start + args.steps] and names[dom] in rec:
-            traffic = rec[names[dom]]
-            traffic_note = rec.get("how", "")
+            recs = json.load(f).get(args.workload, [])
+        for rec in (recs if isinstance(recs, list) else [recs]):
+            if rec.get("window") == [start, start + args.steps] and names[dom] in rec:
+                traffic = rec[names[dom]]
+                traffic_note = rec.get("how", "")
 
     if rank == 0:
         (cpu_v, cpu_steps, cpu_s), (hv, h_steps, h_s), _ = cpu_sample(
