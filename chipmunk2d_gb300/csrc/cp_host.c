@@ -1311,8 +1311,8 @@ static int space_supported(cpSpace *sp)
 	}
 	for(int i = 0; i < sp->ncons; i++){
 		cpConstraint *c = sp->cons[i];
-		if(c->preSolve || c->postSolve){
-			set_error(CP_GPU_ERR_UNSUPPORTED, "constraint pre/post-solve callbacks are not run on the GPU");
+		if((c->preSolve || c->postSolve) && (sp->mode != CP_GPU_SOLVER_ORDERED || (sp->dev && !sp->ownsDev))){
+			set_error(CP_GPU_ERR_UNSUPPORTED, "constraint pre/post-solve callbacks run in the exact-order mode of a standalone space");
 			return 0;
 		}
 		if((c->kind == CPG_DSPRING && c->springForceFunc != (cpDampedSpringForceFunc)default_spring_force_) ||
@@ -1360,6 +1360,27 @@ static int space_device_ready_(cpSpace *sp)
 	return 1;
 }
 
+/* The joints' pre-solve callbacks (cpSpaceStep.c:389-396; run before the
+ * device's pre-step, their edits uploaded with it) or post-solve callbacks
+ * (:428-434; after the solve, the accumulators read back on demand), over
+ * the awake joints in the space's order, with the space locked. */
+static int constraint_callbacks_(cpSpace *sp)
+{
+	for(int i = 0; i < sp->ncons; i++) if(sp->cons[i]->preSolve || sp->cons[i]->postSolve) return 1;
+	return 0;
+}
+
+static void constraints_solve_callbacks_(cpSpace *sp, int post)
+{
+	sp->locked++;
+	for(int i = 0; i < sp->ncons; i++){
+		cpConstraint *c = sp->cons[i];
+		if(!post && c->preSolve) c->preSolve(c, sp);
+		if(post && c->postSolve) c->postSolve(c, sp);
+	}
+	space_unlock_(sp);
+}
+
 void cpSpaceStep(cpSpace *sp, cpFloat dt)
 {
 	if(dt == 0.0) return;
@@ -1370,19 +1391,24 @@ void cpSpaceStep(cpSpace *sp, cpFloat dt)
 	}
 	if(!space_device_ready_(sp)) return;
 	double dts[1] = { dt };
-	int sleep = sleep_mode_(sp), bridge = sp->handlersOn;
-	if(sleep || bridge){
+	int sleep = sleep_mode_(sp), bridge = sp->handlersOn, jcb = constraint_callbacks_(sp);
+	if(sleep || bridge || jcb){
 		/* the host's parts of the step between the device's: the handlers'
 		 * begin and pre-solve (cpSpaceStep.c:259-286), cpSpaceProcessComponents
-		 * (:375), separate (:307-313), post-solve (:439-444) */
+		 * (:375), separate (:307-313), the joints' pre-solve (:389-396) and
+		 * post-solve (:428-434), the handlers' post-solve (:439-444) */
 		if(sleep) graph_start_(sp); else graph_stop_(sp);
 		sp->sleepMutated = 0;
 		if(devset_step_part(sp->dev, dts, NULL, 1) != 0) return;
 		if(bridge && !handlers_collide_(sp)) return;
 		if(sleep && !sleep_sync_(sp, dt)) return;
-		if(bridge){
-			if(devset_step_part(sp->dev, dts, NULL, 3) != 0 || !handlers_separate_(sp)) return;
-			if(devset_step_part(sp->dev, dts, NULL, 4) != 0 || !handlers_post_solve_(sp)) return;
+		if(bridge || jcb){
+			if(devset_step_part(sp->dev, dts, NULL, 3) != 0) return;
+			if(bridge && !handlers_separate_(sp)) return;
+			if(jcb) constraints_solve_callbacks_(sp, 0);
+			if(devset_step_part(sp->dev, dts, NULL, 4) != 0) return;
+			if(jcb) constraints_solve_callbacks_(sp, 1);
+			if(bridge && !handlers_post_solve_(sp)) return;
 		} else {
 			devset_step_part(sp->dev, dts, NULL, 2);
 		}

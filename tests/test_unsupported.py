@@ -65,8 +65,11 @@ def test_custom_velocity_integration_is_refused(lib):
     lib.cpSpaceFree(sp); lib.cpBodyFree(b)
 
 
-def test_constraint_callbacks_are_refused(lib):
+def test_constraint_callbacks_in_the_coloured_mode_are_refused(lib):
+    """The joints' pre/post-solve callbacks run on the host between the
+    exact-order mode's device parts; the coloured mode refuses them."""
     sp, b = one_body_space(lib)
+    lib.cpGpuSetSolverMode(sp, 1)
     c = lib.cpSpaceAddConstraint(sp, lib.cpPivotJointNew(lib.cpSpaceGetStaticBody(sp), b, cpVect(0, 0)))
     cb = PRESOLVE_FUNC(lambda con, space: None)
     lib.cpConstraintSetPreSolveFunc(c, cb)
