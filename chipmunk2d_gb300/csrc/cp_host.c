@@ -4857,9 +4857,9 @@ void cpSpaceUseSpatialHash(cpSpace *sp, cpFloat dim, int count)
 cpBody *cpSpaceAddBody(cpSpace *sp, cpBody *b)
 {
 	/* cpSpace.c:440-451 */
-	ASSERT_HARD(!sp->locked, "This operation cannot be done safely during a call to cpSpaceStep() or during a query. Put these calls into a post-step callback.");
 	ASSERT_HARD(b->space != sp, "You have already added this body to this space. You must not add it a second time.");
 	ASSERT_HARD(!b->space, "You have already added this body to another space. You cannot add it to a second.");
+	ASSERT_HARD(!sp->locked, "This operation cannot be done safely during a call to cpSpaceStep() or during a query. Put these calls into a post-step callback.");
 	if(!space_edit_ok(sp)) return b;
 	if(body_type_(b) == CP_BODY_TYPE_STATIC) push_((void ***)&sp->stat, &sp->nstat, &sp->capstat, b);
 	else push_((void ***)&sp->dyn, &sp->ndyn, &sp->capdyn, b);
@@ -4870,11 +4870,11 @@ cpBody *cpSpaceAddBody(cpSpace *sp, cpBody *b)
 cpShape *cpSpaceAddShape(cpSpace *sp, cpShape *s)
 {
 	/* cpSpace.c:417-438 */
-	ASSERT_HARD(!sp->locked, "This operation cannot be done safely during a call to cpSpaceStep() or during a query. Put these calls into a post-step callback.");
 	ASSERT_HARD(s->space != sp, "You have already added this shape to this space. You must not add it a second time.");
 	ASSERT_HARD(!s->space, "You have already added this shape to another space. You cannot add it to a second.");
 	ASSERT_HARD(s->body, "The shape's body is not defined.");
 	ASSERT_HARD(s->body->space == sp, "The shape's body must be added to the space before the shape.");
+	ASSERT_HARD(!sp->locked, "This operation cannot be done safely during a call to cpSpaceStep() or during a query. Put these calls into a post-step callback.");
 	if(!space_edit_ok(sp)) return s;
 	cpBody *body = s->body;
 	rd(body);
@@ -4898,10 +4898,10 @@ cpShape *cpSpaceAddShape(cpSpace *sp, cpShape *s)
 cpConstraint *cpSpaceAddConstraint(cpSpace *sp, cpConstraint *c)
 {
 	/* cpSpace.c:453-474 */
-	ASSERT_HARD(!sp->locked, "This operation cannot be done safely during a call to cpSpaceStep() or during a query. Put these calls into a post-step callback.");
 	ASSERT_HARD(c->space != sp, "You have already added this constraint to this space. You must not add it a second time.");
 	ASSERT_HARD(!c->space, "You have already added this constraint to another space. You cannot add it to a second.");
 	ASSERT_HARD(c->a != NULL && c->b != NULL, "Constraint is attached to a NULL body.");
+	ASSERT_HARD(!sp->locked, "This operation cannot be done safely during a call to cpSpaceStep() or during a query. Put these calls into a post-step callback.");
 	if(!space_edit_ok(sp)) return c;
 	cpBody *a = c->a, *b = c->b;
 	cpBodyActivate(a);
@@ -4917,8 +4917,8 @@ cpConstraint *cpSpaceAddConstraint(cpSpace *sp, cpConstraint *c)
 void cpSpaceRemoveShape(cpSpace *sp, cpShape *s)
 {
 	/* cpSpace.c:523-545 */
-	ASSERT_HARD(!sp->locked, "This operation cannot be done safely during a call to cpSpaceStep() or during a query. Put these calls into a post-step callback.");
 	ASSERT_HARD(cpSpaceContainsShape(sp, s), "Cannot remove a shape that was not added to the space. (Removed twice maybe?)");
+	ASSERT_HARD(!sp->locked, "This operation cannot be done safely during a call to cpSpaceStep() or during a query. Put these calls into a post-step callback.");
 	if(!space_edit_ok(sp)) return;
 	cpBody *body = s->body;
 	int isStatic = (body_type_(body) == CP_BODY_TYPE_STATIC);
@@ -4960,9 +4960,9 @@ void cpSpaceRemoveShape(cpSpace *sp, cpShape *s)
 void cpSpaceRemoveBody(cpSpace *sp, cpBody *b)
 {
 	/* cpSpace.c:547-562 */
-	ASSERT_HARD(!sp->locked, "This operation cannot be done safely during a call to cpSpaceStep() or during a query. Put these calls into a post-step callback.");
 	ASSERT_HARD(b != cpSpaceGetStaticBody(sp), "Cannot remove the designated static body for the space.");
 	ASSERT_HARD(cpSpaceContainsBody(sp, b), "Cannot remove a body that was not added to the space. (Removed twice maybe?)");
+	ASSERT_HARD(!sp->locked, "This operation cannot be done safely during a call to cpSpaceStep() or during a query. Put these calls into a post-step callback.");
 	if(!space_edit_ok(sp)) return;
 	cpBodyActivate(b);
 	if(body_type_(b) == CP_BODY_TYPE_STATIC) array_delete_((void **)sp->stat, &sp->nstat, b);
@@ -4987,8 +4987,8 @@ void cpSpaceRemoveConstraint(cpSpace *sp, cpConstraint *c)
 	/* cpSpace.c:564-577: the constraint array loses it like
 	 * cpArrayDeleteObj, so the last constraint takes its place in the
 	 * solve order */
-	ASSERT_HARD(!sp->locked, "This operation cannot be done safely during a call to cpSpaceStep() or during a query. Put these calls into a post-step callback.");
 	ASSERT_HARD(cpSpaceContainsConstraint(sp, c), "Cannot remove a constraint that was not added to the space. (Removed twice maybe?)");
+	ASSERT_HARD(!sp->locked, "This operation cannot be done safely during a call to cpSpaceStep() or during a query. Put these calls into a post-step callback.");
 	if(!space_edit_ok(sp)) return;
 	cpBodyActivate(c->a);
 	cpBodyActivate(c->b);

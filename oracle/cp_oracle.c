@@ -2505,8 +2505,8 @@ cpBool cpSpaceContainsConstraint(cpSpace *sp, cpConstraint *c) { return c->space
 cpBody *cpSpaceAddBody(cpSpace *sp, cpBody *body)
 {
 	/* cpSpace.c:440-451 */
-	ORC_ASSERT(!sp->locked, "This operation cannot be done safely during a call to cpSpaceStep() or during a query. Put these calls into a post-step callback.");
 	ORC_ASSERT(!body->space, "You have already added this body to a space.");
+	ORC_ASSERT(!sp->locked, "This operation cannot be done safely during a call to cpSpaceStep() or during a query. Put these calls into a post-step callback.");
 	if(body_type(body) == CP_BODY_TYPE_STATIC) push_ptr_((void ***)&sp->stat, &sp->nstat, &sp->capstat, body);
 	else push_ptr_((void ***)&sp->dyn, &sp->ndyn, &sp->capdyn, body);
 	body->space = sp;
@@ -2516,10 +2516,10 @@ cpBody *cpSpaceAddBody(cpSpace *sp, cpBody *body)
 cpShape *cpSpaceAddShape(cpSpace *sp, cpShape *s)
 {
 	/* cpSpace.c:417-438 */
-	ORC_ASSERT(!sp->locked, "This operation cannot be done safely during a call to cpSpaceStep() or during a query. Put these calls into a post-step callback.");
 	ORC_ASSERT(!s->space, "You have already added this shape to a space.");
 	cpBody *body = s->body;
 	ORC_ASSERT(body->space == sp, "The shape's body must be added to the space before the shape.");
+	ORC_ASSERT(!sp->locked, "This operation cannot be done safely during a call to cpSpaceStep() or during a query. Put these calls into a post-step callback.");
 	int isStatic = (body_type(body) == CP_BODY_TYPE_STATIC);
 	if(!isStatic) cpBodyActivate(body);
 	/* cpBody.c:182-194: push on the body's shape list */
@@ -2599,8 +2599,8 @@ void cpSpaceReindexStatic(cpSpace *sp)
 cpConstraint *cpSpaceAddConstraint(cpSpace *sp, cpConstraint *c)
 {
 	/* cpSpace.c:453-474 */
-	ORC_ASSERT(!sp->locked, "This operation cannot be done safely during a call to cpSpaceStep() or during a query. Put these calls into a post-step callback.");
 	ORC_ASSERT(!c->space, "You have already added this constraint to a space.");
+	ORC_ASSERT(!sp->locked, "This operation cannot be done safely during a call to cpSpaceStep() or during a query. Put these calls into a post-step callback.");
 	cpBody *a = c->a, *b = c->b;
 	cpBodyActivate(a);
 	cpBodyActivate(b);
@@ -2896,8 +2896,8 @@ static void filter_arbiters_of(cpSpace *sp, cpShape *s)
 void cpSpaceRemoveShape(cpSpace *sp, cpShape *s)
 {
 	/* cpSpace.c:523-545 */
-	ORC_ASSERT(!sp->locked, "This operation cannot be done safely during a call to cpSpaceStep() or during a query. Put these calls into a post-step callback.");
 	ORC_ASSERT(s->space == sp, "Cannot remove a shape that was not added to the space.");
+	ORC_ASSERT(!sp->locked, "This operation cannot be done safely during a call to cpSpaceStep() or during a query. Put these calls into a post-step callback.");
 	cpBody *body = s->body;
 	int isStatic = (body_type(body) == CP_BODY_TYPE_STATIC);
 	if(isStatic) cpBodyActivateStatic(body, s);
@@ -2916,9 +2916,9 @@ void cpSpaceRemoveShape(cpSpace *sp, cpShape *s)
 void cpSpaceRemoveBody(cpSpace *sp, cpBody *body)
 {
 	/* cpSpace.c:547-562 */
-	ORC_ASSERT(!sp->locked, "This operation cannot be done safely during a call to cpSpaceStep() or during a query. Put these calls into a post-step callback.");
 	ORC_ASSERT(body != &sp->staticBody, "Cannot remove the designated static body for the space.");
 	ORC_ASSERT(body->space == sp, "Cannot remove a body that was not added to the space.");
+	ORC_ASSERT(!sp->locked, "This operation cannot be done safely during a call to cpSpaceStep() or during a query. Put these calls into a post-step callback.");
 	cpBodyActivate(body);
 	if(body_type(body) == CP_BODY_TYPE_STATIC) array_delete_((void **)sp->stat, &sp->nstat, body);
 	else array_delete_((void **)sp->dyn, &sp->ndyn, body);
@@ -2937,8 +2937,8 @@ static cpConstraint *filter_constraints_(cpConstraint *node, cpBody *body, cpCon
 void cpSpaceRemoveConstraint(cpSpace *sp, cpConstraint *c)
 {
 	/* cpSpace.c:564-577 */
-	ORC_ASSERT(!sp->locked, "This operation cannot be done safely during a call to cpSpaceStep() or during a query. Put these calls into a post-step callback.");
 	ORC_ASSERT(c->space == sp, "Cannot remove a constraint that was not added to the space.");
+	ORC_ASSERT(!sp->locked, "This operation cannot be done safely during a call to cpSpaceStep() or during a query. Put these calls into a post-step callback.");
 	cpBodyActivate(c->a);
 	cpBodyActivate(c->b);
 	array_delete_((void **)sp->cons, &sp->ncons, c);
