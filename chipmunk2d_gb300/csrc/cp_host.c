@@ -1157,7 +1157,9 @@ static int bridge_buf_(DevSet *ds, int n);
 
 /* part 0: the whole step; 1: up to the arbiter list; 2: the rest of the
  * step begun by part 1 (a single space; its set may have been rebuilt in
- * between, so the parameters go up again without advancing the stamp). */
+ * between, so the parameters go up again without advancing the stamp);
+ * 3: the arbiter filter of part 2; 4: the rest of part 2 after the filter;
+ * 5: part 4 through the velocity update; 6: the rest of part 4. */
 static int devset_step_part(DevSet *ds, const double *dts, cpSpace **only, int part)
 {
 	cpgSet *d = &ds->d;
@@ -1253,7 +1255,7 @@ static int devset_step_part(DevSet *ds, const double *dts, cpSpace **only, int p
 		set_error(CP_GPU_ERR_CUDA, "step launch failed");
 		return -1;
 	}
-	if(part == 1 || part == 3) return 0;
+	if(part == 1 || part == 3 || part == 5) return 0;
 	if(g_timing) for(int w = 0; w < ds->nspaces; w++) memcpy(ds->spaces[w]->phaseMs, ms, sizeof(ms));
 	if(tuning >= 0){
 		ds->tuneMs[tuning] += (double)ms[1] + (double)ms[6];
@@ -1288,6 +1290,8 @@ static void graph_start_(cpSpace *sp);
 static void graph_stop_(cpSpace *sp);
 static int sleep_sync_(cpSpace *sp, cpFloat dt);
 
+static inline cpConstraint *cons_next_(cpConstraint *c, cpBody *b);
+
 static int space_supported(cpSpace *sp)
 {
 	if(sleep_mode_(sp) && (sp->mode != CP_GPU_SOLVER_ORDERED || (sp->dev && !sp->ownsDev))){
@@ -1304,9 +1308,21 @@ static int space_supported(cpSpace *sp)
 	}
 	for(int i = 0; i < sp->ndyn; i++){
 		cpBody *b = sp->dyn[i];
-		if(b->velocity_func != cpBodyUpdateVelocity || b->position_func != cpBodyUpdatePosition){
-			set_error(CP_GPU_ERR_UNSUPPORTED, "custom body integration callbacks are not run on the GPU");
+		if(b->position_func != cpBodyUpdatePosition){
+			set_error(CP_GPU_ERR_UNSUPPORTED, "custom position functions are not run on the GPU");
 			return 0;
+		}
+		if(b->velocity_func != cpBodyUpdateVelocity){
+			if(sp->mode != CP_GPU_SOLVER_ORDERED || (sp->dev && !sp->ownsDev)){
+				set_error(CP_GPU_ERR_UNSUPPORTED, "custom velocity functions run in the exact-order mode of a standalone space");
+				return 0;
+			}
+			for(cpConstraint *c = b->constraintList; c; c = cons_next_(c, b)){
+				if(c->kind == CPG_DSPRING || c->kind == CPG_DRSPRING){
+					set_error(CP_GPU_ERR_UNSUPPORTED, "a body with a custom velocity function cannot carry a damped spring");
+					return 0;
+				}
+			}
 		}
 	}
 	for(int i = 0; i < sp->ncons; i++){
@@ -1360,6 +1376,79 @@ static int space_device_ready_(cpSpace *sp)
 	return 1;
 }
 
+/* Bodies with their own velocity function (cpSpaceStep.c:399-403).  The
+ * functions run on the host after the joints' pre-solve callbacks, in the
+ * order of the awake bodies, with the space locked, on the state the
+ * device's velocity update would read (a body with one is not allowed a
+ * damped spring, whose pre-step impulse the device adds first); a function
+ * that reads another body's velocity sees the bodies with the default
+ * update before it, and the earlier ones with their own functions after.  Their
+ * results (velocity, angular velocity, the force and torque left behind)
+ * are kept and the bodies put back; the device then updates every body as
+ * usual (part 5) and the kept results replace the updates of these bodies,
+ * packed solver records included, before the solve (part 6). */
+typedef struct VelocityOut { int index; double v[6], orig[6]; } VelocityOut;
+
+static inline const cpBody *rd(const cpBody *b);
+
+static int velocity_callbacks_(cpSpace *sp)
+{
+	for(int i = 0; i < sp->ndyn; i++) if(sp->dyn[i]->velocity_func != cpBodyUpdateVelocity) return 1;
+	return 0;
+}
+
+static int run_velocity_funcs_(cpSpace *sp, cpFloat dt, VelocityOut **out)
+{
+	/* the joints' pre-solve edits go up first: the device must read them */
+	devset_flush_space(sp->dev, sp->world);
+	VelocityOut *o = HALLOC(VelocityOut, sp->ndyn > 0 ? sp->ndyn : 1);
+	int n = 0;
+	cpVect g = sp->gravity;
+	cpFloat damping = pow(sp->damping, dt);
+	sp->locked++;
+	for(int i = 0; i < sp->ndyn; i++){
+		cpBody *b = sp->dyn[i];
+		if(b->velocity_func == cpBodyUpdateVelocity) continue;
+		rd(b);
+		VelocityOut *r = &o[n++];
+		r->index = i;
+		r->orig[0] = b->v.x; r->orig[1] = b->v.y; r->orig[2] = b->w;
+		r->orig[3] = b->f.x; r->orig[4] = b->f.y; r->orig[5] = b->t;
+		b->velocity_func(b, g, damping, dt);
+		rd(b);
+		r->v[0] = b->v.x; r->v[1] = b->v.y; r->v[2] = b->w;
+		r->v[3] = b->f.x; r->v[4] = b->f.y; r->v[5] = b->t;
+	}
+	space_unlock_(sp);
+	/* the bodies as the device holds them until its update */
+	for(int k = 0; k < n; k++){
+		cpBody *b = sp->dyn[o[k].index];
+		b->v = cpv(o[k].orig[0], o[k].orig[1]); b->w = o[k].orig[2];
+		b->f = cpv(o[k].orig[3], o[k].orig[4]); b->t = o[k].orig[5];
+	}
+	*out = o;
+	return n;
+}
+
+static int put_velocities_(cpSpace *sp, const VelocityOut *o, int n)
+{
+	DevSet *ds = sp->dev;
+	size_t off = (size_t)ds->hworld[sp->world].bodyOff;
+	int ok = 1;
+	for(int k = 0; k < n && ok; k++){
+		size_t g = off + (size_t)o[k].index;
+		ok &= h2d(ds->d.vx + g, &o[k].v[0], sizeof(double));
+		ok &= h2d(ds->d.vy + g, &o[k].v[1], sizeof(double));
+		ok &= h2d(ds->d.w + g, &o[k].v[2], sizeof(double));
+		ok &= h2d(ds->d.fx + g, &o[k].v[3], sizeof(double));
+		ok &= h2d(ds->d.fy + g, &o[k].v[4], sizeof(double));
+		ok &= h2d(ds->d.tq + g, &o[k].v[5], sizeof(double));
+		ok &= h2d(ds->d.pbody + 8*g, &o[k].v[0], 3*sizeof(double));   /* packed vx, vy, w */
+	}
+	if(!ok){ set_error(CP_GPU_ERR_CUDA, "velocity functions: upload failed"); return -1; }
+	return 0;
+}
+
 /* The joints' pre-solve callbacks (cpSpaceStep.c:389-396; run before the
  * device's pre-step, their edits uploaded with it) or post-solve callbacks
  * (:428-434; after the solve, the accumulators read back on demand), over
@@ -1391,8 +1480,8 @@ void cpSpaceStep(cpSpace *sp, cpFloat dt)
 	}
 	if(!space_device_ready_(sp)) return;
 	double dts[1] = { dt };
-	int sleep = sleep_mode_(sp), bridge = sp->handlersOn, jcb = constraint_callbacks_(sp);
-	if(sleep || bridge || jcb){
+	int sleep = sleep_mode_(sp), bridge = sp->handlersOn, jcb = constraint_callbacks_(sp), vcb = velocity_callbacks_(sp);
+	if(sleep || bridge || jcb || vcb){
 		/* the host's parts of the step between the device's: the handlers'
 		 * begin and pre-solve (cpSpaceStep.c:259-286), cpSpaceProcessComponents
 		 * (:375), separate (:307-313), the joints' pre-solve (:389-396) and
@@ -1402,11 +1491,18 @@ void cpSpaceStep(cpSpace *sp, cpFloat dt)
 		if(devset_step_part(sp->dev, dts, NULL, 1) != 0) return;
 		if(bridge && !handlers_collide_(sp)) return;
 		if(sleep && !sleep_sync_(sp, dt)) return;
-		if(bridge || jcb){
+		if(bridge || jcb || vcb){
 			if(devset_step_part(sp->dev, dts, NULL, 3) != 0) return;
 			if(bridge && !handlers_separate_(sp)) return;
 			if(jcb) constraints_solve_callbacks_(sp, 0);
-			if(devset_step_part(sp->dev, dts, NULL, 4) != 0) return;
+			if(vcb){
+				VelocityOut *vo = NULL;
+				int n = run_velocity_funcs_(sp, dt, &vo);
+				int rc = devset_step_part(sp->dev, dts, NULL, 5);
+				if(rc == 0) rc = put_velocities_(sp, vo, n);
+				free(vo);
+				if(rc != 0 || devset_step_part(sp->dev, dts, NULL, 6) != 0) return;
+			} else if(devset_step_part(sp->dev, dts, NULL, 4) != 0) return;
 			if(jcb) constraints_solve_callbacks_(sp, 1);
 			if(bridge && !handlers_post_solve_(sp)) return;
 		} else {

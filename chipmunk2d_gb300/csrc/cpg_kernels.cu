@@ -3426,7 +3426,8 @@ extern "C" int cpg_launch_step_part(const cpgSet *s, const cpgSet *h, int mode, 
 	}
 	if(part == 1) goto done;
 second:
-	if(part != 4){
+	if(part == 6) goto after_velocity;
+	if(part != 4 && part != 5){
 		if(s->sepCount) cudaMemsetAsync(s->sepCount, 0, sizeof(int), st);
 		LAUNCH(k_arb_filter<<<blocks_for(h->arbCap, 256), 256, 0, st>>>(*s));
 	}
@@ -3447,6 +3448,8 @@ second:
 	if(h->tape.on) cpg_launch_tape(s, st);
 	LAUNCH(k_integrate_vel<<<blocks_for(h->totalBodies, 128), 128, 0, st>>>(sv));
 	if(h->tape.on) cpg_launch_tape_vel(s, st);
+	if(part == 5) goto done;
+after_velocity:
 	if(timing) cudaEventRecord(ev[6], st);
 	if(W == 1 && colored){
 		COOP(k_solve_coop<true>, CPG_COOP_SOLVE_THREADS);

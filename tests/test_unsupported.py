@@ -56,10 +56,26 @@ def test_sleeping_in_the_coloured_mode_is_refused(lib):
     lib.cpSpaceFree(sp); lib.cpBodyFree(b)
 
 
-def test_custom_velocity_integration_is_refused(lib):
+def test_custom_velocity_functions_in_the_coloured_mode_are_refused(lib):
+    """Velocity functions run on the host between the exact-order mode's
+    device parts; the coloured mode refuses them."""
     sp, b = one_body_space(lib)
+    lib.cpGpuSetSolverMode(sp, 1)
     cb = VELOCITY_FUNC(lambda body, g, damping, dt: None)
     lib.cpBodySetVelocityUpdateFunc(b, cb)
+    err, unmoved = refused(lib, sp, b)
+    assert err == CP_GPU_ERR_UNSUPPORTED and unmoved
+    lib.cpSpaceFree(sp); lib.cpBodyFree(b)
+
+
+POSITION_FUNC = ctypes.CFUNCTYPE(None, P, D)
+
+
+def test_custom_position_functions_are_refused(lib):
+    lib.cpBodySetPositionUpdateFunc.argtypes = [P, POSITION_FUNC]
+    sp, b = one_body_space(lib)
+    cb = POSITION_FUNC(lambda body, dt: None)
+    lib.cpBodySetPositionUpdateFunc(b, cb)
     err, unmoved = refused(lib, sp, b)
     assert err == CP_GPU_ERR_UNSUPPORTED and unmoved
     lib.cpSpaceFree(sp); lib.cpBodyFree(b)
