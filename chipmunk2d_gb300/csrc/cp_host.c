@@ -1159,7 +1159,8 @@ static int bridge_buf_(DevSet *ds, int n);
  * step begun by part 1 (a single space; its set may have been rebuilt in
  * between, so the parameters go up again without advancing the stamp);
  * 3: the arbiter filter of part 2; 4: the rest of part 2 after the filter;
- * 5: part 4 through the velocity update; 6: the rest of part 4. */
+ * 5: part 4 through the velocity update; 6: the rest of part 4; 7: part 1
+ * through the position update; 8: the rest of part 1. */
 static int devset_step_part(DevSet *ds, const double *dts, cpSpace **only, int part)
 {
 	cpgSet *d = &ds->d;
@@ -1180,7 +1181,7 @@ static int devset_step_part(DevSet *ds, const double *dts, cpSpace **only, int p
 		double dt = dts[w];
 		/* cpSpaceStep.c:339-344, 384, 399, 407 */
 		cpFloat prev_dt;
-		if(part >= 2) prev_dt = sp->prevDt;
+		if(part >= 2 && part != 7) prev_dt = sp->prevDt;
 		else {
 			sp->stamp++;
 			prev_dt = sp->prevDt = sp->curr_dt;
@@ -1255,7 +1256,7 @@ static int devset_step_part(DevSet *ds, const double *dts, cpSpace **only, int p
 		set_error(CP_GPU_ERR_CUDA, "step launch failed");
 		return -1;
 	}
-	if(part == 1 || part == 3 || part == 5) return 0;
+	if(part == 1 || part == 3 || part == 5 || part == 7 || part == 8) return 0;
 	if(g_timing) for(int w = 0; w < ds->nspaces; w++) memcpy(ds->spaces[w]->phaseMs, ms, sizeof(ms));
 	if(tuning >= 0){
 		ds->tuneMs[tuning] += (double)ms[1] + (double)ms[6];
@@ -1308,16 +1309,12 @@ static int space_supported(cpSpace *sp)
 	}
 	for(int i = 0; i < sp->ndyn; i++){
 		cpBody *b = sp->dyn[i];
-		if(b->position_func != cpBodyUpdatePosition){
-			set_error(CP_GPU_ERR_UNSUPPORTED, "custom position functions are not run on the GPU");
-			return 0;
-		}
-		if(b->velocity_func != cpBodyUpdateVelocity){
+		if(b->velocity_func != cpBodyUpdateVelocity || b->position_func != cpBodyUpdatePosition){
 			if(sp->mode != CP_GPU_SOLVER_ORDERED || (sp->dev && !sp->ownsDev)){
-				set_error(CP_GPU_ERR_UNSUPPORTED, "custom velocity functions run in the exact-order mode of a standalone space");
+				set_error(CP_GPU_ERR_UNSUPPORTED, "custom velocity and position functions run in the exact-order mode of a standalone space");
 				return 0;
 			}
-			for(cpConstraint *c = b->constraintList; c; c = cons_next_(c, b)){
+			for(cpConstraint *c = b->constraintList; b->velocity_func != cpBodyUpdateVelocity && c; c = cons_next_(c, b)){
 				if(c->kind == CPG_DSPRING || c->kind == CPG_DRSPRING){
 					set_error(CP_GPU_ERR_UNSUPPORTED, "a body with a custom velocity function cannot carry a damped spring");
 					return 0;
@@ -1376,6 +1373,76 @@ static int space_device_ready_(cpSpace *sp)
 	return 1;
 }
 
+/* Bodies with their own position function (cpSpaceStep.c:362-366).  The
+ * functions run on the host before the step, over the awake bodies in
+ * order with the space locked; their results (position, angle, transform,
+ * bias velocities and velocities) are kept and the bodies put back; the
+ * device's part 7 updates every body's position as usual, the kept results
+ * replace those bodies' values, and part 8 goes on with the shape caches. */
+typedef struct PositionOut { int index; double v[15], orig[15]; } PositionOut;
+
+static inline const cpBody *rd(const cpBody *b);
+
+static int position_callbacks_(cpSpace *sp)
+{
+	for(int i = 0; i < sp->ndyn; i++) if(sp->dyn[i]->position_func != cpBodyUpdatePosition) return 1;
+	return 0;
+}
+
+static void body_pos_get_(const cpBody *b, double *o)
+{
+	o[0] = b->p.x; o[1] = b->p.y; o[2] = b->a;
+	o[3] = b->transform.a; o[4] = b->transform.b; o[5] = b->transform.c;
+	o[6] = b->transform.d; o[7] = b->transform.tx; o[8] = b->transform.ty;
+	o[9] = b->v_bias.x; o[10] = b->v_bias.y; o[11] = b->w_bias;
+	o[12] = b->v.x; o[13] = b->v.y; o[14] = b->w;
+}
+
+static int run_position_funcs_(cpSpace *sp, cpFloat dt, PositionOut **out)
+{
+	PositionOut *o = HALLOC(PositionOut, sp->ndyn > 0 ? sp->ndyn : 1);
+	int n = 0;
+	sp->locked++;
+	for(int i = 0; i < sp->ndyn; i++){
+		cpBody *b = sp->dyn[i];
+		if(b->position_func == cpBodyUpdatePosition) continue;
+		rd(b);
+		PositionOut *r = &o[n++];
+		r->index = i;
+		body_pos_get_(b, r->orig);
+		b->position_func(b, dt);
+		rd(b);
+		body_pos_get_(b, r->v);
+	}
+	space_unlock_(sp);
+	/* the bodies as the device holds them until its update */
+	for(int k = 0; k < n; k++){
+		cpBody *b = sp->dyn[o[k].index];
+		const double *q = o[k].orig;
+		b->p = cpv(q[0], q[1]); b->a = q[2];
+		b->transform = (cpTransform){q[3], q[4], q[5], q[6], q[7], q[8]};
+		b->v_bias = cpv(q[9], q[10]); b->w_bias = q[11];
+		b->v = cpv(q[12], q[13]); b->w = q[14];
+	}
+	*out = o;
+	return n;
+}
+
+static int put_positions_(cpSpace *sp, const PositionOut *o, int n)
+{
+	DevSet *ds = sp->dev;
+	size_t off = (size_t)ds->hworld[sp->world].bodyOff;
+	int ok = 1;
+	for(int k = 0; k < n && ok; k++){
+		size_t g = off + (size_t)o[k].index;
+		double *dst[15] = { ds->d.px, ds->d.py, ds->d.ang, ds->d.ta, ds->d.tb, ds->d.tc, ds->d.td, ds->d.ttx, ds->d.tty,
+		                    ds->d.vbx, ds->d.vby, ds->d.wb, ds->d.vx, ds->d.vy, ds->d.w };
+		for(int j = 0; j < 15; j++) ok &= h2d(dst[j] + g, &o[k].v[j], sizeof(double));
+	}
+	if(!ok){ set_error(CP_GPU_ERR_CUDA, "position functions: upload failed"); return -1; }
+	return 0;
+}
+
 /* Bodies with their own velocity function (cpSpaceStep.c:399-403).  The
  * functions run on the host after the joints' pre-solve callbacks, in the
  * order of the awake bodies, with the space locked, on the state the
@@ -1388,8 +1455,6 @@ static int space_device_ready_(cpSpace *sp)
  * usual (part 5) and the kept results replace the updates of these bodies,
  * packed solver records included, before the solve (part 6). */
 typedef struct VelocityOut { int index; double v[6], orig[6]; } VelocityOut;
-
-static inline const cpBody *rd(const cpBody *b);
 
 static int velocity_callbacks_(cpSpace *sp)
 {
@@ -1481,14 +1546,22 @@ void cpSpaceStep(cpSpace *sp, cpFloat dt)
 	if(!space_device_ready_(sp)) return;
 	double dts[1] = { dt };
 	int sleep = sleep_mode_(sp), bridge = sp->handlersOn, jcb = constraint_callbacks_(sp), vcb = velocity_callbacks_(sp);
-	if(sleep || bridge || jcb || vcb){
+	int pcb = position_callbacks_(sp);
+	if(sleep || bridge || jcb || vcb || pcb){
 		/* the host's parts of the step between the device's: the handlers'
 		 * begin and pre-solve (cpSpaceStep.c:259-286), cpSpaceProcessComponents
 		 * (:375), separate (:307-313), the joints' pre-solve (:389-396) and
 		 * post-solve (:428-434), the handlers' post-solve (:439-444) */
 		if(sleep) graph_start_(sp); else graph_stop_(sp);
 		sp->sleepMutated = 0;
-		if(devset_step_part(sp->dev, dts, NULL, 1) != 0) return;
+		if(pcb){
+			PositionOut *po = NULL;
+			int n = run_position_funcs_(sp, dt, &po);
+			int rc = devset_step_part(sp->dev, dts, NULL, 7);
+			if(rc == 0) rc = put_positions_(sp, po, n);
+			free(po);
+			if(rc != 0 || devset_step_part(sp->dev, dts, NULL, 8) != 0) return;
+		} else if(devset_step_part(sp->dev, dts, NULL, 1) != 0) return;
 		if(bridge && !handlers_collide_(sp)) return;
 		if(sleep && !sleep_sync_(sp, dt)) return;
 		if(bridge || jcb || vcb){

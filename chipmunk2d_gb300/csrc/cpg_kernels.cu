@@ -3366,10 +3366,13 @@ extern "C" int cpg_launch_step_part(const cpgSet *s, const cpgSet *h, int mode, 
 	 * fails the step: the kernels after it would run on a half-done step */
 	cudaError_t coop = cudaSuccess;
 #define COOP(kernel, threads) do { cudaError_t e_ = launch_coop((const void *)(kernel), (threads), &sv, 0, st); if(e_ != cudaSuccess && coop == cudaSuccess) coop = e_; } while(0)
-	if(part >= 2) goto second;
+	if(part == 8) goto after_position;
+	if(part >= 2 && part != 7) goto second;
 	cudaMemsetAsync(s->stats, 0, 16*sizeof(int), st);
 	LAUNCH(k_reset_prev<<<dim3(perWorldX, W), 128, 0, st>>>(*s));
 	LAUNCH(k_integrate_pos<<<blocks_for(h->totalBodies, 128), 128, 0, st>>>(*s));
+	if(part == 7) goto done;
+after_position:
 	LAUNCH(k_shape_cache<<<blocks_for(h->totalShapes, 128), 128, 0, st>>>(*s));
 	if(timing) cudaEventRecord(ev[1], st);
 	if(colored){
@@ -3424,7 +3427,7 @@ extern "C" int cpg_launch_step_part(const cpgSet *s, const cpgSet *h, int mode, 
 	} else {
 		LAUNCH(k_solve_list<<<W, 256, 0, st>>>(*s));
 	}
-	if(part == 1) goto done;
+	if(part == 1 || part == 8) goto done;
 second:
 	if(part == 6) goto after_velocity;
 	if(part != 4 && part != 5){

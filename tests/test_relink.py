@@ -12,7 +12,7 @@ import numpy as np
 import pytest
 
 REPO = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
-PROGRAMS = ["relink_program.c", "relink_program2.c", "relink_program3.c", "relink_program4.c", "relink_program5.c", "relink_program6.c", "relink_program7.c", "relink_program8.c"]
+PROGRAMS = ["relink_program.c", "relink_program2.c", "relink_program3.c", "relink_program4.c", "relink_program5.c", "relink_program6.c", "relink_program7.c", "relink_program8.c", "relink_program9.c"]
 GPU_DIR = os.path.join(REPO, "chipmunk2d_gb300", "_build")
 ORACLE_DIR = os.path.join(REPO, "oracle", "_build")
 REF_DIR = os.path.join(REPO, "oracle", "_ref")

@@ -71,9 +71,10 @@ def test_custom_velocity_functions_in_the_coloured_mode_are_refused(lib):
 POSITION_FUNC = ctypes.CFUNCTYPE(None, P, D)
 
 
-def test_custom_position_functions_are_refused(lib):
+def test_custom_position_functions_in_the_coloured_mode_are_refused(lib):
     lib.cpBodySetPositionUpdateFunc.argtypes = [P, POSITION_FUNC]
     sp, b = one_body_space(lib)
+    lib.cpGpuSetSolverMode(sp, 1)
     cb = POSITION_FUNC(lambda body, dt: None)
     lib.cpBodySetPositionUpdateFunc(b, cb)
     err, unmoved = refused(lib, sp, b)
